@@ -1,0 +1,276 @@
+"""ctypes declarations of include/aither_gb300.h and thin Python wrappers.
+
+The native library is the product; these wrappers only marshal arguments.
+Loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libaither_gb300.so")
+
+ATH_OK = 0
+BC = dict(SLIP_WALL=0, VISCOUS_WALL=1, CHARACTERISTIC=2, STAGNATION_INLET=3,
+          PRESSURE_OUTLET=4, SUPERSONIC_INFLOW=5, SUPERSONIC_OUTFLOW=6,
+          PERIODIC=7, INTERBLOCK=8)
+PREC_FP64, PREC_MIXED = 0, 1
+FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6)
+
+
+class GhostOp(C.Structure):
+    _fields_ = [("dst", C.c_int64), ("src", C.c_int64), ("src_block", C.c_int32),
+                ("type", C.c_int32), ("layer", C.c_int32), ("dir", C.c_int32),
+                ("lower", C.c_int32), ("state", C.c_int32), ("face", C.c_int64),
+                ("src2", C.c_int64)]
+
+
+class BCState(C.Structure):
+    _fields_ = [("tag", C.c_int32), ("type", C.c_int32),
+                ("rho", C.c_double), ("u", C.c_double), ("v", C.c_double),
+                ("w", C.c_double), ("p", C.c_double),
+                ("p0", C.c_double), ("t0", C.c_double), ("dir", C.c_double * 3),
+                ("p_out", C.c_double),
+                ("wall_u", C.c_double), ("wall_v", C.c_double), ("wall_w", C.c_double),
+                ("wall_t", C.c_double), ("wall_q", C.c_double),
+                ("isothermal", C.c_int32), ("heat_flux", C.c_int32),
+                ("turb_intensity", C.c_double), ("eddy_visc_ratio", C.c_double)]
+
+
+class SolveView(C.Structure):
+    _fields_ = [("eqn", C.c_int32), ("recon", C.c_int32), ("limiter", C.c_int32),
+                ("flux", C.c_int32), ("solver", C.c_int32), ("turb", C.c_int32),
+                ("nv", C.c_int32), ("ng", C.c_int32), ("sweeps", C.c_int32),
+                ("kappa", C.c_double), ("cfl_start", C.c_double), ("cfl_step", C.c_double),
+                ("cfl_max", C.c_double), ("theta", C.c_double), ("zeta", C.c_double),
+                ("relax", C.c_double),
+                ("gas_r", C.c_double), ("gas_n", C.c_double), ("gas_hf", C.c_double),
+                ("mu_c1", C.c_double), ("mu_s", C.c_double), ("mu_ref", C.c_double),
+                ("t_ref", C.c_double),
+                ("r_ref", C.c_double), ("a_ref", C.c_double), ("l_ref", C.c_double),
+                ("visc_scale", C.c_double), ("visc_cfl_coeff", C.c_double),
+                ("nstates", C.c_int32), ("states", C.POINTER(BCState))]
+
+
+class BlockView(C.Structure):
+    _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32),
+                ("ng", C.c_int32), ("nv", C.c_int32), ("solve", C.c_int32),
+                ("ncell_padded", C.c_int64), ("nface_padded", C.c_int64 * 3),
+                ("vol", C.POINTER(C.c_double)), ("center", C.POINTER(C.c_double)),
+                ("width", C.POINTER(C.c_double)),
+                ("farea", C.POINTER(C.c_double) * 3),
+                ("wall_dist", C.POINTER(C.c_double)),
+                ("state0", C.POINTER(C.c_double)),
+                ("nops", C.c_int32), ("ops", C.POINTER(GhostOp)),
+                ("nplanes", C.c_int32), ("plane_offsets", C.POINTER(C.c_int32)),
+                ("plane_cells", C.POINTER(C.c_int32)),
+                ("nbr_mask", C.POINTER(C.c_uint8))]
+
+
+class Norms(C.Structure):
+    _fields_ = [("l2", C.c_double * 7), ("linf", C.c_double),
+                ("linf_block", C.c_int32), ("linf_i", C.c_int32), ("linf_j", C.c_int32),
+                ("linf_k", C.c_int32), ("linf_eqn", C.c_int32),
+                ("matrix_resid", C.c_double), ("cfl", C.c_double), ("status", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_int64), ("device_ms", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"native library {LIB_PATH} is not built; run "
+                               "`python -m aither_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        sig = {
+            "ath_last_error": (C.c_char_p, []),
+            "ath_setup_from_input": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+            "ath_setup_append": (C.c_int, [vp, C.c_char_p]),
+            "ath_setup_destroy": (C.c_int, [vp]),
+            "ath_setup_counts": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int64)]),
+            "ath_setup_block": (C.c_int, [vp, C.c_int, C.POINTER(BlockView)]),
+            "ath_setup_solve": (C.c_int, [vp, C.c_int, C.POINTER(SolveView)]),
+            "ath_setup_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_ctx_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(vp)]),
+            "ath_ctx_destroy": (C.c_int, [vp]),
+            "ath_batch_create": (C.c_int, [vp, vp, C.c_int, C.c_int, C.POINTER(vp)]),
+            "ath_batch_destroy": (C.c_int, [vp]),
+            "ath_batch_iterate": (C.c_int, [vp, C.c_int, C.POINTER(Norms)]),
+            "ath_batch_fill_ghosts": (C.c_int, [vp]),
+            "ath_batch_residual": (C.c_int, [vp]),
+            "ath_batch_timestep": (C.c_int, [vp]),
+            "ath_batch_diag_invert": (C.c_int, [vp]),
+            "ath_batch_relax": (C.c_int, [vp]),
+            "ath_batch_update": (C.c_int, [vp, C.POINTER(Norms)]),
+            "ath_batch_get_field": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+            "ath_batch_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_batch_field_width": (C.c_int, [vp, C.c_int]),
+            "ath_batch_stats": (C.c_int, [vp, C.POINTER(Stats)]),
+        }
+        missing = []
+        for name, (res, args) in sig.items():
+            try:
+                f = getattr(L, name)
+            except AttributeError:
+                missing.append(name)
+                continue
+            f.restype = res
+            f.argtypes = args
+        if missing:
+            raise RuntimeError(f"{LIB_PATH} lacks exported symbols: {missing}")
+        _lib = L
+    return _lib
+
+
+class AthError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"aither_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def check(code: int) -> None:
+    if code != ATH_OK:
+        raise AthError(code, lib().ath_last_error().decode())
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _arr(ptr, n, dtype=np.float64):
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+class Setup:
+    """Host-side case setup: parse + geometry + ghost-cell bookkeeping."""
+
+    def __init__(self, inp_paths):
+        if isinstance(inp_paths, str):
+            inp_paths = [inp_paths]
+        h = C.c_void_p()
+        check(lib().ath_setup_from_input(inp_paths[0].encode(), C.byref(h)))
+        self.h = h
+        for p in inp_paths[1:]:
+            check(lib().ath_setup_append(self.h, p.encode()))
+
+    def close(self):
+        if self.h:
+            lib().ath_setup_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def counts(self):
+        ns, nb, nc = C.c_int(), C.c_int(), C.c_int64()
+        check(lib().ath_setup_counts(self.h, C.byref(ns), C.byref(nb), C.byref(nc)))
+        return ns.value, nb.value, nc.value
+
+    def block_view(self, b: int) -> BlockView:
+        v = BlockView()
+        check(lib().ath_setup_block(self.h, b, C.byref(v)))
+        return v
+
+    def solve_view(self, s: int) -> SolveView:
+        v = SolveView()
+        check(lib().ath_setup_solve(self.h, s, C.byref(v)))
+        return v
+
+    def set_state(self, b: int, prim: np.ndarray) -> None:
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        check(lib().ath_setup_set_state(self.h, b, dptr(prim)))
+
+    def geometry(self, b: int) -> dict:
+        """Copies of the padded geometry arrays of block b."""
+        v = self.block_view(b)
+        nc = v.ncell_padded
+        NI, NJ, NK = v.ni + 2 * v.ng, v.nj + 2 * v.ng, v.nk + 2 * v.ng
+        g = {"vol": _arr(v.vol, nc).reshape(NK, NJ, NI),
+             "center": _arr(v.center, 3 * nc).reshape(3, NK, NJ, NI),
+             "width": _arr(v.width, 3 * nc).reshape(3, NK, NJ, NI)}
+        shp = [(NK, NJ, NI + 1), (NK, NJ + 1, NI), (NK + 1, NJ, NI)]
+        for d, nm in enumerate(["fareai", "fareaj", "fareak"]):
+            nf = v.nface_padded[d]
+            g[nm] = _arr(v.farea[d], 4 * nf).reshape((4,) + shp[d])
+        g["ops"] = np.ctypeslib.as_array(v.ops, shape=(v.nops,)).copy() if v.nops else None
+        g["ng"] = v.ng
+        return g
+
+
+class Context:
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        h = C.c_void_p()
+        check(lib().ath_ctx_create(device, hbm_budget, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().ath_ctx_destroy(self.h)
+            self.h = None
+
+
+class Batch:
+    """Device-resident blocks of one or more solves."""
+
+    def __init__(self, ctx: Context, setup: Setup, precision: int = PREC_FP64,
+                 flags: int = 0):
+        h = C.c_void_p()
+        check(lib().ath_batch_create(ctx.h, setup.h, precision, flags, C.byref(h)))
+        self.h = h
+        self.setup = setup
+        self.nsolves, self.nblocks, self.ncells = setup.counts()
+
+    def close(self):
+        if self.h:
+            lib().ath_batch_destroy(self.h)
+            self.h = None
+
+    def iterate(self, n: int = 1) -> np.ndarray:
+        norms = (Norms * (n * self.nsolves))()
+        check(lib().ath_batch_iterate(self.h, n, norms))
+        return norms
+
+    def stage(self, name: str, norms=None):
+        f = getattr(lib(), "ath_batch_" + name)
+        if name == "update":
+            out = (Norms * self.nsolves)()
+            check(f(self.h, out))
+            return out
+        check(f(self.h))
+
+    def field(self, b: int, field: str) -> np.ndarray:
+        v = self.setup.block_view(b)
+        fid = FIELD[field]
+        w = lib().ath_batch_field_width(self.h, fid)
+        if w < 0:
+            check(w)
+        n = (v.ncell_padded if field == "STATE_GHOSTS" else v.ni * v.nj * v.nk) * w
+        out = np.empty(n, dtype=np.float64)
+        check(lib().ath_batch_get_field(self.h, b, fid, dptr(out)))
+        if field == "STATE_GHOSTS":
+            return out.reshape(v.nk + 2 * v.ng, v.nj + 2 * v.ng, v.ni + 2 * v.ng, w)
+        return out.reshape(v.nk, v.nj, v.ni, w)
+
+    def set_state(self, b: int, prim: np.ndarray) -> None:
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        check(lib().ath_batch_set_state(self.h, b, dptr(prim)))
+
+    def stats(self) -> Stats:
+        s = Stats()
+        check(lib().ath_batch_stats(self.h, C.byref(s)))
+        return s

@@ -1,0 +1,246 @@
+"""Seeded synthetic cases in the reference's file formats.
+
+Each generator writes ``<name>.inp`` (the reference input format,
+src/input.cpp:167-643) and ``<name>.xyz`` (binary multi-block Plot3D,
+src/plot3d.cpp:363) into a directory and returns the input path plus the
+analytic initial primitive state (nondimensional, per block, AoS over
+physical cells with k slowest) when the case has one.
+
+Workloads:
+  vortex_box   -- single-block Cartesian box with an isentropic convecting
+                  vortex, periodic in i and j, slip walls in k; inviscid
+                  Euler, MUSCL (kappa=1/3) + minmod, Roe, LU-SGS.
+                  Full size 64x32x8 cells on [0,10]x[0,5]x[0,1.25].
+  bump_channel -- channel with a sinusoidal bump on the lower wall,
+                  characteristic inflow/outflow, slip walls; inviscid Euler,
+                  MUSCL minmod, Roe, LU-SGS, CFL 20.  Batches of these with
+                  sizes drawn between 32^3 and 96x64x48 and Mach in
+                  [0.3, 0.85] form the batched workload.
+"""
+from __future__ import annotations
+
+import math
+import os
+import struct
+from dataclasses import dataclass
+
+import numpy as np
+
+GAS_N = 2.5
+MOLAR_MASS = 28.97e-3
+R_UNIV = 8.3144598
+R_AIR = R_UNIV / MOLAR_MASS
+GAMMA = (GAS_N + 1.0) / GAS_N
+
+
+def write_plot3d(path: str, blocks: list[np.ndarray]) -> None:
+    """blocks: arrays of shape (3, nk+1, nj+1, ni+1) (node coordinates)."""
+    with open(path, "wb") as f:
+        f.write(struct.pack("<i", len(blocks)))
+        for b in blocks:
+            _, nk1, nj1, ni1 = b.shape
+            f.write(struct.pack("<iii", ni1, nj1, nk1))
+        for b in blocks:
+            for c in range(3):
+                f.write(np.ascontiguousarray(b[c], dtype="<f8").tobytes())
+
+
+def read_plot3d(path: str) -> list[np.ndarray]:
+    with open(path, "rb") as f:
+        (nb,) = struct.unpack("<i", f.read(4))
+        dims = [struct.unpack("<iii", f.read(12)) for _ in range(nb)]
+        out = []
+        for ni1, nj1, nk1 in dims:
+            n = ni1 * nj1 * nk1
+            arr = np.frombuffer(f.read(3 * n * 8), dtype="<f8").reshape(3, nk1, nj1, ni1)
+            out.append(arr.copy())
+    return out
+
+
+def box_nodes(ni, nj, nk, lx, ly, lz, x0=0.0, y0=0.0, z0=0.0) -> np.ndarray:
+    x = x0 + lx * np.arange(ni + 1) / ni
+    y = y0 + ly * np.arange(nj + 1) / nj
+    z = z0 + lz * np.arange(nk + 1) / nk
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    return np.stack([X, Y, Z])
+
+
+def cell_centres(nodes: np.ndarray) -> np.ndarray:
+    """Arithmetic mean of the 8 corner nodes, shape (3, nk, nj, ni)."""
+    n = nodes
+    return 0.125 * (n[:, :-1, :-1, :-1] + n[:, :-1, :-1, 1:] + n[:, :-1, 1:, :-1]
+                    + n[:, :-1, 1:, 1:] + n[:, 1:, :-1, :-1] + n[:, 1:, :-1, 1:]
+                    + n[:, 1:, 1:, :-1] + n[:, 1:, 1:, 1:])
+
+
+@dataclass
+class Refs:
+    """Reference quantities as the reference derives them (src/input.cpp:617-621)."""
+
+    t_ref: float
+    r_ref: float
+
+    @property
+    def a_ref(self) -> float:
+        return math.sqrt(0.0 + 1.0 * GAMMA * R_AIR * self.t_ref)
+
+
+def _fmt(x: float) -> str:
+    return repr(float(x))
+
+
+def _bc_block(surfs: list[tuple]) -> str:
+    """surfs: (name, i1, i2, j1, j2, k1, k2, tag) grouped i, j, k."""
+    counts = [0, 0, 0]
+    for s in surfs:
+        _, i1, i2, j1, j2, k1, k2, _ = s
+        d = 0 if i1 == i2 else (1 if j1 == j2 else 2)
+        counts[d] += 1
+    lines = [f"{counts[0]} {counts[1]} {counts[2]}"]
+    surfs_sorted = sorted(surfs, key=lambda s: 0 if s[1] == s[2] else (1 if s[3] == s[4] else 2))
+    for s in surfs_sorted:
+        lines.append("   " + " ".join(str(x) for x in s))
+    return "\n".join(lines)
+
+
+def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
+                states: list[str], bcs: list[list[tuple]], iterations: int = 1) -> None:
+    body = [
+        "# generated by aither_gb300.cases",
+        f"gridName: {grid}",
+        f"equationSet: {scheme.get('equationSet', 'euler')}",
+        "timeIntegration: implicitEuler",
+        f"cflStart: {_fmt(scheme['cfl'])}",
+        f"cflMax: {_fmt(scheme['cfl'])}",
+        f"faceReconstruction: {scheme.get('faceReconstruction', 'thirdOrder')}",
+        f"limiter: {scheme.get('limiter', 'minmod')}",
+        f"inviscidFlux: {scheme.get('inviscidFlux', 'roe')}",
+        f"iterations: {iterations}",
+        f"outputFrequency: {max(iterations, 1)}",
+        "outputVariables: <density, vel_x, vel_y, vel_z, pressure>",
+        "fluids: <fluid(name=air; referenceMassFraction=1.0)>",
+        f"referenceTemperature: {_fmt(refs.t_ref)}",
+        f"referenceDensity: {_fmt(refs.r_ref)}",
+        f"initialConditions: <{ic}>",
+        f"matrixSolver: {scheme.get('matrixSolver', 'lusgs')}",
+        "matrixRelaxation: 1.0",
+    ]
+    if states:
+        body.append("boundaryStates: <" + ",\n                 ".join(states) + ">")
+    body.append(f"boundaryConditions: {len(bcs)}")
+    for b in bcs:
+        body.append(_bc_block(b))
+    with open(path, "w") as f:
+        f.write("\n".join(body) + "\n")
+
+
+def isentropic_vortex(xc: np.ndarray, yc: np.ndarray, mach: float, p_inf: float,
+                      t_inf: float, strength: float, radius: float, x0: float,
+                      y0: float) -> tuple[np.ndarray, ...]:
+    """Dimensional primitive state of an isentropic vortex in a uniform stream.
+
+    Velocity perturbation (scaled by the freestream speed of sound)
+      du = -b/(2 pi) (y-y0)/R exp((1-r^2)/2),  dv = b/(2 pi) (x-x0)/R exp((1-r^2)/2)
+    temperature T = T_inf (1 - (g-1) b^2 / (8 g pi^2) exp(1-r^2)),
+    density rho = rho_inf (T/T_inf)^(1/(g-1)), pressure p = rho R T,
+    with r the distance from (x0, y0) divided by R.
+    """
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    rho_inf = p_inf / (R_AIR * t_inf)
+    dx = (xc - x0) / radius
+    dy = (yc - y0) / radius
+    r2 = dx * dx + dy * dy
+    e = np.exp(0.5 * (1.0 - r2))
+    u = mach * a_inf - a_inf * strength / (2 * math.pi) * dy * e
+    v = a_inf * strength / (2 * math.pi) * dx * e
+    w = np.zeros_like(u)
+    tt = t_inf * (1.0 - (GAMMA - 1.0) * strength ** 2 / (8.0 * GAMMA * math.pi ** 2) * e * e)
+    rho = rho_inf * (tt / t_inf) ** (1.0 / (GAMMA - 1.0))
+    p = rho * R_AIR * tt
+    return rho, u, v, w, p
+
+
+def nondimensional_prim(rho, u, v, w, p, refs: Refs) -> np.ndarray:
+    """Reference nondimensionalisation (src/inputStates.cpp:464-473)."""
+    a = refs.a_ref
+    return np.stack([rho / refs.r_ref, u / a, v / a, w / a, p / (refs.r_ref * a * a)], axis=-1)
+
+
+def vortex_box(outdir: str, ni: int = 64, nj: int = 32, nk: int = 8,
+               lx: float = 10.0, ly: float = 5.0, lz: float = 1.25,
+               cfl: float = 10.0, limiter: str = "minmod", name: str = "vortex_box"):
+    os.makedirs(outdir, exist_ok=True)
+    nodes = box_nodes(ni, nj, nk, lx, ly, lz)
+    write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
+    p_inf, t_inf, mach = 101325.0, 288.0, 0.5
+    refs = Refs(t_ref=t_inf, r_ref=p_inf / (R_AIR * t_inf))
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    ic = (f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; "
+          f"velocity=[{_fmt(mach * a_inf)}, 0, 0])")
+    states = [f"periodic(startTag=1; endTag=2; translation=[{_fmt(lx)}, 0, 0])",
+              f"periodic(startTag=3; endTag=4; translation=[0, {_fmt(ly)}, 0])"]
+    bcs = [[("periodic", 0, 0, 0, nj, 0, nk, 1),
+            ("periodic", ni, ni, 0, nj, 0, nk, 2),
+            ("periodic", 0, ni, 0, 0, 0, nk, 3),
+            ("periodic", 0, ni, nj, nj, 0, nk, 4),
+            ("slipWall", 0, ni, 0, nj, 0, 0, 5),
+            ("slipWall", 0, ni, 0, nj, nk, nk, 6)]]
+    inp = os.path.join(outdir, name + ".inp")
+    write_input(inp, name, {"cfl": cfl, "limiter": limiter}, refs, ic, states, bcs)
+    cen = cell_centres(nodes)
+    rho, u, v, w, p = isentropic_vortex(cen[0], cen[1], mach, p_inf, t_inf, 5.0, 1.0,
+                                        lx / 2, ly / 2)
+    prim = nondimensional_prim(rho, u, v, w, p, refs)  # (nk, nj, ni, 5)
+    return inp, [np.ascontiguousarray(prim.reshape(-1))]
+
+
+def bump_nodes(ni: int, nj: int, nk: int, height: float, length: float = 3.0,
+               h_chan: float = 1.0, depth: float = 0.5) -> np.ndarray:
+    """Channel [-1, length-1] x [0, h_chan] x [0, depth] with a sin^2 bump
+    of the given height (fraction of the unit chord) on x in [0, 1]."""
+    x = -1.0 + length * np.arange(ni + 1) / ni
+    eta = np.arange(nj + 1) / nj
+    z = depth * np.arange(nk + 1) / nk
+    yb = np.where((x >= 0.0) & (x <= 1.0), height * np.sin(np.pi * x) ** 2, 0.0)
+    X = np.broadcast_to(x[None, None, :], (nk + 1, nj + 1, ni + 1))
+    Y = yb[None, None, :] + eta[None, :, None] * (h_chan - yb[None, None, :])
+    Y = np.broadcast_to(Y, (nk + 1, nj + 1, ni + 1))
+    Z = np.broadcast_to(z[:, None, None], (nk + 1, nj + 1, ni + 1))
+    return np.ascontiguousarray(np.stack([X, Y, Z]))
+
+
+def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: float,
+                 cfl: float = 20.0, name: str = "bump"):
+    os.makedirs(outdir, exist_ok=True)
+    nodes = bump_nodes(ni, nj, nk, height)
+    write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
+    p_inf, t_inf = 101325.0, 288.0
+    refs = Refs(t_ref=t_inf, r_ref=p_inf / (R_AIR * t_inf))
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    vel = f"[{_fmt(mach * a_inf)}, 0, 0]"
+    ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; velocity={vel})"
+    states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; "
+              f"velocity={vel})"]
+    bcs = [[("characteristic", 0, 0, 0, nj, 0, nk, 1),
+            ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+            ("slipWall", 0, ni, 0, 0, 0, nk, 2),
+            ("slipWall", 0, ni, nj, nj, 0, nk, 2),
+            ("slipWall", 0, ni, 0, nj, 0, 0, 2),
+            ("slipWall", 0, ni, 0, nj, nk, nk, 2)]]
+    inp = os.path.join(outdir, name + ".inp")
+    write_input(inp, name, {"cfl": cfl, "limiter": "minmod"}, refs, ic, states, bcs)
+    return inp, None
+
+
+def bump_batch_specs(n: int = 64, seed: int = 2024, lo=(32, 32, 32), hi=(96, 64, 48)):
+    """Sizes, bump heights and Mach numbers of the batched workload."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for c in range(n):
+        ni = int(rng.integers(lo[0], hi[0] + 1))
+        nj = int(rng.integers(lo[1], hi[1] + 1))
+        nk = int(rng.integers(lo[2], hi[2] + 1))
+        h = float(rng.uniform(0.04, 0.10))
+        m = float(rng.uniform(0.3, 0.85))
+        specs.append((ni, nj, nk, h, m))
+    return specs

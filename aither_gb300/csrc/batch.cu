@@ -1,0 +1,803 @@
+// Device batch: HBM pools for every block of every solve, the work lists
+// that drive the kernels, and the iteration sequence (captured once as a
+// CUDA graph and replayed).  Implements the ath_ctx / ath_batch part of the
+// C ABI (include/aither_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "aither_gb300.h"
+#include "errors.hpp"
+#include "kernels.cuh"
+#include "setup.hpp"
+
+struct ath_setup {
+  ath::Setup s;
+};
+
+struct ath_ctx {
+  int device = 0;
+  size_t budget = 0;  // 0 = whatever the device has
+  size_t used = 0;
+};
+
+namespace ath {
+
+namespace {
+
+void Check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess)
+    throw Error(ATH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Device allocation accounted against the context's HBM budget.
+class DevMem {
+ public:
+  explicit DevMem(ath_ctx *ctx) : ctx_(ctx) {}
+  ~DevMem() { Release(); }
+  template <typename T>
+  T *Alloc(size_t count) {
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    if (ctx_->budget && ctx_->used + bytes > ctx_->budget)
+      throw Error(ATH_ERR_NOMEM, "device memory budget exceeded");
+    void *p = nullptr;
+    Check(cudaMalloc(&p, bytes), "cudaMalloc");
+    ctx_->used += bytes;
+    ptrs_.push_back({p, bytes});
+    return static_cast<T *>(p);
+  }
+  template <typename T>
+  T *Upload(const std::vector<T> &v) {
+    T *p = Alloc<T>(v.size());
+    if (!v.empty())
+      Check(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice),
+            "upload");
+    return p;
+  }
+  void Release() {
+    for (auto &e : ptrs_) {
+      cudaFree(e.first);
+      ctx_->used -= e.second;
+    }
+    ptrs_.clear();
+  }
+
+ private:
+  ath_ctx *ctx_;
+  std::vector<std::pair<void *, size_t>> ptrs_;
+};
+
+struct Lists {
+  std::vector<int32_t> cells, cell_cta_block, cell_cta_pos0;
+  std::vector<int32_t> faces[3], face_cta_block[3];
+  std::vector<int2> sweep_items;
+  std::vector<int32_t> step_off;
+  std::vector<int32_t> solve_cta0;
+  std::vector<GhostOpDev> ops, conn_ops;
+  std::vector<int32_t> op_solve;
+};
+
+}  // namespace
+
+// Per-batch state that does not depend on the arithmetic type.
+struct BatchCore {
+  ath_ctx *ctx;
+  const Setup *setup;
+  int precision, flags;
+  int nsolves = 0, nblocks = 0;
+  int64_t ncell = 0;
+  std::vector<int64_t> cell0;        // pool offset of each block
+  std::vector<int64_t> solve_pos0;   // per block: loop-order offset inside its solve
+  Lists L;
+  int nsteps = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::unique_ptr<DevMem> mem;
+  // device lists
+  int32_t *d_cells = nullptr, *d_cell_cta_block = nullptr, *d_cell_cta_pos0 = nullptr;
+  int32_t *d_faces[3] = {nullptr, nullptr, nullptr};
+  int32_t *d_face_cta_block[3] = {nullptr, nullptr, nullptr};
+  int2 *d_sweep = nullptr;
+  int32_t *d_solve_cta0 = nullptr;
+  GhostOpDev *d_ops = nullptr, *d_conn_ops = nullptr;
+  int32_t *d_op_solve = nullptr;
+  NormPartial *d_partials = nullptr;
+  NormOut *d_ring = nullptr;
+  int ring_cap = 1024;
+  int64_t *d_iter = nullptr;
+  int64_t iter_host = 0;
+  double *d_cfl = nullptr;
+  BlockDev *d_blocks = nullptr;
+  SolveDev *d_solves = nullptr;
+  ath_bc_state *d_states = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int64_t launches_per_iter = 0;
+  ath_stats stats{};
+};
+
+__global__ void k_cfl(const SolveDev *solves, int nsolves, const int64_t *iter_counter,
+                      double *cfl) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsolves) return;
+  const SolveDev sv = solves[s];
+  const double it = (double)(*iter_counter);
+  cfl[s] = fmin(sv.cfl_start + it * sv.cfl_step, sv.cfl_max);
+}
+
+__global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
+                        int nsolves, NormOut *ring, int ring_cap,
+                        int64_t *iter_counter, const SolveDev *solves,
+                        double *cfl) {
+  const int s = blockIdx.x;
+  if (s >= nsolves) return;
+  const int lane = threadIdx.x;
+  const int c0 = solve_cta0[s], c1 = solve_cta0[s + 1];
+  double l2[kNv] = {0, 0, 0, 0, 0};
+  double mx = 0.0;
+  int64_t mpos = INT64_MAX;
+  int bad = 0;
+  for (int c = c0 + lane; c < c1; c += 32) {
+    const NormPartial p = partials[c];
+#pragma unroll
+    for (int v = 0; v < kNv; ++v) l2[v] += p.l2[v];
+    if (p.linf > mx || (p.linf == mx && p.linf_pos < mpos)) {
+      mx = p.linf;
+      mpos = p.linf_pos;
+    }
+    bad |= p.bad;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int v = 0; v < kNv; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    const double om = __shfl_down_sync(0xffffffffu, mx, off);
+    const int64_t op = __shfl_down_sync(0xffffffffu, mpos, off);
+    if (om > mx || (om == mx && op < mpos)) {
+      mx = om;
+      mpos = op;
+    }
+    bad |= __shfl_down_sync(0xffffffffu, bad, off);
+  }
+  const int64_t it = *iter_counter;
+  __syncwarp();
+  if (lane == 0) {
+    NormOut o;
+    for (int v = 0; v < 7; ++v) o.l2[v] = v < kNv ? sqrt(l2[v]) : 0.0;
+    o.linf = mx;
+    o.linf_pos = mpos;
+    o.bad = bad;
+    o.pad = 0;
+    o.cfl = cfl[s];
+    ring[(it % ring_cap) * nsolves + s] = o;
+  }
+}
+
+__global__ void k_iter_advance(int64_t *iter_counter) { *iter_counter += 1; }
+
+// ---------------------------------------------------------------------------
+class RunnerBase {
+ public:
+  virtual ~RunnerBase() = default;
+  virtual void FillGhosts() = 0;
+  virtual void Residual() = 0;
+  virtual void Relax() = 0;
+  virtual void Update() = 0;
+  virtual void Iterate(int n) = 0;
+  virtual void GetDU(int b, double *out) = 0;
+  virtual void GetAinv(int b, double *out) = 0;
+};
+
+template <typename T>
+class Runner : public RunnerBase {
+ public:
+  explicit Runner(BatchCore &c) : c_(c) {
+    DevMem &m = *c.mem;
+    const int64_t n = c.ncell;
+    P_.ncell = n;
+    P_.W = m.Alloc<double>(5 * n);
+    P_.R = m.Alloc<double>(5 * n);
+    P_.dU = m.Alloc<T>(5 * n);
+    for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<T>(5 * n);
+    P_.lam = m.Alloc<double>(n);
+    P_.dt = m.Alloc<double>(n);
+    P_.Ainv = m.Alloc<T>(n);
+    Check(cudaMemset(P_.R, 0, 5 * n * sizeof(double)), "memset");
+    Check(cudaMemset(P_.dU, 0, 5 * n * sizeof(T)), "memset");
+    Check(cudaMemset(P_.lam, 0, n * sizeof(double)), "memset");
+    Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
+    Check(cudaMemset(P_.Ainv, 0, n * sizeof(T)), "memset");
+    for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(T)), "memset");
+    // geometry and state
+    std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
+    std::vector<uint8_t> mask(n, 0);
+    for (int d = 0; d < 3; ++d) {
+      wid[d].assign(n, 0.0);
+      fa[d].assign(4 * n, 0.0);
+    }
+    for (int bi = 0; bi < c.nblocks; ++bi) {
+      const Block &b = c.setup->blocks[bi];
+      const int64_t o = c.cell0[bi];
+      const int64_t nc = b.NCell();
+      for (int64_t x = 0; x < nc; ++x) {
+        for (int v = 0; v < 5; ++v) W[v * n + o + x] = b.state0[x * b.nv + v];
+        vol[o + x] = b.vol[x];
+        for (int d = 0; d < 3; ++d) wid[d][o + x] = b.width[d * nc + x];
+        mask[o + x] = b.nbr_mask.empty() ? 0 : b.nbr_mask[x];
+      }
+      for (int d = 0; d < 3; ++d) {
+        const int64_t nf = b.NFace(d);
+        const int fi = b.NI + (d == 0), fj = b.NJ + (d == 1);
+        for (int64_t f = 0; f < nf; ++f) {
+          const int ii = (int)(f % fi);
+          const int64_t r = f / fi;
+          const int jj = (int)(r % fj);
+          const int kk = (int)(r / fj);
+          if (ii >= b.NI || jj >= b.NJ || kk >= b.NK) continue;
+          const int64_t x = ii + (int64_t)b.NI * (jj + (int64_t)b.NJ * kk);
+          for (int q = 0; q < 4; ++q) fa[d][q * n + o + x] = b.farea[d][q * nf + f];
+        }
+      }
+    }
+    P_.W = P_.W;
+    Check(cudaMemcpy(P_.W, W.data(), W.size() * 8, cudaMemcpyHostToDevice), "upload");
+    P_.vol = m.Upload(vol);
+    for (int d = 0; d < 3; ++d) {
+      P_.width[d] = m.Upload(wid[d]);
+      P_.fa[d] = m.Upload(fa[d]);
+    }
+    P_.mask = m.Upload(mask);
+    P_.blocks = c.d_blocks;
+    P_.solves = c.d_solves;
+    P_.states = c.d_states;
+    P_.cfl = c.d_cfl;
+  }
+
+  ~Runner() override {
+    if (c_.graph) cudaGraphExecDestroy(c_.graph);
+    c_.graph = nullptr;
+  }
+
+  const Pools<T> &P() const { return P_; }
+
+  void StartIteration() {
+    k_cfl<<<(c_.nsolves + 127) / 128, 128, 0, c_.stream>>>(c_.d_solves, c_.nsolves, c_.d_iter,
+                                                            c_.d_cfl);
+  }
+  void FillGhosts() override {
+    StartIteration();
+    Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
+  }
+  void Residual() override {
+    for (int d = 0; d < 3; ++d)
+      Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
+                      (int)c_.L.face_cta_block[d].size(), c_.stream);
+    Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
+                    c_.stream);
+  }
+  void Relax() override {
+    Check(cudaMemsetAsync(P_.dU, 0, 5 * c_.ncell * sizeof(T), c_.stream), "memset");
+    for (int s = 0; s < c_.nsteps; ++s) {
+      const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+      Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
+    }
+    Launch<T>::ConnDu(P_, c_.d_conn_ops, (int)c_.L.conn_ops.size(), c_.stream);
+    for (int s = c_.nsteps - 1; s >= 0; --s) {
+      const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+      Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
+    }
+  }
+  void Update() override {
+    Launch<T>::Update(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_cell_cta_pos0,
+                      c_.d_partials, (int)c_.L.cell_cta_block.size(), c_.stream);
+    k_norms<<<c_.nsolves, 32, 0, c_.stream>>>(c_.d_partials, c_.d_solve_cta0, c_.nsolves,
+                                              c_.d_ring, c_.ring_cap, c_.d_iter,
+                                              c_.d_solves, c_.d_cfl);
+    k_iter_advance<<<1, 1, 0, c_.stream>>>(c_.d_iter);
+  }
+  void OneIteration() {
+    FillGhosts();
+    Residual();
+    Relax();
+    Update();
+  }
+  void Iterate(int n) override {
+    if (!c_.graph) {
+      cudaGraph_t g;
+      Check(cudaStreamBeginCapture(c_.stream, cudaStreamCaptureModeThreadLocal),
+            "begin capture");
+      OneIteration();
+      Check(cudaStreamEndCapture(c_.stream, &g), "end capture");
+      Check(cudaGraphInstantiate(&c_.graph, g, 0), "graph instantiate");
+      cudaGraphDestroy(g);
+    }
+    for (int i = 0; i < n; ++i) Check(cudaGraphLaunch(c_.graph, c_.stream), "graph launch");
+  }
+  void GetDU(int b, double *out) override { CopyOut(P_.dU, 5, b, out); }
+  void GetAinv(int b, double *out) override { CopyOut(P_.Ainv, 1, b, out); }
+
+ private:
+  template <typename U>
+  void CopyOut(const U *pool, int w, int bi, double *out) {
+    const Block &b = c_.setup->blocks[bi];
+    const int64_t nc = b.NCell(), o = c_.cell0[bi], n = c_.ncell;
+    std::vector<U> h(nc);
+    size_t q = 0;
+    std::vector<double> tmp((size_t)b.ni * b.nj * b.nk * w);
+    for (int v = 0; v < w; ++v) {
+      Check(cudaMemcpy(h.data(), pool + v * n + o, nc * sizeof(U), cudaMemcpyDeviceToHost),
+            "download");
+      q = 0;
+      for (int k = 0; k < b.nk; ++k)
+        for (int j = 0; j < b.nj; ++j)
+          for (int i = 0; i < b.ni; ++i) tmp[(q++) * w + v] = (double)h[b.Cell(i, j, k)];
+    }
+    std::memcpy(out, tmp.data(), tmp.size() * sizeof(double));
+  }
+
+  BatchCore &c_;
+  Pools<T> P_{};
+};
+
+}  // namespace ath
+
+struct ath_batch {
+  ath::BatchCore core;
+  std::unique_ptr<ath::RunnerBase> run;
+  double *W = nullptr, *R = nullptr, *dt = nullptr, *lam = nullptr;
+};
+
+namespace ath {
+namespace {
+
+void BuildLists(BatchCore &c) {
+  const auto &st = *c.setup;
+  auto &L = c.L;
+  c.cell0.resize(c.nblocks);
+  c.solve_pos0.resize(c.nblocks);
+  int64_t off = 0;
+  for (int b = 0; b < c.nblocks; ++b) {
+    c.cell0[b] = off;
+    off += st.blocks[b].NCell();
+  }
+  c.ncell = off;
+  if (off >= (int64_t)INT32_MAX) throw Error(ATH_ERR_UNSUPPORTED, "batch too large");
+  // physical cells, padded per block to whole CTAs
+  L.solve_cta0.assign(c.nsolves + 1, 0);
+  for (int s = 0; s < c.nsolves; ++s) {
+    L.solve_cta0[s] = (int32_t)L.cell_cta_block.size();
+    int64_t pos = 0;
+    for (int b : st.solves[s].blocks) {
+      const Block &bk = st.blocks[b];
+      c.solve_pos0[b] = pos;
+      const int64_t start = (int64_t)L.cells.size();
+      for (int k = 0; k < bk.nk; ++k)
+        for (int j = 0; j < bk.nj; ++j)
+          for (int i = 0; i < bk.ni; ++i)
+            L.cells.push_back((int32_t)(c.cell0[b] + bk.Cell(i, j, k)));
+      const int64_t cnt = (int64_t)L.cells.size() - start;
+      const int64_t ncta = (cnt + kCta - 1) / kCta;
+      L.cells.resize(start + ncta * kCta, -1);
+      for (int64_t t = 0; t < ncta; ++t) {
+        L.cell_cta_block.push_back(b);
+        L.cell_cta_pos0.push_back((int32_t)(pos + t * kCta));
+      }
+      pos += cnt;
+    }
+  }
+  L.solve_cta0[c.nsolves] = (int32_t)L.cell_cta_block.size();
+  // faces per direction
+  for (int d = 0; d < 3; ++d) {
+    for (int b = 0; b < c.nblocks; ++b) {
+      const Block &bk = st.blocks[b];
+      const int64_t start = (int64_t)L.faces[d].size();
+      for (int k = 0; k < bk.nk + (d == 2); ++k)
+        for (int j = 0; j < bk.nj + (d == 1); ++j)
+          for (int i = 0; i < bk.ni + (d == 0); ++i)
+            L.faces[d].push_back((int32_t)(c.cell0[b] + bk.Cell(i, j, k)));
+      const int64_t cnt = (int64_t)L.faces[d].size() - start;
+      const int64_t ncta = (cnt + kCta - 1) / kCta;
+      L.faces[d].resize(start + ncta * kCta, -1);
+      for (int64_t t = 0; t < ncta; ++t) L.face_cta_block[d].push_back(b);
+    }
+  }
+  // hyperplane steps: step s holds plane s of every block that has one
+  c.nsteps = 0;
+  for (auto &b : st.blocks) c.nsteps = std::max(c.nsteps, (int)b.plane_offsets.size() - 1);
+  L.step_off.assign(c.nsteps + 1, 0);
+  for (int s = 0; s < c.nsteps; ++s) {
+    L.step_off[s] = (int32_t)L.sweep_items.size();
+    for (int b = 0; b < c.nblocks; ++b) {
+      const Block &bk = st.blocks[b];
+      if (s + 1 >= (int)bk.plane_offsets.size()) continue;
+      for (int q = bk.plane_offsets[s]; q < bk.plane_offsets[s + 1]; ++q)
+        L.sweep_items.push_back(make_int2((int)(c.cell0[b] + bk.plane_cells[q]), b));
+    }
+  }
+  L.step_off[c.nsteps] = (int32_t)L.sweep_items.size();
+  // ghost operations with pool indices
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &bk = st.blocks[b];
+    for (const auto &op : bk.ops) {
+      GhostOpDev g{};
+      g.dst = (int32_t)(c.cell0[b] + op.dst);
+      g.src = (int32_t)(c.cell0[op.src_block] + op.src);
+      g.type = op.type;
+      g.lower = op.lower;
+      g.dir = op.dir;
+      g.state = op.state;
+      g.layer = op.layer;
+      {
+        const int d = op.dir;
+        const int fi = bk.NI + (d == 0), fj = bk.NJ + (d == 1);
+        const int ii = (int)(op.face % fi);
+        const int64_t r = op.face / fi;
+        const int jj = (int)(r % fj), kk = (int)(r / fj);
+        g.face = (int32_t)(c.cell0[b] + ii + (int64_t)bk.NI * (jj + (int64_t)bk.NJ * kk));
+      }
+      L.ops.push_back(g);
+      L.op_solve.push_back(bk.solve);
+      if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK) L.conn_ops.push_back(g);
+    }
+  }
+}
+
+void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags) {
+  auto &c = B->core;
+  c.ctx = ctx;
+  c.setup = &st;
+  c.precision = precision;
+  c.flags = flags;
+  c.nsolves = (int)st.solves.size();
+  c.nblocks = (int)st.blocks.size();
+  for (const auto &b : st.blocks)
+    if (b.nv != 5 || b.ng < 2)
+      throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
+  Check(cudaSetDevice(ctx->device), "cudaSetDevice");
+  BuildLists(c);
+  c.mem.reset(new DevMem(ctx));
+  DevMem &m = *c.mem;
+  std::vector<BlockDev> bd(c.nblocks);
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &k = st.blocks[b];
+    bd[b] = BlockDev{k.ni, k.nj, k.nk, k.ng, k.NI, k.NJ, k.NK, k.solve, c.cell0[b]};
+  }
+  std::vector<SolveDev> sd(c.nsolves);
+  std::vector<ath_bc_state> states;
+  for (int s = 0; s < c.nsolves; ++s) {
+    const auto &p = st.solves[s].phys;
+    SolveDev x{};
+    x.gas_r = p.gas_r;
+    x.gas_n = p.gas_n;
+    x.gas_hf = p.gas_hf;
+    x.kappa = p.kappa;
+    x.theta = p.theta;
+    x.zeta = p.zeta;
+    x.relax = p.relax;
+    x.cfl_start = p.cfl_start;
+    x.cfl_step = p.cfl_step;
+    x.cfl_max = p.cfl_max;
+    x.limiter = p.limiter;
+    x.nstates = (int32_t)st.solves[s].states.size();
+    x.state0 = (int32_t)states.size();
+    for (auto &q : st.solves[s].states) states.push_back(q);
+    sd[s] = x;
+  }
+  c.d_blocks = m.Upload(bd);
+  c.d_solves = m.Upload(sd);
+  c.d_states = m.Upload(states);
+  c.d_cfl = m.Alloc<double>(c.nsolves);
+  c.d_iter = m.Alloc<int64_t>(1);
+  Check(cudaMemset(c.d_iter, 0, sizeof(int64_t)), "memset");
+  c.d_cells = m.Upload(c.L.cells);
+  c.d_cell_cta_block = m.Upload(c.L.cell_cta_block);
+  c.d_cell_cta_pos0 = m.Upload(c.L.cell_cta_pos0);
+  for (int d = 0; d < 3; ++d) {
+    c.d_faces[d] = m.Upload(c.L.faces[d]);
+    c.d_face_cta_block[d] = m.Upload(c.L.face_cta_block[d]);
+  }
+  c.d_sweep = m.Upload(c.L.sweep_items);
+  c.d_solve_cta0 = m.Upload(c.L.solve_cta0);
+  c.d_ops = m.Upload(c.L.ops);
+  c.d_conn_ops = m.Upload(c.L.conn_ops);
+  c.d_op_solve = m.Upload(c.L.op_solve);
+  c.d_partials = m.Alloc<NormPartial>(c.L.cell_cta_block.size());
+  c.d_ring = m.Alloc<NormOut>((size_t)c.ring_cap * c.nsolves);
+  Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  Check(cudaEventCreate(&c.ev0), "event");
+  Check(cudaEventCreate(&c.ev1), "event");
+  if (precision == ATH_PREC_FP64) {
+    auto *r = new Runner<double>(c);
+    B->run.reset(r);
+    B->W = r->P().W;
+    B->R = r->P().R;
+    B->dt = r->P().dt;
+    B->lam = r->P().lam;
+  } else if (precision == ATH_PREC_MIXED) {
+    auto *r = new Runner<float>(c);
+    B->run.reset(r);
+    B->W = r->P().W;
+    B->R = r->P().R;
+    B->dt = r->P().dt;
+    B->lam = r->P().lam;
+  } else {
+    throw Error(ATH_ERR_ARG, "unknown precision");
+  }
+  // launches of one iteration: cfl, ghost, 3 faces, cell, 2 x steps of
+  // sweeps, dU connection copy, update, norms, counter
+  c.launches_per_iter = 1 + (c.L.ops.empty() ? 0 : 1) + 3 + 1 + 2 * c.nsteps +
+                        (c.L.conn_ops.empty() ? 0 : 1) + 3;
+}
+
+// Reads norms of iterations [it0, it0+n) from the ring into norms_h.
+void ReadNorms(BatchCore &c, int64_t it0, int n, ath_norms *norms_h) {
+  if (!norms_h || n <= 0) return;
+  std::vector<NormOut> ring((size_t)c.ring_cap * c.nsolves);
+  Check(cudaMemcpyAsync(ring.data(), c.d_ring, ring.size() * sizeof(NormOut),
+                        cudaMemcpyDeviceToHost, c.stream),
+        "norms download");
+  Check(cudaStreamSynchronize(c.stream), "sync");
+  const auto &st = *c.setup;
+  for (int q = 0; q < n; ++q) {
+    const int64_t it = it0 + q;
+    for (int s = 0; s < c.nsolves; ++s) {
+      const NormOut &o = ring[(it % c.ring_cap) * c.nsolves + s];
+      ath_norms &d = norms_h[(size_t)q * c.nsolves + s];
+      std::memset(&d, 0, sizeof(d));
+      for (int v = 0; v < 7; ++v) d.l2[v] = o.l2[v];
+      d.linf = o.linf;
+      d.cfl = o.cfl;
+      d.status = o.bad ? ATH_ERR_NONPHYSICAL : ATH_OK;
+      d.linf_block = d.linf_i = d.linf_j = d.linf_k = d.linf_eqn = -1;
+      if (o.linf_pos != INT64_MAX) {
+        const int64_t cellpos = o.linf_pos / kNv;
+        d.linf_eqn = (int32_t)(o.linf_pos % kNv) + 1;
+        const auto &blocks = st.solves[s].blocks;
+        for (size_t bi = 0; bi < blocks.size(); ++bi) {
+          const Block &b = st.blocks[blocks[bi]];
+          const int64_t p0 = c.solve_pos0[blocks[bi]];
+          const int64_t cnt = (int64_t)b.ni * b.nj * b.nk;
+          if (cellpos >= p0 && cellpos < p0 + cnt) {
+            const int64_t l = cellpos - p0;
+            d.linf_block = (int32_t)bi;
+            d.linf_i = (int32_t)(l % b.ni);
+            d.linf_j = (int32_t)((l / b.ni) % b.nj);
+            d.linf_k = (int32_t)(l / ((int64_t)b.ni * b.nj));
+          }
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace ath
+
+using ath::Check;
+using ath::Guard;
+
+extern "C" {
+
+int ath_ctx_create(int device, size_t hbm_budget_bytes, ath_ctx **out) {
+  return Guard([&] {
+    if (!out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    int n = 0;
+    Check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (device < 0 || device >= n) throw ath::Error(ATH_ERR_ARG, "no such CUDA device");
+    Check(cudaSetDevice(device), "cudaSetDevice");
+    auto *c = new ath_ctx();
+    c->device = device;
+    c->budget = hbm_budget_bytes;
+    *out = c;
+  });
+}
+
+int ath_ctx_destroy(ath_ctx *ctx) {
+  delete ctx;
+  return ATH_OK;
+}
+
+int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision, int flags,
+                     ath_batch **out) {
+  return Guard([&] {
+    if (!ctx || !setup || !out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto *b = new ath_batch();
+    try {
+      ath::CreateBatch(b, ctx, setup->s, precision, flags);
+    } catch (...) {
+      delete b;
+      throw;
+    }
+    *out = b;
+  });
+}
+
+int ath_batch_destroy(ath_batch *batch) {
+  if (!batch) return ATH_OK;
+  cudaSetDevice(batch->core.ctx->device);
+  if (batch->core.stream) cudaStreamSynchronize(batch->core.stream);
+  batch->run.reset();
+  batch->core.mem.reset();
+  if (batch->core.ev0) cudaEventDestroy(batch->core.ev0);
+  if (batch->core.ev1) cudaEventDestroy(batch->core.ev1);
+  if (batch->core.stream) cudaStreamDestroy(batch->core.stream);
+  delete batch;
+  return ATH_OK;
+}
+
+int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h) {
+  return Guard([&] {
+    if (!batch || n < 0) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    auto &c = batch->core;
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    Check(cudaEventRecord(c.ev0, c.stream), "event");
+    int done = 0;
+    while (done < n) {
+      const int chunk = std::min(n - done, c.ring_cap);
+      const int64_t it0 = c.iter_host;
+      batch->run->Iterate(chunk);
+      c.iter_host += chunk;
+      if (norms_h) ath::ReadNorms(c, it0, chunk, norms_h + (size_t)done * c.nsolves);
+      done += chunk;
+    }
+    Check(cudaEventRecord(c.ev1, c.stream), "event");
+    Check(cudaEventSynchronize(c.ev1), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+    float ms = 0.f;
+    Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
+    c.stats.device_ms = ms;
+    c.stats.kernel_launches = (int64_t)n * c.launches_per_iter;
+  });
+}
+
+int ath_batch_fill_ghosts(ath_batch *batch) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    batch->run->FillGhosts();
+    Check(cudaStreamSynchronize(batch->core.stream), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+  });
+}
+
+int ath_batch_residual(ath_batch *batch) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    batch->run->Residual();
+    Check(cudaStreamSynchronize(batch->core.stream), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+  });
+}
+
+// The local time step and the inverted diagonal are produced by the
+// residual stage's cell kernel (they need only the spectral radius, the
+// volume and the CFL); these two stages exist for call-surface parity and
+// have nothing left to do.
+int ath_batch_timestep(ath_batch *batch) { return batch ? ATH_OK : ATH_ERR_ARG; }
+int ath_batch_diag_invert(ath_batch *batch) { return batch ? ATH_OK : ATH_ERR_ARG; }
+
+int ath_batch_relax(ath_batch *batch) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    batch->run->Relax();
+    Check(cudaStreamSynchronize(batch->core.stream), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+  });
+}
+
+int ath_batch_update(ath_batch *batch, ath_norms *norms_h) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    auto &c = batch->core;
+    const int64_t it0 = c.iter_host;
+    batch->run->Update();
+    c.iter_host += 1;
+    Check(cudaStreamSynchronize(c.stream), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+    ath::ReadNorms(c, it0, 1, norms_h);
+  });
+}
+
+int ath_batch_field_width(ath_batch *batch, int field) {
+  if (!batch) return ATH_ERR_ARG;
+  switch (field) {
+    case ATH_FIELD_STATE:
+    case ATH_FIELD_STATE_GHOSTS:
+    case ATH_FIELD_RESID:
+    case ATH_FIELD_DU:
+      return 5;
+    case ATH_FIELD_DT:
+    case ATH_FIELD_AINV:
+      return 1;
+    case ATH_FIELD_SPECRAD:
+      return 2;
+    default:
+      return ATH_ERR_ARG;
+  }
+}
+
+int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h) {
+  return Guard([&] {
+    if (!batch || !out_h) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto &c = batch->core;
+    if (block < 0 || block >= c.nblocks) throw ath::Error(ATH_ERR_ARG, "block out of range");
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    Check(cudaStreamSynchronize(c.stream), "sync");
+    const ath::Block &b = c.setup->blocks[block];
+    const int64_t nc = b.NCell(), o = c.cell0[block], n = c.ncell;
+    auto gather = [&](const double *pool, int w, bool ghosts) {
+      std::vector<double> h(nc);
+      for (int v = 0; v < w; ++v) {
+        Check(cudaMemcpy(h.data(), pool + v * n + o, nc * 8, cudaMemcpyDeviceToHost),
+              "download");
+        if (ghosts) {
+          for (int64_t x = 0; x < nc; ++x) out_h[x * w + v] = h[x];
+        } else {
+          size_t q = 0;
+          for (int k = 0; k < b.nk; ++k)
+            for (int j = 0; j < b.nj; ++j)
+              for (int i = 0; i < b.ni; ++i) out_h[(q++) * w + v] = h[b.Cell(i, j, k)];
+        }
+      }
+    };
+    switch (field) {
+      case ATH_FIELD_STATE: gather(batch->W, 5, false); break;
+      case ATH_FIELD_STATE_GHOSTS: gather(batch->W, 5, true); break;
+      case ATH_FIELD_RESID: gather(batch->R, 5, false); break;
+      case ATH_FIELD_DT: gather(batch->dt, 1, false); break;
+      case ATH_FIELD_SPECRAD: {
+        const size_t m = (size_t)b.ni * b.nj * b.nk;
+        std::vector<double> lam(m);
+        // spectral radius (flow, turb); no turbulence equations here
+        std::vector<double> h(nc);
+        Check(cudaMemcpy(h.data(), batch->lam + o, nc * 8, cudaMemcpyDeviceToHost), "download");
+        size_t q = 0;
+        for (int k = 0; k < b.nk; ++k)
+          for (int j = 0; j < b.nj; ++j)
+            for (int i = 0; i < b.ni; ++i) {
+              out_h[2 * q] = h[b.Cell(i, j, k)];
+              out_h[2 * q + 1] = 0.0;
+              ++q;
+            }
+        break;
+      }
+      case ATH_FIELD_DU: batch->run->GetDU(block, out_h); break;
+      case ATH_FIELD_AINV: batch->run->GetAinv(block, out_h); break;
+      default: throw ath::Error(ATH_ERR_ARG, "unknown field");
+    }
+  });
+}
+
+int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h) {
+  return Guard([&] {
+    if (!batch || !prim_h) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto &c = batch->core;
+    if (block < 0 || block >= c.nblocks) throw ath::Error(ATH_ERR_ARG, "block out of range");
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    Check(cudaStreamSynchronize(c.stream), "sync");
+    const ath::Block &b = c.setup->blocks[block];
+    const int64_t nc = b.NCell(), o = c.cell0[block], n = c.ncell;
+    std::vector<double> h(nc);
+    for (int v = 0; v < 5; ++v) {
+      Check(cudaMemcpy(h.data(), batch->W + v * n + o, nc * 8, cudaMemcpyDeviceToHost),
+            "download");
+      size_t q = 0;
+      for (int k = 0; k < b.nk; ++k)
+        for (int j = 0; j < b.nj; ++j)
+          for (int i = 0; i < b.ni; ++i) h[b.Cell(i, j, k)] = prim_h[(q++) * 5 + v];
+      Check(cudaMemcpy(batch->W + v * n + o, h.data(), nc * 8, cudaMemcpyHostToDevice),
+            "upload");
+    }
+  });
+}
+
+int ath_batch_stats(ath_batch *batch, ath_stats *out) {
+  if (!batch || !out) return ATH_ERR_ARG;
+  *out = batch->core.stats;
+  return ATH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+// Kernels of the per-iteration path and their device data layout.
+//
+// Layout in HBM (all blocks of all solves of a batch share one pool):
+//   * cell fields are structure-of-arrays, [var][pool cell], over the padded
+//     cells of every block (ghost layers included), i fastest inside a
+//     block;
+//   * face fields of direction d are stored at the pool index of the cell
+//     on the upper side of the face (face i of a block sits at cell i), so
+//     faces and cells share one index space;
+//   * work lists (physical cells, faces of direction d) are padded per block
+//     to a multiple of the CTA size, so every CTA works inside one block and
+//     reads that block's strides once.
+#pragma once
+
+#include <cstdint>
+
+#include "aither_gb300.h"
+#include "physics.cuh"
+
+namespace ath {
+
+constexpr int kCta = 256;   // threads per CTA of the cell/face kernels
+constexpr int kNv = 5;      // equations of the inviscid/laminar path
+
+struct BlockDev {
+  int32_t ni, nj, nk, ng, NI, NJ, NK, solve;
+  int64_t cell0;  // pool index of padded cell (-ng,-ng,-ng)
+};
+
+struct SolveDev {
+  double gas_r, gas_n, gas_hf;
+  double kappa, theta, zeta, relax, cfl_start, cfl_step, cfl_max;
+  int32_t limiter, nstates, state0, pad;
+};
+
+// A ghost-cell assignment with pool indices.
+struct GhostOpDev {
+  int32_t dst, src, type, lower;
+  int32_t face, dir, state, layer;
+};
+
+// Partial norms of one CTA of the update kernel.
+struct NormPartial {
+  double l2[kNv];
+  double linf;
+  int64_t linf_pos;  // position in the solve's loop order, for ties
+  int32_t linf_cell, linf_eqn;
+  int32_t bad;       // nonphysical state produced
+  int32_t pad;
+};
+
+// Device pointers of a batch.  Passed by value to every kernel.
+template <typename T>
+struct Pools {
+  double *W;        // [5][ncell] primitive state, FP64
+  double *R;        // [5][ncell] residual, FP64
+  T *dU;            // [5][ncell] implicit update
+  T *flux[3];       // [5][ncell] F.|A| on faces of direction d
+  double *lam;      // [ncell] cell spectral radius
+  double *dt;       // [ncell]
+  T *Ainv;          // [ncell] inverse of the scalar main diagonal
+  const double *vol;       // [ncell]
+  const double *width[3];  // [ncell]
+  const double *fa[3];     // [4][ncell] unit normal x,y,z and magnitude
+  const uint8_t *mask;     // [ncell] neighbour bits for the sweeps
+  const BlockDev *blocks;
+  const SolveDev *solves;
+  const ath_bc_state *states;
+  const double *cfl;       // [nsolves] current CFL
+  int64_t ncell;
+};
+
+__device__ __forceinline__ int64_t StrideOf(const BlockDev &b, int d) {
+  return d == 0 ? 1 : (d == 1 ? (int64_t)b.NI : (int64_t)b.NI * b.NJ);
+}
+
+template <typename T>
+__device__ __forceinline__ Prim<T> LoadW(const double *W, int64_t n, int64_t c) {
+  Prim<T> s;
+  s.rho = (T)W[c];
+  s.u = (T)W[n + c];
+  s.v = (T)W[2 * n + c];
+  s.w = (T)W[3 * n + c];
+  s.p = (T)W[4 * n + c];
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ Gas<T> GasOf(const SolveDev &s) {
+  Gas<T> g;
+  g.r = (T)s.gas_r;
+  g.n = (T)s.gas_n;
+  g.hf = (T)s.gas_hf;
+  return g;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost cells: boundary states (procBlock::AssignInviscidGhostCells,
+// src/procBlock.cpp:2449, GetGhostState src/ghostStates.cpp:62) and
+// connection copies (SwapStateSlice, src/procBlock.cpp:3050).
+template <typename T>
+__global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
+                        const int32_t *op_solve);
+
+// Face fluxes of direction D over the face list (CalcInvFluxI/J/K,
+// src/procBlock.cpp:384,522,660).
+template <typename T, int D>
+__global__ void k_face(Pools<T> P, const int32_t *list, const int32_t *cta_block);
+
+// Residual assembly, spectral radius, local time step and inverted
+// diagonal of every physical cell (procBlock residual accumulation,
+// CalcBlockTimeStep src/procBlock.cpp:798, AddDiagonalTerms/Invert
+// src/linearSolver.cpp:146,177).
+template <typename T>
+__global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block);
+
+// One hyperplane of the LU-SGS forward / backward sweep
+// (lusgs::LUSGS_Forward/Backward, src/linearSolver.cpp:341,385).
+template <typename T>
+__global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward);
+
+// dU ghost copies across connections (SwapImplicitUpdate, src/utility.cpp:400).
+template <typename T>
+__global__ void k_conn_du(Pools<T> P, const GhostOpDev *ops, int nops);
+
+// Conserved update and per-CTA partial norms (procBlock::UpdateBlock,
+// src/procBlock.cpp:826).
+template <typename T>
+__global__ void k_update(Pools<T> P, const int32_t *list, const int32_t *cta_block,
+                         const int32_t *cta_pos0, NormPartial *partials);
+
+// Per-solve reduction of the CTA partials into the norm ring, CFL of the
+// next iteration, iteration counter (one warp per solve).
+struct NormOut {
+  double l2[7];
+  double linf;
+  int64_t linf_pos;
+  int32_t bad;
+  int32_t pad;
+  double cfl;
+};
+__global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
+                        int nsolves, NormOut *ring, int ring_cap,
+                        int64_t *iter_counter, const SolveDev *solves,
+                        double *cfl);
+// Sets the CFL of the current iteration from the iteration counter
+// (input::CalcCFL, src/input.cpp:647).
+__global__ void k_cfl(const SolveDev *solves, int nsolves,
+                      const int64_t *iter_counter, double *cfl);
+
+// Host-side launchers, one instantiation per arithmetic type (defined in
+// kernels_fp64.cu / kernels_fp32.cu).
+template <typename T>
+struct Launch {
+  static void Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
+                    const int32_t *op_solve, cudaStream_t s);
+  static void Face(int d, const Pools<T> &P, const int32_t *list,
+                   const int32_t *cta_block, int ncta, cudaStream_t s);
+  static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                   int ncta, cudaStream_t s);
+  static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward,
+                    cudaStream_t s);
+  static void ConnDu(const Pools<T> &P, const GhostOpDev *ops, int nops, cudaStream_t s);
+  static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                     const int32_t *cta_pos0, NormPartial *partials, int ncta,
+                     cudaStream_t s);
+};
+
+}  // namespace ath

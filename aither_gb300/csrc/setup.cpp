@@ -1,0 +1,1039 @@
+// Host-side case setup.  Restates, in this project's own code, the parts of
+// the reference that run once before the iteration loop:
+//   input file format           src/input.cpp:167-643
+//   fluid data and reference    src/fluid.cpp:89-101, src/input.cpp:604-621
+//     speed of sound, BC-state  src/inputStates.cpp:464,590,674,775
+//     nondimensionalisation
+//   Plot3D grid                 src/plot3d.cpp:363-445
+//   cell geometry               src/plot3d.cpp:36-360 (centroid, six-pyramid
+//                               volume, diagonal cross-product face areas)
+//   ghost-cell geometry         src/procBlock.cpp:2160-2294
+//   cell widths                 src/procBlock.cpp:6397
+//   connections (periodic,      src/boundaryConditions.cpp:293-1150
+//     interblock) by patch-corner matching
+//   hyperplane visit order      src/utility.cpp:377
+// The arithmetic of the geometry follows the reference operation by
+// operation so the device path sees the same metric terms.
+#include "setup.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+
+namespace ath {
+
+namespace {
+
+std::string Trim(const std::string &s) {
+  size_t a = 0, b = s.size();
+  while (a < b && std::isspace(static_cast<unsigned char>(s[a]))) ++a;
+  while (b > a && std::isspace(static_cast<unsigned char>(s[b - 1]))) --b;
+  return s.substr(a, b - a);
+}
+
+std::vector<std::string> Split(const std::string &s, char sep) {
+  std::vector<std::string> out;
+  std::string cur;
+  for (char c : s) {
+    if (c == sep) {
+      out.push_back(Trim(cur));
+      cur.clear();
+    } else {
+      cur += c;
+    }
+  }
+  out.push_back(Trim(cur));
+  return out;
+}
+
+[[noreturn]] void Fail(const std::string &msg) { throw std::runtime_error(msg); }
+
+int BCType(const std::string &name) {
+  if (name == "slipWall") return ATH_BC_SLIP_WALL;
+  if (name == "viscousWall") return ATH_BC_VISCOUS_WALL;
+  if (name == "characteristic") return ATH_BC_CHARACTERISTIC;
+  if (name == "stagnationInlet") return ATH_BC_STAGNATION_INLET;
+  if (name == "pressureOutlet") return ATH_BC_PRESSURE_OUTLET;
+  if (name == "supersonicInflow") return ATH_BC_SUPERSONIC_INFLOW;
+  if (name == "supersonicOutflow") return ATH_BC_SUPERSONIC_OUTFLOW;
+  if (name == "periodic") return ATH_BC_PERIODIC;
+  if (name == "interblock") return ATH_BC_INTERBLOCK;
+  Fail("unsupported boundary condition type '" + name + "'");
+}
+
+bool IsConnection(int type) {
+  return type == ATH_BC_PERIODIC || type == ATH_BC_INTERBLOCK;
+}
+
+// "[a, b, c]" -> 3 doubles
+void ParseVec3(const std::string &s, double out[3]) {
+  std::string t = s;
+  for (auto &c : t)
+    if (c == '[' || c == ']' || c == ',') c = ' ';
+  std::istringstream is(t);
+  for (int i = 0; i < 3; ++i) {
+    if (!(is >> out[i])) Fail("bad vector '" + s + "'");
+  }
+}
+
+// name(k1=v1; k2=v2; ...) -> name, map
+std::pair<std::string, std::map<std::string, std::string>> ParseCall(
+    const std::string &s) {
+  const auto open = s.find('(');
+  const auto close = s.rfind(')');
+  if (open == std::string::npos || close == std::string::npos || close < open)
+    Fail("bad state definition '" + s + "'");
+  std::map<std::string, std::string> kv;
+  for (auto &tok : Split(s.substr(open + 1, close - open - 1), ';')) {
+    if (tok.empty()) continue;
+    const auto eq = tok.find('=');
+    if (eq == std::string::npos) Fail("bad parameter '" + tok + "'");
+    kv[Trim(tok.substr(0, eq))] = Trim(tok.substr(eq + 1));
+  }
+  return {Trim(s.substr(0, open)), kv};
+}
+
+// split "<a(...), b(...)>" into the individual calls
+std::vector<std::string> SplitList(const std::string &s) {
+  std::vector<std::string> out;
+  std::string body = Trim(s);
+  if (!body.empty() && body.front() == '<') body = body.substr(1);
+  if (!body.empty() && body.back() == '>') body.pop_back();
+  int depth = 0;
+  std::string cur;
+  for (char c : body) {
+    if (c == '(') ++depth;
+    if (c == ')') --depth;
+    if (c == ',' && depth == 0) {
+      if (!Trim(cur).empty()) out.push_back(Trim(cur));
+      cur.clear();
+    } else {
+      cur += c;
+    }
+  }
+  if (!Trim(cur).empty()) out.push_back(Trim(cur));
+  return out;
+}
+
+struct Fluid {
+  double n = 2.5;
+  double molar_mass = 28.97 / 1000.;  // kg/mol
+  double hf = 0.0;
+  double mu_c1 = 1.458e-6, mu_s = 110.4;
+  double k_c1 = 2.495e-3, k_s = 194.0;
+};
+
+// Reads "key: value" lines of a fluid database file (air.dat format).
+bool ReadFluidFile(const std::string &path, Fluid &f) {
+  std::ifstream in(path);
+  if (!in) return false;
+  std::string line;
+  while (std::getline(in, line)) {
+    line = Trim(line);
+    if (line.empty() || line[0] == '#') continue;
+    const auto c = line.find(':');
+    if (c == std::string::npos) continue;
+    const auto key = Trim(line.substr(0, c));
+    const auto val = Trim(line.substr(c + 1));
+    if (key == "n") f.n = std::stod(val);
+    else if (key == "molarMass") f.molar_mass = std::stod(val) / 1000.;
+    else if (key == "heatOfFormation") f.hf = std::stod(val);
+    else if (key == "sutherlandViscosityC1") f.mu_c1 = std::stod(val);
+    else if (key == "sutherlandViscosityS") f.mu_s = std::stod(val);
+    else if (key == "sutherlandConductivityC1") f.k_c1 = std::stod(val);
+    else if (key == "sutherlandConductivityS") f.k_s = std::stod(val);
+  }
+  return true;
+}
+
+std::string DirName(const std::string &p) {
+  const auto s = p.find_last_of('/');
+  return s == std::string::npos ? std::string(".") : p.substr(0, s);
+}
+
+}  // namespace
+
+int Surface::SurfaceId() const {
+  if (i1 == i2) return i1 == 0 ? 1 : 2;
+  if (j1 == j2) return j1 == 0 ? 3 : 4;
+  if (k1 == k2) return k1 == 0 ? 5 : 6;
+  Fail("boundary surface is not a constant-index plane");
+}
+
+std::vector<Block> ReadPlot3d(const std::string &path, double lref) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) Fail("cannot open grid file " + path);
+  int32_t nb = 0;
+  in.read(reinterpret_cast<char *>(&nb), 4);
+  if (!in || nb <= 0 || nb > 1000000) Fail("bad Plot3D header in " + path);
+  std::vector<std::array<int32_t, 3>> dims(nb);
+  for (auto &d : dims) {
+    in.read(reinterpret_cast<char *>(d.data()), 12);
+    if (!in || d[0] < 2 || d[1] < 2 || d[2] < 2) Fail("bad block size in " + path);
+  }
+  std::vector<Block> blocks(nb);
+  for (int b = 0; b < nb; ++b) {
+    auto &blk = blocks[b];
+    blk.ni = dims[b][0] - 1;
+    blk.nj = dims[b][1] - 1;
+    blk.nk = dims[b][2] - 1;
+    const size_t nn = (size_t)dims[b][0] * dims[b][1] * dims[b][2];
+    blk.nodes.resize(3 * nn);
+    in.read(reinterpret_cast<char *>(blk.nodes.data()), 3 * nn * sizeof(double));
+    if (!in) Fail("truncated Plot3D file " + path);
+    for (auto &x : blk.nodes) x = x / lref;
+  }
+  return blocks;
+}
+
+// ---------------------------------------------------------------------------
+// geometry
+namespace {
+struct V3 {
+  double x, y, z;
+};
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double Dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 Cross(V3 a, V3 b) {
+  return {a.y * b.z - a.z * b.y, -1.0 * (a.x * b.z - a.z * b.x),
+          a.x * b.y - a.y * b.x};
+}
+inline double Mag(V3 a) { return std::sqrt(Dot(a, a)); }
+
+V3 NodeV(const Block &b, int i, int j, int k) {
+  return {b.Node(0, i, j, k), b.Node(1, i, j, k), b.Node(2, i, j, k)};
+}
+
+double Pyramid(V3 p, V3 a, V3 bb, V3 c, V3 d) {
+  const V3 xp = 0.25 * ((((a - p) + (bb - p)) + (c - p)) + (d - p));
+  const V3 xac = c - a;
+  const V3 xbd = d - bb;
+  return 1.0 / 6.0 * Dot(xp, Cross(xac, xbd));
+}
+
+void StoreArea(std::vector<double> &fa, int64_t nf, int64_t idx, V3 a) {
+  const double m = Mag(a);
+  fa[idx] = a.x / m;
+  fa[nf + idx] = a.y / m;
+  fa[2 * nf + idx] = a.z / m;
+  fa[3 * nf + idx] = m;
+}
+
+V3 GetV(const std::vector<double> &v, int64_t n, int64_t idx) {
+  return {v[idx], v[n + idx], v[2 * n + idx]};
+}
+void SetV(std::vector<double> &v, int64_t n, int64_t idx, V3 a) {
+  v[idx] = a.x;
+  v[n + idx] = a.y;
+  v[2 * n + idx] = a.z;
+}
+}  // namespace
+
+void BuildGeometry(Block &b) {
+  b.NI = b.ni + 2 * b.ng;
+  b.NJ = b.nj + 2 * b.ng;
+  b.NK = b.nk + 2 * b.ng;
+  const int64_t nc = b.NCell();
+  b.vol.assign(nc, 0.0);
+  b.center.assign(3 * nc, 0.0);
+  b.width.assign(3 * nc, 0.0);
+  b.wall_dist.assign(nc, 1.0e10);
+  for (int d = 0; d < 3; ++d) {
+    b.farea[d].assign(4 * b.NFace(d), 0.0);
+    b.fcenter[d].assign(3 * b.NFace(d), 0.0);
+  }
+  for (int k = 0; k < b.nk; ++k)
+    for (int j = 0; j < b.nj; ++j)
+      for (int i = 0; i < b.ni; ++i) {
+        const V3 c0 = NodeV(b, i, j, k), c1 = NodeV(b, i + 1, j, k),
+                 c2 = NodeV(b, i, j + 1, k), c3 = NodeV(b, i + 1, j + 1, k),
+                 c4 = NodeV(b, i, j, k + 1), c5 = NodeV(b, i + 1, j, k + 1),
+                 c6 = NodeV(b, i, j + 1, k + 1),
+                 c7 = NodeV(b, i + 1, j + 1, k + 1);
+        const V3 cen =
+            0.125 * (((((((c0 + c1) + c2) + c3) + c4) + c5) + c6) + c7);
+        double v = 0.0;
+        v += Pyramid(cen, c0, c4, c6, c2);
+        v += Pyramid(cen, c1, c3, c7, c5);
+        v += Pyramid(cen, c0, c1, c5, c4);
+        v += Pyramid(cen, c2, c6, c7, c3);
+        v += Pyramid(cen, c0, c2, c3, c1);
+        v += Pyramid(cen, c4, c5, c7, c6);
+        if (!(v > 0)) Fail("non-positive cell volume in grid");
+        const auto id = b.Cell(i, j, k);
+        b.vol[id] = v;
+        SetV(b.center, nc, id, cen);
+      }
+  // i-faces
+  {
+    const int64_t nf = b.NFace(0);
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i <= b.ni; ++i) {
+          const V3 xac = NodeV(b, i, j + 1, k + 1) - NodeV(b, i, j, k);
+          const V3 xbd = NodeV(b, i, j + 1, k) - NodeV(b, i, j, k + 1);
+          const auto id = b.Face(0, i, j, k);
+          StoreArea(b.farea[0], nf, id, 0.5 * Cross(xbd, xac));
+          SetV(b.fcenter[0], nf, id,
+               0.25 * (((NodeV(b, i, j, k) + NodeV(b, i, j + 1, k)) +
+                        NodeV(b, i, j, k + 1)) +
+                       NodeV(b, i, j + 1, k + 1)));
+        }
+  }
+  // j-faces
+  {
+    const int64_t nf = b.NFace(1);
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j <= b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i) {
+          const V3 xac = NodeV(b, i, j, k + 1) - NodeV(b, i + 1, j, k);
+          const V3 xbd = NodeV(b, i, j, k) - NodeV(b, i + 1, j, k + 1);
+          const auto id = b.Face(1, i, j, k);
+          StoreArea(b.farea[1], nf, id, 0.5 * Cross(xbd, xac));
+          SetV(b.fcenter[1], nf, id,
+               0.25 * (((NodeV(b, i, j, k) + NodeV(b, i + 1, j, k)) +
+                        NodeV(b, i, j, k + 1)) +
+                       NodeV(b, i + 1, j, k + 1)));
+        }
+  }
+  // k-faces
+  {
+    const int64_t nf = b.NFace(2);
+    for (int k = 0; k <= b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i) {
+          const V3 xac = NodeV(b, i, j + 1, k) - NodeV(b, i + 1, j, k);
+          const V3 xbd = NodeV(b, i + 1, j + 1, k) - NodeV(b, i, j, k);
+          const auto id = b.Face(2, i, j, k);
+          StoreArea(b.farea[2], nf, id, 0.5 * Cross(xbd, xac));
+          SetV(b.fcenter[2], nf, id,
+               0.25 * (((NodeV(b, i, j, k) + NodeV(b, i + 1, j, k)) +
+                        NodeV(b, i, j + 1, k)) +
+                       NodeV(b, i + 1, j + 1, k)));
+        }
+  }
+}
+
+namespace {
+// Index helpers for a surface-normal direction d and in-plane directions
+// (d1, d2) following the reference's convention: i-surface (j, k),
+// j-surface (k, i), k-surface (i, j).
+inline void InPlane(int d, int &d1, int &d2) {
+  d1 = (d + 1) % 3;
+  d2 = (d + 2) % 3;
+}
+inline std::array<int, 3> Ijk(int d, int a, int d1, int b1, int d2, int b2) {
+  std::array<int, 3> r{};
+  r[d] = a;
+  r[d1] = b1;
+  r[d2] = b2;
+  return r;
+}
+inline int Ncell(const Block &b, int d) {
+  return d == 0 ? b.ni : (d == 1 ? b.nj : b.nk);
+}
+inline void SurfRange(const Surface &s, int d, int &lo, int &hi) {
+  if (d == 0) { lo = s.i1; hi = s.i2; }
+  else if (d == 1) { lo = s.j1; hi = s.j2; }
+  else { lo = s.k1; hi = s.k2; }
+}
+}  // namespace
+
+void BuildGhostGeometry(Block &b) {
+  const int64_t nc = b.NCell();
+  for (int layer = 1; layer <= b.ng; ++layer) {
+    for (const auto &s : b.surfs) {
+      if (s.type == ATH_BC_INTERBLOCK) continue;
+      const int d = s.Dir();
+      int d1, d2;
+      InPlane(d, d1, d2);
+      const int n = Ncell(b, d);
+      const bool lower = s.Lower();
+      int g, ic, pc, pic, ifc, pifc;
+      if (!lower) {
+        g = n + layer - 1;
+        ic = n - layer;
+        pc = g - 1;
+        if (ic < 0) ic = 0;
+        pic = ic + 1;
+        ifc = n - layer;
+        if (ifc < 0) ifc = 0;
+        pifc = ifc + 1;
+      } else {
+        g = -layer;
+        ic = layer - 1;
+        pc = g + 1;
+        if (ic >= n) ic = n - 1;
+        pic = ic - 1;
+        ifc = layer;
+        if (ifc > n) ifc = n;
+        pifc = ifc - 1;
+      }
+      int lo1, hi1, lo2, hi2;
+      SurfRange(s, d1, lo1, hi1);
+      SurfRange(s, d2, lo2, hi2);
+      for (int b2 = lo2; b2 < hi2; ++b2)
+        for (int b1 = lo1; b1 < hi1; ++b1) {
+          const auto G = Ijk(d, g, d1, b1, d2, b2);
+          const auto I = Ijk(d, ic, d1, b1, d2, b2);
+          const auto P = Ijk(d, pc, d1, b1, d2, b2);
+          const auto PI = Ijk(d, pic, d1, b1, d2, b2);
+          const auto gid = b.Cell(G[0], G[1], G[2]);
+          const auto iid = b.Cell(I[0], I[1], I[2]);
+          b.vol[gid] = b.vol[iid];
+          // face areas: the ghost's outward face mirrors the interior
+          // cell's face on the far side; the other faces copy straight over
+          for (int fd = 0; fd < 3; ++fd) {
+            const int64_t nf = b.NFace(fd);
+            auto copy_face = [&](std::array<int, 3> to, std::array<int, 3> from) {
+              const auto t = b.Face(fd, to[0], to[1], to[2]);
+              const auto f = b.Face(fd, from[0], from[1], from[2]);
+              for (int c = 0; c < 4; ++c) b.farea[fd][c * nf + t] = b.farea[fd][c * nf + f];
+            };
+            if (fd == d) {
+              auto to = G, from = I;
+              if (lower) { from[d] = ic + 1; }   // far face of the interior
+              else { to[d] = g + 1; }            // far face of the ghost
+              copy_face(to, from);
+            } else {
+              copy_face(G, I);
+              auto G2 = G, I2 = I;
+              G2[fd] += 1;
+              I2[fd] += 1;
+              copy_face(G2, I2);
+            }
+          }
+          // centres
+          auto FcAt = [&](int fd, std::array<int, 3> c) {
+            return GetV(b.fcenter[fd], b.NFace(fd), b.Face(fd, c[0], c[1], c[2]));
+          };
+          auto IF = Ijk(d, ifc, d1, b1, d2, b2);
+          auto PIF = Ijk(d, pifc, d1, b1, d2, b2);
+          const V3 distF2F = FcAt(d, PIF) - FcAt(d, IF);
+          const V3 distC2C =
+              layer > 1 ? GetV(b.center, nc, b.Cell(PI[0], PI[1], PI[2])) -
+                              GetV(b.center, nc, iid)
+                        : distF2F;
+          for (int fd = 0; fd < 3; ++fd) {
+            const int64_t nf = b.NFace(fd);
+            if (fd == d) {
+              auto to = G, from = P;
+              if (!lower) { to[d] = g + 1; from[d] = pc + 1; }
+              SetV(b.fcenter[fd], nf, b.Face(fd, to[0], to[1], to[2]),
+                   distF2F + FcAt(fd, from));
+            } else {
+              SetV(b.fcenter[fd], nf, b.Face(fd, G[0], G[1], G[2]),
+                   distC2C + FcAt(fd, P));
+              auto G2 = G, P2 = P;
+              G2[fd] += 1;
+              P2[fd] += 1;
+              SetV(b.fcenter[fd], nf, b.Face(fd, G2[0], G2[1], G2[2]),
+                   distC2C + FcAt(fd, P2));
+            }
+          }
+          SetV(b.center, nc, gid,
+               GetV(b.center, nc, b.Cell(P[0], P[1], P[2])) + distC2C);
+        }
+    }
+  }
+}
+
+void BuildCellWidths(Block &b) {
+  const int64_t nc = b.NCell();
+  for (int k = -b.ng; k < b.nk + b.ng; ++k)
+    for (int j = -b.ng; j < b.nj + b.ng; ++j)
+      for (int i = -b.ng; i < b.ni + b.ng; ++i) {
+        const auto id = b.Cell(i, j, k);
+        for (int d = 0; d < 3; ++d) {
+          const int64_t nf = b.NFace(d);
+          const V3 a = GetV(b.fcenter[d], nf, b.Face(d, i, j, k));
+          const V3 c = GetV(b.fcenter[d], nf,
+                            b.Face(d, i + (d == 0), j + (d == 1), k + (d == 2)));
+          b.width[d * nc + id] = Mag(a - c);
+        }
+      }
+}
+
+void BuildHyperplanes(Block &b) {
+  const int np = b.ni + b.nj + b.nk - 2;
+  b.plane_offsets.assign(np + 1, 0);
+  b.plane_cells.clear();
+  b.plane_cells.reserve((size_t)b.ni * b.nj * b.nk);
+  // planes p = i+j+k; inside a plane k, then j, then i ascending (the
+  // reference's visit order; cells of one plane are independent)
+  std::vector<int32_t> count(np, 0);
+  for (int k = 0; k < b.nk; ++k)
+    for (int j = 0; j < b.nj; ++j)
+      for (int i = 0; i < b.ni; ++i) count[i + j + k]++;
+  for (int p = 0; p < np; ++p) b.plane_offsets[p + 1] = b.plane_offsets[p] + count[p];
+  b.plane_cells.resize(b.plane_offsets[np]);
+  std::vector<int32_t> fill(b.plane_offsets.begin(), b.plane_offsets.end() - 1);
+  for (int k = 0; k < b.nk; ++k)
+    for (int j = 0; j < b.nj; ++j)
+      for (int i = 0; i < b.ni; ++i)
+        b.plane_cells[fill[i + j + k]++] = (int32_t)b.Cell(i, j, k);
+}
+
+// ---------------------------------------------------------------------------
+// ghost-cell operations and connections
+namespace {
+
+struct Patch {
+  int block, surf;
+  int d, d1, d2;
+  bool lower;
+  int lo1, hi1, lo2, hi2;  // node ranges in d1, d2
+  int plane;               // node index of the plane along d
+  V3 Corner(const Block &b, int a1, int a2) const {
+    const auto c = Ijk(d, plane, d1, a1, d2, a2);
+    return NodeV(b, c[0], c[1], c[2]);
+  }
+};
+
+bool Close(V3 a, V3 b, double tol) {
+  return std::fabs(a.x - b.x) < tol && std::fabs(a.y - b.y) < tol &&
+         std::fabs(a.z - b.z) < tol;
+}
+
+// Maps each node (a1, a2) of patch A to a node of patch B.  Returns false
+// when the four corners of the patches do not coincide (after shifting A by
+// `shift`) in any of the 8 orientations.
+bool MatchPatches(const Setup &st, const Patch &A, const Patch &B, V3 shift,
+                  int m[2][3]) {
+  const Block &ba = st.blocks[A.block], &bb = st.blocks[B.block];
+  const int na1 = A.hi1 - A.lo1, na2 = A.hi2 - A.lo2;
+  const int nb1 = B.hi1 - B.lo1, nb2 = B.hi2 - B.lo2;
+  if (!((na1 == nb1 && na2 == nb2) || (na1 == nb2 && na2 == nb1))) return false;
+  double scale = 0.0;
+  for (int a2 : {A.lo2, A.hi2})
+    for (int a1 : {A.lo1, A.hi1}) scale = std::max(scale, Mag(A.Corner(ba, a1, a2)));
+  const double tol = 1e-10 * std::max(1.0, scale);
+  const V3 oA = A.Corner(ba, A.lo1, A.lo2) + shift;
+  const V3 cA1 = A.Corner(ba, A.hi1, A.lo2) + shift;
+  const V3 cA2 = A.Corner(ba, A.lo1, A.hi2) + shift;
+  // candidate B node for a corner of A: try all four B corners
+  const int cb1[2] = {B.lo1, B.hi1}, cb2[2] = {B.lo2, B.hi2};
+  for (int o = 0; o < 4; ++o) {
+    const int ob1 = cb1[o & 1], ob2 = cb2[o >> 1];
+    if (!Close(oA, B.Corner(bb, ob1, ob2), tol)) continue;
+    for (int c = 0; c < 4; ++c) {
+      const int x1 = cb1[c & 1], x2 = cb2[c >> 1];
+      if (!Close(cA1, B.Corner(bb, x1, x2), tol)) continue;
+      for (int e = 0; e < 4; ++e) {
+        const int y1 = cb1[e & 1], y2 = cb2[e >> 1];
+        if (!Close(cA2, B.Corner(bb, y1, y2), tol)) continue;
+        // b = o + a1*(c-o)/na1 + a2*(e-o)/na2 in node space
+        const int s11 = (x1 - ob1) / std::max(na1, 1), s12 = (x2 - ob2) / std::max(na1, 1);
+        const int s21 = (y1 - ob1) / std::max(na2, 1), s22 = (y2 - ob2) / std::max(na2, 1);
+        if (std::abs(s11) + std::abs(s12) != 1 || std::abs(s21) + std::abs(s22) != 1)
+          continue;
+        m[0][0] = ob1 - (A.lo1 * s11 + A.lo2 * s21);
+        m[0][1] = s11;
+        m[0][2] = s21;
+        m[1][0] = ob2 - (A.lo1 * s12 + A.lo2 * s22);
+        m[1][1] = s12;
+        m[1][2] = s22;
+        return true;
+      }
+    }
+  }
+  return false;
+}
+
+// Adds the ghost ops that copy B's interior into A's ghost layers, plus
+// ghost geometry of those cells.
+void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const int m[2][3],
+                   int type, V3 shift) {
+  Block &ba = st.blocks[A.block];
+  const Block &bb = st.blocks[B.block];
+  const int nA = Ncell(ba, A.d), nB = Ncell(bb, B.d);
+  const int64_t ncA = ba.NCell(), ncB = bb.NCell();
+  for (int layer = 1; layer <= ba.ng; ++layer) {
+    const int g = A.lower ? -layer : nA + layer - 1;
+    int s = B.lower ? layer - 1 : nB - layer;
+    if (s < 0) s = 0;
+    if (s >= nB) s = nB - 1;
+    for (int a2 = A.lo2; a2 < A.hi2; ++a2)
+      for (int a1 = A.lo1; a1 < A.hi1; ++a1) {
+        // the cell spans nodes a1..a1+1, a2..a2+1 of A; map both ends
+        int bn1[2], bn2[2];
+        for (int t = 0; t < 2; ++t) {
+          const int n1 = a1 + t, n2 = a2 + t;
+          bn1[t] = m[0][0] + n1 * m[0][1] + n2 * m[0][2];
+          bn2[t] = m[1][0] + n1 * m[1][1] + n2 * m[1][2];
+        }
+        const int c1 = std::min(bn1[0], bn1[1]), c2 = std::min(bn2[0], bn2[1]);
+        const auto G = Ijk(A.d, g, A.d1, a1, A.d2, a2);
+        const auto S = Ijk(B.d, s, B.d1, c1, B.d2, c2);
+        ath_ghost_op op{};
+        op.dst = ba.Cell(G[0], G[1], G[2]);
+        op.src = bb.Cell(S[0], S[1], S[2]);
+        op.src_block = B.block;
+        op.type = type;
+        op.layer = layer;
+        op.dir = A.d;
+        op.lower = A.lower ? 1 : 0;
+        op.state = -1;
+        {
+          auto F = Ijk(A.d, A.lower ? 0 : nA, A.d1, a1, A.d2, a2);
+          op.face = ba.Face(A.d, F[0], F[1], F[2]);
+        }
+        op.src2 = -1;
+        ba.ops.push_back(op);
+        // ghost geometry from the donor cell
+        ba.vol[op.dst] = bb.vol[op.src];
+        for (int c = 0; c < 3; ++c)
+          ba.center[c * ncA + op.dst] =
+              bb.center[c * ncB + op.src] - (c == 0 ? shift.x : c == 1 ? shift.y : shift.z);
+        // widths: A's direction d maps to B's direction d; in-plane
+        // directions map through the orientation
+        auto wB = [&](int dir) { return bb.width[dir * ncB + op.src]; };
+        ba.width[A.d * ncA + op.dst] = wB(B.d);
+        const int dir_of_a1 = (m[0][1] != 0) ? B.d1 : B.d2;
+        const int dir_of_a2 = (m[0][2] != 0) ? B.d1 : B.d2;
+        ba.width[A.d1 * ncA + op.dst] = wB(dir_of_a1);
+        ba.width[A.d2 * ncA + op.dst] = wB(dir_of_a2);
+      }
+  }
+}
+
+}  // namespace
+
+void BuildGhostOps(Setup &st, int solve) {
+  auto &sv = st.solves[solve];
+  // boundary-state lookup by tag
+  auto state_of_tag = [&](int tag) {
+    for (size_t i = 0; i < sv.states.size(); ++i)
+      if (sv.states[i].tag == tag) return (int)i;
+    return -1;
+  };
+  std::vector<Patch> conns;
+  for (int bi : sv.blocks) {
+    Block &b = st.blocks[bi];
+    b.ops.clear();
+    for (size_t si = 0; si < b.surfs.size(); ++si) {
+      const auto &s = b.surfs[si];
+      const int d = s.Dir();
+      int d1, d2;
+      InPlane(d, d1, d2);
+      Patch p{bi, (int)si, d, d1, d2, s.Lower(), 0, 0, 0, 0, 0};
+      SurfRange(s, d1, p.lo1, p.hi1);
+      SurfRange(s, d2, p.lo2, p.hi2);
+      int lo, hi;
+      SurfRange(s, d, lo, hi);
+      p.plane = lo;
+      if (IsConnection(s.type)) {
+        conns.push_back(p);
+        continue;
+      }
+      int st_idx = -1;
+      if (s.type != ATH_BC_SLIP_WALL && s.type != ATH_BC_SUPERSONIC_OUTFLOW) {
+        st_idx = state_of_tag(s.tag);
+        if (st_idx < 0)
+          Fail("no boundary state for tag " + std::to_string(s.tag));
+      }
+      const int n = Ncell(b, d);
+      for (int layer = 1; layer <= b.ng; ++layer) {
+        int g, ic, ac;
+        if (s.Lower()) {
+          g = -layer;
+          ic = std::min(layer - 1, n - 1);
+          ac = 0;
+        } else {
+          g = n + layer - 1;
+          ic = std::max(n - layer, 0);
+          ac = n - 1;
+        }
+        const bool reflect =
+            s.type == ATH_BC_SLIP_WALL || s.type == ATH_BC_VISCOUS_WALL;
+        for (int b2 = p.lo2; b2 < p.hi2; ++b2)
+          for (int b1 = p.lo1; b1 < p.hi1; ++b1) {
+            const auto G = Ijk(d, g, d1, b1, d2, b2);
+            const auto I = Ijk(d, reflect ? ic : ac, d1, b1, d2, b2);
+            const auto F = Ijk(d, s.Lower() ? 0 : n, d1, b1, d2, b2);
+            ath_ghost_op op{};
+            op.dst = b.Cell(G[0], G[1], G[2]);
+            op.src = b.Cell(I[0], I[1], I[2]);
+            op.src_block = bi;
+            op.type = s.type;
+            op.layer = layer;
+            op.dir = d;
+            op.lower = s.Lower() ? 1 : 0;
+            op.state = st_idx;
+            op.face = b.Face(d, F[0], F[1], F[2]);
+            op.src2 = -1;
+            b.ops.push_back(op);
+          }
+      }
+    }
+  }
+  // pair up connection patches: periodic by tag pairs, interblock by
+  // coincident corners
+  std::vector<bool> used(conns.size(), false);
+  for (size_t a = 0; a < conns.size(); ++a) {
+    if (used[a]) continue;
+    const Patch &A = conns[a];
+    const Surface &sa = st.blocks[A.block].surfs[A.surf];
+    bool found = false;
+    for (size_t c = a + 1; c < conns.size() && !found; ++c) {
+      if (used[c]) continue;
+      const Patch &B = conns[c];
+      const Surface &sb = st.blocks[B.block].surfs[B.surf];
+      if (sa.type != sb.type) continue;
+      V3 shift{0, 0, 0};
+      if (sa.type == ATH_BC_PERIODIC) {
+        const BCStateIn *ps = nullptr;
+        for (auto &si : sv.states_in)
+          if ((si.start_tag == sa.tag && si.end_tag == sb.tag) ||
+              (si.start_tag == sb.tag && si.end_tag == sa.tag))
+            ps = &si;
+        if (!ps) continue;
+        shift = {ps->translation[0], ps->translation[1], ps->translation[2]};
+        if (ps->start_tag == sb.tag) shift = -1.0 * shift;
+      }
+      int mab[2][3], mba[2][3];
+      if (!MatchPatches(st, A, B, shift, mab)) continue;
+      if (!MatchPatches(st, B, A, -1.0 * shift, mba))
+        Fail("connection patches match one way only");
+      ConnectOneWay(st, A, B, mab, sa.type, shift);
+      ConnectOneWay(st, B, A, mba, sa.type, -1.0 * shift);
+      used[a] = used[c] = true;
+      found = true;
+    }
+    if (!found)
+      Fail("no partner found for connection surface with tag " +
+           std::to_string(sa.tag));
+  }
+  // neighbour masks for the implicit off-diagonal sums
+  for (int bi : sv.blocks) {
+    Block &b = st.blocks[bi];
+    b.nbr_mask.assign(b.NCell(), 0);
+    std::vector<uint8_t> conn_face[3];
+    for (int d = 0; d < 3; ++d) conn_face[d].assign(b.NFace(d), 0);
+    for (const auto &s : b.surfs) {
+      if (!IsConnection(s.type)) continue;
+      const int d = s.Dir();
+      int d1, d2;
+      InPlane(d, d1, d2);
+      int lo1, hi1, lo2, hi2, lo, hi;
+      SurfRange(s, d1, lo1, hi1);
+      SurfRange(s, d2, lo2, hi2);
+      SurfRange(s, d, lo, hi);
+      for (int b2 = lo2; b2 < hi2; ++b2)
+        for (int b1 = lo1; b1 < hi1; ++b1) {
+          const auto F = Ijk(d, lo, d1, b1, d2, b2);
+          conn_face[d][b.Face(d, F[0], F[1], F[2])] = 1;
+        }
+    }
+    const int n[3] = {b.ni, b.nj, b.nk};
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i) {
+          const int c[3] = {i, j, k};
+          uint8_t m = 0;
+          for (int d = 0; d < 3; ++d) {
+            int lc[3] = {i, j, k}, uc[3] = {i, j, k};
+            uc[d] += 1;
+            if (c[d] > 0 || conn_face[d][b.Face(d, lc[0], lc[1], lc[2])])
+              m |= (uint8_t)(1u << (2 * d));
+            if (c[d] < n[d] - 1 || conn_face[d][b.Face(d, uc[0], uc[1], uc[2])])
+              m |= (uint8_t)(1u << (2 * d + 1));
+          }
+          b.nbr_mask[b.Cell(i, j, k)] = m;
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// input file
+void AppendInput(Setup &st, const std::string &path) {
+  std::ifstream in(path);
+  if (!in) Fail("cannot open input file " + path);
+  std::map<std::string, std::string> kv;
+  std::vector<std::string> bc_lines;
+  std::string line;
+  std::string pending_key, pending_val;
+  bool reading_bcs = false;
+  while (std::getline(in, line)) {
+    const auto hash = line.find('#');
+    if (hash != std::string::npos) line = line.substr(0, hash);
+    line = Trim(line);
+    if (line.empty()) continue;
+    if (!pending_key.empty()) {
+      pending_val += " " + line;
+      if (line.find('>') != std::string::npos) {
+        kv[pending_key] = pending_val;
+        pending_key.clear();
+      }
+      continue;
+    }
+    if (reading_bcs) {
+      bc_lines.push_back(line);
+      continue;
+    }
+    const auto colon = line.find(':');
+    if (colon == std::string::npos) Fail("cannot parse input line '" + line + "'");
+    const auto key = Trim(line.substr(0, colon));
+    const auto val = Trim(line.substr(colon + 1));
+    if (key == "boundaryConditions") {
+      kv[key] = val;
+      reading_bcs = true;
+      continue;
+    }
+    if (val.find('<') != std::string::npos && val.find('>') == std::string::npos) {
+      pending_key = key;
+      pending_val = val;
+      continue;
+    }
+    kv[key] = val;
+  }
+  auto get = [&](const std::string &k, const std::string &def) {
+    auto it = kv.find(k);
+    return it == kv.end() ? def : it->second;
+  };
+  auto getd = [&](const std::string &k, double def) {
+    auto it = kv.find(k);
+    return it == kv.end() ? def : std::stod(it->second);
+  };
+
+  Solve sv;
+  sv.name = path;
+  auto &ph = sv.phys;
+  // scheme
+  const auto eqn = get("equationSet", "euler");
+  ph.eqn = eqn == "euler" ? ATH_EQN_EULER
+           : eqn == "navierStokes" ? ATH_EQN_NAVIER_STOKES
+           : eqn == "rans" ? ATH_EQN_RANS
+           : (Fail("unsupported equationSet " + eqn), 0);
+  const auto ti = get("timeIntegration", "explicitEuler");
+  if (ti != "implicitEuler") Fail("only timeIntegration implicitEuler is supported");
+  ph.theta = 1.0;
+  ph.zeta = 0.0;
+  const auto fr = get("faceReconstruction", "constant");
+  ph.kappa = -2.0;
+  if (fr == "upwind") { ph.recon = ATH_RECON_MUSCL; ph.kappa = -1.0; }
+  else if (fr == "fromm") { ph.recon = ATH_RECON_MUSCL; ph.kappa = 0.0; }
+  else if (fr == "quick") { ph.recon = ATH_RECON_MUSCL; ph.kappa = 0.5; }
+  else if (fr == "central") { ph.recon = ATH_RECON_MUSCL; ph.kappa = 1.0; }
+  else if (fr == "thirdOrder") { ph.recon = ATH_RECON_MUSCL; ph.kappa = 1.0 / 3.0; }
+  else if (fr == "constant") { ph.recon = ATH_RECON_CONSTANT; }
+  else if (fr == "weno") { ph.recon = ATH_RECON_WENO; }
+  else if (fr == "wenoZ") { ph.recon = ATH_RECON_WENOZ; }
+  else Fail("unsupported faceReconstruction " + fr);
+  if (ph.recon != ATH_RECON_MUSCL) Fail("only MUSCL reconstruction is supported");
+  const auto lim = get("limiter", "none");
+  ph.limiter = lim == "none" ? ATH_LIMITER_NONE
+               : lim == "minmod" ? ATH_LIMITER_MINMOD
+               : lim == "vanAlbada" ? ATH_LIMITER_VANALBADA
+               : (Fail("unsupported limiter " + lim), 0);
+  const auto flux = get("inviscidFlux", "roe");
+  ph.flux = flux == "roe" ? ATH_FLUX_ROE : flux == "ausm" ? ATH_FLUX_AUSM
+            : (Fail("unsupported inviscidFlux " + flux), 0);
+  if (ph.flux != ATH_FLUX_ROE) Fail("only the roe inviscid flux is supported");
+  const auto ms = get("matrixSolver", "lusgs");
+  ph.solver = ms == "lusgs" ? ATH_SOLVER_LUSGS : ms == "blusgs" ? ATH_SOLVER_BLUSGS
+              : (Fail("unsupported matrixSolver " + ms), 0);
+  if (ph.solver != ATH_SOLVER_LUSGS) Fail("only matrixSolver lusgs is supported");
+  ph.sweeps = (int)getd("matrixSweeps", 1);
+  if (ph.sweeps != 1) Fail("only matrixSweeps 1 is supported");
+  ph.relax = getd("matrixRelaxation", 1.0);
+  ph.cfl_start = getd("cflStart", 1.0);
+  ph.cfl_step = getd("cflStep", 0.0);
+  ph.cfl_max = getd("cflMax", 1.0);
+  if (get("timeStep", "-1") != "-1" && getd("timeStep", -1.0) > 0)
+    Fail("global time step (timeStep) is not supported");
+  if (getd("dualTimeCFL", -1.0) > 0) Fail("dualTimeCFL is not supported");
+  if (get("inviscidFluxJacobian", "rusanov") != "rusanov")
+    Fail("only the rusanov inviscid flux jacobian is supported");
+  if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
+  if (get("turbulenceModel", "none") != "none" && ph.eqn != ATH_EQN_RANS)
+    Fail("turbulence model needs equationSet rans");
+  if (ph.eqn != ATH_EQN_EULER) Fail("only equationSet euler is supported");
+  ph.turb = ATH_TURB_NONE;
+  ph.nv = 5;
+  ph.ng = 2;
+
+  // fluid and references
+  Fluid fl;
+  {
+    const auto dir = DirName(path);
+    if (!ReadFluidFile(dir + "/air.dat", fl)) {
+      const char *inst = std::getenv("AITHER_INSTALL_DIRECTORY");
+      if (inst) ReadFluidFile(std::string(inst) + "/fluidDatabase/air.dat", fl);
+    }
+  }
+  const double tref = getd("referenceTemperature", -1.0);
+  const double rref = getd("referenceDensity", -1.0);
+  const double lref = getd("referenceLength", 1.0);
+  if (!(tref > 0) || !(rref > 0)) Fail("reference temperature and density are required");
+  const double ru = 8.3144598;  // J/mol-K
+  const double gas_const_dim = ru / fl.molar_mass;
+  double aref = 0.0;
+  {
+    const double gamma = (fl.n + 1) / fl.n;
+    aref += 1.0 * gamma * gas_const_dim * tref;
+    aref = std::sqrt(aref);
+  }
+  const double hf_nd = fl.hf / (fl.molar_mass * (aref * aref));
+  const double mm_nd = fl.molar_mass / (rref / std::pow(lref, 3.0));
+  const double ru_nd = ru / (aref * aref * rref / (tref * std::pow(lref, 3.0)));
+  ph.gas_r = ru_nd / mm_nd;
+  ph.gas_n = fl.n;
+  ph.gas_hf = hf_nd;
+  ph.mu_c1 = fl.mu_c1;
+  ph.mu_s = fl.mu_s;
+  ph.t_ref = tref;
+  ph.r_ref = rref;
+  ph.a_ref = aref;
+  ph.l_ref = lref;
+  ph.visc_scale = 1.0;
+  ph.visc_cfl_coeff = ph.kappa == 1.0 ? 4.0 : (ph.kappa == -2.0 ? 2.0 : 1.0);
+
+  // boundary states
+  const double pscale = rref * aref * aref;
+  for (auto &call : SplitList(get("boundaryStates", "<>"))) {
+    auto pc = ParseCall(call);
+    BCStateIn si;
+    auto &s = si.s;
+    const auto &name = pc.first;
+    auto &m = pc.second;
+    auto num = [&](const char *k, double def) {
+      auto it = m.find(k);
+      return it == m.end() ? def : std::stod(it->second);
+    };
+    if (name == "periodic") {
+      s.type = ATH_BC_PERIODIC;
+      si.start_tag = (int)num("startTag", -1);
+      si.end_tag = (int)num("endTag", -1);
+      if (m.count("translation")) {
+        ParseVec3(m["translation"], si.translation);
+        for (auto &t : si.translation) t = t / lref;
+      } else {
+        Fail("only translational periodic boundaries are supported");
+      }
+      s.tag = si.start_tag;
+    } else {
+      s.type = BCType(name);
+      s.tag = (int)num("tag", -1);
+      if (m.count("density")) s.rho = std::stod(m["density"]) / rref;
+      if (m.count("pressure")) {
+        s.p = std::stod(m["pressure"]) / pscale;
+        s.p_out = s.p;
+      }
+      if (m.count("velocity")) {
+        double v[3];
+        ParseVec3(m["velocity"], v);
+        if (s.type == ATH_BC_VISCOUS_WALL) {
+          s.wall_u = v[0] / aref; s.wall_v = v[1] / aref; s.wall_w = v[2] / aref;
+        } else {
+          s.u = v[0] / aref; s.v = v[1] / aref; s.w = v[2] / aref;
+        }
+      }
+      if (m.count("p0")) s.p0 = std::stod(m["p0"]) / pscale;
+      if (m.count("t0")) s.t0 = std::stod(m["t0"]) / tref;
+      if (m.count("direction")) {
+        ParseVec3(m["direction"], s.dir);
+        const double mg = std::sqrt(s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1] +
+                                    s.dir[2] * s.dir[2]);
+        for (auto &x : s.dir) x = x / mg;
+      }
+      if (m.count("temperature")) {
+        s.isothermal = 1;
+        s.wall_t = std::stod(m["temperature"]) / tref;
+      }
+      if (m.count("turbulenceIntensity")) s.turb_intensity = num("turbulenceIntensity", 0);
+      if (m.count("eddyViscosityRatio")) s.eddy_visc_ratio = num("eddyViscosityRatio", 0);
+      if (s.type == ATH_BC_STAGNATION_INLET || s.type == ATH_BC_PRESSURE_OUTLET ||
+          s.type == ATH_BC_VISCOUS_WALL)
+        Fail("boundary state " + name + " is not supported yet");
+    }
+    sv.states_in.push_back(si);
+    sv.states.push_back(s);
+  }
+
+  // initial condition: a uniform icState (tag -1)
+  double ic[5] = {0, 0, 0, 0, 0};
+  {
+    bool have = false;
+    for (auto &call : SplitList(get("initialConditions", "<>"))) {
+      auto pc = ParseCall(call);
+      auto &m = pc.second;
+      if (m.count("file")) continue;  // point clouds: state set by caller
+      double v[3] = {0, 0, 0};
+      if (m.count("velocity")) ParseVec3(m["velocity"], v);
+      ic[0] = std::stod(m["density"]) / rref;
+      ic[1] = v[0] / aref;
+      ic[2] = v[1] / aref;
+      ic[3] = v[2] / aref;
+      ic[4] = std::stod(m["pressure"]) / pscale;
+      have = true;
+    }
+    if (!have) {
+      ic[0] = 1.0;
+      ic[4] = 1.0 / 1.4;
+    }
+  }
+
+  // grid
+  const auto grid = DirName(path) + "/" + get("gridName", "") + ".xyz";
+  auto blocks = ReadPlot3d(grid, lref);
+
+  // boundary conditions table: number of blocks, then per block a line
+  // with the surface counts (i, j, k) followed by the surfaces
+  {
+    size_t li = 0;
+    const int nbc = std::stoi(kv["boundaryConditions"]);
+    if (nbc != (int)blocks.size())
+      Fail("boundaryConditions block count does not match the grid");
+    for (int b = 0; b < nbc; ++b) {
+      if (li >= bc_lines.size()) Fail("truncated boundaryConditions");
+      std::istringstream cnt(bc_lines[li++]);
+      int ci = 0, cj = 0, ck = 0;
+      cnt >> ci >> cj >> ck;
+      for (int s = 0; s < ci + cj + ck; ++s) {
+        if (li >= bc_lines.size()) Fail("truncated boundaryConditions");
+        std::istringstream is(bc_lines[li++]);
+        Surface sf;
+        is >> sf.name >> sf.i1 >> sf.i2 >> sf.j1 >> sf.j2 >> sf.k1 >> sf.k2 >> sf.tag;
+        if (!is) Fail("bad boundary surface line");
+        sf.type = BCType(sf.name);
+        blocks[b].surfs.push_back(sf);
+      }
+    }
+  }
+
+  const int solve = (int)st.solves.size();
+  const int first = (int)st.blocks.size();
+  for (auto &b : blocks) {
+    b.ng = ph.ng;
+    b.nv = ph.nv;
+    b.solve = solve;
+    BuildGeometry(b);
+    BuildGhostGeometry(b);
+    BuildCellWidths(b);
+    BuildHyperplanes(b);
+    b.state0.assign((size_t)b.NCell() * b.nv, 0.0);
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i)
+          for (int v = 0; v < b.nv; ++v)
+            b.state0[(size_t)b.Cell(i, j, k) * b.nv + v] = ic[v];
+    sv.blocks.push_back((int)st.blocks.size());
+    st.blocks.push_back(std::move(b));
+  }
+  (void)first;
+  st.solves.push_back(std::move(sv));
+  BuildGhostOps(st, solve);
+  // connection ghost geometry changes the donor-side widths only through
+  // the ops; recompute nothing else
+}
+
+}  // namespace ath

@@ -1,0 +1,240 @@
+/* aither_gb300 — GB300-native per-iteration structured-grid solver step.
+ *
+ * C ABI between the host side (the reference's procBlock / linearSolver /
+ * gridLevel call surface, input and Plot3D formats) and the sm_103a CUDA
+ * kernels.  Plain pointers and sizes only; every function returns an int
+ * status (0 = ATH_OK, negative = error) and never exits the process.  The
+ * text of the last error of a thread is returned by ath_last_error().
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   ath_setup_from_input   input::ReadInput (src/input.cpp:167) +
+ *                          ReadP3dGrid (src/plot3d.cpp:363) + procBlock ctor
+ *                          geometry (src/procBlock.cpp:59) +
+ *                          AssignGhostCellsGeom (src/procBlock.cpp:2160) +
+ *                          GetConnectionBCs (src/boundaryConditions.cpp:500)
+ *                          + HyperplaneReorder (src/utility.cpp:377)
+ *   ath_batch_iterate      mgSolution::Iterate (src/mgSolution.cpp:246) with
+ *                          the norm reductions of src/main.cpp:254-271
+ *   ath_batch_fill_ghosts  gridLevel::GetBoundaryConditions
+ *                          (src/gridLevel.cpp:287)
+ *   ath_batch_residual     gridLevel::CalcResidual (src/gridLevel.cpp:372)
+ *                          -> procBlock::CalcResidualNoSource
+ *                          (src/procBlock.cpp:6111)
+ *   ath_batch_timestep     gridLevel::CalcTimeStep (src/gridLevel.cpp:240)
+ *   ath_batch_diag_invert  gridLevel::InvertDiagonal (src/gridLevel.cpp:402)
+ *                          -> linearSolver::AddDiagonalTerms / Invert
+ *                          (src/linearSolver.cpp:146,177)
+ *   ath_batch_relax        lusgs::Relax (src/linearSolver.cpp:430) with
+ *                          LUSGS_Forward / LUSGS_Backward (:341,:385)
+ *   ath_batch_update       gridLevel::UpdateBlocks (src/gridLevel.cpp:418)
+ *                          -> procBlock::UpdateBlock (src/procBlock.cpp:826)
+ *   ath_batch_matrix_resid linearSolver::Residual (src/linearSolver.cpp:92)
+ */
+#ifndef AITHER_GB300_H
+#define AITHER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATH_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  ATH_OK = 0,
+  ATH_ERR_ARG = -1,       /* invalid argument */
+  ATH_ERR_IO = -2,        /* file could not be read or parsed */
+  ATH_ERR_UNSUPPORTED = -3,
+  ATH_ERR_CUDA = -4,      /* a CUDA runtime call failed */
+  ATH_ERR_NOMEM = -5,     /* device memory budget exceeded */
+  ATH_ERR_NONPHYSICAL = -6, /* non-finite or non-positive density/pressure */
+  ATH_ERR_TIMEOUT = -7    /* a bounded device-side wait gave up */
+};
+
+/* ---- enumerations mirroring the reference's string keywords ------------ */
+enum { ATH_EQN_EULER = 0, ATH_EQN_NAVIER_STOKES = 1, ATH_EQN_RANS = 2 };
+enum { ATH_RECON_CONSTANT = 0, ATH_RECON_MUSCL = 1, ATH_RECON_WENO = 2,
+       ATH_RECON_WENOZ = 3 };
+enum { ATH_LIMITER_NONE = 0, ATH_LIMITER_MINMOD = 1,
+       ATH_LIMITER_VANALBADA = 2 };
+enum { ATH_FLUX_ROE = 0, ATH_FLUX_AUSM = 1 };
+enum { ATH_SOLVER_LUSGS = 0, ATH_SOLVER_BLUSGS = 1 };
+enum { ATH_TURB_NONE = 0, ATH_TURB_SST2003 = 1, ATH_TURB_KW2006 = 2 };
+
+/* boundary condition types (reference keyword in brackets) */
+enum {
+  ATH_BC_SLIP_WALL = 0,           /* slipWall */
+  ATH_BC_VISCOUS_WALL = 1,        /* viscousWall */
+  ATH_BC_CHARACTERISTIC = 2,      /* characteristic */
+  ATH_BC_STAGNATION_INLET = 3,    /* stagnationInlet */
+  ATH_BC_PRESSURE_OUTLET = 4,     /* pressureOutlet */
+  ATH_BC_SUPERSONIC_INFLOW = 5,   /* supersonicInflow */
+  ATH_BC_SUPERSONIC_OUTFLOW = 6,  /* supersonicOutflow */
+  ATH_BC_PERIODIC = 7,            /* periodic (connection) */
+  ATH_BC_INTERBLOCK = 8           /* interblock (connection) */
+};
+
+/* arithmetic of the per-iteration path */
+enum {
+  ATH_PREC_FP64 = 0,  /* everything in FP64 */
+  ATH_PREC_MIXED = 1  /* FP32 reconstruction/fluxes/sweeps inside an FP64
+                         defect-correction loop (FP64 residual assembly,
+                         conserved update and norms) */
+};
+
+/* ---- host-side setup ---------------------------------------------------- */
+typedef struct ath_setup ath_setup;
+
+/* One ghost-cell assignment.  All ghost cells of a block are filled by a
+ * list of these, applied in order (boundary states first, then connection
+ * copies, then block-edge cells). */
+typedef struct {
+  int64_t dst;        /* padded cell index of the ghost cell (own block) */
+  int64_t src;        /* padded cell index of the donor cell */
+  int32_t src_block;  /* block of the donor (connections), else own block */
+  int32_t type;       /* ATH_BC_* */
+  int32_t layer;      /* 1..ng */
+  int32_t dir;        /* 0,1,2 = boundary normal direction i,j,k */
+  int32_t lower;      /* 1 = lower surface (normal flipped outward) */
+  int32_t state;      /* index into the solve's boundary-state table */
+  int64_t face;       /* padded face index of the boundary face (dir) */
+  int64_t src2;       /* edge cells: second donor (-1 when unused) */
+} ath_ghost_op;
+
+/* Boundary-state data, nondimensional (reference inputStates.cpp). */
+typedef struct {
+  int32_t tag;
+  int32_t type;
+  double rho, u, v, w, p;      /* characteristic / supersonic inflow */
+  double p0, t0, dir[3];       /* stagnationInlet */
+  double p_out;                /* pressureOutlet */
+  double wall_u, wall_v, wall_w, wall_t, wall_q; /* viscousWall */
+  int32_t isothermal, heat_flux;
+  double turb_intensity, eddy_visc_ratio;
+} ath_bc_state;
+
+/* Per-solve physics and scheme constants, nondimensional. */
+typedef struct {
+  int32_t eqn, recon, limiter, flux, solver, turb;
+  int32_t nv, ng, sweeps;
+  double kappa, cfl_start, cfl_step, cfl_max, theta, zeta, relax;
+  double gas_r, gas_n, gas_hf;          /* calorically perfect, one species */
+  double mu_c1, mu_s, mu_ref, t_ref;    /* Sutherland constants */
+  double r_ref, a_ref, l_ref;           /* dimensional reference values */
+  double visc_scale;                    /* transport NondimScaling */
+  double visc_cfl_coeff;                /* input::ViscousCFLCoefficient */
+  int32_t nstates;
+  const ath_bc_state *states;
+} ath_solve_view;
+
+/* Read-only view of one block of a setup; arrays are host memory owned by
+ * the setup.  Padded layout: cell (i,j,k), i in [-ng, ni+ng), has index
+ * (i+ng) + NI*((j+ng) + NJ*(k+ng)), NI = ni+2ng.  Face arrays of direction
+ * d have one more entry along d.  Vectors are stored as separate
+ * components (x plane, then y, then z). */
+typedef struct {
+  int32_t ni, nj, nk, ng, nv, solve;
+  int64_t ncell_padded;
+  int64_t nface_padded[3];
+  const double *vol;        /* [ncell_padded] */
+  const double *center;     /* [3][ncell_padded] */
+  const double *width;      /* [3][ncell_padded] cell widths i,j,k */
+  const double *farea[3];   /* [4][nface_padded[d]]: unit x,y,z, magnitude */
+  const double *wall_dist;  /* [ncell_padded] */
+  const double *state0;     /* initial primitive, padded AoS [cell][nv] */
+  int32_t nops;
+  const ath_ghost_op *ops;
+  int32_t nplanes;
+  const int32_t *plane_offsets; /* [nplanes+1] */
+  const int32_t *plane_cells;   /* padded cell index, hyperplane order */
+  /* per padded cell: bit 2d (lower face of direction d) or 2d+1 (upper
+   * face) is set when the neighbour across that face enters the implicit
+   * off-diagonal sums: it is a physical cell or the face lies on a
+   * periodic/interblock connection (procBlock::ImplicitLower/Upper). */
+  const uint8_t *nbr_mask;
+} ath_block_view;
+
+/* Load a case from the reference's input file format (and the Plot3D grid
+ * it names, read from the input file's directory).  A setup may hold many
+ * independent solves: ath_setup_append() adds the blocks of another input
+ * file as a new solve. */
+int ath_setup_from_input(const char *inp_path, ath_setup **out);
+int ath_setup_append(ath_setup *setup, const char *inp_path);
+int ath_setup_destroy(ath_setup *setup);
+int ath_setup_counts(const ath_setup *setup, int *nsolves, int *nblocks,
+                     int64_t *ncells);
+int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out);
+int ath_setup_solve(const ath_setup *setup, int solve, ath_solve_view *out);
+/* Replace the initial primitive state (nondimensional, AoS over physical
+ * cells, k slowest, i fastest). */
+int ath_setup_set_state(ath_setup *setup, int block, const double *prim);
+
+/* ---- device context and batches ----------------------------------------- */
+typedef struct ath_ctx ath_ctx;
+typedef struct ath_batch ath_batch;
+
+typedef struct {
+  double l2[7];        /* sqrt(sum over cells of R^2), per equation */
+  double linf;         /* max residual entry */
+  int32_t linf_block, linf_i, linf_j, linf_k, linf_eqn;
+  double matrix_resid; /* linear-system residual (0 when not computed) */
+  double cfl;
+  int32_t status;      /* ATH_OK or ATH_ERR_NONPHYSICAL for this solve */
+} ath_norms;
+
+int ath_ctx_create(int device, size_t hbm_budget_bytes, ath_ctx **out);
+int ath_ctx_destroy(ath_ctx *ctx);
+const char *ath_last_error(void);
+
+/* Copy a setup to the device.  precision = ATH_PREC_*.  flags: bit 0 =
+ * compute the logged matrix residual every iteration (the reference always
+ * does, src/linearSolver.cpp:470). */
+int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision,
+                     int flags, ath_batch **out);
+int ath_batch_destroy(ath_batch *batch);
+
+/* Run n nonlinear iterations on every solve of the batch.  norms_h receives
+ * n * nsolves entries (iteration-major) when not NULL.  The iteration
+ * counter advances (CFL ramp, src/input.cpp:647). */
+int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h);
+
+/* Same as one iteration but split into the reference's stages, for parity
+ * tests.  Stage order: fill_ghosts, residual, timestep, diag_invert, relax,
+ * update. */
+int ath_batch_fill_ghosts(ath_batch *batch);
+int ath_batch_residual(ath_batch *batch);
+int ath_batch_timestep(ath_batch *batch);
+int ath_batch_diag_invert(ath_batch *batch);
+int ath_batch_relax(ath_batch *batch);
+int ath_batch_update(ath_batch *batch, ath_norms *norms_h);
+
+/* Field download/upload.  Fields are per physical cell, AoS, k slowest;
+ * ATH_FIELD_STATE_GHOSTS covers the padded block. */
+enum {
+  ATH_FIELD_STATE = 0,        /* primitive W, nv per cell */
+  ATH_FIELD_STATE_GHOSTS = 1, /* primitive W incl. ghosts, nv per cell */
+  ATH_FIELD_RESID = 2,        /* residual R, nv */
+  ATH_FIELD_DT = 3,           /* local time step, 1 */
+  ATH_FIELD_SPECRAD = 4,      /* cell spectral radius (flow, turb), 2 */
+  ATH_FIELD_DU = 5,           /* implicit update, nv */
+  ATH_FIELD_AINV = 6          /* inverse main diagonal, 1 (scalar) */
+};
+int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h);
+int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h);
+int ath_batch_field_width(ath_batch *batch, int field);
+
+/* Device work counters of the last ath_batch_iterate call. */
+typedef struct {
+  int64_t kernel_launches;   /* kernels launched (graph nodes included) */
+  double device_ms;          /* CUDA-event time on the batch stream */
+} ath_stats;
+int ath_batch_stats(ath_batch *batch, ath_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AITHER_GB300_H */

@@ -1,0 +1,697 @@
+/* CPU oracle of the per-iteration solver step -- TEST INFRASTRUCTURE ONLY.
+ * See aither_oracle.h.  Every function names the reference function it
+ * restates (paths inside the reference project).  Arithmetic is written in
+ * the reference's evaluation order; build with -ffp-contract=off. */
+#include "aither_oracle.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NV 5
+
+typedef struct {
+  double r, n, hf;
+} gas_t;
+
+typedef struct {
+  int ni, nj, nk, ng, NI, NJ, NK, solve;
+  int64_t nc, nf[3];
+  double *vol, *width; /* width: [3][nc] */
+  double *fa[3];       /* [4][nf] */
+  double *W;           /* [nc][5] primitive, AoS as in the reference */
+  double *R;           /* [nc][5] */
+  double *dU;          /* [nc][5] */
+  double *lam, *dt, *A, *Ainv; /* [nc] */
+  uint8_t *mask;
+  int nops;
+  ath_ghost_op *ops;
+  int nplanes;
+  int32_t *plane_off, *plane_cells;
+} oblock;
+
+typedef struct {
+  ath_solve_view v;
+  ath_bc_state *states;
+  gas_t gas;
+  double cfl;
+} osolve;
+
+struct orc_case {
+  int nb, ns;
+  oblock *b;
+  osolve *s;
+  int64_t iter;
+  int nthreads;
+};
+
+/* ---------------------------------------------------------------- thermo */
+/* caloricallyPerfect (include/thermodynamic.hpp:102-115) and idealGas
+ * (src/eos.cpp), one species, mass fraction 1. */
+static double cv_of(const gas_t *g) { return g->r * g->n; }
+static double cp_of(const gas_t *g) { return g->r * (g->n + 1.0); }
+static double gamma_of(const gas_t *g) { return cp_of(g) / cv_of(g); }
+static double temp_of(const double *w, const gas_t *g) { return w[4] / (w[0] * g->r); }
+static double velmag(const double *w) {
+  return sqrt(w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+}
+/* SpeedOfSound (include/arrayView.hpp:384) */
+static double sos_of(const double *w, const gas_t *g) {
+  return sqrt(gamma_of(g) * w[4] / w[0]);
+}
+/* EnthalpyFunc (include/arrayView.hpp:401) */
+static double enthalpy_of(const double *w, const gas_t *g) {
+  const double t = temp_of(w, g);
+  const double vm = velmag(w);
+  return (g->hf + cp_of(g) * t) + 0.5 * vm * vm;
+}
+/* InternalEnergy (include/arrayView.hpp:436) */
+static double energy_of(const double *w, const gas_t *g) {
+  const double t = temp_of(w, g);
+  const double vm = velmag(w);
+  return (g->hf + cv_of(g) * t) + 0.5 * vm * vm;
+}
+/* PrimToCons (include/primitive.hpp:183) */
+static void prim_to_cons(const double *w, const gas_t *g, double *c) {
+  c[0] = w[0];
+  c[1] = w[0] * w[1];
+  c[2] = w[0] * w[2];
+  c[3] = w[0] * w[3];
+  c[4] = w[0] * energy_of(w, g);
+}
+/* primitive(conserved) (include/primitive.hpp:137), PressFromEnergy
+ * (src/eos.cpp:40), TemperatureFromSpecEnergy (src/thermodynamic.cpp:107) */
+static void cons_to_prim(const double *c, const gas_t *g, double *w) {
+  const double rho = c[0];
+  w[0] = rho;
+  w[1] = c[1] / rho;
+  w[2] = c[2] / rho;
+  w[3] = c[3] / rho;
+  const double energy = c[4] / rho;
+  const double vel = velmag(w);
+  const double spec = energy - 0.5 * vel * vel;
+  const double t = (spec - g->hf) / cv_of(g);
+  w[4] = rho * g->r * t;
+}
+/* UpdatePrimWithCons (include/primitive.hpp:206) */
+static void update_with_cons(const double *w, const gas_t *g, const double *du,
+                             double *out) {
+  double c[NV];
+  prim_to_cons(w, g, c);
+  for (int v = 0; v < NV; ++v) c[v] = c[v] + du[v];
+  cons_to_prim(c, g, out);
+}
+/* inviscidFlux::ConstructFromPrim (include/inviscidFlux.hpp:129) */
+static void inv_flux(const double *w, const gas_t *g, const double *n, double *f) {
+  const double vn = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  f[0] = w[0] * vn;
+  f[1] = w[0] * vn * w[1] + w[4] * n[0];
+  f[2] = w[0] * vn * w[2] + w[4] * n[1];
+  f[3] = w[0] * vn * w[3] + w[4] * n[2];
+  f[4] = w[0] * vn * enthalpy_of(w, g);
+}
+
+/* ------------------------------------------------------- reconstruction */
+static double lim_minmod(double r) {
+  const double m = (r < 1.0) ? r : 1.0; /* std::min(1.0, r) */
+  return (0.0 < m) ? m : 0.0;           /* std::max(0.0, m) */
+}
+static double lim_vanalbada(double r) {
+  const double r2 = r * r;
+  const double l = (r + r2) / (1.0 + r2);
+  return (0.0 < l) ? l : 0.0;
+}
+/* FaceReconMUSCL (include/reconstruction.hpp:110), limiters
+ * src/limiter.cpp:24,36 */
+static void muscl(const double *up2, const double *up1, const double *dw1,
+                  double kappa, int limiter, double uw2, double uw, double dw,
+                  double *out) {
+  const double dPlus = (uw + uw) / (uw + dw);
+  const double dMinus = (uw + uw) / (uw + uw2);
+  for (int v = 0; v < NV; ++v) {
+    const double r = (1.0e-30 + (dw1[v] - up1[v]) * dPlus) /
+                     (1.0e-30 + (up1[v] - up2[v]) * dMinus);
+    double l, il;
+    if (limiter == ATH_LIMITER_MINMOD) {
+      l = lim_minmod(r);
+      il = lim_minmod(1.0 / r);
+    } else if (limiter == ATH_LIMITER_VANALBADA) {
+      l = lim_vanalbada(r);
+      il = lim_vanalbada(1.0 / r);
+    } else {
+      l = 1.0;
+      il = 1.0;
+    }
+    out[v] = up1[v] + 0.25 * ((up1[v] - up2[v]) * dMinus) *
+                          ((1.0 - kappa) * l + (1.0 + kappa) * r * il);
+  }
+}
+
+/* ------------------------------------------------------------- Roe flux */
+/* RoeFlux (include/inviscidFlux.hpp:260), RoeAveragedState
+ * (include/primitive.hpp:245), inviscidFlux::RoeFlux (src/inviscidFlux.cpp:27) */
+static void roe_flux(const double *L, const double *R, const gas_t *g,
+                     const double *n, double *f) {
+  const double denRatio = sqrt(R[0] / L[0]);
+  double roe[NV];
+  roe[0] = L[0] * denRatio;
+  roe[1] = (L[1] + denRatio * R[1]) / (1.0 + denRatio);
+  roe[2] = (L[2] + denRatio * R[2]) / (1.0 + denRatio);
+  roe[3] = (L[3] + denRatio * R[3]) / (1.0 + denRatio);
+  roe[4] = (L[4] + denRatio * R[4]) / (1.0 + denRatio);
+  const double hR = enthalpy_of(roe, g);
+  const double aR = sos_of(roe, g);
+  const double rhoR = roe[0];
+  const double velNormR = roe[1] * n[0] + roe[2] * n[1] + roe[3] * n[2];
+  const double mfR = roe[0] / rhoR;
+  double delta[NV];
+  for (int v = 0; v < NV; ++v) delta[v] = R[v] - L[v];
+  const double nvd = delta[1] * n[0] + delta[2] * n[1] + delta[3] * n[2];
+  double d[NV] = {0, 0, 0, 0, 0};
+  const double fix = 0.1;
+
+  double ws = fabs(velNormR - aR);
+  if (ws < fix) ws = 0.5 * (ws * ws / fix + fix);
+  double st = (delta[4] - rhoR * aR * nvd) / (2.0 * aR * aR);
+  double wss = ws * st;
+  d[0] += wss * mfR;
+  d[1] += wss * (roe[1] - aR * n[0]);
+  d[2] += wss * (roe[2] - aR * n[1]);
+  d[3] += wss * (roe[3] - aR * n[2]);
+  d[4] += wss * (hR - aR * velNormR);
+
+  ws = fabs(velNormR);
+  st = -delta[4] / (aR * aR);
+  wss = ws * st;
+  d[0] += wss * mfR + ws * delta[0];
+  st = delta[0] - delta[4] / (aR * aR);
+  wss = ws * st;
+  d[1] += wss * roe[1];
+  d[2] += wss * roe[2];
+  d[3] += wss * roe[3];
+  d[4] += wss * 0.5 * (roe[1] * roe[1] + roe[2] * roe[2] + roe[3] * roe[3]);
+
+  st = rhoR;
+  wss = ws * st;
+  d[1] += wss * (delta[1] - nvd * n[0]);
+  d[2] += wss * (delta[2] - nvd * n[1]);
+  d[3] += wss * (delta[3] - nvd * n[2]);
+  d[4] += wss * ((roe[1] * delta[1] + roe[2] * delta[2] + roe[3] * delta[3]) -
+                 velNormR * nvd);
+
+  ws = fabs(velNormR + aR);
+  if (ws < fix) ws = 0.5 * (ws * ws / fix + fix);
+  st = (delta[4] + rhoR * aR * nvd) / (2.0 * aR * aR);
+  wss = ws * st;
+  d[0] += wss * mfR;
+  d[1] += wss * (roe[1] + aR * n[0]);
+  d[2] += wss * (roe[2] + aR * n[1]);
+  d[3] += wss * (roe[3] + aR * n[2]);
+  d[4] += wss * (hR + aR * velNormR);
+
+  double fl[NV], fr[NV];
+  inv_flux(L, g, n, fl);
+  inv_flux(R, g, n, fr);
+  for (int v = 0; v < NV; ++v) {
+    f[v] = fl[v] + (fr[v] - d[v]);
+    f[v] *= 0.5;
+  }
+}
+
+/* ------------------------------------------------------ spectral radius */
+/* InvCellSpectralRadius (include/spectralRadius.hpp:44) */
+static double inv_cell_specrad(const double *w, const gas_t *g, const double *lo,
+                               double lom, const double *hi, double him) {
+  double a[3];
+  for (int q = 0; q < 3; ++q) a[q] = 0.5 * (lo[q] + hi[q]);
+  const double m = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  for (int q = 0; q < 3; ++q) a[q] = a[q] / m;
+  const double fMag = 0.5 * (lom + him);
+  return (fabs(w[1] * a[0] + w[2] * a[1] + w[3] * a[2]) + sos_of(w, g)) * fMag;
+}
+
+/* RusanovScalarOffDiagonal (src/fluxJacobian.cpp:122) with
+ * ConvectiveFluxUpdate (include/inviscidFlux.hpp:544) and
+ * InvFaceSpectralRadius (include/spectralRadius.hpp:67); inviscid */
+static void scalar_offdiag(const double *w, const double *du, const gas_t *g,
+                           const double *n, double mag, int positive, double *out) {
+  double wu[NV], fo[NV], fn[NV];
+  update_with_cons(w, g, du, wu);
+  inv_flux(w, g, n, fo);
+  inv_flux(wu, g, n, fn);
+  const double lam =
+      0.5 * mag * (fabs(w[1] * n[0] + w[2] * n[1] + w[3] * n[2]) + sos_of(w, g));
+  for (int v = 0; v < NV; ++v) {
+    const double fc = 0.5 * mag * (fn[v] - fo[v]);
+    out[v] = positive ? fc + lam * du[v] : fc - lam * du[v];
+  }
+}
+
+/* ------------------------------------------------------------- helpers */
+static inline int64_t cell_idx(const oblock *b, int i, int j, int k) {
+  return (int64_t)(i + b->ng) + (int64_t)b->NI * ((j + b->ng) + (int64_t)b->NJ * (k + b->ng));
+}
+static inline int64_t face_idx(const oblock *b, int d, int i, int j, int k) {
+  const int fi = b->NI + (d == 0), fj = b->NJ + (d == 1);
+  return (int64_t)(i + b->ng) + (int64_t)fi * ((j + b->ng) + (int64_t)fj * (k + b->ng));
+}
+static inline void face_normal(const oblock *b, int d, int64_t f, double *n, double *mag) {
+  const int64_t nf = b->nf[d];
+  n[0] = b->fa[d][f];
+  n[1] = b->fa[d][nf + f];
+  n[2] = b->fa[d][2 * nf + f];
+  *mag = b->fa[d][3 * nf + f];
+}
+
+static void *dup_arr(const void *src, size_t bytes) {
+  void *p = malloc(bytes ? bytes : 1);
+  if (src && bytes) memcpy(p, src, bytes);
+  else memset(p, 0, bytes ? bytes : 1);
+  return p;
+}
+
+/* ---------------------------------------------------------------- API */
+orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
+                     const ath_solve_view *sv) {
+  orc_case *c = (orc_case *)calloc(1, sizeof(orc_case));
+  c->nb = nblocks;
+  c->ns = nsolves;
+  c->b = (oblock *)calloc(nblocks, sizeof(oblock));
+  c->s = (osolve *)calloc(nsolves, sizeof(osolve));
+  for (int s = 0; s < nsolves; ++s) {
+    c->s[s].v = sv[s];
+    c->s[s].states = (ath_bc_state *)dup_arr(sv[s].states, sizeof(ath_bc_state) * sv[s].nstates);
+    c->s[s].v.states = c->s[s].states;
+    c->s[s].gas.r = sv[s].gas_r;
+    c->s[s].gas.n = sv[s].gas_n;
+    c->s[s].gas.hf = sv[s].gas_hf;
+  }
+  for (int bi = 0; bi < nblocks; ++bi) {
+    const ath_block_view *v = &bv[bi];
+    oblock *b = &c->b[bi];
+    b->ni = v->ni; b->nj = v->nj; b->nk = v->nk; b->ng = v->ng;
+    b->NI = v->ni + 2 * v->ng; b->NJ = v->nj + 2 * v->ng; b->NK = v->nk + 2 * v->ng;
+    b->solve = v->solve;
+    b->nc = v->ncell_padded;
+    b->vol = (double *)dup_arr(v->vol, 8 * b->nc);
+    b->width = (double *)dup_arr(v->width, 8 * 3 * b->nc);
+    for (int d = 0; d < 3; ++d) {
+      b->nf[d] = v->nface_padded[d];
+      b->fa[d] = (double *)dup_arr(v->farea[d], 8 * 4 * b->nf[d]);
+    }
+    b->W = (double *)dup_arr(v->state0, 8 * NV * b->nc);
+    b->R = (double *)dup_arr(NULL, 8 * NV * b->nc);
+    b->dU = (double *)dup_arr(NULL, 8 * NV * b->nc);
+    b->lam = (double *)dup_arr(NULL, 8 * b->nc);
+    b->dt = (double *)dup_arr(NULL, 8 * b->nc);
+    b->A = (double *)dup_arr(NULL, 8 * b->nc);
+    b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
+    b->mask = (uint8_t *)dup_arr(v->nbr_mask, b->nc);
+    b->nops = v->nops;
+    b->ops = (ath_ghost_op *)dup_arr(v->ops, sizeof(ath_ghost_op) * v->nops);
+    b->nplanes = v->nplanes;
+    b->plane_off = (int32_t *)dup_arr(v->plane_offsets, 4 * (v->nplanes + 1));
+    b->plane_cells = (int32_t *)dup_arr(v->plane_cells, 4 * (size_t)v->ni * v->nj * v->nk);
+  }
+  return c;
+}
+
+void orc_destroy(orc_case *c) {
+  if (!c) return;
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    free(b->vol); free(b->width);
+    for (int d = 0; d < 3; ++d) free(b->fa[d]);
+    free(b->W); free(b->R); free(b->dU); free(b->lam); free(b->dt); free(b->A);
+    free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
+  }
+  for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
+  free(c->b);
+  free(c->s);
+  free(c);
+}
+
+void orc_set_threads(orc_case *c, int n) { c->nthreads = n; }
+
+#ifdef _OPENMP
+#define PAR_BLOCKS _Pragma("omp parallel for schedule(dynamic, 1) num_threads(nth)")
+#define NTH int nth = c->nthreads > 0 ? c->nthreads : omp_get_max_threads();
+#else
+#define PAR_BLOCKS
+#define NTH
+#endif
+
+/* ExtrapolateHoldMixture (src/ghostStates.cpp:693), one species */
+static void extrap_hold(double *g, double factor, const double *in) {
+  const double ghostRho = factor * g[0] - in[0];
+  if (ghostRho <= 0.0) return;
+  const double mf = g[0] / g[0];
+  for (int v = 0; v < NV; ++v) g[v] = factor * g[v] - in[v];
+  const double r = ghostRho * mf;
+  g[0] = (r > 0.0) ? r : 0.0;
+}
+
+/* GetGhostState (src/ghostStates.cpp:62) for the supported types;
+ * interblock/periodic: copy of the partner cell (SwapStateSlice). */
+void orc_fill_ghosts(orc_case *c) {
+  /* CalcCFL for this iteration (src/input.cpp:647) */
+  for (int s = 0; s < c->ns; ++s) {
+    const ath_solve_view *v = &c->s[s].v;
+    const double cfl = v->cfl_start + (double)c->iter * v->cfl_step;
+    c->s[s].cfl = cfl < v->cfl_max ? cfl : v->cfl_max;
+  }
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const osolve *sv = &c->s[b->solve];
+    for (int o = 0; o < b->nops; ++o) {
+      const ath_ghost_op *op = &b->ops[o];
+      const oblock *src = &c->b[op->src_block];
+      const double *in = &src->W[op->src * NV];
+      double g[NV];
+      memcpy(g, in, sizeof(g));
+      if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) {
+        double n[3], mag;
+        face_normal(b, op->dir, op->face, n, &mag);
+        if (op->lower) {
+          n[0] = -1.0 * n[0];
+          n[1] = -1.0 * n[1];
+          n[2] = -1.0 * n[2];
+        }
+        if (op->type == ATH_BC_SLIP_WALL) {
+          const double vn = in[1] * n[0] + in[2] * n[1] + in[3] * n[2];
+          g[1] = in[1] - 2.0 * n[0] * vn;
+          g[2] = in[2] - 2.0 * n[1] * vn;
+          g[3] = in[3] - 2.0 * n[2] * vn;
+        } else if (op->type == ATH_BC_CHARACTERISTIC) {
+          const ath_bc_state *bs = &sv->states[op->state];
+          const double fr[NV] = {bs->rho, bs->u, bs->v, bs->w, bs->p};
+          const double vin = in[1] * n[0] + in[2] * n[1] + in[3] * n[2];
+          const double sosInt = sos_of(in, &sv->gas);
+          const double machInt = fabs(vin) / sosInt;
+          if (machInt >= 1.0 && vin < 0.0) {
+            memcpy(g, fr, sizeof(g));
+          } else if (machInt >= 1.0 && vin >= 0.0) {
+          } else if (machInt < 1.0 && vin < 0.0) {
+            const double rhoSoSInt = in[0] * sosInt;
+            const double dv[3] = {fr[1] - in[1], fr[2] - in[2], fr[3] - in[3]};
+            g[4] = 0.5 * (fr[4] + in[4] -
+                          rhoSoSInt * (n[0] * dv[0] + n[1] * dv[1] + n[2] * dv[2]));
+            const double dp = fr[4] - g[4];
+            const double rho = fr[0] - dp / (sosInt * sosInt);
+            g[0] = rho * (fr[0] / fr[0]);
+            g[1] = fr[1] - n[0] * dp / rhoSoSInt;
+            g[2] = fr[2] - n[1] * dp / rhoSoSInt;
+            g[3] = fr[3] - n[2] * dp / rhoSoSInt;
+          } else {
+            const double rhoSoSInt = in[0] * sosInt;
+            const double dp = in[4] - fr[4];
+            const double rho = in[0] - dp / (sosInt * sosInt);
+            g[0] = rho * (in[0] / in[0]);
+            g[1] = in[1] + n[0] * dp / rhoSoSInt;
+            g[2] = in[2] + n[1] * dp / rhoSoSInt;
+            g[3] = in[3] + n[2] * dp / rhoSoSInt;
+            g[4] = fr[4];
+          }
+          extrap_hold(g, 2.0, in);
+          if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
+        } else if (op->type == ATH_BC_SUPERSONIC_INFLOW) {
+          const ath_bc_state *bs = &sv->states[op->state];
+          g[0] = bs->rho; g[1] = bs->u; g[2] = bs->v; g[3] = bs->w; g[4] = bs->p;
+        } else if (op->type == ATH_BC_SUPERSONIC_OUTFLOW) {
+          if (op->layer > 1)
+            for (int v = 0; v < NV; ++v) g[v] = (double)op->layer * in[v] - in[v];
+        }
+      }
+      memcpy(&b->W[op->dst * NV], g, sizeof(g));
+    }
+  }
+}
+
+/* procBlock::CalcResidualNoSource (src/procBlock.cpp:6111) for inviscid
+ * flow: ResetResidWS, then CalcInvFluxI/J/K (src/procBlock.cpp:384,522,660):
+ * per face, MUSCL states, Roe flux, scatter +F|A| to the lower cell and
+ * -F|A| to the upper cell, cell spectral radius and scalar diagonal for the
+ * upper cell. */
+void orc_residual(orc_case *c) {
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const osolve *sv = &c->s[b->solve];
+    const gas_t *g = &sv->gas;
+    memset(b->R, 0, 8 * NV * b->nc);
+    memset(b->lam, 0, 8 * b->nc);
+    memset(b->A, 0, 8 * b->nc);
+    for (int d = 0; d < 3; ++d) {
+      const int ei = b->ni + (d == 0), ej = b->nj + (d == 1), ek = b->nk + (d == 2);
+      const int nd = d == 0 ? b->ni : (d == 1 ? b->nj : b->nk);
+      const int64_t st = d == 0 ? 1 : (d == 1 ? b->NI : (int64_t)b->NI * b->NJ);
+      const double *wd = &b->width[d * b->nc];
+      for (int k = 0; k < ek; ++k)
+        for (int j = 0; j < ej; ++j)
+          for (int i = 0; i < ei; ++i) {
+            const int fpos = d == 0 ? i : (d == 1 ? j : k);
+            const int64_t cu = cell_idx(b, i, j, k); /* upper cell of the face */
+            const int64_t cl = cu - st;
+            const double *wm2 = &b->W[(cl - st) * NV], *wm1 = &b->W[cl * NV],
+                         *w0 = &b->W[cu * NV], *wp1 = &b->W[(cu + st) * NV];
+            double fL[NV], fR[NV], f[NV], n[3], mag;
+            muscl(wm2, wm1, w0, sv->v.kappa, sv->v.limiter, wd[cl - st], wd[cl],
+                  wd[cu], fL);
+            muscl(wp1, w0, wm1, sv->v.kappa, sv->v.limiter, wd[cu + st], wd[cu],
+                  wd[cl], fR);
+            face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
+            roe_flux(fL, fR, g, n, f);
+            if (fpos > 0)
+              for (int v = 0; v < NV; ++v) b->R[cl * NV + v] += f[v] * mag;
+            if (fpos < nd) {
+              for (int v = 0; v < NV; ++v) b->R[cu * NV + v] -= f[v] * mag;
+              double nl[3], ml, nh[3], mh;
+              face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
+              face_normal(b, d,
+                          face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
+              const double lam = inv_cell_specrad(w0, g, nl, ml, nh, mh);
+              b->lam[cu] += lam;
+              b->A[cu] += lam;
+            }
+          }
+    }
+  }
+}
+
+/* procBlock::CalcBlockTimeStep / CalcCellDt (src/procBlock.cpp:782,798) */
+void orc_timestep(orc_case *c) {
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const double cfl = c->s[b->solve].cfl;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          b->dt[x] = cfl * (b->vol[x] / b->lam[x]);
+        }
+  }
+}
+
+/* linearSolver::AddDiagonalTerms / Invert (src/linearSolver.cpp:146,177),
+ * scalar diagonal */
+void orc_diag_invert(orc_case *c) {
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const ath_solve_view *v = &c->s[b->solve].v;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          const double diagVolTime = (b->vol[x] * (1.0 + v->zeta)) / (b->dt[x] * v->theta);
+          b->A[x] *= v->relax;
+          b->A[x] += diagVolTime;
+          b->Ainv[x] = 1.0 / b->A[x];
+        }
+  }
+}
+
+/* off-diagonal sum of one cell: procBlock::ImplicitLower (forward) or
+ * ImplicitUpper (backward), src/procBlock.cpp:1056,1106 */
+static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower,
+                        double *acc) {
+  const gas_t *g = &c->s[b->solve].gas;
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  const int64_t nfst[3] = {1, b->NI + 1, (int64_t)b->NI * (b->NJ + 1)};
+  (void)nfst;
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  /* padded (i,j,k) of x */
+  const int64_t ii = x % b->NI, jj = (x / b->NI) % b->NJ, kk = x / ((int64_t)b->NI * b->NJ);
+  for (int d = 0; d < 3; ++d) {
+    if (!(b->mask[x] & (1u << (2 * d + (lower ? 0 : 1))))) continue;
+    const int64_t nb = lower ? x - st[d] : x + st[d];
+    const int fi = (int)ii - b->ng + (!lower && d == 0);
+    const int fj = (int)jj - b->ng + (!lower && d == 1);
+    const int fk = (int)kk - b->ng + (!lower && d == 2);
+    double n[3], mag, o[NV];
+    face_normal(b, d, face_idx(b, d, fi, fj, fk), n, &mag);
+    scalar_offdiag(&b->W[nb * NV], &b->dU[nb * NV], g, n, mag, lower, o);
+    for (int v = 0; v < NV; ++v) acc[v] += o[v];
+  }
+}
+
+/* SwapImplicitUpdate (src/utility.cpp:400) */
+static void swap_du(orc_case *c) {
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    for (int o = 0; o < b->nops; ++o) {
+      const ath_ghost_op *op = &b->ops[o];
+      if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) continue;
+      memcpy(&b->dU[op->dst * NV], &c->b[op->src_block].dU[op->src * NV], 8 * NV);
+    }
+  }
+}
+
+/* lusgs::Relax with one sweep and no initialisation (src/linearSolver.cpp:
+ * 430, LUSGS_Forward :341, LUSGS_Backward :385) */
+void orc_relax(orc_case *c) {
+  for (int bi = 0; bi < c->nb; ++bi) memset(c->b[bi].dU, 0, 8 * NV * c->b[bi].nc);
+  swap_du(c);
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const double thetaInv = 1.0 / c->s[b->solve].v.theta;
+    const int ncell = b->ni * b->nj * b->nk;
+    for (int q = 0; q < ncell; ++q) {
+      const int64_t x = b->plane_cells[q];
+      double L[NV];
+      offdiag_sum(c, b, x, 1, L);
+      for (int v = 0; v < NV; ++v) {
+        const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+        b->dU[x * NV + v] = (bb + L[v]) * b->Ainv[x];
+      }
+    }
+  }
+  swap_du(c);
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const int ncell = b->ni * b->nj * b->nk;
+    for (int q = ncell - 1; q >= 0; --q) {
+      const int64_t x = b->plane_cells[q];
+      double U[NV];
+      offdiag_sum(c, b, x, 0, U);
+      for (int v = 0; v < NV; ++v) {
+        const double xold = b->dU[x * NV + v];
+        b->dU[x * NV + v] = xold - U[v] * b->Ainv[x];
+      }
+    }
+  }
+  swap_du(c);
+}
+
+/* procBlock::UpdateBlock / ImplicitTimeAdvance (src/procBlock.cpp:826,902)
+ * and the L2 sums of src/main.cpp:254-268 */
+int orc_update(orc_case *c, double *l2_out, double *linf_out) {
+  int bad = 0;
+  double *l2 = (double *)calloc((size_t)c->ns * NV, sizeof(double));
+  double *linf = (double *)calloc((size_t)c->ns, sizeof(double));
+  NTH
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const gas_t *g = &c->s[b->solve].gas;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          double w[NV];
+          update_with_cons(&b->W[x * NV], g, &b->dU[x * NV], w);
+          if (!(w[0] > 0.0) || !(w[4] > 0.0) || !isfinite(w[1]) || !isfinite(w[2]) ||
+              !isfinite(w[3]))
+            bad = 1;
+          memcpy(&b->W[x * NV], w, sizeof(w));
+        }
+  }
+  /* sequential norm sums in the reference's block, k, j, i order */
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          for (int v = 0; v < NV; ++v) {
+            const double r = b->R[x * NV + v];
+            l2[b->solve * NV + v] += r * r;
+            if (r > linf[b->solve]) linf[b->solve] = r;
+          }
+        }
+  }
+  for (int q = 0; q < c->ns * NV; ++q)
+    if (l2_out) l2_out[q] = sqrt(l2[q]);
+  for (int s = 0; s < c->ns; ++s)
+    if (linf_out) linf_out[s] = linf[s];
+  free(l2);
+  free(linf);
+  c->iter += 1;
+  return bad ? ATH_ERR_NONPHYSICAL : 0;
+}
+
+int orc_iterate(orc_case *c, int n, double *l2_out) {
+  int rc = 0;
+  for (int it = 0; it < n; ++it) {
+    orc_fill_ghosts(c);
+    orc_residual(c);
+    orc_timestep(c);
+    orc_diag_invert(c);
+    orc_relax(c);
+    const int r = orc_update(c, l2_out ? l2_out + (size_t)it * c->ns * NV : NULL, NULL);
+    if (r) rc = r;
+  }
+  return rc;
+}
+
+int orc_get_field(orc_case *c, int block, int field, double *out) {
+  if (block < 0 || block >= c->nb) return ATH_ERR_ARG;
+  oblock *b = &c->b[block];
+  size_t q = 0;
+  if (field == ATH_FIELD_STATE_GHOSTS) {
+    memcpy(out, b->W, 8 * NV * b->nc);
+    return 0;
+  }
+  for (int k = 0; k < b->nk; ++k)
+    for (int j = 0; j < b->nj; ++j)
+      for (int i = 0; i < b->ni; ++i) {
+        const int64_t x = cell_idx(b, i, j, k);
+        switch (field) {
+          case ATH_FIELD_STATE: memcpy(out + NV * q, &b->W[x * NV], 8 * NV); break;
+          case ATH_FIELD_RESID: memcpy(out + NV * q, &b->R[x * NV], 8 * NV); break;
+          case ATH_FIELD_DU: memcpy(out + NV * q, &b->dU[x * NV], 8 * NV); break;
+          case ATH_FIELD_DT: out[q] = b->dt[x]; break;
+          case ATH_FIELD_SPECRAD: out[2 * q] = b->lam[x]; out[2 * q + 1] = 0.0; break;
+          case ATH_FIELD_AINV: out[q] = b->Ainv[x]; break;
+          default: return ATH_ERR_ARG;
+        }
+        ++q;
+      }
+  return 0;
+}
+
+int orc_set_state(orc_case *c, int block, const double *prim) {
+  if (block < 0 || block >= c->nb) return ATH_ERR_ARG;
+  oblock *b = &c->b[block];
+  size_t q = 0;
+  for (int k = 0; k < b->nk; ++k)
+    for (int j = 0; j < b->nj; ++j)
+      for (int i = 0; i < b->ni; ++i) {
+        memcpy(&b->W[cell_idx(b, i, j, k) * NV], prim + NV * q, 8 * NV);
+        ++q;
+      }
+  return 0;
+}

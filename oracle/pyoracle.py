@@ -1,0 +1,106 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py; never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(_HERE, "liboracle.so")
+FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6)
+WIDTH = dict(STATE=5, STATE_GHOSTS=5, RESID=5, DT=1, SPECRAD=2, DU=5, AINV=1)
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise RuntimeError(f"{ORACLE_LIB} is not built; run `python -m aither_gb300.build`")
+        from aither_gb300._lib import BlockView, SolveView
+        L = C.CDLL(ORACLE_LIB)
+        vp = C.c_void_p
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [C.c_int, C.POINTER(BlockView), C.c_int, C.POINTER(SolveView)]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_set_threads.argtypes = [vp, C.c_int]
+        for f in ("orc_fill_ghosts", "orc_residual", "orc_timestep", "orc_diag_invert",
+                  "orc_relax"):
+            getattr(L, f).argtypes = [vp]
+        L.orc_update.restype = C.c_int
+        L.orc_update.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_iterate.restype = C.c_int
+        L.orc_iterate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        L.orc_get_field.restype = C.c_int
+        L.orc_get_field.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.orc_set_state.restype = C.c_int
+        L.orc_set_state.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """CPU oracle instance built from an aither_gb300 Setup."""
+
+    def __init__(self, setup, threads: int = 0):
+        from aither_gb300._lib import BlockView, SolveView
+        self.setup = setup
+        self.nsolves, self.nblocks, self.ncells = setup.counts()
+        bv = (BlockView * self.nblocks)(*[setup.block_view(b) for b in range(self.nblocks)])
+        sv = (SolveView * self.nsolves)(*[setup.solve_view(s) for s in range(self.nsolves)])
+        self.h = lib().orc_create(self.nblocks, bv, self.nsolves, sv)
+        if threads:
+            lib().orc_set_threads(self.h, threads)
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, n: int = 1) -> np.ndarray:
+        l2 = np.zeros(n * self.nsolves * 5)
+        rc = lib().orc_iterate(self.h, n, _dp(l2))
+        if rc:
+            raise RuntimeError(f"oracle reported status {rc}")
+        return l2.reshape(n, self.nsolves, 5)
+
+    def stage(self, name: str):
+        if name == "update":
+            l2 = np.zeros(self.nsolves * 5)
+            rc = lib().orc_update(self.h, _dp(l2), None)
+            if rc:
+                raise RuntimeError(f"oracle reported status {rc}")
+            return l2.reshape(self.nsolves, 5)
+        getattr(lib(), "orc_" + name)(self.h)
+
+    def field(self, b: int, field: str) -> np.ndarray:
+        v = self.setup.block_view(b)
+        w = WIDTH[field]
+        n = (v.ncell_padded if field == "STATE_GHOSTS" else v.ni * v.nj * v.nk) * w
+        out = np.empty(n)
+        rc = lib().orc_get_field(self.h, b, FIELD[field], _dp(out))
+        if rc:
+            raise RuntimeError(f"oracle field error {rc}")
+        if field == "STATE_GHOSTS":
+            return out.reshape(v.nk + 2 * v.ng, v.nj + 2 * v.ng, v.ni + 2 * v.ng, w)
+        return out.reshape(v.nk, v.nj, v.ni, w)
+
+    def set_state(self, b: int, prim: np.ndarray) -> None:
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        lib().orc_set_state(self.h, b, _dp(prim))

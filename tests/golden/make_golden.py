@@ -1,0 +1,86 @@
+"""Generates the golden fixtures of tests/golden/ by running the reference
+solver itself (built from its sources by oracle/ref_build into oracle/_ref)
+through oracle/ref_build/ref_harness.cpp on seeded synthetic cases.
+
+    python tests/golden/make_golden.py [--reference /path/to/aither]
+
+Each fixture is an .npz with the fields the reference produced:
+  <case>_it<N>.npz : state0, state (physical, after N iterations), resid,
+                     dt, specrad, du (of iteration N), l2 (per iteration)
+Small grids keep the fixtures a few hundred kB; the full-size vortex-box
+configuration (64x32x8, 200 iterations) stores its L2 history and summary
+statistics of the final state only.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+from aither_gb300 import cases  # noqa: E402
+from refdump import read_dump  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# (fixture name, generator, kwargs, iterations, full fields?)
+CASES = [
+    ("vortex16", cases.vortex_box, dict(ni=16, nj=8, nk=4), [1, 20], True),
+    ("bump24", cases.bump_channel, dict(ni=24, nj=12, nk=4, height=0.08, mach=0.7), [1, 30], True),
+    ("bump_sup", cases.bump_channel, dict(ni=20, nj=10, nk=3, height=0.10, mach=0.85), [1, 40], True),
+    ("vortex_c1", cases.vortex_box, dict(), [200], False),
+]
+
+
+def run_case(name, gen, kw, niter, full, ref_dir):
+    with tempfile.TemporaryDirectory() as d:
+        inp, st = gen(d, name=name, **kw)
+        args = [HARNESS, os.path.basename(inp), str(niter), "out.bin"]
+        if st is not None:
+            np.asarray(st[0], dtype="<f8").tofile(os.path.join(d, "state.bin"))
+            args.append("state.bin")
+        env = dict(os.environ, AITHER_INSTALL_DIRECTORY=ref_dir)
+        r = subprocess.run(args, cwd=d, env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference harness failed on {name}: {r.stderr[-2000:]}")
+        R = read_dump(os.path.join(d, "out.bin"))
+    ng = 2
+    state = R["b0_state"][ng:-ng, ng:-ng, ng:-ng]
+    out = {"l2": R["l2"], "kwargs": np.array(repr(kw)), "iterations": np.array(niter)}
+    if full:
+        out.update(state0=R["b0_state0"], state=state, resid=R["b0_resid"], dt=R["b0_dt"],
+                   specrad=R["b0_specrad"], du=R["b0_du"])
+    else:
+        out.update(state_sum=state.reshape(-1, 5).sum(axis=0),
+                   state_sumsq=(state.reshape(-1, 5) ** 2).sum(axis=0),
+                   state_samples=state[::3, ::7, ::11].copy())
+    path = os.path.join(HERE, f"{name}_it{niter}.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    if not os.path.exists(HARNESS):
+        sys.path.insert(0, ROOT)
+        from aither_gb300 import build
+        os.environ["AITHER_REFERENCE_SRC"] = a.reference
+        build.REF_SRC = a.reference
+        build.build_reference()
+    for name, gen, kw, iters, full in CASES:
+        for n in iters:
+            run_case(name, gen, kw, n, full, a.reference)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,145 @@
+"""Parity of the sm_103a path with the reference, through the C ABI.
+
+Tolerances (relative to the largest magnitude of the compared field):
+  * FP64 path, per cell, after one iteration and after tens of
+    iterations: 1e-12;
+  * FP64 path, L2 residual histories (incl. 200 iterations of the full
+    64x32x8 vortex box): 1e-10.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+CELL_TOL = 1e-12
+NORM_TOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from aither_gb300 import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _batch(ctx, inp, st, precision=0):
+    from aither_gb300 import Batch, Setup
+    s = Setup(inp)
+    if st is not None:
+        s.set_state(0, st[0])
+    return s, Batch(ctx, s, precision)
+
+
+def _l2(norms, nsolves=1, solve=0):
+    a = np.array([[n.l2[v] for v in range(5)] for n in norms])
+    return a.reshape(-1, nsolves, 5)[:, solve, :]
+
+
+@pytest.mark.parametrize("name", ["vortex16_it1", "vortex16_it20", "bump24_it1",
+                                  "bump24_it30", "bump_sup_it1", "bump_sup_it40"])
+def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
+    inp, st, g = golden_case(name, str(tmp_path))
+    s, b = _batch(ctx, inp, st)
+    n = int(g["iterations"])
+    norms = b.iterate(n)
+    assert rel_err(b.field(0, "STATE"), g["state"]) <= CELL_TOL
+    assert rel_err(b.field(0, "RESID"), g["resid"]) <= CELL_TOL
+    assert rel_err(b.field(0, "DT")[..., 0], g["dt"]) <= CELL_TOL
+    assert rel_err(b.field(0, "SPECRAD")[..., 0], g["specrad"][..., 0]) <= CELL_TOL
+    assert rel_err(b.field(0, "DU"), g["du"]) <= CELL_TOL
+    assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    assert all(x.status == 0 for x in norms)
+    b.close()
+
+
+def test_fp64_full_vortex_box_200_iterations(ctx, tmp_path):
+    inp, st, g = golden_case("vortex_c1_it200", str(tmp_path))
+    s, b = _batch(ctx, inp, st)
+    norms = b.iterate(200)
+    assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    w = b.field(0, "STATE")
+    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["state_sum"]) <= NORM_TOL
+    assert rel_err(w[::3, ::7, ::11], g["state_samples"]) <= CELL_TOL * 100
+    b.close()
+
+
+def test_stages_match_oracle(ctx, tmp_path):
+    """Each stage of one iteration against the CPU oracle on a bump channel."""
+    from aither_gb300 import cases
+    from pyoracle import Oracle
+    inp, _ = cases.bump_channel(str(tmp_path), 30, 14, 5, 0.09, 0.8, name="stg")
+    s, b = _batch(ctx, inp, None)
+    o = Oracle(s)
+    b.iterate(3)
+    o.iterate(3)
+    b.stage("fill_ghosts")
+    o.stage("fill_ghosts")
+    assert rel_err(b.field(0, "STATE_GHOSTS"), o.field(0, "STATE_GHOSTS")) <= CELL_TOL
+    b.stage("residual")
+    o.stage("residual")
+    assert rel_err(b.field(0, "RESID"), o.field(0, "RESID")) <= CELL_TOL
+    for nm in ("timestep", "diag_invert"):
+        b.stage(nm)
+        o.stage(nm)
+    assert rel_err(b.field(0, "DT"), o.field(0, "DT")) <= CELL_TOL
+    assert rel_err(b.field(0, "AINV"), o.field(0, "AINV")) <= CELL_TOL
+    b.stage("relax")
+    o.stage("relax")
+    assert rel_err(b.field(0, "DU"), o.field(0, "DU")) <= CELL_TOL
+    nb = b.stage("update")
+    no = o.stage("update")
+    assert rel_err(b.field(0, "STATE"), o.field(0, "STATE")) <= CELL_TOL
+    assert rel_err(np.array([nb[0].l2[v] for v in range(5)]), no[0]) <= CELL_TOL
+    b.close()
+
+
+def test_batched_solves_equal_solves_alone(ctx, tmp_path):
+    """Several independent solves of different sizes in one batch give the
+    same results as each solve run alone (FP64: bit for bit)."""
+    from aither_gb300 import Batch, Setup, cases
+    specs = [(20, 10, 4, 0.05, 0.5), (33, 12, 3, 0.08, 0.75), (16, 16, 6, 0.1, 0.4)]
+    inps = []
+    for q, (ni, nj, nk, h, m) in enumerate(specs):
+        d = tmp_path / f"c{q}"
+        inp, _ = cases.bump_channel(str(d), ni, nj, nk, h, m, name=f"b{q}")
+        inps.append(inp)
+    sb = Setup(inps)
+    bb = Batch(ctx, sb)
+    nb = bb.iterate(15)
+    for q, inp in enumerate(inps):
+        s1, b1 = _batch(ctx, inp, None)
+        n1 = b1.iterate(15)
+        assert np.array_equal(_l2(nb, 3, q), _l2(n1))
+        assert np.array_equal(bb.field(q, "STATE"), b1.field(0, "STATE"))
+        b1.close()
+    bb.close()
+
+
+def test_nonphysical_state_reported(ctx, tmp_path):
+    """A negative pressure planted on the host is reported through the
+    solve's status; the context stays usable."""
+    from aither_gb300 import cases
+    inp, st = cases.vortex_box(str(tmp_path), 8, 4, 2, name="bad")
+    w = st[0].reshape(2, 4, 8, 5).copy()
+    w[1, 2, 3, 4] = -1.0
+    s, b = _batch(ctx, inp, [w.reshape(-1)])
+    norms = b.iterate(1)
+    assert norms[0].status != 0
+    b.close()
+    inp2, st2 = cases.vortex_box(str(tmp_path / "ok"), 8, 4, 2, name="ok")
+    s2, b2 = _batch(ctx, inp2, st2)
+    assert all(n.status == 0 for n in b2.iterate(2))
+    b2.close()
+
+
+def test_memory_budget_is_enforced(tmp_path):
+    from aither_gb300 import AthError, Batch, Context, Setup, cases
+    c = Context(0, hbm_budget=1 << 20)
+    inp, _ = cases.bump_channel(str(tmp_path), 40, 20, 10, 0.05, 0.5, name="big")
+    with pytest.raises(AthError) as e:
+        Batch(c, Setup(inp))
+    assert e.value.code == -5
+    c.close()

@@ -1,0 +1,89 @@
+"""CPU oracle against the reference: golden fixtures produced by the
+reference solver itself (tests/golden/make_golden.py) and, where the
+reference sources are present, a live run of the reference build."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REF_HARNESS, REF_SRC, golden_case, rel_err
+
+# The oracle restates the reference operation by operation and is built
+# with -ffp-contract=off; it reproduces the reference bit for bit on these
+# cases.  The stated tolerance leaves room for a different libm sqrt only.
+TOL = 1e-13
+
+FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
+        "bump_sup_it1", "bump_sup_it40"]
+
+
+def _oracle(inp, st):
+    from aither_gb300 import Setup
+    from pyoracle import Oracle
+    s = Setup(inp)
+    if st is not None:
+        s.set_state(0, st[0])
+    return s, Oracle(s)
+
+
+@pytest.mark.parametrize("name", FULL)
+def test_oracle_matches_reference_fixture(name, tmp_path):
+    inp, st, g = golden_case(name, str(tmp_path))
+    _, o = _oracle(inp, st)
+    n = int(g["iterations"])
+    l2 = o.iterate(n)
+    assert rel_err(o.field(0, "STATE"), g["state"]) <= TOL
+    assert rel_err(o.field(0, "RESID"), g["resid"]) <= TOL
+    assert rel_err(o.field(0, "DT")[..., 0], g["dt"]) <= TOL
+    assert rel_err(o.field(0, "SPECRAD")[..., 0], g["specrad"][..., 0]) <= TOL
+    assert rel_err(o.field(0, "DU"), g["du"]) <= TOL
+    assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
+
+
+def test_oracle_full_vortex_box_200_iterations(tmp_path):
+    """The 64x32x8 vortex box, 200 LU-SGS iterations at CFL 10: L2 history
+    and state statistics equal the reference's."""
+    inp, st, g = golden_case("vortex_c1_it200", str(tmp_path))
+    _, o = _oracle(inp, st)
+    l2 = o.iterate(200)
+    assert rel_err(l2[:, 0, :], g["l2"]) <= 1e-12
+    w = o.field(0, "STATE")
+    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["state_sum"]) <= 1e-12
+    assert rel_err(w[::3, ::7, ::11], g["state_samples"]) <= 1e-12
+
+
+@pytest.mark.skipif(not (os.path.exists(REF_HARNESS) and os.path.isdir(REF_SRC)),
+                    reason="reference build not available on this machine")
+@pytest.mark.parametrize("seed", [1, 2])
+def test_oracle_matches_live_reference(seed, tmp_path):
+    """Random small bump channels, run through the reference build here."""
+    from refdump import read_dump
+
+    from aither_gb300 import cases
+    rng = np.random.default_rng(seed)
+    ni, nj, nk = (int(x) for x in rng.integers([10, 6, 2], [20, 12, 5]))
+    inp, _ = cases.bump_channel(str(tmp_path), ni, nj, nk, float(rng.uniform(0.04, 0.1)),
+                                float(rng.uniform(0.3, 0.85)), name="live")
+    env = dict(os.environ, AITHER_INSTALL_DIRECTORY=REF_SRC)
+    r = subprocess.run([REF_HARNESS, "live.inp", "5", "out.bin"], cwd=str(tmp_path),
+                       env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    R = read_dump(str(tmp_path / "out.bin"))
+    _, o = _oracle(inp, None)
+    l2 = o.iterate(5)
+    assert rel_err(o.field(0, "STATE"), R["b0_state"][2:-2, 2:-2, 2:-2]) <= TOL
+    assert rel_err(o.field(0, "DU"), R["b0_du"]) <= TOL
+    assert rel_err(l2[:, 0, :], R["l2"]) <= TOL
+
+
+def test_oracle_detects_nonphysical_state(tmp_path):
+    """A negative pressure planted in the initial state is reported, not
+    silently propagated (host-side fault injection)."""
+    from aither_gb300 import cases
+    inp, st = cases.vortex_box(str(tmp_path), 8, 4, 2, name="bad")
+    w = st[0].reshape(2, 4, 8, 5).copy()
+    w[1, 2, 3, 4] = -1.0
+    _, o = _oracle(inp, [w.reshape(-1)])
+    with pytest.raises(RuntimeError):
+        o.iterate(1)
