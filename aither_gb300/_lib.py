@@ -117,6 +117,9 @@ def lib() -> C.CDLL:
             "ath_batch_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_field_width": (C.c_int, [vp, C.c_int]),
             "ath_batch_stats": (C.c_int, [vp, C.POINTER(Stats)]),
+            "ath_batch_pool_cells": (C.c_int, [vp, C.POINTER(C.c_int64)]),
+            "ath_batch_copy_state": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
+            "ath_batch_profile": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
         }
         missing = []
         for name, (res, args) in sig.items():
@@ -269,6 +272,20 @@ class Batch:
     def set_state(self, b: int, prim: np.ndarray) -> None:
         prim = np.ascontiguousarray(prim, dtype=np.float64)
         check(lib().ath_batch_set_state(self.h, b, dptr(prim)))
+
+    def pool_cells(self) -> int:
+        n = C.c_int64()
+        check(lib().ath_batch_pool_cells(self.h, C.byref(n)))
+        return n.value
+
+    def copy_state(self, host: np.ndarray, to_device: bool) -> None:
+        assert host.dtype == np.float64 and host.flags.c_contiguous
+        check(lib().ath_batch_copy_state(self.h, dptr(host), 1 if to_device else 0))
+
+    def profile(self, reps: int = 3) -> np.ndarray:
+        ms = np.zeros(8)
+        check(lib().ath_batch_profile(self.h, reps, dptr(ms)))
+        return ms
 
     def stats(self) -> Stats:
         s = Stats()

@@ -190,6 +190,7 @@ class RunnerBase {
   virtual void Iterate(int n) = 0;
   virtual void GetDU(int b, double *out) = 0;
   virtual void GetAinv(int b, double *out) = 0;
+  virtual void Profile(int reps, double ms[8]) = 0;
 };
 
 template <typename T>
@@ -316,6 +317,47 @@ class Runner : public RunnerBase {
       cudaGraphDestroy(g);
     }
     for (int i = 0; i < n; ++i) Check(cudaGraphLaunch(c_.graph, c_.stream), "graph launch");
+  }
+  void Profile(int reps, double ms[8]) override {
+    cudaEvent_t e[9];
+    for (auto &x : e) Check(cudaEventCreate(&x), "event");
+    for (int q = 0; q < 8; ++q) ms[q] = 0.0;
+    for (int r = 0; r < reps; ++r) {
+      Check(cudaEventRecord(e[0], c_.stream), "event");
+      FillGhosts();
+      Check(cudaEventRecord(e[1], c_.stream), "event");
+      for (int d = 0; d < 3; ++d) {
+        Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
+                        (int)c_.L.face_cta_block[d].size(), c_.stream);
+        Check(cudaEventRecord(e[2 + d], c_.stream), "event");
+      }
+      Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
+                      c_.stream);
+      Check(cudaEventRecord(e[5], c_.stream), "event");
+      Check(cudaMemsetAsync(P_.dU, 0, 5 * c_.ncell * sizeof(T), c_.stream), "memset");
+      for (int s = 0; s < c_.nsteps; ++s) {
+        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
+      }
+      Check(cudaEventRecord(e[6], c_.stream), "event");
+      Launch<T>::ConnDu(P_, c_.d_conn_ops, (int)c_.L.conn_ops.size(), c_.stream);
+      for (int s = c_.nsteps - 1; s >= 0; --s) {
+        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
+      }
+      Check(cudaEventRecord(e[7], c_.stream), "event");
+      Update();
+      c_.iter_host += 1;
+      Check(cudaEventRecord(e[8], c_.stream), "event");
+      Check(cudaEventSynchronize(e[8]), "sync");
+      for (int q = 0; q < 8; ++q) {
+        float t = 0.f;
+        Check(cudaEventElapsedTime(&t, e[q], e[q + 1]), "elapsed");
+        ms[q] += t;
+      }
+    }
+    for (int q = 0; q < 8; ++q) ms[q] /= std::max(reps, 1);
+    for (auto &x : e) cudaEventDestroy(x);
   }
   void GetDU(int b, double *out) override { CopyOut(P_.dU, 5, b, out); }
   void GetAinv(int b, double *out) override { CopyOut(P_.Ainv, 1, b, out); }
@@ -791,6 +833,35 @@ int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h) {
       Check(cudaMemcpy(batch->W + v * n + o, h.data(), nc * 8, cudaMemcpyHostToDevice),
             "upload");
     }
+  });
+}
+
+int ath_batch_pool_cells(ath_batch *batch, int64_t *ncell) {
+  if (!batch || !ncell) return ATH_ERR_ARG;
+  *ncell = batch->core.ncell;
+  return ATH_OK;
+}
+
+int ath_batch_copy_state(ath_batch *batch, double *host, int to_device) {
+  return Guard([&] {
+    if (!batch || !host) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto &c = batch->core;
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    const size_t bytes = 5 * (size_t)c.ncell * sizeof(double);
+    if (to_device)
+      Check(cudaMemcpyAsync(batch->W, host, bytes, cudaMemcpyHostToDevice, c.stream), "H2D");
+    else
+      Check(cudaMemcpyAsync(host, batch->W, bytes, cudaMemcpyDeviceToHost, c.stream), "D2H");
+    Check(cudaStreamSynchronize(c.stream), "sync");
+  });
+}
+
+int ath_batch_profile(ath_batch *batch, int reps, double ms[8]) {
+  return Guard([&] {
+    if (!batch || !ms || reps <= 0) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    Check(cudaSetDevice(batch->core.ctx->device), "cudaSetDevice");
+    batch->run->Profile(reps, ms);
+    Check(cudaGetLastError(), "kernel launch");
   });
 }
 

@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Throughput of the per-iteration structured-grid solver step on GB300.
+
+Workload (default): the batched bump-channel configuration -- 64 independent
+single-block channels with a sinusoidal lower-wall bump (height 4-10 % of
+chord), sizes drawn uniformly between 32^3 and 96x64x48 cells, Mach
+0.3-0.85, inviscid Euler, MUSCL + minmod, Roe flux, scalar LU-SGS, CFL 20
+(seeded synthetic grids; no dataset).  One step = one nonlinear iteration of
+every case of the batch.  Metric: cell-iterations/s.
+
+Arms:
+  default            this project's sm_103a path through the C ABI.  `value`
+                     is the FP64 path (the reference's arithmetic); the
+                     mixed FP32/FP64 path is reported beside it under
+                     "mixed".
+  --impl reference   the reference algorithm on the host cores.  The
+                     reference's own build needs its source tree, which this
+                     machine may not have; the CPU oracle (a plain-C
+                     restatement of the reference, bit-exact against it) is
+                     timed instead, with every host thread.
+
+Multi-GPU: replicas only (independent batches per rank, no data-path
+collective); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-iterations/s"
+
+
+# ----------------------------------------------------------------- workload
+def make_workload(tmp: str, ncases: int):
+    from aither_gb300 import cases
+    specs = cases.bump_batch_specs(ncases)
+    inps = []
+    for q, (ni, nj, nk, h, m) in enumerate(specs):
+        inp, _ = cases.bump_channel(os.path.join(tmp, f"c{q:03d}"), ni, nj, nk, h, m,
+                                    cfl=20.0, name=f"bump{q:03d}")
+        inps.append(inp)
+    return inps, specs
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------- roofline model
+def algorithmic_bytes(nv: int = 5, d: int = 1, b: int = 8) -> dict:
+    """Compulsory traffic per cell-iteration of the four irreducible passes
+    (values counted once per pass that needs them; ghosts and metadata
+    excluded): residual (2nv+17+d), forward sweep (4nv+d+12), backward
+    sweep (4nv+d+12), update+norms (4nv); b bytes per value."""
+    return {"residual": (2 * nv + 17 + d) * b, "forward": (4 * nv + d + 12) * b,
+            "backward": (4 * nv + d + 12) * b, "update": 4 * nv * b,
+            "total": (14 * nv + 3 * d + 41) * b}
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return {**json.load(f), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ------------------------------------------------------------------- arms
+def run_native(args, rank: int, world: int, device: int):
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Context, Setup
+    with tempfile.TemporaryDirectory() as tmp:
+        inps, specs = make_workload(tmp, args.ncases)
+        t0 = time.time()
+        setup = Setup(inps)
+        t_setup = time.time() - t0
+    nsolves, nblocks, ncells = setup.counts()
+    ctx = Context(device)
+    out = {}
+    for prec_name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        if args.precision not in ("both", prec_name):
+            continue
+        batch = Batch(ctx, setup, prec)
+        for _ in range(args.warmup):
+            batch.iterate(1)
+        _barrier(world)
+        clocks = ClockSampler(device)
+        clocks.start()
+        t0 = time.time()
+        norms = batch.iterate(args.steps)
+        wall = time.time() - t0
+        st = batch.stats()
+        clk = clocks.stop()
+        ms = st.device_ms
+        ms = _max_over_ranks(ms, world)
+        status_ok = all(n.status == 0 for n in norms)
+        res = {"value": ncells * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
+               "wall_s": wall, "gpu_launches": int(st.kernel_launches), "clocks": clk,
+               "status_ok": status_ok}
+        # per-kernel-class CUDA-event times (one iteration's worth each)
+        prof = batch.profile(2)
+        res["kernel_ms"] = dict(zip(["ghost", "face_i", "face_j", "face_k", "cell",
+                                     "sweep_fwd", "sweep_bwd", "update"], prof.tolist()))
+        # end to end through the C ABI with host buffers: every step uploads
+        # the state from page-locked host memory, iterates, reads back the
+        # norms and the state
+        res["e2e"] = run_e2e(batch, ncells, args.steps, world)
+        batch.close()
+        out[prec_name] = res
+    ctx.close()
+    return out, ncells, nsolves, t_setup, specs
+
+
+def run_e2e(batch, ncells: int, steps: int, world: int) -> dict:
+    n = batch.pool_cells()
+    host = _pinned(5 * n)
+    batch.copy_state(host, to_device=False)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        batch.copy_state(host, to_device=True)
+        batch.iterate(1)
+        batch.copy_state(host, to_device=False)
+    dt = time.perf_counter() - t0
+    dt = _max_over_ranks(dt * 1e3, world) * 1e-3
+    from aither_gb300._lib import Norms
+    import ctypes
+    nb = 5 * n * 8
+    return {"value": ncells * steps * world / dt, "unit": METRIC,
+            "h2d_bytes_per_step": nb,
+            "d2h_bytes_per_step": nb + ctypes.sizeof(Norms) * batch.nsolves}
+
+
+def _pinned(count: int) -> np.ndarray:
+    try:
+        import torch
+        if torch.cuda.is_available():
+            t = torch.empty(count, dtype=torch.float64, pin_memory=True)
+            a = t.numpy()
+            a._keep = t  # noqa: SLF001 -- keep the pinned allocation alive
+            return a
+    except Exception:
+        pass
+    return np.empty(count, dtype=np.float64)
+
+
+def cpu_baseline(sample_cases: int, iters: int, threads: int) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from pyoracle import Oracle
+
+    from aither_gb300 import Setup
+    with tempfile.TemporaryDirectory() as tmp:
+        inps, _ = make_workload(tmp, sample_cases)
+        setup = Setup(inps)
+    _, _, ncells = setup.counts()
+    orc = Oracle(setup, threads)
+    orc.iterate(1)
+    t0 = time.perf_counter()
+    orc.iterate(iters)
+    dt = time.perf_counter() - t0
+    return {"value": ncells * iters / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"first {sample_cases} cases of the batched workload "
+                      f"({ncells} cells), {iters} iterations, oracle "
+                      f"(C restatement of the reference, bit-exact against it), "
+                      f"OpenMP over blocks"}
+
+
+# ------------------------------------------------------------- distributed
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("BENCH_BACKEND", "") != "gloo" else "gloo"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def _barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# -------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--ncases", type=int, default=64)
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = _dist()
+    config = {"workload": f"batched bump channels: {args.ncases} single-block cases, "
+                          "32^3..96x64x48 cells, Mach 0.3-0.85, inviscid Euler, MUSCL minmod, "
+                          "Roe, scalar LU-SGS, CFL 20",
+              "ncases": args.ncases, "l2_flush": "inputs larger than L2 (GB-scale working set)",
+              "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        threads = os.cpu_count() or 1
+        base = cpu_baseline(args.ncases, 1, threads)  # one step = one iteration of the batch
+        # warm-up and timed steps of the full workload
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+
+        from aither_gb300 import Setup
+        with tempfile.TemporaryDirectory() as tmp:
+            inps, _ = make_workload(tmp, args.ncases)
+            setup = Setup(inps)
+        _, _, ncells = setup.counts()
+        orc = Oracle(setup, threads)
+        orc.iterate(args.warmup)
+        t0 = time.perf_counter()
+        orc.iterate(args.steps)
+        dt = time.perf_counter() - t0
+        v = ncells * args.steps / dt
+        line = {"metric": METRIC, "value": v, "unit": METRIC, "impl": "reference",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                                 "sample": f"full batched workload ({ncells} cells), "
+                                           f"{args.steps} iterations; the reference's own "
+                                           "build is unavailable on this host (its sources "
+                                           "are not shipped), so its C restatement is timed"},
+                "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    res, ncells, nsolves, t_setup, specs = run_native(args, rank, world, local)
+    if rank != 0:
+        return
+    fp = res.get("fp64") or res.get("mixed")
+    km = fp["kernel_ms"]
+    peaks = measured_peaks()
+    ab = algorithmic_bytes()
+    # per kernel class: algorithmic bytes of its pass over the batch
+    pass_bytes = {"residual": ab["residual"] * ncells, "sweep_fwd": ab["forward"] * ncells,
+                  "sweep_bwd": ab["backward"] * ncells, "update": ab["update"] * ncells}
+    pass_ms = {"residual": km["face_i"] + km["face_j"] + km["face_k"] + km["cell"],
+               "sweep_fwd": km["sweep_fwd"], "sweep_bwd": km["sweep_bwd"],
+               "update": km["update"]}
+    dom = max(pass_ms, key=pass_ms.get)
+    achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+            "peak_source": peaks["source"], "traffic": None,
+            "bytes_per_cell": {k: v for k, v in ab.items()}}
+    line = {"metric": METRIC, "value": fp["value"], "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fp["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if "fp64" in res else "f32+f64",
+            "data": "synthetic (seeded bump-channel grids)", "config": config,
+            "cells": ncells, "solves": nsolves, "setup_s": t_setup,
+            "gpu_launches": fp["gpu_launches"], "clocks": fp["clocks"],
+            "e2e": fp["e2e"], "roofline": roof, "kernel_ms": km}
+    if "mixed" in res and "fp64" in res:
+        m = res["mixed"]
+        line["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"],
+                         "speedup_vs_fp64": m["value"] / fp["value"], "e2e": m["e2e"],
+                         "kernel_ms": m["kernel_ms"], "gpu_launches": m["gpu_launches"]}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

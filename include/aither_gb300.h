@@ -233,6 +233,24 @@ typedef struct {
 } ath_stats;
 int ath_batch_stats(ath_batch *batch, ath_stats *out);
 
+/* Whole-batch snapshot of the primitive state in the device layout:
+ * [5][pool cells] FP64, every block's padded cells back to back (block b
+ * starts at the sum of the padded cell counts of blocks 0..b-1).  One copy
+ * each way; pass page-locked host memory for full link bandwidth.
+ * to_device = 1 uploads host -> device, 0 downloads.  (Restart snapshots of
+ * resident solutions, reference WriteRestart/ReadRestart src/output.cpp:
+ * 591,756, go through this.) */
+int ath_batch_pool_cells(ath_batch *batch, int64_t *ncell);
+int ath_batch_copy_state(ath_batch *batch, double *host, int to_device);
+
+/* CUDA-event timing of each kernel class on the batch stream, averaged
+ * over reps launches of one iteration's worth of work (outside the graph).
+ * ms[]: 0 ghost fill, 1 i-face fluxes, 2 j-face fluxes, 3 k-face fluxes,
+ * 4 residual/dt/diagonal cells, 5 forward sweep (all hyperplanes),
+ * 6 backward sweep (all hyperplanes), 7 update + norms.  The batch state
+ * advances by reps iterations. */
+int ath_batch_profile(ath_batch *batch, int reps, double ms[8]);
+
 #ifdef __cplusplus
 }
 #endif
