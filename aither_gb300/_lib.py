@@ -77,6 +77,14 @@ class Norms(C.Structure):
                 ("matrix_resid", C.c_double), ("cfl", C.c_double), ("status", C.c_int32)]
 
 
+class BlockDev(C.Structure):
+    """ath_block_dev: caller-owned device arrays of one block."""
+    _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("ng", C.c_int32),
+                ("W", C.c_void_p), ("vol", C.c_void_p), ("width", C.c_void_p * 3),
+                ("farea", C.c_void_p * 3), ("R", C.c_void_p), ("lam", C.c_void_p),
+                ("dt", C.c_void_p), ("ainv", C.c_void_p)]
+
+
 class Stats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("device_ms", C.c_double)]
 
@@ -120,6 +128,8 @@ def lib() -> C.CDLL:
             "ath_batch_pool_cells": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "ath_batch_copy_state": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
             "ath_batch_profile": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_block_residual_noalloc": (C.c_int, [C.POINTER(BlockDev), C.POINTER(SolveView),
+                                                     C.c_double, vp]),
         }
         missing = []
         for name, (res, args) in sig.items():

@@ -38,6 +38,7 @@ CU_UNITS = {
     "kernels_fp64.cu": ["--fmad=false"],
     "kernels_fp32.cu": ["--fmad=true"],
     "batch.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
 }
 CPP_UNITS = ["setup.cpp", "capi_setup.cpp"]
 

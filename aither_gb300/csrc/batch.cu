@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "aither_gb300.h"
+#include "cuda_check.hpp"
 #include "errors.hpp"
 #include "kernels.cuh"
 #include "setup.hpp"
@@ -29,11 +30,6 @@ struct ath_ctx {
 namespace ath {
 
 namespace {
-
-void Check(cudaError_t e, const char *what) {
-  if (e != cudaSuccess)
-    throw Error(ATH_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
 
 // Device allocation accounted against the context's HBM budget.
 class DevMem {

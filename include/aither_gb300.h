@@ -251,6 +251,45 @@ int ath_batch_copy_state(ath_batch *batch, double *host, int to_device);
  * advances by reps iterations. */
 int ath_batch_profile(ath_batch *batch, int reps, double ms[8]);
 
+/* ---- allocation-free residual of one block ------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory while the solver step runs (a code that records
+ * the step into a CUDA graph it owns, a serving loop that has handed every
+ * byte of HBM to its admission budget, a plugin host that owns the device
+ * allocator).  The caller passes its own device arrays for every input and
+ * output; the face-flux scratch of the stage is a fixed device array inside
+ * this library of ATH_NOALLOC_MAX_CELLS padded cells (15.7 MB, held on every
+ * GPU that loads the library until the process exits).  Blocks with more
+ * padded cells are rejected with ATH_ERR_UNSUPPORTED.
+ *
+ * Computes the same residual R, cell spectral radius, local time step and
+ * inverse scalar diagonal as ath_batch_residual (FP64).  Arrays use the
+ * padded layout of ath_block_view (cell (i,j,k) at (i+ng) + NI*((j+ng) +
+ * NJ*(k+ng))), all [var][cell]; face data of direction d are stored at the
+ * index of the cell above the face (face i at cell i).  Ghost layers of W
+ * must already be filled.
+ *
+ * The first call on a device looks up the scratch array's device address
+ * with that device current; make the first call before any stream capture.
+ * Every call on a device shares the one scratch array, so calls that
+ * overlap on the GPU (other streams, other host threads) race: serialise
+ * them.  stream: a cudaStream_t (NULL = legacy default stream); the call
+ * returns after enqueueing, without synchronising. */
+#define ATH_NOALLOC_MAX_CELLS 131072
+typedef struct {
+  int32_t ni, nj, nk, ng;   /* physical cells and ghost layers (ng >= 2) */
+  const double *W;          /* [5][ncell] primitive state incl. ghosts */
+  const double *vol;        /* [ncell] cell volumes */
+  const double *width[3];   /* [ncell] cell widths in i, j, k */
+  const double *farea[3];   /* [4][ncell] unit normal x,y,z and magnitude */
+  double *R;                /* out [5][ncell] residual (physical cells) */
+  double *lam;              /* out [ncell] inviscid cell spectral radius */
+  double *dt;               /* out [ncell] local time step */
+  double *ainv;             /* out [ncell] inverse scalar main diagonal */
+} ath_block_dev;
+int ath_block_residual_noalloc(const ath_block_dev *blk, const ath_solve_view *phys,
+                               double cfl, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
