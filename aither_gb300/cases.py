@@ -210,7 +210,8 @@ def bump_nodes(ni: int, nj: int, nk: int, height: float, length: float = 3.0,
 
 
 def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: float,
-                 cfl: float = 20.0, name: str = "bump"):
+                 cfl: float = 20.0, name: str = "bump", recon: str = "thirdOrder",
+                 limiter: str = "minmod", flux: str = "roe"):
     os.makedirs(outdir, exist_ok=True)
     nodes = bump_nodes(ni, nj, nk, height)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
@@ -228,7 +229,8 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
             ("slipWall", 0, ni, 0, nj, 0, 0, 2),
             ("slipWall", 0, ni, 0, nj, nk, nk, 2)]]
     inp = os.path.join(outdir, name + ".inp")
-    write_input(inp, name, {"cfl": cfl, "limiter": "minmod"}, refs, ic, states, bcs)
+    write_input(inp, name, {"cfl": cfl, "limiter": limiter, "faceReconstruction": recon,
+                            "inviscidFlux": flux}, refs, ic, states, bcs)
     return inp, None
 
 

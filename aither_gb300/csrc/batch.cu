@@ -71,11 +71,17 @@ class DevMem {
 struct Lists {
   std::vector<int32_t> cells, cell_cta_block, cell_cta_pos0;
   std::vector<int32_t> faces[3], face_cta_block[3];
-  std::vector<int2> sweep_items;
+  std::vector<int2> sweep_items;  // (q index, block)
   std::vector<int32_t> step_off;
   std::vector<int32_t> solve_cta0;
   std::vector<GhostOpDev> ops, conn_ops;
   std::vector<int32_t> op_solve;
+  // hyperplane-ordered sweep tables
+  std::vector<int64_t> q0;        // per block: first q index
+  std::vector<int32_t> qpos;      // per pool cell
+  std::vector<int32_t> nbq;       // [6][nq]
+  std::vector<double> face_lo, face_hi;  // [3][4][nq]
+  std::vector<int32_t> ghost_cell, ghost_src;
 };
 
 }  // namespace
@@ -86,7 +92,7 @@ struct BatchCore {
   const Setup *setup;
   int precision, flags;
   int nsolves = 0, nblocks = 0;
-  int64_t ncell = 0;
+  int64_t ncell = 0, nq = 0;
   std::vector<int64_t> cell0;        // pool offset of each block
   std::vector<int64_t> solve_pos0;   // per block: loop-order offset inside its solve
   Lists L;
@@ -103,6 +109,7 @@ struct BatchCore {
   GhostOpDev *d_ops = nullptr, *d_conn_ops = nullptr;
   int32_t *d_op_solve = nullptr;
   NormPartial *d_partials = nullptr;
+  double *d_mres = nullptr;
   NormOut *d_ring = nullptr;
   int ring_cap = 1024;
   int64_t *d_iter = nullptr;
@@ -125,19 +132,20 @@ __global__ void k_cfl(const SolveDev *solves, int nsolves, const int64_t *iter_c
   cfl[s] = fmin(sv.cfl_start + it * sv.cfl_step, sv.cfl_max);
 }
 
-__global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
-                        int nsolves, NormOut *ring, int ring_cap,
-                        int64_t *iter_counter, const SolveDev *solves,
+__global__ void k_norms(const NormPartial *partials, const double *mres_partials,
+                        const int32_t *solve_cta0, int nsolves, NormOut *ring,
+                        int ring_cap, int64_t *iter_counter, const SolveDev *solves,
                         double *cfl) {
   const int s = blockIdx.x;
   if (s >= nsolves) return;
   const int lane = threadIdx.x;
   const int c0 = solve_cta0[s], c1 = solve_cta0[s + 1];
   double l2[kNv] = {0, 0, 0, 0, 0};
-  double mx = 0.0;
+  double mx = 0.0, mres = 0.0;
   int64_t mpos = INT64_MAX;
   int bad = 0;
   for (int c = c0 + lane; c < c1; c += 32) {
+    if (mres_partials) mres += mres_partials[c];
     const NormPartial p = partials[c];
 #pragma unroll
     for (int v = 0; v < kNv; ++v) l2[v] += p.l2[v];
@@ -158,6 +166,7 @@ __global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
       mpos = op;
     }
     bad |= __shfl_down_sync(0xffffffffu, bad, off);
+    mres += __shfl_down_sync(0xffffffffu, mres, off);
   }
   const int64_t it = *iter_counter;
   __syncwarp();
@@ -169,6 +178,10 @@ __global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
     o.bad = bad;
     o.pad = 0;
     o.cfl = cfl[s];
+    // src/mgSolution.cpp:196-206 divides by the padded size, src/main.cpp:271
+    // by cells x equations
+    const SolveDev sv = solves[s];
+    o.matrix_resid = mres_partials ? sqrt((mres / sv.padded_values) / (sv.cells * kNv)) : 0.0;
     ring[(it % ring_cap) * nsolves + s] = o;
   }
 }
@@ -198,20 +211,41 @@ class Runner : public RunnerBase {
     P_.ncell = n;
     P_.W = m.Alloc<double>(5 * n);
     P_.R = m.Alloc<double>(5 * n);
-    P_.dU = m.Alloc<T>(5 * n);
     for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<T>(5 * n);
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
-    P_.Ainv = m.Alloc<T>(n);
     Check(cudaMemset(P_.R, 0, 5 * n * sizeof(double)), "memset");
-    Check(cudaMemset(P_.dU, 0, 5 * n * sizeof(T)), "memset");
     Check(cudaMemset(P_.lam, 0, n * sizeof(double)), "memset");
     Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
-    Check(cudaMemset(P_.Ainv, 0, n * sizeof(T)), "memset");
+    // hyperplane-ordered sweep working set
+    const int64_t nq = c.nq, ngh = (int64_t)c.L.ghost_cell.size();
+    P_.nq = nq;
+    P_.nghost = ngh;
+    P_.Wq = m.Alloc<T>(5 * nq);
+    P_.Rq = m.Alloc<T>(5 * nq);
+    P_.Ainvq = m.Alloc<T>(nq);
+    P_.Aq = m.Alloc<T>(nq);
+    P_.dUq = m.Alloc<T>(5 * nq);
+    P_.dUg = m.Alloc<T>(5 * std::max<int64_t>(ngh, 1));
+    Check(cudaMemset(P_.Wq, 0, 5 * nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.Rq, 0, 5 * nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.Ainvq, 0, nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.Aq, 0, nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
+    {
+      std::vector<T> lo(c.L.face_lo.begin(), c.L.face_lo.end());
+      std::vector<T> hi(c.L.face_hi.begin(), c.L.face_hi.end());
+      P_.face_lo = m.Upload(lo);
+      P_.face_hi = m.Upload(hi);
+    }
+    P_.nbq = m.Upload(c.L.nbq);
+    P_.qpos = m.Upload(c.L.qpos);
+    P_.ghost_cell = m.Upload(c.L.ghost_cell);
+    P_.ghost_src = m.Upload(c.L.ghost_src);
     for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(T)), "memset");
     // geometry and state
     std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
-    std::vector<uint8_t> mask(n, 0);
     for (int d = 0; d < 3; ++d) {
       wid[d].assign(n, 0.0);
       fa[d].assign(4 * n, 0.0);
@@ -224,7 +258,6 @@ class Runner : public RunnerBase {
         for (int v = 0; v < 5; ++v) W[v * n + o + x] = b.state0[x * b.nv + v];
         vol[o + x] = b.vol[x];
         for (int d = 0; d < 3; ++d) wid[d][o + x] = b.width[d * nc + x];
-        mask[o + x] = b.nbr_mask.empty() ? 0 : b.nbr_mask[x];
       }
       for (int d = 0; d < 3; ++d) {
         const int64_t nf = b.NFace(d);
@@ -247,7 +280,6 @@ class Runner : public RunnerBase {
       P_.width[d] = m.Upload(wid[d]);
       P_.fa[d] = m.Upload(fa[d]);
     }
-    P_.mask = m.Upload(mask);
     P_.blocks = c.d_blocks;
     P_.solves = c.d_solves;
     P_.states = c.d_states;
@@ -277,23 +309,33 @@ class Runner : public RunnerBase {
                     c_.stream);
   }
   void Relax() override {
-    Check(cudaMemsetAsync(P_.dU, 0, 5 * c_.ncell * sizeof(T), c_.stream), "memset");
+    // x = 0 before the first sweep: only the connection ghosts are read
+    // before being written
+    if (P_.nghost > 0)
+      Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
     for (int s = 0; s < c_.nsteps; ++s) {
       const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
       Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
     }
-    Launch<T>::ConnDu(P_, c_.d_conn_ops, (int)c_.L.conn_ops.size(), c_.stream);
+    Launch<T>::ConnDu(P_, c_.stream);
     for (int s = c_.nsteps - 1; s >= 0; --s) {
       const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
       Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
+    }
+    if (c_.flags & 1) {
+      Launch<T>::ConnDu(P_, c_.stream);
+      Launch<T>::MatRes(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_mres,
+                        (int)c_.L.cell_cta_block.size(), c_.stream);
     }
   }
   void Update() override {
     Launch<T>::Update(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_cell_cta_pos0,
                       c_.d_partials, (int)c_.L.cell_cta_block.size(), c_.stream);
-    k_norms<<<c_.nsolves, 32, 0, c_.stream>>>(c_.d_partials, c_.d_solve_cta0, c_.nsolves,
-                                              c_.d_ring, c_.ring_cap, c_.d_iter,
-                                              c_.d_solves, c_.d_cfl);
+    k_norms<<<c_.nsolves, 32, 0, c_.stream>>>(c_.d_partials,
+                                              (c_.flags & 1) ? c_.d_mres : nullptr,
+                                              c_.d_solve_cta0, c_.nsolves, c_.d_ring,
+                                              c_.ring_cap, c_.d_iter, c_.d_solves,
+                                              c_.d_cfl);
     k_iter_advance<<<1, 1, 0, c_.stream>>>(c_.d_iter);
   }
   void OneIteration() {
@@ -330,13 +372,14 @@ class Runner : public RunnerBase {
       Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                       c_.stream);
       Check(cudaEventRecord(e[5], c_.stream), "event");
-      Check(cudaMemsetAsync(P_.dU, 0, 5 * c_.ncell * sizeof(T), c_.stream), "memset");
+      if (P_.nghost > 0)
+        Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
       }
       Check(cudaEventRecord(e[6], c_.stream), "event");
-      Launch<T>::ConnDu(P_, c_.d_conn_ops, (int)c_.L.conn_ops.size(), c_.stream);
+      Launch<T>::ConnDu(P_, c_.stream);
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
@@ -355,8 +398,8 @@ class Runner : public RunnerBase {
     for (int q = 0; q < 8; ++q) ms[q] /= std::max(reps, 1);
     for (auto &x : e) cudaEventDestroy(x);
   }
-  void GetDU(int b, double *out) override { CopyOut(P_.dU, 5, b, out); }
-  void GetAinv(int b, double *out) override { CopyOut(P_.Ainv, 1, b, out); }
+  void GetDU(int b, double *out) override { CopyOutQ(P_.dUq, 5, b, out); }
+  void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, b, out); }
 
  private:
   template <typename U>
@@ -375,6 +418,24 @@ class Runner : public RunnerBase {
           for (int i = 0; i < b.ni; ++i) tmp[(q++) * w + v] = (double)h[b.Cell(i, j, k)];
     }
     std::memcpy(out, tmp.data(), tmp.size() * sizeof(double));
+  }
+
+  // q-ordered array -> physical cells of block bi, AoS, k slowest
+  template <typename U>
+  void CopyOutQ(const U *arr, int w, int bi, double *out) {
+    const Block &b = c_.setup->blocks[bi];
+    const int64_t cnt = (int64_t)b.ni * b.nj * b.nk, q0 = c_.L.q0[bi];
+    std::vector<U> h(cnt);
+    for (int v = 0; v < w; ++v) {
+      Check(cudaMemcpy(h.data(), arr + v * c_.nq + q0, cnt * sizeof(U),
+                       cudaMemcpyDeviceToHost),
+            "download");
+      size_t q = 0;
+      for (int k = 0; k < b.nk; ++k)
+        for (int j = 0; j < b.nj; ++j)
+          for (int i = 0; i < b.ni; ++i)
+            out[(q++) * w + v] = (double)h[c_.L.qpos[c_.cell0[bi] + b.Cell(i, j, k)] - q0];
+    }
   }
 
   BatchCore &c_;
@@ -443,17 +504,85 @@ void BuildLists(BatchCore &c) {
       for (int64_t t = 0; t < ncta; ++t) L.face_cta_block[d].push_back(b);
     }
   }
+  // hyperplane-ordered (q) numbering of the physical cells: block by block,
+  // in each block the reference's visit order (plane, then k, then j)
+  L.q0.assign(c.nblocks + 1, 0);
+  for (int b = 0; b < c.nblocks; ++b)
+    L.q0[b + 1] = L.q0[b] + (int64_t)st.blocks[b].ni * st.blocks[b].nj * st.blocks[b].nk;
+  c.nq = L.q0[c.nblocks];
+  L.qpos.assign(c.ncell, -1);
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &bk = st.blocks[b];
+    for (size_t q = 0; q < bk.plane_cells.size(); ++q)
+      L.qpos[c.cell0[b] + bk.plane_cells[q]] = (int32_t)(L.q0[b] + (int64_t)q);
+  }
+  // connection ghosts adjacent to a physical cell (layer 1): their W and dU
+  // enter the off-diagonal sums
+  std::vector<int32_t> ghost_slot(c.ncell, -1);
+  for (int b = 0; b < c.nblocks; ++b) {
+    for (const auto &op : st.blocks[b].ops) {
+      if (op.layer != 1 || (op.type != ATH_BC_PERIODIC && op.type != ATH_BC_INTERBLOCK)) continue;
+      const int64_t gcell = c.cell0[b] + op.dst;
+      if (ghost_slot[gcell] >= 0) continue;
+      ghost_slot[gcell] = (int32_t)L.ghost_cell.size();
+      L.ghost_cell.push_back((int32_t)gcell);
+      const int32_t src_q = L.qpos[c.cell0[op.src_block] + op.src];
+      if (src_q < 0) throw Error(ATH_ERR_ARG, "connection donor is not a physical cell");
+      L.ghost_src.push_back(src_q);
+    }
+  }
+  const int64_t nq = c.nq;
+  L.nbq.assign(6 * nq, -1);
+  L.face_lo.assign(12 * nq, 0.0);
+  L.face_hi.assign(12 * nq, 0.0);
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &bk = st.blocks[b];
+    const int64_t st3[3] = {1, (int64_t)bk.NI, (int64_t)bk.NI * bk.NJ};
+    const int nd[3] = {bk.ni, bk.nj, bk.nk};
+    for (size_t ql = 0; ql < bk.plane_cells.size(); ++ql) {
+      const int64_t q = L.q0[b] + (int64_t)ql;
+      const int64_t cl = bk.plane_cells[ql];
+      const int ijk[3] = {(int)(cl % bk.NI) - bk.ng, (int)((cl / bk.NI) % bk.NJ) - bk.ng,
+                          (int)(cl / ((int64_t)bk.NI * bk.NJ)) - bk.ng};
+      const uint8_t m = bk.nbr_mask[cl];
+      for (int d = 0; d < 3; ++d) {
+        for (int up = 0; up < 2; ++up) {
+          const int64_t nbl = up ? cl + st3[d] : cl - st3[d];
+          int32_t code = -1;
+          if (m & (1u << (2 * d + up))) {
+            const int nbi = ijk[d] + (up ? 1 : -1);
+            if (nbi >= 0 && nbi < nd[d]) {
+              code = L.qpos[c.cell0[b] + nbl];
+            } else {
+              const int32_t slot = ghost_slot[c.cell0[b] + nbl];
+              if (slot < 0) throw Error(ATH_ERR_ARG, "connection ghost without a donor");
+              code = -slot - 2;
+            }
+          }
+          L.nbq[(int64_t)(3 * up + d) * nq + q] = code;
+          // face between the cell and this neighbour
+          int fi = ijk[0], fj = ijk[1], fk = ijk[2];
+          if (up) (d == 0 ? fi : d == 1 ? fj : fk) += 1;
+          const int64_t f = bk.Face(d, fi, fj, fk);
+          const int64_t nf = bk.NFace(d);
+          auto &dst = up ? L.face_hi : L.face_lo;
+          for (int comp = 0; comp < 4; ++comp)
+            dst[(int64_t)(d * 4 + comp) * nq + q] = bk.farea[d][comp * nf + f];
+        }
+      }
+    }
+  }
   // hyperplane steps: step s holds plane s of every block that has one
   c.nsteps = 0;
   for (auto &b : st.blocks) c.nsteps = std::max(c.nsteps, (int)b.plane_offsets.size() - 1);
   L.step_off.assign(c.nsteps + 1, 0);
-  for (int s = 0; s < c.nsteps; ++s) {
-    L.step_off[s] = (int32_t)L.sweep_items.size();
+  for (int s2 = 0; s2 < c.nsteps; ++s2) {
+    L.step_off[s2] = (int32_t)L.sweep_items.size();
     for (int b = 0; b < c.nblocks; ++b) {
       const Block &bk = st.blocks[b];
-      if (s + 1 >= (int)bk.plane_offsets.size()) continue;
-      for (int q = bk.plane_offsets[s]; q < bk.plane_offsets[s + 1]; ++q)
-        L.sweep_items.push_back(make_int2((int)(c.cell0[b] + bk.plane_cells[q]), b));
+      if (s2 + 1 >= (int)bk.plane_offsets.size()) continue;
+      for (int q = bk.plane_offsets[s2]; q < bk.plane_offsets[s2 + 1]; ++q)
+        L.sweep_items.push_back(make_int2((int)(L.q0[b] + q), b));
     }
   }
   L.step_off[c.nsteps] = (int32_t)L.sweep_items.size();
@@ -493,7 +622,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.nsolves = (int)st.solves.size();
   c.nblocks = (int)st.blocks.size();
   for (const auto &b : st.blocks)
-    if (b.nv != 5 || b.ng < 2)
+    if (b.nv != 5 || b.ng < 1)
       throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");
   BuildLists(c);
@@ -520,6 +649,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.cfl_step = p.cfl_step;
     x.cfl_max = p.cfl_max;
     x.limiter = p.limiter;
+    x.recon = p.recon;
+    x.flux = p.flux;
+    x.padded_values = 0.0;
+    x.cells = 0.0;
+    for (int b : st.solves[s].blocks) {
+      x.padded_values += (double)st.blocks[b].NCell() * kNv;
+      x.cells += (double)st.blocks[b].ni * st.blocks[b].nj * st.blocks[b].nk;
+    }
     x.nstates = (int32_t)st.solves[s].states.size();
     x.state0 = (int32_t)states.size();
     for (auto &q : st.solves[s].states) states.push_back(q);
@@ -544,6 +681,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_conn_ops = m.Upload(c.L.conn_ops);
   c.d_op_solve = m.Upload(c.L.op_solve);
   c.d_partials = m.Alloc<NormPartial>(c.L.cell_cta_block.size());
+  c.d_mres = m.Alloc<double>(c.L.cell_cta_block.size());
   c.d_ring = m.Alloc<NormOut>((size_t)c.ring_cap * c.nsolves);
   Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
   Check(cudaEventCreate(&c.ev0), "event");
@@ -568,7 +706,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   // launches of one iteration: cfl, ghost, 3 faces, cell, 2 x steps of
   // sweeps, dU connection copy, update, norms, counter
   c.launches_per_iter = 1 + (c.L.ops.empty() ? 0 : 1) + 3 + 1 + 2 * c.nsteps +
-                        (c.L.conn_ops.empty() ? 0 : 1) + 3;
+                        (c.L.ghost_cell.empty() ? 0 : 1) + 3 +
+                        ((flags & 1) ? 1 + (c.L.ghost_cell.empty() ? 0 : 1) : 0);
 }
 
 // Reads norms of iterations [it0, it0+n) from the ring into norms_h.
@@ -589,6 +728,7 @@ void ReadNorms(BatchCore &c, int64_t it0, int n, ath_norms *norms_h) {
       for (int v = 0; v < 7; ++v) d.l2[v] = o.l2[v];
       d.linf = o.linf;
       d.cfl = o.cfl;
+      d.matrix_resid = o.matrix_resid;
       d.status = o.bad ? ATH_ERR_NONPHYSICAL : ATH_OK;
       d.linf_block = d.linf_i = d.linf_j = d.linf_k = d.linf_eqn = -1;
       if (o.linf_pos != INT64_MAX) {

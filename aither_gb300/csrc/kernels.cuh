@@ -30,7 +30,10 @@ struct BlockDev {
 struct SolveDev {
   double gas_r, gas_n, gas_hf;
   double kappa, theta, zeta, relax, cfl_start, cfl_step, cfl_max;
-  int32_t limiter, nstates, state0, pad;
+  double padded_values;  // sum over blocks of padded cells x nv
+  double cells;          // physical cells of the solve
+  int32_t limiter, nstates, state0, recon;
+  int32_t flux, pad0, pad1, pad2;
 };
 
 // A ghost-cell assignment with pool indices.
@@ -50,24 +53,42 @@ struct NormPartial {
 };
 
 // Device pointers of a batch.  Passed by value to every kernel.
+//
+// The LU-SGS sweeps work on a second copy of their working set stored in
+// hyperplane order ("q order": block by block, plane by plane, inside a
+// plane by k then j), so that the cells of one hyperplane and of its
+// neighbour plane are contiguous runs: Wq, Rq, Ainvq, dUq, the face
+// normals of each cell's lower and upper faces, and the q index of each
+// neighbour (nbq; -1 = no off-diagonal term, <= -2 = a ghost cell across a
+// connection, slot -nbq-2 of the ghost tables).
 template <typename T>
 struct Pools {
   double *W;        // [5][ncell] primitive state, FP64
   double *R;        // [5][ncell] residual, FP64
-  T *dU;            // [5][ncell] implicit update
   T *flux[3];       // [5][ncell] F.|A| on faces of direction d
   double *lam;      // [ncell] cell spectral radius
   double *dt;       // [ncell]
-  T *Ainv;          // [ncell] inverse of the scalar main diagonal
   const double *vol;       // [ncell]
   const double *width[3];  // [ncell]
   const double *fa[3];     // [4][ncell] unit normal x,y,z and magnitude
-  const uint8_t *mask;     // [ncell] neighbour bits for the sweeps
+  const int32_t *qpos;     // [ncell] q index of a physical cell, -1 for ghosts
+  // hyperplane-ordered sweep working set, nq = physical cells of the batch
+  T *Wq;            // [5][nq] state in the sweep's arithmetic
+  T *Rq;            // [5][nq]
+  T *Ainvq;         // [nq] inverse of the scalar main diagonal
+  T *Aq;            // [nq] the scalar main diagonal (matrix residual)
+  T *dUq;           // [5][nq] implicit update
+  const T *face_lo; // [3 dirs][4][nq] lower face of each direction
+  const T *face_hi; // [3 dirs][4][nq] upper face
+  const int32_t *nbq;      // [6][nq] neighbours: lower i,j,k then upper i,j,k
+  const int32_t *ghost_cell;  // [nghost] pool cell of each connection ghost
+  const int32_t *ghost_src;   // [nghost] q index of the partner interior cell
+  T *dUg;           // [5][nghost] update of the connection ghosts
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
   const double *cfl;       // [nsolves] current CFL
-  int64_t ncell;
+  int64_t ncell, nq, nghost;
 };
 
 __device__ __forceinline__ int64_t StrideOf(const BlockDev &b, int d) {
@@ -115,13 +136,14 @@ template <typename T>
 __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block);
 
 // One hyperplane of the LU-SGS forward / backward sweep
-// (lusgs::LUSGS_Forward/Backward, src/linearSolver.cpp:341,385).
+// (lusgs::LUSGS_Forward/Backward, src/linearSolver.cpp:341,385); items are
+// (q index, block) pairs.
 template <typename T>
 __global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward);
 
 // dU ghost copies across connections (SwapImplicitUpdate, src/utility.cpp:400).
 template <typename T>
-__global__ void k_conn_du(Pools<T> P, const GhostOpDev *ops, int nops);
+__global__ void k_conn_du(Pools<T> P);
 
 // Conserved update and per-CTA partial norms (procBlock::UpdateBlock,
 // src/procBlock.cpp:826).
@@ -138,11 +160,18 @@ struct NormOut {
   int32_t bad;
   int32_t pad;
   double cfl;
+  double matrix_resid;
 };
-__global__ void k_norms(const NormPartial *partials, const int32_t *solve_cta0,
-                        int nsolves, NormOut *ring, int ring_cap,
-                        int64_t *iter_counter, const SolveDev *solves,
+__global__ void k_norms(const NormPartial *partials, const double *mres_partials,
+                        const int32_t *solve_cta0, int nsolves, NormOut *ring,
+                        int ring_cap, int64_t *iter_counter, const SolveDev *solves,
                         double *cfl);
+
+// Logged matrix residual r = -(A x - (L x - U x) - b) summed as r^2 per CTA
+// (linearSolver::Residual / AXmB, src/linearSolver.cpp:58,92).
+template <typename T>
+__global__ void k_matres(Pools<T> P, const int32_t *list, const int32_t *cta_block,
+                         double *mres_partials);
 // Sets the CFL of the current iteration from the iteration counter
 // (input::CalcCFL, src/input.cpp:647).
 __global__ void k_cfl(const SolveDev *solves, int nsolves,
@@ -160,10 +189,12 @@ struct Launch {
                    int ncta, cudaStream_t s);
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward,
                     cudaStream_t s);
-  static void ConnDu(const Pools<T> &P, const GhostOpDev *ops, int nops, cudaStream_t s);
+  static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,
                      cudaStream_t s);
+  static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                     double *mres_partials, int ncta, cudaStream_t s);
 };
 
 }  // namespace ath

@@ -124,23 +124,43 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
   const Gas<T> g = GasOf<T>(sv);
   const int64_t n = P.ncell;
   const int64_t s = StrideOf(b, D);
-  const Prim<T> wm2 = LoadW<T>(P.W, n, c - 2 * s);
+  const double *wd = P.width[D];
   const Prim<T> wm1 = LoadW<T>(P.W, n, c - s);
   const Prim<T> w0 = LoadW<T>(P.W, n, c);
-  const Prim<T> wp1 = LoadW<T>(P.W, n, c + s);
-  const double *wd = P.width[D];
-  const T xm2 = (T)wd[c - 2 * s], xm1 = (T)wd[c - s], x0 = (T)wd[c],
-          xp1 = (T)wd[c + s];
-  const T kappa = (T)sv.kappa;
-  // face state from the lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
-  const Prim<T> L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
-  // from the upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
-  const Prim<T> R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+  Prim<T> L, R;
+  if (sv.recon == ATH_RECON_CONSTANT) {
+    L = wm1;
+    R = w0;
+  } else if (sv.recon == ATH_RECON_MUSCL) {
+    const Prim<T> wm2 = LoadW<T>(P.W, n, c - 2 * s);
+    const Prim<T> wp1 = LoadW<T>(P.W, n, c + s);
+    const T xm2 = (T)wd[c - 2 * s], xm1 = (T)wd[c - s], x0 = (T)wd[c], xp1 = (T)wd[c + s];
+    const T kappa = (T)sv.kappa;
+    // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
+    L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
+    // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
+    R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+  } else {
+    const Prim<T> wm3 = LoadW<T>(P.W, n, c - 3 * s);
+    const Prim<T> wm2 = LoadW<T>(P.W, n, c - 2 * s);
+    const Prim<T> wp1 = LoadW<T>(P.W, n, c + s);
+    const Prim<T> wp2 = LoadW<T>(P.W, n, c + 2 * s);
+    const bool z = sv.recon == ATH_RECON_WENOZ;
+    const T wl[5] = {(T)wd[c - 3 * s], (T)wd[c - 2 * s], (T)wd[c - s], (T)wd[c],
+                     (T)wd[c + s]};
+    const T wu[5] = {(T)wd[c + 2 * s], (T)wd[c + s], (T)wd[c], (T)wd[c - s],
+                     (T)wd[c - 2 * s]};
+    L = Weno(wm3, wm2, wm1, w0, wp1, wl, z);
+    R = Weno(wp2, wp1, w0, wm1, wm2, wu, z);
+  }
   const double *fa = P.fa[D];
   const T nx = (T)fa[c], ny = (T)fa[n + c], nz = (T)fa[2 * n + c],
           mag = (T)fa[3 * n + c];
   T f[5];
-  RoeFlux(L, R, g, nx, ny, nz, f);
+  if (sv.flux == ATH_FLUX_AUSM)
+    AusmFlux(L, R, g, nx, ny, nz, f);
+  else
+    RoeFlux(L, R, g, nx, ny, nz, f);
   T *out = P.flux[D];
 #pragma unroll
   for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * mag;
@@ -189,66 +209,99 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   const double dt = cfl * (vol / lam);
   P.dt[c] = dt;
   const double a = lam * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
-  P.Ainv[c] = (T)(1.0 / a);
+  // hyperplane-ordered copies for the sweeps
+  const int64_t q = P.qpos[c];
+  const int64_t nq = P.nq;
+  P.Ainvq[q] = (T)(1.0 / a);
+  P.Aq[q] = (T)a;
+  P.Wq[q] = w.rho;
+  P.Wq[nq + q] = w.u;
+  P.Wq[2 * nq + q] = w.v;
+  P.Wq[3 * nq + q] = w.w;
+  P.Wq[4 * nq + q] = w.p;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) P.Rq[v * nq + q] = (T)P.R[v * n + c];
 }
 
 // ---------------------------------------------------------------------------
-// LU-SGS hyperplane sweep
+// Off-diagonal sum of one cell: lower neighbours with the "positive" sign
+// (procBlock::ImplicitLower) or upper neighbours with the negative sign
+// (ImplicitUpper), accumulated i, j, k from zero.
+template <typename T>
+__device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g, int64_t q,
+                                           bool lower, T acc[5]) {
+  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
+  const T *face = lower ? P.face_lo : P.face_hi;
+  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = T(0);
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    const int32_t nb = nbq[d * nq + q];
+    if (nb == -1) continue;
+    Prim<T> s;
+    T du[5];
+    if (nb >= 0) {
+      s.rho = P.Wq[nb];
+      s.u = P.Wq[nq + nb];
+      s.v = P.Wq[2 * nq + nb];
+      s.w = P.Wq[3 * nq + nb];
+      s.p = P.Wq[4 * nq + nb];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
+    } else {
+      const int64_t slot = -(int64_t)nb - 2;
+      s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
+    }
+    const T *f = face + (int64_t)d * 4 * nq;
+    T o[5];
+    ScalarOffDiag(s, du, g, f[q], f[nq + q], f[2 * nq + q], f[3 * nq + q], lower, o);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// LU-SGS hyperplane sweep on the q-ordered working set
 template <typename T>
 __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, int n_items,
                                                int forward) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
   const int2 it = items[t];
-  const int64_t c = it.x;
+  const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
   const Gas<T> g = GasOf<T>(sv);
-  const int64_t n = P.ncell;
-  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
-  const uint8_t m = P.mask[c];
-  T acc[5] = {T(0), T(0), T(0), T(0), T(0)};
-#pragma unroll 1
-  for (int d = 0; d < 3; ++d) {
-    if (!(m & (1u << (2 * d + (forward ? 0 : 1))))) continue;
-    const int64_t nb = forward ? c - st[d] : c + st[d];
-    const int64_t f = forward ? c : c + st[d];  // face between c and nb
-    const double *fa = P.fa[d];
-    const Prim<T> s = LoadW<T>(P.W, n, nb);
-    T du[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) du[v] = P.dU[v * n + nb];
-    T o[5];
-    ScalarOffDiag(s, du, g, (T)fa[f], (T)fa[n + f], (T)fa[2 * n + f], (T)fa[3 * n + f],
-                  forward != 0, o);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
-  }
-  const T ainv = P.Ainv[c];
+  const int64_t nq = P.nq;
+  T acc[5];
+  OffDiagSum(P, g, q, forward != 0, acc);
+  const T ainv = P.Ainvq[q];
   if (forward) {
     const T thetaInv = (T)(1.0 / sv.theta);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T bv = -thetaInv * (T)P.R[v * n + c];
-      P.dU[v * n + c] = (bv + acc[v]) * ainv;
+      const T bv = -thetaInv * P.Rq[v * nq + q];
+      P.dUq[v * nq + q] = (bv + acc[v]) * ainv;
     }
   } else {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T xold = P.dU[v * n + c];
-      P.dU[v * n + c] = xold - acc[v] * ainv;
+      const T xold = P.dUq[v * nq + q];
+      P.dUq[v * nq + q] = xold - acc[v] * ainv;
     }
   }
 }
 
 template <typename T>
-__global__ void k_conn_du(Pools<T> P, const GhostOpDev *ops, int nops) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nops) return;
-  const GhostOpDev op = ops[t];
-  const int64_t n = P.ncell;
+__global__ void k_conn_du(Pools<T> P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P.nghost) return;
+  const int64_t src = P.ghost_src[t];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) P.dU[v * n + op.dst] = P.dU[v * n + op.src];
+  for (int v = 0; v < 5; ++v) P.dUg[v * P.nghost + t] = P.dUq[v * P.nq + src];
 }
 
 // ---------------------------------------------------------------------------
@@ -274,8 +327,9 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     const Gas<double> g = GasOf<double>(sv);
     const Prim<double> w = LoadW<double>(P.W, n, c);
     double du[5];
+    const int64_t q = P.qpos[c];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) du[v] = (double)P.dU[v * n + c];
+    for (int v = 0; v < 5; ++v) du[v] = (double)P.dUq[v * P.nq + q];
     const Prim<double> u = UpdateWithCons(w, g, du);
     if (!(u.rho > 0.0) || !(u.p > 0.0) || !isfinite(u.u) || !isfinite(u.v) ||
         !isfinite(u.w))
@@ -343,6 +397,50 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
 }
 
 // ---------------------------------------------------------------------------
+// logged matrix residual
+template <typename T>
+__global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list,
+                                                 const int32_t *cta_block,
+                                                 double *mres_partials) {
+  __shared__ double s_sum[kCta / 32];
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  double sum = 0.0;
+  if (c >= 0) {
+    const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+    const SolveDev sv = P.solves[b.solve];
+    const Gas<T> g = GasOf<T>(sv);
+    const int64_t q = P.qpos[c], nq = P.nq;
+    T L[5], U[5];
+    OffDiagSum(P, g, q, true, L);
+    OffDiagSum(P, g, q, false, U);
+    const T thetaInv = (T)(1.0 / sv.theta);
+    const T a = P.Aq[q];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const T off = L[v] - U[v];
+      const T bv = -thetaInv * P.Rq[v * nq + q];
+      const T axmb = P.dUq[v * nq + q] * a - off - bv;
+      const double r = 0.0 - (double)axmb;
+      sum += r * r;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kCta / 32; ++w) t += s_sum[w];
+    mres_partials[blockIdx.x] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+void Launch<T>::MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                       double *mres_partials, int ncta, cudaStream_t s) {
+  if (ncta > 0) k_matres<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
+}
 template <typename T>
 void Launch<T>::Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
                       const int32_t *op_solve, cudaStream_t s) {
@@ -367,8 +465,8 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward,
   if (n > 0) k_sweep<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n, forward);
 }
 template <typename T>
-void Launch<T>::ConnDu(const Pools<T> &P, const GhostOpDev *ops, int nops, cudaStream_t s) {
-  if (nops > 0) k_conn_du<T><<<(nops + 127) / 128, 128, 0, s>>>(P, ops, nops);
+void Launch<T>::ConnDu(const Pools<T> &P, cudaStream_t s) {
+  if (P.nghost > 0) k_conn_du<T><<<(unsigned)((P.nghost + 127) / 128), 128, 0, s>>>(P);
 }
 template <typename T>
 void Launch<T>::Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

@@ -160,6 +160,9 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
                            std::to_string((long long)ATH_NOALLOC_MAX_CELLS));
     if (phys->limiter < ATH_LIMITER_NONE || phys->limiter > ATH_LIMITER_VANALBADA)
       throw ath::Error(ATH_ERR_ARG, "unknown limiter");
+    if (phys->recon != ATH_RECON_MUSCL || phys->flux != ATH_FLUX_ROE)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual implements MUSCL reconstruction with the Roe flux");
     int device = 0;
     ath::Check(cudaGetDevice(&device), "cudaGetDevice");
     ath::BlockArgs a{};
@@ -190,6 +193,8 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
     sv.zeta = phys->zeta;
     sv.relax = phys->relax;
     sv.limiter = phys->limiter;
+    sv.recon = ATH_RECON_MUSCL;
+    sv.flux = ATH_FLUX_ROE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int64_t nf[3] = {(int64_t)(blk->ni + 1) * blk->nj * blk->nk,
                            (int64_t)blk->ni * (blk->nj + 1) * blk->nk,

@@ -255,6 +255,187 @@ __device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
   for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - d[v])) * T(0.5);
 }
 
+// ---------------------------------------------------------------------------
+// WENO5 / WENO-Z on non-uniform cell widths (FaceReconWENO,
+// include/reconstruction.hpp:244)
+
+// StencilWidth (include/utility.hpp:104)
+template <typename T>
+__device__ __forceinline__ T StencilWidth(const T w[5], int start, int end) {
+  T width = T(0);
+  if (end > start) {
+    for (int q = start; q < end; ++q) width += w[q];
+  } else if (start > end) {
+    T a = T(0);
+    for (int q = end; q < start; ++q) a += w[q];
+    width = T(-1) * a;
+  }
+  return width;
+}
+
+// LagrangeCoeff (src/utility.cpp:449)
+template <typename T, int DEG>
+__device__ __forceinline__ void LagrangeCoeff(const T w[5], int rr, int ii, T coeffs[DEG + 1]) {
+#pragma unroll
+  for (int jj = 0; jj <= DEG; ++jj) {
+    coeffs[jj] = T(0);
+    for (int mm = jj + 1; mm <= DEG + 1; ++mm) {
+      T numer = T(0), denom = T(1);
+      for (int ll = 0; ll <= DEG + 1; ++ll) {
+        if (ll != mm) {
+          T numProd = T(1);
+          for (int qq = 0; qq <= DEG + 1; ++qq)
+            if (qq != mm && qq != ll) numProd *= StencilWidth(w, ii - rr + qq, ii + 1);
+          numer += numProd;
+          denom *= StencilWidth(w, ii - rr + ll, ii - rr + mm);
+        }
+      }
+      coeffs[jj] += numer / denom;
+    }
+    coeffs[jj] *= w[ii - rr + jj];
+  }
+}
+
+// Derivative2nd (include/utility.hpp:117)
+template <typename T>
+__device__ __forceinline__ T Deriv2nd(T x0, T x1, T x2, T y0, T y1, T y2) {
+  const T fwd = (y2 - y1) / (T(0.5) * (x2 + x1));
+  const T bck = (y1 - y0) / (T(0.5) * (x1 + x0));
+  return (fwd - bck) / (T(0.25) * (x2 + x0) + T(0.5) * x1);
+}
+
+// BetaIntegral (include/reconstruction.hpp:157,171)
+template <typename T>
+__device__ __forceinline__ T BetaInt(T d1, T d2, T dx, T x) {
+  return (d1 * d1 * x + d1 * d2 * x * x + d2 * d2 * pow(x, T(3)) / T(3)) * dx +
+         d2 * d2 * x * pow(dx, T(3));
+}
+template <typename T>
+__device__ __forceinline__ T BetaInt2(T d1, T d2, T dx) {
+  return BetaInt(d1, d2, dx, T(0.5) * dx) - BetaInt(d1, d2, dx, T(-0.5) * dx);
+}
+
+// per-face WENO weights, shared by the five variables
+template <typename T>
+struct WenoCoeffs {
+  T c0[3], c1[3], c2[3], lw0, lw1, lw2;
+};
+template <typename T>
+__device__ __forceinline__ WenoCoeffs<T> MakeWeno(const T w[5]) {
+  WenoCoeffs<T> k;
+  T full[5];
+  LagrangeCoeff<T, 2>(w, 2, 2, k.c0);
+  LagrangeCoeff<T, 2>(w, 1, 2, k.c1);
+  LagrangeCoeff<T, 2>(w, 0, 2, k.c2);
+  LagrangeCoeff<T, 4>(w, 2, 2, full);
+  k.lw0 = full[0] / k.c0[0];
+  k.lw1 = full[4] / k.c2[2];
+  k.lw2 = T(1) - k.lw0 - k.lw1;
+  return k;
+}
+// one variable: y = (upwind3, upwind2, upwind1, downwind1, downwind2)
+template <typename T>
+__device__ __forceinline__ T Weno1(const WenoCoeffs<T> &k, const T w[5], T y3, T y2, T y1,
+                                   T d1, T d2, bool wenoz) {
+  const T st0 = k.c0[0] * y3 + k.c0[1] * y2 + k.c0[2] * y1;
+  const T st1 = k.c1[0] * y2 + k.c1[1] * y1 + k.c1[2] * d1;
+  const T st2 = k.c2[0] * y1 + k.c2[1] * d1 + k.c2[2] * d2;
+  // Beta0/Beta1/Beta2 (include/reconstruction.hpp:186-240)
+  T dd = Deriv2nd(w[0], w[1], w[2], y3, y2, y1);
+  T d = (y1 - y2) / (T(0.5) * (w[2] + w[1])) + T(0.5) * w[2] * dd;
+  const T b0 = BetaInt2(d, dd, w[2]);
+  dd = Deriv2nd(w[1], w[2], w[3], y2, y1, d1);
+  d = (d1 - y1) / (T(0.5) * (w[3] + w[2])) - T(0.5) * w[2] * dd;
+  const T b1 = BetaInt2(d, dd, w[2]);
+  dd = Deriv2nd(w[2], w[3], w[4], y1, d1, d2);
+  d = (d1 - y1) / (T(0.5) * (w[3] + w[2])) - T(0.5) * w[2] * dd;
+  const T b2 = BetaInt2(d, dd, w[2]);
+  T n0, n1, n2;
+  if (wenoz) {
+    const T eps = T(1.0e-40);
+    const T tau5 = fabs(b0 - b2);
+    const T t0 = tau5 / (eps + b0), t1 = tau5 / (eps + b1), t2 = tau5 / (eps + b2);
+    n0 = k.lw0 * (T(1) + t0 * t0);
+    n1 = k.lw1 * (T(1) + t1 * t1);
+    n2 = k.lw2 * (T(1) + t2 * t2);
+  } else {
+    const T eps = T(1.0e-6);
+    n0 = k.lw0 / ((eps + b0) * (eps + b0));
+    n1 = k.lw1 / ((eps + b1) * (eps + b1));
+    n2 = k.lw2 / ((eps + b2) * (eps + b2));
+  }
+  const T sum = n0 + n1 + n2;
+  n0 /= sum;
+  n1 /= sum;
+  n2 /= sum;
+  return n0 * st0 + n1 * st1 + n2 * st2;
+}
+template <typename T>
+__device__ __forceinline__ Prim<T> Weno(const Prim<T> &u3, const Prim<T> &u2,
+                                        const Prim<T> &u1, const Prim<T> &d1,
+                                        const Prim<T> &d2, const T w[5], bool wenoz) {
+  const WenoCoeffs<T> k = MakeWeno(w);
+  Prim<T> o;
+  o.rho = Weno1(k, w, u3.rho, u2.rho, u1.rho, d1.rho, d2.rho, wenoz);
+  o.u = Weno1(k, w, u3.u, u2.u, u1.u, d1.u, d2.u, wenoz);
+  o.v = Weno1(k, w, u3.v, u2.v, u1.v, d1.v, d2.v, wenoz);
+  o.w = Weno1(k, w, u3.w, u2.w, u1.w, d1.w, d2.w, wenoz);
+  o.p = Weno1(k, w, u3.p, u2.p, u1.p, d1.p, d2.p, wenoz);
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// AUSMPW+ (Kim, Kim & Rho 1998) with c* = sqrt(cL cR) (AUSMFlux,
+// include/inviscidFlux.hpp:396; inviscidFlux::AUSMFlux :162)
+template <typename T>
+__device__ __forceinline__ T SignOf(T x) {
+  return (T)((T(0) < x) - (x < T(0)));
+}
+template <typename T>
+__device__ __forceinline__ void AusmFlux(const Prim<T> &L, const Prim<T> &R, const Gas<T> &g,
+                                         T nx, T ny, T nz, T f[5]) {
+  const T vnL = Dot(L.u, L.v, L.w, nx, ny, nz);
+  const T vnR = Dot(R.u, R.v, R.w, nx, ny, nz);
+  const T sosStar = sqrt(SoS(L, g) * SoS(R, g));
+  const T vel = T(0.5) * (vnL + vnR);
+  T sos = sosStar;
+  if (vel < T(0)) {
+    sos = sosStar * sosStar / ((vnR < sosStar) ? sosStar : vnR);
+  } else if (vel > T(0)) {
+    sos = sosStar * sosStar / ((vnL < sosStar) ? sosStar : vnL);
+  }
+  const T ml = vnL / sos, mr = vnR / sos;
+  const T mlp = ml + T(1), mrm = mr - T(1);
+  const T mPlusL = fabs(ml) <= T(1) ? T(0.25) * (mlp * mlp) : T(0.5) * (ml + fabs(ml));
+  const T mMinusR = fabs(mr) <= T(1) ? T(-0.25) * (mrm * mrm) : T(0.5) * (mr - fabs(mr));
+  const T pPlus = fabs(ml) <= T(1) ? T(0.25) * (mlp * mlp) * (T(2) - ml)
+                                   : T(0.5) * (T(1) + SignOf(ml));
+  const T pMinus = fabs(mr) <= T(1) ? T(0.25) * (mrm * mrm) * (T(2) + mr)
+                                    : T(0.5) * (T(1) - SignOf(mr));
+  const T ps = pPlus * L.p + pMinus * R.p;
+  const T ra = L.p / R.p, rb = R.p / L.p;
+  const T w = T(1) - pow((rb < ra) ? rb : ra, T(3));
+  const T fl = fabs(ml) < T(1) ? L.p / ps - T(1) : T(0);
+  const T fr = fabs(mr) < T(1) ? R.p / ps - T(1) : T(0);
+  const T mavg = mPlusL + mMinusR;
+  const T mPlusLBar = mavg >= T(0) ? mPlusL + mMinusR * ((T(1) - w) * (T(1) + fr) - fl)
+                                   : mPlusL * w * (T(1) + fl);
+  const T mMinusRBar = mavg >= T(0) ? mMinusR * w * (T(1) + fr)
+                                    : mMinusR + mPlusL * ((T(1) - w) * (T(1) + fl) - fr);
+  const T vl = mPlusLBar * sos;
+  f[0] = L.rho * vl;
+  f[1] = L.rho * vl * L.u + pPlus * L.p * nx;
+  f[2] = L.rho * vl * L.v + pPlus * L.p * ny;
+  f[3] = L.rho * vl * L.w + pPlus * L.p * nz;
+  f[4] = L.rho * vl * Enthalpy(L, g);
+  const T vr = mMinusRBar * sos;
+  f[0] += R.rho * vr;
+  f[1] += R.rho * vr * R.u + pMinus * R.p * nx;
+  f[2] += R.rho * vr * R.v + pMinus * R.p * ny;
+  f[3] += R.rho * vr * R.w + pMinus * R.p * nz;
+  f[4] += R.rho * vr * Enthalpy(R, g);
+}
+
 // InvCellSpectralRadius (include/spectralRadius.hpp:44)
 template <typename T>
 __device__ __forceinline__ T InvCellSpecRad(const Prim<T> &s, const Gas<T> &g,

@@ -828,7 +828,7 @@ void AppendInput(Setup &st, const std::string &path) {
   else if (fr == "weno") { ph.recon = ATH_RECON_WENO; }
   else if (fr == "wenoZ") { ph.recon = ATH_RECON_WENOZ; }
   else Fail("unsupported faceReconstruction " + fr);
-  if (ph.recon != ATH_RECON_MUSCL) Fail("only MUSCL reconstruction is supported");
+
   const auto lim = get("limiter", "none");
   ph.limiter = lim == "none" ? ATH_LIMITER_NONE
                : lim == "minmod" ? ATH_LIMITER_MINMOD
@@ -837,7 +837,7 @@ void AppendInput(Setup &st, const std::string &path) {
   const auto flux = get("inviscidFlux", "roe");
   ph.flux = flux == "roe" ? ATH_FLUX_ROE : flux == "ausm" ? ATH_FLUX_AUSM
             : (Fail("unsupported inviscidFlux " + flux), 0);
-  if (ph.flux != ATH_FLUX_ROE) Fail("only the roe inviscid flux is supported");
+
   const auto ms = get("matrixSolver", "lusgs");
   ph.solver = ms == "lusgs" ? ATH_SOLVER_LUSGS : ms == "blusgs" ? ATH_SOLVER_BLUSGS
               : (Fail("unsupported matrixSolver " + ms), 0);
@@ -859,7 +859,8 @@ void AppendInput(Setup &st, const std::string &path) {
   if (ph.eqn != ATH_EQN_EULER) Fail("only equationSet euler is supported");
   ph.turb = ATH_TURB_NONE;
   ph.nv = 5;
-  ph.ng = 2;
+  // input::NumberGhostLayers (src/input.cpp:1127): 1 constant, 2 MUSCL, 3 WENO
+  ph.ng = ph.recon == ATH_RECON_CONSTANT ? 1 : (ph.recon == ATH_RECON_MUSCL ? 2 : 3);
 
   // fluid and references
   Fluid fl;

@@ -47,6 +47,8 @@ struct orc_case {
   osolve *s;
   int64_t iter;
   int nthreads;
+  int matrix_resid;     /* compute the logged matrix residual */
+  double *mres;         /* [ns] last matrix residual */
 };
 
 /* ---------------------------------------------------------------- thermo */
@@ -222,6 +224,156 @@ static void roe_flux(const double *L, const double *R, const gas_t *g,
   }
 }
 
+/* ------------------------------------------------------------ WENO5 */
+/* StencilWidth (include/utility.hpp:104) */
+static double stencil_width(const double *w, int start, int end) {
+  double width = 0.0;
+  if (end > start) {
+    for (int q = start; q < end; ++q) width += w[q];
+  } else if (start > end) {
+    double a = 0.0;
+    for (int q = end; q < start; ++q) a += w[q];
+    width = -1.0 * a;
+  }
+  return width;
+}
+/* LagrangeCoeff (src/utility.cpp:449): weights of the cell averages that
+ * reconstruct the value at the upper face of cell ii on a non-uniform
+ * stencil starting rr cells left of ii */
+static void lagrange_coeff(const double *w, int degree, int rr, int ii, double *coeffs) {
+  for (int jj = 0; jj <= degree; ++jj) {
+    coeffs[jj] = 0.0;
+    for (int mm = jj + 1; mm <= degree + 1; ++mm) {
+      double numer = 0.0, denom = 1.0;
+      for (int ll = 0; ll <= degree + 1; ++ll) {
+        if (ll != mm) {
+          double numProd = 1.0;
+          for (int qq = 0; qq <= degree + 1; ++qq)
+            if (qq != mm && qq != ll) numProd *= stencil_width(w, ii - rr + qq, ii + 1);
+          numer += numProd;
+          denom *= stencil_width(w, ii - rr + ll, ii - rr + mm);
+        }
+      }
+      coeffs[jj] += numer / denom;
+    }
+    coeffs[jj] *= w[ii - rr + jj];
+  }
+}
+/* Derivative2nd (include/utility.hpp:117) */
+static double deriv2nd(double x0, double x1, double x2, double y0, double y1, double y2) {
+  const double fwd = (y2 - y1) / (0.5 * (x2 + x1));
+  const double bck = (y1 - y0) / (0.5 * (x1 + x0));
+  return (fwd - bck) / (0.25 * (x2 + x0) + 0.5 * x1);
+}
+/* BetaIntegral (include/reconstruction.hpp:157,171) */
+static double beta_int(double d1, double d2, double dx, double x) {
+  return (d1 * d1 * x + d1 * d2 * x * x + d2 * d2 * pow(x, 3.0) / 3.0) * dx +
+         d2 * d2 * x * pow(dx, 3.0);
+}
+static double beta_int2(double d1, double d2, double dx, double xl, double xh) {
+  return beta_int(d1, d2, dx, xh) - beta_int(d1, d2, dx, xl);
+}
+/* FaceReconWENO (include/reconstruction.hpp:244) with Beta0/1/2 (:186-240);
+ * c[5] = (upwind3, upwind2, upwind1, downwind1, downwind2), w[5] widths */
+static void weno(const double *const c[5], const double w[5], int wenoz, double *out) {
+  double c0[3], c1[3], c2[3], full[5];
+  lagrange_coeff(w, 2, 2, 2, c0);
+  lagrange_coeff(w, 2, 1, 2, c1);
+  lagrange_coeff(w, 2, 0, 2, c2);
+  lagrange_coeff(w, 4, 2, 2, full);
+  const double lw0 = full[0] / c0[0];
+  const double lw1 = full[4] / c2[2];
+  const double lw2 = 1.0 - lw0 - lw1;
+  for (int v = 0; v < NV; ++v) {
+    const double y3 = c[0][v], y2 = c[1][v], y1 = c[2][v], d1 = c[3][v], d2 = c[4][v];
+    const double st0 = c0[0] * y3 + c0[1] * y2 + c0[2] * y1;
+    const double st1 = c1[0] * y2 + c1[1] * y1 + c1[2] * d1;
+    const double st2 = c2[0] * y1 + c2[1] * d1 + c2[2] * d2;
+    double b0, b1, b2;
+    {
+      const double dd = deriv2nd(w[0], w[1], w[2], y3, y2, y1);
+      const double d = (y1 - y2) / (0.5 * (w[2] + w[1])) + 0.5 * w[2] * dd;
+      b0 = beta_int2(d, dd, w[2], -0.5 * w[2], 0.5 * w[2]);
+    }
+    {
+      const double dd = deriv2nd(w[1], w[2], w[3], y2, y1, d1);
+      const double d = (d1 - y1) / (0.5 * (w[3] + w[2])) - 0.5 * w[2] * dd;
+      b1 = beta_int2(d, dd, w[2], -0.5 * w[2], 0.5 * w[2]);
+    }
+    {
+      const double dd = deriv2nd(w[2], w[3], w[4], y1, d1, d2);
+      const double d = (d1 - y1) / (0.5 * (w[3] + w[2])) - 0.5 * w[2] * dd;
+      b2 = beta_int2(d, dd, w[2], -0.5 * w[2], 0.5 * w[2]);
+    }
+    double n0, n1, n2;
+    if (wenoz) {
+      const double tau5 = fabs(b0 - b2);
+      const double t0 = tau5 / (1.0e-40 + b0), t1 = tau5 / (1.0e-40 + b1),
+                   t2 = tau5 / (1.0e-40 + b2);
+      n0 = lw0 * (1.0 + t0 * t0);
+      n1 = lw1 * (1.0 + t1 * t1);
+      n2 = lw2 * (1.0 + t2 * t2);
+    } else {
+      n0 = lw0 / ((1.0e-6 + b0) * (1.0e-6 + b0));
+      n1 = lw1 / ((1.0e-6 + b1) * (1.0e-6 + b1));
+      n2 = lw2 / ((1.0e-6 + b2) * (1.0e-6 + b2));
+    }
+    const double sum = n0 + n1 + n2;
+    n0 /= sum;
+    n1 /= sum;
+    n2 /= sum;
+    out[v] = n0 * st0 + n1 * st1 + n2 * st2;
+  }
+}
+
+/* ---------------------------------------------------------- AUSMPW+ flux */
+/* AUSMFlux (include/inviscidFlux.hpp:396) and inviscidFlux::AUSMFlux
+ * (:162), Sign (include/utility.hpp:126) */
+static double sign_of(double x) { return (double)((0.0 < x) - (x < 0.0)); }
+static void ausm_flux(const double *L, const double *R, const gas_t *g, const double *n,
+                      double *f) {
+  const double vnL = L[1] * n[0] + L[2] * n[1] + L[3] * n[2];
+  const double vnR = R[1] * n[0] + R[2] * n[1] + R[3] * n[2];
+  const double sosL = sos_of(L, g), sosR = sos_of(R, g);
+  const double sosStar = sqrt(sosL * sosR);
+  const double vel = 0.5 * (vnL + vnR);
+  double sos = sosStar;
+  if (vel < 0.0) {
+    sos = sosStar * sosStar / ((vnR < sosStar) ? sosStar : vnR);
+  } else if (vel > 0.0) {
+    sos = sosStar * sosStar / ((vnL < sosStar) ? sosStar : vnL);
+  }
+  const double ml = vnL / sos, mr = vnR / sos;
+  const double mPlusL = fabs(ml) <= 1.0 ? 0.25 * pow(ml + 1.0, 2.0) : 0.5 * (ml + fabs(ml));
+  const double mMinusR = fabs(mr) <= 1.0 ? -0.25 * pow(mr - 1.0, 2.0) : 0.5 * (mr - fabs(mr));
+  const double pPlus = fabs(ml) <= 1.0 ? 0.25 * pow(ml + 1.0, 2.0) * (2.0 - ml)
+                                       : 0.5 * (1.0 + sign_of(ml));
+  const double pMinus = fabs(mr) <= 1.0 ? 0.25 * pow(mr - 1.0, 2.0) * (2.0 + mr)
+                                        : 0.5 * (1.0 - sign_of(mr));
+  const double ps = pPlus * L[4] + pMinus * R[4];
+  const double ra = L[4] / R[4], rb = R[4] / L[4];
+  const double w = 1.0 - pow((rb < ra) ? rb : ra, 3.0);
+  const double fl = fabs(ml) < 1.0 ? L[4] / ps - 1.0 : 0.0;
+  const double fr = fabs(mr) < 1.0 ? R[4] / ps - 1.0 : 0.0;
+  const double mavg = mPlusL + mMinusR;
+  const double mPlusLBar = mavg >= 0.0 ? mPlusL + mMinusR * ((1.0 - w) * (1.0 + fr) - fl)
+                                       : mPlusL * w * (1.0 + fl);
+  const double mMinusRBar = mavg >= 0.0 ? mMinusR * w * (1.0 + fr)
+                                        : mMinusR + mPlusL * ((1.0 - w) * (1.0 + fl) - fr);
+  const double vl = mPlusLBar * sos;
+  f[0] = L[0] * vl;
+  f[1] = L[0] * vl * L[1] + pPlus * L[4] * n[0];
+  f[2] = L[0] * vl * L[2] + pPlus * L[4] * n[1];
+  f[3] = L[0] * vl * L[3] + pPlus * L[4] * n[2];
+  f[4] = L[0] * vl * enthalpy_of(L, g);
+  const double vr = mMinusRBar * sos;
+  f[0] += R[0] * vr;
+  f[1] += R[0] * vr * R[1] + pMinus * R[4] * n[0];
+  f[2] += R[0] * vr * R[2] + pMinus * R[4] * n[1];
+  f[3] += R[0] * vr * R[3] + pMinus * R[4] * n[2];
+  f[4] += R[0] * vr * enthalpy_of(R, g);
+}
+
 /* ------------------------------------------------------ spectral radius */
 /* InvCellSpectralRadius (include/spectralRadius.hpp:44) */
 static double inv_cell_specrad(const double *w, const gas_t *g, const double *lo,
@@ -282,6 +434,7 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
   c->ns = nsolves;
   c->b = (oblock *)calloc(nblocks, sizeof(oblock));
   c->s = (osolve *)calloc(nsolves, sizeof(osolve));
+  c->mres = (double *)calloc(nsolves, sizeof(double));
   for (int s = 0; s < nsolves; ++s) {
     c->s[s].v = sv[s];
     c->s[s].states = (ath_bc_state *)dup_arr(sv[s].states, sizeof(ath_bc_state) * sv[s].nstates);
@@ -332,10 +485,15 @@ void orc_destroy(orc_case *c) {
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
   free(c->s);
+  free(c->mres);
   free(c);
 }
 
 void orc_set_threads(orc_case *c, int n) { c->nthreads = n; }
+void orc_set_matrix_resid(orc_case *c, int on) { c->matrix_resid = on; }
+double orc_matrix_resid(const orc_case *c, int solve) {
+  return (solve >= 0 && solve < c->ns) ? c->mres[solve] : 0.0;
+}
 
 #ifdef _OPENMP
 #define PAR_BLOCKS _Pragma("omp parallel for schedule(dynamic, 1) num_threads(nth)")
@@ -459,15 +617,33 @@ void orc_residual(orc_case *c) {
             const int fpos = d == 0 ? i : (d == 1 ? j : k);
             const int64_t cu = cell_idx(b, i, j, k); /* upper cell of the face */
             const int64_t cl = cu - st;
-            const double *wm2 = &b->W[(cl - st) * NV], *wm1 = &b->W[cl * NV],
-                         *w0 = &b->W[cu * NV], *wp1 = &b->W[(cu + st) * NV];
+            const double *wm1 = &b->W[cl * NV], *w0 = &b->W[cu * NV];
             double fL[NV], fR[NV], f[NV], n[3], mag;
-            muscl(wm2, wm1, w0, sv->v.kappa, sv->v.limiter, wd[cl - st], wd[cl],
-                  wd[cu], fL);
-            muscl(wp1, w0, wm1, sv->v.kappa, sv->v.limiter, wd[cu + st], wd[cu],
-                  wd[cl], fR);
+            const int recon = sv->v.recon;
+            if (recon == ATH_RECON_CONSTANT) {
+              memcpy(fL, wm1, sizeof(fL));
+              memcpy(fR, w0, sizeof(fR));
+            } else if (recon == ATH_RECON_MUSCL) {
+              const double *wm2 = &b->W[(cl - st) * NV], *wp1 = &b->W[(cu + st) * NV];
+              muscl(wm2, wm1, w0, sv->v.kappa, sv->v.limiter, wd[cl - st], wd[cl],
+                    wd[cu], fL);
+              muscl(wp1, w0, wm1, sv->v.kappa, sv->v.limiter, wd[cu + st], wd[cu],
+                    wd[cl], fR);
+            } else {
+              const double *wm3 = &b->W[(cl - 2 * st) * NV], *wm2 = &b->W[(cl - st) * NV],
+                           *wp1 = &b->W[(cu + st) * NV], *wp2 = &b->W[(cu + 2 * st) * NV];
+              const double *cl5[5] = {wm3, wm2, wm1, w0, wp1};
+              const double wl5[5] = {wd[cl - 2 * st], wd[cl - st], wd[cl], wd[cu], wd[cu + st]};
+              const double *cu5[5] = {wp2, wp1, w0, wm1, wm2};
+              const double wu5[5] = {wd[cu + 2 * st], wd[cu + st], wd[cu], wd[cl], wd[cl - st]};
+              weno(cl5, wl5, recon == ATH_RECON_WENOZ, fL);
+              weno(cu5, wu5, recon == ATH_RECON_WENOZ, fR);
+            }
             face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
-            roe_flux(fL, fR, g, n, f);
+            if (sv->v.flux == ATH_FLUX_AUSM)
+              ausm_flux(fL, fR, g, n, f);
+            else
+              roe_flux(fL, fR, g, n, f);
             if (fpos > 0)
               for (int v = 0; v < NV; ++v) b->R[cl * NV + v] += f[v] * mag;
             if (fpos < nd) {
@@ -557,6 +733,39 @@ static void swap_du(orc_case *c) {
   }
 }
 
+/* linearSolver::Residual / AXmB (src/linearSolver.cpp:58,92) and the L2 of
+ * mgSolution::CycleAtLevel (src/mgSolution.cpp:196-206) with the second
+ * normalisation of src/main.cpp:271: sqrt(sum(r^2)/padded_size/(cells*nv)),
+ * r = f - (A x - (L x - U x) - b), f = 0 on the finest level. */
+static void matrix_residual(orc_case *c) {
+  for (int s = 0; s < c->ns; ++s) {
+    double sum = 0.0, padded = 0.0, cells = 0.0;
+    for (int bi = 0; bi < c->nb; ++bi) {
+      oblock *b = &c->b[bi];
+      if (b->solve != s) continue;
+      const double thetaInv = 1.0 / c->s[s].v.theta;
+      for (int k = 0; k < b->nk; ++k)
+        for (int j = 0; j < b->nj; ++j)
+          for (int i = 0; i < b->ni; ++i) {
+            const int64_t x = cell_idx(b, i, j, k);
+            double L[NV], U[NV];
+            offdiag_sum(c, b, x, 1, L);
+            offdiag_sum(c, b, x, 0, U);
+            for (int v = 0; v < NV; ++v) {
+              const double off = L[v] - U[v];
+              const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+              const double axmb = b->dU[x * NV + v] * b->A[x] - off - bb;
+              const double r = 0.0 - axmb;
+              sum += r * r;
+            }
+          }
+      padded += (double)b->nc * NV;
+      cells += (double)b->ni * b->nj * b->nk;
+    }
+    c->mres[s] = sqrt((sum / padded) / (cells * NV));
+  }
+}
+
 /* lusgs::Relax with one sweep and no initialisation (src/linearSolver.cpp:
  * 430, LUSGS_Forward :341, LUSGS_Backward :385) */
 void orc_relax(orc_case *c) {
@@ -594,6 +803,7 @@ void orc_relax(orc_case *c) {
     }
   }
   swap_du(c);
+  if (c->matrix_resid) matrix_residual(c);
 }
 
 /* procBlock::UpdateBlock / ImplicitTimeAdvance (src/procBlock.cpp:826,902)

@@ -31,6 +31,11 @@ void orc_destroy(orc_case *c);
 /* Number of OpenMP threads used across blocks (0 = library default). */
 void orc_set_threads(orc_case *c, int nthreads);
 
+/* Also compute the logged matrix residual in orc_relax (the reference
+ * always does, src/linearSolver.cpp:470); read it with orc_matrix_resid. */
+void orc_set_matrix_resid(orc_case *c, int on);
+double orc_matrix_resid(const orc_case *c, int solve);
+
 /* Stages of one nonlinear iteration, in order. */
 void orc_fill_ghosts(orc_case *c);
 void orc_residual(orc_case *c);

@@ -39,6 +39,9 @@ def lib():
         L.orc_iterate.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_get_field.restype = C.c_int
         L.orc_get_field.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.orc_set_matrix_resid.argtypes = [vp, C.c_int]
+        L.orc_matrix_resid.restype = C.c_double
+        L.orc_matrix_resid.argtypes = [vp, C.c_int]
         L.orc_set_state.restype = C.c_int
         L.orc_set_state.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         _lib = L
@@ -52,7 +55,7 @@ def _dp(a):
 class Oracle:
     """CPU oracle instance built from an aither_gb300 Setup."""
 
-    def __init__(self, setup, threads: int = 0):
+    def __init__(self, setup, threads: int = 0, matrix_resid: bool = False):
         from aither_gb300._lib import BlockView, SolveView
         self.setup = setup
         self.nsolves, self.nblocks, self.ncells = setup.counts()
@@ -61,6 +64,8 @@ class Oracle:
         self.h = lib().orc_create(self.nblocks, bv, self.nsolves, sv)
         if threads:
             lib().orc_set_threads(self.h, threads)
+        if matrix_resid:
+            lib().orc_set_matrix_resid(self.h, 1)
 
     def close(self):
         if self.h:
@@ -75,9 +80,13 @@ class Oracle:
 
     def iterate(self, n: int = 1) -> np.ndarray:
         l2 = np.zeros(n * self.nsolves * 5)
-        rc = lib().orc_iterate(self.h, n, _dp(l2))
-        if rc:
-            raise RuntimeError(f"oracle reported status {rc}")
+        self.mres = np.zeros((n, self.nsolves))
+        for it in range(n):
+            rc = lib().orc_iterate(self.h, 1, _dp(l2[it * self.nsolves * 5:]))
+            if rc:
+                raise RuntimeError(f"oracle reported status {rc}")
+            for s in range(self.nsolves):
+                self.mres[it, s] = lib().orc_matrix_resid(self.h, s)
         return l2.reshape(n, self.nsolves, 5)
 
     def stage(self, name: str):

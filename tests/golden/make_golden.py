@@ -37,6 +37,17 @@ CASES = [
     ("bump24", cases.bump_channel, dict(ni=24, nj=12, nk=4, height=0.08, mach=0.7), [1, 30], True),
     ("bump_sup", cases.bump_channel, dict(ni=20, nj=10, nk=3, height=0.10, mach=0.85), [1, 40], True),
     ("vortex_c1", cases.vortex_box, dict(), [200], False),
+    ("bump_weno", cases.bump_channel,
+     dict(ni=20, nj=10, nk=4, height=0.1, mach=0.8, recon="weno", limiter="none"), [1, 20], True),
+    ("bump_wenoz_ausm", cases.bump_channel,
+     dict(ni=18, nj=9, nk=4, height=0.07, mach=0.6, recon="wenoZ", limiter="none", flux="ausm"),
+     [1, 20], True),
+    ("bump_const_ausm", cases.bump_channel,
+     dict(ni=16, nj=8, nk=3, height=0.05, mach=0.5, recon="constant", limiter="none",
+          flux="ausm"), [1, 20], True),
+    ("bump_vanalbada_ausm", cases.bump_channel,
+     dict(ni=22, nj=11, nk=3, height=0.09, mach=0.75, limiter="vanAlbada", flux="ausm"),
+     [1, 20], True),
 ]
 
 
@@ -52,9 +63,10 @@ def run_case(name, gen, kw, niter, full, ref_dir):
         if r.returncode != 0:
             raise RuntimeError(f"reference harness failed on {name}: {r.stderr[-2000:]}")
         R = read_dump(os.path.join(d, "out.bin"))
-    ng = 2
+    ng = (R["b0_state"].shape[0] - R["b0_resid"].shape[0]) // 2
     state = R["b0_state"][ng:-ng, ng:-ng, ng:-ng]
-    out = {"l2": R["l2"], "kwargs": np.array(repr(kw)), "iterations": np.array(niter)}
+    out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "kwargs": np.array(repr(kw)),
+           "iterations": np.array(niter)}
     if full:
         out.update(state0=R["b0_state0"], state=state, resid=R["b0_resid"], dt=R["b0_dt"],
                    specrad=R["b0_specrad"], du=R["b0_du"])

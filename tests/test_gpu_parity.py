@@ -39,7 +39,10 @@ def _l2(norms, nsolves=1, solve=0):
 
 
 @pytest.mark.parametrize("name", ["vortex16_it1", "vortex16_it20", "bump24_it1",
-                                  "bump24_it30", "bump_sup_it1", "bump_sup_it40"])
+                                  "bump24_it30", "bump_sup_it1", "bump_sup_it40",
+                                  "bump_weno_it1", "bump_weno_it20", "bump_wenoz_ausm_it1",
+                                  "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
+                                  "bump_vanalbada_ausm_it20"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
@@ -52,6 +55,23 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     assert rel_err(b.field(0, "DU"), g["du"]) <= CELL_TOL
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
     assert all(x.status == 0 for x in norms)
+    b.close()
+
+
+@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40"])
+def test_fp64_matrix_residual(ctx, name, tmp_path):
+    """flags bit 0: the logged matrix residual of every iteration; it is a
+    log-only quantity, so the solution is unchanged."""
+    from aither_gb300 import Batch, Setup
+    inp, st, g = golden_case(name, str(tmp_path))
+    s = Setup(inp)
+    if st is not None:
+        s.set_state(0, st[0])
+    b = Batch(ctx, s, 0, flags=1)
+    norms = b.iterate(int(g["iterations"]))
+    mres = np.array([n.matrix_resid for n in norms])
+    assert rel_err(mres, g["matrix_resid"]) <= NORM_TOL
+    assert rel_err(b.field(0, "STATE"), g["state"]) <= CELL_TOL
     b.close()
 
 

@@ -15,7 +15,9 @@ from conftest import REF_HARNESS, REF_SRC, golden_case, rel_err
 TOL = 1e-13
 
 FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
-        "bump_sup_it1", "bump_sup_it40"]
+        "bump_sup_it1", "bump_sup_it40", "bump_weno_it1", "bump_weno_it20",
+        "bump_wenoz_ausm_it1", "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
+        "bump_vanalbada_ausm_it20"]
 
 
 def _oracle(inp, st):
@@ -39,6 +41,20 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
     assert rel_err(o.field(0, "SPECRAD")[..., 0], g["specrad"][..., 0]) <= TOL
     assert rel_err(o.field(0, "DU"), g["du"]) <= TOL
     assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
+
+
+@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40"])
+def test_oracle_matrix_residual(name, tmp_path):
+    """The logged linear-system residual (linearSolver::Residual)."""
+    from aither_gb300 import Setup
+    from pyoracle import Oracle
+    inp, st, g = golden_case(name, str(tmp_path))
+    s = Setup(inp)
+    if st is not None:
+        s.set_state(0, st[0])
+    o = Oracle(s, matrix_resid=True)
+    o.iterate(int(g["iterations"]))
+    assert rel_err(o.mres[:, 0], g["matrix_resid"]) <= TOL
 
 
 def test_oracle_full_vortex_box_200_iterations(tmp_path):
