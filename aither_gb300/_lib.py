@@ -52,6 +52,7 @@ class SolveView(C.Structure):
                 ("t_ref", C.c_double),
                 ("r_ref", C.c_double), ("a_ref", C.c_double), ("l_ref", C.c_double),
                 ("visc_scale", C.c_double), ("visc_cfl_coeff", C.c_double),
+                ("k_c1", C.c_double), ("k_s", C.c_double), ("k_ref", C.c_double),
                 ("nstates", C.c_int32), ("states", C.POINTER(BCState))]
 
 
@@ -65,6 +66,9 @@ class BlockView(C.Structure):
                 ("wall_dist", C.POINTER(C.c_double)),
                 ("state0", C.POINTER(C.c_double)),
                 ("nops", C.c_int32), ("ops", C.POINTER(GhostOp)),
+                ("nedge_ops", C.c_int32), ("edge_ops", C.POINTER(GhostOp)),
+                ("nvops", C.c_int32), ("vops", C.POINTER(GhostOp)),
+                ("nvedge_ops", C.c_int32), ("vedge_ops", C.POINTER(GhostOp)),
                 ("nplanes", C.c_int32), ("plane_offsets", C.POINTER(C.c_int32)),
                 ("plane_cells", C.POINTER(C.c_int32)),
                 ("nbr_mask", C.POINTER(C.c_uint8))]

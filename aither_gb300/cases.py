@@ -246,3 +246,62 @@ def bump_batch_specs(n: int = 64, seed: int = 2024, lo=(32, 32, 32), hi=(96, 64,
         m = float(rng.uniform(0.3, 0.85))
         specs.append((ni, nj, nk, h, m))
     return specs
+
+
+def sutherland_mu(t: float, c1: float = 1.458e-6, s: float = 110.4) -> float:
+    return c1 * t ** 1.5 / (t + s)
+
+
+def plate_nodes(x0: float, x1: float, ni: int, nj: int, nk: int, dy0: float, ratio: float,
+                dz: float) -> np.ndarray:
+    """Block on [x0, x1] in x, geometric wall-normal spacing from y=0."""
+    x = x0 + (x1 - x0) * np.arange(ni + 1) / ni
+    dy = dy0 * ratio ** np.arange(nj)
+    y = np.concatenate([[0.0], np.cumsum(dy)])
+    z = dz * np.arange(nk + 1)
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    return np.stack([X, Y, Z])
+
+
+def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float = 1e-5,
+               ratio: float = 1.08, length: float = 1.0, mach: float = 0.3,
+               reynolds: float = 1e5, t_inf: float = 288.0, cfl: float = 100.0,
+               wall_t: float | None = None, limiter: str = "vanAlbada",
+               name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder"):
+    """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
+    interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
+    or isothermal at wall_t), characteristic far field on the other sides of
+    the x-y plane, slip walls in z.  Freestream density from Re_L with
+    Sutherland's law at t_inf."""
+    os.makedirs(outdir, exist_ok=True)
+    dz = 0.02 * length
+    b0 = plate_nodes(0.0, 0.5 * length, ni, nj, nk, dy0, ratio, dz)
+    b1 = plate_nodes(0.5 * length, length, ni, nj, nk, dy0, ratio, dz)
+    write_plot3d(os.path.join(outdir, name + ".xyz"), [b0, b1])
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    u_inf = mach * a_inf
+    rho_inf = reynolds * sutherland_mu(t_inf) / (u_inf * length)
+    p_inf = rho_inf * R_AIR * t_inf
+    refs = Refs(t_ref=t_inf, r_ref=rho_inf)
+    vel = f"[{_fmt(u_inf)}, 0, 0]"
+    ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel})"
+    wall = "viscousWall(tag=2)" if wall_t is None else f"viscousWall(tag=2; temperature={_fmt(wall_t)})"
+    states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
+              f"velocity={vel})", wall]
+    blk0 = [("characteristic", 0, 0, 0, nj, 0, nk, 1),
+            ("interblock", ni, ni, 0, nj, 0, nk, 1001),
+            ("viscousWall", 0, ni, 0, 0, 0, nk, 2),
+            ("characteristic", 0, ni, nj, nj, 0, nk, 1),
+            ("slipWall", 0, ni, 0, nj, 0, 0, 4),
+            ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
+    blk1 = [("interblock", 0, 0, 0, nj, 0, nk, 2000),
+            ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+            ("viscousWall", 0, ni, 0, 0, 0, nk, 2),
+            ("characteristic", 0, ni, nj, nj, 0, nk, 1),
+            ("slipWall", 0, ni, 0, nj, 0, 0, 4),
+            ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
+    inp = os.path.join(outdir, name + ".inp")
+    write_input(inp, name, {"cfl": cfl, "limiter": limiter, "equationSet": "navierStokes",
+                            "matrixSolver": matrix_solver, "faceReconstruction": recon},
+                refs, ic, states, [blk0, blk1])
+    return inp, None

@@ -82,6 +82,14 @@ struct Lists {
   std::vector<int32_t> nbq;       // [6][nq]
   std::vector<double> face_lo, face_hi;  // [3][4][nq]
   std::vector<int32_t> ghost_cell, ghost_src;
+  std::vector<double> dist_lo, dist_hi;  // [3][nq]
+  // block-edge ghosts, viscous-wall ghosts: ops grouped by phase
+  std::vector<GhostOpDev> edge_ops, vops, vedge_ops;
+  std::vector<int32_t> edge_solve, vop_solve, vedge_solve;
+  std::vector<int32_t> edge_phase_off, vedge_phase_off;
+  // cells whose laminar viscosity is needed (viscous blocks, all but corners)
+  std::vector<int32_t> aux_cells, aux_block;
+  bool any_viscous = false;
 };
 
 }  // namespace
@@ -107,6 +115,9 @@ struct BatchCore {
   int2 *d_sweep = nullptr;
   int32_t *d_solve_cta0 = nullptr;
   GhostOpDev *d_ops = nullptr, *d_conn_ops = nullptr;
+  GhostOpDev *d_edge_ops = nullptr, *d_vops = nullptr, *d_vedge_ops = nullptr;
+  int32_t *d_edge_solve = nullptr, *d_vop_solve = nullptr, *d_vedge_solve = nullptr;
+  int32_t *d_aux_cells = nullptr, *d_aux_block = nullptr;
   int32_t *d_op_solve = nullptr;
   NormPartial *d_partials = nullptr;
   double *d_mres = nullptr;
@@ -212,6 +223,14 @@ class Runner : public RunnerBase {
     P_.W = m.Alloc<double>(5 * n);
     P_.R = m.Alloc<double>(5 * n);
     for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<T>(5 * n);
+    if (c.L.any_viscous) {
+      for (int d = 0; d < 3; ++d) {
+        P_.vflux[d] = m.Alloc<T>(5 * n);
+        Check(cudaMemset(P_.vflux[d], 0, 5 * n * sizeof(T)), "memset");
+      }
+      P_.mu = m.Alloc<double>(n);
+      Check(cudaMemset(P_.mu, 0, n * sizeof(double)), "memset");
+    }
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
     Check(cudaMemset(P_.R, 0, 5 * n * sizeof(double)), "memset");
@@ -240,6 +259,13 @@ class Runner : public RunnerBase {
       P_.face_hi = m.Upload(hi);
     }
     P_.nbq = m.Upload(c.L.nbq);
+    {
+      std::vector<T> dl(c.L.dist_lo.begin(), c.L.dist_lo.end());
+      std::vector<T> dh(c.L.dist_hi.begin(), c.L.dist_hi.end());
+      P_.dist_lo = m.Upload(dl);
+      P_.dist_hi = m.Upload(dh);
+    }
+    P_.muq = m.Alloc<T>(c.L.any_viscous ? nq : 1);
     P_.qpos = m.Upload(c.L.qpos);
     P_.ghost_cell = m.Upload(c.L.ghost_cell);
     P_.ghost_src = m.Upload(c.L.ghost_src);
@@ -297,14 +323,30 @@ class Runner : public RunnerBase {
     k_cfl<<<(c_.nsolves + 127) / 128, 128, 0, c_.stream>>>(c_.d_solves, c_.nsolves, c_.d_iter,
                                                             c_.d_cfl);
   }
+  void EdgePhases(const GhostOpDev *ops, const int32_t *solve,
+                  const std::vector<int32_t> &off) {
+    for (size_t ph = 0; ph + 1 < off.size(); ++ph)
+      Launch<T>::Ghost(P_, ops + off[ph], off[ph + 1] - off[ph], solve + off[ph], c_.stream);
+  }
   void FillGhosts() override {
     StartIteration();
     Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
+    EdgePhases(c_.d_edge_ops, c_.d_edge_solve, c_.L.edge_phase_off);
+  }
+  void Viscous() {
+    if (!c_.L.any_viscous) return;
+    Launch<T>::Ghost(P_, c_.d_vops, (int)c_.L.vops.size(), c_.d_vop_solve, c_.stream);
+    EdgePhases(c_.d_vedge_ops, c_.d_vedge_solve, c_.L.vedge_phase_off);
+    Launch<T>::Aux(P_, c_.d_aux_cells, c_.d_aux_block, (int)c_.L.aux_cells.size(), c_.stream);
+    for (int d = 0; d < 3; ++d)
+      Launch<T>::ViscFace(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
+                          (int)c_.L.face_cta_block[d].size(), c_.stream);
   }
   void Residual() override {
     for (int d = 0; d < 3; ++d)
       Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
                       (int)c_.L.face_cta_block[d].size(), c_.stream);
+    Viscous();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                     c_.stream);
   }
@@ -369,6 +411,7 @@ class Runner : public RunnerBase {
                         (int)c_.L.face_cta_block[d].size(), c_.stream);
         Check(cudaEventRecord(e[2 + d], c_.stream), "event");
       }
+      Viscous();
       Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                       c_.stream);
       Check(cudaEventRecord(e[5], c_.stream), "event");
@@ -535,6 +578,8 @@ void BuildLists(BatchCore &c) {
   L.nbq.assign(6 * nq, -1);
   L.face_lo.assign(12 * nq, 0.0);
   L.face_hi.assign(12 * nq, 0.0);
+  L.dist_lo.assign(3 * nq, 1.0);
+  L.dist_hi.assign(3 * nq, 1.0);
   for (int b = 0; b < c.nblocks; ++b) {
     const Block &bk = st.blocks[b];
     const int64_t st3[3] = {1, (int64_t)bk.NI, (int64_t)bk.NI * bk.NJ};
@@ -568,6 +613,16 @@ void BuildLists(BatchCore &c) {
           auto &dst = up ? L.face_hi : L.face_lo;
           for (int comp = 0; comp < 4; ++comp)
             dst[(int64_t)(d * 4 + comp) * nq + q] = bk.farea[d][comp * nf + f];
+          // ProjC2CDist (src/procBlock.cpp:6316): centre above the face
+          // minus centre below, along the face's unit normal
+          const int64_t above = up ? nbl : cl, below = up ? cl : nbl;
+          const int64_t ncb = bk.NCell();
+          double dc[3];
+          for (int comp = 0; comp < 3; ++comp)
+            dc[comp] = bk.center[comp * ncb + above] - bk.center[comp * ncb + below];
+          (up ? L.dist_hi : L.dist_lo)[(int64_t)d * nq + q] =
+              dc[0] * bk.farea[d][f] + dc[1] * bk.farea[d][nf + f] +
+              dc[2] * bk.farea[d][2 * nf + f];
         }
       }
     }
@@ -611,6 +666,68 @@ void BuildLists(BatchCore &c) {
       if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK) L.conn_ops.push_back(g);
     }
   }
+  // block-edge and viscous-wall ghost ops, pool indices, grouped by phase
+  auto convert = [&](int b, const ath_ghost_op &op) {
+    const Block &bk = st.blocks[b];
+    GhostOpDev g{};
+    g.dst = (int32_t)(c.cell0[b] + op.dst);
+    g.src = (int32_t)(c.cell0[op.src_block] + op.src);
+    g.src2 = op.src2 >= 0 ? (int32_t)(c.cell0[b] + op.src2) : -1;
+    g.type = op.type;
+    g.lower = op.lower;
+    g.dir = op.dir;
+    g.state = op.state;
+    g.layer = op.layer;
+    const int d = op.dir;
+    const int fi = bk.NI + (d == 0), fj = bk.NJ + (d == 1);
+    const int ii = (int)(op.face % fi);
+    const int64_t r = op.face / fi;
+    const int jj = (int)(r % fj), kk = (int)(r / fj);
+    g.face = (ii < bk.NI && jj < bk.NJ && kk < bk.NK)
+                 ? (int32_t)(c.cell0[b] + ii + (int64_t)bk.NI * (jj + (int64_t)bk.NJ * kk))
+                 : -1;
+    return g;
+  };
+  int max_phase = 0;
+  for (auto &bk : st.blocks) max_phase = std::max(max_phase, bk.ng * bk.ng);
+  L.edge_phase_off.assign(max_phase + 1, 0);
+  L.vedge_phase_off.assign(max_phase + 1, 0);
+  for (int ph = 0; ph < max_phase; ++ph) {
+    L.edge_phase_off[ph] = (int32_t)L.edge_ops.size();
+    L.vedge_phase_off[ph] = (int32_t)L.vedge_ops.size();
+    for (int b = 0; b < c.nblocks; ++b) {
+      const Block &bk = st.blocks[b];
+      for (const auto &op : bk.edge_ops)
+        if (op.layer == ph) {
+          L.edge_ops.push_back(convert(b, op));
+          L.edge_solve.push_back(bk.solve);
+        }
+      for (const auto &op : bk.vedge_ops)
+        if (op.layer == ph) {
+          L.vedge_ops.push_back(convert(b, op));
+          L.vedge_solve.push_back(bk.solve);
+        }
+    }
+  }
+  L.edge_phase_off[max_phase] = (int32_t)L.edge_ops.size();
+  L.vedge_phase_off[max_phase] = (int32_t)L.vedge_ops.size();
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &bk = st.blocks[b];
+    for (const auto &op : bk.vops) {
+      L.vops.push_back(convert(b, op));
+      L.vop_solve.push_back(bk.solve);
+    }
+    if (st.solves[bk.solve].phys.eqn == ATH_EQN_EULER) continue;
+    L.any_viscous = true;
+    for (int k = -bk.ng; k < bk.nk + bk.ng; ++k)
+      for (int j = -bk.ng; j < bk.nj + bk.ng; ++j)
+        for (int i = -bk.ng; i < bk.ni + bk.ng; ++i) {
+          const bool gi = i < 0 || i >= bk.ni, gj = j < 0 || j >= bk.nj, gk = k < 0 || k >= bk.nk;
+          if (gi && gj && gk) continue;  // corner cells are never used
+          L.aux_cells.push_back((int32_t)(c.cell0[b] + bk.Cell(i, j, k)));
+          L.aux_block.push_back(b);
+        }
+  }
 }
 
 void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags) {
@@ -651,6 +768,16 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.limiter = p.limiter;
     x.recon = p.recon;
     x.flux = p.flux;
+    x.viscous = p.eqn != ATH_EQN_EULER;
+    x.visc_scale = p.visc_scale;
+    x.mu_c1 = p.mu_c1;
+    x.mu_s = p.mu_s;
+    x.mu_ref = p.mu_ref;
+    x.t_ref = p.t_ref;
+    x.k_c1 = p.k_c1;
+    x.k_s = p.k_s;
+    x.k_ref = p.k_ref;
+    x.visc_coeff = p.visc_cfl_coeff;
     x.padded_values = 0.0;
     x.cells = 0.0;
     for (int b : st.solves[s].blocks) {
@@ -680,6 +807,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_ops = m.Upload(c.L.ops);
   c.d_conn_ops = m.Upload(c.L.conn_ops);
   c.d_op_solve = m.Upload(c.L.op_solve);
+  c.d_edge_ops = m.Upload(c.L.edge_ops);
+  c.d_edge_solve = m.Upload(c.L.edge_solve);
+  c.d_vops = m.Upload(c.L.vops);
+  c.d_vop_solve = m.Upload(c.L.vop_solve);
+  c.d_vedge_ops = m.Upload(c.L.vedge_ops);
+  c.d_vedge_solve = m.Upload(c.L.vedge_solve);
+  c.d_aux_cells = m.Upload(c.L.aux_cells);
+  c.d_aux_block = m.Upload(c.L.aux_block);
   c.d_partials = m.Alloc<NormPartial>(c.L.cell_cta_block.size());
   c.d_mres = m.Alloc<double>(c.L.cell_cta_block.size());
   c.d_ring = m.Alloc<NormOut>((size_t)c.ring_cap * c.nsolves);
@@ -705,7 +840,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   }
   // launches of one iteration: cfl, ghost, 3 faces, cell, 2 x steps of
   // sweeps, dU connection copy, update, norms, counter
-  c.launches_per_iter = 1 + (c.L.ops.empty() ? 0 : 1) + 3 + 1 + 2 * c.nsteps +
+  int edge_phases = 0, vedge_phases = 0;
+  for (size_t ph = 0; ph + 1 < c.L.edge_phase_off.size(); ++ph) {
+    edge_phases += c.L.edge_phase_off[ph + 1] > c.L.edge_phase_off[ph];
+    vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
+  }
+  c.launches_per_iter = edge_phases +
+                        (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 : 0) +
+                        1 + (c.L.ops.empty() ? 0 : 1) + 3 + 1 + 2 * c.nsteps +
                         (c.L.ghost_cell.empty() ? 0 : 1) + 3 +
                         ((flags & 1) ? 1 + (c.L.ghost_cell.empty() ? 0 : 1) : 0);
 }

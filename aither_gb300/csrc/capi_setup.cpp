@@ -90,6 +90,12 @@ int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out) {
     out->state0 = b.state0.data();
     out->nops = (int32_t)b.ops.size();
     out->ops = b.ops.data();
+    out->nedge_ops = (int32_t)b.edge_ops.size();
+    out->edge_ops = b.edge_ops.data();
+    out->nvops = (int32_t)b.vops.size();
+    out->vops = b.vops.data();
+    out->nvedge_ops = (int32_t)b.vedge_ops.size();
+    out->vedge_ops = b.vedge_ops.data();
     out->nplanes = (int32_t)b.plane_offsets.size() - 1;
     out->plane_offsets = b.plane_offsets.data();
     out->plane_cells = b.plane_cells.data();

@@ -32,6 +32,9 @@ struct SolveDev {
   double kappa, theta, zeta, relax, cfl_start, cfl_step, cfl_max;
   double padded_values;  // sum over blocks of padded cells x nv
   double cells;          // physical cells of the solve
+  // laminar transport (Sutherland), nondimensional
+  double visc_scale, mu_c1, mu_s, mu_ref, t_ref, k_c1, k_s, k_ref, visc_coeff;
+  int32_t viscous, pad3;
   int32_t limiter, nstates, state0, recon;
   int32_t flux, pad0, pad1, pad2;
 };
@@ -40,6 +43,7 @@ struct SolveDev {
 struct GhostOpDev {
   int32_t dst, src, type, lower;
   int32_t face, dir, state, layer;
+  int32_t src2, pad;
 };
 
 // Partial norms of one CTA of the update kernel.
@@ -66,6 +70,8 @@ struct Pools {
   double *W;        // [5][ncell] primitive state, FP64
   double *R;        // [5][ncell] residual, FP64
   T *flux[3];       // [5][ncell] F.|A| on faces of direction d
+  T *vflux[3];      // [5][ncell] viscous F.|A| (viscous solves)
+  double *mu;       // [ncell] laminar viscosity (viscous solves)
   double *lam;      // [ncell] cell spectral radius
   double *dt;       // [ncell]
   const double *vol;       // [ncell]
@@ -77,6 +83,9 @@ struct Pools {
   T *Rq;            // [5][nq]
   T *Ainvq;         // [nq] inverse of the scalar main diagonal
   T *Aq;            // [nq] the scalar main diagonal (matrix residual)
+  T *muq;           // [nq] laminar viscosity, q order
+  const T *dist_lo; // [3][nq] centre-to-centre distance along the lower face normal
+  const T *dist_hi; // [3][nq] same for the upper face
   T *dUq;           // [5][nq] implicit update
   const T *face_lo; // [3 dirs][4][nq] lower face of each direction
   const T *face_hi; // [3 dirs][4][nq] upper face
@@ -183,6 +192,11 @@ template <typename T>
 struct Launch {
   static void Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
                     const int32_t *op_solve, cudaStream_t s);
+  // laminar viscosity of the listed cells (UpdateAuxillaryVariables)
+  static void Aux(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block,
+                  int n, cudaStream_t s);
+  static void ViscFace(int d, const Pools<T> &P, const int32_t *list,
+                       const int32_t *cta_block, int ncta, cudaStream_t s);
   static void Face(int d, const Pools<T> &P, const int32_t *list,
                    const int32_t *cta_block, int ncta, cudaStream_t s);
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

@@ -33,8 +33,39 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
   const int64_t n = P.ncell;
   Prim<double> in = LoadW<double>(P.W, n, op.src);
   Prim<double> g = in;
-  if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK) {
-    // plain copy of the partner's interior cell
+  if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK || op.type == ATH_EDGE_COPY) {
+    // plain copy of the partner's interior cell / of the adjacent ghost
+  } else if (op.type == ATH_EDGE_AVG) {
+    const Prim<double> o = LoadW<double>(P.W, n, op.src2);
+    g.rho = 0.5 * (in.rho + o.rho);
+    g.u = 0.5 * (in.u + o.u);
+    g.v = 0.5 * (in.v + o.v);
+    g.w = 0.5 * (in.w + o.w);
+    g.p = 0.5 * (in.p + o.p);
+  } else if (op.type == ATH_EDGE_SLIP) {
+    // slip-wall reflection of the adjacent ghost across a ghost-layer face
+    const double *fa = P.fa[op.dir];
+    const double sgn = op.lower ? -1.0 : 1.0;
+    const double nx = sgn * fa[op.face], ny = sgn * fa[n + op.face],
+                 nz = sgn * fa[2 * n + op.face];
+    const double vn = Dot(in.u, in.v, in.w, nx, ny, nz);
+    g.u = in.u - 2.0 * nx * vn;
+    g.v = in.v - 2.0 * ny * vn;
+    g.w = in.w - 2.0 * nz * vn;
+  } else if (op.type == ATH_BC_VISCOUS_WALL) {
+    // viscousWall, low-Re treatment (src/ghostStates.cpp:130-200): velocity
+    // 2 u_wall - u; isothermal walls set the density from 2 T_wall - T
+    const SolveDev sv = P.solves[op_solve[t]];
+    const ath_bc_state bs = P.states[sv.state0 + op.state];
+    g.u = 2.0 * bs.wall_u - in.u;
+    g.v = 2.0 * bs.wall_v - in.v;
+    g.w = 2.0 * bs.wall_w - in.w;
+    if (bs.isothermal) {
+      const Gas<double> gas = GasOf<double>(sv);
+      const double tGhost = 2.0 * bs.wall_t - Temperature(in, gas);
+      const double rho = g.p / ((0.0 + 1.0 * gas.r) * tGhost);
+      g.rho = rho * (in.rho / in.rho);
+    }
   } else {
     const SolveDev sv = P.solves[op_solve[t]];
     const Gas<double> gas = GasOf<double>(sv);
@@ -178,7 +209,8 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   const int64_t n = P.ncell;
   const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
   // R = 0 - Fi(lo) + Fi(hi) - Fj(lo) + Fj(hi) - Fk(lo) + Fk(hi), each face
-  // term rounded in this order (src/procBlock.cpp:447-463)
+  // term rounded in this order (src/procBlock.cpp:447-463); viscous faces
+  // follow with + Fv(lo) - Fv(hi) per direction (:1392-1429)
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     double r = 0.0;
@@ -187,6 +219,14 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       const T *F = P.flux[d] + v * n;
       r = r - (double)F[c];
       r = r + (double)F[c + st[d]];
+    }
+    if (sv.viscous) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const T *F = P.vflux[d] + v * n;
+        r = r + (double)F[c];
+        r = r - (double)F[c + st[d]];
+      }
     }
     P.R[v * n + c] = r;
   }
@@ -202,15 +242,31 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                                        (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u],
                                        (T)fa[2 * n + u], (T)fa[3 * n + u]);
   }
-  P.lam[c] = lam;
-  // local time step and diagonal: A = lam*relax + V(1+zeta)/(dt theta)
-  const double cfl = P.cfl[b.solve];
+  double adiag = lam;  // scalar main diagonal accumulates like the radius
   const double vol = P.vol[c];
+  const int64_t q = P.qpos[c];
+  if (sv.viscous) {
+    // viscous cell spectral radii (ViscCellSpectralRadius): the time-step
+    // radius takes them times the viscous CFL coefficient, the diagonal
+    // twice (CalcViscFluxI/J/K)
+    const T mu = (T)P.mu[c];
+    const T vt = ViscMaxTerm(w, g) * ViscTerm(mu, (T)sv.visc_scale, g);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const T fMag = T(0.5) * ((T)P.fa[d][3 * n + c] + (T)P.fa[d][3 * n + c + st[d]]);
+      const T lv = vt * fMag * fMag / (T)vol;
+      lam = lam + (double)(lv * (T)sv.visc_coeff);
+      adiag = adiag + (double)(T(2) * lv);
+    }
+    P.muq[q] = mu;
+  }
+  P.lam[c] = lam;
+  // local time step and diagonal: A = A*relax + V(1+zeta)/(dt theta)
+  const double cfl = P.cfl[b.solve];
   const double dt = cfl * (vol / lam);
   P.dt[c] = dt;
-  const double a = lam * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+  const double a = adiag * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
   // hyperplane-ordered copies for the sweeps
-  const int64_t q = P.qpos[c];
   const int64_t nq = P.nq;
   P.Ainvq[q] = (T)(1.0 / a);
   P.Aq[q] = (T)a;
@@ -228,10 +284,12 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
 // (procBlock::ImplicitLower) or upper neighbours with the negative sign
 // (ImplicitUpper), accumulated i, j, k from zero.
 template <typename T>
-__device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g, int64_t q,
-                                           bool lower, T acc[5]) {
+__device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
+                                           const SolveDev &sv, int64_t q, bool lower,
+                                           T acc[5]) {
   const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
   const T *face = lower ? P.face_lo : P.face_hi;
+  const T *dist = lower ? P.dist_lo : P.dist_hi;
   const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
@@ -241,6 +299,7 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g, i
     if (nb == -1) continue;
     Prim<T> s;
     T du[5];
+    T mu = T(0);
     if (nb >= 0) {
       s.rho = P.Wq[nb];
       s.u = P.Wq[nq + nb];
@@ -249,15 +308,23 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g, i
       s.p = P.Wq[4 * nq + nb];
 #pragma unroll
       for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
+      if (sv.viscous) mu = P.muq[nb];
     } else {
       const int64_t slot = -(int64_t)nb - 2;
       s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
 #pragma unroll
       for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
+      if (sv.viscous) mu = (T)P.mu[P.ghost_cell[slot]];
     }
     const T *f = face + (int64_t)d * 4 * nq;
+    const T mag = f[3 * nq + q];
+    // ViscFaceSpectralRadius (include/spectralRadius.hpp:126) across this
+    // face, ProjC2CDist as the length
+    const T vsr = sv.viscous ? mag / dist[d * nq + q] * ViscMaxTerm(s, g) *
+                                   ViscTerm(mu, (T)sv.visc_scale, g)
+                             : T(0);
     T o[5];
-    ScalarOffDiag(s, du, g, f[q], f[nq + q], f[2 * nq + q], f[3 * nq + q], lower, o);
+    ScalarOffDiag(s, du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, o);
 #pragma unroll
     for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
   }
@@ -277,7 +344,7 @@ __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, in
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   T acc[5];
-  OffDiagSum(P, g, q, forward != 0, acc);
+  OffDiagSum(P, g, sv, q, forward != 0, acc);
   const T ainv = P.Ainvq[q];
   if (forward) {
     const T thetaInv = (T)(1.0 / sv.theta);
@@ -397,6 +464,143 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
 }
 
 // ---------------------------------------------------------------------------
+// laminar viscosity of every listed cell (UpdateAuxillaryVariables,
+// src/procBlock.cpp:6171); temperature is recomputed from W where needed
+template <typename T>
+__global__ void k_aux(Pools<T> P, const int32_t *cells, const int32_t *cell_block, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int64_t c = cells[t];
+  const SolveDev sv = P.solves[P.blocks[cell_block[t]].solve];
+  const Gas<double> g = GasOf<double>(sv);
+  const Prim<double> w = LoadW<double>(P.W, P.ncell, c);
+  P.mu[c] = SutherlandRatio(Temperature(w, g), sv.t_ref, sv.mu_c1, sv.mu_s, sv.mu_ref);
+}
+
+// viscous flux on faces of direction D (procBlock::CalcViscFluxI/J/K,
+// src/procBlock.cpp:1233,1556,1879): Green-Gauss gradients on the dual
+// cell around the face (CalcGradsI/J/K :5173-5955, VectorGradGG/ScalarGradGG
+// src/utility.cpp:59,138), central face state and viscosity, laminar
+// viscousFlux::CalcFlux (src/viscousFlux.cpp:58) with TauNormal
+// (src/utility.cpp:426)
+template <typename T, int D>
+__global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
+                                                const int32_t *cta_block) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const SolveDev sv = P.solves[b.solve];
+  if (!sv.viscous) return;
+  const Gas<T> g = GasOf<T>(sv);
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  const Prim<T> Wl = LoadW<T>(P.W, n, cl), Wu = LoadW<T>(P.W, n, cu);
+  const T Tl = Temperature(Wl, g), Tu = Temperature(Wu, g);
+  auto area = [&](int e, int64_t x, T a[3]) {
+    const double *fa = P.fa[e];
+    const T m = (T)fa[3 * n + x];
+    a[0] = (T)fa[x] * m;
+    a[1] = (T)fa[n + x] * m;
+    a[2] = (T)fa[2 * n + x] * m;
+  };
+  T vlo[3][3], vhi[3][3], tlo[3], thi[3], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e == D) {
+      vlo[e][0] = Wl.u; vlo[e][1] = Wl.v; vlo[e][2] = Wl.w;
+      vhi[e][0] = Wu.u; vhi[e][1] = Wu.v; vhi[e][2] = Wu.w;
+      tlo[e] = Tl;
+      thi[e] = Tu;
+      T A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = T(0.5) * (A0[r] + A1[r]);
+        alo[e][r] = T(0.5) * (A0[r] + A2[r]);
+      }
+    } else {
+      const Prim<T> Wup = LoadW<T>(P.W, n, cu + st[e]), Wlp = LoadW<T>(P.W, n, cl + st[e]);
+      const Prim<T> Wum = LoadW<T>(P.W, n, cu - st[e]), Wlm = LoadW<T>(P.W, n, cl - st[e]);
+      vhi[e][0] = T(0.25) * (((Wl.u + Wu.u) + Wup.u) + Wlp.u);
+      vhi[e][1] = T(0.25) * (((Wl.v + Wu.v) + Wup.v) + Wlp.v);
+      vhi[e][2] = T(0.25) * (((Wl.w + Wu.w) + Wup.w) + Wlp.w);
+      vlo[e][0] = T(0.25) * (((Wl.u + Wu.u) + Wum.u) + Wlm.u);
+      vlo[e][1] = T(0.25) * (((Wl.v + Wu.v) + Wum.v) + Wlm.v);
+      vlo[e][2] = T(0.25) * (((Wl.w + Wu.w) + Wum.w) + Wlm.w);
+      thi[e] = T(0.25) * (((Tl + Tu) + Temperature(Wup, g)) + Temperature(Wlp, g));
+      tlo[e] = T(0.25) * (((Tl + Tu) + Temperature(Wum, g)) + Temperature(Wlm, g));
+      T Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = T(0.5) * (Aup[r] + Alp[r]);
+        alo[e][r] = T(0.5) * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const T vol = T(0.5) * ((T)P.vol[cl] + (T)P.vol[cu]);
+  const T invVol = T(1) / vol;
+  T grad[3][3], tg[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int qv = 0; qv < 3; ++qv) {
+      grad[r][qv] = vhi[0][qv] * ahi[0][r] - vlo[0][qv] * alo[0][r] +
+                    vhi[1][qv] * ahi[1][r] - vlo[1][qv] * alo[1][r] +
+                    vhi[2][qv] * ahi[2][r] - vlo[2][qv] * alo[2][r];
+      grad[r][qv] *= invVol;
+    }
+    tg[r] = thi[0] * ahi[0][r] - tlo[0] * alo[0][r] + thi[1] * ahi[1][r] -
+            tlo[1] * alo[1][r] + thi[2] * ahi[2][r] - tlo[2] * alo[2][r];
+    tg[r] *= invVol;
+  }
+  // central face state and viscosity
+  const double *wd = P.width[D];
+  T cd, cw;
+  CentralCoeffs((T)wd[cl], (T)wd[cu], cd, cw);
+  Prim<T> fs;
+  fs.rho = cd * Wu.rho + cw * Wl.rho;
+  fs.u = cd * Wu.u + cw * Wl.u;
+  fs.v = cd * Wu.v + cw * Wl.v;
+  fs.w = cd * Wu.w + cw * Wl.w;
+  fs.p = cd * Wu.p + cw * Wl.p;
+  const T muf = cd * (T)P.mu[cu] + cw * (T)P.mu[cl];
+  const double *fa = P.fa[D];
+  const T nx = (T)fa[c], ny = (T)fa[n + c], nz = (T)fa[2 * n + c], mag = (T)fa[3 * n + c];
+  const T nrm[3] = {nx, ny, nz};
+  const T scale = (T)sv.visc_scale;
+  const T mus = scale * muf, muts = scale * T(0);
+  const T lambda = T(0) - (T(2) / T(3)) * (mus + muts);
+  const T trace = grad[0][0] + grad[1][1] + grad[2][2];
+  T tau[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const T sn = (grad[r][0] + grad[0][r]) * nrm[0] + (grad[r][1] + grad[1][r]) * nrm[1] +
+                 (grad[r][2] + grad[2][r]) * nrm[2];
+    tau[r] = lambda * trace * nrm[r] + (mus + muts) * sn;
+  }
+  const T tf = Temperature(fs, g);
+  const T kf = SutherlandRatio(tf, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref) * scale;
+  const T kt = muts * g.Cp() / T(0.9);
+  T F[5];
+  F[0] = T(0);
+  F[1] = tau[0];
+  F[2] = tau[1];
+  F[3] = tau[2];
+  F[4] = Dot(tau[0], tau[1], tau[2], fs.u, fs.v, fs.w) +
+         (kf + kt) * Dot(tg[0], tg[1], tg[2], nx, ny, nz) + T(0);
+  T *out = P.vflux[D];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v * n + c] = F[v] * mag;
+}
+
+// ---------------------------------------------------------------------------
 // logged matrix residual
 template <typename T>
 __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list,
@@ -411,8 +615,8 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
     const Gas<T> g = GasOf<T>(sv);
     const int64_t q = P.qpos[c], nq = P.nq;
     T L[5], U[5];
-    OffDiagSum(P, g, q, true, L);
-    OffDiagSum(P, g, q, false, U);
+    OffDiagSum(P, g, sv, q, true, L);
+    OffDiagSum(P, g, sv, q, false, U);
     const T thetaInv = (T)(1.0 / sv.theta);
     const T a = P.Aq[q];
 #pragma unroll
@@ -445,6 +649,19 @@ template <typename T>
 void Launch<T>::Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
                       const int32_t *op_solve, cudaStream_t s) {
   if (nops > 0) k_ghost<T><<<(nops + 127) / 128, 128, 0, s>>>(P, ops, nops, op_solve);
+}
+template <typename T>
+void Launch<T>::Aux(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block,
+                    int n, cudaStream_t s) {
+  if (n > 0) k_aux<T><<<(n + 127) / 128, 128, 0, s>>>(P, cells, cell_block, n);
+}
+template <typename T>
+void Launch<T>::ViscFace(int d, const Pools<T> &P, const int32_t *list,
+                         const int32_t *cta_block, int ncta, cudaStream_t s) {
+  if (ncta <= 0) return;
+  if (d == 0) k_vface<T, 0><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  else if (d == 1) k_vface<T, 1><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  else k_vface<T, 2><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
 void Launch<T>::Face(int d, const Pools<T> &P, const int32_t *list,

@@ -436,6 +436,45 @@ __device__ __forceinline__ void AusmFlux(const Prim<T> &L, const Prim<T> &R, con
   f[4] += R.rho * vr * Enthalpy(R, g);
 }
 
+// ---------------------------------------------------------------------------
+// laminar viscous terms
+
+// thermodynamic::Prandtl (include/thermodynamic.hpp:61)
+template <typename T>
+__device__ __forceinline__ T Prandtl(const Gas<T> &g) {
+  const T gamma = g.Gamma();
+  return (T(4) * gamma) / (T(9) * gamma - T(5));
+}
+// max(4/(3 rho), gamma/rho) of ViscCell/ViscFaceSpectralRadius
+// (include/spectralRadius.hpp:94,126)
+template <typename T>
+__device__ __forceinline__ T ViscMaxTerm(const Prim<T> &s, const Gas<T> &g) {
+  const T a = T(4) / (T(3) * s.rho), b = g.Gamma() / s.rho;
+  return (a < b) ? b : a;
+}
+// NondimScaling * (mu/Pr + mut/Prt), laminar (mut = 0, Prt = 0.9)
+template <typename T>
+__device__ __forceinline__ T ViscTerm(T mu, T scale, const Gas<T> &g) {
+  return scale * (mu / Prandtl(g) + T(0) / T(0.9));
+}
+// sutherland::SpeciesViscosity / SpeciesConductivity (src/transport.cpp:100,108)
+template <typename T>
+__device__ __forceinline__ T SutherlandRatio(T t, T tref, T c1, T s, T ref) {
+  const T temp = t * tref;
+  const T v = (c1 * pow(temp, T(1.5))) / (temp + s);
+  return v / ref;
+}
+// FaceReconCentral (include/reconstruction.hpp:315) weights of the upper
+// (downwind) and lower (upwind) cell: LagrangeCoeff of a 2-cell stencil
+template <typename T>
+__device__ __forceinline__ void CentralCoeffs(T wl, T wu, T &cdown, T &cup) {
+  const T w[5] = {wl, wu, T(0), T(0), T(0)};
+  T c[2];
+  LagrangeCoeff<T, 1>(w, 0, 0, c);
+  cdown = c[0];
+  cup = c[1];
+}
+
 // InvCellSpectralRadius (include/spectralRadius.hpp:44)
 template <typename T>
 __device__ __forceinline__ T InvCellSpecRad(const Prim<T> &s, const Gas<T> &g,
@@ -462,13 +501,14 @@ __device__ __forceinline__ T InvFaceSpecRad(const Prim<T> &s, const Gas<T> &g,
 template <typename T>
 __device__ __forceinline__ void ScalarOffDiag(const Prim<T> &s, const T du[5],
                                               const Gas<T> &g, T nx, T ny, T nz,
-                                              T mag, bool positive, T out[5]) {
+                                              T mag, bool positive, T visc_sr, T out[5]) {
   const Prim<T> su = UpdateWithCons(s, g, du);
   T fo[5], fn[5];
   InvFlux(s, g, nx, ny, nz, fo);
   InvFlux(su, g, nx, ny, nz, fn);
   const T half = T(0.5) * mag;
-  const T lam = InvFaceSpecRad(s, g, nx, ny, nz, mag);
+  T lam = InvFaceSpecRad(s, g, nx, ny, nz, mag);
+  lam += visc_sr;  // FaceSpectralRadius (include/spectralRadius.hpp:182)
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     const T fc = half * (fn[v] - fo[v]);

@@ -389,8 +389,9 @@ void BuildGhostGeometry(Block &b) {
           const auto gid = b.Cell(G[0], G[1], G[2]);
           const auto iid = b.Cell(I[0], I[1], I[2]);
           b.vol[gid] = b.vol[iid];
-          // face areas: the ghost's outward face mirrors the interior
-          // cell's face on the far side; the other faces copy straight over
+          // face areas: the ghost's outward face takes the interior cell's
+          // face on the same side (lower: face g <- face ic; upper: face
+          // g+1 <- face ic+1); the other faces copy straight over
           for (int fd = 0; fd < 3; ++fd) {
             const int64_t nf = b.NFace(fd);
             auto copy_face = [&](std::array<int, 3> to, std::array<int, 3> from) {
@@ -400,8 +401,10 @@ void BuildGhostGeometry(Block &b) {
             };
             if (fd == d) {
               auto to = G, from = I;
-              if (lower) { from[d] = ic + 1; }   // far face of the interior
-              else { to[d] = g + 1; }            // far face of the ghost
+              if (!lower) {
+                to[d] = g + 1;
+                from[d] = ic + 1;
+              }
               copy_face(to, from);
             } else {
               copy_face(G, I);
@@ -601,6 +604,32 @@ void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const int m[2][3],
         const int dir_of_a2 = (m[0][2] != 0) ? B.d1 : B.d2;
         ba.width[A.d1 * ncA + op.dst] = wB(dir_of_a1);
         ba.width[A.d2 * ncA + op.dst] = wB(dir_of_a2);
+        // face areas of the ghost from the donor (procBlock::PutGeomSlice):
+        // per A direction, the matching B direction and whether increasing
+        // index runs the same way; a reversed axis swaps the ghost's low and
+        // high faces and flips the unit normal
+        const int bdir[3] = {B.d, dir_of_a1, dir_of_a2};
+        const int sgn_d = (A.lower ? -1 : 1) * (B.lower ? 1 : -1);
+        const int sgn1 = m[0][1] != 0 ? m[0][1] : m[1][1];
+        const int sgn2 = m[0][2] != 0 ? m[0][2] : m[1][2];
+        const int sgn[3] = {sgn_d, sgn1, sgn2};
+        const int adir[3] = {A.d, A.d1, A.d2};
+        for (int q = 0; q < 3; ++q) {
+          const int ea = adir[q], eb = bdir[q];
+          const int64_t nfa = ba.NFace(ea), nfb = bb.NFace(eb);
+          for (int side = 0; side < 2; ++side) {
+            auto gf = G;
+            gf[ea] += side;
+            auto sf = S;
+            sf[eb] += (sgn[q] > 0) ? side : 1 - side;
+            const int64_t ta = ba.Face(ea, gf[0], gf[1], gf[2]);
+            const int64_t fb = bb.Face(eb, sf[0], sf[1], sf[2]);
+            const double flip = sgn[q] > 0 ? 1.0 : -1.0;
+            for (int comp = 0; comp < 3; ++comp)
+              ba.farea[ea][comp * nfa + ta] = flip * bb.farea[eb][comp * nfb + fb];
+            ba.farea[ea][3 * nfa + ta] = bb.farea[eb][3 * nfb + fb];
+          }
+        }
       }
   }
 }
@@ -619,6 +648,7 @@ void BuildGhostOps(Setup &st, int solve) {
   for (int bi : sv.blocks) {
     Block &b = st.blocks[bi];
     b.ops.clear();
+    b.vops.clear();
     for (size_t si = 0; si < b.surfs.size(); ++si) {
       const auto &s = b.surfs[si];
       const int d = s.Dir();
@@ -654,6 +684,10 @@ void BuildGhostOps(Setup &st, int solve) {
         }
         const bool reflect =
             s.type == ATH_BC_SLIP_WALL || s.type == ATH_BC_VISCOUS_WALL;
+        // inviscid ghosts treat a viscous wall as a slip wall
+        // (AssignInviscidGhostCells); the viscous-wall state is applied
+        // before the viscous fluxes (AssignViscousGhostCells)
+        const int inv_type = s.type == ATH_BC_VISCOUS_WALL ? ATH_BC_SLIP_WALL : s.type;
         for (int b2 = p.lo2; b2 < p.hi2; ++b2)
           for (int b1 = p.lo1; b1 < p.hi1; ++b1) {
             const auto G = Ijk(d, g, d1, b1, d2, b2);
@@ -663,7 +697,7 @@ void BuildGhostOps(Setup &st, int solve) {
             op.dst = b.Cell(G[0], G[1], G[2]);
             op.src = b.Cell(I[0], I[1], I[2]);
             op.src_block = bi;
-            op.type = s.type;
+            op.type = inv_type;
             op.layer = layer;
             op.dir = d;
             op.lower = s.Lower() ? 1 : 0;
@@ -671,6 +705,10 @@ void BuildGhostOps(Setup &st, int solve) {
             op.face = b.Face(d, F[0], F[1], F[2]);
             op.src2 = -1;
             b.ops.push_back(op);
+            if (s.type == ATH_BC_VISCOUS_WALL) {
+              op.type = ATH_BC_VISCOUS_WALL;
+              b.vops.push_back(op);
+            }
           }
       }
     }
@@ -688,6 +726,14 @@ void BuildGhostOps(Setup &st, int solve) {
       const Patch &B = conns[c];
       const Surface &sb = st.blocks[B.block].surfs[B.surf];
       if (sa.type != sb.type) continue;
+      if (sa.type == ATH_BC_INTERBLOCK) {
+        // interblock tag = partner surface * 1000 + partner block
+        // (boundarySurface::PartnerBlock/PartnerSurface)
+        const auto &blks = sv.blocks;
+        const int pb = sa.tag % 1000, ps = sa.tag / 1000;
+        if (pb < 0 || pb >= (int)blks.size() || blks[pb] != B.block || ps != sb.SurfaceId())
+          continue;
+      }
       V3 shift{0, 0, 0};
       if (sa.type == ATH_BC_PERIODIC) {
         const BCStateIn *ps = nullptr;
@@ -749,6 +795,144 @@ void BuildGhostOps(Setup &st, int solve) {
           }
           b.nbr_mask[b.Cell(i, j, k)] = m;
         }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// block-edge ghost cells
+namespace {
+
+// boundary surface of id surf (1..6) holding the face at cell indices
+// (i, j, k), the index along the surface normal being the face index
+// (boundaryConditions::GetBCSurface)
+const Surface &SurfaceAt(const Block &b, int i, int j, int k, int surf) {
+  for (const auto &s : b.surfs) {
+    if (s.SurfaceId() != surf) continue;
+    const int d = s.Dir();
+    const int c[3] = {i, j, k};
+    int lo, hi;
+    SurfRange(s, d, lo, hi);
+    if (c[d] != lo) continue;
+    bool inside = true;
+    for (int e = 0; e < 3 && inside; ++e) {
+      if (e == d) continue;
+      SurfRange(s, e, lo, hi);
+      if (c[e] < lo || c[e] >= hi) inside = false;
+    }
+    if (inside) return s;
+  }
+  Fail("no boundary surface covers a block edge");
+}
+
+}  // namespace
+
+// procBlock::AssignInviscidGhostCellsEdge (src/procBlock.cpp:2565) and
+// AssignViscousGhostCellsEdge (:2840): for each of the 12 block edges, each
+// pair of ghost layers and each cell along the edge, one op; phases
+// (layer3-1)*ng + layer2-1 run in order, cells inside a phase are
+// independent.
+void BuildEdgeOps(Setup &st, int solve) {
+  const bool viscous = st.solves[solve].phys.eqn != ATH_EQN_EULER;
+  for (int bi : st.solves[solve].blocks) {
+    Block &b = st.blocks[bi];
+    b.edge_ops.clear();
+    b.vedge_ops.clear();
+    const int n[3] = {b.ni, b.nj, b.nk};
+    for (int dd = 0; dd < 3; ++dd) {
+      const int a2 = (dd + 1) % 3, a3 = (dd + 2) % 3;  // j,k for i; k,i for j; i,j for k
+      const int max1 = n[dd], max2 = n[a2], max3 = n[a3];
+      const int surfStart2 = 2 * a2 + 1, surfStart3 = 2 * a3 + 1;
+      auto ijk = [&](int d1, int x2, int x3) {
+        std::array<int, 3> c{};
+        c[dd] = d1;
+        c[a2] = x2;
+        c[a3] = x3;
+        return c;
+      };
+      for (int layer3 = 1; layer3 <= b.ng; ++layer3)
+        for (int layer2 = 1; layer2 <= b.ng; ++layer2)
+          for (int cc = 0; cc < 4; ++cc) {
+            const bool upper2 = cc > 1, upper3 = cc % 2 == 1;
+            const int pCellD2 = upper2 ? max2 + layer2 - 2 : 1 - layer2;
+            const int gCellD2 = upper2 ? pCellD2 + 1 : pCellD2 - 1;
+            const int pCellD3 = upper3 ? max3 + layer3 - 2 : 1 - layer3;
+            const int gCellD3 = upper3 ? pCellD3 + 1 : pCellD3 - 1;
+            const int surf2 = upper2 ? surfStart2 + 1 : surfStart2;
+            const int surf3 = upper3 ? surfStart3 + 1 : surfStart3;
+            const int cFaceD2_2 = upper2 ? max2 : 0;
+            const int cFaceD2_3 = upper3 ? max3 - 1 : 0;
+            const int cFaceD3_2 = upper2 ? max2 - 1 : 0;
+            const int cFaceD3_3 = upper3 ? max3 : 0;
+            const int phase = (layer3 - 1) * b.ng + (layer2 - 1);
+            for (int d1 = 0; d1 < max1; ++d1) {
+              const auto s2c = ijk(d1, cFaceD2_2, cFaceD2_3);
+              const auto s3c = ijk(d1, cFaceD3_2, cFaceD3_3);
+              const Surface &bs2 = SurfaceAt(b, s2c[0], s2c[1], s2c[2], surf2);
+              const Surface &bs3 = SurfaceAt(b, s3c[0], s3c[1], s3c[2], surf3);
+              const auto dst = ijk(d1, gCellD2, gCellD3);
+              const auto from2 = ijk(d1, pCellD2, gCellD3);
+              const auto from3 = ijk(d1, gCellD2, pCellD3);
+              const auto f2 = ijk(d1, cFaceD2_2, gCellD3);  // face along a2
+              const auto f3 = ijk(d1, gCellD2, cFaceD3_3);  // face along a3
+              ath_ghost_op op{};
+              op.dst = b.Cell(dst[0], dst[1], dst[2]);
+              op.src_block = bi;
+              op.layer = phase;
+              op.state = -1;
+              op.src2 = -1;
+              auto slip2 = [&]() {
+                op.type = ATH_EDGE_SLIP;
+                op.src = b.Cell(from2[0], from2[1], from2[2]);
+                op.dir = a2;
+                op.face = b.Face(a2, f2[0], f2[1], f2[2]);
+                op.lower = surf2 % 2 == 1;
+              };
+              auto slip3 = [&]() {
+                op.type = ATH_EDGE_SLIP;
+                op.src = b.Cell(from3[0], from3[1], from3[2]);
+                op.dir = a3;
+                op.face = b.Face(a3, f3[0], f3[1], f3[2]);
+                op.lower = surf3 % 2 == 1;
+              };
+              auto average = [&]() {
+                if (layer2 == layer3) {
+                  op.type = ATH_EDGE_AVG;
+                  op.src = b.Cell(from2[0], from2[1], from2[2]);
+                  op.src2 = b.Cell(from3[0], from3[1], from3[2]);
+                } else if (layer2 > layer3) {
+                  op.type = ATH_EDGE_COPY;
+                  op.src = b.Cell(from3[0], from3[1], from3[2]);
+                } else {
+                  op.type = ATH_EDGE_COPY;
+                  op.src = b.Cell(from2[0], from2[1], from2[2]);
+                }
+              };
+              // inviscid: viscous walls count as slip walls
+              {
+                const bool w2 = bs2.type == ATH_BC_SLIP_WALL || bs2.type == ATH_BC_VISCOUS_WALL;
+                const bool w3 = bs3.type == ATH_BC_SLIP_WALL || bs3.type == ATH_BC_VISCOUS_WALL;
+                if (w2 && !w3) slip2();
+                else if (!w2 && w3) slip3();
+                else average();
+                b.edge_ops.push_back(op);
+              }
+              if (viscous) {
+                op.src2 = -1;
+                const bool s2 = bs2.type == ATH_BC_SLIP_WALL, s3 = bs3.type == ATH_BC_SLIP_WALL;
+                const bool v2 = bs2.type == ATH_BC_VISCOUS_WALL, v3 = bs3.type == ATH_BC_VISCOUS_WALL;
+                bool add = true;
+                if (s2 && !s3) slip2();
+                else if (!s2 && s3) slip3();
+                else if (v2 && v3) average();
+                else add = false;
+                if (add) b.vedge_ops.push_back(op);
+              }
+            }
+          }
+    }
+    auto by_phase = [](const ath_ghost_op &x, const ath_ghost_op &y) { return x.layer < y.layer; };
+    std::stable_sort(b.edge_ops.begin(), b.edge_ops.end(), by_phase);
+    std::stable_sort(b.vedge_ops.begin(), b.vedge_ops.end(), by_phase);
   }
 }
 
@@ -856,7 +1040,7 @@ void AppendInput(Setup &st, const std::string &path) {
   if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
   if (get("turbulenceModel", "none") != "none" && ph.eqn != ATH_EQN_RANS)
     Fail("turbulence model needs equationSet rans");
-  if (ph.eqn != ATH_EQN_EULER) Fail("only equationSet euler is supported");
+  if (ph.eqn == ATH_EQN_RANS) Fail("equationSet rans is not supported yet");
   ph.turb = ATH_TURB_NONE;
   ph.nv = 5;
   // input::NumberGhostLayers (src/input.cpp:1127): 1 constant, 2 MUSCL, 3 WENO
@@ -891,11 +1075,17 @@ void AppendInput(Setup &st, const std::string &path) {
   ph.gas_hf = hf_nd;
   ph.mu_c1 = fl.mu_c1;
   ph.mu_s = fl.mu_s;
+  ph.k_c1 = fl.k_c1;
+  ph.k_s = fl.k_s;
   ph.t_ref = tref;
+  // sutherland ctor (src/transport.cpp:31): mixture reference viscosity,
+  // conductivity reference, and transport::SetScaling mu/(rho a l)
+  ph.mu_ref = fl.mu_c1 * std::pow(tref, 1.5) / (tref + fl.mu_s);
+  ph.k_ref = (aref * aref * ph.mu_ref) / tref;
   ph.r_ref = rref;
   ph.a_ref = aref;
   ph.l_ref = lref;
-  ph.visc_scale = 1.0;
+  ph.visc_scale = ph.mu_ref / (rref * aref * lref);
   ph.visc_cfl_coeff = ph.kappa == 1.0 ? 4.0 : (ph.kappa == -2.0 ? 2.0 : 1.0);
 
   // boundary states
@@ -950,10 +1140,12 @@ void AppendInput(Setup &st, const std::string &path) {
         s.isothermal = 1;
         s.wall_t = std::stod(m["temperature"]) / tref;
       }
+      if (m.count("heatFlux")) Fail("constant heat-flux walls are not supported");
+      if (m.count("wallTreatment") && m["wallTreatment"] != "lowRe")
+        Fail("wall laws are not supported");
       if (m.count("turbulenceIntensity")) s.turb_intensity = num("turbulenceIntensity", 0);
       if (m.count("eddyViscosityRatio")) s.eddy_visc_ratio = num("eddyViscosityRatio", 0);
-      if (s.type == ATH_BC_STAGNATION_INLET || s.type == ATH_BC_PRESSURE_OUTLET ||
-          s.type == ATH_BC_VISCOUS_WALL)
+      if (s.type == ATH_BC_STAGNATION_INLET || s.type == ATH_BC_PRESSURE_OUTLET)
         Fail("boundary state " + name + " is not supported yet");
     }
     sv.states_in.push_back(si);
@@ -1033,6 +1225,7 @@ void AppendInput(Setup &st, const std::string &path) {
   (void)first;
   st.solves.push_back(std::move(sv));
   BuildGhostOps(st, solve);
+  BuildEdgeOps(st, solve);
   // connection ghost geometry changes the donor-side widths only through
   // the ops; recompute nothing else
 }

@@ -42,7 +42,7 @@ struct Block {
   // padded geometry
   std::vector<double> vol, center, width, fcenter[3], farea[3], wall_dist;
   std::vector<double> state0;  // padded AoS primitive
-  std::vector<ath_ghost_op> ops;
+  std::vector<ath_ghost_op> ops, edge_ops, vops, vedge_ops;
   std::vector<int32_t> plane_offsets, plane_cells;
   std::vector<uint8_t> nbr_mask;
 
@@ -86,6 +86,7 @@ void BuildGhostGeometry(Block &b);
 void BuildCellWidths(Block &b);
 void BuildGhostOps(Setup &setup, int solve);
 void BuildHyperplanes(Block &b);
+void BuildEdgeOps(Setup &setup, int solve);
 
 // Reads the binary multi-block Plot3D grid format.
 std::vector<Block> ReadPlot3d(const std::string &path, double lref);

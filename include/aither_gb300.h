@@ -74,7 +74,13 @@ enum {
   ATH_BC_SUPERSONIC_INFLOW = 5,   /* supersonicInflow */
   ATH_BC_SUPERSONIC_OUTFLOW = 6,  /* supersonicOutflow */
   ATH_BC_PERIODIC = 7,            /* periodic (connection) */
-  ATH_BC_INTERBLOCK = 8           /* interblock (connection) */
+  ATH_BC_INTERBLOCK = 8,          /* interblock (connection) */
+  /* block-edge ghost cells (procBlock::AssignInviscidGhostCellsEdge /
+   * AssignViscousGhostCellsEdge): copy of src, average of src and src2,
+   * or a slip-wall reflection of src across a ghost-layer face */
+  ATH_EDGE_COPY = 20,
+  ATH_EDGE_AVG = 21,
+  ATH_EDGE_SLIP = 22
 };
 
 /* arithmetic of the per-iteration path */
@@ -96,7 +102,7 @@ typedef struct {
   int64_t src;        /* padded cell index of the donor cell */
   int32_t src_block;  /* block of the donor (connections), else own block */
   int32_t type;       /* ATH_BC_* */
-  int32_t layer;      /* 1..ng */
+  int32_t layer;      /* 1..ng; edge ops: phase (layer3-1)*ng + layer2-1 */
   int32_t dir;        /* 0,1,2 = boundary normal direction i,j,k */
   int32_t lower;      /* 1 = lower surface (normal flipped outward) */
   int32_t state;      /* index into the solve's boundary-state table */
@@ -122,10 +128,13 @@ typedef struct {
   int32_t nv, ng, sweeps;
   double kappa, cfl_start, cfl_step, cfl_max, theta, zeta, relax;
   double gas_r, gas_n, gas_hf;          /* calorically perfect, one species */
-  double mu_c1, mu_s, mu_ref, t_ref;    /* Sutherland constants */
+  double mu_c1, mu_s, mu_ref, t_ref;    /* Sutherland viscosity constants,
+                                           mu_ref = mixture reference viscosity */
   double r_ref, a_ref, l_ref;           /* dimensional reference values */
   double visc_scale;                    /* transport NondimScaling */
   double visc_cfl_coeff;                /* input::ViscousCFLCoefficient */
+  double k_c1, k_s, k_ref;              /* Sutherland conductivity constants,
+                                           k_ref = conductivity reference */
   int32_t nstates;
   const ath_bc_state *states;
 } ath_solve_view;
@@ -146,7 +155,13 @@ typedef struct {
   const double *wall_dist;  /* [ncell_padded] */
   const double *state0;     /* initial primitive, padded AoS [cell][nv] */
   int32_t nops;
-  const ath_ghost_op *ops;
+  const ath_ghost_op *ops;          /* boundary states and connections */
+  int32_t nedge_ops;
+  const ath_ghost_op *edge_ops;     /* block-edge ghosts, by phase */
+  int32_t nvops;
+  const ath_ghost_op *vops;         /* viscous-wall ghosts (viscous flux) */
+  int32_t nvedge_ops;
+  const ath_ghost_op *vedge_ops;    /* block-edge ghosts after vops */
   int32_t nplanes;
   const int32_t *plane_offsets; /* [nplanes+1] */
   const int32_t *plane_cells;   /* padded cell index, hyperplane order */

@@ -28,8 +28,13 @@ typedef struct {
   double *dU;          /* [nc][5] */
   double *lam, *dt, *A, *Ainv; /* [nc] */
   uint8_t *mask;
+  double *center;      /* [3][nc] */
+  double *T, *mu;      /* [nc] temperature, laminar viscosity (aux) */
+  uint8_t *corner;     /* [nc] ghost in all three directions */
   int nops;
   ath_ghost_op *ops;
+  int nedge, nvops, nvedge;
+  ath_ghost_op *edge, *vops, *vedge;
   int nplanes;
   int32_t *plane_off, *plane_cells;
 } oblock;
@@ -39,6 +44,7 @@ typedef struct {
   ath_bc_state *states;
   gas_t gas;
   double cfl;
+  int viscous;
 } osolve;
 
 struct orc_case {
@@ -390,13 +396,15 @@ static double inv_cell_specrad(const double *w, const gas_t *g, const double *lo
  * ConvectiveFluxUpdate (include/inviscidFlux.hpp:544) and
  * InvFaceSpectralRadius (include/spectralRadius.hpp:67); inviscid */
 static void scalar_offdiag(const double *w, const double *du, const gas_t *g,
-                           const double *n, double mag, int positive, double *out) {
+                           const double *n, double mag, int positive, double visc_sr,
+                           double *out) {
   double wu[NV], fo[NV], fn[NV];
   update_with_cons(w, g, du, wu);
   inv_flux(w, g, n, fo);
   inv_flux(wu, g, n, fn);
-  const double lam =
+  double lam =
       0.5 * mag * (fabs(w[1] * n[0] + w[2] * n[1] + w[3] * n[2]) + sos_of(w, g));
+  lam += visc_sr; /* FaceSpectralRadius (include/spectralRadius.hpp:182) */
   for (int v = 0; v < NV; ++v) {
     const double fc = 0.5 * mag * (fn[v] - fo[v]);
     out[v] = positive ? fc + lam * du[v] : fc - lam * du[v];
@@ -426,6 +434,219 @@ static void *dup_arr(const void *src, size_t bytes) {
   return p;
 }
 
+/* --------------------------------------------------------- viscous terms */
+/* sutherland (src/transport.cpp:100-195) */
+static double visc_of(double t, const ath_solve_view *v) {
+  const double temp = t * v->t_ref;
+  const double mu = (v->mu_c1 * pow(temp, 1.5)) / (temp + v->mu_s);
+  return mu / v->mu_ref;
+}
+static double cond_eff(double t, const ath_solve_view *v) {
+  const double temp = t * v->t_ref;
+  const double k = (v->k_c1 * pow(temp, 1.5)) / (temp + v->k_s);
+  return (k / v->k_ref) * v->visc_scale;
+}
+/* thermodynamic::Prandtl (include/thermodynamic.hpp:61) */
+static double prandtl_of(const gas_t *g) {
+  const double gamma = gamma_of(g);
+  return (4.0 * gamma) / (9.0 * gamma - 5.0);
+}
+/* ViscCellSpectralRadius / ViscFaceSpectralRadius
+ * (include/spectralRadius.hpp:94,126), laminar (mut = 0, Prt 0.9) */
+static double visc_max_term(const double *w, const gas_t *g) {
+  const double a = 4.0 / (3.0 * w[0]), b = gamma_of(g) / w[0];
+  return (a < b) ? b : a;
+}
+static double visc_term(double mu, const ath_solve_view *v, const gas_t *g) {
+  return v->visc_scale * (mu / prandtl_of(g) + 0.0 / 0.9);
+}
+/* FaceReconCentral (include/reconstruction.hpp:315): coefficients of the
+ * lower (upwind) and upper (downwind) cell */
+static void central_coeffs(double wl, double wu, double *cd, double *cu) {
+  const double w[2] = {wl, wu};
+  double c[2];
+  lagrange_coeff(w, 1, 0, 0, c);
+  *cd = c[0];
+  *cu = c[1];
+}
+static inline void area_vec(const oblock *b, int d, int64_t f, double *a) {
+  double n[3], m;
+  face_normal(b, d, f, n, &m);
+  a[0] = n[0] * m;
+  a[1] = n[1] * m;
+  a[2] = n[2] * m;
+}
+
+/* GetGhostState for viscousWall, low-Re treatment
+ * (src/ghostStates.cpp:130-200, 243-266) */
+static void viscous_wall_ghost(const double *in, const ath_bc_state *bs, const gas_t *g,
+                               double *out) {
+  memcpy(out, in, 8 * NV);
+  out[1] = 2.0 * bs->wall_u - in[1];
+  out[2] = 2.0 * bs->wall_v - in[2];
+  out[3] = 2.0 * bs->wall_w - in[3];
+  if (bs->isothermal) {
+    const double tGhost = 2.0 * bs->wall_t - temp_of(in, g);
+    const double rho = out[4] / ((0.0 + 1.0 * g->r) * tGhost);
+    out[0] = rho * (in[0] / in[0]);
+  }
+}
+
+/* edge ghost cells (procBlock::AssignInviscidGhostCellsEdge /
+ * AssignViscousGhostCellsEdge) */
+static void apply_edge_ops(oblock *b, int n, const ath_ghost_op *ops) {
+  for (int o = 0; o < n; ++o) {
+    const ath_ghost_op *op = &ops[o];
+    double g[NV];
+    const double *a = &b->W[op->src * NV];
+    if (op->type == ATH_EDGE_COPY) {
+      memcpy(g, a, sizeof(g));
+    } else if (op->type == ATH_EDGE_AVG) {
+      const double *c2 = &b->W[op->src2 * NV];
+      for (int v = 0; v < NV; ++v) g[v] = 0.5 * (a[v] + c2[v]);
+    } else {
+      double nrm[3], mag;
+      face_normal(b, op->dir, op->face, nrm, &mag);
+      if (op->lower) {
+        nrm[0] = -1.0 * nrm[0];
+        nrm[1] = -1.0 * nrm[1];
+        nrm[2] = -1.0 * nrm[2];
+      }
+      memcpy(g, a, sizeof(g));
+      const double vn = a[1] * nrm[0] + a[2] * nrm[1] + a[3] * nrm[2];
+      g[1] = a[1] - 2.0 * nrm[0] * vn;
+      g[2] = a[2] - 2.0 * nrm[1] * vn;
+      g[3] = a[3] - 2.0 * nrm[2] * vn;
+    }
+    memcpy(&b->W[op->dst * NV], g, sizeof(g));
+  }
+}
+
+/* procBlock::CalcViscFluxI/J/K (src/procBlock.cpp:1233,1556,1879) with
+ * CalcGradsI/J/K (:5173,5378,5584), VectorGradGG/ScalarGradGG
+ * (src/utility.cpp:59,138), viscousFlux::CalcFlux (src/viscousFlux.cpp:58),
+ * TauNormal (src/utility.cpp:426); laminar */
+static void viscous_fluxes(orc_case *c, oblock *b) {
+  const osolve *sv = &c->s[b->solve];
+  const ath_solve_view *v = &sv->v;
+  const gas_t *g = &sv->gas;
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  const double coeff = v->visc_cfl_coeff;
+  for (int d = 0; d < 3; ++d) {
+    const int ei = b->ni + (d == 0), ej = b->nj + (d == 1), ek = b->nk + (d == 2);
+    const int nd = d == 0 ? b->ni : (d == 1 ? b->nj : b->nk);
+    const double *wd = &b->width[d * b->nc];
+    for (int k = 0; k < ek; ++k)
+      for (int j = 0; j < ej; ++j)
+        for (int i = 0; i < ei; ++i) {
+          const int fpos = d == 0 ? i : (d == 1 ? j : k);
+          const int64_t cu = cell_idx(b, i, j, k), cl = cu - st[d];
+          /* dual-cell face values and area vectors, axes i, j, k */
+          double vlo[3][3], vhi[3][3], tlo[3], thi[3], alo[3][3], ahi[3][3];
+          for (int e = 0; e < 3; ++e) {
+            const double *Wl = &b->W[cl * NV], *Wu = &b->W[cu * NV];
+            if (e == d) {
+              for (int q = 0; q < 3; ++q) {
+                vlo[e][q] = Wl[1 + q];
+                vhi[e][q] = Wu[1 + q];
+              }
+              tlo[e] = b->T[cl];
+              thi[e] = b->T[cu];
+              double A0[3], A1[3], A2[3];
+              area_vec(b, d, face_idx(b, d, i, j, k), A0);
+              area_vec(b, d, face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), A1);
+              area_vec(b, d, face_idx(b, d, i - (d == 0), j - (d == 1), k - (d == 2)), A2);
+              for (int q = 0; q < 3; ++q) {
+                ahi[e][q] = 0.5 * (A0[q] + A1[q]);
+                alo[e][q] = 0.5 * (A0[q] + A2[q]);
+              }
+            } else {
+              const int64_t cup = cu + st[e], clp = cl + st[e], cum = cu - st[e], clm = cl - st[e];
+              const double *Wup = &b->W[cup * NV], *Wlp = &b->W[clp * NV],
+                           *Wum = &b->W[cum * NV], *Wlm = &b->W[clm * NV];
+              for (int q = 0; q < 3; ++q) {
+                vhi[e][q] = 0.25 * (((Wl[1 + q] + Wu[1 + q]) + Wup[1 + q]) + Wlp[1 + q]);
+                vlo[e][q] = 0.25 * (((Wl[1 + q] + Wu[1 + q]) + Wum[1 + q]) + Wlm[1 + q]);
+              }
+              thi[e] = 0.25 * (((b->T[cl] + b->T[cu]) + b->T[cup]) + b->T[clp]);
+              tlo[e] = 0.25 * (((b->T[cl] + b->T[cu]) + b->T[cum]) + b->T[clm]);
+              /* faces of direction e: cell index (i,j,k) of cu/cl shifted */
+              const int64_t xu = cu, xl = cl;
+              const int uI = (int)(xu % b->NI) - b->ng, uJ = (int)((xu / b->NI) % b->NJ) - b->ng,
+                        uK = (int)(xu / ((int64_t)b->NI * b->NJ)) - b->ng;
+              const int lI = (int)(xl % b->NI) - b->ng, lJ = (int)((xl / b->NI) % b->NJ) - b->ng,
+                        lK = (int)(xl / ((int64_t)b->NI * b->NJ)) - b->ng;
+              double Au[3], Al[3], Aup[3], Alp[3];
+              area_vec(b, e, face_idx(b, e, uI, uJ, uK), Au);
+              area_vec(b, e, face_idx(b, e, lI, lJ, lK), Al);
+              area_vec(b, e, face_idx(b, e, uI + (e == 0), uJ + (e == 1), uK + (e == 2)), Aup);
+              area_vec(b, e, face_idx(b, e, lI + (e == 0), lJ + (e == 1), lK + (e == 2)), Alp);
+              for (int q = 0; q < 3; ++q) {
+                ahi[e][q] = 0.5 * (Aup[q] + Alp[q]);
+                alo[e][q] = 0.5 * (Au[q] + Al[q]);
+              }
+            }
+          }
+          const double vol = 0.5 * (b->vol[cl] + b->vol[cu]);
+          const double invVol = 1.0 / vol;
+          double grad[3][3], tg[3];
+          for (int r = 0; r < 3; ++r) {     /* area component */
+            for (int q = 0; q < 3; ++q) {   /* velocity component */
+              grad[r][q] = vhi[0][q] * ahi[0][r] - vlo[0][q] * alo[0][r] +
+                           vhi[1][q] * ahi[1][r] - vlo[1][q] * alo[1][r] +
+                           vhi[2][q] * ahi[2][r] - vlo[2][q] * alo[2][r];
+              grad[r][q] *= invVol;
+            }
+            tg[r] = thi[0] * ahi[0][r] - tlo[0] * alo[0][r] + thi[1] * ahi[1][r] -
+                    tlo[1] * alo[1][r] + thi[2] * ahi[2][r] - tlo[2] * alo[2][r];
+            tg[r] *= invVol;
+          }
+          /* face state and viscosity by central reconstruction */
+          double cd, cuw;
+          central_coeffs(wd[cl], wd[cu], &cd, &cuw);
+          double fs[NV];
+          for (int q = 0; q < NV; ++q) fs[q] = cd * b->W[cu * NV + q] + cuw * b->W[cl * NV + q];
+          const double muf = cd * b->mu[cu] + cuw * b->mu[cl];
+          /* viscous flux */
+          double n[3], mag;
+          face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
+          const double mus = v->visc_scale * muf, muts = v->visc_scale * 0.0;
+          const double lambda = 0.0 - (2.0 / 3.0) * (mus + muts);
+          const double trace = grad[0][0] + grad[1][1] + grad[2][2];
+          double tau[3];
+          for (int r = 0; r < 3; ++r) {
+            const double sn = (grad[r][0] + grad[0][r]) * n[0] + (grad[r][1] + grad[1][r]) * n[1] +
+                              (grad[r][2] + grad[2][r]) * n[2];
+            tau[r] = lambda * trace * n[r] + (mus + muts) * sn;
+          }
+          const double tf = temp_of(fs, g);
+          const double kk_ = cond_eff(tf, v);
+          const double kt = muts * cp_of(g) / 0.9;
+          double F[NV];
+          F[0] = 0.0;
+          F[1] = tau[0];
+          F[2] = tau[1];
+          F[3] = tau[2];
+          F[4] = (tau[0] * fs[1] + tau[1] * fs[2] + tau[2] * fs[3]) +
+                 (kk_ + kt) * (tg[0] * n[0] + tg[1] * n[1] + tg[2] * n[2]) + 0.0;
+          if (fpos > 0)
+            for (int q = 0; q < NV; ++q) b->R[cl * NV + q] -= F[q] * mag;
+          if (fpos < nd) {
+            for (int q = 0; q < NV; ++q) b->R[cu * NV + q] += F[q] * mag;
+            double nl[3], ml, nh[3], mh;
+            face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
+            face_normal(b, d, face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
+            const double *Wc = &b->W[cu * NV];
+            const double fMag = 0.5 * (ml + mh);
+            const double lv = visc_max_term(Wc, g) * visc_term(b->mu[cu], v, g) * fMag * fMag /
+                              b->vol[cu];
+            b->lam[cu] += lv * coeff;
+            b->A[cu] += 2.0 * lv;
+          }
+        }
+  }
+}
+
 /* ---------------------------------------------------------------- API */
 orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
                      const ath_solve_view *sv) {
@@ -442,6 +663,7 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     c->s[s].gas.r = sv[s].gas_r;
     c->s[s].gas.n = sv[s].gas_n;
     c->s[s].gas.hf = sv[s].gas_hf;
+    c->s[s].viscous = sv[s].eqn != ATH_EQN_EULER;
   }
   for (int bi = 0; bi < nblocks; ++bi) {
     const ath_block_view *v = &bv[bi];
@@ -464,8 +686,24 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     b->A = (double *)dup_arr(NULL, 8 * b->nc);
     b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
     b->mask = (uint8_t *)dup_arr(v->nbr_mask, b->nc);
+    b->center = (double *)dup_arr(v->center, 8 * 3 * b->nc);
+    b->T = (double *)dup_arr(NULL, 8 * b->nc);
+    b->mu = (double *)dup_arr(NULL, 8 * b->nc);
+    b->corner = (uint8_t *)dup_arr(NULL, b->nc);
+    for (int64_t x = 0; x < b->nc; ++x) {
+      const int64_t ii = x % b->NI, jj = (x / b->NI) % b->NJ, kk = x / ((int64_t)b->NI * b->NJ);
+      const int gi = ii < b->ng || ii >= b->NI - b->ng, gj = jj < b->ng || jj >= b->NJ - b->ng,
+                gk = kk < b->ng || kk >= b->NK - b->ng;
+      b->corner[x] = (uint8_t)(gi && gj && gk);
+    }
     b->nops = v->nops;
     b->ops = (ath_ghost_op *)dup_arr(v->ops, sizeof(ath_ghost_op) * v->nops);
+    b->nedge = v->nedge_ops;
+    b->edge = (ath_ghost_op *)dup_arr(v->edge_ops, sizeof(ath_ghost_op) * v->nedge_ops);
+    b->nvops = v->nvops;
+    b->vops = (ath_ghost_op *)dup_arr(v->vops, sizeof(ath_ghost_op) * v->nvops);
+    b->nvedge = v->nvedge_ops;
+    b->vedge = (ath_ghost_op *)dup_arr(v->vedge_ops, sizeof(ath_ghost_op) * v->nvedge_ops);
     b->nplanes = v->nplanes;
     b->plane_off = (int32_t *)dup_arr(v->plane_offsets, 4 * (v->nplanes + 1));
     b->plane_cells = (int32_t *)dup_arr(v->plane_cells, 4 * (size_t)v->ni * v->nj * v->nk);
@@ -481,6 +719,8 @@ void orc_destroy(orc_case *c) {
     for (int d = 0; d < 3; ++d) free(b->fa[d]);
     free(b->W); free(b->R); free(b->dU); free(b->lam); free(b->dt); free(b->A);
     free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
+    free(b->center); free(b->T); free(b->mu); free(b->corner);
+    free(b->edge); free(b->vops); free(b->vedge);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
@@ -589,6 +829,8 @@ void orc_fill_ghosts(orc_case *c) {
       memcpy(&b->W[op->dst * NV], g, sizeof(g));
     }
   }
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) apply_edge_ops(&c->b[bi], c->b[bi].nedge, c->b[bi].edge);
 }
 
 /* procBlock::CalcResidualNoSource (src/procBlock.cpp:6111) for inviscid
@@ -658,6 +900,23 @@ void orc_residual(orc_case *c) {
             }
           }
     }
+    if (sv->viscous) {
+      /* AssignViscousGhostCells (src/procBlock.cpp:2760) + edges */
+      for (int o = 0; o < b->nvops; ++o) {
+        const ath_ghost_op *op = &b->vops[o];
+        double gw[NV];
+        viscous_wall_ghost(&b->W[op->src * NV], &sv->states[op->state], g, gw);
+        memcpy(&b->W[op->dst * NV], gw, sizeof(gw));
+      }
+      apply_edge_ops(b, b->nvedge, b->vedge);
+      /* UpdateAuxillaryVariables (src/procBlock.cpp:6171): all but corners */
+      for (int64_t x = 0; x < b->nc; ++x) {
+        if (b->corner[x]) continue;
+        b->T[x] = temp_of(&b->W[x * NV], g);
+        b->mu[x] = visc_of(b->T[x], &sv->v);
+      }
+      viscous_fluxes(c, b);
+    }
   }
 }
 
@@ -716,7 +975,20 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
     const int fk = (int)kk - b->ng + (!lower && d == 2);
     double n[3], mag, o[NV];
     face_normal(b, d, face_idx(b, d, fi, fj, fk), n, &mag);
-    scalar_offdiag(&b->W[nb * NV], &b->dU[nb * NV], g, n, mag, lower, o);
+    double vsr = 0.0;
+    const osolve *sv = &c->s[b->solve];
+    if (sv->viscous) {
+      /* ProjC2CDist (src/procBlock.cpp:6316): centre of the cell above the
+       * face minus the one below, along the face normal */
+      const int64_t up = lower ? x : nb, lo = lower ? nb : x;
+      const double dc[3] = {b->center[up] - b->center[lo],
+                            b->center[b->nc + up] - b->center[b->nc + lo],
+                            b->center[2 * b->nc + up] - b->center[2 * b->nc + lo]};
+      const double dist = dc[0] * n[0] + dc[1] * n[1] + dc[2] * n[2];
+      const double *wn = &b->W[nb * NV];
+      vsr = mag / dist * visc_max_term(wn, g) * visc_term(b->mu[nb], &sv->v, g);
+    }
+    scalar_offdiag(&b->W[nb * NV], &b->dU[nb * NV], g, n, mag, lower, vsr, o);
     for (int v = 0; v < NV; ++v) acc[v] += o[v];
   }
 }

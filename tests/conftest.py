@@ -41,7 +41,8 @@ def golden_case(name, outdir):
     g = load_golden(name)
     kw = ast.literal_eval(str(g["kwargs"]))
     base = name.split("_it")[0]
-    gen = cases.vortex_box if base.startswith("vortex") else cases.bump_channel
+    gen = (cases.vortex_box if base.startswith("vortex")
+           else cases.flat_plate if base.startswith("plate") else cases.bump_channel)
     inp, st = gen(outdir, name=base, **kw)
     return inp, st, g
 

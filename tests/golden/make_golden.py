@@ -45,6 +45,11 @@ CASES = [
     ("bump_const_ausm", cases.bump_channel,
      dict(ni=16, nj=8, nk=3, height=0.05, mach=0.5, recon="constant", limiter="none",
           flux="ausm"), [1, 20], True),
+    ("plate_adiabatic", cases.flat_plate,
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3), [1, 20], True),
+    ("plate_isothermal", cases.flat_plate,
+     dict(ni=14, nj=9, nk=2, dy0=5e-4, ratio=1.35, wall_t=300.0, mach=0.5), [1, 20], True),
+    ("plate_c2", cases.flat_plate, dict(), [20], False),
     ("bump_vanalbada_ausm", cases.bump_channel,
      dict(ni=22, nj=11, nk=3, height=0.09, mach=0.75, limiter="vanAlbada", flux="ausm"),
      [1, 20], True),
@@ -63,17 +68,21 @@ def run_case(name, gen, kw, niter, full, ref_dir):
         if r.returncode != 0:
             raise RuntimeError(f"reference harness failed on {name}: {r.stderr[-2000:]}")
         R = read_dump(os.path.join(d, "out.bin"))
-    ng = (R["b0_state"].shape[0] - R["b0_resid"].shape[0]) // 2
-    state = R["b0_state"][ng:-ng, ng:-ng, ng:-ng]
+    nblocks = sum(1 for k in R if k.startswith("b") and k.endswith("_resid"))
     out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "kwargs": np.array(repr(kw)),
-           "iterations": np.array(niter)}
-    if full:
-        out.update(state0=R["b0_state0"], state=state, resid=R["b0_resid"], dt=R["b0_dt"],
-                   specrad=R["b0_specrad"], du=R["b0_du"])
-    else:
-        out.update(state_sum=state.reshape(-1, 5).sum(axis=0),
-                   state_sumsq=(state.reshape(-1, 5) ** 2).sum(axis=0),
-                   state_samples=state[::3, ::7, ::11].copy())
+           "iterations": np.array(niter), "nblocks": np.array(nblocks)}
+    for b in range(nblocks):
+        p = f"b{b}_"
+        ng = (R[p + "state"].shape[0] - R[p + "resid"].shape[0]) // 2
+        state = R[p + "state"][ng:-ng, ng:-ng, ng:-ng]
+        if full:
+            out.update({p + "state0": R[p + "state0"], p + "state": state,
+                        p + "resid": R[p + "resid"], p + "dt": R[p + "dt"],
+                        p + "specrad": R[p + "specrad"], p + "du": R[p + "du"]})
+        else:
+            out.update({p + "state_sum": state.reshape(-1, 5).sum(axis=0),
+                        p + "state_sumsq": (state.reshape(-1, 5) ** 2).sum(axis=0),
+                        p + "state_samples": state[::3, ::7, ::11].copy()})
     path = os.path.join(HERE, f"{name}_it{niter}.npz")
     np.savez_compressed(path, **out)
     print("wrote", path)

@@ -42,17 +42,21 @@ def _l2(norms, nsolves=1, solve=0):
                                   "bump24_it30", "bump_sup_it1", "bump_sup_it40",
                                   "bump_weno_it1", "bump_weno_it20", "bump_wenoz_ausm_it1",
                                   "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
-                                  "bump_vanalbada_ausm_it20"])
+                                  "bump_vanalbada_ausm_it20", "plate_adiabatic_it1",
+                                  "plate_adiabatic_it20", "plate_isothermal_it1",
+                                  "plate_isothermal_it20"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
     n = int(g["iterations"])
     norms = b.iterate(n)
-    assert rel_err(b.field(0, "STATE"), g["state"]) <= CELL_TOL
-    assert rel_err(b.field(0, "RESID"), g["resid"]) <= CELL_TOL
-    assert rel_err(b.field(0, "DT")[..., 0], g["dt"]) <= CELL_TOL
-    assert rel_err(b.field(0, "SPECRAD")[..., 0], g["specrad"][..., 0]) <= CELL_TOL
-    assert rel_err(b.field(0, "DU"), g["du"]) <= CELL_TOL
+    for k in range(int(g["nblocks"])):
+        p = f"b{k}_"
+        assert rel_err(b.field(k, "STATE"), g[p + "state"]) <= CELL_TOL
+        assert rel_err(b.field(k, "RESID"), g[p + "resid"]) <= CELL_TOL
+        assert rel_err(b.field(k, "DT")[..., 0], g[p + "dt"]) <= CELL_TOL
+        assert rel_err(b.field(k, "SPECRAD")[..., 0], g[p + "specrad"][..., 0]) <= CELL_TOL
+        assert rel_err(b.field(k, "DU"), g[p + "du"]) <= CELL_TOL
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
     assert all(x.status == 0 for x in norms)
     b.close()
@@ -71,7 +75,21 @@ def test_fp64_matrix_residual(ctx, name, tmp_path):
     norms = b.iterate(int(g["iterations"]))
     mres = np.array([n.matrix_resid for n in norms])
     assert rel_err(mres, g["matrix_resid"]) <= NORM_TOL
-    assert rel_err(b.field(0, "STATE"), g["state"]) <= CELL_TOL
+    assert rel_err(b.field(0, "STATE"), g["b0_state"]) <= CELL_TOL
+    b.close()
+
+
+def test_fp64_laminar_plate_two_blocks(ctx, tmp_path):
+    """Laminar flat plate, two 128x64x2 blocks with an interblock connection:
+    20 iterations against the reference's L2 history and state statistics."""
+    inp, st, g = golden_case("plate_c2_it20", str(tmp_path))
+    s, b = _batch(ctx, inp, st)
+    norms = b.iterate(20)
+    assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    for k in range(2):
+        w = b.field(k, "STATE")
+        assert rel_err(w.reshape(-1, 5).sum(axis=0), g[f"b{k}_state_sum"]) <= NORM_TOL
+        assert rel_err(w[::3, ::7, ::11], g[f"b{k}_state_samples"]) <= CELL_TOL * 100
     b.close()
 
 
@@ -81,8 +99,8 @@ def test_fp64_full_vortex_box_200_iterations(ctx, tmp_path):
     norms = b.iterate(200)
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
     w = b.field(0, "STATE")
-    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["state_sum"]) <= NORM_TOL
-    assert rel_err(w[::3, ::7, ::11], g["state_samples"]) <= CELL_TOL * 100
+    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["b0_state_sum"]) <= NORM_TOL
+    assert rel_err(w[::3, ::7, ::11], g["b0_state_samples"]) <= CELL_TOL * 100
     b.close()
 
 

@@ -17,7 +17,8 @@ TOL = 1e-13
 FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "bump_sup_it1", "bump_sup_it40", "bump_weno_it1", "bump_weno_it20",
         "bump_wenoz_ausm_it1", "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
-        "bump_vanalbada_ausm_it20"]
+        "bump_vanalbada_ausm_it20", "plate_adiabatic_it1", "plate_adiabatic_it20",
+        "plate_isothermal_it1", "plate_isothermal_it20"]
 
 
 def _oracle(inp, st):
@@ -35,11 +36,13 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
     _, o = _oracle(inp, st)
     n = int(g["iterations"])
     l2 = o.iterate(n)
-    assert rel_err(o.field(0, "STATE"), g["state"]) <= TOL
-    assert rel_err(o.field(0, "RESID"), g["resid"]) <= TOL
-    assert rel_err(o.field(0, "DT")[..., 0], g["dt"]) <= TOL
-    assert rel_err(o.field(0, "SPECRAD")[..., 0], g["specrad"][..., 0]) <= TOL
-    assert rel_err(o.field(0, "DU"), g["du"]) <= TOL
+    for b in range(int(g["nblocks"])):
+        p = f"b{b}_"
+        assert rel_err(o.field(b, "STATE"), g[p + "state"]) <= TOL
+        assert rel_err(o.field(b, "RESID"), g[p + "resid"]) <= TOL
+        assert rel_err(o.field(b, "DT")[..., 0], g[p + "dt"]) <= TOL
+        assert rel_err(o.field(b, "SPECRAD")[..., 0], g[p + "specrad"][..., 0]) <= TOL
+        assert rel_err(o.field(b, "DU"), g[p + "du"]) <= TOL
     assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
 
 
@@ -65,8 +68,22 @@ def test_oracle_full_vortex_box_200_iterations(tmp_path):
     l2 = o.iterate(200)
     assert rel_err(l2[:, 0, :], g["l2"]) <= 1e-12
     w = o.field(0, "STATE")
-    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["state_sum"]) <= 1e-12
-    assert rel_err(w[::3, ::7, ::11], g["state_samples"]) <= 1e-12
+    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["b0_state_sum"]) <= 1e-12
+    assert rel_err(w[::3, ::7, ::11], g["b0_state_samples"]) <= 1e-12
+
+
+def test_oracle_laminar_plate_two_blocks(tmp_path):
+    """Two 128x64x2 blocks joined by an interblock connection, laminar
+    Navier-Stokes at Re_L = 1e5 on a wall-normal geometric grid (first cell
+    1e-5, ratio 1.08): 20 iterations against the reference."""
+    inp, st, g = golden_case("plate_c2_it20", str(tmp_path))
+    _, o = _oracle(inp, st)
+    l2 = o.iterate(20)
+    assert rel_err(l2[:, 0, :], g["l2"]) <= 1e-12
+    for b in range(2):
+        w = o.field(b, "STATE")
+        assert rel_err(w.reshape(-1, 5).sum(axis=0), g[f"b{b}_state_sum"]) <= 1e-12
+        assert rel_err(w[::3, ::7, ::11], g[f"b{b}_state_samples"]) <= 1e-12
 
 
 @pytest.mark.skipif(not (os.path.exists(REF_HARNESS) and os.path.isdir(REF_SRC)),
