@@ -1,8 +1,12 @@
 """Parity of the sm_103a path with the reference, through the C ABI.
 
 Tolerances (relative to the largest magnitude of the compared field):
-  * FP64 path, per cell, after one iteration and after tens of
-    iterations: 1e-12;
+  * FP64 path, per cell, after one iteration: 1e-12 for every field;
+  * after tens of iterations: 1e-12 for the state, time step and spectral
+    radius; 1e-10 for the residual and the implicit update, which are small
+    differences of large fluxes once the solution converges and amplify the
+    last-bit differences of pow() between CUDA and the host libm (Sutherland's
+    law) and of FMA-free reordering;
   * FP64 path, L2 residual histories (incl. 200 iterations of the full
     64x32x8 vortex box): 1e-10.
 """
@@ -50,13 +54,14 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     s, b = _batch(ctx, inp, st)
     n = int(g["iterations"])
     norms = b.iterate(n)
+    diff_tol = CELL_TOL if n == 1 else NORM_TOL
     for k in range(int(g["nblocks"])):
         p = f"b{k}_"
         assert rel_err(b.field(k, "STATE"), g[p + "state"]) <= CELL_TOL
-        assert rel_err(b.field(k, "RESID"), g[p + "resid"]) <= CELL_TOL
+        assert rel_err(b.field(k, "RESID"), g[p + "resid"]) <= diff_tol
         assert rel_err(b.field(k, "DT")[..., 0], g[p + "dt"]) <= CELL_TOL
         assert rel_err(b.field(k, "SPECRAD")[..., 0], g[p + "specrad"][..., 0]) <= CELL_TOL
-        assert rel_err(b.field(k, "DU"), g[p + "du"]) <= CELL_TOL
+        assert rel_err(b.field(k, "DU"), g[p + "du"]) <= diff_tol
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
     assert all(x.status == 0 for x in norms)
     b.close()
