@@ -123,6 +123,7 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         f"referenceDensity: {_fmt(refs.r_ref)}",
         f"initialConditions: <{ic}>",
         f"matrixSolver: {scheme.get('matrixSolver', 'lusgs')}",
+        f"matrixSweeps: {int(scheme.get('matrixSweeps', 1))}",
         "matrixRelaxation: 1.0",
     ]
     if states:
@@ -211,7 +212,8 @@ def bump_nodes(ni: int, nj: int, nk: int, height: float, length: float = 3.0,
 
 def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: float,
                  cfl: float = 20.0, name: str = "bump", recon: str = "thirdOrder",
-                 limiter: str = "minmod", flux: str = "roe"):
+                 limiter: str = "minmod", flux: str = "roe", matrix_solver: str = "lusgs",
+                 sweeps: int = 1):
     os.makedirs(outdir, exist_ok=True)
     nodes = bump_nodes(ni, nj, nk, height)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
@@ -230,7 +232,8 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
             ("slipWall", 0, ni, 0, nj, nk, nk, 2)]]
     inp = os.path.join(outdir, name + ".inp")
     write_input(inp, name, {"cfl": cfl, "limiter": limiter, "faceReconstruction": recon,
-                            "inviscidFlux": flux}, refs, ic, states, bcs)
+                            "inviscidFlux": flux, "matrixSolver": matrix_solver,
+                            "matrixSweeps": sweeps}, refs, ic, states, bcs)
     return inp, None
 
 
@@ -267,7 +270,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                ratio: float = 1.08, length: float = 1.0, mach: float = 0.3,
                reynolds: float = 1e5, t_inf: float = 288.0, cfl: float = 100.0,
                wall_t: float | None = None, limiter: str = "vanAlbada",
-               name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder"):
+               name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder",
+               sweeps: int = 1):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -302,6 +306,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
             ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
     inp = os.path.join(outdir, name + ".inp")
     write_input(inp, name, {"cfl": cfl, "limiter": limiter, "equationSet": "navierStokes",
-                            "matrixSolver": matrix_solver, "faceReconstruction": recon},
+                            "matrixSolver": matrix_solver, "faceReconstruction": recon,
+                            "matrixSweeps": sweeps},
                 refs, ic, states, [blk0, blk1])
     return inp, None

@@ -105,6 +105,9 @@ struct BatchCore {
   std::vector<int64_t> solve_pos0;   // per block: loop-order offset inside its solve
   Lists L;
   int nsteps = 0;
+  int kinds = 0;        // bit 0: scalar lusgs solves present, bit 1: block (blusgs)
+  int max_sweeps = 1;   // largest matrixSweeps of the batch
+  bool block_viscous = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::unique_ptr<DevMem> mem;
@@ -242,14 +245,29 @@ class Runner : public RunnerBase {
     P_.nghost = ngh;
     P_.Wq = m.Alloc<T>(5 * nq);
     P_.Rq = m.Alloc<T>(5 * nq);
-    P_.Ainvq = m.Alloc<T>(nq);
-    P_.Aq = m.Alloc<T>(nq);
+    const int64_t aw = (c.kinds & 2) ? 25 : 1;  // width of the diagonal
+    P_.Ainvq = m.Alloc<T>(aw * nq);
+    P_.Aq = m.Alloc<T>(aw * nq);
     P_.dUq = m.Alloc<T>(5 * nq);
     P_.dUg = m.Alloc<T>(5 * std::max<int64_t>(ngh, 1));
     Check(cudaMemset(P_.Wq, 0, 5 * nq * sizeof(T)), "memset");
     Check(cudaMemset(P_.Rq, 0, 5 * nq * sizeof(T)), "memset");
-    Check(cudaMemset(P_.Ainvq, 0, nq * sizeof(T)), "memset");
-    Check(cudaMemset(P_.Aq, 0, nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.Ainvq, 0, aw * nq * sizeof(T)), "memset");
+    Check(cudaMemset(P_.Aq, 0, aw * nq * sizeof(T)), "memset");
+    if (c.kinds & 2) {
+      for (int d = 0; d < 3; ++d) {
+        P_.fst[d] = m.Alloc<T>(10 * n);
+        Check(cudaMemset(P_.fst[d], 0, 10 * n * sizeof(T)), "memset");
+        if (c.block_viscous) {
+          P_.vst[d] = m.Alloc<T>(15 * n);
+          Check(cudaMemset(P_.vst[d], 0, 15 * n * sizeof(T)), "memset");
+        }
+      }
+      if (c.block_viscous) {
+        P_.vgq = m.Alloc<T>(9 * nq);
+        Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
+      }
+    }
     Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
     Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
     {
@@ -348,26 +366,46 @@ class Runner : public RunnerBase {
                       (int)c_.L.face_cta_block[d].size(), c_.stream);
     Viscous();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
-                    c_.stream);
+                    c_.kinds, c_.stream);
   }
-  void Relax() override {
-    // x = 0 before the first sweep: only the connection ghosts are read
-    // before being written
-    if (P_.nghost > 0)
-      Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
-    for (int s = 0; s < c_.nsteps; ++s) {
-      const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-      Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
+  void SweepPass(int forward, int sweep) {
+    const bool full = c_.max_sweeps > 1;
+    if (forward) {
+      for (int s = 0; s < c_.nsteps; ++s) {
+        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.kinds, c_.stream);
+      }
+    } else {
+      for (int s = c_.nsteps - 1; s >= 0; --s) {
+        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.kinds, c_.stream);
+      }
     }
-    Launch<T>::ConnDu(P_, c_.stream);
-    for (int s = c_.nsteps - 1; s >= 0; --s) {
-      const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-      Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
+  }
+  // lusgs::Relax (src/linearSolver.cpp:430): dU ghost swap before every
+  // pass and after the last one
+  void Relax() override {
+    if (c_.max_sweeps <= 1) {
+      // x = 0 before the first sweep: only the connection ghosts are read
+      // before being written
+      if (P_.nghost > 0)
+        Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
+      SweepPass(1, 0);
+      Launch<T>::ConnDu(P_, c_.stream);
+      SweepPass(0, 0);
+    } else {
+      Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
+      for (int sw = 0; sw < c_.max_sweeps; ++sw) {
+        Launch<T>::ConnDu(P_, c_.stream);
+        SweepPass(1, sw);
+        Launch<T>::ConnDu(P_, c_.stream);
+        SweepPass(0, sw);
+      }
     }
     if (c_.flags & 1) {
       Launch<T>::ConnDu(P_, c_.stream);
       Launch<T>::MatRes(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_mres,
-                        (int)c_.L.cell_cta_block.size(), c_.stream);
+                        (int)c_.L.cell_cta_block.size(), c_.kinds, c_.stream);
     }
   }
   void Update() override {
@@ -413,30 +451,45 @@ class Runner : public RunnerBase {
       }
       Viscous();
       Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
-                      c_.stream);
+                      c_.kinds, c_.stream);
       Check(cudaEventRecord(e[5], c_.stream), "event");
-      if (P_.nghost > 0)
+      // forward passes, then backward passes (one-sweep form; the timing
+      // split of a multi-sweep relaxation puts each sweep's passes in turn)
+      if (c_.max_sweeps > 1)
+        Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
+      else if (P_.nghost > 0)
         Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
-      for (int s = 0; s < c_.nsteps; ++s) {
-        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, c_.stream);
+      float fwd = 0.f, bwd = 0.f;
+      for (int sw = 0; sw < c_.max_sweeps; ++sw) {
+        if (c_.max_sweeps > 1) Launch<T>::ConnDu(P_, c_.stream);
+        Check(cudaEventRecord(e[6], c_.stream), "event");
+        SweepPass(1, sw);
+        Check(cudaEventRecord(e[7], c_.stream), "event");
+        Launch<T>::ConnDu(P_, c_.stream);
+        SweepPass(0, sw);
+        Check(cudaEventRecord(e[8], c_.stream), "event");
+        Check(cudaEventSynchronize(e[8]), "sync");
+        float t1 = 0.f, t2 = 0.f;
+        Check(cudaEventElapsedTime(&t1, e[6], e[7]), "elapsed");
+        Check(cudaEventElapsedTime(&t2, e[7], e[8]), "elapsed");
+        fwd += t1;
+        bwd += t2;
       }
       Check(cudaEventRecord(e[6], c_.stream), "event");
-      Launch<T>::ConnDu(P_, c_.stream);
-      for (int s = c_.nsteps - 1; s >= 0; --s) {
-        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, c_.stream);
-      }
-      Check(cudaEventRecord(e[7], c_.stream), "event");
       Update();
       c_.iter_host += 1;
-      Check(cudaEventRecord(e[8], c_.stream), "event");
-      Check(cudaEventSynchronize(e[8]), "sync");
-      for (int q = 0; q < 8; ++q) {
+      Check(cudaEventRecord(e[7], c_.stream), "event");
+      Check(cudaEventSynchronize(e[7]), "sync");
+      for (int q = 0; q < 5; ++q) {
         float t = 0.f;
         Check(cudaEventElapsedTime(&t, e[q], e[q + 1]), "elapsed");
         ms[q] += t;
       }
+      float tu = 0.f;
+      Check(cudaEventElapsedTime(&tu, e[6], e[7]), "elapsed");
+      ms[5] += fwd;
+      ms[6] += bwd;
+      ms[7] += tu;
     }
     for (int q = 0; q < 8; ++q) ms[q] /= std::max(reps, 1);
     for (auto &x : e) cudaEventDestroy(x);
@@ -741,6 +794,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   for (const auto &b : st.blocks)
     if (b.nv != 5 || b.ng < 1)
       throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
+  for (const auto &sv : st.solves) {
+    const bool blk = sv.phys.solver == ATH_SOLVER_BLUSGS;
+    c.kinds |= blk ? 2 : 1;
+    c.max_sweeps = std::max(c.max_sweeps, (int)sv.phys.sweeps);
+    if (blk && sv.phys.eqn != ATH_EQN_EULER) c.block_viscous = true;
+  }
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");
   BuildLists(c);
   c.mem.reset(new DevMem(ctx));
@@ -778,6 +837,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.k_s = p.k_s;
     x.k_ref = p.k_ref;
     x.visc_coeff = p.visc_cfl_coeff;
+    x.block = p.solver == ATH_SOLVER_BLUSGS;
+    x.sweeps = p.sweeps;
     x.padded_values = 0.0;
     x.cells = 0.0;
     for (int b : st.solves[s].blocks) {
@@ -845,11 +906,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     edge_phases += c.L.edge_phase_off[ph + 1] > c.L.edge_phase_off[ph];
     vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
   }
+  const int nkinds = (c.kinds & 1) + ((c.kinds >> 1) & 1);
+  const int conn = c.L.ghost_cell.empty() ? 0 : 1;
   c.launches_per_iter = edge_phases +
                         (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 : 0) +
-                        1 + (c.L.ops.empty() ? 0 : 1) + 3 + 1 + 2 * c.nsteps +
-                        (c.L.ghost_cell.empty() ? 0 : 1) + 3 +
-                        ((flags & 1) ? 1 + (c.L.ghost_cell.empty() ? 0 : 1) : 0);
+                        1 + (c.L.ops.empty() ? 0 : 1) + 3 + nkinds +
+                        2 * c.nsteps * c.max_sweeps * nkinds +
+                        (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn) + 3 +
+                        ((flags & 1) ? nkinds + conn : 0);
 }
 
 // Reads norms of iterations [it0, it0+n) from the ring into norms_h.

@@ -36,7 +36,10 @@ struct SolveDev {
   double visc_scale, mu_c1, mu_s, mu_ref, t_ref, k_c1, k_s, k_ref, visc_coeff;
   int32_t viscous, pad3;
   int32_t limiter, nstates, state0, recon;
-  int32_t flux, pad0, pad1, pad2;
+  int32_t flux;
+  int32_t block;   // blusgs: 5x5 Jacobian diagonal and off-diagonals
+  int32_t sweeps;  // matrixSweeps
+  int32_t pad2;
 };
 
 // A ghost-cell assignment with pool indices.
@@ -81,8 +84,9 @@ struct Pools {
   // hyperplane-ordered sweep working set, nq = physical cells of the batch
   T *Wq;            // [5][nq] state in the sweep's arithmetic
   T *Rq;            // [5][nq]
-  T *Ainvq;         // [nq] inverse of the scalar main diagonal
-  T *Aq;            // [nq] the scalar main diagonal (matrix residual)
+  T *Ainvq;         // [nq] inverse of the scalar main diagonal; [25][nq]
+                    // row-major 5x5 inverse when the batch has block solves
+  T *Aq;            // the main diagonal (matrix residual), same layout
   T *muq;           // [nq] laminar viscosity, q order
   const T *dist_lo; // [3][nq] centre-to-centre distance along the lower face normal
   const T *dist_hi; // [3][nq] same for the upper face
@@ -93,6 +97,11 @@ struct Pools {
   const int32_t *ghost_cell;  // [nghost] pool cell of each connection ghost
   const int32_t *ghost_src;   // [nghost] q index of the partner interior cell
   T *dUg;           // [5][nghost] update of the connection ghosts
+  // block (blusgs) solves only
+  T *fst[3];        // [10][ncell] reconstructed face states, lower side then upper
+  T *vst[3];        // [15][ncell] viscous face state, face viscosity, face
+                    // velocity gradient (row = derivative axis)
+  T *vgq;           // [9][nq] cell-averaged velocity gradient, q order
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -141,14 +150,22 @@ __global__ void k_face(Pools<T> P, const int32_t *list, const int32_t *cta_block
 // diagonal of every physical cell (procBlock residual accumulation,
 // CalcBlockTimeStep src/procBlock.cpp:798, AddDiagonalTerms/Invert
 // src/linearSolver.cpp:146,177).
-template <typename T>
+template <typename T, bool BLOCK>
 __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block);
 
 // One hyperplane of the LU-SGS forward / backward sweep
 // (lusgs::LUSGS_Forward/Backward, src/linearSolver.cpp:341,385); items are
-// (q index, block) pairs.
+// (q index, block) pairs.  FULL: some solve runs more than one sweep, so
+// both triangles may enter a pass.  k_sweep serves scalar solves, k_sweepb
+// block solves.
+template <typename T, bool FULL>
+__global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward, int sweep);
 template <typename T>
-__global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward);
+__global__ void k_sweepb(Pools<T> P, const int2 *items, int n, int forward, int sweep);
+// Initial update x = A^-1 b of solves with more than one sweep, x = 0 for
+// the others (linearSolver::InitializeMatrixUpdate, src/linearSolver.cpp:111).
+template <typename T>
+__global__ void k_init(Pools<T> P, const int2 *items, int n);
 
 // dU ghost copies across connections (SwapImplicitUpdate, src/utility.cpp:400).
 template <typename T>
@@ -178,7 +195,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
 
 // Logged matrix residual r = -(A x - (L x - U x) - b) summed as r^2 per CTA
 // (linearSolver::Residual / AXmB, src/linearSolver.cpp:58,92).
-template <typename T>
+template <typename T, bool BLOCK>
 __global__ void k_matres(Pools<T> P, const int32_t *list, const int32_t *cta_block,
                          double *mres_partials);
 // Sets the CFL of the current iteration from the iteration counter
@@ -199,16 +216,18 @@ struct Launch {
                        const int32_t *cta_block, int ncta, cudaStream_t s);
   static void Face(int d, const Pools<T> &P, const int32_t *list,
                    const int32_t *cta_block, int ncta, cudaStream_t s);
+  // kinds: bit 0 = the batch has scalar solves, bit 1 = block solves
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                   int ncta, cudaStream_t s);
-  static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward,
-                    cudaStream_t s);
+                   int ncta, int kinds, cudaStream_t s);
+  static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
+                    bool full, int kinds, cudaStream_t s);
+  static void Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,
                      cudaStream_t s);
   static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                     double *mres_partials, int ncta, cudaStream_t s);
+                     double *mres_partials, int ncta, int kinds, cudaStream_t s);
 };
 
 }  // namespace ath

@@ -2,6 +2,7 @@
 // arithmetic type so each is compiled with its own contraction setting.
 #pragma once
 
+#include "block.cuh"
 #include "kernels.cuh"
 
 namespace ath {
@@ -195,17 +196,27 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
   T *out = P.flux[D];
 #pragma unroll
   for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * mag;
+  if (sv.block) {
+    // face states for the block diagonal's Rusanov Jacobians
+    T *fs = P.fst[D];
+    const T lr[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
+#pragma unroll
+    for (int v = 0; v < 10; ++v) fs[v * n + c] = lr[v];
+  }
 }
 
 // ---------------------------------------------------------------------------
-// residual assembly + spectral radius + dt + diagonal
-template <typename T>
+// residual assembly + spectral radius + dt + diagonal.  BLOCK: the 5x5
+// diagonal of block solves (scalar solves are served by the other
+// instantiation; a CTA never mixes the two).
+template <typename T, bool BLOCK>
 __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
-  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
-  if (c < 0) return;
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
+  if ((sv.block != 0) != BLOCK) return;
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
   const int64_t n = P.ncell;
   const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
   // R = 0 - Fi(lo) + Fi(hi) - Fj(lo) + Fj(hi) - Fk(lo) + Fk(hi), each face
@@ -265,11 +276,78 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   const double cfl = P.cfl[b.solve];
   const double dt = cfl * (vol / lam);
   P.dt[c] = dt;
-  const double a = adiag * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
-  // hyperplane-ordered copies for the sweeps
   const int64_t nq = P.nq;
-  P.Ainvq[q] = (T)(1.0 / a);
-  P.Aq[q] = (T)a;
+  if constexpr (BLOCK) {
+    // 5x5 diagonal (CalcInvFluxI/J/K, CalcViscFluxI/J/K block branches,
+    // src/procBlock.cpp:452-484,1417-1474): per direction, minus the
+    // Rusanov Jacobian of the upper-side state of the lower face, plus the
+    // one of the lower-side state of the upper face; then per direction the
+    // thin-shear-layer Jacobians, plus at the lower face, minus at the
+    // upper face
+    T A[kJac];
+#pragma unroll
+    for (int e = 0; e < kJac; ++e) A[e] = T(0);
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+      const double *fa = P.fa[d];
+      const T *fs = P.fst[d];
+      T J[kJac];
+      const int64_t u = c + st[d];
+      const Prim<T> sR{fs[5 * n + c], fs[6 * n + c], fs[7 * n + c], fs[8 * n + c],
+                       fs[9 * n + c]};
+      RusanovJac(sR, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c], (T)fa[3 * n + c], false, J);
+#pragma unroll
+      for (int e = 0; e < kJac; ++e) A[e] = A[e] - J[e];
+      const Prim<T> sL{fs[u], fs[n + u], fs[2 * n + u], fs[3 * n + u], fs[4 * n + u]};
+      RusanovJac(sL, g, (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u], (T)fa[3 * n + u], true, J);
+#pragma unroll
+      for (int e = 0; e < kJac; ++e) A[e] = A[e] + J[e];
+    }
+    if (sv.viscous) {
+      const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s,
+                            (T)sv.k_ref};
+      T vg[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) vg[e] = T(0);
+      const T sixth = T(1) / T(6);
+#pragma unroll 1
+      for (int d = 0; d < 3; ++d) {
+        const double *fa = P.fa[d];
+        const T *vs = P.vst[d];
+#pragma unroll 1
+        for (int side = 0; side < 2; ++side) {
+          const int64_t f = side ? c + st[d] : c;
+          const Prim<T> fsx{vs[f], vs[n + f], vs[2 * n + f], vs[3 * n + f], vs[4 * n + f]};
+          T gr[9];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) {
+            gr[e] = vs[(6 + e) * n + f];
+            vg[e] = vg[e] + sixth * gr[e];
+          }
+          const T dist = side ? P.dist_hi[d * nq + q] : P.dist_lo[d * nq + q];
+          TslJacAccum(fsx, vs[5 * n + f], g, tk, (T)fa[f], (T)fa[n + f], (T)fa[2 * n + f],
+                      (T)fa[3 * n + f], dist, side != 0, gr, side != 0, A);
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = vg[e];
+    }
+    const T diagVolTime = (T)((vol * (1.0 + sv.zeta)) / (dt * sv.theta));
+#pragma unroll
+    for (int r = 0; r < 5; ++r) A[r * 6] *= (T)sv.relax;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) A[r * 6] += diagVolTime;
+#pragma unroll
+    for (int e = 0; e < kJac; ++e) P.Aq[e * nq + q] = A[e];
+    Inverse5(A);
+#pragma unroll
+    for (int e = 0; e < kJac; ++e) P.Ainvq[e * nq + q] = A[e];
+  } else {
+    const double a = adiag * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+    P.Ainvq[q] = (T)(1.0 / a);
+    P.Aq[q] = (T)a;
+  }
+  // hyperplane-ordered copies for the sweeps
   P.Wq[q] = w.rho;
   P.Wq[nq + q] = w.u;
   P.Wq[2 * nq + q] = w.v;
@@ -330,24 +408,98 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
   }
 }
 
-// ---------------------------------------------------------------------------
-// LU-SGS hyperplane sweep on the q-ordered working set
+// Off-diagonal sum of one cell of a block solve (RusanovBlockOffDiagonal,
+// src/fluxJacobian.cpp:164): per neighbour the Rusanov Jacobian of its state
+// minus (lower) or plus (upper) its thin-shear-layer Jacobian with its
+// viscosity and cell-averaged gradient, times its update.
 template <typename T>
+__device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const Gas<T> &g,
+                                                const SolveDev &sv, int64_t q, bool lower,
+                                                T acc[5]) {
+  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
+  const T *face = lower ? P.face_lo : P.face_hi;
+  const T *dist = lower ? P.dist_lo : P.dist_hi;
+  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+  const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref};
+#pragma unroll
+  for (int v = 0; v < 5; ++v) acc[v] = T(0);
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    const int32_t nb = nbq[d * nq + q];
+    if (nb == -1) continue;
+    Prim<T> s;
+    T du[5], vg[9];
+    T mu = T(0);
+    int64_t vq;  // q index whose cell gradient the neighbour carries
+    if (nb >= 0) {
+      s.rho = P.Wq[nb];
+      s.u = P.Wq[nq + nb];
+      s.v = P.Wq[2 * nq + nb];
+      s.w = P.Wq[3 * nq + nb];
+      s.p = P.Wq[4 * nq + nb];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
+      if (sv.viscous) mu = P.muq[nb];
+      vq = nb;
+    } else {
+      const int64_t slot = -(int64_t)nb - 2;
+      s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
+      if (sv.viscous) mu = (T)P.mu[P.ghost_cell[slot]];
+      vq = P.ghost_src[slot];  // the connection copies the partner's gradient
+    }
+    const T *f = face + (int64_t)d * 4 * nq;
+    const T fx = f[q], fy = f[nq + q], fz = f[2 * nq + q], mag = f[3 * nq + q];
+    T J[kJac];
+    RusanovJac(s, g, fx, fy, fz, mag, lower, J);
+    if (sv.viscous) {
+#pragma unroll
+      for (int e = 0; e < 9; ++e) vg[e] = P.vgq[e * nq + vq];
+      TslJacAccum(s, mu, g, tk, fx, fy, fz, mag, dist[d * nq + q], lower, vg, lower, J);
+    }
+    T o[5];
+    MatVec5(J, du, o);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// LU-SGS hyperplane sweep on the q-ordered working set.  A pass uses one
+// triangle (sweep 0 of a one-sweep solve: forward x = A^-1 (b + L x),
+// backward x -= A^-1 U x) or both (x = A^-1 (b + L x - U x)).
+template <typename T, bool FULL>
 __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, int n_items,
-                                               int forward) {
+                                               int forward, int sweep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
   const int2 it = items[t];
   const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
+  if (sv.block) return;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   T acc[5];
   OffDiagSum(P, g, sv, q, forward != 0, acc);
   const T ainv = P.Ainvq[q];
+  const T thetaInv = (T)(1.0 / sv.theta);
+  if constexpr (FULL) {
+    if (sweep >= sv.sweeps) return;
+    if (sweep > 0 || sv.sweeps > 1) {
+      T other[5];
+      OffDiagSum(P, g, sv, q, forward == 0, other);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const T bv = -thetaInv * P.Rq[v * nq + q];
+        const T in = forward ? bv + (acc[v] - other[v]) : (bv + other[v]) - acc[v];
+        P.dUq[v * nq + q] = in * ainv;
+      }
+      return;
+    }
+  }
   if (forward) {
-    const T thetaInv = (T)(1.0 / sv.theta);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T bv = -thetaInv * P.Rq[v * nq + q];
@@ -360,6 +512,82 @@ __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, in
       P.dUq[v * nq + q] = xold - acc[v] * ainv;
     }
   }
+}
+
+// Block version: A^-1 is the 5x5 inverse, products by ArrayMultiplication.
+template <typename T>
+__global__ void __launch_bounds__(128) k_sweepb(Pools<T> P, const int2 *items, int n_items,
+                                                int forward, int sweep) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const int64_t q = it.x;
+  const BlockDev b = P.blocks[it.y];
+  const SolveDev sv = P.solves[b.solve];
+  if (!sv.block || sweep >= sv.sweeps) return;
+  const bool full = sweep > 0 || sv.sweeps > 1;
+  const Gas<T> g = GasOf<T>(sv);
+  const int64_t nq = P.nq;
+  const T thetaInv = (T)(1.0 / sv.theta);
+  T acc[5], in[5], x[5];
+  OffDiagSumBlock(P, g, sv, q, forward != 0, acc);
+  T Ai[kJac];
+#pragma unroll
+  for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
+  if (full) {
+    T other[5];
+    OffDiagSumBlock(P, g, sv, q, forward == 0, other);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const T bv = -thetaInv * P.Rq[v * nq + q];
+      in[v] = forward ? bv + (acc[v] - other[v]) : (bv + other[v]) - acc[v];
+    }
+    MatVec5(Ai, in, x);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
+  } else if (forward) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q] + acc[v];
+    MatVec5(Ai, in, x);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
+  } else {
+    MatVec5(Ai, acc, x);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = P.dUq[v * nq + q] - x[v];
+  }
+}
+
+// x = A^-1 b before the first sweep of multi-sweep solves, 0 otherwise
+template <typename T>
+__global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int n_items) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const int64_t q = it.x, nq = P.nq;
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  T x[5];
+  if (sv.sweeps <= 1) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) x[v] = T(0);
+  } else {
+    const T thetaInv = (T)(1.0 / sv.theta);
+    T in[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q];
+    if (sv.block) {
+      T Ai[kJac];
+#pragma unroll
+      for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
+      MatVec5(Ai, in, x);
+    } else {
+      const T ainv = P.Ainvq[q];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) x[v] = in[v] * ainv;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
 }
 
 template <typename T>
@@ -598,32 +826,61 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
   T *out = P.vflux[D];
 #pragma unroll
   for (int v = 0; v < 5; ++v) out[v * n + c] = F[v] * mag;
+  if (sv.block) {
+    // face state, viscosity and gradient for the block diagonal's
+    // thin-shear-layer Jacobians and the cell-averaged gradients
+    T *vs = P.vst[D];
+    vs[0 * n + c] = fs.rho;
+    vs[1 * n + c] = fs.u;
+    vs[2 * n + c] = fs.v;
+    vs[3 * n + c] = fs.w;
+    vs[4 * n + c] = fs.p;
+    vs[5 * n + c] = muf;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int qv = 0; qv < 3; ++qv) vs[(6 + r * 3 + qv) * n + c] = grad[r][qv];
+  }
 }
 
 // ---------------------------------------------------------------------------
 // logged matrix residual
-template <typename T>
+template <typename T, bool BLOCK>
 __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list,
                                                  const int32_t *cta_block,
                                                  double *mres_partials) {
   __shared__ double s_sum[kCta / 32];
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const SolveDev sv = P.solves[b.solve];
+  if ((sv.block != 0) != BLOCK) return;
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   double sum = 0.0;
   if (c >= 0) {
-    const BlockDev b = P.blocks[cta_block[blockIdx.x]];
-    const SolveDev sv = P.solves[b.solve];
     const Gas<T> g = GasOf<T>(sv);
     const int64_t q = P.qpos[c], nq = P.nq;
-    T L[5], U[5];
-    OffDiagSum(P, g, sv, q, true, L);
-    OffDiagSum(P, g, sv, q, false, U);
+    T L[5], U[5], Ax[5], x[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) x[v] = P.dUq[v * nq + q];
+    if constexpr (BLOCK) {
+      OffDiagSumBlock(P, g, sv, q, true, L);
+      OffDiagSumBlock(P, g, sv, q, false, U);
+      T A[kJac];
+#pragma unroll
+      for (int e = 0; e < kJac; ++e) A[e] = P.Aq[e * nq + q];
+      MatVec5(A, x, Ax);
+    } else {
+      OffDiagSum(P, g, sv, q, true, L);
+      OffDiagSum(P, g, sv, q, false, U);
+      const T a = P.Aq[q];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) Ax[v] = x[v] * a;
+    }
     const T thetaInv = (T)(1.0 / sv.theta);
-    const T a = P.Aq[q];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T off = L[v] - U[v];
       const T bv = -thetaInv * P.Rq[v * nq + q];
-      const T axmb = P.dUq[v * nq + q] * a - off - bv;
+      const T axmb = Ax[v] - off - bv;
       const double r = 0.0 - (double)axmb;
       sum += r * r;
     }
@@ -642,8 +899,10 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
 // ---------------------------------------------------------------------------
 template <typename T>
 void Launch<T>::MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                       double *mres_partials, int ncta, cudaStream_t s) {
-  if (ncta > 0) k_matres<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
+                       double *mres_partials, int ncta, int kinds, cudaStream_t s) {
+  if (ncta <= 0) return;
+  if (kinds & 1) k_matres<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
+  if (kinds & 2) k_matres<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
 }
 template <typename T>
 void Launch<T>::Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
@@ -673,13 +932,25 @@ void Launch<T>::Face(int d, const Pools<T> &P, const int32_t *list,
 }
 template <typename T>
 void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                     int ncta, cudaStream_t s) {
-  if (ncta > 0) k_cell<T><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+                     int ncta, int kinds, cudaStream_t s) {
+  if (ncta <= 0) return;
+  if (kinds & 1) k_cell<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (kinds & 2) k_cell<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
-void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward,
-                      cudaStream_t s) {
-  if (n > 0) k_sweep<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n, forward);
+void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
+                      bool full, int kinds, cudaStream_t s) {
+  if (n <= 0) return;
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (kinds & 1) {
+    if (full) k_sweep<T, true><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweep<T, false><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
+  }
+  if (kinds & 2) k_sweepb<T><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
+}
+template <typename T>
+void Launch<T>::Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {
+  if (n > 0) k_init<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n);
 }
 template <typename T>
 void Launch<T>::ConnDu(const Pools<T> &P, cudaStream_t s) {

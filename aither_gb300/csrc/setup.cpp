@@ -1025,9 +1025,8 @@ void AppendInput(Setup &st, const std::string &path) {
   const auto ms = get("matrixSolver", "lusgs");
   ph.solver = ms == "lusgs" ? ATH_SOLVER_LUSGS : ms == "blusgs" ? ATH_SOLVER_BLUSGS
               : (Fail("unsupported matrixSolver " + ms), 0);
-  if (ph.solver != ATH_SOLVER_LUSGS) Fail("only matrixSolver lusgs is supported");
   ph.sweeps = (int)getd("matrixSweeps", 1);
-  if (ph.sweeps != 1) Fail("only matrixSweeps 1 is supported");
+  if (ph.sweeps < 1) Fail("matrixSweeps must be at least 1");
   ph.relax = getd("matrixRelaxation", 1.0);
   ph.cfl_start = getd("cflStart", 1.0);
   ph.cfl_step = getd("cflStep", 0.0);

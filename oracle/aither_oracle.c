@@ -27,6 +27,8 @@ typedef struct {
   double *R;           /* [nc][5] */
   double *dU;          /* [nc][5] */
   double *lam, *dt, *A, *Ainv; /* [nc] */
+  double *Ab, *Ainvb;  /* [nc][25] block diagonal and its inverse (blusgs) */
+  double *vg;          /* [nc][9] cell-averaged velocity gradient (blusgs) */
   uint8_t *mask;
   double *center;      /* [3][nc] */
   double *T, *mu;      /* [nc] temperature, laminar viscosity (aux) */
@@ -45,6 +47,8 @@ typedef struct {
   gas_t gas;
   double cfl;
   int viscous;
+  int block;   /* blusgs: 5x5 Jacobian diagonal and off-diagonals */
+  int sweeps;  /* matrixSweeps */
 } osolve;
 
 struct orc_case {
@@ -526,6 +530,184 @@ static void apply_edge_ops(oblock *b, int n, const ath_ghost_op *ops) {
  * CalcGradsI/J/K (:5173,5378,5584), VectorGradGG/ScalarGradGG
  * (src/utility.cpp:59,138), viscousFlux::CalcFlux (src/viscousFlux.cpp:58),
  * TauNormal (src/utility.cpp:426); laminar */
+/* ------------------------------------------------ block implicit operator */
+/* 5x5 matrices are row-major, m[r * 5 + c] (fluxJacobian flow part with
+ * one species and no turbulence equations, include/fluxJacobian.hpp:92). */
+#define NJAC (NV * NV)
+
+/* fluxJacobian::InvFluxJacobian (include/fluxJacobian.hpp:432): convective
+ * flux Jacobian along the unit normal n, times 0.5|A| */
+static void inv_flux_jac(const double *w, const gas_t *g, const double *n, double mag,
+                         double *J) {
+  const double velNorm = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  const double mf = w[0] / w[0];
+  const double gamma = gamma_of(g);
+  const double gm1 = gamma - 1.0;
+  const double phi = 0.5 * gm1 * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  const double a1 = gamma * energy_of(w, g) - phi;
+  const double a3 = gamma - 2.0;
+  for (int e = 0; e < NJAC; ++e) J[e] = 0.0;
+  J[0 * 5 + 0] = velNorm * (1.0 - mf);
+  J[0 * 5 + 1] = mf * n[0];
+  J[0 * 5 + 2] = mf * n[1];
+  J[0 * 5 + 3] = mf * n[2];
+  J[1 * 5 + 0] = phi * n[0] - w[1] * velNorm;
+  J[2 * 5 + 0] = phi * n[1] - w[2] * velNorm;
+  J[3 * 5 + 0] = phi * n[2] - w[3] * velNorm;
+  J[4 * 5 + 0] = velNorm * (phi - a1);
+  J[1 * 5 + 1] = velNorm - a3 * n[0] * w[1];
+  J[2 * 5 + 1] = w[2] * n[0] - gm1 * w[1] * n[1];
+  J[3 * 5 + 1] = w[3] * n[0] - gm1 * w[1] * n[2];
+  J[4 * 5 + 1] = a1 * n[0] - gm1 * w[1] * velNorm;
+  J[1 * 5 + 2] = w[1] * n[1] - gm1 * w[2] * n[0];
+  J[2 * 5 + 2] = velNorm - a3 * n[1] * w[2];
+  J[3 * 5 + 2] = w[3] * n[1] - gm1 * w[2] * n[2];
+  J[4 * 5 + 2] = a1 * n[1] - gm1 * w[2] * velNorm;
+  J[1 * 5 + 3] = w[1] * n[2] - gm1 * w[3] * n[0];
+  J[2 * 5 + 3] = w[2] * n[2] - gm1 * w[3] * n[1];
+  J[3 * 5 + 3] = velNorm - a3 * n[2] * w[3];
+  J[4 * 5 + 3] = a1 * n[2] - gm1 * w[3] * velNorm;
+  J[1 * 5 + 4] = gm1 * n[0];
+  J[2 * 5 + 4] = gm1 * n[1];
+  J[3 * 5 + 4] = gm1 * n[2];
+  J[4 * 5 + 4] = gamma * velNorm;
+  const double f = 0.5 * mag;
+  for (int e = 0; e < NJAC; ++e) J[e] *= f;
+}
+
+/* fluxJacobian::RusanovFluxJacobian (include/fluxJacobian.hpp:405):
+ * J = A(W) 0.5|A| +/- lambda_face I */
+static void rusanov_jac(const double *w, const gas_t *g, const double *n, double mag,
+                        int positive, double *J) {
+  const double specRad =
+      0.5 * mag * (fabs(w[1] * n[0] + w[2] * n[1] + w[3] * n[2]) + sos_of(w, g));
+  inv_flux_jac(w, g, n, mag, J);
+  for (int r = 0; r < NV; ++r)
+    for (int cc = 0; cc < NV; ++cc) {
+      const double dis = (r == cc) ? 1.0 * specRad : 0.0;
+      J[r * 5 + cc] = positive ? J[r * 5 + cc] + dis : J[r * 5 + cc] - dis;
+    }
+}
+
+/* fluxJacobian::ApproxTSLJacobian (include/fluxJacobian.hpp:667), laminar,
+ * one species, no diffusion model; vg[r][c] is the velocity gradient
+ * tensor (row = derivative direction, as TauNormal reads it) */
+static void tsl_jac(const double *w, double mu_lam, const gas_t *g, const ath_solve_view *v,
+                    const double *n, double mag, double dist, int left, const double *vg,
+                    double *J) {
+  const double t = temp_of(w, g);
+  const double mu = v->visc_scale * mu_lam;
+  const double mut = v->visc_scale * 0.0;
+  const double velNorm = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  const double rho = w[0];
+  const double k = cond_eff(t, v);
+  const double kt = mut * cp_of(g) / 0.9;
+  /* TauNormal (src/utility.cpp:426) */
+  const double lambda = 0.0 - (2.0 / 3.0) * (mu + mut);
+  const double trace = vg[0] + vg[4] + vg[8];
+  double tau[3];
+  for (int r = 0; r < 3; ++r) {
+    const double sn = (vg[r * 3 + 0] + vg[0 * 3 + r]) * n[0] +
+                      (vg[r * 3 + 1] + vg[1 * 3 + r]) * n[1] +
+                      (vg[r * 3 + 2] + vg[2 * 3 + r]) * n[2];
+    tau[r] = lambda * trace * n[r] + (mu + mut) * sn;
+  }
+  const double fac = left ? -1.0 : 1.0;
+  const double third = 1.0 / 3.0;
+  double T[NJAC];
+  for (int e = 0; e < NJAC; ++e) T[e] = 0.0;
+  /* species row and column: DiffCoeff = 0 (no diffusion model) */
+  const double speciesEnthalpy = 0.0;
+  T[4 * 5 + 0] = -(k + kt) * t / ((mu + mut) * rho) + speciesEnthalpy;
+  T[1 * 5 + 1] = third * n[0] * n[0] + 1.0;
+  T[2 * 5 + 1] = third * n[0] * n[1];
+  T[3 * 5 + 1] = third * n[0] * n[2];
+  T[4 * 5 + 1] = fac * 0.5 * dist / (mu + mut) * tau[0] + third * n[0] * velNorm + w[1];
+  T[1 * 5 + 2] = third * n[1] * n[0];
+  T[2 * 5 + 2] = third * n[1] * n[1] + 1.0;
+  T[3 * 5 + 2] = third * n[1] * n[2];
+  T[4 * 5 + 2] = fac * 0.5 * dist / (mu + mut) * tau[1] + third * n[1] * velNorm + w[2];
+  T[1 * 5 + 3] = third * n[2] * n[0];
+  T[2 * 5 + 3] = third * n[2] * n[1];
+  T[3 * 5 + 3] = third * n[2] * n[2] + 1.0;
+  T[4 * 5 + 3] = fac * 0.5 * dist / (mu + mut) * tau[2] + third * n[2] * velNorm + w[3];
+  T[4 * 5 + 4] = (k + kt) / ((mu + mut) * rho);
+  const double f = mag * (mu + mut) / dist;
+  for (int e = 0; e < NJAC; ++e) T[e] *= f;
+  /* DelprimitiveDelConservative (include/fluxJacobian.hpp:626) */
+  const double gm1 = gamma_of(g) - 1.0;
+  const double invRho = 1.0 / rho;
+  double P[NJAC];
+  for (int e = 0; e < NJAC; ++e) P[e] = 0.0;
+  P[0 * 5 + 0] = 1.0;
+  P[1 * 5 + 0] = -invRho * w[1];
+  P[2 * 5 + 0] = -invRho * w[2];
+  P[3 * 5 + 0] = -invRho * w[3];
+  P[4 * 5 + 0] = 0.5 * gm1 * (w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  P[1 * 5 + 1] = invRho;
+  P[4 * 5 + 1] = -gm1 * w[1];
+  P[2 * 5 + 2] = invRho;
+  P[4 * 5 + 2] = -gm1 * w[2];
+  P[3 * 5 + 3] = invRho;
+  P[4 * 5 + 3] = -gm1 * w[3];
+  P[4 * 5 + 4] = gm1;
+  /* MatrixMultiply (src/matrix.cpp:197): column of the left operand
+   * outermost, accumulated from zero */
+  for (int e = 0; e < NJAC; ++e) J[e] = 0.0;
+  for (int cc = 0; cc < NV; ++cc)
+    for (int r = 0; r < NV; ++r)
+      for (int i = 0; i < NV; ++i) J[r * 5 + i] += T[r * 5 + cc] * P[cc * 5 + i];
+}
+
+/* ArrayMultiplication (include/fluxJacobian.hpp:46): out = M x, each row
+ * accumulated from zero */
+static void mat_vec(const double *M, const double *x, double *out) {
+  for (int r = 0; r < NV; ++r) {
+    double s = 0.0;
+    for (int cc = 0; cc < NV; ++cc) s += M[r * 5 + cc] * x[cc];
+    out[r] = s;
+  }
+}
+
+/* MatrixInverse (src/matrix.cpp:57): Gauss-Jordan with the reference's
+ * pivot search (FindMaxInColumn before the row is reduced) */
+static void mat_inverse(double *a) {
+  double I[NJAC];
+  for (int r = 0; r < NV; ++r)
+    for (int cc = 0; cc < NV; ++cc) I[r * 5 + cc] = (r == cc) ? 1.0 : 0.0;
+  for (int r = 0; r < NV; ++r) {
+    const int cp = r;
+    double maxVal = 0.0;
+    int rp = 0;
+    for (int ii = cp; ii <= NV - 1; ++ii)
+      if (fabs(a[ii * 5 + r]) > maxVal) {
+        maxVal = fabs(a[ii * 5 + r]);
+        rp = ii;
+      }
+    if (rp != r)
+      for (int cc = 0; cc < NV; ++cc) {
+        double t = a[r * 5 + cc]; a[r * 5 + cc] = a[rp * 5 + cc]; a[rp * 5 + cc] = t;
+        t = I[r * 5 + cc]; I[r * 5 + cc] = I[rp * 5 + cc]; I[rp * 5 + cc] = t;
+      }
+    if (r != 0)
+      for (int ii = 0; ii < cp; ++ii) {
+        const double factor = a[r * 5 + ii] / a[ii * 5 + ii];
+        for (int cc = 0; cc < NV; ++cc) a[r * 5 + cc] = a[r * 5 + cc] - factor * a[ii * 5 + cc];
+        for (int cc = 0; cc < NV; ++cc) I[r * 5 + cc] = I[r * 5 + cc] - factor * I[ii * 5 + cc];
+      }
+    const double normFactor = 1.0 / a[r * 5 + cp];
+    for (int cc = cp; cc < NV; ++cc) a[r * 5 + cc] *= normFactor;
+    for (int cc = 0; cc < NV; ++cc) I[r * 5 + cc] *= normFactor;
+  }
+  for (int cp = NV - 2, r = NV - 2; r >= 0; --r, --cp)
+    for (int ii = NV - 1; ii > cp; --ii) {
+      const double factor = a[r * 5 + ii];
+      for (int cc = 0; cc < NV; ++cc) a[r * 5 + cc] = a[r * 5 + cc] - factor * a[ii * 5 + cc];
+      for (int cc = 0; cc < NV; ++cc) I[r * 5 + cc] = I[r * 5 + cc] - factor * I[ii * 5 + cc];
+    }
+  memcpy(a, I, sizeof(I));
+}
+
 static void viscous_fluxes(orc_case *c, oblock *b) {
   const osolve *sv = &c->s[b->solve];
   const ath_solve_view *v = &sv->v;
@@ -629,10 +811,29 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           F[3] = tau[2];
           F[4] = (tau[0] * fs[1] + tau[1] * fs[2] + tau[2] * fs[3]) +
                  (kk_ + kt) * (tg[0] * n[0] + tg[1] * n[1] + tg[2] * n[2]) + 0.0;
-          if (fpos > 0)
+          /* block diagonal: ApproxTSLJacobian at the face with the face
+           * state, viscosity and gradient, ProjC2CDist as the length; cell
+           * gradients: one sixth of each face gradient */
+          double c2c = 0.0, Jt[NJAC];
+          const double sixth = 1.0 / 6.0;
+          if (sv->block) {
+            const double dc[3] = {b->center[cu] - b->center[cl],
+                                  b->center[b->nc + cu] - b->center[b->nc + cl],
+                                  b->center[2 * b->nc + cu] - b->center[2 * b->nc + cl]};
+            c2c = dc[0] * n[0] + dc[1] * n[1] + dc[2] * n[2];
+          }
+          if (fpos > 0) {
             for (int q = 0; q < NV; ++q) b->R[cl * NV + q] -= F[q] * mag;
+            if (sv->block) {
+              for (int e = 0; e < 9; ++e) b->vg[cl * 9 + e] += sixth * grad[e / 3][e % 3];
+              tsl_jac(fs, muf, g, v, n, mag, c2c, 1, &grad[0][0], Jt);
+              for (int e = 0; e < NJAC; ++e) b->Ab[cl * NJAC + e] -= Jt[e];
+            }
+          }
           if (fpos < nd) {
             for (int q = 0; q < NV; ++q) b->R[cu * NV + q] += F[q] * mag;
+            if (sv->block)
+              for (int e = 0; e < 9; ++e) b->vg[cu * 9 + e] += sixth * grad[e / 3][e % 3];
             double nl[3], ml, nh[3], mh;
             face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
             face_normal(b, d, face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
@@ -641,7 +842,12 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
             const double lv = visc_max_term(Wc, g) * visc_term(b->mu[cu], v, g) * fMag * fMag /
                               b->vol[cu];
             b->lam[cu] += lv * coeff;
-            b->A[cu] += 2.0 * lv;
+            if (sv->block) {
+              tsl_jac(fs, muf, g, v, n, mag, c2c, 0, &grad[0][0], Jt);
+              for (int e = 0; e < NJAC; ++e) b->Ab[cu * NJAC + e] += Jt[e];
+            } else {
+              b->A[cu] += 2.0 * lv;
+            }
           }
         }
   }
@@ -664,6 +870,8 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     c->s[s].gas.n = sv[s].gas_n;
     c->s[s].gas.hf = sv[s].gas_hf;
     c->s[s].viscous = sv[s].eqn != ATH_EQN_EULER;
+    c->s[s].block = sv[s].solver == ATH_SOLVER_BLUSGS;
+    c->s[s].sweeps = sv[s].sweeps > 0 ? sv[s].sweeps : 1;
   }
   for (int bi = 0; bi < nblocks; ++bi) {
     const ath_block_view *v = &bv[bi];
@@ -685,6 +893,11 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     b->dt = (double *)dup_arr(NULL, 8 * b->nc);
     b->A = (double *)dup_arr(NULL, 8 * b->nc);
     b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
+    if (c->s[b->solve].block) {
+      b->Ab = (double *)dup_arr(NULL, 8 * NJAC * b->nc);
+      b->Ainvb = (double *)dup_arr(NULL, 8 * NJAC * b->nc);
+      b->vg = (double *)dup_arr(NULL, 8 * 9 * b->nc);
+    }
     b->mask = (uint8_t *)dup_arr(v->nbr_mask, b->nc);
     b->center = (double *)dup_arr(v->center, 8 * 3 * b->nc);
     b->T = (double *)dup_arr(NULL, 8 * b->nc);
@@ -721,6 +934,7 @@ void orc_destroy(orc_case *c) {
     free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
+    free(b->Ab); free(b->Ainvb); free(b->vg);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
@@ -848,6 +1062,10 @@ void orc_residual(orc_case *c) {
     memset(b->R, 0, 8 * NV * b->nc);
     memset(b->lam, 0, 8 * b->nc);
     memset(b->A, 0, 8 * b->nc);
+    if (sv->block) {
+      memset(b->Ab, 0, 8 * NJAC * b->nc);
+      memset(b->vg, 0, 8 * 9 * b->nc);
+    }
     for (int d = 0; d < 3; ++d) {
       const int ei = b->ni + (d == 0), ej = b->nj + (d == 1), ek = b->nk + (d == 2);
       const int nd = d == 0 ? b->ni : (d == 1 ? b->nj : b->nk);
@@ -886,8 +1104,14 @@ void orc_residual(orc_case *c) {
               ausm_flux(fL, fR, g, n, f);
             else
               roe_flux(fL, fR, g, n, f);
-            if (fpos > 0)
+            double J[NJAC];
+            if (fpos > 0) {
               for (int v = 0; v < NV; ++v) b->R[cl * NV + v] += f[v] * mag;
+              if (sv->block) {
+                rusanov_jac(fL, g, n, mag, 1, J);
+                for (int e = 0; e < NJAC; ++e) b->Ab[cl * NJAC + e] += J[e];
+              }
+            }
             if (fpos < nd) {
               for (int v = 0; v < NV; ++v) b->R[cu * NV + v] -= f[v] * mag;
               double nl[3], ml, nh[3], mh;
@@ -896,7 +1120,12 @@ void orc_residual(orc_case *c) {
                           face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
               const double lam = inv_cell_specrad(w0, g, nl, ml, nh, mh);
               b->lam[cu] += lam;
-              b->A[cu] += lam;
+              if (sv->block) {
+                rusanov_jac(fR, g, n, mag, 0, J);
+                for (int e = 0; e < NJAC; ++e) b->Ab[cu * NJAC + e] -= J[e];
+              } else {
+                b->A[cu] += lam;
+              }
             }
           }
     }
@@ -918,6 +1147,17 @@ void orc_residual(orc_case *c) {
       viscous_fluxes(c, b);
     }
   }
+  /* SwapEddyViscAndGradients (src/gridLevel.cpp:343): cell gradients of
+   * the connection ghosts from the partner block */
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    if (!c->s[b->solve].block) continue;
+    for (int o = 0; o < b->nops; ++o) {
+      const ath_ghost_op *op = &b->ops[o];
+      if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) continue;
+      memcpy(&b->vg[op->dst * 9], &c->b[op->src_block].vg[op->src * 9], 8 * 9);
+    }
+  }
 }
 
 /* procBlock::CalcBlockTimeStep / CalcCellDt (src/procBlock.cpp:782,798) */
@@ -937,7 +1177,7 @@ void orc_timestep(orc_case *c) {
 }
 
 /* linearSolver::AddDiagonalTerms / Invert (src/linearSolver.cpp:146,177),
- * scalar diagonal */
+ * scalar diagonal or 5x5 block (MatrixInverse, src/matrix.cpp:57) */
 void orc_diag_invert(orc_case *c) {
   NTH
   PAR_BLOCKS
@@ -949,6 +1189,14 @@ void orc_diag_invert(orc_case *c) {
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
           const double diagVolTime = (b->vol[x] * (1.0 + v->zeta)) / (b->dt[x] * v->theta);
+          if (c->s[b->solve].block) {
+            double *a = &b->Ab[x * NJAC];
+            for (int r = 0; r < NV; ++r) a[r * 5 + r] *= v->relax;
+            for (int r = 0; r < NV; ++r) a[r * 5 + r] += diagVolTime;
+            memcpy(&b->Ainvb[x * NJAC], a, 8 * NJAC);
+            mat_inverse(&b->Ainvb[x * NJAC]);
+            continue;
+          }
           b->A[x] *= v->relax;
           b->A[x] += diagVolTime;
           b->Ainv[x] = 1.0 / b->A[x];
@@ -975,8 +1223,9 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
     const int fk = (int)kk - b->ng + (!lower && d == 2);
     double n[3], mag, o[NV];
     face_normal(b, d, face_idx(b, d, fi, fj, fk), n, &mag);
-    double vsr = 0.0;
+    double vsr = 0.0, dist = 0.0;
     const osolve *sv = &c->s[b->solve];
+    const double *wn = &b->W[nb * NV];
     if (sv->viscous) {
       /* ProjC2CDist (src/procBlock.cpp:6316): centre of the cell above the
        * face minus the one below, along the face normal */
@@ -984,11 +1233,22 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
       const double dc[3] = {b->center[up] - b->center[lo],
                             b->center[b->nc + up] - b->center[b->nc + lo],
                             b->center[2 * b->nc + up] - b->center[2 * b->nc + lo]};
-      const double dist = dc[0] * n[0] + dc[1] * n[1] + dc[2] * n[2];
-      const double *wn = &b->W[nb * NV];
+      dist = dc[0] * n[0] + dc[1] * n[1] + dc[2] * n[2];
       vsr = mag / dist * visc_max_term(wn, g) * visc_term(b->mu[nb], &sv->v, g);
     }
-    scalar_offdiag(&b->W[nb * NV], &b->dU[nb * NV], g, n, mag, lower, vsr, o);
+    if (sv->block) {
+      /* RusanovBlockOffDiagonal (src/fluxJacobian.cpp:164) */
+      double J[NJAC];
+      rusanov_jac(wn, g, n, mag, lower, J);
+      if (sv->viscous) {
+        double Tj[NJAC];
+        tsl_jac(wn, b->mu[nb], g, &sv->v, n, mag, dist, lower, &b->vg[nb * 9], Tj);
+        for (int e = 0; e < NJAC; ++e) J[e] = lower ? J[e] - Tj[e] : J[e] + Tj[e];
+      }
+      mat_vec(J, &b->dU[nb * NV], o);
+    } else {
+      scalar_offdiag(wn, &b->dU[nb * NV], g, n, mag, lower, vsr, o);
+    }
     for (int v = 0; v < NV; ++v) acc[v] += o[v];
   }
 }
@@ -1016,6 +1276,7 @@ static void matrix_residual(orc_case *c) {
       oblock *b = &c->b[bi];
       if (b->solve != s) continue;
       const double thetaInv = 1.0 / c->s[s].v.theta;
+      double bsum = 0.0; /* std::accumulate per block (src/mgSolution.cpp:199-203) */
       for (int k = 0; k < b->nk; ++k)
         for (int j = 0; j < b->nj; ++j)
           for (int i = 0; i < b->ni; ++i) {
@@ -1023,14 +1284,18 @@ static void matrix_residual(orc_case *c) {
             double L[NV], U[NV];
             offdiag_sum(c, b, x, 1, L);
             offdiag_sum(c, b, x, 0, U);
+            double Ax[NV];
+            if (c->s[s].block) mat_vec(&b->Ab[x * NJAC], &b->dU[x * NV], Ax);
             for (int v = 0; v < NV; ++v) {
               const double off = L[v] - U[v];
               const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
-              const double axmb = b->dU[x * NV + v] * b->A[x] - off - bb;
+              const double ax = c->s[s].block ? Ax[v] : b->dU[x * NV + v] * b->A[x];
+              const double axmb = ax - off - bb;
               const double r = 0.0 - axmb;
-              sum += r * r;
+              bsum += r * r;
             }
           }
+      sum += bsum;
       padded += (double)b->nc * NV;
       cells += (double)b->ni * b->nj * b->nk;
     }
@@ -1038,39 +1303,91 @@ static void matrix_residual(orc_case *c) {
   }
 }
 
-/* lusgs::Relax with one sweep and no initialisation (src/linearSolver.cpp:
- * 430, LUSGS_Forward :341, LUSGS_Backward :385) */
+/* x = A^-1 v: scalar (orig * A^-1) or 5x5 block (ArrayMultiplication) */
+static void apply_ainv(const orc_case *c, const oblock *b, int64_t x, const double *in,
+                       double *out) {
+  if (c->s[b->solve].block) {
+    mat_vec(&b->Ainvb[x * NJAC], in, out);
+  } else {
+    for (int v = 0; v < NV; ++v) out[v] = in[v] * b->Ainv[x];
+  }
+}
+
+/* lusgs::Relax (src/linearSolver.cpp:430) with LUSGS_Forward :341 and
+ * LUSGS_Backward :385: matrixSweeps sweeps; with more than one sweep the
+ * update starts from A^-1 b (InitializeMatrixUpdate :111) and every sweep
+ * uses both triangles, otherwise from zero with one triangle per pass */
 void orc_relax(orc_case *c) {
-  for (int bi = 0; bi < c->nb; ++bi) memset(c->b[bi].dU, 0, 8 * NV * c->b[bi].nc);
-  swap_du(c);
   NTH
+  int maxsw = 1;
+  for (int s = 0; s < c->ns; ++s) maxsw = c->s[s].sweeps > maxsw ? c->s[s].sweeps : maxsw;
   PAR_BLOCKS
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
-    const double thetaInv = 1.0 / c->s[b->solve].v.theta;
-    const int ncell = b->ni * b->nj * b->nk;
-    for (int q = 0; q < ncell; ++q) {
-      const int64_t x = b->plane_cells[q];
-      double L[NV];
-      offdiag_sum(c, b, x, 1, L);
-      for (int v = 0; v < NV; ++v) {
-        const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
-        b->dU[x * NV + v] = (bb + L[v]) * b->Ainv[x];
+    const osolve *sv = &c->s[b->solve];
+    if (sv->sweeps <= 1) {
+      memset(b->dU, 0, 8 * NV * b->nc);
+      continue;
+    }
+    const double thetaInv = 1.0 / sv->v.theta;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          double in[NV];
+          for (int v = 0; v < NV; ++v) in[v] = -thetaInv * b->R[x * NV + v] + 0.0 - 0.0;
+          apply_ainv(c, b, x, in, &b->dU[x * NV]);
+        }
+  }
+  for (int sw = 0; sw < maxsw; ++sw) {
+    swap_du(c);
+    PAR_BLOCKS
+    for (int bi = 0; bi < c->nb; ++bi) {
+      oblock *b = &c->b[bi];
+      const osolve *sv = &c->s[b->solve];
+      if (sw >= sv->sweeps) continue;
+      const int full = sw > 0 || sv->sweeps > 1;
+      const double thetaInv = 1.0 / sv->v.theta;
+      const int ncell = b->ni * b->nj * b->nk;
+      for (int q = 0; q < ncell; ++q) {
+        const int64_t x = b->plane_cells[q];
+        double L[NV], U[NV], in[NV];
+        offdiag_sum(c, b, x, 1, L);
+        if (full) {
+          offdiag_sum(c, b, x, 0, U);
+          for (int v = 0; v < NV; ++v) L[v] -= U[v];
+        }
+        for (int v = 0; v < NV; ++v) {
+          const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+          in[v] = bb + L[v];
+        }
+        apply_ainv(c, b, x, in, &b->dU[x * NV]);
       }
     }
-  }
-  swap_du(c);
-  PAR_BLOCKS
-  for (int bi = 0; bi < c->nb; ++bi) {
-    oblock *b = &c->b[bi];
-    const int ncell = b->ni * b->nj * b->nk;
-    for (int q = ncell - 1; q >= 0; --q) {
-      const int64_t x = b->plane_cells[q];
-      double U[NV];
-      offdiag_sum(c, b, x, 0, U);
-      for (int v = 0; v < NV; ++v) {
-        const double xold = b->dU[x * NV + v];
-        b->dU[x * NV + v] = xold - U[v] * b->Ainv[x];
+    swap_du(c);
+    PAR_BLOCKS
+    for (int bi = 0; bi < c->nb; ++bi) {
+      oblock *b = &c->b[bi];
+      const osolve *sv = &c->s[b->solve];
+      if (sw >= sv->sweeps) continue;
+      const int full = sw > 0 || sv->sweeps > 1;
+      const double thetaInv = 1.0 / sv->v.theta;
+      const int ncell = b->ni * b->nj * b->nk;
+      for (int q = ncell - 1; q >= 0; --q) {
+        const int64_t x = b->plane_cells[q];
+        double U[NV], L[NV], in[NV], t[NV];
+        offdiag_sum(c, b, x, 0, U);
+        if (full) {
+          offdiag_sum(c, b, x, 1, L);
+          for (int v = 0; v < NV; ++v) {
+            const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+            in[v] = bb + L[v] - U[v];
+          }
+          apply_ainv(c, b, x, in, &b->dU[x * NV]);
+        } else {
+          apply_ainv(c, b, x, U, t);
+          for (int v = 0; v < NV; ++v) b->dU[x * NV + v] = b->dU[x * NV + v] - t[v];
+        }
       }
     }
   }

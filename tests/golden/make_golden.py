@@ -53,6 +53,20 @@ CASES = [
     ("bump_vanalbada_ausm", cases.bump_channel,
      dict(ni=22, nj=11, nk=3, height=0.09, mach=0.75, limiter="vanAlbada", flux="ausm"),
      [1, 20], True),
+    # block LU-SGS (blusgs) and multi-sweep relaxation
+    ("bump_blusgs", cases.bump_channel,
+     dict(ni=20, nj=10, nk=3, height=0.08, mach=0.7, matrix_solver="blusgs"), [1, 20], True),
+    ("bump_sweeps3", cases.bump_channel,
+     dict(ni=18, nj=9, nk=3, height=0.06, mach=0.6, sweeps=3), [1, 20], True),
+    ("bump_blusgs_weno_sw2", cases.bump_channel,
+     dict(ni=16, nj=8, nk=4, height=0.07, mach=0.8, recon="weno", limiter="none",
+          matrix_solver="blusgs", sweeps=2), [1, 20], True),
+    ("plate_blusgs", cases.flat_plate,
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, matrix_solver="blusgs"), [1, 20], True),
+    ("plate_blusgs_sw2", cases.flat_plate,
+     dict(ni=10, nj=8, nk=2, dy0=5e-4, ratio=1.35, wall_t=300.0, mach=0.5,
+          matrix_solver="blusgs", sweeps=2), [1, 20], True),
+    ("plate_c2b", cases.flat_plate, dict(matrix_solver="blusgs", sweeps=4), [20], False),
 ]
 
 
@@ -91,6 +105,7 @@ def run_case(name, gen, kw, niter, full, ref_dir):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="fixture base names to (re)generate")
     a = ap.parse_args()
     if not os.path.exists(HARNESS):
         sys.path.insert(0, ROOT)
@@ -99,6 +114,8 @@ def main():
         build.REF_SRC = a.reference
         build.build_reference()
     for name, gen, kw, iters, full in CASES:
+        if a.only and name not in a.only:
+            continue
         for n in iters:
             run_case(name, gen, kw, n, full, a.reference)
 

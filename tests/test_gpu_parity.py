@@ -48,7 +48,11 @@ def _l2(norms, nsolves=1, solve=0):
                                   "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
                                   "bump_vanalbada_ausm_it20", "plate_adiabatic_it1",
                                   "plate_adiabatic_it20", "plate_isothermal_it1",
-                                  "plate_isothermal_it20"])
+                                  "plate_isothermal_it20", "bump_blusgs_it1",
+                                  "bump_blusgs_it20", "bump_sweeps3_it1", "bump_sweeps3_it20",
+                                  "bump_blusgs_weno_sw2_it1", "bump_blusgs_weno_sw2_it20",
+                                  "plate_blusgs_it1", "plate_blusgs_it20",
+                                  "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
@@ -67,7 +71,9 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     b.close()
 
 
-@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40"])
+@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
+                                  "bump_blusgs_it20", "bump_sweeps3_it20",
+                                  "plate_blusgs_sw2_it20"])
 def test_fp64_matrix_residual(ctx, name, tmp_path):
     """flags bit 0: the logged matrix residual of every iteration; it is a
     log-only quantity, so the solution is unchanged."""
@@ -84,10 +90,12 @@ def test_fp64_matrix_residual(ctx, name, tmp_path):
     b.close()
 
 
-def test_fp64_laminar_plate_two_blocks(ctx, tmp_path):
-    """Laminar flat plate, two 128x64x2 blocks with an interblock connection:
-    20 iterations against the reference's L2 history and state statistics."""
-    inp, st, g = golden_case("plate_c2_it20", str(tmp_path))
+@pytest.mark.parametrize("name", ["plate_c2_it20", "plate_c2b_it20"])
+def test_fp64_laminar_plate_two_blocks(ctx, name, tmp_path):
+    """Laminar flat plate, two 128x64x2 blocks with an interblock connection,
+    scalar LU-SGS (plate_c2) and block LU-SGS with 4 sweeps (plate_c2b): 20
+    iterations against the reference's L2 history and state statistics."""
+    inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
     norms = b.iterate(20)
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL

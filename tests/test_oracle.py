@@ -18,7 +18,10 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "bump_sup_it1", "bump_sup_it40", "bump_weno_it1", "bump_weno_it20",
         "bump_wenoz_ausm_it1", "bump_wenoz_ausm_it20", "bump_const_ausm_it20",
         "bump_vanalbada_ausm_it20", "plate_adiabatic_it1", "plate_adiabatic_it20",
-        "plate_isothermal_it1", "plate_isothermal_it20"]
+        "plate_isothermal_it1", "plate_isothermal_it20", "bump_blusgs_it1", "bump_blusgs_it20",
+        "bump_sweeps3_it1", "bump_sweeps3_it20", "bump_blusgs_weno_sw2_it1",
+        "bump_blusgs_weno_sw2_it20", "plate_blusgs_it1", "plate_blusgs_it20",
+        "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20"]
 
 
 def _oracle(inp, st):
@@ -46,7 +49,9 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
     assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
 
 
-@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40"])
+@pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
+                                  "bump_blusgs_it20", "bump_sweeps3_it20",
+                                  "plate_blusgs_sw2_it20"])
 def test_oracle_matrix_residual(name, tmp_path):
     """The logged linear-system residual (linearSolver::Residual)."""
     from aither_gb300 import Setup
@@ -72,11 +77,13 @@ def test_oracle_full_vortex_box_200_iterations(tmp_path):
     assert rel_err(w[::3, ::7, ::11], g["b0_state_samples"]) <= 1e-12
 
 
-def test_oracle_laminar_plate_two_blocks(tmp_path):
+@pytest.mark.parametrize("name", ["plate_c2_it20", "plate_c2b_it20"])
+def test_oracle_laminar_plate_two_blocks(name, tmp_path):
     """Two 128x64x2 blocks joined by an interblock connection, laminar
     Navier-Stokes at Re_L = 1e5 on a wall-normal geometric grid (first cell
-    1e-5, ratio 1.08): 20 iterations against the reference."""
-    inp, st, g = golden_case("plate_c2_it20", str(tmp_path))
+    1e-5, ratio 1.08), scalar LU-SGS and 4-sweep block LU-SGS: 20 iterations
+    against the reference."""
+    inp, st, g = golden_case(name, str(tmp_path))
     _, o = _oracle(inp, st)
     l2 = o.iterate(20)
     assert rel_err(l2[:, 0, :], g["l2"]) <= 1e-12
