@@ -78,7 +78,14 @@ class Norms(C.Structure):
     _fields_ = [("l2", C.c_double * 7), ("linf", C.c_double),
                 ("linf_block", C.c_int32), ("linf_i", C.c_int32), ("linf_j", C.c_int32),
                 ("linf_k", C.c_int32), ("linf_eqn", C.c_int32),
-                ("matrix_resid", C.c_double), ("cfl", C.c_double), ("status", C.c_int32)]
+                ("matrix_resid", C.c_double), ("cfl", C.c_double), ("status", C.c_int32),
+                ("force", C.c_double * 6)]
+
+
+class ConvergeInfo(C.Structure):
+    """ath_converge_info: per-solve record of a run to convergence."""
+    _fields_ = [("iterations", C.c_int64), ("drop", C.c_double), ("ms", C.c_double),
+                ("converged", C.c_int32), ("pad", C.c_int32)]
 
 
 class BlockDev(C.Structure):
@@ -132,6 +139,10 @@ def lib() -> C.CDLL:
             "ath_batch_pool_cells": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "ath_batch_copy_state": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
             "ath_batch_profile": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_batch_converge": (C.c_int, [vp, C.c_int, C.c_double, C.c_int,
+                                             C.POINTER(ConvergeInfo)]),
+            "ath_batch_set_target": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
+            "ath_batch_solve_info": (C.c_int, [vp, C.POINTER(ConvergeInfo)]),
             "ath_block_residual_noalloc": (C.c_int, [C.POINTER(BlockDev), C.POINTER(SolveView),
                                                      C.c_double, vp]),
         }
@@ -261,6 +272,21 @@ class Batch:
         norms = (Norms * (n * self.nsolves))()
         check(lib().ath_batch_iterate(self.h, n, norms))
         return norms
+
+    def converge(self, max_iters: int, drop: float, check_every: int = 50):
+        """Iterates until every solve has retired (total L2 drop reached or
+        nonphysical state) or max_iters; returns per-solve ConvergeInfo."""
+        info = (ConvergeInfo * self.nsolves)()
+        check(lib().ath_batch_converge(self.h, max_iters, drop, check_every, info))
+        return info
+
+    def set_target(self, solve: int, drop: float, active: bool = True) -> None:
+        check(lib().ath_batch_set_target(self.h, solve, drop, 1 if active else 0))
+
+    def solve_info(self):
+        info = (ConvergeInfo * self.nsolves)()
+        check(lib().ath_batch_solve_info(self.h, info))
+        return info
 
     def stage(self, name: str, norms=None):
         f = getattr(lib(), "ath_batch_" + name)

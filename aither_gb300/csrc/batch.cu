@@ -87,6 +87,9 @@ struct Lists {
   std::vector<GhostOpDev> edge_ops, vops, vedge_ops;
   std::vector<int32_t> edge_solve, vop_solve, vedge_solve;
   std::vector<int32_t> edge_phase_off, vedge_phase_off;
+  // viscous-wall faces, ordered by solve, and each solve's first entry
+  std::vector<WallFaceDev> wall_faces;
+  std::vector<int32_t> solve_face0;
   // cells whose laminar viscosity is needed (viscous blocks, all but corners)
   std::vector<int32_t> aux_cells, aux_block;
   bool any_viscous = false;
@@ -124,7 +127,13 @@ struct BatchCore {
   int32_t *d_op_solve = nullptr;
   NormPartial *d_partials = nullptr;
   double *d_mres = nullptr;
+  WallFaceDev *d_wall_faces = nullptr;
+  int32_t *d_solve_face0 = nullptr;
+  double *d_wbuf = nullptr;   // [6][wall faces]
+  double *d_fring = nullptr;  // [ring_cap][nsolves][6] wall forces
   NormOut *d_ring = nullptr;
+  SolveState *d_sstate = nullptr;
+  uint64_t *d_now = nullptr;
   int ring_cap = 1024;
   int64_t *d_iter = nullptr;
   int64_t iter_host = 0;
@@ -137,19 +146,19 @@ struct BatchCore {
   ath_stats stats{};
 };
 
-__global__ void k_cfl(const SolveDev *solves, int nsolves, const int64_t *iter_counter,
+__global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sstate,
                       double *cfl) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsolves) return;
   const SolveDev sv = solves[s];
-  const double it = (double)(*iter_counter);
+  const double it = (double)sstate[s].iter;
   cfl[s] = fmin(sv.cfl_start + it * sv.cfl_step, sv.cfl_max);
 }
 
 __global__ void k_norms(const NormPartial *partials, const double *mres_partials,
                         const int32_t *solve_cta0, int nsolves, NormOut *ring,
-                        int ring_cap, int64_t *iter_counter, const SolveDev *solves,
-                        double *cfl) {
+                        int ring_cap, int64_t *iter_counter, SolveDev *solves,
+                        SolveState *sstate, double *cfl) {
   const int s = blockIdx.x;
   if (s >= nsolves) return;
   const int lane = threadIdx.x;
@@ -185,22 +194,75 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
   const int64_t it = *iter_counter;
   __syncwarp();
   if (lane == 0) {
+    const SolveDev sv = solves[s];
     NormOut o;
     for (int v = 0; v < 7; ++v) o.l2[v] = v < kNv ? sqrt(l2[v]) : 0.0;
     o.linf = mx;
     o.linf_pos = mpos;
-    o.bad = bad;
+    o.bad = sv.active ? bad : 2;
     o.pad = 0;
     o.cfl = cfl[s];
     // src/mgSolution.cpp:196-206 divides by the padded size, src/main.cpp:271
     // by cells x equations
-    const SolveDev sv = solves[s];
     o.matrix_resid = mres_partials ? sqrt((mres / sv.padded_values) / (sv.cells * kNv)) : 0.0;
     ring[(it % ring_cap) * nsolves + s] = o;
+    if (sv.active) {
+      // retirement: the drop of the total L2 against the solve's first
+      // iteration (the reference normalises its residual history by the
+      // first iteration's norms, src/main.cpp:254-271)
+      SolveState &ss = sstate[s];
+      double tot = 0.0;
+      for (int v = 0; v < kNv; ++v) tot += o.l2[v] * o.l2[v];
+      tot = sqrt(tot);
+      uint64_t now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (ss.iter == 0) {
+        ss.l2_first = tot;
+        ss.t_first_ns = now;
+      }
+      ss.iter += 1;
+      ss.l2_last = tot;
+      const bool reached = ss.target > 0.0 && tot <= ss.target * ss.l2_first;
+      if (bad || reached) {
+        solves[s].active = 0;
+        ss.retire_iter = ss.iter;
+        ss.t_retire_ns = now;
+        ss.converged = bad ? -1 : 1;
+      }
+    }
   }
 }
 
 __global__ void k_iter_advance(int64_t *iter_counter) { *iter_counter += 1; }
+
+__global__ void k_clock(uint64_t *out) {
+  uint64_t now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  *out = now;
+}
+
+__global__ void k_wallsum(const double *wbuf, int nfaces, const int32_t *solve_face0,
+                          int nsolves, double *fring, int ring_cap,
+                          const int64_t *iter_counter) {
+  const int s = blockIdx.x;
+  if (s >= nsolves) return;
+  const int lane = threadIdx.x;
+  const int f0 = solve_face0[s], f1 = solve_face0[s + 1];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int f = f0 + lane; f < f1; f += 32)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] += wbuf[(int64_t)q * nfaces + f];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], off);
+  if (lane == 0) {
+    const int64_t it = *iter_counter;
+    double *o = fring + ((it % ring_cap) * nsolves + s) * 6;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) o[q] = acc[q];
+  }
+}
 
 // ---------------------------------------------------------------------------
 class RunnerBase {
@@ -225,7 +287,7 @@ class Runner : public RunnerBase {
     P_.ncell = n;
     P_.W = m.Alloc<double>(5 * n);
     P_.R = m.Alloc<double>(5 * n);
-    for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<T>(5 * n);
+    for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<double>(5 * n);
     if (c.L.any_viscous) {
       for (int d = 0; d < 3; ++d) {
         P_.vflux[d] = m.Alloc<T>(5 * n);
@@ -287,7 +349,7 @@ class Runner : public RunnerBase {
     P_.qpos = m.Upload(c.L.qpos);
     P_.ghost_cell = m.Upload(c.L.ghost_cell);
     P_.ghost_src = m.Upload(c.L.ghost_src);
-    for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(T)), "memset");
+    for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(double)), "memset");
     // geometry and state
     std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
     for (int d = 0; d < 3; ++d) {
@@ -338,8 +400,8 @@ class Runner : public RunnerBase {
   const Pools<T> &P() const { return P_; }
 
   void StartIteration() {
-    k_cfl<<<(c_.nsolves + 127) / 128, 128, 0, c_.stream>>>(c_.d_solves, c_.nsolves, c_.d_iter,
-                                                            c_.d_cfl);
+    k_cfl<<<(c_.nsolves + 127) / 128, 128, 0, c_.stream>>>(c_.d_solves, c_.nsolves,
+                                                            c_.d_sstate, c_.d_cfl);
   }
   void EdgePhases(const GhostOpDev *ops, const int32_t *solve,
                   const std::vector<int32_t> &off) {
@@ -359,6 +421,12 @@ class Runner : public RunnerBase {
     for (int d = 0; d < 3; ++d)
       Launch<T>::ViscFace(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
                           (int)c_.L.face_cta_block[d].size(), c_.stream);
+    const int nw = (int)c_.L.wall_faces.size();
+    if (nw > 0) {
+      Launch<T>::Wall(P_, c_.d_wall_faces, nw, c_.d_wbuf, c_.stream);
+      k_wallsum<<<c_.nsolves, 32, 0, c_.stream>>>(c_.d_wbuf, nw, c_.d_solve_face0, c_.nsolves,
+                                                  c_.d_fring, c_.ring_cap, c_.d_iter);
+    }
   }
   void Residual() override {
     for (int d = 0; d < 3; ++d)
@@ -415,7 +483,7 @@ class Runner : public RunnerBase {
                                               (c_.flags & 1) ? c_.d_mres : nullptr,
                                               c_.d_solve_cta0, c_.nsolves, c_.d_ring,
                                               c_.ring_cap, c_.d_iter, c_.d_solves,
-                                              c_.d_cfl);
+                                              c_.d_sstate, c_.d_cfl);
     k_iter_advance<<<1, 1, 0, c_.stream>>>(c_.d_iter);
   }
   void OneIteration() {
@@ -764,6 +832,17 @@ void BuildLists(BatchCore &c) {
   }
   L.edge_phase_off[max_phase] = (int32_t)L.edge_ops.size();
   L.vedge_phase_off[max_phase] = (int32_t)L.vedge_ops.size();
+  L.solve_face0.assign(c.nsolves + 1, 0);
+  for (int s = 0; s < c.nsolves; ++s) {
+    L.solve_face0[s] = (int32_t)L.wall_faces.size();
+    for (int b : st.solves[s].blocks)
+      for (const auto &op : st.blocks[b].vops) {
+        if (op.layer != 1) continue;
+        const GhostOpDev g = convert(b, op);
+        L.wall_faces.push_back(WallFaceDev{g.face, g.dir, b, 0});
+      }
+  }
+  L.solve_face0[c.nsolves] = (int32_t)L.wall_faces.size();
   for (int b = 0; b < c.nblocks; ++b) {
     const Block &bk = st.blocks[b];
     for (const auto &op : bk.vops) {
@@ -839,6 +918,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.visc_coeff = p.visc_cfl_coeff;
     x.block = p.solver == ATH_SOLVER_BLUSGS;
     x.sweeps = p.sweeps;
+    x.active = 1;
     x.padded_values = 0.0;
     x.cells = 0.0;
     for (int b : st.solves[s].blocks) {
@@ -856,6 +936,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_cfl = m.Alloc<double>(c.nsolves);
   c.d_iter = m.Alloc<int64_t>(1);
   Check(cudaMemset(c.d_iter, 0, sizeof(int64_t)), "memset");
+  c.d_now = m.Alloc<uint64_t>(1);
+  c.d_sstate = m.Alloc<SolveState>(c.nsolves);
+  Check(cudaMemset(c.d_sstate, 0, c.nsolves * sizeof(SolveState)), "memset");
   c.d_cells = m.Upload(c.L.cells);
   c.d_cell_cta_block = m.Upload(c.L.cell_cta_block);
   c.d_cell_cta_pos0 = m.Upload(c.L.cell_cta_pos0);
@@ -879,6 +962,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_partials = m.Alloc<NormPartial>(c.L.cell_cta_block.size());
   c.d_mres = m.Alloc<double>(c.L.cell_cta_block.size());
   c.d_ring = m.Alloc<NormOut>((size_t)c.ring_cap * c.nsolves);
+  c.d_wall_faces = m.Upload(c.L.wall_faces);
+  c.d_solve_face0 = m.Upload(c.L.solve_face0);
+  c.d_wbuf = m.Alloc<double>(6 * std::max<size_t>(c.L.wall_faces.size(), 1));
+  c.d_fring = m.Alloc<double>((size_t)c.ring_cap * c.nsolves * 6);
+  Check(cudaMemset(c.d_fring, 0, (size_t)c.ring_cap * c.nsolves * 6 * sizeof(double)),
+        "memset");
   Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
   Check(cudaEventCreate(&c.ev0), "event");
   Check(cudaEventCreate(&c.ev1), "event");
@@ -910,6 +999,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   const int conn = c.L.ghost_cell.empty() ? 0 : 1;
   c.launches_per_iter = edge_phases +
                         (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 : 0) +
+                        (c.L.wall_faces.empty() ? 0 : 2) +
                         1 + (c.L.ops.empty() ? 0 : 1) + 3 + nkinds +
                         2 * c.nsteps * c.max_sweeps * nkinds +
                         (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn) + 3 +
@@ -923,6 +1013,10 @@ void ReadNorms(BatchCore &c, int64_t it0, int n, ath_norms *norms_h) {
   Check(cudaMemcpyAsync(ring.data(), c.d_ring, ring.size() * sizeof(NormOut),
                         cudaMemcpyDeviceToHost, c.stream),
         "norms download");
+  std::vector<double> fring((size_t)c.ring_cap * c.nsolves * 6);
+  Check(cudaMemcpyAsync(fring.data(), c.d_fring, fring.size() * sizeof(double),
+                        cudaMemcpyDeviceToHost, c.stream),
+        "forces download");
   Check(cudaStreamSynchronize(c.stream), "sync");
   const auto &st = *c.setup;
   for (int q = 0; q < n; ++q) {
@@ -935,7 +1029,9 @@ void ReadNorms(BatchCore &c, int64_t it0, int n, ath_norms *norms_h) {
       d.linf = o.linf;
       d.cfl = o.cfl;
       d.matrix_resid = o.matrix_resid;
-      d.status = o.bad ? ATH_ERR_NONPHYSICAL : ATH_OK;
+      d.status = o.bad == 2 ? ATH_RETIRED : o.bad ? ATH_ERR_NONPHYSICAL : ATH_OK;
+      for (int q2 = 0; q2 < 6; ++q2)
+        d.force[q2] = fring[((it % c.ring_cap) * c.nsolves + s) * 6 + q2];
       d.linf_block = d.linf_i = d.linf_j = d.linf_k = d.linf_eqn = -1;
       if (o.linf_pos != INT64_MAX) {
         const int64_t cellpos = o.linf_pos / kNv;
@@ -1035,6 +1131,99 @@ int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h) {
     Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
     c.stats.device_ms = ms;
     c.stats.kernel_launches = (int64_t)n * c.launches_per_iter;
+  });
+}
+
+namespace {
+void SolveInfo(ath::BatchCore &c, ath_converge_info *info) {
+  std::vector<ath::SolveState> ss(c.nsolves);
+  Check(cudaMemcpyAsync(ss.data(), c.d_sstate, ss.size() * sizeof(ath::SolveState),
+                        cudaMemcpyDeviceToHost, c.stream),
+        "solve state download");
+  // device clock now, for solves still running
+  ath::k_clock<<<1, 1, 0, c.stream>>>(c.d_now);
+  uint64_t now = 0;
+  Check(cudaMemcpyAsync(&now, c.d_now, sizeof(now), cudaMemcpyDeviceToHost, c.stream), "clock");
+  Check(cudaStreamSynchronize(c.stream), "sync");
+  for (int s = 0; s < c.nsolves; ++s) {
+    ath_converge_info &o = info[s];
+    const ath::SolveState &x = ss[s];
+    o.iterations = x.iter;
+    o.drop = x.l2_first > 0.0 ? x.l2_last / x.l2_first : 0.0;
+    const uint64_t end = x.converged ? x.t_retire_ns : now;
+    o.ms = x.iter > 0 ? (double)(end - x.t_first_ns) * 1e-6 : 0.0;
+    o.converged = x.converged;
+    o.pad = 0;
+  }
+}
+}  // namespace
+
+int ath_batch_set_target(ath_batch *batch, int solve, double drop, int active) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    auto &c = batch->core;
+    if (solve < 0 || solve >= c.nsolves) throw ath::Error(ATH_ERR_ARG, "solve out of range");
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    Check(cudaMemcpyAsync(&c.d_sstate[solve].target, &drop, sizeof(double),
+                          cudaMemcpyHostToDevice, c.stream),
+          "target upload");
+    const int32_t a = active ? 1 : 0;
+    Check(cudaMemcpyAsync(&c.d_solves[solve].active, &a, sizeof(int32_t),
+                          cudaMemcpyHostToDevice, c.stream),
+          "active upload");
+    if (active) {
+      const int32_t z = 0;
+      Check(cudaMemcpyAsync(&c.d_sstate[solve].converged, &z, sizeof(int32_t),
+                            cudaMemcpyHostToDevice, c.stream),
+            "state upload");
+    }
+    Check(cudaStreamSynchronize(c.stream), "sync");
+  });
+}
+
+int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info) {
+  return Guard([&] {
+    if (!batch || !info) throw ath::Error(ATH_ERR_ARG, "null argument");
+    Check(cudaSetDevice(batch->core.ctx->device), "cudaSetDevice");
+    SolveInfo(batch->core, info);
+  });
+}
+
+int ath_batch_converge(ath_batch *batch, int max_iters, double drop, int check_every,
+                       ath_converge_info *info) {
+  return Guard([&] {
+    if (!batch || max_iters < 0 || !(drop > 0.0) || check_every < 1)
+      throw ath::Error(ATH_ERR_ARG, "bad argument");
+    auto &c = batch->core;
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    for (int s = 0; s < c.nsolves; ++s)
+      Check(cudaMemcpyAsync(&c.d_sstate[s].target, &drop, sizeof(double),
+                            cudaMemcpyHostToDevice, c.stream),
+            "target upload");
+    std::vector<ath::SolveDev> sv(c.nsolves);
+    int done = 0;
+    Check(cudaEventRecord(c.ev0, c.stream), "event");
+    while (done < max_iters) {
+      const int chunk = std::min(max_iters - done, std::min(check_every, c.ring_cap));
+      batch->run->Iterate(chunk);
+      c.iter_host += chunk;
+      done += chunk;
+      Check(cudaMemcpyAsync(sv.data(), c.d_solves, sv.size() * sizeof(ath::SolveDev),
+                            cudaMemcpyDeviceToHost, c.stream),
+            "solve flags download");
+      Check(cudaStreamSynchronize(c.stream), "sync");
+      bool any = false;
+      for (auto &x : sv) any |= x.active != 0;
+      if (!any) break;
+    }
+    Check(cudaEventRecord(c.ev1, c.stream), "event");
+    Check(cudaEventSynchronize(c.ev1), "sync");
+    Check(cudaGetLastError(), "kernel launch");
+    float ms = 0.f;
+    Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
+    c.stats.device_ms = ms;
+    c.stats.kernel_launches = (int64_t)done * c.launches_per_iter;
+    if (info) SolveInfo(c, info);
   });
 }
 

@@ -39,7 +39,7 @@ struct SolveDev {
   int32_t flux;
   int32_t block;   // blusgs: 5x5 Jacobian diagonal and off-diagonals
   int32_t sweeps;  // matrixSweeps
-  int32_t pad2;
+  int32_t active;  // 0 once the solve is retired: its kernels skip their work
 };
 
 // A ghost-cell assignment with pool indices.
@@ -47,6 +47,12 @@ struct GhostOpDev {
   int32_t dst, src, type, lower;
   int32_t face, dir, state, layer;
   int32_t src2, pad;
+};
+
+// A viscous-wall face: pool index of the face (cell above it), direction,
+// block.  Lists are ordered by solve.
+struct WallFaceDev {
+  int32_t face, dir, block, pad;
 };
 
 // Partial norms of one CTA of the update kernel.
@@ -72,7 +78,8 @@ template <typename T>
 struct Pools {
   double *W;        // [5][ncell] primitive state, FP64
   double *R;        // [5][ncell] residual, FP64
-  T *flux[3];       // [5][ncell] F.|A| on faces of direction d
+  double *flux[3];  // [5][ncell] F.|A| on faces of direction d (FP64 in both
+                    // paths: the residual is their FP64 sum)
   T *vflux[3];      // [5][ncell] viscous F.|A| (viscous solves)
   double *mu;       // [ncell] laminar viscosity (viscous solves)
   double *lam;      // [ncell] cell spectral radius
@@ -188,20 +195,39 @@ struct NormOut {
   double cfl;
   double matrix_resid;
 };
+// Per-solve iteration bookkeeping on the device: the solve's own iteration
+// count (it drives the CFL ramp and the residual normalisation), the total
+// L2 norm of its first iteration, its retirement target and record.
+struct SolveState {
+  int64_t iter;          // iterations run by this solve
+  double l2_first;       // total L2 (over the equations) of its first iteration
+  double target;         // retire when total L2 <= target * l2_first (0: never)
+  int64_t retire_iter;   // iterations run when it retired (0: still active)
+  uint64_t t_first_ns;   // device clock at the end of its first iteration
+  uint64_t t_retire_ns;  // device clock at retirement
+  double l2_last;        // total L2 of its last iteration
+  int32_t converged;     // 1 target reached, -1 retired on a nonphysical state
+  int32_t pad;
+};
 __global__ void k_norms(const NormPartial *partials, const double *mres_partials,
                         const int32_t *solve_cta0, int nsolves, NormOut *ring,
-                        int ring_cap, int64_t *iter_counter, const SolveDev *solves,
-                        double *cfl);
+                        int ring_cap, int64_t *iter_counter, SolveDev *solves,
+                        SolveState *sstate, double *cfl);
 
 // Logged matrix residual r = -(A x - (L x - U x) - b) summed as r^2 per CTA
 // (linearSolver::Residual / AXmB, src/linearSolver.cpp:58,92).
 template <typename T, bool BLOCK>
 __global__ void k_matres(Pools<T> P, const int32_t *list, const int32_t *cta_block,
                          double *mres_partials);
-// Sets the CFL of the current iteration from the iteration counter
-// (input::CalcCFL, src/input.cpp:647).
-__global__ void k_cfl(const SolveDev *solves, int nsolves,
-                      const int64_t *iter_counter, double *cfl);
+// Wall forces per solve: fixed-order sum of the per-face values of each
+// solve's range into the forces ring (one warp per solve).
+__global__ void k_wallsum(const double *wbuf, int nfaces, const int32_t *solve_face0,
+                          int nsolves, double *fring, int ring_cap,
+                          const int64_t *iter_counter);
+// Sets the CFL of each solve's current iteration from its own iteration
+// count (input::CalcCFL, src/input.cpp:647).
+__global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sstate,
+                      double *cfl);
 
 // Host-side launchers, one instantiation per arithmetic type (defined in
 // kernels_fp64.cu / kernels_fp32.cu).
@@ -228,6 +254,9 @@ struct Launch {
                      cudaStream_t s);
   static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      double *mres_partials, int ncta, int kinds, cudaStream_t s);
+  // per-face wall forces [6][n] of the viscous-wall faces
+  static void Wall(const Pools<T> &P, const WallFaceDev *faces, int n, double *wbuf,
+                   cudaStream_t s);
 };
 
 }  // namespace ath

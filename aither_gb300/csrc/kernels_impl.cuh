@@ -2,6 +2,8 @@
 // arithmetic type so each is compiled with its own contraction setting.
 #pragma once
 
+#include <type_traits>
+
 #include "block.cuh"
 #include "kernels.cuh"
 
@@ -146,6 +148,108 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 
 // ---------------------------------------------------------------------------
 // face fluxes
+
+// Reconstruction and inviscid flux of face c (direction D) in arithmetic U:
+// f is the flux per unit area, L and R the reconstructed face states.
+template <typename U, int D, typename PT>
+__device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
+                                         int64_t s, U f[5], Prim<U> &L, Prim<U> &R) {
+  const Gas<U> g = GasOf<U>(sv);
+  const int64_t n = P.ncell;
+  const double *wd = P.width[D];
+  const Prim<U> wm1 = LoadW<U>(P.W, n, c - s);
+  const Prim<U> w0 = LoadW<U>(P.W, n, c);
+  if (sv.recon == ATH_RECON_CONSTANT) {
+    L = wm1;
+    R = w0;
+  } else if (sv.recon == ATH_RECON_MUSCL) {
+    const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s);
+    const Prim<U> wp1 = LoadW<U>(P.W, n, c + s);
+    const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
+    const U kappa = (U)sv.kappa;
+    // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
+    L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
+    // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
+    R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+  } else {
+    const Prim<U> wm3 = LoadW<U>(P.W, n, c - 3 * s);
+    const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s);
+    const Prim<U> wp1 = LoadW<U>(P.W, n, c + s);
+    const Prim<U> wp2 = LoadW<U>(P.W, n, c + 2 * s);
+    const bool z = sv.recon == ATH_RECON_WENOZ;
+    const U wl[5] = {(U)wd[c - 3 * s], (U)wd[c - 2 * s], (U)wd[c - s], (U)wd[c],
+                     (U)wd[c + s]};
+    const U wu[5] = {(U)wd[c + 2 * s], (U)wd[c + s], (U)wd[c], (U)wd[c - s],
+                     (U)wd[c - 2 * s]};
+    L = Weno(wm3, wm2, wm1, w0, wp1, wl, z);
+    R = Weno(wp2, wp1, w0, wm1, wm2, wu, z);
+  }
+  const double *fa = P.fa[D];
+  const U nx = (U)fa[c], ny = (U)fa[n + c], nz = (U)fa[2 * n + c];
+  if (sv.flux == ATH_FLUX_AUSM)
+    AusmFlux(L, R, g, nx, ny, nz, f);
+  else
+    RoeFlux(L, R, g, nx, ny, nz, f);
+}
+
+// Mixed-precision Roe/MUSCL face: the face states are the FP64 upwind cell
+// values plus MUSCL increments computed in FP32 from differences formed in
+// FP64; the central part 0.5 (F(L) + F(R)) is FP64 and only the Roe
+// dissipation is FP32, evaluated from the jumps R - L formed in FP64.  The
+// flux's rounding error is then relative to the increments and to the
+// dissipation, not to the flux itself, so the iteration converges to the
+// FP64 fixed point to within that error.
+template <int D, typename PT>
+__device__ __forceinline__ void FaceFluxMixedRoe(const Pools<PT> &P, const SolveDev &sv,
+                                                 int64_t c, int64_t s, double f[5],
+                                                 Prim<double> &L, Prim<double> &R) {
+  const int64_t n = P.ncell;
+  const double *wd = P.width[D];
+  const Prim<double> wm1 = LoadW<double>(P.W, n, c - s);
+  const Prim<double> w0 = LoadW<double>(P.W, n, c);
+  L = wm1;
+  R = w0;
+  if (sv.recon == ATH_RECON_MUSCL) {
+    const Prim<double> wm2 = LoadW<double>(P.W, n, c - 2 * s);
+    const Prim<double> wp1 = LoadW<double>(P.W, n, c + s);
+    const float xm2 = (float)wd[c - 2 * s], xm1 = (float)wd[c - s], x0 = (float)wd[c],
+                xp1 = (float)wd[c + s];
+    const float kappa = (float)sv.kappa;
+    const float dpL = (xm1 + xm1) / (xm1 + x0), dmL = (xm1 + xm1) / (xm1 + xm2);
+    const float dpR = (x0 + x0) / (x0 + xm1), dmR = (x0 + x0) / (x0 + xp1);
+    const double am[5] = {wm2.rho, wm2.u, wm2.v, wm2.w, wm2.p};
+    const double a1[5] = {wm1.rho, wm1.u, wm1.v, wm1.w, wm1.p};
+    const double a0[5] = {w0.rho, w0.u, w0.v, w0.w, w0.p};
+    const double ap[5] = {wp1.rho, wp1.u, wp1.v, wp1.w, wp1.p};
+    double l[5], r[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const float dl = MusclDelta1((float)(a1[v] - am[v]), (float)(a0[v] - a1[v]), dpL, dmL,
+                                   kappa, sv.limiter);
+      const float dr = MusclDelta1((float)(a0[v] - ap[v]), (float)(a1[v] - a0[v]), dpR, dmR,
+                                   kappa, sv.limiter);
+      l[v] = a1[v] + (double)dl;
+      r[v] = a0[v] + (double)dr;
+    }
+    L = Prim<double>{l[0], l[1], l[2], l[3], l[4]};
+    R = Prim<double>{r[0], r[1], r[2], r[3], r[4]};
+  }
+  const double *fa = P.fa[D];
+  const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c];
+  const float dq[5] = {(float)(R.rho - L.rho), (float)(R.u - L.u), (float)(R.v - L.v),
+                       (float)(R.w - L.w), (float)(R.p - L.p)};
+  const Prim<float> Lf{(float)L.rho, (float)L.u, (float)L.v, (float)L.w, (float)L.p};
+  const Prim<float> Rf{(float)R.rho, (float)R.u, (float)R.v, (float)R.w, (float)R.p};
+  float d[5];
+  RoeDissipation(Lf, Rf, dq, GasOf<float>(sv), (float)nx, (float)ny, (float)nz, d);
+  const Gas<double> g = GasOf<double>(sv);
+  double fl[5], fr[5];
+  InvFluxCentral(L, g, nx, ny, nz, fl);
+  InvFluxCentral(R, g, nx, ny, nz, fr);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - (double)d[v])) * 0.5;
+}
+
 template <typename T, int D>
 __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
@@ -153,53 +257,39 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
   if (c < 0) return;
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
-  const Gas<T> g = GasOf<T>(sv);
+  if (!sv.active) return;
   const int64_t n = P.ncell;
   const int64_t s = StrideOf(b, D);
-  const double *wd = P.width[D];
-  const Prim<T> wm1 = LoadW<T>(P.W, n, c - s);
-  const Prim<T> w0 = LoadW<T>(P.W, n, c);
-  Prim<T> L, R;
-  if (sv.recon == ATH_RECON_CONSTANT) {
-    L = wm1;
-    R = w0;
-  } else if (sv.recon == ATH_RECON_MUSCL) {
-    const Prim<T> wm2 = LoadW<T>(P.W, n, c - 2 * s);
-    const Prim<T> wp1 = LoadW<T>(P.W, n, c + s);
-    const T xm2 = (T)wd[c - 2 * s], xm1 = (T)wd[c - s], x0 = (T)wd[c], xp1 = (T)wd[c + s];
-    const T kappa = (T)sv.kappa;
-    // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
-    L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
-    // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
-    R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
-  } else {
-    const Prim<T> wm3 = LoadW<T>(P.W, n, c - 3 * s);
-    const Prim<T> wm2 = LoadW<T>(P.W, n, c - 2 * s);
-    const Prim<T> wp1 = LoadW<T>(P.W, n, c + s);
-    const Prim<T> wp2 = LoadW<T>(P.W, n, c + 2 * s);
-    const bool z = sv.recon == ATH_RECON_WENOZ;
-    const T wl[5] = {(T)wd[c - 3 * s], (T)wd[c - 2 * s], (T)wd[c - s], (T)wd[c],
-                     (T)wd[c + s]};
-    const T wu[5] = {(T)wd[c + 2 * s], (T)wd[c + s], (T)wd[c], (T)wd[c - s],
-                     (T)wd[c - 2 * s]};
-    L = Weno(wm3, wm2, wm1, w0, wp1, wl, z);
-    R = Weno(wp2, wp1, w0, wm1, wm2, wu, z);
-  }
-  const double *fa = P.fa[D];
-  const T nx = (T)fa[c], ny = (T)fa[n + c], nz = (T)fa[2 * n + c],
-          mag = (T)fa[3 * n + c];
-  T f[5];
-  if (sv.flux == ATH_FLUX_AUSM)
-    AusmFlux(L, R, g, nx, ny, nz, f);
-  else
-    RoeFlux(L, R, g, nx, ny, nz, f);
-  T *out = P.flux[D];
+  double *out = P.flux[D];
+  const double mag = P.fa[D][3 * n + c];
+  T lr[10];
+  if constexpr (std::is_same<T, float>::value) {
+    double f[5];
+    Prim<double> L, R;
+    if (sv.flux == ATH_FLUX_ROE &&
+        (sv.recon == ATH_RECON_MUSCL || sv.recon == ATH_RECON_CONSTANT))
+      FaceFluxMixedRoe<D>(P, sv, c, s, f, L, R);
+    else
+      FaceFlux<double, D>(P, sv, c, s, f, L, R);  // AUSM, WENO: FP64 faces
 #pragma unroll
-  for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * mag;
+    for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * mag;
+    const double q[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
+#pragma unroll
+    for (int v = 0; v < 10; ++v) lr[v] = (T)q[v];
+  } else {
+    T f[5];
+    Prim<T> L, R;
+    FaceFlux<T, D>(P, sv, c, s, f, L, R);
+    const T magT = (T)mag;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * magT;
+    const T q[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
+#pragma unroll
+    for (int v = 0; v < 10; ++v) lr[v] = q[v];
+  }
   if (sv.block) {
     // face states for the block diagonal's Rusanov Jacobians
     T *fs = P.fst[D];
-    const T lr[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
 #pragma unroll
     for (int v = 0; v < 10; ++v) fs[v * n + c] = lr[v];
   }
@@ -214,7 +304,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
-  if ((sv.block != 0) != BLOCK) return;
+  if ((sv.block != 0) != BLOCK || !sv.active) return;
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
   const int64_t n = P.ncell;
@@ -227,9 +317,9 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     double r = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const T *F = P.flux[d] + v * n;
-      r = r - (double)F[c];
-      r = r + (double)F[c + st[d]];
+      const double *F = P.flux[d] + v * n;
+      r = r - F[c];
+      r = r + F[c + st[d]];
     }
     if (sv.viscous) {
 #pragma unroll
@@ -478,7 +568,7 @@ __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, in
   const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
-  if (sv.block) return;
+  if (sv.block || !sv.active) return;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   T acc[5];
@@ -524,7 +614,7 @@ __global__ void __launch_bounds__(128) k_sweepb(Pools<T> P, const int2 *items, i
   const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
-  if (!sv.block || sweep >= sv.sweeps) return;
+  if (!sv.block || !sv.active || sweep >= sv.sweeps) return;
   const bool full = sweep > 0 || sv.sweeps > 1;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
@@ -566,6 +656,7 @@ __global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int
   const int2 it = items[t];
   const int64_t q = it.x, nq = P.nq;
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (!sv.active) return;
   T x[5];
   if (sv.sweeps <= 1) {
 #pragma unroll
@@ -616,9 +707,9 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
   double mx = 0.0;
   int64_t mpos = INT64_MAX;
   int bad = 0;
-  if (c >= 0) {
-    const BlockDev b = P.blocks[cta_block[blockIdx.x]];
-    const SolveDev sv = P.solves[b.solve];
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const SolveDev sv = P.solves[b.solve];
+  if (c >= 0 && sv.active) {
     const Gas<double> g = GasOf<double>(sv);
     const Prim<double> w = LoadW<double>(P.W, n, c);
     double du[5];
@@ -700,6 +791,7 @@ __global__ void k_aux(Pools<T> P, const int32_t *cells, const int32_t *cell_bloc
   if (t >= n) return;
   const int64_t c = cells[t];
   const SolveDev sv = P.solves[P.blocks[cell_block[t]].solve];
+  if (!sv.active) return;
   const Gas<double> g = GasOf<double>(sv);
   const Prim<double> w = LoadW<double>(P.W, P.ncell, c);
   P.mu[c] = SutherlandRatio(Temperature(w, g), sv.t_ref, sv.mu_c1, sv.mu_s, sv.mu_ref);
@@ -711,15 +803,12 @@ __global__ void k_aux(Pools<T> P, const int32_t *cells, const int32_t *cell_bloc
 // src/utility.cpp:59,138), central face state and viscosity, laminar
 // viscousFlux::CalcFlux (src/viscousFlux.cpp:58) with TauNormal
 // (src/utility.cpp:426)
-template <typename T, int D>
-__global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
-                                                const int32_t *cta_block) {
-  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
-  if (c < 0) return;
-  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
-  const SolveDev sv = P.solves[b.solve];
-  if (!sv.viscous) return;
-  const Gas<T> g = GasOf<T>(sv);
+// Face gradients of velocity and temperature on the dual cell around face c
+// of direction D, central face state and face viscosity.
+template <typename T, int D, typename PT>
+__device__ __forceinline__ void ViscFaceGather(const Pools<PT> &P, const BlockDev &b,
+                                               const Gas<T> &g, int64_t c, T grad[3][3],
+                                               T tg[3], Prim<T> &fs, T &muf) {
   const int64_t n = P.ncell;
   const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
   const int64_t cu = c, cl = c - st[D];
@@ -774,7 +863,6 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
   }
   const T vol = T(0.5) * ((T)P.vol[cl] + (T)P.vol[cu]);
   const T invVol = T(1) / vol;
-  T grad[3][3], tg[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
 #pragma unroll
@@ -792,13 +880,127 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
   const double *wd = P.width[D];
   T cd, cw;
   CentralCoeffs((T)wd[cl], (T)wd[cu], cd, cw);
-  Prim<T> fs;
   fs.rho = cd * Wu.rho + cw * Wl.rho;
   fs.u = cd * Wu.u + cw * Wl.u;
   fs.v = cd * Wu.v + cw * Wl.v;
   fs.w = cd * Wu.w + cw * Wl.w;
   fs.p = cd * Wu.p + cw * Wl.p;
-  const T muf = cd * (T)P.mu[cu] + cw * (T)P.mu[cl];
+  muf = cd * (T)P.mu[cu] + cw * (T)P.mu[cl];
+}
+
+// Mixed-precision version of ViscFaceGather: velocities and temperatures
+// enter the dual-cell sums as offsets from the upper cell's values, formed
+// in FP64 (the temperature offset as (p rho_u - p_u rho) / (rho rho_u R)),
+// so that the FP32 sums carry rounding relative to the differences across
+// the dual cell rather than to the values; the dual cell is closed, so the
+// offsets leave the gradients unchanged.  Face state and viscosity in FP32.
+template <int D, typename PT>
+__device__ __forceinline__ void ViscFaceGatherMixed(const Pools<PT> &P, const BlockDev &b,
+                                                    const SolveDev &sv, int64_t c,
+                                                    float grad[3][3], float tg[3],
+                                                    Prim<float> &fs, float &muf) {
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  const Prim<double> Wu = LoadW<double>(P.W, n, cu), Wl = LoadW<double>(P.W, n, cl);
+  const float rgas = (float)sv.gas_r;
+  auto rel = [&](const Prim<double> &w, float o[4]) {
+    o[0] = (float)(w.u - Wu.u);
+    o[1] = (float)(w.v - Wu.v);
+    o[2] = (float)(w.w - Wu.w);
+    o[3] = (float)(w.p * Wu.rho - Wu.p * w.rho) / ((float)w.rho * (float)Wu.rho * rgas);
+  };
+  auto area = [&](int e, int64_t x, float a[3]) {
+    const double *fa = P.fa[e];
+    const float m = (float)fa[3 * n + x];
+    a[0] = (float)fa[x] * m;
+    a[1] = (float)fa[n + x] * m;
+    a[2] = (float)fa[2 * n + x] * m;
+  };
+  float ol[4], ou[4] = {0.f, 0.f, 0.f, 0.f};
+  rel(Wl, ol);
+  float vlo[3][4], vhi[3][4], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e == D) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        vlo[e][k] = ol[k];
+        vhi[e][k] = ou[k];
+      }
+      float A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5f * (A0[r] + A1[r]);
+        alo[e][r] = 0.5f * (A0[r] + A2[r]);
+      }
+    } else {
+      float oup[4], olp[4], oum[4], olm[4];
+      rel(LoadW<double>(P.W, n, cu + st[e]), oup);
+      rel(LoadW<double>(P.W, n, cl + st[e]), olp);
+      rel(LoadW<double>(P.W, n, cu - st[e]), oum);
+      rel(LoadW<double>(P.W, n, cl - st[e]), olm);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        vhi[e][k] = 0.25f * (((ol[k] + ou[k]) + oup[k]) + olp[k]);
+        vlo[e][k] = 0.25f * (((ol[k] + ou[k]) + oum[k]) + olm[k]);
+      }
+      float Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5f * (Aup[r] + Alp[r]);
+        alo[e][r] = 0.5f * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const float invVol = 1.f / (0.5f * ((float)P.vol[cl] + (float)P.vol[cu]));
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int qv = 0; qv < 3; ++qv)
+      grad[r][qv] = (vhi[0][qv] * ahi[0][r] - vlo[0][qv] * alo[0][r] +
+                     vhi[1][qv] * ahi[1][r] - vlo[1][qv] * alo[1][r] +
+                     vhi[2][qv] * ahi[2][r] - vlo[2][qv] * alo[2][r]) *
+                    invVol;
+    tg[r] = (vhi[0][3] * ahi[0][r] - vlo[0][3] * alo[0][r] + vhi[1][3] * ahi[1][r] -
+             vlo[1][3] * alo[1][r] + vhi[2][3] * ahi[2][r] - vlo[2][3] * alo[2][r]) *
+            invVol;
+  }
+  const double *wd = P.width[D];
+  float cd, cw;
+  CentralCoeffs((float)wd[cl], (float)wd[cu], cd, cw);
+  fs.rho = cd * (float)Wu.rho + cw * (float)Wl.rho;
+  fs.u = cd * (float)Wu.u + cw * (float)Wl.u;
+  fs.v = cd * (float)Wu.v + cw * (float)Wl.v;
+  fs.w = cd * (float)Wu.w + cw * (float)Wl.w;
+  fs.p = cd * (float)Wu.p + cw * (float)Wl.p;
+  muf = cd * (float)P.mu[cu] + cw * (float)P.mu[cl];
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
+                                                const int32_t *cta_block) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const SolveDev sv = P.solves[b.solve];
+  if (!sv.viscous || !sv.active) return;
+  const Gas<T> g = GasOf<T>(sv);
+  const int64_t n = P.ncell;
+  T grad[3][3], tg[3];
+  Prim<T> fs;
+  T muf;
+  if constexpr (std::is_same<T, float>::value)
+    ViscFaceGatherMixed<D>(P, b, sv, c, grad, tg, fs, muf);
+  else
+    ViscFaceGather<T, D>(P, b, g, c, grad, tg, fs, muf);
   const double *fa = P.fa[D];
   const T nx = (T)fa[c], ny = (T)fa[n + c], nz = (T)fa[2 * n + c], mag = (T)fa[3 * n + c];
   const T nrm[3] = {nx, ny, nz};
@@ -841,6 +1043,40 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
 #pragma unroll
       for (int qv = 0; qv < 3; ++qv) vs[(6 + r * 3 + qv) * n + c] = grad[r][qv];
   }
+}
+
+// ---------------------------------------------------------------------------
+// Wall data of the viscous-wall faces (viscousFlux::CalcWallFlux,
+// src/viscousFlux.cpp:137; wallData::WallPressure src/wallData.cpp:140),
+// always in FP64: per face p_w A (area vector) and tau_w |A|.
+template <typename T>
+__global__ void k_wall(Pools<T> P, const WallFaceDev *faces, int nfaces, double *wbuf) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nfaces) return;
+  const WallFaceDev wf = faces[t];
+  const BlockDev b = P.blocks[wf.block];
+  const SolveDev sv = P.solves[b.solve];
+  const Gas<double> g = GasOf<double>(sv);
+  const int64_t n = P.ncell, c = wf.face;
+  double grad[3][3], tg[3], muf;
+  Prim<double> fs;
+  if (wf.dir == 0) ViscFaceGather<double, 0>(P, b, g, c, grad, tg, fs, muf);
+  else if (wf.dir == 1) ViscFaceGather<double, 1>(P, b, g, c, grad, tg, fs, muf);
+  else ViscFaceGather<double, 2>(P, b, g, c, grad, tg, fs, muf);
+  const double *fa = P.fa[wf.dir];
+  const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c], mag = fa[3 * n + c];
+  const double mus = sv.visc_scale * muf, muts = sv.visc_scale * 0.0;
+  const double vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
+                        grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
+  double tau[3];
+  TauNormal(vg, nx, ny, nz, mus, muts, tau);
+  const double pw = fs.rho * g.r * Temperature(fs, g);
+  wbuf[0 * (int64_t)nfaces + t] = pw * nx * mag;
+  wbuf[1 * (int64_t)nfaces + t] = pw * ny * mag;
+  wbuf[2 * (int64_t)nfaces + t] = pw * nz * mag;
+  wbuf[3 * (int64_t)nfaces + t] = tau[0] * mag;
+  wbuf[4 * (int64_t)nfaces + t] = tau[1] * mag;
+  wbuf[5 * (int64_t)nfaces + t] = tau[2] * mag;
 }
 
 // ---------------------------------------------------------------------------
@@ -903,6 +1139,11 @@ void Launch<T>::MatRes(const Pools<T> &P, const int32_t *list, const int32_t *ct
   if (ncta <= 0) return;
   if (kinds & 1) k_matres<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
   if (kinds & 2) k_matres<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
+}
+template <typename T>
+void Launch<T>::Wall(const Pools<T> &P, const WallFaceDev *faces, int n, double *wbuf,
+                     cudaStream_t s) {
+  if (n > 0) k_wall<T><<<(n + 127) / 128, 128, 0, s>>>(P, faces, n, wbuf);
 }
 template <typename T>
 void Launch<T>::Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,

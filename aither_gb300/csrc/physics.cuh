@@ -165,6 +165,28 @@ __device__ __forceinline__ T Muscl1(T up2, T up1, T dw1, T dplus, T dminus,
                    ((T(1) - kappa) * lim + (T(1) + kappa) * r * ilim);
 }
 
+// Delta form of Muscl1 for the mixed path: the increment over the upwind
+// cell value, from the upwind difference a = up1 - up2 and the downwind
+// difference b = dw1 - up1 (formed in FP64 before rounding).
+template <typename T>
+__device__ __forceinline__ T MusclDelta1(T a, T b, T dplus, T dminus, T kappa,
+                                         int limiter) {
+  const T eps = T(1.0e-30);
+  const T r = (eps + b * dplus) / (eps + a * dminus);
+  T lim, ilim;
+  if (limiter == 1) {
+    lim = LimMinmod(r);
+    ilim = LimMinmod(T(1) / r);
+  } else if (limiter == 2) {
+    lim = LimVanAlbada(r);
+    ilim = LimVanAlbada(T(1) / r);
+  } else {
+    lim = T(1);
+    ilim = T(1);
+  }
+  return T(0.25) * (a * dminus) * ((T(1) - kappa) * lim + (T(1) + kappa) * r * ilim);
+}
+
 template <typename T>
 __device__ __forceinline__ Prim<T> Muscl(const Prim<T> &up2, const Prim<T> &up1,
                                          const Prim<T> &dw1, T uw2, T uw, T dw,
@@ -182,10 +204,12 @@ __device__ __forceinline__ Prim<T> Muscl(const Prim<T> &up2, const Prim<T> &up1,
 
 // RoeFlux with Harten's entropy fix (include/inviscidFlux.hpp:260-382,
 // src/inviscidFlux.cpp:27): F = 0.5 (FL + (FR - D)).
+// Dissipation D of the Roe flux from the face states L, R and their jumps
+// dq = R - L (rho, u, v, w, p).
 template <typename T>
-__device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
-                                        const Gas<T> &g, T nx, T ny, T nz,
-                                        T f[5]) {
+__device__ __forceinline__ void RoeDissipation(const Prim<T> &L, const Prim<T> &R,
+                                               const T dq[5], const Gas<T> &g, T nx, T ny,
+                                               T nz, T dout[5]) {
   // RoeAveragedState (include/primitive.hpp:245)
   const T denRatio = sqrt(R.rho / L.rho);
   Prim<T> roe;
@@ -200,8 +224,7 @@ __device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
   const T rhoR = roe.rho;
   const T velNormR = Dot(roe.u, roe.v, roe.w, nx, ny, nz);
   const T mfR = roe.rho / rhoR;  // mass fraction of the single species
-  const T dRho = R.rho - L.rho, dU = R.u - L.u, dV = R.v - L.v,
-          dW = R.w - L.w, dP = R.p - L.p;
+  const T dRho = dq[0], dU = dq[1], dV = dq[2], dW = dq[3], dP = dq[4];
   const T normVelDiff = Dot(dU, dV, dW, nx, ny, nz);
   const T entropyFix = T(0.1);
 
@@ -246,13 +269,41 @@ __device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
   d2 += ws * (roe.v + aR * ny);
   d3 += ws * (roe.w + aR * nz);
   d4 += ws * (hR + aR * velNormR);
+  dout[0] = d0;
+  dout[1] = d1;
+  dout[2] = d2;
+  dout[3] = d3;
+  dout[4] = d4;
+}
 
+template <typename T>
+__device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
+                                        const Gas<T> &g, T nx, T ny, T nz,
+                                        T f[5]) {
+  const T dq[5] = {R.rho - L.rho, R.u - L.u, R.v - L.v, R.w - L.w, R.p - L.p};
+  T d[5];
+  RoeDissipation(L, R, dq, g, nx, ny, nz, d);
   T fl[5], fr[5];
   InvFlux(L, g, nx, ny, nz, fl);
   InvFlux(R, g, nx, ny, nz, fr);
-  const T d[5] = {d0, d1, d2, d3, d4};
 #pragma unroll
   for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - d[v])) * T(0.5);
+}
+
+// Convective flux for the mixed path's FP64 central part: the kinetic
+// energy without the square root of the reference's |v| |v|.
+__device__ __forceinline__ void InvFluxCentral(const Prim<double> &s, const Gas<double> &g,
+                                               double nx, double ny, double nz,
+                                               double f[5]) {
+  const double vn = s.u * nx + s.v * ny + s.w * nz;
+  const double t = s.p / (s.rho * g.r);
+  const double h = (g.hf + g.Cp() * t) + 0.5 * (s.u * s.u + s.v * s.v + s.w * s.w);
+  const double m = s.rho * vn;
+  f[0] = m;
+  f[1] = m * s.u + s.p * nx;
+  f[2] = m * s.v + s.p * ny;
+  f[3] = m * s.w + s.p * nz;
+  f[4] = m * h;
 }
 
 // ---------------------------------------------------------------------------
@@ -496,22 +547,62 @@ __device__ __forceinline__ T InvFaceSpecRad(const Prim<T> &s, const Gas<T> &g,
   return T(0.5) * mag * (fabs(Dot(s.u, s.v, s.w, nx, ny, nz)) + SoS(s, g));
 }
 
+// F(W') - F(W) with W' = prim(cons(W) + dU) (ConvectiveFluxUpdate,
+// include/inviscidFlux.hpp:544) rewritten exactly in terms of the
+// increments, for the FP32 sweeps: every term carries a factor of dU, so the
+// rounding error is relative to the update instead of to the flux (the
+// reference form subtracts two O(|F|) fluxes).
+template <typename T>
+__device__ __forceinline__ void ConvFluxDelta(const Prim<T> &s, const T du[5],
+                                              const Gas<T> &g, T nx, T ny, T nz, T out[5]) {
+  const T rho1 = s.rho + du[0];
+  const T ir1 = T(1) / rho1;
+  const T dux = (du[1] - s.u * du[0]) * ir1;
+  const T duy = (du[2] - s.v * du[0]) * ir1;
+  const T duz = (du[3] - s.w * du[0]) * ir1;
+  const T t = s.p / (s.rho * g.r);
+  const T ke = T(0.5) * (s.u * s.u + s.v * s.v + s.w * s.w);
+  const T E = (g.hf + g.Cv() * t) + ke;  // specific total energy
+  const T dE = (du[4] - E * du[0]) * ir1;
+  const T dke = T(0.5) * ((T(2) * s.u + dux) * dux + (T(2) * s.v + duy) * duy +
+                          (T(2) * s.w + duz) * duz);
+  const T dt = (dE - dke) / g.Cv();
+  const T dp = g.r * (rho1 * dt + du[0] * t);
+  const T vn = s.u * nx + s.v * ny + s.w * nz;
+  const T dvn = dux * nx + duy * ny + duz * nz;
+  const T rhoE = s.rho * E;
+  const T m0 = rho1 * dvn + du[0] * vn;  // (rho vn)' - rho vn
+  const T rvn = s.rho * vn;
+  out[0] = m0;
+  out[1] = m0 * (s.u + dux) + rvn * dux + dp * nx;
+  out[2] = m0 * (s.v + duy) + rvn * duy + dp * ny;
+  out[3] = m0 * (s.w + duz) + rvn * duz + dp * nz;
+  out[4] = dvn * (rhoE + du[4] + s.p + dp) + vn * (du[4] + dp);
+}
+
 // RusanovScalarOffDiagonal (src/fluxJacobian.cpp:122) for an inviscid,
 // non-turbulent case: 0.5|A| (F(W+dU) - F(W)) +/- lambda_face dU.
 template <typename T>
 __device__ __forceinline__ void ScalarOffDiag(const Prim<T> &s, const T du[5],
                                               const Gas<T> &g, T nx, T ny, T nz,
                                               T mag, bool positive, T visc_sr, T out[5]) {
-  const Prim<T> su = UpdateWithCons(s, g, du);
-  T fo[5], fn[5];
-  InvFlux(s, g, nx, ny, nz, fo);
-  InvFlux(su, g, nx, ny, nz, fn);
+  T df[5];
+  if constexpr (sizeof(T) == sizeof(float)) {
+    ConvFluxDelta(s, du, g, nx, ny, nz, df);
+  } else {
+    const Prim<T> su = UpdateWithCons(s, g, du);
+    T fo[5], fn[5];
+    InvFlux(s, g, nx, ny, nz, fo);
+    InvFlux(su, g, nx, ny, nz, fn);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) df[v] = fn[v] - fo[v];
+  }
   const T half = T(0.5) * mag;
   T lam = InvFaceSpecRad(s, g, nx, ny, nz, mag);
   lam += visc_sr;  // FaceSpectralRadius (include/spectralRadius.hpp:182)
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    const T fc = half * (fn[v] - fo[v]);
+    const T fc = half * df[v];
     out[v] = positive ? fc + lam * du[v] : fc - lam * du[v];
   }
 }

@@ -44,6 +44,8 @@ extern "C" {
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
+  ATH_RETIRED = 1,        /* (per-solve status) the solve had retired before
+                             this iteration: converged or nonphysical */
   ATH_OK = 0,
   ATH_ERR_ARG = -1,       /* invalid argument */
   ATH_ERR_IO = -2,        /* file could not be read or parsed */
@@ -198,6 +200,12 @@ typedef struct {
   double matrix_resid; /* linear-system residual (0 when not computed) */
   double cfl;
   int32_t status;      /* ATH_OK or ATH_ERR_NONPHYSICAL for this solve */
+  /* integrated wall forces of the iteration's residual, summed over the
+   * viscous-wall faces: p_w A (area vector, x y z) then tau_w |A| (x y z);
+   * zero for solves without viscous walls.  The reference keeps the wall
+   * data (procBlock::WallPressure / WallShearStress, include/procBlock.hpp:
+   * 525-552) but does not integrate it. */
+  double force[6];
 } ath_norms;
 
 int ath_ctx_create(int device, size_t hbm_budget_bytes, ath_ctx **out);
@@ -215,6 +223,34 @@ int ath_batch_destroy(ath_batch *batch);
  * n * nsolves entries (iteration-major) when not NULL.  The iteration
  * counter advances (CFL ramp, src/input.cpp:647). */
 int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h);
+
+/* Per-solve record of a run to convergence. */
+typedef struct {
+  int64_t iterations;  /* iterations the solve ran in this batch */
+  double drop;         /* last total L2 / first-iteration total L2; the total
+                          L2 is sqrt(sum over equations of l2^2) */
+  double ms;           /* device time from the end of the solve's first
+                          iteration in this batch to its retirement (or to
+                          now while it runs) */
+  int32_t converged;   /* 1: drop reached, -1: retired nonphysical, 0: running */
+  int32_t pad;
+} ath_converge_info;
+
+/* Runs iterations until every solve has retired or max_iters iterations
+ * have passed.  A solve retires, on the device and in the iteration where
+ * it happens, when its total L2 norm falls to `drop` times that of its first
+ * iteration (the reference normalises its residual history by the first
+ * iteration, src/main.cpp:254-271) or when its state turns nonphysical;
+ * from then on its kernels skip their work, so a solve's result does not
+ * depend on what else shares the batch.  The host checks every
+ * `check_every` iterations.  info: nsolves entries (may be NULL). */
+int ath_batch_converge(ath_batch *batch, int max_iters, double drop, int check_every,
+                       ath_converge_info *info);
+/* Retirement target of one solve (0 = never), or reactivation: active = 1
+ * resumes a retired solve from its current state. */
+int ath_batch_set_target(ath_batch *batch, int solve, double drop, int active);
+/* Current per-solve records (nsolves entries). */
+int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
 
 /* Same as one iteration but split into the reference's stages, for parity
  * tests.  Stage order: fill_ghosts, residual, timestep, diag_invert, relax,

@@ -29,6 +29,8 @@ typedef struct {
   double *lam, *dt, *A, *Ainv; /* [nc] */
   double *Ab, *Ainvb;  /* [nc][25] block diagonal and its inverse (blusgs) */
   double *vg;          /* [nc][9] cell-averaged velocity gradient (blusgs) */
+  uint8_t *wallf[3];   /* [nf] face is a viscous wall */
+  double force[6];     /* wall forces of the last residual: p A, tau |A| */
   uint8_t *mask;
   double *center;      /* [3][nc] */
   double *T, *mu;      /* [nc] temperature, laminar viscosity (aux) */
@@ -59,6 +61,7 @@ struct orc_case {
   int nthreads;
   int matrix_resid;     /* compute the logged matrix residual */
   double *mres;         /* [ns] last matrix residual */
+  double *forces;       /* [ns][6] wall forces of the last residual */
 };
 
 /* ---------------------------------------------------------------- thermo */
@@ -811,6 +814,13 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           F[3] = tau[2];
           F[4] = (tau[0] * fs[1] + tau[1] * fs[2] + tau[2] * fs[3]) +
                  (kk_ + kt) * (tg[0] * n[0] + tg[1] * n[1] + tg[2] * n[2]) + 0.0;
+          if (b->wallf[d][face_idx(b, d, i, j, k)]) {
+            /* wall data (viscousFlux::CalcWallFlux, src/viscousFlux.cpp:137)
+             * and wallData::WallPressure (src/wallData.cpp:140) */
+            const double pw = fs[0] * g->r * tf;
+            for (int q = 0; q < 3; ++q) b->force[q] += pw * n[q] * mag;
+            for (int q = 0; q < 3; ++q) b->force[3 + q] += tau[q] * mag;
+          }
           /* block diagonal: ApproxTSLJacobian at the face with the face
            * state, viscosity and gradient, ProjC2CDist as the length; cell
            * gradients: one sixth of each face gradient */
@@ -862,6 +872,7 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
   c->b = (oblock *)calloc(nblocks, sizeof(oblock));
   c->s = (osolve *)calloc(nsolves, sizeof(osolve));
   c->mres = (double *)calloc(nsolves, sizeof(double));
+  c->forces = (double *)calloc((size_t)nsolves * 6, sizeof(double));
   for (int s = 0; s < nsolves; ++s) {
     c->s[s].v = sv[s];
     c->s[s].states = (ath_bc_state *)dup_arr(sv[s].states, sizeof(ath_bc_state) * sv[s].nstates);
@@ -920,6 +931,9 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     b->nplanes = v->nplanes;
     b->plane_off = (int32_t *)dup_arr(v->plane_offsets, 4 * (v->nplanes + 1));
     b->plane_cells = (int32_t *)dup_arr(v->plane_cells, 4 * (size_t)v->ni * v->nj * v->nk);
+    for (int d = 0; d < 3; ++d) b->wallf[d] = (uint8_t *)dup_arr(NULL, b->nf[d]);
+    for (int o = 0; o < b->nvops; ++o)
+      if (b->vops[o].layer == 1) b->wallf[b->vops[o].dir][b->vops[o].face] = 1;
   }
   return c;
 }
@@ -935,16 +949,21 @@ void orc_destroy(orc_case *c) {
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
     free(b->Ab); free(b->Ainvb); free(b->vg);
+    for (int d = 0; d < 3; ++d) free(b->wallf[d]);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
   free(c->s);
   free(c->mres);
+  free(c->forces);
   free(c);
 }
 
 void orc_set_threads(orc_case *c, int n) { c->nthreads = n; }
 void orc_set_matrix_resid(orc_case *c, int on) { c->matrix_resid = on; }
+void orc_forces(const orc_case *c, int solve, double *out) {
+  for (int q = 0; q < 6; ++q) out[q] = (solve >= 0 && solve < c->ns) ? c->forces[solve * 6 + q] : 0.0;
+}
 double orc_matrix_resid(const orc_case *c, int solve) {
   return (solve >= 0 && solve < c->ns) ? c->mres[solve] : 0.0;
 }
@@ -1062,6 +1081,7 @@ void orc_residual(orc_case *c) {
     memset(b->R, 0, 8 * NV * b->nc);
     memset(b->lam, 0, 8 * b->nc);
     memset(b->A, 0, 8 * b->nc);
+    memset(b->force, 0, sizeof(b->force));
     if (sv->block) {
       memset(b->Ab, 0, 8 * NJAC * b->nc);
       memset(b->vg, 0, 8 * 9 * b->nc);
@@ -1147,6 +1167,9 @@ void orc_residual(orc_case *c) {
       viscous_fluxes(c, b);
     }
   }
+  memset(c->forces, 0, sizeof(double) * 6 * c->ns);
+  for (int bi = 0; bi < c->nb; ++bi)
+    for (int q = 0; q < 6; ++q) c->forces[c->b[bi].solve * 6 + q] += c->b[bi].force[q];
   /* SwapEddyViscAndGradients (src/gridLevel.cpp:343): cell gradients of
    * the connection ghosts from the partner block */
   for (int bi = 0; bi < c->nb; ++bi) {

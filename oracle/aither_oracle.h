@@ -36,6 +36,10 @@ void orc_set_threads(orc_case *c, int nthreads);
 void orc_set_matrix_resid(orc_case *c, int on);
 double orc_matrix_resid(const orc_case *c, int solve);
 
+/* Integrated wall forces of the last residual evaluation: sum over the
+ * viscous-wall faces of p_w A (area vector, 3 values) then tau_w |A| (3). */
+void orc_forces(const orc_case *c, int solve, double *out6);
+
 /* Stages of one nonlinear iteration, in order. */
 void orc_fill_ghosts(orc_case *c);
 void orc_residual(orc_case *c);

@@ -42,6 +42,7 @@ def lib():
         L.orc_set_matrix_resid.argtypes = [vp, C.c_int]
         L.orc_matrix_resid.restype = C.c_double
         L.orc_matrix_resid.argtypes = [vp, C.c_int]
+        L.orc_forces.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_set_state.restype = C.c_int
         L.orc_set_state.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         _lib = L
@@ -81,12 +82,16 @@ class Oracle:
     def iterate(self, n: int = 1) -> np.ndarray:
         l2 = np.zeros(n * self.nsolves * 5)
         self.mres = np.zeros((n, self.nsolves))
+        self.forces = np.zeros((n, self.nsolves, 6))
         for it in range(n):
             rc = lib().orc_iterate(self.h, 1, _dp(l2[it * self.nsolves * 5:]))
             if rc:
                 raise RuntimeError(f"oracle reported status {rc}")
             for s in range(self.nsolves):
                 self.mres[it, s] = lib().orc_matrix_resid(self.h, s)
+                f = np.zeros(6)
+                lib().orc_forces(self.h, s, _dp(f))
+                self.forces[it, s] = f
         return l2.reshape(n, self.nsolves, 5)
 
     def stage(self, name: str):

@@ -301,6 +301,41 @@ int main(int argc, char *argv[]) {
       DumpBlock(w, local.Finest().Block(bb), nullptr, du[bb], phys, bb);
     }
   }
+  {
+    // integrated wall forces from the wall data of the last residual:
+    // sum over viscous-wall faces of p_w A (area vector) and tau_w |A|,
+    // blocks in order, wall surfaces in wall-data order, faces k, j, i
+    std::vector<double> forces(6, 0.0);
+    for (int bb = 0; bb < local.Finest().NumBlocks(); ++bb) {
+      const auto &blk = local.Finest().Block(bb);
+      for (int ss = 0; ss < blk.WallDataSize(); ++ss) {
+        const auto surf = blk.WallSurface(ss);
+        const int dir = (surf.SurfaceType() - 1) / 2;
+        const int i1 = dir == 0 ? surf.IMin() + 1 : surf.IMax();
+        const int j1 = dir == 1 ? surf.JMin() + 1 : surf.JMax();
+        const int k1 = dir == 2 ? surf.KMin() + 1 : surf.KMax();
+        for (int kk = surf.KMin(); kk < k1; ++kk)
+          for (int jj = surf.JMin(); jj < j1; ++jj)
+            for (int ii = surf.IMin(); ii < i1; ++ii) {
+              const double p = blk.WallPressure(ss, ii, jj, kk, phys.EoS());
+              const auto tau = blk.WallShearStress(ss, ii, jj, kk);
+              const auto n = dir == 0 ? blk.FAreaUnitI(ii, jj, kk)
+                             : dir == 1 ? blk.FAreaUnitJ(ii, jj, kk)
+                                        : blk.FAreaUnitK(ii, jj, kk);
+              const double mag = dir == 0 ? blk.FAreaMagI(ii, jj, kk)
+                                 : dir == 1 ? blk.FAreaMagJ(ii, jj, kk)
+                                            : blk.FAreaMagK(ii, jj, kk);
+              forces[0] += p * n.X() * mag;
+              forces[1] += p * n.Y() * mag;
+              forces[2] += p * n.Z() * mag;
+              forces[3] += tau.X() * mag;
+              forces[4] += tau.Y() * mag;
+              forces[5] += tau.Z() * mag;
+            }
+      }
+    }
+    w.Put("forces", {6}, forces);
+  }
   std::vector<double> consts = {inp.ARef(), inp.RRef(), inp.TRef(), inp.LRef(),
                                 inp.CFL()};
   w.Put("refs", {static_cast<int64_t>(consts.size())}, consts);

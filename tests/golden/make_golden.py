@@ -6,7 +6,8 @@ through oracle/ref_build/ref_harness.cpp on seeded synthetic cases.
 
 Each fixture is an .npz with the fields the reference produced:
   <case>_it<N>.npz : state0, state (physical, after N iterations), resid,
-                     dt, specrad, du (of iteration N), l2 (per iteration)
+                     dt, specrad, du (of iteration N), l2 and matrix_resid
+                     (per iteration), forces (wall forces of iteration N)
 Small grids keep the fixtures a few hundred kB; the full-size vortex-box
 configuration (64x32x8, 200 iterations) stores its L2 history and summary
 statistics of the final state only.
@@ -83,7 +84,8 @@ def run_case(name, gen, kw, niter, full, ref_dir):
             raise RuntimeError(f"reference harness failed on {name}: {r.stderr[-2000:]}")
         R = read_dump(os.path.join(d, "out.bin"))
     nblocks = sum(1 for k in R if k.startswith("b") and k.endswith("_resid"))
-    out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "kwargs": np.array(repr(kw)),
+    out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "forces": R["forces"],
+           "kwargs": np.array(repr(kw)),
            "iterations": np.array(niter), "nblocks": np.array(nblocks)}
     for b in range(nblocks):
         p = f"b{b}_"

@@ -8,7 +8,7 @@ Tolerances (relative to the largest magnitude of the compared field):
     last-bit differences of pow() between CUDA and the host libm (Sutherland's
     law) and of FMA-free reordering;
   * FP64 path, L2 residual histories (incl. 200 iterations of the full
-    64x32x8 vortex box): 1e-10.
+    64x32x8 vortex box) and integrated wall forces: 1e-10.
 """
 import numpy as np
 import pytest
@@ -68,6 +68,8 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
         assert rel_err(b.field(k, "DU"), g[p + "du"]) <= diff_tol
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
     assert all(x.status == 0 for x in norms)
+    if "forces" in g and np.abs(g["forces"]).max() > 0:
+        assert rel_err(np.array(norms[-1].force[:]), g["forces"]) <= NORM_TOL
     b.close()
 
 
@@ -99,6 +101,7 @@ def test_fp64_laminar_plate_two_blocks(ctx, name, tmp_path):
     s, b = _batch(ctx, inp, st)
     norms = b.iterate(20)
     assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    assert rel_err(np.array(norms[-1].force[:]), g["forces"]) <= NORM_TOL
     for k in range(2):
         w = b.field(k, "STATE")
         assert rel_err(w.reshape(-1, 5).sum(axis=0), g[f"b{k}_state_sum"]) <= NORM_TOL

@@ -47,6 +47,9 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
         assert rel_err(o.field(b, "SPECRAD")[..., 0], g[p + "specrad"][..., 0]) <= TOL
         assert rel_err(o.field(b, "DU"), g[p + "du"]) <= TOL
     assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
+    if "forces" in g and np.abs(g["forces"]).max() > 0:
+        # integrated wall forces: same terms, summed in another order
+        assert rel_err(o.forces[-1, 0], g["forces"]) <= 1e-12
 
 
 @pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
@@ -87,6 +90,7 @@ def test_oracle_laminar_plate_two_blocks(name, tmp_path):
     _, o = _oracle(inp, st)
     l2 = o.iterate(20)
     assert rel_err(l2[:, 0, :], g["l2"]) <= 1e-12
+    assert rel_err(o.forces[-1, 0], g["forces"]) <= 1e-12
     for b in range(2):
         w = o.field(b, "STATE")
         assert rel_err(w.reshape(-1, 5).sum(axis=0), g[f"b{b}_state_sum"]) <= 1e-12
