@@ -143,6 +143,7 @@ def lib() -> C.CDLL:
                                              C.POINTER(ConvergeInfo)]),
             "ath_batch_set_target": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
             "ath_batch_solve_info": (C.c_int, [vp, C.POINTER(ConvergeInfo)]),
+            "ath_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
             "ath_block_residual_noalloc": (C.c_int, [C.POINTER(BlockDev), C.POINTER(SolveView),
                                                      C.c_double, vp]),
         }
@@ -279,6 +280,12 @@ class Batch:
         info = (ConvergeInfo * self.nsolves)()
         check(lib().ath_batch_converge(self.h, max_iters, drop, check_every, info))
         return info
+
+    def autotune(self, reps: int = 3) -> int:
+        """Picks the sweep CTA size by timing; the solves are not advanced."""
+        t = C.c_int()
+        check(lib().ath_batch_autotune(self.h, reps, C.byref(t)))
+        return t.value
 
     def set_target(self, solve: int, drop: float, active: bool = True) -> None:
         check(lib().ath_batch_set_target(self.h, solve, drop, 1 if active else 0))

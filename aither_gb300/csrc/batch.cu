@@ -55,6 +55,15 @@ class DevMem {
             "upload");
     return p;
   }
+  void Free(void *p) {
+    for (size_t i = 0; i < ptrs_.size(); ++i)
+      if (ptrs_[i].first == p) {
+        cudaFree(p);
+        ctx_->used -= ptrs_[i].second;
+        ptrs_.erase(ptrs_.begin() + (long)i);
+        return;
+      }
+  }
   void Release() {
     for (auto &e : ptrs_) {
       cudaFree(e.first);
@@ -110,6 +119,7 @@ struct BatchCore {
   int nsteps = 0;
   int kinds = 0;        // bit 0: scalar lusgs solves present, bit 1: block (blusgs)
   int max_sweeps = 1;   // largest matrixSweeps of the batch
+  int sweep_threads = 128;  // CTA size of the sweep kernels (autotuned)
   bool block_viscous = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -276,6 +286,12 @@ class RunnerBase {
   virtual void GetDU(int b, double *out) = 0;
   virtual void GetAinv(int b, double *out) = 0;
   virtual void Profile(int reps, double ms[8]) = 0;
+  // drop the captured iteration graph (launch shapes changed)
+  virtual void ResetGraph() = 0;
+  // save (restore = false) or restore the iteration state: solution,
+  // per-solve counters and flags, CFL, iteration counter
+  virtual void Snapshot(bool restore) = 0;
+  virtual void FreeSnapshot() = 0;
 };
 
 template <typename T>
@@ -441,12 +457,14 @@ class Runner : public RunnerBase {
     if (forward) {
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.kinds, c_.stream);
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.kinds,
+                         c_.sweep_threads, c_.stream);
       }
     } else {
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.kinds, c_.stream);
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.kinds,
+                         c_.sweep_threads, c_.stream);
       }
     }
   }
@@ -562,6 +580,50 @@ class Runner : public RunnerBase {
     for (int q = 0; q < 8; ++q) ms[q] /= std::max(reps, 1);
     for (auto &x : e) cudaEventDestroy(x);
   }
+  void ResetGraph() override {
+    if (c_.graph) cudaGraphExecDestroy(c_.graph);
+    c_.graph = nullptr;
+  }
+  void Snapshot(bool restore) override {
+    DevMem &m = *c_.mem;
+    const size_t wbytes = 5 * (size_t)c_.ncell * sizeof(double);
+    if (!snap_w_) {
+      snap_w_ = m.Alloc<double>(5 * (size_t)c_.ncell);
+      snap_ss_ = m.Alloc<SolveState>(c_.nsolves);
+      snap_sv_ = m.Alloc<SolveDev>(c_.nsolves);
+      snap_cfl_ = m.Alloc<double>(c_.nsolves);
+      snap_it_ = m.Alloc<int64_t>(1);
+    }
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+      Check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c_.stream), "snapshot");
+    };
+    if (!restore) {
+      cp(snap_w_, P_.W, wbytes);
+      cp(snap_ss_, c_.d_sstate, c_.nsolves * sizeof(SolveState));
+      cp(snap_sv_, c_.d_solves, c_.nsolves * sizeof(SolveDev));
+      cp(snap_cfl_, c_.d_cfl, c_.nsolves * sizeof(double));
+      cp(snap_it_, c_.d_iter, sizeof(int64_t));
+      snap_iter_host_ = c_.iter_host;
+    } else {
+      cp(P_.W, snap_w_, wbytes);
+      cp(c_.d_sstate, snap_ss_, c_.nsolves * sizeof(SolveState));
+      cp(c_.d_solves, snap_sv_, c_.nsolves * sizeof(SolveDev));
+      cp(c_.d_cfl, snap_cfl_, c_.nsolves * sizeof(double));
+      cp(c_.d_iter, snap_it_, sizeof(int64_t));
+      c_.iter_host = snap_iter_host_;
+    }
+    Check(cudaStreamSynchronize(c_.stream), "sync");
+  }
+  void FreeSnapshot() override {
+    if (!snap_w_) return;
+    DevMem &m = *c_.mem;
+    m.Free(snap_w_);
+    m.Free(snap_ss_);
+    m.Free(snap_sv_);
+    m.Free(snap_cfl_);
+    m.Free(snap_it_);
+    snap_w_ = nullptr;
+  }
   void GetDU(int b, double *out) override { CopyOutQ(P_.dUq, 5, b, out); }
   void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, b, out); }
 
@@ -604,6 +666,10 @@ class Runner : public RunnerBase {
 
   BatchCore &c_;
   Pools<T> P_{};
+  double *snap_w_ = nullptr, *snap_cfl_ = nullptr;
+  SolveState *snap_ss_ = nullptr;
+  SolveDev *snap_sv_ = nullptr;
+  int64_t *snap_it_ = nullptr, snap_iter_host_ = 0;
 };
 
 }  // namespace ath
@@ -1224,6 +1290,40 @@ int ath_batch_converge(ath_batch *batch, int max_iters, double drop, int check_e
     c.stats.device_ms = ms;
     c.stats.kernel_launches = (int64_t)done * c.launches_per_iter;
     if (info) SolveInfo(c, info);
+  });
+}
+
+int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
+  return Guard([&] {
+    if (!batch || reps < 1) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    auto &c = batch->core;
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    auto &run = *batch->run;
+    run.Snapshot(false);
+    const int cand[4] = {32, 64, 128, 256};
+    float best = 1e30f;
+    int best_t = c.sweep_threads;
+    for (int t : cand) {
+      c.sweep_threads = t;
+      run.ResetGraph();
+      run.Iterate(1);  // capture and warm
+      Check(cudaEventRecord(c.ev0, c.stream), "event");
+      run.Iterate(reps);
+      Check(cudaEventRecord(c.ev1, c.stream), "event");
+      Check(cudaEventSynchronize(c.ev1), "sync");
+      float ms = 0.f;
+      Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
+      if (ms < best) {
+        best = ms;
+        best_t = t;
+      }
+      run.Snapshot(true);
+    }
+    c.sweep_threads = best_t;
+    run.ResetGraph();
+    run.FreeSnapshot();
+    Check(cudaGetLastError(), "kernel launch");
+    if (sweep_threads) *sweep_threads = best_t;
   });
 }
 

@@ -246,7 +246,7 @@ struct Launch {
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                    int ncta, int kinds, cudaStream_t s);
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                    bool full, int kinds, cudaStream_t s);
+                    bool full, int kinds, int threads, cudaStream_t s);
   static void Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

@@ -560,7 +560,7 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const Gas<T> 
 // triangle (sweep 0 of a one-sweep solve: forward x = A^-1 (b + L x),
 // backward x -= A^-1 U x) or both (x = A^-1 (b + L x - U x)).
 template <typename T, bool FULL>
-__global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, int n_items,
+__global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, int n_items,
                                                int forward, int sweep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(128) k_sweep(Pools<T> P, const int2 *items, in
 
 // Block version: A^-1 is the 5x5 inverse, products by ArrayMultiplication.
 template <typename T>
-__global__ void __launch_bounds__(128) k_sweepb(Pools<T> P, const int2 *items, int n_items,
+__global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
                                                 int forward, int sweep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
@@ -1180,14 +1180,14 @@ void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_
 }
 template <typename T>
 void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                      bool full, int kinds, cudaStream_t s) {
+                      bool full, int kinds, int threads, cudaStream_t s) {
   if (n <= 0) return;
-  const unsigned grid = (unsigned)((n + 127) / 128);
+  const unsigned grid = (unsigned)((n + threads - 1) / threads);
   if (kinds & 1) {
-    if (full) k_sweep<T, true><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweep<T, false><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
+    if (full) k_sweep<T, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
-  if (kinds & 2) k_sweepb<T><<<grid, 128, 0, s>>>(P, items, n, forward, sweep);
+  if (kinds & 2) k_sweepb<T><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
 }
 template <typename T>
 void Launch<T>::Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {

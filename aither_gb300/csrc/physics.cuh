@@ -290,20 +290,21 @@ __device__ __forceinline__ void RoeFlux(const Prim<T> &L, const Prim<T> &R,
   for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - d[v])) * T(0.5);
 }
 
-// Convective flux for the mixed path's FP64 central part: the kinetic
-// energy without the square root of the reference's |v| |v|.
+// Convective flux for the mixed path's FP64 central part, free of
+// divisions and square roots: rho H = rho hf + (n + 1) p + rho |v|^2 / 2
+// (cp T rho = (n + 1) p for the calorically perfect gas, cv = n R).
 __device__ __forceinline__ void InvFluxCentral(const Prim<double> &s, const Gas<double> &g,
                                                double nx, double ny, double nz,
                                                double f[5]) {
   const double vn = s.u * nx + s.v * ny + s.w * nz;
-  const double t = s.p / (s.rho * g.r);
-  const double h = (g.hf + g.Cp() * t) + 0.5 * (s.u * s.u + s.v * s.v + s.w * s.w);
   const double m = s.rho * vn;
+  const double rhoH = s.rho * (g.hf + 0.5 * (s.u * s.u + s.v * s.v + s.w * s.w)) +
+                      (g.n + 1.0) * s.p;
   f[0] = m;
   f[1] = m * s.u + s.p * nx;
   f[2] = m * s.v + s.p * ny;
   f[3] = m * s.w + s.p * nz;
-  f[4] = m * h;
+  f[4] = vn * rhoH;
 }
 
 // ---------------------------------------------------------------------------

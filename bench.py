@@ -145,6 +145,7 @@ def run_native(args, rank: int, world: int, device: int):
         batch = Batch(ctx, setup, prec)
         for _ in range(args.warmup):
             batch.iterate(1)
+        sweep_threads = batch.autotune(3)  # restores the state it ran on
         _barrier(world)
         clocks = ClockSampler(device)
         clocks.start()
@@ -158,7 +159,7 @@ def run_native(args, rank: int, world: int, device: int):
         status_ok = all(n.status == 0 for n in norms)
         res = {"value": ncells * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
                "wall_s": wall, "gpu_launches": int(st.kernel_launches), "clocks": clk,
-               "status_ok": status_ok}
+               "status_ok": status_ok, "sweep_threads": sweep_threads}
         # per-kernel-class CUDA-event times (one iteration's worth each)
         prof = batch.profile(2)
         res["kernel_ms"] = dict(zip(["ghost", "face_i", "face_j", "face_k", "cell",
@@ -169,8 +170,72 @@ def run_native(args, rank: int, world: int, device: int):
         res["e2e"] = run_e2e(batch, ncells, args.steps, world)
         batch.close()
         out[prec_name] = res
+    if args.converge_drop > 0 and args.precision == "both":
+        out["converge"] = run_converge(args, ctx, setup, specs, world)
     ctx.close()
     return out, ncells, nsolves, t_setup, specs
+
+
+def _pct(x, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(x, dtype=float), q)) if len(x) else None
+
+
+def _converge_once(ctx, setup, prec, args, world):
+    """Runs every solve of `setup` to the residual drop; per-solve times are
+    device-clock intervals from the end of the solve's first iteration to
+    its retirement (all solves start together)."""
+    from aither_gb300 import Batch
+    b = Batch(ctx, setup, prec)
+    tuned = b.autotune(3)
+    _barrier(world)
+    t0 = time.time()
+    info = b.converge(args.converge_max, args.converge_drop, check_every=100)
+    wall = time.time() - t0
+    st = b.stats()
+    states = [b.field(s, "STATE") for s in range(b.nsolves)]
+    b.close()
+    ms = [x.ms for x in info]
+    its = [int(x.iterations) for x in info]
+    conv = [x.converged == 1 for x in info]
+    dev_s = _max_over_ranks(st.device_ms * 1e-3, world)
+    return {"solves": len(info), "converged": int(sum(conv)), "device_s": dev_s, "wall_s": wall,
+            "solves_per_s": sum(conv) * world / dev_s, "p50_ms": _pct(ms, 50),
+            "p99_ms": _pct(ms, 99), "iterations_p50": _pct(its, 50),
+            "iterations_max": max(its) if its else None, "sweep_threads": tuned}, states, its
+
+
+def run_converge(args, ctx, setup, specs, world):
+    """Solves/s and time-to-convergence: the mixed path on the whole batch
+    (the batched configuration runs mixed precision to a 1e-6 drop), and the
+    FP64 and mixed paths on the smallest cases, whose converged states give
+    the mixed path's error against FP64."""
+    import numpy as np
+
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Setup
+    out = {"drop": args.converge_drop, "max_iterations": args.converge_max,
+           "definition": "per solve: total L2 over the equations relative to its first "
+                         "iteration; a solve retires on the device in the iteration that "
+                         "reaches the drop; p50/p99 over solves of the time from the end of "
+                         "its first iteration to retirement (all solves start together)"}
+    out["mixed"], _, _ = _converge_once(ctx, setup, PREC_MIXED, args, world)
+    k = min(args.converge_fp64_cases, len(specs))
+    if k > 0:
+        order = sorted(range(len(specs)), key=lambda i: specs[i][0] * specs[i][1] * specs[i][2])
+        pick = sorted(order[:k])
+        with tempfile.TemporaryDirectory() as tmp:
+            inps, _ = make_workload(tmp, args.ncases)
+            sub = Setup([inps[i] for i in pick])
+        f64, w64, it64 = _converge_once(ctx, sub, PREC_FP64, args, world)
+        mix, wmx, itmx = _converge_once(ctx, sub, PREC_MIXED, args, world)
+        err = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(wmx, w64))
+        out["subset"] = {"cases": pick, "cells": int(sum(specs[i][0] * specs[i][1] * specs[i][2]
+                                                         for i in pick)),
+                         "fp64": f64, "mixed": mix,
+                         "mixed_speedup": f64["device_s"] / mix["device_s"],
+                         "mixed_vs_fp64_state_max_rel_err": err,
+                         "iterations_max_abs_diff": int(max(abs(a - b) for a, b in zip(itmx, it64)))}
+    return out
 
 
 def run_e2e(batch, ncells: int, steps: int, world: int) -> dict:
@@ -273,6 +338,11 @@ def main():
     ap.add_argument("--ncases", type=int, default=64)
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--converge-drop", type=float, default=1e-6,
+                    help="residual drop of the time-to-convergence runs (0: skip them)")
+    ap.add_argument("--converge-max", type=int, default=12000)
+    ap.add_argument("--converge-fp64-cases", type=int, default=8,
+                    help="smallest cases also run to convergence in FP64 for the comparison")
     args = ap.parse_args()
     rank, world, local = _dist()
     config = {"workload": f"batched bump channels: {args.ncases} single-block cases, "
@@ -342,12 +412,16 @@ def main():
             "data": "synthetic (seeded bump-channel grids)", "config": config,
             "cells": ncells, "solves": nsolves, "setup_s": t_setup,
             "gpu_launches": fp["gpu_launches"], "clocks": fp["clocks"],
-            "e2e": fp["e2e"], "roofline": roof, "kernel_ms": km}
+            "e2e": fp["e2e"], "roofline": roof, "kernel_ms": km,
+            "autotune": {"sweep_threads": fp["sweep_threads"]}}
     if "mixed" in res and "fp64" in res:
         m = res["mixed"]
         line["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"],
                          "speedup_vs_fp64": m["value"] / fp["value"], "e2e": m["e2e"],
-                         "kernel_ms": m["kernel_ms"], "gpu_launches": m["gpu_launches"]}
+                         "kernel_ms": m["kernel_ms"], "gpu_launches": m["gpu_launches"],
+                         "sweep_threads": m["sweep_threads"]}
+    if "converge" in res:
+        line["converge"] = res["converge"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
     print(json.dumps(line))

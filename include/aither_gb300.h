@@ -252,6 +252,14 @@ int ath_batch_set_target(ath_batch *batch, int solve, double drop, int active);
 /* Current per-solve records (nsolves entries). */
 int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
 
+/* Autotuner of the launch shapes: times `reps` graph-captured iterations for
+ * each candidate CTA size of the hyperplane sweep kernels (32, 64, 128, 256;
+ * small batches spread a hyperplane over more SMs with small CTAs, large
+ * ones prefer larger CTAs) and keeps the fastest.  The solution, per-solve
+ * counters and CFL are restored afterwards, so tuning does not advance the
+ * solves.  The chosen size is written to *sweep_threads (may be NULL). */
+int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
+
 /* Same as one iteration but split into the reference's stages, for parity
  * tests.  Stage order: fill_ghosts, residual, timestep, diag_invert, relax,
  * update. */

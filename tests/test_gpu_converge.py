@@ -98,3 +98,23 @@ def test_mixed_precision_converged_state_against_fp64(ctx, case, tmp_path):
           f"{out[1][1]} vs {out[0][1]}")
     assert err <= 1e-6
     assert abs(out[1][1] - out[0][1]) <= max(2, 0.01 * out[0][1])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_leaves_the_solution_unchanged(ctx, precision, tmp_path):
+    """The launch-shape autotuner times real iterations, then restores the
+    solution and the per-solve counters: the results are those of an
+    untuned batch."""
+    from aither_gb300 import Batch, Setup
+    inps = _cases(tmp_path)
+    ref = Batch(ctx, Setup(inps), precision)
+    ref.iterate(7)
+    tuned = Batch(ctx, Setup(inps), precision)
+    tuned.iterate(3)
+    t = tuned.autotune(2)
+    assert t in (32, 64, 128, 256)
+    tuned.iterate(4)
+    for s in range(3):
+        assert np.array_equal(tuned.field(s, "STATE"), ref.field(s, "STATE"))
+    ref.close()
+    tuned.close()
