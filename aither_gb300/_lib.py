@@ -88,6 +88,13 @@ class ConvergeInfo(C.Structure):
                 ("converged", C.c_int32), ("pad", C.c_int32)]
 
 
+class RequestStatus(C.Structure):
+    """ath_request_status: one retired request of a Server."""
+    _fields_ = [("id", C.c_int64), ("iterations", C.c_int64), ("drop", C.c_double),
+                ("converged", C.c_int32), ("pad", C.c_int32), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("device_ms", C.c_double)]
+
+
 class BlockDev(C.Structure):
     """ath_block_dev: caller-owned device arrays of one block."""
     _fields_ = [("ni", C.c_int32), ("nj", C.c_int32), ("nk", C.c_int32), ("ng", C.c_int32),
@@ -144,6 +151,15 @@ def lib() -> C.CDLL:
             "ath_batch_set_target": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
             "ath_batch_solve_info": (C.c_int, [vp, C.POINTER(ConvergeInfo)]),
             "ath_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+            "ath_server_create": (C.c_int, [vp, C.c_int, C.c_double, C.c_int64, C.c_int,
+                                            C.c_int, C.POINTER(vp)]),
+            "ath_server_submit": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_int64)]),
+            "ath_server_step": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+            "ath_server_poll": (C.c_int, [vp, C.POINTER(RequestStatus), C.c_int,
+                                          C.POINTER(C.c_int)]),
+            "ath_server_fetch": (C.c_int, [vp, C.c_int64, C.c_int, C.POINTER(C.c_double)]),
+            "ath_server_release": (C.c_int, [vp, C.c_int64]),
+            "ath_server_destroy": (C.c_int, [vp]),
             "ath_block_residual_noalloc": (C.c_int, [C.POINTER(BlockDev), C.POINTER(SolveView),
                                                      C.c_double, vp]),
         }
@@ -338,3 +354,52 @@ class Batch:
         s = Stats()
         check(lib().ath_batch_stats(self.h, C.byref(s)))
         return s
+
+
+class Server:
+    """Continuous-batching request loop (ath_server_*): every admitted request
+    is a device-resident batch on its own stream; admission by slots and by
+    the context's device-memory budget; retirement on the device at the
+    residual drop."""
+
+    def __init__(self, ctx: Context, precision: int = PREC_FP64, drop: float = 1e-6,
+                 max_iters: int = 100000, chunk: int = 50, max_active: int = 16):
+        h = C.c_void_p()
+        check(lib().ath_server_create(ctx.h, precision, drop, max_iters, chunk, max_active,
+                                      C.byref(h)))
+        self.h = h
+        self.shapes = {}
+
+    def submit(self, inp_path: str) -> int:
+        i = C.c_int64()
+        check(lib().ath_server_submit(self.h, inp_path.encode(), C.byref(i)))
+        s = Setup(inp_path)
+        self.shapes[i.value] = [(v.nk, v.nj, v.ni) for v in
+                                (s.block_view(b) for b in range(s.counts()[1]))]
+        s.close()
+        return i.value
+
+    def step(self):
+        a, q = C.c_int(), C.c_int()
+        check(lib().ath_server_step(self.h, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def poll(self, max_n: int = 256):
+        out = (RequestStatus * max_n)()
+        n = C.c_int()
+        check(lib().ath_server_poll(self.h, out, max_n, C.byref(n)))
+        return [out[i] for i in range(n.value)]
+
+    def fetch(self, rid: int, block: int = 0) -> np.ndarray:
+        nk, nj, ni = self.shapes[rid][block]
+        out = np.empty(nk * nj * ni * 5)
+        check(lib().ath_server_fetch(self.h, rid, block, dptr(out)))
+        return out.reshape(nk, nj, ni, 5)
+
+    def release(self, rid: int) -> None:
+        check(lib().ath_server_release(self.h, rid))
+
+    def close(self):
+        if self.h:
+            lib().ath_server_destroy(self.h)
+            self.h = None

@@ -110,7 +110,8 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         f"gridName: {grid}",
         f"equationSet: {scheme.get('equationSet', 'euler')}",
         "timeIntegration: implicitEuler",
-        f"cflStart: {_fmt(scheme['cfl'])}",
+        f"cflStart: {_fmt(scheme.get('cflStart', scheme['cfl']))}",
+        f"cflStep: {_fmt(scheme.get('cflStep', 0.0))}",
         f"cflMax: {_fmt(scheme['cfl'])}",
         f"faceReconstruction: {scheme.get('faceReconstruction', 'thirdOrder')}",
         f"limiter: {scheme.get('limiter', 'minmod')}",
@@ -235,6 +236,97 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                             "inviscidFlux": flux, "matrixSolver": matrix_solver,
                             "matrixSweeps": sweeps}, refs, ic, states, bcs)
     return inp, None
+
+
+def wall_channel_nodes(ni: int, nj: int, nk: int, kind: str, param: float,
+                       stretch: float = 1.0, length: float = 3.0, h_chan: float = 1.0,
+                       depth: float = 0.5) -> np.ndarray:
+    """Channel [-1, length-1] x [0, h_chan] x [0, depth] whose lower wall is
+    a sin^2 bump of height `param` on x in [0, 1] (kind "bump") or a
+    compression ramp of angle `param` degrees starting at x = 0 (kind
+    "wedge"); wall-normal spacing grows geometrically by `stretch`."""
+    x = -1.0 + length * np.arange(ni + 1) / ni
+    if stretch == 1.0:
+        eta = np.arange(nj + 1) / nj
+    else:
+        eta = (stretch ** np.arange(nj + 1) - 1.0) / (stretch ** nj - 1.0)
+    z = depth * np.arange(nk + 1) / nk
+    if kind == "bump":
+        yb = np.where((x >= 0.0) & (x <= 1.0), param * np.sin(np.pi * x) ** 2, 0.0)
+    else:
+        yb = np.where(x > 0.0, x * math.tan(math.radians(param)), 0.0)
+        yb = np.minimum(yb, 0.15 * h_chan)
+    X = np.broadcast_to(x[None, None, :], (nk + 1, nj + 1, ni + 1))
+    Y = yb[None, None, :] + eta[None, :, None] * (h_chan - yb[None, None, :])
+    Y = np.broadcast_to(Y, (nk + 1, nj + 1, ni + 1))
+    Z = np.broadcast_to(z[:, None, None], (nk + 1, nj + 1, ni + 1))
+    return np.ascontiguousarray(np.stack([X, Y, Z]))
+
+
+def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float,
+                 mach: float, alpha: float = 0.0, viscous: bool = False,
+                 reynolds: float = 1e5, stretch: float = 1.0, cfl: float = 20.0,
+                 name: str = "chan", precision_note: str = ""):
+    """Bump or wedge channel with free-stream Mach `mach` at angle of attack
+    `alpha` (degrees, in the x-y plane); characteristic in- and outflow,
+    slip upper and side walls; the lower wall is a slip wall (Euler) or an
+    adiabatic viscous wall (laminar Navier-Stokes, density from Re based on
+    the unit chord and Sutherland's viscosity)."""
+    os.makedirs(outdir, exist_ok=True)
+    nodes = wall_channel_nodes(ni, nj, nk, kind, param, stretch)
+    write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
+    t_inf = 288.0
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    u_inf = mach * a_inf
+    if viscous:
+        rho_inf = reynolds * sutherland_mu(t_inf) / u_inf
+    else:
+        rho_inf = 101325.0 / (R_AIR * t_inf)
+    p_inf = rho_inf * R_AIR * t_inf
+    refs = Refs(t_ref=t_inf, r_ref=rho_inf)
+    ca, sa = math.cos(math.radians(alpha)), math.sin(math.radians(alpha))
+    vel = f"[{_fmt(u_inf * ca)}, {_fmt(u_inf * sa)}, 0]"
+    ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel})"
+    states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
+              f"velocity={vel})"]
+    lower = ("slipWall", 0, ni, 0, 0, 0, nk, 2)
+    if viscous:
+        states.append("viscousWall(tag=3)")
+        lower = ("viscousWall", 0, ni, 0, 0, 0, nk, 3)
+    bcs = [[("characteristic", 0, 0, 0, nj, 0, nk, 1),
+            ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+            lower,
+            ("slipWall", 0, ni, nj, nj, 0, nk, 2),
+            ("slipWall", 0, ni, 0, nj, 0, 0, 2),
+            ("slipWall", 0, ni, 0, nj, nk, nk, 2)]]
+    inp = os.path.join(outdir, name + ".inp")
+    scheme = {"cfl": cfl, "cflStart": 1.0, "cflStep": 1.0,
+              "limiter": "vanAlbada" if viscous else "minmod",
+              "equationSet": "navierStokes" if viscous else "euler"}
+    write_input(inp, name, scheme, refs, ic, states, bcs)
+    return inp, None
+
+
+def served_specs(n: int, seed: int = 7, min_cells: int = 16_000, max_cells: int = 4_000_000,
+                 log_mean: float = math.log(150_000.0), log_sigma: float = 1.2):
+    """Request stream of the served workload: cell counts log-normal, clipped
+    to [min_cells, max_cells], shaped ni : nj : nk = 4 : 2 : 1; bump or wedge
+    lower wall; Mach U[0.3, 2.5]; angle of attack U[-4, 4] degrees; every
+    second request laminar Navier-Stokes with a stretched wall-normal grid,
+    the others Euler."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(n):
+        cells = float(np.clip(math.exp(rng.normal(log_mean, log_sigma)), min_cells, max_cells))
+        nk = max(2, int(round((cells / 8.0) ** (1.0 / 3.0))))
+        nj = 2 * nk
+        ni = max(8, int(round(cells / (nj * nk))))
+        kind = "bump" if rng.uniform() < 0.5 else "wedge"
+        param = float(rng.uniform(0.04, 0.10)) if kind == "bump" else float(rng.uniform(4, 10))
+        out.append({"ni": ni, "nj": nj, "nk": nk, "kind": kind, "param": param,
+                    "mach": float(rng.uniform(0.3, 2.5)), "alpha": float(rng.uniform(-4, 4)),
+                    "viscous": q % 2 == 1})
+    return out
 
 
 def bump_batch_specs(n: int = 64, seed: int = 2024, lo=(32, 32, 32), hi=(96, 64, 48)):

@@ -5,8 +5,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -1499,6 +1502,285 @@ int ath_batch_profile(ath_batch *batch, int reps, double ms[8]) {
 int ath_batch_stats(ath_batch *batch, ath_stats *out) {
   if (!batch || !out) return ATH_ERR_ARG;
   *out = batch->core.stats;
+  return ATH_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Serving: a request loop over independent solves.  Each admitted request
+// is a device-resident batch with its own stream, so the iterations of all
+// admitted requests overlap on the device; admission is first come, first
+// served, when a slot is free and the request's device memory (estimated
+// before anything is allocated) fits the context's budget.  Requests retire
+// on the device when their residual drop is reached (or nonphysical); the
+// host then copies the final state out and frees the request's memory,
+// which admits the next requests.  A request's result does not depend on
+// what else is resident: the batches share no data.
+namespace ath {
+namespace {
+
+double NowMs() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// Device bytes of a batch of this setup, estimated from its cell counts
+// (the per-cell sizes of the pools plus the work lists), with headroom.
+size_t EstimateBatchBytes(const Setup &st, int precision) {
+  double bytes = 64.0 * (1 << 20);
+  const double ts = precision == ATH_PREC_FP64 ? 8.0 : 4.0;
+  for (const auto &b : st.blocks) {
+    const auto &ph = st.solves[b.solve].phys;
+    const double n = (double)b.NCell();
+    const double nq = (double)b.ni * b.nj * b.nk;
+    const bool visc = ph.eqn != ATH_EQN_EULER, blk = ph.solver == ATH_SOLVER_BLUSGS;
+    double pc = 8.0 * (5 + 5 + 15 + 1 + 1 + 1 + 3 + 12) + 4.0 * 6;  // pools, lists
+    if (visc) pc += 15 * ts + 8;
+    if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);
+    double qc = ts * (5 + 5 + 5 + 24 + 6 + 2 + 1) + 4.0 * 8;
+    if (blk) qc += ts * (48 + (visc ? 9 : 0));
+    bytes += n * pc + nq * qc;
+  }
+  return (size_t)(bytes * 1.25);
+}
+
+}  // namespace
+}  // namespace ath
+
+struct ath_server {
+  struct Req {
+    int64_t id = 0;
+    ath_setup *setup = nullptr;
+    ath_batch *batch = nullptr;
+    size_t est = 0;
+    int state = 0;  // 0 queued, 1 active, 2 done
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int64_t launched = 0;
+    int32_t *flag_h = nullptr;  // page-locked copy of the solve's active flag
+    cudaEvent_t ev = nullptr;
+    ath_converge_info info{};
+    std::vector<std::vector<double>> result;  // final state per block
+  };
+  ath_ctx *ctx = nullptr;
+  int precision = ATH_PREC_FP64, chunk = 50, max_active = 16;
+  int64_t max_iters = 100000;
+  double drop = 1e-6;
+  int64_t next_id = 1;
+  size_t capacity = 0;  // device bytes the server may hand out
+  size_t reserved = 0;  // estimates of the admitted requests
+  std::deque<Req *> queue;
+  std::vector<Req *> active;
+  std::map<int64_t, Req *> all;
+  std::vector<int64_t> finished;  // done, not yet reported by poll
+};
+
+namespace ath {
+namespace {
+
+
+void LaunchChunk(ath_server *S, ath_server::Req *r) {
+  auto &c = r->batch->core;
+  const int n = (int)std::min<int64_t>(S->chunk, S->max_iters - r->launched);
+  r->batch->run->Iterate(n);
+  c.iter_host += n;
+  r->launched += n;
+  Check(cudaMemcpyAsync(r->flag_h, &c.d_solves[0].active, sizeof(int32_t),
+                        cudaMemcpyDeviceToHost, c.stream),
+        "flag download");
+  Check(cudaEventRecord(r->ev, c.stream), "event");
+}
+
+void Finish(ath_server *S, ath_server::Req *r) {
+  auto &c = r->batch->core;
+  Check(cudaStreamSynchronize(c.stream), "sync");
+  SolveInfo(c, &r->info);
+  r->result.resize(c.nblocks);
+  for (int b = 0; b < c.nblocks; ++b) {
+    const Block &bk = c.setup->blocks[b];
+    r->result[b].resize((size_t)bk.ni * bk.nj * bk.nk * 5);
+    const int rc = ath_batch_get_field(r->batch, b, ATH_FIELD_STATE, r->result[b].data());
+    if (rc != ATH_OK) throw Error(rc, "result download");
+  }
+  ath_batch_destroy(r->batch);
+  r->batch = nullptr;
+  S->reserved -= r->est;
+  cudaEventDestroy(r->ev);
+  r->ev = nullptr;
+  cudaFreeHost(r->flag_h);
+  r->flag_h = nullptr;
+  ath_setup_destroy(r->setup);
+  r->setup = nullptr;
+  r->state = 2;
+  r->t_done = NowMs();
+  S->finished.push_back(r->id);
+}
+
+bool Admit(ath_server *S, ath_server::Req *r) {
+  if (S->reserved + r->est > S->capacity) return false;
+  ath_batch *b = nullptr;
+  const int rc = ath_batch_create(S->ctx, r->setup, S->precision, 0, &b);
+  if (rc == ATH_ERR_NOMEM) return false;
+  if (rc != ATH_OK) throw Error(rc, std::string("admission: ") + ath_last_error());
+  r->batch = b;
+  S->reserved += r->est;
+  const int rt = ath_batch_set_target(b, 0, S->drop, 1);
+  if (rt != ATH_OK) throw Error(rt, "target");
+  Check(cudaMallocHost(&r->flag_h, sizeof(int32_t)), "cudaMallocHost");
+  *r->flag_h = 1;
+  Check(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming), "event");
+  r->state = 1;
+  r->t_admit = NowMs();
+  LaunchChunk(S, r);
+  return true;
+}
+
+}  // namespace
+}  // namespace ath
+
+extern "C" {
+
+int ath_server_create(ath_ctx *ctx, int precision, double drop, int64_t max_iters,
+                      int chunk, int max_active, ath_server **out) {
+  return Guard([&] {
+    if (!ctx || !out || !(drop > 0.0) || max_iters < 1 || chunk < 1 || chunk > 1024 ||
+        max_active < 1)
+      throw ath::Error(ATH_ERR_ARG, "bad argument");
+    if (precision != ATH_PREC_FP64 && precision != ATH_PREC_MIXED)
+      throw ath::Error(ATH_ERR_ARG, "unknown precision");
+    auto *S = new ath_server();
+    S->ctx = ctx;
+    S->precision = precision;
+    S->drop = drop;
+    S->max_iters = max_iters;
+    S->chunk = chunk;
+    S->max_active = max_active;
+    if (ctx->budget) {
+      S->capacity = ctx->budget;
+    } else {
+      Check(cudaSetDevice(ctx->device), "cudaSetDevice");
+      size_t fr = 0, tot = 0;
+      Check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+      const size_t reserve = (size_t)1 << 30;
+      S->capacity = fr > reserve ? fr - reserve : 0;
+    }
+    *out = S;
+  });
+}
+
+int ath_server_submit(ath_server *S, const char *inp_path, int64_t *id) {
+  return Guard([&] {
+    if (!S || !inp_path || !id) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto *r = new ath_server::Req();
+    r->t_submit = ath::NowMs();
+    const int rc = ath_setup_from_input(inp_path, &r->setup);
+    if (rc != ATH_OK) {
+      delete r;
+      throw ath::Error(rc, ath_last_error());
+    }
+    if (r->setup->s.solves.size() != 1) {
+      ath_setup_destroy(r->setup);
+      delete r;
+      throw ath::Error(ATH_ERR_ARG, "a request is one solve");
+    }
+    r->est = ath::EstimateBatchBytes(r->setup->s, S->precision);
+    r->id = S->next_id++;
+    S->queue.push_back(r);
+    S->all[r->id] = r;
+    *id = r->id;
+  });
+}
+
+int ath_server_step(ath_server *S, int *n_active, int *n_queued) {
+  return Guard([&] {
+    if (!S) throw ath::Error(ATH_ERR_ARG, "null server");
+    Check(cudaSetDevice(S->ctx->device), "cudaSetDevice");
+    // progress: every request whose last chunk finished either retires or
+    // gets its next chunk
+    for (size_t i = 0; i < S->active.size();) {
+      auto *r = S->active[i];
+      const cudaError_t q = cudaEventQuery(r->ev);
+      if (q == cudaErrorNotReady) {
+        ++i;
+        continue;
+      }
+      Check(q, "event query");
+      if (*r->flag_h == 0 || r->launched >= S->max_iters) {
+        ath::Finish(S, r);
+        S->active.erase(S->active.begin() + (long)i);
+        continue;
+      }
+      ath::LaunchChunk(S, r);
+      ++i;
+    }
+    // admission, first come first served
+    while (!S->queue.empty() && (int)S->active.size() < S->max_active) {
+      auto *r = S->queue.front();
+      if (!ath::Admit(S, r)) break;
+      S->queue.pop_front();
+      S->active.push_back(r);
+    }
+    if (n_active) *n_active = (int)S->active.size();
+    if (n_queued) *n_queued = (int)S->queue.size();
+  });
+}
+
+int ath_server_poll(ath_server *S, ath_request_status *out, int max, int *n) {
+  return Guard([&] {
+    if (!S || !n || (max > 0 && !out)) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    int k = 0;
+    while (k < max && !S->finished.empty()) {
+      auto *r = S->all.at(S->finished.front());
+      S->finished.erase(S->finished.begin());
+      ath_request_status &o = out[k++];
+      std::memset(&o, 0, sizeof(o));
+      o.id = r->id;
+      o.iterations = r->info.iterations;
+      o.drop = r->info.drop;
+      o.converged = r->info.converged;
+      o.queue_ms = r->t_admit - r->t_submit;
+      o.latency_ms = r->t_done - r->t_submit;
+      o.device_ms = r->info.ms;
+    }
+    *n = k;
+  });
+}
+
+int ath_server_fetch(ath_server *S, int64_t id, int block, double *prim_out) {
+  return Guard([&] {
+    if (!S || !prim_out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto it = S->all.find(id);
+    if (it == S->all.end() || it->second->state != 2) throw ath::Error(ATH_ERR_ARG, "not done");
+    auto *r = it->second;
+    if (block < 0 || block >= (int)r->result.size()) throw ath::Error(ATH_ERR_ARG, "block");
+    std::memcpy(prim_out, r->result[block].data(), r->result[block].size() * sizeof(double));
+  });
+}
+
+int ath_server_release(ath_server *S, int64_t id) {
+  return Guard([&] {
+    if (!S) throw ath::Error(ATH_ERR_ARG, "null server");
+    auto it = S->all.find(id);
+    if (it == S->all.end() || it->second->state != 2) throw ath::Error(ATH_ERR_ARG, "not done");
+    delete it->second;
+    S->all.erase(it);
+  });
+}
+
+int ath_server_destroy(ath_server *S) {
+  if (!S) return ATH_OK;
+  for (auto &kv : S->all) {
+    auto *r = kv.second;
+    if (r->batch) {
+      cudaStreamSynchronize(r->batch->core.stream);
+      ath_batch_destroy(r->batch);
+    }
+    if (r->ev) cudaEventDestroy(r->ev);
+    if (r->flag_h) cudaFreeHost(r->flag_h);
+    if (r->setup) ath_setup_destroy(r->setup);
+    delete r;
+  }
+  delete S;
   return ATH_OK;
 }
 

@@ -172,8 +172,68 @@ def run_native(args, rank: int, world: int, device: int):
         out[prec_name] = res
     if args.converge_drop > 0 and args.precision == "both":
         out["converge"] = run_converge(args, ctx, setup, specs, world)
+    if args.served_n > 0:
+        out["served"] = {"definition": "latency = submit to retirement (host clock), "
+                                       "retirement at the residual drop; solves/s = "
+                                       "converged requests / makespan",
+                         "drop": args.served_drop, "slots": args.served_slots,
+                         "max_cells": args.served_max_cells}
+        for pname, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+            out["served"][pname] = [run_served(args, ctx, prec, r, 11 + rank)
+                                    for r in args.served_rates]
     ctx.close()
     return out, ncells, nsolves, t_setup, specs
+
+
+def run_served(args, ctx, precision, rate, seed):
+    """The served configuration: a Poisson stream of `args.served_n` solve
+    requests at `rate` per second (cells log-normal, clipped; bump and
+    wedge channels; Mach 0.3-2.5; angle of attack -4..4 degrees; half laminar
+    Navier-Stokes, half Euler), admitted by the server as slots and device
+    memory free up, retired on the device at the residual drop.  Returns
+    time-to-convergence percentiles (submit to retirement) and solves/s."""
+    import numpy as np
+
+    from aither_gb300 import Server, cases
+    specs = cases.served_specs(args.served_n, seed=seed, max_cells=args.served_max_cells)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(specs)))
+    with tempfile.TemporaryDirectory() as tmp:
+        inps = []
+        for q, sp in enumerate(specs):
+            kw = dict(sp)
+            vis = kw.pop("viscous")
+            inp, _ = cases.wall_channel(os.path.join(tmp, f"s{q}"), viscous=vis,
+                                        stretch=1.1 if vis else 1.0, name=f"s{q}", **kw)
+            inps.append(inp)
+        srv = Server(ctx, precision, drop=args.served_drop, max_iters=args.served_max_iters,
+                     chunk=50, max_active=args.served_slots)
+        t0 = time.time()
+        nxt, done, max_active = 0, {}, 0
+        while len(done) < len(specs):
+            now = time.time() - t0
+            while nxt < len(specs) and arrivals[nxt] <= now:
+                srv.submit(inps[nxt])
+                nxt += 1
+            a, _ = srv.step()
+            max_active = max(max_active, a)
+            for st in srv.poll():
+                done[st.id] = st
+                srv.release(st.id)
+            time.sleep(0.0002)
+        makespan = time.time() - t0
+        srv.close()
+    st = list(done.values())
+    conv = [x for x in st if x.converged == 1]
+    lat = [x.latency_ms for x in conv]
+    return {"rate_per_s": rate, "requests": len(specs), "converged": len(conv),
+            "nonphysical": sum(1 for x in st if x.converged == -1),
+            "iteration_cap": sum(1 for x in st if x.converged == 0),
+            "makespan_s": makespan, "solves_per_s": len(conv) / makespan,
+            "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+            "queue_p50_ms": _pct([x.queue_ms for x in st], 50),
+            "max_concurrent": max_active,
+            "cells": int(sum(sp["ni"] * sp["nj"] * sp["nk"] for sp in specs))}
 
 
 def _pct(x, q):
@@ -340,7 +400,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--converge-drop", type=float, default=1e-6,
                     help="residual drop of the time-to-convergence runs (0: skip them)")
-    ap.add_argument("--converge-max", type=int, default=12000)
+    ap.add_argument("--converge-max", type=int, default=8000)
+    ap.add_argument("--served-n", type=int, default=6,
+                    help="requests of the served configuration (0: skip it)")
+    ap.add_argument("--served-rates", type=float, nargs="+", default=[2.0],
+                    help="Poisson arrival rates (requests/s) to sweep")
+    ap.add_argument("--served-max-cells", type=int, default=64_000,
+                    help="upper clip of the request sizes (the configuration's is 4M)")
+    ap.add_argument("--served-drop", type=float, default=1e-6)
+    ap.add_argument("--served-slots", type=int, default=16)
+    ap.add_argument("--served-max-iters", type=int, default=6000)
     ap.add_argument("--converge-fp64-cases", type=int, default=8,
                     help="smallest cases also run to convergence in FP64 for the comparison")
     args = ap.parse_args()
@@ -422,6 +491,8 @@ def main():
                          "sweep_threads": m["sweep_threads"]}
     if "converge" in res:
         line["converge"] = res["converge"]
+    if "served" in res:
+        line["served"] = res["served"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
     print(json.dumps(line))

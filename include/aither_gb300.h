@@ -260,6 +260,50 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
  * solves.  The chosen size is written to *sweep_threads (may be NULL). */
 int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
 
+/* ---- serving ------------------------------------------------------------
+ * A request loop over independent solves (continuous batching).  Every
+ * admitted request is its own device-resident batch on its own stream, so
+ * the iterations of all admitted requests overlap on the device.  Requests
+ * are admitted first come, first served, while fewer than max_active are
+ * resident and the estimated device memory of the resident requests plus
+ * this one fits the context's budget (or, when the budget is 0, the device
+ * memory free at server creation less 1 GiB).  A
+ * request retires on the device in the iteration where its total L2 drop
+ * reaches `drop` (or its state turns nonphysical, or after max_iters); the
+ * host then copies its final state out and frees its device memory.  The
+ * batches share no data, so a request's result is the same alone and in
+ * any mix.  The reference has no serving layer: every run is one MPI job
+ * (src/main.cpp). */
+typedef struct ath_server ath_server;
+typedef struct {
+  int64_t id;
+  int64_t iterations;
+  double drop;        /* last total L2 / first total L2 */
+  int32_t converged;  /* 1 drop reached, -1 nonphysical, 0 iteration cap */
+  int32_t pad;
+  double queue_ms;    /* submit to admission (host clock) */
+  double latency_ms;  /* submit to retirement (host clock): time to convergence */
+  double device_ms;   /* first iteration to retirement (device clock) */
+} ath_request_status;
+
+/* precision = ATH_PREC_*; iterations are launched `chunk` at a time (1..1024)
+ * between host checks. */
+int ath_server_create(ath_ctx *ctx, int precision, double drop, int64_t max_iters,
+                      int chunk, int max_active, ath_server **out);
+/* Parses the input file (the reference's format) and queues the request. */
+int ath_server_submit(ath_server *server, const char *inp_path, int64_t *id);
+/* One scheduling pass, non-blocking: requests whose last chunk finished
+ * retire or get their next chunk; queued requests are admitted while slots
+ * and memory allow. */
+int ath_server_step(ath_server *server, int *n_active, int *n_queued);
+/* Requests retired since the last poll (up to max). */
+int ath_server_poll(ath_server *server, ath_request_status *out, int max, int *n);
+/* Final primitive state of a retired request's block (AoS, physical cells,
+ * k slowest), kept on the host until released. */
+int ath_server_fetch(ath_server *server, int64_t id, int block, double *prim_out);
+int ath_server_release(ath_server *server, int64_t id);
+int ath_server_destroy(ath_server *server);
+
 /* Same as one iteration but split into the reference's stages, for parity
  * tests.  Stage order: fill_ghosts, residual, timestep, diag_invert, relax,
  * update. */
