@@ -109,6 +109,7 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         "# generated by aither_gb300.cases",
         f"gridName: {grid}",
         f"equationSet: {scheme.get('equationSet', 'euler')}",
+        f"turbulenceModel: {scheme.get('turbulenceModel', 'none')}",
         "timeIntegration: implicitEuler",
         f"cflStart: {_fmt(scheme.get('cflStart', scheme['cfl']))}",
         f"cflStep: {_fmt(scheme.get('cflStep', 0.0))}",
@@ -363,7 +364,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                reynolds: float = 1e5, t_inf: float = 288.0, cfl: float = 100.0,
                wall_t: float | None = None, limiter: str = "vanAlbada",
                name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder",
-               sweeps: int = 1):
+               sweeps: int = 1, rans: bool = False, tint: float = 0.001, vratio: float = 10.0,
+               flux: str = "roe", nblocks: int = 2):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -380,10 +382,12 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
     p_inf = rho_inf * R_AIR * t_inf
     refs = Refs(t_ref=t_inf, r_ref=rho_inf)
     vel = f"[{_fmt(u_inf)}, 0, 0]"
-    ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel})"
+    turb = f"; turbulenceIntensity={_fmt(tint)}; eddyViscosityRatio={_fmt(vratio)}" if rans else ""
+    ic = (f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel}"
+          f"{turb})")
     wall = "viscousWall(tag=2)" if wall_t is None else f"viscousWall(tag=2; temperature={_fmt(wall_t)})"
     states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
-              f"velocity={vel})", wall]
+              f"velocity={vel}{turb})", wall]
     blk0 = [("characteristic", 0, 0, 0, nj, 0, nk, 1),
             ("interblock", ni, ni, 0, nj, 0, nk, 1001),
             ("viscousWall", 0, ni, 0, 0, 0, nk, 2),
@@ -397,8 +401,19 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
             ("slipWall", 0, ni, 0, nj, 0, 0, 4),
             ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
     inp = os.path.join(outdir, name + ".inp")
-    write_input(inp, name, {"cfl": cfl, "limiter": limiter, "equationSet": "navierStokes",
-                            "matrixSolver": matrix_solver, "faceReconstruction": recon,
-                            "matrixSweeps": sweeps},
-                refs, ic, states, [blk0, blk1])
+    scheme = {"cfl": cfl, "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
+              "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
+              "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps}
+    if nblocks == 1:
+        nodes = plate_nodes(0.0, length, ni, nj, nk, dy0, ratio, dz)
+        write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
+        blk = [("characteristic", 0, 0, 0, nj, 0, nk, 1),
+               ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+               ("viscousWall", 0, ni, 0, 0, 0, nk, 2),
+               ("characteristic", 0, ni, nj, nj, 0, nk, 1),
+               ("slipWall", 0, ni, 0, nj, 0, 0, 4),
+               ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
+        write_input(inp, name, scheme, refs, ic, states, [blk])
+    else:
+        write_input(inp, name, scheme, refs, ic, states, [blk0, blk1])
     return inp, None

@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <sstream>
 #include <stdexcept>
 
@@ -938,6 +939,110 @@ void BuildEdgeOps(Setup &st, int solve) {
 
 // ---------------------------------------------------------------------------
 // input file
+// primitive::ApplyFarfieldTurbBC (src/primitive.cpp:83) with
+// primitive::LimitTurb (:100): k = 1.5 (I |v|)^2, omega = rho k / (ratio mu(T)),
+// floors 1e-20 (turbModel::TkeMin / OmegaMin, include/turbulence.hpp:63)
+void FarfieldTurbulence(double *w, double tint, double ratio, const ath_solve_view &ph) {
+  const double vmag = std::sqrt(w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  w[5] = 1.5 * std::pow(tint * vmag, 2.0);
+  const double t = w[4] / (w[0] * ph.gas_r);
+  const double temp = t * ph.t_ref;
+  const double mu = (ph.mu_c1 * std::pow(temp, 1.5)) / (temp + ph.mu_s) / ph.mu_ref;
+  w[6] = w[0] * w[5] / (ratio * mu);
+  w[5] = std::max(w[5], 1.0e-20);
+  w[6] = std::max(w[6], 1.0e-20);
+}
+
+// procBlock::CalcWallDistance (src/procBlock.cpp:6030): distance of every
+// physical cell centre to the nearest viscous-wall face centre of the solve
+// (the reference's k-d tree returns the exact nearest neighbour: the
+// minimum of |c - f|^2, then its square root); non-edge ghost cells take
+// minus the mirrored interior value across a viscous wall, the value of the
+// boundary cell elsewhere; edge ghosts keep the default 1e10.
+void BuildWallDistance(Setup &setup, int solve) {
+  std::vector<double> wf;  // x, y, z of every viscous-wall face centre
+  for (int bi : setup.solves[solve].blocks) {
+    const Block &b = setup.blocks[bi];
+    for (const auto &sf : b.surfs) {
+      if (sf.type != ATH_BC_VISCOUS_WALL) continue;
+      const int d = sf.Dir();
+      const int64_t nf = b.NFace(d);
+      const int ib = d == 0 ? sf.i1 + 1 : sf.i2;
+      const int jb = d == 1 ? sf.j1 + 1 : sf.j2;
+      const int kb = d == 2 ? sf.k1 + 1 : sf.k2;
+      for (int k = sf.k1; k < kb; ++k)
+        for (int j = sf.j1; j < jb; ++j)
+          for (int i = sf.i1; i < ib; ++i) {
+            const int64_t f = b.Face(d, i, j, k);
+            wf.push_back(b.fcenter[d][f]);
+            wf.push_back(b.fcenter[d][nf + f]);
+            wf.push_back(b.fcenter[d][2 * nf + f]);
+          }
+    }
+  }
+  if (wf.empty()) return;
+  const size_t nw = wf.size() / 3;
+  for (int bi : setup.solves[solve].blocks) {
+    Block &b = setup.blocks[bi];
+    const int64_t nc = b.NCell();
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i) {
+          const int64_t c = b.Cell(i, j, k);
+          const double cx = b.center[c], cy = b.center[nc + c], cz = b.center[2 * nc + c];
+          double best = std::numeric_limits<double>::max();
+          for (size_t q = 0; q < nw; ++q) {
+            const double dx = cx - wf[3 * q], dy = cy - wf[3 * q + 1], dz = cz - wf[3 * q + 2];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < best) best = d2;
+          }
+          b.wall_dist[c] = std::sqrt(best);
+        }
+    // boundary condition of the block face crossed by a non-edge ghost
+    auto bc_at = [&](int d, bool lower, const int p[3]) {
+      for (const auto &sf : b.surfs) {
+        if (sf.Dir() != d || sf.Lower() != lower) continue;
+        const int lo[3] = {sf.i1, sf.j1, sf.k1}, hi[3] = {sf.i2, sf.j2, sf.k2};
+        bool in = true;
+        for (int e = 0; e < 3; ++e)
+          if (e != d && (p[e] < lo[e] || p[e] >= hi[e])) in = false;
+        if (in) return sf.type;
+      }
+      return -1;
+    };
+    const int n3[3] = {b.ni, b.nj, b.nk};
+    for (int k = -b.ng; k < b.nk + b.ng; ++k)
+      for (int j = -b.ng; j < b.nj + b.ng; ++j)
+        for (int i = -b.ng; i < b.ni + b.ng; ++i) {
+          const int p[3] = {i, j, k};
+          int d = -1, nout = 0;
+          for (int e = 0; e < 3; ++e)
+            if (p[e] < 0 || p[e] >= n3[e]) {
+              d = e;
+              ++nout;
+            }
+          if (nout != 1) continue;
+          const bool lower = p[d] < 0;
+          int q[3] = {i, j, k};
+          if (bc_at(d, lower, p) == ATH_BC_VISCOUS_WALL) {
+            q[d] = lower ? -p[d] - 1 : n3[d] - (p[d] - n3[d] + 1);
+            b.wall_dist[b.Cell(i, j, k)] = -1.0 * b.wall_dist[b.Cell(q[0], q[1], q[2])];
+          } else {
+            q[d] = lower ? 0 : n3[d] - 1;
+            b.wall_dist[b.Cell(i, j, k)] = b.wall_dist[b.Cell(q[0], q[1], q[2])];
+          }
+        }
+  }
+  // connection ghosts take the partner's value (SwapWallDistSlice,
+  // src/procBlock.cpp:3105); block-edge ghosts are left as they are
+  for (int bi : setup.solves[solve].blocks) {
+    Block &b = setup.blocks[bi];
+    for (const auto &op : b.ops)
+      if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK)
+        b.wall_dist[op.dst] = setup.blocks[op.src_block].wall_dist[op.src];
+  }
+}
+
 void AppendInput(Setup &st, const std::string &path) {
   std::ifstream in(path);
   if (!in) Fail("cannot open input file " + path);
@@ -1037,11 +1142,14 @@ void AppendInput(Setup &st, const std::string &path) {
   if (get("inviscidFluxJacobian", "rusanov") != "rusanov")
     Fail("only the rusanov inviscid flux jacobian is supported");
   if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
-  if (get("turbulenceModel", "none") != "none" && ph.eqn != ATH_EQN_RANS)
-    Fail("turbulence model needs equationSet rans");
-  if (ph.eqn == ATH_EQN_RANS) Fail("equationSet rans is not supported yet");
+  const auto tm = get("turbulenceModel", "none");
+  if (tm != "none" && ph.eqn != ATH_EQN_RANS) Fail("turbulence model needs equationSet rans");
   ph.turb = ATH_TURB_NONE;
-  ph.nv = 5;
+  if (ph.eqn == ATH_EQN_RANS) {
+    if (tm != "sst2003") Fail("only turbulenceModel sst2003 is supported");
+    ph.turb = ATH_TURB_SST2003;
+  }
+  ph.nv = ph.eqn == ATH_EQN_RANS ? 7 : 5;
   // input::NumberGhostLayers (src/input.cpp:1127): 1 constant, 2 MUSCL, 3 WENO
   ph.ng = ph.recon == ATH_RECON_CONSTANT ? 1 : (ph.recon == ATH_RECON_MUSCL ? 2 : 3);
 
@@ -1113,6 +1221,9 @@ void AppendInput(Setup &st, const std::string &path) {
     } else {
       s.type = BCType(name);
       s.tag = (int)num("tag", -1);
+      // DEFAULT_TURB_INTENSITY / DEFAULT_EDDY_VISC_RATIO (include/inputStates.hpp:41)
+      s.turb_intensity = 0.01;
+      s.eddy_visc_ratio = 0.01;
       if (m.count("density")) s.rho = std::stod(m["density"]) / rref;
       if (m.count("pressure")) {
         s.p = std::stod(m["pressure"]) / pscale;
@@ -1152,9 +1263,10 @@ void AppendInput(Setup &st, const std::string &path) {
   }
 
   // initial condition: a uniform icState (tag -1)
-  double ic[5] = {0, 0, 0, 0, 0};
+  double ic[7] = {0, 0, 0, 0, 0, 0, 0};
   {
     bool have = false;
+    double tint = 0.01, vrat = 0.01;
     for (auto &call : SplitList(get("initialConditions", "<>"))) {
       auto pc = ParseCall(call);
       auto &m = pc.second;
@@ -1166,12 +1278,15 @@ void AppendInput(Setup &st, const std::string &path) {
       ic[2] = v[1] / aref;
       ic[3] = v[2] / aref;
       ic[4] = std::stod(m["pressure"]) / pscale;
+      if (m.count("turbulenceIntensity")) tint = std::stod(m["turbulenceIntensity"]);
+      if (m.count("eddyViscosityRatio")) vrat = std::stod(m["eddyViscosityRatio"]);
       have = true;
     }
     if (!have) {
       ic[0] = 1.0;
       ic[4] = 1.0 / 1.4;
     }
+    if (ph.nv == 7) FarfieldTurbulence(ic, tint, vrat, ph);
   }
 
   // grid
@@ -1225,6 +1340,7 @@ void AppendInput(Setup &st, const std::string &path) {
   st.solves.push_back(std::move(sv));
   BuildGhostOps(st, solve);
   BuildEdgeOps(st, solve);
+  if (st.solves[solve].phys.eqn == ATH_EQN_RANS) BuildWallDistance(st, solve);
   // connection ghost geometry changes the donor-side widths only through
   // the ops; recompute nothing else
 }

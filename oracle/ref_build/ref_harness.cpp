@@ -162,17 +162,23 @@ void DumpBlock(Writer &w, const procBlock &blk, const linearSolver *,
   }
   // auxiliary fields used by viscous paths
   {
-    std::vector<double> t, mu, wd;
+    std::vector<double> t, mu, wd, mut, f1, f2;
     for (int k = -ng; k < nk + ng; ++k)
       for (int j = -ng; j < nj + ng; ++j)
         for (int i = -ng; i < ni + ng; ++i) {
           t.push_back(blk.Temperature(i, j, k));
           mu.push_back(blk.Viscosity(i, j, k));
           wd.push_back(blk.WallDist(i, j, k));
+          mut.push_back(blk.EddyViscosity(i, j, k));
+          f1.push_back(blk.F1(i, j, k));
+          f2.push_back(blk.F2(i, j, k));
         }
     w.Put(pre + "temperature", {NK, NJ, NI}, t);
     w.Put(pre + "viscosity", {NK, NJ, NI}, mu);
     w.Put(pre + "walldist", {NK, NJ, NI}, wd);
+    w.Put(pre + "eddyvisc", {NK, NJ, NI}, mut);
+    w.Put(pre + "f1", {NK, NJ, NI}, f1);
+    w.Put(pre + "f2", {NK, NJ, NI}, f2);
   }
   (void)phys;
 }
