@@ -707,7 +707,11 @@ void BuildGhostOps(Setup &st, int solve) {
             op.src2 = -1;
             b.ops.push_back(op);
             if (s.type == ATH_BC_VISCOUS_WALL) {
+              // the wall-adjacent cell supplies the wall distance and the
+              // kinematic viscosity of the omega wall value at every layer
+              const auto A = Ijk(d, ac, d1, b1, d2, b2);
               op.type = ATH_BC_VISCOUS_WALL;
+              op.src2 = b.Cell(A[0], A[1], A[2]);
               b.vops.push_back(op);
             }
           }

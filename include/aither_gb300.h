@@ -109,7 +109,8 @@ typedef struct {
   int32_t lower;      /* 1 = lower surface (normal flipped outward) */
   int32_t state;      /* index into the solve's boundary-state table */
   int64_t face;       /* padded face index of the boundary face (dir) */
-  int64_t src2;       /* edge cells: second donor (-1 when unused) */
+  int64_t src2;       /* edge cells: second donor; viscous-wall cells: the
+                         wall-adjacent cell (-1 when unused) */
 } ath_ghost_op;
 
 /* Boundary-state data, nondimensional (reference inputStates.cpp). */

@@ -30,6 +30,13 @@ typedef struct {
   double *Ab, *Ainvb;  /* [nc][25] block diagonal and its inverse (blusgs) */
   double *vg;          /* [nc][9] cell-averaged velocity gradient (blusgs) */
   uint8_t *wallf[3];   /* [nf] face is a viscous wall */
+  /* RANS (SST-2003): turbulence variables beside the five flow variables */
+  double *Wt, *Rt, *dUt;        /* [nc][2] k, omega; residual; update */
+  double *lamt, *At, *Ainvt;    /* [nc] turbulence radius, scalar diagonal */
+  double *Abt, *Ainvbt;         /* [nc][4] 2x2 block diagonal */
+  double *mutc, *f1c, *f2c;     /* [nc] cell eddy viscosity, blending */
+  double *kgc, *wgc;            /* [nc][3] cell k, omega gradients */
+  double *wd;                   /* [nc] wall distance */
   double force[6];     /* wall forces of the last residual: p A, tau |A| */
   uint8_t *mask;
   double *center;      /* [3][nc] */
@@ -50,6 +57,7 @@ typedef struct {
   double cfl;
   int viscous;
   int block;   /* blusgs: 5x5 Jacobian diagonal and off-diagonals */
+  int rans;    /* SST-2003 turbulence equations */
   int sweeps;  /* matrixSweeps */
 } osolve;
 
@@ -142,12 +150,12 @@ static double lim_vanalbada(double r) {
 }
 /* FaceReconMUSCL (include/reconstruction.hpp:110), limiters
  * src/limiter.cpp:24,36 */
-static void muscl(const double *up2, const double *up1, const double *dw1,
-                  double kappa, int limiter, double uw2, double uw, double dw,
-                  double *out) {
+static void muscl_n(const double *up2, const double *up1, const double *dw1,
+                    double kappa, int limiter, double uw2, double uw, double dw,
+                    double *out, int n) {
   const double dPlus = (uw + uw) / (uw + dw);
   const double dMinus = (uw + uw) / (uw + uw2);
-  for (int v = 0; v < NV; ++v) {
+  for (int v = 0; v < n; ++v) {
     const double r = (1.0e-30 + (dw1[v] - up1[v]) * dPlus) /
                      (1.0e-30 + (up1[v] - up2[v]) * dMinus);
     double l, il;
@@ -169,8 +177,8 @@ static void muscl(const double *up2, const double *up1, const double *dw1,
 /* ------------------------------------------------------------- Roe flux */
 /* RoeFlux (include/inviscidFlux.hpp:260), RoeAveragedState
  * (include/primitive.hpp:245), inviscidFlux::RoeFlux (src/inviscidFlux.cpp:27) */
-static void roe_flux(const double *L, const double *R, const gas_t *g,
-                     const double *n, double *f) {
+static void roe_flux(const double *L, const double *R, const double *Lt, const double *Rt,
+                     const gas_t *g, const double *n, double *f, double *ft) {
   const double denRatio = sqrt(R[0] / L[0]);
   double roe[NV];
   roe[0] = L[0] * denRatio;
@@ -193,6 +201,7 @@ static void roe_flux(const double *L, const double *R, const gas_t *g,
   if (ws < fix) ws = 0.5 * (ws * ws / fix + fix);
   double st = (delta[4] - rhoR * aR * nvd) / (2.0 * aR * aR);
   double wss = ws * st;
+  const double wssL = wss;
   d[0] += wss * mfR;
   d[1] += wss * (roe[1] - aR * n[0]);
   d[2] += wss * (roe[2] - aR * n[1]);
@@ -234,6 +243,24 @@ static void roe_flux(const double *L, const double *R, const gas_t *g,
   for (int v = 0; v < NV; ++v) {
     f[v] = fl[v] + (fr[v] - d[v]);
     f[v] *= 0.5;
+  }
+  if (ft) {
+    /* turbulence: both acoustic waves carry the Roe-averaged k, omega, plus
+     * the turbulence waves (include/inviscidFlux.hpp:311-368) */
+    const double vnL = L[1] * n[0] + L[2] * n[1] + L[3] * n[2];
+    const double vnR = R[1] * n[0] + R[2] * n[1] + R[3] * n[2];
+    for (int q = 0; q < 2; ++q) {
+      const double rt = (Lt[q] + denRatio * Rt[q]) / (1.0 + denRatio);
+      double dq = 0.0;
+      dq += wssL * rt;
+      dq += wss * rt;
+      const double wsT = fabs(velNormR);
+      const double stT = rhoR * (Rt[q] - Lt[q]) + rt * delta[0] - delta[4] * rt / (aR * aR);
+      dq += wsT * stT * 1.0;
+      const double flt = L[0] * vnL * Lt[q], frt = R[0] * vnR * Rt[q];
+      ft[q] = flt + (frt - dq);
+      ft[q] *= 0.5;
+    }
   }
 }
 
@@ -288,7 +315,7 @@ static double beta_int2(double d1, double d2, double dx, double xl, double xh) {
 }
 /* FaceReconWENO (include/reconstruction.hpp:244) with Beta0/1/2 (:186-240);
  * c[5] = (upwind3, upwind2, upwind1, downwind1, downwind2), w[5] widths */
-static void weno(const double *const c[5], const double w[5], int wenoz, double *out) {
+static void weno_n(const double *const c[5], const double w[5], int wenoz, double *out, int n) {
   double c0[3], c1[3], c2[3], full[5];
   lagrange_coeff(w, 2, 2, 2, c0);
   lagrange_coeff(w, 2, 1, 2, c1);
@@ -297,7 +324,7 @@ static void weno(const double *const c[5], const double w[5], int wenoz, double 
   const double lw0 = full[0] / c0[0];
   const double lw1 = full[4] / c2[2];
   const double lw2 = 1.0 - lw0 - lw1;
-  for (int v = 0; v < NV; ++v) {
+  for (int v = 0; v < n; ++v) {
     const double y3 = c[0][v], y2 = c[1][v], y1 = c[2][v], d1 = c[3][v], d2 = c[4][v];
     const double st0 = c0[0] * y3 + c0[1] * y2 + c0[2] * y1;
     const double st1 = c1[0] * y2 + c1[1] * y1 + c1[2] * d1;
@@ -343,8 +370,8 @@ static void weno(const double *const c[5], const double w[5], int wenoz, double 
 /* AUSMFlux (include/inviscidFlux.hpp:396) and inviscidFlux::AUSMFlux
  * (:162), Sign (include/utility.hpp:126) */
 static double sign_of(double x) { return (double)((0.0 < x) - (x < 0.0)); }
-static void ausm_flux(const double *L, const double *R, const gas_t *g, const double *n,
-                      double *f) {
+static void ausm_flux(const double *L, const double *R, const double *Lt, const double *Rt,
+                      const gas_t *g, const double *n, double *f, double *ft) {
   const double vnL = L[1] * n[0] + L[2] * n[1] + L[3] * n[2];
   const double vnR = R[1] * n[0] + R[2] * n[1] + R[3] * n[2];
   const double sosL = sos_of(L, g), sosR = sos_of(R, g);
@@ -385,6 +412,11 @@ static void ausm_flux(const double *L, const double *R, const gas_t *g, const do
   f[2] += R[0] * vr * R[2] + pMinus * R[4] * n[1];
   f[3] += R[0] * vr * R[3] + pMinus * R[4] * n[2];
   f[4] += R[0] * vr * enthalpy_of(R, g);
+  if (ft)
+    for (int q = 0; q < 2; ++q) {
+      ft[q] = L[0] * vl * Lt[q];
+      ft[q] += R[0] * vr * Rt[q];
+    }
 }
 
 /* ------------------------------------------------------ spectral radius */
@@ -464,8 +496,8 @@ static double visc_max_term(const double *w, const gas_t *g) {
   const double a = 4.0 / (3.0 * w[0]), b = gamma_of(g) / w[0];
   return (a < b) ? b : a;
 }
-static double visc_term(double mu, const ath_solve_view *v, const gas_t *g) {
-  return v->visc_scale * (mu / prandtl_of(g) + 0.0 / 0.9);
+static double visc_term(double mu, double mut, const ath_solve_view *v, const gas_t *g) {
+  return v->visc_scale * (mu / prandtl_of(g) + mut / 0.9);
 }
 /* FaceReconCentral (include/reconstruction.hpp:315): coefficients of the
  * lower (upwind) and upper (downwind) cell */
@@ -506,6 +538,19 @@ static void apply_edge_ops(oblock *b, int n, const ath_ghost_op *ops) {
     const ath_ghost_op *op = &ops[o];
     double g[NV];
     const double *a = &b->W[op->src * NV];
+    if (b->Wt) {
+      /* turbulence: copied, or averaged for the averaged edges */
+      double *gt = &b->Wt[op->dst * 2];
+      const double *at = &b->Wt[op->src * 2];
+      if (op->type == ATH_EDGE_AVG) {
+        const double *ct = &b->Wt[op->src2 * 2];
+        gt[0] = 0.5 * (at[0] + ct[0]);
+        gt[1] = 0.5 * (at[1] + ct[1]);
+      } else {
+        gt[0] = at[0];
+        gt[1] = at[1];
+      }
+    }
     if (op->type == ATH_EDGE_COPY) {
       memcpy(g, a, sizeof(g));
     } else if (op->type == ATH_EDGE_AVG) {
@@ -595,16 +640,16 @@ static void rusanov_jac(const double *w, const gas_t *g, const double *n, double
 /* fluxJacobian::ApproxTSLJacobian (include/fluxJacobian.hpp:667), laminar,
  * one species, no diffusion model; vg[r][c] is the velocity gradient
  * tensor (row = derivative direction, as TauNormal reads it) */
-static void tsl_jac(const double *w, double mu_lam, const gas_t *g, const ath_solve_view *v,
-                    const double *n, double mag, double dist, int left, const double *vg,
-                    double *J) {
+static void tsl_jac(const double *w, double mu_lam, double mut_lam, const gas_t *g,
+                    const ath_solve_view *v, const double *n, double mag, double dist,
+                    int left, const double *vg, double *J) {
   const double t = temp_of(w, g);
   const double mu = v->visc_scale * mu_lam;
-  const double mut = v->visc_scale * 0.0;
+  const double mut = v->visc_scale * mut_lam;
   const double velNorm = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
   const double rho = w[0];
   const double k = cond_eff(t, v);
-  const double kt = mut * cp_of(g) / 0.9;
+  const double kt = mut * cp_of(g) / 0.9;  /* turbulent Prandtl number 0.9 */
   /* TauNormal (src/utility.cpp:426) */
   const double lambda = 0.0 - (2.0 / 3.0) * (mu + mut);
   const double trace = vg[0] + vg[4] + vg[8];
@@ -711,6 +756,209 @@ static void mat_inverse(double *a) {
   memcpy(a, I, sizeof(I));
 }
 
+/* ------------------------------------------------------- SST-2003 model */
+/* turbKWSst constants (include/turbulence.hpp:489-501) and the turbulence
+ * floors of turbModel (include/turbulence.hpp:63-64) */
+#define SST_BETASTAR 0.09
+#define SST_SIGMAK1 0.85
+#define SST_SIGMAK2 1.0
+#define SST_SIGMAW1 0.5
+#define SST_SIGMAW2 0.856
+#define SST_BETA1 0.075
+#define SST_BETA2 0.0828
+#define SST_GAMMA1 (5.0 / 9.0)
+#define SST_GAMMA2 0.44
+#define SST_A1 0.31
+#define SST_PRT 0.9
+#define SST_PROD2DEST 10.0
+#define TURB_MIN 1.0e-20
+
+/* std::max / std::min */
+static double cmax(double a, double b) { return (a < b) ? b : a; }
+static double cmin(double a, double b) { return (b < a) ? b : a; }
+/* turbKWSst::BlendedCoeff (src/turbulence.cpp:598) */
+static double blended(double c1, double c2, double f1) { return f1 * c1 + (1.0 - f1) * c2; }
+
+/* primitive::ApplyFarfieldTurbBC (src/primitive.cpp:83) + LimitTurb (:100):
+ * k, omega of state w from the velocity vel, intensity and viscosity ratio */
+static void farfield_turb(const double *w, const double *vel, double tint, double ratio,
+                          const gas_t *g, const ath_solve_view *v, double *kw) {
+  const double vmag = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+  kw[0] = 1.5 * pow(tint * vmag, 2.0);
+  kw[1] = w[0] * kw[0] / (ratio * visc_of(temp_of(w, g), v));
+  kw[0] = cmax(kw[0], TURB_MIN);
+  kw[1] = cmax(kw[1], TURB_MIN);
+}
+
+/* ExtrapolateHoldMixture (src/ghostStates.cpp:693) over the flow and the
+ * turbulence variables */
+static void extrap_hold7(double *g, double *gt, double factor, const double *in,
+                         const double *int_) {
+  const double ghostRho = factor * g[0] - in[0];
+  if (ghostRho <= 0.0) return;
+  const double mf = g[0] / g[0];
+  for (int v = 0; v < NV; ++v) g[v] = factor * g[v] - in[v];
+  for (int v = 0; v < 2; ++v) gt[v] = factor * gt[v] - int_[v];
+  const double r = ghostRho * mf;
+  g[0] = (r > 0.0) ? r : 0.0;
+}
+
+/* tensor DoubleDotTrans of two tensors (include/tensor.hpp:353): sum of the
+ * element-by-element products, accumulated from zero in storage order */
+static double ddot(const double *a, const double *b) {
+  double s = 0.0;
+  for (int e = 0; e < 9; ++e) s += a[e] * b[e];
+  return s;
+}
+
+/* turbKWSst::EddyViscAndBlending (src/turbulence.cpp:668) with Alpha1-3,
+ * CDkw, F1, F2 and EddyVisc (:573-634, include/turbulence.hpp:529); mu is
+ * the (unscaled) laminar viscosity, wd the wall distance, vg the velocity
+ * gradient tensor (row = derivative axis) */
+static void sst_eddy_visc(const double *w, const double *kw, const double *vg,
+                          const double *kg, const double *wg, double mu, double wd,
+                          double scale, double *mut, double *f1, double *f2) {
+  const double k = kw[0], om = kw[1], rho = w[0];
+  const double a1 = scale * sqrt(k) / (SST_BETASTAR * om * (wd + 1.0e-30));
+  const double a2 = scale * scale * 500.0 * mu / ((wd + 1.0e-30) * (wd + 1.0e-30) * rho * om);
+  const double cd = cmax(2.0 * rho * SST_SIGMAW2 / om * (kg[0] * wg[0] + kg[1] * wg[1] +
+                                                          kg[2] * wg[2]),
+                         1.0e-10);
+  const double a3 = 4.0 * rho * SST_SIGMAW2 * k / (cd * (wd + 1.0e-30) * (wd + 1.0e-30));
+  *f1 = tanh(pow(cmin(cmax(a1, a2), a3), 4.0));
+  const double arg2 = cmax(2.0 * a1, a2);
+  *f2 = tanh(arg2 * arg2);
+  double S[9];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) S[r * 3 + q] = 0.5 * (vg[r * 3 + q] + vg[q * 3 + r]);
+  const double msr = sqrt(2.0 * ddot(S, S));
+  *mut = rho * SST_A1 * k / cmax(SST_A1 * om, scale * msr * *f2);
+}
+
+/* turbKWSst::CalcTurbSrc (src/turbulence.cpp:637) with the Boussinesq
+ * Reynolds stress (turbModel::ReynoldsStressDDotVelGrad, :53); returns the
+ * blended beta for the source Jacobian */
+static double sst_source(const double *w, const double *kw, const double *vg,
+                         const double *kg, const double *wg, double mut, double f1,
+                         double scale, double *src) {
+  const double k = kw[0], om = kw[1], rho = w[0];
+  const double inv = 1.0 / scale;
+  const double cd = cmax(2.0 * rho * SST_SIGMAW2 / om * (kg[0] * wg[0] + kg[1] * wg[1] +
+                                                          kg[2] * wg[2]),
+                         1.0e-10);
+  const double gamma = blended(SST_GAMMA1, SST_GAMMA2, f1);
+  const double beta = blended(SST_BETA1, SST_BETA2, f1);
+  const double tkeDest = inv * SST_BETASTAR * (rho * k * om * 1.0);
+  const double omgDest = inv * beta * (rho * om * om);
+  const double lambda = 0.0 - (2.0 / 3.0) * mut;
+  const double tr = vg[0] + vg[4] + vg[8];
+  const double c23 = 2.0 / 3.0 * rho * k;
+  double tau[9];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      const double I = (r == q) ? 1.0 : 0.0;
+      tau[r * 3 + q] = (I * (lambda * tr) + (vg[r * 3 + q] + vg[q * 3 + r]) * mut) - I * c23;
+    }
+  double tkeProd = cmin(scale * ddot(tau, vg), SST_PROD2DEST * tkeDest);
+  tkeProd = cmax(tkeProd, 0.0);
+  double omgProd = gamma * rho / mut * tkeProd;
+  omgProd = cmax(omgProd, 0.0);
+  const double omgCd = scale * (1.0 - f1) * cd;
+  src[0] = tkeProd - tkeDest;
+  src[1] = omgProd - omgDest + omgCd;
+  return beta;
+}
+
+/* turbulence spectral radii and Jacobians (src/turbulence.cpp:105-160,
+ * 749-797): inviscid cell radius |v.n_avg| |A|; viscous cell radius
+ * scale |A|^2/(V rho) (mu + sigma_k mut); face radii; viscous Jacobian */
+static double turb_inv_cell_sr(const double *w, const double *lo, double lom,
+                               const double *hi, double him) {
+  double a[3];
+  for (int q = 0; q < 3; ++q) a[q] = 0.5 * (lo[q] + hi[q]);
+  const double m = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  for (int q = 0; q < 3; ++q) a[q] = a[q] / m;
+  const double fMag = 0.5 * (lom + him);
+  return fabs(w[1] * a[0] + w[2] * a[1] + w[3] * a[2]) * fMag;
+}
+static double turb_visc_cell_sr(const double *w, double lom, double him, double vol,
+                                double mu, double mut, double f1, double scale) {
+  const double fMag = 0.5 * (lom + him);
+  const double length = fMag * fMag / vol;
+  return scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
+}
+static double turb_face_sr(const double *w, const double *n, double mag, double mu,
+                           double mut, double f1, double dist, double scale, int positive,
+                           int viscous) {
+  const double vn = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  double sr = positive ? 0.5 * mag * fabs(vn + fabs(vn)) : 0.5 * mag * fabs(vn - fabs(vn));
+  if (viscous) {
+    const double length = mag / dist;
+    sr += scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
+  }
+  return sr;
+}
+/* 2x2 turbulence part of RusanovFluxJacobian: 0.5 conv +/- 0.5 diss */
+static void turb_rusanov_jac(const double *w, const double *n, double mag, int positive,
+                             double *J) {
+  const double vn = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
+  const double conv = vn * mag, diss = fabs(vn) * mag;
+  const double cj[4] = {0.5 * conv, 0.5 * 0.0, 0.5 * 0.0, 0.5 * conv};
+  const double dj[4] = {0.5 * diss, 0.5 * 0.0, 0.5 * 0.0, 0.5 * diss};
+  for (int e = 0; e < 4; ++e) J[e] = positive ? cj[e] + dj[e] : cj[e] - dj[e];
+}
+/* turbKWSst::ViscJac (src/turbulence.cpp:764) times the sign factor */
+static void turb_visc_jac(const double *w, double mag, double mu, double mut, double f1,
+                          double dist, double scale, double fac, double *J) {
+  const double length = mag / dist;
+  const double j00 = scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
+  const double j11 = scale * length / w[0] * (mu + blended(SST_SIGMAW1, SST_SIGMAW2, f1) * mut);
+  J[0] = fac * j00;
+  J[1] = fac * 0.0;
+  J[2] = fac * 0.0;
+  J[3] = fac * j11;
+}
+/* MatrixInverse of a 2x2 (src/matrix.cpp:57) */
+static void mat_inverse2(double *a) {
+  double I[4] = {1.0, 0.0, 0.0, 1.0};
+  for (int r = 0; r < 2; ++r) {
+    double maxVal = 0.0;
+    int rp = 0;
+    for (int ii = r; ii <= 1; ++ii)
+      if (fabs(a[ii * 2 + r]) > maxVal) {
+        maxVal = fabs(a[ii * 2 + r]);
+        rp = ii;
+      }
+    if (rp != r)
+      for (int cc = 0; cc < 2; ++cc) {
+        double t = a[r * 2 + cc]; a[r * 2 + cc] = a[rp * 2 + cc]; a[rp * 2 + cc] = t;
+        t = I[r * 2 + cc]; I[r * 2 + cc] = I[rp * 2 + cc]; I[rp * 2 + cc] = t;
+      }
+    if (r != 0)
+      for (int ii = 0; ii < r; ++ii) {
+        const double factor = a[r * 2 + ii] / a[ii * 2 + ii];
+        for (int cc = 0; cc < 2; ++cc) a[r * 2 + cc] = a[r * 2 + cc] - factor * a[ii * 2 + cc];
+        for (int cc = 0; cc < 2; ++cc) I[r * 2 + cc] = I[r * 2 + cc] - factor * I[ii * 2 + cc];
+      }
+    const double normFactor = 1.0 / a[r * 2 + r];
+    for (int cc = r; cc < 2; ++cc) a[r * 2 + cc] *= normFactor;
+    for (int cc = 0; cc < 2; ++cc) I[r * 2 + cc] *= normFactor;
+  }
+  {
+    const double factor = a[0 * 2 + 1];
+    for (int cc = 0; cc < 2; ++cc) a[0 * 2 + cc] = a[0 * 2 + cc] - factor * a[1 * 2 + cc];
+    for (int cc = 0; cc < 2; ++cc) I[0 * 2 + cc] = I[0 * 2 + cc] - factor * I[1 * 2 + cc];
+  }
+  memcpy(a, I, sizeof(I));
+}
+static void mat_vec2(const double *M, const double *x, double *out) {
+  for (int r = 0; r < 2; ++r) {
+    double s = 0.0;
+    for (int cc = 0; cc < 2; ++cc) s += M[r * 2 + cc] * x[cc];
+    out[r] = s;
+  }
+}
+
 static void viscous_fluxes(orc_case *c, oblock *b) {
   const osolve *sv = &c->s[b->solve];
   const ath_solve_view *v = &sv->v;
@@ -728,8 +976,27 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           const int64_t cu = cell_idx(b, i, j, k), cl = cu - st[d];
           /* dual-cell face values and area vectors, axes i, j, k */
           double vlo[3][3], vhi[3][3], tlo[3], thi[3], alo[3][3], ahi[3][3];
+          double klo[3] = {0, 0, 0}, khi[3] = {0, 0, 0}, olo[3] = {0, 0, 0}, ohi[3] = {0, 0, 0};
+          const int rans = sv->rans;
+          const double *Tt = b->Wt;
           for (int e = 0; e < 3; ++e) {
             const double *Wl = &b->W[cl * NV], *Wu = &b->W[cu * NV];
+            if (rans) {
+              if (e == d) {
+                klo[e] = Tt[cl * 2];
+                khi[e] = Tt[cu * 2];
+                olo[e] = Tt[cl * 2 + 1];
+                ohi[e] = Tt[cu * 2 + 1];
+              } else {
+                const int64_t up = cu + st[e], lp = cl + st[e], um = cu - st[e], lm = cl - st[e];
+                khi[e] = 0.25 * (((Tt[cl * 2] + Tt[cu * 2]) + Tt[up * 2]) + Tt[lp * 2]);
+                klo[e] = 0.25 * (((Tt[cl * 2] + Tt[cu * 2]) + Tt[um * 2]) + Tt[lm * 2]);
+                ohi[e] = 0.25 * (((Tt[cl * 2 + 1] + Tt[cu * 2 + 1]) + Tt[up * 2 + 1]) +
+                                 Tt[lp * 2 + 1]);
+                olo[e] = 0.25 * (((Tt[cl * 2 + 1] + Tt[cu * 2 + 1]) + Tt[um * 2 + 1]) +
+                                 Tt[lm * 2 + 1]);
+              }
+            }
             if (e == d) {
               for (int q = 0; q < 3; ++q) {
                 vlo[e][q] = Wl[1 + q];
@@ -786,16 +1053,45 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
                     tlo[1] * alo[1][r] + thi[2] * ahi[2][r] - tlo[2] * alo[2][r];
             tg[r] *= invVol;
           }
+          double kg[3] = {0, 0, 0}, wg[3] = {0, 0, 0};
+          if (rans)
+            for (int r = 0; r < 3; ++r) {
+              kg[r] = khi[0] * ahi[0][r] - klo[0] * alo[0][r] + khi[1] * ahi[1][r] -
+                      klo[1] * alo[1][r] + khi[2] * ahi[2][r] - klo[2] * alo[2][r];
+              kg[r] *= invVol;
+              wg[r] = ohi[0] * ahi[0][r] - olo[0] * alo[0][r] + ohi[1] * ahi[1][r] -
+                      olo[1] * alo[1][r] + ohi[2] * ahi[2][r] - olo[2] * alo[2][r];
+              wg[r] *= invVol;
+            }
           /* face state and viscosity by central reconstruction */
           double cd, cuw;
           central_coeffs(wd[cl], wd[cu], &cd, &cuw);
           double fs[NV];
           for (int q = 0; q < NV; ++q) fs[q] = cd * b->W[cu * NV + q] + cuw * b->W[cl * NV + q];
           const double muf = cd * b->mu[cu] + cuw * b->mu[cl];
+          /* SST at the face: k, omega by central reconstruction with the
+           * turbulence floors, wall distance likewise (clipped to 0 within
+           * WALL_DIST_NEG_TOL), eddy viscosity and blending */
+          double fst[2] = {0, 0}, mutf = 0.0, f1f = 0.0, f2f = 0.0;
+          if (rans) {
+            for (int q = 0; q < 2; ++q)
+              fst[q] = cmax(cd * Tt[cu * 2 + q] + cuw * Tt[cl * 2 + q], TURB_MIN);
+            double wdf = cd * b->wd[cu] + cuw * b->wd[cl];
+            if (wdf < 0.0 && wdf > -1.0e-10) wdf = 0.0;
+            sst_eddy_visc(fs, fst, &grad[0][0], kg, wg, muf, wdf, v->visc_scale, &mutf, &f1f,
+                          &f2f);
+          }
           /* viscous flux */
           double n[3], mag;
           face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
-          const double mus = v->visc_scale * muf, muts = v->visc_scale * 0.0;
+          const double mus = v->visc_scale * muf, muts = v->visc_scale * mutf;
+          double Ft[2] = {0, 0};
+          if (rans) {
+            Ft[0] = (mus + blended(SST_SIGMAK1, SST_SIGMAK2, f1f) * muts) *
+                    (kg[0] * n[0] + kg[1] * n[1] + kg[2] * n[2]);
+            Ft[1] = (mus + blended(SST_SIGMAW1, SST_SIGMAW2, f1f) * muts) *
+                    (wg[0] * n[0] + wg[1] * n[1] + wg[2] * n[2]);
+          }
           const double lambda = 0.0 - (2.0 / 3.0) * (mus + muts);
           const double trace = grad[0][0] + grad[1][1] + grad[2][2];
           double tau[3];
@@ -824,7 +1120,7 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           /* block diagonal: ApproxTSLJacobian at the face with the face
            * state, viscosity and gradient, ProjC2CDist as the length; cell
            * gradients: one sixth of each face gradient */
-          double c2c = 0.0, Jt[NJAC];
+          double c2c = 0.0, Jt[NJAC], Jtt[4];
           const double sixth = 1.0 / 6.0;
           if (sv->block) {
             const double dc[3] = {b->center[cu] - b->center[cl],
@@ -834,29 +1130,59 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           }
           if (fpos > 0) {
             for (int q = 0; q < NV; ++q) b->R[cl * NV + q] -= F[q] * mag;
-            if (sv->block) {
+            if (rans) {
+              for (int q = 0; q < 2; ++q) b->Rt[cl * 2 + q] -= Ft[q] * mag;
+              b->mutc[cl] += sixth * mutf;
+              for (int q = 0; q < 3; ++q) b->kgc[cl * 3 + q] += sixth * kg[q];
+              for (int q = 0; q < 3; ++q) b->wgc[cl * 3 + q] += sixth * wg[q];
+              b->f1c[cl] += sixth * f1f;
+              b->f2c[cl] += sixth * f2f;
+            }
+            if (sv->block || rans)
               for (int e = 0; e < 9; ++e) b->vg[cl * 9 + e] += sixth * grad[e / 3][e % 3];
-              tsl_jac(fs, muf, g, v, n, mag, c2c, 1, &grad[0][0], Jt);
+            if (sv->block) {
+              tsl_jac(fs, muf, mutf, g, v, n, mag, c2c, 1, &grad[0][0], Jt);
               for (int e = 0; e < NJAC; ++e) b->Ab[cl * NJAC + e] -= Jt[e];
+              if (rans) {
+                turb_visc_jac(fs, mag, muf, mutf, f1f, c2c, v->visc_scale, -1.0, Jtt);
+                for (int e = 0; e < 4; ++e) b->Abt[cl * 4 + e] -= Jtt[e];
+              }
             }
           }
           if (fpos < nd) {
             for (int q = 0; q < NV; ++q) b->R[cu * NV + q] += F[q] * mag;
-            if (sv->block)
+            if (rans) {
+              for (int q = 0; q < 2; ++q) b->Rt[cu * 2 + q] += Ft[q] * mag;
+              b->mutc[cu] += sixth * mutf;
+              for (int q = 0; q < 3; ++q) b->kgc[cu * 3 + q] += sixth * kg[q];
+              for (int q = 0; q < 3; ++q) b->wgc[cu * 3 + q] += sixth * wg[q];
+              b->f1c[cu] += sixth * f1f;
+              b->f2c[cu] += sixth * f2f;
+            }
+            if (sv->block || rans)
               for (int e = 0; e < 9; ++e) b->vg[cu * 9 + e] += sixth * grad[e / 3][e % 3];
             double nl[3], ml, nh[3], mh;
             face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
             face_normal(b, d, face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
             const double *Wc = &b->W[cu * NV];
             const double fMag = 0.5 * (ml + mh);
-            const double lv = visc_max_term(Wc, g) * visc_term(b->mu[cu], v, g) * fMag * fMag /
-                              b->vol[cu];
+            const double lv = visc_max_term(Wc, g) * visc_term(b->mu[cu], mutf, v, g) * fMag *
+                              fMag / b->vol[cu];
             b->lam[cu] += lv * coeff;
+            const double lvt = rans ? turb_visc_cell_sr(Wc, ml, mh, b->vol[cu], b->mu[cu], mutf,
+                                                        f1f, v->visc_scale)
+                                    : 0.0;
+            if (rans) b->lamt[cu] += lvt * coeff;
             if (sv->block) {
-              tsl_jac(fs, muf, g, v, n, mag, c2c, 0, &grad[0][0], Jt);
+              tsl_jac(fs, muf, mutf, g, v, n, mag, c2c, 0, &grad[0][0], Jt);
               for (int e = 0; e < NJAC; ++e) b->Ab[cu * NJAC + e] += Jt[e];
+              if (rans) {
+                turb_visc_jac(fs, mag, muf, mutf, f1f, c2c, v->visc_scale, 1.0, Jtt);
+                for (int e = 0; e < 4; ++e) b->Abt[cu * 4 + e] += Jtt[e];
+              }
             } else {
               b->A[cu] += 2.0 * lv;
+              if (rans) b->At[cu] += 2.0 * lvt;
             }
           }
         }
@@ -882,6 +1208,7 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     c->s[s].gas.hf = sv[s].gas_hf;
     c->s[s].viscous = sv[s].eqn != ATH_EQN_EULER;
     c->s[s].block = sv[s].solver == ATH_SOLVER_BLUSGS;
+    c->s[s].rans = sv[s].eqn == ATH_EQN_RANS;
     c->s[s].sweeps = sv[s].sweeps > 0 ? sv[s].sweeps : 1;
   }
   for (int bi = 0; bi < nblocks; ++bi) {
@@ -897,17 +1224,40 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
       b->nf[d] = v->nface_padded[d];
       b->fa[d] = (double *)dup_arr(v->farea[d], 8 * 4 * b->nf[d]);
     }
-    b->W = (double *)dup_arr(v->state0, 8 * NV * b->nc);
+    const int rans = c->s[b->solve].rans;
+    b->W = (double *)dup_arr(NULL, 8 * NV * b->nc);
+    for (int64_t x = 0; x < b->nc; ++x)
+      for (int q = 0; q < NV; ++q) b->W[x * NV + q] = v->state0[x * v->nv + q];
+    if (rans) {
+      b->Wt = (double *)dup_arr(NULL, 8 * 2 * b->nc);
+      for (int64_t x = 0; x < b->nc; ++x)
+        for (int q = 0; q < 2; ++q) b->Wt[x * 2 + q] = v->state0[x * v->nv + 5 + q];
+      b->Rt = (double *)dup_arr(NULL, 8 * 2 * b->nc);
+      b->dUt = (double *)dup_arr(NULL, 8 * 2 * b->nc);
+      b->lamt = (double *)dup_arr(NULL, 8 * b->nc);
+      b->At = (double *)dup_arr(NULL, 8 * b->nc);
+      b->Ainvt = (double *)dup_arr(NULL, 8 * b->nc);
+      b->Abt = (double *)dup_arr(NULL, 8 * 4 * b->nc);
+      b->Ainvbt = (double *)dup_arr(NULL, 8 * 4 * b->nc);
+      b->mutc = (double *)dup_arr(NULL, 8 * b->nc);
+      b->f1c = (double *)dup_arr(NULL, 8 * b->nc);
+      b->f2c = (double *)dup_arr(NULL, 8 * b->nc);
+      b->kgc = (double *)dup_arr(NULL, 8 * 3 * b->nc);
+      b->wgc = (double *)dup_arr(NULL, 8 * 3 * b->nc);
+      b->wd = (double *)dup_arr(v->wall_dist, 8 * b->nc);
+    }
     b->R = (double *)dup_arr(NULL, 8 * NV * b->nc);
     b->dU = (double *)dup_arr(NULL, 8 * NV * b->nc);
     b->lam = (double *)dup_arr(NULL, 8 * b->nc);
     b->dt = (double *)dup_arr(NULL, 8 * b->nc);
     b->A = (double *)dup_arr(NULL, 8 * b->nc);
     b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
+    if (c->s[b->solve].block || c->s[b->solve].rans) {
+      b->vg = (double *)dup_arr(NULL, 8 * 9 * b->nc);
+    }
     if (c->s[b->solve].block) {
       b->Ab = (double *)dup_arr(NULL, 8 * NJAC * b->nc);
       b->Ainvb = (double *)dup_arr(NULL, 8 * NJAC * b->nc);
-      b->vg = (double *)dup_arr(NULL, 8 * 9 * b->nc);
     }
     b->mask = (uint8_t *)dup_arr(v->nbr_mask, b->nc);
     b->center = (double *)dup_arr(v->center, 8 * 3 * b->nc);
@@ -920,6 +1270,16 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
                 gk = kk < b->ng || kk >= b->NK - b->ng;
       b->corner[x] = (uint8_t)(gi && gj && gk);
     }
+    /* gridLevel::AuxillaryAndWidths (src/gridLevel.cpp:433): temperature
+     * and viscosity of the physical cells of the initial state */
+    if (c->s[b->solve].viscous)
+      for (int k = 0; k < b->nk; ++k)
+        for (int j = 0; j < b->nj; ++j)
+          for (int i = 0; i < b->ni; ++i) {
+            const int64_t x = cell_idx(b, i, j, k);
+            b->T[x] = temp_of(&b->W[x * NV], &c->s[b->solve].gas);
+            b->mu[x] = visc_of(b->T[x], &c->s[b->solve].v);
+          }
     b->nops = v->nops;
     b->ops = (ath_ghost_op *)dup_arr(v->ops, sizeof(ath_ghost_op) * v->nops);
     b->nedge = v->nedge_ops;
@@ -949,6 +1309,9 @@ void orc_destroy(orc_case *c) {
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
     free(b->Ab); free(b->Ainvb); free(b->vg);
+    free(b->Wt); free(b->Rt); free(b->dUt); free(b->lamt); free(b->At); free(b->Ainvt);
+    free(b->Abt); free(b->Ainvbt); free(b->mutc); free(b->f1c); free(b->f2c);
+    free(b->kgc); free(b->wgc); free(b->wd);
     for (int d = 0; d < 3; ++d) free(b->wallf[d]);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
@@ -1006,6 +1369,13 @@ void orc_fill_ghosts(orc_case *c) {
       const double *in = &src->W[op->src * NV];
       double g[NV];
       memcpy(g, in, sizeof(g));
+      const int rans = sv->rans;
+      const double *int_ = rans ? &src->Wt[op->src * 2] : NULL;
+      double gt[2] = {0.0, 0.0};
+      if (rans) {
+        gt[0] = int_[0];
+        gt[1] = int_[1];
+      }
       if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) {
         double n[3], mag;
         face_normal(b, op->dir, op->face, n, &mag);
@@ -1022,11 +1392,15 @@ void orc_fill_ghosts(orc_case *c) {
         } else if (op->type == ATH_BC_CHARACTERISTIC) {
           const ath_bc_state *bs = &sv->states[op->state];
           const double fr[NV] = {bs->rho, bs->u, bs->v, bs->w, bs->p};
+          const double freeVel[3] = {bs->u, bs->v, bs->w};
           const double vin = in[1] * n[0] + in[2] * n[1] + in[3] * n[2];
           const double sosInt = sos_of(in, &sv->gas);
           const double machInt = fabs(vin) / sosInt;
           if (machInt >= 1.0 && vin < 0.0) {
             memcpy(g, fr, sizeof(g));
+            if (rans)
+              farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
           } else if (machInt >= 1.0 && vin >= 0.0) {
           } else if (machInt < 1.0 && vin < 0.0) {
             const double rhoSoSInt = in[0] * sosInt;
@@ -1039,6 +1413,9 @@ void orc_fill_ghosts(orc_case *c) {
             g[1] = fr[1] - n[0] * dp / rhoSoSInt;
             g[2] = fr[2] - n[1] * dp / rhoSoSInt;
             g[3] = fr[3] - n[2] * dp / rhoSoSInt;
+            if (rans)
+              farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
           } else {
             const double rhoSoSInt = in[0] * sosInt;
             const double dp = in[4] - fr[4];
@@ -1049,17 +1426,35 @@ void orc_fill_ghosts(orc_case *c) {
             g[3] = in[3] + n[2] * dp / rhoSoSInt;
             g[4] = fr[4];
           }
-          extrap_hold(g, 2.0, in);
-          if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
+          if (rans) {
+            extrap_hold7(g, gt, 2.0, in, int_);
+            if (op->layer > 1) {
+              extrap_hold7(g, gt, (double)op->layer, in, int_);
+              farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
+            }
+          } else {
+            extrap_hold(g, 2.0, in);
+            if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
+          }
         } else if (op->type == ATH_BC_SUPERSONIC_INFLOW) {
           const ath_bc_state *bs = &sv->states[op->state];
           g[0] = bs->rho; g[1] = bs->u; g[2] = bs->v; g[3] = bs->w; g[4] = bs->p;
+          if (rans) {
+            const double vel[3] = {bs->u, bs->v, bs->w};
+            farfield_turb(g, vel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas, &sv->v,
+                          gt);
+          }
         } else if (op->type == ATH_BC_SUPERSONIC_OUTFLOW) {
-          if (op->layer > 1)
+          if (op->layer > 1) {
             for (int v = 0; v < NV; ++v) g[v] = (double)op->layer * in[v] - in[v];
+            if (rans)
+              for (int v = 0; v < 2; ++v) gt[v] = (double)op->layer * int_[v] - int_[v];
+          }
         }
       }
       memcpy(&b->W[op->dst * NV], g, sizeof(g));
+      if (rans) memcpy(&b->Wt[op->dst * 2], gt, sizeof(gt));
     }
   }
   PAR_BLOCKS
@@ -1082,6 +1477,18 @@ void orc_residual(orc_case *c) {
     memset(b->lam, 0, 8 * b->nc);
     memset(b->A, 0, 8 * b->nc);
     memset(b->force, 0, sizeof(b->force));
+    if (sv->rans) {
+      memset(b->Rt, 0, 8 * 2 * b->nc);
+      memset(b->lamt, 0, 8 * b->nc);
+      memset(b->At, 0, 8 * b->nc);
+      memset(b->Abt, 0, 8 * 4 * b->nc);
+      memset(b->mutc, 0, 8 * b->nc);
+      memset(b->f1c, 0, 8 * b->nc);
+      memset(b->f2c, 0, 8 * b->nc);
+      memset(b->kgc, 0, 8 * 3 * b->nc);
+      memset(b->wgc, 0, 8 * 3 * b->nc);
+      memset(b->vg, 0, 8 * 9 * b->nc);
+    }
     if (sv->block) {
       memset(b->Ab, 0, 8 * NJAC * b->nc);
       memset(b->vg, 0, 8 * 9 * b->nc);
@@ -1099,16 +1506,42 @@ void orc_residual(orc_case *c) {
             const int64_t cl = cu - st;
             const double *wm1 = &b->W[cl * NV], *w0 = &b->W[cu * NV];
             double fL[NV], fR[NV], f[NV], n[3], mag;
+            double fLt[2] = {0, 0}, fRt[2] = {0, 0}, ft[2] = {0, 0};
             const int recon = sv->v.recon;
+            const int rans = sv->rans;
+            if (rans) {
+              /* k, omega reconstructed like the flow variables */
+              const double *T_ = b->Wt;
+              if (recon == ATH_RECON_CONSTANT) {
+                memcpy(fLt, &T_[cl * 2], sizeof(fLt));
+                memcpy(fRt, &T_[cu * 2], sizeof(fRt));
+              } else if (recon == ATH_RECON_MUSCL) {
+                muscl_n(&T_[(cl - st) * 2], &T_[cl * 2], &T_[cu * 2], sv->v.kappa,
+                        sv->v.limiter, wd[cl - st], wd[cl], wd[cu], fLt, 2);
+                muscl_n(&T_[(cu + st) * 2], &T_[cu * 2], &T_[cl * 2], sv->v.kappa,
+                        sv->v.limiter, wd[cu + st], wd[cu], wd[cl], fRt, 2);
+              } else {
+                const double *cl5[5] = {&T_[(cl - 2 * st) * 2], &T_[(cl - st) * 2],
+                                        &T_[cl * 2], &T_[cu * 2], &T_[(cu + st) * 2]};
+                const double wl5[5] = {wd[cl - 2 * st], wd[cl - st], wd[cl], wd[cu],
+                                       wd[cu + st]};
+                const double *cu5[5] = {&T_[(cu + 2 * st) * 2], &T_[(cu + st) * 2],
+                                        &T_[cu * 2], &T_[cl * 2], &T_[(cl - st) * 2]};
+                const double wu5[5] = {wd[cu + 2 * st], wd[cu + st], wd[cu], wd[cl],
+                                       wd[cl - st]};
+                weno_n(cl5, wl5, recon == ATH_RECON_WENOZ, fLt, 2);
+                weno_n(cu5, wu5, recon == ATH_RECON_WENOZ, fRt, 2);
+              }
+            }
             if (recon == ATH_RECON_CONSTANT) {
               memcpy(fL, wm1, sizeof(fL));
               memcpy(fR, w0, sizeof(fR));
             } else if (recon == ATH_RECON_MUSCL) {
               const double *wm2 = &b->W[(cl - st) * NV], *wp1 = &b->W[(cu + st) * NV];
-              muscl(wm2, wm1, w0, sv->v.kappa, sv->v.limiter, wd[cl - st], wd[cl],
-                    wd[cu], fL);
-              muscl(wp1, w0, wm1, sv->v.kappa, sv->v.limiter, wd[cu + st], wd[cu],
-                    wd[cl], fR);
+              muscl_n(wm2, wm1, w0, sv->v.kappa, sv->v.limiter, wd[cl - st], wd[cl],
+                      wd[cu], fL, NV);
+              muscl_n(wp1, w0, wm1, sv->v.kappa, sv->v.limiter, wd[cu + st], wd[cu],
+                      wd[cl], fR, NV);
             } else {
               const double *wm3 = &b->W[(cl - 2 * st) * NV], *wm2 = &b->W[(cl - st) * NV],
                            *wp1 = &b->W[(cu + st) * NV], *wp2 = &b->W[(cu + 2 * st) * NV];
@@ -1116,35 +1549,50 @@ void orc_residual(orc_case *c) {
               const double wl5[5] = {wd[cl - 2 * st], wd[cl - st], wd[cl], wd[cu], wd[cu + st]};
               const double *cu5[5] = {wp2, wp1, w0, wm1, wm2};
               const double wu5[5] = {wd[cu + 2 * st], wd[cu + st], wd[cu], wd[cl], wd[cl - st]};
-              weno(cl5, wl5, recon == ATH_RECON_WENOZ, fL);
-              weno(cu5, wu5, recon == ATH_RECON_WENOZ, fR);
+              weno_n(cl5, wl5, recon == ATH_RECON_WENOZ, fL, NV);
+              weno_n(cu5, wu5, recon == ATH_RECON_WENOZ, fR, NV);
             }
             face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
             if (sv->v.flux == ATH_FLUX_AUSM)
-              ausm_flux(fL, fR, g, n, f);
+              ausm_flux(fL, fR, fLt, fRt, g, n, f, rans ? ft : NULL);
             else
-              roe_flux(fL, fR, g, n, f);
-            double J[NJAC];
+              roe_flux(fL, fR, fLt, fRt, g, n, f, rans ? ft : NULL);
+            double J[NJAC], Jt[4];
             if (fpos > 0) {
               for (int v = 0; v < NV; ++v) b->R[cl * NV + v] += f[v] * mag;
+              if (rans)
+                for (int v = 0; v < 2; ++v) b->Rt[cl * 2 + v] += ft[v] * mag;
               if (sv->block) {
                 rusanov_jac(fL, g, n, mag, 1, J);
                 for (int e = 0; e < NJAC; ++e) b->Ab[cl * NJAC + e] += J[e];
+                if (rans) {
+                  turb_rusanov_jac(fL, n, mag, 1, Jt);
+                  for (int e = 0; e < 4; ++e) b->Abt[cl * 4 + e] += Jt[e];
+                }
               }
             }
             if (fpos < nd) {
               for (int v = 0; v < NV; ++v) b->R[cu * NV + v] -= f[v] * mag;
+              if (rans)
+                for (int v = 0; v < 2; ++v) b->Rt[cu * 2 + v] -= ft[v] * mag;
               double nl[3], ml, nh[3], mh;
               face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
               face_normal(b, d,
                           face_idx(b, d, i + (d == 0), j + (d == 1), k + (d == 2)), nh, &mh);
               const double lam = inv_cell_specrad(w0, g, nl, ml, nh, mh);
               b->lam[cu] += lam;
+              const double lamt = rans ? turb_inv_cell_sr(w0, nl, ml, nh, mh) : 0.0;
+              if (rans) b->lamt[cu] += lamt;
               if (sv->block) {
                 rusanov_jac(fR, g, n, mag, 0, J);
                 for (int e = 0; e < NJAC; ++e) b->Ab[cu * NJAC + e] -= J[e];
+                if (rans) {
+                  turb_rusanov_jac(fR, n, mag, 0, Jt);
+                  for (int e = 0; e < 4; ++e) b->Abt[cu * 4 + e] -= Jt[e];
+                }
               } else {
                 b->A[cu] += lam;
+                if (rans) b->At[cu] += lamt;
               }
             }
           }
@@ -1156,6 +1604,20 @@ void orc_residual(orc_case *c) {
         double gw[NV];
         viscous_wall_ghost(&b->W[op->src * NV], &sv->states[op->state], g, gw);
         memcpy(&b->W[op->dst * NV], gw, sizeof(gw));
+        if (sv->rans) {
+          /* low-Re wall: k = 0 and omega = 60 nu / (beta1 d^2) at the face
+           * (src/ghostStates.cpp:262-275); nu and d of the wall-adjacent
+           * cell, nu from the previous auxiliary update */
+          const double *it = &b->Wt[op->src * 2];
+          const int64_t a = op->src2;
+          const double nuW = b->mu[a] / b->W[a * NV];
+          const double s_ = sv->v.visc_scale;
+          const double wWall = s_ * s_ * 60.0 * nuW / (b->wd[a] * b->wd[a] * SST_BETA1);
+          double *gt = &b->Wt[op->dst * 2];
+          gt[0] = -1.0 * it[0];
+          gt[1] = 2.0 * wWall - it[1];
+          if (op->layer > 1) gt[1] = (double)op->layer * gt[1] - wWall;
+        }
       }
       apply_edge_ops(b, b->nvedge, b->vedge);
       /* UpdateAuxillaryVariables (src/procBlock.cpp:6171): all but corners */
@@ -1174,12 +1636,59 @@ void orc_residual(orc_case *c) {
    * the connection ghosts from the partner block */
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
-    if (!c->s[b->solve].block) continue;
+    const int rans = c->s[b->solve].rans;
+    if (!c->s[b->solve].block && !rans) continue;
     for (int o = 0; o < b->nops; ++o) {
       const ath_ghost_op *op = &b->ops[o];
       if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) continue;
-      memcpy(&b->vg[op->dst * 9], &c->b[op->src_block].vg[op->src * 9], 8 * 9);
+      const oblock *sb = &c->b[op->src_block];
+      memcpy(&b->vg[op->dst * 9], &sb->vg[op->src * 9], 8 * 9);
+      if (rans) {
+        /* and SwapTurbVars (src/gridLevel.cpp:321): eddy viscosity,
+         * blending functions, k and omega gradients */
+        b->mutc[op->dst] = sb->mutc[op->src];
+        b->f1c[op->dst] = sb->f1c[op->src];
+        b->f2c[op->dst] = sb->f2c[op->src];
+        memcpy(&b->kgc[op->dst * 3], &sb->kgc[op->src * 3], 8 * 3);
+        memcpy(&b->wgc[op->dst * 3], &sb->wgc[op->src * 3], 8 * 3);
+      }
     }
+  }
+  /* procBlock::CalcSrcTerms (src/procBlock.cpp:5956): SST sources of the
+   * physical cells from the cell-averaged gradients, eddy viscosity and
+   * blending; the source Jacobian's radius (negative) is subtracted from
+   * the turbulence radius and diagonal */
+  PAR_BLOCKS
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const osolve *sv = &c->s[b->solve];
+    if (!sv->rans) continue;
+    const double scale = sv->v.visc_scale;
+    const double inv = 1.0 / scale;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          const double *w = &b->W[x * NV], *kw = &b->Wt[x * 2];
+          double src[2];
+          const double beta = sst_source(w, kw, &b->vg[x * 9], &b->kgc[x * 3], &b->wgc[x * 3],
+                                         b->mutc[x], b->f1c[x], scale, src);
+          const double vol = b->vol[x];
+          const double srcSR = -2.0 * SST_BETASTAR * kw[1] * vol * inv;
+          b->lamt[x] -= srcSR;
+          if (sv->block) {
+            const double j00 = -2.0 * SST_BETASTAR * kw[1] * 1.0 * vol * inv;
+            const double j11 = -2.0 * beta * kw[1] * vol * inv;
+            b->Abt[x * 4 + 0] -= j00;
+            b->Abt[x * 4 + 1] -= 0.0;
+            b->Abt[x * 4 + 2] -= 0.0;
+            b->Abt[x * 4 + 3] -= j11;
+          } else {
+            b->A[x] -= 0.0;
+            b->At[x] -= srcSR;
+          }
+          for (int q = 0; q < 2; ++q) b->Rt[x * 2 + q] -= src[q] * vol;
+        }
   }
 }
 
@@ -1194,7 +1703,9 @@ void orc_timestep(orc_case *c) {
       for (int j = 0; j < b->nj; ++j)
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
-          b->dt[x] = cfl * (b->vol[x] / b->lam[x]);
+          /* uncoupledScalar::Max of the flow and turbulence radii */
+          const double lm = b->Wt ? cmax(b->lam[x], b->lamt[x]) : b->lam[x];
+          b->dt[x] = cfl * (b->vol[x] / lm);
         }
   }
 }
@@ -1218,11 +1729,25 @@ void orc_diag_invert(orc_case *c) {
             for (int r = 0; r < NV; ++r) a[r * 5 + r] += diagVolTime;
             memcpy(&b->Ainvb[x * NJAC], a, 8 * NJAC);
             mat_inverse(&b->Ainvb[x * NJAC]);
+            if (b->Wt) {
+              double *at = &b->Abt[x * 4];
+              at[0] *= v->relax;
+              at[3] *= v->relax;
+              at[0] += diagVolTime;
+              at[3] += diagVolTime;
+              memcpy(&b->Ainvbt[x * 4], at, 8 * 4);
+              mat_inverse2(&b->Ainvbt[x * 4]);
+            }
             continue;
           }
           b->A[x] *= v->relax;
           b->A[x] += diagVolTime;
           b->Ainv[x] = 1.0 / b->A[x];
+          if (b->Wt) {
+            b->At[x] *= v->relax;
+            b->At[x] += diagVolTime;
+            b->Ainvt[x] = 1.0 / b->At[x];
+          }
         }
   }
 }
@@ -1233,9 +1758,7 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
                         double *acc) {
   const gas_t *g = &c->s[b->solve].gas;
   const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
-  const int64_t nfst[3] = {1, b->NI + 1, (int64_t)b->NI * (b->NJ + 1)};
-  (void)nfst;
-  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  for (int v = 0; v < NV + 2; ++v) acc[v] = 0.0;
   /* padded (i,j,k) of x */
   const int64_t ii = x % b->NI, jj = (x / b->NI) % b->NJ, kk = x / ((int64_t)b->NI * b->NJ);
   for (int d = 0; d < 3; ++d) {
@@ -1257,7 +1780,8 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
                             b->center[b->nc + up] - b->center[b->nc + lo],
                             b->center[2 * b->nc + up] - b->center[2 * b->nc + lo]};
       dist = dc[0] * n[0] + dc[1] * n[1] + dc[2] * n[2];
-      vsr = mag / dist * visc_max_term(wn, g) * visc_term(b->mu[nb], &sv->v, g);
+      vsr = mag / dist * visc_max_term(wn, g) *
+            visc_term(b->mu[nb], sv->rans ? b->mutc[nb] : 0.0, &sv->v, g);
     }
     if (sv->block) {
       /* RusanovBlockOffDiagonal (src/fluxJacobian.cpp:164) */
@@ -1265,7 +1789,8 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
       rusanov_jac(wn, g, n, mag, lower, J);
       if (sv->viscous) {
         double Tj[NJAC];
-        tsl_jac(wn, b->mu[nb], g, &sv->v, n, mag, dist, lower, &b->vg[nb * 9], Tj);
+        tsl_jac(wn, b->mu[nb], sv->rans ? b->mutc[nb] : 0.0, g, &sv->v, n, mag, dist, lower,
+                &b->vg[nb * 9], Tj);
         for (int e = 0; e < NJAC; ++e) J[e] = lower ? J[e] - Tj[e] : J[e] + Tj[e];
       }
       mat_vec(J, &b->dU[nb * NV], o);
@@ -1273,6 +1798,29 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
       scalar_offdiag(wn, &b->dU[nb * NV], g, n, mag, lower, vsr, o);
     }
     for (int v = 0; v < NV; ++v) acc[v] += o[v];
+    if (sv->rans) {
+      /* turbulence rows: the turbulence face radius (scalar) or the 2x2
+       * Rusanov and viscous Jacobians (block) times the update */
+      const double *dut = &b->dUt[nb * 2];
+      const double scale = sv->v.visc_scale;
+      double ot[2];
+      if (sv->block) {
+        double Jt[4];
+        turb_rusanov_jac(wn, n, mag, lower, Jt);
+        if (sv->viscous) {
+          double Tv[4];
+          turb_visc_jac(wn, mag, b->mu[nb], b->mutc[nb], b->f1c[nb], dist, scale,
+                        lower ? -1.0 : 1.0, Tv);
+          for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
+        }
+        mat_vec2(Jt, dut, ot);
+      } else {
+        const double srt = turb_face_sr(wn, n, mag, b->mu[nb], b->mutc[nb], b->f1c[nb], dist,
+                                        scale, lower, sv->viscous);
+        for (int q = 0; q < 2; ++q) ot[q] = lower ? 0.0 + dut[q] * srt : 0.0 - dut[q] * srt;
+      }
+      for (int q = 0; q < 2; ++q) acc[NV + q] += ot[q];
+    }
   }
 }
 
@@ -1284,8 +1832,27 @@ static void swap_du(orc_case *c) {
       const ath_ghost_op *op = &b->ops[o];
       if (op->type != ATH_BC_PERIODIC && op->type != ATH_BC_INTERBLOCK) continue;
       memcpy(&b->dU[op->dst * NV], &c->b[op->src_block].dU[op->src * NV], 8 * NV);
+      if (b->dUt)
+        memcpy(&b->dUt[op->dst * 2], &c->b[op->src_block].dUt[op->src * 2], 8 * 2);
     }
   }
+}
+
+/* update of cell x as 7 values (flow, then k and omega when present) */
+static void get_du(const oblock *b, int64_t x, double *u) {
+  memcpy(u, &b->dU[x * NV], 8 * NV);
+  u[NV] = b->dUt ? b->dUt[x * 2] : 0.0;
+  u[NV + 1] = b->dUt ? b->dUt[x * 2 + 1] : 0.0;
+}
+static void set_du(oblock *b, int64_t x, const double *u) {
+  memcpy(&b->dU[x * NV], u, 8 * NV);
+  if (b->dUt) memcpy(&b->dUt[x * 2], u + NV, 8 * 2);
+}
+static void get_rhs(const orc_case *c, const oblock *b, int64_t x, double *r) {
+  (void)c;
+  memcpy(r, &b->R[x * NV], 8 * NV);
+  r[NV] = b->Rt ? b->Rt[x * 2] : 0.0;
+  r[NV + 1] = b->Rt ? b->Rt[x * 2 + 1] : 0.0;
 }
 
 /* linearSolver::Residual / AXmB (src/linearSolver.cpp:58,92) and the L2 of
@@ -1295,6 +1862,7 @@ static void swap_du(orc_case *c) {
 static void matrix_residual(orc_case *c) {
   for (int s = 0; s < c->ns; ++s) {
     double sum = 0.0, padded = 0.0, cells = 0.0;
+    const int nv = c->s[s].rans ? NV + 2 : NV;
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       if (b->solve != s) continue;
@@ -1304,25 +1872,32 @@ static void matrix_residual(orc_case *c) {
         for (int j = 0; j < b->nj; ++j)
           for (int i = 0; i < b->ni; ++i) {
             const int64_t x = cell_idx(b, i, j, k);
-            double L[NV], U[NV];
+            double L[NV + 2], U[NV + 2], u[NV + 2], r[NV + 2], Ax[NV + 2];
             offdiag_sum(c, b, x, 1, L);
             offdiag_sum(c, b, x, 0, U);
-            double Ax[NV];
-            if (c->s[s].block) mat_vec(&b->Ab[x * NJAC], &b->dU[x * NV], Ax);
-            for (int v = 0; v < NV; ++v) {
+            get_du(b, x, u);
+            get_rhs(c, b, x, r);
+            if (c->s[s].block) {
+              mat_vec(&b->Ab[x * NJAC], u, Ax);
+              if (b->Wt) mat_vec2(&b->Abt[x * 4], u + NV, Ax + NV);
+            } else {
+              for (int v = 0; v < NV; ++v) Ax[v] = u[v] * b->A[x];
+              if (b->Wt)
+                for (int v = 0; v < 2; ++v) Ax[NV + v] = u[NV + v] * b->At[x];
+            }
+            for (int v = 0; v < nv; ++v) {
               const double off = L[v] - U[v];
-              const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
-              const double ax = c->s[s].block ? Ax[v] : b->dU[x * NV + v] * b->A[x];
-              const double axmb = ax - off - bb;
-              const double r = 0.0 - axmb;
-              bsum += r * r;
+              const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+              const double axmb = Ax[v] - off - bb;
+              const double rr = 0.0 - axmb;
+              bsum += rr * rr;
             }
           }
       sum += bsum;
-      padded += (double)b->nc * NV;
+      padded += (double)b->nc * nv;
       cells += (double)b->ni * b->nj * b->nk;
     }
-    c->mres[s] = sqrt((sum / padded) / (cells * NV));
+    c->mres[s] = sqrt((sum / padded) / (cells * nv));
   }
 }
 
@@ -1331,8 +1906,11 @@ static void apply_ainv(const orc_case *c, const oblock *b, int64_t x, const doub
                        double *out) {
   if (c->s[b->solve].block) {
     mat_vec(&b->Ainvb[x * NJAC], in, out);
+    if (b->Wt) mat_vec2(&b->Ainvbt[x * 4], in + NV, out + NV);
   } else {
     for (int v = 0; v < NV; ++v) out[v] = in[v] * b->Ainv[x];
+    if (b->Wt)
+      for (int v = 0; v < 2; ++v) out[NV + v] = in[NV + v] * b->Ainvt[x];
   }
 }
 
@@ -1348,8 +1926,10 @@ void orc_relax(orc_case *c) {
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
     const osolve *sv = &c->s[b->solve];
+    const int nv = sv->rans ? NV + 2 : NV;
     if (sv->sweeps <= 1) {
       memset(b->dU, 0, 8 * NV * b->nc);
+      if (b->dUt) memset(b->dUt, 0, 8 * 2 * b->nc);
       continue;
     }
     const double thetaInv = 1.0 / sv->v.theta;
@@ -1357,9 +1937,11 @@ void orc_relax(orc_case *c) {
       for (int j = 0; j < b->nj; ++j)
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
-          double in[NV];
-          for (int v = 0; v < NV; ++v) in[v] = -thetaInv * b->R[x * NV + v] + 0.0 - 0.0;
-          apply_ainv(c, b, x, in, &b->dU[x * NV]);
+          double in[NV + 2], r[NV + 2], out[NV + 2];
+          get_rhs(c, b, x, r);
+          for (int v = 0; v < nv; ++v) in[v] = -thetaInv * r[v] + 0.0 - 0.0;
+          apply_ainv(c, b, x, in, out);
+          set_du(b, x, out);
         }
   }
   for (int sw = 0; sw < maxsw; ++sw) {
@@ -1369,22 +1951,25 @@ void orc_relax(orc_case *c) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
       if (sw >= sv->sweeps) continue;
+      const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;
       const int ncell = b->ni * b->nj * b->nk;
       for (int q = 0; q < ncell; ++q) {
         const int64_t x = b->plane_cells[q];
-        double L[NV], U[NV], in[NV];
+        double L[NV + 2], U[NV + 2], in[NV + 2], r[NV + 2], out[NV + 2];
         offdiag_sum(c, b, x, 1, L);
         if (full) {
           offdiag_sum(c, b, x, 0, U);
-          for (int v = 0; v < NV; ++v) L[v] -= U[v];
+          for (int v = 0; v < nv; ++v) L[v] -= U[v];
         }
-        for (int v = 0; v < NV; ++v) {
-          const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+        get_rhs(c, b, x, r);
+        for (int v = 0; v < nv; ++v) {
+          const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
           in[v] = bb + L[v];
         }
-        apply_ainv(c, b, x, in, &b->dU[x * NV]);
+        apply_ainv(c, b, x, in, out);
+        set_du(b, x, out);
       }
     }
     swap_du(c);
@@ -1393,23 +1978,29 @@ void orc_relax(orc_case *c) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
       if (sw >= sv->sweeps) continue;
+      const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;
       const int ncell = b->ni * b->nj * b->nk;
       for (int q = ncell - 1; q >= 0; --q) {
         const int64_t x = b->plane_cells[q];
-        double U[NV], L[NV], in[NV], t[NV];
+        double U[NV + 2], L[NV + 2], in[NV + 2], t[NV + 2], r[NV + 2], out[NV + 2];
         offdiag_sum(c, b, x, 0, U);
         if (full) {
           offdiag_sum(c, b, x, 1, L);
-          for (int v = 0; v < NV; ++v) {
-            const double bb = -thetaInv * b->R[x * NV + v] + 0.0 + 0.0 - 0.0;
+          get_rhs(c, b, x, r);
+          for (int v = 0; v < nv; ++v) {
+            const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
             in[v] = bb + L[v] - U[v];
           }
-          apply_ainv(c, b, x, in, &b->dU[x * NV]);
+          apply_ainv(c, b, x, in, out);
+          set_du(b, x, out);
         } else {
+          double cur[NV + 2];
           apply_ainv(c, b, x, U, t);
-          for (int v = 0; v < NV; ++v) b->dU[x * NV + v] = b->dU[x * NV + v] - t[v];
+          get_du(b, x, cur);
+          for (int v = 0; v < nv; ++v) out[v] = cur[v] - t[v];
+          set_du(b, x, out);
         }
       }
     }
@@ -1422,7 +2013,7 @@ void orc_relax(orc_case *c) {
  * and the L2 sums of src/main.cpp:254-268 */
 int orc_update(orc_case *c, double *l2_out, double *linf_out) {
   int bad = 0;
-  double *l2 = (double *)calloc((size_t)c->ns * NV, sizeof(double));
+  double *l2 = (double *)calloc((size_t)c->ns * (NV + 2), sizeof(double));
   double *linf = (double *)calloc((size_t)c->ns, sizeof(double));
   NTH
   PAR_BLOCKS
@@ -1434,11 +2025,21 @@ int orc_update(orc_case *c, double *l2_out, double *linf_out) {
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
           double w[NV];
+          const double rho0 = b->W[x * NV];
           update_with_cons(&b->W[x * NV], g, &b->dU[x * NV], w);
           if (!(w[0] > 0.0) || !(w[4] > 0.0) || !isfinite(w[1]) || !isfinite(w[2]) ||
               !isfinite(w[3]))
             bad = 1;
           memcpy(&b->W[x * NV], w, sizeof(w));
+          if (b->Wt) {
+            /* conserved rho k, rho omega updated, divided by the new density
+             * and held above the floors (primitive(conserved), LimitTurb) */
+            const double rho1 = rho0 + b->dU[x * NV];
+            for (int q = 0; q < 2; ++q) {
+              const double cq = rho0 * b->Wt[x * 2 + q] + b->dUt[x * 2 + q];
+              b->Wt[x * 2 + q] = cmax(cq / rho1, TURB_MIN);
+            }
+          }
         }
   }
   /* sequential norm sums in the reference's block, k, j, i order */
@@ -1448,14 +2049,17 @@ int orc_update(orc_case *c, double *l2_out, double *linf_out) {
       for (int j = 0; j < b->nj; ++j)
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
-          for (int v = 0; v < NV; ++v) {
-            const double r = b->R[x * NV + v];
-            l2[b->solve * NV + v] += r * r;
+          double rr[NV + 2];
+          get_rhs(c, b, x, rr);
+          const int nv = b->Wt ? NV + 2 : NV;
+          for (int v = 0; v < nv; ++v) {
+            const double r = rr[v];
+            l2[b->solve * (NV + 2) + v] += r * r;
             if (r > linf[b->solve]) linf[b->solve] = r;
           }
         }
   }
-  for (int q = 0; q < c->ns * NV; ++q)
+  for (int q = 0; q < c->ns * (NV + 2); ++q)
     if (l2_out) l2_out[q] = sqrt(l2[q]);
   for (int s = 0; s < c->ns; ++s)
     if (linf_out) linf_out[s] = linf[s];
@@ -1473,7 +2077,7 @@ int orc_iterate(orc_case *c, int n, double *l2_out) {
     orc_timestep(c);
     orc_diag_invert(c);
     orc_relax(c);
-    const int r = orc_update(c, l2_out ? l2_out + (size_t)it * c->ns * NV : NULL, NULL);
+    const int r = orc_update(c, l2_out ? l2_out + (size_t)it * c->ns * (NV + 2) : NULL, NULL);
     if (r) rc = r;
   }
   return rc;
@@ -1482,21 +2086,38 @@ int orc_iterate(orc_case *c, int n, double *l2_out) {
 int orc_get_field(orc_case *c, int block, int field, double *out) {
   if (block < 0 || block >= c->nb) return ATH_ERR_ARG;
   oblock *b = &c->b[block];
+  const int nv = b->Wt ? NV + 2 : NV;
   size_t q = 0;
   if (field == ATH_FIELD_STATE_GHOSTS) {
-    memcpy(out, b->W, 8 * NV * b->nc);
+    for (int64_t x = 0; x < b->nc; ++x) {
+      memcpy(out + nv * x, &b->W[x * NV], 8 * NV);
+      if (b->Wt) memcpy(out + nv * x + NV, &b->Wt[x * 2], 8 * 2);
+    }
     return 0;
   }
   for (int k = 0; k < b->nk; ++k)
     for (int j = 0; j < b->nj; ++j)
       for (int i = 0; i < b->ni; ++i) {
         const int64_t x = cell_idx(b, i, j, k);
+        double u[NV + 2];
         switch (field) {
-          case ATH_FIELD_STATE: memcpy(out + NV * q, &b->W[x * NV], 8 * NV); break;
-          case ATH_FIELD_RESID: memcpy(out + NV * q, &b->R[x * NV], 8 * NV); break;
-          case ATH_FIELD_DU: memcpy(out + NV * q, &b->dU[x * NV], 8 * NV); break;
+          case ATH_FIELD_STATE:
+            memcpy(out + nv * q, &b->W[x * NV], 8 * NV);
+            if (b->Wt) memcpy(out + nv * q + NV, &b->Wt[x * 2], 8 * 2);
+            break;
+          case ATH_FIELD_RESID:
+            get_rhs(c, b, x, u);
+            memcpy(out + nv * q, u, 8 * nv);
+            break;
+          case ATH_FIELD_DU:
+            get_du(b, x, u);
+            memcpy(out + nv * q, u, 8 * nv);
+            break;
           case ATH_FIELD_DT: out[q] = b->dt[x]; break;
-          case ATH_FIELD_SPECRAD: out[2 * q] = b->lam[x]; out[2 * q + 1] = 0.0; break;
+          case ATH_FIELD_SPECRAD:
+            out[2 * q] = b->lam[x];
+            out[2 * q + 1] = b->lamt ? b->lamt[x] : 0.0;
+            break;
           case ATH_FIELD_AINV: out[q] = b->Ainv[x]; break;
           default: return ATH_ERR_ARG;
         }
@@ -1508,11 +2129,14 @@ int orc_get_field(orc_case *c, int block, int field, double *out) {
 int orc_set_state(orc_case *c, int block, const double *prim) {
   if (block < 0 || block >= c->nb) return ATH_ERR_ARG;
   oblock *b = &c->b[block];
+  const int nv = b->Wt ? NV + 2 : NV;
   size_t q = 0;
   for (int k = 0; k < b->nk; ++k)
     for (int j = 0; j < b->nj; ++j)
       for (int i = 0; i < b->ni; ++i) {
-        memcpy(&b->W[cell_idx(b, i, j, k) * NV], prim + NV * q, 8 * NV);
+        const int64_t x = cell_idx(b, i, j, k);
+        memcpy(&b->W[x * NV], prim + nv * q, 8 * NV);
+        if (b->Wt) memcpy(&b->Wt[x * 2], prim + nv * q + NV, 8 * 2);
         ++q;
       }
   return 0;

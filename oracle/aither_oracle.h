@@ -2,7 +2,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the
  * reference solver's (aither v0.10.0) per-iteration algorithm for the
- * inviscid LU-SGS path, used by the parity tests, by smoke checks and as
+ * per-iteration path (Euler, laminar and SST-2003 RANS; scalar and block
+ * LU-SGS), used by the parity tests, by smoke checks and as
  * the timed CPU baseline.  The product library never links or calls it.
  *
  * It consumes the same host setup (geometry, ghost-cell op lists, hyperplane
@@ -46,10 +47,11 @@ void orc_residual(orc_case *c);
 void orc_timestep(orc_case *c);
 void orc_diag_invert(orc_case *c);
 void orc_relax(orc_case *c);
-/* l2_out: nsolves*5 (sqrt taken); linf_out: nsolves (may be NULL) */
+/* l2_out: nsolves*7 (sqrt taken; entries 5 and 6 are the k and omega
+ * equations of RANS solves, 0 otherwise); linf_out: nsolves (may be NULL) */
 int orc_update(orc_case *c, double *l2_out, double *linf_out);
 
-/* n full iterations; l2_out receives n*nsolves*5 values (may be NULL).
+/* n full iterations; l2_out receives n*nsolves*7 values (may be NULL).
  * Returns 0, or -6 when a nonphysical state appeared. */
 int orc_iterate(orc_case *c, int n, double *l2_out);
 

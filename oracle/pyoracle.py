@@ -62,6 +62,8 @@ class Oracle:
         self.nsolves, self.nblocks, self.ncells = setup.counts()
         bv = (BlockView * self.nblocks)(*[setup.block_view(b) for b in range(self.nblocks)])
         sv = (SolveView * self.nsolves)(*[setup.solve_view(s) for s in range(self.nsolves)])
+        # equations per cell: 7 when any solve is RANS (k, omega), else 5
+        self.nv = max(x.nv for x in sv)
         self.h = lib().orc_create(self.nblocks, bv, self.nsolves, sv)
         if threads:
             lib().orc_set_threads(self.h, threads)
@@ -80,11 +82,11 @@ class Oracle:
             pass
 
     def iterate(self, n: int = 1) -> np.ndarray:
-        l2 = np.zeros(n * self.nsolves * 5)
+        l2 = np.zeros(n * self.nsolves * 7)
         self.mres = np.zeros((n, self.nsolves))
         self.forces = np.zeros((n, self.nsolves, 6))
         for it in range(n):
-            rc = lib().orc_iterate(self.h, 1, _dp(l2[it * self.nsolves * 5:]))
+            rc = lib().orc_iterate(self.h, 1, _dp(l2[it * self.nsolves * 7:]))
             if rc:
                 raise RuntimeError(f"oracle reported status {rc}")
             for s in range(self.nsolves):
@@ -92,20 +94,22 @@ class Oracle:
                 f = np.zeros(6)
                 lib().orc_forces(self.h, s, _dp(f))
                 self.forces[it, s] = f
-        return l2.reshape(n, self.nsolves, 5)
+        return l2.reshape(n, self.nsolves, 7)[:, :, :self.nv]
 
     def stage(self, name: str):
         if name == "update":
-            l2 = np.zeros(self.nsolves * 5)
+            l2 = np.zeros(self.nsolves * 7)
             rc = lib().orc_update(self.h, _dp(l2), None)
             if rc:
                 raise RuntimeError(f"oracle reported status {rc}")
-            return l2.reshape(self.nsolves, 5)
+            return l2.reshape(self.nsolves, 7)[:, :self.nv]
         getattr(lib(), "orc_" + name)(self.h)
 
     def field(self, b: int, field: str) -> np.ndarray:
         v = self.setup.block_view(b)
         w = WIDTH[field]
+        if field in ("STATE", "STATE_GHOSTS", "RESID", "DU"):
+            w = v.nv
         n = (v.ncell_padded if field == "STATE_GHOSTS" else v.ni * v.nj * v.nk) * w
         out = np.empty(n)
         rc = lib().orc_get_field(self.h, b, FIELD[field], _dp(out))

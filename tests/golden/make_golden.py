@@ -68,6 +68,17 @@ CASES = [
      dict(ni=10, nj=8, nk=2, dy0=5e-4, ratio=1.35, wall_t=300.0, mach=0.5,
           matrix_solver="blusgs", sweeps=2), [1, 20], True),
     ("plate_c2b", cases.flat_plate, dict(matrix_solver="blusgs", sweeps=4), [20], False),
+    # RANS, SST-2003 (k, omega as equations 6 and 7)
+    ("sst_plate", cases.flat_plate,
+     dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1), [1, 20], True),
+    ("sst_plate2_blusgs", cases.flat_plate,
+     dict(ni=10, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          matrix_solver="blusgs", sweeps=2), [1, 10], True),
+    ("sst_weno_ausm", cases.flat_plate,
+     dict(ni=14, nj=12, nk=3, dy0=5e-5, ratio=1.25, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1, recon="weno", limiter="none", flux="ausm", matrix_solver="blusgs"),
+     [1, 10], True),
 ]
 
 

@@ -21,7 +21,9 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "plate_isothermal_it1", "plate_isothermal_it20", "bump_blusgs_it1", "bump_blusgs_it20",
         "bump_sweeps3_it1", "bump_sweeps3_it20", "bump_blusgs_weno_sw2_it1",
         "bump_blusgs_weno_sw2_it20", "plate_blusgs_it1", "plate_blusgs_it20",
-        "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20"]
+        "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20", "sst_plate_it1", "sst_plate_it20",
+        "sst_plate2_blusgs_it1", "sst_plate2_blusgs_it10", "sst_weno_ausm_it1",
+        "sst_weno_ausm_it10"]
 
 
 def _oracle(inp, st):
@@ -45,6 +47,8 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
         assert rel_err(o.field(b, "RESID"), g[p + "resid"]) <= TOL
         assert rel_err(o.field(b, "DT")[..., 0], g[p + "dt"]) <= TOL
         assert rel_err(o.field(b, "SPECRAD")[..., 0], g[p + "specrad"][..., 0]) <= TOL
+        if g[p + "state"].shape[-1] == 7:  # RANS: the turbulence radius too
+            assert rel_err(o.field(b, "SPECRAD")[..., 1], g[p + "specrad"][..., 1]) <= TOL
         assert rel_err(o.field(b, "DU"), g[p + "du"]) <= TOL
     assert rel_err(l2[:, 0, :], g["l2"]) <= TOL
     if "forces" in g and np.abs(g["forces"]).max() > 0:
