@@ -141,7 +141,8 @@ def lib() -> C.CDLL:
             "ath_batch_update": (C.c_int, [vp, C.POINTER(Norms)]),
             "ath_batch_get_field": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
-            "ath_batch_field_width": (C.c_int, [vp, C.c_int]),
+            "ath_batch_field_width": (C.c_int, [vp, C.c_int, C.c_int]),
+            "ath_batch_pool_vars": (C.c_int, [vp, C.POINTER(C.c_int)]),
             "ath_batch_stats": (C.c_int, [vp, C.POINTER(Stats)]),
             "ath_batch_pool_cells": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "ath_batch_copy_state": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
@@ -322,7 +323,7 @@ class Batch:
     def field(self, b: int, field: str) -> np.ndarray:
         v = self.setup.block_view(b)
         fid = FIELD[field]
-        w = lib().ath_batch_field_width(self.h, fid)
+        w = lib().ath_batch_field_width(self.h, b, fid)
         if w < 0:
             check(w)
         n = (v.ncell_padded if field == "STATE_GHOSTS" else v.ni * v.nj * v.nk) * w
@@ -339,6 +340,12 @@ class Batch:
     def pool_cells(self) -> int:
         n = C.c_int64()
         check(lib().ath_batch_pool_cells(self.h, C.byref(n)))
+        return n.value
+
+    def pool_vars(self) -> int:
+        """Values per cell of the copy_state snapshot (5, or 7 with SST)."""
+        n = C.c_int()
+        check(lib().ath_batch_pool_vars(self.h, C.byref(n)))
         return n.value
 
     def copy_state(self, host: np.ndarray, to_device: bool) -> None:
@@ -374,7 +381,7 @@ class Server:
         i = C.c_int64()
         check(lib().ath_server_submit(self.h, inp_path.encode(), C.byref(i)))
         s = Setup(inp_path)
-        self.shapes[i.value] = [(v.nk, v.nj, v.ni) for v in
+        self.shapes[i.value] = [(v.nk, v.nj, v.ni, v.nv) for v in
                                 (s.block_view(b) for b in range(s.counts()[1]))]
         s.close()
         return i.value
@@ -391,10 +398,10 @@ class Server:
         return [out[i] for i in range(n.value)]
 
     def fetch(self, rid: int, block: int = 0) -> np.ndarray:
-        nk, nj, ni = self.shapes[rid][block]
-        out = np.empty(nk * nj * ni * 5)
+        nk, nj, ni, nv = self.shapes[rid][block]
+        out = np.empty(nk * nj * ni * nv)
         check(lib().ath_server_fetch(self.h, rid, block, dptr(out)))
-        return out.reshape(nk, nj, ni, 5)
+        return out.reshape(nk, nj, ni, nv)
 
     def release(self, rid: int) -> None:
         check(lib().ath_server_release(self.h, rid))

@@ -124,6 +124,9 @@ struct BatchCore {
   int max_sweeps = 1;   // largest matrixSweeps of the batch
   int sweep_threads = 128;  // CTA size of the sweep kernels (autotuned)
   bool block_viscous = false;
+  bool any_rans = false;  // SST solves present: k, omega pools allocated
+  int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
+  int vkinds = 0;  // bit 0: laminar viscous solves, bit 1: SST
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::unique_ptr<DevMem> mem;
@@ -176,7 +179,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
   if (s >= nsolves) return;
   const int lane = threadIdx.x;
   const int c0 = solve_cta0[s], c1 = solve_cta0[s + 1];
-  double l2[kNv] = {0, 0, 0, 0, 0};
+  double l2[kNvMax] = {0, 0, 0, 0, 0, 0, 0};
   double mx = 0.0, mres = 0.0;
   int64_t mpos = INT64_MAX;
   int bad = 0;
@@ -184,7 +187,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
     if (mres_partials) mres += mres_partials[c];
     const NormPartial p = partials[c];
 #pragma unroll
-    for (int v = 0; v < kNv; ++v) l2[v] += p.l2[v];
+    for (int v = 0; v < kNvMax; ++v) l2[v] += p.l2[v];
     if (p.linf > mx || (p.linf == mx && p.linf_pos < mpos)) {
       mx = p.linf;
       mpos = p.linf_pos;
@@ -194,7 +197,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
-    for (int v = 0; v < kNv; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    for (int v = 0; v < kNvMax; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
     const double om = __shfl_down_sync(0xffffffffu, mx, off);
     const int64_t op = __shfl_down_sync(0xffffffffu, mpos, off);
     if (om > mx || (om == mx && op < mpos)) {
@@ -209,7 +212,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
   if (lane == 0) {
     const SolveDev sv = solves[s];
     NormOut o;
-    for (int v = 0; v < 7; ++v) o.l2[v] = v < kNv ? sqrt(l2[v]) : 0.0;
+    for (int v = 0; v < 7; ++v) o.l2[v] = sqrt(l2[v]);
     o.linf = mx;
     o.linf_pos = mpos;
     o.bad = sv.active ? bad : 2;
@@ -217,7 +220,8 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
     o.cfl = cfl[s];
     // src/mgSolution.cpp:196-206 divides by the padded size, src/main.cpp:271
     // by cells x equations
-    o.matrix_resid = mres_partials ? sqrt((mres / sv.padded_values) / (sv.cells * kNv)) : 0.0;
+    const double nv = sv.rans ? (double)kNvMax : (double)kNv;
+    o.matrix_resid = mres_partials ? sqrt((mres / sv.padded_values) / (sv.cells * nv)) : 0.0;
     ring[(it % ring_cap) * nsolves + s] = o;
     if (sv.active) {
       // retirement: the drop of the total L2 against the solve's first
@@ -225,7 +229,7 @@ __global__ void k_norms(const NormPartial *partials, const double *mres_partials
       // first iteration's norms, src/main.cpp:254-271)
       SolveState &ss = sstate[s];
       double tot = 0.0;
-      for (int v = 0; v < kNv; ++v) tot += o.l2[v] * o.l2[v];
+      for (int v = 0; v < 7; ++v) tot += o.l2[v] * o.l2[v];
       tot = sqrt(tot);
       uint64_t now;
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
@@ -369,6 +373,7 @@ class Runner : public RunnerBase {
     P_.ghost_cell = m.Upload(c.L.ghost_cell);
     P_.ghost_src = m.Upload(c.L.ghost_src);
     for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(double)), "memset");
+    if (c.any_rans) AllocTurbulence(m, n, nq, ngh);
     // geometry and state
     std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
     for (int d = 0; d < 3; ++d) {
@@ -398,8 +403,24 @@ class Runner : public RunnerBase {
         }
       }
     }
-    P_.W = P_.W;
     Check(cudaMemcpy(P_.W, W.data(), W.size() * 8, cudaMemcpyHostToDevice), "upload");
+    if (c.any_rans) {
+      // k, omega of the initial state and the wall distance (0 outside
+      // RANS solves)
+      std::vector<double> Wt(2 * n, 0.0), wd(n, 0.0);
+      for (int bi = 0; bi < c.nblocks; ++bi) {
+        const Block &b = c.setup->blocks[bi];
+        if (b.nv < 7) continue;
+        const int64_t o = c.cell0[bi];
+        for (int64_t x = 0; x < b.NCell(); ++x) {
+          Wt[o + x] = b.state0[x * b.nv + 5];
+          Wt[n + o + x] = b.state0[x * b.nv + 6];
+          if (!b.wall_dist.empty()) wd[o + x] = b.wall_dist[x];
+        }
+      }
+      Check(cudaMemcpy(P_.Wt, Wt.data(), Wt.size() * 8, cudaMemcpyHostToDevice), "upload");
+      P_.wd = m.Upload(wd);
+    }
     P_.vol = m.Upload(vol);
     for (int d = 0; d < 3; ++d) {
       P_.width[d] = m.Upload(wid[d]);
@@ -409,6 +430,7 @@ class Runner : public RunnerBase {
     P_.solves = c.d_solves;
     P_.states = c.d_states;
     P_.cfl = c.d_cfl;
+    if (c.L.any_viscous) InitialViscosity(m);
   }
 
   ~Runner() override {
@@ -417,6 +439,55 @@ class Runner : public RunnerBase {
   }
 
   const Pools<T> &P() const { return P_; }
+
+  // k, omega and their residual, fluxes, radii, sweep arrays and the
+  // per-face SST data (gradients, eddy viscosity, blending)
+  void AllocTurbulence(DevMem &m, int64_t n, int64_t nq, int64_t ngh) {
+    auto zero = [&](auto *p, size_t count) {
+      Check(cudaMemset(p, 0, count * sizeof(*p)), "memset");
+      return p;
+    };
+    P_.Wt = zero(m.Alloc<double>(2 * n), 2 * n);
+    P_.Rt = zero(m.Alloc<double>(2 * n), 2 * n);
+    P_.lamt = zero(m.Alloc<double>(n), n);
+    for (int d = 0; d < 3; ++d) {
+      P_.fluxt[d] = zero(m.Alloc<double>(2 * n), 2 * n);
+      P_.vfluxt[d] = zero(m.Alloc<T>(2 * n), 2 * n);
+      P_.rst[d] = zero(m.Alloc<T>(18 * n), 18 * n);
+    }
+    const int64_t aw = (c_.kinds & 2) ? 4 : 1;
+    P_.Rtq = zero(m.Alloc<T>(2 * nq), 2 * nq);
+    P_.dUtq = zero(m.Alloc<T>(2 * nq), 2 * nq);
+    const int64_t g = std::max<int64_t>(ngh, 1);
+    P_.dUtg = zero(m.Alloc<T>(2 * g), 2 * g);
+    P_.Ainvtq = zero(m.Alloc<T>(aw * nq), aw * nq);
+    P_.Atq = zero(m.Alloc<T>(aw * nq), aw * nq);
+    P_.mutq = zero(m.Alloc<T>(nq), nq);
+    P_.f1q = zero(m.Alloc<T>(nq), nq);
+  }
+
+  // gridLevel::AuxillaryAndWidths (src/gridLevel.cpp:433): laminar
+  // viscosity of the physical cells of the initial state (the wall ghost
+  // omega of the first iteration reads it)
+  void InitialViscosity(DevMem &m) {
+    std::vector<int32_t> cells, blk;
+    for (int bi = 0; bi < c_.nblocks; ++bi) {
+      const Block &b = c_.setup->blocks[bi];
+      if (c_.setup->solves[b.solve].phys.eqn == ATH_EQN_EULER) continue;
+      for (int k = 0; k < b.nk; ++k)
+        for (int j = 0; j < b.nj; ++j)
+          for (int i = 0; i < b.ni; ++i) {
+            cells.push_back((int32_t)(c_.cell0[bi] + b.Cell(i, j, k)));
+            blk.push_back(bi);
+          }
+    }
+    if (cells.empty()) return;
+    int32_t *dc = m.Upload(cells), *db = m.Upload(blk);
+    Launch<T>::Aux(P_, dc, db, (int)cells.size(), c_.stream);
+    Check(cudaStreamSynchronize(c_.stream), "sync");
+    m.Free(dc);
+    m.Free(db);
+  }
 
   void StartIteration() {
     k_cfl<<<(c_.nsolves + 127) / 128, 128, 0, c_.stream>>>(c_.d_solves, c_.nsolves,
@@ -439,7 +510,7 @@ class Runner : public RunnerBase {
     Launch<T>::Aux(P_, c_.d_aux_cells, c_.d_aux_block, (int)c_.L.aux_cells.size(), c_.stream);
     for (int d = 0; d < 3; ++d)
       Launch<T>::ViscFace(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
-                          (int)c_.L.face_cta_block[d].size(), c_.stream);
+                          (int)c_.L.face_cta_block[d].size(), c_.vkinds, c_.stream);
     const int nw = (int)c_.L.wall_faces.size();
     if (nw > 0) {
       Launch<T>::Wall(P_, c_.d_wall_faces, nw, c_.d_wbuf, c_.stream);
@@ -450,7 +521,7 @@ class Runner : public RunnerBase {
   void Residual() override {
     for (int d = 0; d < 3; ++d)
       Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
-                      (int)c_.L.face_cta_block[d].size(), c_.stream);
+                      (int)c_.L.face_cta_block[d].size(), c_.fkinds, c_.stream);
     Viscous();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                     c_.kinds, c_.stream);
@@ -471,14 +542,19 @@ class Runner : public RunnerBase {
       }
     }
   }
+  void ZeroGhostUpdates() {
+    if (P_.nghost <= 0) return;
+    Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
+    if (P_.dUtg)
+      Check(cudaMemsetAsync(P_.dUtg, 0, 2 * P_.nghost * sizeof(T), c_.stream), "memset");
+  }
   // lusgs::Relax (src/linearSolver.cpp:430): dU ghost swap before every
   // pass and after the last one
   void Relax() override {
     if (c_.max_sweeps <= 1) {
       // x = 0 before the first sweep: only the connection ghosts are read
       // before being written
-      if (P_.nghost > 0)
-        Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
+      ZeroGhostUpdates();
       SweepPass(1, 0);
       Launch<T>::ConnDu(P_, c_.stream);
       SweepPass(0, 0);
@@ -535,7 +611,7 @@ class Runner : public RunnerBase {
       Check(cudaEventRecord(e[1], c_.stream), "event");
       for (int d = 0; d < 3; ++d) {
         Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
-                        (int)c_.L.face_cta_block[d].size(), c_.stream);
+                        (int)c_.L.face_cta_block[d].size(), c_.fkinds, c_.stream);
         Check(cudaEventRecord(e[2 + d], c_.stream), "event");
       }
       Viscous();
@@ -546,8 +622,8 @@ class Runner : public RunnerBase {
       // split of a multi-sweep relaxation puts each sweep's passes in turn)
       if (c_.max_sweeps > 1)
         Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
-      else if (P_.nghost > 0)
-        Check(cudaMemsetAsync(P_.dUg, 0, 5 * P_.nghost * sizeof(T), c_.stream), "memset");
+      else
+        ZeroGhostUpdates();
       float fwd = 0.f, bwd = 0.f;
       for (int sw = 0; sw < c_.max_sweeps; ++sw) {
         if (c_.max_sweeps > 1) Launch<T>::ConnDu(P_, c_.stream);
@@ -592,6 +668,7 @@ class Runner : public RunnerBase {
     const size_t wbytes = 5 * (size_t)c_.ncell * sizeof(double);
     if (!snap_w_) {
       snap_w_ = m.Alloc<double>(5 * (size_t)c_.ncell);
+      if (P_.Wt) snap_wt_ = m.Alloc<double>(2 * (size_t)c_.ncell);
       snap_ss_ = m.Alloc<SolveState>(c_.nsolves);
       snap_sv_ = m.Alloc<SolveDev>(c_.nsolves);
       snap_cfl_ = m.Alloc<double>(c_.nsolves);
@@ -602,6 +679,7 @@ class Runner : public RunnerBase {
     };
     if (!restore) {
       cp(snap_w_, P_.W, wbytes);
+      if (P_.Wt) cp(snap_wt_, P_.Wt, wbytes / 5 * 2);
       cp(snap_ss_, c_.d_sstate, c_.nsolves * sizeof(SolveState));
       cp(snap_sv_, c_.d_solves, c_.nsolves * sizeof(SolveDev));
       cp(snap_cfl_, c_.d_cfl, c_.nsolves * sizeof(double));
@@ -609,6 +687,7 @@ class Runner : public RunnerBase {
       snap_iter_host_ = c_.iter_host;
     } else {
       cp(P_.W, snap_w_, wbytes);
+      if (P_.Wt) cp(P_.Wt, snap_wt_, wbytes / 5 * 2);
       cp(c_.d_sstate, snap_ss_, c_.nsolves * sizeof(SolveState));
       cp(c_.d_solves, snap_sv_, c_.nsolves * sizeof(SolveDev));
       cp(c_.d_cfl, snap_cfl_, c_.nsolves * sizeof(double));
@@ -621,14 +700,20 @@ class Runner : public RunnerBase {
     if (!snap_w_) return;
     DevMem &m = *c_.mem;
     m.Free(snap_w_);
+    if (snap_wt_) m.Free(snap_wt_);
+    snap_wt_ = nullptr;
     m.Free(snap_ss_);
     m.Free(snap_sv_);
     m.Free(snap_cfl_);
     m.Free(snap_it_);
     snap_w_ = nullptr;
   }
-  void GetDU(int b, double *out) override { CopyOutQ(P_.dUq, 5, b, out); }
-  void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, b, out); }
+  void GetDU(int b, double *out) override {
+    const int nv = c_.setup->blocks[b].nv;
+    CopyOutQ(P_.dUq, 5, nv, 0, b, out);
+    if (nv > 5) CopyOutQ(P_.dUtq, 2, nv, 5, b, out);
+  }
+  void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, 1, 0, b, out); }
 
  private:
   template <typename U>
@@ -649,9 +734,10 @@ class Runner : public RunnerBase {
     std::memcpy(out, tmp.data(), tmp.size() * sizeof(double));
   }
 
-  // q-ordered array -> physical cells of block bi, AoS, k slowest
+  // q-ordered array of w values -> physical cells of block bi, AoS with
+  // `stride` values per cell starting at `voff`, k slowest
   template <typename U>
-  void CopyOutQ(const U *arr, int w, int bi, double *out) {
+  void CopyOutQ(const U *arr, int w, int stride, int voff, int bi, double *out) {
     const Block &b = c_.setup->blocks[bi];
     const int64_t cnt = (int64_t)b.ni * b.nj * b.nk, q0 = c_.L.q0[bi];
     std::vector<U> h(cnt);
@@ -663,13 +749,14 @@ class Runner : public RunnerBase {
       for (int k = 0; k < b.nk; ++k)
         for (int j = 0; j < b.nj; ++j)
           for (int i = 0; i < b.ni; ++i)
-            out[(q++) * w + v] = (double)h[c_.L.qpos[c_.cell0[bi] + b.Cell(i, j, k)] - q0];
+            out[(q++) * stride + voff + v] =
+                (double)h[c_.L.qpos[c_.cell0[bi] + b.Cell(i, j, k)] - q0];
     }
   }
 
   BatchCore &c_;
   Pools<T> P_{};
-  double *snap_w_ = nullptr, *snap_cfl_ = nullptr;
+  double *snap_w_ = nullptr, *snap_wt_ = nullptr, *snap_cfl_ = nullptr;
   SolveState *snap_ss_ = nullptr;
   SolveDev *snap_sv_ = nullptr;
   int64_t *snap_it_ = nullptr, snap_iter_host_ = 0;
@@ -681,6 +768,7 @@ struct ath_batch {
   ath::BatchCore core;
   std::unique_ptr<ath::RunnerBase> run;
   double *W = nullptr, *R = nullptr, *dt = nullptr, *lam = nullptr;
+  double *Wt = nullptr, *Rt = nullptr, *lamt = nullptr;  // RANS solves only
 };
 
 namespace ath {
@@ -939,14 +1027,20 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.flags = flags;
   c.nsolves = (int)st.solves.size();
   c.nblocks = (int)st.blocks.size();
-  for (const auto &b : st.blocks)
-    if (b.nv != 5 || b.ng < 1)
+  for (const auto &b : st.blocks) {
+    const bool rans = st.solves[b.solve].phys.eqn == ATH_EQN_RANS;
+    if (b.nv != (rans ? 7 : 5) || b.ng < 1)
       throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
+    if (rans) c.any_rans = true;
+  }
   for (const auto &sv : st.solves) {
     const bool blk = sv.phys.solver == ATH_SOLVER_BLUSGS;
     c.kinds |= blk ? 2 : 1;
     c.max_sweeps = std::max(c.max_sweeps, (int)sv.phys.sweeps);
     if (blk && sv.phys.eqn != ATH_EQN_EULER) c.block_viscous = true;
+    const bool rans = sv.phys.eqn == ATH_EQN_RANS;
+    c.fkinds |= rans ? 2 : 1;
+    if (sv.phys.eqn != ATH_EQN_EULER) c.vkinds |= rans ? 2 : 1;
   }
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");
   BuildLists(c);
@@ -986,12 +1080,13 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.k_ref = p.k_ref;
     x.visc_coeff = p.visc_cfl_coeff;
     x.block = p.solver == ATH_SOLVER_BLUSGS;
+    x.rans = p.eqn == ATH_EQN_RANS;
     x.sweeps = p.sweeps;
     x.active = 1;
     x.padded_values = 0.0;
     x.cells = 0.0;
     for (int b : st.solves[s].blocks) {
-      x.padded_values += (double)st.blocks[b].NCell() * kNv;
+      x.padded_values += (double)st.blocks[b].NCell() * st.blocks[b].nv;
       x.cells += (double)st.blocks[b].ni * st.blocks[b].nj * st.blocks[b].nk;
     }
     x.nstates = (int32_t)st.solves[s].states.size();
@@ -1047,6 +1142,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->R = r->P().R;
     B->dt = r->P().dt;
     B->lam = r->P().lam;
+    B->Wt = r->P().Wt;
+    B->Rt = r->P().Rt;
+    B->lamt = r->P().lamt;
   } else if (precision == ATH_PREC_MIXED) {
     auto *r = new Runner<float>(c);
     B->run.reset(r);
@@ -1054,6 +1152,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->R = r->P().R;
     B->dt = r->P().dt;
     B->lam = r->P().lam;
+    B->Wt = r->P().Wt;
+    B->Rt = r->P().Rt;
+    B->lamt = r->P().lamt;
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
@@ -1065,11 +1166,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
   }
   const int nkinds = (c.kinds & 1) + ((c.kinds >> 1) & 1);
+  const int nf = (c.fkinds & 1) + ((c.fkinds >> 1) & 1);
+  const int nvf = (c.vkinds & 1) + ((c.vkinds >> 1) & 1);
   const int conn = c.L.ghost_cell.empty() ? 0 : 1;
   c.launches_per_iter = edge_phases +
-                        (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 : 0) +
+                        (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 * nvf
+                                         : 0) +
                         (c.L.wall_faces.empty() ? 0 : 2) +
-                        1 + (c.L.ops.empty() ? 0 : 1) + 3 + nkinds +
+                        1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds +
                         2 * c.nsteps * c.max_sweeps * nkinds +
                         (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn) + 3 +
                         ((flags & 1) ? nkinds + conn : 0);
@@ -1103,8 +1207,8 @@ void ReadNorms(BatchCore &c, int64_t it0, int n, ath_norms *norms_h) {
         d.force[q2] = fring[((it % c.ring_cap) * c.nsolves + s) * 6 + q2];
       d.linf_block = d.linf_i = d.linf_j = d.linf_k = d.linf_eqn = -1;
       if (o.linf_pos != INT64_MAX) {
-        const int64_t cellpos = o.linf_pos / kNv;
-        d.linf_eqn = (int32_t)(o.linf_pos % kNv) + 1;
+        const int64_t cellpos = o.linf_pos / kNvMax;
+        d.linf_eqn = (int32_t)(o.linf_pos % kNvMax) + 1;
         const auto &blocks = st.solves[s].blocks;
         for (size_t bi = 0; bi < blocks.size(); ++bi) {
           const Block &b = st.blocks[blocks[bi]];
@@ -1377,14 +1481,14 @@ int ath_batch_update(ath_batch *batch, ath_norms *norms_h) {
   });
 }
 
-int ath_batch_field_width(ath_batch *batch, int field) {
-  if (!batch) return ATH_ERR_ARG;
+int ath_batch_field_width(ath_batch *batch, int block, int field) {
+  if (!batch || block < 0 || block >= batch->core.nblocks) return ATH_ERR_ARG;
   switch (field) {
     case ATH_FIELD_STATE:
     case ATH_FIELD_STATE_GHOSTS:
     case ATH_FIELD_RESID:
     case ATH_FIELD_DU:
-      return 5;
+      return batch->core.setup->blocks[block].nv;
     case ATH_FIELD_DT:
     case ATH_FIELD_AINV:
       return 1;
@@ -1404,40 +1508,45 @@ int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h) {
     Check(cudaStreamSynchronize(c.stream), "sync");
     const ath::Block &b = c.setup->blocks[block];
     const int64_t nc = b.NCell(), o = c.cell0[block], n = c.ncell;
-    auto gather = [&](const double *pool, int w, bool ghosts) {
+    const int nv = b.nv;
+    // w values of an SoA pool -> AoS output with `stride` values per cell
+    // from `voff`; physical cells (k slowest) or the padded block
+    auto gather = [&](const double *pool, int w, int stride, int voff, bool ghosts) {
       std::vector<double> h(nc);
       for (int v = 0; v < w; ++v) {
         Check(cudaMemcpy(h.data(), pool + v * n + o, nc * 8, cudaMemcpyDeviceToHost),
               "download");
         if (ghosts) {
-          for (int64_t x = 0; x < nc; ++x) out_h[x * w + v] = h[x];
+          for (int64_t x = 0; x < nc; ++x) out_h[x * stride + voff + v] = h[x];
         } else {
           size_t q = 0;
           for (int k = 0; k < b.nk; ++k)
             for (int j = 0; j < b.nj; ++j)
-              for (int i = 0; i < b.ni; ++i) out_h[(q++) * w + v] = h[b.Cell(i, j, k)];
+              for (int i = 0; i < b.ni; ++i)
+                out_h[(q++) * stride + voff + v] = h[b.Cell(i, j, k)];
         }
       }
     };
+    const bool turb = nv > 5;
     switch (field) {
-      case ATH_FIELD_STATE: gather(batch->W, 5, false); break;
-      case ATH_FIELD_STATE_GHOSTS: gather(batch->W, 5, true); break;
-      case ATH_FIELD_RESID: gather(batch->R, 5, false); break;
-      case ATH_FIELD_DT: gather(batch->dt, 1, false); break;
+      case ATH_FIELD_STATE:
+      case ATH_FIELD_STATE_GHOSTS: {
+        const bool gh = field == ATH_FIELD_STATE_GHOSTS;
+        gather(batch->W, 5, nv, 0, gh);
+        if (turb) gather(batch->Wt, 2, nv, 5, gh);
+        break;
+      }
+      case ATH_FIELD_RESID:
+        gather(batch->R, 5, nv, 0, false);
+        if (turb) gather(batch->Rt, 2, nv, 5, false);
+        break;
+      case ATH_FIELD_DT: gather(batch->dt, 1, 1, 0, false); break;
       case ATH_FIELD_SPECRAD: {
+        // spectral radius (flow, turbulence; 0 without turbulence equations)
         const size_t m = (size_t)b.ni * b.nj * b.nk;
-        std::vector<double> lam(m);
-        // spectral radius (flow, turb); no turbulence equations here
-        std::vector<double> h(nc);
-        Check(cudaMemcpy(h.data(), batch->lam + o, nc * 8, cudaMemcpyDeviceToHost), "download");
-        size_t q = 0;
-        for (int k = 0; k < b.nk; ++k)
-          for (int j = 0; j < b.nj; ++j)
-            for (int i = 0; i < b.ni; ++i) {
-              out_h[2 * q] = h[b.Cell(i, j, k)];
-              out_h[2 * q + 1] = 0.0;
-              ++q;
-            }
+        std::fill(out_h, out_h + 2 * m, 0.0);
+        gather(batch->lam, 1, 2, 0, false);
+        if (turb) gather(batch->lamt, 1, 2, 1, false);
         break;
       }
       case ATH_FIELD_DU: batch->run->GetDU(block, out_h); break;
@@ -1456,16 +1565,16 @@ int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h) {
     Check(cudaStreamSynchronize(c.stream), "sync");
     const ath::Block &b = c.setup->blocks[block];
     const int64_t nc = b.NCell(), o = c.cell0[block], n = c.ncell;
+    const int nv = b.nv;
     std::vector<double> h(nc);
-    for (int v = 0; v < 5; ++v) {
-      Check(cudaMemcpy(h.data(), batch->W + v * n + o, nc * 8, cudaMemcpyDeviceToHost),
-            "download");
+    for (int v = 0; v < nv; ++v) {
+      double *pool = v < 5 ? batch->W + v * n + o : batch->Wt + (v - 5) * n + o;
+      Check(cudaMemcpy(h.data(), pool, nc * 8, cudaMemcpyDeviceToHost), "download");
       size_t q = 0;
       for (int k = 0; k < b.nk; ++k)
         for (int j = 0; j < b.nj; ++j)
-          for (int i = 0; i < b.ni; ++i) h[b.Cell(i, j, k)] = prim_h[(q++) * 5 + v];
-      Check(cudaMemcpy(batch->W + v * n + o, h.data(), nc * 8, cudaMemcpyHostToDevice),
-            "upload");
+          for (int i = 0; i < b.ni; ++i) h[b.Cell(i, j, k)] = prim_h[(q++) * nv + v];
+      Check(cudaMemcpy(pool, h.data(), nc * 8, cudaMemcpyHostToDevice), "upload");
     }
   });
 }
@@ -1476,16 +1585,29 @@ int ath_batch_pool_cells(ath_batch *batch, int64_t *ncell) {
   return ATH_OK;
 }
 
+int ath_batch_pool_vars(ath_batch *batch, int *nv) {
+  if (!batch || !nv) return ATH_ERR_ARG;
+  *nv = batch->core.any_rans ? 7 : 5;
+  return ATH_OK;
+}
+
 int ath_batch_copy_state(ath_batch *batch, double *host, int to_device) {
   return Guard([&] {
     if (!batch || !host) throw ath::Error(ATH_ERR_ARG, "null argument");
     auto &c = batch->core;
     Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
     const size_t bytes = 5 * (size_t)c.ncell * sizeof(double);
-    if (to_device)
+    const size_t tbytes = c.any_rans ? 2 * (size_t)c.ncell * sizeof(double) : 0;
+    double *ht = host + 5 * (size_t)c.ncell;
+    if (to_device) {
       Check(cudaMemcpyAsync(batch->W, host, bytes, cudaMemcpyHostToDevice, c.stream), "H2D");
-    else
+      if (tbytes)
+        Check(cudaMemcpyAsync(batch->Wt, ht, tbytes, cudaMemcpyHostToDevice, c.stream), "H2D");
+    } else {
       Check(cudaMemcpyAsync(host, batch->W, bytes, cudaMemcpyDeviceToHost, c.stream), "D2H");
+      if (tbytes)
+        Check(cudaMemcpyAsync(ht, batch->Wt, tbytes, cudaMemcpyDeviceToHost, c.stream), "D2H");
+    }
     Check(cudaStreamSynchronize(c.stream), "sync");
   });
 }
@@ -1540,6 +1662,12 @@ size_t EstimateBatchBytes(const Setup &st, int precision) {
     if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);
     double qc = ts * (5 + 5 + 5 + 24 + 6 + 2 + 1) + 4.0 * 8;
     if (blk) qc += ts * (48 + (visc ? 9 : 0));
+    if (ph.eqn == ATH_EQN_RANS) {
+      // k, omega, their residual, radius, wall distance, inviscid fluxes
+      // (FP64); viscous fluxes and per-face SST data; sweep arrays
+      pc += 8.0 * (2 + 2 + 1 + 1 + 6) + ts * (6 + 54);
+      qc += ts * (2 + 2 + (blk ? 8 : 2) + 2);
+    }
     bytes += n * pc + nq * qc;
   }
   return (size_t)(bytes * 1.25);
@@ -1598,7 +1726,7 @@ void Finish(ath_server *S, ath_server::Req *r) {
   r->result.resize(c.nblocks);
   for (int b = 0; b < c.nblocks; ++b) {
     const Block &bk = c.setup->blocks[b];
-    r->result[b].resize((size_t)bk.ni * bk.nj * bk.nk * 5);
+    r->result[b].resize((size_t)bk.ni * bk.nj * bk.nk * bk.nv);
     const int rc = ath_batch_get_field(r->batch, b, ATH_FIELD_STATE, r->result[b].data());
     if (rc != ATH_OK) throw Error(rc, "result download");
   }

@@ -102,13 +102,13 @@ struct TslCoeffs {
 // MatrixMultiply (src/matrix.cpp:197); laminar, one species, no diffusion
 // model.  `left` is the reference's flag (sign of the tau term).
 template <typename T>
-__device__ __forceinline__ void TslJacAccum(const Prim<T> &s, T mu_lam, const Gas<T> &g,
-                                            const TslCoeffs<T> &k_, T nx, T ny, T nz, T mag,
-                                            T dist, bool left, const T vg[9], bool subtract,
-                                            T J[kJac]) {
+__device__ __forceinline__ void TslJacAccum(const Prim<T> &s, T mu_lam, T mut_lam,
+                                            const Gas<T> &g, const TslCoeffs<T> &k_, T nx,
+                                            T ny, T nz, T mag, T dist, bool left,
+                                            const T vg[9], bool subtract, T J[kJac]) {
   const T t = Temperature(s, g);
   const T mu = k_.scale * mu_lam;
-  const T mut = k_.scale * T(0);
+  const T mut = k_.scale * mut_lam;
   const T velNorm = Dot(s.u, s.v, s.w, nx, ny, nz);
   const T rho = s.rho;
   const T k = SutherlandRatio(t, k_.t_ref, k_.k_c1, k_.k_s, k_.k_ref) * k_.scale;
@@ -176,6 +176,80 @@ __device__ __forceinline__ void MatVec5(const T M[kJac], const T x[5], T out[5])
     for (int c = 0; c < 5; ++c) s = s + M[r * 5 + c] * x[c];
     out[r] = s;
   }
+}
+
+// 2x2 turbulence parts of the block operator: Rusanov Jacobian 0.5 conv
+// +/- 0.5 diss (turbModel::InviscidConvectiveJacobian /
+// InviscidDissipationJacobian, src/turbulence.cpp:73-92) and the SST
+// viscous Jacobian times fac (turbKWSst::ViscJac, :764).
+template <typename T>
+__device__ __forceinline__ void TurbRusanovJac(const Prim<T> &s, T nx, T ny, T nz, T mag,
+                                               bool positive, T J[4]) {
+  const T vn = Dot(s.u, s.v, s.w, nx, ny, nz);
+  const T conv = vn * mag, diss = fabs(vn) * mag;
+  const T cj[4] = {T(0.5) * conv, T(0.5) * T(0), T(0.5) * T(0), T(0.5) * conv};
+  const T dj[4] = {T(0.5) * diss, T(0.5) * T(0), T(0.5) * T(0), T(0.5) * diss};
+#pragma unroll
+  for (int e = 0; e < 4; ++e) J[e] = positive ? cj[e] + dj[e] : cj[e] - dj[e];
+}
+template <typename T>
+__device__ __forceinline__ void TurbViscJac(T rho, T mag, T mu, T mut, T f1, T dist, T scale,
+                                            T fac, T J[4]) {
+  const T length = mag / dist;
+  const T sk = f1 * T(0.85) + (T(1) - f1) * T(1.0);
+  const T sw = f1 * T(0.5) + (T(1) - f1) * T(0.856);
+  const T j00 = scale * length / rho * (mu + sk * mut);
+  const T j11 = scale * length / rho * (mu + sw * mut);
+  J[0] = fac * j00;
+  J[1] = fac * T(0);
+  J[2] = fac * T(0);
+  J[3] = fac * j11;
+}
+// MatrixInverse of the 2x2 turbulence block (src/matrix.cpp:57)
+template <typename T>
+__device__ __forceinline__ void Inverse2(T a[4]) {
+  T I[4] = {T(1), T(0), T(0), T(1)};
+  // column 0: pivot among rows 0, 1 (row 0 when both are zero)
+  const int rp = (fabs(a[2]) > fabs(a[0])) ? 1 : 0;
+  if (rp == 1) {
+    T t = a[0]; a[0] = a[2]; a[2] = t;
+    t = a[1]; a[1] = a[3]; a[3] = t;
+    t = I[0]; I[0] = I[2]; I[2] = t;
+    t = I[1]; I[1] = I[3]; I[3] = t;
+  }
+  T nf = T(1) / a[0];
+  a[0] *= nf;
+  a[1] *= nf;
+  I[0] *= nf;
+  I[1] *= nf;
+  // column 1: only row 1 remains
+  const T factor = a[2] / a[0];
+  a[2] = a[2] - factor * a[0];
+  a[3] = a[3] - factor * a[1];
+  I[2] = I[2] - factor * I[0];
+  I[3] = I[3] - factor * I[1];
+  nf = T(1) / a[3];
+  a[3] *= nf;
+  I[2] *= nf;
+  I[3] *= nf;
+  // back substitution
+  const T f2 = a[1];
+  a[0] = a[0] - f2 * a[2];
+  a[1] = a[1] - f2 * a[3];
+  I[0] = I[0] - f2 * I[2];
+  I[1] = I[1] - f2 * I[3];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) a[e] = I[e];
+}
+template <typename T>
+__device__ __forceinline__ void MatVec2(const T M[4], const T x[2], T out[2]) {
+  T s0 = T(0), s1 = T(0);
+  s0 = s0 + M[0] * x[0];
+  s0 = s0 + M[1] * x[1];
+  s1 = s1 + M[2] * x[0];
+  s1 = s1 + M[3] * x[1];
+  out[0] = s0;
+  out[1] = s1;
 }
 
 // MatrixInverse (src/matrix.cpp:57): Gauss-Jordan with the reference's pivot

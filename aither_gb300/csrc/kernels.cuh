@@ -20,7 +20,8 @@
 namespace ath {
 
 constexpr int kCta = 256;   // threads per CTA of the cell/face kernels
-constexpr int kNv = 5;      // equations of the inviscid/laminar path
+constexpr int kNv = 5;      // flow equations
+constexpr int kNvMax = 7;   // with the k and omega equations of RANS solves
 
 struct BlockDev {
   int32_t ni, nj, nk, ng, NI, NJ, NK, solve;
@@ -38,6 +39,8 @@ struct SolveDev {
   int32_t limiter, nstates, state0, recon;
   int32_t flux;
   int32_t block;   // blusgs: 5x5 Jacobian diagonal and off-diagonals
+  int32_t rans;    // SST-2003: k and omega beside the flow equations
+  int32_t pad4;
   int32_t sweeps;  // matrixSweeps
   int32_t active;  // 0 once the solve is retired: its kernels skip their work
 };
@@ -57,7 +60,7 @@ struct WallFaceDev {
 
 // Partial norms of one CTA of the update kernel.
 struct NormPartial {
-  double l2[kNv];
+  double l2[7];     // per equation (the k and omega equations of RANS solves last)
   double linf;
   int64_t linf_pos;  // position in the solve's loop order, for ties
   int32_t linf_cell, linf_eqn;
@@ -109,6 +112,19 @@ struct Pools {
   T *vst[3];        // [15][ncell] viscous face state, face viscosity, face
                     // velocity gradient (row = derivative axis)
   T *vgq;           // [9][nq] cell-averaged velocity gradient, q order
+  // RANS (SST-2003) solves only
+  double *Wt;       // [2][ncell] k, omega
+  double *Rt;       // [2][ncell] turbulence residual
+  double *fluxt[3]; // [2][ncell] turbulence inviscid flux F.|A|
+  T *vfluxt[3];     // [2][ncell] turbulence viscous flux F.|A|
+  T *rst[3];        // [18][ncell] face: velocity gradient (9), k gradient (3),
+                    // omega gradient (3), eddy viscosity, F1, F2
+  double *lamt;     // [ncell] turbulence spectral radius
+  const double *wd; // [ncell] wall distance
+  T *Rtq, *dUtq;    // [2][nq]
+  T *dUtg;          // [2][nghost]
+  T *Ainvtq, *Atq;  // [nq] scalar or [4][nq] 2x2 turbulence diagonal (inverse)
+  T *mutq, *f1q;    // [nq] cell eddy viscosity and F1
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -238,10 +254,13 @@ struct Launch {
   // laminar viscosity of the listed cells (UpdateAuxillaryVariables)
   static void Aux(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block,
                   int n, cudaStream_t s);
+  // rkinds: bit 0 = the batch has solves without turbulence equations
+  // (for ViscFace: laminar viscous solves), bit 1 = SST solves; each kind
+  // has its own kernel so the laminar one keeps its register budget
   static void ViscFace(int d, const Pools<T> &P, const int32_t *list,
-                       const int32_t *cta_block, int ncta, cudaStream_t s);
+                       const int32_t *cta_block, int ncta, int rkinds, cudaStream_t s);
   static void Face(int d, const Pools<T> &P, const int32_t *list,
-                   const int32_t *cta_block, int ncta, cudaStream_t s);
+                   const int32_t *cta_block, int ncta, int rkinds, cudaStream_t s);
   // kinds: bit 0 = the batch has scalar solves, bit 1 = block solves
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                    int ncta, int kinds, cudaStream_t s);

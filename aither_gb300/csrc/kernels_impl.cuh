@@ -27,6 +27,106 @@ __device__ __forceinline__ Prim<double> ExtrapHold(const Prim<double> &bnd,
   return g;
 }
 
+// SST-2003 constants (turbKWSst, include/turbulence.hpp:489-501) and the
+// turbulence floors (turbModel::TkeMin / OmegaMin, :63-64)
+constexpr double kSstBetaStar = 0.09, kSstSigmaK1 = 0.85, kSstSigmaK2 = 1.0;
+constexpr double kSstSigmaW1 = 0.5, kSstSigmaW2 = 0.856, kSstBeta1 = 0.075;
+constexpr double kSstBeta2 = 0.0828, kSstGamma2 = 0.44, kSstA1 = 0.31;
+constexpr double kSstProd2Dest = 10.0, kTurbMin = 1.0e-20;
+__device__ __forceinline__ double SstGamma1() { return 5.0 / 9.0; }
+// std::max / std::min
+template <typename T>
+__device__ __forceinline__ T CMax(T a, T b) { return (a < b) ? b : a; }
+template <typename T>
+__device__ __forceinline__ T CMin(T a, T b) { return (b < a) ? b : a; }
+// turbKWSst::BlendedCoeff (src/turbulence.cpp:598)
+template <typename T>
+__device__ __forceinline__ T Blended(T c1, T c2, T f1) { return f1 * c1 + (T(1) - f1) * c2; }
+
+// tensor DoubleDotTrans (include/tensor.hpp:353)
+__device__ __forceinline__ double DDot(const double *a, const double *b) {
+  double s = 0.0;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) s += a[e] * b[e];
+  return s;
+}
+
+// turbKWSst::EddyViscAndBlending (src/turbulence.cpp:668) with Alpha1-3,
+// CDkw, F1, F2 and EddyVisc (:573-634, include/turbulence.hpp:529)
+__device__ __forceinline__ void SstEddyVisc(const Prim<double> &w, const double kw[2],
+                                            const double vg[9], const double kg[3],
+                                            const double wg[3], double mu, double wd,
+                                            double scale, double &mut, double &f1,
+                                            double &f2) {
+  const double k = kw[0], om = kw[1], rho = w.rho;
+  const double a1 = scale * sqrt(k) / (kSstBetaStar * om * (wd + 1.0e-30));
+  const double a2 = scale * scale * 500.0 * mu / ((wd + 1.0e-30) * (wd + 1.0e-30) * rho * om);
+  const double cd = CMax(2.0 * rho * kSstSigmaW2 / om * Dot(kg[0], kg[1], kg[2], wg[0], wg[1],
+                                                            wg[2]),
+                         1.0e-10);
+  const double a3 = 4.0 * rho * kSstSigmaW2 * k / (cd * (wd + 1.0e-30) * (wd + 1.0e-30));
+  f1 = tanh(pow(CMin(CMax(a1, a2), a3), 4.0));
+  const double arg2 = CMax(2.0 * a1, a2);
+  f2 = tanh(arg2 * arg2);
+  double S[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) S[r * 3 + q] = 0.5 * (vg[r * 3 + q] + vg[q * 3 + r]);
+  const double msr = sqrt(2.0 * DDot(S, S));
+  mut = rho * kSstA1 * k / CMax(kSstA1 * om, scale * msr * f2);
+}
+
+// turbKWSst::CalcTurbSrc (src/turbulence.cpp:637) with the Boussinesq
+// Reynolds stress (turbModel::ReynoldsStressDDotVelGrad, :53); returns the
+// blended beta of the source Jacobian
+__device__ __forceinline__ double SstSource(const Prim<double> &w, const double kw[2],
+                                            const double vg[9], const double kg[3],
+                                            const double wg[3], double mut, double f1,
+                                            double scale, double src[2]) {
+  const double k = kw[0], om = kw[1], rho = w.rho;
+  const double inv = 1.0 / scale;
+  const double cd = CMax(2.0 * rho * kSstSigmaW2 / om * Dot(kg[0], kg[1], kg[2], wg[0], wg[1],
+                                                            wg[2]),
+                         1.0e-10);
+  const double gamma = Blended(SstGamma1(), kSstGamma2, f1);
+  const double beta = Blended(kSstBeta1, kSstBeta2, f1);
+  const double tkeDest = inv * kSstBetaStar * (rho * k * om * 1.0);
+  const double omgDest = inv * beta * (rho * om * om);
+  const double lambda = 0.0 - (2.0 / 3.0) * mut;
+  const double tr = vg[0] + vg[4] + vg[8];
+  const double c23 = 2.0 / 3.0 * rho * k;
+  double tau[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double I = (r == q) ? 1.0 : 0.0;
+      tau[r * 3 + q] = (I * (lambda * tr) + (vg[r * 3 + q] + vg[q * 3 + r]) * mut) - I * c23;
+    }
+  double tkeProd = CMin(scale * DDot(tau, vg), kSstProd2Dest * tkeDest);
+  tkeProd = CMax(tkeProd, 0.0);
+  double omgProd = gamma * rho / mut * tkeProd;
+  omgProd = CMax(omgProd, 0.0);
+  const double omgCd = scale * (1.0 - f1) * cd;
+  src[0] = tkeProd - tkeDest;
+  src[1] = omgProd - omgDest + omgCd;
+  return beta;
+}
+
+// primitive::ApplyFarfieldTurbBC (src/primitive.cpp:83) + LimitTurb
+__device__ __forceinline__ void FarfieldTurb(const Prim<double> &g, double vx, double vy,
+                                             double vz, double tint, double ratio,
+                                             const SolveDev &sv, const Gas<double> &gas,
+                                             double kw[2]) {
+  const double vmag = sqrt(vx * vx + vy * vy + vz * vz);
+  kw[0] = 1.5 * pow(tint * vmag, 2.0);
+  const double mu = SutherlandRatio(Temperature(g, gas), sv.t_ref, sv.mu_c1, sv.mu_s, sv.mu_ref);
+  kw[1] = g.rho * kw[0] / (ratio * mu);
+  kw[0] = CMax(kw[0], kTurbMin);
+  kw[1] = CMax(kw[1], kTurbMin);
+}
+
 template <typename T>
 __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
                         const int32_t *op_solve) {
@@ -36,6 +136,15 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
   const int64_t n = P.ncell;
   Prim<double> in = LoadW<double>(P.W, n, op.src);
   Prim<double> g = in;
+  // turbulence (RANS solves): copied unless the boundary sets it
+  const bool rans = P.Wt != nullptr && P.solves[op_solve[t]].rans;
+  double tin[2] = {0.0, 0.0}, gt[2] = {0.0, 0.0};
+  if (rans) {
+    tin[0] = P.Wt[op.src];
+    tin[1] = P.Wt[n + op.src];
+    gt[0] = tin[0];
+    gt[1] = tin[1];
+  }
   if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK || op.type == ATH_EDGE_COPY) {
     // plain copy of the partner's interior cell / of the adjacent ghost
   } else if (op.type == ATH_EDGE_AVG) {
@@ -45,6 +154,10 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
     g.v = 0.5 * (in.v + o.v);
     g.w = 0.5 * (in.w + o.w);
     g.p = 0.5 * (in.p + o.p);
+    if (rans) {
+      gt[0] = 0.5 * (tin[0] + P.Wt[op.src2]);
+      gt[1] = 0.5 * (tin[1] + P.Wt[n + op.src2]);
+    }
   } else if (op.type == ATH_EDGE_SLIP) {
     // slip-wall reflection of the adjacent ghost across a ghost-layer face
     const double *fa = P.fa[op.dir];
@@ -68,6 +181,18 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       const double tGhost = 2.0 * bs.wall_t - Temperature(in, gas);
       const double rho = g.p / ((0.0 + 1.0 * gas.r) * tGhost);
       g.rho = rho * (in.rho / in.rho);
+    }
+    if (rans) {
+      // low-Re wall (src/ghostStates.cpp:262-275): k = 0 and omega =
+      // 60 nu / (beta1 d^2) at the face; nu and d of the wall-adjacent cell,
+      // nu from the previous auxiliary update
+      const int64_t a = op.src2;
+      const double nuW = P.mu[a] / P.W[a];
+      const double s = sv.visc_scale;
+      const double wWall = s * s * 60.0 * nuW / (P.wd[a] * P.wd[a] * kSstBeta1);
+      gt[0] = -1.0 * tin[0];
+      gt[1] = 2.0 * wWall - tin[1];
+      if (op.layer > 1) gt[1] = (double)op.layer * gt[1] - wWall;
     }
   } else {
     const SolveDev sv = P.solves[op_solve[t]];
@@ -97,6 +222,8 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       const double machInt = fabs(velIntNorm) / sosInt;
       if (machInt >= 1.0 && velIntNorm < 0.0) {
         g = fr;
+        if (rans)
+          FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
       } else if (machInt >= 1.0 && velIntNorm >= 0.0) {
         // all characteristics leave: interior values
       } else if (machInt < 1.0 && velIntNorm < 0.0) {
@@ -109,6 +236,8 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
         g.u = fr.u - nx * deltaPressure / rhoSoSInt;
         g.v = fr.v - ny * deltaPressure / rhoSoSInt;
         g.w = fr.w - nz * deltaPressure / rhoSoSInt;
+        if (rans)
+          FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
       } else {
         const double rhoSoSInt = in.rho * sosInt;
         const double deltaPressure = in.p - fr.p;
@@ -119,8 +248,22 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
         g.w = in.w + nz * deltaPressure / rhoSoSInt;
         g.p = fr.p;
       }
-      g = ExtrapHold(g, 2.0, in);
-      if (op.layer > 1) g = ExtrapHold(g, (double)op.layer, in);
+      // ExtrapolateHoldMixture over every variable: the turbulence follows
+      // the flow's density test
+      auto hold = [&](double f) {
+        const bool applies = f * g.rho - in.rho > 0.0;
+        g = ExtrapHold(g, f, in);
+        if (rans && applies) {
+          gt[0] = f * gt[0] - tin[0];
+          gt[1] = f * gt[1] - tin[1];
+        }
+      };
+      hold(2.0);
+      if (op.layer > 1) {
+        hold((double)op.layer);
+        if (rans)
+          FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+      }
     } else if (op.type == ATH_BC_SUPERSONIC_INFLOW) {
       const ath_bc_state bs = P.states[sv.state0 + op.state];
       g.rho = bs.rho;
@@ -128,6 +271,8 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       g.v = bs.v;
       g.w = bs.w;
       g.p = bs.p;
+      if (rans)
+        FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
     } else if (op.type == ATH_BC_SUPERSONIC_OUTFLOW) {
       if (op.layer > 1) {
         const double f = (double)op.layer;
@@ -136,8 +281,16 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
         g.v = f * in.v - in.v;
         g.w = f * in.w - in.w;
         g.p = f * in.p - in.p;
+        if (rans) {
+          gt[0] = f * tin[0] - tin[0];
+          gt[1] = f * tin[1] - tin[1];
+        }
       }
     }
+  }
+  if (rans) {
+    P.Wt[op.dst] = gt[0];
+    P.Wt[n + op.dst] = gt[1];
   }
   P.W[op.dst] = g.rho;
   P.W[n + op.dst] = g.u;
@@ -153,7 +306,8 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 // f is the flux per unit area, L and R the reconstructed face states.
 template <typename U, int D, typename PT>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
-                                         int64_t s, U f[5], Prim<U> &L, Prim<U> &R) {
+                                         int64_t s, U f[5], Prim<U> &L, Prim<U> &R,
+                                         U ft[2] = nullptr) {
   const Gas<U> g = GasOf<U>(sv);
   const int64_t n = P.ncell;
   const double *wd = P.width[D];
@@ -186,10 +340,51 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
   }
   const double *fa = P.fa[D];
   const U nx = (U)fa[c], ny = (U)fa[n + c], nz = (U)fa[2 * n + c];
+  U vlr[2];
   if (sv.flux == ATH_FLUX_AUSM)
-    AusmFlux(L, R, g, nx, ny, nz, f);
+    AusmFlux(L, R, g, nx, ny, nz, f, vlr);
   else
     RoeFlux(L, R, g, nx, ny, nz, f);
+  if (ft) {
+    // k and omega reconstructed like the flow variables, then their fluxes
+    const double *Wt = P.Wt;
+    auto kt = [&](int64_t x, int q) { return (U)Wt[q * n + x]; };
+    U Lt[2], Rt[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (sv.recon == ATH_RECON_CONSTANT) {
+        Lt[q] = kt(c - s, q);
+        Rt[q] = kt(c, q);
+      } else if (sv.recon == ATH_RECON_MUSCL) {
+        const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
+        const U kappa = (U)sv.kappa;
+        const U dpL = (xm1 + xm1) / (xm1 + x0), dmL = (xm1 + xm1) / (xm1 + xm2);
+        const U dpR = (x0 + x0) / (x0 + xm1), dmR = (x0 + x0) / (x0 + xp1);
+        Lt[q] = Muscl1(kt(c - 2 * s, q), kt(c - s, q), kt(c, q), dpL, dmL, kappa, sv.limiter);
+        Rt[q] = Muscl1(kt(c + s, q), kt(c, q), kt(c - s, q), dpR, dmR, kappa, sv.limiter);
+      } else {
+        const bool z = sv.recon == ATH_RECON_WENOZ;
+        const U wl[5] = {(U)wd[c - 3 * s], (U)wd[c - 2 * s], (U)wd[c - s], (U)wd[c],
+                         (U)wd[c + s]};
+        const U wu[5] = {(U)wd[c + 2 * s], (U)wd[c + s], (U)wd[c], (U)wd[c - s],
+                         (U)wd[c - 2 * s]};
+        const WenoCoeffs<U> kl = MakeWeno(wl), ku = MakeWeno(wu);
+        Lt[q] = Weno1(kl, wl, kt(c - 3 * s, q), kt(c - 2 * s, q), kt(c - s, q), kt(c, q),
+                      kt(c + s, q), z);
+        Rt[q] = Weno1(ku, wu, kt(c + 2 * s, q), kt(c + s, q), kt(c, q), kt(c - s, q),
+                      kt(c - 2 * s, q), z);
+      }
+    }
+    if (sv.flux == ATH_FLUX_AUSM) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        ft[q] = L.rho * vlr[0] * Lt[q];
+        ft[q] += R.rho * vlr[1] * Rt[q];
+      }
+    } else {
+      RoeTurbFlux(L, R, Lt, Rt, g, nx, ny, nz, ft);
+    }
+  }
 }
 
 // Mixed-precision Roe/MUSCL face: the face states are the FP64 upwind cell
@@ -250,14 +445,14 @@ __device__ __forceinline__ void FaceFluxMixedRoe(const Pools<PT> &P, const Solve
   for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - (double)d[v])) * 0.5;
 }
 
-template <typename T, int D>
+template <typename T, int D, bool RANS>
 __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
-  if (!sv.active) return;
+  if (!sv.active || (sv.rans != 0) != RANS) return;
   const int64_t n = P.ncell;
   const int64_t s = StrideOf(b, D);
   double *out = P.flux[D];
@@ -266,23 +461,30 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
   if constexpr (std::is_same<T, float>::value) {
     double f[5];
     Prim<double> L, R;
-    if (sv.flux == ATH_FLUX_ROE &&
+    double ft[2];
+    if (!RANS && sv.flux == ATH_FLUX_ROE &&
         (sv.recon == ATH_RECON_MUSCL || sv.recon == ATH_RECON_CONSTANT))
       FaceFluxMixedRoe<D>(P, sv, c, s, f, L, R);
     else
-      FaceFlux<double, D>(P, sv, c, s, f, L, R);  // AUSM, WENO: FP64 faces
+      FaceFlux<double, D>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);  // AUSM, WENO, RANS
+    if (RANS)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) P.fluxt[D][q * n + c] = ft[q] * mag;
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * mag;
     const double q[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
 #pragma unroll
     for (int v = 0; v < 10; ++v) lr[v] = (T)q[v];
   } else {
-    T f[5];
+    T f[5], ft[2];
     Prim<T> L, R;
-    FaceFlux<T, D>(P, sv, c, s, f, L, R);
+    FaceFlux<T, D>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
     const T magT = (T)mag;
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * magT;
+    if (RANS)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) P.fluxt[D][q * n + c] = ft[q] * magT;
     const T q[10] = {L.rho, L.u, L.v, L.w, L.p, R.rho, R.u, R.v, R.w, R.p};
 #pragma unroll
     for (int v = 0; v < 10; ++v) lr[v] = q[v];
@@ -298,7 +500,10 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
 // ---------------------------------------------------------------------------
 // residual assembly + spectral radius + dt + diagonal.  BLOCK: the 5x5
 // diagonal of block solves (scalar solves are served by the other
-// instantiation; a CTA never mixes the two).
+// instantiation; a CTA never mixes the two).  RANS solves add the k and
+// omega residuals, turbulence radii, SST sources (from cell averages of the
+// six faces' gradients, eddy viscosity and blending) and the turbulence
+// diagonal (scalar, or 2x2 for block solves).
 template <typename T, bool BLOCK>
 __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
@@ -309,6 +514,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   if (c < 0) return;
   const int64_t n = P.ncell;
   const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const bool rans = sv.rans != 0;
   // R = 0 - Fi(lo) + Fi(hi) - Fj(lo) + Fj(hi) - Fk(lo) + Fk(hi), each face
   // term rounded in this order (src/procBlock.cpp:447-463); viscous faces
   // follow with + Fv(lo) - Fv(hi) per direction (:1392-1429)
@@ -331,10 +537,28 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     }
     P.R[v * n + c] = r;
   }
+  double rt[2] = {0.0, 0.0};
+  if (rans) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const double *F = P.fluxt[d] + q * n;
+        rt[q] = rt[q] - F[c];
+        rt[q] = rt[q] + F[c + st[d]];
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const T *F = P.vfluxt[d] + q * n;
+        rt[q] = rt[q] + (double)F[c];
+        rt[q] = rt[q] - (double)F[c + st[d]];
+      }
+    }
+  }
   // inviscid cell spectral radius, summed i, j, k
   const Gas<T> g = GasOf<T>(sv);
   const Prim<T> w = LoadW<T>(P.W, n, c);
-  double lam = 0.0;
+  double lam = 0.0, lamt = 0.0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double *fa = P.fa[d];
@@ -342,29 +566,104 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     lam = lam + (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
                                        (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u],
                                        (T)fa[2 * n + u], (T)fa[3 * n + u]);
+    if (rans) {
+      // turbModel::InviscidCellSpectralRadius (src/turbulence.cpp:94): |v.n_avg| |A|
+      const Prim<double> wd = LoadW<double>(P.W, n, c);
+      double ax = 0.5 * (fa[c] + fa[u]), ay = 0.5 * (fa[n + c] + fa[n + u]),
+             az = 0.5 * (fa[2 * n + c] + fa[2 * n + u]);
+      const double am = sqrt(Dot(ax, ay, az, ax, ay, az));
+      ax = ax / am;
+      ay = ay / am;
+      az = az / am;
+      lamt = lamt + fabs(Dot(wd.u, wd.v, wd.w, ax, ay, az)) * (0.5 * (fa[3 * n + c] + fa[3 * n + u]));
+    }
   }
-  double adiag = lam;  // scalar main diagonal accumulates like the radius
+  double adiag = lam;    // scalar main diagonal accumulates like the radius
+  double adiagt = lamt;  // and its turbulence part
   const double vol = P.vol[c];
   const int64_t q = P.qpos[c];
   if (sv.viscous) {
     // viscous cell spectral radii (ViscCellSpectralRadius): the time-step
     // radius takes them times the viscous CFL coefficient, the diagonal
-    // twice (CalcViscFluxI/J/K)
+    // twice (CalcViscFluxI/J/K); with RANS the eddy viscosity and F1 of the
+    // cell's lower face enter them
     const T mu = (T)P.mu[c];
-    const T vt = ViscMaxTerm(w, g) * ViscTerm(mu, (T)sv.visc_scale, g);
+    const T vmax = ViscMaxTerm(w, g);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+      const T mutf = rans ? P.rst[d][15 * n + c] : T(0);
+      const T vt = vmax * ViscTerm2(mu, mutf, (T)sv.visc_scale, g);
       const T fMag = T(0.5) * ((T)P.fa[d][3 * n + c] + (T)P.fa[d][3 * n + c + st[d]]);
       const T lv = vt * fMag * fMag / (T)vol;
       lam = lam + (double)(lv * (T)sv.visc_coeff);
       adiag = adiag + (double)(T(2) * lv);
+      if (rans) {
+        // turbKWSst::ViscousCellSpectralRadius (src/turbulence.cpp:785)
+        const double f1f = P.rst[d][16 * n + c];
+        const double fm = 0.5 * (P.fa[d][3 * n + c] + P.fa[d][3 * n + c + st[d]]);
+        const double length = fm * fm / vol;
+        const double lvt = sv.visc_scale * length / (double)P.W[c] *
+                           ((double)P.mu[c] + Blended(kSstSigmaK1, kSstSigmaK2, f1f) * (double)mutf);
+        lamt = lamt + lvt * sv.visc_coeff;
+        adiagt = adiagt + 2.0 * lvt;
+      }
     }
     P.muq[q] = mu;
   }
+  double srcJ[2] = {0.0, 0.0};
+  if (rans) {
+    // cell averages of the six faces (one sixth each, i lo, i hi, j lo, ...)
+    const double sixth = 1.0 / 6.0;
+    double vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, kg[3] = {0, 0, 0}, wg[3] = {0, 0, 0};
+    double mutc = 0.0, f1c = 0.0, f2c = 0.0;
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d)
+#pragma unroll 1
+      for (int side = 0; side < 2; ++side) {
+        const int64_t f = side ? c + st[d] : c;
+        const T *rs = P.rst[d];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) vg[e] += sixth * (double)rs[e * n + f];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          kg[e] += sixth * (double)rs[(9 + e) * n + f];
+          wg[e] += sixth * (double)rs[(12 + e) * n + f];
+        }
+        mutc += sixth * (double)rs[15 * n + f];
+        f1c += sixth * (double)rs[16 * n + f];
+        f2c += sixth * (double)rs[17 * n + f];
+      }
+    (void)f2c;
+    const Prim<double> wd = LoadW<double>(P.W, n, c);
+    const double kw[2] = {P.Wt[c], P.Wt[n + c]};
+    double src[2];
+    const double beta = SstSource(wd, kw, vg, kg, wg, mutc, f1c, sv.visc_scale, src);
+    const double inv = 1.0 / sv.visc_scale;
+    const double srcSR = -2.0 * kSstBetaStar * kw[1] * vol * inv;
+    lamt = lamt - srcSR;
+    adiagt = adiagt - srcSR;
+    srcJ[0] = -2.0 * kSstBetaStar * kw[1] * 1.0 * vol * inv;
+    srcJ[1] = -2.0 * beta * kw[1] * vol * inv;
+#pragma unroll
+    for (int qq = 0; qq < 2; ++qq) {
+      rt[qq] = rt[qq] - src[qq] * vol;
+      P.Rt[qq * n + c] = rt[qq];
+    }
+    const int64_t nq = P.nq;
+    P.mutq[q] = (T)mutc;
+    P.f1q[q] = (T)f1c;
+    P.Rtq[q] = (T)rt[0];
+    P.Rtq[nq + q] = (T)rt[1];
+    if (BLOCK)
+#pragma unroll
+      for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = (T)vg[e];
+  }
   P.lam[c] = lam;
+  if (rans) P.lamt[c] = lamt;
   // local time step and diagonal: A = A*relax + V(1+zeta)/(dt theta)
   const double cfl = P.cfl[b.solve];
-  const double dt = cfl * (vol / lam);
+  const double lmax = rans ? CMax(lam, lamt) : lam;
+  const double dt = cfl * (vol / lmax);
   P.dt[c] = dt;
   const int64_t nq = P.nq;
   if constexpr (BLOCK) {
@@ -373,25 +672,35 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     // Rusanov Jacobian of the upper-side state of the lower face, plus the
     // one of the lower-side state of the upper face; then per direction the
     // thin-shear-layer Jacobians, plus at the lower face, minus at the
-    // upper face
-    T A[kJac];
+    // upper face; the 2x2 turbulence block alongside
+    T A[kJac], At[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int e = 0; e < kJac; ++e) A[e] = T(0);
 #pragma unroll 1
     for (int d = 0; d < 3; ++d) {
       const double *fa = P.fa[d];
       const T *fs = P.fst[d];
-      T J[kJac];
+      T J[kJac], Jt[4];
       const int64_t u = c + st[d];
       const Prim<T> sR{fs[5 * n + c], fs[6 * n + c], fs[7 * n + c], fs[8 * n + c],
                        fs[9 * n + c]};
       RusanovJac(sR, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c], (T)fa[3 * n + c], false, J);
 #pragma unroll
       for (int e = 0; e < kJac; ++e) A[e] = A[e] - J[e];
+      if (rans) {
+        TurbRusanovJac(sR, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c], (T)fa[3 * n + c], false, Jt);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) At[e] = At[e] - Jt[e];
+      }
       const Prim<T> sL{fs[u], fs[n + u], fs[2 * n + u], fs[3 * n + u], fs[4 * n + u]};
       RusanovJac(sL, g, (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u], (T)fa[3 * n + u], true, J);
 #pragma unroll
       for (int e = 0; e < kJac; ++e) A[e] = A[e] + J[e];
+      if (rans) {
+        TurbRusanovJac(sL, (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u], (T)fa[3 * n + u], true, Jt);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) At[e] = At[e] + Jt[e];
+      }
     }
     if (sv.viscous) {
       const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s,
@@ -415,12 +724,27 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
             vg[e] = vg[e] + sixth * gr[e];
           }
           const T dist = side ? P.dist_hi[d * nq + q] : P.dist_lo[d * nq + q];
-          TslJacAccum(fsx, vs[5 * n + f], g, tk, (T)fa[f], (T)fa[n + f], (T)fa[2 * n + f],
+          const T mutf = rans ? P.rst[d][15 * n + f] : T(0);
+          TslJacAccum(fsx, vs[5 * n + f], mutf, g, tk, (T)fa[f], (T)fa[n + f], (T)fa[2 * n + f],
                       (T)fa[3 * n + f], dist, side != 0, gr, side != 0, A);
+          if (rans) {
+            T Jt[4];
+            TurbViscJac(fsx.rho, (T)fa[3 * n + f], vs[5 * n + f], mutf, P.rst[d][16 * n + f],
+                        dist, (T)sv.visc_scale, side ? T(-1) : T(1), Jt);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) At[e] = side ? At[e] - Jt[e] : At[e] + Jt[e];
+          }
         }
       }
+      if (!rans)
 #pragma unroll
-      for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = vg[e];
+        for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = vg[e];
+    }
+    if (rans) {
+      At[0] = At[0] - (T)srcJ[0];
+      At[1] = At[1] - T(0);
+      At[2] = At[2] - T(0);
+      At[3] = At[3] - (T)srcJ[1];
     }
     const T diagVolTime = (T)((vol * (1.0 + sv.zeta)) / (dt * sv.theta));
 #pragma unroll
@@ -432,10 +756,26 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     Inverse5(A);
 #pragma unroll
     for (int e = 0; e < kJac; ++e) P.Ainvq[e * nq + q] = A[e];
+    if (rans) {
+      At[0] *= (T)sv.relax;
+      At[3] *= (T)sv.relax;
+      At[0] += diagVolTime;
+      At[3] += diagVolTime;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) P.Atq[e * nq + q] = At[e];
+      Inverse2(At);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) P.Ainvtq[e * nq + q] = At[e];
+    }
   } else {
     const double a = adiag * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
     P.Ainvq[q] = (T)(1.0 / a);
     P.Aq[q] = (T)a;
+    if (rans) {
+      const double at = adiagt * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+      P.Ainvtq[q] = (T)(1.0 / at);
+      P.Atq[q] = (T)at;
+    }
   }
   // hyperplane-ordered copies for the sweeps
   P.Wq[q] = w.rho;
@@ -447,111 +787,158 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   for (int v = 0; v < 5; ++v) P.Rq[v * nq + q] = (T)P.R[v * n + c];
 }
 
-// ---------------------------------------------------------------------------
+// Neighbour data of an off-diagonal term: the state, laminar viscosity and
+// update of the neighbour across face d of q-ordered cell q, and, for RANS
+// solves, its eddy viscosity, F1 and turbulence update.  Connection ghosts
+// (nb <= -2) carry the partner cell's data (SwapImplicitUpdate,
+// SwapEddyViscAndGradients, SwapTurbVars; src/gridLevel.cpp:321,343).
+template <typename T>
+struct Nbr {
+  Prim<T> s;
+  T du[5], dut[2];
+  T mu, mut, f1;
+  int64_t vq;  // q index whose cell-averaged gradient the neighbour carries
+};
+template <typename T>
+__device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, int32_t nb,
+                                        Nbr<T> &o) {
+  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
+  o.mu = o.mut = o.f1 = T(0);
+  o.dut[0] = o.dut[1] = T(0);
+  int64_t cq;  // q index of the cell whose turbulence data applies
+  if (nb >= 0) {
+    o.s.rho = P.Wq[nb];
+    o.s.u = P.Wq[nq + nb];
+    o.s.v = P.Wq[2 * nq + nb];
+    o.s.w = P.Wq[3 * nq + nb];
+    o.s.p = P.Wq[4 * nq + nb];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) o.du[v] = P.dUq[v * nq + nb];
+    if (sv.viscous) o.mu = P.muq[nb];
+    if (sv.rans) {
+      o.dut[0] = P.dUtq[nb];
+      o.dut[1] = P.dUtq[nq + nb];
+    }
+    cq = nb;
+  } else {
+    const int64_t slot = -(int64_t)nb - 2;
+    o.s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) o.du[v] = P.dUg[v * ng + slot];
+    if (sv.viscous) o.mu = (T)P.mu[P.ghost_cell[slot]];
+    if (sv.rans) {
+      o.dut[0] = P.dUtg[slot];
+      o.dut[1] = P.dUtg[ng + slot];
+    }
+    cq = P.ghost_src[slot];
+  }
+  if (sv.rans) {
+    o.mut = P.mutq[cq];
+    o.f1 = P.f1q[cq];
+  }
+  o.vq = cq;
+}
+
 // Off-diagonal sum of one cell: lower neighbours with the "positive" sign
 // (procBlock::ImplicitLower) or upper neighbours with the negative sign
-// (ImplicitUpper), accumulated i, j, k from zero.
+// (ImplicitUpper), accumulated i, j, k from zero.  RANS solves add the
+// turbulence rows: the neighbour's turbulence face radius times its update
+// (turbModel::FaceSpectralRadius, include/spectralRadius.hpp).
 template <typename T>
 __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
                                            const SolveDev &sv, int64_t q, bool lower,
-                                           T acc[5]) {
-  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
+                                           T acc[5], T acct[2]) {
+  const int64_t nq = P.nq;
   const T *face = lower ? P.face_lo : P.face_hi;
   const T *dist = lower ? P.dist_lo : P.dist_hi;
   const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
+  acct[0] = acct[1] = T(0);
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     const int32_t nb = nbq[d * nq + q];
     if (nb == -1) continue;
-    Prim<T> s;
-    T du[5];
-    T mu = T(0);
-    if (nb >= 0) {
-      s.rho = P.Wq[nb];
-      s.u = P.Wq[nq + nb];
-      s.v = P.Wq[2 * nq + nb];
-      s.w = P.Wq[3 * nq + nb];
-      s.p = P.Wq[4 * nq + nb];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
-      if (sv.viscous) mu = P.muq[nb];
-    } else {
-      const int64_t slot = -(int64_t)nb - 2;
-      s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
-      if (sv.viscous) mu = (T)P.mu[P.ghost_cell[slot]];
-    }
+    Nbr<T> o;
+    LoadNbr(P, sv, nb, o);
     const T *f = face + (int64_t)d * 4 * nq;
     const T mag = f[3 * nq + q];
     // ViscFaceSpectralRadius (include/spectralRadius.hpp:126) across this
     // face, ProjC2CDist as the length
-    const T vsr = sv.viscous ? mag / dist[d * nq + q] * ViscMaxTerm(s, g) *
-                                   ViscTerm(mu, (T)sv.visc_scale, g)
+    const T vsr = sv.viscous ? mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
+                                   ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g)
                              : T(0);
-    T o[5];
-    ScalarOffDiag(s, du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, o);
+    T r[5];
+    ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
+    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + r[v];
+    if (sv.rans) {
+      const T vn = Dot(o.s.u, o.s.v, o.s.w, f[q], f[nq + q], f[2 * nq + q]);
+      T sr = lower ? T(0.5) * mag * fabs(vn + fabs(vn)) : T(0.5) * mag * fabs(vn - fabs(vn));
+      if (sv.viscous) {
+        const T length = mag / dist[d * nq + q];
+        const T sk = o.f1 * T(0.85) + (T(1) - o.f1) * T(1.0);
+        sr += (T)sv.visc_scale * length / o.s.rho * (o.mu + sk * o.mut);
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) acct[k] = acct[k] + (lower ? o.dut[k] * sr : -(o.dut[k] * sr));
+    }
   }
 }
 
 // Off-diagonal sum of one cell of a block solve (RusanovBlockOffDiagonal,
 // src/fluxJacobian.cpp:164): per neighbour the Rusanov Jacobian of its state
 // minus (lower) or plus (upper) its thin-shear-layer Jacobian with its
-// viscosity and cell-averaged gradient, times its update.
+// viscosity and cell-averaged gradient, times its update; the turbulence
+// rows likewise with the 2x2 Rusanov and viscous Jacobians (turbKWSst::ViscJac,
+// src/turbulence.cpp:764).
 template <typename T>
 __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const Gas<T> &g,
                                                 const SolveDev &sv, int64_t q, bool lower,
-                                                T acc[5]) {
-  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
+                                                T acc[5], T acct[2]) {
+  const int64_t nq = P.nq;
   const T *face = lower ? P.face_lo : P.face_hi;
   const T *dist = lower ? P.dist_lo : P.dist_hi;
   const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
   const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref};
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
+  acct[0] = acct[1] = T(0);
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     const int32_t nb = nbq[d * nq + q];
     if (nb == -1) continue;
-    Prim<T> s;
-    T du[5], vg[9];
-    T mu = T(0);
-    int64_t vq;  // q index whose cell gradient the neighbour carries
-    if (nb >= 0) {
-      s.rho = P.Wq[nb];
-      s.u = P.Wq[nq + nb];
-      s.v = P.Wq[2 * nq + nb];
-      s.w = P.Wq[3 * nq + nb];
-      s.p = P.Wq[4 * nq + nb];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
-      if (sv.viscous) mu = P.muq[nb];
-      vq = nb;
-    } else {
-      const int64_t slot = -(int64_t)nb - 2;
-      s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
-#pragma unroll
-      for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
-      if (sv.viscous) mu = (T)P.mu[P.ghost_cell[slot]];
-      vq = P.ghost_src[slot];  // the connection copies the partner's gradient
-    }
+    Nbr<T> o;
+    LoadNbr(P, sv, nb, o);
     const T *f = face + (int64_t)d * 4 * nq;
     const T fx = f[q], fy = f[nq + q], fz = f[2 * nq + q], mag = f[3 * nq + q];
     T J[kJac];
-    RusanovJac(s, g, fx, fy, fz, mag, lower, J);
+    RusanovJac(o.s, g, fx, fy, fz, mag, lower, J);
     if (sv.viscous) {
+      T vg[9];
 #pragma unroll
-      for (int e = 0; e < 9; ++e) vg[e] = P.vgq[e * nq + vq];
-      TslJacAccum(s, mu, g, tk, fx, fy, fz, mag, dist[d * nq + q], lower, vg, lower, J);
+      for (int e = 0; e < 9; ++e) vg[e] = P.vgq[e * nq + o.vq];
+      TslJacAccum(o.s, o.mu, o.mut, g, tk, fx, fy, fz, mag, dist[d * nq + q], lower, vg, lower,
+                  J);
     }
-    T o[5];
-    MatVec5(J, du, o);
+    T r[5];
+    MatVec5(J, o.du, r);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + o[v];
+    for (int v = 0; v < 5; ++v) acc[v] = acc[v] + r[v];
+    if (sv.rans) {
+      T Jt[4], rt[2];
+      TurbRusanovJac(o.s, fx, fy, fz, mag, lower, Jt);
+      if (sv.viscous) {
+        T Tv[4];
+        TurbViscJac(o.s.rho, mag, o.mu, o.mut, o.f1, dist[d * nq + q], (T)sv.visc_scale,
+                    lower ? T(-1) : T(1), Tv);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
+      }
+      MatVec2(Jt, o.dut, rt);
+      acct[0] = acct[0] + rt[0];
+      acct[1] = acct[1] + rt[1];
+    }
   }
 }
 
@@ -571,20 +958,29 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
   if (sv.block || !sv.active) return;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
-  T acc[5];
-  OffDiagSum(P, g, sv, q, forward != 0, acc);
+  T acc[5], acct[2];
+  OffDiagSum(P, g, sv, q, forward != 0, acc, acct);
   const T ainv = P.Ainvq[q];
   const T thetaInv = (T)(1.0 / sv.theta);
   if constexpr (FULL) {
     if (sweep >= sv.sweeps) return;
     if (sweep > 0 || sv.sweeps > 1) {
-      T other[5];
-      OffDiagSum(P, g, sv, q, forward == 0, other);
+      T other[5], othert[2];
+      OffDiagSum(P, g, sv, q, forward == 0, other, othert);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const T bv = -thetaInv * P.Rq[v * nq + q];
         const T in = forward ? bv + (acc[v] - other[v]) : (bv + other[v]) - acc[v];
         P.dUq[v * nq + q] = in * ainv;
+      }
+      if (sv.rans) {
+        const T ainvt = P.Ainvtq[q];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const T bv = -thetaInv * P.Rtq[v * nq + q];
+          const T in = forward ? bv + (acct[v] - othert[v]) : (bv + othert[v]) - acct[v];
+          P.dUtq[v * nq + q] = in * ainvt;
+        }
       }
       return;
     }
@@ -595,16 +991,33 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
       const T bv = -thetaInv * P.Rq[v * nq + q];
       P.dUq[v * nq + q] = (bv + acc[v]) * ainv;
     }
+    if (sv.rans) {
+      const T ainvt = P.Ainvtq[q];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const T bv = -thetaInv * P.Rtq[v * nq + q];
+        P.dUtq[v * nq + q] = (bv + acct[v]) * ainvt;
+      }
+    }
   } else {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T xold = P.dUq[v * nq + q];
       P.dUq[v * nq + q] = xold - acc[v] * ainv;
     }
+    if (sv.rans) {
+      const T ainvt = P.Ainvtq[q];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const T xold = P.dUtq[v * nq + q];
+        P.dUtq[v * nq + q] = xold - acct[v] * ainvt;
+      }
+    }
   }
 }
 
-// Block version: A^-1 is the 5x5 inverse, products by ArrayMultiplication.
+// Block version: A^-1 is the 5x5 inverse (2x2 for the turbulence rows),
+// products by ArrayMultiplication.
 template <typename T>
 __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
                                                 int forward, int sweep) {
@@ -619,14 +1032,17 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   const T thetaInv = (T)(1.0 / sv.theta);
-  T acc[5], in[5], x[5];
-  OffDiagSumBlock(P, g, sv, q, forward != 0, acc);
-  T Ai[kJac];
+  T acc[5], in[5], x[5], acct[2], int_[2], xt[2];
+  OffDiagSumBlock(P, g, sv, q, forward != 0, acc, acct);
+  T Ai[kJac], Ait[4];
 #pragma unroll
   for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
+  if (sv.rans)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) Ait[e] = P.Ainvtq[e * nq + q];
   if (full) {
-    T other[5];
-    OffDiagSumBlock(P, g, sv, q, forward == 0, other);
+    T other[5], othert[2];
+    OffDiagSumBlock(P, g, sv, q, forward == 0, other, othert);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T bv = -thetaInv * P.Rq[v * nq + q];
@@ -635,16 +1051,38 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
     MatVec5(Ai, in, x);
 #pragma unroll
     for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
+    if (sv.rans) {
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const T bv = -thetaInv * P.Rtq[v * nq + q];
+        int_[v] = forward ? bv + (acct[v] - othert[v]) : (bv + othert[v]) - acct[v];
+      }
+      MatVec2(Ait, int_, xt);
+      P.dUtq[q] = xt[0];
+      P.dUtq[nq + q] = xt[1];
+    }
   } else if (forward) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q] + acc[v];
     MatVec5(Ai, in, x);
 #pragma unroll
     for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
+    if (sv.rans) {
+#pragma unroll
+      for (int v = 0; v < 2; ++v) int_[v] = -thetaInv * P.Rtq[v * nq + q] + acct[v];
+      MatVec2(Ait, int_, xt);
+      P.dUtq[q] = xt[0];
+      P.dUtq[nq + q] = xt[1];
+    }
   } else {
     MatVec5(Ai, acc, x);
 #pragma unroll
     for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = P.dUq[v * nq + q] - x[v];
+    if (sv.rans) {
+      MatVec2(Ait, acct, xt);
+      P.dUtq[q] = P.dUtq[q] - xt[0];
+      P.dUtq[nq + q] = P.dUtq[nq + q] - xt[1];
+    }
   }
 }
 
@@ -657,28 +1095,46 @@ __global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int
   const int64_t q = it.x, nq = P.nq;
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
   if (!sv.active) return;
-  T x[5];
+  T x[5], xt[2] = {T(0), T(0)};
   if (sv.sweeps <= 1) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) x[v] = T(0);
   } else {
     const T thetaInv = (T)(1.0 / sv.theta);
-    T in[5];
+    T in[5], int_[2];
 #pragma unroll
     for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q];
+    if (sv.rans)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) int_[v] = -thetaInv * P.Rtq[v * nq + q];
     if (sv.block) {
       T Ai[kJac];
 #pragma unroll
       for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
       MatVec5(Ai, in, x);
+      if (sv.rans) {
+        T Ait[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) Ait[e] = P.Ainvtq[e * nq + q];
+        MatVec2(Ait, int_, xt);
+      }
     } else {
       const T ainv = P.Ainvq[q];
 #pragma unroll
       for (int v = 0; v < 5; ++v) x[v] = in[v] * ainv;
+      if (sv.rans) {
+        const T ainvt = P.Ainvtq[q];
+        xt[0] = int_[0] * ainvt;
+        xt[1] = int_[1] * ainvt;
+      }
     }
   }
 #pragma unroll
   for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
+  if (sv.rans) {
+    P.dUtq[q] = xt[0];
+    P.dUtq[nq + q] = xt[1];
+  }
 }
 
 template <typename T>
@@ -688,6 +1144,10 @@ __global__ void k_conn_du(Pools<T> P) {
   const int64_t src = P.ghost_src[t];
 #pragma unroll
   for (int v = 0; v < 5; ++v) P.dUg[v * P.nghost + t] = P.dUq[v * P.nq + src];
+  if (P.dUtg != nullptr) {
+    P.dUtg[t] = P.dUtq[src];
+    P.dUtg[P.nghost + t] = P.dUtq[P.nq + src];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -697,13 +1157,13 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
                                                  const int32_t *cta_block,
                                                  const int32_t *cta_pos0,
                                                  NormPartial *partials) {
-  __shared__ double s_l2[kCta / 32][kNv];
+  __shared__ double s_l2[kCta / 32][kNvMax];
   __shared__ double s_max[kCta / 32];
   __shared__ int64_t s_pos[kCta / 32];
   __shared__ int32_t s_bad[kCta / 32];
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   const int64_t n = P.ncell;
-  double l2[kNv] = {0, 0, 0, 0, 0};
+  double l2[kNvMax] = {0, 0, 0, 0, 0, 0, 0};
   double mx = 0.0;
   int64_t mpos = INT64_MAX;
   int bad = 0;
@@ -713,7 +1173,7 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     const Gas<double> g = GasOf<double>(sv);
     const Prim<double> w = LoadW<double>(P.W, n, c);
     double du[5];
-    const int64_t q = P.qpos[c];
+    const int64_t q = P.qpos[c], qpos = q;
 #pragma unroll
     for (int v = 0; v < 5; ++v) du[v] = (double)P.dUq[v * P.nq + q];
     const Prim<double> u = UpdateWithCons(w, g, du);
@@ -725,17 +1185,33 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     P.W[2 * n + c] = u.v;
     P.W[3 * n + c] = u.w;
     P.W[4 * n + c] = u.p;
-    const int64_t pos0 = (int64_t)cta_pos0[blockIdx.x] + threadIdx.x;
+    double rv[kNvMax];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      const double r = P.R[v * n + c];
+    for (int v = 0; v < 5; ++v) rv[v] = P.R[v * n + c];
+    rv[5] = rv[6] = 0.0;
+    if (sv.rans) {
+      // conserved rho k, rho omega updated, divided by the new density and
+      // held above the floors (primitive(conserved), primitive::LimitTurb)
+      const double rho1 = w.rho + du[0];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const double cq = w.rho * P.Wt[q * n + c] + (double)P.dUtq[q * P.nq + qpos];
+        const double t = cq / rho1;
+        P.Wt[q * n + c] = (t < 1.0e-20) ? 1.0e-20 : t;
+        rv[5 + q] = P.Rt[q * n + c];
+      }
+    }
+    const int nv = sv.rans ? kNvMax : kNv;
+    const int64_t pos0 = (int64_t)cta_pos0[blockIdx.x] + threadIdx.x;
+    for (int v = 0; v < nv; ++v) {
+      const double r = rv[v];
       l2[v] = r * r;
       // L-infinity follows the reference's signed comparison
       // (procBlock::UpdateBlock): a new maximum replaces the old one only
       // when strictly larger; ties keep the first in loop order
       if (r > mx) {
         mx = r;
-        mpos = pos0 * kNv + v;
+        mpos = pos0 * kNvMax + v;
       }
     }
   }
@@ -744,7 +1220,7 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
-    for (int v = 0; v < kNv; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    for (int v = 0; v < kNvMax; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
     const double om = __shfl_down_sync(0xffffffffu, mx, off);
     const int64_t op = __shfl_down_sync(0xffffffffu, mpos, off);
     if (om > mx || (om == mx && op < mpos)) {
@@ -755,7 +1231,7 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
   }
   if (lane == 0) {
 #pragma unroll
-    for (int v = 0; v < kNv; ++v) s_l2[warp][v] = l2[v];
+    for (int v = 0; v < kNvMax; ++v) s_l2[warp][v] = l2[v];
     s_max[warp] = mx;
     s_pos[warp] = mpos;
     s_bad[warp] = bad;
@@ -763,12 +1239,12 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
   __syncthreads();
   if (threadIdx.x == 0) {
     NormPartial p;
-    for (int v = 0; v < kNv; ++v) p.l2[v] = 0.0;
+    for (int v = 0; v < kNvMax; ++v) p.l2[v] = 0.0;
     p.linf = 0.0;
     p.linf_pos = INT64_MAX;
     p.bad = 0;
     for (int w = 0; w < kCta / 32; ++w) {
-      for (int v = 0; v < kNv; ++v) p.l2[v] += s_l2[w][v];
+      for (int v = 0; v < kNvMax; ++v) p.l2[v] += s_l2[w][v];
       if (s_max[w] > p.linf || (s_max[w] == p.linf && s_pos[w] < p.linf_pos)) {
         p.linf = s_max[w];
         p.linf_pos = s_pos[w];
@@ -984,14 +1460,162 @@ __device__ __forceinline__ void ViscFaceGatherMixed(const Pools<PT> &P, const Bl
   muf = cd * (float)P.mu[cu] + cw * (float)P.mu[cl];
 }
 
+// Dual-cell Green-Gauss gradients of k and omega at face c of direction D
+// (ScalarGradGG, src/utility.cpp:138): values on the dual faces are the
+// cells themselves along D and 4-cell averages across
+template <int D, typename PT>
+__device__ __forceinline__ void TurbFaceGrads(const Pools<PT> &P, const BlockDev &b, int64_t c,
+                                              double kg[3], double wg[3]) {
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  auto area = [&](int e, int64_t x, double a[3]) {
+    const double *fa = P.fa[e];
+    const double m = fa[3 * n + x];
+    a[0] = fa[x] * m;
+    a[1] = fa[n + x] * m;
+    a[2] = fa[2 * n + x] * m;
+  };
+  double lo[3][2], hi[3][2], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const double *T_ = P.Wt + q * n;
+      if (e == D) {
+        lo[e][q] = T_[cl];
+        hi[e][q] = T_[cu];
+      } else {
+        hi[e][q] = 0.25 * (((T_[cl] + T_[cu]) + T_[cu + st[e]]) + T_[cl + st[e]]);
+        lo[e][q] = 0.25 * (((T_[cl] + T_[cu]) + T_[cu - st[e]]) + T_[cl - st[e]]);
+      }
+    }
+    if (e == D) {
+      double A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (A0[r] + A1[r]);
+        alo[e][r] = 0.5 * (A0[r] + A2[r]);
+      }
+    } else {
+      double Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (Aup[r] + Alp[r]);
+        alo[e][r] = 0.5 * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const double invVol = 1.0 / (0.5 * (P.vol[cl] + P.vol[cu]));
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    kg[r] = hi[0][0] * ahi[0][r] - lo[0][0] * alo[0][r] + hi[1][0] * ahi[1][r] -
+            lo[1][0] * alo[1][r] + hi[2][0] * ahi[2][r] - lo[2][0] * alo[2][r];
+    kg[r] *= invVol;
+    wg[r] = hi[0][1] * ahi[0][r] - lo[0][1] * alo[0][r] + hi[1][1] * ahi[1][r] -
+            lo[1][1] * alo[1][r] + hi[2][1] * ahi[2][r] - lo[2][1] * alo[2][r];
+    wg[r] *= invVol;
+  }
+}
+
+// Viscous face of a RANS solve (CalcViscFluxI/J/K with SST, in FP64 for
+// both precisions): eddy viscosity and blending from the central face
+// state (turbulence floors applied), the face gradients and the central
+// wall distance (clipped to 0 within WALL_DIST_NEG_TOL); flow flux with
+// mu + mut and the turbulent conductivity, k and omega diffusion fluxes.
+// Stores the flux, the per-face SST data and (block solves) the face state.
 template <typename T, int D>
+__device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, const SolveDev &sv,
+                                             int64_t c) {
+  const Gas<double> g = GasOf<double>(sv);
+  const int64_t n = P.ncell;
+  double grad[3][3], tg[3], muf;
+  Prim<double> fs;
+  ViscFaceGather<double, D>(P, b, g, c, grad, tg, fs, muf);
+  double kg[3], wg[3];
+  TurbFaceGrads<D>(P, b, c, kg, wg);
+  const int64_t cu = c, cl = c - StrideOf(b, D);
+  const double *wd = P.width[D];
+  double cd, cw;
+  CentralCoeffs(wd[cl], wd[cu], cd, cw);
+  double fst[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    fst[q] = CMax(cd * P.Wt[q * n + cu] + cw * P.Wt[q * n + cl], kTurbMin);
+  double wdf = cd * P.wd[cu] + cw * P.wd[cl];
+  if (wdf < 0.0 && wdf > -1.0e-10) wdf = 0.0;
+  const double scale = sv.visc_scale;
+  const double vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
+                        grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
+  double mutf, f1f, f2f;
+  SstEddyVisc(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
+  const double *fa = P.fa[D];
+  const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c], mag = fa[3 * n + c];
+  const double mus = scale * muf, muts = scale * mutf;
+  double tau[3];
+  TauNormal(vg, nx, ny, nz, mus, muts, tau);
+  const double kf = SutherlandRatio(Temperature(fs, g), sv.t_ref, sv.k_c1, sv.k_s, sv.k_ref) *
+                    scale;
+  const double kt = muts * g.Cp() / 0.9;
+  double F[5];
+  F[0] = 0.0;
+  F[1] = tau[0];
+  F[2] = tau[1];
+  F[3] = tau[2];
+  F[4] = Dot(tau[0], tau[1], tau[2], fs.u, fs.v, fs.w) +
+         (kf + kt) * Dot(tg[0], tg[1], tg[2], nx, ny, nz) + 0.0;
+  const double Ft0 = (mus + Blended(kSstSigmaK1, kSstSigmaK2, f1f) * muts) *
+                     Dot(kg[0], kg[1], kg[2], nx, ny, nz);
+  const double Ft1 = (mus + Blended(kSstSigmaW1, kSstSigmaW2, f1f) * muts) *
+                     Dot(wg[0], wg[1], wg[2], nx, ny, nz);
+  T *out = P.vflux[D];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v * n + c] = (T)(F[v] * mag);
+  P.vfluxt[D][c] = (T)(Ft0 * mag);
+  P.vfluxt[D][n + c] = (T)(Ft1 * mag);
+  T *rs = P.rst[D];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) rs[e * n + c] = (T)vg[e];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    rs[(9 + e) * n + c] = (T)kg[e];
+    rs[(12 + e) * n + c] = (T)wg[e];
+  }
+  rs[15 * n + c] = (T)mutf;
+  rs[16 * n + c] = (T)f1f;
+  rs[17 * n + c] = (T)f2f;
+  if (sv.block) {
+    T *vs = P.vst[D];
+    vs[0 * n + c] = (T)fs.rho;
+    vs[1 * n + c] = (T)fs.u;
+    vs[2 * n + c] = (T)fs.v;
+    vs[3 * n + c] = (T)fs.w;
+    vs[4 * n + c] = (T)fs.p;
+    vs[5 * n + c] = (T)muf;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) vs[(6 + e) * n + c] = (T)vg[e];
+  }
+}
+
+template <typename T, int D, bool RANS>
 __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
                                                 const int32_t *cta_block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
-  if (!sv.viscous || !sv.active) return;
+  if (!sv.viscous || !sv.active || (sv.rans != 0) != RANS) return;
+  if constexpr (RANS) {
+    RansViscFace<T, D>(P, b, sv, c);
+    return;
+  }
   const Gas<T> g = GasOf<T>(sv);
   const int64_t n = P.ncell;
   T grad[3][3], tg[3];
@@ -1065,7 +1689,9 @@ __global__ void k_wall(Pools<T> P, const WallFaceDev *faces, int nfaces, double 
   else ViscFaceGather<double, 2>(P, b, g, c, grad, tg, fs, muf);
   const double *fa = P.fa[wf.dir];
   const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c], mag = fa[3 * n + c];
-  const double mus = sv.visc_scale * muf, muts = sv.visc_scale * 0.0;
+  // RANS: the face eddy viscosity of the viscous flux kernel
+  const double mutf = sv.rans ? (double)P.rst[wf.dir][15 * n + c] : 0.0;
+  const double mus = sv.visc_scale * muf, muts = sv.visc_scale * mutf;
   const double vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
                         grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
   double tau[3];
@@ -1094,28 +1720,51 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
   if (c >= 0) {
     const Gas<T> g = GasOf<T>(sv);
     const int64_t q = P.qpos[c], nq = P.nq;
-    T L[5], U[5], Ax[5], x[5];
+    const int nv = sv.rans ? 7 : 5;
+    T L[7], U[7], Ax[7], x[7], bt[7];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) x[v] = P.dUq[v * nq + q];
+    for (int v = 0; v < 5; ++v) {
+      x[v] = P.dUq[v * nq + q];
+      bt[v] = P.Rq[v * nq + q];
+    }
+    x[5] = x[6] = bt[5] = bt[6] = T(0);
+    if (sv.rans)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        x[5 + v] = P.dUtq[v * nq + q];
+        bt[5 + v] = P.Rtq[v * nq + q];
+      }
     if constexpr (BLOCK) {
-      OffDiagSumBlock(P, g, sv, q, true, L);
-      OffDiagSumBlock(P, g, sv, q, false, U);
+      OffDiagSumBlock(P, g, sv, q, true, L, L + 5);
+      OffDiagSumBlock(P, g, sv, q, false, U, U + 5);
       T A[kJac];
 #pragma unroll
       for (int e = 0; e < kJac; ++e) A[e] = P.Aq[e * nq + q];
       MatVec5(A, x, Ax);
+      if (sv.rans) {
+        T At[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) At[e] = P.Atq[e * nq + q];
+        MatVec2(At, x + 5, Ax + 5);
+      }
     } else {
-      OffDiagSum(P, g, sv, q, true, L);
-      OffDiagSum(P, g, sv, q, false, U);
+      OffDiagSum(P, g, sv, q, true, L, L + 5);
+      OffDiagSum(P, g, sv, q, false, U, U + 5);
       const T a = P.Aq[q];
 #pragma unroll
       for (int v = 0; v < 5; ++v) Ax[v] = x[v] * a;
+      if (sv.rans) {
+        const T at = P.Atq[q];
+        Ax[5] = x[5] * at;
+        Ax[6] = x[6] * at;
+      }
     }
     const T thetaInv = (T)(1.0 / sv.theta);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) {
+    for (int v = 0; v < 7; ++v) {
+      if (v >= nv) break;
       const T off = L[v] - U[v];
-      const T bv = -thetaInv * P.Rq[v * nq + q];
+      const T bv = -thetaInv * bt[v];
       const T axmb = Ax[v] - off - bv;
       const double r = 0.0 - (double)axmb;
       sum += r * r;
@@ -1155,21 +1804,33 @@ void Launch<T>::Aux(const Pools<T> &P, const int32_t *cells, const int32_t *cell
                     int n, cudaStream_t s) {
   if (n > 0) k_aux<T><<<(n + 127) / 128, 128, 0, s>>>(P, cells, cell_block, n);
 }
+template <typename T, int D>
+static void LaunchVFace(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                        int ncta, int rkinds, cudaStream_t s) {
+  if (rkinds & 1) k_vface<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (rkinds & 2) k_vface<T, D, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+}
 template <typename T>
 void Launch<T>::ViscFace(int d, const Pools<T> &P, const int32_t *list,
-                         const int32_t *cta_block, int ncta, cudaStream_t s) {
+                         const int32_t *cta_block, int ncta, int rkinds, cudaStream_t s) {
   if (ncta <= 0) return;
-  if (d == 0) k_vface<T, 0><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  else if (d == 1) k_vface<T, 1><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  else k_vface<T, 2><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (d == 0) LaunchVFace<T, 0>(P, list, cta_block, ncta, rkinds, s);
+  else if (d == 1) LaunchVFace<T, 1>(P, list, cta_block, ncta, rkinds, s);
+  else LaunchVFace<T, 2>(P, list, cta_block, ncta, rkinds, s);
+}
+template <typename T, int D>
+static void LaunchFace(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                       int ncta, int rkinds, cudaStream_t s) {
+  if (rkinds & 1) k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (rkinds & 2) k_face<T, D, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
 void Launch<T>::Face(int d, const Pools<T> &P, const int32_t *list,
-                     const int32_t *cta_block, int ncta, cudaStream_t s) {
+                     const int32_t *cta_block, int ncta, int rkinds, cudaStream_t s) {
   if (ncta <= 0) return;
-  if (d == 0) k_face<T, 0><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  else if (d == 1) k_face<T, 1><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  else k_face<T, 2><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (d == 0) LaunchFace<T, 0>(P, list, cta_block, ncta, rkinds, s);
+  else if (d == 1) LaunchFace<T, 1>(P, list, cta_block, ncta, rkinds, s);
+  else LaunchFace<T, 2>(P, list, cta_block, ncta, rkinds, s);
 }
 template <typename T>
 void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

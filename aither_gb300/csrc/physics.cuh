@@ -445,7 +445,7 @@ __device__ __forceinline__ T SignOf(T x) {
 }
 template <typename T>
 __device__ __forceinline__ void AusmFlux(const Prim<T> &L, const Prim<T> &R, const Gas<T> &g,
-                                         T nx, T ny, T nz, T f[5]) {
+                                         T nx, T ny, T nz, T f[5], T *vlr = nullptr) {
   const T vnL = Dot(L.u, L.v, L.w, nx, ny, nz);
   const T vnR = Dot(R.u, R.v, R.w, nx, ny, nz);
   const T sosStar = sqrt(SoS(L, g) * SoS(R, g));
@@ -486,6 +486,50 @@ __device__ __forceinline__ void AusmFlux(const Prim<T> &L, const Prim<T> &R, con
   f[2] += R.rho * vr * R.v + pMinus * R.p * ny;
   f[3] += R.rho * vr * R.w + pMinus * R.p * nz;
   f[4] += R.rho * vr * Enthalpy(R, g);
+  if (vlr) {
+    vlr[0] = vl;
+    vlr[1] = vr;
+  }
+}
+
+// Turbulence components of the Roe flux (include/inviscidFlux.hpp:311-368):
+// both acoustic waves carry the Roe-averaged k and omega, plus the
+// turbulence waves; F = 0.5 (FL + (FR - D)) with F = rho vn k.
+template <typename T>
+__device__ __forceinline__ void RoeTurbFlux(const Prim<T> &L, const Prim<T> &R, const T Lt[2],
+                                            const T Rt[2], const Gas<T> &g, T nx, T ny, T nz,
+                                            T ft[2]) {
+  const T denRatio = sqrt(R.rho / L.rho);
+  Prim<T> roe;
+  roe.rho = L.rho * denRatio;
+  roe.u = (L.u + denRatio * R.u) / (T(1) + denRatio);
+  roe.v = (L.v + denRatio * R.v) / (T(1) + denRatio);
+  roe.w = (L.w + denRatio * R.w) / (T(1) + denRatio);
+  roe.p = (L.p + denRatio * R.p) / (T(1) + denRatio);
+  const T aR = SoS(roe, g);
+  const T rhoR = roe.rho;
+  const T velNormR = Dot(roe.u, roe.v, roe.w, nx, ny, nz);
+  const T dRho = R.rho - L.rho, dP = R.p - L.p;
+  const T normVelDiff = Dot(R.u - L.u, R.v - L.v, R.w - L.w, nx, ny, nz);
+  const T entropyFix = T(0.1);
+  T ws = fabs(velNormR - aR);
+  if (ws < entropyFix) ws = T(0.5) * (ws * ws / entropyFix + entropyFix);
+  const T wssL = ws * ((dP - rhoR * aR * normVelDiff) / (T(2) * aR * aR));
+  ws = fabs(velNormR + aR);
+  if (ws < entropyFix) ws = T(0.5) * (ws * ws / entropyFix + entropyFix);
+  const T wssR = ws * ((dP + rhoR * aR * normVelDiff) / (T(2) * aR * aR));
+  const T wsT = fabs(velNormR);
+  const T vnL = Dot(L.u, L.v, L.w, nx, ny, nz), vnR = Dot(R.u, R.v, R.w, nx, ny, nz);
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const T rt = (Lt[q] + denRatio * Rt[q]) / (T(1) + denRatio);
+    T d = T(0);
+    d += wssL * rt;
+    d += wssR * rt;
+    d += wsT * (rhoR * (Rt[q] - Lt[q]) + rt * dRho - dP * rt / (aR * aR)) * T(1);
+    const T fl = L.rho * vnL * Lt[q], fr = R.rho * vnR * Rt[q];
+    ft[q] = (fl + (fr - d)) * T(0.5);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -508,6 +552,11 @@ __device__ __forceinline__ T ViscMaxTerm(const Prim<T> &s, const Gas<T> &g) {
 template <typename T>
 __device__ __forceinline__ T ViscTerm(T mu, T scale, const Gas<T> &g) {
   return scale * (mu / Prandtl(g) + T(0) / T(0.9));
+}
+// the same with the eddy viscosity mut (turbulent Prandtl number 0.9)
+template <typename T>
+__device__ __forceinline__ T ViscTerm2(T mu, T mut, T scale, const Gas<T> &g) {
+  return scale * (mu / Prandtl(g) + mut / T(0.9));
 }
 // sutherland::SpeciesViscosity / SpeciesConductivity (src/transport.cpp:100,108)
 template <typename T>

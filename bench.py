@@ -300,7 +300,7 @@ def run_converge(args, ctx, setup, specs, world):
 
 def run_e2e(batch, ncells: int, steps: int, world: int) -> dict:
     n = batch.pool_cells()
-    host = _pinned(5 * n)
+    host = _pinned(batch.pool_vars() * n)
     batch.copy_state(host, to_device=False)
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -311,7 +311,7 @@ def run_e2e(batch, ncells: int, steps: int, world: int) -> dict:
     dt = _max_over_ranks(dt * 1e3, world) * 1e-3
     from aither_gb300._lib import Norms
     import ctypes
-    nb = 5 * n * 8
+    nb = host.size * 8
     return {"value": ncells * steps * world / dt, "unit": METRIC,
             "h2d_bytes_per_step": nb,
             "d2h_bytes_per_step": nb + ctypes.sizeof(Norms) * batch.nsolves}

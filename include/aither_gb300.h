@@ -328,7 +328,9 @@ enum {
 };
 int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h);
 int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h);
-int ath_batch_field_width(ath_batch *batch, int field);
+/* Values per cell of `field` for block `block`: the block's nv (5, or 7
+ * with the SST k and omega) for STATE, STATE_GHOSTS, RESID and DU. */
+int ath_batch_field_width(ath_batch *batch, int block, int field);
 
 /* Device work counters of the last ath_batch_iterate call. */
 typedef struct {
@@ -338,13 +340,16 @@ typedef struct {
 int ath_batch_stats(ath_batch *batch, ath_stats *out);
 
 /* Whole-batch snapshot of the primitive state in the device layout:
- * [5][pool cells] FP64, every block's padded cells back to back (block b
- * starts at the sum of the padded cell counts of blocks 0..b-1).  One copy
- * each way; pass page-locked host memory for full link bandwidth.
- * to_device = 1 uploads host -> device, 0 downloads.  (Restart snapshots of
- * resident solutions, reference WriteRestart/ReadRestart src/output.cpp:
- * 591,756, go through this.) */
+ * [nv][pool cells] FP64 with nv from ath_batch_pool_vars (5, or 7 when the
+ * batch holds SST solves: rho, u, v, w, p, then k, omega; k and omega are
+ * 0 in the blocks of other solves), every block's padded cells back to back
+ * (block b starts at the sum of the padded cell counts of blocks 0..b-1).
+ * One copy per pool each way; pass page-locked host memory for full link
+ * bandwidth.  to_device = 1 uploads host -> device, 0 downloads.  (Restart
+ * snapshots of resident solutions, reference WriteRestart/ReadRestart
+ * src/output.cpp:591,756, go through this.) */
 int ath_batch_pool_cells(ath_batch *batch, int64_t *ncell);
+int ath_batch_pool_vars(ath_batch *batch, int *nv);
 int ath_batch_copy_state(ath_batch *batch, double *host, int to_device);
 
 /* CUDA-event timing of each kernel class on the batch stream, averaged
