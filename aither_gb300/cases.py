@@ -267,12 +267,15 @@ def wall_channel_nodes(ni: int, nj: int, nk: int, kind: str, param: float,
 def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float,
                  mach: float, alpha: float = 0.0, viscous: bool = False,
                  reynolds: float = 1e5, stretch: float = 1.0, cfl: float = 20.0,
-                 name: str = "chan", precision_note: str = ""):
+                 name: str = "chan", precision_note: str = "", rans: bool = False,
+                 tint: float = 0.001, vratio: float = 10.0):
     """Bump or wedge channel with free-stream Mach `mach` at angle of attack
     `alpha` (degrees, in the x-y plane); characteristic in- and outflow,
     slip upper and side walls; the lower wall is a slip wall (Euler) or an
-    adiabatic viscous wall (laminar Navier-Stokes, density from Re based on
-    the unit chord and Sutherland's viscosity)."""
+    adiabatic viscous wall (laminar Navier-Stokes, or SST-2003 RANS with
+    `rans`; density from Re based on the unit chord and Sutherland's
+    viscosity)."""
+    viscous = viscous or rans
     os.makedirs(outdir, exist_ok=True)
     nodes = wall_channel_nodes(ni, nj, nk, kind, param, stretch)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
@@ -287,9 +290,11 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
     refs = Refs(t_ref=t_inf, r_ref=rho_inf)
     ca, sa = math.cos(math.radians(alpha)), math.sin(math.radians(alpha))
     vel = f"[{_fmt(u_inf * ca)}, {_fmt(u_inf * sa)}, 0]"
-    ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel})"
+    turb = f"; turbulenceIntensity={_fmt(tint)}; eddyViscosityRatio={_fmt(vratio)}" if rans else ""
+    ic = (f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel}"
+          f"{turb})")
     states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
-              f"velocity={vel})"]
+              f"velocity={vel}{turb})"]
     lower = ("slipWall", 0, ni, 0, 0, 0, nk, 2)
     if viscous:
         states.append("viscousWall(tag=3)")
@@ -303,18 +308,21 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
     inp = os.path.join(outdir, name + ".inp")
     scheme = {"cfl": cfl, "cflStart": 1.0, "cflStep": 1.0,
               "limiter": "vanAlbada" if viscous else "minmod",
-              "equationSet": "navierStokes" if viscous else "euler"}
+              "equationSet": "rans" if rans else ("navierStokes" if viscous else "euler"),
+              "turbulenceModel": "sst2003" if rans else "none"}
     write_input(inp, name, scheme, refs, ic, states, bcs)
     return inp, None
 
 
 def served_specs(n: int, seed: int = 7, min_cells: int = 16_000, max_cells: int = 4_000_000,
-                 log_mean: float = math.log(150_000.0), log_sigma: float = 1.2):
+                 log_mean: float = math.log(150_000.0), log_sigma: float = 1.2,
+                 mix: str = "ns_sst"):
     """Request stream of the served workload: cell counts log-normal, clipped
     to [min_cells, max_cells], shaped ni : nj : nk = 4 : 2 : 1; bump or wedge
-    lower wall; Mach U[0.3, 2.5]; angle of attack U[-4, 4] degrees; every
-    second request laminar Navier-Stokes with a stretched wall-normal grid,
-    the others Euler."""
+    lower wall; Mach U[0.3, 2.5]; angle of attack U[-4, 4] degrees.  mix
+    "ns_sst": every second request SST-2003 RANS, the others laminar
+    Navier-Stokes, both with a stretched wall-normal grid; "euler_ns": every
+    second request laminar Navier-Stokes, the others Euler."""
     rng = np.random.default_rng(seed)
     out = []
     for q in range(n):
@@ -326,7 +334,11 @@ def served_specs(n: int, seed: int = 7, min_cells: int = 16_000, max_cells: int 
         param = float(rng.uniform(0.04, 0.10)) if kind == "bump" else float(rng.uniform(4, 10))
         out.append({"ni": ni, "nj": nj, "nk": nk, "kind": kind, "param": param,
                     "mach": float(rng.uniform(0.3, 2.5)), "alpha": float(rng.uniform(-4, 4)),
-                    "viscous": q % 2 == 1})
+                    "viscous": mix == "ns_sst" or q % 2 == 1,
+                    "rans": mix == "ns_sst" and q % 2 == 1,
+                    # SST requests ramp to CFL 5: at 20 the supersonic ones
+                    # turn nonphysical
+                    "cfl": 5.0 if (mix == "ns_sst" and q % 2 == 1) else 20.0})
     return out
 
 
@@ -349,10 +361,13 @@ def sutherland_mu(t: float, c1: float = 1.458e-6, s: float = 110.4) -> float:
 
 
 def plate_nodes(x0: float, x1: float, ni: int, nj: int, nk: int, dy0: float, ratio: float,
-                dz: float) -> np.ndarray:
-    """Block on [x0, x1] in x, geometric wall-normal spacing from y=0."""
+                dz: float, dy_max: float | None = None) -> np.ndarray:
+    """Block on [x0, x1] in x, geometric wall-normal spacing from y=0
+    (held at dy_max once it reaches it)."""
     x = x0 + (x1 - x0) * np.arange(ni + 1) / ni
     dy = dy0 * ratio ** np.arange(nj)
+    if dy_max is not None:
+        dy = np.minimum(dy, dy_max)
     y = np.concatenate([[0.0], np.cumsum(dy)])
     z = dz * np.arange(nk + 1)
     Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
@@ -365,7 +380,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                wall_t: float | None = None, limiter: str = "vanAlbada",
                name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder",
                sweeps: int = 1, rans: bool = False, tint: float = 0.001, vratio: float = 10.0,
-               flux: str = "roe", nblocks: int = 2):
+               flux: str = "roe", nblocks: int = 2, dy_max: float | None = None):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -373,8 +388,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
     Sutherland's law at t_inf."""
     os.makedirs(outdir, exist_ok=True)
     dz = 0.02 * length
-    b0 = plate_nodes(0.0, 0.5 * length, ni, nj, nk, dy0, ratio, dz)
-    b1 = plate_nodes(0.5 * length, length, ni, nj, nk, dy0, ratio, dz)
+    b0 = plate_nodes(0.0, 0.5 * length, ni, nj, nk, dy0, ratio, dz, dy_max)
+    b1 = plate_nodes(0.5 * length, length, ni, nj, nk, dy0, ratio, dz, dy_max)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [b0, b1])
     a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
     u_inf = mach * a_inf
@@ -405,7 +420,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
               "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
               "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps}
     if nblocks == 1:
-        nodes = plate_nodes(0.0, length, ni, nj, nk, dy0, ratio, dz)
+        nodes = plate_nodes(0.0, length, ni, nj, nk, dy0, ratio, dz, dy_max)
         write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
         blk = [("characteristic", 0, 0, 0, nj, 0, nk, 1),
                ("characteristic", ni, ni, 0, nj, 0, nk, 1),
@@ -417,3 +432,26 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
     else:
         write_input(inp, name, scheme, refs, ic, states, [blk0, blk1])
     return inp, None
+
+
+def turbulent_plate_dy0(reynolds: float, yplus: float = 1.0, length: float = 1.0) -> float:
+    """Wall spacing for a target y+ at the end of a turbulent flat plate:
+    skin friction from the 1/7-power correlation Cf = 0.026 Re^(-1/7),
+    u_tau = U sqrt(Cf/2), y = y+ nu / u_tau."""
+    cf = 0.026 * reynolds ** (-1.0 / 7.0)
+    return yplus * length / (reynolds * math.sqrt(0.5 * cf))
+
+
+def sst_plate(outdir: str, ni: int = 256, nj: int = 192, nk: int = 4, name: str = "sstplate",
+              cfl: float = 50.0, **kw):
+    """SST-2003 turbulent flat plate: one block of ni x nj x nk cells,
+    Re_L = 5e6, Mach 0.2, turbulence intensity 0.1 %, eddy viscosity ratio
+    10, first cell at y+ = 1, growth 1.1 up to 0.05 L, WENO, AUSM, block
+    LU-SGS."""
+    re = kw.pop("reynolds", 5e6)
+    args = dict(ni=ni, nj=nj, nk=nk, dy0=turbulent_plate_dy0(re), ratio=1.1, mach=0.2,
+                reynolds=re, cfl=cfl, name=name, matrix_solver="blusgs", recon="weno",
+                limiter="none", flux="ausm", rans=True, tint=0.001, vratio=10.0, nblocks=1,
+                dy_max=0.05)
+    args.update(kw)
+    return flat_plate(outdir, **args)

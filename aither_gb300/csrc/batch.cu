@@ -352,6 +352,12 @@ class Runner : public RunnerBase {
         P_.vgq = m.Alloc<T>(9 * nq);
         Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
       }
+      P_.Joff = m.Alloc<T>(150 * nq);
+      Check(cudaMemset(P_.Joff, 0, 150 * nq * sizeof(T)), "memset");
+      if (c.any_rans) {
+        P_.Jtoff = m.Alloc<T>(24 * nq);
+        Check(cudaMemset(P_.Jtoff, 0, 24 * nq * sizeof(T)), "memset");
+      }
     }
     Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
     Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
@@ -525,6 +531,8 @@ class Runner : public RunnerBase {
     Viscous();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                     c_.kinds, c_.stream);
+    if (c_.kinds & 2)
+      Launch<T>::OffJac(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
   }
   void SweepPass(int forward, int sweep) {
     const bool full = c_.max_sweeps > 1;
@@ -617,6 +625,8 @@ class Runner : public RunnerBase {
       Viscous();
       Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                       c_.kinds, c_.stream);
+      if (c_.kinds & 2)
+        Launch<T>::OffJac(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
       Check(cudaEventRecord(e[5], c_.stream), "event");
       // forward passes, then backward passes (one-sweep form; the timing
       // split of a multi-sweep relaxation puts each sweep's passes in turn)
@@ -1173,7 +1183,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
                         (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 * nvf
                                          : 0) +
                         (c.L.wall_faces.empty() ? 0 : 2) +
-                        1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds +
+                        1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
                         2 * c.nsteps * c.max_sweeps * nkinds +
                         (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn) + 3 +
                         ((flags & 1) ? nkinds + conn : 0);
@@ -1661,12 +1671,12 @@ size_t EstimateBatchBytes(const Setup &st, int precision) {
     if (visc) pc += 15 * ts + 8;
     if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);
     double qc = ts * (5 + 5 + 5 + 24 + 6 + 2 + 1) + 4.0 * 8;
-    if (blk) qc += ts * (48 + (visc ? 9 : 0));
+    if (blk) qc += ts * (48 + (visc ? 9 : 0) + 150);  // + stored off-diagonal blocks
     if (ph.eqn == ATH_EQN_RANS) {
       // k, omega, their residual, radius, wall distance, inviscid fluxes
       // (FP64); viscous fluxes and per-face SST data; sweep arrays
       pc += 8.0 * (2 + 2 + 1 + 1 + 6) + ts * (6 + 54);
-      qc += ts * (2 + 2 + (blk ? 8 : 2) + 2);
+      qc += ts * (2 + 2 + (blk ? 8 + 24 : 2) + 2);
     }
     bytes += n * pc + nq * qc;
   }

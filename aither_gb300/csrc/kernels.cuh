@@ -125,6 +125,10 @@ struct Pools {
   T *dUtg;          // [2][nghost]
   T *Ainvtq, *Atq;  // [nq] scalar or [4][nq] 2x2 turbulence diagonal (inverse)
   T *mutq, *f1q;    // [nq] cell eddy viscosity and F1
+  // block solves: off-diagonal Jacobians of each cell's six neighbours,
+  // [(side*3 + d)*25 + e][nq] (side 0 = lower) and the turbulence blocks
+  // [(side*3 + d)*4 + e][nq]
+  T *Joff, *Jtoff;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -266,6 +270,8 @@ struct Launch {
                    int ncta, int kinds, cudaStream_t s);
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
                     bool full, int kinds, int threads, cudaStream_t s);
+  // off-diagonal Jacobians of the block solves' cells, once per iteration
+  static void OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   static void Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

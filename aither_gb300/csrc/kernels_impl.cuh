@@ -886,21 +886,110 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
   }
 }
 
-// Off-diagonal sum of one cell of a block solve (RusanovBlockOffDiagonal,
-// src/fluxJacobian.cpp:164): per neighbour the Rusanov Jacobian of its state
-// minus (lower) or plus (upper) its thin-shear-layer Jacobian with its
-// viscosity and cell-averaged gradient, times its update; the turbulence
-// rows likewise with the 2x2 Rusanov and viscous Jacobians (turbKWSst::ViscJac,
-// src/turbulence.cpp:764).
+// Off-diagonal Jacobians of one neighbour of a block solve's cell
+// (RusanovBlockOffDiagonal, src/fluxJacobian.cpp:164): the Rusanov Jacobian
+// of the neighbour's state minus (lower) or plus (upper) its thin-shear-
+// layer Jacobian with its viscosity and cell-averaged gradient; the 2x2
+// turbulence block likewise from the Rusanov and viscous Jacobians
+// (turbKWSst::ViscJac, src/turbulence.cpp:764).  They depend on nothing the
+// sweeps change, so k_offjac evaluates them once per iteration.
 template <typename T>
-__device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const Gas<T> &g,
-                                                const SolveDev &sv, int64_t q, bool lower,
-                                                T acc[5], T acct[2]) {
+__device__ __forceinline__ void BlockOffJac(const Pools<T> &P, const Gas<T> &g,
+                                            const SolveDev &sv, const TslCoeffs<T> &tk,
+                                            int64_t q, bool lower, int d, int32_t nb,
+                                            T J[kJac], T Jt[4]) {
   const int64_t nq = P.nq;
   const T *face = lower ? P.face_lo : P.face_hi;
   const T *dist = lower ? P.dist_lo : P.dist_hi;
-  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+  Nbr<T> o;
+  LoadNbr(P, sv, nb, o);
+  const T *f = face + (int64_t)d * 4 * nq;
+  const T fx = f[q], fy = f[nq + q], fz = f[2 * nq + q], mag = f[3 * nq + q];
+  RusanovJac(o.s, g, fx, fy, fz, mag, lower, J);
+  if (sv.viscous) {
+    T vg[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) vg[e] = P.vgq[e * nq + o.vq];
+    TslJacAccum(o.s, o.mu, o.mut, g, tk, fx, fy, fz, mag, dist[d * nq + q], lower, vg, lower,
+                J);
+  }
+  if (sv.rans) {
+    TurbRusanovJac(o.s, fx, fy, fz, mag, lower, Jt);
+    if (sv.viscous) {
+      T Tv[4];
+      TurbViscJac(o.s.rho, mag, o.mu, o.mut, o.f1, dist[d * nq + q], (T)sv.visc_scale,
+                  lower ? T(-1) : T(1), Tv);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
+    }
+  }
+}
+
+// Stored off-diagonal blocks: Joff[(side*3 + d)*25 + e][nq] (side 0 =
+// lower neighbours), Jtoff[(side*3 + d)*4 + e][nq]
+template <typename T>
+__global__ void __launch_bounds__(128) k_offjac(Pools<T> P, const int2 *items, int n_items) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const int64_t q = it.x, nq = P.nq;
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (!sv.block || !sv.active) return;
+  const Gas<T> g = GasOf<T>(sv);
   const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref};
+#pragma unroll 1
+  for (int side = 0; side < 2; ++side) {
+    const int32_t *nbq = P.nbq + (side == 0 ? 0 : 3 * nq);
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+      const int32_t nb = nbq[d * nq + q];
+      if (nb == -1) continue;
+      T J[kJac], Jt[4];
+      BlockOffJac(P, g, sv, tk, q, side == 0, d, nb, J, Jt);
+      T *out = P.Joff + (int64_t)(side * 3 + d) * kJac * nq + q;
+#pragma unroll
+      for (int e = 0; e < kJac; ++e) out[e * nq] = J[e];
+      if (sv.rans) {
+        T *ot = P.Jtoff + (int64_t)(side * 3 + d) * 4 * nq + q;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ot[e * nq] = Jt[e];
+      }
+    }
+  }
+}
+
+// Update of the neighbour across face d (flow and turbulence)
+template <typename T>
+__device__ __forceinline__ void LoadNbrDu(const Pools<T> &P, const SolveDev &sv, int32_t nb,
+                                          T du[5], T dut[2]) {
+  const int64_t nq = P.nq, ng = P.nghost;
+  dut[0] = dut[1] = T(0);
+  if (nb >= 0) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) du[v] = P.dUq[v * nq + nb];
+    if (sv.rans) {
+      dut[0] = P.dUtq[nb];
+      dut[1] = P.dUtq[nq + nb];
+    }
+  } else {
+    const int64_t slot = -(int64_t)nb - 2;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) du[v] = P.dUg[v * ng + slot];
+    if (sv.rans) {
+      dut[0] = P.dUtg[slot];
+      dut[1] = P.dUtg[ng + slot];
+    }
+  }
+}
+
+// Off-diagonal sum of one cell of a block solve: the stored Jacobian of each
+// neighbour times its update (ArrayMultiplication), accumulated i, j, k.
+template <typename T>
+__device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const SolveDev &sv,
+                                                int64_t q, bool lower, T acc[5], T acct[2]) {
+  const int64_t nq = P.nq;
+  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+  const int side = lower ? 0 : 1;
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
   acct[0] = acct[1] = T(0);
@@ -908,34 +997,20 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const Gas<T> 
   for (int d = 0; d < 3; ++d) {
     const int32_t nb = nbq[d * nq + q];
     if (nb == -1) continue;
-    Nbr<T> o;
-    LoadNbr(P, sv, nb, o);
-    const T *f = face + (int64_t)d * 4 * nq;
-    const T fx = f[q], fy = f[nq + q], fz = f[2 * nq + q], mag = f[3 * nq + q];
-    T J[kJac];
-    RusanovJac(o.s, g, fx, fy, fz, mag, lower, J);
-    if (sv.viscous) {
-      T vg[9];
+    T du[5], dut[2], J[kJac], r[5];
+    LoadNbrDu(P, sv, nb, du, dut);
+    const T *Jp = P.Joff + (int64_t)(side * 3 + d) * kJac * nq + q;
 #pragma unroll
-      for (int e = 0; e < 9; ++e) vg[e] = P.vgq[e * nq + o.vq];
-      TslJacAccum(o.s, o.mu, o.mut, g, tk, fx, fy, fz, mag, dist[d * nq + q], lower, vg, lower,
-                  J);
-    }
-    T r[5];
-    MatVec5(J, o.du, r);
+    for (int e = 0; e < kJac; ++e) J[e] = Jp[e * nq];
+    MatVec5(J, du, r);
 #pragma unroll
     for (int v = 0; v < 5; ++v) acc[v] = acc[v] + r[v];
     if (sv.rans) {
       T Jt[4], rt[2];
-      TurbRusanovJac(o.s, fx, fy, fz, mag, lower, Jt);
-      if (sv.viscous) {
-        T Tv[4];
-        TurbViscJac(o.s.rho, mag, o.mu, o.mut, o.f1, dist[d * nq + q], (T)sv.visc_scale,
-                    lower ? T(-1) : T(1), Tv);
+      const T *Jtp = P.Jtoff + (int64_t)(side * 3 + d) * 4 * nq + q;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
-      }
-      MatVec2(Jt, o.dut, rt);
+      for (int e = 0; e < 4; ++e) Jt[e] = Jtp[e * nq];
+      MatVec2(Jt, dut, rt);
       acct[0] = acct[0] + rt[0];
       acct[1] = acct[1] + rt[1];
     }
@@ -1033,7 +1108,7 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
   const int64_t nq = P.nq;
   const T thetaInv = (T)(1.0 / sv.theta);
   T acc[5], in[5], x[5], acct[2], int_[2], xt[2];
-  OffDiagSumBlock(P, g, sv, q, forward != 0, acc, acct);
+  OffDiagSumBlock(P, sv, q, forward != 0, acc, acct);
   T Ai[kJac], Ait[4];
 #pragma unroll
   for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
@@ -1042,7 +1117,7 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
     for (int e = 0; e < 4; ++e) Ait[e] = P.Ainvtq[e * nq + q];
   if (full) {
     T other[5], othert[2];
-    OffDiagSumBlock(P, g, sv, q, forward == 0, other, othert);
+    OffDiagSumBlock(P, sv, q, forward == 0, other, othert);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       const T bv = -thetaInv * P.Rq[v * nq + q];
@@ -1735,8 +1810,8 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
         bt[5 + v] = P.Rtq[v * nq + q];
       }
     if constexpr (BLOCK) {
-      OffDiagSumBlock(P, g, sv, q, true, L, L + 5);
-      OffDiagSumBlock(P, g, sv, q, false, U, U + 5);
+      OffDiagSumBlock(P, sv, q, true, L, L + 5);
+      OffDiagSumBlock(P, sv, q, false, U, U + 5);
       T A[kJac];
 #pragma unroll
       for (int e = 0; e < kJac; ++e) A[e] = P.Aq[e * nq + q];
@@ -1849,6 +1924,10 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, 
     else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
   if (kinds & 2) k_sweepb<T><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+}
+template <typename T>
+void Launch<T>::OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {
+  if (n > 0) k_offjac<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n);
 }
 template <typename T>
 void Launch<T>::Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {

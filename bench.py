@@ -110,14 +110,21 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------- roofline model
-def algorithmic_bytes(nv: int = 5, d: int = 1, b: int = 8) -> dict:
+def algorithmic_bytes(nv: int = 5, d: int = 1, b: int = 8, viscous: bool = False,
+                      block: bool = False, rans: bool = False) -> dict:
     """Compulsory traffic per cell-iteration of the four irreducible passes
     (values counted once per pass that needs them; ghosts and metadata
     excluded): residual (2nv+17+d), forward sweep (4nv+d+12), backward
-    sweep (4nv+d+12), update+norms (4nv); b bytes per value."""
-    return {"residual": (2 * nv + 17 + d) * b, "forward": (4 * nv + d + 12) * b,
-            "backward": (4 * nv + d + 12) * b, "update": 4 * nv * b,
-            "total": (14 * nv + 3 * d + 41) * b}
+    sweep (4nv+d+12), update+norms (4nv); b bytes per value.  Viscous
+    solves add 24 values to the residual (centres, wall distance, velocity,
+    temperature, density and pressure gradients, viscosity, temperature) and
+    4 per sweep (centres, viscosity), 13 with block solves (the velocity
+    gradient); SST adds 9 to the residual (k and omega gradients, eddy
+    viscosity, F1, F2) and 2 per sweep (eddy viscosity, F1)."""
+    res = 2 * nv + 17 + d + (24 if viscous else 0) + (9 if rans else 0)
+    sw = 4 * nv + d + 12 + ((13 if block else 4) if viscous else 0) + (2 if rans else 0)
+    return {"residual": res * b, "forward": sw * b, "backward": sw * b, "update": 4 * nv * b,
+            "total": (res + 2 * sw + 4 * nv) * b}
 
 
 def measured_peaks() -> dict:
@@ -172,6 +179,8 @@ def run_native(args, rank: int, world: int, device: int):
         out[prec_name] = res
     if args.converge_drop > 0 and args.precision == "both":
         out["converge"] = run_converge(args, ctx, setup, specs, world)
+    if args.sst_steps > 0:
+        out["sst"] = run_sst(args, ctx, world)
     if args.served_n > 0:
         out["served"] = {"definition": "latency = submit to retirement (host clock), "
                                        "retirement at the residual drop; solves/s = "
@@ -189,13 +198,14 @@ def run_served(args, ctx, precision, rate, seed):
     """The served configuration: a Poisson stream of `args.served_n` solve
     requests at `rate` per second (cells log-normal, clipped; bump and
     wedge channels; Mach 0.3-2.5; angle of attack -4..4 degrees; half laminar
-    Navier-Stokes, half Euler), admitted by the server as slots and device
+    Navier-Stokes, half SST-2003 RANS by default), admitted by the server as slots and device
     memory free up, retired on the device at the residual drop.  Returns
     time-to-convergence percentiles (submit to retirement) and solves/s."""
     import numpy as np
 
     from aither_gb300 import Server, cases
-    specs = cases.served_specs(args.served_n, seed=seed, max_cells=args.served_max_cells)
+    specs = cases.served_specs(args.served_n, seed=seed, max_cells=args.served_max_cells,
+                               mix=args.served_mix)
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(specs)))
     with tempfile.TemporaryDirectory() as tmp:
@@ -226,7 +236,12 @@ def run_served(args, ctx, precision, rate, seed):
     st = list(done.values())
     conv = [x for x in st if x.converged == 1]
     lat = [x.latency_ms for x in conv]
+    kinds = {"sst": [x.latency_ms for x, sp in zip(sorted(st, key=lambda x: x.id), specs)
+                     if x.converged == 1 and sp.get("rans")],
+             "laminar": [x.latency_ms for x, sp in zip(sorted(st, key=lambda x: x.id), specs)
+                         if x.converged == 1 and not sp.get("rans")]}
     return {"rate_per_s": rate, "requests": len(specs), "converged": len(conv),
+            "p50_ms_by_kind": {k: _pct(v, 50) for k, v in kinds.items()},
             "nonphysical": sum(1 for x in st if x.converged == -1),
             "iteration_cap": sum(1 for x in st if x.converged == 0),
             "makespan_s": makespan, "solves_per_s": len(conv) / makespan,
@@ -234,6 +249,71 @@ def run_served(args, ctx, precision, rate, seed):
             "queue_p50_ms": _pct([x.queue_ms for x in st], 50),
             "max_concurrent": max_active,
             "cells": int(sum(sp["ni"] * sp["nj"] * sp["nk"] for sp in specs))}
+
+
+def run_sst(args, ctx, world):
+    """Turbulent flat plate (SST-2003 k-omega RANS, seven equations): one
+    256x192x4 block, Re_L 5e6, Mach 0.2, first cell at y+ = 1, WENO, AUSM,
+    block LU-SGS, CFL 10.  Cell-iterations/s of the FP64 and mixed paths over
+    `args.sst_steps` iterations after warm-up, per-pass kernel times, the
+    HBM roofline of the dominant FP64 pass and, on rank 0, the oracle's time
+    for a bounded sample of the same case."""
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Setup, cases
+    with tempfile.TemporaryDirectory() as tmp:
+        inp, _ = cases.sst_plate(tmp, ni=args.sst_ni, nj=args.sst_nj, nk=args.sst_nk, cfl=10.0)
+        setup = Setup(inp)
+    _, _, ncells = setup.counts()
+    out = {"workload": f"SST-2003 turbulent flat plate {args.sst_ni}x{args.sst_nj}x"
+                       f"{args.sst_nk} cells, Re 5e6, Mach 0.2, y+ 1, WENO, AUSM, block "
+                       "LU-SGS, CFL 10", "cells": ncells, "steps": args.sst_steps}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        b = Batch(ctx, setup, prec)
+        for _ in range(max(args.warmup, 3)):
+            b.iterate(1)
+        tuned = b.autotune(2)
+        _barrier(world)
+        clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+        clocks.start()
+        norms = b.iterate(args.sst_steps)
+        st = b.stats()
+        clk = clocks.stop()
+        ms = _max_over_ranks(st.device_ms, world)
+        prof = b.profile(2)
+        out[name] = {"value": ncells * args.sst_steps * world / (ms * 1e-3),
+                     "unit": METRIC, "ms_per_step": ms / args.sst_steps,
+                     "gpu_launches": int(st.kernel_launches), "sweep_threads": tuned,
+                     "status_ok": all(n.status == 0 for n in norms), "clocks": clk,
+                     "kernel_ms": dict(zip(["ghost", "face_i", "face_j", "face_k",
+                                            "viscous+cell", "sweep_fwd", "sweep_bwd",
+                                            "update"], prof.tolist()))}
+        b.close()
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    km = out["fp64"]["kernel_ms"]
+    ab = algorithmic_bytes(nv=7, d=29, b=8, viscous=True, block=True, rans=True)
+    pass_ms = {"residual": km["face_i"] + km["face_j"] + km["face_k"] + km["viscous+cell"],
+               "forward": km["sweep_fwd"], "backward": km["sweep_bwd"], "update": km["update"]}
+    dom = max(pass_ms, key=pass_ms.get)
+    peaks = measured_peaks()
+    achieved = ab[dom] * ncells / (pass_ms[dom] * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                       "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                       "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                       "bytes_per_cell": ab}
+    if not args.no_cpu_baseline and int(os.environ.get("RANK", "0")) == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        threads = os.cpu_count() or 1
+        orc = Oracle(setup, threads)
+        orc.iterate(1)
+        t0 = time.perf_counter()
+        orc.iterate(1)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": ncells / dt, "unit": METRIC, "cores": 1, "kind": "port",
+                               "sample": "1 iteration of the full case after 1 warm-up "
+                                         "iteration; oracle (C restatement of the "
+                                         "reference), one block so one thread"}
+        orc.close()
+    return out
 
 
 def _pct(x, q):
@@ -409,6 +489,13 @@ def main():
                     help="upper clip of the request sizes (the configuration's is 4M)")
     ap.add_argument("--served-drop", type=float, default=1e-6)
     ap.add_argument("--served-slots", type=int, default=16)
+    ap.add_argument("--served-mix", default="ns_sst", choices=["ns_sst", "euler_ns"],
+                    help="half laminar / half SST-2003 requests, or half Euler / half laminar")
+    ap.add_argument("--sst-steps", type=int, default=20,
+                    help="iterations of the SST flat plate section (0 skips it)")
+    ap.add_argument("--sst-ni", type=int, default=256)
+    ap.add_argument("--sst-nj", type=int, default=192)
+    ap.add_argument("--sst-nk", type=int, default=4)
     ap.add_argument("--served-max-iters", type=int, default=6000)
     ap.add_argument("--converge-fp64-cases", type=int, default=8,
                     help="smallest cases also run to convergence in FP64 for the comparison")
@@ -493,6 +580,8 @@ def main():
         line["converge"] = res["converge"]
     if "served" in res:
         line["served"] = res["served"]
+    if "sst" in res:
+        line["sst"] = res["sst"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
     print(json.dumps(line))

@@ -118,3 +118,28 @@ def test_autotune_leaves_the_solution_unchanged(ctx, precision, tmp_path):
         assert np.array_equal(tuned.field(s, "STATE"), ref.field(s, "STATE"))
     ref.close()
     tuned.close()
+
+
+def test_sst_mixed_precision_converged_state_against_fp64(ctx, tmp_path):
+    """SST-2003 RANS bump channel (seven equations) to a 1e-6 drop of the
+    total L2 over all seven: the mixed path retires within 1 % of the FP64
+    iteration count, and its converged flow variables and each turbulence
+    variable agree with FP64 to 1e-6 relative (each to its own scale)."""
+    from aither_gb300 import Batch, Setup, cases
+    inp, _ = cases.wall_channel(str(tmp_path / "sst"), 32, 16, 4, "bump", 0.08, 0.6,
+                                alpha=2.0, rans=True, stretch=1.1, name="sst")
+    out = {}
+    for prec in (0, 1):
+        b = Batch(ctx, Setup(inp), prec)
+        info = b.converge(20000, 1e-6, check_every=100)
+        assert info[0].converged == 1
+        out[prec] = (b.field(0, "STATE"), info[0].iterations)
+        b.close()
+    a, ref = out[1][0], out[0][0]
+    assert ref.shape[-1] == 7
+    errs = [rel_err(a[..., :5], ref[..., :5])] + [rel_err(a[..., v], ref[..., v])
+                                                  for v in (5, 6)]
+    print(f"SST mixed vs FP64: rel err flow {errs[0]:.2e} k {errs[1]:.2e} "
+          f"omega {errs[2]:.2e}; iterations {out[1][1]} vs {out[0][1]}")
+    assert max(errs) <= 1e-6
+    assert abs(out[1][1] - out[0][1]) <= max(2, 0.01 * out[0][1])

@@ -32,6 +32,9 @@ def _requests(tmp):
     pinp, _ = cases.flat_plate(str(tmp / "plate"), ni=10, nj=8, nk=2, dy0=1e-3, ratio=1.3,
                                name="plate")
     out.append(pinp)
+    sinp, _ = cases.wall_channel(str(tmp / "sst"), 24, 12, 3, "bump", 0.08, 0.6, alpha=2.0,
+                                 rans=True, stretch=1.1, name="sst")
+    out.append(sinp)
     return out
 
 
