@@ -18,7 +18,8 @@ BC = dict(SLIP_WALL=0, VISCOUS_WALL=1, CHARACTERISTIC=2, STAGNATION_INLET=3,
           PRESSURE_OUTLET=4, SUPERSONIC_INFLOW=5, SUPERSONIC_OUTFLOW=6,
           PERIODIC=7, INTERBLOCK=8)
 PREC_FP64, PREC_MIXED = 0, 1
-FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6)
+FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
+             WALLDIST=9)
 
 
 class GhostOp(C.Structure):
@@ -103,6 +104,12 @@ class BlockDev(C.Structure):
                 ("dt", C.c_void_p), ("ainv", C.c_void_p)]
 
 
+class BlockFields(C.Structure):
+    """ath_block_fields: host fields of one block for the output writers."""
+    _fields_ = [("prim", C.c_void_p), ("dt", C.c_void_p), ("resid", C.c_void_p),
+                ("aux", C.c_void_p), ("velgrad", C.c_void_p), ("wall_dist", C.c_void_p)]
+
+
 class Stats(C.Structure):
     _fields_ = [("kernel_launches", C.c_int64), ("device_ms", C.c_double)]
 
@@ -143,6 +150,22 @@ def lib() -> C.CDLL:
             "ath_batch_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_field_width": (C.c_int, [vp, C.c_int, C.c_int]),
             "ath_batch_pool_vars": (C.c_int, [vp, C.POINTER(C.c_int)]),
+            "ath_output_function": (C.c_int, [vp, C.c_int, C.c_char_p, C.POINTER(BlockFields),
+                                              C.c_char_p]),
+            "ath_output_restart": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                             C.POINTER(BlockFields), C.c_char_p]),
+            "ath_input_restart": (C.c_int, [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double),
+                                            C.POINTER(C.POINTER(C.c_double))]),
+            "ath_output_center_grid": (C.c_int, [vp, C.c_int, C.c_char_p]),
+            "ath_output_meta": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, C.c_char_p]),
+            "ath_output_resid": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(Norms), C.POINTER(C.c_double)]),
+            "ath_batch_write_function": (C.c_int, [vp, vp, C.c_int, C.c_char_p, C.c_char_p]),
+            "ath_batch_write_restart": (C.c_int, [vp, vp, C.c_int, C.c_int,
+                                                  C.POINTER(C.c_double), C.c_char_p]),
+            "ath_batch_read_restart": (C.c_int, [vp, vp, C.c_int, C.c_char_p,
+                                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]),
             "ath_batch_stats": (C.c_int, [vp, C.POINTER(Stats)]),
             "ath_batch_pool_cells": (C.c_int, [vp, C.POINTER(C.c_int64)]),
             "ath_batch_copy_state": (C.c_int, [vp, C.POINTER(C.c_double), C.c_int]),
@@ -226,6 +249,69 @@ class Setup:
         ns, nb, nc = C.c_int(), C.c_int(), C.c_int64()
         check(lib().ath_setup_counts(self.h, C.byref(ns), C.byref(nb), C.byref(nc)))
         return ns.value, nb.value, nc.value
+
+    # ---- output files in the reference's formats
+    def solve_blocks(self, solve: int) -> list:
+        return [b for b in range(self.counts()[1]) if self.block_view(b).solve == solve]
+
+    def solve_nv(self, solve: int) -> int:
+        return self.block_view(self.solve_blocks(solve)[0]).nv
+
+    @staticmethod
+    def _fields(blocks: list) -> "C.Array":
+        keep = []
+        arr = (BlockFields * len(blocks))()
+        for k, fl in enumerate(blocks):
+            for name in ("prim", "dt", "resid", "aux", "velgrad", "wall_dist"):
+                a = fl.get(name)
+                if a is not None:
+                    a = np.ascontiguousarray(a, dtype=np.float64)
+                    keep.append(a)
+                    setattr(arr[k], name, a.ctypes.data)
+        arr._keep = keep
+        return arr
+
+    def write_function(self, solve: int, fields: list, path: str, variables=None) -> None:
+        """Plot3D cell-centre function file from host fields (one dict per
+        block of the solve: prim, dt, resid, aux, velgrad, wall_dist)."""
+        arr = self._fields(fields)
+        v = ",".join(variables).encode() if variables else None
+        check(lib().ath_output_function(self.h, solve, v, arr, path.encode()))
+
+    def write_restart(self, solve: int, iteration: int, resid_first, prims: list,
+                      path: str) -> None:
+        arr = self._fields([{"prim": p} for p in prims])
+        rf = np.ascontiguousarray(resid_first, dtype=np.float64)
+        check(lib().ath_output_restart(self.h, solve, iteration, dptr(rf), arr, path.encode()))
+
+    def read_restart(self, solve: int, path: str):
+        """(iteration, L2 normalisation, [primitive state per block])."""
+        blocks = self.solve_blocks(solve)
+        nv = self.solve_nv(solve)
+        outs = []
+        for b in blocks:
+            v = self.block_view(b)
+            outs.append(np.empty((v.nk, v.nj, v.ni, nv)))
+        ptrs = (C.POINTER(C.c_double) * len(outs))(*[dptr(o) for o in outs])
+        it = C.c_int()
+        rf = np.empty(nv)
+        check(lib().ath_input_restart(self.h, solve, path.encode(), C.byref(it), dptr(rf), ptrs))
+        return it.value, rf, outs
+
+    def write_center_grid(self, solve: int, path: str) -> None:
+        check(lib().ath_output_center_grid(self.h, solve, path.encode()))
+
+    def write_meta(self, solve: int, iteration: int, path: str, variables=None) -> None:
+        v = ",".join(variables).encode() if variables else None
+        check(lib().ath_output_meta(self.h, solve, v, iteration, path.encode()))
+
+    def write_resid(self, solve: int, path: str, norms: list, first_step: int,
+                    resid_first: np.ndarray, append: bool = False) -> None:
+        """Residual history rows of one solve; resid_first (nv values) is
+        the running normalisation, updated in place."""
+        arr = (Norms * len(norms))(*norms)
+        check(lib().ath_output_resid(self.h, solve, path.encode(), 1 if append else 0,
+                                     first_step, len(norms), arr, dptr(resid_first)))
 
     def block_view(self, b: int) -> BlockView:
         v = BlockView()
@@ -341,6 +427,25 @@ class Batch:
         n = C.c_int64()
         check(lib().ath_batch_pool_cells(self.h, C.byref(n)))
         return n.value
+
+    def write_function(self, solve: int, path: str, variables=None) -> None:
+        """Plot3D cell-centre function file of a solve's resident solution."""
+        v = ",".join(variables).encode() if variables else None
+        check(lib().ath_batch_write_function(self.h, self.setup.h, solve, v, path.encode()))
+
+    def write_restart(self, solve: int, iteration: int, resid_first, path: str) -> None:
+        rf = np.ascontiguousarray(resid_first, dtype=np.float64)
+        check(lib().ath_batch_write_restart(self.h, self.setup.h, solve, iteration, dptr(rf),
+                                            path.encode()))
+
+    def read_restart(self, solve: int, path: str):
+        """Loads a restart file into the solve's resident state; returns
+        (iteration, L2 normalisation)."""
+        it = C.c_int()
+        rf = np.empty(7)
+        check(lib().ath_batch_read_restart(self.h, self.setup.h, solve, path.encode(),
+                                           C.byref(it), dptr(rf)))
+        return it.value, rf[:self.setup.solve_nv(solve)]
 
     def pool_vars(self) -> int:
         """Values per cell of the copy_state snapshot (5, or 7 with SST)."""

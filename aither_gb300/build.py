@@ -40,7 +40,7 @@ CU_UNITS = {
     "batch.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
 }
-CPP_UNITS = ["setup.cpp", "capi_setup.cpp"]
+CPP_UNITS = ["setup.cpp", "capi_setup.cpp", "output.cpp"]
 
 
 def _run(cmd: list[str]) -> None:

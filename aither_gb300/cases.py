@@ -455,3 +455,27 @@ def sst_plate(outdir: str, ni: int = 256, nj: int = 192, nk: int = 4, name: str 
                 dy_max=0.05)
     args.update(kw)
     return flat_plate(outdir, **args)
+
+
+def set_output_keys(inp: str, iterations: int, variables: list | None = None,
+                    output_freq: int | None = None, restart_freq: int = 0) -> None:
+    """Rewrites the output controls of an input file written by this module:
+    iterations, outputFrequency, restartFrequency and outputVariables."""
+    with open(inp) as f:
+        lines = f.read().split("\n")
+    out = []
+    for ln in lines:
+        key = ln.split(":", 1)[0].strip()
+        if key in ("iterations", "outputFrequency", "restartFrequency", "outputVariables"):
+            continue
+        out.append(ln)
+    at = next(i for i, ln in enumerate(out) if ln.startswith("gridName:")) + 1
+    extra = [f"iterations: {iterations}",
+             f"outputFrequency: {output_freq if output_freq else iterations}"]
+    if restart_freq:
+        extra.append(f"restartFrequency: {restart_freq}")
+    if variables:
+        extra.append("outputVariables: <" + ", ".join(variables) + ">")
+    out[at:at] = extra
+    with open(inp, "w") as f:
+        f.write("\n".join(out))

@@ -20,9 +20,6 @@
 #include "kernels.cuh"
 #include "setup.hpp"
 
-struct ath_setup {
-  ath::Setup s;
-};
 
 struct ath_ctx {
   int device = 0;
@@ -292,6 +289,8 @@ class RunnerBase {
   virtual void Iterate(int n) = 0;
   virtual void GetDU(int b, double *out) = 0;
   virtual void GetAinv(int b, double *out) = 0;
+  virtual void GetAux(int b, double *out) = 0;
+  virtual void GetVelGrad(int b, double *out) = 0;
   virtual void Profile(int reps, double ms[8]) = 0;
   // drop the captured iteration graph (launch shapes changed)
   virtual void ResetGraph() = 0;
@@ -318,6 +317,8 @@ class Runner : public RunnerBase {
       }
       P_.mu = m.Alloc<double>(n);
       Check(cudaMemset(P_.mu, 0, n * sizeof(double)), "memset");
+      P_.Taux = m.Alloc<double>(n);
+      Check(cudaMemset(P_.Taux, 0, n * sizeof(double)), "memset");
     }
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
@@ -348,16 +349,17 @@ class Runner : public RunnerBase {
           Check(cudaMemset(P_.vst[d], 0, 15 * n * sizeof(T)), "memset");
         }
       }
-      if (c.block_viscous) {
-        P_.vgq = m.Alloc<T>(9 * nq);
-        Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
-      }
       P_.Joff = m.Alloc<T>(150 * nq);
       Check(cudaMemset(P_.Joff, 0, 150 * nq * sizeof(T)), "memset");
       if (c.any_rans) {
         P_.Jtoff = m.Alloc<T>(24 * nq);
         Check(cudaMemset(P_.Jtoff, 0, 24 * nq * sizeof(T)), "memset");
       }
+    }
+    if (c.block_viscous || c.any_rans) {
+      // cell-averaged velocity gradients (block diagonal, SST sources, output)
+      P_.vgq = m.Alloc<T>(9 * nq);
+      Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
     }
     Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
     Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
@@ -470,6 +472,7 @@ class Runner : public RunnerBase {
     P_.Atq = zero(m.Alloc<T>(aw * nq), aw * nq);
     P_.mutq = zero(m.Alloc<T>(nq), nq);
     P_.f1q = zero(m.Alloc<T>(nq), nq);
+    P_.f2q = zero(m.Alloc<T>(nq), nq);
   }
 
   // gridLevel::AuxillaryAndWidths (src/gridLevel.cpp:433): laminar
@@ -724,6 +727,36 @@ class Runner : public RunnerBase {
     if (nv > 5) CopyOutQ(P_.dUtq, 2, nv, 5, b, out);
   }
   void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, 1, 0, b, out); }
+  void GetAux(int bi, double *out) override {
+    const Block &b = c_.setup->blocks[bi];
+    const auto &ph = c_.setup->solves[b.solve].phys;
+    const size_t m = (size_t)b.ni * b.nj * b.nk;
+    std::fill(out, out + 5 * m, 0.0);
+    if (ph.eqn != ATH_EQN_EULER) {
+      GatherPool(P_.Taux, bi, 5, 0, out);
+      GatherPool(P_.mu, bi, 5, 1, out);
+    } else {
+      // idealGas::Temperature (src/eos.cpp:100) of the current state
+      std::vector<double> w(5 * m);
+      for (int v = 0; v < 5; ++v) GatherPool(P_.W + v * c_.ncell, bi, 5, v, w.data());
+      for (size_t q = 0; q < m; ++q) out[5 * q] = w[5 * q + 4] / (0.0 + w[5 * q] * ph.gas_r);
+    }
+    if (ph.eqn == ATH_EQN_RANS) {
+      CopyOutQ(P_.mutq, 1, 5, 2, bi, out);
+      CopyOutQ(P_.f1q, 1, 5, 3, bi, out);
+      CopyOutQ(P_.f2q, 1, 5, 4, bi, out);
+    }
+  }
+  void GetVelGrad(int bi, double *out) override {
+    const Block &b = c_.setup->blocks[bi];
+    const auto &ph = c_.setup->solves[b.solve].phys;
+    const bool have = ph.eqn == ATH_EQN_RANS ||
+                      (ph.eqn != ATH_EQN_EULER && ph.solver == ATH_SOLVER_BLUSGS);
+    if (!have || !P_.vgq)
+      throw Error(ATH_ERR_UNSUPPORTED, "cell velocity gradients are kept for block LU-SGS "
+                                       "viscous and SST solves only");
+    CopyOutQ(P_.vgq, 9, 9, 0, bi, out);
+  }
 
  private:
   template <typename U>
@@ -742,6 +775,20 @@ class Runner : public RunnerBase {
           for (int i = 0; i < b.ni; ++i) tmp[(q++) * w + v] = (double)h[b.Cell(i, j, k)];
     }
     std::memcpy(out, tmp.data(), tmp.size() * sizeof(double));
+  }
+
+  // one cell-indexed FP64 pool -> physical cells of block bi, AoS with
+  // `stride` values per cell at `voff`, k slowest
+  void GatherPool(const double *pool, int bi, int stride, int voff, double *out) {
+    const Block &b = c_.setup->blocks[bi];
+    const int64_t nc = b.NCell(), o = c_.cell0[bi];
+    std::vector<double> h(nc);
+    Check(cudaMemcpy(h.data(), pool + o, nc * sizeof(double), cudaMemcpyDeviceToHost),
+          "download");
+    size_t q = 0;
+    for (int k = 0; k < b.nk; ++k)
+      for (int j = 0; j < b.nj; ++j)
+        for (int i = 0; i < b.ni; ++i) out[(q++) * stride + voff] = h[b.Cell(i, j, k)];
   }
 
   // q-ordered array of w values -> physical cells of block bi, AoS with
@@ -1504,6 +1551,12 @@ int ath_batch_field_width(ath_batch *batch, int block, int field) {
       return 1;
     case ATH_FIELD_SPECRAD:
       return 2;
+    case ATH_FIELD_AUX:
+      return 5;
+    case ATH_FIELD_VELGRAD:
+      return 9;
+    case ATH_FIELD_WALLDIST:
+      return 1;
     default:
       return ATH_ERR_ARG;
   }
@@ -1561,6 +1614,15 @@ int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h) {
       }
       case ATH_FIELD_DU: batch->run->GetDU(block, out_h); break;
       case ATH_FIELD_AINV: batch->run->GetAinv(block, out_h); break;
+      case ATH_FIELD_AUX: batch->run->GetAux(block, out_h); break;
+      case ATH_FIELD_VELGRAD: batch->run->GetVelGrad(block, out_h); break;
+      case ATH_FIELD_WALLDIST: {
+        size_t q = 0;
+        for (int k = 0; k < b.nk; ++k)
+          for (int j = 0; j < b.nj; ++j)
+            for (int i = 0; i < b.ni; ++i) out_h[q++] = b.wall_dist[b.Cell(i, j, k)];
+        break;
+      }
       default: throw ath::Error(ATH_ERR_ARG, "unknown field");
     }
   });

@@ -7,9 +7,6 @@
 #include "errors.hpp"
 #include "setup.hpp"
 
-struct ath_setup {
-  ath::Setup s;
-};
 
 namespace ath {
 namespace {

@@ -125,6 +125,8 @@ struct Pools {
   T *dUtg;          // [2][nghost]
   T *Ainvtq, *Atq;  // [nq] scalar or [4][nq] 2x2 turbulence diagonal (inverse)
   T *mutq, *f1q;    // [nq] cell eddy viscosity and F1
+  T *f2q;           // [nq] cell F2 (output only)
+  double *Taux;     // [ncell] temperature of the last auxiliary update (viscous)
   // block solves: off-diagonal Jacobians of each cell's six neighbours,
   // [(side*3 + d)*25 + e][nq] (side 0 = lower) and the turbulence blocks
   // [(side*3 + d)*4 + e][nq]

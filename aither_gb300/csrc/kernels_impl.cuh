@@ -633,7 +633,6 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
         f1c += sixth * (double)rs[16 * n + f];
         f2c += sixth * (double)rs[17 * n + f];
       }
-    (void)f2c;
     const Prim<double> wd = LoadW<double>(P.W, n, c);
     const double kw[2] = {P.Wt[c], P.Wt[n + c]};
     double src[2];
@@ -652,11 +651,11 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     const int64_t nq = P.nq;
     P.mutq[q] = (T)mutc;
     P.f1q[q] = (T)f1c;
+    P.f2q[q] = (T)f2c;
     P.Rtq[q] = (T)rt[0];
     P.Rtq[nq + q] = (T)rt[1];
-    if (BLOCK)
 #pragma unroll
-      for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = (T)vg[e];
+    for (int e = 0; e < 9; ++e) P.vgq[e * nq + q] = (T)vg[e];
   }
   P.lam[c] = lam;
   if (rans) P.lamt[c] = lamt;
@@ -1345,7 +1344,9 @@ __global__ void k_aux(Pools<T> P, const int32_t *cells, const int32_t *cell_bloc
   if (!sv.active) return;
   const Gas<double> g = GasOf<double>(sv);
   const Prim<double> w = LoadW<double>(P.W, P.ncell, c);
-  P.mu[c] = SutherlandRatio(Temperature(w, g), sv.t_ref, sv.mu_c1, sv.mu_s, sv.mu_ref);
+  const double temp = Temperature(w, g);
+  P.mu[c] = SutherlandRatio(temp, sv.t_ref, sv.mu_c1, sv.mu_s, sv.mu_ref);
+  if (P.Taux) P.Taux[c] = temp;
 }
 
 // viscous flux on faces of direction D (procBlock::CalcViscFluxI/J/K,

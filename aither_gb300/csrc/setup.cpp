@@ -24,6 +24,7 @@
 #include <cstring>
 #include <fstream>
 #include <limits>
+#include <set>
 #include <sstream>
 #include <stdexcept>
 
@@ -963,6 +964,64 @@ void FarfieldTurbulence(double *w, double tint, double ratio, const ath_solve_vi
 // minimum of |c - f|^2, then its square root); non-edge ghost cells take
 // minus the mirrored interior value across a viscous wall, the value of the
 // boundary cell elsewhere; edge ghosts keep the default 1e10.
+// Nearest wall-face centre: a k-d tree over the centres (split on the axis
+// of largest extent at the median), searched with the same squared distance
+// dx*dx + dy*dy + dz*dz as an exhaustive scan, so the minimum is the same
+// value (kdtree::NearestNeighbor, src/kdtree.cpp, is also an exact search).
+class WallTree {
+ public:
+  explicit WallTree(std::vector<double> pts) : p_(std::move(pts)) {
+    const size_t n = p_.size() / 3;
+    idx_.resize(n);
+    for (size_t q = 0; q < n; ++q) idx_[q] = (int32_t)q;
+    axis_.assign(n, 0);
+    Build(0, n);
+  }
+  double MinDist2(double x, double y, double z) const {
+    double best = std::numeric_limits<double>::max();
+    Search(0, idx_.size(), x, y, z, best);
+    return best;
+  }
+
+ private:
+  void Build(size_t lo, size_t hi) {
+    if (hi - lo <= 1) return;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (size_t q = lo; q < hi; ++q)
+      for (int e = 0; e < 3; ++e) {
+        mn[e] = std::min(mn[e], p_[3 * idx_[q] + e]);
+        mx[e] = std::max(mx[e], p_[3 * idx_[q] + e]);
+      }
+    int ax = 0;
+    for (int e = 1; e < 3; ++e)
+      if (mx[e] - mn[e] > mx[ax] - mn[ax]) ax = e;
+    const size_t mid = (lo + hi) / 2;
+    std::nth_element(idx_.begin() + lo, idx_.begin() + mid, idx_.begin() + hi,
+                     [&](int32_t a, int32_t b) { return p_[3 * a + ax] < p_[3 * b + ax]; });
+    axis_[mid] = (int8_t)ax;
+    Build(lo, mid);
+    Build(mid + 1, hi);
+  }
+  void Search(size_t lo, size_t hi, double x, double y, double z, double &best) const {
+    if (lo >= hi) return;
+    const size_t mid = (lo + hi) / 2;
+    const double *c = &p_[3 * idx_[mid]];
+    const double dx = x - c[0], dy = y - c[1], dz = z - c[2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < best) best = d2;
+    if (hi - lo == 1) return;
+    const int ax = axis_[mid];
+    const double diff = (ax == 0 ? x : ax == 1 ? y : z) - c[ax];
+    const bool left_first = diff < 0.0;
+    Search(left_first ? lo : mid + 1, left_first ? mid : hi, x, y, z, best);
+    // the other side can only hold a closer centre within |diff| of the plane
+    if (diff * diff <= best) Search(left_first ? mid + 1 : lo, left_first ? hi : mid, x, y, z, best);
+  }
+  std::vector<double> p_;
+  std::vector<int32_t> idx_;
+  std::vector<int8_t> axis_;
+};
+
 void BuildWallDistance(Setup &setup, int solve) {
   std::vector<double> wf;  // x, y, z of every viscous-wall face centre
   for (int bi : setup.solves[solve].blocks) {
@@ -985,7 +1044,7 @@ void BuildWallDistance(Setup &setup, int solve) {
     }
   }
   if (wf.empty()) return;
-  const size_t nw = wf.size() / 3;
+  const WallTree tree(wf);
   for (int bi : setup.solves[solve].blocks) {
     Block &b = setup.blocks[bi];
     const int64_t nc = b.NCell();
@@ -994,13 +1053,7 @@ void BuildWallDistance(Setup &setup, int solve) {
         for (int i = 0; i < b.ni; ++i) {
           const int64_t c = b.Cell(i, j, k);
           const double cx = b.center[c], cy = b.center[nc + c], cz = b.center[2 * nc + c];
-          double best = std::numeric_limits<double>::max();
-          for (size_t q = 0; q < nw; ++q) {
-            const double dx = cx - wf[3 * q], dy = cy - wf[3 * q + 1], dz = cz - wf[3 * q + 2];
-            const double d2 = dx * dx + dy * dy + dz * dz;
-            if (d2 < best) best = d2;
-          }
-          b.wall_dist[c] = std::sqrt(best);
+          b.wall_dist[c] = std::sqrt(tree.MinDist2(cx, cy, cz));
         }
     // boundary condition of the block face crossed by a non-edge ghost
     auto bc_at = [&](int d, bool lower, const int p[3]) {
@@ -1099,6 +1152,44 @@ void AppendInput(Setup &st, const std::string &path) {
 
   Solve sv;
   sv.name = path;
+  {
+    // input::SimNameRoot (src/input.cpp:872) and the output keys
+    // (src/input.cpp:321-327,463-467); the default output set is the
+    // reference's
+    const auto slash = path.find_last_of('/');
+    const auto file = slash == std::string::npos ? path : path.substr(slash + 1);
+    sv.sim_root = file.substr(0, file.find('.'));
+    sv.grid_name = get("gridName", "");
+    sv.output_freq = (int)getd("outputFrequency", 1);
+    sv.restart_freq = (int)getd("restartFrequency", 0);
+    sv.iterations = (int)getd("iterations", 1);
+    std::set<std::string> vars = {"density", "vel_x", "vel_y", "vel_z", "pressure"};
+    const auto ov = get("outputVariables", "");
+    if (!ov.empty()) {
+      vars.clear();
+      std::string body = ov;
+      const auto a = body.find('<'), z = body.rfind('>');
+      if (a != std::string::npos && z != std::string::npos && z > a)
+        body = body.substr(a + 1, z - a - 1);
+      std::stringstream ss(body);
+      std::string tok;
+      while (std::getline(ss, tok, ',')) {
+        tok = Trim(tok);
+        if (!tok.empty()) vars.insert(tok);
+      }
+    }
+    sv.output_vars.assign(vars.begin(), vars.end());
+    // fluids: <fluid(name=air; ...)> -- one species, whose properties are
+    // read from <name>.dat
+    const auto fl = get("fluids", "");
+    const auto np = fl.find("name=");
+    if (np != std::string::npos) {
+      auto e = fl.find_first_of(";) ", np + 5);
+      sv.species = Trim(fl.substr(np + 5, e == std::string::npos ? std::string::npos : e - np - 5));
+      if (fl.find("fluid(", fl.find("fluid(") + 1) != std::string::npos)
+        Fail("only one fluid species is supported");
+    }
+  }
   auto &ph = sv.phys;
   // scheme
   const auto eqn = get("equationSet", "euler");
@@ -1161,9 +1252,10 @@ void AppendInput(Setup &st, const std::string &path) {
   Fluid fl;
   {
     const auto dir = DirName(path);
-    if (!ReadFluidFile(dir + "/air.dat", fl)) {
+    const std::string file = sv.species + ".dat";
+    if (!ReadFluidFile(dir + "/" + file, fl)) {
       const char *inst = std::getenv("AITHER_INSTALL_DIRECTORY");
-      if (inst) ReadFluidFile(std::string(inst) + "/fluidDatabase/air.dat", fl);
+      if (inst) ReadFluidFile(std::string(inst) + "/fluidDatabase/" + file, fl);
     }
   }
   const double tref = getd("referenceTemperature", -1.0);
@@ -1344,7 +1436,10 @@ void AppendInput(Setup &st, const std::string &path) {
   st.solves.push_back(std::move(sv));
   BuildGhostOps(st, solve);
   BuildEdgeOps(st, solve);
-  if (st.solves[solve].phys.eqn == ATH_EQN_RANS) BuildWallDistance(st, solve);
+  // procBlock::CalcWallDistance (src/procBlock.cpp:6030) runs for every case
+  // with viscous walls (src/main.cpp:200); without walls the distance keeps
+  // its default of 1e10
+  if (st.solves[solve].phys.eqn != ATH_EQN_EULER) BuildWallDistance(st, solve);
   // connection ghost geometry changes the donor-side widths only through
   // the ops; recompute nothing else
 }

@@ -66,6 +66,14 @@ struct Block {
 
 struct Solve {
   std::string name;
+  // output controls of the input file: outputVariables (a sorted set, as
+  // the reference keeps it), outputFrequency, restartFrequency, iterations;
+  // the simulation name root (input file name up to its first '.') and the
+  // grid name
+  std::vector<std::string> output_vars;
+  int output_freq = 1, restart_freq = 0, iterations = 1;
+  std::string sim_root, grid_name;
+  std::string species = "air";  // the one fluid of the case (fluids key)
   ath_solve_view phys{};  // states pointer refreshed on access
   std::vector<ath_bc_state> states;
   std::vector<BCStateIn> states_in;
@@ -92,3 +100,8 @@ void BuildEdgeOps(Setup &setup, int solve);
 std::vector<Block> ReadPlot3d(const std::string &path, double lref);
 
 }  // namespace ath
+
+// The C handle of a host setup.
+struct ath_setup {
+  ath::Setup s;
+};

@@ -324,7 +324,22 @@ enum {
   ATH_FIELD_DT = 3,           /* local time step, 1 */
   ATH_FIELD_SPECRAD = 4,      /* cell spectral radius (flow, turb), 2 */
   ATH_FIELD_DU = 5,           /* implicit update, nv */
-  ATH_FIELD_AINV = 6          /* inverse main diagonal, 1 (scalar) */
+  ATH_FIELD_AINV = 6,         /* inverse main diagonal, 1 (scalar) */
+  /* auxiliary cell values as the reference holds them at output time
+   * (procBlock temperature_, viscosity_, eddyViscosity_, f1_, f2_): 5 =
+   * temperature and laminar viscosity of the last auxiliary update (the
+   * residual of the last iteration, UpdateAuxillaryVariables
+   * src/procBlock.cpp:6171; Euler solves: temperature of the current
+   * state, viscosity 0), then eddy viscosity, F1, F2 of the last SST
+   * residual (0 without turbulence), nondimensional */
+  ATH_FIELD_AUX = 7,
+  /* cell-averaged velocity gradient of the last residual (velocityGrad_),
+   * 9 = d(u,v,w)/dx, d(u,v,w)/dy, d(u,v,w)/dz; block LU-SGS viscous and SST
+   * solves only (others: ATH_ERR_UNSUPPORTED) */
+  ATH_FIELD_VELGRAD = 8,
+  /* wall distance (procBlock::CalcWallDistance src/procBlock.cpp:6030), 1;
+   * 1e10 without viscous walls */
+  ATH_FIELD_WALLDIST = 9
 };
 int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h);
 int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h);
@@ -338,6 +353,62 @@ typedef struct {
   double device_ms;          /* CUDA-event time on the batch stream */
 } ath_stats;
 int ath_batch_stats(ath_batch *batch, ath_stats *out);
+
+/* ---- output files (reference formats) ------------------------------------
+ * Host fields of one block for the writers, physical cells with i fastest
+ * and k slowest (AoS), nondimensional; NULL where not available (a variable
+ * that needs a missing field is an ATH_ERR_ARG). */
+typedef struct {
+  const double *prim;      /* nv per cell: rho, u, v, w, p [, k, omega] */
+  const double *dt;        /* 1 per cell: local time step */
+  const double *resid;     /* nv per cell: residual */
+  const double *aux;       /* 5 per cell: as ATH_FIELD_AUX */
+  const double *velgrad;   /* 9 per cell: as ATH_FIELD_VELGRAD */
+  const double *wall_dist; /* 1 per cell */
+} ath_block_fields;
+
+/* Plot3D cell-centre function file (WriteFunFile, src/output.cpp:209) of
+ * one solve: `variables` is a comma-separated list of the reference's
+ * output variable names (NULL or "" = the input file's outputVariables),
+ * written in sorted order as the reference's set keeps them; `fields` has
+ * one entry per block of the solve.  Supported: density, vel_x/y/z,
+ * pressure, mach, sos, dt, temperature, energy, enthalpy, cp, cv, rank,
+ * globalPosition, viscosityRatio, turbulentViscosity, viscosity, tke, sdr,
+ * f1, f2, wallDistance, velGrad_*, resid_*, mf_<species>, vf_<species>;
+ * the temperature, density, pressure, k and omega gradients are not kept
+ * and are ATH_ERR_UNSUPPORTED. */
+int ath_output_function(const ath_setup *setup, int solve, const char *variables,
+                        const ath_block_fields *fields, const char *path);
+/* Restart file (WriteRestart, src/output.cpp:591): iteration, the L2
+ * normalisation per equation (nv), dimensional primitives per cell. */
+int ath_output_restart(const ath_setup *setup, int solve, int iteration,
+                       const double *resid_first, const ath_block_fields *fields,
+                       const char *path);
+/* Reads a restart file (ReadRestart, src/output.cpp:756) into prim_out[k]
+ * (one nv-per-cell array per block of the solve, may be NULL), checking it
+ * against the solve's equations, species and block sizes. */
+int ath_input_restart(const ath_setup *setup, int solve, const char *path, int *iteration,
+                      double *resid_first, double *const *prim_out);
+/* Cell-centre grid (WriteCellCenter, src/output.cpp:57) and Paraview meta
+ * file (WriteMeta, :903) naming <grid>_center.xyz and
+ * <sim>_<iteration>_center.fun. */
+int ath_output_center_grid(const ath_setup *setup, int solve, const char *path);
+int ath_output_meta(const ath_setup *setup, int solve, const char *variables, int iteration,
+                    const char *path);
+/* Residual history (PrintHeaders / PrintResiduals, src/output.cpp:1007,
+ * 1028): n rows for steps first_step.. from the solve's norms; a header
+ * first unless append.  resid_first (nv) carries the normalisation: it is
+ * set at step 0 and raised to each equation's largest L2 through step 4. */
+int ath_output_resid(const ath_setup *setup, int solve, const char *path, int append,
+                     int first_step, int n, const ath_norms *norms, double *resid_first);
+/* The same from a batch's resident solution (fields gathered from the
+ * device; the setup is the one the batch was created from). */
+int ath_batch_write_function(ath_batch *batch, const ath_setup *setup, int solve,
+                             const char *variables, const char *path);
+int ath_batch_write_restart(ath_batch *batch, const ath_setup *setup, int solve,
+                            int iteration, const double *resid_first, const char *path);
+int ath_batch_read_restart(ath_batch *batch, const ath_setup *setup, int solve,
+                           const char *path, int *iteration, double *resid_first);
 
 /* Whole-batch snapshot of the primitive state in the device layout:
  * [nv][pool cells] FP64 with nv from ath_batch_pool_vars (5, or 7 when the

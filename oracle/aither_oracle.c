@@ -1138,7 +1138,7 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
               b->f1c[cl] += sixth * f1f;
               b->f2c[cl] += sixth * f2f;
             }
-            if (sv->block || rans)
+            if (b->vg)
               for (int e = 0; e < 9; ++e) b->vg[cl * 9 + e] += sixth * grad[e / 3][e % 3];
             if (sv->block) {
               tsl_jac(fs, muf, mutf, g, v, n, mag, c2c, 1, &grad[0][0], Jt);
@@ -1159,7 +1159,7 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
               b->f1c[cu] += sixth * f1f;
               b->f2c[cu] += sixth * f2f;
             }
-            if (sv->block || rans)
+            if (b->vg)
               for (int e = 0; e < 9; ++e) b->vg[cu * 9 + e] += sixth * grad[e / 3][e % 3];
             double nl[3], ml, nh[3], mh;
             face_normal(b, d, face_idx(b, d, i, j, k), nl, &ml);
@@ -1244,15 +1244,16 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
       b->f2c = (double *)dup_arr(NULL, 8 * b->nc);
       b->kgc = (double *)dup_arr(NULL, 8 * 3 * b->nc);
       b->wgc = (double *)dup_arr(NULL, 8 * 3 * b->nc);
-      b->wd = (double *)dup_arr(v->wall_dist, 8 * b->nc);
     }
+    b->wd = v->wall_dist ? (double *)dup_arr(v->wall_dist, 8 * b->nc) : NULL;
     b->R = (double *)dup_arr(NULL, 8 * NV * b->nc);
     b->dU = (double *)dup_arr(NULL, 8 * NV * b->nc);
     b->lam = (double *)dup_arr(NULL, 8 * b->nc);
     b->dt = (double *)dup_arr(NULL, 8 * b->nc);
     b->A = (double *)dup_arr(NULL, 8 * b->nc);
     b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
-    if (c->s[b->solve].block || c->s[b->solve].rans) {
+    if (c->s[b->solve].viscous) {
+      /* cell-averaged velocity gradients (block diagonal, SST sources, output) */
       b->vg = (double *)dup_arr(NULL, 8 * 9 * b->nc);
     }
     if (c->s[b->solve].block) {
@@ -1487,12 +1488,9 @@ void orc_residual(orc_case *c) {
       memset(b->f2c, 0, 8 * b->nc);
       memset(b->kgc, 0, 8 * 3 * b->nc);
       memset(b->wgc, 0, 8 * 3 * b->nc);
-      memset(b->vg, 0, 8 * 9 * b->nc);
     }
-    if (sv->block) {
-      memset(b->Ab, 0, 8 * NJAC * b->nc);
-      memset(b->vg, 0, 8 * 9 * b->nc);
-    }
+    if (sv->block) memset(b->Ab, 0, 8 * NJAC * b->nc);
+    if (b->vg) memset(b->vg, 0, 8 * 9 * b->nc);
     for (int d = 0; d < 3; ++d) {
       const int ei = b->ni + (d == 0), ej = b->nj + (d == 1), ek = b->nk + (d == 2);
       const int nd = d == 0 ? b->ni : (d == 1 ? b->nj : b->nk);
@@ -2119,6 +2117,22 @@ int orc_get_field(orc_case *c, int block, int field, double *out) {
             out[2 * q + 1] = b->lamt ? b->lamt[x] : 0.0;
             break;
           case ATH_FIELD_AINV: out[q] = b->Ainv[x]; break;
+          case ATH_FIELD_AUX: {
+            /* temperature and viscosity of the last auxiliary update (Euler:
+             * temperature of the current state), eddy viscosity, F1, F2 */
+            const osolve *sv = &c->s[b->solve];
+            out[5 * q] = sv->viscous ? b->T[x] : temp_of(&b->W[x * NV], &sv->gas);
+            out[5 * q + 1] = sv->viscous ? b->mu[x] : 0.0;
+            out[5 * q + 2] = b->mutc ? b->mutc[x] : 0.0;
+            out[5 * q + 3] = b->f1c ? b->f1c[x] : 0.0;
+            out[5 * q + 4] = b->f2c ? b->f2c[x] : 0.0;
+            break;
+          }
+          case ATH_FIELD_VELGRAD:
+            if (!b->vg) return ATH_ERR_UNSUPPORTED;
+            memcpy(out + 9 * q, &b->vg[x * 9], 8 * 9);
+            break;
+          case ATH_FIELD_WALLDIST: out[q] = b->wd ? b->wd[x] : 1.0e10; break;
           default: return ATH_ERR_ARG;
         }
         ++q;

@@ -12,8 +12,10 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(_HERE, "liboracle.so")
-FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6)
-WIDTH = dict(STATE=5, STATE_GHOSTS=5, RESID=5, DT=1, SPECRAD=2, DU=5, AINV=1)
+FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
+             WALLDIST=9)
+WIDTH = dict(STATE=5, STATE_GHOSTS=5, RESID=5, DT=1, SPECRAD=2, DU=5, AINV=1, AUX=5, VELGRAD=9,
+             WALLDIST=1)
 
 _lib = None
 

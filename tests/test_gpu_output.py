@@ -1,0 +1,136 @@
+"""Output files written from device-resident solutions (ath_batch_write_*,
+ath_batch_read_restart) against the files the reference's own executable
+wrote on the same cases: restart and function values to the FP64 parity
+tolerance, headers byte for byte, the residual history's columns as
+printed, and a restart file read back into the device state."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from test_output import NAMES, OUT, output_case, ref_bytes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def read_fun(path, variables):
+    """{variable: [per-block arrays]} of a Plot3D cell-centre function file."""
+    b = open(path, "rb").read()
+    nb = int(np.frombuffer(b, np.int32, 1, 0)[0])
+    dims = np.frombuffer(b, np.int32, 4 * nb, 4).reshape(nb, 4)
+    data = np.frombuffer(b, np.float64, offset=4 + 16 * nb)
+    out, o = {v: [] for v in variables}, 0
+    for ni, nj, nk, nvar in dims:
+        n = int(ni * nj * nk)
+        assert nvar == len(variables)
+        for v in variables:
+            out[v].append(data[o:o + n])
+            o += n
+    return out
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from aither_gb300 import Context
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module", params=NAMES)
+def run(request, ctx, tmp_path_factory):
+    from aither_gb300 import Batch, Setup
+    name = request.param
+    tmp = tmp_path_factory.mktemp(name)
+    inp, meta = output_case(name, tmp)
+    s = Setup(inp)
+    b = Batch(ctx, s, 0, flags=1)  # with the logged matrix residual
+    norms = list(b.iterate(meta["iterations"]))
+    yield name, meta, s, b, norms, tmp
+    b.close()
+    s.close()
+
+
+def test_function_file_values(run):
+    name, meta, s, b, _, tmp = run
+    n, sim = meta["iterations"], meta["sim"]
+    variables = sorted(meta["variables"])
+    kw = meta["kwargs"]
+    if kw.get("matrix_solver") != "blusgs" and not kw.get("rans"):
+        # scalar LU-SGS laminar solves keep no cell velocity gradients
+        variables = [v for v in variables if not v.startswith("velGrad_")]
+    path = str(tmp / "dev.fun")
+    b.write_function(0, path, variables)
+    got = read_fun(path, variables)
+    want = read_fun(os.path.join(OUT, name, f"{sim}_{n}_center.fun"), sorted(meta["variables"]))
+    for v in variables:
+        for g, w in zip(got[v], want[v]):
+            assert rel_err(g, w) <= TOL, v
+
+
+def test_restart_file(run):
+    name, meta, s, b, norms, tmp = run
+    n, sim = meta["iterations"], meta["sim"]
+    nv = s.solve_nv(0)
+    l2 = np.array([[x.l2[v] for v in range(nv)] for x in norms])
+    first = l2[0].copy()
+    for k in range(1, min(5, len(l2))):
+        first = np.maximum(first, l2[k])
+    path = str(tmp / "dev.rst")
+    b.write_restart(0, n, first, path)
+    got, want = open(path, "rb").read(), ref_bytes(name, f"{sim}_{n}.rst")
+    assert len(got) == len(want)
+    # header up to the normalisation, then the block sizes, exactly
+    head = 16 + 8 + 3
+    assert got[:head] == want[:head]
+    nb = len(s.solve_blocks(0))
+    o = head + 8 * nv
+    assert got[o:o + 4 + 16 * nb] == want[o:o + 4 + 16 * nb]
+    assert rel_err(np.frombuffer(got[head:o]), np.frombuffer(want[head:o])) <= TOL
+    d = o + 4 + 16 * nb
+    g = np.frombuffer(got[d:]).reshape(-1, nv + 1)
+    w = np.frombuffer(want[d:]).reshape(-1, nv + 1)
+    assert rel_err(g[:, :5], w[:, :5]) <= 1e-12
+    for v in range(5, nv + 1):
+        assert rel_err(g[:, v], w[:, v]) <= 1e-12
+
+
+def test_restart_read_into_device(run, ctx):
+    """The reference's restart file loaded into a fresh batch gives the
+    state the host reader decodes from it."""
+    from aither_gb300 import Batch
+    name, meta, s, _, _, tmp = run
+    n, sim = meta["iterations"], meta["sim"]
+    path = os.path.join(OUT, name, f"{sim}_{n}.rst")
+    it_h, rf_h, prims = s.read_restart(0, path)
+    fresh = Batch(ctx, s, 0)
+    it, rf = fresh.read_restart(0, path)
+    assert it == it_h == n and np.array_equal(rf, rf_h)
+    for k, blk in enumerate(s.solve_blocks(0)):
+        assert np.array_equal(fresh.field(blk, "STATE"), prims[k])
+    fresh.close()
+
+
+def test_residual_history(run):
+    """Every column of the reference's residual file from the device norms:
+    integers exactly, the 4-digit values to their last printed digit."""
+    name, meta, s, _, norms, tmp = run
+    nv = s.solve_nv(0)
+    rf = np.zeros(7)
+    s.write_resid(0, str(tmp / "dev.resid"), norms, 0, rf)
+    got = open(tmp / "dev.resid").read().splitlines()
+    want = ref_bytes(name, f"{meta['sim']}.resid").decode().splitlines()
+    assert got[0] == want[0] and len(got) == len(want)
+    for gl, wl in zip(got[1:], want[1:]):
+        g, w = gl.split(), wl.split()
+        assert len(g) == len(w)
+        ints = [0, 1] + list(range(3 + nv, 8 + nv))
+        for c in range(len(w)):
+            if c in ints:
+                assert g[c] == w[c], (c, gl, wl)
+            else:
+                assert abs(float(g[c]) - float(w[c])) <= 1.5e-4 * abs(float(w[c])) + 1e-300, \
+                    (c, gl, wl)
