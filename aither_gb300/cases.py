@@ -380,12 +380,15 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                wall_t: float | None = None, limiter: str = "vanAlbada",
                name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder",
                sweeps: int = 1, rans: bool = False, tint: float = 0.001, vratio: float = 10.0,
-               flux: str = "roe", nblocks: int = 2, dy_max: float | None = None):
+               flux: str = "roe", nblocks: int = 2, dy_max: float | None = None,
+               lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
     the x-y plane, slip walls in z.  Freestream density from Re_L with
-    Sutherland's law at t_inf."""
+    Sutherland's law at t_inf.  One block (nblocks=1) may start `lead` ahead
+    of the leading edge, with a slip wall (symmetry plane) on y = 0 there.
+    The CFL ramps from cfl_start by cfl_step per iteration up to cfl."""
     os.makedirs(outdir, exist_ok=True)
     dz = 0.02 * length
     b0 = plate_nodes(0.0, 0.5 * length, ni, nj, nk, dy0, ratio, dz, dy_max)
@@ -416,15 +419,22 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
             ("slipWall", 0, ni, 0, nj, 0, 0, 4),
             ("slipWall", 0, ni, 0, nj, nk, nk, 4)]
     inp = os.path.join(outdir, name + ".inp")
-    scheme = {"cfl": cfl, "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
+    scheme = {"cfl": cfl, "cflStart": cfl if cfl_start is None else cfl_start,
+              "cflStep": cfl_step,
+              "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
               "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
               "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps}
     if nblocks == 1:
-        nodes = plate_nodes(0.0, length, ni, nj, nk, dy0, ratio, dz, dy_max)
+        nodes = plate_nodes(-lead, length, ni, nj, nk, dy0, ratio, dz, dy_max)
         write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
+        # first node at or behind x = 0 starts the viscous wall
+        i_le = int(np.searchsorted(nodes[0, 0, 0, :], -1e-12 * length)) if lead > 0 else 0
+        bottom = [("viscousWall", i_le, ni, 0, 0, 0, nk, 2)]
+        if i_le > 0:
+            bottom.insert(0, ("slipWall", 0, i_le, 0, 0, 0, nk, 4))
         blk = [("characteristic", 0, 0, 0, nj, 0, nk, 1),
                ("characteristic", ni, ni, 0, nj, 0, nk, 1),
-               ("viscousWall", 0, ni, 0, 0, 0, nk, 2),
+               *bottom,
                ("characteristic", 0, ni, nj, nj, 0, nk, 1),
                ("slipWall", 0, ni, 0, nj, 0, 0, 4),
                ("slipWall", 0, ni, 0, nj, nk, nk, 4)]

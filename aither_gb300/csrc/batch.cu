@@ -117,8 +117,11 @@ struct BatchCore {
   std::vector<int64_t> solve_pos0;   // per block: loop-order offset inside its solve
   Lists L;
   int nsteps = 0;
-  int kinds = 0;        // bit 0: scalar lusgs solves present, bit 1: block (blusgs)
-  int max_sweeps = 1;   // largest matrixSweeps of the batch
+  int kinds = 0;        // bit 0: scalar solves present, bit 1: block solves
+  int skinds = 0;       // the same for the LU-SGS solves (hyperplane sweeps)
+  int jkinds = 0;       // and for the DP-LUR solves (Jacobi sweeps)
+  int max_sweeps = 1;   // largest matrixSweeps of the LU-SGS solves
+  int max_jsweeps = 0;  // largest matrixSweeps of the DP-LUR solves
   int sweep_threads = 128;  // CTA size of the sweep kernels (autotuned)
   bool block_viscous = false;
   bool any_rans = false;  // SST solves present: k, omega pools allocated
@@ -362,6 +365,10 @@ class Runner : public RunnerBase {
       Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
     }
     Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
+    if (c.jkinds) {
+      P_.dUq2 = m.Alloc<T>(5 * nq);
+      Check(cudaMemset(P_.dUq2, 0, 5 * nq * sizeof(T)), "memset");
+    }
     Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
     {
       std::vector<T> lo(c.L.face_lo.begin(), c.L.face_lo.end());
@@ -466,6 +473,7 @@ class Runner : public RunnerBase {
     const int64_t aw = (c_.kinds & 2) ? 4 : 1;
     P_.Rtq = zero(m.Alloc<T>(2 * nq), 2 * nq);
     P_.dUtq = zero(m.Alloc<T>(2 * nq), 2 * nq);
+    if (c_.jkinds) P_.dUtq2 = zero(m.Alloc<T>(2 * nq), 2 * nq);
     const int64_t g = std::max<int64_t>(ngh, 1);
     P_.dUtg = zero(m.Alloc<T>(2 * g), 2 * g);
     P_.Ainvtq = zero(m.Alloc<T>(aw * nq), aw * nq);
@@ -542,13 +550,13 @@ class Runner : public RunnerBase {
     if (forward) {
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.kinds,
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.skinds,
                          c_.sweep_threads, c_.stream);
       }
     } else {
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.kinds,
+        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.skinds,
                          c_.sweep_threads, c_.stream);
       }
     }
@@ -559,9 +567,28 @@ class Runner : public RunnerBase {
     if (P_.dUtg)
       Check(cudaMemsetAsync(P_.dUtg, 0, 2 * P_.nghost * sizeof(T), c_.stream), "memset");
   }
+  // dplur::Relax (src/linearSolver.cpp:501): x0 = A^-1 b, then per sweep a
+  // ghost swap and one Jacobi pass over every cell at once, alternating
+  // between the two update buffers; the final iterate ends in dUq
+  void JacobiPhase() {
+    const int n = (int)c_.L.sweep_items.size();
+    Launch<T>::Init(P_, c_.d_sweep, n, 1, c_.stream);
+    Pools<T> other = P_;
+    other.dUq = P_.dUq2;
+    other.dUtq = P_.dUtq2;
+    for (int sw = 0; sw < c_.max_jsweeps; ++sw) {
+      const bool even = sw % 2 == 0;
+      const Pools<T> &src = even ? P_ : other;
+      Launch<T>::ConnDu(src, c_.stream);
+      Launch<T>::Jacobi(src, even ? P_.dUq2 : P_.dUq, even ? P_.dUtq2 : P_.dUtq, c_.d_sweep, n,
+                        sw, c_.jkinds, c_.stream);
+    }
+    if (c_.max_jsweeps % 2 == 1)
+      Launch<T>::JacobiCopy(P_, P_.dUq2, P_.dUtq2, c_.d_sweep, n, c_.stream);
+  }
   // lusgs::Relax (src/linearSolver.cpp:430): dU ghost swap before every
   // pass and after the last one
-  void Relax() override {
+  void SweepPhase() {
     if (c_.max_sweeps <= 1) {
       // x = 0 before the first sweep: only the connection ghosts are read
       // before being written
@@ -570,7 +597,7 @@ class Runner : public RunnerBase {
       Launch<T>::ConnDu(P_, c_.stream);
       SweepPass(0, 0);
     } else {
-      Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
+      Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), 0, c_.stream);
       for (int sw = 0; sw < c_.max_sweeps; ++sw) {
         Launch<T>::ConnDu(P_, c_.stream);
         SweepPass(1, sw);
@@ -578,6 +605,10 @@ class Runner : public RunnerBase {
         SweepPass(0, sw);
       }
     }
+  }
+  void Relax() override {
+    if (c_.jkinds) JacobiPhase();
+    if (c_.skinds) SweepPhase();
     if (c_.flags & 1) {
       Launch<T>::ConnDu(P_, c_.stream);
       Launch<T>::MatRes(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_mres,
@@ -632,13 +663,23 @@ class Runner : public RunnerBase {
         Launch<T>::OffJac(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
       Check(cudaEventRecord(e[5], c_.stream), "event");
       // forward passes, then backward passes (one-sweep form; the timing
-      // split of a multi-sweep relaxation puts each sweep's passes in turn)
-      if (c_.max_sweeps > 1)
-        Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
-      else
-        ZeroGhostUpdates();
+      // split of a multi-sweep relaxation puts each sweep's passes in turn);
+      // DP-LUR sweeps count as forward passes
       float fwd = 0.f, bwd = 0.f;
-      for (int sw = 0; sw < c_.max_sweeps; ++sw) {
+      if (c_.jkinds) {
+        Check(cudaEventRecord(e[6], c_.stream), "event");
+        JacobiPhase();
+        Check(cudaEventRecord(e[7], c_.stream), "event");
+        Check(cudaEventSynchronize(e[7]), "sync");
+        float tj = 0.f;
+        Check(cudaEventElapsedTime(&tj, e[6], e[7]), "elapsed");
+        fwd += tj;
+      }
+      if (c_.skinds && c_.max_sweeps > 1)
+        Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), 0, c_.stream);
+      else if (c_.skinds)
+        ZeroGhostUpdates();
+      for (int sw = 0; sw < (c_.skinds ? c_.max_sweeps : 0); ++sw) {
         if (c_.max_sweeps > 1) Launch<T>::ConnDu(P_, c_.stream);
         Check(cudaEventRecord(e[6], c_.stream), "event");
         SweepPass(1, sw);
@@ -751,7 +792,7 @@ class Runner : public RunnerBase {
     const Block &b = c_.setup->blocks[bi];
     const auto &ph = c_.setup->solves[b.solve].phys;
     const bool have = ph.eqn == ATH_EQN_RANS ||
-                      (ph.eqn != ATH_EQN_EULER && ph.solver == ATH_SOLVER_BLUSGS);
+                      (ph.eqn != ATH_EQN_EULER && IsBlockSolver(ph.solver));
     if (!have || !P_.vgq)
       throw Error(ATH_ERR_UNSUPPORTED, "cell velocity gradients are kept for block LU-SGS "
                                        "viscous and SST solves only");
@@ -1091,9 +1132,15 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     if (rans) c.any_rans = true;
   }
   for (const auto &sv : st.solves) {
-    const bool blk = sv.phys.solver == ATH_SOLVER_BLUSGS;
+    const bool blk = IsBlockSolver(sv.phys.solver), jac = IsJacobiSolver(sv.phys.solver);
     c.kinds |= blk ? 2 : 1;
-    c.max_sweeps = std::max(c.max_sweeps, (int)sv.phys.sweeps);
+    if (jac) {
+      c.jkinds |= blk ? 2 : 1;
+      c.max_jsweeps = std::max(c.max_jsweeps, (int)sv.phys.sweeps);
+    } else {
+      c.skinds |= blk ? 2 : 1;
+      c.max_sweeps = std::max(c.max_sweeps, (int)sv.phys.sweeps);
+    }
     if (blk && sv.phys.eqn != ATH_EQN_EULER) c.block_viscous = true;
     const bool rans = sv.phys.eqn == ATH_EQN_RANS;
     c.fkinds |= rans ? 2 : 1;
@@ -1136,7 +1183,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.k_s = p.k_s;
     x.k_ref = p.k_ref;
     x.visc_coeff = p.visc_cfl_coeff;
-    x.block = p.solver == ATH_SOLVER_BLUSGS;
+    x.block = IsBlockSolver(p.solver);
+    x.jacobi = IsJacobiSolver(p.solver);
     x.rans = p.eqn == ATH_EQN_RANS;
     x.sweeps = p.sweeps;
     x.active = 1;
@@ -1223,6 +1271,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
   }
   const int nkinds = (c.kinds & 1) + ((c.kinds >> 1) & 1);
+  const int nskinds = (c.skinds & 1) + ((c.skinds >> 1) & 1);
+  const int njkinds = (c.jkinds & 1) + ((c.jkinds >> 1) & 1);
   const int nf = (c.fkinds & 1) + ((c.fkinds >> 1) & 1);
   const int nvf = (c.vkinds & 1) + ((c.vkinds >> 1) & 1);
   const int conn = c.L.ghost_cell.empty() ? 0 : 1;
@@ -1231,8 +1281,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
                                          : 0) +
                         (c.L.wall_faces.empty() ? 0 : 2) +
                         1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
-                        2 * c.nsteps * c.max_sweeps * nkinds +
-                        (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn) + 3 +
+                        (nskinds ? 2 * c.nsteps * c.max_sweeps * nskinds +
+                                       (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
+                                 : 0) +
+                        (njkinds ? 1 + c.max_jsweeps * (conn + njkinds) + (c.max_jsweeps % 2)
+                                 : 0) +
+                        3 +
                         ((flags & 1) ? nkinds + conn : 0);
 }
 
@@ -1728,7 +1782,7 @@ size_t EstimateBatchBytes(const Setup &st, int precision) {
     const auto &ph = st.solves[b.solve].phys;
     const double n = (double)b.NCell();
     const double nq = (double)b.ni * b.nj * b.nk;
-    const bool visc = ph.eqn != ATH_EQN_EULER, blk = ph.solver == ATH_SOLVER_BLUSGS;
+    const bool visc = ph.eqn != ATH_EQN_EULER, blk = IsBlockSolver(ph.solver);
     double pc = 8.0 * (5 + 5 + 15 + 1 + 1 + 1 + 3 + 12) + 4.0 * 6;  // pools, lists
     if (visc) pc += 15 * ts + 8;
     if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);

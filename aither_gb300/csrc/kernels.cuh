@@ -40,7 +40,7 @@ struct SolveDev {
   int32_t flux;
   int32_t block;   // blusgs: 5x5 Jacobian diagonal and off-diagonals
   int32_t rans;    // SST-2003: k and omega beside the flow equations
-  int32_t pad4;
+  int32_t jacobi;  // dplur / bdplur: Jacobi sweeps instead of LU-SGS
   int32_t sweeps;  // matrixSweeps
   int32_t active;  // 0 once the solve is retired: its kernels skip their work
 };
@@ -131,6 +131,8 @@ struct Pools {
   // [(side*3 + d)*25 + e][nq] (side 0 = lower) and the turbulence blocks
   // [(side*3 + d)*4 + e][nq]
   T *Joff, *Jtoff;
+  // Jacobi (DP-LUR) solves: the second update buffer of the sweeps
+  T *dUq2, *dUtq2;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -274,7 +276,16 @@ struct Launch {
                     bool full, int kinds, int threads, cudaStream_t s);
   // off-diagonal Jacobians of the block solves' cells, once per iteration
   static void OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
-  static void Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
+  // jacobi = 0: x0 of the LU-SGS solves, 1: of the DP-LUR solves
+  static void Init(const Pools<T> &P, const int2 *items, int n, int jacobi, cudaStream_t s);
+  // one DP-LUR sweep of the Jacobi solves from P.dUq into dst (kinds:
+  // scalar / block solves present); solves past their sweep count carry
+  // their iterate over
+  static void Jacobi(const Pools<T> &P, T *dst, T *dstt, const int2 *items, int n, int sweep,
+                     int kinds, cudaStream_t s);
+  // the Jacobi solves' final iterate from (src, srct) into dUq, dUtq
+  static void JacobiCopy(const Pools<T> &P, const T *src, const T *srct, const int2 *items,
+                         int n, cudaStream_t s);
   static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,

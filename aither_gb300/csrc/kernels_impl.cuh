@@ -1029,7 +1029,7 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
   const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
-  if (sv.block || !sv.active) return;
+  if (sv.block || sv.jacobi || !sv.active) return;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   T acc[5], acct[2];
@@ -1101,7 +1101,7 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
   const int64_t q = it.x;
   const BlockDev b = P.blocks[it.y];
   const SolveDev sv = P.solves[b.solve];
-  if (!sv.block || !sv.active || sweep >= sv.sweeps) return;
+  if (!sv.block || sv.jacobi || !sv.active || sweep >= sv.sweeps) return;
   const bool full = sweep > 0 || sv.sweeps > 1;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
@@ -1160,17 +1160,20 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
   }
 }
 
-// x = A^-1 b before the first sweep of multi-sweep solves, 0 otherwise
+// x = A^-1 b before the first sweep of multi-sweep and DP-LUR solves
+// (InitializeMatrixUpdate, src/linearSolver.cpp:111), 0 otherwise; `jacobi`
+// selects the DP-LUR solves or the LU-SGS ones
 template <typename T>
-__global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int n_items) {
+__global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int n_items,
+                                              int jacobi) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
   const int2 it = items[t];
   const int64_t q = it.x, nq = P.nq;
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
-  if (!sv.active) return;
+  if (!sv.active || (sv.jacobi != 0) != (jacobi != 0)) return;
   T x[5], xt[2] = {T(0), T(0)};
-  if (sv.sweeps <= 1) {
+  if (sv.sweeps <= 1 && !sv.jacobi) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) x[v] = T(0);
   } else {
@@ -1208,6 +1211,93 @@ __global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int
   if (sv.rans) {
     P.dUtq[q] = xt[0];
     P.dUtq[nq + q] = xt[1];
+  }
+}
+
+// One DP-LUR sweep (dplur::DPLUR, src/linearSolver.cpp:473): from the
+// previous iterate P.dUq (and its connection ghosts), x = A^-1 (b + L(x) -
+// U(x)) into dst; every cell is independent
+template <typename T, bool BLOCK>
+__global__ void __launch_bounds__(128) k_jacobi(Pools<T> P, T *dst, T *dstt, const int2 *items,
+                                                int n_items, int sweep) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const int64_t q = it.x, nq = P.nq;
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (!sv.jacobi || !sv.active || (sv.block != 0) != BLOCK) return;
+  if (sweep >= sv.sweeps) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[v * nq + q] = P.dUq[v * nq + q];
+    if (sv.rans) {
+      dstt[q] = P.dUtq[q];
+      dstt[nq + q] = P.dUtq[nq + q];
+    }
+    return;
+  }
+  const T thetaInv = (T)(1.0 / sv.theta);
+  T L[5], U[5], Lt[2], Ut[2], in[5], x[5];
+  if constexpr (BLOCK) {
+    OffDiagSumBlock(P, sv, q, true, L, Lt);
+    OffDiagSumBlock(P, sv, q, false, U, Ut);
+  } else {
+    const Gas<T> g = GasOf<T>(sv);
+    OffDiagSum(P, g, sv, q, true, L, Lt);
+    OffDiagSum(P, g, sv, q, false, U, Ut);
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const T bv = -thetaInv * P.Rq[v * nq + q];
+    in[v] = bv + (L[v] - U[v]);
+  }
+  if constexpr (BLOCK) {
+    T Ai[kJac];
+#pragma unroll
+    for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
+    MatVec5(Ai, in, x);
+  } else {
+    const T ainv = P.Ainvq[q];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) x[v] = in[v] * ainv;
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) dst[v * nq + q] = x[v];
+  if (sv.rans) {
+    T int_[2], xt[2];
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const T bv = -thetaInv * P.Rtq[v * nq + q];
+      int_[v] = bv + (Lt[v] - Ut[v]);
+    }
+    if constexpr (BLOCK) {
+      T Ait[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) Ait[e] = P.Ainvtq[e * nq + q];
+      MatVec2(Ait, int_, xt);
+    } else {
+      const T ainvt = P.Ainvtq[q];
+      xt[0] = int_[0] * ainvt;
+      xt[1] = int_[1] * ainvt;
+    }
+    dstt[q] = xt[0];
+    dstt[nq + q] = xt[1];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_jacobi_copy(Pools<T> P, const T *src, const T *srct,
+                                                     const int2 *items, int n_items) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const int64_t q = it.x, nq = P.nq;
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (!sv.jacobi || !sv.active) return;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = src[v * nq + q];
+  if (sv.rans) {
+    P.dUtq[q] = srct[q];
+    P.dUtq[nq + q] = srct[nq + q];
   }
 }
 
@@ -1931,8 +2021,21 @@ void Launch<T>::OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t
   if (n > 0) k_offjac<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n);
 }
 template <typename T>
-void Launch<T>::Init(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {
-  if (n > 0) k_init<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n);
+void Launch<T>::Init(const Pools<T> &P, const int2 *items, int n, int jacobi, cudaStream_t s) {
+  if (n > 0) k_init<T><<<(n + 127) / 128, 128, 0, s>>>(P, items, n, jacobi);
+}
+template <typename T>
+void Launch<T>::Jacobi(const Pools<T> &P, T *dst, T *dstt, const int2 *items, int n, int sweep,
+                       int kinds, cudaStream_t s) {
+  if (n <= 0) return;
+  const unsigned grid = (unsigned)((n + 127) / 128);
+  if (kinds & 1) k_jacobi<T, false><<<grid, 128, 0, s>>>(P, dst, dstt, items, n, sweep);
+  if (kinds & 2) k_jacobi<T, true><<<grid, 128, 0, s>>>(P, dst, dstt, items, n, sweep);
+}
+template <typename T>
+void Launch<T>::JacobiCopy(const Pools<T> &P, const T *src, const T *srct, const int2 *items,
+                           int n, cudaStream_t s) {
+  if (n > 0) k_jacobi_copy<T><<<(n + 127) / 128, 128, 0, s>>>(P, src, srct, items, n);
 }
 template <typename T>
 void Launch<T>::ConnDu(const Pools<T> &P, cudaStream_t s) {

@@ -1224,6 +1224,7 @@ void AppendInput(Setup &st, const std::string &path) {
 
   const auto ms = get("matrixSolver", "lusgs");
   ph.solver = ms == "lusgs" ? ATH_SOLVER_LUSGS : ms == "blusgs" ? ATH_SOLVER_BLUSGS
+              : ms == "dplur" ? ATH_SOLVER_DPLUR : ms == "bdplur" ? ATH_SOLVER_BDPLUR
               : (Fail("unsupported matrixSolver " + ms), 0);
   ph.sweeps = (int)getd("matrixSweeps", 1);
   if (ph.sweeps < 1) Fail("matrixSweeps must be at least 1");

@@ -101,6 +101,10 @@ std::vector<Block> ReadPlot3d(const std::string &path, double lref);
 
 }  // namespace ath
 
+// Block (5x5) solvers and Jacobi (DP-LUR) solvers among ATH_SOLVER_*
+inline bool IsBlockSolver(int s) { return s == ATH_SOLVER_BLUSGS || s == ATH_SOLVER_BDPLUR; }
+inline bool IsJacobiSolver(int s) { return s == ATH_SOLVER_DPLUR || s == ATH_SOLVER_BDPLUR; }
+
 // The C handle of a host setup.
 struct ath_setup {
   ath::Setup s;

@@ -63,7 +63,10 @@ enum { ATH_RECON_CONSTANT = 0, ATH_RECON_MUSCL = 1, ATH_RECON_WENO = 2,
 enum { ATH_LIMITER_NONE = 0, ATH_LIMITER_MINMOD = 1,
        ATH_LIMITER_VANALBADA = 2 };
 enum { ATH_FLUX_ROE = 0, ATH_FLUX_AUSM = 1 };
-enum { ATH_SOLVER_LUSGS = 0, ATH_SOLVER_BLUSGS = 1 };
+/* linear solvers (input::AssignLinearSolver, src/input.cpp:843): LU-SGS and
+ * block LU-SGS hyperplane sweeps; DP-LUR and block DP-LUR Jacobi sweeps */
+enum { ATH_SOLVER_LUSGS = 0, ATH_SOLVER_BLUSGS = 1, ATH_SOLVER_DPLUR = 2,
+       ATH_SOLVER_BDPLUR = 3 };
 enum { ATH_TURB_NONE = 0, ATH_TURB_SST2003 = 1, ATH_TURB_KW2006 = 2 };
 
 /* boundary condition types (reference keyword in brackets) */

@@ -59,6 +59,7 @@ typedef struct {
   int block;   /* blusgs: 5x5 Jacobian diagonal and off-diagonals */
   int rans;    /* SST-2003 turbulence equations */
   int sweeps;  /* matrixSweeps */
+  int jacobi;  /* dplur / bdplur: Jacobi sweeps instead of LU-SGS */
 } osolve;
 
 struct orc_case {
@@ -1207,7 +1208,8 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     c->s[s].gas.n = sv[s].gas_n;
     c->s[s].gas.hf = sv[s].gas_hf;
     c->s[s].viscous = sv[s].eqn != ATH_EQN_EULER;
-    c->s[s].block = sv[s].solver == ATH_SOLVER_BLUSGS;
+    c->s[s].block = sv[s].solver == ATH_SOLVER_BLUSGS || sv[s].solver == ATH_SOLVER_BDPLUR;
+    c->s[s].jacobi = sv[s].solver == ATH_SOLVER_DPLUR || sv[s].solver == ATH_SOLVER_BDPLUR;
     c->s[s].rans = sv[s].eqn == ATH_EQN_RANS;
     c->s[s].sweeps = sv[s].sweeps > 0 ? sv[s].sweeps : 1;
   }
@@ -1915,17 +1917,23 @@ static void apply_ainv(const orc_case *c, const oblock *b, int64_t x, const doub
 /* lusgs::Relax (src/linearSolver.cpp:430) with LUSGS_Forward :341 and
  * LUSGS_Backward :385: matrixSweeps sweeps; with more than one sweep the
  * update starts from A^-1 b (InitializeMatrixUpdate :111) and every sweep
- * uses both triangles, otherwise from zero with one triangle per pass */
+ * uses both triangles, otherwise from zero with one triangle per pass.
+ * dplur::Relax (:501) with DPLUR (:473): from A^-1 b (MatrixRequires-
+ * Initialization, src/input.cpp:1120), matrixSweeps Jacobi sweeps, each
+ * after a ghost swap: x = A^-1 (b + L(x_old) - U(x_old)) */
 void orc_relax(orc_case *c) {
   NTH
-  int maxsw = 1;
-  for (int s = 0; s < c->ns; ++s) maxsw = c->s[s].sweeps > maxsw ? c->s[s].sweeps : maxsw;
+  int maxsw = 1, maxj = 0;
+  for (int s = 0; s < c->ns; ++s) {
+    if (c->s[s].jacobi) maxj = c->s[s].sweeps > maxj ? c->s[s].sweeps : maxj;
+    else maxsw = c->s[s].sweeps > maxsw ? c->s[s].sweeps : maxsw;
+  }
   PAR_BLOCKS
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
     const osolve *sv = &c->s[b->solve];
     const int nv = sv->rans ? NV + 2 : NV;
-    if (sv->sweeps <= 1) {
+    if (sv->sweeps <= 1 && !sv->jacobi) {
       memset(b->dU, 0, 8 * NV * b->nc);
       if (b->dUt) memset(b->dUt, 0, 8 * 2 * b->nc);
       continue;
@@ -1942,13 +1950,47 @@ void orc_relax(orc_case *c) {
           set_du(b, x, out);
         }
   }
+  for (int sw = 0; sw < maxj; ++sw) {
+    swap_du(c);
+    PAR_BLOCKS
+    for (int bi = 0; bi < c->nb; ++bi) {
+      oblock *b = &c->b[bi];
+      const osolve *sv = &c->s[b->solve];
+      if (!sv->jacobi || sw >= sv->sweeps) continue;
+      const int nv = sv->rans ? NV + 2 : NV;
+      const double thetaInv = 1.0 / sv->v.theta;
+      /* new iterate beside the old one (ghosts keep the swapped values) */
+      double *nu = (double *)dup_arr(b->dU, 8 * NV * b->nc);
+      double *nut = b->dUt ? (double *)dup_arr(b->dUt, 8 * 2 * b->nc) : NULL;
+      for (int k = 0; k < b->nk; ++k)
+        for (int j = 0; j < b->nj; ++j)
+          for (int i = 0; i < b->ni; ++i) {
+            const int64_t x = cell_idx(b, i, j, k);
+            double L[NV + 2], U[NV + 2], in[NV + 2], r[NV + 2], out[NV + 2];
+            offdiag_sum(c, b, x, 1, L);
+            offdiag_sum(c, b, x, 0, U);
+            get_rhs(c, b, x, r);
+            for (int v = 0; v < nv; ++v) {
+              const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+              in[v] = bb + 0.0 + (L[v] - U[v]);
+            }
+            apply_ainv(c, b, x, in, out);
+            memcpy(&nu[x * NV], out, 8 * NV);
+            if (nut) memcpy(&nut[x * 2], out + NV, 8 * 2);
+          }
+      memcpy(b->dU, nu, 8 * NV * b->nc);
+      if (nut) memcpy(b->dUt, nut, 8 * 2 * b->nc);
+      free(nu);
+      free(nut);
+    }
+  }
   for (int sw = 0; sw < maxsw; ++sw) {
     swap_du(c);
     PAR_BLOCKS
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
-      if (sw >= sv->sweeps) continue;
+      if (sv->jacobi || sw >= sv->sweeps) continue;
       const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;
@@ -1975,7 +2017,7 @@ void orc_relax(orc_case *c) {
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
-      if (sw >= sv->sweeps) continue;
+      if (sv->jacobi || sw >= sv->sweeps) continue;
       const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;

@@ -79,6 +79,16 @@ CASES = [
      dict(ni=14, nj=12, nk=3, dy0=5e-5, ratio=1.25, reynolds=5e6, mach=0.2, rans=True,
           nblocks=1, recon="weno", limiter="none", flux="ausm", matrix_solver="blusgs"),
      [1, 10], True),
+    # DP-LUR and block DP-LUR (Jacobi sweeps)
+    ("bump_dplur", cases.bump_channel,
+     dict(ni=20, nj=10, nk=3, height=0.08, mach=0.7, matrix_solver="dplur", sweeps=3),
+     [1, 20], True),
+    ("plate_bdplur", cases.flat_plate,
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, cfl=20.0, matrix_solver="bdplur", sweeps=4),
+     [1, 20], True),
+    ("sst_plate_dplur", cases.flat_plate,
+     dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1, cfl=20.0, matrix_solver="dplur", sweeps=2), [1, 10], True),
 ]
 
 

@@ -143,3 +143,24 @@ def test_sst_mixed_precision_converged_state_against_fp64(ctx, tmp_path):
           f"omega {errs[2]:.2e}; iterations {out[1][1]} vs {out[0][1]}")
     assert max(errs) <= 1e-6
     assert abs(out[1][1] - out[0][1]) <= max(2, 0.01 * out[0][1])
+
+
+@pytest.mark.parametrize("solver", ["dplur", "bdplur"])
+def test_jacobi_relaxation_reaches_the_lusgs_steady_state(ctx, solver, tmp_path):
+    """DP-LUR (Jacobi sweeps, every cell at once) and LU-SGS relax the same
+    linear system differently but drive the same residual to zero: at a
+    1e-8 drop their converged states agree to 1e-6."""
+    from aither_gb300 import Batch, Setup, cases
+    out = {}
+    for ms in ("lusgs", solver):
+        inp, _ = cases.bump_channel(str(tmp_path / ms), 16, 8, 4, 0.06, 0.55, name=ms,
+                                    matrix_solver=ms, sweeps=1 if ms == "lusgs" else 4)
+        b = Batch(ctx, Setup(inp), 0)
+        info = b.converge(20000, 1e-8, check_every=200)
+        assert info[0].converged == 1
+        out[ms] = (b.field(0, "STATE"), info[0].iterations)
+        b.close()
+    err = rel_err(out[solver][0], out["lusgs"][0])
+    print(f"{solver} vs lusgs: rel err {err:.2e}, iterations {out[solver][1]} vs "
+          f"{out['lusgs'][1]}")
+    assert err <= 1e-6

@@ -62,7 +62,9 @@ def _cols_err(a, b):
                                   "bump_blusgs_it20", "bump_sweeps3_it1", "bump_sweeps3_it20",
                                   "bump_blusgs_weno_sw2_it1", "bump_blusgs_weno_sw2_it20",
                                   "plate_blusgs_it1", "plate_blusgs_it20",
-                                  "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20"])
+                                  "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20",
+                                  "bump_dplur_it1", "bump_dplur_it20", "plate_bdplur_it1",
+                                  "plate_bdplur_it20"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
@@ -84,7 +86,8 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
 
 
 SST_CASES = ["sst_plate_it1", "sst_plate_it20", "sst_plate2_blusgs_it1",
-             "sst_plate2_blusgs_it10", "sst_weno_ausm_it1", "sst_weno_ausm_it10"]
+             "sst_plate2_blusgs_it10", "sst_weno_ausm_it1", "sst_weno_ausm_it10",
+             "sst_plate_dplur_it1", "sst_plate_dplur_it10"]
 
 
 @pytest.mark.parametrize("name", SST_CASES)
@@ -122,7 +125,8 @@ def test_fp64_sst_matches_reference_fixture(ctx, name, tmp_path):
 @pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
                                   "bump_blusgs_it20", "bump_sweeps3_it20",
                                   "plate_blusgs_sw2_it20", "sst_plate_it20",
-                                  "sst_plate2_blusgs_it10"])
+                                  "sst_plate2_blusgs_it10", "bump_dplur_it20",
+                                  "plate_bdplur_it20"])
 def test_fp64_matrix_residual(ctx, name, tmp_path):
     """flags bit 0: the logged matrix residual of every iteration; it is a
     log-only quantity, so the solution is unchanged."""
