@@ -175,6 +175,8 @@ def lib() -> C.CDLL:
             "ath_batch_set_target": (C.c_int, [vp, C.c_int, C.c_double, C.c_int]),
             "ath_batch_solve_info": (C.c_int, [vp, C.POINTER(ConvergeInfo)]),
             "ath_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
+            "ath_batch_sweep_shape": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                                C.POINTER(C.c_int)]),
             "ath_server_create": (C.c_int, [vp, C.c_int, C.c_double, C.c_int64, C.c_int,
                                             C.c_int, C.POINTER(vp)]),
             "ath_server_submit": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_int64)]),
@@ -446,6 +448,13 @@ class Batch:
         check(lib().ath_batch_read_restart(self.h, self.setup.h, solve, path.encode(),
                                            C.byref(it), dptr(rf)))
         return it.value, rf[:self.setup.solve_nv(solve)]
+
+    def sweep_shape(self) -> dict:
+        """LU-SGS sweep shape: mode 1 persistent (cluster CTAs per solve),
+        0 one launch per hyperplane."""
+        m, t, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().ath_batch_sweep_shape(self.h, C.byref(m), C.byref(t), C.byref(c)))
+        return {"mode": m.value, "threads": t.value, "cluster": c.value}
 
     def pool_vars(self) -> int:
         """Values per cell of the copy_state snapshot (5, or 7 with SST)."""

@@ -82,6 +82,10 @@ struct Lists {
   std::vector<int32_t> faces[3], face_cta_block[3];
   std::vector<int2> sweep_items;  // (q index, block)
   std::vector<int32_t> step_off;
+  // the same items per solve, then plane, for the persistent sweep
+  std::vector<int2> cl_items;
+  std::vector<int32_t> cl_step_off, solve_step0, solve_nsteps;
+  int max_plane = 0;  // largest plane of one solve
   std::vector<int32_t> solve_cta0;
   std::vector<GhostOpDev> ops, conn_ops;
   std::vector<int32_t> op_solve;
@@ -122,7 +126,15 @@ struct BatchCore {
   int jkinds = 0;       // and for the DP-LUR solves (Jacobi sweeps)
   int max_sweeps = 1;   // largest matrixSweeps of the LU-SGS solves
   int max_jsweeps = 0;  // largest matrixSweeps of the DP-LUR solves
-  int sweep_threads = 128;  // CTA size of the sweep kernels (autotuned)
+  int sweep_threads = 128;  // CTA size of the per-plane sweep kernels (autotuned)
+  // sweep shape: mode 1 = persistent (one cluster of cl_size CTAs of
+  // cl_threads per solve), 0 = one launch per hyperplane; autotuned
+  int sweep_mode = 0, cl_size = 1, cl_threads = 256;
+  int2 *d_cl_items = nullptr;
+  int32_t *d_cl_step_off = nullptr, *d_solve_step0 = nullptr, *d_solve_nsteps = nullptr;
+  SweepLists Lists() const {
+    return SweepLists{d_cl_items, d_cl_step_off, d_solve_step0, d_solve_nsteps, nsolves};
+  }
   bool block_viscous = false;
   bool any_rans = false;  // SST solves present: k, omega pools allocated
   int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
@@ -301,6 +313,7 @@ class RunnerBase {
   // per-solve counters and flags, CFL, iteration counter
   virtual void Snapshot(bool restore) = 0;
   virtual void FreeSnapshot() = 0;
+  virtual int MaxClusters(int kinds, int threads, int cluster) = 0;
 };
 
 template <typename T>
@@ -547,6 +560,11 @@ class Runner : public RunnerBase {
   }
   void SweepPass(int forward, int sweep) {
     const bool full = c_.max_sweeps > 1;
+    if (c_.sweep_mode == 1) {
+      Launch<T>::SweepCl(P_, c_.Lists(), forward, sweep, full, c_.skinds, c_.cl_threads,
+                         c_.cl_size, c_.stream);
+      return;
+    }
     if (forward) {
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
@@ -716,6 +734,9 @@ class Runner : public RunnerBase {
   void ResetGraph() override {
     if (c_.graph) cudaGraphExecDestroy(c_.graph);
     c_.graph = nullptr;
+  }
+  int MaxClusters(int kinds, int threads, int cluster) override {
+    return Launch<T>::MaxClusters(kinds, threads, cluster);
   }
   void Snapshot(bool restore) override {
     DevMem &m = *c_.mem;
@@ -1017,6 +1038,24 @@ void BuildLists(BatchCore &c) {
     }
   }
   L.step_off[c.nsteps] = (int32_t)L.sweep_items.size();
+  for (int s = 0; s < c.nsolves; ++s) {
+    int ns = 0;
+    for (int b : st.solves[s].blocks)
+      ns = std::max(ns, (int)st.blocks[b].plane_offsets.size() - 1);
+    L.solve_step0.push_back((int32_t)L.cl_step_off.size());
+    L.solve_nsteps.push_back(ns);
+    for (int p = 0; p < ns; ++p) {
+      L.cl_step_off.push_back((int32_t)L.cl_items.size());
+      for (int b : st.solves[s].blocks) {
+        const Block &bk = st.blocks[b];
+        if (p + 1 >= (int)bk.plane_offsets.size()) continue;
+        for (int q = bk.plane_offsets[p]; q < bk.plane_offsets[p + 1]; ++q)
+          L.cl_items.push_back(make_int2((int)(L.q0[b] + q), b));
+      }
+      L.max_plane = std::max(L.max_plane, (int)L.cl_items.size() - L.cl_step_off.back());
+    }
+    L.cl_step_off.push_back((int32_t)L.cl_items.size());
+  }
   // ghost operations with pool indices
   for (int b = 0; b < c.nblocks; ++b) {
     const Block &bk = st.blocks[b];
@@ -1115,6 +1154,37 @@ void BuildLists(BatchCore &c) {
           L.aux_block.push_back(b);
         }
   }
+}
+
+// Kernel launches of one iteration (the graph's nodes): cfl, ghost ops and
+// edge phases, viscous ghosts, aux, faces, wall forces, cell, off-diagonal
+// Jacobians, the relaxations' launches, update, norms, counter, and the
+// optional matrix residual
+void CountLaunches(BatchCore &c) {
+  int edge_phases = 0, vedge_phases = 0;
+  for (size_t ph = 0; ph + 1 < c.L.edge_phase_off.size(); ++ph) {
+    edge_phases += c.L.edge_phase_off[ph + 1] > c.L.edge_phase_off[ph];
+    vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
+  }
+  const int nkinds = (c.kinds & 1) + ((c.kinds >> 1) & 1);
+  const int nskinds = (c.skinds & 1) + ((c.skinds >> 1) & 1);
+  const int njkinds = (c.jkinds & 1) + ((c.jkinds >> 1) & 1);
+  const int nf = (c.fkinds & 1) + ((c.fkinds >> 1) & 1);
+  const int nvf = (c.vkinds & 1) + ((c.vkinds >> 1) & 1);
+  const int conn = c.L.ghost_cell.empty() ? 0 : 1;
+  const int per_pass = c.sweep_mode == 1 ? 1 : c.nsteps;
+  c.launches_per_iter = edge_phases +
+                        (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 * nvf
+                                         : 0) +
+                        (c.L.wall_faces.empty() ? 0 : 2) +
+                        1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
+                        (nskinds ? 2 * per_pass * c.max_sweeps * nskinds +
+                                       (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
+                                 : 0) +
+                        (njkinds ? 1 + c.max_jsweeps * (conn + njkinds) + (c.max_jsweeps % 2)
+                                 : 0) +
+                        3 +
+                        ((c.flags & 1) ? nkinds + conn : 0);
 }
 
 void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags) {
@@ -1216,6 +1286,10 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     c.d_face_cta_block[d] = m.Upload(c.L.face_cta_block[d]);
   }
   c.d_sweep = m.Upload(c.L.sweep_items);
+  c.d_cl_items = m.Upload(c.L.cl_items);
+  c.d_cl_step_off = m.Upload(c.L.cl_step_off);
+  c.d_solve_step0 = m.Upload(c.L.solve_step0);
+  c.d_solve_nsteps = m.Upload(c.L.solve_nsteps);
   c.d_solve_cta0 = m.Upload(c.L.solve_cta0);
   c.d_ops = m.Upload(c.L.ops);
   c.d_conn_ops = m.Upload(c.L.conn_ops);
@@ -1263,31 +1337,19 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
-  // launches of one iteration: cfl, ghost, 3 faces, cell, 2 x steps of
-  // sweeps, dU connection copy, update, norms, counter
-  int edge_phases = 0, vedge_phases = 0;
-  for (size_t ph = 0; ph + 1 < c.L.edge_phase_off.size(); ++ph) {
-    edge_phases += c.L.edge_phase_off[ph + 1] > c.L.edge_phase_off[ph];
-    vedge_phases += c.L.vedge_phase_off[ph + 1] > c.L.vedge_phase_off[ph];
+  // default sweep shape: the persistent sweep with a cluster wide enough for
+  // the largest plane (at most 8 CTAs of 256 threads), when launchable
+  if (c.skinds) {
+    const int want = std::min(8, std::max(1, (c.L.max_plane + 255) / 256));
+    for (int cl = want; cl >= 1; --cl)
+      if (B->run->MaxClusters(c.skinds, 256, cl) > 0) {
+        c.sweep_mode = 1;
+        c.cl_size = cl;
+        c.cl_threads = 256;
+        break;
+      }
   }
-  const int nkinds = (c.kinds & 1) + ((c.kinds >> 1) & 1);
-  const int nskinds = (c.skinds & 1) + ((c.skinds >> 1) & 1);
-  const int njkinds = (c.jkinds & 1) + ((c.jkinds >> 1) & 1);
-  const int nf = (c.fkinds & 1) + ((c.fkinds >> 1) & 1);
-  const int nvf = (c.vkinds & 1) + ((c.vkinds >> 1) & 1);
-  const int conn = c.L.ghost_cell.empty() ? 0 : 1;
-  c.launches_per_iter = edge_phases +
-                        (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 * nvf
-                                         : 0) +
-                        (c.L.wall_faces.empty() ? 0 : 2) +
-                        1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
-                        (nskinds ? 2 * c.nsteps * c.max_sweeps * nskinds +
-                                       (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
-                                 : 0) +
-                        (njkinds ? 1 + c.max_jsweeps * (conn + njkinds) + (c.max_jsweeps % 2)
-                                 : 0) +
-                        3 +
-                        ((flags & 1) ? nkinds + conn : 0);
+  CountLaunches(c);
 }
 
 // Reads norms of iterations [it0, it0+n) from the ring into norms_h.
@@ -1517,12 +1579,31 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     auto &c = batch->core;
     Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
     auto &run = *batch->run;
+    // candidates: one launch per hyperplane with CTAs of 32..256 threads, and
+    // the persistent sweep with clusters of 1..8 CTAs of 256 threads
+    struct Shape {
+      int mode, threads, cluster;
+    };
+    std::vector<Shape> cand = {{0, 32, 1}, {0, 64, 1}, {0, 128, 1}, {0, 256, 1}};
+    if (c.skinds)
+      for (int cl : {1, 2, 4, 8})
+        if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
+    const Shape keep{c.sweep_mode, c.sweep_mode == 1 ? c.cl_threads : c.sweep_threads,
+                     c.cl_size};
+    auto apply = [&](const Shape &sh) {
+      c.sweep_mode = sh.mode;
+      if (sh.mode == 1) {
+        c.cl_threads = sh.threads;
+        c.cl_size = sh.cluster;
+      } else {
+        c.sweep_threads = sh.threads;
+      }
+    };
     run.Snapshot(false);
-    const int cand[4] = {32, 64, 128, 256};
     float best = 1e30f;
-    int best_t = c.sweep_threads;
-    for (int t : cand) {
-      c.sweep_threads = t;
+    Shape best_sh = keep;
+    for (const Shape &sh : cand) {
+      apply(sh);
       run.ResetGraph();
       run.Iterate(1);  // capture and warm
       Check(cudaEventRecord(c.ev0, c.stream), "event");
@@ -1533,16 +1614,26 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
       Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
       if (ms < best) {
         best = ms;
-        best_t = t;
+        best_sh = sh;
       }
       run.Snapshot(true);
     }
-    c.sweep_threads = best_t;
+    apply(best_sh);
+    ath::CountLaunches(c);
     run.ResetGraph();
     run.FreeSnapshot();
     Check(cudaGetLastError(), "kernel launch");
-    if (sweep_threads) *sweep_threads = best_t;
+    if (sweep_threads) *sweep_threads = best_sh.threads;
   });
+}
+
+int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster) {
+  if (!batch) return ATH_ERR_ARG;
+  const auto &c = batch->core;
+  if (mode) *mode = c.sweep_mode;
+  if (threads) *threads = c.sweep_mode == 1 ? c.cl_threads : c.sweep_threads;
+  if (cluster) *cluster = c.sweep_mode == 1 ? c.cl_size : 0;
+  return ATH_OK;
 }
 
 int ath_batch_fill_ghosts(ath_batch *batch) {

@@ -45,6 +45,15 @@ struct SolveDev {
   int32_t active;  // 0 once the solve is retired: its kernels skip their work
 };
 
+// Per-solve hyperplane lists of the persistent sweep: items (q index,
+// block) ordered by solve, then plane; step_off[solve_step0[s] + p] .. +1
+// bound plane p of solve s (solve_nsteps[s] planes)
+struct SweepLists {
+  const int2 *items;
+  const int32_t *step_off, *solve_step0, *solve_nsteps;
+  int nsolves;
+};
+
 // A ghost-cell assignment with pool indices.
 struct GhostOpDev {
   int32_t dst, src, type, lower;
@@ -274,6 +283,12 @@ struct Launch {
                    int ncta, int kinds, cudaStream_t s);
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
                     bool full, int kinds, int threads, cudaStream_t s);
+  // one pass of every LU-SGS solve as one launch: a cluster of `cluster`
+  // CTAs of `threads` per solve walks its hyperplanes with cluster barriers
+  static void SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,
+                      bool full, int kinds, int threads, int cluster, cudaStream_t s);
+  // clusters of that shape the device can hold at once (0 = not launchable)
+  static int MaxClusters(int kinds, int threads, int cluster);
   // off-diagonal Jacobians of the block solves' cells, once per iteration
   static void OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   // jacobi = 0: x0 of the LU-SGS solves, 1: of the DP-LUR solves

@@ -2,6 +2,7 @@
 // arithmetic type so each is compiled with its own contraction setting.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <type_traits>
 
 #include "block.cuh"
@@ -854,12 +855,19 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
   acct[0] = acct[1] = T(0);
-#pragma unroll 1
+  // neighbour indices and records first, so their dependent loads overlap;
+  // the sum keeps the i, j, k order
+  int32_t nbs[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) nbs[d] = nbq[d * nq + q];
+  Nbr<T> os[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (nbs[d] != -1) LoadNbr(P, sv, nbs[d], os[d]);
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int32_t nb = nbq[d * nq + q];
-    if (nb == -1) continue;
-    Nbr<T> o;
-    LoadNbr(P, sv, nb, o);
+    if (nbs[d] == -1) continue;
+    const Nbr<T> &o = os[d];
     const T *f = face + (int64_t)d * 4 * nq;
     const T mag = f[3 * nq + q];
     // ViscFaceSpectralRadius (include/spectralRadius.hpp:126) across this
@@ -989,19 +997,27 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const SolveDe
   const int64_t nq = P.nq;
   const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
   const int side = lower ? 0 : 1;
+  // the three neighbour indices, then their updates, are requested before
+  // any product so the dependent loads of the neighbours overlap; the sum
+  // keeps the i, j, k order
+  int32_t nb[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) nb[d] = nbq[d * nq + q];
+  T du[3][5], dut[3][2];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (nb[d] != -1) LoadNbrDu(P, sv, nb[d], du[d], dut[d]);
 #pragma unroll
   for (int v = 0; v < 5; ++v) acc[v] = T(0);
   acct[0] = acct[1] = T(0);
-#pragma unroll 1
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int32_t nb = nbq[d * nq + q];
-    if (nb == -1) continue;
-    T du[5], dut[2], J[kJac], r[5];
-    LoadNbrDu(P, sv, nb, du, dut);
+    if (nb[d] == -1) continue;
+    T J[kJac], r[5];
     const T *Jp = P.Joff + (int64_t)(side * 3 + d) * kJac * nq + q;
 #pragma unroll
     for (int e = 0; e < kJac; ++e) J[e] = Jp[e * nq];
-    MatVec5(J, du, r);
+    MatVec5(J, du[d], r);
 #pragma unroll
     for (int v = 0; v < 5; ++v) acc[v] = acc[v] + r[v];
     if (sv.rans) {
@@ -1009,7 +1025,7 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const SolveDe
       const T *Jtp = P.Jtoff + (int64_t)(side * 3 + d) * 4 * nq + q;
 #pragma unroll
       for (int e = 0; e < 4; ++e) Jt[e] = Jtp[e * nq];
-      MatVec2(Jt, dut, rt);
+      MatVec2(Jt, dut[d], rt);
       acct[0] = acct[0] + rt[0];
       acct[1] = acct[1] + rt[1];
     }
@@ -1021,15 +1037,8 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const SolveDe
 // triangle (sweep 0 of a one-sweep solve: forward x = A^-1 (b + L x),
 // backward x -= A^-1 U x) or both (x = A^-1 (b + L x - U x)).
 template <typename T, bool FULL>
-__global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, int n_items,
-                                               int forward, int sweep) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_items) return;
-  const int2 it = items[t];
-  const int64_t q = it.x;
-  const BlockDev b = P.blocks[it.y];
-  const SolveDev sv = P.solves[b.solve];
-  if (sv.block || sv.jacobi || !sv.active) return;
+__device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                             int forward, int sweep) {
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
   T acc[5], acct[2];
@@ -1089,19 +1098,22 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
     }
   }
 }
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, int n_items,
+                                               int forward, int sweep) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (sv.block || sv.jacobi || !sv.active) return;
+  SweepScalarQ<T, FULL>(P, sv, it.x, forward, sweep);
+}
 
 // Block version: A^-1 is the 5x5 inverse (2x2 for the turbulence rows),
 // products by ArrayMultiplication.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
-                                                int forward, int sweep) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_items) return;
-  const int2 it = items[t];
-  const int64_t q = it.x;
-  const BlockDev b = P.blocks[it.y];
-  const SolveDev sv = P.solves[b.solve];
-  if (!sv.block || sv.jacobi || !sv.active || sweep >= sv.sweeps) return;
+__device__ __forceinline__ void SweepBlockQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                            int forward, int sweep) {
   const bool full = sweep > 0 || sv.sweeps > 1;
   const Gas<T> g = GasOf<T>(sv);
   const int64_t nq = P.nq;
@@ -1157,6 +1169,52 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
       P.dUtq[q] = P.dUtq[q] - xt[0];
       P.dUtq[nq + q] = P.dUtq[nq + q] - xt[1];
     }
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
+                                                int forward, int sweep) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const int2 it = items[t];
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if (!sv.block || sv.jacobi || !sv.active || sweep >= sv.sweeps) return;
+  SweepBlockQ<T>(P, sv, it.x, forward, sweep);
+}
+
+// Persistent sweep: one thread-block cluster per solve walks the solve's
+// hyperplanes in order (forward or backward), the cluster's threads sharing
+// each plane, with a cluster barrier (release/acquire at cluster scope, so
+// a plane's updates are visible to the next plane's readers) between
+// planes.  One launch per pass for every solve of the batch instead of one
+// launch per hyperplane; each cell runs the same arithmetic as k_sweep /
+// k_sweepb.  Every exit condition depends on the solve alone, so either all
+// CTAs of a cluster leave before the first barrier or none does.
+template <typename T, bool FULL, bool BLOCK>
+__global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
+                                                  const int32_t *step_off,
+                                                  const int32_t *solve_step0,
+                                                  const int32_t *solve_nsteps, int forward,
+                                                  int sweep) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int csize = (int)cluster.num_blocks();
+  const int s = (int)(blockIdx.x / csize);
+  const SolveDev sv = P.solves[s];
+  if (!sv.active || sv.jacobi || (sv.block != 0) != BLOCK || sweep >= sv.sweeps) return;
+  const int nst = solve_nsteps[s], base = solve_step0[s];
+  const int tid = (int)cluster.block_rank() * (int)blockDim.x + (int)threadIdx.x;
+  const int nthr = csize * (int)blockDim.x;
+  for (int k = 0; k < nst; ++k) {
+    const int p = forward ? k : nst - 1 - k;
+    const int a = step_off[base + p], b = step_off[base + p + 1];
+    for (int i = a + tid; i < b; i += nthr) {
+      if constexpr (BLOCK)
+        SweepBlockQ<T>(P, sv, items[i].x, forward, sweep);
+      else
+        SweepScalarQ<T, FULL>(P, sv, items[i].x, forward, sweep);
+    }
+    cluster.sync();
   }
 }
 
@@ -2015,6 +2073,62 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, 
     else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
   if (kinds & 2) k_sweepb<T><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+}
+template <typename T, bool FULL, bool BLOCK>
+static void LaunchSweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,
+                          int threads, int cluster, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(L.nsolves * cluster));
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_sweep_cl<T, FULL, BLOCK>, P, L.items, L.step_off, L.solve_step0,
+                     L.solve_nsteps, forward, sweep);
+}
+template <typename T>
+void Launch<T>::SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,
+                        bool full, int kinds, int threads, int cluster, cudaStream_t s) {
+  if (L.nsolves <= 0) return;
+  if (kinds & 1) {
+    if (full) LaunchSweepCl<T, true, false>(P, L, forward, sweep, threads, cluster, s);
+    else LaunchSweepCl<T, false, false>(P, L, forward, sweep, threads, cluster, s);
+  }
+  if (kinds & 2) LaunchSweepCl<T, true, true>(P, L, forward, sweep, threads, cluster, s);
+}
+template <typename T>
+int Launch<T>::MaxClusters(int kinds, int threads, int cluster) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cluster);
+  cfg.blockDim = dim3((unsigned)threads);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int best = 1 << 30, n = 0;
+  if (kinds & 1) {
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cl<T, true, false>, &cfg) != cudaSuccess)
+      n = 0;
+    best = std::min(best, n);
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cl<T, false, false>, &cfg) != cudaSuccess)
+      n = 0;
+    best = std::min(best, n);
+  }
+  if (kinds & 2) {
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_cl<T, true, true>, &cfg) != cudaSuccess)
+      n = 0;
+    best = std::min(best, n);
+  }
+  cudaGetLastError();  // a refused query leaves no sticky error
+  return best == (1 << 30) ? 0 : best;
 }
 template <typename T>
 void Launch<T>::OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s) {

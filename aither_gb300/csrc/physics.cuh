@@ -356,11 +356,19 @@ __device__ __forceinline__ T Deriv2nd(T x0, T x1, T x2, T y0, T y1, T y2) {
   return (fwd - bck) / (T(0.25) * (x2 + x0) + T(0.5) * x1);
 }
 
-// BetaIntegral (include/reconstruction.hpp:157,171)
+// BetaIntegral (include/reconstruction.hpp:157,171).  The reference's
+// pow(x, 3) is a cube here: CUDA's FP64 pow costs ~100 FP64 instructions and
+// twelve of them per variable and side made WENO faces pow-bound; the
+// product differs from a correctly rounded cube by at most an ulp, as
+// CUDA's pow itself may.
+template <typename T>
+__device__ __forceinline__ T Cube(T x) {
+  return x * x * x;
+}
 template <typename T>
 __device__ __forceinline__ T BetaInt(T d1, T d2, T dx, T x) {
-  return (d1 * d1 * x + d1 * d2 * x * x + d2 * d2 * pow(x, T(3)) / T(3)) * dx +
-         d2 * d2 * x * pow(dx, T(3));
+  return (d1 * d1 * x + d1 * d2 * x * x + d2 * d2 * Cube(x) / T(3)) * dx +
+         d2 * d2 * x * Cube(dx);
 }
 template <typename T>
 __device__ __forceinline__ T BetaInt2(T d1, T d2, T dx) {
@@ -466,7 +474,7 @@ __device__ __forceinline__ void AusmFlux(const Prim<T> &L, const Prim<T> &R, con
                                     : T(0.5) * (T(1) - SignOf(mr));
   const T ps = pPlus * L.p + pMinus * R.p;
   const T ra = L.p / R.p, rb = R.p / L.p;
-  const T w = T(1) - pow((rb < ra) ? rb : ra, T(3));
+  const T w = T(1) - Cube((rb < ra) ? rb : ra);
   const T fl = fabs(ml) < T(1) ? L.p / ps - T(1) : T(0);
   const T fr = fabs(mr) < T(1) ? R.p / ps - T(1) : T(0);
   const T mavg = mPlusL + mMinusR;

@@ -153,6 +153,7 @@ def run_native(args, rank: int, world: int, device: int):
         for _ in range(args.warmup):
             batch.iterate(1)
         sweep_threads = batch.autotune(3)  # restores the state it ran on
+        shape = batch.sweep_shape()
         _barrier(world)
         clocks = ClockSampler(device)
         clocks.start()
@@ -166,7 +167,7 @@ def run_native(args, rank: int, world: int, device: int):
         status_ok = all(n.status == 0 for n in norms)
         res = {"value": ncells * args.steps * world / (ms * 1e-3), "ms_per_step": ms / args.steps,
                "wall_s": wall, "gpu_launches": int(st.kernel_launches), "clocks": clk,
-               "status_ok": status_ok, "sweep_threads": sweep_threads}
+               "status_ok": status_ok, "sweep_threads": sweep_threads, "sweep_shape": shape}
         # per-kernel-class CUDA-event times (one iteration's worth each)
         prof = batch.profile(2)
         res["kernel_ms"] = dict(zip(["ghost", "face_i", "face_j", "face_k", "cell",
@@ -181,6 +182,8 @@ def run_native(args, rank: int, world: int, device: int):
         out["converge"] = run_converge(args, ctx, setup, specs, world)
     if args.sst_steps > 0:
         out["sst"] = run_sst(args, ctx, world)
+    if args.plate_drop > 0:
+        out["plate"] = run_plate(args, ctx, world)
     if args.served_n > 0:
         out["served"] = {"definition": "latency = submit to retirement (host clock), "
                                        "retirement at the residual drop; solves/s = "
@@ -271,6 +274,7 @@ def run_sst(args, ctx, world):
         for _ in range(max(args.warmup, 3)):
             b.iterate(1)
         tuned = b.autotune(2)
+        shape = b.sweep_shape()
         _barrier(world)
         clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
         clocks.start()
@@ -282,6 +286,7 @@ def run_sst(args, ctx, world):
         out[name] = {"value": ncells * args.sst_steps * world / (ms * 1e-3),
                      "unit": METRIC, "ms_per_step": ms / args.sst_steps,
                      "gpu_launches": int(st.kernel_launches), "sweep_threads": tuned,
+                     "sweep_shape": shape,
                      "status_ok": all(n.status == 0 for n in norms), "clocks": clk,
                      "kernel_ms": dict(zip(["ghost", "face_i", "face_j", "face_k",
                                             "viscous+cell", "sweep_fwd", "sweep_bwd",
@@ -312,6 +317,61 @@ def run_sst(args, ctx, world):
                                "sample": "1 iteration of the full case after 1 warm-up "
                                          "iteration; oracle (C restatement of the "
                                          "reference), one block so one thread"}
+        orc.close()
+    return out
+
+
+def run_plate(args, ctx, world):
+    """Laminar flat plate, two 128x64x2 blocks joined by an interblock
+    connection (first cell 1e-5, growth 1.08, Mach 0.3, Re_L 1e5, van
+    Albada, Roe, block LU-SGS with 4 sweeps; with one sweep the reference
+    itself turns nonphysical at CFL 100): one solve run to a `plate_drop` drop of its
+    total L2 in FP64 and in mixed precision.  Reports device time to
+    retirement, iterations, the mixed state's error against FP64 and, on
+    rank 0, the oracle's time per iteration on the same case."""
+    import numpy as np
+
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Setup, cases
+    with tempfile.TemporaryDirectory() as tmp:
+        inp, _ = cases.flat_plate(tmp, matrix_solver="blusgs", sweeps=4, name="plate")
+        setup = Setup(inp)
+    _, _, ncells = setup.counts()
+    out = {"workload": "laminar flat plate, two 128x64x2 blocks, interblock, block LU-SGS "
+                       "with 4 sweeps, CFL 100", "cells": ncells, "drop": args.plate_drop}
+    states = {}
+    for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+        b = Batch(ctx, setup, prec)
+        tuned = b.autotune(2)
+        _barrier(world)
+        t0 = time.time()
+        info = b.converge(args.plate_max, args.plate_drop, check_every=200)[0]
+        wall = time.time() - t0
+        st = b.stats()
+        states[name] = [b.field(k, "STATE") for k in range(2)]
+        out[name] = {"converged": int(info.converged), "iterations": int(info.iterations),
+                     "drop": info.drop, "time_to_converge_s": info.ms * 1e-3,
+                     "device_s": st.device_ms * 1e-3, "wall_s": wall,
+                     "cell_iterations_per_s": ncells * info.iterations / (st.device_ms * 1e-3),
+                     "sweep_threads": tuned, "sweep_shape": b.sweep_shape()}
+        b.close()
+    out["mixed_speedup"] = out["fp64"]["device_s"] / out["mixed"]["device_s"]
+    out["mixed_vs_fp64_state_max_rel_err"] = max(
+        float(np.abs(a - b).max() / np.abs(b).max())
+        for a, b in zip(states["mixed"], states["fp64"]))
+    if not args.no_cpu_baseline and int(os.environ.get("RANK", "0")) == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        threads = os.cpu_count() or 1
+        orc = Oracle(setup, threads)
+        orc.iterate(1)
+        t0 = time.perf_counter()
+        orc.iterate(10)
+        dt = (time.perf_counter() - t0) / 10
+        out["cpu_baseline"] = {"value": ncells / dt, "unit": METRIC, "cores": min(2, threads),
+                               "kind": "port", "s_per_iteration": dt,
+                               "projected_time_to_converge_s": dt * out["fp64"]["iterations"],
+                               "sample": "10 iterations after 1 warm-up; oracle, OpenMP over "
+                                         "the two blocks"}
         orc.close()
     return out
 
@@ -493,6 +553,9 @@ def main():
                     help="half laminar / half SST-2003 requests, or half Euler / half laminar")
     ap.add_argument("--sst-steps", type=int, default=20,
                     help="iterations of the SST flat plate section (0 skips it)")
+    ap.add_argument("--plate-drop", type=float, default=1e-8,
+                    help="residual drop of the laminar plate section (0 skips it)")
+    ap.add_argument("--plate-max", type=int, default=20000)
     ap.add_argument("--sst-ni", type=int, default=256)
     ap.add_argument("--sst-nj", type=int, default=192)
     ap.add_argument("--sst-nk", type=int, default=4)
@@ -569,19 +632,21 @@ def main():
             "cells": ncells, "solves": nsolves, "setup_s": t_setup,
             "gpu_launches": fp["gpu_launches"], "clocks": fp["clocks"],
             "e2e": fp["e2e"], "roofline": roof, "kernel_ms": km,
-            "autotune": {"sweep_threads": fp["sweep_threads"]}}
+            "autotune": {"sweep_threads": fp["sweep_threads"], "sweep_shape": fp["sweep_shape"]}}
     if "mixed" in res and "fp64" in res:
         m = res["mixed"]
         line["mixed"] = {"value": m["value"], "ms_per_step": m["ms_per_step"],
                          "speedup_vs_fp64": m["value"] / fp["value"], "e2e": m["e2e"],
                          "kernel_ms": m["kernel_ms"], "gpu_launches": m["gpu_launches"],
-                         "sweep_threads": m["sweep_threads"]}
+                         "sweep_threads": m["sweep_threads"], "sweep_shape": m["sweep_shape"]}
     if "converge" in res:
         line["converge"] = res["converge"]
     if "served" in res:
         line["served"] = res["served"]
     if "sst" in res:
         line["sst"] = res["sst"]
+    if "plate" in res:
+        line["plate"] = res["plate"]
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
     print(json.dumps(line))

@@ -256,13 +256,19 @@ int ath_batch_set_target(ath_batch *batch, int solve, double drop, int active);
 /* Current per-solve records (nsolves entries). */
 int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
 
-/* Autotuner of the launch shapes: times `reps` graph-captured iterations for
- * each candidate CTA size of the hyperplane sweep kernels (32, 64, 128, 256;
- * small batches spread a hyperplane over more SMs with small CTAs, large
- * ones prefer larger CTAs) and keeps the fastest.  The solution, per-solve
- * counters and CFL are restored afterwards, so tuning does not advance the
- * solves.  The chosen size is written to *sweep_threads (may be NULL). */
+/* Autotuner of the LU-SGS sweep shape: times `reps` graph-captured
+ * iterations for each candidate and keeps the fastest -- one launch per
+ * hyperplane with CTAs of 32, 64, 128 or 256 threads, or the persistent
+ * sweep (one launch per pass; a thread-block cluster of 1, 2, 4 or 8 CTAs
+ * of 256 threads per solve walks the solve's hyperplanes with cluster
+ * barriers).  The solution, per-solve counters and CFL are restored
+ * afterwards, so tuning does not advance the solves.  The chosen CTA size
+ * is written to *sweep_threads (may be NULL).  A new batch starts with the
+ * persistent sweep sized to its largest hyperplane. */
 int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
+/* Current sweep shape: mode 1 persistent (cluster = CTAs per solve), 0 one
+ * launch per hyperplane (cluster = 0). */
+int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster);
 
 /* ---- serving ------------------------------------------------------------
  * A request loop over independent solves (continuous batching).  Every

@@ -2,8 +2,9 @@
 
 Tolerances (relative to the largest magnitude of the compared field):
   * FP64 path, per cell, after one iteration: 1e-12 for every field;
-  * after tens of iterations: 1e-12 for the state, time step and spectral
-    radius; 1e-10 for the residual and the implicit update, which are small
+  * after tens of iterations: 1e-12 for the state, time step and flow
+    spectral radius; 1e-10 for the residual, the implicit update and the
+    turbulence spectral radius (it carries the omega source), which are small
     differences of large fluxes once the solution converges and amplify the
     last-bit differences of pow() between CUDA and the host libm (Sutherland's
     law) and of FMA-free reordering;
@@ -113,7 +114,10 @@ def test_fp64_sst_matches_reference_fixture(ctx, name, tmp_path):
         assert rel_err(b.field(k, "DT")[..., 0], g[p + "dt"]) <= CELL_TOL
         sr = b.field(k, "SPECRAD")
         assert rel_err(sr[..., 0], g[p + "specrad"][..., 0]) <= CELL_TOL
-        assert rel_err(sr[..., 1], g[p + "specrad"][..., 1]) <= CELL_TOL
+        # the turbulence radius carries the source radius 2 beta* omega V,
+        # which amplifies last-bit differences of omega over many iterations
+        # like the residual does
+        assert rel_err(sr[..., 1], g[p + "specrad"][..., 1]) <= diff_tol
         assert _cols_err(b.field(k, "DU"), g[p + "du"]) <= diff_tol
     assert _cols_err(_l2(norms, nv=7), g["l2"]) <= NORM_TOL
     assert all(x.status == 0 for x in norms)
