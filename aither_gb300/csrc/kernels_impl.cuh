@@ -1109,77 +1109,115 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
   SweepScalarQ<T, FULL>(P, sv, it.x, forward, sweep);
 }
 
-// Block version: A^-1 is the 5x5 inverse (2x2 for the turbulence rows),
-// products by ArrayMultiplication.
+// Block version, one 8-lane group per cell: lanes 0-4 own the flow rows,
+// lanes 5-6 the k and omega rows of SST solves.  Each lane forms its row of
+// the off-diagonal products (stored Jacobian row times the neighbour's
+// update, neighbours i, j, k) and of b + L - U, the group exchanges those by
+// warp shuffles, and each lane forms its row of A^-1 (...) -- the sums of
+// MatVec5/MatVec2 row by row, so the result is that of the whole-cell form.
+// A plane's cells spread over five times as many threads, and SMs, which is
+// what the FP64 rate of small planes needs.  Every lane of the warp must
+// call this (the shuffles name the whole warp); `valid` marks lanes of a
+// group that owns a cell of this solve and pass.
 template <typename T>
-__device__ __forceinline__ void SweepBlockQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
-                                            int forward, int sweep) {
-  const bool full = sweep > 0 || sv.sweeps > 1;
-  const Gas<T> g = GasOf<T>(sv);
-  const int64_t nq = P.nq;
-  const T thetaInv = (T)(1.0 / sv.theta);
-  T acc[5], in[5], x[5], acct[2], int_[2], xt[2];
-  OffDiagSumBlock(P, sv, q, forward != 0, acc, acct);
-  T Ai[kJac], Ait[4];
+__device__ __forceinline__ T BlockRowOffDiag(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                             bool lower, int row) {
+  const int64_t nq = P.nq, ng = P.nghost;
+  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+  const int side = lower ? 0 : 1;
+  const bool turb = row >= 5;
+  const int r = turb ? row - 5 : row;
+  int32_t nb[3];
 #pragma unroll
-  for (int e = 0; e < kJac; ++e) Ai[e] = P.Ainvq[e * nq + q];
-  if (sv.rans)
+  for (int d = 0; d < 3; ++d) nb[d] = nbq[d * nq + q];
+  T du[3][5];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) Ait[e] = P.Ainvtq[e * nq + q];
-  if (full) {
-    T other[5], othert[2];
-    OffDiagSumBlock(P, sv, q, forward == 0, other, othert);
+  for (int d = 0; d < 3; ++d) {
+    if (nb[d] == -1) continue;
+    const int nv = turb ? 2 : 5;
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T bv = -thetaInv * P.Rq[v * nq + q];
-      in[v] = forward ? bv + (acc[v] - other[v]) : (bv + other[v]) - acc[v];
-    }
-    MatVec5(Ai, in, x);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
-    if (sv.rans) {
-#pragma unroll
-      for (int v = 0; v < 2; ++v) {
-        const T bv = -thetaInv * P.Rtq[v * nq + q];
-        int_[v] = forward ? bv + (acct[v] - othert[v]) : (bv + othert[v]) - acct[v];
+      if (v >= nv) break;
+      if (nb[d] >= 0)
+        du[d][v] = turb ? P.dUtq[v * nq + nb[d]] : P.dUq[v * nq + nb[d]];
+      else {
+        const int64_t slot = -(int64_t)nb[d] - 2;
+        du[d][v] = turb ? P.dUtg[v * ng + slot] : P.dUg[v * ng + slot];
       }
-      MatVec2(Ait, int_, xt);
-      P.dUtq[q] = xt[0];
-      P.dUtq[nq + q] = xt[1];
-    }
-  } else if (forward) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q] + acc[v];
-    MatVec5(Ai, in, x);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = x[v];
-    if (sv.rans) {
-#pragma unroll
-      for (int v = 0; v < 2; ++v) int_[v] = -thetaInv * P.Rtq[v * nq + q] + acct[v];
-      MatVec2(Ait, int_, xt);
-      P.dUtq[q] = xt[0];
-      P.dUtq[nq + q] = xt[1];
-    }
-  } else {
-    MatVec5(Ai, acc, x);
-#pragma unroll
-    for (int v = 0; v < 5; ++v) P.dUq[v * nq + q] = P.dUq[v * nq + q] - x[v];
-    if (sv.rans) {
-      MatVec2(Ait, acct, xt);
-      P.dUtq[q] = P.dUtq[q] - xt[0];
-      P.dUtq[nq + q] = P.dUtq[nq + q] - xt[1];
     }
   }
+  T acc = T(0);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (nb[d] == -1) continue;
+    T s = T(0);
+    if (turb) {
+      const T *Jt = P.Jtoff + ((int64_t)(side * 3 + d) * 4 + r * 2) * nq + q;
+      s = s + Jt[0] * du[d][0];
+      s = s + Jt[nq] * du[d][1];
+    } else {
+      const T *J = P.Joff + ((int64_t)(side * 3 + d) * kJac + r * 5) * nq + q;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) s = s + J[c * nq] * du[d][c];
+    }
+    acc = acc + s;
+  }
+  return acc;
 }
+
+template <typename T>
+__device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                              bool valid, int row, int forward, int sweep) {
+  const int64_t nq = P.nq;
+  const bool full = sweep > 0 || sv.sweeps > 1;
+  const T thetaInv = (T)(1.0 / sv.theta);
+  const int lane = (int)(threadIdx.x & 31), g0 = lane & ~7;
+  const bool turb = row == 5 || row == 6;
+  const bool mine = valid && (row < 5 || (turb && sv.rans));
+  T in = T(0);
+  if (mine) {
+    const T acc = BlockRowOffDiag(P, sv, q, forward != 0, row);
+    const T bv = -thetaInv * (turb ? P.Rtq[(row - 5) * nq + q] : P.Rq[row * nq + q]);
+    if (full) {
+      const T other = BlockRowOffDiag(P, sv, q, forward == 0, row);
+      in = forward ? bv + (acc - other) : (bv + other) - acc;
+    } else {
+      in = forward ? bv + acc : acc;
+    }
+  }
+  T v5[5], v2[2];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) v5[c] = __shfl_sync(0xffffffffu, in, g0 + c);
+#pragma unroll
+  for (int c = 0; c < 2; ++c) v2[c] = __shfl_sync(0xffffffffu, in, g0 + 5 + c);
+  if (!mine) return;
+  T x = T(0);
+  if (turb) {
+    const int r = row - 5;
+    x = x + P.Ainvtq[(r * 2) * nq + q] * v2[0];
+    x = x + P.Ainvtq[(r * 2 + 1) * nq + q] * v2[1];
+    T *dst = P.dUtq + r * nq + q;
+    *dst = (full || forward) ? x : *dst - x;
+  } else {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) x = x + P.Ainvq[(row * 5 + c) * nq + q] * v5[c];
+    T *dst = P.dUq + row * nq + q;
+    *dst = (full || forward) ? x : *dst - x;
+  }
+}
+
+// one plane of every block solve: thread 8 c + r handles row r of item c
 template <typename T>
 __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
                                                 int forward, int sweep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_items) return;
-  const int2 it = items[t];
+  const int c = t >> 3, row = t & 7;
+  bool valid = c < n_items;
+  int2 it = make_int2(0, 0);
+  if (valid) it = items[c];
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
-  if (!sv.block || sv.jacobi || !sv.active || sweep >= sv.sweeps) return;
-  SweepBlockQ<T>(P, sv, it.x, forward, sweep);
+  valid = valid && sv.block && !sv.jacobi && sv.active && sweep < sv.sweeps;
+  SweepBlockRow<T>(P, sv, it.x, valid, row, forward, sweep);
 }
 
 // Persistent sweep: one thread-block cluster per solve walks the solve's
@@ -1208,11 +1246,14 @@ __global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
   for (int k = 0; k < nst; ++k) {
     const int p = forward ? k : nst - 1 - k;
     const int a = step_off[base + p], b = step_off[base + p + 1];
-    for (int i = a + tid; i < b; i += nthr) {
-      if constexpr (BLOCK)
-        SweepBlockQ<T>(P, sv, items[i].x, forward, sweep);
-      else
-        SweepScalarQ<T, FULL>(P, sv, items[i].x, forward, sweep);
+    if constexpr (BLOCK) {
+      // 8-lane groups; every lane runs the same number of rounds
+      for (int i0 = a; i0 < b; i0 += nthr >> 3) {
+        const int i = i0 + (tid >> 3);
+        SweepBlockRow<T>(P, sv, i < b ? items[i].x : 0, i < b, tid & 7, forward, sweep);
+      }
+    } else {
+      for (int i = a + tid; i < b; i += nthr) SweepScalarQ<T, FULL>(P, sv, items[i].x, forward, sweep);
     }
     cluster.sync();
   }
@@ -2072,7 +2113,10 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, 
     if (full) k_sweep<T, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
     else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
-  if (kinds & 2) k_sweepb<T><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+  if (kinds & 2) {
+    const unsigned gridb = (unsigned)(((int64_t)n * 8 + threads - 1) / threads);
+    k_sweepb<T><<<gridb, threads, 0, s>>>(P, items, n, forward, sweep);
+  }
 }
 template <typename T, bool FULL, bool BLOCK>
 static void LaunchSweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,
