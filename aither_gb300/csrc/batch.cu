@@ -1340,7 +1340,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   // default sweep shape: the persistent sweep with a cluster wide enough for
   // the largest plane (at most 8 CTAs of 256 threads), when launchable
   if (c.skinds) {
-    const int want = std::min(8, std::max(1, (c.L.max_plane + 255) / 256));
+    const int lanes = (c.skinds & 2) ? 8 : 1;  // block sweeps: 8 lanes per cell
+    const int want = std::min(8, std::max(1, (c.L.max_plane * lanes + 255) / 256));
     for (int cl = want; cl >= 1; --cl)
       if (B->run->MaxClusters(c.skinds, 256, cl) > 0) {
         c.sweep_mode = 1;

@@ -336,8 +336,39 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
                      (U)wd[c + s]};
     const U wu[5] = {(U)wd[c + 2 * s], (U)wd[c + s], (U)wd[c], (U)wd[c - s],
                      (U)wd[c - 2 * s]};
-    L = Weno(wm3, wm2, wm1, w0, wp1, wl, z);
-    R = Weno(wp2, wp1, w0, wm1, wm2, wu, z);
+    // the interpolation weights depend on the widths only: one set per side
+    // serves the flow variables and k, omega
+    const WenoCoeffs<U> kl = MakeWeno(wl), ku = MakeWeno(wu);
+    L = Weno(kl, wm3, wm2, wm1, w0, wp1, wl, z);
+    R = Weno(ku, wp2, wp1, w0, wm1, wm2, wu, z);
+    if (ft) {
+      // k and omega with the same weights, then their fluxes
+      const double *Wt = P.Wt;
+      auto kt = [&](int64_t x, int q) { return (U)Wt[q * n + x]; };
+      U Lt[2], Rt[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        Lt[q] = Weno1(kl, wl, kt(c - 3 * s, q), kt(c - 2 * s, q), kt(c - s, q), kt(c, q),
+                      kt(c + s, q), z);
+        Rt[q] = Weno1(ku, wu, kt(c + 2 * s, q), kt(c + s, q), kt(c, q), kt(c - s, q),
+                      kt(c - 2 * s, q), z);
+      }
+      const double *fa = P.fa[D];
+      const U nx = (U)fa[c], ny = (U)fa[n + c], nz = (U)fa[2 * n + c];
+      U vlr[2];
+      if (sv.flux == ATH_FLUX_AUSM) {
+        AusmFlux(L, R, g, nx, ny, nz, f, vlr);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          ft[q] = L.rho * vlr[0] * Lt[q];
+          ft[q] += R.rho * vlr[1] * Rt[q];
+        }
+      } else {
+        RoeFlux(L, R, g, nx, ny, nz, f);
+        RoeTurbFlux(L, R, Lt, Rt, g, nx, ny, nz, ft);
+      }
+      return;
+    }
   }
   const double *fa = P.fa[D];
   const U nx = (U)fa[c], ny = (U)fa[n + c], nz = (U)fa[2 * n + c];

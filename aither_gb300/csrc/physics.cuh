@@ -431,10 +431,10 @@ __device__ __forceinline__ T Weno1(const WenoCoeffs<T> &k, const T w[5], T y3, T
   return n0 * st0 + n1 * st1 + n2 * st2;
 }
 template <typename T>
-__device__ __forceinline__ Prim<T> Weno(const Prim<T> &u3, const Prim<T> &u2,
-                                        const Prim<T> &u1, const Prim<T> &d1,
-                                        const Prim<T> &d2, const T w[5], bool wenoz) {
-  const WenoCoeffs<T> k = MakeWeno(w);
+__device__ __forceinline__ Prim<T> Weno(const WenoCoeffs<T> &k, const Prim<T> &u3,
+                                        const Prim<T> &u2, const Prim<T> &u1,
+                                        const Prim<T> &d1, const Prim<T> &d2, const T w[5],
+                                        bool wenoz) {
   Prim<T> o;
   o.rho = Weno1(k, w, u3.rho, u2.rho, u1.rho, d1.rho, d2.rho, wenoz);
   o.u = Weno1(k, w, u3.u, u2.u, u1.u, d1.u, d2.u, wenoz);

@@ -182,7 +182,7 @@ def run_native(args, rank: int, world: int, device: int):
         out["converge"] = run_converge(args, ctx, setup, specs, world)
     if args.sst_steps > 0:
         out["sst"] = run_sst(args, ctx, world)
-    if args.plate_drop > 0:
+    if args.plate_iters > 0:
         out["plate"] = run_plate(args, ctx, world)
     if args.served_n > 0:
         out["served"] = {"definition": "latency = submit to retirement (host clock), "
@@ -325,10 +325,12 @@ def run_plate(args, ctx, world):
     """Laminar flat plate, two 128x64x2 blocks joined by an interblock
     connection (first cell 1e-5, growth 1.08, Mach 0.3, Re_L 1e5, van
     Albada, Roe, block LU-SGS with 4 sweeps; with one sweep the reference
-    itself turns nonphysical at CFL 100): one solve run to a `plate_drop` drop of its
-    total L2 in FP64 and in mixed precision.  Reports device time to
-    retirement, iterations, the mixed state's error against FP64 and, on
-    rank 0, the oracle's time per iteration on the same case."""
+    itself turns nonphysical at CFL 100): `plate_iters` iterations in FP64
+    and in mixed precision after autotuning.  The case's residual stalls
+    near a 0.3 drop (a limit cycle, the same in the reference), so the
+    section reports time per iteration rather than time to a drop, the
+    mixed state's deviation from FP64 after the run and, on rank 0, the
+    oracle's time per iteration."""
     import numpy as np
 
     from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Setup, cases
@@ -337,24 +339,25 @@ def run_plate(args, ctx, world):
         setup = Setup(inp)
     _, _, ncells = setup.counts()
     out = {"workload": "laminar flat plate, two 128x64x2 blocks, interblock, block LU-SGS "
-                       "with 4 sweeps, CFL 100", "cells": ncells, "drop": args.plate_drop}
+                       "with 4 sweeps, CFL 100", "cells": ncells, "iterations": args.plate_iters}
     states = {}
     for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
         b = Batch(ctx, setup, prec)
         tuned = b.autotune(2)
         _barrier(world)
-        t0 = time.time()
-        info = b.converge(args.plate_max, args.plate_drop, check_every=200)[0]
-        wall = time.time() - t0
+        norms = b.iterate(args.plate_iters)
         st = b.stats()
         states[name] = [b.field(k, "STATE") for k in range(2)]
-        out[name] = {"converged": int(info.converged), "iterations": int(info.iterations),
-                     "drop": info.drop, "time_to_converge_s": info.ms * 1e-3,
-                     "device_s": st.device_ms * 1e-3, "wall_s": wall,
-                     "cell_iterations_per_s": ncells * info.iterations / (st.device_ms * 1e-3),
+        l2 = np.array([[x.l2[v] for v in range(5)] for x in norms])
+        tot = np.sqrt((l2 ** 2).sum(axis=1))
+        ms = _max_over_ranks(st.device_ms, world)
+        out[name] = {"ms_per_iteration": ms / args.plate_iters,
+                     "cell_iterations_per_s": ncells * args.plate_iters * world / (ms * 1e-3),
+                     "drop": float(tot[-1] / tot[:5].max()),
+                     "status_ok": all(x.status == 0 for x in norms),
                      "sweep_threads": tuned, "sweep_shape": b.sweep_shape()}
         b.close()
-    out["mixed_speedup"] = out["fp64"]["device_s"] / out["mixed"]["device_s"]
+    out["mixed_speedup"] = out["fp64"]["ms_per_iteration"] / out["mixed"]["ms_per_iteration"]
     out["mixed_vs_fp64_state_max_rel_err"] = max(
         float(np.abs(a - b).max() / np.abs(b).max())
         for a, b in zip(states["mixed"], states["fp64"]))
@@ -368,8 +371,7 @@ def run_plate(args, ctx, world):
         orc.iterate(10)
         dt = (time.perf_counter() - t0) / 10
         out["cpu_baseline"] = {"value": ncells / dt, "unit": METRIC, "cores": min(2, threads),
-                               "kind": "port", "s_per_iteration": dt,
-                               "projected_time_to_converge_s": dt * out["fp64"]["iterations"],
+                               "kind": "port", "ms_per_iteration": dt * 1e3,
                                "sample": "10 iterations after 1 warm-up; oracle, OpenMP over "
                                          "the two blocks"}
         orc.close()
@@ -553,9 +555,8 @@ def main():
                     help="half laminar / half SST-2003 requests, or half Euler / half laminar")
     ap.add_argument("--sst-steps", type=int, default=20,
                     help="iterations of the SST flat plate section (0 skips it)")
-    ap.add_argument("--plate-drop", type=float, default=1e-8,
-                    help="residual drop of the laminar plate section (0 skips it)")
-    ap.add_argument("--plate-max", type=int, default=20000)
+    ap.add_argument("--plate-iters", type=int, default=500,
+                    help="iterations of the laminar plate section (0 skips it)")
     ap.add_argument("--sst-ni", type=int, default=256)
     ap.add_argument("--sst-nj", type=int, default=192)
     ap.add_argument("--sst-nk", type=int, default=4)
