@@ -215,7 +215,14 @@ def bump_nodes(ni: int, nj: int, nk: int, height: float, length: float = 3.0,
 def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: float,
                  cfl: float = 20.0, name: str = "bump", recon: str = "thirdOrder",
                  limiter: str = "minmod", flux: str = "roe", matrix_solver: str = "lusgs",
-                 sweeps: int = 1):
+                 sweeps: int = 1, inflow: str = "characteristic",
+                 outflow: str = "characteristic", back_pressure: float = 1.0):
+    """Inviscid channel over a sin^2 bump.  Inflow at i = 0 and outflow at
+    i = ni are characteristic far fields, or (inflow "stagnation") a
+    stagnation inlet at the freestream's total pressure and temperature
+    along +x, (inflow "inlet") the reference's inlet boundary with the
+    freestream state, and (outflow "pressure") a pressure outlet at
+    back_pressure times the freestream pressure."""
     os.makedirs(outdir, exist_ok=True)
     nodes = bump_nodes(ni, nj, nk, height)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
@@ -226,8 +233,22 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
     ic = f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; velocity={vel})"
     states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; "
               f"velocity={vel})"]
-    bcs = [[("characteristic", 0, 0, 0, nj, 0, nk, 1),
-            ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+    in_bc, out_bc = ("characteristic", 0, 0, 0, nj, 0, nk, 1), ("characteristic", ni, ni, 0, nj,
+                                                                  0, nk, 1)
+    ratio = 1.0 + 0.5 * (GAMMA - 1.0) * mach * mach
+    if inflow == "stagnation":
+        p0, t0 = p_inf * ratio ** (GAMMA / (GAMMA - 1.0)), t_inf * ratio
+        states.append(f"stagnationInlet(tag=3; p0={_fmt(p0)}; t0={_fmt(t0)}; "
+                      "direction=[1, 0, 0])")
+        in_bc = ("stagnationInlet", 0, 0, 0, nj, 0, nk, 3)
+    elif inflow == "inlet":
+        states.append(f"inlet(tag=3; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; "
+                      f"velocity={vel})")
+        in_bc = ("inlet", 0, 0, 0, nj, 0, nk, 3)
+    if outflow == "pressure":
+        states.append(f"pressureOutlet(tag=4; pressure={_fmt(back_pressure * p_inf)})")
+        out_bc = ("pressureOutlet", ni, ni, 0, nj, 0, nk, 4)
+    bcs = [[in_bc, out_bc,
             ("slipWall", 0, ni, 0, 0, 0, nk, 2),
             ("slipWall", 0, ni, nj, nj, 0, nk, 2),
             ("slipWall", 0, ni, 0, nj, 0, 0, 2),
@@ -268,9 +289,12 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
                  mach: float, alpha: float = 0.0, viscous: bool = False,
                  reynolds: float = 1e5, stretch: float = 1.0, cfl: float = 20.0,
                  name: str = "chan", precision_note: str = "", rans: bool = False,
-                 tint: float = 0.001, vratio: float = 10.0):
+                 tint: float = 0.001, vratio: float = 10.0, inflow: str = "characteristic",
+                 outflow: str = "characteristic", back_pressure: float = 1.0):
     """Bump or wedge channel with free-stream Mach `mach` at angle of attack
-    `alpha` (degrees, in the x-y plane); characteristic in- and outflow,
+    `alpha` (degrees, in the x-y plane); characteristic in- and outflow
+    (or a stagnation inlet at the free stream's total state and a pressure
+    outlet at back_pressure times its pressure),
     slip upper and side walls; the lower wall is a slip wall (Euler) or an
     adiabatic viscous wall (laminar Navier-Stokes, or SST-2003 RANS with
     `rans`; density from Re based on the unit chord and Sutherland's
@@ -299,8 +323,18 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
     if viscous:
         states.append("viscousWall(tag=3)")
         lower = ("viscousWall", 0, ni, 0, 0, 0, nk, 3)
-    bcs = [[("characteristic", 0, 0, 0, nj, 0, nk, 1),
-            ("characteristic", ni, ni, 0, nj, 0, nk, 1),
+    in_bc, out_bc = ("characteristic", 0, 0, 0, nj, 0, nk, 1), ("characteristic", ni, ni, 0, nj,
+                                                                  0, nk, 1)
+    ratio = 1.0 + 0.5 * (GAMMA - 1.0) * mach * mach
+    if inflow == "stagnation":
+        p0, t0 = p_inf * ratio ** (GAMMA / (GAMMA - 1.0)), t_inf * ratio
+        states.append(f"stagnationInlet(tag=5; p0={_fmt(p0)}; t0={_fmt(t0)}; "
+                      f"direction=[{_fmt(ca)}, {_fmt(sa)}, 0]{turb})")
+        in_bc = ("stagnationInlet", 0, 0, 0, nj, 0, nk, 5)
+    if outflow == "pressure":
+        states.append(f"pressureOutlet(tag=6; pressure={_fmt(back_pressure * p_inf)})")
+        out_bc = ("pressureOutlet", ni, ni, 0, nj, 0, nk, 6)
+    bcs = [[in_bc, out_bc,
             lower,
             ("slipWall", 0, ni, nj, nj, 0, nk, 2),
             ("slipWall", 0, ni, 0, nj, 0, 0, 2),
@@ -381,12 +415,14 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                name: str = "plate", matrix_solver: str = "lusgs", recon: str = "thirdOrder",
                sweeps: int = 1, rans: bool = False, tint: float = 0.001, vratio: float = 10.0,
                flux: str = "roe", nblocks: int = 2, dy_max: float | None = None,
-               lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0):
+               lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0,
+               wall_q: float | None = None):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
     the x-y plane, slip walls in z.  Freestream density from Re_L with
-    Sutherland's law at t_inf.  One block (nblocks=1) may start `lead` ahead
+    Sutherland's law at t_inf; a wall heat flux wall_q (W/m^2) instead of an
+    adiabatic or isothermal wall.  One block (nblocks=1) may start `lead` ahead
     of the leading edge, with a slip wall (symmetry plane) on y = 0 there.
     The CFL ramps from cfl_start by cfl_step per iteration up to cfl."""
     os.makedirs(outdir, exist_ok=True)
@@ -403,7 +439,9 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
     turb = f"; turbulenceIntensity={_fmt(tint)}; eddyViscosityRatio={_fmt(vratio)}" if rans else ""
     ic = (f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel}"
           f"{turb})")
-    wall = "viscousWall(tag=2)" if wall_t is None else f"viscousWall(tag=2; temperature={_fmt(wall_t)})"
+    wall = ("viscousWall(tag=2)" if wall_t is None and wall_q is None
+            else f"viscousWall(tag=2; temperature={_fmt(wall_t)})" if wall_t is not None
+            else f"viscousWall(tag=2; heatFlux={_fmt(wall_q)})")
     states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
               f"velocity={vel}{turb})", wall]
     blk0 = [("characteristic", 0, 0, 0, nj, 0, nk, 1),

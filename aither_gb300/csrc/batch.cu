@@ -433,9 +433,8 @@ class Runner : public RunnerBase {
     }
     Check(cudaMemcpy(P_.W, W.data(), W.size() * 8, cudaMemcpyHostToDevice), "upload");
     if (c.any_rans) {
-      // k, omega of the initial state and the wall distance (0 outside
-      // RANS solves)
-      std::vector<double> Wt(2 * n, 0.0), wd(n, 0.0);
+      // k, omega of the initial state (0 outside RANS solves)
+      std::vector<double> Wt(2 * n, 0.0);
       for (int bi = 0; bi < c.nblocks; ++bi) {
         const Block &b = c.setup->blocks[bi];
         if (b.nv < 7) continue;
@@ -443,10 +442,19 @@ class Runner : public RunnerBase {
         for (int64_t x = 0; x < b.NCell(); ++x) {
           Wt[o + x] = b.state0[x * b.nv + 5];
           Wt[n + o + x] = b.state0[x * b.nv + 6];
-          if (!b.wall_dist.empty()) wd[o + x] = b.wall_dist[x];
         }
       }
       Check(cudaMemcpy(P_.Wt, Wt.data(), Wt.size() * 8, cudaMemcpyHostToDevice), "upload");
+    }
+    if (c.L.any_viscous) {
+      // wall distance (SST sources and wall omega, heat-flux walls)
+      std::vector<double> wd(n, 0.0);
+      for (int bi = 0; bi < c.nblocks; ++bi) {
+        const Block &b = c.setup->blocks[bi];
+        const int64_t o = c.cell0[bi];
+        if (!b.wall_dist.empty())
+          for (int64_t x = 0; x < b.NCell(); ++x) wd[o + x] = b.wall_dist[x];
+      }
       P_.wd = m.Upload(wd);
     }
     P_.vol = m.Upload(vol);

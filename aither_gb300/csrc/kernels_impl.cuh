@@ -182,6 +182,17 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       const double tGhost = 2.0 * bs.wall_t - Temperature(in, gas);
       const double rho = g.p / ((0.0 + 1.0 * gas.r) * tGhost);
       g.rho = rho * (in.rho / in.rho);
+    } else if (bs.heat_flux) {
+      // constant heat flux, low-Re (src/ghostStates.cpp:230-241): the
+      // temperature gradient q / kappa over twice the wall distance of the
+      // wall-adjacent cell; kappa = EffectiveConductivity of the interior
+      const Gas<double> gas = GasOf<double>(sv);
+      const double t = Temperature(in, gas);
+      const double kappa =
+          SutherlandRatio(t, sv.t_ref, sv.k_c1, sv.k_s, sv.k_ref) * sv.visc_scale;
+      const double tGhost = Temperature(in, gas) - bs.wall_q / kappa * 2.0 * P.wd[op.src2];
+      const double rho = g.p / ((0.0 + 1.0 * gas.r) * tGhost);
+      g.rho = rho * (in.rho / in.rho);
     }
     if (rans) {
       // low-Re wall (src/ghostStates.cpp:262-275): k = 0 and omega =
@@ -264,6 +275,113 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
         hold((double)op.layer);
         if (rans)
           FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+      }
+    } else if (op.type == ATH_BC_PRESSURE_OUTLET) {
+      // src/ghostStates.cpp:605-672, reflecting form: the boundary pressure
+      // with the outgoing characteristics of the interior; the interior
+      // state where the ghost's normal Mach number reaches 1; then linear
+      // extrapolation of every variable
+      const ath_bc_state bs = P.states[sv.state0 + op.state];
+      const double sosInt = SoS(in, gas);
+      const double rhoSoSInt = in.rho * sosInt;
+      g.p = bs.p_out;
+      const double deltaPressure = in.p - g.p;
+      const double rho = in.rho - deltaPressure / (sosInt * sosInt);
+      g.rho = rho * (in.rho / in.rho);
+      g.u = in.u + nx * deltaPressure / rhoSoSInt;
+      g.v = in.v + ny * deltaPressure / rhoSoSInt;
+      g.w = in.w + nz * deltaPressure / rhoSoSInt;
+      if (Dot(g.u, g.v, g.w, nx, ny, nz) / SoS(g, gas) >= 1.0) g = in;
+      auto extrap = [&](double f) {
+        g.rho = f * g.rho - in.rho;
+        g.u = f * g.u - in.u;
+        g.v = f * g.v - in.v;
+        g.w = f * g.w - in.w;
+        g.p = f * g.p - in.p;
+        if (rans) {
+          gt[0] = f * gt[0] - tin[0];
+          gt[1] = f * gt[1] - tin[1];
+        }
+      };
+      extrap(2.0);
+      if (op.layer > 1) extrap((double)op.layer);
+    } else if (op.type == ATH_BC_STAGNATION_INLET) {
+      // src/ghostStates.cpp:535-604: the outgoing Riemann invariant and the
+      // inflow angle give the boundary speed of sound; temperature,
+      // pressure and speed follow from the stagnation values (isentropic),
+      // along the prescribed direction; extrapolated with the hold rule
+      const ath_bc_state bs = P.states[sv.state0 + op.state];
+      const double gm1 = gas.Gamma() - 1.0;
+      const double vn = Dot(in.u, in.v, in.w, nx, ny, nz);
+      const double sosInt = SoS(in, gas);
+      const double rNeg = vn - 2.0 * sosInt / gm1;
+      const double cosTheta = -1.0 * vn / VelMag(in);
+      const double stagSoSsq = sosInt * sosInt + 0.5 * gm1 * Dot(in.u, in.v, in.w, in.u, in.v, in.w);
+      const double sosB = -1.0 * rNeg * gm1 / (gm1 * cosTheta * cosTheta + 2.0) *
+                          (1.0 + cosTheta * sqrt((gm1 * cosTheta * cosTheta + 2.0) * stagSoSsq /
+                                                     (gm1 * rNeg * rNeg) -
+                                                 0.5 * gm1));
+      const double tb = bs.t0 * (sosB * sosB / stagSoSsq);
+      const double pb = bs.p0 * pow(sosB * sosB / stagSoSsq, gas.Gamma() / gm1);
+      const double vbMag = sqrt(2.0 / gm1 * (bs.t0 - tb));
+      const double rhoGhost = pb / ((0.0 + 1.0 * gas.r) * tb);
+      g.rho = rhoGhost * 1.0;
+      g.u = vbMag * bs.dir[0];
+      g.v = vbMag * bs.dir[1];
+      g.w = vbMag * bs.dir[2];
+      g.p = pb;
+      if (rans)
+        FarfieldTurb(g, g.u, g.v, g.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+      auto hold = [&](double f) {
+        const bool applies = f * g.rho - in.rho > 0.0;
+        g = ExtrapHold(g, f, in);
+        if (rans && applies) {
+          gt[0] = f * gt[0] - tin[0];
+          gt[1] = f * gt[1] - tin[1];
+        }
+      };
+      hold(2.0);
+      if (op.layer > 1) {
+        hold((double)op.layer);
+        if (rans)
+          FarfieldTurb(g, g.u, g.v, g.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+      }
+    } else if (op.type == ATH_BC_INLET) {
+      // src/ghostStates.cpp:392-493, reflecting form: the freestream state
+      // when the interior's normal Mach number reaches 1, else the incoming
+      // characteristics of the freestream and the outgoing one of the
+      // interior, extrapolated with the hold rule
+      const ath_bc_state bs = P.states[sv.state0 + op.state];
+      const Prim<double> fr{bs.rho, bs.u, bs.v, bs.w, bs.p};
+      const double velIntNorm = Dot(in.u, in.v, in.w, nx, ny, nz);
+      const double sosInt = SoS(in, gas);
+      const double machInt = fabs(velIntNorm) / sosInt;
+      if (machInt >= 1.0) {
+        g = fr;
+        if (rans)
+          FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+      } else {
+        const double rhoSoSInt = in.rho * sosInt;
+        const double dvx = fr.u - in.u, dvy = fr.v - in.v, dvz = fr.w - in.w;
+        g.p = 0.5 * (fr.p + in.p - rhoSoSInt * Dot(nx, ny, nz, dvx, dvy, dvz));
+        const double deltaPressure = fr.p - g.p;
+        const double rho = fr.rho - deltaPressure / (sosInt * sosInt);
+        g.rho = rho * (fr.rho / fr.rho);
+        g.u = fr.u - nx * deltaPressure / rhoSoSInt;
+        g.v = fr.v - ny * deltaPressure / rhoSoSInt;
+        g.w = fr.w - nz * deltaPressure / rhoSoSInt;
+        if (rans)
+          FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
+        auto hold = [&](double f) {
+          const bool applies = f * g.rho - in.rho > 0.0;
+          g = ExtrapHold(g, f, in);
+          if (rans && applies) {
+            gt[0] = f * gt[0] - tin[0];
+            gt[1] = f * gt[1] - tin[1];
+          }
+        };
+        hold(2.0);
+        if (op.layer > 1) hold((double)op.layer);
       }
     } else if (op.type == ATH_BC_SUPERSONIC_INFLOW) {
       const ath_bc_state bs = P.states[sv.state0 + op.state];

@@ -66,6 +66,7 @@ int BCType(const std::string &name) {
   if (name == "supersonicOutflow") return ATH_BC_SUPERSONIC_OUTFLOW;
   if (name == "periodic") return ATH_BC_PERIODIC;
   if (name == "interblock") return ATH_BC_INTERBLOCK;
+  if (name == "inlet") return ATH_BC_INLET;
   Fail("unsupported boundary condition type '" + name + "'");
 }
 
@@ -1347,13 +1348,18 @@ void AppendInput(Setup &st, const std::string &path) {
         s.isothermal = 1;
         s.wall_t = std::stod(m["temperature"]) / tref;
       }
-      if (m.count("heatFlux")) Fail("constant heat-flux walls are not supported");
+      if (m.count("heatFlux")) {
+        // viscousWall::Nondimensionalize (src/inputStates.cpp:775)
+        s.heat_flux = 1;
+        s.wall_q = std::stod(m["heatFlux"]) / std::pow(aref / lref, 3.0);
+      }
+      if (m.count("nonreflecting") && (m["nonreflecting"] == "true" || m["nonreflecting"] == "1"))
+        Fail("nonreflecting " + name + " boundaries need the time-accurate modes, which are "
+             "not supported");
       if (m.count("wallTreatment") && m["wallTreatment"] != "lowRe")
         Fail("wall laws are not supported");
       if (m.count("turbulenceIntensity")) s.turb_intensity = num("turbulenceIntensity", 0);
       if (m.count("eddyViscosityRatio")) s.eddy_visc_ratio = num("eddyViscosityRatio", 0);
-      if (s.type == ATH_BC_STAGNATION_INLET || s.type == ATH_BC_PRESSURE_OUTLET)
-        Fail("boundary state " + name + " is not supported yet");
     }
     sv.states_in.push_back(si);
     sv.states.push_back(s);

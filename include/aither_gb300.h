@@ -80,6 +80,7 @@ enum {
   ATH_BC_SUPERSONIC_OUTFLOW = 6,  /* supersonicOutflow */
   ATH_BC_PERIODIC = 7,            /* periodic (connection) */
   ATH_BC_INTERBLOCK = 8,          /* interblock (connection) */
+  ATH_BC_INLET = 9,               /* inlet (reflecting form) */
   /* block-edge ghost cells (procBlock::AssignInviscidGhostCellsEdge /
    * AssignViscousGhostCellsEdge): copy of src, average of src and src2,
    * or a slip-wall reflection of src across a ghost-layer face */
@@ -123,7 +124,8 @@ typedef struct {
   double rho, u, v, w, p;      /* characteristic / supersonic inflow */
   double p0, t0, dir[3];       /* stagnationInlet */
   double p_out;                /* pressureOutlet */
-  double wall_u, wall_v, wall_w, wall_t, wall_q; /* viscousWall */
+  double wall_u, wall_v, wall_w, wall_t, wall_q; /* viscousWall; wall_q is the
+                                                    heat flux over (a_ref/l_ref)^3 */
   int32_t isothermal, heat_flux;
   double turb_intensity, eddy_visc_ratio;
 } ath_bc_state;

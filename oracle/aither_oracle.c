@@ -518,15 +518,23 @@ static inline void area_vec(const oblock *b, int d, int64_t f, double *a) {
 }
 
 /* GetGhostState for viscousWall, low-Re treatment
- * (src/ghostStates.cpp:130-200, 243-266) */
+ * (src/ghostStates.cpp:130-200, 230-241, 243-266); wd is the wall distance
+ * of the wall-adjacent cell */
+static double cond_eff(double t, const ath_solve_view *v);
 static void viscous_wall_ghost(const double *in, const ath_bc_state *bs, const gas_t *g,
-                               double *out) {
+                               const ath_solve_view *v, double wd, double *out) {
   memcpy(out, in, 8 * NV);
   out[1] = 2.0 * bs->wall_u - in[1];
   out[2] = 2.0 * bs->wall_v - in[2];
   out[3] = 2.0 * bs->wall_w - in[3];
   if (bs->isothermal) {
     const double tGhost = 2.0 * bs->wall_t - temp_of(in, g);
+    const double rho = out[4] / ((0.0 + 1.0 * g->r) * tGhost);
+    out[0] = rho * (in[0] / in[0]);
+  } else if (bs->heat_flux) {
+    const double t = temp_of(in, g);
+    const double kappa = cond_eff(t, v);
+    const double tGhost = temp_of(in, g) - bs->wall_q / kappa * 2.0 * wd;
     const double rho = out[4] / ((0.0 + 1.0 * g->r) * tGhost);
     out[0] = rho * (in[0] / in[0]);
   }
@@ -1440,6 +1448,106 @@ void orc_fill_ghosts(orc_case *c) {
             extrap_hold(g, 2.0, in);
             if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
           }
+        } else if (op->type == ATH_BC_PRESSURE_OUTLET) {
+          /* src/ghostStates.cpp:605-672, reflecting form */
+          const ath_bc_state *bs = &sv->states[op->state];
+          const double sosInt = sos_of(in, &sv->gas);
+          const double rhoSoSInt = in[0] * sosInt;
+          g[4] = bs->p_out;
+          const double dp = in[4] - g[4];
+          const double rho = in[0] - dp / (sosInt * sosInt);
+          g[0] = rho * (in[0] / in[0]);
+          g[1] = in[1] + n[0] * dp / rhoSoSInt;
+          g[2] = in[2] + n[1] * dp / rhoSoSInt;
+          g[3] = in[3] + n[2] * dp / rhoSoSInt;
+          if ((g[1] * n[0] + g[2] * n[1] + g[3] * n[2]) / sos_of(g, &sv->gas) >= 1.0) {
+            memcpy(g, in, sizeof(g));
+            if (rans) {
+              gt[0] = int_[0];
+              gt[1] = int_[1];
+            }
+          }
+          for (int v = 0; v < NV; ++v) g[v] = 2.0 * g[v] - in[v];
+          if (rans)
+            for (int v = 0; v < 2; ++v) gt[v] = 2.0 * gt[v] - int_[v];
+          if (op->layer > 1) {
+            for (int v = 0; v < NV; ++v) g[v] = (double)op->layer * g[v] - in[v];
+            if (rans)
+              for (int v = 0; v < 2; ++v) gt[v] = (double)op->layer * gt[v] - int_[v];
+          }
+        } else if (op->type == ATH_BC_STAGNATION_INLET) {
+          /* src/ghostStates.cpp:535-604 */
+          const ath_bc_state *bs = &sv->states[op->state];
+          const double gm1 = gamma_of(&sv->gas) - 1.0;
+          const double vn = in[1] * n[0] + in[2] * n[1] + in[3] * n[2];
+          const double sosInt = sos_of(in, &sv->gas);
+          const double rNeg = vn - 2.0 * sosInt / gm1;
+          const double cosTheta = -1.0 * vn / velmag(in);
+          /* pow(sos, 2.0) is the correctly rounded square */
+          const double stagSoSsq =
+              sosInt * sosInt + 0.5 * gm1 * (in[1] * in[1] + in[2] * in[2] + in[3] * in[3]);
+          const double sosB = -1.0 * rNeg * gm1 / (gm1 * cosTheta * cosTheta + 2.0) *
+                              (1.0 + cosTheta * sqrt((gm1 * cosTheta * cosTheta + 2.0) *
+                                                         stagSoSsq / (gm1 * rNeg * rNeg) -
+                                                     0.5 * gm1));
+          const double tb = bs->t0 * (sosB * sosB / stagSoSsq);
+          const double pb = bs->p0 * pow(sosB * sosB / stagSoSsq, gamma_of(&sv->gas) / gm1);
+          const double vbMag = sqrt(2.0 / gm1 * (bs->t0 - tb));
+          const double rhoGhost = pb / ((0.0 + 1.0 * sv->gas.r) * tb);
+          g[0] = rhoGhost * 1.0;
+          g[1] = vbMag * bs->dir[0];
+          g[2] = vbMag * bs->dir[1];
+          g[3] = vbMag * bs->dir[2];
+          g[4] = pb;
+          if (rans) {
+            const double vel[3] = {g[1], g[2], g[3]};
+            farfield_turb(g, vel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas, &sv->v,
+                          gt);
+            extrap_hold7(g, gt, 2.0, in, int_);
+            if (op->layer > 1) {
+              extrap_hold7(g, gt, (double)op->layer, in, int_);
+              const double vel2[3] = {g[1], g[2], g[3]};
+              farfield_turb(g, vel2, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
+            }
+          } else {
+            extrap_hold(g, 2.0, in);
+            if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
+          }
+        } else if (op->type == ATH_BC_INLET) {
+          /* src/ghostStates.cpp:392-493, reflecting form */
+          const ath_bc_state *bs = &sv->states[op->state];
+          const double fr[NV] = {bs->rho, bs->u, bs->v, bs->w, bs->p};
+          const double freeVel[3] = {bs->u, bs->v, bs->w};
+          const double vin = in[1] * n[0] + in[2] * n[1] + in[3] * n[2];
+          const double sosInt = sos_of(in, &sv->gas);
+          const double machInt = fabs(vin) / sosInt;
+          if (machInt >= 1.0) {
+            memcpy(g, fr, sizeof(g));
+            if (rans)
+              farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
+          } else {
+            const double rhoSoSInt = in[0] * sosInt;
+            const double dv[3] = {fr[1] - in[1], fr[2] - in[2], fr[3] - in[3]};
+            g[4] = 0.5 * (fr[4] + in[4] -
+                          rhoSoSInt * (n[0] * dv[0] + n[1] * dv[1] + n[2] * dv[2]));
+            const double dp = fr[4] - g[4];
+            const double rho = fr[0] - dp / (sosInt * sosInt);
+            g[0] = rho * (fr[0] / fr[0]);
+            g[1] = fr[1] - n[0] * dp / rhoSoSInt;
+            g[2] = fr[2] - n[1] * dp / rhoSoSInt;
+            g[3] = fr[3] - n[2] * dp / rhoSoSInt;
+            if (rans) {
+              farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
+                            &sv->v, gt);
+              extrap_hold7(g, gt, 2.0, in, int_);
+              if (op->layer > 1) extrap_hold7(g, gt, (double)op->layer, in, int_);
+            } else {
+              extrap_hold(g, 2.0, in);
+              if (op->layer > 1) extrap_hold(g, (double)op->layer, in);
+            }
+          }
         } else if (op->type == ATH_BC_SUPERSONIC_INFLOW) {
           const ath_bc_state *bs = &sv->states[op->state];
           g[0] = bs->rho; g[1] = bs->u; g[2] = bs->v; g[3] = bs->w; g[4] = bs->p;
@@ -1602,7 +1710,8 @@ void orc_residual(orc_case *c) {
       for (int o = 0; o < b->nvops; ++o) {
         const ath_ghost_op *op = &b->vops[o];
         double gw[NV];
-        viscous_wall_ghost(&b->W[op->src * NV], &sv->states[op->state], g, gw);
+        viscous_wall_ghost(&b->W[op->src * NV], &sv->states[op->state], g, &sv->v,
+                           b->wd ? b->wd[op->src2] : 0.0, gw);
         memcpy(&b->W[op->dst * NV], gw, sizeof(gw));
         if (sv->rans) {
           /* low-Re wall: k = 0 and omega = 60 nu / (beta1 d^2) at the face

@@ -42,6 +42,7 @@ def golden_case(name, outdir):
     kw = ast.literal_eval(str(g["kwargs"]))
     base = name.split("_it")[0]
     gen = (cases.vortex_box if base.startswith("vortex")
+           else cases.wall_channel if base.startswith("sst_chan")
            else cases.flat_plate if base.startswith(("plate", "sst")) else cases.bump_channel)
     inp, st = gen(outdir, name=base, **kw)
     return inp, st, g

@@ -89,6 +89,18 @@ CASES = [
     ("sst_plate_dplur", cases.flat_plate,
      dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
           nblocks=1, cfl=20.0, matrix_solver="dplur", sweeps=2), [1, 10], True),
+    # stagnation inlet, reference inlet, pressure outlet, heat-flux wall
+    ("bump_stag_pout", cases.bump_channel,
+     dict(ni=20, nj=10, nk=3, height=0.08, mach=0.5, inflow="stagnation", outflow="pressure"),
+     [1, 20], True),
+    ("bump_inlet_pout", cases.bump_channel,
+     dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
+          back_pressure=1.02, recon="weno", limiter="none"), [1, 20], True),
+    ("plate_heatflux", cases.flat_plate,
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, wall_q=500.0), [1, 20], True),
+    ("sst_chan_stag_pout", cases.wall_channel,
+     dict(ni=16, nj=10, nk=3, kind="bump", param=0.06, mach=0.5, alpha=2.0, rans=True,
+          stretch=1.1, cfl=5.0, inflow="stagnation", outflow="pressure"), [1, 10], True),
 ]
 
 

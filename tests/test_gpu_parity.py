@@ -65,7 +65,10 @@ def _cols_err(a, b):
                                   "plate_blusgs_it1", "plate_blusgs_it20",
                                   "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20",
                                   "bump_dplur_it1", "bump_dplur_it20", "plate_bdplur_it1",
-                                  "plate_bdplur_it20"])
+                                  "plate_bdplur_it20", "bump_stag_pout_it1",
+                                  "bump_stag_pout_it20", "bump_inlet_pout_it1",
+                                  "bump_inlet_pout_it20", "plate_heatflux_it1",
+                                  "plate_heatflux_it20"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
@@ -88,7 +91,8 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
 
 SST_CASES = ["sst_plate_it1", "sst_plate_it20", "sst_plate2_blusgs_it1",
              "sst_plate2_blusgs_it10", "sst_weno_ausm_it1", "sst_weno_ausm_it10",
-             "sst_plate_dplur_it1", "sst_plate_dplur_it10"]
+             "sst_plate_dplur_it1", "sst_plate_dplur_it10", "sst_chan_stag_pout_it1",
+             "sst_chan_stag_pout_it10"]
 
 
 @pytest.mark.parametrize("name", SST_CASES)

@@ -24,7 +24,10 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "plate_blusgs_sw2_it1", "plate_blusgs_sw2_it20", "sst_plate_it1", "sst_plate_it20",
         "sst_plate2_blusgs_it1", "sst_plate2_blusgs_it10", "sst_weno_ausm_it1",
         "sst_weno_ausm_it10", "bump_dplur_it1", "bump_dplur_it20", "plate_bdplur_it1",
-        "plate_bdplur_it20", "sst_plate_dplur_it1", "sst_plate_dplur_it10"]
+        "plate_bdplur_it20", "sst_plate_dplur_it1", "sst_plate_dplur_it10",
+        "bump_stag_pout_it1", "bump_stag_pout_it20", "bump_inlet_pout_it1",
+        "bump_inlet_pout_it20", "plate_heatflux_it1", "plate_heatflux_it20",
+        "sst_chan_stag_pout_it1", "sst_chan_stag_pout_it10"]
 
 
 def _oracle(inp, st):
