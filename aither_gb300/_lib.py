@@ -54,7 +54,9 @@ class SolveView(C.Structure):
                 ("r_ref", C.c_double), ("a_ref", C.c_double), ("l_ref", C.c_double),
                 ("visc_scale", C.c_double), ("visc_cfl_coeff", C.c_double),
                 ("k_c1", C.c_double), ("k_s", C.c_double), ("k_ref", C.c_double),
-                ("nstates", C.c_int32), ("states", C.POINTER(BCState))]
+                ("nstates", C.c_int32), ("states", C.POINTER(BCState)),
+                ("dt_global", C.c_double), ("dual_cfl", C.c_double),
+                ("nl_iters", C.c_int32), ("multilevel", C.c_int32)]
 
 
 class BlockView(C.Structure):

@@ -110,7 +110,7 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         f"gridName: {grid}",
         f"equationSet: {scheme.get('equationSet', 'euler')}",
         f"turbulenceModel: {scheme.get('turbulenceModel', 'none')}",
-        "timeIntegration: implicitEuler",
+        f"timeIntegration: {scheme.get('timeIntegration', 'implicitEuler')}",
         f"cflStart: {_fmt(scheme.get('cflStart', scheme['cfl']))}",
         f"cflStep: {_fmt(scheme.get('cflStep', 0.0))}",
         f"cflMax: {_fmt(scheme['cfl'])}",
@@ -128,6 +128,9 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         f"matrixSweeps: {int(scheme.get('matrixSweeps', 1))}",
         "matrixRelaxation: 1.0",
     ]
+    for key in ("timeStep", "nonlinearIterations", "dualTimeCFL"):
+        if key in scheme:
+            body.append(f"{key}: {_fmt(scheme[key]) if isinstance(scheme[key], float) else scheme[key]}")
     if states:
         body.append("boundaryStates: <" + ",\n                 ".join(states) + ">")
     body.append(f"boundaryConditions: {len(bcs)}")
@@ -169,9 +172,24 @@ def nondimensional_prim(rho, u, v, w, p, refs: Refs) -> np.ndarray:
     return np.stack([rho / refs.r_ref, u / a, v / a, w / a, p / (refs.r_ref * a * a)], axis=-1)
 
 
+def time_keys(time: str = "implicitEuler", dt: float | None = None, nl: int = 1,
+              dual_cfl: float | None = None) -> dict:
+    """Input-file keys of the time integration: scheme (implicitEuler,
+    crankNicholson, bdf2), global time step in seconds, nonlinear iterations
+    per time step and dual-time CFL."""
+    keys = {"timeIntegration": time, "nonlinearIterations": int(nl)}
+    if dt is not None:
+        keys["timeStep"] = float(dt)
+    if dual_cfl is not None:
+        keys["dualTimeCFL"] = float(dual_cfl)
+    return keys
+
+
 def vortex_box(outdir: str, ni: int = 64, nj: int = 32, nk: int = 8,
                lx: float = 10.0, ly: float = 5.0, lz: float = 1.25,
-               cfl: float = 10.0, limiter: str = "minmod", name: str = "vortex_box"):
+               cfl: float = 10.0, limiter: str = "minmod", name: str = "vortex_box",
+               time: str = "implicitEuler", dt: float | None = None, nl: int = 1,
+               dual_cfl: float | None = None):
     os.makedirs(outdir, exist_ok=True)
     nodes = box_nodes(ni, nj, nk, lx, ly, lz)
     write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])
@@ -189,7 +207,8 @@ def vortex_box(outdir: str, ni: int = 64, nj: int = 32, nk: int = 8,
             ("slipWall", 0, ni, 0, nj, 0, 0, 5),
             ("slipWall", 0, ni, 0, nj, nk, nk, 6)]]
     inp = os.path.join(outdir, name + ".inp")
-    write_input(inp, name, {"cfl": cfl, "limiter": limiter}, refs, ic, states, bcs)
+    write_input(inp, name, {"cfl": cfl, "limiter": limiter, **time_keys(time, dt, nl, dual_cfl)},
+                refs, ic, states, bcs)
     cen = cell_centres(nodes)
     rho, u, v, w, p = isentropic_vortex(cen[0], cen[1], mach, p_inf, t_inf, 5.0, 1.0,
                                         lx / 2, ly / 2)
@@ -416,7 +435,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                sweeps: int = 1, rans: bool = False, tint: float = 0.001, vratio: float = 10.0,
                flux: str = "roe", nblocks: int = 2, dy_max: float | None = None,
                lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0,
-               wall_q: float | None = None):
+               wall_q: float | None = None, time: str = "implicitEuler",
+               dt: float | None = None, nl: int = 1, dual_cfl: float | None = None):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -461,7 +481,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
               "cflStep": cfl_step,
               "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
               "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
-              "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps}
+              "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps,
+              **time_keys(time, dt, nl, dual_cfl)}
     if nblocks == 1:
         nodes = plate_nodes(-lead, length, ni, nj, nk, dy0, ratio, dz, dy_max)
         write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])

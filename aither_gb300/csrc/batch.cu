@@ -137,6 +137,7 @@ struct BatchCore {
   }
   bool block_viscous = false;
   bool any_rans = false;  // SST solves present: k, omega pools allocated
+  bool any_unsteady = false;  // time-accurate solves: time levels kept
   int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
   int vkinds = 0;  // bit 0: laminar viscous solves, bit 1: SST
   cudaStream_t stream = nullptr;
@@ -179,7 +180,8 @@ __global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sst
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nsolves) return;
   const SolveDev sv = solves[s];
-  const double it = (double)sstate[s].iter;
+  // input::CalcCFL of the time step (src/input.cpp:647)
+  const double it = (double)(sstate[s].iter / sv.nl_iters);
   cfl[s] = fmin(sv.cfl_start + it * sv.cfl_step, sv.cfl_max);
 }
 
@@ -402,6 +404,16 @@ class Runner : public RunnerBase {
     P_.ghost_src = m.Upload(c.L.ghost_src);
     for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(double)), "memset");
     if (c.any_rans) AllocTurbulence(m, n, nq, ngh);
+    if (c.any_unsteady) {
+      P_.Un = m.Alloc<double>(7 * n);
+      P_.Unm1 = m.Alloc<double>(7 * n);
+      Check(cudaMemset(P_.Un, 0, 7 * n * sizeof(double)), "memset");
+      Check(cudaMemset(P_.Unm1, 0, 7 * n * sizeof(double)), "memset");
+      P_.Bq = m.Alloc<T>(5 * nq);
+      P_.Btq = m.Alloc<T>(2 * nq);
+      Check(cudaMemset(P_.Bq, 0, 5 * nq * sizeof(T)), "memset");
+      Check(cudaMemset(P_.Btq, 0, 2 * nq * sizeof(T)), "memset");
+    }
     // geometry and state
     std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
     for (int d = 0; d < 3; ++d) {
@@ -538,6 +550,9 @@ class Runner : public RunnerBase {
   }
   void FillGhosts() override {
     StartIteration();
+    if (c_.any_unsteady)
+      Launch<T>::StoreN(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
+                        c_.d_sstate, c_.stream);
     Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
     EdgePhases(c_.d_edge_ops, c_.d_edge_solve, c_.L.edge_phase_off);
   }
@@ -643,7 +658,7 @@ class Runner : public RunnerBase {
   }
   void Update() override {
     Launch<T>::Update(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_cell_cta_pos0,
-                      c_.d_partials, (int)c_.L.cell_cta_block.size(), c_.stream);
+                      c_.d_partials, (int)c_.L.cell_cta_block.size(), c_.d_sstate, c_.stream);
     k_norms<<<c_.nsolves, 32, 0, c_.stream>>>(c_.d_partials,
                                               (c_.flags & 1) ? c_.d_mres : nullptr,
                                               c_.d_solve_cta0, c_.nsolves, c_.d_ring,
@@ -752,6 +767,7 @@ class Runner : public RunnerBase {
     if (!snap_w_) {
       snap_w_ = m.Alloc<double>(5 * (size_t)c_.ncell);
       if (P_.Wt) snap_wt_ = m.Alloc<double>(2 * (size_t)c_.ncell);
+      if (P_.Un) snap_un_ = m.Alloc<double>(14 * (size_t)c_.ncell);
       snap_ss_ = m.Alloc<SolveState>(c_.nsolves);
       snap_sv_ = m.Alloc<SolveDev>(c_.nsolves);
       snap_cfl_ = m.Alloc<double>(c_.nsolves);
@@ -763,6 +779,10 @@ class Runner : public RunnerBase {
     if (!restore) {
       cp(snap_w_, P_.W, wbytes);
       if (P_.Wt) cp(snap_wt_, P_.Wt, wbytes / 5 * 2);
+      if (P_.Un) {
+        cp(snap_un_, P_.Un, wbytes / 5 * 7);
+        cp(snap_un_ + 7 * (size_t)c_.ncell, P_.Unm1, wbytes / 5 * 7);
+      }
       cp(snap_ss_, c_.d_sstate, c_.nsolves * sizeof(SolveState));
       cp(snap_sv_, c_.d_solves, c_.nsolves * sizeof(SolveDev));
       cp(snap_cfl_, c_.d_cfl, c_.nsolves * sizeof(double));
@@ -771,6 +791,10 @@ class Runner : public RunnerBase {
     } else {
       cp(P_.W, snap_w_, wbytes);
       if (P_.Wt) cp(P_.Wt, snap_wt_, wbytes / 5 * 2);
+      if (P_.Un) {
+        cp(P_.Un, snap_un_, wbytes / 5 * 7);
+        cp(P_.Unm1, snap_un_ + 7 * (size_t)c_.ncell, wbytes / 5 * 7);
+      }
       cp(c_.d_sstate, snap_ss_, c_.nsolves * sizeof(SolveState));
       cp(c_.d_solves, snap_sv_, c_.nsolves * sizeof(SolveDev));
       cp(c_.d_cfl, snap_cfl_, c_.nsolves * sizeof(double));
@@ -785,6 +809,8 @@ class Runner : public RunnerBase {
     m.Free(snap_w_);
     if (snap_wt_) m.Free(snap_wt_);
     snap_wt_ = nullptr;
+    if (snap_un_) m.Free(snap_un_);
+    snap_un_ = nullptr;
     m.Free(snap_ss_);
     m.Free(snap_sv_);
     m.Free(snap_cfl_);
@@ -883,7 +909,7 @@ class Runner : public RunnerBase {
 
   BatchCore &c_;
   Pools<T> P_{};
-  double *snap_w_ = nullptr, *snap_wt_ = nullptr, *snap_cfl_ = nullptr;
+  double *snap_w_ = nullptr, *snap_wt_ = nullptr, *snap_un_ = nullptr, *snap_cfl_ = nullptr;
   SolveState *snap_ss_ = nullptr;
   SolveDev *snap_sv_ = nullptr;
   int64_t *snap_it_ = nullptr, snap_iter_host_ = 0;
@@ -1186,6 +1212,7 @@ void CountLaunches(BatchCore &c) {
                                          : 0) +
                         (c.L.wall_faces.empty() ? 0 : 2) +
                         1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
+                        (c.any_unsteady ? 1 : 0) +
                         (nskinds ? 2 * per_pass * c.max_sweeps * nskinds +
                                        (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
                                  : 0) +
@@ -1263,6 +1290,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.visc_coeff = p.visc_cfl_coeff;
     x.block = IsBlockSolver(p.solver);
     x.jacobi = IsJacobiSolver(p.solver);
+    x.dt_global = p.dt_global;
+    x.dual_cfl = p.dual_cfl;
+    x.nl_iters = std::max(1, (int)p.nl_iters);
+    x.multilevel = p.multilevel;
+    x.unsteady = (p.multilevel || p.nl_iters > 1) ? 1 : 0;
+    if (x.unsteady) c.any_unsteady = true;
     x.rans = p.eqn == ATH_EQN_RANS;
     x.sweeps = p.sweeps;
     x.active = 1;

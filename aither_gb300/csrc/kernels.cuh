@@ -43,6 +43,12 @@ struct SolveDev {
   int32_t jacobi;  // dplur / bdplur: Jacobi sweeps instead of LU-SGS
   int32_t sweeps;  // matrixSweeps
   int32_t active;  // 0 once the solve is retired: its kernels skip their work
+  // time integration: global nondimensional time step (0: local from the
+  // CFL), dual-time CFL (0: none), nonlinear iterations per time step,
+  // bdf2's time n-1 level, and whether the right-hand side carries the
+  // time-level terms (multilevel or several nonlinear iterations)
+  double dt_global, dual_cfl;
+  int32_t nl_iters, multilevel, unsteady, pad5;
 };
 
 // Per-solve hyperplane lists of the persistent sweep: items (q index,
@@ -142,6 +148,11 @@ struct Pools {
   T *Joff, *Jtoff;
   // Jacobi (DP-LUR) solves: the second update buffer of the sweeps
   T *dUq2, *dUtq2;
+  // time-accurate solves: conserved state of time levels n and n-1
+  // [7][ncell] (rho, rho u, rho v, rho w, rho E, rho k, rho omega) and the
+  // linear system's right-hand side in q order ([5][nq], [2][nq])
+  double *Un, *Unm1;
+  T *Bq, *Btq;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -304,7 +315,10 @@ struct Launch {
   static void ConnDu(const Pools<T> &P, cudaStream_t s);
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,
-                     cudaStream_t s);
+                     const SolveState *ss, cudaStream_t s);
+  // StoreOldSolution of the time-accurate solves at a time step's start
+  static void StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                     int ncta, const SolveState *ss, cudaStream_t s);
   static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      double *mres_partials, int ncta, int kinds, cudaStream_t s);
   // per-face wall forces [6][n] of the viscous-wall faces

@@ -809,12 +809,40 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   }
   P.lam[c] = lam;
   if (rans) P.lamt[c] = lamt;
-  // local time step and diagonal: A = A*relax + V(1+zeta)/(dt theta)
+  // time step (global when given, else local from the CFL) and the diagonal
+  // A = A*relax + V(1+zeta)/(dt theta) [+ max radius / dual-time CFL]
+  // (CalcBlockTimeStep src/procBlock.cpp:798, AddDiagonalTerms
+  // src/linearSolver.cpp:146)
   const double cfl = P.cfl[b.solve];
   const double lmax = rans ? CMax(lam, lamt) : lam;
-  const double dt = cfl * (vol / lmax);
+  const double dt = sv.dt_global > 0.0 ? sv.dt_global : cfl * (vol / lmax);
   P.dt[c] = dt;
   const int64_t nq = P.nq;
+  double diagVolTimeD = (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+  if (sv.dual_cfl > 0.0) diagVolTimeD += (rans ? lmax : CMax(lam, 0.0)) / sv.dual_cfl;
+  if (sv.unsteady) {
+    // b = -R/theta + SolDeltaNm1 - SolDeltaMmN (procBlock::SolDeltaMmN /
+    // SolDeltaNm1, src/procBlock.cpp:1015-1034) in FP64
+    const Gas<double> gd = GasOf<double>(sv);
+    const Prim<double> wd = LoadW<double>(P.W, n, c);
+    double cn[7];
+    PrimToCons(wd, gd, cn);
+    cn[5] = rans ? wd.rho * P.Wt[c] : 0.0;
+    cn[6] = rans ? wd.rho * P.Wt[n + c] : 0.0;
+    const double thetaInvD = 1.0 / sv.theta;
+    const double coeffN = (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+    const double coeffNm1 = (vol * sv.zeta) / (dt * sv.theta);
+    const int nvs = rans ? 7 : 5;
+    for (int v = 0; v < nvs; ++v) {
+      const double un = P.Un[v * n + c];
+      const double dMmN = coeffN * (cn[v] - un);
+      const double dNm1 = sv.multilevel ? coeffNm1 * (un - P.Unm1[v * n + c]) : 0.0;
+      const double r = v < 5 ? P.R[v * n + c] : P.Rt[(v - 5) * n + c];
+      const double bb = -thetaInvD * r + dNm1 - dMmN;
+      if (v < 5) P.Bq[v * nq + q] = (T)bb;
+      else P.Btq[(v - 5) * nq + q] = (T)bb;
+    }
+  }
   if constexpr (BLOCK) {
     // 5x5 diagonal (CalcInvFluxI/J/K, CalcViscFluxI/J/K block branches,
     // src/procBlock.cpp:452-484,1417-1474): per direction, minus the
@@ -895,7 +923,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       At[2] = At[2] - T(0);
       At[3] = At[3] - (T)srcJ[1];
     }
-    const T diagVolTime = (T)((vol * (1.0 + sv.zeta)) / (dt * sv.theta));
+    const T diagVolTime = (T)diagVolTimeD;
 #pragma unroll
     for (int r = 0; r < 5; ++r) A[r * 6] *= (T)sv.relax;
 #pragma unroll
@@ -917,11 +945,11 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       for (int e = 0; e < 4; ++e) P.Ainvtq[e * nq + q] = At[e];
     }
   } else {
-    const double a = adiag * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+    const double a = adiag * sv.relax + diagVolTimeD;
     P.Ainvq[q] = (T)(1.0 / a);
     P.Aq[q] = (T)a;
     if (rans) {
-      const double at = adiagt * sv.relax + (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+      const double at = adiagt * sv.relax + diagVolTimeD;
       P.Ainvtq[q] = (T)(1.0 / at);
       P.Atq[q] = (T)at;
     }
@@ -934,6 +962,18 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   P.Wq[4 * nq + q] = w.p;
 #pragma unroll
   for (int v = 0; v < 5; ++v) P.Rq[v * nq + q] = (T)P.R[v * n + c];
+}
+
+// Right-hand side b of the linear system for equation v (flow 0-4, k and
+// omega 5-6) of q-ordered cell q: -R / theta, or for time-accurate solves
+// the value k_cell formed with the time-level terms
+// (src/linearSolver.cpp:350-352)
+template <typename T>
+__device__ __forceinline__ T RhsB(const Pools<T> &P, const SolveDev &sv, T thetaInv, int v,
+                                  int64_t q) {
+  const int64_t nq = P.nq;
+  if (sv.unsteady) return v < 5 ? P.Bq[v * nq + q] : P.Btq[(v - 5) * nq + q];
+  return -thetaInv * (v < 5 ? P.Rq[v * nq + q] : P.Rtq[(v - 5) * nq + q]);
 }
 
 // Neighbour data of an off-diagonal term: the state, laminar viscosity and
@@ -1201,7 +1241,7 @@ __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &
       OffDiagSum(P, g, sv, q, forward == 0, other, othert);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const T bv = -thetaInv * P.Rq[v * nq + q];
+        const T bv = RhsB(P, sv, thetaInv, v, q);
         const T in = forward ? bv + (acc[v] - other[v]) : (bv + other[v]) - acc[v];
         P.dUq[v * nq + q] = in * ainv;
       }
@@ -1209,7 +1249,7 @@ __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &
         const T ainvt = P.Ainvtq[q];
 #pragma unroll
         for (int v = 0; v < 2; ++v) {
-          const T bv = -thetaInv * P.Rtq[v * nq + q];
+          const T bv = RhsB(P, sv, thetaInv, 5 + v, q);
           const T in = forward ? bv + (acct[v] - othert[v]) : (bv + othert[v]) - acct[v];
           P.dUtq[v * nq + q] = in * ainvt;
         }
@@ -1220,14 +1260,14 @@ __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &
   if (forward) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T bv = -thetaInv * P.Rq[v * nq + q];
+      const T bv = RhsB(P, sv, thetaInv, v, q);
       P.dUq[v * nq + q] = (bv + acc[v]) * ainv;
     }
     if (sv.rans) {
       const T ainvt = P.Ainvtq[q];
 #pragma unroll
       for (int v = 0; v < 2; ++v) {
-        const T bv = -thetaInv * P.Rtq[v * nq + q];
+        const T bv = RhsB(P, sv, thetaInv, 5 + v, q);
         P.dUtq[v * nq + q] = (bv + acct[v]) * ainvt;
       }
     }
@@ -1326,7 +1366,7 @@ __device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev 
   T in = T(0);
   if (mine) {
     const T acc = BlockRowOffDiag(P, sv, q, forward != 0, row);
-    const T bv = -thetaInv * (turb ? P.Rtq[(row - 5) * nq + q] : P.Rq[row * nq + q]);
+    const T bv = RhsB(P, sv, thetaInv, row, q);
     if (full) {
       const T other = BlockRowOffDiag(P, sv, q, forward == 0, row);
       in = forward ? bv + (acc - other) : (bv + other) - acc;
@@ -1428,10 +1468,10 @@ __global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int
     const T thetaInv = (T)(1.0 / sv.theta);
     T in[5], int_[2];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) in[v] = -thetaInv * P.Rq[v * nq + q];
+    for (int v = 0; v < 5; ++v) in[v] = RhsB(P, sv, thetaInv, v, q);
     if (sv.rans)
 #pragma unroll
-      for (int v = 0; v < 2; ++v) int_[v] = -thetaInv * P.Rtq[v * nq + q];
+      for (int v = 0; v < 2; ++v) int_[v] = RhsB(P, sv, thetaInv, 5 + v, q);
     if (sv.block) {
       T Ai[kJac];
 #pragma unroll
@@ -1495,7 +1535,7 @@ __global__ void __launch_bounds__(128) k_jacobi(Pools<T> P, T *dst, T *dstt, con
   }
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    const T bv = -thetaInv * P.Rq[v * nq + q];
+    const T bv = RhsB(P, sv, thetaInv, v, q);
     in[v] = bv + (L[v] - U[v]);
   }
   if constexpr (BLOCK) {
@@ -1514,7 +1554,7 @@ __global__ void __launch_bounds__(128) k_jacobi(Pools<T> P, T *dst, T *dstt, con
     T int_[2], xt[2];
 #pragma unroll
     for (int v = 0; v < 2; ++v) {
-      const T bv = -thetaInv * P.Rtq[v * nq + q];
+      const T bv = RhsB(P, sv, thetaInv, 5 + v, q);
       int_[v] = bv + (Lt[v] - Ut[v]);
     }
     if constexpr (BLOCK) {
@@ -1562,13 +1602,42 @@ __global__ void k_conn_du(Pools<T> P) {
   }
 }
 
+// StoreOldSolution (src/mgSolution.cpp:103) for the time-accurate solves:
+// at a time step's first nonlinear iteration the conserved state of time
+// n, and at the first step of a bdf2 solve that of time n-1 as well
+template <typename T>
+__global__ void __launch_bounds__(kCta) k_store_n(Pools<T> P, const int32_t *list,
+                                                  const int32_t *cta_block,
+                                                  const SolveState *sstate) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const int s = P.blocks[cta_block[blockIdx.x]].solve;
+  const SolveDev sv = P.solves[s];
+  if (!sv.unsteady || !sv.active) return;
+  const int64_t it = sstate[s].iter;
+  if (it % sv.nl_iters != 0) return;
+  const int64_t n = P.ncell;
+  const Gas<double> g = GasOf<double>(sv);
+  const Prim<double> w = LoadW<double>(P.W, n, c);
+  double cn[7];
+  PrimToCons(w, g, cn);
+  cn[5] = sv.rans ? w.rho * P.Wt[c] : 0.0;
+  cn[6] = sv.rans ? w.rho * P.Wt[n + c] : 0.0;
+#pragma unroll
+  for (int v = 0; v < 7; ++v) {
+    P.Un[v * n + c] = cn[v];
+    if (sv.multilevel && it == 0) P.Unm1[v * n + c] = cn[v];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // conserved update and partial norms
 template <typename T>
 __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list,
                                                  const int32_t *cta_block,
                                                  const int32_t *cta_pos0,
-                                                 NormPartial *partials) {
+                                                 NormPartial *partials,
+                                                 const SolveState *sstate) {
   __shared__ double s_l2[kCta / 32][kNvMax];
   __shared__ double s_max[kCta / 32];
   __shared__ int64_t s_pos[kCta / 32];
@@ -1597,6 +1666,11 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     P.W[2 * n + c] = u.v;
     P.W[3 * n + c] = u.w;
     P.W[4 * n + c] = u.p;
+    // gridLevel::UpdateBlocks (src/gridLevel.cpp:418): time n becomes n-1
+    // after the last nonlinear iteration of a bdf2 time step
+    if (sv.multilevel && sstate[b.solve].iter % sv.nl_iters == sv.nl_iters - 1)
+#pragma unroll
+      for (int v = 0; v < 7; ++v) P.Unm1[v * n + c] = P.Un[v * n + c];
     double rv[kNvMax];
 #pragma unroll
     for (int v = 0; v < 5; ++v) rv[v] = P.R[v * n + c];
@@ -2178,7 +2252,7 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
     for (int v = 0; v < 7; ++v) {
       if (v >= nv) break;
       const T off = L[v] - U[v];
-      const T bv = -thetaInv * bt[v];
+      const T bv = RhsB(P, sv, thetaInv, v, q);
       const T axmb = Ax[v] - off - bv;
       const double r = 0.0 - (double)axmb;
       sum += r * r;
@@ -2351,8 +2425,13 @@ void Launch<T>::ConnDu(const Pools<T> &P, cudaStream_t s) {
 template <typename T>
 void Launch<T>::Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        const int32_t *cta_pos0, NormPartial *partials, int ncta,
-                       cudaStream_t s) {
-  if (ncta > 0) k_update<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, cta_pos0, partials);
+                       const SolveState *ss, cudaStream_t s) {
+  if (ncta > 0) k_update<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, cta_pos0, partials, ss);
+}
+template <typename T>
+void Launch<T>::StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                       int ncta, const SolveState *ss, cudaStream_t s) {
+  if (ncta > 0) k_store_n<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, ss);
 }
 
 }  // namespace ath

@@ -1198,10 +1198,27 @@ void AppendInput(Setup &st, const std::string &path) {
            : eqn == "navierStokes" ? ATH_EQN_NAVIER_STOKES
            : eqn == "rans" ? ATH_EQN_RANS
            : (Fail("unsupported equationSet " + eqn), 0);
+  // input::ReadInput (src/input.cpp:255-267): theta and zeta of the
+  // implicit schemes; nonlinear iterations per time step (:353)
   const auto ti = get("timeIntegration", "explicitEuler");
-  if (ti != "implicitEuler") Fail("only timeIntegration implicitEuler is supported");
-  ph.theta = 1.0;
-  ph.zeta = 0.0;
+  ph.multilevel = 0;
+  if (ti == "implicitEuler") {
+    ph.theta = 1.0;
+    ph.zeta = 0.0;
+  } else if (ti == "crankNicholson") {
+    ph.theta = 0.5;
+    ph.zeta = 0.0;
+  } else if (ti == "bdf2") {
+    ph.theta = 1.0;
+    ph.zeta = 0.5;
+    ph.multilevel = 1;
+  } else {
+    Fail("only the implicit time integrations (implicitEuler, crankNicholson, bdf2) are "
+         "supported");
+  }
+  ph.nl_iters = (int)getd("nonlinearIterations", 1);
+  if (ph.nl_iters < 1) Fail("nonlinearIterations must be at least 1");
+  ph.dual_cfl = getd("dualTimeCFL", -1.0) > 0.0 ? getd("dualTimeCFL", -1.0) : 0.0;
   const auto fr = get("faceReconstruction", "constant");
   ph.kappa = -2.0;
   if (fr == "upwind") { ph.recon = ATH_RECON_MUSCL; ph.kappa = -1.0; }
@@ -1233,9 +1250,6 @@ void AppendInput(Setup &st, const std::string &path) {
   ph.cfl_start = getd("cflStart", 1.0);
   ph.cfl_step = getd("cflStep", 0.0);
   ph.cfl_max = getd("cflMax", 1.0);
-  if (get("timeStep", "-1") != "-1" && getd("timeStep", -1.0) > 0)
-    Fail("global time step (timeStep) is not supported");
-  if (getd("dualTimeCFL", -1.0) > 0) Fail("dualTimeCFL is not supported");
   if (get("inviscidFluxJacobian", "rusanov") != "rusanov")
     Fail("only the rusanov inviscid flux jacobian is supported");
   if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
@@ -1291,6 +1305,9 @@ void AppendInput(Setup &st, const std::string &path) {
   ph.a_ref = aref;
   ph.l_ref = lref;
   ph.visc_scale = ph.mu_ref / (rref * aref * lref);
+  // global time step, nondimensional (procBlock::CalcBlockTimeStep,
+  // src/procBlock.cpp:808)
+  ph.dt_global = getd("timeStep", -1.0) > 0.0 ? getd("timeStep", -1.0) * aref / lref : 0.0;
   ph.visc_cfl_coeff = ph.kappa == 1.0 ? 4.0 : (ph.kappa == -2.0 ? 2.0 : 1.0);
 
   // boundary states

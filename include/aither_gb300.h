@@ -145,6 +145,14 @@ typedef struct {
                                            k_ref = conductivity reference */
   int32_t nstates;
   const ath_bc_state *states;
+  /* time integration (timeIntegration, src/input.cpp:259-266): theta and
+   * zeta above are implicitEuler 1/0, crankNicholson 0.5/0, bdf2 1/0.5 (with
+   * the time n-1 solution: multilevel = 1); dt_global is the nondimensional
+   * global time step (timeStep * a_ref / l_ref; 0: local time stepping from
+   * the CFL), dual_cfl the dual-time CFL (0: none), nl_iters the nonlinear
+   * iterations per time step */
+  double dt_global, dual_cfl;
+  int32_t nl_iters, multilevel;
 } ath_solve_view;
 
 /* Read-only view of one block of a setup; arrays are host memory owned by

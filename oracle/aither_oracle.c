@@ -26,6 +26,7 @@ typedef struct {
   double *W;           /* [nc][5] primitive, AoS as in the reference */
   double *R;           /* [nc][5] */
   double *dU;          /* [nc][5] */
+  double *Un, *Unm1;   /* [nc][7] conserved state of time levels n, n-1 */
   double *lam, *dt, *A, *Ainv; /* [nc] */
   double *Ab, *Ainvb;  /* [nc][25] block diagonal and its inverse (blusgs) */
   double *vg;          /* [nc][9] cell-averaged velocity gradient (blusgs) */
@@ -1260,6 +1261,8 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     b->dU = (double *)dup_arr(NULL, 8 * NV * b->nc);
     b->lam = (double *)dup_arr(NULL, 8 * b->nc);
     b->dt = (double *)dup_arr(NULL, 8 * b->nc);
+    b->Un = (double *)dup_arr(NULL, 8 * 7 * b->nc);
+    b->Unm1 = (double *)dup_arr(NULL, 8 * 7 * b->nc);
     b->A = (double *)dup_arr(NULL, 8 * b->nc);
     b->Ainv = (double *)dup_arr(NULL, 8 * b->nc);
     if (c->s[b->solve].viscous) {
@@ -1316,6 +1319,7 @@ void orc_destroy(orc_case *c) {
     free(b->vol); free(b->width);
     for (int d = 0; d < 3; ++d) free(b->fa[d]);
     free(b->W); free(b->R); free(b->dU); free(b->lam); free(b->dt); free(b->A);
+    free(b->Un); free(b->Unm1);
     free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
@@ -1363,11 +1367,31 @@ static void extrap_hold(double *g, double factor, const double *in) {
 /* GetGhostState (src/ghostStates.cpp:62) for the supported types;
  * interblock/periodic: copy of the partner cell (SwapStateSlice). */
 void orc_fill_ghosts(orc_case *c) {
-  /* CalcCFL for this iteration (src/input.cpp:647) */
+  /* CalcCFL of the time step (src/input.cpp:647); at a time step's first
+   * nonlinear iteration StoreOldSolution (src/mgSolution.cpp:103): the
+   * conserved state of time n, and of time n-1 too at the first step of a
+   * multilevel (bdf2) solve */
   for (int s = 0; s < c->ns; ++s) {
     const ath_solve_view *v = &c->s[s].v;
-    const double cfl = v->cfl_start + (double)c->iter * v->cfl_step;
+    const int nl = v->nl_iters > 0 ? v->nl_iters : 1;
+    const double cfl = v->cfl_start + (double)(c->iter / nl) * v->cfl_step;
     c->s[s].cfl = cfl < v->cfl_max ? cfl : v->cfl_max;
+  }
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const ath_solve_view *v = &c->s[b->solve].v;
+    const int nl = v->nl_iters > 0 ? v->nl_iters : 1;
+    if (c->iter % nl != 0) continue;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          double *un = &b->Un[x * 7];
+          prim_to_cons(&b->W[x * NV], &c->s[b->solve].gas, un);
+          un[5] = b->Wt ? b->W[x * NV] * b->Wt[x * 2] : 0.0;
+          un[6] = b->Wt ? b->W[x * NV] * b->Wt[x * 2 + 1] : 0.0;
+          if (v->multilevel && c->iter == 0) memcpy(&b->Unm1[x * 7], un, 8 * 7);
+        }
   }
   NTH
   PAR_BLOCKS
@@ -1812,9 +1836,11 @@ void orc_timestep(orc_case *c) {
       for (int j = 0; j < b->nj; ++j)
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
-          /* uncoupledScalar::Max of the flow and turbulence radii */
+          /* global time step when given, else local from the CFL with
+           * uncoupledScalar::Max of the flow and turbulence radii */
+          const double dtg = c->s[b->solve].v.dt_global;
           const double lm = b->Wt ? cmax(b->lam[x], b->lamt[x]) : b->lam[x];
-          b->dt[x] = cfl * (b->vol[x] / lm);
+          b->dt[x] = dtg > 0.0 ? dtg : cfl * (b->vol[x] / lm);
         }
   }
 }
@@ -1831,7 +1857,12 @@ void orc_diag_invert(orc_case *c) {
       for (int j = 0; j < b->nj; ++j)
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
-          const double diagVolTime = (b->vol[x] * (1.0 + v->zeta)) / (b->dt[x] * v->theta);
+          double diagVolTime = (b->vol[x] * (1.0 + v->zeta)) / (b->dt[x] * v->theta);
+          if (v->dual_cfl > 0.0) {
+            /* dual time stepping: volume / tau */
+            const double lm = b->Wt ? cmax(b->lam[x], b->lamt[x]) : cmax(b->lam[x], 0.0);
+            diagVolTime += lm / v->dual_cfl;
+          }
           if (c->s[b->solve].block) {
             double *a = &b->Ab[x * NJAC];
             for (int r = 0; r < NV; ++r) a[r * 5 + r] *= v->relax;
@@ -1964,6 +1995,35 @@ static void get_rhs(const orc_case *c, const oblock *b, int64_t x, double *r) {
   r[NV + 1] = b->Rt ? b->Rt[x * 2 + 1] : 0.0;
 }
 
+/* right-hand side b of the linear system per equation: -R/theta +
+ * SolDeltaNm1 - SolDeltaMmN (src/linearSolver.cpp:350-352, procBlock::
+ * SolDeltaNm1 / SolDeltaMmN src/procBlock.cpp:1015-1034): the change since
+ * time n times V(1+zeta)/(dt theta), and for bdf2 the change from n-1 to n
+ * times V zeta/(dt theta); without time levels (one nonlinear iteration of
+ * a one-level scheme) both are zero */
+static void rhs_b(const orc_case *c, const oblock *b, int64_t x, double *bb) {
+  const ath_solve_view *v = &c->s[b->solve].v;
+  const double thetaInv = 1.0 / v->theta;
+  double r[NV + 2];
+  get_rhs(c, b, x, r);
+  const int unsteady = v->multilevel || v->nl_iters > 1;
+  if (!unsteady) {
+    for (int q = 0; q < NV + 2; ++q) bb[q] = -thetaInv * r[q] + 0.0 + 0.0 - 0.0;
+    return;
+  }
+  double cn[7];
+  prim_to_cons(&b->W[x * NV], &c->s[b->solve].gas, cn);
+  cn[5] = b->Wt ? b->W[x * NV] * b->Wt[x * 2] : 0.0;
+  cn[6] = b->Wt ? b->W[x * NV] * b->Wt[x * 2 + 1] : 0.0;
+  const double coeffN = (b->vol[x] * (1.0 + v->zeta)) / (b->dt[x] * v->theta);
+  const double coeffNm1 = (b->vol[x] * v->zeta) / (b->dt[x] * v->theta);
+  for (int q = 0; q < NV + 2; ++q) {
+    const double dMmN = coeffN * (cn[q] - b->Un[x * 7 + q]);
+    const double dNm1 = v->multilevel ? coeffNm1 * (b->Un[x * 7 + q] - b->Unm1[x * 7 + q]) : 0.0;
+    bb[q] = -thetaInv * r[q] + dNm1 - dMmN;
+  }
+}
+
 /* linearSolver::Residual / AXmB (src/linearSolver.cpp:58,92) and the L2 of
  * mgSolution::CycleAtLevel (src/mgSolution.cpp:196-206) with the second
  * normalisation of src/main.cpp:271: sqrt(sum(r^2)/padded_size/(cells*nv)),
@@ -1985,7 +2045,7 @@ static void matrix_residual(orc_case *c) {
             offdiag_sum(c, b, x, 1, L);
             offdiag_sum(c, b, x, 0, U);
             get_du(b, x, u);
-            get_rhs(c, b, x, r);
+            rhs_b(c, b, x, r);
             if (c->s[s].block) {
               mat_vec(&b->Ab[x * NJAC], u, Ax);
               if (b->Wt) mat_vec2(&b->Abt[x * 4], u + NV, Ax + NV);
@@ -1996,7 +2056,7 @@ static void matrix_residual(orc_case *c) {
             }
             for (int v = 0; v < nv; ++v) {
               const double off = L[v] - U[v];
-              const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+              const double bb = r[v];
               const double axmb = Ax[v] - off - bb;
               const double rr = 0.0 - axmb;
               bsum += rr * rr;
@@ -2053,8 +2113,8 @@ void orc_relax(orc_case *c) {
         for (int i = 0; i < b->ni; ++i) {
           const int64_t x = cell_idx(b, i, j, k);
           double in[NV + 2], r[NV + 2], out[NV + 2];
-          get_rhs(c, b, x, r);
-          for (int v = 0; v < nv; ++v) in[v] = -thetaInv * r[v] + 0.0 - 0.0;
+          rhs_b(c, b, x, r);
+          for (int v = 0; v < nv; ++v) in[v] = r[v];
           apply_ainv(c, b, x, in, out);
           set_du(b, x, out);
         }
@@ -2078,9 +2138,9 @@ void orc_relax(orc_case *c) {
             double L[NV + 2], U[NV + 2], in[NV + 2], r[NV + 2], out[NV + 2];
             offdiag_sum(c, b, x, 1, L);
             offdiag_sum(c, b, x, 0, U);
-            get_rhs(c, b, x, r);
+            rhs_b(c, b, x, r);
             for (int v = 0; v < nv; ++v) {
-              const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+              const double bb = r[v];
               in[v] = bb + 0.0 + (L[v] - U[v]);
             }
             apply_ainv(c, b, x, in, out);
@@ -2112,9 +2172,9 @@ void orc_relax(orc_case *c) {
           offdiag_sum(c, b, x, 0, U);
           for (int v = 0; v < nv; ++v) L[v] -= U[v];
         }
-        get_rhs(c, b, x, r);
+        rhs_b(c, b, x, r);
         for (int v = 0; v < nv; ++v) {
-          const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+          const double bb = r[v];
           in[v] = bb + L[v];
         }
         apply_ainv(c, b, x, in, out);
@@ -2137,9 +2197,9 @@ void orc_relax(orc_case *c) {
         offdiag_sum(c, b, x, 0, U);
         if (full) {
           offdiag_sum(c, b, x, 1, L);
-          get_rhs(c, b, x, r);
+          rhs_b(c, b, x, r);
           for (int v = 0; v < nv; ++v) {
-            const double bb = -thetaInv * r[v] + 0.0 + 0.0 - 0.0;
+            const double bb = r[v];
             in[v] = bb + L[v] - U[v];
           }
           apply_ainv(c, b, x, in, out);
@@ -2214,6 +2274,14 @@ int orc_update(orc_case *c, double *l2_out, double *linf_out) {
     if (linf_out) linf_out[s] = linf[s];
   free(l2);
   free(linf);
+  /* gridLevel::UpdateBlocks (src/gridLevel.cpp:418): time n becomes n-1
+   * after the last nonlinear iteration of a multilevel step */
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const ath_solve_view *v = &c->s[b->solve].v;
+    const int nl = v->nl_iters > 0 ? v->nl_iters : 1;
+    if (v->multilevel && c->iter % nl == nl - 1) memcpy(b->Unm1, b->Un, 8 * 7 * b->nc);
+  }
   c->iter += 1;
   return bad ? ATH_ERR_NONPHYSICAL : 0;
 }

@@ -52,3 +52,11 @@ def rel_err(a, b):
     import numpy as np
     scale = max(float(np.abs(b).max()), 1e-300)
     return float(np.abs(np.asarray(a) - np.asarray(b)).max()) / scale
+
+
+def total_iterations(g):
+    """Nonlinear iterations a fixture ran: its time steps times the
+    nonlinear iterations per step of time-accurate cases."""
+    import ast
+    kw = ast.literal_eval(str(g["kwargs"]))
+    return int(g["iterations"]) * int(kw.get("nl", 1))

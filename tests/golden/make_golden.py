@@ -101,6 +101,17 @@ CASES = [
     ("sst_chan_stag_pout", cases.wall_channel,
      dict(ni=16, nj=10, nk=3, kind="bump", param=0.06, mach=0.5, alpha=2.0, rans=True,
           stretch=1.1, cfl=5.0, inflow="stagnation", outflow="pressure"), [1, 10], True),
+    # time-accurate: iterations count time steps, each of nl nonlinear iterations
+    ("vortex_bdf2", cases.vortex_box,
+     dict(ni=16, nj=8, nk=4, time="bdf2", dt=5e-4, nl=3), [1, 4], True),
+    ("vortex_cn_dual", cases.vortex_box,
+     dict(ni=16, nj=8, nk=4, time="crankNicholson", dt=5e-4, nl=3, dual_cfl=5.0), [1, 4], True),
+    ("plate_bdf2_blusgs", cases.flat_plate,
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, matrix_solver="blusgs", time="bdf2",
+          dt=1e-4, nl=2), [1, 4], True),
+    ("sst_plate_bdf2", cases.flat_plate,
+     dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1, time="bdf2", dt=1e-5, nl=2), [1, 4], True),
 ]
 
 

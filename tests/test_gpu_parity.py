@@ -14,7 +14,7 @@ Tolerances (relative to the largest magnitude of the compared field):
 import numpy as np
 import pytest
 
-from conftest import golden_case, rel_err
+from conftest import golden_case, rel_err, total_iterations
 
 pytestmark = pytest.mark.gpu
 
@@ -68,11 +68,13 @@ def _cols_err(a, b):
                                   "plate_bdplur_it20", "bump_stag_pout_it1",
                                   "bump_stag_pout_it20", "bump_inlet_pout_it1",
                                   "bump_inlet_pout_it20", "plate_heatflux_it1",
-                                  "plate_heatflux_it20"])
+                                  "plate_heatflux_it20", "vortex_bdf2_it1", "vortex_bdf2_it4",
+                                  "vortex_cn_dual_it1", "vortex_cn_dual_it4",
+                                  "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)
-    n = int(g["iterations"])
+    n = total_iterations(g)
     norms = b.iterate(n)
     diff_tol = CELL_TOL if n == 1 else NORM_TOL
     for k in range(int(g["nblocks"])):
@@ -92,7 +94,7 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
 SST_CASES = ["sst_plate_it1", "sst_plate_it20", "sst_plate2_blusgs_it1",
              "sst_plate2_blusgs_it10", "sst_weno_ausm_it1", "sst_weno_ausm_it10",
              "sst_plate_dplur_it1", "sst_plate_dplur_it10", "sst_chan_stag_pout_it1",
-             "sst_chan_stag_pout_it10"]
+             "sst_chan_stag_pout_it10", "sst_plate_bdf2_it1", "sst_plate_bdf2_it4"]
 
 
 @pytest.mark.parametrize("name", SST_CASES)
@@ -107,7 +109,7 @@ def test_fp64_sst_matches_reference_fixture(ctx, name, tmp_path):
     for k in range(int(g["nblocks"])):
         s_k = g[f"b{k}_state0"]
         assert rel_err(b.field(k, "STATE"), s_k) == 0.0
-    n = int(g["iterations"])
+    n = total_iterations(g)
     norms = b.iterate(n)
     diff_tol = CELL_TOL if n == 1 else NORM_TOL
     for k in range(int(g["nblocks"])):
@@ -134,7 +136,7 @@ def test_fp64_sst_matches_reference_fixture(ctx, name, tmp_path):
                                   "bump_blusgs_it20", "bump_sweeps3_it20",
                                   "plate_blusgs_sw2_it20", "sst_plate_it20",
                                   "sst_plate2_blusgs_it10", "bump_dplur_it20",
-                                  "plate_bdplur_it20"])
+                                  "plate_bdplur_it20", "vortex_bdf2_it4", "vortex_cn_dual_it4"])
 def test_fp64_matrix_residual(ctx, name, tmp_path):
     """flags bit 0: the logged matrix residual of every iteration; it is a
     log-only quantity, so the solution is unchanged."""
@@ -144,7 +146,7 @@ def test_fp64_matrix_residual(ctx, name, tmp_path):
     if st is not None:
         s.set_state(0, st[0])
     b = Batch(ctx, s, 0, flags=1)
-    norms = b.iterate(int(g["iterations"]))
+    norms = b.iterate(total_iterations(g))
     mres = np.array([n.matrix_resid for n in norms])
     assert rel_err(mres, g["matrix_resid"]) <= NORM_TOL
     assert _cols_err(b.field(0, "STATE"), g["b0_state"]) <= CELL_TOL

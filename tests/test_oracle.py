@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import REF_HARNESS, REF_SRC, golden_case, rel_err
+from conftest import REF_HARNESS, REF_SRC, golden_case, rel_err, total_iterations
 
 # The oracle restates the reference operation by operation and is built
 # with -ffp-contract=off; it reproduces the reference bit for bit on these
@@ -27,7 +27,9 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "plate_bdplur_it20", "sst_plate_dplur_it1", "sst_plate_dplur_it10",
         "bump_stag_pout_it1", "bump_stag_pout_it20", "bump_inlet_pout_it1",
         "bump_inlet_pout_it20", "plate_heatflux_it1", "plate_heatflux_it20",
-        "sst_chan_stag_pout_it1", "sst_chan_stag_pout_it10"]
+        "sst_chan_stag_pout_it1", "sst_chan_stag_pout_it10", "vortex_bdf2_it1", "vortex_bdf2_it4",
+        "vortex_cn_dual_it1", "vortex_cn_dual_it4", "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
+        "sst_plate_bdf2_it1", "sst_plate_bdf2_it4"]
 
 
 def _oracle(inp, st):
@@ -43,8 +45,7 @@ def _oracle(inp, st):
 def test_oracle_matches_reference_fixture(name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     _, o = _oracle(inp, st)
-    n = int(g["iterations"])
-    l2 = o.iterate(n)
+    l2 = o.iterate(total_iterations(g))
     for b in range(int(g["nblocks"])):
         p = f"b{b}_"
         assert rel_err(o.field(b, "STATE"), g[p + "state"]) <= TOL
@@ -62,7 +63,8 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
 
 @pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
                                   "bump_blusgs_it20", "bump_sweeps3_it20",
-                                  "plate_blusgs_sw2_it20"])
+                                  "plate_blusgs_sw2_it20", "vortex_bdf2_it4",
+                                  "vortex_cn_dual_it4", "sst_plate_bdf2_it4"])
 def test_oracle_matrix_residual(name, tmp_path):
     """The logged linear-system residual (linearSolver::Residual)."""
     from aither_gb300 import Setup
@@ -72,7 +74,7 @@ def test_oracle_matrix_residual(name, tmp_path):
     if st is not None:
         s.set_state(0, st[0])
     o = Oracle(s, matrix_resid=True)
-    o.iterate(int(g["iterations"]))
+    o.iterate(total_iterations(g))
     assert rel_err(o.mres[:, 0], g["matrix_resid"]) <= TOL
 
 
