@@ -19,7 +19,7 @@ BC = dict(SLIP_WALL=0, VISCOUS_WALL=1, CHARACTERISTIC=2, STAGNATION_INLET=3,
           PERIODIC=7, INTERBLOCK=8)
 PREC_FP64, PREC_MIXED = 0, 1
 FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
-             WALLDIST=9)
+             WALLDIST=9, CONS_N=10, CONS_NM1=11)
 
 
 class GhostOp(C.Structure):
@@ -109,7 +109,8 @@ class BlockDev(C.Structure):
 class BlockFields(C.Structure):
     """ath_block_fields: host fields of one block for the output writers."""
     _fields_ = [("prim", C.c_void_p), ("dt", C.c_void_p), ("resid", C.c_void_p),
-                ("aux", C.c_void_p), ("velgrad", C.c_void_p), ("wall_dist", C.c_void_p)]
+                ("aux", C.c_void_p), ("velgrad", C.c_void_p), ("wall_dist", C.c_void_p),
+                ("cons_nm1", C.c_void_p)]
 
 
 class Stats(C.Structure):
@@ -150,6 +151,7 @@ def lib() -> C.CDLL:
             "ath_batch_update": (C.c_int, [vp, C.POINTER(Norms)]),
             "ath_batch_get_field": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_batch_set_state_nm1": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_field_width": (C.c_int, [vp, C.c_int, C.c_int]),
             "ath_batch_pool_vars": (C.c_int, [vp, C.POINTER(C.c_int)]),
             "ath_output_function": (C.c_int, [vp, C.c_int, C.c_char_p, C.POINTER(BlockFields),
@@ -158,6 +160,8 @@ def lib() -> C.CDLL:
                                              C.POINTER(BlockFields), C.c_char_p]),
             "ath_input_restart": (C.c_int, [vp, C.c_int, C.c_char_p, C.POINTER(C.c_int),
                                             C.POINTER(C.c_double),
+                                            C.POINTER(C.POINTER(C.c_double)),
+                                            C.POINTER(C.c_int),
                                             C.POINTER(C.POINTER(C.c_double))]),
             "ath_output_center_grid": (C.c_int, [vp, C.c_int, C.c_char_p]),
             "ath_output_meta": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int, C.c_char_p]),
@@ -266,7 +270,7 @@ class Setup:
         keep = []
         arr = (BlockFields * len(blocks))()
         for k, fl in enumerate(blocks):
-            for name in ("prim", "dt", "resid", "aux", "velgrad", "wall_dist"):
+            for name in ("prim", "dt", "resid", "aux", "velgrad", "wall_dist", "cons_nm1"):
                 a = fl.get(name)
                 if a is not None:
                     a = np.ascontiguousarray(a, dtype=np.float64)
@@ -283,24 +287,34 @@ class Setup:
         check(lib().ath_output_function(self.h, solve, v, arr, path.encode()))
 
     def write_restart(self, solve: int, iteration: int, resid_first, prims: list,
-                      path: str) -> None:
-        arr = self._fields([{"prim": p} for p in prims])
+                      path: str, nm1: list | None = None) -> None:
+        """Restart file from host states; nm1 (conserved state of time n-1
+        per block) is required for bdf2 solves."""
+        arr = self._fields([{"prim": p, "cons_nm1": None if nm1 is None else nm1[k]}
+                            for k, p in enumerate(prims)])
         rf = np.ascontiguousarray(resid_first, dtype=np.float64)
         check(lib().ath_output_restart(self.h, solve, iteration, dptr(rf), arr, path.encode()))
 
-    def read_restart(self, solve: int, path: str):
-        """(iteration, L2 normalisation, [primitive state per block])."""
+    def read_restart(self, solve: int, path: str, levels: bool = False):
+        """(iteration, L2 normalisation, [primitive state per block]); with
+        levels=True also the file's time levels and [conserved state of time
+        n-1 per block] (None for a one-level file)."""
         blocks = self.solve_blocks(solve)
         nv = self.solve_nv(solve)
-        outs = []
+        outs, nm1 = [], []
         for b in blocks:
             v = self.block_view(b)
             outs.append(np.empty((v.nk, v.nj, v.ni, nv)))
+            nm1.append(np.empty((v.nk, v.nj, v.ni, nv)))
         ptrs = (C.POINTER(C.c_double) * len(outs))(*[dptr(o) for o in outs])
-        it = C.c_int()
+        ptrs1 = (C.POINTER(C.c_double) * len(nm1))(*[dptr(o) for o in nm1])
+        it, nl = C.c_int(), C.c_int()
         rf = np.empty(nv)
-        check(lib().ath_input_restart(self.h, solve, path.encode(), C.byref(it), dptr(rf), ptrs))
-        return it.value, rf, outs
+        check(lib().ath_input_restart(self.h, solve, path.encode(), C.byref(it), dptr(rf), ptrs,
+                                      C.byref(nl), ptrs1))
+        if not levels:
+            return it.value, rf, outs
+        return it.value, rf, outs, nl.value, (nm1 if nl.value >= 2 else None)
 
     def write_center_grid(self, solve: int, path: str) -> None:
         check(lib().ath_output_center_grid(self.h, solve, path.encode()))
@@ -310,11 +324,14 @@ class Setup:
         check(lib().ath_output_meta(self.h, solve, v, iteration, path.encode()))
 
     def write_resid(self, solve: int, path: str, norms: list, first_step: int,
-                    resid_first: np.ndarray, append: bool = False) -> None:
-        """Residual history rows of one solve; resid_first (nv values) is
-        the running normalisation, updated in place."""
+                    resid_first: np.ndarray, append: bool = False,
+                    restarted: bool = False) -> None:
+        """Residual history rows of one solve from nonlinear iteration
+        first_step on; resid_first (nv values) is the running normalisation,
+        updated in place (left as given in a restarted run)."""
         arr = (Norms * len(norms))(*norms)
-        check(lib().ath_output_resid(self.h, solve, path.encode(), 1 if append else 0,
+        flags = (1 if append else 0) | (2 if restarted else 0)
+        check(lib().ath_output_resid(self.h, solve, path.encode(), flags,
                                      first_step, len(norms), arr, dptr(resid_first)))
 
     def block_view(self, b: int) -> BlockView:
@@ -426,6 +443,15 @@ class Batch:
     def set_state(self, b: int, prim: np.ndarray) -> None:
         prim = np.ascontiguousarray(prim, dtype=np.float64)
         check(lib().ath_batch_set_state(self.h, b, dptr(prim)))
+
+    def set_state_nm1(self, b: int, cons: np.ndarray | None) -> None:
+        """Time n-1 of a bdf2 solve's block (conserved, nv per cell), kept
+        through the first time step; None copies the current state."""
+        if cons is None:
+            check(lib().ath_batch_set_state_nm1(self.h, b, None))
+            return
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        check(lib().ath_batch_set_state_nm1(self.h, b, dptr(cons)))
 
     def pool_cells(self) -> int:
         n = C.c_int64()

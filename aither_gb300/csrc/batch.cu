@@ -308,6 +308,10 @@ class RunnerBase {
   virtual void GetAinv(int b, double *out) = 0;
   virtual void GetAux(int b, double *out) = 0;
   virtual void GetVelGrad(int b, double *out) = 0;
+  // block's current state into both time levels (a one-level restart)
+  virtual void StoreTimeLevels(int b) = 0;
+  // temperature and viscosity of a block's physical cells from its state
+  virtual void RefreshAux(int b) = 0;
   virtual void Profile(int reps, double ms[8]) = 0;
   // drop the captured iteration graph (launch shapes changed)
   virtual void ResetGraph() = 0;
@@ -518,10 +522,11 @@ class Runner : public RunnerBase {
 
   // gridLevel::AuxillaryAndWidths (src/gridLevel.cpp:433): laminar
   // viscosity of the physical cells of the initial state (the wall ghost
-  // omega of the first iteration reads it)
-  void InitialViscosity(DevMem &m) {
+  // omega of the first iteration reads it); only >= 0: that block's
+  void InitialViscosity(DevMem &m, int only = -1) {
     std::vector<int32_t> cells, blk;
     for (int bi = 0; bi < c_.nblocks; ++bi) {
+      if (only >= 0 && bi != only) continue;
       const Block &b = c_.setup->blocks[bi];
       if (c_.setup->solves[b.solve].phys.eqn == ATH_EQN_EULER) continue;
       for (int k = 0; k < b.nk; ++k)
@@ -552,7 +557,7 @@ class Runner : public RunnerBase {
     StartIteration();
     if (c_.any_unsteady)
       Launch<T>::StoreN(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
-                        c_.d_sstate, c_.stream);
+                        c_.d_sstate, -1, c_.stream);
     Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
     EdgePhases(c_.d_edge_ops, c_.d_edge_solve, c_.L.edge_phase_off);
   }
@@ -823,6 +828,13 @@ class Runner : public RunnerBase {
     if (nv > 5) CopyOutQ(P_.dUtq, 2, nv, 5, b, out);
   }
   void GetAinv(int b, double *out) override { CopyOutQ(P_.Ainvq, 1, 1, 0, b, out); }
+  void RefreshAux(int b) override { InitialViscosity(*c_.mem, b); }
+  void StoreTimeLevels(int b) override {
+    Launch<T>::StoreN(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
+                      c_.d_sstate, b, c_.stream);
+    Check(cudaGetLastError(), "kernel launch");
+    Check(cudaStreamSynchronize(c_.stream), "sync");
+  }
   void GetAux(int bi, double *out) override {
     const Block &b = c_.setup->blocks[bi];
     const auto &ph = c_.setup->solves[b.solve].phys;
@@ -922,6 +934,7 @@ struct ath_batch {
   std::unique_ptr<ath::RunnerBase> run;
   double *W = nullptr, *R = nullptr, *dt = nullptr, *lam = nullptr;
   double *Wt = nullptr, *Rt = nullptr, *lamt = nullptr;  // RANS solves only
+  double *Un = nullptr, *Unm1 = nullptr;  // time-accurate solves only
 };
 
 namespace ath {
@@ -1365,6 +1378,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->Wt = r->P().Wt;
     B->Rt = r->P().Rt;
     B->lamt = r->P().lamt;
+    B->Un = r->P().Un;
+    B->Unm1 = r->P().Unm1;
   } else if (precision == ATH_PREC_MIXED) {
     auto *r = new Runner<float>(c);
     B->run.reset(r);
@@ -1375,6 +1390,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->Wt = r->P().Wt;
     B->Rt = r->P().Rt;
     B->lamt = r->P().lamt;
+    B->Un = r->P().Un;
+    B->Unm1 = r->P().Unm1;
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
@@ -1744,6 +1761,9 @@ int ath_batch_field_width(ath_batch *batch, int block, int field) {
       return 9;
     case ATH_FIELD_WALLDIST:
       return 1;
+    case ATH_FIELD_CONS_N:
+    case ATH_FIELD_CONS_NM1:
+      return batch->core.setup->blocks[block].nv;
     default:
       return ATH_ERR_ARG;
   }
@@ -1810,6 +1830,17 @@ int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h) {
             for (int i = 0; i < b.ni; ++i) out_h[q++] = b.wall_dist[b.Cell(i, j, k)];
         break;
       }
+      case ATH_FIELD_CONS_N:
+      case ATH_FIELD_CONS_NM1: {
+        const auto &ph = c.setup->solves[b.solve].phys;
+        const bool nm1 = field == ATH_FIELD_CONS_NM1;
+        if (!batch->Un || !(nm1 ? ph.multilevel : (ph.multilevel || ph.nl_iters > 1)))
+          throw ath::Error(ATH_ERR_UNSUPPORTED, nm1 ? "time n-1 is kept for bdf2 solves only"
+                                                    : "time n is kept for time-accurate "
+                                                      "solves only");
+        gather(nm1 ? batch->Unm1 : batch->Un, nv, nv, 0, false);
+        break;
+      }
       default: throw ath::Error(ATH_ERR_ARG, "unknown field");
     }
   });
@@ -1835,6 +1866,43 @@ int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h) {
           for (int i = 0; i < b.ni; ++i) h[b.Cell(i, j, k)] = prim_h[(q++) * nv + v];
       Check(cudaMemcpy(pool, h.data(), nc * 8, cudaMemcpyHostToDevice), "upload");
     }
+    // a state loaded before the run (initial condition or restart) gets its
+    // temperature and viscosity, as after ReadRestart in the reference
+    // (gridLevel::AuxillaryAndWidths src/gridLevel.cpp:433); the lagged
+    // eddy viscosity stays that of the initial condition
+    batch->run->RefreshAux(block);
+  });
+}
+
+int ath_batch_set_state_nm1(ath_batch *batch, int block, const double *cons_h) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null argument");
+    auto &c = batch->core;
+    if (block < 0 || block >= c.nblocks) throw ath::Error(ATH_ERR_ARG, "block out of range");
+    const ath::Block &b = c.setup->blocks[block];
+    if (!batch->Unm1 || !c.setup->solves[b.solve].phys.multilevel)
+      throw ath::Error(ATH_ERR_UNSUPPORTED, "time n-1 is kept for bdf2 solves only");
+    Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    Check(cudaStreamSynchronize(c.stream), "sync");
+    if (cons_h) {
+      const int64_t nc = b.NCell(), o = c.cell0[block], n = c.ncell;
+      const int nv = b.nv;
+      std::vector<double> h(nc);
+      for (int v = 0; v < nv; ++v) {
+        double *pool = batch->Unm1 + v * n + o;
+        Check(cudaMemcpy(h.data(), pool, nc * 8, cudaMemcpyDeviceToHost), "download");
+        size_t q = 0;
+        for (int k = 0; k < b.nk; ++k)
+          for (int j = 0; j < b.nj; ++j)
+            for (int i = 0; i < b.ni; ++i) h[b.Cell(i, j, k)] = cons_h[(q++) * nv + v];
+        Check(cudaMemcpy(pool, h.data(), nc * 8, cudaMemcpyHostToDevice), "upload");
+      }
+    } else {
+      batch->run->StoreTimeLevels(block);
+    }
+    const int32_t one = 1;
+    Check(cudaMemcpy(&c.d_sstate[b.solve].nm1_given, &one, sizeof(one), cudaMemcpyHostToDevice),
+          "upload");
   });
 }
 

@@ -222,12 +222,6 @@ __global__ void k_init(Pools<T> P, const int2 *items, int n);
 template <typename T>
 __global__ void k_conn_du(Pools<T> P);
 
-// Conserved update and per-CTA partial norms (procBlock::UpdateBlock,
-// src/procBlock.cpp:826).
-template <typename T>
-__global__ void k_update(Pools<T> P, const int32_t *list, const int32_t *cta_block,
-                         const int32_t *cta_pos0, NormPartial *partials);
-
 // Per-solve reduction of the CTA partials into the norm ring, CFL of the
 // next iteration, iteration counter (one warp per solve).
 struct NormOut {
@@ -251,7 +245,7 @@ struct SolveState {
   uint64_t t_retire_ns;  // device clock at retirement
   double l2_last;        // total L2 of its last iteration
   int32_t converged;     // 1 target reached, -1 retired on a nonphysical state
-  int32_t pad;
+  int32_t nm1_given;     // time n-1 set by the host (restart): kept at the first step
 };
 __global__ void k_norms(const NormPartial *partials, const double *mres_partials,
                         const int32_t *solve_cta0, int nsolves, NormOut *ring,
@@ -316,9 +310,10 @@ struct Launch {
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,
                      const SolveState *ss, cudaStream_t s);
-  // StoreOldSolution of the time-accurate solves at a time step's start
+  // StoreOldSolution of the time-accurate solves at a time step's start;
+  // block >= 0: that block's current state into both time levels
   static void StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                     int ncta, const SolveState *ss, cudaStream_t s);
+                     int ncta, const SolveState *ss, int block, cudaStream_t s);
   static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      double *mres_partials, int ncta, int kinds, cudaStream_t s);
   // per-face wall forces [6][n] of the viscous-wall faces

@@ -1604,18 +1604,25 @@ __global__ void k_conn_du(Pools<T> P) {
 
 // StoreOldSolution (src/mgSolution.cpp:103) for the time-accurate solves:
 // at a time step's first nonlinear iteration the conserved state of time
-// n, and at the first step of a bdf2 solve that of time n-1 as well
+// n, and at the first step of a bdf2 solve that of time n-1 as well unless
+// the host set it (a restart).  block >= 0: only that block, both levels,
+// whatever the iteration (AssignSolToTimeN + AssignSolToTimeNm1 of a
+// one-level restart, src/output.cpp:892)
 template <typename T>
 __global__ void __launch_bounds__(kCta) k_store_n(Pools<T> P, const int32_t *list,
                                                   const int32_t *cta_block,
-                                                  const SolveState *sstate) {
+                                                  const SolveState *sstate, int block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
-  const int s = P.blocks[cta_block[blockIdx.x]].solve;
+  const int bk = cta_block[blockIdx.x];
+  if (block >= 0 && bk != block) return;
+  const int s = P.blocks[bk].solve;
   const SolveDev sv = P.solves[s];
-  if (!sv.unsteady || !sv.active) return;
+  if (!sv.unsteady) return;
   const int64_t it = sstate[s].iter;
-  if (it % sv.nl_iters != 0) return;
+  const bool forced = block >= 0;
+  if (!forced && (!sv.active || it % sv.nl_iters != 0)) return;
+  const bool nm1 = sv.multilevel && (forced || (it == 0 && !sstate[s].nm1_given));
   const int64_t n = P.ncell;
   const Gas<double> g = GasOf<double>(sv);
   const Prim<double> w = LoadW<double>(P.W, n, c);
@@ -1626,7 +1633,7 @@ __global__ void __launch_bounds__(kCta) k_store_n(Pools<T> P, const int32_t *lis
 #pragma unroll
   for (int v = 0; v < 7; ++v) {
     P.Un[v * n + c] = cn[v];
-    if (sv.multilevel && it == 0) P.Unm1[v * n + c] = cn[v];
+    if (nm1) P.Unm1[v * n + c] = cn[v];
   }
 }
 
@@ -2430,8 +2437,8 @@ void Launch<T>::Update(const Pools<T> &P, const int32_t *list, const int32_t *ct
 }
 template <typename T>
 void Launch<T>::StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
-                       int ncta, const SolveState *ss, cudaStream_t s) {
-  if (ncta > 0) k_store_n<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, ss);
+                       int ncta, const SolveState *ss, int block, cudaStream_t s) {
+  if (ncta > 0) k_store_n<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, ss, block);
 }
 
 }  // namespace ath

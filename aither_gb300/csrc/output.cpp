@@ -201,14 +201,19 @@ void WriteFunction(const Setup &s, const Solve &sv, const std::vector<std::strin
   if (!f) throw Error(ATH_ERR_IO, std::string("write failed: ") + path);
 }
 
-// WriteRestart (src/output.cpp:591): one time level
+// WriteRestart (src/output.cpp:591): the state, and for a bdf2 solve the
+// conserved state of time n-1 as a second time level
 void WriteRestart(const Setup &s, const Solve &sv, int iteration, const double *resid_first,
                   const ath_block_fields *fields, const char *path) {
   CheckFields(sv, fields);
   if (!resid_first) throw Error(ATH_ERR_ARG, "null residual normalisation");
   const int nv = sv.phys.nv;
+  const int levels = sv.phys.multilevel ? 2 : 1;
+  if (levels == 2)
+    for (size_t k = 0; k < sv.blocks.size(); ++k)
+      if (!fields[k].cons_nm1) throw Error(ATH_ERR_ARG, "bdf2 restart needs time n-1");
   auto f = OpenOut(path, true);
-  Put(f, (int)1);          // time levels
+  Put(f, levels);          // time levels
   Put(f, iteration);       // solution iteration
   Put(f, nv);              // equations
   Put(f, (int)1);          // species
@@ -238,6 +243,28 @@ void WriteRestart(const Setup &s, const Solve &sv, int iteration, const double *
     }
     f.write(reinterpret_cast<const char *>(out.data()), out.size() * 8);
   }
+  // time n-1: rho, rho u, rho v, rho w, rho E [, rho k, rho omega] times
+  // their reference scales, then the species' share of the density
+  for (size_t k = 0; levels == 2 && k < sv.blocks.size(); ++k) {
+    const Block &b = s.blocks[sv.blocks[k]];
+    const size_t m = Cells(b);
+    std::vector<double> out;
+    out.reserve(m * (nv + 1));
+    for (size_t q = 0; q < m; ++q) {
+      const double *u = fields[k].cons_nm1 + q * nv;
+      out.push_back(u[0] * sc.r);
+      out.push_back(u[1] * (sc.a * sc.r));
+      out.push_back(u[2] * (sc.a * sc.r));
+      out.push_back(u[3] * (sc.a * sc.r));
+      out.push_back(u[4] * (sc.a * sc.a * sc.r));
+      if (nv == 7) {
+        out.push_back(u[5] * (sc.a * sc.a * sc.r));
+        out.push_back(u[6] * (sc.a * sc.a * sc.r * sc.r / sc.mu));
+      }
+      out.push_back(u[0] / u[0]);
+    }
+    f.write(reinterpret_cast<const char *>(out.data()), out.size() * 8);
+  }
   if (!f) throw Error(ATH_ERR_IO, std::string("write failed: ") + path);
 }
 
@@ -245,7 +272,8 @@ void WriteRestart(const Setup &s, const Solve &sv, int iteration, const double *
 // checked against the solve (equations, species, blocks and their sizes);
 // values are made nondimensional and the species density is rho * mf
 void ReadRestart(const Setup &s, const Solve &sv, const char *path, int *iteration,
-                 double *resid_first, double *const *prim_out) {
+                 double *resid_first, double *const *prim_out, int *levels,
+                 double *const *cons_nm1_out) {
   if (!path) throw Error(ATH_ERR_ARG, "null path");
   std::ifstream f(path, std::ios::in | std::ios::binary);
   if (!f) throw Error(ATH_ERR_IO, std::string("cannot open ") + path);
@@ -303,6 +331,31 @@ void ReadRestart(const Setup &s, const Solve &sv, const char *path, int *iterati
       w[0] = 0.0 + rho * x[nv];  // species density, then their sum
     }
   }
+  // ReadSolNm1FromRestart (src/output.cpp:1242): conserved values over
+  // their scales, the species density rho * mf
+  for (int k = 0; nsol >= 2 && cons_nm1_out && k < nb; ++k) {
+    const Block &b = s.blocks[sv.blocks[k]];
+    const size_t m = Cells(b);
+    std::vector<double> in(m * (nv + 1));
+    f.read(reinterpret_cast<char *>(in.data()), in.size() * 8);
+    if (!f) throw Error(ATH_ERR_IO, "restart file ends early");
+    if (!cons_nm1_out[k]) continue;
+    for (size_t q = 0; q < m; ++q) {
+      const double *x = &in[q * (nv + 1)];
+      double *u = cons_nm1_out[k] + q * nv;
+      const double rho = x[0] / sc.r;
+      u[1] = x[1] / (sc.a * sc.r);
+      u[2] = x[2] / (sc.a * sc.r);
+      u[3] = x[3] / (sc.a * sc.r);
+      u[4] = x[4] / (sc.r * sc.a * sc.a);
+      if (nv == 7) {
+        u[5] = x[5] / (sc.a * sc.a * sc.r);
+        u[6] = x[6] / (sc.a * sc.a * sc.r * sc.r / sc.mu);
+      }
+      u[0] = rho * x[nv];
+    }
+  }
+  if (levels) *levels = nsol;
   if (iteration) *iteration = iter;
   if (resid_first) std::memcpy(resid_first, rf.data(), neq * sizeof(double));
 }
@@ -362,10 +415,13 @@ std::string Sci(double x) {
 // PrintHeaders (src/output.cpp:1007) as the residual file gets it: the
 // file's header is written when the log opens, before the first CFL is set,
 // so it has no CFL column although every row carries one
-std::string ResidHeader(bool rans) {
+std::string ResidHeader(bool rans, bool time_step) {
   std::string h;
   Cell(h, "Step", 7);
   Cell(h, "NL-Iter", 8);
+  // the CFL column has no header: the reference prints the header while
+  // its CFL is still 0
+  if (time_step) Cell(h, "Time-Step", 12);
   for (const char *t : {"Res-Mass", "Res-Mom-X", "Res-Mom-Y", "Res-Mom-Z", "Res-Energy"})
     Cell(h, t, 12);
   if (rans) {
@@ -378,22 +434,28 @@ std::string ResidHeader(bool rans) {
   return h + "\n";
 }
 
-// PrintResiduals (src/output.cpp:1028): the normalisation is the first
-// step's L2, raised to the largest of each equation over steps 1-4; every
-// L2 is shown as (L2 + EPS) / (L2_first + EPS) with EPS = 1e-30
-std::string ResidLine(bool rans, int step, const ath_norms &nm, double *first) {
+// PrintResiduals (src/output.cpp:1028): time step nn, nonlinear iteration
+// mm; the normalisation is the L2 of the first time step's first nonlinear
+// iteration, raised to the largest of each equation over the first
+// nonlinear iterations of time steps 1-4 (never changed in a restarted
+// run); every L2 is shown as (L2 + EPS) / (L2_first + EPS), EPS = 1e-30;
+// the third column is the input's timeStep, or else the CFL
+std::string ResidLine(bool rans, int nn, int mm, double time_step, bool restarted,
+                      const ath_norms &nm, double *first) {
   const int nv = rans ? 7 : 5;
-  if (step == 0) {
-    for (int v = 0; v < nv; ++v) first[v] = nm.l2[v];
-  } else if (step < 5) {
-    if (nm.l2[0] > first[0]) first[0] = nm.l2[0];
-    for (int v = 1; v < nv; ++v) first[v] = first[v] < nm.l2[v] ? nm.l2[v] : first[v];
+  if (!restarted && mm == 0) {
+    if (nn == 0) {
+      for (int v = 0; v < nv; ++v) first[v] = nm.l2[v];
+    } else if (nn < 5) {
+      if (nm.l2[0] > first[0]) first[0] = nm.l2[0];
+      for (int v = 1; v < nv; ++v) first[v] = first[v] < nm.l2[v] ? nm.l2[v] : first[v];
+    }
   }
   const double eps = 1.0e-30;
   std::string r;
-  Cell(r, std::to_string(step), 7);
-  Cell(r, "0", 8);
-  Cell(r, Sci(nm.cfl), 12);
+  Cell(r, std::to_string(nn), 7);
+  Cell(r, std::to_string(mm), 8);
+  Cell(r, Sci(time_step > 0.0 ? time_step : nm.cfl), 12);
   for (int v = 0; v < nv; ++v) Cell(r, Sci((nm.l2[v] + eps) / (first[v] + eps)), 12);
   Cell(r, std::to_string(nm.linf_eqn), 8);
   Cell(r, std::to_string(nm.linf_block), 8);
@@ -407,14 +469,16 @@ std::string ResidLine(bool rans, int step, const ath_norms &nm, double *first) {
 
 // per-block fields of one solve gathered from a batch
 struct Gathered {
-  std::vector<std::vector<double>> prim, dt, resid, aux, velgrad, wd;
+  std::vector<std::vector<double>> prim, dt, resid, aux, velgrad, wd, nm1;
   std::vector<ath_block_fields> f;
 };
 
 void GatherFields(ath_batch *batch, const Setup &s, const Solve &sv, bool want_dt,
-                  bool want_resid, bool want_aux, bool want_velgrad, bool want_wd, Gathered &g) {
+                  bool want_resid, bool want_aux, bool want_velgrad, bool want_wd, Gathered &g,
+                  bool want_nm1 = false) {
   const size_t nb = sv.blocks.size();
   g.prim.resize(nb);
+  g.nm1.resize(nb);
   g.dt.resize(nb);
   g.resid.resize(nb);
   g.aux.resize(nb);
@@ -436,6 +500,7 @@ void GatherFields(ath_batch *batch, const Setup &s, const Solve &sv, bool want_d
     if (want_aux) g.f[k].aux = get(bi, ATH_FIELD_AUX, g.aux[k], 5);
     if (want_velgrad) g.f[k].velgrad = get(bi, ATH_FIELD_VELGRAD, g.velgrad[k], 9);
     if (want_wd) g.f[k].wall_dist = get(bi, ATH_FIELD_WALLDIST, g.wd[k], 1);
+    if (want_nm1) g.f[k].cons_nm1 = get(bi, ATH_FIELD_CONS_NM1, g.nm1[k], nv);
   }
 }
 
@@ -473,9 +538,11 @@ int ath_output_restart(const ath_setup *setup, int solve, int iteration,
 }
 
 int ath_input_restart(const ath_setup *setup, int solve, const char *path, int *iteration,
-                      double *resid_first, double *const *prim_out) {
+                      double *resid_first, double *const *prim_out, int *levels,
+                      double *const *cons_nm1_out) {
   return Guard([&] {
-    ReadRestart(setup->s, SolveOf(setup, solve), path, iteration, resid_first, prim_out);
+    ReadRestart(setup->s, SolveOf(setup, solve), path, iteration, resid_first, prim_out,
+                levels, cons_nm1_out);
   });
 }
 
@@ -491,17 +558,24 @@ int ath_output_meta(const ath_setup *setup, int solve, const char *variables, in
   });
 }
 
-int ath_output_resid(const ath_setup *setup, int solve, const char *path, int append,
+int ath_output_resid(const ath_setup *setup, int solve, const char *path, int flags,
                      int first_step, int n, const ath_norms *norms, double *resid_first) {
   return Guard([&] {
     const Solve &sv = SolveOf(setup, solve);
-    if (n < 0 || (n > 0 && !norms) || !resid_first) throw Error(ATH_ERR_ARG, "bad argument");
+    if (n < 0 || (n > 0 && !norms) || !resid_first || first_step < 0)
+      throw Error(ATH_ERR_ARG, "bad argument");
     if (!path) throw Error(ATH_ERR_ARG, "null path");
     const bool rans = sv.phys.nv == 7;
+    const bool append = (flags & ATH_RESID_APPEND) != 0;
+    const bool restarted = (flags & ATH_RESID_RESTARTED) != 0;
+    const int nl = std::max(1, (int)sv.phys.nl_iters);
     std::ofstream f(path, append ? std::ios::app : std::ios::out);
     if (!f) throw Error(ATH_ERR_IO, std::string("cannot open ") + path);
-    if (!append) f << ResidHeader(rans);
-    for (int k = 0; k < n; ++k) f << ResidLine(rans, first_step + k, norms[k], resid_first);
+    if (!append) f << ResidHeader(rans, sv.time_step > 0.0);
+    for (int k = 0; k < n; ++k) {
+      const int it = first_step + k;
+      f << ResidLine(rans, it / nl, it % nl, sv.time_step, restarted, norms[k], resid_first);
+    }
     if (!f) throw Error(ATH_ERR_IO, std::string("write failed: ") + path);
   });
 }
@@ -525,7 +599,8 @@ int ath_batch_write_restart(ath_batch *batch, const ath_setup *setup, int solve,
   return Guard([&] {
     const Solve &sv = SolveOf(setup, solve);
     Gathered g;
-    GatherFields(batch, setup->s, sv, false, false, false, false, false, g);
+    GatherFields(batch, setup->s, sv, false, false, false, false, false, g,
+                 sv.phys.multilevel != 0);
     WriteRestart(setup->s, sv, iteration, resid_first, g.f.data(), path);
   });
 }
@@ -534,16 +609,30 @@ int ath_batch_read_restart(ath_batch *batch, const ath_setup *setup, int solve,
                            const char *path, int *iteration, double *resid_first) {
   return Guard([&] {
     const Solve &sv = SolveOf(setup, solve);
-    std::vector<std::vector<double>> prim(sv.blocks.size());
-    std::vector<double *> ptr(sv.blocks.size());
-    for (size_t k = 0; k < sv.blocks.size(); ++k) {
+    const size_t nb = sv.blocks.size();
+    std::vector<std::vector<double>> prim(nb), nm1(nb);
+    std::vector<double *> ptr(nb), ptr1(nb);
+    for (size_t k = 0; k < nb; ++k) {
       const Block &b = setup->s.blocks[sv.blocks[k]];
       prim[k].resize(Cells(b) * b.nv);
       ptr[k] = prim[k].data();
+      if (sv.phys.multilevel) {
+        nm1[k].resize(Cells(b) * b.nv);
+        ptr1[k] = nm1[k].data();
+      }
     }
-    ReadRestart(setup->s, sv, path, iteration, resid_first, ptr.data());
-    for (size_t k = 0; k < sv.blocks.size(); ++k) {
+    int levels = 0;
+    ReadRestart(setup->s, sv, path, iteration, resid_first, ptr.data(), &levels,
+                sv.phys.multilevel ? ptr1.data() : nullptr);
+    for (size_t k = 0; k < nb; ++k) {
       const int rc = ath_batch_set_state(batch, sv.blocks[k], prim[k].data());
+      if (rc != ATH_OK) throw Error(rc, ath_last_error());
+    }
+    // bdf2: time n-1 from the file, or the state itself (ReadRestart
+    // src/output.cpp:869-895)
+    for (size_t k = 0; sv.phys.multilevel && k < nb; ++k) {
+      const int rc =
+          ath_batch_set_state_nm1(batch, sv.blocks[k], levels >= 2 ? nm1[k].data() : nullptr);
       if (rc != ATH_OK) throw Error(rc, ath_last_error());
     }
   });

@@ -1308,6 +1308,7 @@ void AppendInput(Setup &st, const std::string &path) {
   // global time step, nondimensional (procBlock::CalcBlockTimeStep,
   // src/procBlock.cpp:808)
   ph.dt_global = getd("timeStep", -1.0) > 0.0 ? getd("timeStep", -1.0) * aref / lref : 0.0;
+  sv.time_step = getd("timeStep", -1.0);
   ph.visc_cfl_coeff = ph.kappa == 1.0 ? 4.0 : (ph.kappa == -2.0 ? 2.0 : 1.0);
 
   // boundary states

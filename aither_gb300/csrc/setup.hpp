@@ -74,6 +74,7 @@ struct Solve {
   int output_freq = 1, restart_freq = 0, iterations = 1;
   std::string sim_root, grid_name;
   std::string species = "air";  // the one fluid of the case (fluids key)
+  double time_step = -1.0;      // timeStep as written (dimensional; <= 0: none)
   ath_solve_view phys{};  // states pointer refreshed on access
   std::vector<ath_bc_state> states;
   std::vector<BCStateIn> states_in;

@@ -358,10 +358,24 @@ enum {
   ATH_FIELD_VELGRAD = 8,
   /* wall distance (procBlock::CalcWallDistance src/procBlock.cpp:6030), 1;
    * 1e10 without viscous walls */
-  ATH_FIELD_WALLDIST = 9
+  ATH_FIELD_WALLDIST = 9,
+  /* conserved state of time n and of time n-1 (procBlock consVarsN_,
+   * consVarsNm1_), nv per cell (rho, rho u, rho v, rho w, rho E [, rho k,
+   * rho omega]); time-accurate solves only (time n-1: bdf2 solves) */
+  ATH_FIELD_CONS_N = 10,
+  ATH_FIELD_CONS_NM1 = 11
 };
 int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h);
 int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h);
+/* Sets the conserved state of time n-1 of a bdf2 solve's block (nv per
+ * cell, as ATH_FIELD_CONS_NM1; procBlock::GetSolNm1FromRestart
+ * src/procBlock.cpp:6418).  The solve then keeps it through its first
+ * time step instead of copying time n into it, as a restarted reference
+ * run does (mgSolution::StoreOldSolution src/mgSolution.cpp:103); set every
+ * block of the solve.  NULL cons_h copies the block's current state into
+ * time n-1 instead (the one-level restart of a bdf2 solve, ReadRestart
+ * src/output.cpp:892). */
+int ath_batch_set_state_nm1(ath_batch *batch, int block, const double *cons_h);
 /* Values per cell of `field` for block `block`: the block's nv (5, or 7
  * with the SST k and omega) for STATE, STATE_GHOSTS, RESID and DU. */
 int ath_batch_field_width(ath_batch *batch, int block, int field);
@@ -384,6 +398,8 @@ typedef struct {
   const double *aux;       /* 5 per cell: as ATH_FIELD_AUX */
   const double *velgrad;   /* 9 per cell: as ATH_FIELD_VELGRAD */
   const double *wall_dist; /* 1 per cell */
+  const double *cons_nm1;  /* nv per cell: conserved state of time n-1 (bdf2
+                              solves: the restart file's second level) */
 } ath_block_fields;
 
 /* Plot3D cell-centre function file (WriteFunFile, src/output.cpp:209) of
@@ -399,15 +415,21 @@ typedef struct {
 int ath_output_function(const ath_setup *setup, int solve, const char *variables,
                         const ath_block_fields *fields, const char *path);
 /* Restart file (WriteRestart, src/output.cpp:591): iteration, the L2
- * normalisation per equation (nv), dimensional primitives per cell. */
+ * normalisation per equation (nv), dimensional primitives per cell; for a
+ * bdf2 solve a second time level, the dimensional conserved state of time
+ * n-1 (fields[k].cons_nm1, required). */
 int ath_output_restart(const ath_setup *setup, int solve, int iteration,
                        const double *resid_first, const ath_block_fields *fields,
                        const char *path);
 /* Reads a restart file (ReadRestart, src/output.cpp:756) into prim_out[k]
  * (one nv-per-cell array per block of the solve, may be NULL), checking it
- * against the solve's equations, species and block sizes. */
+ * against the solve's equations, species and block sizes.  *levels (may be
+ * NULL) receives the file's time levels; with two, cons_nm1_out[k] (may be
+ * NULL) receives the nondimensional conserved state of time n-1
+ * (ReadSolNm1FromRestart, :1242). */
 int ath_input_restart(const ath_setup *setup, int solve, const char *path, int *iteration,
-                      double *resid_first, double *const *prim_out);
+                      double *resid_first, double *const *prim_out, int *levels,
+                      double *const *cons_nm1_out);
 /* Cell-centre grid (WriteCellCenter, src/output.cpp:57) and Paraview meta
  * file (WriteMeta, :903) naming <grid>_center.xyz and
  * <sim>_<iteration>_center.fun. */
@@ -415,10 +437,17 @@ int ath_output_center_grid(const ath_setup *setup, int solve, const char *path);
 int ath_output_meta(const ath_setup *setup, int solve, const char *variables, int iteration,
                     const char *path);
 /* Residual history (PrintHeaders / PrintResiduals, src/output.cpp:1007,
- * 1028): n rows for steps first_step.. from the solve's norms; a header
- * first unless append.  resid_first (nv) carries the normalisation: it is
- * set at step 0 and raised to each equation's largest L2 through step 4. */
-int ath_output_resid(const ath_setup *setup, int solve, const char *path, int append,
+ * 1028): n rows from the solve's norms of nonlinear iterations
+ * first_step.., each shown as time step it / nonlinearIterations and
+ * nonlinear iteration it % nonlinearIterations, with the input's timeStep
+ * (when given) or the CFL; a header first unless flags has
+ * ATH_RESID_APPEND.  resid_first (nv) carries the normalisation: set at
+ * the first time step's first nonlinear iteration and raised to each
+ * equation's largest L2 over the first nonlinear iterations of time steps
+ * 1-4, unless flags has ATH_RESID_RESTARTED (a run restarted from a file,
+ * whose normalisation the file gave). */
+enum { ATH_RESID_APPEND = 1, ATH_RESID_RESTARTED = 2 };
+int ath_output_resid(const ath_setup *setup, int solve, const char *path, int flags,
                      int first_step, int n, const ath_norms *norms, double *resid_first);
 /* The same from a batch's resident solution (fields gathered from the
  * device; the setup is the one the batch was created from). */
@@ -426,6 +455,9 @@ int ath_batch_write_function(ath_batch *batch, const ath_setup *setup, int solve
                              const char *variables, const char *path);
 int ath_batch_write_restart(ath_batch *batch, const ath_setup *setup, int solve,
                             int iteration, const double *resid_first, const char *path);
+/* The restart read into a batch sets the state and, for a bdf2 solve, time
+ * n-1: the file's second level, or the state itself when the file holds
+ * one (ath_batch_set_state_nm1). */
 int ath_batch_read_restart(ath_batch *batch, const ath_setup *setup, int solve,
                            const char *path, int *iteration, double *resid_first);
 

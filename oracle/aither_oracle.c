@@ -61,6 +61,7 @@ typedef struct {
   int rans;    /* SST-2003 turbulence equations */
   int sweeps;  /* matrixSweeps */
   int jacobi;  /* dplur / bdplur: Jacobi sweeps instead of LU-SGS */
+  int nm1_given; /* time n-1 set from a restart: kept at the first step */
 } osolve;
 
 struct orc_case {
@@ -1390,7 +1391,9 @@ void orc_fill_ghosts(orc_case *c) {
           prim_to_cons(&b->W[x * NV], &c->s[b->solve].gas, un);
           un[5] = b->Wt ? b->W[x * NV] * b->Wt[x * 2] : 0.0;
           un[6] = b->Wt ? b->W[x * NV] * b->Wt[x * 2 + 1] : 0.0;
-          if (v->multilevel && c->iter == 0) memcpy(&b->Unm1[x * 7], un, 8 * 7);
+          /* a restarted run keeps the file's time n-1 (!IsRestart()) */
+          if (v->multilevel && c->iter == 0 && !c->s[b->solve].nm1_given)
+            memcpy(&b->Unm1[x * 7], un, 8 * 7);
         }
   }
   NTH
@@ -2352,10 +2355,51 @@ int orc_get_field(orc_case *c, int block, int field, double *out) {
             memcpy(out + 9 * q, &b->vg[x * 9], 8 * 9);
             break;
           case ATH_FIELD_WALLDIST: out[q] = b->wd ? b->wd[x] : 1.0e10; break;
+          case ATH_FIELD_CONS_N:
+          case ATH_FIELD_CONS_NM1: {
+            const ath_solve_view *v = &c->s[b->solve].v;
+            const int nm1 = field == ATH_FIELD_CONS_NM1;
+            if (nm1 ? !v->multilevel : !(v->multilevel || v->nl_iters > 1))
+              return ATH_ERR_UNSUPPORTED;
+            memcpy(out + nv * q, nm1 ? &b->Unm1[x * 7] : &b->Un[x * 7], 8 * nv);
+            break;
+          }
           default: return ATH_ERR_ARG;
         }
         ++q;
       }
+  return 0;
+}
+
+/* Time n-1 of a bdf2 solve's block from a restart (GetSolNm1FromRestart,
+ * src/procBlock.cpp:6418; nv conserved values per cell), or, with cons
+ * NULL, the current state into both levels (AssignSolToTimeN and
+ * AssignSolToTimeNm1 of a one-level restart, src/output.cpp:892).  The
+ * solve then keeps time n-1 through its first time step. */
+int orc_set_state_nm1(orc_case *c, int block, const double *cons) {
+  if (block < 0 || block >= c->nb) return ATH_ERR_ARG;
+  oblock *b = &c->b[block];
+  osolve *sv = &c->s[b->solve];
+  if (!sv->v.multilevel) return ATH_ERR_UNSUPPORTED;
+  const int nv = b->Wt ? NV + 2 : NV;
+  size_t q = 0;
+  for (int k = 0; k < b->nk; ++k)
+    for (int j = 0; j < b->nj; ++j)
+      for (int i = 0; i < b->ni; ++i) {
+        const int64_t x = cell_idx(b, i, j, k);
+        double *um = &b->Unm1[x * 7];
+        if (cons) {
+          for (int v = 0; v < 7; ++v) um[v] = v < nv ? cons[nv * q + v] : 0.0;
+        } else {
+          double *un = &b->Un[x * 7];
+          prim_to_cons(&b->W[x * NV], &sv->gas, un);
+          un[5] = b->Wt ? b->W[x * NV] * b->Wt[x * 2] : 0.0;
+          un[6] = b->Wt ? b->W[x * NV] * b->Wt[x * 2 + 1] : 0.0;
+          memcpy(um, un, 8 * 7);
+        }
+        ++q;
+      }
+  sv->nm1_given = 1;
   return 0;
 }
 
@@ -2370,6 +2414,13 @@ int orc_set_state(orc_case *c, int block, const double *prim) {
         const int64_t x = cell_idx(b, i, j, k);
         memcpy(&b->W[x * NV], prim + nv * q, 8 * NV);
         if (b->Wt) memcpy(&b->Wt[x * 2], prim + nv * q + NV, 8 * 2);
+        /* temperature and viscosity of the loaded state, as after
+         * ReadRestart (gridLevel::AuxillaryAndWidths src/gridLevel.cpp:433);
+         * the lagged eddy viscosity stays that of the initial condition */
+        if (c->s[b->solve].viscous) {
+          b->T[x] = temp_of(&b->W[x * NV], &c->s[b->solve].gas);
+          b->mu[x] = visc_of(b->T[x], &c->s[b->solve].v);
+        }
         ++q;
       }
   return 0;

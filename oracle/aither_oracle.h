@@ -58,6 +58,7 @@ int orc_iterate(orc_case *c, int n, double *l2_out);
 /* Fields as in ath_batch_get_field (ATH_FIELD_*). */
 int orc_get_field(orc_case *c, int block, int field, double *out);
 int orc_set_state(orc_case *c, int block, const double *prim);
+int orc_set_state_nm1(orc_case *c, int block, const double *cons);
 
 #ifdef __cplusplus
 }

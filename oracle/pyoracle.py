@@ -13,9 +13,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(_HERE, "liboracle.so")
 FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
-             WALLDIST=9)
+             WALLDIST=9, CONS_N=10, CONS_NM1=11)
 WIDTH = dict(STATE=5, STATE_GHOSTS=5, RESID=5, DT=1, SPECRAD=2, DU=5, AINV=1, AUX=5, VELGRAD=9,
-             WALLDIST=1)
+             WALLDIST=1, CONS_N=5, CONS_NM1=5)
 
 _lib = None
 
@@ -47,6 +47,8 @@ def lib():
         L.orc_forces.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_set_state.restype = C.c_int
         L.orc_set_state.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        L.orc_set_state_nm1.restype = C.c_int
+        L.orc_set_state_nm1.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -110,7 +112,7 @@ class Oracle:
     def field(self, b: int, field: str) -> np.ndarray:
         v = self.setup.block_view(b)
         w = WIDTH[field]
-        if field in ("STATE", "STATE_GHOSTS", "RESID", "DU"):
+        if field in ("STATE", "STATE_GHOSTS", "RESID", "DU", "CONS_N", "CONS_NM1"):
             w = v.nv
         n = (v.ncell_padded if field == "STATE_GHOSTS" else v.ni * v.nj * v.nk) * w
         out = np.empty(n)
@@ -124,3 +126,13 @@ class Oracle:
     def set_state(self, b: int, prim: np.ndarray) -> None:
         prim = np.ascontiguousarray(prim, dtype=np.float64)
         lib().orc_set_state(self.h, b, _dp(prim))
+
+    def set_state_nm1(self, b: int, cons) -> None:
+        """Time n-1 of a bdf2 solve's block (None: the current state)."""
+        if cons is None:
+            rc = lib().orc_set_state_nm1(self.h, b, None)
+        else:
+            cons = np.ascontiguousarray(cons, dtype=np.float64)
+            rc = lib().orc_set_state_nm1(self.h, b, _dp(cons))
+        if rc:
+            raise RuntimeError(f"oracle time level error {rc}")

@@ -11,6 +11,13 @@ the files the reference wrote after N iterations:
     <sim>.resid            residual history (PrintHeaders / PrintResiduals)
     case.json              generator, arguments, iterations, variables
 
+Restart cases (bdf2, two time levels in the restart file) keep the restart
+file after N time steps and the one the reference wrote after M more time
+steps of a run restarted from it:
+
+    <sim>_<N>.rst, <sim>_<N+M>.rst, case.json
+    <sim>_<N>.resid, <sim>_<N+M>.resid   residual histories of the two runs
+
     python tests/golden/make_output_golden.py [--reference /path/to/aither]
 """
 from __future__ import annotations
@@ -52,6 +59,17 @@ CASES = [
 ]
 
 
+# (name, generator, kwargs, time steps before the restart, time steps after)
+RESTARTS = [
+    ("plate_bdf2_rst", "flat_plate",
+     dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, time="bdf2", dt=1e-4, nl=2, name="plate"),
+     3, 2),
+    ("sst_bdf2_rst", "flat_plate",
+     dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1, matrix_solver="blusgs", time="bdf2", dt=1e-5, nl=2, name="sst"), 3, 2),
+]
+
+
 def case_input(tmp: str, gen: str, kw: dict, iterations: int, variables: list) -> str:
     inp, _ = getattr(cases, gen)(tmp, **kw)
     cases.set_output_keys(inp, iterations, variables, restart_freq=iterations)
@@ -63,10 +81,44 @@ def main():
     ap.add_argument("--reference", default=REF_EXE)
     ap.add_argument("--install-dir", default=os.environ.get("AITHER_REFERENCE_SRC",
                                                             "/root/reference"))
+    ap.add_argument("--only", nargs="*", help="case names to (re)generate")
     args = ap.parse_args()
     os.makedirs(OUT, exist_ok=True)
     env = dict(os.environ, AITHER_INSTALL_DIRECTORY=args.install_dir)
+
+    def run(tmp, name, *argv):
+        r = subprocess.run([args.reference, *argv], cwd=tmp, env=env, capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{name}: reference failed\n{r.stdout[-2000:]}{r.stderr}")
+
+    for name, gen, kw, n1, n2 in RESTARTS:
+        if args.only and name not in args.only:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            inp = case_input(tmp, gen, kw, n1, ["density"])
+            cases.set_output_keys(inp, n1, ["density"], restart_freq=n1)
+            sim = os.path.splitext(os.path.basename(inp))[0]
+            run(tmp, name, os.path.basename(inp))
+            shutil.copy(os.path.join(tmp, f"{sim}.resid"), os.path.join(tmp, f"{sim}_{n1}.resid"))
+            cases.set_output_keys(inp, n2, ["density"], restart_freq=n2)
+            run(tmp, name, os.path.basename(inp), f"{sim}_{n1}.rst")
+            shutil.copy(os.path.join(tmp, f"{sim}.resid"),
+                        os.path.join(tmp, f"{sim}_{n1 + n2}.resid"))
+            dest = os.path.join(OUT, name)
+            shutil.rmtree(dest, ignore_errors=True)
+            os.makedirs(dest)
+            for fn in (f"{sim}_{n1}.rst", f"{sim}_{n1 + n2}.rst", f"{sim}_{n1}.resid",
+                       f"{sim}_{n1 + n2}.resid"):
+                shutil.copy(os.path.join(tmp, fn), os.path.join(dest, fn))
+            with open(os.path.join(dest, "case.json"), "w") as f:
+                json.dump({"generator": gen, "kwargs": kw, "steps": [n1, n2], "sim": sim}, f,
+                          indent=1)
+            print(name, "->", dest, sorted(os.listdir(dest)))
+
     for name, gen, kw, iters, variables in CASES:
+        if args.only is not None and name not in args.only:
+            continue
         with tempfile.TemporaryDirectory() as tmp:
             inp = case_input(tmp, gen, kw, iters, variables)
             r = subprocess.run([args.reference, os.path.basename(inp)], cwd=tmp, env=env,

@@ -134,3 +134,55 @@ def test_residual_history(run):
             else:
                 assert abs(float(g[c]) - float(w[c])) <= 1.5e-4 * abs(float(w[c])) + 1e-300, \
                     (c, gl, wl)
+
+
+def compare_restart(got, want, nv, nb):
+    """Header through the species name exactly, the normalisation to the
+    parity tolerance, block sizes exactly, every value of both time levels
+    to 1e-12."""
+    head = 16 + 8 + 3
+    assert len(got) == len(want) and got[:head] == want[:head]
+    o = head + 8 * nv
+    assert rel_err(np.frombuffer(got[head:o]), np.frombuffer(want[head:o])) <= TOL
+    assert got[o:o + 4 + 16 * nb] == want[o:o + 4 + 16 * nb]
+    d = o + 4 + 16 * nb
+    g = np.frombuffer(got[d:]).reshape(-1, nv + 1)
+    w = np.frombuffer(want[d:]).reshape(-1, nv + 1)
+    for v in range(nv + 1):
+        assert rel_err(g[:, v], w[:, v]) <= 1e-12, v
+
+
+@pytest.mark.parametrize("name", ["plate_bdf2_rst", "sst_bdf2_rst"])
+def test_bdf2_restart_device(name, ctx, tmp_path):
+    """bdf2 on the device: the restart file after N time steps (state and
+    time n-1 gathered from the device) against the reference's, then a
+    fresh batch restarted from the reference's file (state and time n-1
+    loaded) and run M more time steps against the reference's restarted
+    run."""
+    from test_output import restart_case, time_normalisation
+
+    from aither_gb300 import Batch, Setup
+    inp, meta = restart_case(name, tmp_path)
+    n1, n2 = meta["steps"]
+    nl, sim = meta["kwargs"]["nl"], meta["sim"]
+    s = Setup(inp)
+    nv, nb = s.solve_nv(0), len(s.solve_blocks(0))
+    b = Batch(ctx, s, 0)
+    norms = list(b.iterate(n1 * nl))
+    l2 = np.array([[x.l2[v] for v in range(nv)] for x in norms])
+    path = str(tmp_path / "a.rst")
+    b.write_restart(0, n1, time_normalisation(l2, nl), path)
+    compare_restart(open(path, "rb").read(),
+                    open(os.path.join(OUT, name, f"{sim}_{n1}.rst"), "rb").read(), nv, nb)
+    b.close()
+
+    fresh = Batch(ctx, s, 0)
+    it, rf = fresh.read_restart(0, os.path.join(OUT, name, f"{sim}_{n1}.rst"))
+    assert it == n1
+    fresh.iterate(n2 * nl)
+    path2 = str(tmp_path / "b.rst")
+    fresh.write_restart(0, n1 + n2, rf, path2)
+    compare_restart(open(path2, "rb").read(),
+                    open(os.path.join(OUT, name, f"{sim}_{n1 + n2}.rst"), "rb").read(), nv, nb)
+    fresh.close()
+    s.close()
