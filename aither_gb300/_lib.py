@@ -479,7 +479,8 @@ class Batch:
 
     def sweep_shape(self) -> dict:
         """LU-SGS sweep shape: mode 1 persistent (cluster CTAs per solve),
-        0 one launch per hyperplane."""
+        0 one launch per hyperplane, 2 the same with a group of lanes per
+        scalar cell."""
         m, t, c = C.c_int(), C.c_int(), C.c_int()
         check(lib().ath_batch_sweep_shape(self.h, C.byref(m), C.byref(t), C.byref(c)))
         return {"mode": m.value, "threads": t.value, "cluster": c.value}

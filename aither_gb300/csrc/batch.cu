@@ -128,7 +128,8 @@ struct BatchCore {
   int max_jsweeps = 0;  // largest matrixSweeps of the DP-LUR solves
   int sweep_threads = 128;  // CTA size of the per-plane sweep kernels (autotuned)
   // sweep shape: mode 1 = persistent (one cluster of cl_size CTAs of
-  // cl_threads per solve), 0 = one launch per hyperplane; autotuned
+  // cl_threads per solve), 0 = one launch per hyperplane, 2 = the same with
+  // a group of lanes per scalar cell (one per neighbour term); autotuned
   int sweep_mode = 0, cl_size = 1, cl_threads = 256;
   int2 *d_cl_items = nullptr;
   int32_t *d_cl_step_off = nullptr, *d_solve_step0 = nullptr, *d_solve_nsteps = nullptr;
@@ -403,6 +404,8 @@ class Runner : public RunnerBase {
       P_.dist_hi = m.Upload(dh);
     }
     P_.muq = m.Alloc<T>(c.L.any_viscous ? nq : 1);
+    // per-cell neighbour terms of the FP64 scalar sweeps
+    if (sizeof(T) == sizeof(double) && (c.kinds & 1)) P_.Npre = m.Alloc<T>(9 * nq);
     P_.qpos = m.Upload(c.L.qpos);
     P_.ghost_cell = m.Upload(c.L.ghost_cell);
     P_.ghost_src = m.Upload(c.L.ghost_src);
@@ -597,13 +600,13 @@ class Runner : public RunnerBase {
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.stream);
+                         c_.sweep_threads, c_.sweep_mode == 2, c_.stream);
       }
     } else {
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.stream);
+                         c_.sweep_threads, c_.sweep_mode == 2, c_.stream);
       }
     }
   }
@@ -1638,12 +1641,16 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     auto &c = batch->core;
     Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
     auto &run = *batch->run;
-    // candidates: one launch per hyperplane with CTAs of 32..256 threads, and
-    // the persistent sweep with clusters of 1..8 CTAs of 256 threads
+    // candidates: one launch per hyperplane with CTAs of 32..256 threads (a
+    // thread per scalar cell, or with scalar solves present a group of lanes
+    // per cell), and the persistent sweep with clusters of 1..8 CTAs of 256
+    // threads
     struct Shape {
       int mode, threads, cluster;
     };
     std::vector<Shape> cand = {{0, 32, 1}, {0, 64, 1}, {0, 128, 1}, {0, 256, 1}};
+    if (c.skinds & 1)
+      for (int t : {32, 64, 128, 256}) cand.push_back({2, t, 1});
     if (c.skinds)
       for (int cl : {1, 2, 4, 8})
         if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
@@ -1989,6 +1996,7 @@ size_t EstimateBatchBytes(const Setup &st, int precision) {
     if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);
     double qc = ts * (5 + 5 + 5 + 24 + 6 + 2 + 1) + 4.0 * 8;
     if (blk) qc += ts * (48 + (visc ? 9 : 0) + 150);  // + stored off-diagonal blocks
+    if (!blk && precision == ATH_PREC_FP64) qc += 8.0 * 9;  // neighbour terms of the sweeps
     if (ph.eqn == ATH_EQN_RANS) {
       // k, omega, their residual, radius, wall distance, inviscid fluxes
       // (FP64); viscous fluxes and per-face SST data; sweep arrays

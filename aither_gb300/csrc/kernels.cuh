@@ -113,6 +113,8 @@ struct Pools {
                     // row-major 5x5 inverse when the batch has block solves
   T *Aq;            // the main diagonal (matrix residual), same layout
   T *muq;           // [nq] laminar viscosity, q order
+  T *Npre;          // [9][nq] NbrPre of each cell (FP64 batches with scalar
+                    // solves; null otherwise)
   const T *dist_lo; // [3][nq] centre-to-centre distance along the lower face normal
   const T *dist_hi; // [3][nq] same for the upper face
   T *dUq;           // [5][nq] implicit update
@@ -178,9 +180,7 @@ __device__ __forceinline__ Prim<T> LoadW(const double *W, int64_t n, int64_t c) 
 template <typename T>
 __device__ __forceinline__ Gas<T> GasOf(const SolveDev &s) {
   Gas<T> g;
-  g.r = (T)s.gas_r;
-  g.n = (T)s.gas_n;
-  g.hf = (T)s.gas_hf;
+  g.Set((T)s.gas_r, (T)s.gas_n, (T)s.gas_hf);
   return g;
 }
 
@@ -207,12 +207,16 @@ __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block
 // One hyperplane of the LU-SGS forward / backward sweep
 // (lusgs::LUSGS_Forward/Backward, src/linearSolver.cpp:341,385); items are
 // (q index, block) pairs.  FULL: some solve runs more than one sweep, so
-// both triangles may enter a pass.  k_sweep serves scalar solves, k_sweepb
-// block solves.
+// both triangles may enter a pass.  k_sweep (a thread per cell) and
+// k_sweepg (a group of lanes per cell, one per neighbour term) serve scalar
+// solves, k_sweepb block solves.
 template <typename T, bool FULL>
 __global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward, int sweep);
+template <typename T, bool FULL>
+__global__ void k_sweepg(Pools<T> P, const int2 *items, int n, int forward, int sweep);
 template <typename T>
-__global__ void k_sweepb(Pools<T> P, const int2 *items, int n, int forward, int sweep);
+__global__ void k_sweepb(Pools<T> P, const int2 *items, int n, int forward, int sweep,
+                         int full_any);
 // Initial update x = A^-1 b of solves with more than one sweep, x = 0 for
 // the others (linearSolver::InitializeMatrixUpdate, src/linearSolver.cpp:111).
 template <typename T>
@@ -287,7 +291,7 @@ struct Launch {
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                    int ncta, int kinds, cudaStream_t s);
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                    bool full, int kinds, int threads, cudaStream_t s);
+                    bool full, int kinds, int threads, bool group, cudaStream_t s);
   // one pass of every LU-SGS solve as one launch: a cluster of `cluster`
   // CTAs of `threads` per solve walks its hyperplanes with cluster barriers
   static void SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,

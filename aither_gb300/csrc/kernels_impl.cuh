@@ -962,6 +962,24 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   P.Wq[4 * nq + q] = w.p;
 #pragma unroll
   for (int v = 0; v < 5; ++v) P.Rq[v * nq + q] = (T)P.R[v * n + c];
+  // the cell's state terms of the off-diagonal contributions it makes as a
+  // neighbour in the scalar sweeps (FP64 batches)
+  if constexpr (!BLOCK) {
+    if (P.Npre) {
+      const Gas<T> gq = GasOf<T>(sv);
+      T cc[5];
+      PrimToCons(w, gq, cc);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) P.Npre[v * nq + q] = cc[v];
+      P.Npre[5 * nq + q] = Enthalpy(w, gq);
+      P.Npre[6 * nq + q] = SoS(w, gq);
+      if (sv.viscous) {
+        P.Npre[7 * nq + q] = ViscMaxTerm(w, gq);
+        P.Npre[8 * nq + q] =
+            ViscTerm2(P.muq[q], rans ? P.mutq[q] : T(0), (T)sv.visc_scale, gq);
+      }
+    }
+  }
 }
 
 // Right-hand side b of the linear system for equation v (flow 0-4, k and
@@ -987,6 +1005,8 @@ struct Nbr {
   T du[5], dut[2];
   T mu, mut, f1;
   int64_t vq;  // q index whose cell-averaged gradient the neighbour carries
+  bool has_pre;    // pre holds the neighbour's precomputed state terms
+  NbrPre<T> pre;
 };
 template <typename T>
 __device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, int32_t nb,
@@ -1009,7 +1029,19 @@ __device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, i
       o.dut[1] = P.dUtq[nq + nb];
     }
     cq = nb;
+    o.has_pre = P.Npre != nullptr;
+    if (o.has_pre) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) o.pre.c[v] = P.Npre[v * nq + nb];
+      o.pre.h = P.Npre[5 * nq + nb];
+      o.pre.sos = P.Npre[6 * nq + nb];
+      if (sv.viscous) {
+        o.pre.vmax = P.Npre[7 * nq + nb];
+        o.pre.vt2 = P.Npre[8 * nq + nb];
+      }
+    }
   } else {
+    o.has_pre = false;
     const int64_t slot = -(int64_t)nb - 2;
     o.s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
 #pragma unroll
@@ -1061,11 +1093,15 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
     const T mag = f[3 * nq + q];
     // ViscFaceSpectralRadius (include/spectralRadius.hpp:126) across this
     // face, ProjC2CDist as the length
-    const T vsr = sv.viscous ? mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
-                                   ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g)
-                             : T(0);
+    const T vsr = !sv.viscous ? T(0)
+                  : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
+                              : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
+                                    ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g);
     T r[5];
-    ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+    if (o.has_pre)
+      ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+    else
+      ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
 #pragma unroll
     for (int v = 0; v < 5; ++v) acc[v] = acc[v] + r[v];
     if (sv.rans) {
@@ -1080,6 +1116,43 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
       for (int k = 0; k < 2; ++k) acct[k] = acct[k] + (lower ? o.dut[k] * sr : -(o.dut[k] * sr));
     }
   }
+}
+
+// The term of one neighbour (face d) of OffDiagSum, for the grouped sweep
+// that gives each neighbour its own lane: r (flow) and rt (turbulence) as
+// OffDiagSum adds them; false where the cell has no neighbour (nb == -1)
+template <typename T>
+__device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, const SolveDev &sv,
+                                        int64_t q, bool lower, int d, T r[5], T rt[2]) {
+  const int64_t nq = P.nq;
+  const int32_t nb = P.nbq[(lower ? 0 : 3 * nq) + d * nq + q];
+  if (nb == -1) return false;
+  Nbr<T> o;
+  LoadNbr(P, sv, nb, o);
+  const T *f = (lower ? P.face_lo : P.face_hi) + (int64_t)d * 4 * nq;
+  const T *dist = lower ? P.dist_lo : P.dist_hi;
+  const T mag = f[3 * nq + q];
+  const T vsr = !sv.viscous ? T(0)
+                : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
+                            : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
+                                  ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g);
+  if (o.has_pre)
+    ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+  else
+    ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+  rt[0] = rt[1] = T(0);
+  if (sv.rans) {
+    const T vn = Dot(o.s.u, o.s.v, o.s.w, f[q], f[nq + q], f[2 * nq + q]);
+    T sr = lower ? T(0.5) * mag * fabs(vn + fabs(vn)) : T(0.5) * mag * fabs(vn - fabs(vn));
+    if (sv.viscous) {
+      const T length = mag / dist[d * nq + q];
+      const T sk = o.f1 * T(0.85) + (T(1) - o.f1) * T(1.0);
+      sr += (T)sv.visc_scale * length / o.s.rho * (o.mu + sk * o.mut);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) rt[k] = lower ? o.dut[k] * sr : -(o.dut[k] * sr);
+  }
+  return true;
 }
 
 // Off-diagonal Jacobians of one neighbour of a block solve's cell
@@ -1225,20 +1298,19 @@ __device__ __forceinline__ void OffDiagSumBlock(const Pools<T> &P, const SolveDe
 // LU-SGS hyperplane sweep on the q-ordered working set.  A pass uses one
 // triangle (sweep 0 of a one-sweep solve: forward x = A^-1 (b + L x),
 // backward x -= A^-1 U x) or both (x = A^-1 (b + L x - U x)).
+// New update of one cell of a scalar LU-SGS pass from its off-diagonal
+// sums: acc over the pass's triangle, other over the opposite one (used
+// from the second sweep on, or with several sweeps)
 template <typename T, bool FULL>
-__device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
-                                             int forward, int sweep) {
-  const Gas<T> g = GasOf<T>(sv);
+__device__ __forceinline__ void ScalarFinish(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                             int forward, bool both, const T acc[5],
+                                             const T acct[2], const T other[5],
+                                             const T othert[2]) {
   const int64_t nq = P.nq;
-  T acc[5], acct[2];
-  OffDiagSum(P, g, sv, q, forward != 0, acc, acct);
   const T ainv = P.Ainvq[q];
   const T thetaInv = (T)(1.0 / sv.theta);
   if constexpr (FULL) {
-    if (sweep >= sv.sweeps) return;
-    if (sweep > 0 || sv.sweeps > 1) {
-      T other[5], othert[2];
-      OffDiagSum(P, g, sv, q, forward == 0, other, othert);
+    if (both) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const T bv = RhsB(P, sv, thetaInv, v, q);
@@ -1287,6 +1359,23 @@ __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &
     }
   }
 }
+
+template <typename T, bool FULL>
+__device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
+                                             int forward, int sweep) {
+  const Gas<T> g = GasOf<T>(sv);
+  T acc[5], acct[2], other[5], othert[2];
+  OffDiagSum(P, g, sv, q, forward != 0, acc, acct);
+  bool both = false;
+  if constexpr (FULL) {
+    if (sweep >= sv.sweeps) return;
+    both = sweep > 0 || sv.sweeps > 1;
+    if (both) OffDiagSum(P, g, sv, q, forward == 0, other, othert);
+  }
+  ScalarFinish<T, FULL>(P, sv, q, forward, both, acc, acct, other, othert);
+}
+
+// one plane of every scalar solve, one thread per cell
 template <typename T, bool FULL>
 __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, int n_items,
                                                int forward, int sweep) {
@@ -1296,6 +1385,108 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
   if (sv.block || sv.jacobi || !sv.active) return;
   SweepScalarQ<T, FULL>(P, sv, it.x, forward, sweep);
+}
+
+// Scalar pass with a group of lanes per cell: lane d (0-2) evaluates the
+// term of neighbour d of the pass's triangle and, when both triangles
+// enter (FULL sweeps after the first, or several sweeps), lane 3 + d that
+// of the opposite one; the group's first lane sums the terms in i, j, k
+// order from zero and updates the cell -- SweepScalarQ's arithmetic, with
+// the three (six) independent neighbour terms in parallel, so a plane
+// keeps three (six) times as many warps busy: the faster form where a
+// plane has too few cells to fill the SMs (the autotuner chooses).  A warp
+// holds 10 (5) groups; its last 2 lanes idle.  Every lane of the warp
+// reaches the shuffles.
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(256) k_sweepg(Pools<T> P, const int2 *items, int n_items,
+                                                int forward, int sweep) {
+  constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = (int)(threadIdx.x & 31);
+  const int c = (t >> 5) * CPW + lane / L, li = lane % L;
+  bool valid = lane < CPW * L && c < n_items;
+  const int2 it = valid ? items[c] : make_int2(0, 0);
+  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  valid = valid && !sv.block && !sv.jacobi && sv.active;
+  bool both = false;
+  if constexpr (FULL) {
+    valid = valid && sweep < sv.sweeps;
+    both = sweep > 0 || sv.sweeps > 1;
+  }
+  const int side = li / 3, d = li % 3;
+  const bool lower = side == 0 ? forward != 0 : forward == 0;
+  const Gas<T> g = GasOf<T>(sv);
+  T r[5] = {T(0), T(0), T(0), T(0), T(0)}, rt[2] = {T(0), T(0)};
+  int have = 0;
+  if (valid && (side == 0 || both)) have = NbrTerm(P, g, sv, it.x, lower, d, r, rt);
+  const int g0 = lane < CPW * L ? lane - li : lane;
+  T acc[5], acct[2], other[5], othert[2];
+#pragma unroll
+  for (int s2 = 0; s2 < (FULL ? 2 : 1); ++s2) {
+    T *a = s2 == 0 ? acc : other, *at = s2 == 0 ? acct : othert;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) a[v] = T(0);
+    at[0] = at[1] = T(0);
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) {
+      const int src = g0 + 3 * s2 + dd;
+      const int h = __shfl_sync(0xffffffffu, have, src);
+      T x[5], xt[2];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) x[v] = __shfl_sync(0xffffffffu, r[v], src);
+#pragma unroll
+      for (int k = 0; k < 2; ++k) xt[k] = __shfl_sync(0xffffffffu, rt[k], src);
+      if (h) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) a[v] = a[v] + x[v];
+        if (sv.rans) {
+#pragma unroll
+          for (int k = 0; k < 2; ++k) at[k] = at[k] + xt[k];
+        }
+      }
+    }
+  }
+  if (!valid || li != 0) return;
+  ScalarFinish<T, FULL>(P, sv, it.x, forward, both, acc, acct, other, othert);
+}
+
+// Loads of one row of a block sweep that depend on the cell alone: the
+// neighbour indices and the stored Jacobian row of each neighbour of one
+// triangle.  They are issued before the solve's flags are read, so the
+// cell's chain of dependent loads (neighbour index, then its update) does
+// not wait behind the solve lookup.  Rows 5-6 read the turbulence
+// Jacobians only in batches that hold them.
+template <typename T>
+struct BlockRowPre {
+  int32_t nb[3];
+  T j[3][5];
+};
+template <typename T>
+__device__ __forceinline__ void PreloadBlockRow(const Pools<T> &P, int64_t q, bool lower,
+                                                int row, BlockRowPre<T> &o) {
+  const int64_t nq = P.nq;
+  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
+  const int side = lower ? 0 : 1;
+  const bool turb = row >= 5;
+  const int r = turb ? row - 5 : row;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) o.nb[d] = nbq[d * nq + q];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) o.j[d][c] = T(0);
+    if (turb) {
+      if (P.Jtoff) {
+        const T *Jt = P.Jtoff + ((int64_t)(side * 3 + d) * 4 + r * 2) * nq + q;
+        o.j[d][0] = Jt[0];
+        o.j[d][1] = Jt[nq];
+      }
+    } else {
+      const T *J = P.Joff + ((int64_t)(side * 3 + d) * kJac + r * 5) * nq + q;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) o.j[d][c] = J[c * nq];
+    }
+  }
 }
 
 // Block version, one 8-lane group per cell: lanes 0-4 own the flow rows,
@@ -1309,28 +1500,22 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
 // call this (the shuffles name the whole warp); `valid` marks lanes of a
 // group that owns a cell of this solve and pass.
 template <typename T>
-__device__ __forceinline__ T BlockRowOffDiag(const Pools<T> &P, const SolveDev &sv, int64_t q,
-                                             bool lower, int row) {
+__device__ __forceinline__ T BlockRowOffDiag(const Pools<T> &P, const BlockRowPre<T> &pre,
+                                             bool turb) {
   const int64_t nq = P.nq, ng = P.nghost;
-  const int32_t *nbq = P.nbq + (lower ? 0 : 3 * nq);
-  const int side = lower ? 0 : 1;
-  const bool turb = row >= 5;
-  const int r = turb ? row - 5 : row;
-  int32_t nb[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) nb[d] = nbq[d * nq + q];
+  const int nv = turb ? 2 : 5;
   T du[3][5];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    if (nb[d] == -1) continue;
-    const int nv = turb ? 2 : 5;
+    const int32_t nb = pre.nb[d];
+    if (nb == -1) continue;
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       if (v >= nv) break;
-      if (nb[d] >= 0)
-        du[d][v] = turb ? P.dUtq[v * nq + nb[d]] : P.dUq[v * nq + nb[d]];
+      if (nb >= 0)
+        du[d][v] = turb ? P.dUtq[v * nq + nb] : P.dUq[v * nq + nb];
       else {
-        const int64_t slot = -(int64_t)nb[d] - 2;
+        const int64_t slot = -(int64_t)nb - 2;
         du[d][v] = turb ? P.dUtg[v * ng + slot] : P.dUg[v * ng + slot];
       }
     }
@@ -1338,37 +1523,58 @@ __device__ __forceinline__ T BlockRowOffDiag(const Pools<T> &P, const SolveDev &
   T acc = T(0);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    if (nb[d] == -1) continue;
+    if (pre.nb[d] == -1) continue;
     T s = T(0);
     if (turb) {
-      const T *Jt = P.Jtoff + ((int64_t)(side * 3 + d) * 4 + r * 2) * nq + q;
-      s = s + Jt[0] * du[d][0];
-      s = s + Jt[nq] * du[d][1];
+      s = s + pre.j[d][0] * du[d][0];
+      s = s + pre.j[d][1] * du[d][1];
     } else {
-      const T *J = P.Joff + ((int64_t)(side * 3 + d) * kJac + r * 5) * nq + q;
 #pragma unroll
-      for (int c = 0; c < 5; ++c) s = s + J[c * nq] * du[d][c];
+      for (int c = 0; c < 5; ++c) s = s + pre.j[d][c] * du[d][c];
     }
     acc = acc + s;
   }
   return acc;
 }
 
+// Row `row` of one cell of a block pass.  `sv` may still be in flight:
+// everything read before its flags depends on the cell alone.  item: the
+// lane's group has a cell (q valid); valid: its solve takes part in this
+// pass.  full_any: some solve of the launch runs both triangles (preload
+// the other one too).
 template <typename T>
 __device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev &sv, int64_t q,
-                                              bool valid, int row, int forward, int sweep) {
+                                              bool item, bool valid, int row, int forward,
+                                              int sweep, bool full_any) {
   const int64_t nq = P.nq;
-  const bool full = sweep > 0 || sv.sweeps > 1;
-  const T thetaInv = (T)(1.0 / sv.theta);
   const int lane = (int)(threadIdx.x & 31), g0 = lane & ~7;
   const bool turb = row == 5 || row == 6;
+  const int r = turb ? row - 5 : row;
+  BlockRowPre<T> pre, pre_o;
+  T ainv[5] = {T(0), T(0), T(0), T(0), T(0)};
+  if (item && row < 7) {
+    PreloadBlockRow(P, q, forward != 0, row, pre);
+    if (full_any) PreloadBlockRow(P, q, forward == 0, row, pre_o);
+    if (turb) {
+      if (P.Ainvtq) {
+        ainv[0] = P.Ainvtq[(r * 2) * nq + q];
+        ainv[1] = P.Ainvtq[(r * 2 + 1) * nq + q];
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 5; ++c) ainv[c] = P.Ainvq[(row * 5 + c) * nq + q];
+    }
+  }
+  const bool full = sweep > 0 || sv.sweeps > 1;
+  const T thetaInv = (T)(1.0 / sv.theta);
   const bool mine = valid && (row < 5 || (turb && sv.rans));
   T in = T(0);
   if (mine) {
-    const T acc = BlockRowOffDiag(P, sv, q, forward != 0, row);
+    const T acc = BlockRowOffDiag(P, pre, turb);
     const T bv = RhsB(P, sv, thetaInv, row, q);
     if (full) {
-      const T other = BlockRowOffDiag(P, sv, q, forward == 0, row);
+      if (!full_any) PreloadBlockRow(P, q, forward == 0, row, pre_o);
+      const T other = BlockRowOffDiag(P, pre_o, turb);
       in = forward ? bv + (acc - other) : (bv + other) - acc;
     } else {
       in = forward ? bv + acc : acc;
@@ -1382,14 +1588,13 @@ __device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev 
   if (!mine) return;
   T x = T(0);
   if (turb) {
-    const int r = row - 5;
-    x = x + P.Ainvtq[(r * 2) * nq + q] * v2[0];
-    x = x + P.Ainvtq[(r * 2 + 1) * nq + q] * v2[1];
+    x = x + ainv[0] * v2[0];
+    x = x + ainv[1] * v2[1];
     T *dst = P.dUtq + r * nq + q;
     *dst = (full || forward) ? x : *dst - x;
   } else {
 #pragma unroll
-    for (int c = 0; c < 5; ++c) x = x + P.Ainvq[(row * 5 + c) * nq + q] * v5[c];
+    for (int c = 0; c < 5; ++c) x = x + ainv[c] * v5[c];
     T *dst = P.dUq + row * nq + q;
     *dst = (full || forward) ? x : *dst - x;
   }
@@ -1398,15 +1603,15 @@ __device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev 
 // one plane of every block solve: thread 8 c + r handles row r of item c
 template <typename T>
 __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, int n_items,
-                                                int forward, int sweep) {
+                                                int forward, int sweep, int full_any) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = t >> 3, row = t & 7;
-  bool valid = c < n_items;
+  const bool item = c < n_items;
   int2 it = make_int2(0, 0);
-  if (valid) it = items[c];
+  if (item) it = items[c];
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
-  valid = valid && sv.block && !sv.jacobi && sv.active && sweep < sv.sweeps;
-  SweepBlockRow<T>(P, sv, it.x, valid, row, forward, sweep);
+  const bool valid = item && sv.block && !sv.jacobi && sv.active && sweep < sv.sweeps;
+  SweepBlockRow<T>(P, sv, it.x, item, valid, row, forward, sweep, full_any != 0);
 }
 
 // Persistent sweep: one thread-block cluster per solve walks the solve's
@@ -1414,7 +1619,7 @@ __global__ void __launch_bounds__(256) k_sweepb(Pools<T> P, const int2 *items, i
 // each plane, with a cluster barrier (release/acquire at cluster scope, so
 // a plane's updates are visible to the next plane's readers) between
 // planes.  One launch per pass for every solve of the batch instead of one
-// launch per hyperplane; each cell runs the same arithmetic as k_sweep /
+// launch per hyperplane; each cell runs the same arithmetic as k_sweepg /
 // k_sweepb.  Every exit condition depends on the solve alone, so either all
 // CTAs of a cluster leave before the first barrier or none does.
 template <typename T, bool FULL, bool BLOCK>
@@ -1439,7 +1644,8 @@ __global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
       // 8-lane groups; every lane runs the same number of rounds
       for (int i0 = a; i0 < b; i0 += nthr >> 3) {
         const int i = i0 + (tid >> 3);
-        SweepBlockRow<T>(P, sv, i < b ? items[i].x : 0, i < b, tid & 7, forward, sweep);
+        SweepBlockRow<T>(P, sv, i < b ? items[i].x : 0, i < b, i < b, tid & 7, forward, sweep,
+                         FULL);
       }
     } else {
       for (int i = a + tid; i < b; i += nthr) SweepScalarQ<T, FULL>(P, sv, items[i].x, forward, sweep);
@@ -2336,16 +2542,21 @@ void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_
 }
 template <typename T>
 void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                      bool full, int kinds, int threads, cudaStream_t s) {
+                      bool full, int kinds, int threads, bool group, cudaStream_t s) {
   if (n <= 0) return;
-  const unsigned grid = (unsigned)((n + threads - 1) / threads);
-  if (kinds & 1) {
+  if ((kinds & 1) && group) {
+    const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
+    const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
+    if (full) k_sweepg<T, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweepg<T, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+  } else if (kinds & 1) {
+    const unsigned grid = (unsigned)((n + threads - 1) / threads);
     if (full) k_sweep<T, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
     else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
   if (kinds & 2) {
     const unsigned gridb = (unsigned)(((int64_t)n * 8 + threads - 1) / threads);
-    k_sweepb<T><<<gridb, threads, 0, s>>>(P, items, n, forward, sweep);
+    k_sweepb<T><<<gridb, threads, 0, s>>>(P, items, n, forward, sweep, full ? 1 : 0);
   }
 }
 template <typename T, bool FULL, bool BLOCK>

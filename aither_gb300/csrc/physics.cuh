@@ -20,10 +20,21 @@ struct Gas {
   T n;   // cv / R
   T hf;  // nondimensional heat of formation
   // caloricallyPerfect::SpeciesCv / SpeciesCp (include/thermodynamic.hpp:110-115)
-  __device__ __forceinline__ T Cv() const { return r * n; }
-  __device__ __forceinline__ T Cp() const { return r * (n + T(1)); }
-  // thermodynamic::Gamma (include/thermodynamic.hpp:58)
-  __device__ __forceinline__ T Gamma() const { return Cp() / Cv(); }
+  // and thermodynamic::Gamma (include/thermodynamic.hpp:58), formed once by
+  // Set() with the reference's expressions: cv = R n, cp = R (n + 1),
+  // gamma = cp / cv
+  T cv, cp, gam;
+  __device__ __forceinline__ void Set(T r_, T n_, T hf_) {
+    r = r_;
+    n = n_;
+    hf = hf_;
+    cv = r * n;
+    cp = r * (n + T(1));
+    gam = cp / cv;
+  }
+  __device__ __forceinline__ T Cv() const { return cv; }
+  __device__ __forceinline__ T Cp() const { return cp; }
+  __device__ __forceinline__ T Gamma() const { return gam; }
 };
 
 template <typename T>
@@ -605,6 +616,16 @@ __device__ __forceinline__ T InvFaceSpecRad(const Prim<T> &s, const Gas<T> &g,
   return T(0.5) * mag * (fabs(Dot(s.u, s.v, s.w, nx, ny, nz)) + SoS(s, g));
 }
 
+// Terms of a neighbour's off-diagonal contribution that depend on its state
+// alone, formed once per cell and iteration for the FP64 scalar sweeps
+// (each cell is the neighbour of up to six off-diagonal terms): conserved
+// state, enthalpy, speed of sound; viscous solves also ViscMaxTerm and
+// ViscTerm2.  Each is the value the term itself would form.
+template <typename T>
+struct NbrPre {
+  T c[5], h, sos, vmax, vt2;
+};
+
 // F(W') - F(W) with W' = prim(cons(W) + dU) (ConvectiveFluxUpdate,
 // include/inviscidFlux.hpp:544) rewritten exactly in terms of the
 // increments, for the FP32 sweeps: every term carries a factor of dU, so the
@@ -658,6 +679,38 @@ __device__ __forceinline__ void ScalarOffDiag(const Prim<T> &s, const T du[5],
   const T half = T(0.5) * mag;
   T lam = InvFaceSpecRad(s, g, nx, ny, nz, mag);
   lam += visc_sr;  // FaceSpectralRadius (include/spectralRadius.hpp:182)
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const T fc = half * df[v];
+    out[v] = positive ? fc + lam * du[v] : fc - lam * du[v];
+  }
+}
+
+// ScalarOffDiag with the neighbour's precomputed state terms (FP64): the
+// same operations, with cons(W), H(W) and a(W) read instead of re-formed
+template <typename T>
+__device__ __forceinline__ void ScalarOffDiagPre(const Prim<T> &s, const NbrPre<T> &pre,
+                                                 const T du[5], const Gas<T> &g, T nx, T ny,
+                                                 T nz, T mag, bool positive, T visc_sr,
+                                                 T out[5]) {
+  T c[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) c[v] = pre.c[v] + du[v];
+  const Prim<T> su = ConsToPrim(c, g);
+  T fo[5], fn[5];
+  const T vn = Dot(s.u, s.v, s.w, nx, ny, nz);
+  fo[0] = s.rho * vn;
+  fo[1] = s.rho * vn * s.u + s.p * nx;
+  fo[2] = s.rho * vn * s.v + s.p * ny;
+  fo[3] = s.rho * vn * s.w + s.p * nz;
+  fo[4] = s.rho * vn * pre.h;
+  InvFlux(su, g, nx, ny, nz, fn);
+  T df[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) df[v] = fn[v] - fo[v];
+  const T half = T(0.5) * mag;
+  T lam = T(0.5) * mag * (fabs(vn) + pre.sos);
+  lam += visc_sr;
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     const T fc = half * df[v];

@@ -277,7 +277,8 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
  * persistent sweep sized to its largest hyperplane. */
 int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
 /* Current sweep shape: mode 1 persistent (cluster = CTAs per solve), 0 one
- * launch per hyperplane (cluster = 0). */
+ * launch per hyperplane (cluster = 0), 2 one launch per hyperplane with a
+ * group of lanes per scalar-solve cell, one per neighbour term. */
 int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster);
 
 /* ---- serving ------------------------------------------------------------
