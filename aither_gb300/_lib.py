@@ -38,7 +38,14 @@ class BCState(C.Structure):
                 ("wall_u", C.c_double), ("wall_v", C.c_double), ("wall_w", C.c_double),
                 ("wall_t", C.c_double), ("wall_q", C.c_double),
                 ("isothermal", C.c_int32), ("heat_flux", C.c_int32),
-                ("turb_intensity", C.c_double), ("eddy_visc_ratio", C.c_double)]
+                ("turb_intensity", C.c_double), ("eddy_visc_ratio", C.c_double),
+                ("nonreflecting", C.c_int32), ("pad_nr", C.c_int32),
+                ("length_scale", C.c_double)]
+
+
+class NrCell(C.Structure):
+    _fields_ = [("cell", C.c_int64), ("face", C.c_int64), ("surf", C.c_int32),
+                ("dir", C.c_int32), ("lower", C.c_int32), ("pad", C.c_int32)]
 
 
 class SolveView(C.Structure):
@@ -74,7 +81,8 @@ class BlockView(C.Structure):
                 ("nvedge_ops", C.c_int32), ("vedge_ops", C.POINTER(GhostOp)),
                 ("nplanes", C.c_int32), ("plane_offsets", C.POINTER(C.c_int32)),
                 ("plane_cells", C.POINTER(C.c_int32)),
-                ("nbr_mask", C.POINTER(C.c_uint8))]
+                ("nbr_mask", C.POINTER(C.c_uint8)),
+                ("n_nr", C.c_int32), ("nr", C.POINTER(NrCell))]
 
 
 class Norms(C.Structure):

@@ -235,8 +235,12 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                  cfl: float = 20.0, name: str = "bump", recon: str = "thirdOrder",
                  limiter: str = "minmod", flux: str = "roe", matrix_solver: str = "lusgs",
                  sweeps: int = 1, inflow: str = "characteristic",
-                 outflow: str = "characteristic", back_pressure: float = 1.0):
-    """Inviscid channel over a sin^2 bump.  Inflow at i = 0 and outflow at
+                 outflow: str = "characteristic", back_pressure: float = 1.0,
+                 nonreflecting: float | None = None, time: str = "implicitEuler",
+                 dt: float | None = None, nl: int = 1):
+    """Inviscid channel over a sin^2 bump.  `nonreflecting` (a length in
+    metres) makes the inlet nonreflecting with that lengthScale; time, dt
+    and nl select the time integration.    Inflow at i = 0 and outflow at
     i = ni are characteristic far fields, or (inflow "stagnation") a
     stagnation inlet at the freestream's total pressure and temperature
     along +x, (inflow "inlet") the reference's inlet boundary with the
@@ -261,8 +265,10 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                       "direction=[1, 0, 0])")
         in_bc = ("stagnationInlet", 0, 0, 0, nj, 0, nk, 3)
     elif inflow == "inlet":
+        nr = (f"; nonreflecting=true; lengthScale={_fmt(nonreflecting)}"
+              if nonreflecting else "")
         states.append(f"inlet(tag=3; pressure={_fmt(p_inf)}; density={_fmt(refs.r_ref)}; "
-                      f"velocity={vel})")
+                      f"velocity={vel}{nr})")
         in_bc = ("inlet", 0, 0, 0, nj, 0, nk, 3)
     if outflow == "pressure":
         states.append(f"pressureOutlet(tag=4; pressure={_fmt(back_pressure * p_inf)})")
@@ -275,7 +281,8 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
     inp = os.path.join(outdir, name + ".inp")
     write_input(inp, name, {"cfl": cfl, "limiter": limiter, "faceReconstruction": recon,
                             "inviscidFlux": flux, "matrixSolver": matrix_solver,
-                            "matrixSweeps": sweeps}, refs, ic, states, bcs)
+                            "matrixSweeps": sweeps, **time_keys(time, dt, nl)},
+                refs, ic, states, bcs)
     return inp, None
 
 

@@ -89,6 +89,9 @@ struct Lists {
   std::vector<int32_t> solve_cta0;
   std::vector<GhostOpDev> ops, conn_ops;
   std::vector<int32_t> op_solve;
+  // nonreflecting surfaces: their cells grouped by surface, offsets
+  std::vector<NrDev> nr;
+  std::vector<int32_t> nr_off;
   // hyperplane-ordered sweep tables
   std::vector<int64_t> q0;        // per block: first q index
   std::vector<int32_t> qpos;      // per pool cell
@@ -138,7 +141,7 @@ struct BatchCore {
   }
   bool block_viscous = false;
   bool any_rans = false;  // SST solves present: k, omega pools allocated
-  bool any_unsteady = false;  // time-accurate solves: time levels kept
+  bool any_unsteady = false;  // time-accurate or nonreflecting solves: time levels kept
   int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
   int vkinds = 0;  // bit 0: laminar viscous solves, bit 1: SST
   cudaStream_t stream = nullptr;
@@ -151,6 +154,9 @@ struct BatchCore {
   int2 *d_sweep = nullptr;
   int32_t *d_solve_cta0 = nullptr;
   GhostOpDev *d_ops = nullptr, *d_conn_ops = nullptr;
+  NrDev *d_nr = nullptr;
+  int32_t *d_nr_off = nullptr;
+  int n_nr_surf = 0;
   GhostOpDev *d_edge_ops = nullptr, *d_vops = nullptr, *d_vedge_ops = nullptr;
   int32_t *d_edge_solve = nullptr, *d_vop_solve = nullptr, *d_vedge_solve = nullptr;
   int32_t *d_aux_cells = nullptr, *d_aux_block = nullptr;
@@ -345,6 +351,7 @@ class Runner : public RunnerBase {
     }
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
+    Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
     Check(cudaMemset(P_.R, 0, 5 * n * sizeof(double)), "memset");
     Check(cudaMemset(P_.lam, 0, n * sizeof(double)), "memset");
     Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
@@ -411,6 +418,10 @@ class Runner : public RunnerBase {
     P_.ghost_src = m.Upload(c.L.ghost_src);
     for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(double)), "memset");
     if (c.any_rans) AllocTurbulence(m, n, nq, ngh);
+    if (c.n_nr_surf > 0) {
+      P_.nr_mach = m.Alloc<double>(2 * (size_t)c.n_nr_surf);
+      Check(cudaMemset(P_.nr_mach, 0, 2 * (size_t)c.n_nr_surf * sizeof(double)), "memset");
+    }
     if (c.any_unsteady) {
       P_.Un = m.Alloc<double>(7 * n);
       P_.Unm1 = m.Alloc<double>(7 * n);
@@ -561,6 +572,7 @@ class Runner : public RunnerBase {
     if (c_.any_unsteady)
       Launch<T>::StoreN(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                         c_.d_sstate, -1, c_.stream);
+    if (c_.n_nr_surf > 0) Launch<T>::NrMach(P_, c_.d_nr, c_.d_nr_off, c_.n_nr_surf, c_.stream);
     Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
     EdgePhases(c_.d_edge_ops, c_.d_edge_solve, c_.L.edge_phase_off);
   }
@@ -1107,10 +1119,32 @@ void BuildLists(BatchCore &c) {
     L.cl_step_off.push_back((int32_t)L.cl_items.size());
   }
   // ghost operations with pool indices
+  auto face_pool = [&](int b, int d, int64_t face) {
+    const Block &bk = st.blocks[b];
+    const int fi = bk.NI + (d == 0), fj = bk.NJ + (d == 1);
+    const int ii = (int)(face % fi);
+    const int64_t r = face / fi;
+    const int jj = (int)(r % fj), kk = (int)(r / fj);
+    return (int32_t)(c.cell0[b] + ii + (int64_t)bk.NI * (jj + (int64_t)bk.NJ * kk));
+  };
   for (int b = 0; b < c.nblocks; ++b) {
     const Block &bk = st.blocks[b];
+    // nonreflecting surfaces of the block: batch-wide surface numbers
+    const int nr_base = (int)L.nr_off.size();
+    for (size_t i = 0; i < bk.nr_cells.size(); ++i) {
+      const ath_nr_cell &x = bk.nr_cells[i];
+      if (i == 0 || x.surf != bk.nr_cells[i - 1].surf) L.nr_off.push_back((int32_t)L.nr.size());
+      NrDev e{};
+      e.cell = (int32_t)(c.cell0[b] + x.cell);
+      e.face = face_pool(b, x.dir, x.face);
+      e.lower = x.lower;
+      e.dir = x.dir;
+      e.solve = bk.solve;
+      L.nr.push_back(e);
+    }
     for (const auto &op : bk.ops) {
       GhostOpDev g{};
+      g.src2 = op.src2 >= 0 ? nr_base + (int32_t)op.src2 : -1;
       g.dst = (int32_t)(c.cell0[b] + op.dst);
       g.src = (int32_t)(c.cell0[op.src_block] + op.src);
       g.type = op.type;
@@ -1131,6 +1165,7 @@ void BuildLists(BatchCore &c) {
       if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK) L.conn_ops.push_back(g);
     }
   }
+  if (!L.nr_off.empty()) L.nr_off.push_back((int32_t)L.nr.size());
   // block-edge and viscous-wall ghost ops, pool indices, grouped by phase
   auto convert = [&](int b, const ath_ghost_op &op) {
     const Block &bk = st.blocks[b];
@@ -1228,7 +1263,7 @@ void CountLaunches(BatchCore &c) {
                                          : 0) +
                         (c.L.wall_faces.empty() ? 0 : 2) +
                         1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
-                        (c.any_unsteady ? 1 : 0) +
+                        (c.any_unsteady ? 1 : 0) + (c.n_nr_surf > 0 ? 1 : 0) +
                         (nskinds ? 2 * per_pass * c.max_sweeps * nskinds +
                                        (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
                                  : 0) +
@@ -1311,7 +1346,13 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.nl_iters = std::max(1, (int)p.nl_iters);
     x.multilevel = p.multilevel;
     x.unsteady = (p.multilevel || p.nl_iters > 1) ? 1 : 0;
-    if (x.unsteady) c.any_unsteady = true;
+    // the time-n state is kept for the time-accurate terms and for the
+    // nonreflecting boundaries (every implicit solve stores it in the
+    // reference, procBlock storeTimeN_; only these two read it)
+    bool nonreflecting = false;
+    for (const auto &bs : st.solves[s].states) nonreflecting = nonreflecting || bs.nonreflecting;
+    x.store_n = (x.unsteady || nonreflecting) ? 1 : 0;
+    if (x.store_n) c.any_unsteady = true;
     x.rans = p.eqn == ATH_EQN_RANS;
     x.sweeps = p.sweeps;
     x.active = 1;
@@ -1349,6 +1390,11 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_solve_nsteps = m.Upload(c.L.solve_nsteps);
   c.d_solve_cta0 = m.Upload(c.L.solve_cta0);
   c.d_ops = m.Upload(c.L.ops);
+  if (!c.L.nr_off.empty()) {
+    c.d_nr = m.Upload(c.L.nr);
+    c.d_nr_off = m.Upload(c.L.nr_off);
+    c.n_nr_surf = (int)c.L.nr_off.size() - 1;
+  }
   c.d_conn_ops = m.Upload(c.L.conn_ops);
   c.d_op_solve = m.Upload(c.L.op_solve);
   c.d_edge_ops = m.Upload(c.L.edge_ops);

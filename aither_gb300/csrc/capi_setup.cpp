@@ -97,6 +97,8 @@ int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out) {
     out->plane_offsets = b.plane_offsets.data();
     out->plane_cells = b.plane_cells.data();
     out->nbr_mask = b.nbr_mask.data();
+    out->n_nr = (int32_t)b.nr_cells.size();
+    out->nr = b.nr_cells.data();
   });
 }
 

@@ -48,7 +48,8 @@ struct SolveDev {
   // bdf2's time n-1 level, and whether the right-hand side carries the
   // time-level terms (multilevel or several nonlinear iterations)
   double dt_global, dual_cfl;
-  int32_t nl_iters, multilevel, unsteady, pad5;
+  int32_t nl_iters, multilevel, unsteady;
+  int32_t store_n;  // keep the time-n state: time-accurate or nonreflecting
 };
 
 // Per-solve hyperplane lists of the persistent sweep: items (q index,
@@ -69,6 +70,12 @@ struct GhostOpDev {
 
 // A viscous-wall face: pool index of the face (cell above it), direction,
 // block.  Lists are ordered by solve.
+// A cell next to a nonreflecting surface: pool indices of the cell and of
+// its boundary face, outward-normal sign; grouped by surface.
+struct NrDev {
+  int32_t cell, face, lower, dir, solve, pad;
+};
+
 struct WallFaceDev {
   int32_t face, dir, block, pad;
 };
@@ -155,6 +162,7 @@ struct Pools {
   // linear system's right-hand side in q order ([5][nq], [2][nq])
   double *Un, *Unm1;
   T *Bq, *Btq;
+  double *nr_mach;  // [2][nonreflecting surfaces] average, largest Mach
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -314,6 +322,10 @@ struct Launch {
   static void Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      const int32_t *cta_pos0, NormPartial *partials, int ncta,
                      const SolveState *ss, cudaStream_t s);
+  // average and largest outward normal Mach number of each nonreflecting
+  // surface (items nr[off[s] .. off[s+1]) into P.nr_mach[2 s .. 2 s + 1])
+  static void NrMach(const Pools<T> &P, const NrDev *nr, const int32_t *off, int nsurf,
+                     cudaStream_t s);
   // StoreOldSolution of the time-accurate solves at a time step's start;
   // block >= 0: that block's current state into both time levels
   static void StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

@@ -2,6 +2,7 @@
 // arithmetic type so each is compiled with its own contraction setting.
 #pragma once
 
+#include <cfloat>
 #include <cooperative_groups.h>
 #include <type_traits>
 
@@ -364,12 +365,39 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
         const double rhoSoSInt = in.rho * sosInt;
         const double dvx = fr.u - in.u, dvy = fr.v - in.v, dvz = fr.w - in.w;
         g.p = 0.5 * (fr.p + in.p - rhoSoSInt * Dot(nx, ny, nz, dvx, dvy, dvz));
-        const double deltaPressure = fr.p - g.p;
-        const double rho = fr.rho - deltaPressure / (sosInt * sosInt);
-        g.rho = rho * (fr.rho / fr.rho);
-        g.u = fr.u - nx * deltaPressure / rhoSoSInt;
-        g.v = fr.v - ny * deltaPressure / rhoSoSInt;
-        g.w = fr.w - nz * deltaPressure / rhoSoSInt;
+        if (bs.nonreflecting) {
+          // LODI relaxation of the incoming characteristic towards the
+          // specified state (src/ghostStates.cpp:433-461): the time-n state
+          // of the boundary-adjacent cell, its time step of the previous
+          // iteration and the surface's largest normal Mach number
+          const double *un = P.Un;
+          double cn[5];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) cn[v] = un[v * n + op.src];
+          const Prim<double> sN = ConsToPrim(cn, gas);
+          const double dt = P.dt[op.src];
+          const double maxMach = P.nr_mach[2 * op.src2 + 1];
+          const double sigma = 0.25;
+          const double rhoN = sN.rho;
+          const double sosN = SoS(sN, gas);
+          const double rhoSoSN = rhoN * sosN;
+          const double deltaPressure = g.p - sN.p;
+          const double alpha = sigma * sosN / bs.length_scale;
+          const double rhoNp1 =
+              (rhoN + dt * alpha * fr.rho + deltaPressure / (sosN * sosN)) / (1.0 + dt * alpha);
+          g.rho = rhoNp1 * (fr.rho / fr.rho);
+          const double k = alpha * (1.0 - maxMach * maxMach);
+          g.u = (sN.u + dt * k * fr.u - nx * deltaPressure / rhoSoSN) / (1.0 + dt * k);
+          g.v = (sN.v + dt * k * fr.v - ny * deltaPressure / rhoSoSN) / (1.0 + dt * k);
+          g.w = (sN.w + dt * k * fr.w - nz * deltaPressure / rhoSoSN) / (1.0 + dt * k);
+        } else {
+          const double deltaPressure = fr.p - g.p;
+          const double rho = fr.rho - deltaPressure / (sosInt * sosInt);
+          g.rho = rho * (fr.rho / fr.rho);
+          g.u = fr.u - nx * deltaPressure / rhoSoSInt;
+          g.v = fr.v - ny * deltaPressure / rhoSoSInt;
+          g.w = fr.w - nz * deltaPressure / rhoSoSInt;
+        }
         if (rans)
           FarfieldTurb(g, bs.u, bs.v, bs.w, bs.turb_intensity, bs.eddy_visc_ratio, sv, gas, gt);
         auto hold = [&](double f) {
@@ -1808,6 +1836,34 @@ __global__ void k_conn_du(Pools<T> P) {
   }
 }
 
+// Average and largest outward normal Mach number of each nonreflecting
+// surface over its boundary-adjacent cells (procBlock::GetGhostStates,
+// src/procBlock.cpp:6235-6260): one thread per surface sums in the
+// surface's k, j, i order, as the reference does
+template <typename T>
+__global__ void k_nr_mach(Pools<T> P, const NrDev *nr, const int32_t *off, int nsurf) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsurf) return;
+  const int64_t n = P.ncell;
+  const int a = off[s], b = off[s + 1];
+  double avg = 0.0, mx = -1.0 * DBL_MAX;
+  for (int i = a; i < b; ++i) {
+    const NrDev x = nr[i];
+    const Prim<double> w = LoadW<double>(P.W, n, x.cell);
+    const double *fa = P.fa[x.dir];
+    const double ax = x.lower ? -1.0 * fa[x.face] : fa[x.face];
+    const double ay = x.lower ? -1.0 * fa[n + x.face] : fa[n + x.face];
+    const double az = x.lower ? -1.0 * fa[2 * n + x.face] : fa[2 * n + x.face];
+    const double sos = SoS(w, GasOf<double>(P.solves[x.solve]));
+    const double mach = Dot(w.u, w.v, w.w, ax, ay, az) / sos;
+    mx = mx < mach ? mach : mx;
+    avg += mach;
+  }
+  avg /= (double)(b - a);
+  P.nr_mach[2 * s] = avg;
+  P.nr_mach[2 * s + 1] = mx;
+}
+
 // StoreOldSolution (src/mgSolution.cpp:103) for the time-accurate solves:
 // at a time step's first nonlinear iteration the conserved state of time
 // n, and at the first step of a bdf2 solve that of time n-1 as well unless
@@ -1824,7 +1880,7 @@ __global__ void __launch_bounds__(kCta) k_store_n(Pools<T> P, const int32_t *lis
   if (block >= 0 && bk != block) return;
   const int s = P.blocks[bk].solve;
   const SolveDev sv = P.solves[s];
-  if (!sv.unsteady) return;
+  if (!sv.store_n) return;
   const int64_t it = sstate[s].iter;
   const bool forced = block >= 0;
   if (!forced && (!sv.active || it % sv.nl_iters != 0)) return;
@@ -2645,6 +2701,11 @@ void Launch<T>::Update(const Pools<T> &P, const int32_t *list, const int32_t *ct
                        const int32_t *cta_pos0, NormPartial *partials, int ncta,
                        const SolveState *ss, cudaStream_t s) {
   if (ncta > 0) k_update<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, cta_pos0, partials, ss);
+}
+template <typename T>
+void Launch<T>::NrMach(const Pools<T> &P, const NrDev *nr, const int32_t *off, int nsurf,
+                       cudaStream_t s) {
+  if (nsurf > 0) k_nr_mach<T><<<(nsurf + 127) / 128, 128, 0, s>>>(P, nr, off, nsurf);
 }
 template <typename T>
 void Launch<T>::StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

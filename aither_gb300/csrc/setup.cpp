@@ -652,6 +652,8 @@ void BuildGhostOps(Setup &st, int solve) {
     Block &b = st.blocks[bi];
     b.ops.clear();
     b.vops.clear();
+    b.nr_cells.clear();
+    int nr_surfs = 0;
     for (size_t si = 0; si < b.surfs.size(); ++si) {
       const auto &s = b.surfs[si];
       const int d = s.Dir();
@@ -674,6 +676,33 @@ void BuildGhostOps(Setup &st, int solve) {
           Fail("no boundary state for tag " + std::to_string(s.tag));
       }
       const int n = Ncell(b, d);
+      // nonreflecting inlet / pressureOutlet: the surface's boundary-
+      // adjacent cells in the slice's k, j, i order for its Mach numbers
+      int nr_surf = -1;
+      if ((s.type == ATH_BC_INLET || s.type == ATH_BC_PRESSURE_OUTLET) &&
+          sv.states[st_idx].nonreflecting) {
+        nr_surf = nr_surfs++;
+        int lo3[3], hi3[3];
+        lo3[d] = s.Lower() ? 0 : n - 1;
+        hi3[d] = lo3[d] + 1;
+        lo3[d1] = p.lo1;
+        hi3[d1] = p.hi1;
+        lo3[d2] = p.lo2;
+        hi3[d2] = p.hi2;
+        for (int k = lo3[2]; k < hi3[2]; ++k)
+          for (int j = lo3[1]; j < hi3[1]; ++j)
+            for (int i = lo3[0]; i < hi3[0]; ++i) {
+              int f3[3] = {i, j, k};
+              f3[d] = s.Lower() ? 0 : n;
+              ath_nr_cell x{};
+              x.cell = b.Cell(i, j, k);
+              x.face = b.Face(d, f3[0], f3[1], f3[2]);
+              x.surf = nr_surf;
+              x.dir = d;
+              x.lower = s.Lower() ? 1 : 0;
+              b.nr_cells.push_back(x);
+            }
+      }
       for (int layer = 1; layer <= b.ng; ++layer) {
         int g, ic, ac;
         if (s.Lower()) {
@@ -706,7 +735,7 @@ void BuildGhostOps(Setup &st, int solve) {
             op.lower = s.Lower() ? 1 : 0;
             op.state = st_idx;
             op.face = b.Face(d, F[0], F[1], F[2]);
-            op.src2 = -1;
+            op.src2 = nr_surf;  // -1 unless a nonreflecting surface
             b.ops.push_back(op);
             if (s.type == ATH_BC_VISCOUS_WALL) {
               // the wall-adjacent cell supplies the wall distance and the
@@ -1371,9 +1400,23 @@ void AppendInput(Setup &st, const std::string &path) {
         s.heat_flux = 1;
         s.wall_q = std::stod(m["heatFlux"]) / std::pow(aref / lref, 3.0);
       }
-      if (m.count("nonreflecting") && (m["nonreflecting"] == "true" || m["nonreflecting"] == "1"))
-        Fail("nonreflecting " + name + " boundaries need the time-accurate modes, which are "
-             "not supported");
+      // inlet / pressureOutlet: nonreflecting=true with lengthScale
+      // (inlet::AssignExtraData, pressureOutlet ctor src/inputStates.cpp:475,
+      // 615; the length is divided by the reference length)
+      if (m.count("nonreflecting")) {
+        if (name != "inlet" && name != "pressureOutlet")
+          Fail("nonreflecting is an inlet / pressureOutlet parameter");
+        s.nonreflecting = m["nonreflecting"] == "true" ? 1 : 0;
+      }
+      if (m.count("lengthScale")) s.length_scale = std::stod(m["lengthScale"]) / lref;
+      if (s.nonreflecting && !m.count("lengthScale"))
+        Fail("lengthScale must be specified with nonreflecting");
+      // the transverse terms of the nonreflecting outlet read the cell
+      // pressure and velocity gradients of the previous residual, which the
+      // reference forms for every solve (CalcGradsI/J/K for inviscid ones,
+      // src/procBlock.cpp:6141); they are not kept here
+      if (s.nonreflecting && name == "pressureOutlet")
+        Fail("nonreflecting pressureOutlet boundaries are not supported");
       if (m.count("wallTreatment") && m["wallTreatment"] != "lowRe")
         Fail("wall laws are not supported");
       if (m.count("turbulenceIntensity")) s.turb_intensity = num("turbulenceIntensity", 0);

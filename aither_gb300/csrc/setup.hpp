@@ -43,6 +43,7 @@ struct Block {
   std::vector<double> vol, center, width, fcenter[3], farea[3], wall_dist;
   std::vector<double> state0;  // padded AoS primitive
   std::vector<ath_ghost_op> ops, edge_ops, vops, vedge_ops;
+  std::vector<ath_nr_cell> nr_cells;  // cells of nonreflecting surfaces
   std::vector<int32_t> plane_offsets, plane_cells;
   std::vector<uint8_t> nbr_mask;
 

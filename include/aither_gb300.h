@@ -117,6 +117,16 @@ typedef struct {
                          wall-adjacent cell (-1 when unused) */
 } ath_ghost_op;
 
+/* A cell next to a nonreflecting boundary surface. */
+typedef struct {
+  int64_t cell;    /* padded index of the boundary-adjacent cell */
+  int64_t face;    /* padded face index (direction dir) of its boundary face */
+  int32_t surf;    /* block-local index of the surface */
+  int32_t dir;     /* boundary normal direction */
+  int32_t lower;   /* 1 = lower surface (outward normal flipped) */
+  int32_t pad;
+} ath_nr_cell;
+
 /* Boundary-state data, nondimensional (reference inputStates.cpp). */
 typedef struct {
   int32_t tag;
@@ -128,6 +138,10 @@ typedef struct {
                                                     heat flux over (a_ref/l_ref)^3 */
   int32_t isothermal, heat_flux;
   double turb_intensity, eddy_visc_ratio;
+  /* inlet / pressureOutlet with nonreflecting=true: LODI relaxation towards
+   * the specified state over lengthScale (nondimensional) */
+  int32_t nonreflecting, pad_nr;
+  double length_scale;
 } ath_bc_state;
 
 /* Per-solve physics and scheme constants, nondimensional. */
@@ -186,6 +200,13 @@ typedef struct {
    * off-diagonal sums: it is a physical cell or the face lies on a
    * periodic/interblock connection (procBlock::ImplicitLower/Upper). */
   const uint8_t *nbr_mask;
+  /* cells next to the block's nonreflecting boundary surfaces, surface by
+   * surface, each surface in the reference's k, j, i loop order
+   * (procBlock::GetGhostStates src/procBlock.cpp:6235): the average and
+   * largest outward normal Mach number of each surface enter its ghost
+   * states; the ghost ops of such a surface carry its index in src2 */
+  int32_t n_nr;
+  const ath_nr_cell *nr;
 } ath_block_view;
 
 /* Load a case from the reference's input file format (and the Plot3D grid

@@ -2,6 +2,7 @@
  * See aither_oracle.h.  Every function names the reference function it
  * restates (paths inside the reference project).  Arithmetic is written in
  * the reference's evaluation order; build with -ffp-contract=off. */
+#include <float.h>
 #include "aither_oracle.h"
 
 #include <math.h>
@@ -49,6 +50,9 @@ typedef struct {
   ath_ghost_op *edge, *vops, *vedge;
   int nplanes;
   int32_t *plane_off, *plane_cells;
+  int n_nr, n_nr_surf;     /* nonreflecting surfaces: cells, surfaces */
+  ath_nr_cell *nr;
+  double *nr_mach;         /* [n_nr_surf][2] average, largest Mach */
 } oblock;
 
 typedef struct {
@@ -1303,6 +1307,12 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     b->vops = (ath_ghost_op *)dup_arr(v->vops, sizeof(ath_ghost_op) * v->nvops);
     b->nvedge = v->nvedge_ops;
     b->vedge = (ath_ghost_op *)dup_arr(v->vedge_ops, sizeof(ath_ghost_op) * v->nvedge_ops);
+    b->n_nr = v->n_nr;
+    b->nr = (ath_nr_cell *)dup_arr(v->nr, sizeof(ath_nr_cell) * v->n_nr);
+    b->n_nr_surf = 0;
+    for (int i = 0; i < b->n_nr; ++i)
+      if (b->nr[i].surf + 1 > b->n_nr_surf) b->n_nr_surf = b->nr[i].surf + 1;
+    b->nr_mach = (double *)dup_arr(NULL, 16 * (size_t)b->n_nr_surf);
     b->nplanes = v->nplanes;
     b->plane_off = (int32_t *)dup_arr(v->plane_offsets, 4 * (v->nplanes + 1));
     b->plane_cells = (int32_t *)dup_arr(v->plane_cells, 4 * (size_t)v->ni * v->nj * v->nk);
@@ -1321,6 +1331,7 @@ void orc_destroy(orc_case *c) {
     for (int d = 0; d < 3; ++d) free(b->fa[d]);
     free(b->W); free(b->R); free(b->dU); free(b->lam); free(b->dt); free(b->A);
     free(b->Un); free(b->Unm1);
+    free(b->nr); free(b->nr_mach);
     free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
@@ -1401,6 +1412,29 @@ void orc_fill_ghosts(orc_case *c) {
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
     const osolve *sv = &c->s[b->solve];
+    /* average and largest outward normal Mach number of each nonreflecting
+     * surface over its boundary-adjacent cells, summed in the surface's
+     * k, j, i order (procBlock::GetGhostStates src/procBlock.cpp:6235-6260) */
+    for (int sf = 0; sf < b->n_nr_surf; ++sf) {
+      double avg = 0.0, mx = -1.0 * DBL_MAX;
+      int cnt = 0;
+      for (int i = 0; i < b->n_nr; ++i) {
+        const ath_nr_cell *x = &b->nr[i];
+        if (x->surf != sf) continue;
+        double nn[3], mg;
+        face_normal(b, x->dir, x->face, nn, &mg);
+        if (x->lower)
+          for (int e = 0; e < 3; ++e) nn[e] = -1.0 * nn[e];
+        const double *w = &b->W[x->cell * NV];
+        const double mach = (w[1] * nn[0] + w[2] * nn[1] + w[3] * nn[2]) / sos_of(w, &sv->gas);
+        mx = mx < mach ? mach : mx;
+        avg += mach;
+        ++cnt;
+      }
+      avg /= (double)cnt;
+      b->nr_mach[2 * sf] = avg;
+      b->nr_mach[2 * sf + 1] = mx;
+    }
     for (int o = 0; o < b->nops; ++o) {
       const ath_ghost_op *op = &b->ops[o];
       const oblock *src = &c->b[op->src_block];
@@ -1559,12 +1593,33 @@ void orc_fill_ghosts(orc_case *c) {
             const double dv[3] = {fr[1] - in[1], fr[2] - in[2], fr[3] - in[3]};
             g[4] = 0.5 * (fr[4] + in[4] -
                           rhoSoSInt * (n[0] * dv[0] + n[1] * dv[1] + n[2] * dv[2]));
-            const double dp = fr[4] - g[4];
-            const double rho = fr[0] - dp / (sosInt * sosInt);
-            g[0] = rho * (fr[0] / fr[0]);
-            g[1] = fr[1] - n[0] * dp / rhoSoSInt;
-            g[2] = fr[2] - n[1] * dp / rhoSoSInt;
-            g[3] = fr[3] - n[2] * dp / rhoSoSInt;
+            if (bs->nonreflecting) {
+              /* LODI relaxation of the incoming characteristic
+               * (src/ghostStates.cpp:433-461) */
+              double sN[NV];
+              cons_to_prim(&b->Un[op->src * 7], &sv->gas, sN);
+              const double dt = b->dt[op->src];
+              const double maxMach = b->nr_mach[2 * op->src2 + 1];
+              const double sigma = 0.25;
+              const double rhoN = sN[0];
+              const double sosN = sos_of(sN, &sv->gas);
+              const double rhoSoSN = rhoN * sosN;
+              const double dp = g[4] - sN[4];
+              const double alpha = sigma * sosN / bs->length_scale;
+              const double rhoNp1 =
+                  (rhoN + dt * alpha * fr[0] + dp / (sosN * sosN)) / (1.0 + dt * alpha);
+              g[0] = rhoNp1 * (fr[0] / fr[0]);
+              const double k = alpha * (1.0 - maxMach * maxMach);
+              for (int e = 0; e < 3; ++e)
+                g[1 + e] = (sN[1 + e] + dt * k * fr[1 + e] - n[e] * dp / rhoSoSN) / (1.0 + dt * k);
+            } else {
+              const double dp = fr[4] - g[4];
+              const double rho = fr[0] - dp / (sosInt * sosInt);
+              g[0] = rho * (fr[0] / fr[0]);
+              g[1] = fr[1] - n[0] * dp / rhoSoSInt;
+              g[2] = fr[2] - n[1] * dp / rhoSoSInt;
+              g[3] = fr[3] - n[2] * dp / rhoSoSInt;
+            }
             if (rans) {
               farfield_turb(g, freeVel, bs->turb_intensity, bs->eddy_visc_ratio, &sv->gas,
                             &sv->v, gt);

@@ -96,6 +96,13 @@ CASES = [
     ("bump_inlet_pout", cases.bump_channel,
      dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
           back_pressure=1.02, recon="weno", limiter="none"), [1, 20], True),
+    # nonreflecting inlet: steady, and bdf2 dual time
+    ("bump_nr", cases.bump_channel,
+     dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
+          back_pressure=1.02, nonreflecting=2.0), [1, 20], True),
+    ("bump_nr_bdf2", cases.bump_channel,
+     dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
+          back_pressure=1.02, nonreflecting=0.5, time="bdf2", dt=2e-5, nl=3), [1, 12], True),
     ("plate_heatflux", cases.flat_plate,
      dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, wall_q=500.0), [1, 20], True),
     ("sst_chan_stag_pout", cases.wall_channel,

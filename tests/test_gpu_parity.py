@@ -67,7 +67,8 @@ def _cols_err(a, b):
                                   "bump_dplur_it1", "bump_dplur_it20", "plate_bdplur_it1",
                                   "plate_bdplur_it20", "bump_stag_pout_it1",
                                   "bump_stag_pout_it20", "bump_inlet_pout_it1",
-                                  "bump_inlet_pout_it20", "plate_heatflux_it1",
+                                  "bump_inlet_pout_it20", "bump_nr_it1", "bump_nr_it20",
+                                  "bump_nr_bdf2_it1", "bump_nr_bdf2_it12", "plate_heatflux_it1",
                                   "plate_heatflux_it20", "vortex_bdf2_it1", "vortex_bdf2_it4",
                                   "vortex_cn_dual_it1", "vortex_cn_dual_it4",
                                   "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4"])

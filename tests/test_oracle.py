@@ -26,7 +26,8 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "sst_weno_ausm_it10", "bump_dplur_it1", "bump_dplur_it20", "plate_bdplur_it1",
         "plate_bdplur_it20", "sst_plate_dplur_it1", "sst_plate_dplur_it10",
         "bump_stag_pout_it1", "bump_stag_pout_it20", "bump_inlet_pout_it1",
-        "bump_inlet_pout_it20", "plate_heatflux_it1", "plate_heatflux_it20",
+        "bump_inlet_pout_it20", "bump_nr_it1", "bump_nr_it20", "bump_nr_bdf2_it1",
+        "bump_nr_bdf2_it12", "plate_heatflux_it1", "plate_heatflux_it20",
         "sst_chan_stag_pout_it1", "sst_chan_stag_pout_it10", "vortex_bdf2_it1", "vortex_bdf2_it4",
         "vortex_cn_dual_it1", "vortex_cn_dual_it4", "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
         "sst_plate_bdf2_it1", "sst_plate_bdf2_it4"]

@@ -132,3 +132,32 @@ def test_geometry_matches_reference(tmp_path):
         ext = [slice(ng, -ng)] * 3
         ext[2 - d] = slice(ng, a.shape[2 - d] - ng)
         assert np.array_equal(a[tuple(ext)], R["b0_" + nm][tuple(ext)])
+
+
+def test_nonreflecting_inlet_parsed_and_outlet_rejected(tmp_path):
+    """inlet(...; nonreflecting=true; lengthScale=L) is accepted with L over
+    the reference length; a nonreflecting pressure outlet (its transverse
+    terms need cell gradients that are not kept) and nonreflecting without
+    lengthScale are setup errors."""
+    from aither_gb300 import Setup, cases
+    from aither_gb300._lib import AthError
+    kw = dict(ni=8, nj=4, nk=2, height=0.05, mach=0.4, inflow="inlet", outflow="pressure")
+    inp, _ = cases.bump_channel(str(tmp_path / "a"), nonreflecting=2.0, **kw)
+    s = Setup(inp)
+    sv = s.solve_view(0)
+    st = [sv.states[i] for i in range(sv.nstates)]
+    nr = [x for x in st if x.nonreflecting]
+    assert len(nr) == 1 and nr[0].length_scale == 2.0 / sv.l_ref
+    assert sum(s.block_view(b).n_nr for b in range(s.counts()[1])) == 4 * 2
+    s.close()
+    text = open(inp).read()
+    bad = text.replace("pressureOutlet(tag=4; pressure=",
+                       "pressureOutlet(tag=4; nonreflecting=true; lengthScale=1.0; pressure=")
+    open(inp, "w").write(bad)
+    with pytest.raises(AthError):
+        Setup(inp)
+    bad = re.sub(r"; lengthScale=[^;)]*", "", text)
+    assert "nonreflecting=true" in bad and "lengthScale" not in bad
+    open(inp, "w").write(bad)
+    with pytest.raises(AthError, match="lengthScale"):
+        Setup(inp)
