@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
             "ath_setup_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_ctx_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(vp)]),
             "ath_ctx_destroy": (C.c_int, [vp]),
+            "ath_ctx_fp64_peak": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_batch_create": (C.c_int, [vp, vp, C.c_int, C.c_int, C.POINTER(vp)]),
             "ath_batch_destroy": (C.c_int, [vp]),
             "ath_batch_iterate": (C.c_int, [vp, C.c_int, C.POINTER(Norms)]),
@@ -378,6 +379,12 @@ class Context:
         h = C.c_void_p()
         check(lib().ath_ctx_create(device, hbm_budget, C.byref(h)))
         self.h = h
+
+    def fp64_peak(self, reps: int = 5) -> float:
+        """Measured FP64 FMA issue rate of the context's GPU, TFLOP/s."""
+        t = C.c_double()
+        check(lib().ath_ctx_fp64_peak(self.h, reps, C.byref(t)))
+        return t.value
 
     def close(self):
         if self.h:

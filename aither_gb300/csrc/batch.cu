@@ -2001,6 +2001,57 @@ int ath_batch_profile(ath_batch *batch, int reps, double ms[8]) {
   });
 }
 
+namespace {
+// eight independent FMA chains per thread; the sum is stored only when it
+// matches a value it never takes, so the chains stay live
+__global__ void __launch_bounds__(256) k_fp64_peak(double seed, int iters, double *sink) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + (double)(threadIdx.x + k);
+  const double m = 0.999999999, c = 1e-9;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == -1.0) sink[0] = s;
+}
+}  // namespace
+
+int ath_ctx_fp64_peak(ath_ctx *ctx, int reps, double *tflops) {
+  return Guard([&] {
+    if (!ctx || !tflops || reps < 1) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    Check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int sms = 0;
+    Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attr");
+    double *sink = nullptr;
+    Check(cudaMalloc(&sink, sizeof(double)), "cudaMalloc");
+    cudaEvent_t e0, e1;
+    Check(cudaEventCreate(&e0), "event");
+    Check(cudaEventCreate(&e1), "event");
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_fp64_peak<<<blocks, threads>>>(1.0, iters, sink);  // warm-up
+    double best = 0.0;
+    for (int r = 0; r < reps; ++r) {
+      Check(cudaEventRecord(e0), "event");
+      k_fp64_peak<<<blocks, threads>>>(1.0 + r, iters, sink);
+      Check(cudaEventRecord(e1), "event");
+      Check(cudaEventSynchronize(e1), "sync");
+      float ms = 0.f;
+      Check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+      const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+      best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    Check(cudaGetLastError(), "kernel launch");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    *tflops = best;
+  });
+}
+
 int ath_batch_stats(ath_batch *batch, ath_stats *out) {
   if (!batch || !out) return ATH_ERR_ARG;
   *out = batch->core.stats;

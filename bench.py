@@ -145,7 +145,7 @@ def run_native(args, rank: int, world: int, device: int):
         t_setup = time.time() - t0
     nsolves, nblocks, ncells = setup.counts()
     ctx = Context(device)
-    out = {}
+    out = {"fp64_peak_tflops": ctx.fp64_peak(5)}
     for prec_name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
         if args.precision not in ("both", prec_name):
             continue
@@ -531,6 +531,14 @@ def _max_over_ranks(x: float, world: int) -> float:
 
 
 # -------------------------------------------------------------------- main
+def fp64_flop_per_cell() -> dict:
+    """Executed FP64 FLOP per cell-iteration of the FP64 bump path by
+    kernel class, from ncu's SASS counters (dfma x 2 + dadd + dmul) over one
+    iteration of a 64x48x32 bump channel (profiles/fp64_flops_bump64x48x32.md)."""
+    return {"face_per_direction": 1026.0, "sweeps": 1134.0, "cell": 502.0, "update": 188.0,
+            "ghost": 25.0}
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -621,6 +629,23 @@ def main():
                "update": km["update"]}
     dom = max(pass_ms, key=pass_ms.get)
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
+    # FP64 bound: executed FP64 FLOP per cell-iteration (2 per DFMA, 1 per
+    # DADD / DMUL, from the SASS instruction counters; divisions and square
+    # roots run as FMA sequences) against the measured FP64 issue peak
+    fl = fp64_flop_per_cell()
+    face_ms = km["face_i"] + km["face_j"] + km["face_k"]
+    fp64_peak = res.get("fp64_peak_tflops") or 0.0
+    face_tf = 3 * fl["face_per_direction"] * ncells / (face_ms * 1e-3) / 1e12
+    path_flop = 3 * fl["face_per_direction"] + fl["sweeps"] + fl["cell"] + fl["update"] + \
+        fl["ghost"]
+    path_tf = path_flop * fp["value"] / 1e12
+    roof_fp64 = {"bound": "fp64", "kernel": "face (3 directions)", "achieved": face_tf,
+                 "peak": fp64_peak, "unit": "TFLOP/s",
+                 "frac": face_tf / fp64_peak if fp64_peak else None,
+                 "peak_source": "measured on this GPU (ath_ctx_fp64_peak)",
+                 "path_achieved": path_tf,
+                 "path_frac": path_tf / fp64_peak if fp64_peak else None,
+                 "flop_per_cell_iteration": fl}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
             "peak_source": peaks["source"], "traffic": None,
@@ -632,7 +657,7 @@ def main():
             "data": "synthetic (seeded bump-channel grids)", "config": config,
             "cells": ncells, "solves": nsolves, "setup_s": t_setup,
             "gpu_launches": fp["gpu_launches"], "clocks": fp["clocks"],
-            "e2e": fp["e2e"], "roofline": roof, "kernel_ms": km,
+            "e2e": fp["e2e"], "roofline": roof, "roofline_fp64": roof_fp64, "kernel_ms": km,
             "autotune": {"sweep_threads": fp["sweep_threads"], "sweep_shape": fp["sweep_shape"]}}
     if "mixed" in res and "fp64" in res:
         m = res["mixed"]

@@ -245,6 +245,12 @@ typedef struct {
 
 int ath_ctx_create(int device, size_t hbm_budget_bytes, ath_ctx **out);
 int ath_ctx_destroy(ath_ctx *ctx);
+/* FP64 issue-rate peak of the context's GPU, measured: chains of
+ * independent fused multiply-adds on every SM (2 FLOP each), best of
+ * `reps` timed launches; *tflops receives FP64 TFLOP/s.  The second bound
+ * of the solver's roofline beside HBM bandwidth (its FP64 kernels run
+ * divisions and square roots as FMA sequences). */
+int ath_ctx_fp64_peak(ath_ctx *ctx, int reps, double *tflops);
 const char *ath_last_error(void);
 
 /* Copy a setup to the device.  precision = ATH_PREC_*.  flags: bit 0 =
