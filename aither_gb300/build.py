@@ -27,7 +27,7 @@ BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libaither_gb300.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "liboracle.so")
-REF_SRC = os.environ.get("AITHER_REFERENCE_SRC", "/root/reference")
+REF_BUILD = os.path.join(ORACLE_DIR, "ref_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -113,14 +113,26 @@ def build_oracle() -> str:
     return ORACLE_LIB
 
 
-def build_reference(jobs: int = 8) -> str | None:
+def reference_source() -> str | None:
+    """The reference's source tree: AITHER_REFERENCE_SRC, else the default
+    of the oracle/ref_build recipe; None where neither holds its sources
+    (machines that only receive prebuilt files)."""
+    ref = os.environ.get("AITHER_REFERENCE_SRC")
+    if not ref:
+        r = subprocess.run(["make", "-s", "-C", REF_BUILD, "print-ref"], capture_output=True,
+                           text=True)
+        ref = r.stdout.strip() if r.returncode == 0 else ""
+    return ref if ref and os.path.isdir(os.path.join(ref, "src")) else None
+
+
+def build_reference(ref: str | None = None, jobs: int = 8) -> str | None:
     """Builds the reference solver from its sources in place (only where the
-    sources exist, i.e. not on machines that only receive prebuilt files)."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src")):
+    sources exist)."""
+    ref = ref or reference_source()
+    if ref is None:
         return None
     out = os.path.join(ORACLE_DIR, "_ref")
-    _run(["make", "-C", os.path.join(ORACLE_DIR, "ref_build"), f"REF={REF_SRC}",
-          f"OUT={out}", f"-j{jobs}"])
+    _run(["make", "-C", REF_BUILD, f"REF={ref}", f"OUT={out}", f"-j{jobs}"])
     return out
 
 

@@ -16,6 +16,12 @@ Workloads:
                   MUSCL minmod, Roe, LU-SGS, CFL 20.  Batches of these with
                   sizes drawn between 32^3 and 96x64x48 and Mach in
                   [0.3, 0.85] form the batched workload.
+  block_pair   -- two blocks of a skewed box joined by an interblock
+                  connection whose second block has its index axes in any
+                  of the 24 right-handed signed permutations of the first's, so every
+                  patch orientation (aligned, swapped, reversed; lower or
+                  upper surfaces of any direction) can be exercised, with a
+                  three-dimensional vortex crossing the connection.
 """
 from __future__ import annotations
 
@@ -555,3 +561,175 @@ def set_output_keys(inp: str, iterations: int, variables: list | None = None,
     out[at:at] = extra
     with open(inp, "w") as f:
         f.write("\n".join(out))
+
+
+# ---------------------------------------------------------------------------
+# two-block connections in every orientation
+
+def _signed_perms():
+    """The 24 right-handed signed permutations (ax, sg): index axis t of the
+    second block runs along physical axis ax[t] (0 x, 1 y, 2 z) in direction
+    sg[t] (a left-handed index system has negative cell volumes, which the
+    reference rejects)."""
+    import itertools
+    out = []
+    for ax in itertools.permutations(range(3)):
+        parity = 1 if sum(1 for a in range(3) for b in range(a + 1, 3) if ax[a] > ax[b]) % 2 == 0 \
+            else -1
+        for sg in itertools.product((1, -1), repeat=3):
+            if parity * sg[0] * sg[1] * sg[2] > 0:
+                out.append((tuple(ax), tuple(sg)))
+    return out
+
+
+def patch_orientation(ax, sg) -> tuple:
+    """In-plane orientation of the second block's connection patch relative
+    to the first block's i-upper patch (in-plane axes j, k): whether the
+    first in-plane axes are swapped, and the directions along which y and z
+    run on the second block.  The 8 combinations are the reference's 8
+    patch orientations (connection::Orientation)."""
+    t_n = ax.index(0)
+    d1 = (t_n + 1) % 3
+    t_y, t_z = ax.index(1), ax.index(2)
+    return (t_y != d1, sg[t_y], sg[t_z])
+
+
+def orientation_set():
+    """One signed permutation per in-plane orientation (8), cycling the
+    second block's connecting direction through i, j, k and alternating its
+    lower and upper surface, so that normal directions and surface sides
+    vary too."""
+    seen, picks = set(), []
+    perms = _signed_perms()
+    want_n = 0
+    for _ in range(len(perms)):
+        for ax, sg in perms:
+            o = patch_orientation(ax, sg)
+            t_n = ax.index(0)
+            if o in seen or t_n != want_n % 3:
+                continue
+            if (sg[t_n] > 0) != (want_n % 2 == 0):
+                continue
+            seen.add(o)
+            picks.append((ax, sg))
+            want_n += 1
+            break
+        else:
+            want_n += 1
+        if len(picks) == 8:
+            break
+    return picks
+
+
+def block_pair(outdir: str, orient: int = 0, na: int = 5, nb: int = 6, nc: int = 4,
+               physics: str = "euler", cfl: float = 10.0, name: str = "pair", sweeps: int = 1):
+    """Skewed box [0, 2] x [0, 1] x [0, 0.6] split at x = 1 into two blocks
+    of na x nb x nc cells.  The first block's index axes are x, y, z; the
+    second block's are the signed permutation orientation_set()[orient]
+    of them, so its connecting surface may be any of its six surfaces and
+    the patch may be swapped and reversed in plane.  Characteristic far
+    field at x = 0 and x = 2, slip walls elsewhere.  Initial state: a
+    free stream at Mach 0.4 along x with a vortex about an axis along z
+    centred on the connection, a z-dependent cross-flow and a density
+    perturbation (the field differs along every axis, so an index mapping
+    error across the connection changes the result).
+
+    physics: "euler" (MUSCL minmod, Roe, LU-SGS), "ns" (laminar
+    Navier-Stokes, MUSCL van Albada, Roe, block LU-SGS with 2 sweeps) or
+    "sst" (SST-2003 RANS, as "ns")."""
+    os.makedirs(outdir, exist_ok=True)
+    ax, sg = orientation_set()[orient]
+    # global node array, 2 na cells along x; smooth stretching and a skew so
+    # that face areas and widths vary
+    xi = np.arange(2 * na + 1) / (2 * na)
+    eta = np.arange(nb + 1) / nb
+    zeta = np.arange(nc + 1) / nc
+    Z, Y, X = np.meshgrid(zeta, eta, xi, indexing="ij")
+    x = 2.0 * X
+    y = Y + 0.08 * np.sin(np.pi * Y) * (X - 0.5)
+    z = 0.6 * Z
+    x = x + 0.06 * Y * Z + 0.04 * np.sin(np.pi * Z) * Y
+    G = np.ascontiguousarray(np.stack([x, y, z]))
+    A = np.ascontiguousarray(G[:, :, :, : na + 1])
+    Bg = G[:, :, :, na:]
+    arr_of = {0: 3, 1: 2, 2: 1}  # physical axis -> array axis of (c, z, y, x)
+    B = np.transpose(Bg, (0, arr_of[ax[2]], arr_of[ax[1]], arr_of[ax[0]]))
+    for t in range(3):
+        if sg[t] < 0:
+            B = np.flip(B, axis=3 - t)
+    B = np.ascontiguousarray(B)
+    write_plot3d(os.path.join(outdir, name + ".xyz"), [A, B])
+
+    viscous = physics in ("ns", "sst")
+    rans = physics == "sst"
+    t_inf, mach = 288.0, 0.4
+    a_inf = math.sqrt(GAMMA * R_AIR * t_inf)
+    u_inf = mach * a_inf
+    rho_inf = 2.0e4 * sutherland_mu(t_inf) / u_inf if viscous else 101325.0 / (R_AIR * t_inf)
+    p_inf = rho_inf * R_AIR * t_inf
+    refs = Refs(t_ref=t_inf, r_ref=rho_inf)
+    vel = f"[{_fmt(u_inf)}, 0, 0]"
+    turb = "; turbulenceIntensity=0.01; eddyViscosityRatio=10.0" if rans else ""
+    ic = (f"icState(tag=-1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; velocity={vel}"
+          f"{turb})")
+    states = [f"characteristic(tag=1; pressure={_fmt(p_inf)}; density={_fmt(rho_inf)}; "
+              f"velocity={vel}{turb})"]
+    # surfaces: first block's i-upper joins the second block's surface that
+    # lies on x = 1
+    t_n = ax.index(0)
+    surf_b = 2 * t_n + (1 if sg[t_n] > 0 else 2)
+    dims_b = [B.shape[3] - 1, B.shape[2] - 1, B.shape[1] - 1]
+
+    def surfaces(dims, conn_surf, conn_tag, far_surf):
+        out = []
+        for t in range(3):
+            for upper in (0, 1):
+                sid = 2 * t + 1 + upper
+                r = [[0, dims[0]], [0, dims[1]], [0, dims[2]]]
+                r[t] = [dims[t], dims[t]] if upper else [0, 0]
+                if sid == conn_surf:
+                    kind, tag = "interblock", conn_tag
+                elif sid == far_surf:
+                    kind, tag = "characteristic", 1
+                else:
+                    kind, tag = "slipWall", 2
+                out.append((kind, r[0][0], r[0][1], r[1][0], r[1][1], r[2][0], r[2][1], tag))
+        return out
+
+    far_b = 2 * t_n + (2 if sg[t_n] > 0 else 1)
+    bc_a = surfaces([na, nb, nc], 2, surf_b * 1000 + 1, 1)
+    bc_b = surfaces(dims_b, surf_b, 2 * 1000 + 0, far_b)
+    scheme = {"cfl": cfl, "limiter": "vanAlbada" if viscous else "minmod",
+              "equationSet": "rans" if rans else ("navierStokes" if viscous else "euler"),
+              "turbulenceModel": "sst2003" if rans else "none",
+              "matrixSolver": "blusgs" if viscous else "lusgs",
+              "matrixSweeps": 2 if viscous else sweeps}
+    inp = os.path.join(outdir, name + ".inp")
+    write_input(inp, name, scheme, refs, ic, states, [bc_a, bc_b])
+
+    prims = []
+    for nodes in (A, B):
+        cen = cell_centres(nodes)
+        xc, yc, zc = cen[0], cen[1], cen[2]
+        rho, u, v, w, p = isentropic_vortex(xc, yc, mach, p_inf, t_inf, 1.5, 0.3, 1.0, 0.45)
+        w = w + 0.05 * a_inf * np.sin(2.0 * np.pi * zc / 0.6) * np.exp(-((xc - 1.0) / 0.4) ** 2)
+        rho = rho * (1.0 + 0.02 * zc / 0.6 + 0.01 * yc)
+        prim = nondimensional_prim(rho, u, v, w, p, refs)
+        if rans:
+            kw = _farfield_turbulence(inp)
+            prim = np.concatenate([prim, np.broadcast_to(kw, prim.shape[:3] + (2,))], axis=-1)
+        prims.append(np.ascontiguousarray(prim.reshape(-1)))
+    return inp, prims
+
+
+def _farfield_turbulence(inp: str) -> np.ndarray:
+    """Nondimensional (k, omega) of a solve's initial condition, as its
+    setup forms them from the input's turbulence intensity and eddy
+    viscosity ratio."""
+    from ._lib import Setup
+    s = Setup(inp)
+    v = s.block_view(0)
+    c = v.ng + (v.ni + 2 * v.ng) * (v.ng + (v.nj + 2 * v.ng) * v.ng)
+    kw = np.array([v.state0[c * v.nv + 5], v.state0[c * v.nv + 6]])
+    s.close()
+    return kw

@@ -117,21 +117,29 @@ __global__ void k_cell_blk(BlockArgs a, SolveDev sv, double cfl) {
   a.ainv[c] = 1.0 / diag;
 }
 
-// Device address of g_face_scratch, looked up once per device with that
-// device current (host code may not use the symbol itself as a pointer).
+// Device address of g_face_scratch on the current device (host code may
+// not use the symbol itself as a pointer).  Looked up with that device
+// current on every call whose stream is not being captured, so the address
+// follows a reset of the device's primary context; a call made during a
+// stream capture uses the address of the device's last uncaptured call.
 std::mutex g_mu;
 double *g_scratch_addr[64] = {nullptr};
 
-double *ScratchAddress(int device) {
+double *ScratchAddress(int device, cudaStream_t stream) {
   if (device < 0 || device >= 64) throw Error(ATH_ERR_ARG, "device id out of range");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  Check(cudaStreamIsCapturing(stream, &cap), "cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[device]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_face_scratch);
     if (e != cudaSuccess)
       throw Error(ATH_ERR_CUDA,
                   std::string("cudaGetSymbolAddress(face scratch): ") + cudaGetErrorString(e));
     g_scratch_addr[device] = static_cast<double *>(p);
+  } else if (!g_scratch_addr[device]) {
+    throw Error(ATH_ERR_ARG,
+                "the first allocation-free call on a device must come before any stream capture");
   }
   return g_scratch_addr[device];
 }
@@ -163,8 +171,29 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
     if (phys->recon != ATH_RECON_MUSCL || phys->flux != ATH_FLUX_ROE)
       throw ath::Error(ATH_ERR_UNSUPPORTED,
                        "the allocation-free residual implements MUSCL reconstruction with the Roe flux");
+    // it forms the inviscid residual, radius and scalar diagonal of a
+    // steady (local time step) solve; views it would silently get wrong
+    // are refused
+    if (phys->eqn != ATH_EQN_EULER)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual implements the Euler equations only");
+    if (phys->turb != ATH_TURB_NONE)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual has no turbulence model");
+    if (phys->solver != ATH_SOLVER_LUSGS && phys->solver != ATH_SOLVER_DPLUR)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual forms the scalar diagonal of lusgs/dplur, "
+                       "not the block diagonal of blusgs/bdplur");
+    if (phys->dt_global > 0.0)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual uses the local (CFL) time step, not a "
+                       "global timeStep");
+    if (phys->dual_cfl > 0.0)
+      throw ath::Error(ATH_ERR_UNSUPPORTED,
+                       "the allocation-free residual has no dual-time term");
     int device = 0;
     ath::Check(cudaGetDevice(&device), "cudaGetDevice");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     ath::BlockArgs a{};
     a.ni = blk->ni;
     a.nj = blk->nj;
@@ -183,7 +212,7 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
     a.lam = blk->lam;
     a.dt = blk->dt;
     a.ainv = blk->ainv;
-    a.flux = ath::ScratchAddress(device);
+    a.flux = ath::ScratchAddress(device, s);
     ath::SolveDev sv{};
     sv.gas_r = phys->gas_r;
     sv.gas_n = phys->gas_n;
@@ -195,7 +224,6 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
     sv.limiter = phys->limiter;
     sv.recon = ATH_RECON_MUSCL;
     sv.flux = ATH_FLUX_ROE;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int64_t nf[3] = {(int64_t)(blk->ni + 1) * blk->nj * blk->nk,
                            (int64_t)blk->ni * (blk->nj + 1) * blk->nk,
                            (int64_t)blk->ni * blk->nj * (blk->nk + 1)};

@@ -554,14 +554,64 @@ bool MatchPatches(const Setup &st, const Patch &A, const Patch &B, V3 shift,
   return false;
 }
 
-// Adds the ghost ops that copy B's interior into A's ghost layers, plus
-// ghost geometry of those cells.
-void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const int m[2][3],
-                   int type, V3 shift) {
+// Sides of patch A's surface that touch another surface of the same block
+// face: [direction 1 start, direction 1 end, direction 2 start, direction 2
+// end] (boundaryConditions::BordersSurface, src/boundaryConditions.cpp:193:
+// any surface of the same face, whatever its type, whose range ends where
+// A's begins or begins where A's ends).
+std::array<bool, 4> PatchBorders(const Block &b, const Patch &A) {
+  std::array<bool, 4> r{false, false, false, false};
+  const int id = b.surfs[A.surf].SurfaceId();
+  for (const auto &o : b.surfs) {
+    if (o.SurfaceId() != id) continue;
+    int lo1, hi1, lo2, hi2;
+    SurfRange(o, A.d1, lo1, hi1);
+    SurfRange(o, A.d2, lo2, hi2);
+    if (A.lo1 == hi1) r[0] = true;
+    if (A.hi1 == lo1) r[1] = true;
+    if (A.lo2 == hi2) r[2] = true;
+    if (A.hi2 == lo2) r[3] = true;
+  }
+  return r;
+}
+
+// Adds the ghost ops that copy B's interior into A's ghost layers and, for
+// interblock connections, the ghost geometry of those cells.
+//
+// Geometry follows the reference's order of construction: every ghost layer
+// of a non-interblock surface, periodic ones included, is a mirror of the
+// block's own boundary cells (procBlock::AssignGhostCellsGeom,
+// src/procBlock.cpp:2201, built before this); interblock ghosts then take
+// the partner's volume, centroid and faces (SwapGeomSlice,
+// src/utility.cpp:213 -> procBlock::PutGeomSlice src/procBlock.cpp:3167):
+// the faces normal to the patch from the boundary face outwards, and of
+// each in-plane direction the ghost's lower face; the upper face of the
+// patch's last cell along an in-plane direction only when that end of the
+// patch does not border another surface of the block face (there the
+// reference's insertion stops short of the patch end and the face keeps its
+// mirror value).  Cell widths are formed afterwards from the face centres of
+// the assembled geometry (procBlock::CalcCellWidths src/procBlock.cpp:6397).
+// Geometry of a block as it was before a connection's swap: both sides of a
+// swap read the partner's values from before either side was written, as
+// the reference extracts both slices first (src/utility.cpp:213-232).
+struct GeomSnap {
+  std::vector<double> vol, center, farea[3], fcenter[3];
+  explicit GeomSnap(const Block &b) : vol(b.vol), center(b.center) {
+    for (int d = 0; d < 3; ++d) {
+      farea[d] = b.farea[d];
+      fcenter[d] = b.fcenter[d];
+    }
+  }
+};
+
+void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const GeomSnap *snap,
+                   const int m[2][3], int type) {
   Block &ba = st.blocks[A.block];
   const Block &bb = st.blocks[B.block];
   const int nA = Ncell(ba, A.d), nB = Ncell(bb, B.d);
   const int64_t ncA = ba.NCell(), ncB = bb.NCell();
+  const bool geom = snap != nullptr;  // interblock connections only
+  const auto bord = PatchBorders(ba, A);
   for (int layer = 1; layer <= ba.ng; ++layer) {
     const int g = A.lower ? -layer : nA + layer - 1;
     int s = B.lower ? layer - 1 : nB - layer;
@@ -594,33 +644,28 @@ void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const int m[2][3],
         }
         op.src2 = -1;
         ba.ops.push_back(op);
-        // ghost geometry from the donor cell
-        ba.vol[op.dst] = bb.vol[op.src];
-        for (int c = 0; c < 3; ++c)
-          ba.center[c * ncA + op.dst] =
-              bb.center[c * ncB + op.src] - (c == 0 ? shift.x : c == 1 ? shift.y : shift.z);
-        // widths: A's direction d maps to B's direction d; in-plane
-        // directions map through the orientation
-        auto wB = [&](int dir) { return bb.width[dir * ncB + op.src]; };
-        ba.width[A.d * ncA + op.dst] = wB(B.d);
-        const int dir_of_a1 = (m[0][1] != 0) ? B.d1 : B.d2;
-        const int dir_of_a2 = (m[0][2] != 0) ? B.d1 : B.d2;
-        ba.width[A.d1 * ncA + op.dst] = wB(dir_of_a1);
-        ba.width[A.d2 * ncA + op.dst] = wB(dir_of_a2);
-        // face areas of the ghost from the donor (procBlock::PutGeomSlice):
+        if (!geom) continue;
+        const GeomSnap &bg = *snap;
+        ba.vol[op.dst] = bg.vol[op.src];
+        for (int c = 0; c < 3; ++c) ba.center[c * ncA + op.dst] = bg.center[c * ncB + op.src];
         // per A direction, the matching B direction and whether increasing
         // index runs the same way; a reversed axis swaps the ghost's low and
         // high faces and flips the unit normal
+        const int dir_of_a1 = (m[0][1] != 0) ? B.d1 : B.d2;
+        const int dir_of_a2 = (m[0][2] != 0) ? B.d1 : B.d2;
         const int bdir[3] = {B.d, dir_of_a1, dir_of_a2};
         const int sgn_d = (A.lower ? -1 : 1) * (B.lower ? 1 : -1);
         const int sgn1 = m[0][1] != 0 ? m[0][1] : m[1][1];
         const int sgn2 = m[0][2] != 0 ? m[0][2] : m[1][2];
         const int sgn[3] = {sgn_d, sgn1, sgn2};
         const int adir[3] = {A.d, A.d1, A.d2};
+        const bool upper_face[3] = {true, a1 == A.hi1 - 1 && !bord[1],
+                                    a2 == A.hi2 - 1 && !bord[3]};
         for (int q = 0; q < 3; ++q) {
           const int ea = adir[q], eb = bdir[q];
           const int64_t nfa = ba.NFace(ea), nfb = bb.NFace(eb);
           for (int side = 0; side < 2; ++side) {
+            if (side == 1 && !upper_face[q]) continue;
             auto gf = G;
             gf[ea] += side;
             auto sf = S;
@@ -628,9 +673,11 @@ void ConnectOneWay(Setup &st, const Patch &A, const Patch &B, const int m[2][3],
             const int64_t ta = ba.Face(ea, gf[0], gf[1], gf[2]);
             const int64_t fb = bb.Face(eb, sf[0], sf[1], sf[2]);
             const double flip = sgn[q] > 0 ? 1.0 : -1.0;
-            for (int comp = 0; comp < 3; ++comp)
-              ba.farea[ea][comp * nfa + ta] = flip * bb.farea[eb][comp * nfb + fb];
-            ba.farea[ea][3 * nfa + ta] = bb.farea[eb][3 * nfb + fb];
+            for (int comp = 0; comp < 3; ++comp) {
+              ba.farea[ea][comp * nfa + ta] = flip * bg.farea[eb][comp * nfb + fb];
+              ba.fcenter[ea][comp * nfa + ta] = bg.fcenter[eb][comp * nfb + fb];
+            }
+            ba.farea[ea][3 * nfa + ta] = bg.farea[eb][3 * nfb + fb];
           }
         }
       }
@@ -785,8 +832,14 @@ void BuildGhostOps(Setup &st, int solve) {
       if (!MatchPatches(st, A, B, shift, mab)) continue;
       if (!MatchPatches(st, B, A, -1.0 * shift, mba))
         Fail("connection patches match one way only");
-      ConnectOneWay(st, A, B, mab, sa.type, shift);
-      ConnectOneWay(st, B, A, mba, sa.type, -1.0 * shift);
+      if (sa.type == ATH_BC_INTERBLOCK) {
+        const GeomSnap ga(st.blocks[A.block]), gb(st.blocks[B.block]);
+        ConnectOneWay(st, A, B, &gb, mab, sa.type);
+        ConnectOneWay(st, B, A, &ga, mba, sa.type);
+      } else {
+        ConnectOneWay(st, A, B, nullptr, mab, sa.type);
+        ConnectOneWay(st, B, A, nullptr, mba, sa.type);
+      }
       used[a] = used[c] = true;
       found = true;
     }
@@ -1281,6 +1334,18 @@ void AppendInput(Setup &st, const std::string &path) {
   ph.cfl_max = getd("cflMax", 1.0);
   if (get("inviscidFluxJacobian", "rusanov") != "rusanov")
     Fail("only the rusanov inviscid flux jacobian is supported");
+  // physics models this build implements: one calorically perfect ideal gas
+  // with Sutherland transport, frozen chemistry, central viscous face values
+  // (the reference's defaults, src/input.cpp:59-95); anything else would
+  // silently change the arithmetic, so it is refused
+  for (const auto &kd : {std::make_pair("thermodynamicModel", "caloricallyPerfect"),
+                         std::make_pair("equationOfState", "idealGas"),
+                         std::make_pair("transportModel", "sutherland"),
+                         std::make_pair("diffusionModel", "none"),
+                         std::make_pair("chemistryModel", "frozen"),
+                         std::make_pair("viscousFaceReconstruction", "central")})
+    if (get(kd.first, kd.second) != kd.second)
+      Fail(std::string("only ") + kd.first + " " + kd.second + " is supported");
   if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
   const auto tm = get("turbulenceModel", "none");
   if (tm != "none" && ph.eqn != ATH_EQN_RANS) Fail("turbulence model needs equationSet rans");
@@ -1426,32 +1491,44 @@ void AppendInput(Setup &st, const std::string &path) {
     sv.states.push_back(s);
   }
 
-  // initial condition: a uniform icState (tag -1)
-  double ic[7] = {0, 0, 0, 0, 0, 0, 0};
-  {
-    bool have = false;
-    double tint = 0.01, vrat = 0.01;
-    for (auto &call : SplitList(get("initialConditions", "<>"))) {
-      auto pc = ParseCall(call);
-      auto &m = pc.second;
-      if (m.count("file")) continue;  // point clouds: state set by caller
-      double v[3] = {0, 0, 0};
-      if (m.count("velocity")) ParseVec3(m["velocity"], v);
-      ic[0] = std::stod(m["density"]) / rref;
-      ic[1] = v[0] / aref;
-      ic[2] = v[1] / aref;
-      ic[3] = v[2] / aref;
-      ic[4] = std::stod(m["pressure"]) / pscale;
-      if (m.count("turbulenceIntensity")) tint = std::stod(m["turbulenceIntensity"]);
-      if (m.count("eddyViscosityRatio")) vrat = std::stod(m["eddyViscosityRatio"]);
-      have = true;
-    }
-    if (!have) {
-      ic[0] = 1.0;
-      ic[4] = 1.0 / 1.4;
-    }
-    if (ph.nv == 7) FarfieldTurbulence(ic, tint, vrat, ph);
+  // initial conditions: uniform icStates, one per block tag or a default
+  // (tag -1) for the others (input::ICStateForBlock src/input.cpp:1146:
+  // an exact tag match wins over the default)
+  struct IcIn {
+    int tag;
+    double w[7];
+  };
+  std::vector<IcIn> ics;
+  for (auto &call : SplitList(get("initialConditions", "<>"))) {
+    auto pc = ParseCall(call);
+    auto &m = pc.second;
+    if (m.count("file")) continue;  // point clouds: state set by caller
+    IcIn x{};
+    x.tag = m.count("tag") ? std::stoi(m["tag"]) : -1;
+    double v[3] = {0, 0, 0};
+    if (m.count("velocity")) ParseVec3(m["velocity"], v);
+    x.w[0] = std::stod(m["density"]) / rref;
+    x.w[1] = v[0] / aref;
+    x.w[2] = v[1] / aref;
+    x.w[3] = v[2] / aref;
+    x.w[4] = std::stod(m["pressure"]) / pscale;
+    const double tint = m.count("turbulenceIntensity") ? std::stod(m["turbulenceIntensity"]) : 0.01;
+    const double vrat = m.count("eddyViscosityRatio") ? std::stod(m["eddyViscosityRatio"]) : 0.01;
+    if (ph.nv == 7) FarfieldTurbulence(x.w, tint, vrat, ph);
+    ics.push_back(x);
   }
+  auto ic_for_block = [&](int blk) -> const IcIn * {
+    const IcIn *pick = nullptr;
+    for (auto &x : ics) {
+      if (x.tag == blk) return &x;
+      if (x.tag == -1 && !pick) pick = &x;
+    }
+    return pick;
+  };
+  IcIn ic_none{};
+  ic_none.w[0] = 1.0;
+  ic_none.w[4] = 1.0 / 1.4;
+  if (ph.nv == 7) FarfieldTurbulence(ic_none.w, 0.01, 0.01, ph);
 
   // grid
   const auto grid = DirName(path) + "/" + get("gridName", "") + ".xyz";
@@ -1483,13 +1560,19 @@ void AppendInput(Setup &st, const std::string &path) {
 
   const int solve = (int)st.solves.size();
   const int first = (int)st.blocks.size();
+  int bidx = 0;
   for (auto &b : blocks) {
+    const IcIn *icb = ics.empty() ? &ic_none : ic_for_block(bidx);
+    if (!icb)
+      Fail("no initial condition for block " + std::to_string(bidx) +
+           " (neither its tag nor a default, tag -1)");
+    const double *ic = icb->w;
+    ++bidx;
     b.ng = ph.ng;
     b.nv = ph.nv;
     b.solve = solve;
     BuildGeometry(b);
     BuildGhostGeometry(b);
-    BuildCellWidths(b);
     BuildHyperplanes(b);
     b.state0.assign((size_t)b.NCell() * b.nv, 0.0);
     for (int k = 0; k < b.nk; ++k)
@@ -1504,12 +1587,14 @@ void AppendInput(Setup &st, const std::string &path) {
   st.solves.push_back(std::move(sv));
   BuildGhostOps(st, solve);
   BuildEdgeOps(st, solve);
+  // widths from the face centres of the assembled geometry, ghosts included
+  // (gridLevel::AuxillaryAndWidths src/gridLevel.cpp:431, after the
+  // connection swaps)
+  for (int bi : st.solves[solve].blocks) BuildCellWidths(st.blocks[bi]);
   // procBlock::CalcWallDistance (src/procBlock.cpp:6030) runs for every case
   // with viscous walls (src/main.cpp:200); without walls the distance keeps
   // its default of 1e10
   if (st.solves[solve].phys.eqn != ATH_EQN_EULER) BuildWallDistance(st, solve);
-  // connection ghost geometry changes the donor-side widths only through
-  // the ops; recompute nothing else
 }
 
 }  // namespace ath

@@ -522,14 +522,21 @@ int ath_batch_profile(ath_batch *batch, int reps, double ms[8]);
  * padded cells are rejected with ATH_ERR_UNSUPPORTED.
  *
  * Computes the same residual R, cell spectral radius, local time step and
- * inverse scalar diagonal as ath_batch_residual (FP64).  Arrays use the
+ * inverse scalar diagonal as ath_batch_residual (FP64) for a steady Euler
+ * solve with MUSCL reconstruction, the Roe flux and a scalar diagonal
+ * (lusgs or dplur); any other view (viscous or RANS equations, block
+ * solvers, a global time step, a dual-time CFL, WENO or AUSM) is refused
+ * with ATH_ERR_UNSUPPORTED.  Arrays use the
  * padded layout of ath_block_view (cell (i,j,k) at (i+ng) + NI*((j+ng) +
  * NJ*(k+ng))), all [var][cell]; face data of direction d are stored at the
  * index of the cell above the face (face i at cell i).  Ghost layers of W
  * must already be filled.
  *
- * The first call on a device looks up the scratch array's device address
- * with that device current; make the first call before any stream capture.
+ * Each call outside a stream capture looks up the scratch array's device
+ * address with the calling device current (so it stays valid after a reset
+ * of the device's primary context); a call inside a capture reuses the
+ * address of that device's last uncaptured call, so make the first call on
+ * a device before any stream capture.
  * Every call on a device shares the one scratch array, so calls that
  * overlap on the GPU (other streams, other host threads) race: serialise
  * them.  stream: a cudaStream_t (NULL = legacy default stream); the call

@@ -24,7 +24,16 @@ def built():
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 REF_HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
-REF_SRC = os.environ.get("AITHER_REFERENCE_SRC", "/root/reference")
+REFCASES = os.path.join(ROOT, "tests", "golden", "refcases")
+
+
+def _reference_source():
+    from aither_gb300 import build
+    return build.reference_source() or ""
+
+
+# the reference's source tree where this machine has it ("" elsewhere)
+REF_SRC = _reference_source()
 
 
 def load_golden(name):
@@ -42,10 +51,19 @@ def golden_case(name, outdir):
     kw = ast.literal_eval(str(g["kwargs"]))
     base = name.split("_it")[0]
     gen = (cases.vortex_box if base.startswith("vortex")
+           else cases.block_pair if base.startswith("pair_")
            else cases.wall_channel if base.startswith("sst_chan")
            else cases.flat_plate if base.startswith(("plate", "sst")) else cases.bump_channel)
     inp, st = gen(outdir, name=base, **kw)
     return inp, st, g
+
+
+def set_states(setup, st):
+    """Sets the analytic initial state of every block of a case (st: one
+    array per block, or None)."""
+    if st is not None:
+        for b, x in enumerate(st):
+            setup.set_state(b, x)
 
 
 def rel_err(a, b):

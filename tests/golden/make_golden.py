@@ -1,8 +1,15 @@
 """Generates the golden fixtures of tests/golden/ by running the reference
 solver itself (built from its sources by oracle/ref_build into oracle/_ref)
-through oracle/ref_build/ref_harness.cpp on seeded synthetic cases.
+through oracle/ref_build/ref_harness.cpp on seeded synthetic cases and on
+the reference's own test cases.
 
-    python tests/golden/make_golden.py [--reference /path/to/aither]
+    python tests/golden/make_golden.py --reference /path/to/aither [--only ...]
+    (or AITHER_REFERENCE_SRC=/path/to/aither)
+
+The reference's test cases (testCases/<case>/<case>.inp and its grid) are
+copied into tests/golden/refcases/<case>/, which is not committed, so that
+the tests can set the same cases up on machines without the reference's
+sources; their fixtures are ref_<case>_it<N>.npz.
 
 Each fixture is an .npz with the fields the reference produced:
   <case>_it<N>.npz : state0, state (physical, after N iterations), resid,
@@ -31,6 +38,7 @@ from aither_gb300 import cases  # noqa: E402
 from refdump import read_dump  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+REFCASE_DIR = os.path.join(HERE, "refcases")
 
 # (fixture name, generator, kwargs, iterations, full fields?)
 CASES = [
@@ -120,6 +128,22 @@ CASES = [
      dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
           nblocks=1, time="bdf2", dt=1e-5, nl=2), [1, 4], True),
 ]
+# two blocks joined in each of the 8 patch orientations (block_pair): Euler
+# with scalar LU-SGS, and SST-2003 RANS with block LU-SGS
+CASES += [(f"pair_{ph}_o{o}", cases.block_pair, dict(orient=o, physics=ph), [1, 10], True)
+          for ph in ("euler", "sst") for o in range(8)]
+
+# the reference's own test cases: (case, iteration counts, rows kept of the
+# per-cell fields: None = all; (d, n) = the first n cells along direction d)
+REFCASES = [
+    ("uniformFlow", [1, 20], None),
+    ("subsonicCylinder", [1, 20], None),
+    ("multiblockCylinder", [1, 20], None),
+    ("couette", [1, 20], None),
+    ("viscousFlatPlate", [1, 20], None),
+    ("rae2822", [1, 20], (1, 8)),
+    ("shockTube", [1, 4], None),
+]
 
 
 def run_case(name, gen, kw, niter, full, ref_dir):
@@ -127,7 +151,8 @@ def run_case(name, gen, kw, niter, full, ref_dir):
         inp, st = gen(d, name=name, **kw)
         args = [HARNESS, os.path.basename(inp), str(niter), "out.bin"]
         if st is not None:
-            np.asarray(st[0], dtype="<f8").tofile(os.path.join(d, "state.bin"))
+            np.concatenate([np.asarray(x, dtype="<f8").reshape(-1) for x in st]).tofile(
+                os.path.join(d, "state.bin"))
             args.append("state.bin")
         env = dict(os.environ, AITHER_INSTALL_DIRECTORY=ref_dir)
         r = subprocess.run(args, cwd=d, env=env, capture_output=True, text=True)
@@ -155,22 +180,75 @@ def run_case(name, gen, kw, niter, full, ref_dir):
     print("wrote", path)
 
 
+def copy_refcase(case, ref_dir):
+    """Copies a reference test case (input file and grid) into
+    tests/golden/refcases/<case>/ and returns its input path there."""
+    import shutil
+    src = os.path.join(ref_dir, "testCases", case)
+    dst = os.path.join(REFCASE_DIR, case)
+    os.makedirs(dst, exist_ok=True)
+    for f in os.listdir(src):
+        if f.endswith((".inp", ".xyz")):
+            shutil.copy(os.path.join(src, f), dst)
+    return os.path.join(dst, case + ".inp")
+
+
+def run_refcase(case, niter, rows, ref_dir):
+    inp = copy_refcase(case, ref_dir)
+    with tempfile.TemporaryDirectory() as d:
+        import shutil
+        for f in os.listdir(os.path.dirname(inp)):
+            shutil.copy(os.path.join(os.path.dirname(inp), f), d)
+        env = dict(os.environ, AITHER_INSTALL_DIRECTORY=ref_dir)
+        r = subprocess.run([HARNESS, case + ".inp", str(niter), "out.bin"], cwd=d, env=env,
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference harness failed on {case}: {r.stderr[-2000:]}")
+        R = read_dump(os.path.join(d, "out.bin"))
+    nblocks = sum(1 for k in R if k.startswith("b") and k.endswith("_resid"))
+    out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "forces": R["forces"],
+           "case": np.array(case), "iterations": np.array(niter), "nblocks": np.array(nblocks),
+           "rows": np.array(rows if rows else (-1, -1))}
+    for b in range(nblocks):
+        p = f"b{b}_"
+        ng = (R[p + "state"].shape[0] - R[p + "resid"].shape[0]) // 2
+        fields = {"state": R[p + "state"][ng:-ng, ng:-ng, ng:-ng], "resid": R[p + "resid"],
+                  "dt": R[p + "dt"], "specrad": R[p + "specrad"], "du": R[p + "du"]}
+        for key, a in fields.items():
+            if rows:
+                d_, n_ = rows
+                sl = [slice(None)] * a.ndim
+                sl[2 - d_] = slice(0, n_)
+                out[p + key + "_sum"] = a.reshape(a.shape[0] * a.shape[1] * a.shape[2], -1).sum(0)
+                a = a[tuple(sl)]
+            out[p + key] = np.ascontiguousarray(a)
+    path = os.path.join(HERE, f"ref_{case}_it{niter}.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("AITHER_REFERENCE_SRC"),
+                    help="the reference's source tree (or AITHER_REFERENCE_SRC)")
     ap.add_argument("--only", nargs="*", help="fixture base names to (re)generate")
     a = ap.parse_args()
+    if not a.reference or not os.path.isdir(os.path.join(a.reference, "src")):
+        ap.error("--reference (or AITHER_REFERENCE_SRC) must name the reference's source tree")
     if not os.path.exists(HARNESS):
         sys.path.insert(0, ROOT)
         from aither_gb300 import build
-        os.environ["AITHER_REFERENCE_SRC"] = a.reference
-        build.REF_SRC = a.reference
-        build.build_reference()
+        build.build_reference(a.reference)
     for name, gen, kw, iters, full in CASES:
         if a.only and name not in a.only:
             continue
         for n in iters:
             run_case(name, gen, kw, n, full, a.reference)
+    for case, iters, rows in REFCASES:
+        if a.only and case not in a.only:
+            continue
+        for n in iters:
+            run_refcase(case, n, rows, a.reference)
 
 
 if __name__ == "__main__":

@@ -79,8 +79,9 @@ def case_input(tmp: str, gen: str, kw: dict, iterations: int, variables: list) -
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=REF_EXE)
-    ap.add_argument("--install-dir", default=os.environ.get("AITHER_REFERENCE_SRC",
-                                                            "/root/reference"))
+    ap.add_argument("--install-dir", default=os.environ.get("AITHER_REFERENCE_SRC"),
+                    help="directory holding fluidDatabase/ (the reference's source tree, "
+                         "or AITHER_REFERENCE_SRC)")
     ap.add_argument("--only", nargs="*", help="case names to (re)generate")
     args = ap.parse_args()
     os.makedirs(OUT, exist_ok=True)
