@@ -133,6 +133,14 @@ CASES = [
 CASES += [(f"pair_{ph}_o{o}", cases.block_pair, dict(orient=o, physics=ph), [1, 10], True)
           for ph in ("euler", "sst") for o in range(8)]
 
+# full-size configurations whose per-cell fields are kept only for the first
+# cells along one direction (d, n), with per-variable sums of |value| over
+# every cell: (fixture name, generator, kwargs, iteration counts, rows)
+ROWCASES = [
+    # the 256x192x4 SST-2003 flat plate (WENO, AUSMPW+, block LU-SGS)
+    ("sst_c3", cases.sst_plate, dict(), [1], (1, 16)),
+]
+
 # the reference's own test cases: (case, iteration counts, rows kept of the
 # per-cell fields: None = all; (d, n) = the first n cells along direction d)
 REFCASES = [
@@ -193,14 +201,21 @@ def copy_refcase(case, ref_dir):
     return os.path.join(dst, case + ".inp")
 
 
-def run_refcase(case, niter, rows, ref_dir):
-    inp = copy_refcase(case, ref_dir)
+def run_refcase(case, niter, rows, ref_dir, gen=None, kw=None):
+    """A reference test case (gen None) or a generated full-size case, with
+    the per-cell fields restricted to `rows`."""
     with tempfile.TemporaryDirectory() as d:
         import shutil
-        for f in os.listdir(os.path.dirname(inp)):
-            shutil.copy(os.path.join(os.path.dirname(inp), f), d)
+        if gen is None:
+            inp = copy_refcase(case, ref_dir)
+            for f in os.listdir(os.path.dirname(inp)):
+                shutil.copy(os.path.join(os.path.dirname(inp), f), d)
+            name = case
+        else:
+            inp, _ = gen(d, name=case, **kw)
+            name = os.path.basename(inp)[:-4]
         env = dict(os.environ, AITHER_INSTALL_DIRECTORY=ref_dir)
-        r = subprocess.run([HARNESS, case + ".inp", str(niter), "out.bin"], cwd=d, env=env,
+        r = subprocess.run([HARNESS, name + ".inp", str(niter), "out.bin"], cwd=d, env=env,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference harness failed on {case}: {r.stderr[-2000:]}")
@@ -208,7 +223,7 @@ def run_refcase(case, niter, rows, ref_dir):
     nblocks = sum(1 for k in R if k.startswith("b") and k.endswith("_resid"))
     out = {"l2": R["l2"], "matrix_resid": R["matrix_resid"], "forces": R["forces"],
            "case": np.array(case), "iterations": np.array(niter), "nblocks": np.array(nblocks),
-           "rows": np.array(rows if rows else (-1, -1))}
+           "rows": np.array(rows if rows else (-1, -1)), "kwargs": np.array(repr(kw or {}))}
     for b in range(nblocks):
         p = f"b{b}_"
         ng = (R[p + "state"].shape[0] - R[p + "resid"].shape[0]) // 2
@@ -219,10 +234,11 @@ def run_refcase(case, niter, rows, ref_dir):
                 d_, n_ = rows
                 sl = [slice(None)] * a.ndim
                 sl[2 - d_] = slice(0, n_)
-                out[p + key + "_sum"] = a.reshape(a.shape[0] * a.shape[1] * a.shape[2], -1).sum(0)
+                out[p + key + "_abssum"] = np.abs(a).reshape(
+                    a.shape[0] * a.shape[1] * a.shape[2], -1).sum(0)
                 a = a[tuple(sl)]
             out[p + key] = np.ascontiguousarray(a)
-    path = os.path.join(HERE, f"ref_{case}_it{niter}.npz")
+    path = os.path.join(HERE, f"{'ref_' if gen is None else ''}{case}_it{niter}.npz")
     np.savez_compressed(path, **out)
     print("wrote", path)
 
@@ -249,6 +265,11 @@ def main():
             continue
         for n in iters:
             run_refcase(case, n, rows, a.reference)
+    for name, gen, kw, iters, rows in ROWCASES:
+        if a.only and name not in a.only:
+            continue
+        for n in iters:
+            run_refcase(name, n, rows, a.reference, gen, kw)
 
 
 if __name__ == "__main__":

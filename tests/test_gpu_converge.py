@@ -164,3 +164,37 @@ def test_jacobi_relaxation_reaches_the_lusgs_steady_state(ctx, solver, tmp_path)
     print(f"{solver} vs lusgs: rel err {err:.2e}, iterations {out[solver][1]} vs "
           f"{out['lusgs'][1]}")
     assert err <= 1e-6
+
+
+@pytest.mark.parametrize("kind", ["laminar", "sst"])
+def test_mixed_precision_converged_wall_forces_against_fp64(ctx, kind, tmp_path):
+    """Integrated wall forces (pressure and shear over the viscous wall) of
+    the converged mixed-precision solution against the FP64 one: within
+    1e-6 relative to the largest force component, at a 1e-8 drop (laminar
+    Navier-Stokes bump channel) and a 1e-7 drop (SST-2003 RANS).  The forces
+    of a converged state are taken from one more iteration of the retired
+    solve, reactivated."""
+    from aither_gb300 import Batch, Setup, cases
+    if kind == "laminar":
+        inp, _ = cases.wall_channel(str(tmp_path / kind), 24, 16, 2, "bump", 0.06, 0.5,
+                                    alpha=1.0, viscous=True, reynolds=2e4, stretch=1.1,
+                                    cfl=50.0, name=kind)
+        drop = 1e-8
+    else:
+        inp, _ = cases.wall_channel(str(tmp_path / kind), 32, 16, 4, "bump", 0.08, 0.6,
+                                    alpha=2.0, rans=True, stretch=1.1, name=kind)
+        drop = 1e-7
+    forces, states = {}, {}
+    for prec in (0, 1):
+        b = Batch(ctx, Setup(inp), prec)
+        info = b.converge(40000, drop, check_every=200)
+        assert info[0].converged == 1, (kind, prec, info[0].drop, info[0].iterations)
+        b.set_target(0, 0.0, active=True)
+        f = np.array(b.iterate(1)[0].force[:])
+        assert np.abs(f).max() > 0
+        forces[prec], states[prec] = f, b.field(0, "STATE")
+        b.close()
+    err = float(np.abs(forces[1] - forces[0]).max() / np.abs(forces[0]).max())
+    serr = rel_err(states[1][..., :5], states[0][..., :5])
+    print(f"{kind}: mixed vs FP64 wall forces rel err {err:.2e}, state {serr:.2e}")
+    assert err <= 1e-6
