@@ -54,29 +54,32 @@ __device__ __forceinline__ double DDot(const double *a, const double *b) {
 }
 
 // turbKWSst::EddyViscAndBlending (src/turbulence.cpp:668) with Alpha1-3,
-// CDkw, F1, F2 and EddyVisc (:573-634, include/turbulence.hpp:529)
-__device__ __forceinline__ void SstEddyVisc(const Prim<double> &w, const double kw[2],
-                                            const double vg[9], const double kg[3],
-                                            const double wg[3], double mu, double wd,
-                                            double scale, double &mut, double &f1,
-                                            double &f2) {
-  const double k = kw[0], om = kw[1], rho = w.rho;
-  const double a1 = scale * sqrt(k) / (kSstBetaStar * om * (wd + 1.0e-30));
-  const double a2 = scale * scale * 500.0 * mu / ((wd + 1.0e-30) * (wd + 1.0e-30) * rho * om);
-  const double cd = CMax(2.0 * rho * kSstSigmaW2 / om * Dot(kg[0], kg[1], kg[2], wg[0], wg[1],
-                                                            wg[2]),
-                         1.0e-10);
-  const double a3 = 4.0 * rho * kSstSigmaW2 * k / (cd * (wd + 1.0e-30) * (wd + 1.0e-30));
-  f1 = tanh(pow(CMin(CMax(a1, a2), a3), 4.0));
-  const double arg2 = CMax(2.0 * a1, a2);
+// CDkw, F1, F2 and EddyVisc (:573-634, include/turbulence.hpp:529); T is
+// double on the FP64 path, float for the mixed path's viscous faces
+template <typename T>
+__device__ __forceinline__ void SstEddyVisc(const Prim<T> &w, const T kw[2], const T vg[9],
+                                            const T kg[3], const T wg[3], T mu, T wd, T scale,
+                                            T &mut, T &f1, T &f2) {
+  const T k = kw[0], om = kw[1], rho = w.rho;
+  const T a1 = scale * sqrt(k) / (T(kSstBetaStar) * om * (wd + T(1.0e-30)));
+  const T a2 = scale * scale * T(500.0) * mu / ((wd + T(1.0e-30)) * (wd + T(1.0e-30)) * rho * om);
+  const T cd = CMax(T(2.0) * rho * T(kSstSigmaW2) / om * Dot(kg[0], kg[1], kg[2], wg[0], wg[1],
+                                                              wg[2]),
+                    T(1.0e-10));
+  const T a3 = T(4.0) * rho * T(kSstSigmaW2) * k / (cd * (wd + T(1.0e-30)) * (wd + T(1.0e-30)));
+  f1 = tanh(pow(CMin(CMax(a1, a2), a3), T(4.0)));
+  const T arg2 = CMax(T(2.0) * a1, a2);
   f2 = tanh(arg2 * arg2);
-  double S[9];
+  T S[9];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int q = 0; q < 3; ++q) S[r * 3 + q] = 0.5 * (vg[r * 3 + q] + vg[q * 3 + r]);
-  const double msr = sqrt(2.0 * DDot(S, S));
-  mut = rho * kSstA1 * k / CMax(kSstA1 * om, scale * msr * f2);
+    for (int q = 0; q < 3; ++q) S[r * 3 + q] = T(0.5) * (vg[r * 3 + q] + vg[q * 3 + r]);
+  T ss = T(0);
+#pragma unroll
+  for (int e = 0; e < 9; ++e) ss += S[e] * S[e];
+  const T msr = sqrt(T(2.0) * ss);
+  mut = rho * T(kSstA1) * k / CMax(T(kSstA1) * om, scale * msr * f2);
 }
 
 // turbKWSst::CalcTurbSrc (src/turbulence.cpp:637) with the Boussinesq
@@ -623,6 +626,124 @@ __device__ __forceinline__ void FaceFluxMixedRoe(const Pools<PT> &P, const Solve
   for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - (double)d[v])) * 0.5;
 }
 
+// WENO increment over the upwind cell value in FP32, from differences to
+// it formed in FP64: each stencil's interpolation weights sum to one and
+// the smoothness indicators use differences only, so shifting the five
+// values by the upwind one yields the increment itself.
+__device__ __forceinline__ float WenoDelta1(const WenoCoeffs<float> &k, const float w[5],
+                                            double y3, double y2, double y1, double d1,
+                                            double d2, bool z) {
+  return Weno1<float>(k, w, (float)(y3 - y1), (float)(y2 - y1), 0.0f, (float)(d1 - y1),
+                      (float)(d2 - y1), z);
+}
+
+// Mixed-precision face of any reconstruction and flux: FP64 face states are
+// the FP64 upwind cell values plus increments computed in FP32 (MUSCL or
+// WENO, k and omega too), so their rounding is relative to the increments;
+// Roe faces then take the FP64 central flux and FP32 dissipation
+// (FaceFluxMixedRoe), AUSMPW+ faces and the turbulence fluxes are evaluated
+// in FP64 from the FP64 face states (their pressure splitting is not a
+// small correction to a central flux, so FP32 would put its rounding on the
+// flux itself).
+template <int D, typename PT>
+__device__ __forceinline__ void FaceFluxMixed(const Pools<PT> &P, const SolveDev &sv, int64_t c,
+                                              int64_t s, double f[5], Prim<double> &L,
+                                              Prim<double> &R, double ft[2] = nullptr) {
+  if (!ft && sv.flux == ATH_FLUX_ROE &&
+      (sv.recon == ATH_RECON_MUSCL || sv.recon == ATH_RECON_CONSTANT)) {
+    FaceFluxMixedRoe<D>(P, sv, c, s, f, L, R);
+    return;
+  }
+  const int64_t n = P.ncell;
+  const double *wd = P.width[D];
+  const double *W = P.W;
+  auto val = [&](int v, int64_t x) { return W[v * n + x]; };
+  double l[5], r[5], lt[2] = {0, 0}, rt[2] = {0, 0};
+  const double *Wt = P.Wt;
+  if (sv.recon == ATH_RECON_CONSTANT) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      l[v] = val(v, c - s);
+      r[v] = val(v, c);
+    }
+    if (ft)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        lt[q] = Wt[q * n + c - s];
+        rt[q] = Wt[q * n + c];
+      }
+  } else if (sv.recon == ATH_RECON_MUSCL) {
+    const float xm2 = (float)wd[c - 2 * s], xm1 = (float)wd[c - s], x0 = (float)wd[c],
+                xp1 = (float)wd[c + s];
+    const float kappa = (float)sv.kappa;
+    const float dpL = (xm1 + xm1) / (xm1 + x0), dmL = (xm1 + xm1) / (xm1 + xm2);
+    const float dpR = (x0 + x0) / (x0 + xm1), dmR = (x0 + x0) / (x0 + xp1);
+    auto muscl = [&](double am, double a1, double a0, double ap, double &lo, double &hi) {
+      const float dl = MusclDelta1((float)(a1 - am), (float)(a0 - a1), dpL, dmL, kappa,
+                                   sv.limiter);
+      const float dr = MusclDelta1((float)(a0 - ap), (float)(a1 - a0), dpR, dmR, kappa,
+                                   sv.limiter);
+      lo = a1 + (double)dl;
+      hi = a0 + (double)dr;
+    };
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      muscl(val(v, c - 2 * s), val(v, c - s), val(v, c), val(v, c + s), l[v], r[v]);
+    if (ft)
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        muscl(Wt[q * n + c - 2 * s], Wt[q * n + c - s], Wt[q * n + c], Wt[q * n + c + s],
+              lt[q], rt[q]);
+  } else {
+    const bool z = sv.recon == ATH_RECON_WENOZ;
+    const float wl[5] = {(float)wd[c - 3 * s], (float)wd[c - 2 * s], (float)wd[c - s],
+                         (float)wd[c], (float)wd[c + s]};
+    const float wu[5] = {(float)wd[c + 2 * s], (float)wd[c + s], (float)wd[c],
+                         (float)wd[c - s], (float)wd[c - 2 * s]};
+    const WenoCoeffs<float> kl = MakeWeno(wl), ku = MakeWeno(wu);
+    auto weno = [&](const double *a, double &lo, double &hi) {
+      const double ym3 = a[c - 3 * s], ym2 = a[c - 2 * s], ym1 = a[c - s], y0 = a[c],
+                   yp1 = a[c + s], yp2 = a[c + 2 * s];
+      lo = ym1 + (double)WenoDelta1(kl, wl, ym3, ym2, ym1, y0, yp1, z);
+      hi = y0 + (double)WenoDelta1(ku, wu, yp2, yp1, y0, ym1, ym2, z);
+    };
+#pragma unroll
+    for (int v = 0; v < 5; ++v) weno(W + v * n, l[v], r[v]);
+    if (ft)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) weno(Wt + q * n, lt[q], rt[q]);
+  }
+  L = Prim<double>{l[0], l[1], l[2], l[3], l[4]};
+  R = Prim<double>{r[0], r[1], r[2], r[3], r[4]};
+  const double *fa = P.fa[D];
+  const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c];
+  const Gas<double> g = GasOf<double>(sv);
+  if (sv.flux == ATH_FLUX_AUSM) {
+    double vlr[2];
+    AusmFlux(L, R, g, nx, ny, nz, f, vlr);
+    if (ft)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        ft[q] = L.rho * vlr[0] * lt[q];
+        ft[q] += R.rho * vlr[1] * rt[q];
+      }
+    return;
+  }
+  // Roe: FP64 central flux, FP32 dissipation from FP64-formed jumps
+  const float dq[5] = {(float)(R.rho - L.rho), (float)(R.u - L.u), (float)(R.v - L.v),
+                       (float)(R.w - L.w), (float)(R.p - L.p)};
+  const Prim<float> Lf{(float)L.rho, (float)L.u, (float)L.v, (float)L.w, (float)L.p};
+  const Prim<float> Rf{(float)R.rho, (float)R.u, (float)R.v, (float)R.w, (float)R.p};
+  float d[5];
+  RoeDissipation(Lf, Rf, dq, GasOf<float>(sv), (float)nx, (float)ny, (float)nz, d);
+  double fl[5], fr[5];
+  InvFluxCentral(L, g, nx, ny, nz, fl);
+  InvFluxCentral(R, g, nx, ny, nz, fr);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - (double)d[v])) * 0.5;
+  if (ft) RoeTurbFlux(L, R, lt, rt, g, nx, ny, nz, ft);
+}
+
 template <typename T, int D, bool RANS>
 __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
@@ -640,11 +761,7 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
     double f[5];
     Prim<double> L, R;
     double ft[2];
-    if (!RANS && sv.flux == ATH_FLUX_ROE &&
-        (sv.recon == ATH_RECON_MUSCL || sv.recon == ATH_RECON_CONSTANT))
-      FaceFluxMixedRoe<D>(P, sv, c, s, f, L, R);
-    else
-      FaceFlux<double, D>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);  // AUSM, WENO, RANS
+    FaceFluxMixed<D>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
     if (RANS)
 #pragma unroll
       for (int q = 0; q < 2; ++q) P.fluxt[D][q * n + c] = ft[q] * mag;
@@ -2282,8 +2399,154 @@ __device__ __forceinline__ void TurbFaceGrads(const Pools<PT> &P, const BlockDev
   }
 }
 
-// Viscous face of a RANS solve (CalcViscFluxI/J/K with SST, in FP64 for
-// both precisions): eddy viscosity and blending from the central face
+// The same gradients in FP32 from the dual cell's k and omega minus the
+// upper cell's, differences formed in FP64 (the dual cell is closed, so the
+// offset does not change the gradient; the rounding is relative to the
+// differences rather than to k and omega).
+template <int D, typename PT>
+__device__ __forceinline__ void TurbFaceGradsMixed(const Pools<PT> &P, const BlockDev &b,
+                                                   int64_t c, float kg[3], float wg[3]) {
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  auto area = [&](int e, int64_t x, float a[3]) {
+    const double *fa = P.fa[e];
+    const float m = (float)fa[3 * n + x];
+    a[0] = (float)fa[x] * m;
+    a[1] = (float)fa[n + x] * m;
+    a[2] = (float)fa[2 * n + x] * m;
+  };
+  float lo[3][2], hi[3][2], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const double *T_ = P.Wt + q * n;
+      const double base = T_[cu];
+      const float ol = (float)(T_[cl] - base);
+      if (e == D) {
+        lo[e][q] = ol;
+        hi[e][q] = 0.f;
+      } else {
+        hi[e][q] = 0.25f * ((ol + (float)(T_[cu + st[e]] - base)) + (float)(T_[cl + st[e]] - base));
+        lo[e][q] = 0.25f * ((ol + (float)(T_[cu - st[e]] - base)) + (float)(T_[cl - st[e]] - base));
+      }
+    }
+    if (e == D) {
+      float A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5f * (A0[r] + A1[r]);
+        alo[e][r] = 0.5f * (A0[r] + A2[r]);
+      }
+    } else {
+      float Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5f * (Aup[r] + Alp[r]);
+        alo[e][r] = 0.5f * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const float invVol = 1.f / (0.5f * ((float)P.vol[cl] + (float)P.vol[cu]));
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    kg[r] = (hi[0][0] * ahi[0][r] - lo[0][0] * alo[0][r] + hi[1][0] * ahi[1][r] -
+             lo[1][0] * alo[1][r] + hi[2][0] * ahi[2][r] - lo[2][0] * alo[2][r]) *
+            invVol;
+    wg[r] = (hi[0][1] * ahi[0][r] - lo[0][1] * alo[0][r] + hi[1][1] * ahi[1][r] -
+             lo[1][1] * alo[1][r] + hi[2][1] * ahi[2][r] - lo[2][1] * alo[2][r]) *
+            invVol;
+  }
+}
+
+// Viscous face of a RANS solve on the mixed path: the FP64 face's terms in
+// FP32 (gradients from FP64-formed offsets, eddy viscosity and blending,
+// stresses and the k and omega diffusion fluxes); the viscous flux enters
+// the FP64 residual sum as the inviscid one does.
+template <int D>
+__device__ __forceinline__ void RansViscFaceMixed(Pools<float> &P, const BlockDev &b,
+                                                  const SolveDev &sv, int64_t c) {
+  const Gas<float> g = GasOf<float>(sv);
+  const int64_t n = P.ncell;
+  float grad[3][3], tg[3], muf;
+  Prim<float> fs;
+  ViscFaceGatherMixed<D>(P, b, sv, c, grad, tg, fs, muf);
+  float kg[3], wg[3];
+  TurbFaceGradsMixed<D>(P, b, c, kg, wg);
+  const int64_t cu = c, cl = c - StrideOf(b, D);
+  const double *wd = P.width[D];
+  float cd, cw;
+  CentralCoeffs((float)wd[cl], (float)wd[cu], cd, cw);
+  float fst[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    fst[q] = CMax(cd * (float)P.Wt[q * n + cu] + cw * (float)P.Wt[q * n + cl], (float)kTurbMin);
+  float wdf = cd * (float)P.wd[cu] + cw * (float)P.wd[cl];
+  if (wdf < 0.f && wdf > -1.0e-10f) wdf = 0.f;
+  const float scale = (float)sv.visc_scale;
+  const float vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
+                       grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
+  float mutf, f1f, f2f;
+  SstEddyVisc<float>(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
+  const double *fa = P.fa[D];
+  const float nx = (float)fa[c], ny = (float)fa[n + c], nz = (float)fa[2 * n + c],
+              mag = (float)fa[3 * n + c];
+  const float mus = scale * muf, muts = scale * mutf;
+  float tau[3];
+  TauNormal(vg, nx, ny, nz, mus, muts, tau);
+  const float kf = SutherlandRatio(Temperature(fs, g), (float)sv.t_ref, (float)sv.k_c1,
+                                   (float)sv.k_s, (float)sv.k_ref) *
+                   scale;
+  const float kt = muts * g.Cp() / 0.9f;
+  float F[5];
+  F[0] = 0.f;
+  F[1] = tau[0];
+  F[2] = tau[1];
+  F[3] = tau[2];
+  F[4] = Dot(tau[0], tau[1], tau[2], fs.u, fs.v, fs.w) +
+         (kf + kt) * Dot(tg[0], tg[1], tg[2], nx, ny, nz);
+  const float Ft0 = (mus + Blended((float)kSstSigmaK1, (float)kSstSigmaK2, f1f) * muts) *
+                    Dot(kg[0], kg[1], kg[2], nx, ny, nz);
+  const float Ft1 = (mus + Blended((float)kSstSigmaW1, (float)kSstSigmaW2, f1f) * muts) *
+                    Dot(wg[0], wg[1], wg[2], nx, ny, nz);
+  float *out = P.vflux[D];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v * n + c] = F[v] * mag;
+  P.vfluxt[D][c] = Ft0 * mag;
+  P.vfluxt[D][n + c] = Ft1 * mag;
+  float *rs = P.rst[D];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) rs[e * n + c] = vg[e];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    rs[(9 + e) * n + c] = kg[e];
+    rs[(12 + e) * n + c] = wg[e];
+  }
+  rs[15 * n + c] = mutf;
+  rs[16 * n + c] = f1f;
+  rs[17 * n + c] = f2f;
+  if (sv.block) {
+    float *vs = P.vst[D];
+    vs[0 * n + c] = fs.rho;
+    vs[1 * n + c] = fs.u;
+    vs[2 * n + c] = fs.v;
+    vs[3 * n + c] = fs.w;
+    vs[4 * n + c] = fs.p;
+    vs[5 * n + c] = muf;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) vs[(6 + e) * n + c] = vg[e];
+  }
+}
+
+// Viscous face of a RANS solve (CalcViscFluxI/J/K with SST, in FP64): eddy viscosity and blending from the central face
 // state (turbulence floors applied), the face gradients and the central
 // wall distance (clipped to 0 within WALL_DIST_NEG_TOL); flow flux with
 // mu + mut and the turbulent conductivity, k and omega diffusion fluxes.
@@ -2312,7 +2575,7 @@ __device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, con
   const double vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
                         grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
   double mutf, f1f, f2f;
-  SstEddyVisc(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
+  SstEddyVisc<double>(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
   const double *fa = P.fa[D];
   const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c], mag = fa[3 * n + c];
   const double mus = scale * muf, muts = scale * mutf;
@@ -2370,7 +2633,10 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
   const SolveDev sv = P.solves[b.solve];
   if (!sv.viscous || !sv.active || (sv.rans != 0) != RANS) return;
   if constexpr (RANS) {
-    RansViscFace<T, D>(P, b, sv, c);
+    if constexpr (std::is_same<T, float>::value)
+      RansViscFaceMixed<D>(P, b, sv, c);
+    else
+      RansViscFace<T, D>(P, b, sv, c);
     return;
   }
   const Gas<T> g = GasOf<T>(sv);
