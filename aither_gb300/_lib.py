@@ -18,6 +18,7 @@ BC = dict(SLIP_WALL=0, VISCOUS_WALL=1, CHARACTERISTIC=2, STAGNATION_INLET=3,
           PRESSURE_OUTLET=4, SUPERSONIC_INFLOW=5, SUPERSONIC_OUTFLOW=6,
           PERIODIC=7, INTERBLOCK=8)
 PREC_FP64, PREC_MIXED = 0, 1
+BATCH_MATRIX_RESID, BATCH_FAST_FACES = 1, 2
 FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
              WALLDIST=9, CONS_N=10, CONS_NM1=11)
 
@@ -192,6 +193,8 @@ def lib() -> C.CDLL:
             "ath_batch_autotune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int)]),
             "ath_batch_sweep_shape": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                                 C.POINTER(C.c_int)]),
+            "ath_batch_set_sweep_shape": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
+            "ath_batch_sweep_wait_test": (C.c_int, [vp, C.c_longlong, C.c_int]),
             "ath_server_create": (C.c_int, [vp, C.c_int, C.c_double, C.c_int64, C.c_int,
                                             C.c_int, C.POINTER(vp)]),
             "ath_server_submit": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_int64)]),
@@ -493,12 +496,21 @@ class Batch:
         return it.value, rf[:self.setup.solve_nv(solve)]
 
     def sweep_shape(self) -> dict:
-        """LU-SGS sweep shape: mode 1 persistent (cluster CTAs per solve),
-        0 one launch per hyperplane, 2 the same with a group of lanes per
-        scalar cell."""
+        """LU-SGS sweep shape: mode 1 persistent cluster sweep (cluster CTAs
+        per solve), 0 one launch per hyperplane, 2 the same with a group of
+        lanes per scalar cell, 3 persistent tile queue (threads = cells per
+        tile)."""
         m, t, c = C.c_int(), C.c_int(), C.c_int()
         check(lib().ath_batch_sweep_shape(self.h, C.byref(m), C.byref(t), C.byref(c)))
         return {"mode": m.value, "threads": t.value, "cluster": c.value}
+
+    def set_sweep_shape(self, mode: int, threads: int, cluster: int = 0) -> None:
+        check(lib().ath_batch_set_sweep_shape(self.h, mode, threads, cluster))
+
+    def sweep_wait_test(self, poll_limit: int, wait_never: bool) -> None:
+        """Poll limit of the tile-queue sweep's waits; wait_never makes every
+        wait poll a flag nothing sets (tests of the bounded wait)."""
+        check(lib().ath_batch_sweep_wait_test(self.h, poll_limit, 1 if wait_never else 0))
 
     def pool_vars(self) -> int:
         """Values per cell of the copy_state snapshot (5, or 7 with SST)."""

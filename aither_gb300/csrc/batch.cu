@@ -139,6 +139,21 @@ struct BatchCore {
   SweepLists Lists() const {
     return SweepLists{d_cl_items, d_cl_step_off, d_solve_step0, d_solve_nsteps, nsolves};
   }
+  // mode 3 = the persistent tile-queue sweep: tiles of at most tq_size cells
+  // of one solve's hyperplane, per kind (scalar, block) and direction; the
+  // lists of every candidate tile size are built at batch creation
+  struct TqList {
+    int4 *tiles = nullptr;
+    int32_t *deps = nullptr;
+    int *done = nullptr;
+    int ntiles = 0;
+  };
+  int tq_size = 128;
+  std::map<int, std::array<TqList, 4>> tq;  // tile size -> [kind * 2 + backward]
+  int tq_ctas[2] = {0, 0};                  // resident CTAs, scalar and block kernels
+  int *d_tq_ticket = nullptr, *d_tq_status = nullptr;
+  long long tq_spin_limit = 1LL << 24;      // polls of one wait (~1 s)
+  int tq_wait_never = 0;                    // test mode: every wait polls a flag never set
   bool block_viscous = false;
   bool any_rans = false;  // SST solves present: k, omega pools allocated
   bool any_unsteady = false;  // time-accurate or nonreflecting solves: time levels kept
@@ -327,6 +342,7 @@ class RunnerBase {
   virtual void Snapshot(bool restore) = 0;
   virtual void FreeSnapshot() = 0;
   virtual int MaxClusters(int kinds, int threads, int cluster) = 0;
+  virtual int TqOccupancy(bool full, bool block) = 0;
 };
 
 template <typename T>
@@ -594,15 +610,35 @@ class Runner : public RunnerBase {
   void Residual() override {
     for (int d = 0; d < 3; ++d)
       Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
-                      (int)c_.L.face_cta_block[d].size(), c_.fkinds, c_.stream);
+                      (int)c_.L.face_cta_block[d].size(), FaceKinds(), c_.stream);
     Viscous();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                     c_.kinds, c_.stream);
     if (c_.kinds & 2)
       Launch<T>::OffJac(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), c_.stream);
   }
+  // face kernels to launch: the batch's solve kinds, plus bit 2 for the
+  // fast FP64 faces (batch flag bit 1)
+  int FaceKinds() const { return c_.fkinds | ((c_.flags & 2) ? 4 : 0); }
   void SweepPass(int forward, int sweep) {
     const bool full = c_.max_sweeps > 1;
+    if (c_.sweep_mode == 3) {
+      auto &lists = c_.tq.at(c_.tq_size);
+      for (int kind = 0; kind < 2; ++kind) {
+        if (!(c_.skinds & (1 << kind))) continue;
+        const BatchCore::TqList &t = lists[kind * 2 + (forward ? 0 : 1)];
+        if (t.ntiles == 0) continue;
+        Check(cudaMemsetAsync(t.done, 0, (size_t)(t.ntiles + 1) * sizeof(int), c_.stream),
+              "memset");
+        Check(cudaMemsetAsync(c_.d_tq_ticket, 0, sizeof(int), c_.stream), "memset");
+        TileQueueDev Q{c_.d_cl_items, t.tiles,      t.deps,
+                       t.done,        c_.d_tq_ticket, c_.d_tq_status,
+                       t.ntiles,      c_.tq_wait_never, c_.tq_spin_limit};
+        Launch<T>::SweepTq(P_, Q, forward, sweep, full, kind == 1, c_.tq_ctas[kind],
+                           c_.stream);
+      }
+      return;
+    }
     if (c_.sweep_mode == 1) {
       Launch<T>::SweepCl(P_, c_.Lists(), forward, sweep, full, c_.skinds, c_.cl_threads,
                          c_.cl_size, c_.stream);
@@ -714,7 +750,7 @@ class Runner : public RunnerBase {
       Check(cudaEventRecord(e[1], c_.stream), "event");
       for (int d = 0; d < 3; ++d) {
         Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
-                        (int)c_.L.face_cta_block[d].size(), c_.fkinds, c_.stream);
+                        (int)c_.L.face_cta_block[d].size(), FaceKinds(), c_.stream);
         Check(cudaEventRecord(e[2 + d], c_.stream), "event");
       }
       Viscous();
@@ -781,6 +817,7 @@ class Runner : public RunnerBase {
   int MaxClusters(int kinds, int threads, int cluster) override {
     return Launch<T>::MaxClusters(kinds, threads, cluster);
   }
+  int TqOccupancy(bool full, bool block) override { return Launch<T>::TqOccupancy(full, block); }
   void Snapshot(bool restore) override {
     DevMem &m = *c_.mem;
     const size_t wbytes = 5 * (size_t)c_.ncell * sizeof(double);
@@ -1245,6 +1282,74 @@ void BuildLists(BatchCore &c) {
 // edge phases, viscous ghosts, aux, faces, wall forces, cell, off-diagonal
 // Jacobians, the relaxations' launches, update, norms, counter, and the
 // optional matrix residual
+// Tile-queue lists of one tile size: for each kind of LU-SGS solve (scalar,
+// block) and each pass direction, the tiles in ticket order -- step by step
+// (forward: plane 0 first; backward: each solve's last plane first), the
+// solves of a step in turn, each solve's plane cut into runs of at most
+// `size` cells of the solve-grouped item list -- and for every tile the
+// tiles of the previous step that hold its cells' neighbours on the swept
+// side (lower neighbours forward, upper ones backward; connection
+// neighbours are read from ghost slots filled before the pass, so they add
+// no dependency).
+void BuildTileQueue(BatchCore &c, const Setup &st, DevMem &m, int size) {
+  const int64_t nq = c.nq;
+  std::array<BatchCore::TqList, 4> out;
+  std::vector<int32_t> tile_of(nq, -1);
+  for (int kind = 0; kind < 2; ++kind) {
+    if (!(c.skinds & (1 << kind))) continue;
+    std::vector<int> solves;
+    int maxst = 0;
+    for (int s = 0; s < c.nsolves; ++s) {
+      const auto &ph = st.solves[s].phys;
+      if (IsJacobiSolver(ph.solver) || (IsBlockSolver(ph.solver) ? 1 : 0) != kind) continue;
+      solves.push_back(s);
+      maxst = std::max(maxst, (int)c.L.solve_nsteps[s]);
+    }
+    for (int back = 0; back < 2; ++back) {
+      std::vector<int4> tiles;
+      std::vector<int32_t> deps;
+      std::vector<int32_t> seen;
+      for (int k = 0; k < maxst; ++k)
+        for (int s : solves) {
+          const int ns = c.L.solve_nsteps[s];
+          if (k >= ns) continue;
+          const int p = back ? ns - 1 - k : k;
+          const int base = c.L.solve_step0[s];
+          const int a = c.L.cl_step_off[base + p], b = c.L.cl_step_off[base + p + 1];
+          for (int t0 = a; t0 < b; t0 += size) {
+            const int t1 = std::min(b, t0 + size);
+            const int id = (int)tiles.size();
+            const int dep0 = (int)deps.size();
+            seen.clear();
+            for (int i = t0; i < t1; ++i) {
+              const int64_t q = c.L.cl_items[i].x;
+              for (int d = 0; d < 3; ++d) {
+                const int32_t code = c.L.nbq[(int64_t)(3 * back + d) * nq + q];
+                if (code < 0) continue;
+                const int32_t dt = tile_of[code];
+                if (dt < 0) throw Error(ATH_ERR_ARG, "tile queue: neighbour outside the swept order");
+                if (std::find(seen.begin(), seen.end(), dt) == seen.end()) seen.push_back(dt);
+              }
+            }
+            std::sort(seen.begin(), seen.end());
+            deps.insert(deps.end(), seen.begin(), seen.end());
+            tiles.push_back(make_int4(t0, t1, dep0, (int)deps.size() - dep0));
+            for (int i = t0; i < t1; ++i) tile_of[c.L.cl_items[i].x] = id;
+          }
+        }
+      BatchCore::TqList &tl = out[kind * 2 + back];
+      tl.ntiles = (int)tiles.size();
+      tl.tiles = m.Upload(tiles);
+      tl.deps = m.Upload(deps);
+      tl.done = m.Alloc<int>((size_t)tl.ntiles + 1);
+      Check(cudaMemset(tl.done, 0, ((size_t)tl.ntiles + 1) * sizeof(int)), "memset");
+      for (const int4 &x : tiles)
+        for (int i = x.x; i < x.y; ++i) tile_of[c.L.cl_items[i].x] = -1;
+    }
+  }
+  c.tq[size] = out;
+}
+
 void CountLaunches(BatchCore &c) {
   int edge_phases = 0, vedge_phases = 0;
   for (size_t ph = 0; ph + 1 < c.L.edge_phase_off.size(); ++ph) {
@@ -1257,7 +1362,7 @@ void CountLaunches(BatchCore &c) {
   const int nf = (c.fkinds & 1) + ((c.fkinds >> 1) & 1);
   const int nvf = (c.vkinds & 1) + ((c.vkinds >> 1) & 1);
   const int conn = c.L.ghost_cell.empty() ? 0 : 1;
-  const int per_pass = c.sweep_mode == 1 ? 1 : c.nsteps;
+  const int per_pass = (c.sweep_mode == 1 || c.sweep_mode == 3) ? 1 : c.nsteps;
   c.launches_per_iter = edge_phases +
                         (c.L.any_viscous ? (c.L.vops.empty() ? 0 : 1) + vedge_phases + 1 + 3 * nvf
                                          : 0) +
@@ -1386,6 +1491,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_sweep = m.Upload(c.L.sweep_items);
   c.d_cl_items = m.Upload(c.L.cl_items);
   c.d_cl_step_off = m.Upload(c.L.cl_step_off);
+  if (c.skinds) {
+    for (int size : {32, 64, 128, 256}) BuildTileQueue(c, st, m, size);
+    c.d_tq_ticket = m.Alloc<int>(1);
+    c.d_tq_status = m.Alloc<int>(1);
+    Check(cudaMemset(c.d_tq_status, 0, sizeof(int)), "memset");
+  }
   c.d_solve_step0 = m.Upload(c.L.solve_step0);
   c.d_solve_nsteps = m.Upload(c.L.solve_nsteps);
   c.d_solve_cta0 = m.Upload(c.L.solve_cta0);
@@ -1444,6 +1555,14 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
+  // resident CTAs of the tile-queue sweep kernels (one wave of persistent
+  // CTAs; more would only wait for tickets)
+  if (c.skinds) {
+    int sms = 0;
+    Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attribute");
+    c.tq_ctas[0] = std::max(1, B->run->TqOccupancy(c.max_sweeps > 1, false)) * sms;
+    c.tq_ctas[1] = std::max(1, B->run->TqOccupancy(true, true)) * sms;
+  }
   // default sweep shape: the persistent sweep with a cluster wide enough for
   // the largest plane (at most 8 CTAs of 256 threads), when launchable
   if (c.skinds) {
@@ -1458,6 +1577,20 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
       }
   }
   CountLaunches(c);
+}
+
+// After a synchronised run: a tile-queue sweep wait that ran out (its
+// kernels returned without finishing the pass) is reported, and the status
+// word is cleared so the batch can run again.
+void CheckSweepStatus(BatchCore &c) {
+  if (!c.d_tq_status) return;
+  int st = 0;
+  Check(cudaMemcpy(&st, c.d_tq_status, sizeof(int), cudaMemcpyDeviceToHost), "status download");
+  if (st == 0) return;
+  Check(cudaMemset(c.d_tq_status, 0, sizeof(int)), "memset");
+  throw Error(ATH_ERR_TIMEOUT,
+              "a tile-queue sweep wait gave up after its poll limit; the iteration's update is "
+              "incomplete");
 }
 
 // Reads norms of iterations [it0, it0+n) from the ring into norms_h.
@@ -1585,6 +1718,7 @@ int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h) {
     Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
     c.stats.device_ms = ms;
     c.stats.kernel_launches = (int64_t)n * c.launches_per_iter;
+    ath::CheckSweepStatus(c);
   });
 }
 
@@ -1677,6 +1811,7 @@ int ath_batch_converge(ath_batch *batch, int max_iters, double drop, int check_e
     Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
     c.stats.device_ms = ms;
     c.stats.kernel_launches = (int64_t)done * c.launches_per_iter;
+    ath::CheckSweepStatus(c);
     if (info) SolveInfo(c, info);
   });
 }
@@ -1700,13 +1835,20 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     if (c.skinds)
       for (int cl : {1, 2, 4, 8})
         if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
-    const Shape keep{c.sweep_mode, c.sweep_mode == 1 ? c.cl_threads : c.sweep_threads,
+    // the persistent tile-queue sweep with tiles of 32..256 cells
+    if (c.skinds)
+      for (int ts : {32, 64, 128, 256}) cand.push_back({3, ts, 0});
+    const Shape keep{c.sweep_mode,
+                     c.sweep_mode == 1 ? c.cl_threads
+                                       : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads),
                      c.cl_size};
     auto apply = [&](const Shape &sh) {
       c.sweep_mode = sh.mode;
       if (sh.mode == 1) {
         c.cl_threads = sh.threads;
         c.cl_size = sh.cluster;
+      } else if (sh.mode == 3) {
+        c.tq_size = sh.threads;
       } else {
         c.sweep_threads = sh.threads;
       }
@@ -1722,6 +1864,7 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
       run.Iterate(reps);
       Check(cudaEventRecord(c.ev1, c.stream), "event");
       Check(cudaEventSynchronize(c.ev1), "sync");
+      ath::CheckSweepStatus(c);
       float ms = 0.f;
       Check(cudaEventElapsedTime(&ms, c.ev0, c.ev1), "elapsed");
       if (ms < best) {
@@ -1743,9 +1886,49 @@ int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluste
   if (!batch) return ATH_ERR_ARG;
   const auto &c = batch->core;
   if (mode) *mode = c.sweep_mode;
-  if (threads) *threads = c.sweep_mode == 1 ? c.cl_threads : c.sweep_threads;
+  if (threads)
+    *threads = c.sweep_mode == 1 ? c.cl_threads : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads);
   if (cluster) *cluster = c.sweep_mode == 1 ? c.cl_size : 0;
   return ATH_OK;
+}
+
+int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int cluster) {
+  return Guard([&] {
+    if (!batch) throw ath::Error(ATH_ERR_ARG, "null batch");
+    auto &c = batch->core;
+    if (mode == 0 || mode == 2) {
+      if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
+        throw ath::Error(ATH_ERR_ARG, "per-plane sweeps take CTAs of 32, 64, 128 or 256 threads");
+      if (mode == 2 && !(c.skinds & 1))
+        throw ath::Error(ATH_ERR_ARG, "lane groups serve scalar solves only");
+      c.sweep_threads = threads;
+    } else if (mode == 1) {
+      if (threads != 256 || cluster < 1 || cluster > 8 ||
+          batch->run->MaxClusters(c.skinds, 256, cluster) <= 0)
+        throw ath::Error(ATH_ERR_ARG, "persistent sweep: 256 threads and a launchable cluster");
+      c.cl_threads = threads;
+      c.cl_size = cluster;
+    } else if (mode == 3) {
+      if (!c.tq.count(threads))
+        throw ath::Error(ATH_ERR_ARG, "tile-queue sweep: tiles of 32, 64, 128 or 256 cells");
+      c.tq_size = threads;
+    } else {
+      throw ath::Error(ATH_ERR_ARG, "unknown sweep mode");
+    }
+    c.sweep_mode = mode;
+    ath::CountLaunches(c);
+    batch->run->ResetGraph();
+  });
+}
+
+int ath_batch_sweep_wait_test(ath_batch *batch, long long poll_limit, int wait_never) {
+  return Guard([&] {
+    if (!batch || poll_limit < 0) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    auto &c = batch->core;
+    c.tq_spin_limit = poll_limit;
+    c.tq_wait_never = wait_never ? 1 : 0;
+    batch->run->ResetGraph();
+  });
 }
 
 int ath_batch_fill_ghosts(ath_batch *batch) {
@@ -1779,6 +1962,7 @@ int ath_batch_relax(ath_batch *batch) {
     batch->run->Relax();
     Check(cudaStreamSynchronize(batch->core.stream), "sync");
     Check(cudaGetLastError(), "kernel launch");
+    ath::CheckSweepStatus(batch->core);
   });
 }
 

@@ -55,6 +55,22 @@ struct SolveDev {
 // Per-solve hyperplane lists of the persistent sweep: items (q index,
 // block) ordered by solve, then plane; step_off[solve_step0[s] + p] .. +1
 // bound plane p of solve s (solve_nsteps[s] planes)
+// One pass of the persistent tile-queue sweep (k_sweep_tq): tiles in ticket
+// order (x, y: range of items; z, w: range of deps), the tiles each waits on,
+// per-tile done flags (one more, never set, for the forced-timeout test
+// mode), the ticket counter and the batch's sweep status word.
+struct TileQueueDev {
+  const int2 *items;
+  const int4 *tiles;
+  const int32_t *deps;
+  int *done;
+  int *ticket;
+  int *status;
+  int ntiles;
+  int wait_never;
+  long long spin_limit;
+};
+
 struct SweepLists {
   const int2 *items;
   const int32_t *step_off, *solve_step0, *solve_nsteps;
@@ -306,6 +322,13 @@ struct Launch {
                       bool full, int kinds, int threads, int cluster, cudaStream_t s);
   // clusters of that shape the device can hold at once (0 = not launchable)
   static int MaxClusters(int kinds, int threads, int cluster);
+  // one pass of the LU-SGS solves of one kind (block: 5x5 block solves,
+  // else scalar) as one persistent launch of `ctas` CTAs of 256 threads
+  // over a tile work queue; the queue's done flags and ticket must be zero
+  static void SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, int sweep,
+                      bool full, bool block, int ctas, cudaStream_t s);
+  // CTAs of the tile-queue sweep kernel resident per SM
+  static int TqOccupancy(bool full, bool block);
   // off-diagonal Jacobians of the block solves' cells, once per iteration
   static void OffJac(const Pools<T> &P, const int2 *items, int n, cudaStream_t s);
   // jacobi = 0: x0 of the LU-SGS solves, 1: of the DP-LUR solves

@@ -454,7 +454,10 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 
 // Reconstruction and inviscid flux of face c (direction D) in arithmetic U:
 // f is the flux per unit area, L and R the reconstructed face states.
-template <typename U, int D, typename PT>
+// FAST (FP64 batches with the fast-face option): MUSCL and the Roe flux in
+// their fast forms (MusclFast, RoeFluxFast), equal to the reference to
+// roundoff instead of bit for bit.
+template <typename U, int D, typename PT, bool FAST = false>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
                                          int64_t s, U f[5], Prim<U> &L, Prim<U> &R,
                                          U ft[2] = nullptr) {
@@ -471,10 +474,15 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
     const Prim<U> wp1 = LoadW<U>(P.W, n, c + s);
     const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
     const U kappa = (U)sv.kappa;
-    // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
-    L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
-    // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
-    R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+    if constexpr (FAST) {
+      L = MusclFast(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
+      R = MusclFast(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+    } else {
+      // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
+      L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
+      // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
+      R = Muscl(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+    }
   } else {
     const Prim<U> wm3 = LoadW<U>(P.W, n, c - 3 * s);
     const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s);
@@ -524,6 +532,8 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
   U vlr[2];
   if (sv.flux == ATH_FLUX_AUSM)
     AusmFlux(L, R, g, nx, ny, nz, f, vlr);
+  else if constexpr (FAST && std::is_same<U, double>::value)
+    RoeFluxFast(L, R, g, nx, ny, nz, f);
   else
     RoeFlux(L, R, g, nx, ny, nz, f);
   if (ft) {
@@ -744,7 +754,7 @@ __device__ __forceinline__ void FaceFluxMixed(const Pools<PT> &P, const SolveDev
   if (ft) RoeTurbFlux(L, R, lt, rt, g, nx, ny, nz, ft);
 }
 
-template <typename T, int D, bool RANS>
+template <typename T, int D, bool RANS, bool FAST = false>
 __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
@@ -773,7 +783,7 @@ __global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
   } else {
     T f[5], ft[2];
     Prim<T> L, R;
-    FaceFlux<T, D>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
+    FaceFlux<T, D, T, FAST>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
     const T magT = (T)mag;
 #pragma unroll
     for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * magT;
@@ -1542,13 +1552,17 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
 // plane has too few cells to fill the SMs (the autotuner chooses).  A warp
 // holds 10 (5) groups; its last 2 lanes idle.  Every lane of the warp
 // reaches the shuffles.
+// One scalar-solve cell per group of lanes (3, or 6 with both triangles),
+// a lane per neighbour term, the group's first lane summing the terms by
+// warp shuffles in the reference's i, j, k order.  Every lane of the warp
+// calls it (the shuffles span the warp); c is the cell's position in
+// items, valid for c < n_items.
 template <typename T, bool FULL>
-__global__ void __launch_bounds__(256) k_sweepg(Pools<T> P, const int2 *items, int n_items,
-                                                int forward, int sweep) {
+__device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *items, int c,
+                                               int n_items, int forward, int sweep) {
   constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = (int)(threadIdx.x & 31);
-  const int c = (t >> 5) * CPW + lane / L, li = lane % L;
+  const int li = lane % L;
   bool valid = lane < CPW * L && c < n_items;
   const int2 it = valid ? items[c] : make_int2(0, 0);
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
@@ -1593,6 +1607,15 @@ __global__ void __launch_bounds__(256) k_sweepg(Pools<T> P, const int2 *items, i
   }
   if (!valid || li != 0) return;
   ScalarFinish<T, FULL>(P, sv, it.x, forward, both, acc, acct, other, othert);
+}
+
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(256) k_sweepg(Pools<T> P, const int2 *items, int n_items,
+                                                int forward, int sweep) {
+  constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = (int)(threadIdx.x & 31);
+  SweepGroupItem<T, FULL>(P, items, (t >> 5) * CPW + lane / L, n_items, forward, sweep);
 }
 
 // Loads of one row of a block sweep that depend on the cell alone: the
@@ -1796,6 +1819,94 @@ __global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
       for (int i = a + tid; i < b; i += nthr) SweepScalarQ<T, FULL>(P, sv, items[i].x, forward, sweep);
     }
     cluster.sync();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent LU-SGS sweep over a (solve, hyperplane) tile work queue.
+//
+// A tile is a run of one solve's cells on one hyperplane (at most the
+// queue's tile size).  Tiles are numbered in the pass's step order (plane
+// order, ascending forward, descending backward, solves in turn), and each
+// lists the tiles of the previous step that hold its cells' neighbours on
+// the swept side.  CTAs claim tiles from an atomic ticket; a tile waits
+// until the tiles it lists are done.  Every tile it waits on has a smaller
+// ticket, so it was claimed earlier by a CTA that is running, and the
+// smallest unfinished tile never waits: the queue cannot deadlock whatever
+// the number of resident CTAs.  Neighbour pairs are the only dependencies
+// between cells of a pass (both the read of an updated neighbour and the
+// read of a not-yet-updated one), so a tile that waits for the tiles
+// holding its swept-side neighbours runs in an order the per-plane launches
+// also allow, and the result is bit for bit theirs.  Waits are bounded:
+// after `spin_limit` polls the CTA records ATH_ERR_TIMEOUT in *status and
+// returns, and every CTA stops claiming tiles once *status is set.
+__device__ __forceinline__ int LoadAcquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void StoreRelease(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void FenceAcqRelGpu() {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+template <typename T, bool FULL, bool BLOCK>
+__global__ void __launch_bounds__(256) k_sweep_tq(Pools<T> P, TileQueueDev Q, int forward,
+                                                  int sweep) {
+  __shared__ int s_tile, s_ok;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_tile = LoadAcquire(Q.status) != 0 ? Q.ntiles : atomicAdd(Q.ticket, 1);
+      s_ok = 1;
+    }
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= Q.ntiles) return;
+    const int4 tl = Q.tiles[t];  // items [x, y), deps [z, z + w)
+    if (threadIdx.x == 0) {
+      for (int e = 0; e < tl.w && s_ok; ++e) {
+        const int *flag = Q.wait_never ? Q.done + Q.ntiles : Q.done + Q.deps[tl.z + e];
+        long long polls = 0;
+        while (LoadAcquire(flag) == 0) {
+          if (++polls > Q.spin_limit || LoadAcquire(Q.status) != 0) {
+            atomicCAS(Q.status, 0, ATH_ERR_TIMEOUT);
+            s_ok = 0;
+            break;
+          }
+          __nanosleep(40);
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    FenceAcqRelGpu();
+    if constexpr (BLOCK) {
+      // 8-lane groups, one cell each; every lane runs the same rounds.  A
+      // retired solve, or one past its sweep count, skips the work but
+      // still marks its tiles done
+      const SolveDev sv = P.solves[P.blocks[Q.items[tl.x].y].solve];
+      if (sv.active && !sv.jacobi && sweep < sv.sweeps) {
+        const int per = (int)blockDim.x >> 3;
+        for (int i0 = tl.x; i0 < tl.y; i0 += per) {
+          const int i = i0 + (int)(threadIdx.x >> 3);
+          SweepBlockRow<T>(P, sv, i < tl.y ? Q.items[i].x : 0, i < tl.y, i < tl.y,
+                           (int)(threadIdx.x & 7), forward, sweep, FULL);
+        }
+      }
+    } else {
+      constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
+      const int warp = (int)(threadIdx.x >> 5), nwarps = (int)(blockDim.x >> 5);
+      const int lane = (int)(threadIdx.x & 31);
+      for (int c0 = tl.x + warp * CPW; c0 < tl.y; c0 += nwarps * CPW)
+        SweepGroupItem<T, FULL>(P, Q.items, c0 + lane / L, tl.y, forward, sweep);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      FenceAcqRelGpu();
+      StoreRelease(Q.done + t, 1);
+    }
   }
 }
 
@@ -2399,153 +2510,6 @@ __device__ __forceinline__ void TurbFaceGrads(const Pools<PT> &P, const BlockDev
   }
 }
 
-// The same gradients in FP32 from the dual cell's k and omega minus the
-// upper cell's, differences formed in FP64 (the dual cell is closed, so the
-// offset does not change the gradient; the rounding is relative to the
-// differences rather than to k and omega).
-template <int D, typename PT>
-__device__ __forceinline__ void TurbFaceGradsMixed(const Pools<PT> &P, const BlockDev &b,
-                                                   int64_t c, float kg[3], float wg[3]) {
-  const int64_t n = P.ncell;
-  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
-  const int64_t cu = c, cl = c - st[D];
-  auto area = [&](int e, int64_t x, float a[3]) {
-    const double *fa = P.fa[e];
-    const float m = (float)fa[3 * n + x];
-    a[0] = (float)fa[x] * m;
-    a[1] = (float)fa[n + x] * m;
-    a[2] = (float)fa[2 * n + x] * m;
-  };
-  float lo[3][2], hi[3][2], alo[3][3], ahi[3][3];
-#pragma unroll
-  for (int e = 0; e < 3; ++e) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const double *T_ = P.Wt + q * n;
-      const double base = T_[cu];
-      const float ol = (float)(T_[cl] - base);
-      if (e == D) {
-        lo[e][q] = ol;
-        hi[e][q] = 0.f;
-      } else {
-        hi[e][q] = 0.25f * ((ol + (float)(T_[cu + st[e]] - base)) + (float)(T_[cl + st[e]] - base));
-        lo[e][q] = 0.25f * ((ol + (float)(T_[cu - st[e]] - base)) + (float)(T_[cl - st[e]] - base));
-      }
-    }
-    if (e == D) {
-      float A0[3], A1[3], A2[3];
-      area(D, cu, A0);
-      area(D, cu + st[D], A1);
-      area(D, cl, A2);
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        ahi[e][r] = 0.5f * (A0[r] + A1[r]);
-        alo[e][r] = 0.5f * (A0[r] + A2[r]);
-      }
-    } else {
-      float Au[3], Al[3], Aup[3], Alp[3];
-      area(e, cu, Au);
-      area(e, cl, Al);
-      area(e, cu + st[e], Aup);
-      area(e, cl + st[e], Alp);
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        ahi[e][r] = 0.5f * (Aup[r] + Alp[r]);
-        alo[e][r] = 0.5f * (Au[r] + Al[r]);
-      }
-    }
-  }
-  const float invVol = 1.f / (0.5f * ((float)P.vol[cl] + (float)P.vol[cu]));
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    kg[r] = (hi[0][0] * ahi[0][r] - lo[0][0] * alo[0][r] + hi[1][0] * ahi[1][r] -
-             lo[1][0] * alo[1][r] + hi[2][0] * ahi[2][r] - lo[2][0] * alo[2][r]) *
-            invVol;
-    wg[r] = (hi[0][1] * ahi[0][r] - lo[0][1] * alo[0][r] + hi[1][1] * ahi[1][r] -
-             lo[1][1] * alo[1][r] + hi[2][1] * ahi[2][r] - lo[2][1] * alo[2][r]) *
-            invVol;
-  }
-}
-
-// Viscous face of a RANS solve on the mixed path: the FP64 face's terms in
-// FP32 (gradients from FP64-formed offsets, eddy viscosity and blending,
-// stresses and the k and omega diffusion fluxes); the viscous flux enters
-// the FP64 residual sum as the inviscid one does.
-template <int D>
-__device__ __forceinline__ void RansViscFaceMixed(Pools<float> &P, const BlockDev &b,
-                                                  const SolveDev &sv, int64_t c) {
-  const Gas<float> g = GasOf<float>(sv);
-  const int64_t n = P.ncell;
-  float grad[3][3], tg[3], muf;
-  Prim<float> fs;
-  ViscFaceGatherMixed<D>(P, b, sv, c, grad, tg, fs, muf);
-  float kg[3], wg[3];
-  TurbFaceGradsMixed<D>(P, b, c, kg, wg);
-  const int64_t cu = c, cl = c - StrideOf(b, D);
-  const double *wd = P.width[D];
-  float cd, cw;
-  CentralCoeffs((float)wd[cl], (float)wd[cu], cd, cw);
-  float fst[2];
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-    fst[q] = CMax(cd * (float)P.Wt[q * n + cu] + cw * (float)P.Wt[q * n + cl], (float)kTurbMin);
-  float wdf = cd * (float)P.wd[cu] + cw * (float)P.wd[cl];
-  if (wdf < 0.f && wdf > -1.0e-10f) wdf = 0.f;
-  const float scale = (float)sv.visc_scale;
-  const float vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
-                       grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
-  float mutf, f1f, f2f;
-  SstEddyVisc<float>(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
-  const double *fa = P.fa[D];
-  const float nx = (float)fa[c], ny = (float)fa[n + c], nz = (float)fa[2 * n + c],
-              mag = (float)fa[3 * n + c];
-  const float mus = scale * muf, muts = scale * mutf;
-  float tau[3];
-  TauNormal(vg, nx, ny, nz, mus, muts, tau);
-  const float kf = SutherlandRatio(Temperature(fs, g), (float)sv.t_ref, (float)sv.k_c1,
-                                   (float)sv.k_s, (float)sv.k_ref) *
-                   scale;
-  const float kt = muts * g.Cp() / 0.9f;
-  float F[5];
-  F[0] = 0.f;
-  F[1] = tau[0];
-  F[2] = tau[1];
-  F[3] = tau[2];
-  F[4] = Dot(tau[0], tau[1], tau[2], fs.u, fs.v, fs.w) +
-         (kf + kt) * Dot(tg[0], tg[1], tg[2], nx, ny, nz);
-  const float Ft0 = (mus + Blended((float)kSstSigmaK1, (float)kSstSigmaK2, f1f) * muts) *
-                    Dot(kg[0], kg[1], kg[2], nx, ny, nz);
-  const float Ft1 = (mus + Blended((float)kSstSigmaW1, (float)kSstSigmaW2, f1f) * muts) *
-                    Dot(wg[0], wg[1], wg[2], nx, ny, nz);
-  float *out = P.vflux[D];
-#pragma unroll
-  for (int v = 0; v < 5; ++v) out[v * n + c] = F[v] * mag;
-  P.vfluxt[D][c] = Ft0 * mag;
-  P.vfluxt[D][n + c] = Ft1 * mag;
-  float *rs = P.rst[D];
-#pragma unroll
-  for (int e = 0; e < 9; ++e) rs[e * n + c] = vg[e];
-#pragma unroll
-  for (int e = 0; e < 3; ++e) {
-    rs[(9 + e) * n + c] = kg[e];
-    rs[(12 + e) * n + c] = wg[e];
-  }
-  rs[15 * n + c] = mutf;
-  rs[16 * n + c] = f1f;
-  rs[17 * n + c] = f2f;
-  if (sv.block) {
-    float *vs = P.vst[D];
-    vs[0 * n + c] = fs.rho;
-    vs[1 * n + c] = fs.u;
-    vs[2 * n + c] = fs.v;
-    vs[3 * n + c] = fs.w;
-    vs[4 * n + c] = fs.p;
-    vs[5 * n + c] = muf;
-#pragma unroll
-    for (int e = 0; e < 9; ++e) vs[(6 + e) * n + c] = vg[e];
-  }
-}
-
 // Viscous face of a RANS solve (CalcViscFluxI/J/K with SST, in FP64): eddy viscosity and blending from the central face
 // state (turbulence floors applied), the face gradients and the central
 // wall distance (clipped to 0 within WALL_DIST_NEG_TOL); flow flux with
@@ -2633,10 +2597,11 @@ __global__ void __launch_bounds__(kCta) k_vface(Pools<T> P, const int32_t *list,
   const SolveDev sv = P.solves[b.solve];
   if (!sv.viscous || !sv.active || (sv.rans != 0) != RANS) return;
   if constexpr (RANS) {
-    if constexpr (std::is_same<T, float>::value)
-      RansViscFaceMixed<D>(P, b, sv, c);
-    else
-      RansViscFace<T, D>(P, b, sv, c);
+    // in FP64 for both precisions: near walls the k and omega diffusion
+    // fluxes of a cell's two faces are large and nearly cancel, so FP32
+    // rounding of the flux itself moves the converged k and omega by ~1e-4
+    // (measured against FP64 on an SST bump channel)
+    RansViscFace<T, D>(P, b, sv, c);
     return;
   }
   const Gas<T> g = GasOf<T>(sv);
@@ -2844,7 +2809,11 @@ void Launch<T>::ViscFace(int d, const Pools<T> &P, const int32_t *list,
 template <typename T, int D>
 static void LaunchFace(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        int ncta, int rkinds, cudaStream_t s) {
-  if (rkinds & 1) k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  // rkinds bit 2: the fast-face option of FP64 batches (non-RANS solves)
+  if ((rkinds & 1) && (rkinds & 4) && std::is_same<T, double>::value)
+    k_face<T, D, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  else if (rkinds & 1)
+    k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
   if (rkinds & 2) k_face<T, D, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
@@ -2907,6 +2876,34 @@ void Launch<T>::SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int
     else LaunchSweepCl<T, false, false>(P, L, forward, sweep, threads, cluster, s);
   }
   if (kinds & 2) LaunchSweepCl<T, true, true>(P, L, forward, sweep, threads, cluster, s);
+}
+template <typename T>
+void Launch<T>::SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, int sweep,
+                        bool full, bool block, int ctas, cudaStream_t s) {
+  if (Q.ntiles <= 0) return;
+  const unsigned grid = (unsigned)std::max(1, std::min(ctas, Q.ntiles));
+  if (block)
+    k_sweep_tq<T, true, true><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+  else if (full)
+    k_sweep_tq<T, true, false><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+  else
+    k_sweep_tq<T, false, false><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+}
+template <typename T>
+int Launch<T>::TqOccupancy(bool full, bool block) {
+  int n = 0;
+  cudaError_t e;
+  if (block)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, true>, 256, 0);
+  else if (full)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, false>, 256, 0);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, false, false>, 256, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
 }
 template <typename T>
 int Launch<T>::MaxClusters(int kinds, int threads, int cluster) {

@@ -137,7 +137,7 @@ def measured_peaks() -> dict:
 
 # ------------------------------------------------------------------- arms
 def run_native(args, rank: int, world: int, device: int):
-    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Context, Setup
+    from aither_gb300 import BATCH_FAST_FACES, PREC_FP64, PREC_MIXED, Batch, Context, Setup
     with tempfile.TemporaryDirectory() as tmp:
         inps, specs = make_workload(tmp, args.ncases)
         t0 = time.time()
@@ -149,7 +149,7 @@ def run_native(args, rank: int, world: int, device: int):
     for prec_name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
         if args.precision not in ("both", prec_name):
             continue
-        batch = Batch(ctx, setup, prec)
+        batch = Batch(ctx, setup, prec, BATCH_FAST_FACES if args.fast_faces else 0)
         for _ in range(args.warmup):
             batch.iterate(1)
         sweep_threads = batch.autotune(3)  # restores the state it ran on
@@ -548,6 +548,9 @@ def main():
     ap.add_argument("--ncases", type=int, default=64)
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fast-faces", type=int, default=0,
+                    help="1: FP64 batches use the fast MUSCL/Roe faces (roundoff-equal to "
+                         "the reference instead of bit for bit)")
     ap.add_argument("--converge-drop", type=float, default=1e-6,
                     help="residual drop of the time-to-convergence runs (0: skip them)")
     ap.add_argument("--converge-max", type=int, default=8000)

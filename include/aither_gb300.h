@@ -255,7 +255,12 @@ const char *ath_last_error(void);
 
 /* Copy a setup to the device.  precision = ATH_PREC_*.  flags: bit 0 =
  * compute the logged matrix residual every iteration (the reference always
- * does, src/linearSolver.cpp:470). */
+ * does, src/linearSolver.cpp:470); bit 1 (ATH_BATCH_FAST_FACES) = FP64
+ * batches evaluate the MUSCL reconstruction and the Roe flux of solves
+ * without turbulence equations in a rearranged form with fewer divisions
+ * and square roots (FP64 throughout; equal to the reference to roundoff,
+ * about 1e-15 per face, instead of bit for bit). */
+enum { ATH_BATCH_MATRIX_RESID = 1, ATH_BATCH_FAST_FACES = 2 };
 int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision,
                      int flags, ath_batch **out);
 int ath_batch_destroy(ath_batch *batch);
@@ -295,18 +300,36 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
 
 /* Autotuner of the LU-SGS sweep shape: times `reps` graph-captured
  * iterations for each candidate and keeps the fastest -- one launch per
- * hyperplane with CTAs of 32, 64, 128 or 256 threads, or the persistent
- * sweep (one launch per pass; a thread-block cluster of 1, 2, 4 or 8 CTAs
- * of 256 threads per solve walks the solve's hyperplanes with cluster
- * barriers).  The solution, per-solve counters and CFL are restored
- * afterwards, so tuning does not advance the solves.  The chosen CTA size
+ * hyperplane with CTAs of 32, 64, 128 or 256 threads, the persistent
+ * cluster sweep (one launch per pass; a thread-block cluster of 1, 2, 4 or
+ * 8 CTAs of 256 threads per solve walks the solve's hyperplanes with
+ * cluster barriers), or the persistent tile-queue sweep (one launch per
+ * pass over all solves: CTAs claim (solve, hyperplane) tiles of 32, 64, 128
+ * or 256 cells from an atomic ticket in step order, each tile waiting for
+ * the tiles of the previous step that hold its cells' swept-side
+ * neighbours).  Every shape gives bit-identical results.  The solution,
+ * per-solve counters and CFL are restored afterwards, so tuning does not
+ * advance the solves.  The chosen CTA size (tile size for the tile queue)
  * is written to *sweep_threads (may be NULL).  A new batch starts with the
- * persistent sweep sized to its largest hyperplane. */
+ * persistent cluster sweep sized to its largest hyperplane. */
 int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
-/* Current sweep shape: mode 1 persistent (cluster = CTAs per solve), 0 one
- * launch per hyperplane (cluster = 0), 2 one launch per hyperplane with a
- * group of lanes per scalar-solve cell, one per neighbour term. */
+/* Current sweep shape: mode 1 persistent cluster sweep (cluster = CTAs per
+ * solve), 0 one launch per hyperplane (cluster = 0), 2 one launch per
+ * hyperplane with a group of lanes per scalar-solve cell, one per neighbour
+ * term, 3 persistent tile-queue sweep (threads = cells per tile). */
 int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster);
+/* Sets the sweep shape (as ath_batch_sweep_shape reports it); the next
+ * iteration recaptures the batch's graph. */
+int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int cluster);
+/* The tile-queue sweep's waits are bounded: a wait for another tile polls
+ * at most poll_limit times (default 2^24, about a second), then the sweep
+ * records ATH_ERR_TIMEOUT, every CTA stops taking tiles, and the run that
+ * launched it (ath_batch_iterate, _converge, _relax, _autotune) returns
+ * ATH_ERR_TIMEOUT with that iteration's update incomplete; the context and
+ * the batch stay usable.  wait_never = 1 makes every wait poll a flag that
+ * nothing sets (for tests of the bounded wait).  No counterpart in the
+ * reference (its sweeps are sequential loops). */
+int ath_batch_sweep_wait_test(ath_batch *batch, long long poll_limit, int wait_never);
 
 /* ---- serving ------------------------------------------------------------
  * A request loop over independent solves (continuous batching).  Every

@@ -259,3 +259,50 @@ def test_memory_budget_is_enforced(tmp_path):
         Batch(c, Setup(inp))
     assert e.value.code == -5
     c.close()
+
+
+FAST_CASES = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30", "bump_sup_it1",
+              "bump_sup_it40", "bump_vanalbada_ausm_it20", "plate_adiabatic_it1",
+              "plate_adiabatic_it20", "plate_blusgs_it1", "plate_blusgs_it20",
+              "bump_sweeps3_it20", "vortex_bdf2_it4"]
+
+
+@pytest.mark.parametrize("name", FAST_CASES)
+def test_fp64_fast_faces_match_reference_fixture(ctx, name, tmp_path):
+    """The fast FP64 faces (MUSCL and Roe rearranged to fewer divisions and
+    square roots, ATH_BATCH_FAST_FACES) against the reference: 1e-12 per
+    cell after one iteration, 1e-10 for residual and update after many and
+    for the L2 history (the same tolerances as the bit-exact path, which
+    they meet with roundoff-level differences)."""
+    from aither_gb300 import BATCH_FAST_FACES, Batch, Setup
+    inp, st, g = golden_case(name, str(tmp_path))
+    s = Setup(inp)
+    if st is not None:
+        s.set_state(0, st[0])
+    b = Batch(ctx, s, 0, BATCH_FAST_FACES)
+    n = total_iterations(g)
+    norms = b.iterate(n)
+    diff_tol = CELL_TOL if n == 1 else NORM_TOL
+    for k in range(int(g["nblocks"])):
+        p = f"b{k}_"
+        assert rel_err(b.field(k, "STATE"), g[p + "state"]) <= CELL_TOL
+        assert rel_err(b.field(k, "RESID"), g[p + "resid"]) <= diff_tol
+        assert rel_err(b.field(k, "DT")[..., 0], g[p + "dt"]) <= CELL_TOL
+        assert rel_err(b.field(k, "DU"), g[p + "du"]) <= diff_tol
+    assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    b.close()
+
+
+def test_fp64_fast_faces_full_vortex_box_200_iterations(ctx, tmp_path):
+    """The 64x32x8 vortex box (200 LU-SGS iterations at CFL 10) with the
+    fast faces: L2 history within 1e-10 of the reference's."""
+    from aither_gb300 import BATCH_FAST_FACES, Batch, Setup
+    inp, st, g = golden_case("vortex_c1_it200", str(tmp_path))
+    s = Setup(inp)
+    s.set_state(0, st[0])
+    b = Batch(ctx, s, 0, BATCH_FAST_FACES)
+    norms = b.iterate(200)
+    assert rel_err(_l2(norms), g["l2"]) <= NORM_TOL
+    w = b.field(0, "STATE")
+    assert rel_err(w.reshape(-1, 5).sum(axis=0), g["b0_state_sum"]) <= 1e-12
+    b.close()
