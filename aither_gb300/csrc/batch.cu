@@ -25,16 +25,22 @@ struct ath_ctx {
   int device = 0;
   size_t budget = 0;  // 0 = whatever the device has
   size_t used = 0;
+  // stream-ordered pool of the context's batches: allocations and frees are
+  // ordered on the owning batch's stream and the pool keeps freed memory for
+  // reuse, so creating and destroying batches (serving admission and
+  // retirement) never synchronises the device
+  cudaMemPool_t pool = nullptr;
 };
 
 namespace ath {
 
 namespace {
 
-// Device allocation accounted against the context's HBM budget.
+// Device allocation accounted against the context's HBM budget, stream
+// ordered on the owning batch's stream from the context's pool.
 class DevMem {
  public:
-  explicit DevMem(ath_ctx *ctx) : ctx_(ctx) {}
+  DevMem(ath_ctx *ctx, cudaStream_t stream) : ctx_(ctx), stream_(stream) {}
   ~DevMem() { Release(); }
   template <typename T>
   T *Alloc(size_t count) {
@@ -42,7 +48,7 @@ class DevMem {
     if (ctx_->budget && ctx_->used + bytes > ctx_->budget)
       throw Error(ATH_ERR_NOMEM, "device memory budget exceeded");
     void *p = nullptr;
-    Check(cudaMalloc(&p, bytes), "cudaMalloc");
+    Check(cudaMallocFromPoolAsync(&p, bytes, ctx_->pool, stream_), "cudaMallocFromPoolAsync");
     ctx_->used += bytes;
     ptrs_.push_back({p, bytes});
     return static_cast<T *>(p);
@@ -50,15 +56,20 @@ class DevMem {
   template <typename T>
   T *Upload(const std::vector<T> &v) {
     T *p = Alloc<T>(v.size());
-    if (!v.empty())
-      Check(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice),
+    if (!v.empty()) {
+      Check(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream_),
             "upload");
+      Check(cudaStreamSynchronize(stream_), "upload");  // the host vector may go
+    }
     return p;
+  }
+  void Zero(void *p, int value, size_t bytes) {
+    Check(cudaMemsetAsync(p, value, bytes, stream_), "memset");
   }
   void Free(void *p) {
     for (size_t i = 0; i < ptrs_.size(); ++i)
       if (ptrs_[i].first == p) {
-        cudaFree(p);
+        cudaFreeAsync(p, stream_);
         ctx_->used -= ptrs_[i].second;
         ptrs_.erase(ptrs_.begin() + (long)i);
         return;
@@ -66,7 +77,7 @@ class DevMem {
   }
   void Release() {
     for (auto &e : ptrs_) {
-      cudaFree(e.first);
+      cudaFreeAsync(e.first, stream_);
       ctx_->used -= e.second;
     }
     ptrs_.clear();
@@ -74,6 +85,7 @@ class DevMem {
 
  private:
   ath_ctx *ctx_;
+  cudaStream_t stream_;
   std::vector<std::pair<void *, size_t>> ptrs_;
 };
 
@@ -148,8 +160,9 @@ struct BatchCore {
     int *done = nullptr;
     int ntiles = 0;
   };
-  int tq_size = 128;
-  std::map<int, std::array<TqList, 4>> tq;  // tile size -> [kind * 2 + backward]
+  int tq_size = 32;
+  std::map<int, std::array<TqList, 4>> tq;  // tile size -> [kind * 2 + backward], built
+                                            // on first use (outside graph capture)
   int tq_ctas[2] = {0, 0};                  // resident CTAs, scalar and block kernels
   int *d_tq_ticket = nullptr, *d_tq_status = nullptr;
   long long tq_spin_limit = 1LL << 24;      // polls of one wait (~1 s)
@@ -358,19 +371,19 @@ class Runner : public RunnerBase {
     if (c.L.any_viscous) {
       for (int d = 0; d < 3; ++d) {
         P_.vflux[d] = m.Alloc<T>(5 * n);
-        Check(cudaMemset(P_.vflux[d], 0, 5 * n * sizeof(T)), "memset");
+        c_.mem->Zero(P_.vflux[d], 0, 5 * n * sizeof(T));
       }
       P_.mu = m.Alloc<double>(n);
-      Check(cudaMemset(P_.mu, 0, n * sizeof(double)), "memset");
+      c_.mem->Zero(P_.mu, 0, n * sizeof(double));
       P_.Taux = m.Alloc<double>(n);
-      Check(cudaMemset(P_.Taux, 0, n * sizeof(double)), "memset");
+      c_.mem->Zero(P_.Taux, 0, n * sizeof(double));
     }
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
-    Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
-    Check(cudaMemset(P_.R, 0, 5 * n * sizeof(double)), "memset");
-    Check(cudaMemset(P_.lam, 0, n * sizeof(double)), "memset");
-    Check(cudaMemset(P_.dt, 0, n * sizeof(double)), "memset");
+    c_.mem->Zero(P_.dt, 0, n * sizeof(double));
+    c_.mem->Zero(P_.R, 0, 5 * n * sizeof(double));
+    c_.mem->Zero(P_.lam, 0, n * sizeof(double));
+    c_.mem->Zero(P_.dt, 0, n * sizeof(double));
     // hyperplane-ordered sweep working set
     const int64_t nq = c.nq, ngh = (int64_t)c.L.ghost_cell.size();
     P_.nq = nq;
@@ -382,37 +395,37 @@ class Runner : public RunnerBase {
     P_.Aq = m.Alloc<T>(aw * nq);
     P_.dUq = m.Alloc<T>(5 * nq);
     P_.dUg = m.Alloc<T>(5 * std::max<int64_t>(ngh, 1));
-    Check(cudaMemset(P_.Wq, 0, 5 * nq * sizeof(T)), "memset");
-    Check(cudaMemset(P_.Rq, 0, 5 * nq * sizeof(T)), "memset");
-    Check(cudaMemset(P_.Ainvq, 0, aw * nq * sizeof(T)), "memset");
-    Check(cudaMemset(P_.Aq, 0, aw * nq * sizeof(T)), "memset");
+    c_.mem->Zero(P_.Wq, 0, 5 * nq * sizeof(T));
+    c_.mem->Zero(P_.Rq, 0, 5 * nq * sizeof(T));
+    c_.mem->Zero(P_.Ainvq, 0, aw * nq * sizeof(T));
+    c_.mem->Zero(P_.Aq, 0, aw * nq * sizeof(T));
     if (c.kinds & 2) {
       for (int d = 0; d < 3; ++d) {
         P_.fst[d] = m.Alloc<T>(10 * n);
-        Check(cudaMemset(P_.fst[d], 0, 10 * n * sizeof(T)), "memset");
+        c_.mem->Zero(P_.fst[d], 0, 10 * n * sizeof(T));
         if (c.block_viscous) {
           P_.vst[d] = m.Alloc<T>(15 * n);
-          Check(cudaMemset(P_.vst[d], 0, 15 * n * sizeof(T)), "memset");
+          c_.mem->Zero(P_.vst[d], 0, 15 * n * sizeof(T));
         }
       }
       P_.Joff = m.Alloc<T>(150 * nq);
-      Check(cudaMemset(P_.Joff, 0, 150 * nq * sizeof(T)), "memset");
+      c_.mem->Zero(P_.Joff, 0, 150 * nq * sizeof(T));
       if (c.any_rans) {
         P_.Jtoff = m.Alloc<T>(24 * nq);
-        Check(cudaMemset(P_.Jtoff, 0, 24 * nq * sizeof(T)), "memset");
+        c_.mem->Zero(P_.Jtoff, 0, 24 * nq * sizeof(T));
       }
     }
     if (c.block_viscous || c.any_rans) {
       // cell-averaged velocity gradients (block diagonal, SST sources, output)
       P_.vgq = m.Alloc<T>(9 * nq);
-      Check(cudaMemset(P_.vgq, 0, 9 * nq * sizeof(T)), "memset");
+      c_.mem->Zero(P_.vgq, 0, 9 * nq * sizeof(T));
     }
-    Check(cudaMemset(P_.dUq, 0, 5 * nq * sizeof(T)), "memset");
+    c_.mem->Zero(P_.dUq, 0, 5 * nq * sizeof(T));
     if (c.jkinds) {
       P_.dUq2 = m.Alloc<T>(5 * nq);
-      Check(cudaMemset(P_.dUq2, 0, 5 * nq * sizeof(T)), "memset");
+      c_.mem->Zero(P_.dUq2, 0, 5 * nq * sizeof(T));
     }
-    Check(cudaMemset(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T)), "memset");
+    c_.mem->Zero(P_.dUg, 0, 5 * std::max<int64_t>(ngh, 1) * sizeof(T));
     {
       std::vector<T> lo(c.L.face_lo.begin(), c.L.face_lo.end());
       std::vector<T> hi(c.L.face_hi.begin(), c.L.face_hi.end());
@@ -432,21 +445,21 @@ class Runner : public RunnerBase {
     P_.qpos = m.Upload(c.L.qpos);
     P_.ghost_cell = m.Upload(c.L.ghost_cell);
     P_.ghost_src = m.Upload(c.L.ghost_src);
-    for (int d = 0; d < 3; ++d) Check(cudaMemset(P_.flux[d], 0, 5 * n * sizeof(double)), "memset");
+    for (int d = 0; d < 3; ++d) c_.mem->Zero(P_.flux[d], 0, 5 * n * sizeof(double));
     if (c.any_rans) AllocTurbulence(m, n, nq, ngh);
     if (c.n_nr_surf > 0) {
       P_.nr_mach = m.Alloc<double>(2 * (size_t)c.n_nr_surf);
-      Check(cudaMemset(P_.nr_mach, 0, 2 * (size_t)c.n_nr_surf * sizeof(double)), "memset");
+      c_.mem->Zero(P_.nr_mach, 0, 2 * (size_t)c.n_nr_surf * sizeof(double));
     }
     if (c.any_unsteady) {
       P_.Un = m.Alloc<double>(7 * n);
       P_.Unm1 = m.Alloc<double>(7 * n);
-      Check(cudaMemset(P_.Un, 0, 7 * n * sizeof(double)), "memset");
-      Check(cudaMemset(P_.Unm1, 0, 7 * n * sizeof(double)), "memset");
+      c_.mem->Zero(P_.Un, 0, 7 * n * sizeof(double));
+      c_.mem->Zero(P_.Unm1, 0, 7 * n * sizeof(double));
       P_.Bq = m.Alloc<T>(5 * nq);
       P_.Btq = m.Alloc<T>(2 * nq);
-      Check(cudaMemset(P_.Bq, 0, 5 * nq * sizeof(T)), "memset");
-      Check(cudaMemset(P_.Btq, 0, 2 * nq * sizeof(T)), "memset");
+      c_.mem->Zero(P_.Bq, 0, 5 * nq * sizeof(T));
+      c_.mem->Zero(P_.Btq, 0, 2 * nq * sizeof(T));
     }
     // geometry and state
     std::vector<double> W(5 * n, 0.0), vol(n, 0.0), wid[3], fa[3];
@@ -477,7 +490,9 @@ class Runner : public RunnerBase {
         }
       }
     }
-    Check(cudaMemcpy(P_.W, W.data(), W.size() * 8, cudaMemcpyHostToDevice), "upload");
+    Check(cudaMemcpyAsync(P_.W, W.data(), W.size() * 8, cudaMemcpyHostToDevice, c_.stream),
+          "upload");
+    Check(cudaStreamSynchronize(c_.stream), "upload");
     if (c.any_rans) {
       // k, omega of the initial state (0 outside RANS solves)
       std::vector<double> Wt(2 * n, 0.0);
@@ -490,7 +505,9 @@ class Runner : public RunnerBase {
           Wt[n + o + x] = b.state0[x * b.nv + 6];
         }
       }
-      Check(cudaMemcpy(P_.Wt, Wt.data(), Wt.size() * 8, cudaMemcpyHostToDevice), "upload");
+      Check(cudaMemcpyAsync(P_.Wt, Wt.data(), Wt.size() * 8, cudaMemcpyHostToDevice, c_.stream),
+            "upload");
+      Check(cudaStreamSynchronize(c_.stream), "upload");
     }
     if (c.L.any_viscous) {
       // wall distance (SST sources and wall omega, heat-flux walls)
@@ -526,7 +543,7 @@ class Runner : public RunnerBase {
   // per-face SST data (gradients, eddy viscosity, blending)
   void AllocTurbulence(DevMem &m, int64_t n, int64_t nq, int64_t ngh) {
     auto zero = [&](auto *p, size_t count) {
-      Check(cudaMemset(p, 0, count * sizeof(*p)), "memset");
+      c_.mem->Zero(p, 0, count * sizeof(*p));
       return p;
     };
     P_.Wt = zero(m.Alloc<double>(2 * n), 2 * n);
@@ -1342,12 +1359,26 @@ void BuildTileQueue(BatchCore &c, const Setup &st, DevMem &m, int size) {
       tl.tiles = m.Upload(tiles);
       tl.deps = m.Upload(deps);
       tl.done = m.Alloc<int>((size_t)tl.ntiles + 1);
-      Check(cudaMemset(tl.done, 0, ((size_t)tl.ntiles + 1) * sizeof(int)), "memset");
+      m.Zero(tl.done, 0, ((size_t)tl.ntiles + 1) * sizeof(int));
       for (const int4 &x : tiles)
         for (int i = x.x; i < x.y; ++i) tile_of[c.L.cl_items[i].x] = -1;
     }
   }
   c.tq[size] = out;
+}
+
+void EnsureTileQueue(BatchCore &c, int size) {
+  if (!c.tq.count(size)) BuildTileQueue(c, *c.setup, *c.mem, size);
+}
+
+// Candidate tile sizes of the tile-queue sweep: whole rounds of a warp
+// worker (10 cells of scalar solves, 5 with both triangles, 4 of block
+// solves), one to eight rounds per tile.
+std::vector<int> TileSizes(const BatchCore &c) {
+  if (c.skinds == 1) return c.max_sweeps > 1 ? std::vector<int>{5, 10, 20, 40}
+                                              : std::vector<int>{10, 20, 40, 80};
+  if (c.skinds == 2) return {4, 8, 16, 32};
+  return {8, 16, 32, 64};
 }
 
 void CountLaunches(BatchCore &c) {
@@ -1409,7 +1440,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   }
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");
   BuildLists(c);
-  c.mem.reset(new DevMem(ctx));
+  Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  c.mem.reset(new DevMem(ctx, c.stream));
   DevMem &m = *c.mem;
   std::vector<BlockDev> bd(c.nblocks);
   for (int b = 0; b < c.nblocks; ++b) {
@@ -1477,10 +1509,10 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_states = m.Upload(states);
   c.d_cfl = m.Alloc<double>(c.nsolves);
   c.d_iter = m.Alloc<int64_t>(1);
-  Check(cudaMemset(c.d_iter, 0, sizeof(int64_t)), "memset");
+  c.mem->Zero(c.d_iter, 0, sizeof(int64_t));
   c.d_now = m.Alloc<uint64_t>(1);
   c.d_sstate = m.Alloc<SolveState>(c.nsolves);
-  Check(cudaMemset(c.d_sstate, 0, c.nsolves * sizeof(SolveState)), "memset");
+  c.mem->Zero(c.d_sstate, 0, c.nsolves * sizeof(SolveState));
   c.d_cells = m.Upload(c.L.cells);
   c.d_cell_cta_block = m.Upload(c.L.cell_cta_block);
   c.d_cell_cta_pos0 = m.Upload(c.L.cell_cta_pos0);
@@ -1492,10 +1524,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_cl_items = m.Upload(c.L.cl_items);
   c.d_cl_step_off = m.Upload(c.L.cl_step_off);
   if (c.skinds) {
-    for (int size : {32, 64, 128, 256}) BuildTileQueue(c, st, m, size);
     c.d_tq_ticket = m.Alloc<int>(1);
     c.d_tq_status = m.Alloc<int>(1);
-    Check(cudaMemset(c.d_tq_status, 0, sizeof(int)), "memset");
+    c.mem->Zero(c.d_tq_status, 0, sizeof(int));
   }
   c.d_solve_step0 = m.Upload(c.L.solve_step0);
   c.d_solve_nsteps = m.Upload(c.L.solve_nsteps);
@@ -1523,9 +1554,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   c.d_solve_face0 = m.Upload(c.L.solve_face0);
   c.d_wbuf = m.Alloc<double>(6 * std::max<size_t>(c.L.wall_faces.size(), 1));
   c.d_fring = m.Alloc<double>((size_t)c.ring_cap * c.nsolves * 6);
-  Check(cudaMemset(c.d_fring, 0, (size_t)c.ring_cap * c.nsolves * 6 * sizeof(double)),
-        "memset");
-  Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  c.mem->Zero(c.d_fring, 0, (size_t)c.ring_cap * c.nsolves * 6 * sizeof(double));
   Check(cudaEventCreate(&c.ev0), "event");
   Check(cudaEventCreate(&c.ev1), "event");
   if (precision == ATH_PREC_FP64) {
@@ -1577,6 +1606,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
       }
   }
   CountLaunches(c);
+  // every stream-ordered allocation and fill of the batch is complete before
+  // host calls touch its memory from other streams
+  Check(cudaStreamSynchronize(c.stream), "sync");
 }
 
 // After a synchronised run: a tile-queue sweep wait that ran out (its
@@ -1585,9 +1617,11 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
 void CheckSweepStatus(BatchCore &c) {
   if (!c.d_tq_status) return;
   int st = 0;
-  Check(cudaMemcpy(&st, c.d_tq_status, sizeof(int), cudaMemcpyDeviceToHost), "status download");
+  Check(cudaMemcpyAsync(&st, c.d_tq_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream),
+        "status download");
+  Check(cudaStreamSynchronize(c.stream), "sync");
   if (st == 0) return;
-  Check(cudaMemset(c.d_tq_status, 0, sizeof(int)), "memset");
+  c.mem->Zero(c.d_tq_status, 0, sizeof(int));
   throw Error(ATH_ERR_TIMEOUT,
               "a tile-queue sweep wait gave up after its poll limit; the iteration's update is "
               "incomplete");
@@ -1659,11 +1693,27 @@ int ath_ctx_create(int device, size_t hbm_budget_bytes, ath_ctx **out) {
     auto *c = new ath_ctx();
     c->device = device;
     c->budget = hbm_budget_bytes;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&c->pool, &props) != cudaSuccess) {
+      delete c;
+      throw ath::Error(ATH_ERR_CUDA, "cudaMemPoolCreate failed");
+    }
+    uint64_t keep = UINT64_MAX;  // freed memory stays in the pool for reuse
+    cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     *out = c;
   });
 }
 
 int ath_ctx_destroy(ath_ctx *ctx) {
+  if (!ctx) return ATH_OK;
+  if (ctx->pool) {
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();  // every batch's frees have been ordered before
+    cudaMemPoolDestroy(ctx->pool);
+  }
   delete ctx;
   return ATH_OK;
 }
@@ -1835,9 +1885,9 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     if (c.skinds)
       for (int cl : {1, 2, 4, 8})
         if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
-    // the persistent tile-queue sweep with tiles of 32..256 cells
+    // the persistent tile-queue sweep with tiles of one to eight warp rounds
     if (c.skinds)
-      for (int ts : {32, 64, 128, 256}) cand.push_back({3, ts, 0});
+      for (int ts : ath::TileSizes(c)) cand.push_back({3, ts, 0});
     const Shape keep{c.sweep_mode,
                      c.sweep_mode == 1 ? c.cl_threads
                                        : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads),
@@ -1848,6 +1898,7 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
         c.cl_threads = sh.threads;
         c.cl_size = sh.cluster;
       } else if (sh.mode == 3) {
+        ath::EnsureTileQueue(c, sh.threads);
         c.tq_size = sh.threads;
       } else {
         c.sweep_threads = sh.threads;
@@ -1909,8 +1960,9 @@ int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int clust
       c.cl_threads = threads;
       c.cl_size = cluster;
     } else if (mode == 3) {
-      if (!c.tq.count(threads))
-        throw ath::Error(ATH_ERR_ARG, "tile-queue sweep: tiles of 32, 64, 128 or 256 cells");
+      if (!c.skinds || threads < 1 || threads > 4096)
+        throw ath::Error(ATH_ERR_ARG, "tile-queue sweep: LU-SGS solves and tiles of 1..4096 cells");
+      ath::EnsureTileQueue(c, threads);
       c.tq_size = threads;
     } else {
       throw ath::Error(ATH_ERR_ARG, "unknown sweep mode");
@@ -2301,7 +2353,8 @@ struct ath_server {
     int state = 0;  // 0 queued, 1 active, 2 done
     double t_submit = 0, t_admit = 0, t_done = 0;
     int64_t launched = 0;
-    int32_t *flag_h = nullptr;  // page-locked copy of the solve's active flag
+    int32_t *flag_h = nullptr;  // its slot of the server's page-locked active flags
+    int slot = -1;
     cudaEvent_t ev = nullptr;
     ath_converge_info info{};
     std::vector<std::vector<double>> result;  // final state per block
@@ -2317,6 +2370,11 @@ struct ath_server {
   std::vector<Req *> active;
   std::map<int64_t, Req *> all;
   std::vector<int64_t> finished;  // done, not yet reported by poll
+  // page-locked copies of the admitted solves' active flags, one slot per
+  // active request, allocated once (admission and retirement reuse slots
+  // rather than allocate and free page-locked memory)
+  int32_t *flags_h = nullptr;
+  std::vector<int> free_slots;
 };
 
 namespace ath {
@@ -2351,7 +2409,8 @@ void Finish(ath_server *S, ath_server::Req *r) {
   S->reserved -= r->est;
   cudaEventDestroy(r->ev);
   r->ev = nullptr;
-  cudaFreeHost(r->flag_h);
+  S->free_slots.push_back(r->slot);
+  r->slot = -1;
   r->flag_h = nullptr;
   ath_setup_destroy(r->setup);
   r->setup = nullptr;
@@ -2361,7 +2420,7 @@ void Finish(ath_server *S, ath_server::Req *r) {
 }
 
 bool Admit(ath_server *S, ath_server::Req *r) {
-  if (S->reserved + r->est > S->capacity) return false;
+  if (S->reserved + r->est > S->capacity || S->free_slots.empty()) return false;
   ath_batch *b = nullptr;
   const int rc = ath_batch_create(S->ctx, r->setup, S->precision, 0, &b);
   if (rc == ATH_ERR_NOMEM) return false;
@@ -2370,7 +2429,9 @@ bool Admit(ath_server *S, ath_server::Req *r) {
   S->reserved += r->est;
   const int rt = ath_batch_set_target(b, 0, S->drop, 1);
   if (rt != ATH_OK) throw Error(rt, "target");
-  Check(cudaMallocHost(&r->flag_h, sizeof(int32_t)), "cudaMallocHost");
+  r->slot = S->free_slots.back();
+  S->free_slots.pop_back();
+  r->flag_h = S->flags_h + r->slot;
   *r->flag_h = 1;
   Check(cudaEventCreateWithFlags(&r->ev, cudaEventDisableTiming), "event");
   r->state = 1;
@@ -2408,6 +2469,13 @@ int ath_server_create(ath_ctx *ctx, int precision, double drop, int64_t max_iter
       const size_t reserve = (size_t)1 << 30;
       S->capacity = fr > reserve ? fr - reserve : 0;
     }
+    Check(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (cudaHostAlloc(&S->flags_h, sizeof(int32_t) * (size_t)max_active, cudaHostAllocDefault) !=
+        cudaSuccess) {
+      delete S;
+      throw ath::Error(ATH_ERR_CUDA, "cudaHostAlloc of the active flags failed");
+    }
+    for (int q = max_active - 1; q >= 0; --q) S->free_slots.push_back(q);
     *out = S;
   });
 }
@@ -2520,10 +2588,10 @@ int ath_server_destroy(ath_server *S) {
       ath_batch_destroy(r->batch);
     }
     if (r->ev) cudaEventDestroy(r->ev);
-    if (r->flag_h) cudaFreeHost(r->flag_h);
     if (r->setup) ath_setup_destroy(r->setup);
     delete r;
   }
+  if (S->flags_h) cudaFreeHost(S->flags_h);
   delete S;
   return ATH_OK;
 }

@@ -1831,15 +1831,15 @@ __global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
 // lists the tiles of the previous step that hold its cells' neighbours on
 // the swept side.  CTAs claim tiles from an atomic ticket; a tile waits
 // until the tiles it lists are done.  Every tile it waits on has a smaller
-// ticket, so it was claimed earlier by a CTA that is running, and the
-// smallest unfinished tile never waits: the queue cannot deadlock whatever
-// the number of resident CTAs.  Neighbour pairs are the only dependencies
+// ticket, so it was claimed earlier by a worker (a warp) that is running,
+// and the smallest unfinished tile never waits: the queue cannot deadlock
+// whatever the number of resident warps.  Neighbour pairs are the only dependencies
 // between cells of a pass (both the read of an updated neighbour and the
 // read of a not-yet-updated one), so a tile that waits for the tiles
 // holding its swept-side neighbours runs in an order the per-plane launches
 // also allow, and the result is bit for bit theirs.  Waits are bounded:
-// after `spin_limit` polls the CTA records ATH_ERR_TIMEOUT in *status and
-// returns, and every CTA stops claiming tiles once *status is set.
+// after `spin_limit` polls the warp records ATH_ERR_TIMEOUT in *status and
+// returns; a warp whose wait finds *status set returns at once.
 __device__ __forceinline__ int LoadAcquire(const int *p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -1855,55 +1855,51 @@ __device__ __forceinline__ void FenceAcqRelGpu() {
 template <typename T, bool FULL, bool BLOCK>
 __global__ void __launch_bounds__(256) k_sweep_tq(Pools<T> P, TileQueueDev Q, int forward,
                                                   int sweep) {
-  __shared__ int s_tile, s_ok;
+  // each warp is a worker: it claims a tile, its lane 0 waits for the tiles
+  // the tile lists, the warp sweeps the tile's cells, lane 0 marks it done
+  const int lane = (int)(threadIdx.x & 31);
   for (;;) {
-    if (threadIdx.x == 0) {
-      s_tile = LoadAcquire(Q.status) != 0 ? Q.ntiles : atomicAdd(Q.ticket, 1);
-      s_ok = 1;
-    }
-    __syncthreads();
-    const int t = s_tile;
+    int t = 0;
+    if (lane == 0) t = atomicAdd(Q.ticket, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= Q.ntiles) return;
     const int4 tl = Q.tiles[t];  // items [x, y), deps [z, z + w)
-    if (threadIdx.x == 0) {
-      for (int e = 0; e < tl.w && s_ok; ++e) {
+    int ok = 1;
+    if (lane == 0) {
+      for (int e = 0; e < tl.w && ok; ++e) {
         const int *flag = Q.wait_never ? Q.done + Q.ntiles : Q.done + Q.deps[tl.z + e];
         long long polls = 0;
         while (LoadAcquire(flag) == 0) {
           if (++polls > Q.spin_limit || LoadAcquire(Q.status) != 0) {
             atomicCAS(Q.status, 0, ATH_ERR_TIMEOUT);
-            s_ok = 0;
+            ok = 0;
             break;
           }
-          __nanosleep(40);
+          __nanosleep(20);
         }
       }
     }
-    __syncthreads();
-    if (!s_ok) return;
-    FenceAcqRelGpu();
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) return;
+    __syncwarp();
     if constexpr (BLOCK) {
-      // 8-lane groups, one cell each; every lane runs the same rounds.  A
-      // retired solve, or one past its sweep count, skips the work but
-      // still marks its tiles done
+      // 8-lane groups, one cell each (4 per round).  A retired solve, or one
+      // past its sweep count, skips the work but still marks its tiles done
       const SolveDev sv = P.solves[P.blocks[Q.items[tl.x].y].solve];
       if (sv.active && !sv.jacobi && sweep < sv.sweeps) {
-        const int per = (int)blockDim.x >> 3;
-        for (int i0 = tl.x; i0 < tl.y; i0 += per) {
-          const int i = i0 + (int)(threadIdx.x >> 3);
-          SweepBlockRow<T>(P, sv, i < tl.y ? Q.items[i].x : 0, i < tl.y, i < tl.y,
-                           (int)(threadIdx.x & 7), forward, sweep, FULL);
+        for (int i0 = tl.x; i0 < tl.y; i0 += 4) {
+          const int i = i0 + (lane >> 3);
+          SweepBlockRow<T>(P, sv, i < tl.y ? Q.items[i].x : 0, i < tl.y, i < tl.y, lane & 7,
+                           forward, sweep, FULL);
         }
       }
     } else {
       constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
-      const int warp = (int)(threadIdx.x >> 5), nwarps = (int)(blockDim.x >> 5);
-      const int lane = (int)(threadIdx.x & 31);
-      for (int c0 = tl.x + warp * CPW; c0 < tl.y; c0 += nwarps * CPW)
+      for (int c0 = tl.x; c0 < tl.y; c0 += CPW)
         SweepGroupItem<T, FULL>(P, Q.items, c0 + lane / L, tl.y, forward, sweep);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    __syncwarp();
+    if (lane == 0) {
       FenceAcqRelGpu();
       StoreRelease(Q.done + t, 1);
     }

@@ -304,9 +304,9 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
  * cluster sweep (one launch per pass; a thread-block cluster of 1, 2, 4 or
  * 8 CTAs of 256 threads per solve walks the solve's hyperplanes with
  * cluster barriers), or the persistent tile-queue sweep (one launch per
- * pass over all solves: CTAs claim (solve, hyperplane) tiles of 32, 64, 128
- * or 256 cells from an atomic ticket in step order, each tile waiting for
- * the tiles of the previous step that hold its cells' swept-side
+ * pass over all solves: each warp claims (solve, hyperplane) tiles of one
+ * to eight warp rounds from an atomic ticket in step order, a tile waiting
+ * for the tiles of the previous step that hold its cells' swept-side
  * neighbours).  Every shape gives bit-identical results.  The solution,
  * per-solve counters and CFL are restored afterwards, so tuning does not
  * advance the solves.  The chosen CTA size (tile size for the tile queue)
@@ -318,8 +318,9 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
  * hyperplane with a group of lanes per scalar-solve cell, one per neighbour
  * term, 3 persistent tile-queue sweep (threads = cells per tile). */
 int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster);
-/* Sets the sweep shape (as ath_batch_sweep_shape reports it); the next
- * iteration recaptures the batch's graph. */
+/* Sets the sweep shape (as ath_batch_sweep_shape reports it; mode 3 takes
+ * tiles of 1..4096 cells); the next iteration recaptures the batch's
+ * graph.  Call it outside any stream capture. */
 int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int cluster);
 /* The tile-queue sweep's waits are bounded: a wait for another tile polls
  * at most poll_limit times (default 2^24, about a second), then the sweep
