@@ -141,6 +141,7 @@ def lib() -> C.CDLL:
             "ath_last_error": (C.c_char_p, []),
             "ath_setup_from_input": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
             "ath_setup_append": (C.c_int, [vp, C.c_char_p]),
+            "ath_setup_from_input_dev": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(vp)]),
             "ath_setup_destroy": (C.c_int, [vp]),
             "ath_setup_counts": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                            C.POINTER(C.c_int64)]),
@@ -245,11 +246,16 @@ def _arr(ptr, n, dtype=np.float64):
 class Setup:
     """Host-side case setup: parse + geometry + ghost-cell bookkeeping."""
 
-    def __init__(self, inp_paths):
+    def __init__(self, inp_paths, device: int | None = None):
+        """device: a CUDA device computing the cells' geometry and wall
+        distance (None: the host)."""
         if isinstance(inp_paths, str):
             inp_paths = [inp_paths]
         h = C.c_void_p()
-        check(lib().ath_setup_from_input(inp_paths[0].encode(), C.byref(h)))
+        if device is None:
+            check(lib().ath_setup_from_input(inp_paths[0].encode(), C.byref(h)))
+        else:
+            check(lib().ath_setup_from_input_dev(inp_paths[0].encode(), device, C.byref(h)))
         self.h = h
         for p in inp_paths[1:]:
             check(lib().ath_setup_append(self.h, p.encode()))

@@ -39,6 +39,7 @@ CU_UNITS = {
     "kernels_fp32.cu": ["--fmad=true"],
     "batch.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
+    "geometry.cu": ["--fmad=false"],
 }
 CPP_UNITS = ["setup.cpp", "capi_setup.cpp", "output.cpp"]
 

@@ -2485,7 +2485,8 @@ int ath_server_submit(ath_server *S, const char *inp_path, int64_t *id) {
     if (!S || !inp_path || !id) throw ath::Error(ATH_ERR_ARG, "null argument");
     auto *r = new ath_server::Req();
     r->t_submit = ath::NowMs();
-    const int rc = ath_setup_from_input(inp_path, &r->setup);
+    // the cells' geometry and wall distance are computed on the server's GPU
+    const int rc = ath_setup_from_input_dev(inp_path, S->ctx->device, &r->setup);
     if (rc != ATH_OK) {
       delete r;
       throw ath::Error(rc, ath_last_error());

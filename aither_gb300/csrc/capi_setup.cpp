@@ -36,6 +36,21 @@ int ath_setup_from_input(const char *inp_path, ath_setup **out) {
   });
 }
 
+int ath_setup_from_input_dev(const char *inp_path, int device, ath_setup **out) {
+  return Guard([&] {
+    if (!inp_path || !out || device < 0) throw ath::Error(ATH_ERR_ARG, "bad argument");
+    auto *s = new ath_setup();
+    s->s.geom_device = device;
+    try {
+      ath::AppendInput(s->s, inp_path);
+    } catch (...) {
+      delete s;
+      throw;
+    }
+    *out = s;
+  });
+}
+
 int ath_setup_append(ath_setup *setup, const char *inp_path) {
   return Guard([&] {
     if (!setup || !inp_path) throw ath::Error(ATH_ERR_ARG, "null argument");

@@ -323,8 +323,8 @@ struct Launch {
   // clusters of that shape the device can hold at once (0 = not launchable)
   static int MaxClusters(int kinds, int threads, int cluster);
   // one pass of the LU-SGS solves of one kind (block: 5x5 block solves,
-  // else scalar) as one persistent launch of `ctas` CTAs of 256 threads
-  // over a tile work queue; the queue's done flags and ticket must be zero
+  // else scalar) as one persistent launch of `ctas` CTAs of two warps over
+  // a tile work queue; the queue's done flags and ticket must be zero
   static void SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, int sweep,
                       bool full, bool block, int ctas, cudaStream_t s);
   // CTAs of the tile-queue sweep kernel resident per SM

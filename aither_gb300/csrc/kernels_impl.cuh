@@ -1840,6 +1840,9 @@ __global__ void __launch_bounds__(256) k_sweep_cl(Pools<T> P, const int2 *items,
 // also allow, and the result is bit for bit theirs.  Waits are bounded:
 // after `spin_limit` polls the warp records ATH_ERR_TIMEOUT in *status and
 // returns; a warp whose wait finds *status set returns at once.
+// CTAs of two warp workers: the register-bound occupancy is filled in
+// steps of two warps rather than eight
+constexpr int kTqThreads = 64;
 __device__ __forceinline__ int LoadAcquire(const int *p) {
   int v;
   asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -1853,8 +1856,8 @@ __device__ __forceinline__ void FenceAcqRelGpu() {
 }
 
 template <typename T, bool FULL, bool BLOCK>
-__global__ void __launch_bounds__(256) k_sweep_tq(Pools<T> P, TileQueueDev Q, int forward,
-                                                  int sweep) {
+__global__ void __launch_bounds__(kTqThreads) k_sweep_tq(Pools<T> P, TileQueueDev Q,
+                                                         int forward, int sweep) {
   // each warp is a worker: it claims a tile, its lane 0 waits for the tiles
   // the tile lists, the warp sweeps the tile's cells, lane 0 marks it done
   const int lane = (int)(threadIdx.x & 31);
@@ -2879,22 +2882,25 @@ void Launch<T>::SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, i
   if (Q.ntiles <= 0) return;
   const unsigned grid = (unsigned)std::max(1, std::min(ctas, Q.ntiles));
   if (block)
-    k_sweep_tq<T, true, true><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+    k_sweep_tq<T, true, true><<<grid, kTqThreads, 0, s>>>(P, Q, forward, sweep);
   else if (full)
-    k_sweep_tq<T, true, false><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+    k_sweep_tq<T, true, false><<<grid, kTqThreads, 0, s>>>(P, Q, forward, sweep);
   else
-    k_sweep_tq<T, false, false><<<grid, 256, 0, s>>>(P, Q, forward, sweep);
+    k_sweep_tq<T, false, false><<<grid, kTqThreads, 0, s>>>(P, Q, forward, sweep);
 }
 template <typename T>
 int Launch<T>::TqOccupancy(bool full, bool block) {
   int n = 0;
   cudaError_t e;
   if (block)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, true>, 256, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, true>,
+                                                      kTqThreads, 0);
   else if (full)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, false>, 256, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, true, false>,
+                                                      kTqThreads, 0);
   else
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, false, false>, 256, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_tq<T, false, false>,
+                                                      kTqThreads, 0);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 0;

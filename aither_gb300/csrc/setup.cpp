@@ -24,6 +24,7 @@
 #include <cstring>
 #include <fstream>
 #include <limits>
+#include <memory>
 #include <set>
 #include <sstream>
 #include <stdexcept>
@@ -240,7 +241,7 @@ void SetV(std::vector<double> &v, int64_t n, int64_t idx, V3 a) {
 }
 }  // namespace
 
-void BuildGeometry(Block &b) {
+void BuildGeometry(Block &b, int device) {
   b.NI = b.ni + 2 * b.ng;
   b.NJ = b.nj + 2 * b.ng;
   b.NK = b.nk + 2 * b.ng;
@@ -252,6 +253,10 @@ void BuildGeometry(Block &b) {
   for (int d = 0; d < 3; ++d) {
     b.farea[d].assign(4 * b.NFace(d), 0.0);
     b.fcenter[d].assign(3 * b.NFace(d), 0.0);
+  }
+  if (device >= 0) {
+    DeviceGeometry(b, device);
+    return;
   }
   for (int k = 0; k < b.nk; ++k)
     for (int j = 0; j < b.nj; ++j)
@@ -1127,17 +1132,22 @@ void BuildWallDistance(Setup &setup, int solve) {
     }
   }
   if (wf.empty()) return;
-  const WallTree tree(wf);
+  std::unique_ptr<WallTree> tree;
+  if (setup.geom_device < 0) tree.reset(new WallTree(wf));
   for (int bi : setup.solves[solve].blocks) {
     Block &b = setup.blocks[bi];
     const int64_t nc = b.NCell();
-    for (int k = 0; k < b.nk; ++k)
-      for (int j = 0; j < b.nj; ++j)
-        for (int i = 0; i < b.ni; ++i) {
-          const int64_t c = b.Cell(i, j, k);
-          const double cx = b.center[c], cy = b.center[nc + c], cz = b.center[2 * nc + c];
-          b.wall_dist[c] = std::sqrt(tree.MinDist2(cx, cy, cz));
-        }
+    if (tree) {
+      for (int k = 0; k < b.nk; ++k)
+        for (int j = 0; j < b.nj; ++j)
+          for (int i = 0; i < b.ni; ++i) {
+            const int64_t c = b.Cell(i, j, k);
+            const double cx = b.center[c], cy = b.center[nc + c], cz = b.center[2 * nc + c];
+            b.wall_dist[c] = std::sqrt(tree->MinDist2(cx, cy, cz));
+          }
+    } else {
+      DeviceWallDistance(wf, b, setup.geom_device);
+    }
     // boundary condition of the block face crossed by a non-edge ghost
     auto bc_at = [&](int d, bool lower, const int p[3]) {
       for (const auto &sf : b.surfs) {
@@ -1571,7 +1581,7 @@ void AppendInput(Setup &st, const std::string &path) {
     b.ng = ph.ng;
     b.nv = ph.nv;
     b.solve = solve;
-    BuildGeometry(b);
+    BuildGeometry(b, st.geom_device);
     BuildGhostGeometry(b);
     BuildHyperplanes(b);
     b.state0.assign((size_t)b.NCell() * b.nv, 0.0);

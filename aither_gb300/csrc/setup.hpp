@@ -85,13 +85,21 @@ struct Solve {
 struct Setup {
   std::vector<Block> blocks;
   std::vector<Solve> solves;
+  // CUDA device that computes the physical cells' geometry and wall
+  // distance (-1: the host does)
+  int geom_device = -1;
 };
 
 // Parse an input file and append its blocks as a new solve.
 void AppendInput(Setup &setup, const std::string &path);
 
 // Geometry and boundary bookkeeping for the blocks of one solve.
-void BuildGeometry(Block &b);
+void BuildGeometry(Block &b, int device = -1);
+// The physical cells' and faces' geometry (DeviceGeometry) and the physical
+// cells' wall distance to the centres wf (DeviceWallDistance) computed on a
+// CUDA device, bit for bit the host's (geometry.cu).
+void DeviceGeometry(Block &b, int device);
+void DeviceWallDistance(const std::vector<double> &wf, Block &b, int device);
 void BuildGhostGeometry(Block &b);
 void BuildCellWidths(Block &b);
 void BuildGhostOps(Setup &setup, int solve);

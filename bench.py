@@ -10,8 +10,11 @@ every case of the batch.  Metric: cell-iterations/s.
 
 Arms:
   default            this project's sm_103a path through the C ABI.  `value`
-                     is the FP64 path (the reference's arithmetic); the
-                     mixed FP32/FP64 path is reported beside it under
+                     is the FP64 path with the fast faces (MUSCL and Roe in
+                     FP64 rearranged to fewer divisions; equal to the
+                     reference to roundoff, within the parity tolerances);
+                     the bit-exact FP64 faces are timed beside it under
+                     "fp64_exact" and the mixed FP32/FP64 path under
                      "mixed".
   --impl reference   the reference algorithm on the host cores.  The
                      reference's own build needs its source tree, which this
@@ -149,7 +152,8 @@ def run_native(args, rank: int, world: int, device: int):
     for prec_name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
         if args.precision not in ("both", prec_name):
             continue
-        batch = Batch(ctx, setup, prec, BATCH_FAST_FACES if args.fast_faces else 0)
+        batch = Batch(ctx, setup, prec,
+                      BATCH_FAST_FACES if (args.fast_faces and prec == PREC_FP64) else 0)
         for _ in range(args.warmup):
             batch.iterate(1)
         sweep_threads = batch.autotune(3)  # restores the state it ran on
@@ -178,8 +182,25 @@ def run_native(args, rank: int, world: int, device: int):
         res["e2e"] = run_e2e(batch, ncells, args.steps, world)
         batch.close()
         out[prec_name] = res
+        if prec == PREC_FP64 and args.fast_faces:
+            # the bit-exact faces on the same workload, for comparison
+            ex = Batch(ctx, setup, prec)
+            for _ in range(args.warmup):
+                ex.iterate(1)
+            ex.autotune(2)
+            ex.iterate(args.steps)
+            st2 = ex.stats()
+            pe = ex.profile(1)
+            out["fp64_exact"] = {
+                "value": ncells * args.steps * world / (st2.device_ms * 1e-3),
+                "ms_per_step": st2.device_ms / args.steps,
+                "kernel_ms": dict(zip(["ghost", "face_i", "face_j", "face_k", "cell",
+                                       "sweep_fwd", "sweep_bwd", "update"], pe.tolist()))}
+            ex.close()
     if args.converge_drop > 0 and args.precision == "both":
         out["converge"] = run_converge(args, ctx, setup, specs, world)
+    if args.vortex_iters > 0:
+        out["vortex"] = run_vortex(args, ctx, world)
     if args.sst_steps > 0:
         out["sst"] = run_sst(args, ctx, world)
     if args.plate_iters > 0:
@@ -252,6 +273,48 @@ def run_served(args, ctx, precision, rate, seed):
             "queue_p50_ms": _pct([x.queue_ms for x in st], 50),
             "max_concurrent": max_active,
             "cells": int(sum(sp["ni"] * sp["nj"] * sp["nk"] for sp in specs))}
+
+
+def run_vortex(args, ctx, world):
+    """The plain-method configuration: the 64x32x8 periodic vortex box
+    (inviscid Euler, MUSCL minmod, Roe, LU-SGS at CFL 10), `vortex_iters`
+    iterations timed in FP64 (bit-exact faces, the reference's arithmetic),
+    FP64 with the fast faces and mixed precision; the oracle on rank 0 for
+    a bounded sample."""
+    from aither_gb300 import BATCH_FAST_FACES, PREC_FP64, PREC_MIXED, Batch, Setup, cases
+    with tempfile.TemporaryDirectory() as tmp:
+        inp, st = cases.vortex_box(tmp)
+        setup = Setup(inp)
+        setup.set_state(0, st[0])
+    _, _, ncells = setup.counts()
+    out = {"workload": "periodic vortex box 64x32x8 cells, Euler, MUSCL minmod, Roe, LU-SGS, "
+                       "CFL 10", "cells": ncells, "iterations": args.vortex_iters}
+    for name, prec, flags in (("fp64", PREC_FP64, 0), ("fp64_fast", PREC_FP64, BATCH_FAST_FACES),
+                              ("mixed", PREC_MIXED, 0)):
+        b = Batch(ctx, setup, prec, flags)
+        b.autotune(2)
+        _barrier(world)
+        norms = b.iterate(args.vortex_iters)
+        st2 = b.stats()
+        ms = _max_over_ranks(st2.device_ms, world)
+        out[name] = {"cell_iterations_per_s": ncells * args.vortex_iters * world / (ms * 1e-3),
+                     "ms_per_iteration": ms / args.vortex_iters,
+                     "status_ok": all(x.status == 0 for x in norms),
+                     "sweep_shape": b.sweep_shape()}
+        b.close()
+    if not args.no_cpu_baseline and int(os.environ.get("RANK", "0")) == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from pyoracle import Oracle
+        orc = Oracle(setup, 1)
+        orc.iterate(1)
+        t0 = time.perf_counter()
+        orc.iterate(20)
+        dt = (time.perf_counter() - t0) / 20
+        out["cpu_baseline"] = {"value": ncells / dt, "unit": METRIC, "cores": 1, "kind": "port",
+                               "sample": "20 iterations after 1 warm-up; oracle, one block so "
+                                         "one thread"}
+        orc.close()
+    return out
 
 
 def run_sst(args, ctx, world):
@@ -548,7 +611,7 @@ def main():
     ap.add_argument("--ncases", type=int, default=64)
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fast-faces", type=int, default=0,
+    ap.add_argument("--fast-faces", type=int, default=1,
                     help="1: FP64 batches use the fast MUSCL/Roe faces (roundoff-equal to "
                          "the reference instead of bit for bit)")
     ap.add_argument("--converge-drop", type=float, default=1e-6,
@@ -564,6 +627,8 @@ def main():
     ap.add_argument("--served-slots", type=int, default=16)
     ap.add_argument("--served-mix", default="ns_sst", choices=["ns_sst", "euler_ns"],
                     help="half laminar / half SST-2003 requests, or half Euler / half laminar")
+    ap.add_argument("--vortex-iters", type=int, default=200,
+                    help="iterations of the 64x32x8 vortex box section (0 skips it)")
     ap.add_argument("--sst-steps", type=int, default=20,
                     help="iterations of the SST flat plate section (0 skips it)")
     ap.add_argument("--plate-iters", type=int, default=500,
@@ -674,10 +739,16 @@ def main():
         line["served"] = res["served"]
     if "sst" in res:
         line["sst"] = res["sst"]
+    if "vortex" in res:
+        line["vortex"] = res["vortex"]
+    if "fp64_exact" in res:
+        line["fp64_exact"] = res["fp64_exact"]
     if "plate" in res:
         line["plate"] = res["plate"]
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(8, 2, os.cpu_count() or 1)
+        threads = os.cpu_count() or 1
+        # at least as many cases as host threads (OpenMP over blocks)
+        line["cpu_baseline"] = cpu_baseline(min(args.ncases, max(threads, 8)), 2, threads)
     print(json.dumps(line))
 
 

@@ -214,6 +214,13 @@ typedef struct {
  * independent solves: ath_setup_append() adds the blocks of another input
  * file as a new solve. */
 int ath_setup_from_input(const char *inp_path, ath_setup **out);
+/* The same with the physical cells' and faces' geometry (volumes,
+ * centroids, face areas and centres: the procBlock constructor's
+ * plot3dBlock::Volume / Centroid / FaceArea* / FaceCenter*, src/plot3d.cpp:
+ * 60-360) and the physical cells' wall distance (procBlock::CalcWallDistance,
+ * src/procBlock.cpp:6030) computed on CUDA device `device`, bit for bit the
+ * host setup's; blocks appended later (ath_setup_append) use the device too. */
+int ath_setup_from_input_dev(const char *inp_path, int device, ath_setup **out);
 int ath_setup_append(ath_setup *setup, const char *inp_path);
 int ath_setup_destroy(ath_setup *setup);
 int ath_setup_counts(const ath_setup *setup, int *nsolves, int *nblocks,
