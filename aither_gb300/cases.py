@@ -243,10 +243,10 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                  sweeps: int = 1, inflow: str = "characteristic",
                  outflow: str = "characteristic", back_pressure: float = 1.0,
                  nonreflecting: float | None = None, time: str = "implicitEuler",
-                 dt: float | None = None, nl: int = 1):
+                 dt: float | None = None, nl: int = 1, nr_outlet: float | None = None):
     """Inviscid channel over a sin^2 bump.  `nonreflecting` (a length in
-    metres) makes the inlet nonreflecting with that lengthScale; time, dt
-    and nl select the time integration.    Inflow at i = 0 and outflow at
+    metres) makes the inlet nonreflecting with that lengthScale, `nr_outlet`
+    the pressure outlet; time, dt and nl select the time integration.    Inflow at i = 0 and outflow at
     i = ni are characteristic far fields, or (inflow "stagnation") a
     stagnation inlet at the freestream's total pressure and temperature
     along +x, (inflow "inlet") the reference's inlet boundary with the
@@ -277,7 +277,8 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                       f"velocity={vel}{nr})")
         in_bc = ("inlet", 0, 0, 0, nj, 0, nk, 3)
     if outflow == "pressure":
-        states.append(f"pressureOutlet(tag=4; pressure={_fmt(back_pressure * p_inf)})")
+        nro = (f"; nonreflecting=true; lengthScale={_fmt(nr_outlet)}" if nr_outlet else "")
+        states.append(f"pressureOutlet(tag=4; pressure={_fmt(back_pressure * p_inf)}{nro})")
         out_bc = ("pressureOutlet", ni, ni, 0, nj, 0, nk, 4)
     bcs = [[in_bc, out_bc,
             ("slipWall", 0, ni, 0, 0, 0, nk, 2),
@@ -322,7 +323,8 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
                  reynolds: float = 1e5, stretch: float = 1.0, cfl: float = 20.0,
                  name: str = "chan", precision_note: str = "", rans: bool = False,
                  tint: float = 0.001, vratio: float = 10.0, inflow: str = "characteristic",
-                 outflow: str = "characteristic", back_pressure: float = 1.0):
+                 outflow: str = "characteristic", back_pressure: float = 1.0,
+                 nr_outlet: float | None = None):
     """Bump or wedge channel with free-stream Mach `mach` at angle of attack
     `alpha` (degrees, in the x-y plane); characteristic in- and outflow
     (or a stagnation inlet at the free stream's total state and a pressure
@@ -364,7 +366,8 @@ def wall_channel(outdir: str, ni: int, nj: int, nk: int, kind: str, param: float
                       f"direction=[{_fmt(ca)}, {_fmt(sa)}, 0]{turb})")
         in_bc = ("stagnationInlet", 0, 0, 0, nj, 0, nk, 5)
     if outflow == "pressure":
-        states.append(f"pressureOutlet(tag=6; pressure={_fmt(back_pressure * p_inf)})")
+        nro = (f"; nonreflecting=true; lengthScale={_fmt(nr_outlet)}" if nr_outlet else "")
+        states.append(f"pressureOutlet(tag=6; pressure={_fmt(back_pressure * p_inf)}{nro})")
         out_bc = ("pressureOutlet", ni, ni, 0, nj, 0, nk, 6)
     bcs = [[in_bc, out_bc,
             lower,

@@ -104,6 +104,9 @@ struct Lists {
   // nonreflecting surfaces: their cells grouped by surface, offsets
   std::vector<NrDev> nr;
   std::vector<int32_t> nr_off;
+  // cells whose ghosts a nonreflecting pressure outlet fills (pool index,
+  // block): their gradients of the previous residual are kept
+  std::vector<int32_t> nrg_cells, nrg_block;
   // hyperplane-ordered sweep tables
   std::vector<int64_t> q0;        // per block: first q index
   std::vector<int32_t> qpos;      // per pool cell
@@ -184,6 +187,7 @@ struct BatchCore {
   GhostOpDev *d_ops = nullptr, *d_conn_ops = nullptr;
   NrDev *d_nr = nullptr;
   int32_t *d_nr_off = nullptr;
+  int32_t *d_nrg_cells = nullptr, *d_nrg_block = nullptr;
   int n_nr_surf = 0;
   GhostOpDev *d_edge_ops = nullptr, *d_vops = nullptr, *d_vedge_ops = nullptr;
   int32_t *d_edge_solve = nullptr, *d_vop_solve = nullptr, *d_vedge_solve = nullptr;
@@ -447,6 +451,10 @@ class Runner : public RunnerBase {
     P_.ghost_src = m.Upload(c.L.ghost_src);
     for (int d = 0; d < 3; ++d) c_.mem->Zero(P_.flux[d], 0, 5 * n * sizeof(double));
     if (c.any_rans) AllocTurbulence(m, n, nq, ngh);
+    if (!c.L.nrg_cells.empty()) {
+      P_.nrg = m.Alloc<double>(12 * (size_t)n);
+      c_.mem->Zero(P_.nrg, 0, 12 * (size_t)n * sizeof(double));
+    }
     if (c.n_nr_surf > 0) {
       P_.nr_mach = m.Alloc<double>(2 * (size_t)c.n_nr_surf);
       c_.mem->Zero(P_.nr_mach, 0, 2 * (size_t)c.n_nr_surf * sizeof(double));
@@ -624,11 +632,18 @@ class Runner : public RunnerBase {
                                                   c_.d_fring, c_.ring_cap, c_.d_iter);
     }
   }
+  // gradients the nonreflecting outlets read at the next ghost fill, from
+  // this residual's state and ghosts (viscous ghosts included)
+  void NrGrads() {
+    Launch<T>::NrGrads(P_, c_.d_nrg_cells, c_.d_nrg_block, (int)c_.L.nrg_cells.size(),
+                       c_.stream);
+  }
   void Residual() override {
     for (int d = 0; d < 3; ++d)
       Launch<T>::Face(d, P_, c_.d_faces[d], c_.d_face_cta_block[d],
                       (int)c_.L.face_cta_block[d].size(), FaceKinds(), c_.stream);
     Viscous();
+    NrGrads();
     Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                     c_.kinds, c_.stream);
     if (c_.kinds & 2)
@@ -771,6 +786,7 @@ class Runner : public RunnerBase {
         Check(cudaEventRecord(e[2 + d], c_.stream), "event");
       }
       Viscous();
+      NrGrads();
       Launch<T>::Cell(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
                       c_.kinds, c_.stream);
       if (c_.kinds & 2)
@@ -1216,6 +1232,12 @@ void BuildLists(BatchCore &c) {
       }
       L.ops.push_back(g);
       L.op_solve.push_back(bk.solve);
+      if (op.type == ATH_BC_PRESSURE_OUTLET && op.state >= 0 &&
+          st.solves[bk.solve].states[op.state].nonreflecting &&
+          std::find(L.nrg_cells.begin(), L.nrg_cells.end(), g.src) == L.nrg_cells.end()) {
+        L.nrg_cells.push_back(g.src);
+        L.nrg_block.push_back(b);
+      }
       if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK) L.conn_ops.push_back(g);
     }
   }
@@ -1400,6 +1422,7 @@ void CountLaunches(BatchCore &c) {
                         (c.L.wall_faces.empty() ? 0 : 2) +
                         1 + (c.L.ops.empty() ? 0 : 1) + 3 * nf + nkinds + ((c.kinds & 2) ? 1 : 0) +
                         (c.any_unsteady ? 1 : 0) + (c.n_nr_surf > 0 ? 1 : 0) +
+                        (c.L.nrg_cells.empty() ? 0 : 1) +
                         (nskinds ? 2 * per_pass * c.max_sweeps * nskinds +
                                        (c.max_sweeps > 1 ? 1 + 2 * c.max_sweeps * conn : conn)
                                  : 0) +
@@ -1536,6 +1559,10 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     c.d_nr = m.Upload(c.L.nr);
     c.d_nr_off = m.Upload(c.L.nr_off);
     c.n_nr_surf = (int)c.L.nr_off.size() - 1;
+  }
+  if (!c.L.nrg_cells.empty()) {
+    c.d_nrg_cells = m.Upload(c.L.nrg_cells);
+    c.d_nrg_block = m.Upload(c.L.nrg_block);
   }
   c.d_conn_ops = m.Upload(c.L.conn_ops);
   c.d_op_solve = m.Upload(c.L.op_solve);

@@ -179,6 +179,10 @@ struct Pools {
   double *Un, *Unm1;
   T *Bq, *Btq;
   double *nr_mach;  // [2][nonreflecting surfaces] average, largest Mach
+  // [12][ncell] cell-averaged velocity gradient (9, d/dx rows) and pressure
+  // gradient (3) of the previous residual at the cells nonreflecting
+  // pressure outlets read (null without such outlets)
+  double *nrg;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -349,6 +353,10 @@ struct Launch {
   // surface (items nr[off[s] .. off[s+1]) into P.nr_mach[2 s .. 2 s + 1])
   static void NrMach(const Pools<T> &P, const NrDev *nr, const int32_t *off, int nsurf,
                      cudaStream_t s);
+  // cell-averaged velocity and pressure gradients of the listed cells
+  // (pool index, block) into P.nrg, from the current state and ghosts
+  static void NrGrads(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block, int n,
+                      cudaStream_t s);
   // StoreOldSolution of the time-accurate solves at a time step's start;
   // block >= 0: that block's current state into both time levels
   static void StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

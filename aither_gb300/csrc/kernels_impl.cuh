@@ -289,6 +289,63 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       const double sosInt = SoS(in, gas);
       const double rhoSoSInt = in.rho * sosInt;
       g.p = bs.p_out;
+      if (bs.nonreflecting) {
+        // LODI relaxation of the boundary pressure towards the specified
+        // one with the transverse terms (src/ghostStates.cpp:612-638): the
+        // time-n state, previous time step and previous residual's velocity
+        // and pressure gradients of the boundary-adjacent cell, and the
+        // surface's average and largest normal Mach number
+        double cn[5];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) cn[v] = P.Un[v * n + op.src];
+        const Prim<double> sN = ConsToPrim(cn, gas);
+        const double dt = P.dt[op.src];
+        const double avgMach = P.nr_mach[2 * op.src2], maxMach = P.nr_mach[2 * op.src2 + 1];
+        double vg[9], pgr[3];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) vg[e] = P.nrg[e * n + op.src];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) pgr[e] = P.nrg[(9 + e) * n + op.src];
+        const double deltaVel = Dot(in.u - sN.u, in.v - sN.v, in.w - sN.w, nx, ny, nz);
+        const double sigma = 0.25;
+        const double rhoN = sN.rho;
+        const double sosN = SoS(sN, gas);
+        const double rhoSoSN = rhoN * sosN;
+        const double k = sigma * sosN * (1.0 - maxMach * maxMach) / bs.length_scale;
+        const double beta = avgMach;
+        const double pgn = Dot(pgr[0], pgr[1], pgr[2], nx, ny, nz);
+        const double pgT[3] = {pgr[0] - pgn * nx, pgr[1] - pgn * ny, pgr[2] - pgn * nz};
+        const double vnN = Dot(sN.u, sN.v, sN.w, nx, ny, nz);
+        const double velT[3] = {sN.u - vnN * nx, sN.v - vnN * ny, sN.w - vnN * nz};
+        // velocity gradient without its normal component, row by row
+        // (tensor::RemoveComponent), then the rows' normal-weighted sum
+        // (LinearCombination) and the sum of all entries (Sum)
+        double gT[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const double rn = Dot(vg[r * 3], vg[r * 3 + 1], vg[r * 3 + 2], nx, ny, nz);
+          gT[r * 3] = vg[r * 3] - rn * nx;
+          gT[r * 3 + 1] = vg[r * 3 + 1] - rn * ny;
+          gT[r * 3 + 2] = vg[r * 3 + 2] - rn * nz;
+        }
+        double dVn[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          dVn[q] = gT[q] * nx;
+          dVn[q] += gT[3 + q] * ny;
+          dVn[q] += gT[6 + q] * nz;
+        }
+        double gsum = 0.0;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) gsum += gT[e];
+        const double dVelT = gsum - (((0.0 + dVn[0]) + dVn[1]) + dVn[2]);
+        const double gamma = gas.Gamma();
+        const double tr =
+            -0.5 * (Dot(velT[0], velT[1], velT[2], pgT[0] - rhoSoSN * dVn[0],
+                        pgT[1] - rhoSoSN * dVn[1], pgT[2] - rhoSoSN * dVn[2]) +
+                    gamma * sN.p * dVelT);
+        g.p = (sN.p + rhoSoSN * deltaVel + dt * k * bs.p_out - dt * beta * tr) / (1.0 + dt * k);
+      }
       const double deltaPressure = in.p - g.p;
       const double rho = in.rho - deltaPressure / (sosInt * sosInt);
       g.rho = rho * (in.rho / in.rho);
@@ -2348,6 +2405,127 @@ __device__ __forceinline__ void ViscFaceGather(const Pools<PT> &P, const BlockDe
   muf = cd * (T)P.mu[cu] + cw * (T)P.mu[cl];
 }
 
+// Dual-cell Green-Gauss gradients of velocity and pressure at face c of
+// direction D (procBlock::CalcGradsI/J/K, src/procBlock.cpp:5173: the
+// velocity part of VectorGradGG and ScalarGradGG of the pressure), in the
+// order of ViscFaceGather.
+template <int D, typename PT>
+__device__ __forceinline__ void FaceGradVP(const Pools<PT> &P, const BlockDev &b, int64_t c,
+                                           double grad[3][3], double pg[3]) {
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  const Prim<double> Wl = LoadW<double>(P.W, n, cl), Wu = LoadW<double>(P.W, n, cu);
+  auto area = [&](int e, int64_t x, double a[3]) {
+    const double *fa = P.fa[e];
+    const double m = fa[3 * n + x];
+    a[0] = fa[x] * m;
+    a[1] = fa[n + x] * m;
+    a[2] = fa[2 * n + x] * m;
+  };
+  double vlo[3][3], vhi[3][3], plo[3], phi[3], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e == D) {
+      vlo[e][0] = Wl.u; vlo[e][1] = Wl.v; vlo[e][2] = Wl.w;
+      vhi[e][0] = Wu.u; vhi[e][1] = Wu.v; vhi[e][2] = Wu.w;
+      plo[e] = Wl.p;
+      phi[e] = Wu.p;
+      double A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (A0[r] + A1[r]);
+        alo[e][r] = 0.5 * (A0[r] + A2[r]);
+      }
+    } else {
+      const Prim<double> Wup = LoadW<double>(P.W, n, cu + st[e]),
+                         Wlp = LoadW<double>(P.W, n, cl + st[e]);
+      const Prim<double> Wum = LoadW<double>(P.W, n, cu - st[e]),
+                         Wlm = LoadW<double>(P.W, n, cl - st[e]);
+      vhi[e][0] = 0.25 * (((Wl.u + Wu.u) + Wup.u) + Wlp.u);
+      vhi[e][1] = 0.25 * (((Wl.v + Wu.v) + Wup.v) + Wlp.v);
+      vhi[e][2] = 0.25 * (((Wl.w + Wu.w) + Wup.w) + Wlp.w);
+      vlo[e][0] = 0.25 * (((Wl.u + Wu.u) + Wum.u) + Wlm.u);
+      vlo[e][1] = 0.25 * (((Wl.v + Wu.v) + Wum.v) + Wlm.v);
+      vlo[e][2] = 0.25 * (((Wl.w + Wu.w) + Wum.w) + Wlm.w);
+      phi[e] = 0.25 * (((Wl.p + Wu.p) + Wup.p) + Wlp.p);
+      plo[e] = 0.25 * (((Wl.p + Wu.p) + Wum.p) + Wlm.p);
+      double Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (Aup[r] + Alp[r]);
+        alo[e][r] = 0.5 * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const double vol = 0.5 * (P.vol[cl] + P.vol[cu]);
+  const double invVol = 1.0 / vol;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int qv = 0; qv < 3; ++qv) {
+      grad[r][qv] = vhi[0][qv] * ahi[0][r] - vlo[0][qv] * alo[0][r] +
+                    vhi[1][qv] * ahi[1][r] - vlo[1][qv] * alo[1][r] +
+                    vhi[2][qv] * ahi[2][r] - vlo[2][qv] * alo[2][r];
+      grad[r][qv] *= invVol;
+    }
+    pg[r] = phi[0] * ahi[0][r] - plo[0] * alo[0][r] + phi[1] * ahi[1][r] -
+            plo[1] * alo[1][r] + phi[2] * ahi[2][r] - plo[2] * alo[2][r];
+    pg[r] *= invVol;
+  }
+}
+
+// Cell-averaged velocity and pressure gradients (one sixth of each face's,
+// faces in the order i low, i high, j low, ..., as procBlock::CalcGradsI/J/K
+// and CalcViscFluxI/J/K accumulate them, src/procBlock.cpp:5790) of the
+// cells whose ghosts a nonreflecting pressure outlet fills; they are read
+// at the next iteration's ghost fill, as the reference reads the previous
+// residual's gradients.
+template <typename T>
+__global__ void k_nr_grads(Pools<T> P, const int32_t *cells, const int32_t *cell_block, int ncl) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncl) return;
+  const int64_t c = cells[t];
+  const BlockDev b = P.blocks[cell_block[t]];
+  if (!P.solves[b.solve].active) return;
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const double sixth = 1.0 / 6.0;
+  double vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, pg[3] = {0, 0, 0};
+  auto add = [&](const double grad[3][3], const double p[3]) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) vg[r * 3 + q] += sixth * grad[r][q];
+      pg[r] += sixth * p[r];
+    }
+  };
+  double grad[3][3], p[3];
+  FaceGradVP<0>(P, b, c, grad, p);
+  add(grad, p);
+  FaceGradVP<0>(P, b, c + st[0], grad, p);
+  add(grad, p);
+  FaceGradVP<1>(P, b, c, grad, p);
+  add(grad, p);
+  FaceGradVP<1>(P, b, c + st[1], grad, p);
+  add(grad, p);
+  FaceGradVP<2>(P, b, c, grad, p);
+  add(grad, p);
+  FaceGradVP<2>(P, b, c + st[2], grad, p);
+  add(grad, p);
+#pragma unroll
+  for (int e = 0; e < 9; ++e) P.nrg[e * n + c] = vg[e];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) P.nrg[(9 + e) * n + c] = pg[e];
+}
+
 // Mixed-precision version of ViscFaceGather: velocities and temperatures
 // enter the dual-cell sums as offsets from the upper cell's values, formed
 // in FP64 (the temperature offset as (p rho_u - p_u rho) / (rho rho_u R)),
@@ -2875,6 +3053,11 @@ void Launch<T>::SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int
     else LaunchSweepCl<T, false, false>(P, L, forward, sweep, threads, cluster, s);
   }
   if (kinds & 2) LaunchSweepCl<T, true, true>(P, L, forward, sweep, threads, cluster, s);
+}
+template <typename T>
+void Launch<T>::NrGrads(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block,
+                        int n, cudaStream_t s) {
+  if (n > 0) k_nr_grads<T><<<(n + 127) / 128, 128, 0, s>>>(P, cells, cell_block, n);
 }
 template <typename T>
 void Launch<T>::SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, int sweep,

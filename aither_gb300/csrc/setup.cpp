@@ -1486,12 +1486,6 @@ void AppendInput(Setup &st, const std::string &path) {
       if (m.count("lengthScale")) s.length_scale = std::stod(m["lengthScale"]) / lref;
       if (s.nonreflecting && !m.count("lengthScale"))
         Fail("lengthScale must be specified with nonreflecting");
-      // the transverse terms of the nonreflecting outlet read the cell
-      // pressure and velocity gradients of the previous residual, which the
-      // reference forms for every solve (CalcGradsI/J/K for inviscid ones,
-      // src/procBlock.cpp:6141); they are not kept here
-      if (s.nonreflecting && name == "pressureOutlet")
-        Fail("nonreflecting pressureOutlet boundaries are not supported");
       if (m.count("wallTreatment") && m["wallTreatment"] != "lowRe")
         Fail("wall laws are not supported");
       if (m.count("turbulenceIntensity")) s.turb_intensity = num("turbulenceIntensity", 0);

@@ -594,12 +594,30 @@ def _max_over_ranks(x: float, world: int) -> float:
 
 
 # -------------------------------------------------------------------- main
-def fp64_flop_per_cell() -> dict:
-    """Executed FP64 FLOP per cell-iteration of the FP64 bump path by
-    kernel class, from ncu's SASS counters (dfma x 2 + dadd + dmul) over one
-    iteration of a 64x48x32 bump channel (profiles/fp64_flops_bump64x48x32.md)."""
-    return {"face_per_direction": 1026.0, "sweeps": 1134.0, "cell": 502.0, "update": 188.0,
-            "ghost": 25.0}
+# One-off ncu captures of the FP64 batched path, per cell of the batch (a
+# bump-channel batch's cells; the counts scale with cells):
+#   * fast faces -- `ncu --clock-control none --metrics dram__bytes_read.sum,
+#     dram__bytes_write.sum,gpu__time_duration.sum,smsp__sass_thread_inst_
+#     executed_op_{dfma,dadd,dmul}_pred_on.sum -k regex:'k_face|k_cell' -c 8`
+#     on `python bench.py --ncases 8 --steps 2 --warmup 3 --converge-drop 0
+#     --served-n 0 --plate-iters 0 --sst-steps 0 --vortex-iters 0
+#     --no-cpu-baseline --precision fp64` (the first 8 cases, 888,004 cells;
+#     GB300, 2026-12-04): residual-pass DRAM traffic 804.4 B per cell (faces
+#     102.9 + 112.3 + 112.6, cell kernel 476.6), executed FP64 FLOP 442.1 per
+#     face direction and 502.3 in the cell kernel;
+#   * bit-exact faces, sweeps, update and ghost fill -- the SASS counters
+#     over one iteration of a 64x48x32 bump channel: 1026 FLOP per face
+#     direction, 1134 in the two sweeps, 502 cell, 188 update, 25 ghosts.
+# FLOP = 2 x DFMA + DADD + DMUL (divisions and square roots run as FMA
+# sequences and are counted in those).
+NCU_PER_CELL = {
+    "source": "ncu captures on GB300 of the batched bump-channel path (fast faces: first "
+              "8 cases of the batched workload, 888,004 cells; bit-exact faces and the "
+              "other kernels: one 64x48x32 case), 2026-12-04",
+    "residual_traffic_bytes": {"fast": 804.4},
+    "flop": {"face_per_direction": {"fast": 442.1, "exact": 1026.0}, "sweeps": 1134.0,
+             "cell": 502.3, "update": 188.0, "ghost": 25.0},
+}
 
 
 def main():
@@ -698,25 +716,39 @@ def main():
     dom = max(pass_ms, key=pass_ms.get)
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     # FP64 bound: executed FP64 FLOP per cell-iteration (2 per DFMA, 1 per
-    # DADD / DMUL, from the SASS instruction counters; divisions and square
-    # roots run as FMA sequences) against the measured FP64 issue peak
-    fl = fp64_flop_per_cell()
-    face_ms = km["face_i"] + km["face_j"] + km["face_k"]
+    # DADD / DMUL, from the captures above; divisions and square roots run as
+    # FMA sequences) against the FP64 issue peak measured on this GPU.  Only
+    # for the FP64 arm of this workload (the physics the counts were taken on)
+    roof_fp64 = None
     fp64_peak = res.get("fp64_peak_tflops") or 0.0
-    face_tf = 3 * fl["face_per_direction"] * ncells / (face_ms * 1e-3) / 1e12
-    path_flop = 3 * fl["face_per_direction"] + fl["sweeps"] + fl["cell"] + fl["update"] + \
-        fl["ghost"]
-    path_tf = path_flop * fp["value"] / 1e12
-    roof_fp64 = {"bound": "fp64", "kernel": "face (3 directions)", "achieved": face_tf,
-                 "peak": fp64_peak, "unit": "TFLOP/s",
-                 "frac": face_tf / fp64_peak if fp64_peak else None,
-                 "peak_source": "measured on this GPU (ath_ctx_fp64_peak)",
-                 "path_achieved": path_tf,
-                 "path_frac": path_tf / fp64_peak if fp64_peak else None,
-                 "flop_per_cell_iteration": fl}
+    if "fp64" in res and fp64_peak:
+        fl = NCU_PER_CELL["flop"]
+        mode = "fast" if args.fast_faces else "exact"
+        fpd = fl["face_per_direction"][mode]
+        face_ms = km["face_i"] + km["face_j"] + km["face_k"]
+        face_tf = 3 * fpd * ncells / (face_ms * 1e-3) / 1e12
+        path_flop = 3 * fpd + fl["sweeps"] + fl["cell"] + fl["update"] + fl["ghost"]
+        path_tf = path_flop * fp["value"] / 1e12
+        roof_fp64 = {"bound": "fp64", "kernel": "face (3 directions)", "achieved": face_tf,
+                     "peak": fp64_peak, "unit": "TFLOP/s", "frac": face_tf / fp64_peak,
+                     "peak_source": "measured on this GPU (ath_ctx_fp64_peak)",
+                     "path_achieved": path_tf, "path_frac": path_tf / fp64_peak,
+                     "faces": mode, "flop_per_cell_iteration": path_flop,
+                     "flop_source": NCU_PER_CELL["source"]}
+    traffic = None
+    if "fp64" in res and args.fast_faces and dom == "residual":
+        # DRAM bytes of one residual pass (3 face launches + the cell
+        # launch), from the capture above scaled by the batch's cells
+        traffic = NCU_PER_CELL["residual_traffic_bytes"]["fast"] * ncells
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
-            "peak_source": peaks["source"], "traffic": None,
+            "peak_source": peaks["source"], "traffic": traffic,
+            "traffic_note": "DRAM bytes per residual pass from a one-off ncu capture of "
+                            "the 8-case batch, scaled by cells; above the algorithmic "
+                            "bytes because the face launches write per-face fluxes and "
+                            "spectral radii that the cell launch reads back, and read "
+                            "face areas, ghosts and neighbour states the per-cell count "
+                            "leaves out",
             "bytes_per_cell": {k: v for k, v in ab.items()}}
     line = {"metric": METRIC, "value": fp["value"], "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": fp["ms_per_step"],

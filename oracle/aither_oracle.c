@@ -53,6 +53,9 @@ typedef struct {
   int n_nr, n_nr_surf;     /* nonreflecting surfaces: cells, surfaces */
   ath_nr_cell *nr;
   double *nr_mach;         /* [n_nr_surf][2] average, largest Mach */
+  double *nrg;  /* [nc][12] velocity (9) and pressure (3) gradients of the
+                   previous residual at the cells nonreflecting pressure
+                   outlets read (NULL without such outlets) */
 } oblock;
 
 typedef struct {
@@ -974,6 +977,96 @@ static void mat_vec2(const double *M, const double *x, double *out) {
   }
 }
 
+/* Dual-cell Green-Gauss gradients of velocity and pressure at the face of
+ * direction d below cell cu (procBlock::CalcGradsI/J/K, src/procBlock.cpp:
+ * 5173; VectorGradGG / ScalarGradGG, src/utility.cpp:59,138). */
+static void face_grad_vp(const oblock *b, int d, int64_t cu, double grad[3][3], double pg[3]) {
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  const int64_t cl = cu - st[d];
+  const double *Wl = &b->W[cl * NV], *Wu = &b->W[cu * NV];
+  double vlo[3][3], vhi[3][3], plo[3], phi[3], alo[3][3], ahi[3][3];
+  const int uI = (int)(cu % b->NI) - b->ng, uJ = (int)((cu / b->NI) % b->NJ) - b->ng,
+            uK = (int)(cu / ((int64_t)b->NI * b->NJ)) - b->ng;
+  const int lI = (int)(cl % b->NI) - b->ng, lJ = (int)((cl / b->NI) % b->NJ) - b->ng,
+            lK = (int)(cl / ((int64_t)b->NI * b->NJ)) - b->ng;
+  for (int e = 0; e < 3; ++e) {
+    if (e == d) {
+      for (int q = 0; q < 3; ++q) {
+        vlo[e][q] = Wl[1 + q];
+        vhi[e][q] = Wu[1 + q];
+      }
+      plo[e] = Wl[4];
+      phi[e] = Wu[4];
+      double A0[3], A1[3], A2[3];
+      area_vec(b, d, face_idx(b, d, uI, uJ, uK), A0);
+      area_vec(b, d, face_idx(b, d, uI + (d == 0), uJ + (d == 1), uK + (d == 2)), A1);
+      area_vec(b, d, face_idx(b, d, uI - (d == 0), uJ - (d == 1), uK - (d == 2)), A2);
+      for (int q = 0; q < 3; ++q) {
+        ahi[e][q] = 0.5 * (A0[q] + A1[q]);
+        alo[e][q] = 0.5 * (A0[q] + A2[q]);
+      }
+    } else {
+      const int64_t cup = cu + st[e], clp = cl + st[e], cum = cu - st[e], clm = cl - st[e];
+      const double *Wup = &b->W[cup * NV], *Wlp = &b->W[clp * NV], *Wum = &b->W[cum * NV],
+                   *Wlm = &b->W[clm * NV];
+      for (int q = 0; q < 3; ++q) {
+        vhi[e][q] = 0.25 * (((Wl[1 + q] + Wu[1 + q]) + Wup[1 + q]) + Wlp[1 + q]);
+        vlo[e][q] = 0.25 * (((Wl[1 + q] + Wu[1 + q]) + Wum[1 + q]) + Wlm[1 + q]);
+      }
+      phi[e] = 0.25 * (((Wl[4] + Wu[4]) + Wup[4]) + Wlp[4]);
+      plo[e] = 0.25 * (((Wl[4] + Wu[4]) + Wum[4]) + Wlm[4]);
+      double Au[3], Al[3], Aup[3], Alp[3];
+      area_vec(b, e, face_idx(b, e, uI, uJ, uK), Au);
+      area_vec(b, e, face_idx(b, e, lI, lJ, lK), Al);
+      area_vec(b, e, face_idx(b, e, uI + (e == 0), uJ + (e == 1), uK + (e == 2)), Aup);
+      area_vec(b, e, face_idx(b, e, lI + (e == 0), lJ + (e == 1), lK + (e == 2)), Alp);
+      for (int q = 0; q < 3; ++q) {
+        ahi[e][q] = 0.5 * (Aup[q] + Alp[q]);
+        alo[e][q] = 0.5 * (Au[q] + Al[q]);
+      }
+    }
+  }
+  const double vol = 0.5 * (b->vol[cl] + b->vol[cu]);
+  const double invVol = 1.0 / vol;
+  for (int r = 0; r < 3; ++r) {
+    for (int q = 0; q < 3; ++q) {
+      grad[r][q] = vhi[0][q] * ahi[0][r] - vlo[0][q] * alo[0][r] + vhi[1][q] * ahi[1][r] -
+                   vlo[1][q] * alo[1][r] + vhi[2][q] * ahi[2][r] - vlo[2][q] * alo[2][r];
+      grad[r][q] *= invVol;
+    }
+    pg[r] = phi[0] * ahi[0][r] - plo[0] * alo[0][r] + phi[1] * ahi[1][r] -
+            plo[1] * alo[1][r] + phi[2] * ahi[2][r] - plo[2] * alo[2][r];
+    pg[r] *= invVol;
+  }
+}
+
+/* Cell-averaged velocity and pressure gradients (one sixth per face, i low,
+ * i high, j low, ... as the reference accumulates them, src/procBlock.cpp:
+ * 5790) of the cells nonreflecting pressure outlets read; used at the next
+ * ghost fill. */
+static void nr_grads(const orc_case *c, oblock *b) {
+  const osolve *sv = &c->s[b->solve];
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  for (int o = 0; o < b->nops; ++o) {
+    const ath_ghost_op *op = &b->ops[o];
+    if (op->type != ATH_BC_PRESSURE_OUTLET || !sv->states[op->state].nonreflecting) continue;
+    const int64_t x = op->src;
+    double vg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, pg[3] = {0, 0, 0};
+    const double sixth = 1.0 / 6.0;
+    for (int d = 0; d < 3; ++d)
+      for (int side = 0; side < 2; ++side) {
+        double grad[3][3], p[3];
+        face_grad_vp(b, d, side ? x + st[d] : x, grad, p);
+        for (int r = 0; r < 3; ++r) {
+          for (int q = 0; q < 3; ++q) vg[r * 3 + q] += sixth * grad[r][q];
+          pg[r] += sixth * p[r];
+        }
+      }
+    memcpy(&b->nrg[x * 12], vg, sizeof(vg));
+    memcpy(&b->nrg[x * 12 + 9], pg, sizeof(pg));
+  }
+}
+
 static void viscous_fluxes(orc_case *c, oblock *b) {
   const osolve *sv = &c->s[b->solve];
   const ath_solve_view *v = &sv->v;
@@ -1313,6 +1406,13 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     for (int i = 0; i < b->n_nr; ++i)
       if (b->nr[i].surf + 1 > b->n_nr_surf) b->n_nr_surf = b->nr[i].surf + 1;
     b->nr_mach = (double *)dup_arr(NULL, 16 * (size_t)b->n_nr_surf);
+    b->nrg = NULL;
+    for (int o = 0; o < v->nops; ++o)
+      if (v->ops[o].type == ATH_BC_PRESSURE_OUTLET && v->ops[o].state >= 0 &&
+          c->s[v->solve].states[v->ops[o].state].nonreflecting) {
+        b->nrg = (double *)dup_arr(NULL, sizeof(double) * 12 * (size_t)b->nc);
+        break;
+      }
     b->nplanes = v->nplanes;
     b->plane_off = (int32_t *)dup_arr(v->plane_offsets, 4 * (v->nplanes + 1));
     b->plane_cells = (int32_t *)dup_arr(v->plane_cells, 4 * (size_t)v->ni * v->nj * v->nk);
@@ -1331,7 +1431,7 @@ void orc_destroy(orc_case *c) {
     for (int d = 0; d < 3; ++d) free(b->fa[d]);
     free(b->W); free(b->R); free(b->dU); free(b->lam); free(b->dt); free(b->A);
     free(b->Un); free(b->Unm1);
-    free(b->nr); free(b->nr_mach);
+    free(b->nr); free(b->nr_mach); free(b->nrg);
     free(b->Ainv); free(b->mask); free(b->ops); free(b->plane_off); free(b->plane_cells);
     free(b->center); free(b->T); free(b->mu); free(b->corner);
     free(b->edge); free(b->vops); free(b->vedge);
@@ -1515,6 +1615,52 @@ void orc_fill_ghosts(orc_case *c) {
           const double sosInt = sos_of(in, &sv->gas);
           const double rhoSoSInt = in[0] * sosInt;
           g[4] = bs->p_out;
+          if (bs->nonreflecting) {
+            /* LODI relaxation with transverse terms (src/ghostStates.cpp:
+             * 612-638): time-n state, previous dt and gradients of the
+             * cell, average and largest normal Mach number of the surface */
+            double sN[NV];
+            cons_to_prim(&b->Un[op->src * 7], &sv->gas, sN);
+            const double dt = b->dt[op->src];
+            const double avgMach = b->nr_mach[2 * op->src2];
+            const double maxMach = b->nr_mach[2 * op->src2 + 1];
+            const double *vg = &b->nrg[op->src * 12], *pgr = &b->nrg[op->src * 12 + 9];
+            const double deltaVel =
+                (in[1] - sN[1]) * n[0] + (in[2] - sN[2]) * n[1] + (in[3] - sN[3]) * n[2];
+            const double sigma = 0.25;
+            const double sosN = sos_of(sN, &sv->gas);
+            const double rhoSoSN = sN[0] * sosN;
+            const double k = sigma * sosN * (1.0 - maxMach * maxMach) / bs->length_scale;
+            const double beta = avgMach;
+            const double pgn = pgr[0] * n[0] + pgr[1] * n[1] + pgr[2] * n[2];
+            double pgT[3], velT[3], gT[9], dVn[3];
+            const double vnN = sN[1] * n[0] + sN[2] * n[1] + sN[3] * n[2];
+            for (int e = 0; e < 3; ++e) {
+              pgT[e] = pgr[e] - pgn * n[e];
+              velT[e] = sN[1 + e] - vnN * n[e];
+            }
+            /* tensor::RemoveComponent, LinearCombination, Sum
+             * (include/tensor.hpp:371-389) */
+            for (int r = 0; r < 3; ++r) {
+              const double rn = vg[r * 3] * n[0] + vg[r * 3 + 1] * n[1] + vg[r * 3 + 2] * n[2];
+              for (int q = 0; q < 3; ++q) gT[r * 3 + q] = vg[r * 3 + q] - rn * n[q];
+            }
+            for (int q = 0; q < 3; ++q) {
+              dVn[q] = gT[q] * n[0];
+              dVn[q] += gT[3 + q] * n[1];
+              dVn[q] += gT[6 + q] * n[2];
+            }
+            double gsum = 0.0;
+            for (int e = 0; e < 9; ++e) gsum += gT[e];
+            const double dVelT = gsum - (((0.0 + dVn[0]) + dVn[1]) + dVn[2]);
+            const double gam = gamma_of(&sv->gas);
+            const double w0 = pgT[0] - rhoSoSN * dVn[0], w1 = pgT[1] - rhoSoSN * dVn[1],
+                         w2 = pgT[2] - rhoSoSN * dVn[2];
+            const double tr = -0.5 * ((velT[0] * w0 + velT[1] * w1 + velT[2] * w2) +
+                                      gam * sN[4] * dVelT);
+            g[4] = (sN[4] + rhoSoSN * deltaVel + dt * k * bs->p_out - dt * beta * tr) /
+                   (1.0 + dt * k);
+          }
           const double dp = in[4] - g[4];
           const double rho = in[0] - dp / (sosInt * sosInt);
           g[0] = rho * (in[0] / in[0]);
@@ -1819,6 +1965,7 @@ void orc_residual(orc_case *c) {
       }
       viscous_fluxes(c, b);
     }
+    if (b->nrg) nr_grads(c, b);
   }
   memset(c->forces, 0, sizeof(double) * 6 * c->ns);
   for (int bi = 0; bi < c->nb; ++bi)

@@ -52,7 +52,7 @@ def golden_case(name, outdir):
     base = name.split("_it")[0]
     gen = (cases.vortex_box if base.startswith("vortex")
            else cases.block_pair if base.startswith("pair_")
-           else cases.wall_channel if base.startswith("sst_chan")
+           else cases.wall_channel if base.startswith(("sst_chan", "chan_"))
            else cases.flat_plate if base.startswith(("plate", "sst")) else cases.bump_channel)
     inp, st = gen(outdir, name=base, **kw)
     return inp, st, g

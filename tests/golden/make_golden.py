@@ -111,6 +111,20 @@ CASES = [
     ("bump_nr_bdf2", cases.bump_channel,
      dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
           back_pressure=1.02, nonreflecting=0.5, time="bdf2", dt=2e-5, nl=3), [1, 12], True),
+    # nonreflecting pressure outlet (LODI with transverse terms from the
+    # previous residual's gradients): steady inviscid, with a nonreflecting
+    # inlet in bdf2 dual time, and a laminar viscous channel
+    ("bump_nr_out", cases.bump_channel,
+     dict(ni=18, nj=9, nk=3, height=0.06, mach=0.4, inflow="inlet", outflow="pressure",
+          back_pressure=1.02, nr_outlet=1.5), [1, 20], True),
+    ("bump_nr_both_bdf2", cases.bump_channel,
+     dict(ni=16, nj=8, nk=3, height=0.08, mach=0.5, inflow="inlet", outflow="pressure",
+          back_pressure=0.98, nonreflecting=0.5, nr_outlet=0.8, time="bdf2", dt=2e-5, nl=3),
+     [1, 8], True),
+    ("chan_nr_out_visc", cases.wall_channel,
+     dict(ni=16, nj=10, nk=2, kind="bump", param=0.06, mach=0.4, viscous=True, reynolds=5e4,
+          stretch=1.15, cfl=10.0, inflow="stagnation", outflow="pressure", nr_outlet=1.0),
+     [1, 10], True),
     ("plate_heatflux", cases.flat_plate,
      dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, wall_q=500.0), [1, 20], True),
     ("sst_chan_stag_pout", cases.wall_channel,

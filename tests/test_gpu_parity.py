@@ -71,7 +71,10 @@ def _cols_err(a, b):
                                   "bump_nr_bdf2_it1", "bump_nr_bdf2_it12", "plate_heatflux_it1",
                                   "plate_heatflux_it20", "vortex_bdf2_it1", "vortex_bdf2_it4",
                                   "vortex_cn_dual_it1", "vortex_cn_dual_it4",
-                                  "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4"])
+                                  "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
+                                  "bump_nr_out_it1", "bump_nr_out_it20", "bump_nr_both_bdf2_it1",
+                                  "bump_nr_both_bdf2_it8", "chan_nr_out_visc_it1",
+                                  "chan_nr_out_visc_it10"])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)

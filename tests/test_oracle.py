@@ -30,7 +30,9 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "bump_nr_bdf2_it12", "plate_heatflux_it1", "plate_heatflux_it20",
         "sst_chan_stag_pout_it1", "sst_chan_stag_pout_it10", "vortex_bdf2_it1", "vortex_bdf2_it4",
         "vortex_cn_dual_it1", "vortex_cn_dual_it4", "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
-        "sst_plate_bdf2_it1", "sst_plate_bdf2_it4"]
+        "sst_plate_bdf2_it1", "sst_plate_bdf2_it4", "bump_nr_out_it1", "bump_nr_out_it20",
+        "bump_nr_both_bdf2_it1", "bump_nr_both_bdf2_it8", "chan_nr_out_visc_it1",
+        "chan_nr_out_visc_it10"]
 
 
 def _oracle(inp, st):
