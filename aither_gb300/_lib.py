@@ -64,7 +64,14 @@ class SolveView(C.Structure):
                 ("k_c1", C.c_double), ("k_s", C.c_double), ("k_ref", C.c_double),
                 ("nstates", C.c_int32), ("states", C.POINTER(BCState)),
                 ("dt_global", C.c_double), ("dual_cfl", C.c_double),
-                ("nl_iters", C.c_int32), ("multilevel", C.c_int32)]
+                ("nl_iters", C.c_int32), ("multilevel", C.c_int32),
+                ("mg_levels", C.c_int32), ("mg_cycle", C.c_int32)]
+
+
+class MgMap(C.Structure):
+    _fields_ = [("coarse_block", C.c_int32), ("pad", C.c_int32), ("ncells", C.c_int64),
+                ("coarse_cell", C.POINTER(C.c_int32)), ("volfac", C.POINTER(C.c_double)),
+                ("coef", C.POINTER(C.c_double))]
 
 
 class BlockView(C.Structure):
@@ -148,6 +155,12 @@ def lib() -> C.CDLL:
             "ath_setup_block": (C.c_int, [vp, C.c_int, C.POINTER(BlockView)]),
             "ath_setup_solve": (C.c_int, [vp, C.c_int, C.POINTER(SolveView)]),
             "ath_setup_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
+            "ath_setup_levels": (C.c_int, [vp, C.POINTER(C.c_int)]),
+            "ath_setup_level_counts": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int),
+                                                 C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+            "ath_setup_level_block": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(BlockView)]),
+            "ath_setup_level_solve": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(SolveView)]),
+            "ath_setup_mg_map": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(MgMap)]),
             "ath_ctx_create": (C.c_int, [C.c_int, C.c_size_t, C.POINTER(vp)]),
             "ath_ctx_destroy": (C.c_int, [vp]),
             "ath_ctx_fp64_peak": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
@@ -352,15 +365,39 @@ class Setup:
         check(lib().ath_output_resid(self.h, solve, path.encode(), flags,
                                      first_step, len(norms), arr, dptr(resid_first)))
 
-    def block_view(self, b: int) -> BlockView:
+    def block_view(self, b: int, level: int = 0) -> BlockView:
         v = BlockView()
-        check(lib().ath_setup_block(self.h, b, C.byref(v)))
+        check(lib().ath_setup_level_block(self.h, level, b, C.byref(v)))
         return v
 
-    def solve_view(self, s: int) -> SolveView:
+    def solve_view(self, s: int, level: int = 0) -> SolveView:
         v = SolveView()
-        check(lib().ath_setup_solve(self.h, s, C.byref(v)))
+        check(lib().ath_setup_level_solve(self.h, level, s, C.byref(v)))
         return v
+
+    # ---- multigrid levels
+    def levels(self) -> int:
+        n = C.c_int()
+        check(lib().ath_setup_levels(self.h, C.byref(n)))
+        return n.value
+
+    def level_counts(self, level: int):
+        ns, nb, nc = C.c_int(), C.c_int(), C.c_int64()
+        check(lib().ath_setup_level_counts(self.h, level, C.byref(ns), C.byref(nb),
+                                           C.byref(nc)))
+        return ns.value, nb.value, nc.value
+
+    def mg_map(self, level: int, b: int) -> dict:
+        """Transfer of block b of `level` to the next coarser level: the
+        coarse block, and per fine physical cell (k, j, i order) its coarse
+        cell, restriction weight and 7 prolongation coefficients."""
+        m = MgMap()
+        check(lib().ath_setup_mg_map(self.h, level, b, C.byref(m)))
+        n = m.ncells
+        return {"coarse_block": m.coarse_block,
+                "coarse_cell": np.ctypeslib.as_array(m.coarse_cell, (n,)).copy(),
+                "volfac": np.ctypeslib.as_array(m.volfac, (n,)).copy(),
+                "coef": np.ctypeslib.as_array(m.coef, (n, 7)).copy()}
 
     def set_state(self, b: int, prim: np.ndarray) -> None:
         prim = np.ascontiguousarray(prim, dtype=np.float64)

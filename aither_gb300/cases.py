@@ -134,6 +134,9 @@ def write_input(path: str, grid: str, scheme: dict, refs: Refs, ic: str,
         f"matrixSweeps: {int(scheme.get('matrixSweeps', 1))}",
         "matrixRelaxation: 1.0",
     ]
+    for key in ("multigridLevels", "multigridCycle"):
+        if key in scheme:
+            body.append(f"{key}: {scheme[key]}")
     for key in ("timeStep", "nonlinearIterations", "dualTimeCFL"):
         if key in scheme:
             body.append(f"{key}: {_fmt(scheme[key]) if isinstance(scheme[key], float) else scheme[key]}")
@@ -176,6 +179,13 @@ def nondimensional_prim(rho, u, v, w, p, refs: Refs) -> np.ndarray:
     """Reference nondimensionalisation (src/inputStates.cpp:464-473)."""
     a = refs.a_ref
     return np.stack([rho / refs.r_ref, u / a, v / a, w / a, p / (refs.r_ref * a * a)], axis=-1)
+
+
+def multigrid_keys(multigrid: tuple | None) -> dict:
+    """multigridLevels / multigridCycle input keys from (levels, "V"|"W")."""
+    if not multigrid:
+        return {}
+    return {"multigridLevels": int(multigrid[0]), "multigridCycle": multigrid[1]}
 
 
 def time_keys(time: str = "implicitEuler", dt: float | None = None, nl: int = 1,
@@ -243,8 +253,10 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
                  sweeps: int = 1, inflow: str = "characteristic",
                  outflow: str = "characteristic", back_pressure: float = 1.0,
                  nonreflecting: float | None = None, time: str = "implicitEuler",
-                 dt: float | None = None, nl: int = 1, nr_outlet: float | None = None):
-    """Inviscid channel over a sin^2 bump.  `nonreflecting` (a length in
+                 dt: float | None = None, nl: int = 1, nr_outlet: float | None = None,
+                 multigrid: tuple | None = None):
+    """Inviscid channel over a sin^2 bump.  `multigrid` = (levels, cycle
+    "V" or "W") adds the multigrid keys.  `nonreflecting` (a length in
     metres) makes the inlet nonreflecting with that lengthScale, `nr_outlet`
     the pressure outlet; time, dt and nl select the time integration.    Inflow at i = 0 and outflow at
     i = ni are characteristic far fields, or (inflow "stagnation") a
@@ -288,7 +300,8 @@ def bump_channel(outdir: str, ni: int, nj: int, nk: int, height: float, mach: fl
     inp = os.path.join(outdir, name + ".inp")
     write_input(inp, name, {"cfl": cfl, "limiter": limiter, "faceReconstruction": recon,
                             "inviscidFlux": flux, "matrixSolver": matrix_solver,
-                            "matrixSweeps": sweeps, **time_keys(time, dt, nl)},
+                            "matrixSweeps": sweeps, **time_keys(time, dt, nl),
+                            **multigrid_keys(multigrid)},
                 refs, ic, states, bcs)
     return inp, None
 
@@ -452,7 +465,8 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                flux: str = "roe", nblocks: int = 2, dy_max: float | None = None,
                lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0,
                wall_q: float | None = None, time: str = "implicitEuler",
-               dt: float | None = None, nl: int = 1, dual_cfl: float | None = None):
+               dt: float | None = None, nl: int = 1, dual_cfl: float | None = None,
+               multigrid: tuple | None = None):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -498,7 +512,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
               "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
               "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
               "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps,
-              **time_keys(time, dt, nl, dual_cfl)}
+              **time_keys(time, dt, nl, dual_cfl), **multigrid_keys(multigrid)}
     if nblocks == 1:
         nodes = plate_nodes(-lead, length, ni, nj, nk, dy0, ratio, dz, dy_max)
         write_plot3d(os.path.join(outdir, name + ".xyz"), [nodes])

@@ -176,6 +176,7 @@ struct BatchCore {
   int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
   int vkinds = 0;  // bit 0: laminar viscous solves, bit 1: SST
   cudaStream_t stream = nullptr;
+  bool own_stream = true;  // false: a multigrid level on its finest batch's stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::unique_ptr<DevMem> mem;
   // device lists
@@ -334,6 +335,16 @@ __global__ void k_wallsum(const double *wbuf, int nfaces, const int32_t *solve_f
   }
 }
 
+// A coarse multigrid level follows its finest level's solves: the same
+// CFL (input::CalcCFL of the iteration) and the same active flags
+__global__ void k_mg_sync(const SolveDev *fine, const double *fine_cfl, SolveDev *coarse,
+                          double *coarse_cfl, int nsolves) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsolves) return;
+  coarse_cfl[s] = fine_cfl[s];
+  coarse[s].active = fine[s].active;
+}
+
 // ---------------------------------------------------------------------------
 class RunnerBase {
  public:
@@ -384,9 +395,11 @@ class Runner : public RunnerBase {
     }
     P_.lam = m.Alloc<double>(n);
     P_.dt = m.Alloc<double>(n);
-    c_.mem->Zero(P_.dt, 0, n * sizeof(double));
     c_.mem->Zero(P_.R, 0, 5 * n * sizeof(double));
     c_.mem->Zero(P_.lam, 0, n * sizeof(double));
+    // the nonreflecting boundaries' LODI relaxation of the first iteration
+    // reads the time step before any has been formed: zero, as the
+    // reference's zero-initialised per-cell time step
     c_.mem->Zero(P_.dt, 0, n * sizeof(double));
     // hyperplane-ordered sweep working set
     const int64_t nq = c.nq, ngh = (int64_t)c.L.ghost_cell.size();
@@ -735,7 +748,111 @@ class Runner : public RunnerBase {
       }
     }
   }
+  // ---- multigrid (mgSolution::CycleAtLevel, src/mgSolution.cpp:160-207)
+  // this batch is the finest level; mg_lv_[l] is level l's runner (its own
+  // batch on this batch's stream), mg_link_[l] the transfer from level l to
+  // l+1, with its coarse level's saved update and node buffer
+  void MgAddLevel(Runner<T> *coarse, const MgLinkDev &link, T *du0, T *nodes) {
+    if (mg_lv_.empty()) mg_lv_.push_back(this);
+    mg_lv_.push_back(coarse);
+    mg_link_.push_back(link);
+    mg_du0_.push_back(du0);
+    mg_nodes_.push_back(nodes);
+  }
+  void MgSetup(int cycle, int sweeps) {
+    mg_cycle_ = cycle;
+    mg_sweeps_ = sweeps;
+  }
+  Pools<T> &MutablePools() { return P_; }
+  BatchCore &Core() { return c_; }
+  // a coarse level's ghost fill (the CFL is the finest level's, copied)
+  void LevelGhosts() {
+    Launch<T>::Ghost(P_, c_.d_ops, (int)c_.L.ops.size(), c_.d_op_solve, c_.stream);
+    EdgePhases(c_.d_edge_ops, c_.d_edge_solve, c_.L.edge_phase_off);
+  }
+  // Relax of one level with n sweeps from its current update (lusgs / dplur
+  // ::Relax, src/linearSolver.cpp:430,501), ending with the ghost swap and
+  // the per-cell matrix residual f - (A x - b) into MRq
+  void RelaxN(int n) {
+    if (c_.jkinds) {
+      const int ni = (int)c_.L.sweep_items.size();
+      Pools<T> other = P_;
+      other.dUq = P_.dUq2;
+      other.dUtq = P_.dUtq2;
+      for (int sw = 0; sw < n; ++sw) {
+        const bool even = sw % 2 == 0;
+        const Pools<T> &src = even ? P_ : other;
+        Launch<T>::ConnDu(src, c_.stream);
+        Launch<T>::Jacobi(src, even ? P_.dUq2 : P_.dUq, even ? P_.dUtq2 : P_.dUtq, c_.d_sweep, ni,
+                          sw, c_.jkinds, c_.stream);
+      }
+      if (n % 2 == 1) Launch<T>::JacobiCopy(P_, P_.dUq2, P_.dUtq2, c_.d_sweep, ni, c_.stream);
+    }
+    if (c_.skinds) {
+      for (int sw = 0; sw < n; ++sw) {
+        Launch<T>::ConnDu(P_, c_.stream);
+        SweepPass(1, sw);
+        Launch<T>::ConnDu(P_, c_.stream);
+        SweepPass(0, sw);
+      }
+    }
+    Launch<T>::ConnDu(P_, c_.stream);
+    Launch<T>::MatRes(P_, c_.d_cells, c_.d_cell_cta_block, c_.d_mres,
+                      (int)c_.L.cell_cta_block.size(), c_.kinds, c_.stream);
+  }
+  void MgCycle(int l) {
+    Runner<T> &R = *mg_lv_[l];
+    if (l + 1 == (int)mg_lv_.size()) {
+      R.RelaxN(mg_sweeps_);
+      return;
+    }
+    const int half = std::max(mg_sweeps_ / 2, 1);
+    R.RelaxN(half);
+    Runner<T> &C = *mg_lv_[l + 1];
+    Pools<T> &CP = C.MutablePools();
+    BatchCore &cc = C.Core();
+    const MgLinkDev &k = mg_link_[l];
+    cudaStream_t s = c_.stream;
+    // gridLevel::Restriction (src/gridLevel.cpp:538): the state (into a
+    // zeroed pool, ghosts refilled), the coarse residual, time step and
+    // diagonal from it, the update with its ghost swap, and the forcing
+    Check(cudaMemsetAsync(CP.W, 0, 5 * (size_t)CP.ncell * sizeof(double), s), "memset");
+    Launch<T>::MgRestrictState(k, R.P_.W, R.P_.ncell, CP.W, CP.ncell, s);
+    k_mg_sync<<<(cc.nsolves + 127) / 128, 128, 0, s>>>(c_.d_solves, c_.d_cfl, cc.d_solves,
+                                                       cc.d_cfl, cc.nsolves);
+    CP.mg_accum = ++mg_visits_[l + 1] > 1 ? 1 : 0;
+    C.LevelGhosts();
+    C.Residual();
+    Launch<T>::MgRestrictQ(k, R.P_.dUq, R.P_.nq, CP.dUq, CP.nq, true, s);
+    Launch<T>::ConnDu(CP, s);
+    Launch<T>::MgRestrictQ(k, R.P_.MRq, R.P_.nq, CP.Fq, CP.nq, false, s);
+    Launch<T>::MgForcing(CP, cc.d_cells, cc.d_cell_cta_block, (int)cc.L.cell_cta_block.size(),
+                         cc.kinds, s);
+    T *du0 = mg_du0_[l];
+    Check(cudaMemcpyAsync(du0, CP.dUq, 5 * (size_t)CP.nq * sizeof(T), cudaMemcpyDeviceToDevice,
+                          s),
+          "copy");
+    for (int n = 0; n < mg_cycle_; ++n) MgCycle(l + 1);
+    Launch<T>::MgSubtract(CP.dUq, du0, CP.nq, s);
+    Launch<T>::MgProlong(k, CP.dUq, CP.nq, mg_nodes_[l], R.P_.dUq, R.P_.nq, s);
+    R.RelaxN(half);
+  }
+  // the finest level's relaxation with the coarse-grid corrections:
+  // InitializeMatrixUpdate (A^-1 b or zero), then the cycle
+  void MgRelax() {
+    const int ni = (int)c_.L.sweep_items.size();
+    if (c_.jkinds) Launch<T>::Init(P_, c_.d_sweep, ni, 1, c_.stream);
+    if (c_.skinds) Launch<T>::Init(P_, c_.d_sweep, ni, 0, c_.stream);
+    mg_visits_.assign(mg_lv_.size(), 0);
+    MgCycle(0);
+  }
+  bool Multigrid() const { return !mg_lv_.empty(); }
+
   void Relax() override {
+    if (Multigrid()) {
+      MgRelax();
+      return;
+    }
     if (c_.jkinds) JacobiPhase();
     if (c_.skinds) SweepPhase();
     if (c_.flags & 1) {
@@ -767,6 +884,18 @@ class Runner : public RunnerBase {
             "begin capture");
       OneIteration();
       Check(cudaStreamEndCapture(c_.stream, &g), "end capture");
+      // kernel launches of one iteration: the captured graph's kernel nodes
+      size_t nn = 0;
+      Check(cudaGraphGetNodes(g, nullptr, &nn), "graph nodes");
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (nn) Check(cudaGraphGetNodes(g, nodes.data(), &nn), "graph nodes");
+      int64_t kernels = 0;
+      for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        Check(cudaGraphNodeGetType(nd, &t), "graph node type");
+        kernels += t == cudaGraphNodeTypeKernel;
+      }
+      c_.launches_per_iter = kernels;
       Check(cudaGraphInstantiate(&c_.graph, g, 0), "graph instantiate");
       cudaGraphDestroy(g);
     }
@@ -796,7 +925,14 @@ class Runner : public RunnerBase {
       // split of a multi-sweep relaxation puts each sweep's passes in turn);
       // DP-LUR sweeps count as forward passes
       float fwd = 0.f, bwd = 0.f;
-      if (c_.jkinds) {
+      if (Multigrid()) {
+        // the whole multigrid cycle counts as the forward passes
+        Check(cudaEventRecord(e[6], c_.stream), "event");
+        MgRelax();
+        Check(cudaEventRecord(e[7], c_.stream), "event");
+        Check(cudaEventSynchronize(e[7]), "sync");
+        Check(cudaEventElapsedTime(&fwd, e[6], e[7]), "elapsed");
+      } else if (c_.jkinds) {
         Check(cudaEventRecord(e[6], c_.stream), "event");
         JacobiPhase();
         Check(cudaEventRecord(e[7], c_.stream), "event");
@@ -805,11 +941,12 @@ class Runner : public RunnerBase {
         Check(cudaEventElapsedTime(&tj, e[6], e[7]), "elapsed");
         fwd += tj;
       }
-      if (c_.skinds && c_.max_sweeps > 1)
+      const bool lusgs = c_.skinds && !Multigrid();
+      if (lusgs && c_.max_sweeps > 1)
         Launch<T>::Init(P_, c_.d_sweep, (int)c_.L.sweep_items.size(), 0, c_.stream);
-      else if (c_.skinds)
+      else if (lusgs)
         ZeroGhostUpdates();
-      for (int sw = 0; sw < (c_.skinds ? c_.max_sweeps : 0); ++sw) {
+      for (int sw = 0; sw < (lusgs ? c_.max_sweeps : 0); ++sw) {
         if (c_.max_sweeps > 1) Launch<T>::ConnDu(P_, c_.stream);
         Check(cudaEventRecord(e[6], c_.stream), "event");
         SweepPass(1, sw);
@@ -1005,6 +1142,11 @@ class Runner : public RunnerBase {
   }
 
   BatchCore &c_;
+  std::vector<Runner<T> *> mg_lv_;
+  std::vector<MgLinkDev> mg_link_;
+  std::vector<T *> mg_du0_, mg_nodes_;
+  std::vector<int> mg_visits_;
+  int mg_cycle_ = 1, mg_sweeps_ = 1;
   Pools<T> P_{};
   double *snap_w_ = nullptr, *snap_wt_ = nullptr, *snap_un_ = nullptr, *snap_cfl_ = nullptr;
   SolveState *snap_ss_ = nullptr;
@@ -1017,6 +1159,9 @@ class Runner : public RunnerBase {
 struct ath_batch {
   ath::BatchCore core;
   std::unique_ptr<ath::RunnerBase> run;
+  // coarser multigrid levels: batches of their own on this batch's stream,
+  // driven by this batch's relaxation
+  std::vector<ath_batch *> levels;
   double *W = nullptr, *R = nullptr, *dt = nullptr, *lam = nullptr;
   double *Wt = nullptr, *Rt = nullptr, *lamt = nullptr;  // RANS solves only
   double *Un = nullptr, *Unm1 = nullptr;  // time-accurate solves only
@@ -1432,7 +1577,180 @@ void CountLaunches(BatchCore &c) {
                         ((c.flags & 1) ? nkinds + conn : 0);
 }
 
-void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags) {
+void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags,
+                 cudaStream_t shared = nullptr);
+
+// Releases a batch and its multigrid levels (also a partly built one).
+void DestroyBatch(ath_batch *batch) {
+  if (!batch) return;
+  if (batch->core.ctx) cudaSetDevice(batch->core.ctx->device);
+  if (batch->core.stream) cudaStreamSynchronize(batch->core.stream);
+  for (auto *lv : batch->levels) DestroyBatch(lv);
+  batch->levels.clear();
+  batch->run.reset();
+  batch->core.mem.reset();
+  if (batch->core.ev0) cudaEventDestroy(batch->core.ev0);
+  if (batch->core.ev1) cudaEventDestroy(batch->core.ev1);
+  if (batch->core.stream && batch->core.own_stream) cudaStreamDestroy(batch->core.stream);
+  delete batch;
+}
+
+// Transfer tables between level fine (setup sf, batch cf) and the next
+// coarser level (sc, cc), in pool and q indices of the two batches
+MgLinkDev BuildMgLink(const Setup &sf, const BatchCore &cf, const Setup &sc,
+                      const BatchCore &cc, DevMem &m) {
+  const int64_t ncq = cc.nq;
+  std::vector<std::vector<int32_t>> members(ncq);  // fine gather entries per coarse q
+  std::vector<int32_t> f_pool, f_q;
+  std::vector<double> f_w;
+  std::vector<int32_t> p_q, p_node0, p_sx, p_sxy;
+  std::vector<double> coef;
+  // nodes of the coarse blocks, block by block
+  std::vector<int64_t> node0(sc.blocks.size() + 1, 0);
+  for (size_t b = 0; b < sc.blocks.size(); ++b) {
+    const Block &k = sc.blocks[b];
+    node0[b + 1] = node0[b] + (int64_t)(k.ni + 1) * (k.nj + 1) * (k.nk + 1);
+  }
+  const int64_t nnode = node0.back();
+  for (size_t bi = 0; bi < sf.blocks.size(); ++bi) {
+    const Block &fb = sf.blocks[bi];
+    if (fb.mg_coarse < 0) throw Error(ATH_ERR_UNSUPPORTED, "block without a coarser level");
+    const Block &cb = sc.blocks[fb.mg_coarse];
+    int64_t x = 0;
+    for (int k = 0; k < fb.nk; ++k)
+      for (int j = 0; j < fb.nj; ++j)
+        for (int i = 0; i < fb.ni; ++i, ++x) {
+          const int64_t fp = cf.cell0[bi] + fb.Cell(i, j, k);
+          const int cci = fb.mg_cell[x];
+          const int ci = cci % cb.ni, cj = (cci / cb.ni) % cb.nj, ck = cci / (cb.ni * cb.nj);
+          const int64_t cp = cc.cell0[fb.mg_coarse] + cb.Cell(ci, cj, ck);
+          const int32_t fq = cf.L.qpos[fp], cq = cc.L.qpos[cp];
+          members[cq].push_back((int32_t)f_pool.size());
+          f_pool.push_back((int32_t)fp);
+          f_q.push_back(fq);
+          f_w.push_back(fb.mg_volfac[x]);
+          p_q.push_back(fq);
+          p_node0.push_back((int32_t)(node0[fb.mg_coarse] + ci +
+                                      (int64_t)(cb.ni + 1) * (cj + (int64_t)(cb.nj + 1) * ck)));
+          p_sx.push_back(cb.ni + 1);
+          p_sxy.push_back((cb.ni + 1) * (cb.nj + 1));
+        }
+  }
+  const int64_t nf = (int64_t)f_pool.size();
+  // prolongation coefficients [7][nfine], fine cells in the same order
+  coef.assign(7 * nf, 0.0);
+  {
+    int64_t e = 0;
+    for (size_t bi = 0; bi < sf.blocks.size(); ++bi) {
+      const Block &fb = sf.blocks[bi];
+      const int64_t n = (int64_t)fb.ni * fb.nj * fb.nk;
+      for (int64_t x = 0; x < n; ++x, ++e)
+        for (int a = 0; a < 7; ++a) coef[a * nf + e] = fb.mg_coef[7 * x + a];
+    }
+  }
+  // gather lists in coarse q order; each coarse cell's entries in the fine
+  // cells' k, j, i order
+  std::vector<int32_t> off(ncq + 1, 0), c_pool(ncq, -1), c_q(ncq), gp, gq;
+  std::vector<double> gw;
+  for (int64_t q = 0; q < ncq; ++q) {
+    off[q + 1] = off[q] + (int32_t)members[q].size();
+    c_q[q] = (int32_t)q;
+    for (int32_t e : members[q]) {
+      gp.push_back(f_pool[e]);
+      gq.push_back(f_q[e]);
+      gw.push_back(f_w[e]);
+    }
+  }
+  for (int64_t p = 0; p < cc.ncell; ++p)
+    if (cc.L.qpos[p] >= 0) c_pool[cc.L.qpos[p]] = (int32_t)p;
+  // node sums: the cells around each node in the cell loop's k, j, i order
+  std::vector<int32_t> node_cells(8 * nnode, -1);
+  std::vector<double> node_fac(nnode, 0.125);
+  for (size_t b = 0; b < sc.blocks.size(); ++b) {
+    const Block &k = sc.blocks[b];
+    for (int nk = 0; nk <= k.nk; ++nk)
+      for (int nj = 0; nj <= k.nj; ++nj)
+        for (int ni = 0; ni <= k.ni; ++ni) {
+          const int64_t nd =
+              node0[b] + ni + (int64_t)(k.ni + 1) * (nj + (int64_t)(k.nj + 1) * nk);
+          int e = 0;
+          for (int dk = -1; dk <= 0; ++dk)
+            for (int dj = -1; dj <= 0; ++dj)
+              for (int di = -1; di <= 0; ++di, ++e) {
+                const int ci = ni + di, cj = nj + dj, ck = nk + dk;
+                if (ci < 0 || cj < 0 || ck < 0 || ci >= k.ni || cj >= k.nj || ck >= k.nk) continue;
+                node_cells[8 * nd + e] = cc.L.qpos[cc.cell0[b] + k.Cell(ci, cj, ck)];
+              }
+          const int ei = ni == 0 || ni == k.ni, ej = nj == 0 || nj == k.nj,
+                    ek = nk == 0 || nk == k.nk;
+          node_fac[nd] = (ei && ej && ek) ? 1.0 : (ei + ej + ek == 2) ? 0.5 : 0.125;
+        }
+  }
+  MgLinkDev d{};
+  d.ncoarse = (int)ncq;
+  d.nfine = (int)nf;
+  d.nnode = (int)nnode;
+  d.off = m.Upload(off);
+  d.c_pool = m.Upload(c_pool);
+  d.c_q = m.Upload(c_q);
+  d.f_pool = m.Upload(gp);
+  d.f_q = m.Upload(gq);
+  d.f_w = m.Upload(gw);
+  d.node_cells = m.Upload(node_cells);
+  d.node_fac = m.Upload(node_fac);
+  d.p_q = m.Upload(p_q);
+  d.p_node0 = m.Upload(p_node0);
+  d.p_sx = m.Upload(p_sx);
+  d.p_sxy = m.Upload(p_sxy);
+  d.p_coef = m.Upload(coef);
+  return d;
+}
+
+// The coarser levels of a multigrid batch: every solve has the same levels,
+// cycle and sweeps (one relaxation schedule for the batch)
+template <typename T>
+void WireMultigrid(ath_batch *B, const Setup &st) {
+  BatchCore &c = B->core;
+  const int nl = st.solves[0].phys.mg_levels;
+  for (const auto &sv : st.solves)
+    if (sv.phys.mg_levels != nl || sv.phys.mg_cycle != st.solves[0].phys.mg_cycle ||
+        sv.phys.sweeps != st.solves[0].phys.sweeps ||
+        sv.phys.solver != st.solves[0].phys.solver)
+      throw Error(ATH_ERR_UNSUPPORTED,
+                  "a multigrid batch needs the same multigrid levels, cycle, matrix solver and "
+                  "sweeps in every solve");
+  if ((int)st.levels.size() < nl - 1) throw Error(ATH_ERR_UNSUPPORTED, "multigrid levels missing");
+  auto *fine = static_cast<Runner<T> *>(B->run.get());
+  const int64_t nqf = c.nq;
+  fine->MutablePools().MRq = c.mem->Alloc<T>(5 * (size_t)nqf);
+  fine->MgSetup(st.solves[0].phys.mg_cycle, st.solves[0].phys.sweeps);
+  const Setup *sf = &st;
+  ath_batch *fb = B;
+  for (int l = 1; l < nl; ++l) {
+    const Setup &sc = *st.levels[l - 1];
+    if (sc.solves.size() != st.solves.size())
+      throw Error(ATH_ERR_UNSUPPORTED, "multigrid levels differ between the batch's solves");
+    auto *lb = new ath_batch();
+    B->levels.push_back(lb);
+    CreateBatch(lb, c.ctx, sc, c.precision, c.flags, c.stream);
+    auto *cr = static_cast<Runner<T> *>(lb->run.get());
+    BatchCore &cc = lb->core;
+    Pools<T> &cp = cr->MutablePools();
+    cp.Fq = cc.mem->Alloc<T>(5 * (size_t)cc.nq);
+    cp.MRq = cc.mem->Alloc<T>(5 * (size_t)cc.nq);
+    cc.mem->Zero(cp.Fq, 0, 5 * (size_t)cc.nq * sizeof(T));
+    const MgLinkDev link = BuildMgLink(*sf, fb->core, sc, cc, *c.mem);
+    T *du0 = c.mem->Alloc<T>(5 * (size_t)cc.nq);
+    T *nodes = c.mem->Alloc<T>(5 * (size_t)std::max(link.nnode, 1));
+    fine->MgAddLevel(cr, link, du0, nodes);
+    sf = &sc;
+    fb = lb;
+  }
+  Check(cudaStreamSynchronize(c.stream), "sync");
+}
+
+void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int flags,
+                 cudaStream_t shared) {
   auto &c = B->core;
   c.ctx = ctx;
   c.setup = &st;
@@ -1463,7 +1781,12 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   }
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");
   BuildLists(c);
-  Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  if (shared) {
+    c.stream = shared;
+    c.own_stream = false;
+  } else {
+    Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
+  }
   c.mem.reset(new DevMem(ctx, c.stream));
   DevMem &m = *c.mem;
   std::vector<BlockDev> bd(c.nblocks);
@@ -1611,6 +1934,16 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
+  // multigrid: the coarser levels (only the finest batch builds them)
+  if (!shared && !st.solves.empty() && st.solves[0].phys.mg_levels > 1) {
+    if (precision == ATH_PREC_FP64) WireMultigrid<double>(B, st);
+    else WireMultigrid<float>(B, st);
+  } else if (!shared) {
+    for (const auto &sv : st.solves)
+      if (sv.phys.mg_levels > 1)
+        throw Error(ATH_ERR_UNSUPPORTED,
+                    "a multigrid batch needs the same multigrid levels in every solve");
+  }
   // resident CTAs of the tile-queue sweep kernels (one wave of persistent
   // CTAs; more would only wait for tickets)
   if (c.skinds) {
@@ -1753,7 +2086,7 @@ int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision, int fl
     try {
       ath::CreateBatch(b, ctx, setup->s, precision, flags);
     } catch (...) {
-      delete b;
+      ath::DestroyBatch(b);
       throw;
     }
     *out = b;
@@ -1761,15 +2094,7 @@ int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision, int fl
 }
 
 int ath_batch_destroy(ath_batch *batch) {
-  if (!batch) return ATH_OK;
-  cudaSetDevice(batch->core.ctx->device);
-  if (batch->core.stream) cudaStreamSynchronize(batch->core.stream);
-  batch->run.reset();
-  batch->core.mem.reset();
-  if (batch->core.ev0) cudaEventDestroy(batch->core.ev0);
-  if (batch->core.ev1) cudaEventDestroy(batch->core.ev1);
-  if (batch->core.stream) cudaStreamDestroy(batch->core.stream);
-  delete batch;
+  ath::DestroyBatch(batch);
   return ATH_OK;
 }
 
@@ -2289,28 +2614,42 @@ int ath_ctx_fp64_peak(ath_ctx *ctx, int reps, double *tflops) {
     Check(cudaSetDevice(ctx->device), "cudaSetDevice");
     int sms = 0;
     Check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "attr");
-    double *sink = nullptr;
-    Check(cudaMalloc(&sink, sizeof(double)), "cudaMalloc");
-    cudaEvent_t e0, e1;
-    Check(cudaEventCreate(&e0), "event");
-    Check(cudaEventCreate(&e1), "event");
+    // owned resources released on every path; a private non-blocking stream
+    // so the measurement does not serialise with batches on other streams
+    struct Res {
+      cudaStream_t s = nullptr;
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      double *sink = nullptr;
+      ~Res() {
+        if (s) cudaStreamSynchronize(s);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (sink) cudaFreeAsync(sink, s);
+        if (s) {
+          cudaStreamSynchronize(s);
+          cudaStreamDestroy(s);
+        }
+      }
+    } r;
+    Check(cudaStreamCreateWithFlags(&r.s, cudaStreamNonBlocking), "stream");
+    Check(cudaEventCreate(&r.e0), "event");
+    Check(cudaEventCreate(&r.e1), "event");
+    Check(cudaMallocAsync(&r.sink, sizeof(double), r.s), "cudaMallocAsync");
     const int blocks = sms * 8, threads = 256, iters = 4096;
-    k_fp64_peak<<<blocks, threads>>>(1.0, iters, sink);  // warm-up
+    k_fp64_peak<<<blocks, threads, 0, r.s>>>(1.0, iters, r.sink);  // warm-up
+    Check(cudaGetLastError(), "kernel launch");
     double best = 0.0;
-    for (int r = 0; r < reps; ++r) {
-      Check(cudaEventRecord(e0), "event");
-      k_fp64_peak<<<blocks, threads>>>(1.0 + r, iters, sink);
-      Check(cudaEventRecord(e1), "event");
-      Check(cudaEventSynchronize(e1), "sync");
+    for (int k = 0; k < reps; ++k) {
+      Check(cudaEventRecord(r.e0, r.s), "event");
+      k_fp64_peak<<<blocks, threads, 0, r.s>>>(1.0 + k, iters, r.sink);
+      Check(cudaGetLastError(), "kernel launch");
+      Check(cudaEventRecord(r.e1, r.s), "event");
+      Check(cudaEventSynchronize(r.e1), "sync");
       float ms = 0.f;
-      Check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+      Check(cudaEventElapsedTime(&ms, r.e0, r.e1), "elapsed");
       const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
       best = std::max(best, flops / (ms * 1e-3) / 1e12);
     }
-    Check(cudaGetLastError(), "kernel launch");
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(sink);
     *tflops = best;
   });
 }

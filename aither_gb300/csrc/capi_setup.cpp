@@ -18,6 +18,16 @@ const char *LastError() { return g_last_error.c_str(); }
 
 using ath::Guard;
 
+namespace {
+// level 0 is the setup itself, level l > 0 its l-th coarser multigrid level
+const ath::Setup &LevelOf(const ath_setup *setup, int level) {
+  if (!setup) throw ath::Error(ATH_ERR_ARG, "null setup");
+  if (level < 0 || level > (int)setup->s.levels.size())
+    throw ath::Error(ATH_ERR_ARG, "multigrid level out of range");
+  return level == 0 ? setup->s : *setup->s.levels[level - 1];
+}
+}  // namespace
+
 extern "C" {
 
 const char *ath_last_error(void) { return ath::LastError(); }
@@ -63,26 +73,27 @@ int ath_setup_destroy(ath_setup *setup) {
   return ATH_OK;
 }
 
-int ath_setup_counts(const ath_setup *setup, int *nsolves, int *nblocks,
-                     int64_t *ncells) {
+int ath_setup_level_counts(const ath_setup *setup, int level, int *nsolves, int *nblocks,
+                           int64_t *ncells) {
   return Guard([&] {
-    if (!setup) throw ath::Error(ATH_ERR_ARG, "null setup");
-    if (nsolves) *nsolves = (int)setup->s.solves.size();
-    if (nblocks) *nblocks = (int)setup->s.blocks.size();
+    const ath::Setup &st = LevelOf(setup, level);
+    if (nsolves) *nsolves = (int)st.solves.size();
+    if (nblocks) *nblocks = (int)st.blocks.size();
     if (ncells) {
       int64_t n = 0;
-      for (auto &b : setup->s.blocks) n += (int64_t)b.ni * b.nj * b.nk;
+      for (auto &b : st.blocks) n += (int64_t)b.ni * b.nj * b.nk;
       *ncells = n;
     }
   });
 }
 
-int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out) {
+int ath_setup_level_block(const ath_setup *setup, int level, int block, ath_block_view *out) {
   return Guard([&] {
-    if (!setup || !out) throw ath::Error(ATH_ERR_ARG, "null argument");
-    if (block < 0 || block >= (int)setup->s.blocks.size())
+    const ath::Setup &st = LevelOf(setup, level);
+    if (!out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    if (block < 0 || block >= (int)st.blocks.size())
       throw ath::Error(ATH_ERR_ARG, "block index out of range");
-    const auto &b = setup->s.blocks[block];
+    const auto &b = st.blocks[block];
     std::memset(out, 0, sizeof(*out));
     out->ni = b.ni;
     out->nj = b.nj;
@@ -117,15 +128,51 @@ int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out) {
   });
 }
 
-int ath_setup_solve(const ath_setup *setup, int solve, ath_solve_view *out) {
+int ath_setup_level_solve(const ath_setup *setup, int level, int solve, ath_solve_view *out) {
   return Guard([&] {
-    if (!setup || !out) throw ath::Error(ATH_ERR_ARG, "null argument");
-    if (solve < 0 || solve >= (int)setup->s.solves.size())
+    const ath::Setup &st = LevelOf(setup, level);
+    if (!out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    if (solve < 0 || solve >= (int)st.solves.size())
       throw ath::Error(ATH_ERR_ARG, "solve index out of range");
-    const auto &sv = setup->s.solves[solve];
+    const auto &sv = st.solves[solve];
     *out = sv.phys;
     out->nstates = (int32_t)sv.states.size();
     out->states = sv.states.data();
+  });
+}
+
+int ath_setup_counts(const ath_setup *setup, int *nsolves, int *nblocks, int64_t *ncells) {
+  return ath_setup_level_counts(setup, 0, nsolves, nblocks, ncells);
+}
+
+int ath_setup_block(const ath_setup *setup, int block, ath_block_view *out) {
+  return ath_setup_level_block(setup, 0, block, out);
+}
+
+int ath_setup_solve(const ath_setup *setup, int solve, ath_solve_view *out) {
+  return ath_setup_level_solve(setup, 0, solve, out);
+}
+
+int ath_setup_levels(const ath_setup *setup, int *nlevels) {
+  return Guard([&] {
+    if (!setup || !nlevels) throw ath::Error(ATH_ERR_ARG, "null argument");
+    *nlevels = 1 + (int)setup->s.levels.size();
+  });
+}
+
+int ath_setup_mg_map(const ath_setup *setup, int level, int block, ath_mg_map *out) {
+  return Guard([&] {
+    const ath::Setup &st = LevelOf(setup, level);
+    if (!out) throw ath::Error(ATH_ERR_ARG, "null argument");
+    if (block < 0 || block >= (int)st.blocks.size())
+      throw ath::Error(ATH_ERR_ARG, "block index out of range");
+    const auto &b = st.blocks[block];
+    if (b.mg_coarse < 0) throw ath::Error(ATH_ERR_ARG, "block has no coarser level");
+    out->coarse_block = b.mg_coarse;
+    out->ncells = (int64_t)b.ni * b.nj * b.nk;
+    out->coarse_cell = b.mg_cell.data();
+    out->volfac = b.mg_volfac.data();
+    out->coef = b.mg_coef.data();
   });
 }
 

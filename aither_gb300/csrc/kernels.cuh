@@ -183,6 +183,14 @@ struct Pools {
   // gradient (3) of the previous residual at the cells nonreflecting
   // pressure outlets read (null without such outlets)
   double *nrg;
+  // multigrid: forcing of a coarse level's linear system ([5][nq], null on
+  // the finest level), the matrix residual f - (A x - b) of the level's last
+  // relaxation ([5][nq], null without multigrid), and mg_accum = 1 when the
+  // level's diagonal adds to the one of its previous visit in this
+  // iteration (a W cycle's second visit; gridLevel::ResetDiagonal only
+  // after each update, src/mgSolution.cpp:225-228)
+  T *Fq, *MRq;
+  int mg_accum;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -301,6 +309,24 @@ __global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sst
 
 // Host-side launchers, one instantiation per arithmetic type (defined in
 // kernels_fp64.cu / kernels_fp32.cu).
+// Transfer between a multigrid level (fine) and the next coarser one.
+// Restriction is a gather per coarse physical cell c over its fine cells
+// e in [off[c], off[c+1]), in the fine cells' k, j, i order; prolongation
+// per fine physical cell from the coarse correction at the coarse nodes.
+struct MgLinkDev {
+  int ncoarse, nfine, nnode;
+  const int32_t *off;                       // [ncoarse+1]
+  const int32_t *c_pool, *c_q;              // [ncoarse] coarse pool / q index
+  const int32_t *f_pool, *f_q;              // [nfine] fine pool / q index (gather order)
+  const double *f_w;                        // [nfine] volume weight
+  const int32_t *node_cells;                // [nnode][8] coarse q (-1: none), summing order
+  const double *node_fac;                   // [nnode] 1, 1/2 or 1/8
+  const int32_t *p_q;                       // [nfine] fine q (k, j, i order of each block)
+  const int32_t *p_node0;                   // [nfine] node (ci, cj, ck) of its coarse cell
+  const int32_t *p_sx, *p_sxy;              // [nfine] node strides of that coarse block
+  const double *p_coef;                     // [7][nfine] trilinear coefficients
+};
+
 template <typename T>
 struct Launch {
   static void Ghost(const Pools<T> &P, const GhostOpDev *ops, int nops,
@@ -363,6 +389,21 @@ struct Launch {
                      int ncta, const SolveState *ss, int block, cudaStream_t s);
   static void MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      double *mres_partials, int ncta, int kinds, cudaStream_t s);
+  // multigrid forcing of a coarse level: P.Fq = (A x - (L x - U x) - b) + P.Fq
+  static void MgForcing(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                        int ncta, int kinds, cudaStream_t s);
+  // restrictions: the primitive state (volume-weighted, pool to pool, into a
+  // zeroed coarse pool), the update (volume-weighted, q to q) and the matrix
+  // residual (summed, fine MRq into coarse Fq)
+  static void MgRestrictState(const MgLinkDev &k, const double *fineW, int64_t fine_n,
+                              double *coarseW, int64_t coarse_n, cudaStream_t s);
+  static void MgRestrictQ(const MgLinkDev &k, const T *fine, int64_t fine_nq, T *coarse,
+                          int64_t coarse_nq, bool weighted, cudaStream_t s);
+  // x -= x0 over [5][nq]
+  static void MgSubtract(T *x, const T *x0, int64_t nq, cudaStream_t s);
+  // coarse correction at the coarse nodes, then added to the fine update
+  static void MgProlong(const MgLinkDev &k, const T *coarse_du, int64_t coarse_nq, T *nodes,
+                        T *fine_du, int64_t fine_nq, cudaStream_t s);
   // per-face wall forces [6][n] of the viscous-wall faces
   static void Wall(const Pools<T> &P, const WallFaceDev *faces, int n, double *wbuf,
                    cudaStream_t s);

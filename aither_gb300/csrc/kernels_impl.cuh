@@ -921,13 +921,19 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   const Gas<T> g = GasOf<T>(sv);
   const Prim<T> w = LoadW<T>(P.W, n, c);
   double lam = 0.0, lamt = 0.0;
+  const int64_t q = P.qpos[c];
+  // scalar main diagonal: accumulates like the radius, from zero or (a
+  // multigrid level visited again in this iteration) from its previous value
+  double adiag = (!BLOCK && P.mg_accum) ? (double)P.Aq[q] : 0.0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double *fa = P.fa[d];
     const int64_t u = c + st[d];
-    lam = lam + (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
-                                       (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u],
-                                       (T)fa[2 * n + u], (T)fa[3 * n + u]);
+    const double lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
+                                              (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u],
+                                              (T)fa[2 * n + u], (T)fa[3 * n + u]);
+    lam = lam + lcd;
+    adiag = adiag + lcd;
     if (rans) {
       // turbModel::InviscidCellSpectralRadius (src/turbulence.cpp:94): |v.n_avg| |A|
       const Prim<double> wd = LoadW<double>(P.W, n, c);
@@ -940,10 +946,8 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       lamt = lamt + fabs(Dot(wd.u, wd.v, wd.w, ax, ay, az)) * (0.5 * (fa[3 * n + c] + fa[3 * n + u]));
     }
   }
-  double adiag = lam;    // scalar main diagonal accumulates like the radius
-  double adiagt = lamt;  // and its turbulence part
+  double adiagt = lamt;  // the scalar diagonal's turbulence part
   const double vol = P.vol[c];
-  const int64_t q = P.qpos[c];
   if (sv.viscous) {
     // viscous cell spectral radii (ViscCellSpectralRadius): the time-step
     // radius takes them times the viscous CFL coefficient, the diagonal
@@ -1064,7 +1068,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     // upper face; the 2x2 turbulence block alongside
     T A[kJac], At[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
-    for (int e = 0; e < kJac; ++e) A[e] = T(0);
+    for (int e = 0; e < kJac; ++e) A[e] = P.mg_accum ? P.Aq[e * nq + q] : T(0);
 #pragma unroll 1
     for (int d = 0; d < 3; ++d) {
       const double *fa = P.fa[d];
@@ -1199,11 +1203,20 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
 // the value k_cell formed with the time-level terms
 // (src/linearSolver.cpp:350-352)
 template <typename T>
-__device__ __forceinline__ T RhsB(const Pools<T> &P, const SolveDev &sv, T thetaInv, int v,
-                                  int64_t q) {
+__device__ __forceinline__ T RhsB0(const Pools<T> &P, const SolveDev &sv, T thetaInv, int v,
+                                   int64_t q) {
   const int64_t nq = P.nq;
   if (sv.unsteady) return v < 5 ? P.Bq[v * nq + q] : P.Btq[(v - 5) * nq + q];
   return -thetaInv * (v < 5 ? P.Rq[v * nq + q] : P.Rtq[(v - 5) * nq + q]);
+}
+// ... with the multigrid forcing of a coarse level added, as the sweeps
+// read it (-R/theta + f, src/linearSolver.cpp:350,407,483; multigrid
+// levels are steady, so the time-level terms are zero)
+template <typename T>
+__device__ __forceinline__ T RhsB(const Pools<T> &P, const SolveDev &sv, T thetaInv, int v,
+                                  int64_t q) {
+  const T b0 = RhsB0(P, sv, thetaInv, v, q);
+  return (P.Fq && v < 5) ? b0 + P.Fq[v * P.nq + q] : b0;
 }
 
 // Neighbour data of an off-diagonal term: the state, laminar viscosity and
@@ -2875,7 +2888,7 @@ __global__ void k_wall(Pools<T> P, const WallFaceDev *faces, int nfaces, double 
 template <typename T, bool BLOCK>
 __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list,
                                                  const int32_t *cta_block,
-                                                 double *mres_partials) {
+                                                 double *mres_partials, int forcing) {
   __shared__ double s_sum[kCta / 32];
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
@@ -2929,12 +2942,24 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
     for (int v = 0; v < 7; ++v) {
       if (v >= nv) break;
       const T off = L[v] - U[v];
-      const T bv = RhsB(P, sv, thetaInv, v, q);
+      const T bv = RhsB0(P, sv, thetaInv, v, q);
       const T axmb = Ax[v] - off - bv;
-      const double r = 0.0 - (double)axmb;
+      if (forcing) {
+        // a coarse level's forcing: A x - b of the restricted update plus
+        // the restricted fine matrix residual already in Fq
+        // (gridLevel::Restriction src/gridLevel.cpp:571-589)
+        if (v < 5) P.Fq[v * nq + q] = axmb + P.Fq[v * nq + q];
+        continue;
+      }
+      // linearSolver::Residual (src/linearSolver.cpp:92): f - (A x - b)
+      const T f = (P.Fq && v < 5) ? P.Fq[v * nq + q] : T(0);
+      const T rt = f - axmb;
+      if (P.MRq && v < 5) P.MRq[v * nq + q] = rt;
+      const double r = (double)rt;
       sum += r * r;
     }
   }
+  if (forcing) return;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
   if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
@@ -2951,8 +2976,126 @@ template <typename T>
 void Launch<T>::MatRes(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        double *mres_partials, int ncta, int kinds, cudaStream_t s) {
   if (ncta <= 0) return;
-  if (kinds & 1) k_matres<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
-  if (kinds & 2) k_matres<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials);
+  if (kinds & 1) k_matres<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials, 0);
+  if (kinds & 2) k_matres<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block, mres_partials, 0);
+}
+template <typename T>
+void Launch<T>::MgForcing(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                          int ncta, int kinds, cudaStream_t s) {
+  if (ncta <= 0) return;
+  if (kinds & 1) k_matres<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block, nullptr, 1);
+  if (kinds & 2) k_matres<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block, nullptr, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid transfers (gridLevel::Restriction / Prolongation,
+// src/gridLevel.cpp:538-611; BlockRestriction include/procBlock.hpp:637-690;
+// BlockProlongation include/gridLevel.hpp:160).  Every coarse value is a sum
+// from zero over its fine cells in the fine k, j, i order, as the
+// reference's loop adds them.
+template <typename U, bool WEIGHTED>
+__global__ void k_mg_gather(MgLinkDev k, const U *src, int64_t src_n, bool src_pool, U *dst,
+                            int64_t dst_n, bool dst_pool) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k.ncoarse) return;
+  const int e0 = k.off[c], e1 = k.off[c + 1];
+  const int64_t dc = dst_pool ? k.c_pool[c] : k.c_q[c];
+#pragma unroll 1
+  for (int v = 0; v < 5; ++v) {
+    U acc = U(0);
+    for (int e = e0; e < e1; ++e) {
+      const int64_t sc = src_pool ? k.f_pool[e] : k.f_q[e];
+      const U x = src[v * src_n + sc];
+      const U t = WEIGHTED ? (U)k.f_w[e] * x : x;
+      acc = acc + t;
+    }
+    dst[v * dst_n + dc] = acc;
+  }
+}
+
+template <typename T>
+__global__ void k_mg_sub(T *x, const T *x0, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = x[i] - x0[i];
+}
+
+// ConvertCellToNode without ghosts (include/utility.hpp:187): each node the
+// sum of its cells, times 1 (block corners), 1/2 (block edges) or 1/8
+template <typename T>
+__global__ void k_mg_nodes(MgLinkDev k, const T *du, int64_t nq, T *nodes) {
+  const int nd = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nd >= k.nnode) return;
+  const int32_t *cl = k.node_cells + 8 * (int64_t)nd;
+  const T f = (T)k.node_fac[nd];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    T acc = T(0);
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      if (cl[e] >= 0) acc = acc + du[v * nq + cl[e]];
+    nodes[v * (int64_t)k.nnode + nd] = acc * f;
+  }
+}
+
+// TrilinearInterp (include/utility.hpp:357) of the coarse correction at the
+// fine cell centre, added to the fine update (linearSolver::AddToUpdate)
+template <typename T>
+__device__ __forceinline__ T MgLin(T d0, T d1, T c) { return (T(1) - c) * d0 + c * d1; }
+template <typename T>
+__global__ void k_mg_prolong(MgLinkDev k, const T *nodes, T *du, int64_t nq) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= k.nfine) return;
+  const int64_t n0 = k.p_node0[e], sx = k.p_sx[e], sxy = k.p_sxy[e];
+  const int64_t id[8] = {n0,           n0 + 1,           n0 + sx,       n0 + sx + 1,
+                         n0 + sxy,     n0 + sxy + 1,     n0 + sxy + sx, n0 + sxy + sx + 1};
+  T co[7];
+#pragma unroll
+  for (int a = 0; a < 7; ++a) co[a] = (T)k.p_coef[a * (int64_t)k.nfine + e];
+  const int64_t fq = k.p_q[e];
+  const int64_t nn = k.nnode;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const T *nv = nodes + v * nn;
+    const T d04 = MgLin(nv[id[0]], nv[id[4]], co[0]);
+    const T d15 = MgLin(nv[id[1]], nv[id[5]], co[1]);
+    const T d26 = MgLin(nv[id[2]], nv[id[6]], co[2]);
+    const T d37 = MgLin(nv[id[3]], nv[id[7]], co[3]);
+    const T d0415 = MgLin(d04, d15, co[4]);
+    const T d2637 = MgLin(d26, d37, co[5]);
+    du[v * nq + fq] = du[v * nq + fq] + MgLin(d0415, d2637, co[6]);
+  }
+}
+
+template <typename T>
+void Launch<T>::MgRestrictState(const MgLinkDev &k, const double *fineW, int64_t fine_n,
+                                double *coarseW, int64_t coarse_n, cudaStream_t s) {
+  if (k.ncoarse <= 0) return;
+  k_mg_gather<double, true><<<(k.ncoarse + 127) / 128, 128, 0, s>>>(k, fineW, fine_n, true,
+                                                                    coarseW, coarse_n, true);
+}
+template <typename T>
+void Launch<T>::MgRestrictQ(const MgLinkDev &k, const T *fine, int64_t fine_nq, T *coarse,
+                            int64_t coarse_nq, bool weighted, cudaStream_t s) {
+  if (k.ncoarse <= 0) return;
+  if (weighted)
+    k_mg_gather<T, true><<<(k.ncoarse + 127) / 128, 128, 0, s>>>(k, fine, fine_nq, false,
+                                                                 coarse, coarse_nq, false);
+  else
+    k_mg_gather<T, false><<<(k.ncoarse + 127) / 128, 128, 0, s>>>(k, fine, fine_nq, false,
+                                                                  coarse, coarse_nq, false);
+}
+template <typename T>
+void Launch<T>::MgSubtract(T *x, const T *x0, int64_t nq, cudaStream_t s) {
+  const int64_t n = 5 * nq;
+  if (n > 0) k_mg_sub<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, x0, n);
+}
+template <typename T>
+void Launch<T>::MgProlong(const MgLinkDev &k, const T *coarse_du, int64_t coarse_nq, T *nodes,
+                          T *fine_du, int64_t fine_nq, cudaStream_t s) {
+  if (k.nnode > 0)
+    k_mg_nodes<T><<<(k.nnode + 127) / 128, 128, 0, s>>>(k, coarse_du, coarse_nq, nodes);
+  if (k.nfine > 0)
+    k_mg_prolong<T><<<(k.nfine + 127) / 128, 128, 0, s>>>(k, nodes, fine_du, fine_nq);
 }
 template <typename T>
 void Launch<T>::Wall(const Pools<T> &P, const WallFaceDev *faces, int n, double *wbuf,

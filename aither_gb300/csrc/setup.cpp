@@ -1110,8 +1110,9 @@ class WallTree {
   std::vector<int8_t> axis_;
 };
 
-void BuildWallDistance(Setup &setup, int solve) {
-  std::vector<double> wf;  // x, y, z of every viscous-wall face centre
+// x, y, z of the centre of every viscous-wall face of a solve's blocks
+std::vector<double> WallFaceCentres(const Setup &setup, int solve) {
+  std::vector<double> wf;
   for (int bi : setup.solves[solve].blocks) {
     const Block &b = setup.blocks[bi];
     for (const auto &sf : b.surfs) {
@@ -1131,6 +1132,15 @@ void BuildWallDistance(Setup &setup, int solve) {
           }
     }
   }
+  return wf;
+}
+
+// Wall distance of a solve's cells to the wall-face centres wf (by default
+// its own walls; the coarse multigrid levels use the finest level's, as
+// the reference's k-d tree of the finest faces serves every level,
+// src/main.cpp:186-201)
+void BuildWallDistance(Setup &setup, int solve, const std::vector<double> *faces = nullptr) {
+  const std::vector<double> wf = faces ? *faces : WallFaceCentres(setup, solve);
   if (wf.empty()) return;
   std::unique_ptr<WallTree> tree;
   if (setup.geom_device < 0) tree.reset(new WallTree(wf));
@@ -1190,6 +1200,202 @@ void BuildWallDistance(Setup &setup, int solve) {
     for (const auto &op : b.ops)
       if (op.type == ATH_BC_PERIODIC || op.type == ATH_BC_INTERBLOCK)
         b.wall_dist[op.dst] = setup.blocks[op.src_block].wall_dist[op.src];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid levels (gridLevel::Coarsen, src/gridLevel.cpp:440-535;
+// procBlock::GetCoarseMeshAndBCs, src/procBlock.cpp:6471-6590).
+
+// std::inner_product's order: the sum starts from zero
+inline double DotIP(V3 a, V3 b) { return ((0.0 + a.x * b.x) + a.y * b.y) + a.z * b.z; }
+inline double MagIP(V3 a) { return std::sqrt(DotIP(a, a)); }
+
+// LinearInterpCoeff (src/utility.cpp:625): the position of x along x0 -> x1
+double LinearCoeff(V3 x0, V3 x1, V3 x) {
+  const V3 d = x1 - x0;
+  const double m = MagIP(d);
+  const V3 dir{d.x / m, d.y / m, d.z / m};
+  const double dist = MagIP(x0 - x1);
+  return DotIP(x - x0, dir) / dist;
+}
+V3 LinearAt(V3 x0, V3 x1, double c) { return (1.0 - c) * x0 + c * x1; }
+
+// The node indices of one direction a coarse level keeps: every node a
+// boundary surface starts or ends on, and otherwise every other node; with
+// the surfaces' indices along that direction renumbered on the copy
+std::vector<int> KeptNodes(const Block &fb, int dir, std::vector<Surface> &coarse_surfs) {
+  const int nn = (dir == 0 ? fb.ni : dir == 1 ? fb.nj : fb.nk) + 1;
+  std::vector<int> keep;
+  int since = 0;
+  for (int n = 0; n < nn; ++n) {
+    bool boundary = false;
+    for (const auto &sf : fb.surfs) {
+      const int lo = dir == 0 ? sf.i1 : dir == 1 ? sf.j1 : sf.k1;
+      const int hi = dir == 0 ? sf.i2 : dir == 1 ? sf.j2 : sf.k2;
+      if (lo == n || hi == n) boundary = true;
+    }
+    if (boundary) {
+      keep.push_back(n);
+      const int m = (int)keep.size() - 1;
+      for (auto &sf : coarse_surfs) {
+        int &lo = dir == 0 ? sf.i1 : dir == 1 ? sf.j1 : sf.k1;
+        int &hi = dir == 0 ? sf.i2 : dir == 1 ? sf.j2 : sf.k2;
+        if (lo == n) lo = m;
+        if (hi == n) hi = m;
+      }
+      since = 0;
+    } else if (since > 0) {
+      keep.push_back(n);
+      since = 0;
+    } else {
+      ++since;
+    }
+  }
+  return keep;
+}
+
+// The coarse block of fine block fb (nodes and renumbered surfaces) and
+// fb's fine-to-coarse cell map and volume weights; the prolongation
+// coefficients need the coarse nodes and are formed by MgCoefficients
+Block CoarsenBlock(Block &fb) {
+  Block cb;
+  cb.surfs = fb.surfs;
+  std::vector<int> keep[3];
+  for (int d = 0; d < 3; ++d) keep[d] = KeptNodes(fb, d, cb.surfs);
+  cb.ni = (int)keep[0].size() - 1;
+  cb.nj = (int)keep[1].size() - 1;
+  cb.nk = (int)keep[2].size() - 1;
+  const size_t cnn = (size_t)(cb.ni + 1) * (cb.nj + 1) * (cb.nk + 1);
+  cb.nodes.assign(3 * cnn, 0.0);
+  for (int k = 0; k <= cb.nk; ++k)
+    for (int j = 0; j <= cb.nj; ++j)
+      for (int i = 0; i <= cb.ni; ++i) {
+        const size_t o = (size_t)i + (size_t)(cb.ni + 1) * (j + (size_t)(cb.nj + 1) * k);
+        for (int c = 0; c < 3; ++c) cb.nodes[c * cnn + o] = fb.Node(c, keep[0][i], keep[1][j], keep[2][k]);
+      }
+  // coarse cell of each fine cell: the last kept node at or below it
+  auto coarse_of = [](const std::vector<int> &kp, int f) {
+    int pos = 0;
+    while (pos < (int)kp.size() && !(kp[pos] > f)) ++pos;
+    return pos != 0 ? pos - 1 : pos;
+  };
+  const int64_t nfc = (int64_t)fb.ni * fb.nj * fb.nk;
+  fb.mg_cell.assign(nfc, 0);
+  fb.mg_volfac.assign(nfc, 0.0);
+  const int64_t ncc = (int64_t)cb.ni * cb.nj * cb.nk;
+  std::vector<double> vsum(ncc, 0.0);
+  int64_t x = 0;
+  for (int k = 0; k < fb.nk; ++k)
+    for (int j = 0; j < fb.nj; ++j)
+      for (int i = 0; i < fb.ni; ++i, ++x) {
+        const int ci = coarse_of(keep[0], i), cj = coarse_of(keep[1], j),
+                  ck = coarse_of(keep[2], k);
+        fb.mg_cell[x] = ci + cb.ni * (cj + cb.nj * ck);
+      }
+  // fine volumes summed per coarse cell in the fine cells' k, j, i order
+  x = 0;
+  for (int k = 0; k < fb.nk; ++k)
+    for (int j = 0; j < fb.nj; ++j)
+      for (int i = 0; i < fb.ni; ++i, ++x) vsum[fb.mg_cell[x]] += fb.vol[fb.Cell(i, j, k)];
+  x = 0;
+  for (int k = 0; k < fb.nk; ++k)
+    for (int j = 0; j < fb.nj; ++j)
+      for (int i = 0; i < fb.ni; ++i, ++x)
+        fb.mg_volfac[x] = fb.vol[fb.Cell(i, j, k)] / vsum[fb.mg_cell[x]];
+  return cb;
+}
+
+// TrilinearInterpCoeff (src/utility.cpp:633) of every fine cell centre in
+// the hexahedron of its coarse cell's nodes
+void MgCoefficients(Block &fb, const Block &cb) {
+  const int64_t nfc = (int64_t)fb.ni * fb.nj * fb.nk;
+  const int64_t nc = fb.NCell();
+  fb.mg_coef.assign(7 * nfc, 0.0);
+  int64_t x = 0;
+  for (int k = 0; k < fb.nk; ++k)
+    for (int j = 0; j < fb.nj; ++j)
+      for (int i = 0; i < fb.ni; ++i, ++x) {
+        const int cc = fb.mg_cell[x];
+        const int ci = cc % cb.ni, cj = (cc / cb.ni) % cb.nj, ck = cc / (cb.ni * cb.nj);
+        const V3 c0 = NodeV(cb, ci, cj, ck), c1 = NodeV(cb, ci + 1, cj, ck),
+                 c2 = NodeV(cb, ci, cj + 1, ck), c3 = NodeV(cb, ci + 1, cj + 1, ck),
+                 c4 = NodeV(cb, ci, cj, ck + 1), c5 = NodeV(cb, ci + 1, cj, ck + 1),
+                 c6 = NodeV(cb, ci, cj + 1, ck + 1), c7 = NodeV(cb, ci + 1, cj + 1, ck + 1);
+        const int64_t c = fb.Cell(i, j, k);
+        const V3 p{fb.center[c], fb.center[nc + c], fb.center[2 * nc + c]};
+        double *co = &fb.mg_coef[7 * x];
+        co[0] = LinearCoeff(c0, c4, p);
+        const V3 x04 = LinearAt(c0, c4, co[0]);
+        co[1] = LinearCoeff(c1, c5, p);
+        const V3 x15 = LinearAt(c1, c5, co[1]);
+        co[2] = LinearCoeff(c2, c6, p);
+        const V3 x26 = LinearAt(c2, c6, co[2]);
+        co[3] = LinearCoeff(c3, c7, p);
+        const V3 x37 = LinearAt(c3, c7, co[3]);
+        co[4] = LinearCoeff(x04, x15, p);
+        const V3 x0415 = LinearAt(x04, x15, co[4]);
+        co[5] = LinearCoeff(x26, x37, p);
+        const V3 x2637 = LinearAt(x26, x37, co[5]);
+        co[6] = LinearCoeff(x0415, x2637, p);
+      }
+}
+
+// Levels 1 .. L-1 of a solve: each level's blocks from the finer level's
+// (CoarsenBlock), then the same geometry, boundary and connection
+// bookkeeping as the finest level (the coarse procBlocks are built from
+// their plot3dBlock and boundary conditions like the fine ones,
+// src/gridLevel.cpp:455-500), with the wall distance to the finest level's
+// wall faces
+void BuildCoarseLevels(Setup &st, int solve) {
+  const int nl = st.solves[solve].phys.mg_levels;
+  std::vector<double> wf;
+  if (st.solves[solve].phys.eqn != ATH_EQN_EULER) wf = WallFaceCentres(st, solve);
+  Setup *fine = &st;
+  int fsolve = solve;
+  for (int l = 1; l < nl; ++l) {
+    while ((int)st.levels.size() < l) {
+      st.levels.emplace_back(new Setup());
+      st.levels.back()->geom_device = st.geom_device;
+    }
+    Setup &cs = *st.levels[l - 1];
+    const int csolve = (int)cs.solves.size();
+    Solve csv = fine->solves[fsolve];
+    csv.blocks.clear();
+    for (int fbi : fine->solves[fsolve].blocks) {
+      Block &fb = fine->blocks[fbi];
+      Block cb = CoarsenBlock(fb);
+      cb.ng = fb.ng;
+      cb.nv = fb.nv;
+      cb.solve = csolve;
+      BuildGeometry(cb, st.geom_device);
+      BuildGhostGeometry(cb);
+      BuildHyperplanes(cb);
+      MgCoefficients(fb, cb);
+      // initial state: the volume-weighted restriction of the fine one
+      // (the coarse level's state is replaced by a restriction before each
+      // use)
+      cb.state0.assign((size_t)cb.NCell() * cb.nv, 0.0);
+      int64_t x = 0;
+      for (int k = 0; k < fb.nk; ++k)
+        for (int j = 0; j < fb.nj; ++j)
+          for (int i = 0; i < fb.ni; ++i, ++x) {
+            const int cc = fb.mg_cell[x];
+            const int ci = cc % cb.ni, cj = (cc / cb.ni) % cb.nj, ck = cc / (cb.ni * cb.nj);
+            const int64_t o = cb.Cell(ci, cj, ck) * cb.nv, f = fb.Cell(i, j, k) * fb.nv;
+            for (int v = 0; v < cb.nv; ++v) cb.state0[o + v] += fb.mg_volfac[x] * fb.state0[f + v];
+          }
+      fb.mg_coarse = (int)cs.blocks.size();
+      csv.blocks.push_back((int)cs.blocks.size());
+      cs.blocks.push_back(std::move(cb));
+    }
+    cs.solves.push_back(std::move(csv));
+    BuildGhostOps(cs, csolve);
+    BuildEdgeOps(cs, csolve);
+    for (int bi : cs.solves[csolve].blocks) BuildCellWidths(cs.blocks[bi]);
+    if (!wf.empty()) BuildWallDistance(cs, csolve, &wf);
+    fine = &cs;
+    fsolve = csolve;
   }
 }
 
@@ -1356,7 +1562,17 @@ void AppendInput(Setup &st, const std::string &path) {
                          std::make_pair("viscousFaceReconstruction", "central")})
     if (get(kd.first, kd.second) != kd.second)
       Fail(std::string("only ") + kd.first + " " + kd.second + " is supported");
-  if ((int)getd("multigridLevels", 1) != 1) Fail("multigrid is not supported");
+  // multigrid (input::ReadInput src/input.cpp:437-455, CheckMultigrid
+  // :1042): grid levels and the cycle (input::MultigridCycleIndex,
+  // include/input.hpp:281: W visits each coarser level twice per visit of
+  // its finer one, V once)
+  ph.mg_levels = (int)getd("multigridLevels", 1);
+  if (ph.mg_levels < 1) Fail("multigridLevels must be >= 1");
+  {
+    const auto cyc = get("multigridCycle", "V");
+    if (cyc != "V" && cyc != "W") Fail("multigridCycle must be 'V' or 'W'");
+    ph.mg_cycle = cyc == "W" ? 2 : 1;
+  }
   const auto tm = get("turbulenceModel", "none");
   if (tm != "none" && ph.eqn != ATH_EQN_RANS) Fail("turbulence model needs equationSet rans");
   ph.turb = ATH_TURB_NONE;
@@ -1599,6 +1815,18 @@ void AppendInput(Setup &st, const std::string &path) {
   // with viscous walls (src/main.cpp:200); without walls the distance keeps
   // its default of 1e10
   if (st.solves[solve].phys.eqn != ATH_EQN_EULER) BuildWallDistance(st, solve);
+  if (ph.mg_levels > 1) {
+    // the coarse levels' forcing enters the mean-flow equations of steady
+    // solves here: turbulence equations, time-accurate terms and the
+    // nonreflecting boundaries' time levels are not carried to them
+    const auto &p = st.solves[solve].phys;
+    if (p.eqn == ATH_EQN_RANS) Fail("multigrid with the turbulence equations is not supported");
+    if (p.multilevel || p.nl_iters > 1)
+      Fail("multigrid is supported for steady solves (one nonlinear iteration per step)");
+    for (const auto &bs : st.solves[solve].states)
+      if (bs.nonreflecting) Fail("multigrid with nonreflecting boundaries is not supported");
+    BuildCoarseLevels(st, solve);
+  }
 }
 
 }  // namespace ath

@@ -6,6 +6,7 @@
 #include <array>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,14 @@ struct Block {
   std::vector<ath_nr_cell> nr_cells;  // cells of nonreflecting surfaces
   std::vector<int32_t> plane_offsets, plane_cells;
   std::vector<uint8_t> nbr_mask;
+  // multigrid: this block's block on the next coarser level (its index in
+  // that level's setup) and, per physical cell in k, j, i order, the coarse
+  // physical cell it lies in (i + ni*(j + nj*k) of the coarse block), its
+  // volume weight in the restriction and its 7 trilinear prolongation
+  // coefficients (gridLevel::Coarsen, src/gridLevel.cpp:440-535)
+  int mg_coarse = -1;
+  std::vector<int32_t> mg_cell;
+  std::vector<double> mg_volfac, mg_coef;  // [cells], [cells][7]
 
   int64_t Cell(int i, int j, int k) const {
     return (int64_t)(i + ng) + (int64_t)NI * ((j + ng) + (int64_t)NJ * (k + ng));
@@ -88,6 +97,10 @@ struct Setup {
   // CUDA device that computes the physical cells' geometry and wall
   // distance (-1: the host does)
   int geom_device = -1;
+  // coarser multigrid levels: levels[l-1] holds level l of every solve with
+  // more than l levels, in the order of the solves (mgSolution::
+  // ConstructMultigrids, src/mgSolution.cpp:86)
+  std::vector<std::unique_ptr<Setup>> levels;
 };
 
 // Parse an input file and append its blocks as a new solve.
@@ -105,6 +118,8 @@ void BuildCellWidths(Block &b);
 void BuildGhostOps(Setup &setup, int solve);
 void BuildHyperplanes(Block &b);
 void BuildEdgeOps(Setup &setup, int solve);
+// Coarser multigrid levels of a solve with more than one level.
+void BuildCoarseLevels(Setup &setup, int solve);
 
 // Reads the binary multi-block Plot3D grid format.
 std::vector<Block> ReadPlot3d(const std::string &path, double lref);

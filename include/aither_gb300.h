@@ -167,6 +167,9 @@ typedef struct {
    * iterations per time step */
   double dt_global, dual_cfl;
   int32_t nl_iters, multilevel;
+  /* multigrid (multigridLevels, multigridCycle; mgSolution src/mgSolution.cpp:
+   * 160-207): grid levels (1: none) and the cycle index (1 V, 2 W) */
+  int32_t mg_levels, mg_cycle;
 } ath_solve_view;
 
 /* Read-only view of one block of a setup; arrays are host memory owned by
@@ -230,6 +233,37 @@ int ath_setup_solve(const ath_setup *setup, int solve, ath_solve_view *out);
 /* Replace the initial primitive state (nondimensional, AoS over physical
  * cells, k slowest, i fastest). */
 int ath_setup_set_state(ath_setup *setup, int block, const double *prim);
+
+/* Multigrid levels (multigridLevels > 1; mgSolution::ConstructMultigrids
+ * src/mgSolution.cpp:86, gridLevel::Coarsen src/gridLevel.cpp:440).  Level 0
+ * is the setup itself; level l holds, in the order of the solves, the l-th
+ * coarser grid of every solve with more than l levels: each coarse block
+ * keeps every fine node a boundary surface starts or ends on and otherwise
+ * every other node (procBlock::GetCoarseMeshAndBCs src/procBlock.cpp:6471),
+ * with its own geometry, boundary and connection bookkeeping.  The
+ * ath_setup_level_* calls are ath_setup_counts / _block / _solve of a
+ * level; views stay valid while the setup lives. */
+int ath_setup_levels(const ath_setup *setup, int *nlevels);
+int ath_setup_level_counts(const ath_setup *setup, int level, int *nsolves, int *nblocks,
+                           int64_t *ncells);
+int ath_setup_level_block(const ath_setup *setup, int level, int block, ath_block_view *out);
+int ath_setup_level_solve(const ath_setup *setup, int level, int solve, ath_solve_view *out);
+
+/* Transfer between block `block` of level `level` and its block on level
+ * level+1: per fine physical cell (k, j, i order) the coarse physical cell
+ * it lies in (i + ni*(j + nj*k) of the coarse block), its weight in the
+ * volume-weighted restriction (fine volume over the summed volume of the
+ * fine cells of that coarse cell) and its 7 trilinear prolongation
+ * coefficients from the coarse cell's nodes (TrilinearInterpCoeff
+ * src/utility.cpp:633), [cell][7]. */
+typedef struct {
+  int32_t coarse_block, pad;
+  int64_t ncells;
+  const int32_t *coarse_cell;
+  const double *volfac;
+  const double *coef;
+} ath_mg_map;
+int ath_setup_mg_map(const ath_setup *setup, int level, int block, ath_mg_map *out);
 
 /* ---- device context and batches ----------------------------------------- */
 typedef struct ath_ctx ath_ctx;

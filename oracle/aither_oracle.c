@@ -56,6 +56,14 @@ typedef struct {
   double *nrg;  /* [nc][12] velocity (9) and pressure (3) gradients of the
                    previous residual at the cells nonreflecting pressure
                    outlets read (NULL without such outlets) */
+  /* multigrid: forcing of a coarse level's linear system (gridLevel
+   * mgForcing_), the matrix residual of this level's last relaxation, and
+   * the transfer to the next coarser level (its block, and per physical
+   * cell the coarse cell, restriction weight, 7 prolongation coefficients) */
+  double *F, *mr;      /* [nc][5], NULL without multigrid */
+  int mg_coarse;
+  int32_t *mg_cell;
+  double *mg_volfac, *mg_coef;
 } oblock;
 
 typedef struct {
@@ -80,6 +88,13 @@ struct orc_case {
   int matrix_resid;     /* compute the logged matrix residual */
   double *mres;         /* [ns] last matrix residual */
   double *forces;       /* [ns][6] wall forces of the last residual */
+  struct orc_case *coarse;  /* next coarser multigrid level (NULL: none) */
+  int mg_cycle;             /* 1 V, 2 W */
+  /* visits of this (coarse) level in the current iteration: its implicit
+   * diagonal is zeroed only after each update (gridLevel::ResetDiagonal,
+   * src/mgSolution.cpp:225-228), so a level a W cycle visits again adds its
+   * new spectral radii to the diagonal of the previous visit */
+  int mg_visits;
 };
 
 /* ---------------------------------------------------------------- thermo */
@@ -1440,6 +1455,7 @@ void orc_destroy(orc_case *c) {
     free(b->Abt); free(b->Ainvbt); free(b->mutc); free(b->f1c); free(b->f2c);
     free(b->kgc); free(b->wgc); free(b->wd);
     for (int d = 0; d < 3; ++d) free(b->wallf[d]);
+    free(b->F); free(b->mr); free(b->mg_cell); free(b->mg_volfac); free(b->mg_coef);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
@@ -1814,7 +1830,7 @@ void orc_residual(orc_case *c) {
     const gas_t *g = &sv->gas;
     memset(b->R, 0, 8 * NV * b->nc);
     memset(b->lam, 0, 8 * b->nc);
-    memset(b->A, 0, 8 * b->nc);
+    if (c->mg_visits <= 1) memset(b->A, 0, 8 * b->nc);
     memset(b->force, 0, sizeof(b->force));
     if (sv->rans) {
       memset(b->Rt, 0, 8 * 2 * b->nc);
@@ -1827,7 +1843,7 @@ void orc_residual(orc_case *c) {
       memset(b->kgc, 0, 8 * 3 * b->nc);
       memset(b->wgc, 0, 8 * 3 * b->nc);
     }
-    if (sv->block) memset(b->Ab, 0, 8 * NJAC * b->nc);
+    if (sv->block && c->mg_visits <= 1) memset(b->Ab, 0, 8 * NJAC * b->nc);
     if (b->vg) memset(b->vg, 0, 8 * 9 * b->nc);
     for (int d = 0; d < 3; ++d) {
       const int ei = b->ni + (d == 0), ej = b->nj + (d == 1), ek = b->nk + (d == 2);
@@ -2229,10 +2245,33 @@ static void rhs_b(const orc_case *c, const oblock *b, int64_t x, double *bb) {
   }
 }
 
+/* b with the multigrid forcing f as the LU-SGS sweeps form it (src/
+ * linearSolver.cpp:350-352, 407-409): -R/theta + f + SolDeltaNm1 -
+ * SolDeltaMmN */
+static void rhs_bf(const orc_case *c, const oblock *b, int64_t x, double *bb) {
+  const ath_solve_view *v = &c->s[b->solve].v;
+  const int unsteady = v->multilevel || v->nl_iters > 1;
+  if (!b->F || unsteady) {
+    rhs_b(c, b, x, bb);
+    return;
+  }
+  const double thetaInv = 1.0 / v->theta;
+  double r[NV + 2];
+  get_rhs(c, b, x, r);
+  for (int q = 0; q < NV + 2; ++q) {
+    const double f = q < NV ? b->F[x * NV + q] : 0.0;
+    bb[q] = -thetaInv * r[q] + f + 0.0 - 0.0;
+  }
+}
+static double forcing_of(const oblock *b, int64_t x, int v) {
+  return (b->F && v < NV) ? b->F[x * NV + v] : 0.0;
+}
+
 /* linearSolver::Residual / AXmB (src/linearSolver.cpp:58,92) and the L2 of
  * mgSolution::CycleAtLevel (src/mgSolution.cpp:196-206) with the second
  * normalisation of src/main.cpp:271: sqrt(sum(r^2)/padded_size/(cells*nv)),
- * r = f - (A x - (L x - U x) - b), f = 0 on the finest level. */
+ * r = f - (A x - (L x - U x) - b), f = 0 on the finest level; with
+ * multigrid the per-cell r is kept for the restriction. */
 static void matrix_residual(orc_case *c) {
   for (int s = 0; s < c->ns; ++s) {
     double sum = 0.0, padded = 0.0, cells = 0.0;
@@ -2263,7 +2302,8 @@ static void matrix_residual(orc_case *c) {
               const double off = L[v] - U[v];
               const double bb = r[v];
               const double axmb = Ax[v] - off - bb;
-              const double rr = 0.0 - axmb;
+              const double rr = forcing_of(b, x, v) - axmb;
+              if (b->mr && v < NV) b->mr[x * NV + v] = rr;
               bsum += rr * rr;
             }
           }
@@ -2295,13 +2335,17 @@ static void apply_ainv(const orc_case *c, const oblock *b, int64_t x, const doub
  * dplur::Relax (:501) with DPLUR (:473): from A^-1 b (MatrixRequires-
  * Initialization, src/input.cpp:1120), matrixSweeps Jacobi sweeps, each
  * after a ghost swap: x = A^-1 (b + L(x_old) - U(x_old)) */
-void orc_relax(orc_case *c) {
+/* the sweeps of one relaxation: matrixSweeps of each solve, or (half = 1)
+ * the multigrid pre- and post-relaxation count max(matrixSweeps/2, 1)
+ * (mgSolution::CycleAtLevel src/mgSolution.cpp:175) */
+static int sweeps_of(const osolve *sv, int half) {
+  if (!half) return sv->sweeps;
+  return sv->sweeps / 2 > 1 ? sv->sweeps / 2 : 1;
+}
+
+/* linearSolver::InitializeMatrixUpdate (src/linearSolver.cpp:111) */
+static void relax_init(orc_case *c) {
   NTH
-  int maxsw = 1, maxj = 0;
-  for (int s = 0; s < c->ns; ++s) {
-    if (c->s[s].jacobi) maxj = c->s[s].sweeps > maxj ? c->s[s].sweeps : maxj;
-    else maxsw = c->s[s].sweeps > maxsw ? c->s[s].sweeps : maxsw;
-  }
   PAR_BLOCKS
   for (int bi = 0; bi < c->nb; ++bi) {
     oblock *b = &c->b[bi];
@@ -2324,13 +2368,23 @@ void orc_relax(orc_case *c) {
           set_du(b, x, out);
         }
   }
+}
+
+static void relax_sweeps(orc_case *c, int half) {
+  NTH
+  int maxsw = 0, maxj = 0;
+  for (int s = 0; s < c->ns; ++s) {
+    const int n = sweeps_of(&c->s[s], half);
+    if (c->s[s].jacobi) maxj = n > maxj ? n : maxj;
+    else maxsw = n > maxsw ? n : maxsw;
+  }
   for (int sw = 0; sw < maxj; ++sw) {
     swap_du(c);
     PAR_BLOCKS
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
-      if (!sv->jacobi || sw >= sv->sweeps) continue;
+      if (!sv->jacobi || sw >= sweeps_of(sv, half)) continue;
       const int nv = sv->rans ? NV + 2 : NV;
       const double thetaInv = 1.0 / sv->v.theta;
       /* new iterate beside the old one (ghosts keep the swapped values) */
@@ -2346,7 +2400,7 @@ void orc_relax(orc_case *c) {
             rhs_b(c, b, x, r);
             for (int v = 0; v < nv; ++v) {
               const double bb = r[v];
-              in[v] = bb + 0.0 + (L[v] - U[v]);
+              in[v] = bb + forcing_of(b, x, v) + (L[v] - U[v]);
             }
             apply_ainv(c, b, x, in, out);
             memcpy(&nu[x * NV], out, 8 * NV);
@@ -2364,7 +2418,7 @@ void orc_relax(orc_case *c) {
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
-      if (sv->jacobi || sw >= sv->sweeps) continue;
+      if (sv->jacobi || sw >= sweeps_of(sv, half)) continue;
       const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;
@@ -2377,7 +2431,7 @@ void orc_relax(orc_case *c) {
           offdiag_sum(c, b, x, 0, U);
           for (int v = 0; v < nv; ++v) L[v] -= U[v];
         }
-        rhs_b(c, b, x, r);
+        rhs_bf(c, b, x, r);
         for (int v = 0; v < nv; ++v) {
           const double bb = r[v];
           in[v] = bb + L[v];
@@ -2391,7 +2445,7 @@ void orc_relax(orc_case *c) {
     for (int bi = 0; bi < c->nb; ++bi) {
       oblock *b = &c->b[bi];
       const osolve *sv = &c->s[b->solve];
-      if (sv->jacobi || sw >= sv->sweeps) continue;
+      if (sv->jacobi || sw >= sweeps_of(sv, half)) continue;
       const int nv = sv->rans ? NV + 2 : NV;
       const int full = sw > 0 || sv->sweeps > 1;
       const double thetaInv = 1.0 / sv->v.theta;
@@ -2402,7 +2456,7 @@ void orc_relax(orc_case *c) {
         offdiag_sum(c, b, x, 0, U);
         if (full) {
           offdiag_sum(c, b, x, 1, L);
-          rhs_b(c, b, x, r);
+          rhs_bf(c, b, x, r);
           for (int v = 0; v < nv; ++v) {
             const double bb = r[v];
             in[v] = bb + L[v] - U[v];
@@ -2419,6 +2473,217 @@ void orc_relax(orc_case *c) {
       }
     }
   }
+}
+
+/* ---------------------------------------------------------- multigrid */
+/* coarse cell (padded index) of fine physical cell number x of block b */
+static int64_t mg_coarse_cell(const oblock *b, const oblock *cb, int64_t x) {
+  const int cc = b->mg_cell[x];
+  const int ci = cc % cb->ni, cj = (cc / cb->ni) % cb->nj, ck = cc / (cb->ni * cb->nj);
+  return cell_idx(cb, ci, cj, ck);
+}
+
+/* BlockRestriction (include/procBlock.hpp:637,656): the coarse array is
+ * zeroed (ghosts included), then every fine physical cell, in k, j, i
+ * order, adds its value times its volume weight (weighted) or its value
+ * (sum) to its coarse cell */
+static void mg_restrict(orc_case *c, int what) {
+  orc_case *cc = c->coarse;
+  for (int bi = 0; bi < cc->nb; ++bi) {
+    oblock *cb = &cc->b[bi];
+    double *dst = what == 0 ? cb->W : what == 1 ? cb->dU : cb->F;
+    memset(dst, 0, 8 * NV * cb->nc);
+  }
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    oblock *cb = &cc->b[b->mg_coarse];
+    const double *src = what == 0 ? b->W : what == 1 ? b->dU : b->mr;
+    double *dst = what == 0 ? cb->W : what == 1 ? cb->dU : cb->F;
+    int64_t x = 0;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i, ++x) {
+          const int64_t f = cell_idx(b, i, j, k), q = mg_coarse_cell(b, cb, x);
+          for (int v = 0; v < NV; ++v) {
+            const double t = what == 2 ? src[f * NV + v] : b->mg_volfac[x] * src[f * NV + v];
+            dst[q * NV + v] = dst[q * NV + v] + t;
+          }
+        }
+  }
+}
+
+/* BlockProlongation (include/gridLevel.hpp:160): the coarse correction at
+ * the coarse nodes (ConvertCellToNode without ghosts, include/utility.hpp:
+ * 187: each cell, in k, j, i order, adds to its 8 nodes; corner nodes of
+ * the block keep the sum, nodes on a block edge take half of it, all others
+ * an eighth), interpolated trilinearly to every fine cell centre
+ * (TrilinearInterp include/utility.hpp:357) and added to the fine update */
+static double lin(double d0, double d1, double c) { return (1.0 - c) * d0 + c * d1; }
+static void mg_prolong(orc_case *c) {
+  orc_case *cc = c->coarse;
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const oblock *cb = &cc->b[b->mg_coarse];
+    const int ni = cb->ni + 1, nj = cb->nj + 1, nk = cb->nk + 1;
+    double *nd = (double *)calloc((size_t)ni * nj * nk * NV, sizeof(double));
+#define NODE(i, j, k) (nd + (((size_t)(k) * nj + (j)) * ni + (i)) * NV)
+    for (int k = 0; k < cb->nk; ++k)
+      for (int j = 0; j < cb->nj; ++j)
+        for (int i = 0; i < cb->ni; ++i) {
+          const double *u = &cb->dU[cell_idx(cb, i, j, k) * NV];
+          double *t[8] = {NODE(i, j, k),         NODE(i, j + 1, k),
+                          NODE(i, j + 1, k + 1), NODE(i, j, k + 1),
+                          NODE(i + 1, j, k),     NODE(i + 1, j + 1, k),
+                          NODE(i + 1, j + 1, k + 1), NODE(i + 1, j, k + 1)};
+          for (int n = 0; n < 8; ++n)
+            for (int v = 0; v < NV; ++v) t[n][v] += u[v];
+        }
+    for (int k = 0; k < nk; ++k)
+      for (int j = 0; j < nj; ++j)
+        for (int i = 0; i < ni; ++i) {
+          const int ei = i == 0 || i == ni - 1, ej = j == 0 || j == nj - 1,
+                    ek = k == 0 || k == nk - 1;
+          const double f = (ei && ej && ek) ? 1.0 : (ei + ej + ek == 2) ? 1.0 / 2.0 : 1.0 / 8.0;
+          for (int v = 0; v < NV; ++v) NODE(i, j, k)[v] *= f;
+        }
+    int64_t x = 0;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i, ++x) {
+          const int cc = b->mg_cell[x];
+          const int ci = cc % cb->ni, cj = (cc / cb->ni) % cb->nj, ck = cc / (cb->ni * cb->nj);
+          const double *co = &b->mg_coef[7 * x];
+          const double *d[8] = {NODE(ci, cj, ck),         NODE(ci + 1, cj, ck),
+                                NODE(ci, cj + 1, ck),     NODE(ci + 1, cj + 1, ck),
+                                NODE(ci, cj, ck + 1),     NODE(ci + 1, cj, ck + 1),
+                                NODE(ci, cj + 1, ck + 1), NODE(ci + 1, cj + 1, ck + 1)};
+          const int64_t f = cell_idx(b, i, j, k);
+          for (int v = 0; v < NV; ++v) {
+            const double d04 = lin(d[0][v], d[4][v], co[0]);
+            const double d15 = lin(d[1][v], d[5][v], co[1]);
+            const double d26 = lin(d[2][v], d[6][v], co[2]);
+            const double d37 = lin(d[3][v], d[7][v], co[3]);
+            const double d0415 = lin(d04, d15, co[4]);
+            const double d2637 = lin(d26, d37, co[5]);
+            b->dU[f * NV + v] = b->dU[f * NV + v] + lin(d0415, d2637, co[6]);
+          }
+        }
+#undef NODE
+    free(nd);
+  }
+}
+
+/* A x - (L x - U x) - b per physical cell of every block of level c
+ * (linearSolver::AXmB src/linearSolver.cpp:58), added to the restricted
+ * matrix residual already in F: the coarse level's forcing (gridLevel::
+ * Restriction src/gridLevel.cpp:571-589) */
+static void mg_forcing(orc_case *c) {
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const int s = b->solve;
+    for (int k = 0; k < b->nk; ++k)
+      for (int j = 0; j < b->nj; ++j)
+        for (int i = 0; i < b->ni; ++i) {
+          const int64_t x = cell_idx(b, i, j, k);
+          double L[NV + 2], U[NV + 2], u[NV + 2], r[NV + 2], Ax[NV + 2];
+          offdiag_sum(c, b, x, 1, L);
+          offdiag_sum(c, b, x, 0, U);
+          get_du(b, x, u);
+          rhs_b(c, b, x, r);
+          if (c->s[s].block) {
+            mat_vec(&b->Ab[x * NJAC], u, Ax);
+          } else {
+            for (int v = 0; v < NV; ++v) Ax[v] = u[v] * b->A[x];
+          }
+          for (int v = 0; v < NV; ++v) {
+            const double off = L[v] - U[v];
+            const double axmb = Ax[v] - off - r[v];
+            b->F[x * NV + v] = axmb + b->F[x * NV + v];
+          }
+        }
+  }
+}
+
+/* mgSolution::CycleAtLevel (src/mgSolution.cpp:160-207) from level c:
+ * relaxation (the coarsest level: matrixSweeps; the others max(matrixSweeps
+ * / 2, 1) before and after the coarse-grid correction), each ending with a
+ * ghost swap and the matrix residual f - (A x - b) */
+static void mg_cycle(orc_case *c) {
+  orc_case *cc = c->coarse;
+  if (!cc) {
+    relax_sweeps(c, 0);
+    swap_du(c);
+    matrix_residual(c);
+    return;
+  }
+  relax_sweeps(c, 1);
+  swap_du(c);
+  matrix_residual(c);
+  /* gridLevel::Restriction (src/gridLevel.cpp:538): the state, then the
+   * coarse residual, time step and diagonal from it, the update, and the
+   * forcing */
+  mg_restrict(c, 0);
+  cc->iter = c->iter;
+  cc->mg_visits += 1;
+  orc_fill_ghosts(cc);
+  orc_residual(cc);
+  orc_timestep(cc);
+  orc_diag_invert(cc);
+  mg_restrict(c, 1);
+  swap_du(cc);
+  mg_restrict(c, 2);
+  mg_forcing(cc);
+  size_t tot = 0;
+  for (int bi = 0; bi < cc->nb; ++bi) tot += (size_t)cc->b[bi].nc * NV;
+  double *du0 = (double *)malloc(8 * (tot ? tot : 1));
+  size_t o = 0;
+  for (int bi = 0; bi < cc->nb; ++bi) {
+    memcpy(du0 + o, cc->b[bi].dU, 8 * NV * cc->b[bi].nc);
+    o += (size_t)cc->b[bi].nc * NV;
+  }
+  for (int n = 0; n < c->mg_cycle; ++n) mg_cycle(cc);
+  o = 0;
+  for (int bi = 0; bi < cc->nb; ++bi) {
+    oblock *cb = &cc->b[bi];
+    for (int64_t q = 0; q < cb->nc * NV; ++q) cb->dU[q] -= du0[o + q];
+    o += (size_t)cb->nc * NV;
+  }
+  free(du0);
+  mg_prolong(c);
+  relax_sweeps(c, 1);
+  swap_du(c);
+  matrix_residual(c);
+}
+
+/* Links level c to its next coarser level: maps[b] is the transfer of
+ * block b of c (ath_setup_mg_map) */
+void orc_set_coarse(orc_case *c, orc_case *coarse, int cycle, const ath_mg_map *maps) {
+  c->coarse = coarse;
+  c->mg_cycle = cycle;
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    const int64_t n = maps[bi].ncells;
+    b->mg_coarse = maps[bi].coarse_block;
+    b->mg_cell = (int32_t *)dup_arr(maps[bi].coarse_cell, 4 * n);
+    b->mg_volfac = (double *)dup_arr(maps[bi].volfac, 8 * n);
+    b->mg_coef = (double *)dup_arr(maps[bi].coef, 8 * 7 * n);
+    if (!b->mr) b->mr = (double *)calloc((size_t)b->nc * NV, sizeof(double));
+  }
+  for (int bi = 0; bi < coarse->nb; ++bi) {
+    oblock *cb = &coarse->b[bi];
+    if (!cb->F) cb->F = (double *)calloc((size_t)cb->nc * NV, sizeof(double));
+    if (!cb->mr) cb->mr = (double *)calloc((size_t)cb->nc * NV, sizeof(double));
+  }
+}
+
+void orc_relax(orc_case *c) {
+  relax_init(c);
+  if (c->coarse) {
+    for (orc_case *l = c->coarse; l; l = l->coarse) l->mg_visits = 0;
+    mg_cycle(c);
+    return;
+  }
+  relax_sweeps(c, 0);
   swap_du(c);
   if (c->matrix_resid) matrix_residual(c);
 }

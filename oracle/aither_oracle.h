@@ -35,6 +35,11 @@ void orc_set_threads(orc_case *c, int nthreads);
 /* Also compute the logged matrix residual in orc_relax (the reference
  * always does, src/linearSolver.cpp:470); read it with orc_matrix_resid. */
 void orc_set_matrix_resid(orc_case *c, int on);
+/* Multigrid: link level c to its next coarser level `coarse` (cycle index 1
+ * V, 2 W); maps[b] is the transfer of block b of c (ath_setup_mg_map).
+ * orc_relax of the finest level then runs the cycle over the linked levels
+ * (mgSolution::CycleAtLevel, src/mgSolution.cpp:160). */
+void orc_set_coarse(orc_case *c, orc_case *coarse, int cycle, const ath_mg_map *maps);
 double orc_matrix_resid(const orc_case *c, int solve);
 
 /* Integrated wall forces of the last residual evaluation: sum over the

@@ -49,8 +49,15 @@ def lib():
         L.orc_set_state.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
         L.orc_set_state_nm1.restype = C.c_int
         L.orc_set_state_nm1.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+        from aither_gb300._lib import MgMap
+        L.orc_set_coarse.argtypes = [vp, vp, C.c_int, C.POINTER(MgMap)]
         _lib = L
     return _lib
+
+
+def lib_setup():
+    from aither_gb300._lib import lib as product_lib
+    return product_lib()
 
 
 def _dp(a):
@@ -73,11 +80,33 @@ class Oracle:
             lib().orc_set_threads(self.h, threads)
         if matrix_resid:
             lib().orc_set_matrix_resid(self.h, 1)
+        # coarser multigrid levels, each linked to the next finer one
+        self.levels = []
+        fine = self.h
+        for lv in range(1, setup.levels()):
+            ns, nb, _ = setup.level_counts(lv)
+            lbv = (BlockView * nb)(*[setup.block_view(b, lv) for b in range(nb)])
+            lsv = (SolveView * ns)(*[setup.solve_view(s, lv) for s in range(ns)])
+            h = lib().orc_create(nb, lbv, ns, lsv)
+            if threads:
+                lib().orc_set_threads(h, threads)
+            nfine = setup.level_counts(lv - 1)[1]
+            from aither_gb300._lib import MgMap, check
+            maps = (MgMap * nfine)()
+            for b in range(nfine):
+                check(lib_setup().ath_setup_mg_map(setup.h, lv - 1, b, C.byref(maps[b])))
+            cycle = setup.solve_view(0, lv - 1).mg_cycle
+            lib().orc_set_coarse(fine, h, cycle, maps)
+            self.levels.append(h)
+            fine = h
 
     def close(self):
         if self.h:
             lib().orc_destroy(self.h)
             self.h = None
+        for h in getattr(self, "levels", []):
+            lib().orc_destroy(h)
+        self.levels = []
 
     def __del__(self):
         try:

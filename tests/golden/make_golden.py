@@ -42,6 +42,24 @@ REFCASE_DIR = os.path.join(HERE, "refcases")
 
 # (fixture name, generator, kwargs, iterations, full fields?)
 CASES = [
+    # multigrid (coarse-grid correction of the linear system): V and W
+    # cycles over 2 and 3 levels with LU-SGS (1 and 3 sweeps), DP-LUR, block
+    # LU-SGS and block DP-LUR; the plates have an interblock connection on
+    # every level
+    ("bump_mg_v", cases.bump_channel,
+     dict(ni=24, nj=12, nk=4, height=0.08, mach=0.7, multigrid=(2, "V")), [1, 15], True),
+    ("bump_mg_w3", cases.bump_channel,
+     dict(ni=26, nj=14, nk=5, height=0.07, mach=0.6, sweeps=3, multigrid=(3, "W")),
+     [1, 15], True),
+    ("bump_mg_dplur", cases.bump_channel,
+     dict(ni=20, nj=12, nk=3, height=0.08, mach=0.7, matrix_solver="dplur", sweeps=3,
+          multigrid=(3, "V")), [1, 15], True),
+    ("plate_mg_blusgs", cases.flat_plate,
+     dict(ni=12, nj=10, nk=2, dy0=1e-3, ratio=1.3, matrix_solver="blusgs", sweeps=2,
+          multigrid=(2, "W")), [1, 15], True),
+    ("plate_mg_bdplur", cases.flat_plate,
+     dict(ni=14, nj=8, nk=2, dy0=1e-3, ratio=1.3, cfl=20.0, matrix_solver="bdplur", sweeps=4,
+          multigrid=(3, "V")), [1, 15], True),
     ("vortex16", cases.vortex_box, dict(ni=16, nj=8, nk=4), [1, 20], True),
     ("bump24", cases.bump_channel, dict(ni=24, nj=12, nk=4, height=0.08, mach=0.7), [1, 30], True),
     ("bump_sup", cases.bump_channel, dict(ni=20, nj=10, nk=3, height=0.10, mach=0.85), [1, 40], True),
@@ -165,6 +183,7 @@ REFCASES = [
     ("viscousFlatPlate", [1, 20], None),
     ("rae2822", [1, 20], (1, 8)),
     ("shockTube", [1, 4], None),
+    ("transonicBump", [1, 20], None),
 ]
 
 

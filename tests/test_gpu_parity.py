@@ -22,6 +22,12 @@ CELL_TOL = 1e-12
 NORM_TOL = 1e-10
 
 
+# multigrid: V and W cycles over 2 and 3 levels, LU-SGS (1 and 3 sweeps),
+# DP-LUR, block LU-SGS and block DP-LUR (two-block laminar plates)
+MG_CASES = [f"{c}_it{n}" for c in ("bump_mg_v", "bump_mg_w3", "bump_mg_dplur",
+                                   "plate_mg_blusgs", "plate_mg_bdplur") for n in (1, 15)]
+
+
 @pytest.fixture(scope="module")
 def ctx():
     from aither_gb300 import Context
@@ -74,7 +80,7 @@ def _cols_err(a, b):
                                   "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
                                   "bump_nr_out_it1", "bump_nr_out_it20", "bump_nr_both_bdf2_it1",
                                   "bump_nr_both_bdf2_it8", "chan_nr_out_visc_it1",
-                                  "chan_nr_out_visc_it10"])
+                                  "chan_nr_out_visc_it10", *MG_CASES])
 def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
     inp, st, g = golden_case(name, str(tmp_path))
     s, b = _batch(ctx, inp, st)

@@ -32,7 +32,9 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "vortex_cn_dual_it1", "vortex_cn_dual_it4", "plate_bdf2_blusgs_it1", "plate_bdf2_blusgs_it4",
         "sst_plate_bdf2_it1", "sst_plate_bdf2_it4", "bump_nr_out_it1", "bump_nr_out_it20",
         "bump_nr_both_bdf2_it1", "bump_nr_both_bdf2_it8", "chan_nr_out_visc_it1",
-        "chan_nr_out_visc_it10"]
+        "chan_nr_out_visc_it10", "bump_mg_v_it1", "bump_mg_v_it15", "bump_mg_w3_it1",
+        "bump_mg_w3_it15", "bump_mg_dplur_it1", "bump_mg_dplur_it15", "plate_mg_blusgs_it1",
+        "plate_mg_blusgs_it15", "plate_mg_bdplur_it1", "plate_mg_bdplur_it15"]
 
 
 def _oracle(inp, st):
@@ -67,7 +69,8 @@ def test_oracle_matches_reference_fixture(name, tmp_path):
 @pytest.mark.parametrize("name", ["vortex16_it20", "bump24_it30", "bump_sup_it40",
                                   "bump_blusgs_it20", "bump_sweeps3_it20",
                                   "plate_blusgs_sw2_it20", "vortex_bdf2_it4",
-                                  "vortex_cn_dual_it4", "sst_plate_bdf2_it4"])
+                                  "vortex_cn_dual_it4", "sst_plate_bdf2_it4",
+                                  "bump_mg_w3_it15", "plate_mg_blusgs_it15"])
 def test_oracle_matrix_residual(name, tmp_path):
     """The logged linear-system residual (linearSolver::Residual)."""
     from aither_gb300 import Setup

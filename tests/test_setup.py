@@ -134,11 +134,10 @@ def test_geometry_matches_reference(tmp_path):
         assert np.array_equal(a[tuple(ext)], R["b0_" + nm][tuple(ext)])
 
 
-def test_nonreflecting_inlet_parsed_and_outlet_rejected(tmp_path):
+def test_nonreflecting_inlet_and_outlet_parsed(tmp_path):
     """inlet(...; nonreflecting=true; lengthScale=L) is accepted with L over
-    the reference length; a nonreflecting pressure outlet (its transverse
-    terms need cell gradients that are not kept) and nonreflecting without
-    lengthScale are setup errors."""
+    the reference length, and so is a nonreflecting pressure outlet;
+    nonreflecting without lengthScale is a setup error."""
     from aither_gb300 import Setup, cases
     from aither_gb300._lib import AthError
     kw = dict(ni=8, nj=4, nk=2, height=0.05, mach=0.4, inflow="inlet", outflow="pressure")
@@ -154,10 +153,49 @@ def test_nonreflecting_inlet_parsed_and_outlet_rejected(tmp_path):
     bad = text.replace("pressureOutlet(tag=4; pressure=",
                        "pressureOutlet(tag=4; nonreflecting=true; lengthScale=1.0; pressure=")
     open(inp, "w").write(bad)
-    with pytest.raises(AthError):
-        Setup(inp)
+    s = Setup(inp)
+    sv = s.solve_view(0)
+    po = [sv.states[i] for i in range(sv.nstates) if sv.states[i].nonreflecting]
+    assert len(po) == 2 and po[1].length_scale == 1.0 / sv.l_ref
+    s.close()
     bad = re.sub(r"; lengthScale=[^;)]*", "", text)
     assert "nonreflecting=true" in bad and "lengthScale" not in bad
     open(inp, "w").write(bad)
     with pytest.raises(AthError, match="lengthScale"):
+        Setup(inp)
+
+
+def test_multigrid_levels(tmp_path):
+    """multigridLevels: each coarser level keeps every node a boundary
+    surface starts or ends on and otherwise every other node
+    (procBlock::GetCoarseMeshAndBCs); the transfer maps restrict with
+    weights that sum to one per coarse cell and prolong with coefficients
+    in [0, 1] on these box-like cells; turbulence equations, time-accurate
+    solves and nonreflecting boundaries are refused with multigrid."""
+    from aither_gb300 import Setup, cases
+    from aither_gb300._lib import AthError
+    inp, _ = cases.bump_channel(str(tmp_path / "a"), ni=26, nj=14, nk=5, height=0.07, mach=0.6,
+                                multigrid=(3, "W"))
+    s = Setup(inp)
+    assert s.levels() == 3
+    dims = [(s.block_view(0, lv).ni, s.block_view(0, lv).nj, s.block_view(0, lv).nk)
+            for lv in range(3)]
+    assert dims == [(26, 14, 5), (13, 7, 3), (7, 4, 2)]
+    assert s.solve_view(0, 1).mg_cycle == 2 and s.solve_view(0, 0).mg_levels == 3
+    for lv in range(2):
+        m = s.mg_map(lv, 0)
+        nc = s.level_counts(lv + 1)[2]
+        sums = np.bincount(m["coarse_cell"], weights=m["volfac"], minlength=nc)
+        assert np.allclose(sums, 1.0, atol=1e-14)
+        assert m["coef"].min() >= -1e-12 and m["coef"].max() <= 1 + 1e-12
+    s.close()
+    for kw in (dict(time="bdf2", dt=1e-5, nl=3), dict(inflow="inlet", outflow="pressure",
+                                                      nonreflecting=1.0)):
+        inp, _ = cases.bump_channel(str(tmp_path / "b"), ni=8, nj=4, nk=2, height=0.05, mach=0.4,
+                                    multigrid=(2, "V"), **kw)
+        with pytest.raises(AthError, match="multigrid"):
+            Setup(inp)
+    inp, _ = cases.flat_plate(str(tmp_path / "c"), ni=8, nj=6, nk=2, dy0=1e-3, ratio=1.3,
+                              rans=True, nblocks=1, multigrid=(2, "V"))
+    with pytest.raises(AthError, match="multigrid"):
         Setup(inp)
