@@ -154,9 +154,15 @@ def run_native(args, rank: int, world: int, device: int):
             continue
         batch = Batch(ctx, setup, prec,
                       BATCH_FAST_FACES if (args.fast_faces and prec == PREC_FP64) else 0)
+        if args.sweep_shape:
+            sh = [int(x) for x in args.sweep_shape.split(",")] + [0]
+            batch.set_sweep_shape(sh[0], sh[1], sh[2])
         for _ in range(args.warmup):
             batch.iterate(1)
-        sweep_threads = batch.autotune(3)  # restores the state it ran on
+        if args.sweep_shape:
+            sweep_threads = sh[1]
+        else:
+            sweep_threads = batch.autotune(3)  # restores the state it ran on
         shape = batch.sweep_shape()
         _barrier(world)
         clocks = ClockSampler(device)
@@ -182,7 +188,7 @@ def run_native(args, rank: int, world: int, device: int):
         res["e2e"] = run_e2e(batch, ncells, args.steps, world)
         batch.close()
         out[prec_name] = res
-        if prec == PREC_FP64 and args.fast_faces:
+        if prec == PREC_FP64 and args.fast_faces and args.exact_arm:
             # the bit-exact faces on the same workload, for comparison
             ex = Batch(ctx, setup, prec)
             for _ in range(args.warmup):
@@ -201,6 +207,8 @@ def run_native(args, rank: int, world: int, device: int):
         out["converge"] = run_converge(args, ctx, setup, specs, world)
     if args.vortex_iters > 0:
         out["vortex"] = run_vortex(args, ctx, world)
+    if args.mg_iters > 0 and args.converge_drop > 0:
+        out["multigrid"] = run_mg(args, ctx, world)
     if args.sst_steps > 0:
         out["sst"] = run_sst(args, ctx, world)
     if args.plate_iters > 0:
@@ -503,6 +511,43 @@ def run_converge(args, ctx, setup, specs, world):
     return out
 
 
+def run_mg(args, ctx, world):
+    """Multigrid against single-grid relaxation on one transonic bump channel
+    with the scheme of the reference's multigrid case (testCases/
+    transonicBump: Euler, upwind MUSCL with van Albada, DP-LUR with 4 sweeps,
+    three levels, W cycle; here at CFL 1000): iterations and device time to
+    the residual drop, FP64 and mixed."""
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Setup, cases
+    ni, nj = args.mg_ni, args.mg_nj
+    out = {"workload": f"transonic bump channel {ni}x{nj}x2 cells, Mach 0.7, bump 8 % of the "
+                       "chord, Euler, upwind MUSCL with van Albada, Roe, DP-LUR 4 sweeps, "
+                       "CFL 1000",
+           "cells": ni * nj * 2, "drop": args.converge_drop, "max_iterations": args.mg_iters}
+    for label, mg in (("multigrid_w3", (3, "W")), ("single_grid", None)):
+        with tempfile.TemporaryDirectory() as tmp:
+            inp, _ = cases.bump_channel(tmp, ni=ni, nj=nj, nk=2, height=0.08, mach=0.7,
+                                        cfl=1000.0, matrix_solver="dplur", sweeps=4,
+                                        recon="upwind", limiter="vanAlbada", multigrid=mg,
+                                        name="tb")
+            setup = Setup(inp)
+        res = {}
+        for pname, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+            b = Batch(ctx, setup, prec)
+            _barrier(world)
+            info = b.converge(args.mg_iters, args.converge_drop, check_every=50)
+            st = b.stats()
+            b.close()
+            x = info[0]
+            its = max(int(x.iterations), 1)
+            dev_s = _max_over_ranks(st.device_ms * 1e-3, world)
+            res[pname] = {"iterations": int(x.iterations), "converged": bool(x.converged == 1),
+                          "drop_reached": x.drop, "device_s": dev_s,
+                          "ms_per_iteration": dev_s * 1e3 / its,
+                          "gpu_launches_per_iteration": int(st.kernel_launches) // its}
+        out[label] = res
+    return out
+
+
 def run_e2e(batch, ncells: int, steps: int, world: int) -> dict:
     n = batch.pool_cells()
     host = _pinned(batch.pool_vars() * n)
@@ -655,6 +700,16 @@ def main():
     ap.add_argument("--sst-nj", type=int, default=192)
     ap.add_argument("--sst-nk", type=int, default=4)
     ap.add_argument("--served-max-iters", type=int, default=6000)
+    ap.add_argument("--mg-iters", type=int, default=3000,
+                    help="iteration cap of the multigrid section (0: skip it)")
+    ap.add_argument("--mg-ni", type=int, default=256)
+    ap.add_argument("--mg-nj", type=int, default=128)
+    ap.add_argument("--sweep-shape", default=None,
+                    help="mode,threads[,cluster]: a fixed LU-SGS sweep shape for the batched "
+                         "arms instead of the autotuner's pick (mode 0: a thread per cell, 2: "
+                         "lanes per neighbour term, 1: persistent clusters, 3: tile queue)")
+    ap.add_argument("--exact-arm", type=int, default=1,
+                    help="also time the bit-exact FP64 faces when --fast-faces is on")
     ap.add_argument("--converge-fp64-cases", type=int, default=8,
                     help="smallest cases also run to convergence in FP64 for the comparison")
     args = ap.parse_args()
@@ -773,6 +828,8 @@ def main():
         line["sst"] = res["sst"]
     if "vortex" in res:
         line["vortex"] = res["vortex"]
+    if "multigrid" in res:
+        line["multigrid"] = res["multigrid"]
     if "fp64_exact" in res:
         line["fp64_exact"] = res["fp64_exact"]
     if "plate" in res:
