@@ -36,6 +36,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 # .cu units and their arithmetic flags
 CU_UNITS = {
     "kernels_fp64.cu": ["--fmad=false"],
+    "kernels_fp64_fast.cu": ["--fmad=true"],
     "kernels_fp32.cu": ["--fmad=true"],
     "batch.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],

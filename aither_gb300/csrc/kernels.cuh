@@ -191,6 +191,10 @@ struct Pools {
   // after each update, src/mgSolution.cpp:225-228)
   T *Fq, *MRq;
   int mg_accum;
+  // FP64 batches with the fast-arithmetic option: the launchers run the
+  // faces, cell, scalar sweep and update kernels built with contracted
+  // multiply-adds (kernels_fp64_fast.cu); a host-side switch
+  int fast_fp64;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -309,6 +313,22 @@ __global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sst
 
 // Host-side launchers, one instantiation per arithmetic type (defined in
 // kernels_fp64.cu / kernels_fp32.cu).
+// The fast FP64 faces of direction d (k_face<double, d, false, true>),
+// compiled in their own unit with contracted multiply-adds: roundoff-equal
+// to the reference's faces, not bit-equal.
+void LaunchFastFaceFp64(int d, const Pools<double> &P, const int32_t *list,
+                        const int32_t *cta_block, int ncta, cudaStream_t s);
+// The cell kernel, the scalar LU-SGS sweeps and the update of FP64 batches
+// with the fast option, from the same unit (same arguments as
+// Launch<double>::Cell / Sweep / Update; the sweep: scalar solves only).
+void LaunchFastCellFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
+                        int ncta, int kinds, cudaStream_t s);
+void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int forward,
+                         int sweep, bool full, int threads, bool group, cudaStream_t s);
+void LaunchFastUpdateFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
+                          const int32_t *cta_pos0, NormPartial *partials, int ncta,
+                          const SolveState *ss, cudaStream_t s);
+
 // Transfer between a multigrid level (fine) and the next coarser one.
 // Restriction is a gather per coarse physical cell c over its fine cells
 // e in [off[c], off[c+1]), in the fine cells' k, j, i order; prolongation

@@ -812,7 +812,7 @@ __device__ __forceinline__ void FaceFluxMixed(const Pools<PT> &P, const SolveDev
 }
 
 template <typename T, int D, bool RANS, bool FAST = false>
-__global__ void __launch_bounds__(kCta) k_face(Pools<T> P, const int32_t *list,
+__global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
@@ -3129,11 +3129,16 @@ void Launch<T>::ViscFace(int d, const Pools<T> &P, const int32_t *list,
 template <typename T, int D>
 static void LaunchFace(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        int ncta, int rkinds, cudaStream_t s) {
-  // rkinds bit 2: the fast-face option of FP64 batches (non-RANS solves)
-  if ((rkinds & 1) && (rkinds & 4) && std::is_same<T, double>::value)
-    k_face<T, D, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  else if (rkinds & 1)
-    k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  // rkinds bit 2: the fast-face option of FP64 batches (non-RANS solves),
+  // compiled in its own unit with contracted multiply-adds
+  bool fast = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if ((rkinds & 1) && (rkinds & 4)) {
+      LaunchFastFaceFp64(D, P, list, cta_block, ncta, s);
+      fast = true;
+    }
+  }
+  if ((rkinds & 1) && !fast) k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
   if (rkinds & 2) k_face<T, D, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
@@ -3148,6 +3153,12 @@ template <typename T>
 void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                      int ncta, int kinds, cudaStream_t s) {
   if (ncta <= 0) return;
+  if constexpr (std::is_same<T, double>::value) {
+    if (P.fast_fp64) {
+      LaunchFastCellFp64(P, list, cta_block, ncta, kinds, s);
+      return;
+    }
+  }
   if (kinds & 1) k_cell<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
   if (kinds & 2) k_cell<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
@@ -3155,7 +3166,15 @@ template <typename T>
 void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
                       bool full, int kinds, int threads, bool group, cudaStream_t s) {
   if (n <= 0) return;
-  if ((kinds & 1) && group) {
+  bool fast = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (P.fast_fp64 && (kinds & 1)) {
+      LaunchFastSweepFp64(P, items, n, forward, sweep, full, threads, group, s);
+      fast = true;
+    }
+  }
+  if (fast) {
+  } else if ((kinds & 1) && group) {
     const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
     const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
     if (full) k_sweepg<T, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
@@ -3291,6 +3310,12 @@ template <typename T>
 void Launch<T>::Update(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        const int32_t *cta_pos0, NormPartial *partials, int ncta,
                        const SolveState *ss, cudaStream_t s) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (P.fast_fp64) {
+      LaunchFastUpdateFp64(P, list, cta_block, cta_pos0, partials, ncta, ss, s);
+      return;
+    }
+  }
   if (ncta > 0) k_update<T><<<ncta, kCta, 0, s>>>(P, list, cta_block, cta_pos0, partials, ss);
 }
 template <typename T>

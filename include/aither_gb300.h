@@ -299,8 +299,10 @@ const char *ath_last_error(void);
  * does, src/linearSolver.cpp:470); bit 1 (ATH_BATCH_FAST_FACES) = FP64
  * batches evaluate the MUSCL reconstruction and the Roe flux of solves
  * without turbulence equations in a rearranged form with fewer divisions
- * and square roots (FP64 throughout; equal to the reference to roundoff,
- * about 1e-15 per face, instead of bit for bit). */
+ * and square roots, and run the faces, the cell kernel, the scalar LU-SGS
+ * hyperplane sweeps and the update with contracted multiply-adds (FP64
+ * throughout; equal to the reference to roundoff, about 1e-15 per face,
+ * instead of bit for bit). */
 enum { ATH_BATCH_MATRIX_RESID = 1, ATH_BATCH_FAST_FACES = 2 };
 int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision,
                      int flags, ath_batch **out);
