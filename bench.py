@@ -149,6 +149,12 @@ def run_native(args, rank: int, world: int, device: int):
     nsolves, nblocks, ncells = setup.counts()
     ctx = Context(device)
     out = {"fp64_peak_tflops": ctx.fp64_peak(5)}
+    # the same setup with the cells' geometry and wall distance on the device
+    with tempfile.TemporaryDirectory() as tmp:
+        inps, _ = make_workload(tmp, args.ncases)
+        t0 = time.time()
+        Setup(inps, device=device).close()
+        out["setup_device_s"] = time.time() - t0
     for prec_name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
         if args.precision not in ("both", prec_name):
             continue
@@ -811,6 +817,7 @@ def main():
             "dtype": "f64" if "fp64" in res else "f32+f64",
             "data": "synthetic (seeded bump-channel grids)", "config": config,
             "cells": ncells, "solves": nsolves, "setup_s": t_setup,
+            "setup_device_s": res.get("setup_device_s"),
             "gpu_launches": fp["gpu_launches"], "clocks": fp["clocks"],
             "e2e": fp["e2e"], "roofline": roof, "roofline_fp64": roof_fp64, "kernel_ms": km,
             "autotune": {"sweep_threads": fp["sweep_threads"], "sweep_shape": fp["sweep_shape"]}}
