@@ -18,9 +18,9 @@ BC = dict(SLIP_WALL=0, VISCOUS_WALL=1, CHARACTERISTIC=2, STAGNATION_INLET=3,
           PRESSURE_OUTLET=4, SUPERSONIC_INFLOW=5, SUPERSONIC_OUTFLOW=6,
           PERIODIC=7, INTERBLOCK=8)
 PREC_FP64, PREC_MIXED = 0, 1
-BATCH_MATRIX_RESID, BATCH_FAST_FACES = 1, 2
+BATCH_MATRIX_RESID, BATCH_FAST_FACES, BATCH_OUTPUT_GRADS = 1, 2, 4
 FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
-             WALLDIST=9, CONS_N=10, CONS_NM1=11)
+             WALLDIST=9, CONS_N=10, CONS_NM1=11, GRADS=12)
 
 
 class GhostOp(C.Structure):
@@ -126,7 +126,7 @@ class BlockFields(C.Structure):
     """ath_block_fields: host fields of one block for the output writers."""
     _fields_ = [("prim", C.c_void_p), ("dt", C.c_void_p), ("resid", C.c_void_p),
                 ("aux", C.c_void_p), ("velgrad", C.c_void_p), ("wall_dist", C.c_void_p),
-                ("cons_nm1", C.c_void_p)]
+                ("cons_nm1", C.c_void_p), ("grads", C.c_void_p)]
 
 
 class Stats(C.Structure):
@@ -156,6 +156,7 @@ def lib() -> C.CDLL:
             "ath_setup_solve": (C.c_int, [vp, C.c_int, C.POINTER(SolveView)]),
             "ath_setup_set_state": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
             "ath_setup_levels": (C.c_int, [vp, C.POINTER(C.c_int)]),
+            "ath_batch_flags": (C.c_int, [vp, C.POINTER(C.c_int)]),
             "ath_setup_level_counts": (C.c_int, [vp, C.c_int, C.POINTER(C.c_int),
                                                  C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
             "ath_setup_level_block": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(BlockView)]),
@@ -301,7 +302,8 @@ class Setup:
         keep = []
         arr = (BlockFields * len(blocks))()
         for k, fl in enumerate(blocks):
-            for name in ("prim", "dt", "resid", "aux", "velgrad", "wall_dist", "cons_nm1"):
+            for name in ("prim", "dt", "resid", "aux", "velgrad", "wall_dist", "cons_nm1",
+                         "grads"):
                 a = fl.get(name)
                 if a is not None:
                     a = np.ascontiguousarray(a, dtype=np.float64)

@@ -471,6 +471,11 @@ class Runner : public RunnerBase {
       P_.nrg = m.Alloc<double>(12 * (size_t)n);
       c_.mem->Zero(P_.nrg, 0, 12 * (size_t)n * sizeof(double));
     }
+    if (c.flags & 4) {
+      // the residual's cell gradients kept for output
+      P_.ogr = m.Alloc<double>(24 * (size_t)n);
+      c_.mem->Zero(P_.ogr, 0, 24 * (size_t)n * sizeof(double));
+    }
     if (c.n_nr_surf > 0) {
       P_.nr_mach = m.Alloc<double>(2 * (size_t)c.n_nr_surf);
       c_.mem->Zero(P_.nr_mach, 0, 2 * (size_t)c.n_nr_surf * sizeof(double));
@@ -653,6 +658,9 @@ class Runner : public RunnerBase {
   void NrGrads() {
     Launch<T>::NrGrads(P_, c_.d_nrg_cells, c_.d_nrg_block, (int)c_.L.nrg_cells.size(),
                        c_.stream);
+    if (P_.ogr)
+      Launch<T>::OutGrads(P_, c_.d_cells, c_.d_cell_cta_block, (int)c_.L.cell_cta_block.size(),
+                          c_.fkinds, c_.stream);
   }
   void Residual() override {
     for (int d = 0; d < 3; ++d)
@@ -1168,6 +1176,7 @@ struct ath_batch {
   double *W = nullptr, *R = nullptr, *dt = nullptr, *lam = nullptr;
   double *Wt = nullptr, *Rt = nullptr, *lamt = nullptr;  // RANS solves only
   double *Un = nullptr, *Unm1 = nullptr;  // time-accurate solves only
+  double *ogr = nullptr;  // output gradients (flag ATH_BATCH_OUTPUT_GRADS)
 };
 
 namespace ath {
@@ -1922,6 +1931,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->lamt = r->P().lamt;
     B->Un = r->P().Un;
     B->Unm1 = r->P().Unm1;
+    B->ogr = r->P().ogr;
   } else if (precision == ATH_PREC_MIXED) {
     auto *r = new Runner<float>(c);
     B->run.reset(r);
@@ -1934,6 +1944,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     B->lamt = r->P().lamt;
     B->Un = r->P().Un;
     B->Unm1 = r->P().Unm1;
+    B->ogr = r->P().ogr;
   } else {
     throw Error(ATH_ERR_ARG, "unknown precision");
   }
@@ -2403,6 +2414,8 @@ int ath_batch_field_width(ath_batch *batch, int block, int field) {
       return 5;
     case ATH_FIELD_VELGRAD:
       return 9;
+    case ATH_FIELD_GRADS:
+      return 24;
     case ATH_FIELD_WALLDIST:
       return 1;
     case ATH_FIELD_CONS_N:
@@ -2467,6 +2480,12 @@ int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h) {
       case ATH_FIELD_AINV: batch->run->GetAinv(block, out_h); break;
       case ATH_FIELD_AUX: batch->run->GetAux(block, out_h); break;
       case ATH_FIELD_VELGRAD: batch->run->GetVelGrad(block, out_h); break;
+      case ATH_FIELD_GRADS:
+        if (!batch->ogr)
+          throw ath::Error(ATH_ERR_UNSUPPORTED, "the cell gradients are kept by batches created "
+                                                "with ATH_BATCH_OUTPUT_GRADS");
+        gather(batch->ogr, 24, 24, 0, false);
+        break;
       case ATH_FIELD_WALLDIST: {
         size_t q = 0;
         for (int k = 0; k < b.nk; ++k)
@@ -2655,6 +2674,12 @@ int ath_ctx_fp64_peak(ath_ctx *ctx, int reps, double *tflops) {
     }
     *tflops = best;
   });
+}
+
+int ath_batch_flags(const ath_batch *batch, int *flags) {
+  if (!batch || !flags) return ATH_ERR_ARG;
+  *flags = batch->core.flags;
+  return ATH_OK;
 }
 
 int ath_batch_stats(ath_batch *batch, ath_stats *out) {

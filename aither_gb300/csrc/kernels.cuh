@@ -191,6 +191,9 @@ struct Pools {
   // after each update, src/mgSolution.cpp:225-228)
   T *Fq, *MRq;
   int mg_accum;
+  // [24][ncell] cell-averaged gradients of the last residual kept for
+  // output (batch flag ATH_BATCH_OUTPUT_GRADS; null otherwise)
+  double *ogr;
   // FP64 batches with the fast-arithmetic option: the launchers run the
   // faces, cell, scalar sweep and update kernels built with contracted
   // multiply-adds (kernels_fp64_fast.cu); a host-side switch
@@ -403,6 +406,10 @@ struct Launch {
   // (pool index, block) into P.nrg, from the current state and ghosts
   static void NrGrads(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block, int n,
                       cudaStream_t s);
+  // cell-averaged gradients of every physical cell for output into P.ogr
+  // (fkinds: bit 0 solves without, bit 1 with turbulence equations)
+  static void OutGrads(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                       int ncta, int fkinds, cudaStream_t s);
   // StoreOldSolution of the time-accurate solves at a time step's start;
   // block >= 0: that block's current state into both time levels
   static void StoreN(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,

@@ -2539,6 +2539,145 @@ __global__ void k_nr_grads(Pools<T> P, const int32_t *cells, const int32_t *cell
   for (int e = 0; e < 3; ++e) P.nrg[(9 + e) * n + c] = pg[e];
 }
 
+// Green-Gauss gradients at a face of direction D (upper cell c) of the NS
+// cell scalars u, v, w, T, rho, p and, for RANS, k, omega over the dual
+// cell (procBlock::CalcGradsI/J/K, src/procBlock.cpp:5173-5790): the
+// scalars at the dual cell's lower and upper faces of the other directions
+// are four-cell averages summed in the reference's order; temperature from
+// the state, p / (rho R) (src/eos.cpp:100).
+template <int D, int NS, typename PT>
+__device__ __forceinline__ void FaceGradAll(const Pools<PT> &P, const BlockDev &b,
+                                            const SolveDev &sv, int64_t c, double grad[NS][3]) {
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const int64_t cu = c, cl = c - st[D];
+  auto load = [&](int64_t x, double s[NS]) {
+    s[0] = P.W[n + x];
+    s[1] = P.W[2 * n + x];
+    s[2] = P.W[3 * n + x];
+    const double rho = P.W[x], p = P.W[4 * n + x];
+    s[3] = p / (0.0 + rho * sv.gas_r);
+    s[4] = rho;
+    s[5] = p;
+    if constexpr (NS > 6) {
+      s[6] = P.Wt[x];
+      s[7] = P.Wt[n + x];
+    }
+  };
+  auto area = [&](int e, int64_t x, double a[3]) {
+    const double *fa = P.fa[e];
+    const double m = fa[3 * n + x];
+    a[0] = fa[x] * m;
+    a[1] = fa[n + x] * m;
+    a[2] = fa[2 * n + x] * m;
+  };
+  double sl[NS], su[NS];
+  load(cl, sl);
+  load(cu, su);
+  double lo[3][NS], hi[3][NS], alo[3][3], ahi[3][3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    if (e == D) {
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        lo[e][k] = sl[k];
+        hi[e][k] = su[k];
+      }
+      double A0[3], A1[3], A2[3];
+      area(D, cu, A0);
+      area(D, cu + st[D], A1);
+      area(D, cl, A2);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (A0[r] + A1[r]);
+        alo[e][r] = 0.5 * (A0[r] + A2[r]);
+      }
+    } else {
+      double sup[NS], slp[NS], sum[NS], slm[NS];
+      load(cu + st[e], sup);
+      load(cl + st[e], slp);
+      load(cu - st[e], sum);
+      load(cl - st[e], slm);
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        hi[e][k] = 0.25 * (((sl[k] + su[k]) + sup[k]) + slp[k]);
+        lo[e][k] = 0.25 * (((sl[k] + su[k]) + sum[k]) + slm[k]);
+      }
+      double Au[3], Al[3], Aup[3], Alp[3];
+      area(e, cu, Au);
+      area(e, cl, Al);
+      area(e, cu + st[e], Aup);
+      area(e, cl + st[e], Alp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        ahi[e][r] = 0.5 * (Aup[r] + Alp[r]);
+        alo[e][r] = 0.5 * (Au[r] + Al[r]);
+      }
+    }
+  }
+  const double vol = 0.5 * (P.vol[cl] + P.vol[cu]);
+  const double invVol = 1.0 / vol;
+#pragma unroll
+  for (int k = 0; k < NS; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      double g = hi[0][k] * ahi[0][r] - lo[0][k] * alo[0][r] + hi[1][k] * ahi[1][r] -
+                 lo[1][k] * alo[1][r] + hi[2][k] * ahi[2][r] - lo[2][k] * alo[2][r];
+      grad[k][r] = g * invVol;
+    }
+}
+
+// Cell-averaged gradients of the last residual kept for output (the
+// reference's velocityGrad_, temperatureGrad_, densityGrad_, pressureGrad_,
+// tkeGrad_, omegaGrad_: one sixth of each face's, faces i low, i high, j
+// low, ...; written by WriteFunFile, src/output.cpp:309-395) of every
+// physical cell: P.ogr [24][ncell] = velocity gradient (9, row = derivative
+// axis), T, rho, p, k, omega gradients (3 each; k, omega zero without RANS).
+template <typename T, bool RANS>
+__global__ void __launch_bounds__(kCta) k_out_grads(Pools<T> P, const int32_t *list,
+                                                    const int32_t *cta_block) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const SolveDev sv = P.solves[b.solve];
+  if (!sv.active || (sv.rans != 0) != RANS) return;
+  constexpr int NS = RANS ? 8 : 6;
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+  const double sixth = 1.0 / 6.0;
+  double acc[8][3];  // k, omega stay zero without RANS
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k][0] = acc[k][1] = acc[k][2] = 0.0;
+  double g[NS][3];
+  auto add = [&]() {
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) acc[k][r] += sixth * g[k][r];
+  };
+  FaceGradAll<0, NS>(P, b, sv, c, g);
+  add();
+  FaceGradAll<0, NS>(P, b, sv, c + st[0], g);
+  add();
+  FaceGradAll<1, NS>(P, b, sv, c, g);
+  add();
+  FaceGradAll<1, NS>(P, b, sv, c + st[1], g);
+  add();
+  FaceGradAll<2, NS>(P, b, sv, c, g);
+  add();
+  FaceGradAll<2, NS>(P, b, sv, c + st[2], g);
+  add();
+  double *o = P.ogr;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) o[(r * 3 + q) * n + c] = acc[q][r];
+#pragma unroll
+  for (int k = 3; k < 8; ++k)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) o[(9 + (k - 3) * 3 + r) * n + c] = acc[k][r];
+}
+
 // Mixed-precision version of ViscFaceGather: velocities and temperatures
 // enter the dual-cell sums as offsets from the upper cell's values, formed
 // in FP64 (the temperature offset as (p rho_u - p_u rho) / (rho rho_u R)),
@@ -3220,6 +3359,13 @@ template <typename T>
 void Launch<T>::NrGrads(const Pools<T> &P, const int32_t *cells, const int32_t *cell_block,
                         int n, cudaStream_t s) {
   if (n > 0) k_nr_grads<T><<<(n + 127) / 128, 128, 0, s>>>(P, cells, cell_block, n);
+}
+template <typename T>
+void Launch<T>::OutGrads(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
+                         int ncta, int fkinds, cudaStream_t s) {
+  if (ncta <= 0) return;
+  if (fkinds & 1) k_out_grads<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if (fkinds & 2) k_out_grads<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
 void Launch<T>::SweepTq(const Pools<T> &P, const TileQueueDev &Q, int forward, int sweep,

@@ -112,7 +112,11 @@ double FunValue(const std::string &var, const Solve &sv, int pos, const ath_bloc
     return std::sqrt(cp_of(t) / cv_of(t) * p / rho);
   };
   auto aux = [&](int k) { return need(fl.aux, "auxiliary fields")[q * 5 + k]; };
-  auto vgrad = [&](int k) { return need(fl.velgrad, "velocity gradients")[q * 9 + k]; };
+  auto vgrad = [&](int k) {
+    if (fl.grads) return fl.grads[q * 24 + k];
+    return need(fl.velgrad, "velocity gradients")[q * 9 + k];
+  };
+  auto grad = [&](int k) { return need(fl.grads, "the cell gradients")[q * 24 + k]; };
   auto res = [&](int k) {
     if (k >= nv) throw Error(ATH_ERR_ARG, "output variable " + var + " needs SST");
     return need(fl.resid, "the residual")[q * nv + k];
@@ -159,6 +163,22 @@ double FunValue(const std::string &var, const Solve &sv, int pos, const ath_bloc
                                     "velGrad_uz", "velGrad_vz", "velGrad_wz"};
   for (int k = 0; k < 9; ++k)
     if (var == vg_names[k]) return vgrad(k) * (sc.a / sc.l);
+  // scalar gradients and their dimensional scales (src/output.cpp:336-395)
+  static const char *axes = "xyz";
+  for (int r = 0; r < 3; ++r) {
+    const std::string ax(1, axes[r]);
+    if (var == "tempGrad_" + ax) return grad(9 + r) * (sc.t / sc.l);
+    if (var == "densityGrad_" + ax) return grad(12 + r) * (sc.r / sc.l);
+    if (var == "pressGrad_" + ax) return grad(15 + r) * (sc.r * sc.a * sc.a / sc.l);
+    if (var == "tkeGrad_" + ax) {
+      if (nv < 7) throw Error(ATH_ERR_ARG, "output variable " + var + " needs SST");
+      return grad(18 + r) * (sc.a * sc.a / sc.l);
+    }
+    if (var == "omegaGrad_" + ax) {
+      if (nv < 7) throw Error(ATH_ERR_ARG, "output variable " + var + " needs SST");
+      return grad(21 + r) * (sc.a * sc.a * sc.r / (sc.mu * sc.l));
+    }
+  }
   if (var == "resid_mass") return res(0) * (sc.r * sc.a * sc.l * sc.l);
   if (var == "resid_mom_x") return res(1) * (sc.r * sc.a * sc.a * sc.l * sc.l);
   if (var == "resid_mom_y") return res(2) * (sc.r * sc.a * sc.a * sc.l * sc.l);
@@ -469,13 +489,13 @@ std::string ResidLine(bool rans, int nn, int mm, double time_step, bool restarte
 
 // per-block fields of one solve gathered from a batch
 struct Gathered {
-  std::vector<std::vector<double>> prim, dt, resid, aux, velgrad, wd, nm1;
+  std::vector<std::vector<double>> prim, dt, resid, aux, velgrad, wd, nm1, grads;
   std::vector<ath_block_fields> f;
 };
 
 void GatherFields(ath_batch *batch, const Setup &s, const Solve &sv, bool want_dt,
                   bool want_resid, bool want_aux, bool want_velgrad, bool want_wd, Gathered &g,
-                  bool want_nm1 = false) {
+                  bool want_nm1 = false, bool want_grads = false) {
   const size_t nb = sv.blocks.size();
   g.prim.resize(nb);
   g.nm1.resize(nb);
@@ -484,6 +504,7 @@ void GatherFields(ath_batch *batch, const Setup &s, const Solve &sv, bool want_d
   g.aux.resize(nb);
   g.velgrad.resize(nb);
   g.wd.resize(nb);
+  g.grads.resize(nb);
   g.f.assign(nb, ath_block_fields{});
   auto get = [&](int bi, int field, std::vector<double> &out, size_t w) {
     out.resize(Cells(s.blocks[bi]) * w);
@@ -498,7 +519,8 @@ void GatherFields(ath_batch *batch, const Setup &s, const Solve &sv, bool want_d
     if (want_dt) g.f[k].dt = get(bi, ATH_FIELD_DT, g.dt[k], 1);
     if (want_resid) g.f[k].resid = get(bi, ATH_FIELD_RESID, g.resid[k], nv);
     if (want_aux) g.f[k].aux = get(bi, ATH_FIELD_AUX, g.aux[k], 5);
-    if (want_velgrad) g.f[k].velgrad = get(bi, ATH_FIELD_VELGRAD, g.velgrad[k], 9);
+    if (want_grads) g.f[k].grads = get(bi, ATH_FIELD_GRADS, g.grads[k], 24);
+    if (want_velgrad && !want_grads) g.f[k].velgrad = get(bi, ATH_FIELD_VELGRAD, g.velgrad[k], 9);
     if (want_wd) g.f[k].wall_dist = get(bi, ATH_FIELD_WALLDIST, g.wd[k], 1);
     if (want_nm1) g.f[k].cons_nm1 = get(bi, ATH_FIELD_CONS_NM1, g.nm1[k], nv);
   }
@@ -586,10 +608,20 @@ int ath_batch_write_function(ath_batch *batch, const ath_setup *setup, int solve
     const Solve &sv = SolveOf(setup, solve);
     const auto vars = SplitVars(variables, sv);
     Gathered g;
+    // the scalar gradients come from the batch's kept gradients, and the
+    // velocity gradient too where the batch keeps them
+    const bool scalar_grads = Wants(vars, {}, "tempGrad_") || Wants(vars, {}, "densityGrad_") ||
+                              Wants(vars, {}, "pressGrad_") || Wants(vars, {}, "tkeGrad_") ||
+                              Wants(vars, {}, "omegaGrad_");
+    int flags = 0;
+    const int rc = ath_batch_flags(batch, &flags);
+    if (rc != ATH_OK) throw Error(rc, ath_last_error());
+    const bool kept = (flags & ATH_BATCH_OUTPUT_GRADS) != 0;
     GatherFields(batch, setup->s, sv, Wants(vars, {"dt"}), Wants(vars, {}, "resid_"),
                  Wants(vars, {"temperature", "cp", "cv", "viscosity", "viscosityRatio",
                               "turbulentViscosity", "f1", "f2"}),
-                 Wants(vars, {}, "velGrad_"), Wants(vars, {"wallDistance"}), g);
+                 Wants(vars, {}, "velGrad_"), Wants(vars, {"wallDistance"}), g, false,
+                 scalar_grads || (kept && Wants(vars, {}, "velGrad_")));
     WriteFunction(setup->s, sv, vars, g.f.data(), path);
   });
 }

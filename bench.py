@@ -215,6 +215,8 @@ def run_native(args, rank: int, world: int, device: int):
         out["vortex"] = run_vortex(args, ctx, world)
     if args.mg_iters > 0 and args.converge_drop > 0:
         out["multigrid"] = run_mg(args, ctx, world)
+    if args.long_iters_c2 > 0 or args.long_iters_c3 > 0:
+        out["long"] = run_long(args, ctx, world)
     if args.sst_steps > 0:
         out["sst"] = run_sst(args, ctx, world)
     if args.plate_iters > 0:
@@ -452,6 +454,58 @@ def run_plate(args, ctx, world):
                                "sample": "10 iterations after 1 warm-up; oracle, OpenMP over "
                                          "the two blocks"}
         orc.close()
+    return out
+
+
+def run_long(args, ctx, world):
+    """The single-case configurations run to convergence rather than timed
+    for a fixed count: c2 (the laminar two-block plate with block LU-SGS
+    and 4 sweeps, here with wall-normal growth 1.15 capped at 0.05 L so the
+    domain clears the boundary layer; to a 1e-8 drop) and c3 (the SST plate
+    with a CFL ramp from 1 by 0.009 per iteration to 10; 5000 iterations).
+    Per path: iterations run, the drop reached, device time, and whether the
+    state stayed physical."""
+    import numpy as np
+
+    from aither_gb300 import PREC_FP64, PREC_MIXED, Batch, Setup, cases
+    out = {}
+    specs = [("c2", lambda d: cases.flat_plate(d, matrix_solver="blusgs", sweeps=4, ratio=1.15,
+                                               dy_max=0.05, name="plate"), 1e-8,
+              args.long_iters_c2,
+              "laminar flat plate, two 128x64x2 blocks, first cell 1e-5, growth 1.15 capped "
+              "at 0.05 L, Mach 0.3, Re_L 1e5, block LU-SGS 4 sweeps, CFL 100"),
+             ("c3", lambda d: cases.sst_plate(d, cfl=10.0, cfl_start=1.0, cfl_step=0.009),
+              1e-12, args.long_iters_c3,
+              "SST-2003 flat plate 256x192x4, Re 5e6, Mach 0.2, y+ 1, WENO, AUSM, block "
+              "LU-SGS, CFL 1 ramped by 0.009 per iteration to 10")]
+    for key, gen, drop, iters, desc in specs:
+        if iters <= 0:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            inp, _ = gen(tmp)
+            setup = Setup(inp)
+        _, _, ncells = setup.counts()
+        res = {"workload": desc, "cells": ncells, "drop": drop, "max_iterations": iters}
+        states = {}
+        for name, prec in (("fp64", PREC_FP64), ("mixed", PREC_MIXED)):
+            b = Batch(ctx, setup, prec)
+            b.autotune(2)
+            _barrier(world)
+            info = b.converge(iters, drop, check_every=100)
+            st = b.stats()
+            states[name] = [b.field(k, "STATE") for k in range(b.nblocks)]
+            b.close()
+            x = info[0]
+            res[name] = {"iterations": int(x.iterations), "drop_reached": x.drop,
+                         "status": {1: "converged", 0: "iteration_cap", -1: "nonphysical"}.get(
+                             int(x.converged), int(x.converged)),
+                         "device_s": _max_over_ranks(st.device_ms * 1e-3, world),
+                         "ms_per_iteration": st.device_ms / max(int(x.iterations), 1)}
+        if all(np.isfinite(a).all() for a in states["fp64"] + states["mixed"]):
+            res["mixed_vs_fp64_state_max_rel_err"] = max(
+                float(np.abs(a - b).max() / np.abs(b).max())
+                for a, b in zip(states["mixed"], states["fp64"]))
+        out[key] = res
     return out
 
 
@@ -706,6 +760,10 @@ def main():
     ap.add_argument("--sst-nj", type=int, default=192)
     ap.add_argument("--sst-nk", type=int, default=4)
     ap.add_argument("--served-max-iters", type=int, default=6000)
+    ap.add_argument("--long-iters-c2", type=int, default=0,
+                    help="c2 to a 1e-8 drop with this iteration cap (0: skip)")
+    ap.add_argument("--long-iters-c3", type=int, default=0,
+                    help="c3 with a CFL ramp for this many iterations (0: skip)")
     ap.add_argument("--mg-iters", type=int, default=3000,
                     help="iteration cap of the multigrid section (0: skip it)")
     ap.add_argument("--mg-ni", type=int, default=256)
@@ -837,6 +895,8 @@ def main():
         line["vortex"] = res["vortex"]
     if "multigrid" in res:
         line["multigrid"] = res["multigrid"]
+    if "long" in res:
+        line["long"] = res["long"]
     if "fp64_exact" in res:
         line["fp64_exact"] = res["fp64_exact"]
     if "plate" in res:

@@ -302,10 +302,14 @@ const char *ath_last_error(void);
  * and square roots, and run the faces, the cell kernel, the scalar LU-SGS
  * hyperplane sweeps and the update with contracted multiply-adds (FP64
  * throughout; equal to the reference to roundoff, about 1e-15 per face,
- * instead of bit for bit). */
-enum { ATH_BATCH_MATRIX_RESID = 1, ATH_BATCH_FAST_FACES = 2 };
+ * instead of bit for bit); bit 2 (ATH_BATCH_OUTPUT_GRADS) = every residual
+ * also keeps the cells' velocity, temperature, density, pressure, k and
+ * omega gradients for output (ATH_FIELD_GRADS). */
+enum { ATH_BATCH_MATRIX_RESID = 1, ATH_BATCH_FAST_FACES = 2, ATH_BATCH_OUTPUT_GRADS = 4 };
 int ath_batch_create(ath_ctx *ctx, const ath_setup *setup, int precision,
                      int flags, ath_batch **out);
+/* The flags a batch was created with. */
+int ath_batch_flags(const ath_batch *batch, int *flags);
 int ath_batch_destroy(ath_batch *batch);
 
 /* Run n nonlinear iterations on every solve of the batch.  norms_h receives
@@ -458,7 +462,14 @@ enum {
    * consVarsNm1_), nv per cell (rho, rho u, rho v, rho w, rho E [, rho k,
    * rho omega]); time-accurate solves only (time n-1: bdf2 solves) */
   ATH_FIELD_CONS_N = 10,
-  ATH_FIELD_CONS_NM1 = 11
+  ATH_FIELD_CONS_NM1 = 11,
+  /* cell-averaged gradients of the last residual (batches created with
+   * ATH_BATCH_OUTPUT_GRADS; procBlock velocityGrad_, temperatureGrad_,
+   * densityGrad_, pressureGrad_, tkeGrad_, omegaGrad_, written by
+   * WriteFunFile src/output.cpp:309-395), 24 per cell: velocity gradient (9,
+   * as ATH_FIELD_VELGRAD), then the temperature, density, pressure, k and
+   * omega gradients (x, y, z each; k and omega zero without RANS) */
+  ATH_FIELD_GRADS = 12
 };
 int ath_batch_get_field(ath_batch *batch, int block, int field, double *out_h);
 int ath_batch_set_state(ath_batch *batch, int block, const double *prim_h);
@@ -495,6 +506,9 @@ typedef struct {
   const double *wall_dist; /* 1 per cell */
   const double *cons_nm1;  /* nv per cell: conserved state of time n-1 (bdf2
                               solves: the restart file's second level) */
+  const double *grads;     /* 24 per cell: as ATH_FIELD_GRADS (the gradient
+                              output variables; velGrad_* from here when
+                              given, else from velgrad) */
 } ath_block_fields;
 
 /* Plot3D cell-centre function file (WriteFunFile, src/output.cpp:209) of

@@ -61,6 +61,8 @@ typedef struct {
    * the transfer to the next coarser level (its block, and per physical
    * cell the coarse cell, restriction weight, 7 prolongation coefficients) */
   double *F, *mr;      /* [nc][5], NULL without multigrid */
+  double *og;          /* [nc][24] output gradients of the last residual
+                          (orc_set_output_grads; NULL otherwise) */
   int mg_coarse;
   int32_t *mg_cell;
   double *mg_volfac, *mg_coef;
@@ -1082,6 +1084,114 @@ static void nr_grads(const orc_case *c, oblock *b) {
   }
 }
 
+/* Green-Gauss gradients at the face of direction d below cell cu of the
+ * cell scalars u, v, w, T, rho, p and, with RANS, k, omega
+ * (procBlock::CalcGradsI/J/K, src/procBlock.cpp:5173-5790): face_grad_vp's
+ * dual cell with every scalar; temperature p / (rho R) of the state. */
+static double cell_scalar(const oblock *b, const gas_t *g, int64_t x, int k) {
+  const double *w = &b->W[x * NV];
+  switch (k) {
+    case 0: return w[1];
+    case 1: return w[2];
+    case 2: return w[3];
+    case 3: return w[4] / (0.0 + w[0] * g->r);
+    case 4: return w[0];
+    case 5: return w[4];
+    default: return b->Wt[x * 2 + (k - 6)];
+  }
+}
+static void face_grads_all(const oblock *b, const gas_t *g, int d, int64_t cu, int ns,
+                           double grad[8][3]) {
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  const int64_t cl = cu - st[d];
+  double lo[3][8], hi[3][8], alo[3][3], ahi[3][3];
+  const int uI = (int)(cu % b->NI) - b->ng, uJ = (int)((cu / b->NI) % b->NJ) - b->ng,
+            uK = (int)(cu / ((int64_t)b->NI * b->NJ)) - b->ng;
+  const int lI = (int)(cl % b->NI) - b->ng, lJ = (int)((cl / b->NI) % b->NJ) - b->ng,
+            lK = (int)(cl / ((int64_t)b->NI * b->NJ)) - b->ng;
+  for (int e = 0; e < 3; ++e) {
+    if (e == d) {
+      for (int k = 0; k < ns; ++k) {
+        lo[e][k] = cell_scalar(b, g, cl, k);
+        hi[e][k] = cell_scalar(b, g, cu, k);
+      }
+      double A0[3], A1[3], A2[3];
+      area_vec(b, d, face_idx(b, d, uI, uJ, uK), A0);
+      area_vec(b, d, face_idx(b, d, uI + (d == 0), uJ + (d == 1), uK + (d == 2)), A1);
+      area_vec(b, d, face_idx(b, d, uI - (d == 0), uJ - (d == 1), uK - (d == 2)), A2);
+      for (int q = 0; q < 3; ++q) {
+        ahi[e][q] = 0.5 * (A0[q] + A1[q]);
+        alo[e][q] = 0.5 * (A0[q] + A2[q]);
+      }
+    } else {
+      const int64_t cup = cu + st[e], clp = cl + st[e], cum = cu - st[e], clm = cl - st[e];
+      for (int k = 0; k < ns; ++k) {
+        const double sl = cell_scalar(b, g, cl, k), su = cell_scalar(b, g, cu, k);
+        hi[e][k] = 0.25 * (((sl + su) + cell_scalar(b, g, cup, k)) + cell_scalar(b, g, clp, k));
+        lo[e][k] = 0.25 * (((sl + su) + cell_scalar(b, g, cum, k)) + cell_scalar(b, g, clm, k));
+      }
+      double Au[3], Al[3], Aup[3], Alp[3];
+      area_vec(b, e, face_idx(b, e, uI, uJ, uK), Au);
+      area_vec(b, e, face_idx(b, e, lI, lJ, lK), Al);
+      area_vec(b, e, face_idx(b, e, uI + (e == 0), uJ + (e == 1), uK + (e == 2)), Aup);
+      area_vec(b, e, face_idx(b, e, lI + (e == 0), lJ + (e == 1), lK + (e == 2)), Alp);
+      for (int q = 0; q < 3; ++q) {
+        ahi[e][q] = 0.5 * (Aup[q] + Alp[q]);
+        alo[e][q] = 0.5 * (Au[q] + Al[q]);
+      }
+    }
+  }
+  const double vol = 0.5 * (b->vol[cl] + b->vol[cu]);
+  const double invVol = 1.0 / vol;
+  for (int k = 0; k < ns; ++k)
+    for (int r = 0; r < 3; ++r) {
+      const double v = hi[0][k] * ahi[0][r] - lo[0][k] * alo[0][r] + hi[1][k] * ahi[1][r] -
+                       lo[1][k] * alo[1][r] + hi[2][k] * ahi[2][r] - lo[2][k] * alo[2][r];
+      grad[k][r] = v * invVol;
+    }
+}
+
+/* The cell-averaged gradients the reference keeps from every residual
+ * (velocityGrad_ ... omegaGrad_; one sixth of each face's, faces i low,
+ * i high, j low, ...) for its output files: [24] per cell = velocity
+ * gradient (9, row = derivative axis), T, rho, p, k, omega gradients. */
+static void out_grads(const orc_case *c, oblock *b) {
+  const gas_t *g = &c->s[b->solve].gas;
+  const int ns = b->Wt ? 8 : 6;
+  const int64_t st[3] = {1, b->NI, (int64_t)b->NI * b->NJ};
+  const double sixth = 1.0 / 6.0;
+  for (int k = 0; k < b->nk; ++k)
+    for (int j = 0; j < b->nj; ++j)
+      for (int i = 0; i < b->ni; ++i) {
+        const int64_t x = cell_idx(b, i, j, k);
+        double acc[8][3];
+        memset(acc, 0, sizeof(acc));
+        for (int d = 0; d < 3; ++d)
+          for (int side = 0; side < 2; ++side) {
+            double gr[8][3];
+            face_grads_all(b, g, d, side ? x + st[d] : x, ns, gr);
+            for (int q = 0; q < ns; ++q)
+              for (int r = 0; r < 3; ++r) acc[q][r] += sixth * gr[q][r];
+          }
+        double *o = &b->og[x * 24];
+        for (int r = 0; r < 3; ++r)
+          for (int q = 0; q < 3; ++q) o[r * 3 + q] = acc[q][r];
+        for (int q = 3; q < 8; ++q)
+          for (int r = 0; r < 3; ++r) o[9 + (q - 3) * 3 + r] = acc[q][r];
+      }
+}
+
+void orc_set_output_grads(orc_case *c, int on) {
+  for (int bi = 0; bi < c->nb; ++bi) {
+    oblock *b = &c->b[bi];
+    if (on && !b->og) b->og = (double *)calloc((size_t)b->nc * 24, sizeof(double));
+    if (!on) {
+      free(b->og);
+      b->og = NULL;
+    }
+  }
+}
+
 static void viscous_fluxes(orc_case *c, oblock *b) {
   const osolve *sv = &c->s[b->solve];
   const ath_solve_view *v = &sv->v;
@@ -1456,6 +1566,7 @@ void orc_destroy(orc_case *c) {
     free(b->kgc); free(b->wgc); free(b->wd);
     for (int d = 0; d < 3; ++d) free(b->wallf[d]);
     free(b->F); free(b->mr); free(b->mg_cell); free(b->mg_volfac); free(b->mg_coef);
+    free(b->og);
   }
   for (int s = 0; s < c->ns; ++s) free(c->s[s].states);
   free(c->b);
@@ -1982,6 +2093,7 @@ void orc_residual(orc_case *c) {
       viscous_fluxes(c, b);
     }
     if (b->nrg) nr_grads(c, b);
+    if (b->og) out_grads(c, b);
   }
   memset(c->forces, 0, sizeof(double) * 6 * c->ns);
   for (int bi = 0; bi < c->nb; ++bi)
@@ -2822,6 +2934,10 @@ int orc_get_field(orc_case *c, int block, int field, double *out) {
             memcpy(out + 9 * q, &b->vg[x * 9], 8 * 9);
             break;
           case ATH_FIELD_WALLDIST: out[q] = b->wd ? b->wd[x] : 1.0e10; break;
+          case ATH_FIELD_GRADS:
+            if (!b->og) return ATH_ERR_UNSUPPORTED;
+            memcpy(out + 24 * q, &b->og[x * 24], 8 * 24);
+            break;
           case ATH_FIELD_CONS_N:
           case ATH_FIELD_CONS_NM1: {
             const ath_solve_view *v = &c->s[b->solve].v;

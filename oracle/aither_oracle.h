@@ -35,6 +35,9 @@ void orc_set_threads(orc_case *c, int nthreads);
 /* Also compute the logged matrix residual in orc_relax (the reference
  * always does, src/linearSolver.cpp:470); read it with orc_matrix_resid. */
 void orc_set_matrix_resid(orc_case *c, int on);
+/* Keep the cell-averaged gradients of every residual for output
+ * (ATH_FIELD_GRADS of orc_get_field). */
+void orc_set_output_grads(orc_case *c, int on);
 /* Multigrid: link level c to its next coarser level `coarse` (cycle index 1
  * V, 2 W); maps[b] is the transfer of block b of c (ath_setup_mg_map).
  * orc_relax of the finest level then runs the cycle over the linked levels

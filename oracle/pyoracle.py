@@ -13,9 +13,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(_HERE, "liboracle.so")
 FIELD = dict(STATE=0, STATE_GHOSTS=1, RESID=2, DT=3, SPECRAD=4, DU=5, AINV=6, AUX=7, VELGRAD=8,
-             WALLDIST=9, CONS_N=10, CONS_NM1=11)
+             WALLDIST=9, CONS_N=10, CONS_NM1=11, GRADS=12)
 WIDTH = dict(STATE=5, STATE_GHOSTS=5, RESID=5, DT=1, SPECRAD=2, DU=5, AINV=1, AUX=5, VELGRAD=9,
-             WALLDIST=1, CONS_N=5, CONS_NM1=5)
+             WALLDIST=1, CONS_N=5, CONS_NM1=5, GRADS=24)
 
 _lib = None
 
@@ -42,6 +42,7 @@ def lib():
         L.orc_get_field.restype = C.c_int
         L.orc_get_field.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_set_matrix_resid.argtypes = [vp, C.c_int]
+        L.orc_set_output_grads.argtypes = [vp, C.c_int]
         L.orc_matrix_resid.restype = C.c_double
         L.orc_matrix_resid.argtypes = [vp, C.c_int]
         L.orc_forces.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
@@ -67,7 +68,8 @@ def _dp(a):
 class Oracle:
     """CPU oracle instance built from an aither_gb300 Setup."""
 
-    def __init__(self, setup, threads: int = 0, matrix_resid: bool = False):
+    def __init__(self, setup, threads: int = 0, matrix_resid: bool = False,
+                 output_grads: bool = False):
         from aither_gb300._lib import BlockView, SolveView
         self.setup = setup
         self.nsolves, self.nblocks, self.ncells = setup.counts()
@@ -80,6 +82,8 @@ class Oracle:
             lib().orc_set_threads(self.h, threads)
         if matrix_resid:
             lib().orc_set_matrix_resid(self.h, 1)
+        if output_grads:
+            lib().orc_set_output_grads(self.h, 1)
         # coarser multigrid levels, each linked to the next finer one
         self.levels = []
         fine = self.h

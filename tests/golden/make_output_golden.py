@@ -44,18 +44,20 @@ COMMON = ["density", "vel_x", "vel_y", "vel_z", "pressure", "mach", "sos", "dt",
           "resid_mom_x", "resid_mom_y", "resid_mom_z", "resid_energy"]
 VISC = ["temperature", "viscosity", "wallDistance"]
 VELGRAD = ["velGrad_" + a + b for b in "xyz" for a in "uvw"]
+GRADS = [f"{q}Grad_{a}" for q in ("temp", "density", "press") for a in "xyz"]
+TURB_GRADS = [f"{q}Grad_{a}" for q in ("tke", "omega") for a in "xyz"]
 SST = ["tke", "sdr", "f1", "f2", "viscosityRatio", "turbulentViscosity", "resid_tke",
        "resid_sdr"]
 
 # (name, generator, kwargs, iterations, variables)
 CASES = [
     ("plate", "flat_plate", dict(ni=12, nj=8, nk=2, dy0=1e-3, ratio=1.3, name="plate"), 6,
-     COMMON + VISC + VELGRAD),
+     COMMON + VISC + VELGRAD + GRADS),
     ("sst", "flat_plate", dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2,
                                rans=True, nblocks=1, matrix_solver="blusgs", name="sst"), 4,
-     COMMON + VISC + VELGRAD + SST),
+     COMMON + VISC + VELGRAD + SST + GRADS + TURB_GRADS),
     ("bump", "bump_channel", dict(ni=16, nj=8, nk=3, height=0.08, mach=0.6, name="bump"), 5,
-     COMMON + ["wallDistance"]),
+     COMMON + ["wallDistance"] + VELGRAD + GRADS),
 ]
 
 

@@ -47,7 +47,7 @@ def run(request, ctx, tmp_path_factory):
     tmp = tmp_path_factory.mktemp(name)
     inp, meta = output_case(name, tmp)
     s = Setup(inp)
-    b = Batch(ctx, s, 0, flags=1)  # with the logged matrix residual
+    b = Batch(ctx, s, 0, flags=1 | 4)  # the logged matrix residual, the output gradients
     norms = list(b.iterate(meta["iterations"]))
     yield name, meta, s, b, norms, tmp
     b.close()
@@ -58,10 +58,6 @@ def test_function_file_values(run):
     name, meta, s, b, _, tmp = run
     n, sim = meta["iterations"], meta["sim"]
     variables = sorted(meta["variables"])
-    kw = meta["kwargs"]
-    if kw.get("matrix_solver") != "blusgs" and not kw.get("rans"):
-        # scalar LU-SGS laminar solves keep no cell velocity gradients
-        variables = [v for v in variables if not v.startswith("velGrad_")]
     path = str(tmp / "dev.fun")
     b.write_function(0, path, variables)
     got = read_fun(path, variables)

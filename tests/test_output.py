@@ -49,14 +49,13 @@ def ran(request, tmp_path_factory):
     tmp = tmp_path_factory.mktemp(name)
     inp, meta = output_case(name, tmp)
     s = Setup(inp)
-    o = Oracle(s, 1)
+    o = Oracle(s, 1, output_grads=True)
     l2 = o.iterate(meta["iterations"])[:, 0, :]
     fields = []
     for b in s.solve_blocks(0):
         fl = {"prim": o.field(b, "STATE"), "dt": o.field(b, "DT"), "resid": o.field(b, "RESID"),
-              "aux": o.field(b, "AUX"), "wall_dist": o.field(b, "WALLDIST")}
-        if s.solve_view(0).eqn != 0:
-            fl["velgrad"] = o.field(b, "VELGRAD")
+              "aux": o.field(b, "AUX"), "wall_dist": o.field(b, "WALLDIST"),
+              "grads": o.field(b, "GRADS")}
         fields.append(fl)
     yield name, meta, s, l2, fields, tmp
     o.close()
@@ -138,11 +137,17 @@ def test_residual_history_columns(ran):
 
 
 def test_unsupported_variable_is_an_error(ran):
+    """A variable the reference does not write, and a gradient variable
+    without the kept gradients, are errors and write no file."""
     from aither_gb300._lib import AthError
     _, _, s, _, fields, tmp = ran
     with pytest.raises(AthError):
-        s.write_function(0, fields, str(tmp / "x.fun"), variables=["tempGrad_x"])
+        s.write_function(0, fields, str(tmp / "x.fun"), variables=["notAVariable"])
     assert not os.path.exists(tmp / "x.fun")
+    bare = [{k: v for k, v in f.items() if k != "grads"} for f in fields]
+    with pytest.raises(AthError):
+        s.write_function(0, bare, str(tmp / "y.fun"), variables=["tempGrad_x"])
+    assert not os.path.exists(tmp / "y.fun")
 
 
 # ---- bdf2 restart files: two time levels -----------------------------------
