@@ -466,7 +466,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
                lead: float = 0.0, cfl_start: float | None = None, cfl_step: float = 0.0,
                wall_q: float | None = None, time: str = "implicitEuler",
                dt: float | None = None, nl: int = 1, dual_cfl: float | None = None,
-               multigrid: tuple | None = None):
+               multigrid: tuple | None = None, turb_model: str = "sst2003"):
     """Laminar flat plate as two blocks of ni x nj x nk cells joined by an
     interblock connection at x = length/2; viscous wall at y = 0 (adiabatic,
     or isothermal at wall_t), characteristic far field on the other sides of
@@ -510,7 +510,7 @@ def flat_plate(outdir: str, ni: int = 128, nj: int = 64, nk: int = 2, dy0: float
     scheme = {"cfl": cfl, "cflStart": cfl if cfl_start is None else cfl_start,
               "cflStep": cfl_step,
               "limiter": limiter, "equationSet": "rans" if rans else "navierStokes",
-              "turbulenceModel": "sst2003" if rans else "none", "inviscidFlux": flux,
+              "turbulenceModel": turb_model if rans else "none", "inviscidFlux": flux,
               "matrixSolver": matrix_solver, "faceReconstruction": recon, "matrixSweeps": sweeps,
               **time_keys(time, dt, nl, dual_cfl), **multigrid_keys(multigrid)}
     if nblocks == 1:

@@ -1776,6 +1776,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
       throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
     if (rans) c.any_rans = true;
   }
+  for (const auto &sv : st.solves)
+    if (sv.phys.turb == ATH_TURB_KW2006)
+      throw Error(ATH_ERR_UNSUPPORTED, "the Wilcox k-omega 2006 model runs in the oracle only");
   for (const auto &sv : st.solves) {
     const bool blk = IsBlockSolver(sv.phys.solver), jac = IsJacobiSolver(sv.phys.solver);
     c.kinds |= blk ? 2 : 1;

@@ -255,7 +255,7 @@ __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block
 // solves, k_sweepb block solves.
 template <typename T, bool FULL>
 __global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward, int sweep);
-template <typename T, bool FULL>
+template <typename T, bool FULL, int MINB = 1>
 __global__ void k_sweepg(Pools<T> P, const int2 *items, int n, int forward, int sweep);
 template <typename T>
 __global__ void k_sweepb(Pools<T> P, const int2 *items, int n, int forward, int sweep,

@@ -1679,8 +1679,8 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
   ScalarFinish<T, FULL>(P, sv, it.x, forward, both, acc, acct, other, othert);
 }
 
-template <typename T, bool FULL>
-__global__ void __launch_bounds__(256) k_sweepg(Pools<T> P, const int2 *items, int n_items,
+template <typename T, bool FULL, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_sweepg(Pools<T> P, const int2 *items, int n_items,
                                                 int forward, int sweep) {
   constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;

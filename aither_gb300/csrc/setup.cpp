@@ -1577,8 +1577,10 @@ void AppendInput(Setup &st, const std::string &path) {
   if (tm != "none" && ph.eqn != ATH_EQN_RANS) Fail("turbulence model needs equationSet rans");
   ph.turb = ATH_TURB_NONE;
   if (ph.eqn == ATH_EQN_RANS) {
-    if (tm != "sst2003") Fail("only turbulenceModel sst2003 is supported");
-    ph.turb = ATH_TURB_SST2003;
+    // input::AssignTurbulenceModel (src/input.cpp): sst2003, kOmegaWilcox2006
+    if (tm == "sst2003") ph.turb = ATH_TURB_SST2003;
+    else if (tm == "kOmegaWilcox2006") ph.turb = ATH_TURB_KW2006;
+    else Fail("only turbulenceModel sst2003 and kOmegaWilcox2006 are supported");
   }
   ph.nv = ph.eqn == ATH_EQN_RANS ? 7 : 5;
   // input::NumberGhostLayers (src/input.cpp:1127): 1 constant, 2 MUSCL, 3 WENO

@@ -75,7 +75,8 @@ typedef struct {
   double cfl;
   int viscous;
   int block;   /* blusgs: 5x5 Jacobian diagonal and off-diagonals */
-  int rans;    /* SST-2003 turbulence equations */
+  int rans;    /* k-omega turbulence equations (SST-2003 or Wilcox 2006) */
+  int wilcox;  /* Wilcox k-omega 2006 instead of SST-2003 */
   int sweeps;  /* matrixSweeps */
   int jacobi;  /* dplur / bdplur: Jacobi sweeps instead of LU-SGS */
   int nm1_given; /* time n-1 set from a restart: kept at the first step */
@@ -523,8 +524,12 @@ static double visc_max_term(const double *w, const gas_t *g) {
   const double a = 4.0 / (3.0 * w[0]), b = gamma_of(g) / w[0];
   return (a < b) ? b : a;
 }
+/* turbModel::TurbPrandtlNumber: 0.9, Wilcox 2006 8/9 (include/turbulence.hpp:70,462) */
+static double prt_of(const ath_solve_view *v) {
+  return v->turb == ATH_TURB_KW2006 ? 8.0 / 9.0 : 0.9;
+}
 static double visc_term(double mu, double mut, const ath_solve_view *v, const gas_t *g) {
-  return v->visc_scale * (mu / prandtl_of(g) + mut / 0.9);
+  return v->visc_scale * (mu / prandtl_of(g) + mut / prt_of(v));
 }
 /* FaceReconCentral (include/reconstruction.hpp:315): coefficients of the
  * lower (upwind) and upper (downwind) cell */
@@ -684,7 +689,7 @@ static void tsl_jac(const double *w, double mu_lam, double mut_lam, const gas_t 
   const double velNorm = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
   const double rho = w[0];
   const double k = cond_eff(t, v);
-  const double kt = mut * cp_of(g) / 0.9;  /* turbulent Prandtl number 0.9 */
+  const double kt = mut * cp_of(g) / prt_of(v);  /* turbulent Prandtl number */
   /* TauNormal (src/utility.cpp:426) */
   const double lambda = 0.0 - (2.0 / 3.0) * (mu + mut);
   const double trace = vg[0] + vg[4] + vg[8];
@@ -904,6 +909,78 @@ static double sst_source(const double *w, const double *kw, const double *vg,
   return beta;
 }
 
+/* ---------------------------------------------- Wilcox k-omega 2006 */
+/* turbKWWilcox (include/turbulence.hpp:390-398) */
+#define WK_GAMMA 0.52
+#define WK_BETASTAR 0.09
+#define WK_SIGMA 0.5
+#define WK_SIGMASTAR 0.6
+#define WK_SIGMAD0 0.125
+#define WK_BETA0 0.0708
+#define WK_CLIM 0.875
+
+/* turbKWWilcox::EddyVisc / OmegaTilda (src/turbulence.cpp:270,339): rho k
+ * over omega limited below by clim sqrt(2 S^:S^ / beta*), S^ the traceless
+ * strain rate */
+static double wk_eddy_visc(const double *w, const double *kw, const double *vg, double scale) {
+  const double tr = (vg[0] + vg[4]) + vg[8];
+  const double c = 1.0 / 3.0 * tr;
+  double sh[9];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q)
+      sh[r * 3 + q] = 0.5 * (vg[r * 3 + q] + vg[q * 3 + r]) - c * (r == q ? 1.0 : 0.0);
+  const double omt = cmax(kw[1], scale * WK_CLIM * sqrt(2.0 * ddot(sh, sh) / WK_BETASTAR));
+  return w[0] * kw[0] / omt;
+}
+
+/* turbModel::EddyViscosityNoLim (src/turbulence.cpp:38): rho k / omega */
+static double eddy_visc_nolim(const double *w, const double *kw) { return w[0] * kw[0] / kw[1]; }
+
+/* turbKWWilcox::CalcTurbSrc (src/turbulence.cpp:359) with Beta / FBeta /
+ * Xw / StrainKI / SigmaD (:283-337); returns beta for the source Jacobian */
+static double wk_source(const double *w, const double *kw, const double *vg, const double *kg,
+                        const double *wg, double mut, double scale, double *src) {
+  const double k = kw[0], om = kw[1], rho = w[0];
+  const double inv = 1.0 / scale;
+  const double tkeDest = inv * WK_BETASTAR * (rho * k * om * 1.0);
+  /* vortex stretching: vorticity squared double-dotted with the strain */
+  double vo[9], skI[9], vv[9];
+  const double tr = (vg[0] + vg[4]) + vg[8];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      vo[r * 3 + q] = 0.5 * (vg[r * 3 + q] - vg[q * 3 + r]);
+      skI[r * 3 + q] = 0.5 * ((vg[r * 3 + q] + vg[q * 3 + r]) - tr * (r == q ? 1.0 : 0.0));
+    }
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      double t = 0.0;
+      for (int m = 0; m < 3; ++m) t += vo[r * 3 + m] * vo[m * 3 + q];
+      vv[r * 3 + q] = t;
+    }
+  const double xw = fabs(ddot(vv, skI) / pow(WK_BETASTAR * om, 3.0)) * pow(scale, 3.0);
+  const double fbeta = (1.0 + 85.0 * xw) / (1.0 + 100.0 * xw);
+  const double beta = WK_BETA0 * fbeta;
+  const double omgDest = inv * beta * (rho * om * om);
+  const double lambda = 0.0 - (2.0 / 3.0) * mut;
+  const double c23 = 2.0 / 3.0 * rho * k;
+  double tau[9];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) {
+      const double I = (r == q) ? 1.0 : 0.0;
+      tau[r * 3 + q] = (I * (lambda * tr) + (vg[r * 3 + q] + vg[q * 3 + r]) * mut) - I * c23;
+    }
+  double tkeProd = scale * ddot(tau, vg);
+  tkeProd = cmax(tkeProd, 0.0);
+  double omgProd = WK_GAMMA * om / k * tkeProd;
+  omgProd = cmax(omgProd, 0.0);
+  const double kdw = ((0.0 + kg[0] * wg[0]) + kg[1] * wg[1]) + kg[2] * wg[2];
+  const double sigd = kdw <= 0.0 ? 0.0 : WK_SIGMAD0;
+  const double omgCd = scale * sigd * (rho / om * kdw);
+  src[0] = tkeProd - tkeDest;
+  src[1] = omgProd - omgDest + omgCd;
+  return beta;
+}
+
 /* turbulence spectral radii and Jacobians (src/turbulence.cpp:105-160,
  * 749-797): inviscid cell radius |v.n_avg| |A|; viscous cell radius
  * scale |A|^2/(V rho) (mu + sigma_k mut); face radii; viscous Jacobian */
@@ -916,20 +993,29 @@ static double turb_inv_cell_sr(const double *w, const double *lo, double lom,
   const double fMag = 0.5 * (lom + him);
   return fabs(w[1] * a[0] + w[2] * a[1] + w[3] * a[2]) * fMag;
 }
-static double turb_visc_cell_sr(const double *w, double lom, double him, double vol,
-                                double mu, double mut, double f1, double scale) {
+/* the k equation's diffusivity mu + sigma_k mu_t of the radii and
+ * Jacobians: SST blends sigma_k with F1 and takes the limited mu_t, Wilcox
+ * 2006 takes sigma* and the unlimited rho k / omega of the state (kw) */
+static double turb_diff_k(int wilcox, const double *w, const double *kw, double mu, double mut,
+                          double f1) {
+  return wilcox ? mu + WK_SIGMASTAR * eddy_visc_nolim(w, kw)
+                : mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut;
+}
+static double turb_visc_cell_sr(int wilcox, const double *w, const double *kw, double lom,
+                                double him, double vol, double mu, double mut, double f1,
+                                double scale) {
   const double fMag = 0.5 * (lom + him);
   const double length = fMag * fMag / vol;
-  return scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
+  return scale * length / w[0] * turb_diff_k(wilcox, w, kw, mu, mut, f1);
 }
-static double turb_face_sr(const double *w, const double *n, double mag, double mu,
-                           double mut, double f1, double dist, double scale, int positive,
-                           int viscous) {
+static double turb_face_sr(int wilcox, const double *w, const double *kw, const double *n,
+                           double mag, double mu, double mut, double f1, double dist,
+                           double scale, int positive, int viscous) {
   const double vn = w[1] * n[0] + w[2] * n[1] + w[3] * n[2];
   double sr = positive ? 0.5 * mag * fabs(vn + fabs(vn)) : 0.5 * mag * fabs(vn - fabs(vn));
   if (viscous) {
     const double length = mag / dist;
-    sr += scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
+    sr += scale * length / w[0] * turb_diff_k(wilcox, w, kw, mu, mut, f1);
   }
   return sr;
 }
@@ -942,12 +1028,16 @@ static void turb_rusanov_jac(const double *w, const double *n, double mag, int p
   const double dj[4] = {0.5 * diss, 0.5 * 0.0, 0.5 * 0.0, 0.5 * diss};
   for (int e = 0; e < 4; ++e) J[e] = positive ? cj[e] + dj[e] : cj[e] - dj[e];
 }
-/* turbKWSst::ViscJac (src/turbulence.cpp:764) times the sign factor */
-static void turb_visc_jac(const double *w, double mag, double mu, double mut, double f1,
-                          double dist, double scale, double fac, double *J) {
+/* turbKWSst::ViscJac (src/turbulence.cpp:764), turbKWWilcox::ViscJac
+ * (:485) times the sign factor */
+static void turb_visc_jac(int wilcox, const double *w, const double *kw, double mag, double mu,
+                          double mut, double f1, double dist, double scale, double fac,
+                          double *J) {
   const double length = mag / dist;
-  const double j00 = scale * length / w[0] * (mu + blended(SST_SIGMAK1, SST_SIGMAK2, f1) * mut);
-  const double j11 = scale * length / w[0] * (mu + blended(SST_SIGMAW1, SST_SIGMAW2, f1) * mut);
+  const double j00 = scale * length / w[0] * turb_diff_k(wilcox, w, kw, mu, mut, f1);
+  const double j11 = scale * length / w[0] *
+                     (wilcox ? mu + WK_SIGMA * eddy_visc_nolim(w, kw)
+                             : mu + blended(SST_SIGMAW1, SST_SIGMAW2, f1) * mut);
   J[0] = fac * j00;
   J[1] = fac * 0.0;
   J[2] = fac * 0.0;
@@ -1311,15 +1401,28 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
               fst[q] = cmax(cd * Tt[cu * 2 + q] + cuw * Tt[cl * 2 + q], TURB_MIN);
             double wdf = cd * b->wd[cu] + cuw * b->wd[cl];
             if (wdf < 0.0 && wdf > -1.0e-10) wdf = 0.0;
-            sst_eddy_visc(fs, fst, &grad[0][0], kg, wg, muf, wdf, v->visc_scale, &mutf, &f1f,
-                          &f2f);
+            if (sv->wilcox) {
+              /* turbKWWilcox::EddyViscAndBlending (src/turbulence.cpp:412) */
+              f1f = 1.0;
+              f2f = 0.0;
+              mutf = wk_eddy_visc(fs, fst, &grad[0][0], v->visc_scale);
+            } else {
+              sst_eddy_visc(fs, fst, &grad[0][0], kg, wg, muf, wdf, v->visc_scale, &mutf, &f1f,
+                            &f2f);
+            }
           }
           /* viscous flux */
           double n[3], mag;
           face_normal(b, d, face_idx(b, d, i, j, k), n, &mag);
           const double mus = v->visc_scale * muf, muts = v->visc_scale * mutf;
           double Ft[2] = {0, 0};
-          if (rans) {
+          if (rans && sv->wilcox) {
+            /* the unlimited eddy viscosity in the turbulence diffusion
+             * (viscousFlux::CalcFlux src/viscousFlux.cpp:126) */
+            const double mutt = v->visc_scale * eddy_visc_nolim(fs, fst);
+            Ft[0] = (mus + WK_SIGMASTAR * mutt) * (kg[0] * n[0] + kg[1] * n[1] + kg[2] * n[2]);
+            Ft[1] = (mus + WK_SIGMA * mutt) * (wg[0] * n[0] + wg[1] * n[1] + wg[2] * n[2]);
+          } else if (rans) {
             Ft[0] = (mus + blended(SST_SIGMAK1, SST_SIGMAK2, f1f) * muts) *
                     (kg[0] * n[0] + kg[1] * n[1] + kg[2] * n[2]);
             Ft[1] = (mus + blended(SST_SIGMAW1, SST_SIGMAW2, f1f) * muts) *
@@ -1335,7 +1438,7 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
           }
           const double tf = temp_of(fs, g);
           const double kk_ = cond_eff(tf, v);
-          const double kt = muts * cp_of(g) / 0.9;
+          const double kt = muts * cp_of(g) / prt_of(v);
           double F[NV];
           F[0] = 0.0;
           F[1] = tau[0];
@@ -1377,7 +1480,8 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
               tsl_jac(fs, muf, mutf, g, v, n, mag, c2c, 1, &grad[0][0], Jt);
               for (int e = 0; e < NJAC; ++e) b->Ab[cl * NJAC + e] -= Jt[e];
               if (rans) {
-                turb_visc_jac(fs, mag, muf, mutf, f1f, c2c, v->visc_scale, -1.0, Jtt);
+                turb_visc_jac(sv->wilcox, fs, fst, mag, muf, mutf, f1f, c2c, v->visc_scale, -1.0,
+                              Jtt);
                 for (int e = 0; e < 4; ++e) b->Abt[cl * 4 + e] -= Jtt[e];
               }
             }
@@ -1402,15 +1506,17 @@ static void viscous_fluxes(orc_case *c, oblock *b) {
             const double lv = visc_max_term(Wc, g) * visc_term(b->mu[cu], mutf, v, g) * fMag *
                               fMag / b->vol[cu];
             b->lam[cu] += lv * coeff;
-            const double lvt = rans ? turb_visc_cell_sr(Wc, ml, mh, b->vol[cu], b->mu[cu], mutf,
-                                                        f1f, v->visc_scale)
+            const double lvt = rans ? turb_visc_cell_sr(sv->wilcox, Wc, &Tt[cu * 2], ml, mh,
+                                                        b->vol[cu], b->mu[cu], mutf, f1f,
+                                                        v->visc_scale)
                                     : 0.0;
             if (rans) b->lamt[cu] += lvt * coeff;
             if (sv->block) {
               tsl_jac(fs, muf, mutf, g, v, n, mag, c2c, 0, &grad[0][0], Jt);
               for (int e = 0; e < NJAC; ++e) b->Ab[cu * NJAC + e] += Jt[e];
               if (rans) {
-                turb_visc_jac(fs, mag, muf, mutf, f1f, c2c, v->visc_scale, 1.0, Jtt);
+                turb_visc_jac(sv->wilcox, fs, fst, mag, muf, mutf, f1f, c2c, v->visc_scale, 1.0,
+                              Jtt);
                 for (int e = 0; e < 4; ++e) b->Abt[cu * 4 + e] += Jtt[e];
               }
             } else {
@@ -1443,6 +1549,7 @@ orc_case *orc_create(int nblocks, const ath_block_view *bv, int nsolves,
     c->s[s].block = sv[s].solver == ATH_SOLVER_BLUSGS || sv[s].solver == ATH_SOLVER_BDPLUR;
     c->s[s].jacobi = sv[s].solver == ATH_SOLVER_DPLUR || sv[s].solver == ATH_SOLVER_BDPLUR;
     c->s[s].rans = sv[s].eqn == ATH_EQN_RANS;
+    c->s[s].wilcox = sv[s].turb == ATH_TURB_KW2006;
     c->s[s].sweeps = sv[s].sweeps > 0 ? sv[s].sweeps : 1;
   }
   for (int bi = 0; bi < nblocks; ++bi) {
@@ -2076,7 +2183,9 @@ void orc_residual(orc_case *c) {
           const int64_t a = op->src2;
           const double nuW = b->mu[a] / b->W[a * NV];
           const double s_ = sv->v.visc_scale;
-          const double wWall = s_ * s_ * 60.0 * nuW / (b->wd[a] * b->wd[a] * SST_BETA1);
+          /* turbModel::WallBeta: SST beta1, Wilcox 2006 beta0 */
+          const double wallBeta = c->s[b->solve].wilcox ? WK_BETA0 : SST_BETA1;
+          const double wWall = s_ * s_ * 60.0 * nuW / (b->wd[a] * b->wd[a] * wallBeta);
           double *gt = &b->Wt[op->dst * 2];
           gt[0] = -1.0 * it[0];
           gt[1] = 2.0 * wWall - it[1];
@@ -2137,8 +2246,12 @@ void orc_residual(orc_case *c) {
           const int64_t x = cell_idx(b, i, j, k);
           const double *w = &b->W[x * NV], *kw = &b->Wt[x * 2];
           double src[2];
-          const double beta = sst_source(w, kw, &b->vg[x * 9], &b->kgc[x * 3], &b->wgc[x * 3],
-                                         b->mutc[x], b->f1c[x], scale, src);
+          const double beta =
+              c->s[b->solve].wilcox
+                  ? wk_source(w, kw, &b->vg[x * 9], &b->kgc[x * 3], &b->wgc[x * 3], b->mutc[x],
+                              scale, src)
+                  : sst_source(w, kw, &b->vg[x * 9], &b->kgc[x * 3], &b->wgc[x * 3], b->mutc[x],
+                               b->f1c[x], scale, src);
           const double vol = b->vol[x];
           const double srcSR = -2.0 * SST_BETASTAR * kw[1] * vol * inv;
           b->lamt[x] -= srcSR;
@@ -2282,14 +2395,15 @@ static void offdiag_sum(const orc_case *c, const oblock *b, int64_t x, int lower
         turb_rusanov_jac(wn, n, mag, lower, Jt);
         if (sv->viscous) {
           double Tv[4];
-          turb_visc_jac(wn, mag, b->mu[nb], b->mutc[nb], b->f1c[nb], dist, scale,
-                        lower ? -1.0 : 1.0, Tv);
+          turb_visc_jac(sv->wilcox, wn, &b->Wt[nb * 2], mag, b->mu[nb], b->mutc[nb], b->f1c[nb],
+                        dist, scale, lower ? -1.0 : 1.0, Tv);
           for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
         }
         mat_vec2(Jt, dut, ot);
       } else {
-        const double srt = turb_face_sr(wn, n, mag, b->mu[nb], b->mutc[nb], b->f1c[nb], dist,
-                                        scale, lower, sv->viscous);
+        const double srt = turb_face_sr(sv->wilcox, wn, &b->Wt[nb * 2], n, mag, b->mu[nb],
+                                        b->mutc[nb], b->f1c[nb], dist, scale, lower,
+                                        sv->viscous);
         for (int q = 0; q < 2; ++q) ot[q] = lower ? 0.0 + dut[q] * srt : 0.0 - dut[q] * srt;
       }
       for (int q = 0; q < 2; ++q) acc[NV + q] += ot[q];

@@ -53,7 +53,8 @@ def golden_case(name, outdir):
     gen = (cases.vortex_box if base.startswith("vortex")
            else cases.block_pair if base.startswith("pair_")
            else cases.wall_channel if base.startswith(("sst_chan", "chan_"))
-           else cases.flat_plate if base.startswith(("plate", "sst")) else cases.bump_channel)
+           else cases.flat_plate if base.startswith(("plate", "sst", "wk_"))
+           else cases.bump_channel)
     inp, st = gen(outdir, name=base, **kw)
     return inp, st, g
 

@@ -60,6 +60,14 @@ CASES = [
     ("plate_mg_bdplur", cases.flat_plate,
      dict(ni=14, nj=8, nk=2, dy0=1e-3, ratio=1.3, cfl=20.0, matrix_solver="bdplur", sweeps=4,
           multigrid=(3, "V")), [1, 15], True),
+    # Wilcox k-omega 2006: scalar LU-SGS on one block, block LU-SGS with 2
+    # sweeps on two blocks
+    ("wk_plate", cases.flat_plate,
+     dict(ni=12, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          nblocks=1, turb_model="kOmegaWilcox2006"), [1, 15], True),
+    ("wk_plate2_blusgs", cases.flat_plate,
+     dict(ni=10, nj=10, nk=2, dy0=1e-4, ratio=1.3, reynolds=5e6, mach=0.2, rans=True,
+          matrix_solver="blusgs", sweeps=2, turb_model="kOmegaWilcox2006"), [1, 15], True),
     ("vortex16", cases.vortex_box, dict(ni=16, nj=8, nk=4), [1, 20], True),
     ("bump24", cases.bump_channel, dict(ni=24, nj=12, nk=4, height=0.08, mach=0.7), [1, 30], True),
     ("bump_sup", cases.bump_channel, dict(ni=20, nj=10, nk=3, height=0.10, mach=0.85), [1, 40], True),
@@ -184,6 +192,7 @@ REFCASES = [
     ("rae2822", [1, 20], (1, 8)),
     ("shockTube", [1, 4], None),
     ("transonicBump", [1, 20], None),
+    ("turbFlatPlate", [1, 20], None),
 ]
 
 

@@ -21,7 +21,7 @@ from conftest import GOLDEN, REFCASES, load_golden, rel_err
 FIXTURES = [("uniformFlow", (1, 20)), ("subsonicCylinder", (1, 20)),
             ("multiblockCylinder", (1, 20)), ("couette", (1, 20)),
             ("viscousFlatPlate", (1, 20)), ("rae2822", (1, 20)), ("shockTube", (1, 4)),
-            ("transonicBump", (1, 20))]
+            ("transonicBump", (1, 20)), ("turbFlatPlate", (1, 20))]
 
 # testCases/regressionTests.py: normalised L2 of the last residual-file row
 # after `iterations` (single-process values), 1 % tolerance; columns in
@@ -37,6 +37,9 @@ TRUTH = {
     "rae2822": (20, [5.5618e-01, 6.6813e-01, 5.3620e-01, 1.0000e+00, 4.9726e-01, 2.5769e-09,
                      3.4032e-10], {3}),
     "couette": (100, [1.1816e-01, 5.0725e-01, 6.9807e-02, 5.5916e-01, 2.3024e-01], {3}),
+    # Wilcox k-omega 2006, 137x97 NASA TMR grid (single-process values)
+    "turbFlatPlate": (20, [2.2309e-01, 2.9862e-01, 1.0000e+00, 3.2376e-01, 2.1910e-01,
+                           2.5208e-07, 3.3009e-06], {2}),
     # three multigrid levels, W cycle, DP-LUR (single-process values)
     "transonicBump": (100, [2.6152e-02, 1.5984e-02, 9.6803e-03, 1.0000e+00, 1.9215e-02], {3}),
 }

@@ -34,7 +34,8 @@ FULL = ["vortex16_it1", "vortex16_it20", "bump24_it1", "bump24_it30",
         "bump_nr_both_bdf2_it1", "bump_nr_both_bdf2_it8", "chan_nr_out_visc_it1",
         "chan_nr_out_visc_it10", "bump_mg_v_it1", "bump_mg_v_it15", "bump_mg_w3_it1",
         "bump_mg_w3_it15", "bump_mg_dplur_it1", "bump_mg_dplur_it15", "plate_mg_blusgs_it1",
-        "plate_mg_blusgs_it15", "plate_mg_bdplur_it1", "plate_mg_bdplur_it15"]
+        "plate_mg_blusgs_it15", "plate_mg_bdplur_it1", "plate_mg_bdplur_it15",
+        "wk_plate_it1", "wk_plate_it15", "wk_plate2_blusgs_it1", "wk_plate2_blusgs_it15"]
 
 
 def _oracle(inp, st):
