@@ -581,7 +581,7 @@ class Runner : public RunnerBase {
     for (int d = 0; d < 3; ++d) {
       P_.fluxt[d] = zero(m.Alloc<double>(2 * n), 2 * n);
       P_.vfluxt[d] = zero(m.Alloc<T>(2 * n), 2 * n);
-      P_.rst[d] = zero(m.Alloc<T>(18 * n), 18 * n);
+      P_.rst[d] = zero(m.Alloc<T>(19 * n), 19 * n);
     }
     const int64_t aw = (c_.kinds & 2) ? 4 : 1;
     P_.Rtq = zero(m.Alloc<T>(2 * nq), 2 * nq);
@@ -593,6 +593,9 @@ class Runner : public RunnerBase {
     P_.Atq = zero(m.Alloc<T>(aw * nq), aw * nq);
     P_.mutq = zero(m.Alloc<T>(nq), nq);
     P_.f1q = zero(m.Alloc<T>(nq), nq);
+    bool wilcox = false;
+    for (const auto &sv : c_.setup->solves) wilcox = wilcox || sv.phys.turb == ATH_TURB_KW2006;
+    if (wilcox) P_.nutq = zero(m.Alloc<T>(nq), nq);
     P_.f2q = zero(m.Alloc<T>(nq), nq);
   }
 
@@ -1776,9 +1779,6 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
       throw Error(ATH_ERR_UNSUPPORTED, "block layout not supported by this build");
     if (rans) c.any_rans = true;
   }
-  for (const auto &sv : st.solves)
-    if (sv.phys.turb == ATH_TURB_KW2006)
-      throw Error(ATH_ERR_UNSUPPORTED, "the Wilcox k-omega 2006 model runs in the oracle only");
   for (const auto &sv : st.solves) {
     const bool blk = IsBlockSolver(sv.phys.solver), jac = IsJacobiSolver(sv.phys.solver);
     c.kinds |= blk ? 2 : 1;
@@ -1852,6 +1852,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.store_n = (x.unsteady || nonreflecting) ? 1 : 0;
     if (x.store_n) c.any_unsteady = true;
     x.rans = p.eqn == ATH_EQN_RANS;
+    x.wilcox = x.rans && p.turb == ATH_TURB_KW2006;
     x.sweeps = p.sweeps;
     x.active = 1;
     x.padded_values = 0.0;

@@ -94,6 +94,7 @@ __device__ __forceinline__ void TauNormal(const T vg[9], T nx, T ny, T nz, T mu,
 template <typename T>
 struct TslCoeffs {
   T scale, t_ref, k_c1, k_s, k_ref;
+  T prt;  // turbulent Prandtl number of the solve's model
 };
 
 // J <- J - T(W) (subtract) or J + T(W) with T the approximate thin-shear-
@@ -112,7 +113,7 @@ __device__ __forceinline__ void TslJacAccum(const Prim<T> &s, T mu_lam, T mut_la
   const T velNorm = Dot(s.u, s.v, s.w, nx, ny, nz);
   const T rho = s.rho;
   const T k = SutherlandRatio(t, k_.t_ref, k_.k_c1, k_.k_s, k_.k_ref) * k_.scale;
-  const T kt = mut * g.Cp() / T(0.9);
+  const T kt = mut * g.Cp() / k_.prt;
   T tau[3];
   TauNormal(vg, nx, ny, nz, mu, mut, tau);
   const T fac = left ? T(-1) : T(1);
@@ -192,14 +193,29 @@ __device__ __forceinline__ void TurbRusanovJac(const Prim<T> &s, T nx, T ny, T n
 #pragma unroll
   for (int e = 0; e < 4; ++e) J[e] = positive ? cj[e] + dj[e] : cj[e] - dj[e];
 }
+// The k and omega equations' diffusivities mu + sigma mu_t of the
+// turbulence radii and Jacobians: SST-2003 blends sigma with F1 and takes
+// the limited eddy viscosity mut, Wilcox k-omega 2006 takes sigma* = 0.6,
+// sigma = 0.5 and the unlimited rho k / omega (nut) of the state
+// (turbKWSst / turbKWWilcox ::ViscJac, ViscousCell/FaceSpectralRadius,
+// src/turbulence.cpp:485-547,764-797)
 template <typename T>
-__device__ __forceinline__ void TurbViscJac(T rho, T mag, T mu, T mut, T f1, T dist, T scale,
-                                            T fac, T J[4]) {
-  const T length = mag / dist;
+struct TurbDiff {
+  T k, w;
+};
+template <typename T>
+__device__ __forceinline__ TurbDiff<T> TurbDiffOf(bool wilcox, T mu, T mut, T f1, T nut) {
+  if (wilcox) return TurbDiff<T>{mu + T(0.6) * nut, mu + T(0.5) * nut};
   const T sk = f1 * T(0.85) + (T(1) - f1) * T(1.0);
   const T sw = f1 * T(0.5) + (T(1) - f1) * T(0.856);
-  const T j00 = scale * length / rho * (mu + sk * mut);
-  const T j11 = scale * length / rho * (mu + sw * mut);
+  return TurbDiff<T>{mu + sk * mut, mu + sw * mut};
+}
+template <typename T>
+__device__ __forceinline__ void TurbViscJac(T rho, T mag, const TurbDiff<T> &df, T dist,
+                                            T scale, T fac, T J[4]) {
+  const T length = mag / dist;
+  const T j00 = scale * length / rho * df.k;
+  const T j11 = scale * length / rho * df.w;
   J[0] = fac * j00;
   J[1] = fac * T(0);
   J[2] = fac * T(0);

@@ -35,7 +35,8 @@ struct SolveDev {
   double cells;          // physical cells of the solve
   // laminar transport (Sutherland), nondimensional
   double visc_scale, mu_c1, mu_s, mu_ref, t_ref, k_c1, k_s, k_ref, visc_coeff;
-  int32_t viscous, pad3;
+  int32_t viscous;
+  int32_t wilcox;  // RANS with the Wilcox k-omega 2006 model instead of SST-2003
   int32_t limiter, nstates, state0, recon;
   int32_t flux;
   int32_t block;   // blusgs: 5x5 Jacobian diagonal and off-diagonals
@@ -191,6 +192,10 @@ struct Pools {
   // after each update, src/mgSolution.cpp:225-228)
   T *Fq, *MRq;
   int mg_accum;
+  // [nq] unlimited eddy viscosity rho k / omega of the cells of Wilcox
+  // k-omega 2006 solves (their turbulence radii and Jacobians; null without
+  // such solves)
+  T *nutq;
   // [24][ncell] cell-averaged gradients of the last residual kept for
   // output (batch flag ATH_BATCH_OUTPUT_GRADS; null otherwise)
   double *ogr;

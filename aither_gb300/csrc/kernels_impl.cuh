@@ -119,6 +119,83 @@ __device__ __forceinline__ double SstSource(const Prim<double> &w, const double 
   return beta;
 }
 
+// Wilcox k-omega 2006 constants (turbKWWilcox, include/turbulence.hpp:391-398)
+constexpr double kWkGamma = 0.52, kWkBetaStar = 0.09, kWkSigma = 0.5, kWkSigmaStar = 0.6;
+constexpr double kWkSigmaD0 = 0.125, kWkBeta0 = 0.0708, kWkClim = 0.875;
+// turbModel::TurbPrandtlNumber of the solve's model
+__device__ __forceinline__ double PrtOf(const SolveDev &sv) { return sv.wilcox ? 8.0 / 9.0 : 0.9; }
+
+// turbKWWilcox::EddyVisc with OmegaTilda (src/turbulence.cpp:270,339): rho k
+// over omega limited below by clim sqrt(2 S^:S^ / beta*), S^ the traceless
+// strain rate of the face velocity gradient
+__device__ __forceinline__ double WkEddyVisc(const Prim<double> &w, const double kw[2],
+                                             const double vg[9], double scale) {
+  const double tr = (vg[0] + vg[4]) + vg[8];
+  const double c = 1.0 / 3.0 * tr;
+  double sh[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+      sh[r * 3 + q] = 0.5 * (vg[r * 3 + q] + vg[q * 3 + r]) - c * (r == q ? 1.0 : 0.0);
+  const double omt = CMax(kw[1], scale * kWkClim * sqrt(2.0 * DDot(sh, sh) / kWkBetaStar));
+  return w.rho * kw[0] / omt;
+}
+
+// turbKWWilcox::CalcTurbSrc (src/turbulence.cpp:359) with Beta / FBeta / Xw
+// / StrainKI / SigmaD (:283-337): production (not limited by destruction),
+// destruction with the vortex-stretching beta, and cross diffusion where
+// grad k . grad omega > 0; returns beta for the source Jacobian
+__device__ __forceinline__ double WkSource(const Prim<double> &w, const double kw[2],
+                                           const double vg[9], const double kg[3],
+                                           const double wg[3], double mut, double scale,
+                                           double src[2]) {
+  const double k = kw[0], om = kw[1], rho = w.rho;
+  const double inv = 1.0 / scale;
+  const double tkeDest = inv * kWkBetaStar * (rho * k * om * 1.0);
+  const double tr = (vg[0] + vg[4]) + vg[8];
+  double vo[9], skI[9], vv[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      vo[r * 3 + q] = 0.5 * (vg[r * 3 + q] - vg[q * 3 + r]);
+      skI[r * 3 + q] = 0.5 * ((vg[r * 3 + q] + vg[q * 3 + r]) - tr * (r == q ? 1.0 : 0.0));
+    }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double t = 0.0;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) t += vo[r * 3 + m] * vo[m * 3 + q];
+      vv[r * 3 + q] = t;
+    }
+  const double xw = fabs(DDot(vv, skI) / pow(kWkBetaStar * om, 3.0)) * pow(scale, 3.0);
+  const double beta = kWkBeta0 * ((1.0 + 85.0 * xw) / (1.0 + 100.0 * xw));
+  const double omgDest = inv * beta * (rho * om * om);
+  const double lambda = 0.0 - (2.0 / 3.0) * mut;
+  const double c23 = 2.0 / 3.0 * rho * k;
+  double tau[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double I = (r == q) ? 1.0 : 0.0;
+      tau[r * 3 + q] = (I * (lambda * tr) + (vg[r * 3 + q] + vg[q * 3 + r]) * mut) - I * c23;
+    }
+  double tkeProd = scale * DDot(tau, vg);
+  tkeProd = CMax(tkeProd, 0.0);
+  double omgProd = kWkGamma * om / k * tkeProd;
+  omgProd = CMax(omgProd, 0.0);
+  const double kdw = ((0.0 + kg[0] * wg[0]) + kg[1] * wg[1]) + kg[2] * wg[2];
+  const double sigd = kdw <= 0.0 ? 0.0 : kWkSigmaD0;
+  const double omgCd = scale * sigd * (rho / om * kdw);
+  src[0] = tkeProd - tkeDest;
+  src[1] = omgProd - omgDest + omgCd;
+  return beta;
+}
+
 // primitive::ApplyFarfieldTurbBC (src/primitive.cpp:83) + LimitTurb
 __device__ __forceinline__ void FarfieldTurb(const Prim<double> &g, double vx, double vy,
                                              double vz, double tint, double ratio,
@@ -205,7 +282,9 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
       const int64_t a = op.src2;
       const double nuW = P.mu[a] / P.W[a];
       const double s = sv.visc_scale;
-      const double wWall = s * s * 60.0 * nuW / (P.wd[a] * P.wd[a] * kSstBeta1);
+      // turbModel::WallBeta: SST beta1, Wilcox 2006 beta0
+      const double wWall =
+          s * s * 60.0 * nuW / (P.wd[a] * P.wd[a] * (sv.wilcox ? kWkBeta0 : kSstBeta1));
       gt[0] = -1.0 * tin[0];
       gt[1] = 2.0 * wWall - tin[1];
       if (op.layer > 1) gt[1] = (double)op.layer * gt[1] - wWall;
@@ -958,18 +1037,21 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const T mutf = rans ? P.rst[d][15 * n + c] : T(0);
-      const T vt = vmax * ViscTerm2(mu, mutf, (T)sv.visc_scale, g);
+      const T vt = vmax * ViscTerm2(mu, mutf, (T)sv.visc_scale, g, (T)PrtOf(sv));
       const T fMag = T(0.5) * ((T)P.fa[d][3 * n + c] + (T)P.fa[d][3 * n + c + st[d]]);
       const T lv = vt * fMag * fMag / (T)vol;
       lam = lam + (double)(lv * (T)sv.visc_coeff);
       adiag = adiag + (double)(T(2) * lv);
       if (rans) {
-        // turbKWSst::ViscousCellSpectralRadius (src/turbulence.cpp:785)
+        // ViscousCellSpectralRadius (turbKWSst src/turbulence.cpp:785,
+        // turbKWWilcox :511): the face's mut and F1, or the cell's rho k / omega
         const double f1f = P.rst[d][16 * n + c];
         const double fm = 0.5 * (P.fa[d][3 * n + c] + P.fa[d][3 * n + c + st[d]]);
         const double length = fm * fm / vol;
-        const double lvt = sv.visc_scale * length / (double)P.W[c] *
-                           ((double)P.mu[c] + Blended(kSstSigmaK1, kSstSigmaK2, f1f) * (double)mutf);
+        const double nutc = sv.wilcox ? P.W[c] * P.Wt[c] / P.Wt[n + c] : 0.0;
+        const TurbDiff<double> df =
+            TurbDiffOf<double>(sv.wilcox, (double)P.mu[c], (double)mutf, f1f, nutc);
+        const double lvt = sv.visc_scale * length / (double)P.W[c] * df.k;
         lamt = lamt + lvt * sv.visc_coeff;
         adiagt = adiagt + 2.0 * lvt;
       }
@@ -1002,7 +1084,9 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     const Prim<double> wd = LoadW<double>(P.W, n, c);
     const double kw[2] = {P.Wt[c], P.Wt[n + c]};
     double src[2];
-    const double beta = SstSource(wd, kw, vg, kg, wg, mutc, f1c, sv.visc_scale, src);
+    const double beta = sv.wilcox ? WkSource(wd, kw, vg, kg, wg, mutc, sv.visc_scale, src)
+                                  : SstSource(wd, kw, vg, kg, wg, mutc, f1c, sv.visc_scale, src);
+    if (P.nutq) P.nutq[q] = (T)(wd.rho * kw[0] / kw[1]);
     const double inv = 1.0 / sv.visc_scale;
     const double srcSR = -2.0 * kSstBetaStar * kw[1] * vol * inv;
     lamt = lamt - srcSR;
@@ -1097,7 +1181,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
     }
     if (sv.viscous) {
       const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s,
-                            (T)sv.k_ref};
+                            (T)sv.k_ref, (T)PrtOf(sv)};
       T vg[9];
 #pragma unroll
       for (int e = 0; e < 9; ++e) vg[e] = T(0);
@@ -1122,8 +1206,10 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                       (T)fa[3 * n + f], dist, side != 0, gr, side != 0, A);
           if (rans) {
             T Jt[4];
-            TurbViscJac(fsx.rho, (T)fa[3 * n + f], vs[5 * n + f], mutf, P.rst[d][16 * n + f],
-                        dist, (T)sv.visc_scale, side ? T(-1) : T(1), Jt);
+            const TurbDiff<T> df = TurbDiffOf<T>(sv.wilcox, vs[5 * n + f], mutf,
+                                                 P.rst[d][16 * n + f], P.rst[d][18 * n + f]);
+            TurbViscJac(fsx.rho, (T)fa[3 * n + f], df, dist, (T)sv.visc_scale,
+                        side ? T(-1) : T(1), Jt);
 #pragma unroll
             for (int e = 0; e < 4; ++e) At[e] = side ? At[e] - Jt[e] : At[e] + Jt[e];
           }
@@ -1192,7 +1278,7 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       if (sv.viscous) {
         P.Npre[7 * nq + q] = ViscMaxTerm(w, gq);
         P.Npre[8 * nq + q] =
-            ViscTerm2(P.muq[q], rans ? P.mutq[q] : T(0), (T)sv.visc_scale, gq);
+            ViscTerm2(P.muq[q], rans ? P.mutq[q] : T(0), (T)sv.visc_scale, gq, (T)PrtOf(sv));
       }
     }
   }
@@ -1229,6 +1315,7 @@ struct Nbr {
   Prim<T> s;
   T du[5], dut[2];
   T mu, mut, f1;
+  T nut;       // rho k / omega (Wilcox k-omega 2006 solves)
   int64_t vq;  // q index whose cell-averaged gradient the neighbour carries
   bool has_pre;    // pre holds the neighbour's precomputed state terms
   NbrPre<T> pre;
@@ -1278,9 +1365,11 @@ __device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, i
     }
     cq = P.ghost_src[slot];
   }
+  o.nut = T(0);
   if (sv.rans) {
     o.mut = P.mutq[cq];
     o.f1 = P.f1q[cq];
+    if (sv.wilcox) o.nut = P.nutq[cq];
   }
   o.vq = cq;
 }
@@ -1321,7 +1410,7 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
     const T vsr = !sv.viscous ? T(0)
                   : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
                               : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
-                                    ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g);
+                                    ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
     T r[5];
     if (o.has_pre)
       ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
@@ -1334,8 +1423,8 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
       T sr = lower ? T(0.5) * mag * fabs(vn + fabs(vn)) : T(0.5) * mag * fabs(vn - fabs(vn));
       if (sv.viscous) {
         const T length = mag / dist[d * nq + q];
-        const T sk = o.f1 * T(0.85) + (T(1) - o.f1) * T(1.0);
-        sr += (T)sv.visc_scale * length / o.s.rho * (o.mu + sk * o.mut);
+        sr += (T)sv.visc_scale * length / o.s.rho *
+              TurbDiffOf<T>(sv.wilcox, o.mu, o.mut, o.f1, o.nut).k;
       }
 #pragma unroll
       for (int k = 0; k < 2; ++k) acct[k] = acct[k] + (lower ? o.dut[k] * sr : -(o.dut[k] * sr));
@@ -1360,7 +1449,7 @@ __device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, cons
   const T vsr = !sv.viscous ? T(0)
                 : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
                             : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
-                                  ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g);
+                                  ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
   if (o.has_pre)
     ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
   else
@@ -1371,8 +1460,8 @@ __device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, cons
     T sr = lower ? T(0.5) * mag * fabs(vn + fabs(vn)) : T(0.5) * mag * fabs(vn - fabs(vn));
     if (sv.viscous) {
       const T length = mag / dist[d * nq + q];
-      const T sk = o.f1 * T(0.85) + (T(1) - o.f1) * T(1.0);
-      sr += (T)sv.visc_scale * length / o.s.rho * (o.mu + sk * o.mut);
+      sr += (T)sv.visc_scale * length / o.s.rho *
+            TurbDiffOf<T>(sv.wilcox, o.mu, o.mut, o.f1, o.nut).k;
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) rt[k] = lower ? o.dut[k] * sr : -(o.dut[k] * sr);
@@ -1411,8 +1500,8 @@ __device__ __forceinline__ void BlockOffJac(const Pools<T> &P, const Gas<T> &g,
     TurbRusanovJac(o.s, fx, fy, fz, mag, lower, Jt);
     if (sv.viscous) {
       T Tv[4];
-      TurbViscJac(o.s.rho, mag, o.mu, o.mut, o.f1, dist[d * nq + q], (T)sv.visc_scale,
-                  lower ? T(-1) : T(1), Tv);
+      TurbViscJac(o.s.rho, mag, TurbDiffOf<T>(sv.wilcox, o.mu, o.mut, o.f1, o.nut),
+                  dist[d * nq + q], (T)sv.visc_scale, lower ? T(-1) : T(1), Tv);
 #pragma unroll
       for (int e = 0; e < 4; ++e) Jt[e] = lower ? Jt[e] - Tv[e] : Jt[e] + Tv[e];
     }
@@ -1430,7 +1519,8 @@ __global__ void __launch_bounds__(128) k_offjac(Pools<T> P, const int2 *items, i
   const SolveDev sv = P.solves[P.blocks[it.y].solve];
   if (!sv.block || !sv.active) return;
   const Gas<T> g = GasOf<T>(sv);
-  const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref};
+  const TslCoeffs<T> tk{(T)sv.visc_scale, (T)sv.t_ref, (T)sv.k_c1, (T)sv.k_s, (T)sv.k_ref,
+                        (T)PrtOf(sv)};
 #pragma unroll 1
   for (int side = 0; side < 2; ++side) {
     const int32_t *nbq = P.nbq + (side == 0 ? 0 : 3 * nq);
@@ -2868,7 +2958,17 @@ __device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, con
   const double vg[9] = {grad[0][0], grad[0][1], grad[0][2], grad[1][0], grad[1][1],
                         grad[1][2], grad[2][0], grad[2][1], grad[2][2]};
   double mutf, f1f, f2f;
-  SstEddyVisc<double>(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
+  if (sv.wilcox) {
+    // turbKWWilcox::EddyViscAndBlending (src/turbulence.cpp:412)
+    mutf = WkEddyVisc(fs, fst, vg, scale);
+    f1f = 1.0;
+    f2f = 0.0;
+  } else {
+    SstEddyVisc<double>(fs, fst, vg, kg, wg, muf, wdf, scale, mutf, f1f, f2f);
+  }
+  // the face state's unlimited eddy viscosity (Wilcox: turbulence diffusion
+  // and the 2x2 viscous Jacobian)
+  const double nutf = sv.wilcox ? fs.rho * fst[0] / fst[1] : 0.0;
   const double *fa = P.fa[D];
   const double nx = fa[c], ny = fa[n + c], nz = fa[2 * n + c], mag = fa[3 * n + c];
   const double mus = scale * muf, muts = scale * mutf;
@@ -2876,7 +2976,7 @@ __device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, con
   TauNormal(vg, nx, ny, nz, mus, muts, tau);
   const double kf = SutherlandRatio(Temperature(fs, g), sv.t_ref, sv.k_c1, sv.k_s, sv.k_ref) *
                     scale;
-  const double kt = muts * g.Cp() / 0.9;
+  const double kt = muts * g.Cp() / PrtOf(sv);
   double F[5];
   F[0] = 0.0;
   F[1] = tau[0];
@@ -2884,10 +2984,13 @@ __device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, con
   F[3] = tau[2];
   F[4] = Dot(tau[0], tau[1], tau[2], fs.u, fs.v, fs.w) +
          (kf + kt) * Dot(tg[0], tg[1], tg[2], nx, ny, nz) + 0.0;
-  const double Ft0 = (mus + Blended(kSstSigmaK1, kSstSigmaK2, f1f) * muts) *
-                     Dot(kg[0], kg[1], kg[2], nx, ny, nz);
-  const double Ft1 = (mus + Blended(kSstSigmaW1, kSstSigmaW2, f1f) * muts) *
-                     Dot(wg[0], wg[1], wg[2], nx, ny, nz);
+  // viscousFlux::CalcFlux (src/viscousFlux.cpp:118-133): Wilcox 2006 takes
+  // the unlimited eddy viscosity in the turbulence diffusion
+  const double mutt = sv.wilcox ? scale * nutf : muts;
+  const double sk = sv.wilcox ? kWkSigmaStar : Blended(kSstSigmaK1, kSstSigmaK2, f1f);
+  const double sw = sv.wilcox ? kWkSigma : Blended(kSstSigmaW1, kSstSigmaW2, f1f);
+  const double Ft0 = (mus + sk * mutt) * Dot(kg[0], kg[1], kg[2], nx, ny, nz);
+  const double Ft1 = (mus + sw * mutt) * Dot(wg[0], wg[1], wg[2], nx, ny, nz);
   T *out = P.vflux[D];
 #pragma unroll
   for (int v = 0; v < 5; ++v) out[v * n + c] = (T)(F[v] * mag);
@@ -2903,6 +3006,7 @@ __device__ __forceinline__ void RansViscFace(Pools<T> &P, const BlockDev &b, con
   }
   rs[15 * n + c] = (T)mutf;
   rs[16 * n + c] = (T)f1f;
+  rs[18 * n + c] = (T)nutf;
   rs[17 * n + c] = (T)f2f;
   if (sv.block) {
     T *vs = P.vst[D];

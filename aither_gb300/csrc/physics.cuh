@@ -689,8 +689,8 @@ __device__ __forceinline__ T ViscTerm(T mu, T scale, const Gas<T> &g) {
 }
 // the same with the eddy viscosity mut (turbulent Prandtl number 0.9)
 template <typename T>
-__device__ __forceinline__ T ViscTerm2(T mu, T mut, T scale, const Gas<T> &g) {
-  return scale * (mu / Prandtl(g) + mut / T(0.9));
+__device__ __forceinline__ T ViscTerm2(T mu, T mut, T scale, const Gas<T> &g, T prt = T(0.9)) {
+  return scale * (mu / Prandtl(g) + mut / prt);
 }
 // sutherland::SpeciesViscosity / SpeciesConductivity (src/transport.cpp:100,108)
 template <typename T>

@@ -104,7 +104,8 @@ def test_fp64_matches_reference_fixture(ctx, name, tmp_path):
 SST_CASES = ["sst_plate_it1", "sst_plate_it20", "sst_plate2_blusgs_it1",
              "sst_plate2_blusgs_it10", "sst_weno_ausm_it1", "sst_weno_ausm_it10",
              "sst_plate_dplur_it1", "sst_plate_dplur_it10", "sst_chan_stag_pout_it1",
-             "sst_chan_stag_pout_it10", "sst_plate_bdf2_it1", "sst_plate_bdf2_it4"]
+             "sst_chan_stag_pout_it10", "sst_plate_bdf2_it1", "sst_plate_bdf2_it4",
+             "wk_plate_it1", "wk_plate_it15", "wk_plate2_blusgs_it1", "wk_plate2_blusgs_it15"]
 
 
 @pytest.mark.parametrize("name", SST_CASES)
