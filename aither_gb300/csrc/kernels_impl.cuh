@@ -1412,7 +1412,10 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
                               : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
                                     ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
     T r[5];
-    if (o.has_pre)
+    if (o.has_pre && P.fast_fp64)
+      ScalarOffDiagPreFast(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr,
+                           r);
+    else if (o.has_pre)
       ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
     else
       ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
@@ -1450,7 +1453,9 @@ __device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, cons
                 : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
                             : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
                                   ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
-  if (o.has_pre)
+  if (o.has_pre && P.fast_fp64)
+    ScalarOffDiagPreFast(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+  else if (o.has_pre)
     ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
   else
     ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);

@@ -833,4 +833,40 @@ __device__ __forceinline__ void ScalarOffDiagPre(const Prim<T> &s, const NbrPre<
   }
 }
 
+// ScalarOffDiagPre in the fast-arithmetic form of FP64 batches with the
+// fast option: the updated state with one reciprocal of the density and no
+// square root, p = (gamma - 1) (rho E - rho (hf + |v|^2 / 2)) and
+// rho H = rho E + p; equal to the reference's form to roundoff.
+template <typename T>
+__device__ __forceinline__ void ScalarOffDiagPreFast(const Prim<T> &s, const NbrPre<T> &pre,
+                                                     const T du[5], const Gas<T> &g, T nx, T ny,
+                                                     T nz, T mag, bool positive, T visc_sr,
+                                                     T out[5]) {
+  T c[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) c[v] = pre.c[v] + du[v];
+  const T ir = T(1) / c[0];
+  const T u = c[1] * ir, v = c[2] * ir, w = c[3] * ir;
+  const T ke = T(0.5) * (u * u + v * v + w * w);
+  const T p = (g.gam - T(1)) * (c[4] - c[0] * (g.hf + ke));
+  const T vnn = u * nx + v * ny + w * nz;
+  const T mn = c[0] * vnn;
+  const T vn = Dot(s.u, s.v, s.w, nx, ny, nz);
+  const T mo = s.rho * vn;
+  T df[5];
+  df[0] = mn - mo;
+  df[1] = (mn * u + p * nx) - (mo * s.u + s.p * nx);
+  df[2] = (mn * v + p * ny) - (mo * s.v + s.p * ny);
+  df[3] = (mn * w + p * nz) - (mo * s.w + s.p * nz);
+  df[4] = vnn * (c[4] + p) - mo * pre.h;
+  const T half = T(0.5) * mag;
+  T lam = T(0.5) * mag * (fabs(vn) + pre.sos);
+  lam += visc_sr;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const T fc = half * df[k];
+    out[k] = positive ? fc + lam * du[k] : fc - lam * du[k];
+  }
+}
+
 }  // namespace ath
