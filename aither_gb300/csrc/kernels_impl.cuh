@@ -119,6 +119,17 @@ __device__ __forceinline__ double SstSource(const Prim<double> &w, const double 
   return beta;
 }
 
+// x^3 rounded once: x^2 and x^2 x as exact two-term products (FMA error-free
+// transformation, Dekker's TwoProduct), summed with the error terms; the
+// host's pow(x, 3.0) in the reference rounds the exact cube once too
+__device__ __forceinline__ double Cube(double x) {
+  const double h = x * x;
+  const double l = fma(x, x, -h);
+  const double c = h * x;
+  const double e = fma(h, x, -c);
+  return c + fma(l, x, e);
+}
+
 // Wilcox k-omega 2006 constants (turbKWWilcox, include/turbulence.hpp:391-398)
 constexpr double kWkGamma = 0.52, kWkBetaStar = 0.09, kWkSigma = 0.5, kWkSigmaStar = 0.6;
 constexpr double kWkSigmaD0 = 0.125, kWkBeta0 = 0.0708, kWkClim = 0.875;
@@ -171,7 +182,7 @@ __device__ __forceinline__ double WkSource(const Prim<double> &w, const double k
       for (int m = 0; m < 3; ++m) t += vo[r * 3 + m] * vo[m * 3 + q];
       vv[r * 3 + q] = t;
     }
-  const double xw = fabs(DDot(vv, skI) / pow(kWkBetaStar * om, 3.0)) * pow(scale, 3.0);
+  const double xw = fabs(DDot(vv, skI) / Cube(kWkBetaStar * om)) * Cube(scale);
   const double beta = kWkBeta0 * ((1.0 + 85.0 * xw) / (1.0 + 100.0 * xw));
   const double omgDest = inv * beta * (rho * om * om);
   const double lambda = 0.0 - (2.0 / 3.0) * mut;
