@@ -535,7 +535,8 @@ def _converge_once(ctx, setup, prec, args, world):
     return {"solves": len(info), "converged": int(sum(conv)), "device_s": dev_s, "wall_s": wall,
             "solves_per_s": sum(conv) * world / dev_s, "p50_ms": _pct(ms, 50),
             "p99_ms": _pct(ms, 99), "iterations_p50": _pct(its, 50),
-            "iterations_max": max(its) if its else None, "sweep_threads": tuned}, states, its
+            "iterations_max": max(its) if its else None, "sweep_threads": tuned}, states, \
+        (its, conv)
 
 
 def run_converge(args, ctx, setup, specs, world):
@@ -559,14 +560,19 @@ def run_converge(args, ctx, setup, specs, world):
         with tempfile.TemporaryDirectory() as tmp:
             inps, _ = make_workload(tmp, args.ncases)
             sub = Setup([inps[i] for i in pick])
-        f64, w64, it64 = _converge_once(ctx, sub, PREC_FP64, args, world)
-        mix, wmx, itmx = _converge_once(ctx, sub, PREC_MIXED, args, world)
-        err = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(wmx, w64))
+        f64, w64, (it64, cv64) = _converge_once(ctx, sub, PREC_FP64, args, world)
+        mix, wmx, (itmx, cvmx) = _converge_once(ctx, sub, PREC_MIXED, args, world)
+        # the converged solves' states (an unconverged one is anywhere on its
+        # limit cycle)
+        both = [q for q in range(len(w64)) if cv64[q] and cvmx[q]]
+        err = max((float(np.abs(wmx[q] - w64[q]).max() / np.abs(w64[q]).max()) for q in both),
+                  default=None)
         out["subset"] = {"cases": pick, "cells": int(sum(specs[i][0] * specs[i][1] * specs[i][2]
                                                          for i in pick)),
                          "fp64": f64, "mixed": mix,
                          "mixed_speedup": f64["device_s"] / mix["device_s"],
                          "mixed_vs_fp64_state_max_rel_err": err,
+                         "state_err_over": "solves converged in both precisions",
                          "iterations_max_abs_diff": int(max(abs(a - b) for a, b in zip(itmx, it64)))}
     return out
 
@@ -600,7 +606,9 @@ def run_mg(args, ctx, world):
             x = info[0]
             its = max(int(x.iterations), 1)
             dev_s = _max_over_ranks(st.device_ms * 1e-3, world)
-            res[pname] = {"iterations": int(x.iterations), "converged": bool(x.converged == 1),
+            res[pname] = {"iterations": int(x.iterations),
+                          "status": {1: "converged", 0: "iteration_cap",
+                                     -1: "nonphysical"}.get(int(x.converged), int(x.converged)),
                           "drop_reached": x.drop, "device_s": dev_s,
                           "ms_per_iteration": dev_s * 1e3 / its,
                           "gpu_launches_per_iteration": int(st.kernel_launches) // its}
