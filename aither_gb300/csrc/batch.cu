@@ -383,6 +383,7 @@ class Runner : public RunnerBase {
     // FP64 batches with the fast option: contracted-FMA faces, cell, sweeps
     // and update (batch flag bit 1)
     P_.fast_fp64 = (std::is_same<T, double>::value && (c.flags & 2)) ? 1 : 0;
+    P_.fkinds = c.fkinds;
     P_.W = m.Alloc<double>(5 * n);
     P_.R = m.Alloc<double>(5 * n);
     for (int d = 0; d < 3; ++d) P_.flux[d] = m.Alloc<double>(5 * n);

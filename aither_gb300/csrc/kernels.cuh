@@ -203,6 +203,9 @@ struct Pools {
   // faces, cell, scalar sweep and update kernels built with contracted
   // multiply-adds (kernels_fp64_fast.cu); a host-side switch
   int fast_fp64;
+  // solve kinds of the batch (host-side): bit 0 solves without, bit 1 with
+  // turbulence equations; the cell kernel is built per kind
+  int fkinds;
   const BlockDev *blocks;
   const SolveDev *solves;
   const ath_bc_state *states;
@@ -249,7 +252,7 @@ __global__ void k_face(Pools<T> P, const int32_t *list, const int32_t *cta_block
 // diagonal of every physical cell (procBlock residual accumulation,
 // CalcBlockTimeStep src/procBlock.cpp:798, AddDiagonalTerms/Invert
 // src/linearSolver.cpp:146,177).
-template <typename T, bool BLOCK>
+template <typename T, bool BLOCK, bool RANS>
 __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block);
 
 // One hyperplane of the LU-SGS forward / backward sweep
@@ -258,9 +261,9 @@ __global__ void k_cell(Pools<T> P, const int32_t *list, const int32_t *cta_block
 // both triangles may enter a pass.  k_sweep (a thread per cell) and
 // k_sweepg (a group of lanes per cell, one per neighbour term) serve scalar
 // solves, k_sweepb block solves.
-template <typename T, bool FULL>
+template <typename T, bool FULL, bool TURB>
 __global__ void k_sweep(Pools<T> P, const int2 *items, int n, int forward, int sweep);
-template <typename T, bool FULL, int MINB = 1>
+template <typename T, bool FULL, int MINB, bool TURB>
 __global__ void k_sweepg(Pools<T> P, const int2 *items, int n, int forward, int sweep);
 template <typename T>
 __global__ void k_sweepb(Pools<T> P, const int2 *items, int n, int forward, int sweep,

@@ -20,22 +20,38 @@ void LaunchFastFaceFp64(int d, const Pools<double> &P, const int32_t *list,
 void LaunchFastCellFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
                         int ncta, int kinds, cudaStream_t s) {
   if (ncta <= 0) return;
-  if (kinds & 1) k_cell<double, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  if (kinds & 2) k_cell<double, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 1) && (P.fkinds & 1))
+    k_cell<double, false, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 1) && (P.fkinds & 2))
+    k_cell<double, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 2) && (P.fkinds & 1))
+    k_cell<double, true, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 2) && (P.fkinds & 2))
+    k_cell<double, true, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 
 void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int forward,
                          int sweep, bool full, int threads, bool group, cudaStream_t s) {
   if (n <= 0) return;
+  // without turbulence solves the kernels are built without their rows
+  const bool turb = (P.fkinds & 2) != 0;
   if (group) {
     const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
     const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
-    if (full) k_sweepg<double, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweepg<double, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    if (full && turb)
+      k_sweepg<double, true, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (full)
+      k_sweepg<double, true, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (turb)
+      k_sweepg<double, false, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else
+      k_sweepg<double, false, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
   } else {
     const unsigned grid = (unsigned)((n + threads - 1) / threads);
-    if (full) k_sweep<double, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweep<double, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    if (full && turb) k_sweep<double, true, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (full) k_sweep<double, true, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (turb) k_sweep<double, false, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweep<double, false, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
 }
 

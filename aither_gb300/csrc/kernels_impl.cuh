@@ -956,7 +956,7 @@ __global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const i
 // omega residuals, turbulence radii, SST sources (from cell averages of the
 // six faces' gradients, eddy viscosity and blending) and the turbulence
 // diagonal (scalar, or 2x2 for block solves).
-template <typename T, bool BLOCK>
+template <typename T, bool BLOCK, bool RANS>
 __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
@@ -966,7 +966,8 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   if (c < 0) return;
   const int64_t n = P.ncell;
   const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
-  const bool rans = sv.rans != 0;
+  if ((sv.rans != 0) != RANS) return;
+  constexpr bool rans = RANS;
   // R = 0 - Fi(lo) + Fi(hi) - Fj(lo) + Fj(hi) - Fk(lo) + Fk(hi), each face
   // term rounded in this order (src/procBlock.cpp:447-463); viscous faces
   // follow with + Fv(lo) - Fv(hi) per direction (:1392-1429)
@@ -1707,14 +1708,20 @@ __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &
 }
 
 // one plane of every scalar solve, one thread per cell
-template <typename T, bool FULL>
+// TURB = false: the batch has no solves with turbulence equations, and the
+// kernel is built without their rows (fewer registers)
+template <typename T, bool FULL, bool TURB>
 __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, int n_items,
                                                int forward, int sweep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_items) return;
   const int2 it = items[t];
-  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  SolveDev sv = P.solves[P.blocks[it.y].solve];
   if (sv.block || sv.jacobi || !sv.active) return;
+  if constexpr (!TURB) {
+    sv.rans = 0;
+    sv.wilcox = 0;
+  }
   SweepScalarQ<T, FULL>(P, sv, it.x, forward, sweep);
 }
 
@@ -1733,7 +1740,7 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
 // warp shuffles in the reference's i, j, k order.  Every lane of the warp
 // calls it (the shuffles span the warp); c is the cell's position in
 // items, valid for c < n_items.
-template <typename T, bool FULL>
+template <typename T, bool FULL, bool TURB = true>
 __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *items, int c,
                                                int n_items, int forward, int sweep) {
   constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
@@ -1741,7 +1748,11 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
   const int li = lane % L;
   bool valid = lane < CPW * L && c < n_items;
   const int2 it = valid ? items[c] : make_int2(0, 0);
-  const SolveDev sv = P.solves[P.blocks[it.y].solve];
+  SolveDev sv = P.solves[P.blocks[it.y].solve];
+  if constexpr (!TURB) {
+    sv.rans = 0;
+    sv.wilcox = 0;
+  }
   valid = valid && !sv.block && !sv.jacobi && sv.active;
   bool both = false;
   if constexpr (FULL) {
@@ -1785,13 +1796,13 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
   ScalarFinish<T, FULL>(P, sv, it.x, forward, both, acc, acct, other, othert);
 }
 
-template <typename T, bool FULL, int MINB>
+template <typename T, bool FULL, int MINB, bool TURB>
 __global__ void __launch_bounds__(256, MINB) k_sweepg(Pools<T> P, const int2 *items, int n_items,
                                                 int forward, int sweep) {
   constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = (int)(threadIdx.x & 31);
-  SweepGroupItem<T, FULL>(P, items, (t >> 5) * CPW + lane / L, n_items, forward, sweep);
+  SweepGroupItem<T, FULL, TURB>(P, items, (t >> 5) * CPW + lane / L, n_items, forward, sweep);
 }
 
 // Loads of one row of a block sweep that depend on the cell alone: the
@@ -3418,8 +3429,12 @@ void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_
       return;
     }
   }
-  if (kinds & 1) k_cell<T, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
-  if (kinds & 2) k_cell<T, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  // one kernel per solve kind (block / scalar, with / without turbulence
+  // equations), so the laminar ones keep their register budget
+  if ((kinds & 1) && (P.fkinds & 1)) k_cell<T, false, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 1) && (P.fkinds & 2)) k_cell<T, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 2) && (P.fkinds & 1)) k_cell<T, true, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((kinds & 2) && (P.fkinds & 2)) k_cell<T, true, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
 void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
@@ -3436,12 +3451,18 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, 
   } else if ((kinds & 1) && group) {
     const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
     const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
-    if (full) k_sweepg<T, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweepg<T, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    const bool turb = (P.fkinds & 2) != 0;
+    if (full && turb) k_sweepg<T, true, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (full) k_sweepg<T, true, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (turb) k_sweepg<T, false, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweepg<T, false, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
   } else if (kinds & 1) {
     const unsigned grid = (unsigned)((n + threads - 1) / threads);
-    if (full) k_sweep<T, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweep<T, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    const bool turb = (P.fkinds & 2) != 0;
+    if (full && turb) k_sweep<T, true, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (full) k_sweep<T, true, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else if (turb) k_sweep<T, false, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    else k_sweep<T, false, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
   }
   if (kinds & 2) {
     const unsigned gridb = (unsigned)(((int64_t)n * 8 + threads - 1) / threads);

