@@ -957,7 +957,8 @@ __global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const i
 // six faces' gradients, eddy viscosity and blending) and the turbulence
 // diagonal (scalar, or 2x2 for block solves).
 template <typename T, bool BLOCK, bool RANS>
-__global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
+__global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<T> P,
+                                                                         const int32_t *list,
                                                const int32_t *cta_block) {
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
@@ -1016,13 +1017,25 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
   // scalar main diagonal: accumulates like the radius, from zero or (a
   // multigrid level visited again in this iteration) from its previous value
   double adiag = (!BLOCK && P.mg_accum) ? (double)P.Aq[q] : 0.0;
+  // fast FP64 option: the sound speed once per cell, the averaged face
+  // normal's length by one reciprocal square root per direction
+  const bool fastc = std::is_same<T, double>::value && P.fast_fp64;
+  const T sosc = fastc ? SoS(w, g) : T(0);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double *fa = P.fa[d];
     const int64_t u = c + st[d];
-    const double lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
-                                              (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u],
-                                              (T)fa[2 * n + u], (T)fa[3 * n + u]);
+    double lcd;
+    if (fastc) {
+      const T ax = T(0.5) * ((T)fa[c] + (T)fa[u]), ay = T(0.5) * ((T)fa[n + c] + (T)fa[n + u]),
+              az = T(0.5) * ((T)fa[2 * n + c] + (T)fa[2 * n + u]);
+      const T vn = fabs(Dot(w.u, w.v, w.w, ax, ay, az)) * rsqrt(Dot(ax, ay, az, ax, ay, az));
+      lcd = (double)((vn + sosc) * (T(0.5) * ((T)fa[3 * n + c] + (T)fa[3 * n + u])));
+    } else {
+      lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
+                                   (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u],
+                                   (T)fa[3 * n + u]);
+    }
     lam = lam + lcd;
     adiag = adiag + lcd;
     if (rans) {
@@ -1285,8 +1298,15 @@ __global__ void __launch_bounds__(kCta) k_cell(Pools<T> P, const int32_t *list,
       PrimToCons(w, gq, cc);
 #pragma unroll
       for (int v = 0; v < 5; ++v) P.Npre[v * nq + q] = cc[v];
-      P.Npre[5 * nq + q] = Enthalpy(w, gq);
-      P.Npre[6 * nq + q] = SoS(w, gq);
+      if (fastc) {
+        // h = hf + cp T + |v|^2 / 2 with cp T = (n + 1) p / rho
+        P.Npre[5 * nq + q] = (gq.hf + (gq.n + T(1)) * (w.p / w.rho)) +
+                             T(0.5) * Dot(w.u, w.v, w.w, w.u, w.v, w.w);
+        P.Npre[6 * nq + q] = sosc;
+      } else {
+        P.Npre[5 * nq + q] = Enthalpy(w, gq);
+        P.Npre[6 * nq + q] = SoS(w, gq);
+      }
       if (sv.viscous) {
         P.Npre[7 * nq + q] = ViscMaxTerm(w, gq);
         P.Npre[8 * nq + q] =
