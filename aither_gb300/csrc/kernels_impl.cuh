@@ -2360,7 +2360,24 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     const int64_t q = P.qpos[c], qpos = q;
 #pragma unroll
     for (int v = 0; v < 5; ++v) du[v] = (double)P.dUq[v * P.nq + q];
-    const Prim<double> u = UpdateWithCons(w, g, du);
+    Prim<double> u;
+    if (P.fast_fp64) {
+      // fast FP64 option: rho E = rho hf + n p + rho |v|^2 / 2 (cv T rho = n p),
+      // then the updated state with one reciprocal of the density
+      const double rho1 = w.rho + du[0];
+      const double c1 = w.rho * w.u + du[1], c2 = w.rho * w.v + du[2], c3 = w.rho * w.w + du[3];
+      const double rE = (w.rho * g.hf + g.n * w.p +
+                         0.5 * w.rho * Dot(w.u, w.v, w.w, w.u, w.v, w.w)) + du[4];
+      const double ir = 1.0 / rho1;
+      u.rho = rho1;
+      u.u = c1 * ir;
+      u.v = c2 * ir;
+      u.w = c3 * ir;
+      u.p = (g.Gamma() - 1.0) *
+            (rE - rho1 * (g.hf + 0.5 * Dot(u.u, u.v, u.w, u.u, u.v, u.w)));
+    } else {
+      u = UpdateWithCons(w, g, du);
+    }
     if (!(u.rho > 0.0) || !(u.p > 0.0) || !isfinite(u.u) || !isfinite(u.v) ||
         !isfinite(u.w))
       bad = 1;
