@@ -709,27 +709,31 @@ def _max_over_ranks(x: float, world: int) -> float:
 # -------------------------------------------------------------------- main
 # One-off ncu captures of the FP64 batched path, per cell of the batch (a
 # bump-channel batch's cells; the counts scale with cells):
-#   * fast faces -- `ncu --clock-control none --metrics dram__bytes_read.sum,
+#   * fast option -- `ncu --clock-control none --metrics dram__bytes_read.sum,
 #     dram__bytes_write.sum,gpu__time_duration.sum,smsp__sass_thread_inst_
-#     executed_op_{dfma,dadd,dmul}_pred_on.sum -k regex:'k_face|k_cell' -c 8`
-#     on `python bench.py --ncases 8 --steps 2 --warmup 3 --converge-drop 0
-#     --served-n 0 --plate-iters 0 --sst-steps 0 --vortex-iters 0
-#     --no-cpu-baseline --precision fp64` (the first 8 cases, 888,004 cells;
-#     GB300, 2026-12-04): residual-pass DRAM traffic 804.4 B per cell (faces
-#     102.9 + 112.3 + 112.6, cell kernel 476.6), executed FP64 FLOP 442.1 per
-#     face direction and 502.3 in the cell kernel;
-#   * bit-exact faces, sweeps, update and ghost fill -- the SASS counters
-#     over one iteration of a 64x48x32 bump channel: 1026 FLOP per face
-#     direction, 1134 in the two sweeps, 502 cell, 188 update, 25 ghosts.
+#     executed_op_{dfma,dadd,dmul}_pred_on.sum -s 1103 -c 355` (every launch of
+#     the first timed iteration) on `python bench.py --ncases 8 --steps 1
+#     --warmup 3 --no-cpu-baseline --converge-drop 0 --served-n 0 --sst-steps 0
+#     --plate-iters 0 --vortex-iters 0 --mg-iters 0 --precision fp64
+#     --sweep-shape 2,32 --exact-arm 0` (the first 8 cases, 888,004 cells;
+#     GB300, 2026-12-04): residual-pass DRAM traffic 811.4 B per cell (faces
+#     103.4 + 110.2 + 115.1, cell kernel 482.7); executed FP64 FLOP 440.3 per
+#     face direction, 684.8 in the two sweeps, 297.0 cell, 101.3 update,
+#     23.7 ghost fill;
+#   * bit-exact path -- the same counters over one iteration of a 64x48x32
+#     bump channel: 1026 FLOP per face direction, 1134 in the two sweeps,
+#     502 cell, 188 update, 25 ghosts.
 # FLOP = 2 x DFMA + DADD + DMUL (divisions and square roots run as FMA
 # sequences and are counted in those).
 NCU_PER_CELL = {
-    "source": "ncu captures on GB300 of the batched bump-channel path (fast faces: first "
-              "8 cases of the batched workload, 888,004 cells; bit-exact faces and the "
-              "other kernels: one 64x48x32 case), 2026-12-04",
-    "residual_traffic_bytes": {"fast": 804.4},
-    "flop": {"face_per_direction": {"fast": 442.1, "exact": 1026.0}, "sweeps": 1134.0,
-             "cell": 502.3, "update": 188.0, "ghost": 25.0},
+    "source": "ncu captures on GB300 of the batched bump-channel path (fast option: every "
+              "launch of one iteration of the first 8 cases of the batched workload, "
+              "888,004 cells; bit-exact path: one 64x48x32 case), 2026-12-04",
+    "residual_traffic_bytes": {"fast": 811.4},
+    "flop": {"fast": {"face_per_direction": 440.3, "sweeps": 684.8, "cell": 297.0,
+                      "update": 101.3, "ghost": 23.7},
+             "exact": {"face_per_direction": 1026.0, "sweeps": 1134.0, "cell": 502.0,
+                       "update": 188.0, "ghost": 25.0}},
 }
 
 
@@ -849,9 +853,9 @@ def main():
     roof_fp64 = None
     fp64_peak = res.get("fp64_peak_tflops") or 0.0
     if "fp64" in res and fp64_peak:
-        fl = NCU_PER_CELL["flop"]
         mode = "fast" if args.fast_faces else "exact"
-        fpd = fl["face_per_direction"][mode]
+        fl = NCU_PER_CELL["flop"][mode]
+        fpd = fl["face_per_direction"]
         face_ms = km["face_i"] + km["face_j"] + km["face_k"]
         face_tf = 3 * fpd * ncells / (face_ms * 1e-3) / 1e12
         path_flop = 3 * fpd + fl["sweeps"] + fl["cell"] + fl["update"] + fl["ghost"]
