@@ -705,16 +705,23 @@ class Runner : public RunnerBase {
       return;
     }
     if (forward) {
+      // a plane's launch is chained to the pass's previous launch only
+      bool chained = false;
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        if (b <= a) continue;
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.sweep_mode == 2, c_.stream);
+                         c_.sweep_threads, c_.sweep_mode == 2, chained, c_.stream);
+        chained = true;
       }
     } else {
+      bool chained = false;
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+        if (b <= a) continue;
         Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.sweep_mode == 2, c_.stream);
+                         c_.sweep_threads, c_.sweep_mode == 2, chained, c_.stream);
+        chained = true;
       }
     }
   }
@@ -1865,6 +1872,7 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     x.nstates = (int32_t)st.solves[s].states.size();
     x.state0 = (int32_t)states.size();
     for (auto &q : st.solves[s].states) states.push_back(q);
+    SetDerived(x);
     sd[s] = x;
   }
   c.d_blocks = m.Upload(bd);

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "aither_gb300.h"
 #include "physics.cuh"
@@ -51,7 +52,29 @@ struct SolveDev {
   double dt_global, dual_cfl;
   int32_t nl_iters, multilevel, unsteady;
   int32_t store_n;  // keep the time-n state: time-accurate or nonreflecting
+  // Constants derived from the ones above by SetDerived() on the host, each
+  // one IEEE operation (or Gas::Set's three) so its bits are those a thread
+  // would compute; kernels read them instead of dividing per thread: cv, cp
+  // and gamma in double and in float, and 1 / theta
+  double gas_cv, gas_cp, gas_gam, theta_inv;
+  float gas_cvf, gas_cpf, gas_gamf, pad_f;
 };
+
+// Fills SolveDev's derived constants from gas_r, gas_n, gas_hf and theta
+inline void SetDerived(SolveDev &x) {
+  Gas<double> gd;
+  gd.Set(x.gas_r, x.gas_n, x.gas_hf);
+  x.gas_cv = gd.cv;
+  x.gas_cp = gd.cp;
+  x.gas_gam = gd.gam;
+  Gas<float> gf;
+  gf.Set((float)x.gas_r, (float)x.gas_n, (float)x.gas_hf);
+  x.gas_cvf = gf.cv;
+  x.gas_cpf = gf.cp;
+  x.gas_gamf = gf.gam;
+  x.pad_f = 0.0f;
+  x.theta_inv = 1.0 / x.theta;
+}
 
 // Per-solve hyperplane lists of the persistent sweep: items (q index,
 // block) ordered by solve, then plane; step_off[solve_step0[s] + p] .. +1
@@ -228,10 +251,35 @@ __device__ __forceinline__ Prim<T> LoadW(const double *W, int64_t n, int64_t c) 
   return s;
 }
 
+// Programmatic dependent launch (sm_90 and later).  GridDependencyWait
+// returns once the grid this one was launched after with the
+// programmatic-serialization attribute has completed and its memory
+// operations are visible (at once for a normal launch);
+// GridDependentsLaunch lets the grid launched after this one with that
+// attribute start (a no-op without one).
+__device__ __forceinline__ void GridDependencyWait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void GridDependentsLaunch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <typename T>
 __device__ __forceinline__ Gas<T> GasOf(const SolveDev &s) {
+  static_assert(std::is_same<T, double>::value || std::is_same<T, float>::value, "T");
   Gas<T> g;
-  g.Set((T)s.gas_r, (T)s.gas_n, (T)s.gas_hf);
+  g.r = (T)s.gas_r;
+  g.n = (T)s.gas_n;
+  g.hf = (T)s.gas_hf;
+  if constexpr (std::is_same<T, double>::value) {
+    g.cv = s.gas_cv;
+    g.cp = s.gas_cp;
+    g.gam = s.gas_gam;
+  } else {
+    g.cv = s.gas_cvf;
+    g.cp = s.gas_cpf;
+    g.gam = s.gas_gamf;
+  }
   return g;
 }
 
@@ -335,7 +383,8 @@ void LaunchFastFaceFp64(int d, const Pools<double> &P, const int32_t *list,
 void LaunchFastCellFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
                         int ncta, int kinds, cudaStream_t s);
 void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int forward,
-                         int sweep, bool full, int threads, bool group, cudaStream_t s);
+                         int sweep, bool full, int threads, bool group, bool chained,
+                         cudaStream_t s);
 void LaunchFastUpdateFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
                           const int32_t *cta_pos0, NormPartial *partials, int ncta,
                           const SolveState *ss, cudaStream_t s);
@@ -375,8 +424,12 @@ struct Launch {
   // kinds: bit 0 = the batch has scalar solves, bit 1 = block solves
   static void Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                    int ncta, int kinds, cudaStream_t s);
+  // chained: the launch follows the same pass's previous hyperplane, so the
+  // grouped sweep starts programmatically and overlaps its loads of data the
+  // pass does not change with that plane's kernel
   static void Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                    bool full, int kinds, int threads, bool group, cudaStream_t s);
+                    bool full, int kinds, int threads, bool group, bool chained,
+                    cudaStream_t s);
   // one pass of every LU-SGS solve as one launch: a cluster of `cluster`
   // CTAs of `threads` per solve walks its hyperplanes with cluster barriers
   static void SweepCl(const Pools<T> &P, const SweepLists &L, int forward, int sweep,

@@ -31,21 +31,13 @@ void LaunchFastCellFp64(const Pools<double> &P, const int32_t *list, const int32
 }
 
 void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int forward,
-                         int sweep, bool full, int threads, bool group, cudaStream_t s) {
+                         int sweep, bool full, int threads, bool group, bool chained,
+                         cudaStream_t s) {
   if (n <= 0) return;
   // without turbulence solves the kernels are built without their rows
   const bool turb = (P.fkinds & 2) != 0;
   if (group) {
-    const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
-    const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
-    if (full && turb)
-      k_sweepg<double, true, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (full)
-      k_sweepg<double, true, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (turb)
-      k_sweepg<double, false, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else
-      k_sweepg<double, false, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    LaunchSweepGroup<double>(P, items, n, forward, sweep, full, threads, chained, s);
   } else {
     const unsigned grid = (unsigned)((n + threads - 1) / threads);
     if (full && turb) k_sweep<double, true, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);

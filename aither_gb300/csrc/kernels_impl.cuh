@@ -622,8 +622,10 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
     const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
     const U kappa = (U)sv.kappa;
     if constexpr (FAST) {
-      L = MusclFast(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
-      R = MusclFast(wp1, w0, wm1, xp1, x0, xm1, kappa, sv.limiter);
+      U dpL, dmL, dpR, dmR;
+      MusclFastRatios(xm2, xm1, x0, xp1, dpL, dmL, dpR, dmR);
+      L = MusclFast(wm2, wm1, w0, dpL, dmL, kappa, sv.limiter);
+      R = MusclFast(wp1, w0, wm1, dpR, dmR, kappa, sv.limiter);
     } else {
       // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
       L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
@@ -1154,7 +1156,7 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
     PrimToCons(wd, gd, cn);
     cn[5] = rans ? wd.rho * P.Wt[c] : 0.0;
     cn[6] = rans ? wd.rho * P.Wt[n + c] : 0.0;
-    const double thetaInvD = 1.0 / sv.theta;
+    const double thetaInvD = sv.theta_inv;
     const double coeffN = (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
     const double coeffNm1 = (vol * sv.zeta) / (dt * sv.theta);
     const int nvs = rans ? 7 : 5;
@@ -1352,58 +1354,85 @@ struct Nbr {
   bool has_pre;    // pre holds the neighbour's precomputed state terms
   NbrPre<T> pre;
 };
+// The part of a neighbour's data that depends on the neighbour alone and
+// that the sweeps do not change: its state and, for q-ordered neighbours,
+// the precomputed state terms; for connection ghosts the partner cell's
+// state, and the q index of the cell whose turbulence data applies (vq)
 template <typename T>
-__device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, int32_t nb,
-                                        Nbr<T> &o) {
-  const int64_t nq = P.nq, ng = P.nghost, n = P.ncell;
-  o.mu = o.mut = o.f1 = T(0);
+__device__ __forceinline__ void LoadNbrCell(const Pools<T> &P, int32_t nb, Nbr<T> &o) {
+  const int64_t nq = P.nq, n = P.ncell;
+  o.mu = o.mut = o.f1 = o.nut = T(0);
   o.dut[0] = o.dut[1] = T(0);
-  int64_t cq;  // q index of the cell whose turbulence data applies
   if (nb >= 0) {
     o.s.rho = P.Wq[nb];
     o.s.u = P.Wq[nq + nb];
     o.s.v = P.Wq[2 * nq + nb];
     o.s.w = P.Wq[3 * nq + nb];
     o.s.p = P.Wq[4 * nq + nb];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) o.du[v] = P.dUq[v * nq + nb];
-    if (sv.viscous) o.mu = P.muq[nb];
-    if (sv.rans) {
-      o.dut[0] = P.dUtq[nb];
-      o.dut[1] = P.dUtq[nq + nb];
-    }
-    cq = nb;
     o.has_pre = P.Npre != nullptr;
     if (o.has_pre) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) o.pre.c[v] = P.Npre[v * nq + nb];
       o.pre.h = P.Npre[5 * nq + nb];
       o.pre.sos = P.Npre[6 * nq + nb];
-      if (sv.viscous) {
-        o.pre.vmax = P.Npre[7 * nq + nb];
-        o.pre.vt2 = P.Npre[8 * nq + nb];
-      }
     }
+    o.vq = nb;
   } else {
     o.has_pre = false;
     const int64_t slot = -(int64_t)nb - 2;
     o.s = LoadW<T>(P.W, n, P.ghost_cell[slot]);
+    o.vq = P.ghost_src[slot];
+  }
+}
+// ... its flow update (a connection ghost's: the partner cell's)
+template <typename T>
+__device__ __forceinline__ void LoadNbrDu(const Pools<T> &P, int32_t nb, Nbr<T> &o) {
+  if (nb >= 0) {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) o.du[v] = P.dUg[v * ng + slot];
+    for (int v = 0; v < 5; ++v) o.du[v] = P.dUq[v * P.nq + nb];
+  } else {
+    const int64_t slot = -(int64_t)nb - 2;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) o.du[v] = P.dUg[v * P.nghost + slot];
+  }
+}
+// ... and the part that depends on the solve's equations: laminar
+// viscosity and the precomputed viscous terms (viscous solves), the
+// turbulence update, eddy viscosity, F1 and rho k / omega (RANS solves)
+template <typename T>
+__device__ __forceinline__ void LoadNbrSolve(const Pools<T> &P, const SolveDev &sv, int32_t nb,
+                                             Nbr<T> &o) {
+  const int64_t nq = P.nq, ng = P.nghost;
+  if (nb >= 0) {
+    if (sv.viscous) o.mu = P.muq[nb];
+    if (sv.rans) {
+      o.dut[0] = P.dUtq[nb];
+      o.dut[1] = P.dUtq[nq + nb];
+    }
+    if (o.has_pre && sv.viscous) {
+      o.pre.vmax = P.Npre[7 * nq + nb];
+      o.pre.vt2 = P.Npre[8 * nq + nb];
+    }
+  } else {
+    const int64_t slot = -(int64_t)nb - 2;
     if (sv.viscous) o.mu = (T)P.mu[P.ghost_cell[slot]];
     if (sv.rans) {
       o.dut[0] = P.dUtg[slot];
       o.dut[1] = P.dUtg[ng + slot];
     }
-    cq = P.ghost_src[slot];
   }
-  o.nut = T(0);
   if (sv.rans) {
-    o.mut = P.mutq[cq];
-    o.f1 = P.f1q[cq];
-    if (sv.wilcox) o.nut = P.nutq[cq];
+    o.mut = P.mutq[o.vq];
+    o.f1 = P.f1q[o.vq];
+    if (sv.wilcox) o.nut = P.nutq[o.vq];
   }
-  o.vq = cq;
+}
+template <typename T>
+__device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, int32_t nb,
+                                        Nbr<T> &o) {
+  LoadNbrCell(P, nb, o);
+  LoadNbrDu(P, nb, o);
+  LoadNbrSolve(P, sv, nb, o);
 }
 
 // Off-diagonal sum of one cell: lower neighbours with the "positive" sign
@@ -1469,31 +1498,28 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
 
 // The term of one neighbour (face d) of OffDiagSum, for the grouped sweep
 // that gives each neighbour its own lane: r (flow) and rt (turbulence) as
-// OffDiagSum adds them; false where the cell has no neighbour (nb == -1)
+// OffDiagSum adds them, from the neighbour's loaded data o and the face's
+// normal (fx, fy, fz) and area mag
 template <typename T>
-__device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, const SolveDev &sv,
-                                        int64_t q, bool lower, int d, T r[5], T rt[2]) {
+__device__ __forceinline__ void NbrTermFrom(const Pools<T> &P, const Gas<T> &g,
+                                            const SolveDev &sv, int64_t q, bool lower, int d,
+                                            const Nbr<T> &o, T fx, T fy, T fz, T mag, T r[5],
+                                            T rt[2]) {
   const int64_t nq = P.nq;
-  const int32_t nb = P.nbq[(lower ? 0 : 3 * nq) + d * nq + q];
-  if (nb == -1) return false;
-  Nbr<T> o;
-  LoadNbr(P, sv, nb, o);
-  const T *f = (lower ? P.face_lo : P.face_hi) + (int64_t)d * 4 * nq;
   const T *dist = lower ? P.dist_lo : P.dist_hi;
-  const T mag = f[3 * nq + q];
   const T vsr = !sv.viscous ? T(0)
                 : o.has_pre ? mag / dist[d * nq + q] * o.pre.vmax * o.pre.vt2
                             : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
                                   ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
   if (o.has_pre && P.fast_fp64)
-    ScalarOffDiagPreFast(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+    ScalarOffDiagPreFast(o.s, o.pre, o.du, g, fx, fy, fz, mag, lower, vsr, r);
   else if (o.has_pre)
-    ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+    ScalarOffDiagPre(o.s, o.pre, o.du, g, fx, fy, fz, mag, lower, vsr, r);
   else
-    ScalarOffDiag(o.s, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
+    ScalarOffDiag(o.s, o.du, g, fx, fy, fz, mag, lower, vsr, r);
   rt[0] = rt[1] = T(0);
   if (sv.rans) {
-    const T vn = Dot(o.s.u, o.s.v, o.s.w, f[q], f[nq + q], f[2 * nq + q]);
+    const T vn = Dot(o.s.u, o.s.v, o.s.w, fx, fy, fz);
     T sr = lower ? T(0.5) * mag * fabs(vn + fabs(vn)) : T(0.5) * mag * fabs(vn - fabs(vn));
     if (sv.viscous) {
       const T length = mag / dist[d * nq + q];
@@ -1503,7 +1529,6 @@ __device__ __forceinline__ bool NbrTerm(const Pools<T> &P, const Gas<T> &g, cons
 #pragma unroll
     for (int k = 0; k < 2; ++k) rt[k] = lower ? o.dut[k] * sr : -(o.dut[k] * sr);
   }
-  return true;
 }
 
 // Off-diagonal Jacobians of one neighbour of a block solve's cell
@@ -1660,7 +1685,7 @@ __device__ __forceinline__ void ScalarFinish(const Pools<T> &P, const SolveDev &
                                              const T othert[2]) {
   const int64_t nq = P.nq;
   const T ainv = P.Ainvq[q];
-  const T thetaInv = (T)(1.0 / sv.theta);
+  const T thetaInv = (T)sv.theta_inv;
   if constexpr (FULL) {
     if (both) {
 #pragma unroll
@@ -1748,26 +1773,42 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
 // Scalar pass with a group of lanes per cell: lane d (0-2) evaluates the
 // term of neighbour d of the pass's triangle and, when both triangles
 // enter (FULL sweeps after the first, or several sweeps), lane 3 + d that
-// of the opposite one; the group's first lane sums the terms in i, j, k
-// order from zero and updates the cell -- SweepScalarQ's arithmetic, with
-// the three (six) independent neighbour terms in parallel, so a plane
-// keeps three (six) times as many warps busy: the faster form where a
-// plane has too few cells to fill the SMs (the autotuner chooses).  A warp
-// holds 10 (5) groups; its last 2 lanes idle.  Every lane of the warp
-// reaches the shuffles.
-// One scalar-solve cell per group of lanes (3, or 6 with both triangles),
-// a lane per neighbour term, the group's first lane summing the terms by
-// warp shuffles in the reference's i, j, k order.  Every lane of the warp
-// calls it (the shuffles span the warp); c is the cell's position in
-// items, valid for c < n_items.
+// of the opposite one -- SweepScalarQ's arithmetic with the three (six)
+// independent neighbour terms in parallel, so a plane keeps three (six)
+// times as many warps busy: the faster form where a plane has too few
+// cells to fill the SMs (the autotuner chooses).  A warp holds 10 (5)
+// groups; its last 2 lanes idle.
+//
+// The group's lanes then share the cell's equations: lane li finishes
+// equations e = li + L m (flow 0-4, then k and omega).  In rotation j of
+// a round m every lane sends the term its lane (li - j) mod L needs and
+// receives from lane (li + j) mod L, so the L shuffles of a round move a
+// different term to every lane; each lane then sums its equations' terms
+// from zero in the reference's i, j, k order (a neighbour the cell lacks
+// gives +0, which leaves the sum's bits as skipping it does) and updates
+// them.  The neighbour's index, state and update and the face geometry
+// depend on the cell alone and are requested before the solve's flags.
+// Every lane of the warp calls it (the shuffles span the warp); c is the
+// cell's position in items, valid for c < n_items.
 template <typename T, bool FULL, bool TURB = true>
 __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *items, int c,
                                                int n_items, int forward, int sweep) {
   constexpr int L = FULL ? 6 : 3, CPW = 32 / L;
+  constexpr int NE = TURB ? 7 : 5;         // equations of a cell
+  constexpr int M = (NE + L - 1) / L;      // equations per lane
   const int lane = (int)(threadIdx.x & 31);
   const int li = lane % L;
-  bool valid = lane < CPW * L && c < n_items;
+  const bool grouped = lane < CPW * L;
+  bool valid = grouped && c < n_items;
   const int2 it = valid ? items[c] : make_int2(0, 0);
+  const int64_t nq = P.nq, q = it.x;
+  const int side = li / 3, d = li % 3;
+  const bool lower = side == 0 ? forward != 0 : forward == 0;
+  const int32_t nb = P.nbq[(lower ? 0 : 3 * nq) + d * nq + q];
+  Nbr<T> o;
+  if (nb != -1) LoadNbrCell(P, nb, o);
+  const T *f = (lower ? P.face_lo : P.face_hi) + (int64_t)d * 4 * nq;
+  const T fx = f[q], fy = f[nq + q], fz = f[2 * nq + q], mag = f[3 * nq + q];
   SolveDev sv = P.solves[P.blocks[it.y].solve];
   if constexpr (!TURB) {
     sv.rans = 0;
@@ -1779,41 +1820,72 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
     valid = valid && sweep < sv.sweeps;
     both = sweep > 0 || sv.sweeps > 1;
   }
-  const int side = li / 3, d = li % 3;
-  const bool lower = side == 0 ? forward != 0 : forward == 0;
   const Gas<T> g = GasOf<T>(sv);
-  T r[5] = {T(0), T(0), T(0), T(0), T(0)}, rt[2] = {T(0), T(0)};
-  int have = 0;
-  if (valid && (side == 0 || both)) have = NbrTerm(P, g, sv, it.x, lower, d, r, rt);
-  const int g0 = lane < CPW * L ? lane - li : lane;
-  T acc[5], acct[2], other[5], othert[2];
+  // the previous plane's updates are read from here on: with a programmatic
+  // launch after that plane's kernel, wait for it (a no-op otherwise), and
+  // let the next plane's kernel start its own loads of this kind
+  GridDependencyWait();
+  GridDependentsLaunch();
+  T r[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+  if (valid && (side == 0 || both) && nb != -1) {
+    LoadNbrDu(P, nb, o);
+    LoadNbrSolve(P, sv, nb, o);
+    NbrTermFrom(P, g, sv, q, lower, d, o, fx, fy, fz, mag, r, r + 5);
+  }
+  const int gbase = lane - li;
+  T xs[M][L];
 #pragma unroll
-  for (int s2 = 0; s2 < (FULL ? 2 : 1); ++s2) {
-    T *a = s2 == 0 ? acc : other, *at = s2 == 0 ? acct : othert;
+  for (int m = 0; m < M; ++m) {
 #pragma unroll
-    for (int v = 0; v < 5; ++v) a[v] = T(0);
-    at[0] = at[1] = T(0);
+    for (int j = 0; j < L; ++j) {
+      const int e = (li - j + L) % L + L * m;  // equation the receiving lane finishes
+      T send = T(0);
 #pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-      const int src = g0 + 3 * s2 + dd;
-      const int h = __shfl_sync(0xffffffffu, have, src);
-      T x[5], xt[2];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) x[v] = __shfl_sync(0xffffffffu, r[v], src);
-#pragma unroll
-      for (int k = 0; k < 2; ++k) xt[k] = __shfl_sync(0xffffffffu, rt[k], src);
-      if (h) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) a[v] = a[v] + x[v];
-        if (sv.rans) {
-#pragma unroll
-          for (int k = 0; k < 2; ++k) at[k] = at[k] + xt[k];
-        }
-      }
+      for (int ee = 0; ee < NE; ++ee)
+        if (ee == e) send = r[ee];
+      const int src = grouped ? gbase + (li + j) % L : lane;
+      xs[m][j] = __shfl_sync(0xffffffffu, send, src);
     }
   }
-  if (!valid || li != 0) return;
-  ScalarFinish<T, FULL>(P, sv, it.x, forward, both, acc, acct, other, othert);
+  if (!valid) return;
+  const T thetaInv = (T)sv.theta_inv;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int e = li + L * m;
+    if (e >= NE || (e >= 5 && !sv.rans)) continue;
+    // the term of group lane k arrived in rotation (k - li) mod L
+    T t[L];
+#pragma unroll
+    for (int k = 0; k < L; ++k) {
+      const int jk = (k - li + L) % L;
+      t[k] = xs[m][0];
+#pragma unroll
+      for (int j = 1; j < L; ++j)
+        if (j == jk) t[k] = xs[m][j];
+    }
+    T acc = T(0), other = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc = acc + t[k];
+    if constexpr (FULL) {
+#pragma unroll
+      for (int k = 3; k < L; ++k) other = other + t[k];
+    }
+    const bool turb = e >= 5;
+    const int64_t at = turb ? (int64_t)(e - 5) * nq + q : (int64_t)e * nq + q;
+    T *x = turb ? P.dUtq : P.dUq;
+    const T ainv = turb ? P.Ainvtq[q] : P.Ainvq[q];
+    if (FULL && both) {
+      const T bv = RhsB(P, sv, thetaInv, e, q);
+      const T in = forward ? bv + (acc - other) : (bv + other) - acc;
+      x[at] = in * ainv;
+    } else if (forward) {
+      const T bv = RhsB(P, sv, thetaInv, e, q);
+      x[at] = (bv + acc) * ainv;
+    } else {
+      const T xold = x[at];
+      x[at] = xold - acc * ainv;
+    }
+  }
 }
 
 template <typename T, bool FULL, int MINB, bool TURB>
@@ -1823,6 +1895,33 @@ __global__ void __launch_bounds__(256, MINB) k_sweepg(Pools<T> P, const int2 *it
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = (int)(threadIdx.x & 31);
   SweepGroupItem<T, FULL, TURB>(P, items, (t >> 5) * CPW + lane / L, n_items, forward, sweep);
+}
+
+// One hyperplane of the grouped scalar sweep over n items with CTAs of
+// `threads`; chained launches carry the programmatic-serialization
+// attribute (k_sweepg waits for the previous plane before reading its
+// updates)
+template <typename T>
+void LaunchSweepGroup(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
+                      bool full, int threads, bool chained, cudaStream_t s) {
+  const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
+  const unsigned grid = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
+  const bool turb = (P.fkinds & 2) != 0;
+  void (*kern)(Pools<T>, const int2 *, int, int, int) =
+      full ? (turb ? k_sweepg<T, true, 1, true> : k_sweepg<T, true, 1, false>)
+           : (turb ? k_sweepg<T, false, 1, true> : k_sweepg<T, false, 1, false>);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = chained ? 1 : 0;
+  // a failed launch leaves its error for the caller's cudaGetLastError
+  (void)cudaLaunchKernelEx(&cfg, kern, P, items, n, forward, sweep);
 }
 
 // Loads of one row of a block sweep that depend on the cell alone: the
@@ -1941,7 +2040,7 @@ __device__ __forceinline__ void SweepBlockRow(const Pools<T> &P, const SolveDev 
     }
   }
   const bool full = sweep > 0 || sv.sweeps > 1;
-  const T thetaInv = (T)(1.0 / sv.theta);
+  const T thetaInv = (T)sv.theta_inv;
   const bool mine = valid && (row < 5 || (turb && sv.rans));
   T in = T(0);
   if (mine) {
@@ -2133,7 +2232,7 @@ __global__ void __launch_bounds__(128) k_init(Pools<T> P, const int2 *items, int
 #pragma unroll
     for (int v = 0; v < 5; ++v) x[v] = T(0);
   } else {
-    const T thetaInv = (T)(1.0 / sv.theta);
+    const T thetaInv = (T)sv.theta_inv;
     T in[5], int_[2];
 #pragma unroll
     for (int v = 0; v < 5; ++v) in[v] = RhsB(P, sv, thetaInv, v, q);
@@ -2191,7 +2290,7 @@ __global__ void __launch_bounds__(128) k_jacobi(Pools<T> P, T *dst, T *dstt, con
     }
     return;
   }
-  const T thetaInv = (T)(1.0 / sv.theta);
+  const T thetaInv = (T)sv.theta_inv;
   T L[5], U[5], Lt[2], Ut[2], in[5], x[5];
   if constexpr (BLOCK) {
     OffDiagSumBlock(P, sv, q, true, L, Lt);
@@ -2421,12 +2520,18 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
       }
     }
   }
-  // warp reduction; the sum order is fixed, so results are reproducible
+  // warp reduction over the solve's equations (the CTA lies in one block,
+  // so the turbulence rows are uniform over it; without them their sums
+  // stay zero); the sum order is fixed, so results are reproducible
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
 #pragma unroll
-    for (int v = 0; v < kNvMax; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    for (int v = 0; v < kNv; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    if (sv.rans) {
+#pragma unroll
+      for (int v = kNv; v < kNvMax; ++v) l2[v] += __shfl_down_sync(0xffffffffu, l2[v], off);
+    }
     const double om = __shfl_down_sync(0xffffffffu, mx, off);
     const int64_t op = __shfl_down_sync(0xffffffffu, mpos, off);
     if (om > mx || (om == mx && op < mpos)) {
@@ -2443,14 +2548,21 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     s_bad[warp] = bad;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (warp != 0) return;
+  // lane v of the first warp sums equation v over the warps in warp order
+  double sum = 0.0;
+  if (lane < (sv.rans ? kNvMax : kNv))
+    for (int w = 0; w < kCta / 32; ++w) sum += s_l2[w][lane];
+  double l2s[kNvMax];
+#pragma unroll
+  for (int v = 0; v < kNvMax; ++v) l2s[v] = __shfl_sync(0xffffffffu, sum, v);
+  if (lane == 0) {
     NormPartial p;
-    for (int v = 0; v < kNvMax; ++v) p.l2[v] = 0.0;
+    for (int v = 0; v < kNvMax; ++v) p.l2[v] = l2s[v];
     p.linf = 0.0;
     p.linf_pos = INT64_MAX;
     p.bad = 0;
     for (int w = 0; w < kCta / 32; ++w) {
-      for (int v = 0; v < kNvMax; ++v) p.l2[v] += s_l2[w][v];
       if (s_max[w] > p.linf || (s_max[w] == p.linf && s_pos[w] < p.linf_pos)) {
         p.linf = s_max[w];
         p.linf_pos = s_pos[w];
@@ -3244,7 +3356,7 @@ __global__ void __launch_bounds__(kCta) k_matres(Pools<T> P, const int32_t *list
         Ax[6] = x[6] * at;
       }
     }
-    const T thetaInv = (T)(1.0 / sv.theta);
+    const T thetaInv = (T)sv.theta_inv;
 #pragma unroll
     for (int v = 0; v < 7; ++v) {
       if (v >= nv) break;
@@ -3475,24 +3587,19 @@ void Launch<T>::Cell(const Pools<T> &P, const int32_t *list, const int32_t *cta_
 }
 template <typename T>
 void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
-                      bool full, int kinds, int threads, bool group, cudaStream_t s) {
+                      bool full, int kinds, int threads, bool group, bool chained,
+                      cudaStream_t s) {
   if (n <= 0) return;
   bool fast = false;
   if constexpr (std::is_same<T, double>::value) {
     if (P.fast_fp64 && (kinds & 1)) {
-      LaunchFastSweepFp64(P, items, n, forward, sweep, full, threads, group, s);
+      LaunchFastSweepFp64(P, items, n, forward, sweep, full, threads, group, chained, s);
       fast = true;
     }
   }
   if (fast) {
   } else if ((kinds & 1) && group) {
-    const int cpw = full ? 32 / 6 : 32 / 3;  // cells per warp
-    const unsigned gridg = (unsigned)(((int64_t)(n + cpw - 1) / cpw * 32 + threads - 1) / threads);
-    const bool turb = (P.fkinds & 2) != 0;
-    if (full && turb) k_sweepg<T, true, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (full) k_sweepg<T, true, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (turb) k_sweepg<T, false, 1, true><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweepg<T, false, 1, false><<<gridg, threads, 0, s>>>(P, items, n, forward, sweep);
+    LaunchSweepGroup<T>(P, items, n, forward, sweep, full, threads, chained, s);
   } else if (kinds & 1) {
     const unsigned grid = (unsigned)((n + threads - 1) / threads);
     const bool turb = (P.fkinds & 2) != 0;

@@ -224,6 +224,7 @@ extern "C" int ath_block_residual_noalloc(const ath_block_dev *blk,
     sv.limiter = phys->limiter;
     sv.recon = ATH_RECON_MUSCL;
     sv.flux = ATH_FLUX_ROE;
+    ath::SetDerived(sv);
     const int64_t nf[3] = {(int64_t)(blk->ni + 1) * blk->nj * blk->nk,
                            (int64_t)blk->ni * (blk->nj + 1) * blk->nk,
                            (int64_t)blk->ni * blk->nj * (blk->nk + 1)};

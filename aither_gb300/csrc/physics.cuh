@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 namespace ath {
 
 template <typename T>
@@ -24,7 +26,7 @@ struct Gas {
   // Set() with the reference's expressions: cv = R n, cp = R (n + 1),
   // gamma = cp / cv
   T cv, cp, gam;
-  __device__ __forceinline__ void Set(T r_, T n_, T hf_) {
+  __host__ __device__ __forceinline__ void Set(T r_, T n_, T hf_) {
     r = r_;
     n = n_;
     hf = hf_;
@@ -223,8 +225,11 @@ __device__ __forceinline__ Prim<T> Muscl(const Prim<T> &up2, const Prim<T> &up1,
 // up2) dminus, y = (dw1 - up1) dplus.  For minmod phi(r) = r phi(1/r) =
 // min(max(r, 0), 1): both limiter terms are equal, kappa cancels, and the
 // increment is x / 2 when r >= 1, y / 2 when 0 < r < 1 (to within eps =
-// 1e-30) and 0 otherwise -- no division.  van Albada takes one quotient
-// q = (r + 1) / (r^2 + 1) for both phi(r) = r q and phi(1/r) = q.
+// 1e-30) and 0 otherwise -- no division.  In FP64 the tests r > 0 (A =
+// eps + x and B = eps + y nonzero with one sign) and |B| < |A| read the
+// bit patterns on the integer pipe: for IEEE doubles the sign is the top
+// bit and magnitudes order as the remaining bits do.  van Albada takes one
+// quotient q = (r + 1) / (r^2 + 1) for both phi(r) = r q and phi(1/r) = q.
 template <typename T>
 __device__ __forceinline__ T MusclFast1(T up2, T up1, T dw1, T dplus, T dminus, T kappa,
                                         int limiter) {
@@ -232,8 +237,15 @@ __device__ __forceinline__ T MusclFast1(T up2, T up1, T dw1, T dplus, T dminus, 
   const T x = (up1 - up2) * dminus, y = (dw1 - up1) * dplus;
   if (limiter == 1) {
     const T A = eps + x, B = eps + y;
-    if (!(A * B > T(0))) return up1;
-    return up1 + T(0.5) * (fabs(B) < fabs(A) ? y : x);
+    if constexpr (std::is_same<T, double>::value) {
+      const long long ia = __double_as_longlong(A), ib = __double_as_longlong(B);
+      const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+      if ((ia ^ ib) < 0 || ma == 0 || mb == 0) return up1;
+      return up1 + T(0.5) * (mb < ma ? y : x);
+    } else {
+      if (!(A * B > T(0))) return up1;
+      return up1 + T(0.5) * (fabs(B) < fabs(A) ? y : x);
+    }
   }
   const T r = (eps + y) / (eps + x);
   T lim = T(1), rilim = r;
@@ -246,10 +258,8 @@ __device__ __forceinline__ T MusclFast1(T up2, T up1, T dw1, T dplus, T dminus, 
 }
 template <typename T>
 __device__ __forceinline__ Prim<T> MusclFast(const Prim<T> &up2, const Prim<T> &up1,
-                                             const Prim<T> &dw1, T uw2, T uw, T dw, T kappa,
+                                             const Prim<T> &dw1, T dplus, T dminus, T kappa,
                                              int limiter) {
-  const T dplus = (uw + uw) / (uw + dw);
-  const T dminus = (uw + uw) / (uw + uw2);
   Prim<T> o;
   o.rho = MusclFast1(up2.rho, up1.rho, dw1.rho, dplus, dminus, kappa, limiter);
   o.u = MusclFast1(up2.u, up1.u, dw1.u, dplus, dminus, kappa, limiter);
@@ -257,6 +267,24 @@ __device__ __forceinline__ Prim<T> MusclFast(const Prim<T> &up2, const Prim<T> &
   o.w = MusclFast1(up2.w, up1.w, dw1.w, dplus, dminus, kappa, limiter);
   o.p = MusclFast1(up2.p, up1.p, dw1.p, dplus, dminus, kappa, limiter);
   return o;
+}
+// The width ratios of both sides of the face between cells m1 and 0 (cell
+// widths xm2, xm1 | x0, xp1 along the face normal): lower side dplus =
+// 2 xm1 / (xm1 + x0), dminus = 2 xm1 / (xm1 + xm2); upper side dplus =
+// 2 x0 / (x0 + xm1), dminus = 2 x0 / (x0 + xp1) -- with one reciprocal of
+// the product of the three sums in place of four divisions
+template <typename T>
+__device__ __forceinline__ void MusclFastRatios(T xm2, T xm1, T x0, T xp1, T &dpL, T &dmL,
+                                                T &dpR, T &dmR) {
+  const T a = xm1 + x0, b = xm1 + xm2, c = x0 + xp1;
+  const T ab = a * b;
+  const T r = T(1) / (ab * c);
+  const T ia = (b * c) * r, ib = (a * c) * r, ic = ab * r;
+  const T tm1 = xm1 + xm1, t0 = x0 + x0;
+  dpL = tm1 * ia;
+  dmL = tm1 * ib;
+  dpR = t0 * ia;
+  dmR = t0 * ic;
 }
 
 // RoeFlux with Harten's entropy fix (include/inviscidFlux.hpp:260-382,
@@ -364,26 +392,33 @@ __device__ __forceinline__ void InvFluxCentral(const Prim<double> &s, const Gas<
   f[4] = vn * rhoH;
 }
 
-// Roe flux of RoeFlux in the fast form: one reciprocal of 1 + sqrt(rhoR /
-// rhoL) for the Roe averages, p / rho of the Roe state formed once for its
-// enthalpy (hf + (n + 1) p / rho + |v|^2 / 2, as cp T = (n + 1) p / rho for
-// the calorically perfect gas) and sound speed, one reciprocal of a^2 for
-// the wave strengths, and the division-free central flux.
+// Roe flux of RoeFlux in the fast form: one reciprocal square root of
+// rhoL rhoR gives the density ratio sqrt(rhoR / rhoL) and the reciprocal of
+// the Roe density; one reciprocal of 1 + sqrt(rhoR / rhoL) for the Roe
+// averages; p / rho of the Roe state formed once for its enthalpy (hf +
+// (n + 1) p / rho + |v|^2 / 2, as cp T = (n + 1) p / rho for the
+// calorically perfect gas) and sound speed; one reciprocal square root of
+// a^2 gives a and 1 / a^2; and the division-free central flux.
 __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<double> &R,
                                             const Gas<double> &g, double nx, double ny,
                                             double nz, double f[5]) {
   const double dRho = R.rho - L.rho, dU = R.u - L.u, dV = R.v - L.v, dW = R.w - L.w,
                dP = R.p - L.p;
-  const double denRatio = sqrt(R.rho / L.rho);
+  // t = 1 / sqrt(rhoL rhoR): sqrt(rhoR / rhoL) = rhoR t, and t is the
+  // reciprocal of the Roe density sqrt(rhoL rhoR)
+  const double t = rsqrt(R.rho * L.rho);
+  const double denRatio = R.rho * t;
   const double inv = 1.0 / (1.0 + denRatio);
   const double ru = (L.u + denRatio * R.u) * inv, rv = (L.v + denRatio * R.v) * inv,
                rw = (L.w + denRatio * R.w) * inv, rp = (L.p + denRatio * R.p) * inv;
   const double rhoR = L.rho * denRatio;
-  const double por = rp / rhoR;
+  const double por = rp * t;
   const double hR = (g.hf + (g.n + 1.0) * por) + 0.5 * (ru * ru + rv * rv + rw * rw);
   const double a2 = g.gam * por;
-  const double aR = sqrt(a2);
-  const double ia2 = 1.0 / a2;
+  // s = 1 / a: a = a^2 s, 1 / a^2 = s^2
+  const double sa = rsqrt(a2);
+  const double aR = a2 * sa;
+  const double ia2 = sa * sa;
   const double velNormR = ru * nx + rv * ny + rw * nz;
   const double normVelDiff = dU * nx + dV * ny + dW * nz;
   const double entropyFix = 0.1;
