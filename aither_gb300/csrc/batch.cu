@@ -560,6 +560,22 @@ class Runner : public RunnerBase {
     P_.states = c.d_states;
     P_.cfl = c.d_cfl;
     if (c.L.any_viscous) InitialViscosity(m);
+    if constexpr (std::is_same<T, double>::value) {
+      if (P_.fast_fp64) {
+        // the fast option's geometry tables, formed once
+        for (int d = 0; d < 3; ++d) {
+          P_.fgeo[d] = m.Alloc<double>(4 * n);
+          P_.cgeo[d] = m.Alloc<double>(4 * n);
+          c_.mem->Zero(P_.fgeo[d], 0, 4 * n * sizeof(double));
+          c_.mem->Zero(P_.cgeo[d], 0, 4 * n * sizeof(double));
+        }
+        const int nfc[3] = {(int)c.L.face_cta_block[0].size(), (int)c.L.face_cta_block[1].size(),
+                            (int)c.L.face_cta_block[2].size()};
+        LaunchFastGeomFp64(P_, c.d_faces, c.d_face_cta_block, nfc, c.d_cells,
+                           c.d_cell_cta_block, (int)c.L.cell_cta_block.size(), c_.stream);
+        Check(cudaGetLastError(), "kernel launch");
+      }
+    }
   }
 
   ~Runner() override {

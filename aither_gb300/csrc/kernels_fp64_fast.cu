@@ -47,6 +47,54 @@ void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int f
   }
 }
 
+template <int D>
+__global__ void __launch_bounds__(kCta) k_fast_fgeo(Pools<double> P, const int32_t *list,
+                                                    const int32_t *cta_block) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const int64_t n = P.ncell, s = StrideOf(b, D);
+  const double *wd = P.width[D];
+  double dpL, dmL, dpR, dmR;
+  MusclFastRatios(wd[c - 2 * s], wd[c - s], wd[c], wd[c + s], dpL, dmL, dpR, dmR);
+  double *g = P.fgeo[D];
+  g[c] = dpL;
+  g[n + c] = dmL;
+  g[2 * n + c] = dpR;
+  g[3 * n + c] = dmR;
+}
+
+__global__ void __launch_bounds__(kCta) k_fast_cgeo(Pools<double> P, const int32_t *list,
+                                                    const int32_t *cta_block) {
+  const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
+  if (c < 0) return;
+  const BlockDev b = P.blocks[cta_block[blockIdx.x]];
+  const int64_t n = P.ncell;
+  const int64_t st[3] = {1, (int64_t)b.NI, (int64_t)b.NI * b.NJ};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double *fa = P.fa[d];
+    const int64_t u = c + st[d];
+    const double ax = fa[c] + fa[u], ay = fa[n + c] + fa[n + u], az = fa[2 * n + c] + fa[2 * n + u];
+    const double rs = rsqrt(Dot(ax, ay, az, ax, ay, az));
+    double *g = P.cgeo[d];
+    g[c] = ax * rs;
+    g[n + c] = ay * rs;
+    g[2 * n + c] = az * rs;
+    g[3 * n + c] = 0.5 * (fa[3 * n + c] + fa[3 * n + u]);
+  }
+}
+
+void LaunchFastGeomFp64(const Pools<double> &P, const int32_t *const faces[3],
+                        const int32_t *const face_cta_block[3], const int nface_cta[3],
+                        const int32_t *cells, const int32_t *cell_cta_block, int ncell_cta,
+                        cudaStream_t s) {
+  if (nface_cta[0] > 0) k_fast_fgeo<0><<<nface_cta[0], kCta, 0, s>>>(P, faces[0], face_cta_block[0]);
+  if (nface_cta[1] > 0) k_fast_fgeo<1><<<nface_cta[1], kCta, 0, s>>>(P, faces[1], face_cta_block[1]);
+  if (nface_cta[2] > 0) k_fast_fgeo<2><<<nface_cta[2], kCta, 0, s>>>(P, faces[2], face_cta_block[2]);
+  if (ncell_cta > 0) k_fast_cgeo<<<ncell_cta, kCta, 0, s>>>(P, cells, cell_cta_block);
+}
+
 void LaunchFastUpdateFp64(const Pools<double> &P, const int32_t *list, const int32_t *cta_block,
                           const int32_t *cta_pos0, NormPartial *partials, int ncta,
                           const SolveState *ss, cudaStream_t s) {

@@ -619,14 +619,14 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
   } else if (sv.recon == ATH_RECON_MUSCL) {
     const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s);
     const Prim<U> wp1 = LoadW<U>(P.W, n, c + s);
-    const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
     const U kappa = (U)sv.kappa;
     if constexpr (FAST) {
-      U dpL, dmL, dpR, dmR;
-      MusclFastRatios(xm2, xm1, x0, xp1, dpL, dmL, dpR, dmR);
-      L = MusclFast(wm2, wm1, w0, dpL, dmL, kappa, sv.limiter);
-      R = MusclFast(wp1, w0, wm1, dpR, dmR, kappa, sv.limiter);
+      // the width ratios formed once from the geometry (Pools::fgeo)
+      const double *fg = P.fgeo[D];
+      const U dpL = (U)fg[c], dmL = (U)fg[n + c], dpR = (U)fg[2 * n + c], dmR = (U)fg[3 * n + c];
+      MusclFastPair(wm2, wm1, w0, wp1, dpL, dmL, dpR, dmR, kappa, sv.limiter, L, R);
     } else {
+      const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
       // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
       L = Muscl(wm2, wm1, w0, xm2, xm1, x0, kappa, sv.limiter);
       // upper side: upwind2 = c+1, upwind1 = c, downwind = c-1
@@ -1019,20 +1019,21 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
   // scalar main diagonal: accumulates like the radius, from zero or (a
   // multigrid level visited again in this iteration) from its previous value
   double adiag = (!BLOCK && P.mg_accum) ? (double)P.Aq[q] : 0.0;
-  // fast FP64 option: the sound speed once per cell, the averaged face
-  // normal's length by one reciprocal square root per direction
+  // fast FP64 option: p / rho and the sound speed once per cell (p / rho
+  // also for the enthalpy), the radius's geometry from Pools::cgeo
   const bool fastc = std::is_same<T, double>::value && P.fast_fp64;
-  const T sosc = fastc ? SoS(w, g) : T(0);
+  const T porc = fastc ? w.p / w.rho : T(0);
+  const T sosc = fastc ? sqrt(g.Gamma() * porc) : T(0);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double *fa = P.fa[d];
     const int64_t u = c + st[d];
     double lcd;
     if (fastc) {
-      const T ax = T(0.5) * ((T)fa[c] + (T)fa[u]), ay = T(0.5) * ((T)fa[n + c] + (T)fa[n + u]),
-              az = T(0.5) * ((T)fa[2 * n + c] + (T)fa[2 * n + u]);
-      const T vn = fabs(Dot(w.u, w.v, w.w, ax, ay, az)) * rsqrt(Dot(ax, ay, az, ax, ay, az));
-      lcd = (double)((vn + sosc) * (T(0.5) * ((T)fa[3 * n + c] + (T)fa[3 * n + u])));
+      // normalised normal and average area formed once (Pools::cgeo)
+      const double *cg = P.cgeo[d];
+      const T vn = fabs(Dot(w.u, w.v, w.w, (T)cg[c], (T)cg[n + c], (T)cg[2 * n + c]));
+      lcd = (double)((vn + sosc) * (T)cg[3 * n + c]);
     } else {
       lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
                                    (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u],
@@ -1302,7 +1303,7 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
       for (int v = 0; v < 5; ++v) P.Npre[v * nq + q] = cc[v];
       if (fastc) {
         // h = hf + cp T + |v|^2 / 2 with cp T = (n + 1) p / rho
-        P.Npre[5 * nq + q] = (gq.hf + (gq.n + T(1)) * (w.p / w.rho)) +
+        P.Npre[5 * nq + q] = (gq.hf + (gq.n + T(1)) * porc) +
                              T(0.5) * Dot(w.u, w.v, w.w, w.u, w.v, w.w);
         P.Npre[6 * nq + q] = sosc;
       } else {
@@ -1474,8 +1475,8 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
                                     ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
     T r[5];
     if (o.has_pre && P.fast_fp64)
-      ScalarOffDiagPreFast(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr,
-                           r);
+      ScalarOffDiagPreFast(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower,
+                           sv.viscous != 0, vsr, r);
     else if (o.has_pre)
       ScalarOffDiagPre(o.s, o.pre, o.du, g, f[q], f[nq + q], f[2 * nq + q], mag, lower, vsr, r);
     else
@@ -1512,7 +1513,7 @@ __device__ __forceinline__ void NbrTermFrom(const Pools<T> &P, const Gas<T> &g,
                             : mag / dist[d * nq + q] * ViscMaxTerm(o.s, g) *
                                   ViscTerm2(o.mu, o.mut, (T)sv.visc_scale, g, (T)PrtOf(sv));
   if (o.has_pre && P.fast_fp64)
-    ScalarOffDiagPreFast(o.s, o.pre, o.du, g, fx, fy, fz, mag, lower, vsr, r);
+    ScalarOffDiagPreFast(o.s, o.pre, o.du, g, fx, fy, fz, mag, lower, sv.viscous != 0, vsr, r);
   else if (o.has_pre)
     ScalarOffDiagPre(o.s, o.pre, o.du, g, fx, fy, fz, mag, lower, vsr, r);
   else
@@ -2460,9 +2461,11 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
 #pragma unroll
     for (int v = 0; v < 5; ++v) du[v] = (double)P.dUq[v * P.nq + q];
     Prim<double> u;
-    if (P.fast_fp64) {
-      // fast FP64 option: rho E = rho hf + n p + rho |v|^2 / 2 (cv T rho = n p),
-      // then the updated state with one reciprocal of the density
+    if (P.fast_fp64 || std::is_same<T, float>::value) {
+      // fast FP64 option, and mixed precision (whose results are roundoff-
+      // equal to FP64's by construction): rho E = rho hf + n p + rho |v|^2 / 2
+      // (cv T rho = n p), then the updated state with one reciprocal of the
+      // density
       const double rho1 = w.rho + du[0];
       const double c1 = w.rho * w.u + du[1], c2 = w.rho * w.v + du[2], c3 = w.rho * w.w + du[3];
       const double rE = (w.rho * g.hf + g.n * w.p +
@@ -2477,8 +2480,8 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     } else {
       u = UpdateWithCons(w, g, du);
     }
-    if (!(u.rho > 0.0) || !(u.p > 0.0) || !isfinite(u.u) || !isfinite(u.v) ||
-        !isfinite(u.w))
+    if (!PositiveBits(u.rho) || !PositiveBits(u.p) || !FiniteBits(u.u) || !FiniteBits(u.v) ||
+        !FiniteBits(u.w))
       bad = 1;
     P.W[c] = u.rho;
     P.W[n + c] = u.u;
@@ -2514,7 +2517,7 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
       // L-infinity follows the reference's signed comparison
       // (procBlock::UpdateBlock): a new maximum replaces the old one only
       // when strictly larger; ties keep the first in loop order
-      if (r > mx) {
+      if (GreaterNonNeg(r, mx)) {
         mx = r;
         mpos = pos0 * kNvMax + v;
       }
@@ -2534,7 +2537,8 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     }
     const double om = __shfl_down_sync(0xffffffffu, mx, off);
     const int64_t op = __shfl_down_sync(0xffffffffu, mpos, off);
-    if (om > mx || (om == mx && op < mpos)) {
+    // maxima are +0 or positive, so their bits order them
+    if (Bits(om) > Bits(mx) || (Bits(om) == Bits(mx) && op < mpos)) {
       mx = om;
       mpos = op;
     }
@@ -2563,7 +2567,8 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
     p.linf_pos = INT64_MAX;
     p.bad = 0;
     for (int w = 0; w < kCta / 32; ++w) {
-      if (s_max[w] > p.linf || (s_max[w] == p.linf && s_pos[w] < p.linf_pos)) {
+      if (Bits(s_max[w]) > Bits(p.linf) ||
+          (Bits(s_max[w]) == Bits(p.linf) && s_pos[w] < p.linf_pos)) {
         p.linf = s_max[w];
         p.linf_pos = s_pos[w];
       }

@@ -39,6 +39,25 @@ struct Gas {
   __device__ __forceinline__ T Gamma() const { return gam; }
 };
 
+// Tests of doubles on the integer pipe (FP64 comparisons issue on GB300's
+// narrow FP64 pipe).  An IEEE double's sign is its top bit, and
+// non-negative values order as their bit patterns do as signed integers.
+__device__ __forceinline__ long long Bits(double x) { return __double_as_longlong(x); }
+// x > 0 (x = +inf included, NaN not)
+__device__ __forceinline__ bool PositiveBits(double x) {
+  const long long b = Bits(x);
+  return b > 0 && b <= 0x7ff0000000000000LL;
+}
+// x neither infinite nor NaN
+__device__ __forceinline__ bool FiniteBits(double x) {
+  return (Bits(x) & 0x7fffffffffffffffLL) < 0x7ff0000000000000LL;
+}
+// x > m for m = +0 or positive and not NaN (x NaN: false)
+__device__ __forceinline__ bool GreaterNonNeg(double x, double m) {
+  const long long b = Bits(x);
+  return b > Bits(m) && b <= 0x7ff0000000000000LL;
+}
+
 template <typename T>
 struct Prim {
   T rho, u, v, w, p;
@@ -268,6 +287,52 @@ __device__ __forceinline__ Prim<T> MusclFast(const Prim<T> &up2, const Prim<T> &
   o.p = MusclFast1(up2.p, up1.p, dw1.p, dplus, dminus, kappa, limiter);
   return o;
 }
+// Both face states of the face between cells m1 and 0 in MusclFast's form
+// (lower side: upwind2 m2, upwind1 m1, downwind 0; upper side: upwind2 p1,
+// upwind1 0, downwind m1), the difference across the face formed once:
+// the upper side's y = (wm1 - w0) dplus is -(w0 - wm1) dplus exactly
+template <typename T>
+__device__ __forceinline__ void MusclFastPair1(T wm2, T wm1, T w0, T wp1, T dpL, T dmL, T dpR,
+                                               T dmR, T kappa, int limiter, T &l, T &r) {
+  if (limiter != 1) {
+    l = MusclFast1(wm2, wm1, w0, dpL, dmL, kappa, limiter);
+    r = MusclFast1(wp1, w0, wm1, dpR, dmR, kappa, limiter);
+    return;
+  }
+  const T eps = T(1.0e-30);
+  const T d0 = w0 - wm1;
+  const T xs[2] = {(wm1 - wm2) * dmL, (w0 - wp1) * dmR};
+  const T ys[2] = {d0 * dpL, (-d0) * dpR};
+  const T up[2] = {wm1, w0};
+  T o[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const T x = xs[k], y = ys[k];
+    const T A = eps + x, B = eps + y;
+    if constexpr (std::is_same<T, double>::value) {
+      const long long ia = __double_as_longlong(A), ib = __double_as_longlong(B);
+      const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+      o[k] = ((ia ^ ib) < 0 || ma == 0 || mb == 0) ? up[k]
+                                                     : up[k] + T(0.5) * (mb < ma ? y : x);
+    } else {
+      o[k] = !(A * B > T(0)) ? up[k] : up[k] + T(0.5) * (fabs(B) < fabs(A) ? y : x);
+    }
+  }
+  l = o[0];
+  r = o[1];
+}
+template <typename T>
+__device__ __forceinline__ void MusclFastPair(const Prim<T> &wm2, const Prim<T> &wm1,
+                                              const Prim<T> &w0, const Prim<T> &wp1, T dpL,
+                                              T dmL, T dpR, T dmR, T kappa, int limiter,
+                                              Prim<T> &L, Prim<T> &R) {
+  MusclFastPair1(wm2.rho, wm1.rho, w0.rho, wp1.rho, dpL, dmL, dpR, dmR, kappa, limiter, L.rho,
+                 R.rho);
+  MusclFastPair1(wm2.u, wm1.u, w0.u, wp1.u, dpL, dmL, dpR, dmR, kappa, limiter, L.u, R.u);
+  MusclFastPair1(wm2.v, wm1.v, w0.v, wp1.v, dpL, dmL, dpR, dmR, kappa, limiter, L.v, R.v);
+  MusclFastPair1(wm2.w, wm1.w, w0.w, wp1.w, dpL, dmL, dpR, dmR, kappa, limiter, L.w, R.w);
+  MusclFastPair1(wm2.p, wm1.p, w0.p, wp1.p, dpL, dmL, dpR, dmR, kappa, limiter, L.p, R.p);
+}
 // The width ratios of both sides of the face between cells m1 and 0 (cell
 // widths xm2, xm1 | x0, xp1 along the face normal): lower side dplus =
 // 2 xm1 / (xm1 + x0), dminus = 2 xm1 / (xm1 + xm2); upper side dplus =
@@ -398,7 +463,8 @@ __device__ __forceinline__ void InvFluxCentral(const Prim<double> &s, const Gas<
 // averages; p / rho of the Roe state formed once for its enthalpy (hf +
 // (n + 1) p / rho + |v|^2 / 2, as cp T = (n + 1) p / rho for the
 // calorically perfect gas) and sound speed; one reciprocal square root of
-// a^2 gives a and 1 / a^2; and the division-free central flux.
+// a^2 gives a and 1 / a^2; the dissipation's four waves summed in closed
+// form; and the division-free central flux.
 __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<double> &R,
                                             const Gas<double> &g, double nx, double ny,
                                             double nz, double f[5]) {
@@ -413,7 +479,8 @@ __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<do
                rw = (L.w + denRatio * R.w) * inv, rp = (L.p + denRatio * R.p) * inv;
   const double rhoR = L.rho * denRatio;
   const double por = rp * t;
-  const double hR = (g.hf + (g.n + 1.0) * por) + 0.5 * (ru * ru + rv * rv + rw * rw);
+  const double q2h = 0.5 * (ru * ru + rv * rv + rw * rw);
+  const double hR = (g.hf + (g.n + 1.0) * por) + q2h;
   const double a2 = g.gam * por;
   // s = 1 / a: a = a^2 s, 1 / a^2 = s^2
   const double sa = rsqrt(a2);
@@ -422,42 +489,33 @@ __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<do
   const double velNormR = ru * nx + rv * ny + rw * nz;
   const double normVelDiff = dU * nx + dV * ny + dW * nz;
   const double entropyFix = 0.1;
-  double d0, d1, d2, d3, d4;
-  // left moving acoustic wave
-  double waveSpeed = fabs(velNormR - aR);
-  if (waveSpeed < entropyFix)
-    waveSpeed = 0.5 * (waveSpeed * waveSpeed / entropyFix + entropyFix);
-  double ws = waveSpeed * ((dP - rhoR * aR * normVelDiff) * (0.5 * ia2));
-  d0 = ws;
-  d1 = ws * (ru - aR * nx);
-  d2 = ws * (rv - aR * ny);
-  d3 = ws * (rw - aR * nz);
-  d4 = ws * (hR - aR * velNormR);
-  // entropy wave
-  waveSpeed = fabs(velNormR);
-  const double dPa = dP * ia2;
-  d0 += waveSpeed * (dRho - dPa);
-  ws = waveSpeed * (dRho - dPa);
-  d1 += ws * ru;
-  d2 += ws * rv;
-  d3 += ws * rw;
-  d4 += ws * 0.5 * (ru * ru + rv * rv + rw * rw);
-  // shear waves
-  ws = waveSpeed * rhoR;
-  d1 += ws * (dU - normVelDiff * nx);
-  d2 += ws * (dV - normVelDiff * ny);
-  d3 += ws * (dW - normVelDiff * nz);
-  d4 += ws * ((ru * dU + rv * dV + rw * dW) - velNormR * normVelDiff);
-  // right moving acoustic wave
-  waveSpeed = fabs(velNormR + aR);
-  if (waveSpeed < entropyFix)
-    waveSpeed = 0.5 * (waveSpeed * waveSpeed / entropyFix + entropyFix);
-  ws = waveSpeed * ((dP + rhoR * aR * normVelDiff) * (0.5 * ia2));
-  d0 += ws;
-  d1 += ws * (ru + aR * nx);
-  d2 += ws * (rv + aR * ny);
-  d3 += ws * (rw + aR * nz);
-  d4 += ws * (hR + aR * velNormR);
+  // wave speeds; Harten's fix on the acoustic ones (the tests compare
+  // non-negative speeds by their bits)
+  const long long fixBits = Bits(entropyFix);
+  double lamL = fabs(velNormR - aR), lamR = fabs(velNormR + aR);
+  if (Bits(lamL) < fixBits) lamL = 0.5 * (lamL * lamL / entropyFix + entropyFix);
+  if (Bits(lamR) < fixBits) lamR = 0.5 * (lamR * lamR / entropyFix + entropyFix);
+  const double lamE = fabs(velNormR);
+  // wave strengths: acoustic aL, aR5, entropy aE, shear beta (times the
+  // velocity jump's tangential part)
+  const double rc = rhoR * aR, hia2 = 0.5 * ia2;
+  const double aL = lamL * ((dP - rc * normVelDiff) * hia2);
+  const double aR5 = lamR * ((dP + rc * normVelDiff) * hia2);
+  const double aE = lamE * (dRho - dP * ia2);
+  const double beta = lamE * rhoR;
+  // the four waves' eigenvectors summed in closed form: with sA = aL + aR5
+  // and tA = a (aR5 - aL), D = (sA + aE) [1, u, v, w] + (tA - beta dVn) n
+  // + beta dv in the momenta, and H sA + Vn tA + aE |v|^2 / 2 + beta (v .
+  // dv - Vn dVn) in the energy -- the reference's wave-by-wave sum
+  // regrouped, equal to it to roundoff
+  const double sA = aL + aR5, tA = aR * (aR5 - aL);
+  const double gn = tA - beta * normVelDiff;
+  const double d0 = sA + aE;
+  const double d1 = d0 * ru + (nx * gn + beta * dU);
+  const double d2 = d0 * rv + (ny * gn + beta * dV);
+  const double d3 = d0 * rw + (nz * gn + beta * dW);
+  const double d4 = (hR * sA + velNormR * tA) + aE * q2h +
+                    beta * ((ru * dU + rv * dV + rw * dW) - velNormR * normVelDiff);
   double fl[5], fr[5];
   InvFluxCentral(L, g, nx, ny, nz, fl);
   InvFluxCentral(R, g, nx, ny, nz, fr);
@@ -875,8 +933,8 @@ __device__ __forceinline__ void ScalarOffDiagPre(const Prim<T> &s, const NbrPre<
 template <typename T>
 __device__ __forceinline__ void ScalarOffDiagPreFast(const Prim<T> &s, const NbrPre<T> &pre,
                                                      const T du[5], const Gas<T> &g, T nx, T ny,
-                                                     T nz, T mag, bool positive, T visc_sr,
-                                                     T out[5]) {
+                                                     T nz, T mag, bool positive, bool viscous,
+                                                     T visc_sr, T out[5]) {
   T c[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) c[v] = pre.c[v] + du[v];
@@ -895,8 +953,8 @@ __device__ __forceinline__ void ScalarOffDiagPreFast(const Prim<T> &s, const Nbr
   df[3] = (mn * w + p * nz) - (mo * s.w + s.p * nz);
   df[4] = vnn * (c[4] + p) - mo * pre.h;
   const T half = T(0.5) * mag;
-  T lam = T(0.5) * mag * (fabs(vn) + pre.sos);
-  lam += visc_sr;
+  T lam = half * (fabs(vn) + pre.sos);
+  if (viscous) lam += visc_sr;
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
     const T fc = half * df[k];
