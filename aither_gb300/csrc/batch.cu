@@ -149,6 +149,9 @@ struct BatchCore {
   // cl_threads per solve), 0 = one launch per hyperplane, 2 = the same with
   // a group of lanes per scalar cell (one per neighbour term); autotuned
   int sweep_mode = 0, cl_size = 1, cl_threads = 256;
+  // sweep mode 4: planes of fewer than hy_items cells take lane groups
+  // (CTAs of sweep_threads), larger ones a thread per cell (CTAs of 128)
+  int hy_items = 1 << 15;
   int2 *d_cl_items = nullptr;
   int32_t *d_cl_step_off = nullptr, *d_solve_step0 = nullptr, *d_solve_nsteps = nullptr;
   SweepLists Lists() const {
@@ -726,8 +729,7 @@ class Runner : public RunnerBase {
       for (int s = 0; s < c_.nsteps; ++s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         if (b <= a) continue;
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 1, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.sweep_mode == 2, chained, c_.stream);
+        PlaneSweep(a, b - a, 1, sweep, full, chained);
         chained = true;
       }
     } else {
@@ -735,11 +737,19 @@ class Runner : public RunnerBase {
       for (int s = c_.nsteps - 1; s >= 0; --s) {
         const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
         if (b <= a) continue;
-        Launch<T>::Sweep(P_, c_.d_sweep + a, b - a, 0, sweep, full, c_.skinds,
-                         c_.sweep_threads, c_.sweep_mode == 2, chained, c_.stream);
+        PlaneSweep(a, b - a, 0, sweep, full, chained);
         chained = true;
       }
     }
+  }
+  // one hyperplane's launch in the batch's sweep shape (mode 0: a thread
+  // per cell, 2: lane groups, 4: lane groups below hy_items cells)
+  void PlaneSweep(int a, int n, int forward, int sweep, bool full, bool chained) {
+    const bool group =
+        c_.sweep_mode == 2 || (c_.sweep_mode == 4 && n < c_.hy_items);
+    const int threads = (c_.sweep_mode == 4 && !group) ? 128 : c_.sweep_threads;
+    Launch<T>::Sweep(P_, c_.d_sweep + a, n, forward, sweep, full, c_.skinds, threads, group,
+                     chained, c_.stream);
   }
   void ZeroGhostUpdates() {
     if (P_.nghost <= 0) return;
@@ -2277,6 +2287,9 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     std::vector<Shape> cand = {{0, 32, 1}, {0, 64, 1}, {0, 128, 1}, {0, 256, 1}};
     if (c.skinds & 1)
       for (int t : {32, 64, 128, 256}) cand.push_back({2, t, 1});
+    // lane groups on small planes, a thread per cell on planes of at least
+    // 32768 cells
+    if (c.skinds & 1) cand.push_back({4, 32, 32768});
     if (c.skinds)
       for (int cl : {1, 2, 4, 8})
         if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
@@ -2286,12 +2299,15 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     const Shape keep{c.sweep_mode,
                      c.sweep_mode == 1 ? c.cl_threads
                                        : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads),
-                     c.cl_size};
+                     c.sweep_mode == 4 ? c.hy_items : c.cl_size};
     auto apply = [&](const Shape &sh) {
       c.sweep_mode = sh.mode;
       if (sh.mode == 1) {
         c.cl_threads = sh.threads;
         c.cl_size = sh.cluster;
+      } else if (sh.mode == 4) {
+        c.sweep_threads = sh.threads;
+        c.hy_items = sh.cluster;
       } else if (sh.mode == 3) {
         ath::EnsureTileQueue(c, sh.threads);
         c.tq_size = sh.threads;
@@ -2334,7 +2350,8 @@ int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluste
   if (mode) *mode = c.sweep_mode;
   if (threads)
     *threads = c.sweep_mode == 1 ? c.cl_threads : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads);
-  if (cluster) *cluster = c.sweep_mode == 1 ? c.cl_size : 0;
+  if (cluster)
+    *cluster = c.sweep_mode == 1 ? c.cl_size : (c.sweep_mode == 4 ? c.hy_items : 0);
   return ATH_OK;
 }
 
@@ -2354,6 +2371,13 @@ int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int clust
         throw ath::Error(ATH_ERR_ARG, "persistent sweep: 256 threads and a launchable cluster");
       c.cl_threads = threads;
       c.cl_size = cluster;
+    } else if (mode == 4) {
+      if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
+        throw ath::Error(ATH_ERR_ARG, "per-plane sweeps take CTAs of 32, 64, 128 or 256 threads");
+      if (!(c.skinds & 1)) throw ath::Error(ATH_ERR_ARG, "lane groups serve scalar solves only");
+      if (cluster < 1) throw ath::Error(ATH_ERR_ARG, "hybrid sweep: a threshold of cells >= 1");
+      c.sweep_threads = threads;
+      c.hy_items = cluster;
     } else if (mode == 3) {
       if (!c.skinds || threads < 1 || threads > 4096)
         throw ath::Error(ATH_ERR_ARG, "tile-queue sweep: LU-SGS solves and tiles of 1..4096 cells");

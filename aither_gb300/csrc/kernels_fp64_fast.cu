@@ -34,16 +34,10 @@ void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int f
                          int sweep, bool full, int threads, bool group, bool chained,
                          cudaStream_t s) {
   if (n <= 0) return;
-  // without turbulence solves the kernels are built without their rows
-  const bool turb = (P.fkinds & 2) != 0;
   if (group) {
     LaunchSweepGroup<double>(P, items, n, forward, sweep, full, threads, chained, s);
   } else {
-    const unsigned grid = (unsigned)((n + threads - 1) / threads);
-    if (full && turb) k_sweep<double, true, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (full) k_sweep<double, true, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (turb) k_sweep<double, false, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweep<double, false, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    LaunchSweepCell<double>(P, items, n, forward, sweep, full, threads, chained, s);
   }
 }
 

@@ -1441,7 +1441,9 @@ __device__ __forceinline__ void LoadNbr(const Pools<T> &P, const SolveDev &sv, i
 // (ImplicitUpper), accumulated i, j, k from zero.  RANS solves add the
 // turbulence rows: the neighbour's turbulence face radius times its update
 // (turbModel::FaceSpectralRadius, include/spectralRadius.hpp).
-template <typename T>
+// WAIT: the neighbours' updates are read after GridDependencyWait (a
+// hyperplane kernel launched programmatically after the previous plane's)
+template <typename T, bool WAIT = false>
 __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
                                            const SolveDev &sv, int64_t q, bool lower,
                                            T acc[5], T acct[2]) {
@@ -1460,7 +1462,17 @@ __device__ __forceinline__ void OffDiagSum(const Pools<T> &P, const Gas<T> &g,
   Nbr<T> os[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d)
-    if (nbs[d] != -1) LoadNbr(P, sv, nbs[d], os[d]);
+    if (nbs[d] != -1) LoadNbrCell(P, nbs[d], os[d]);
+  if constexpr (WAIT) {
+    GridDependencyWait();
+    GridDependentsLaunch();
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if (nbs[d] != -1) {
+      LoadNbrDu(P, nbs[d], os[d]);
+      LoadNbrSolve(P, sv, nbs[d], os[d]);
+    }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     if (nbs[d] == -1) continue;
@@ -1738,12 +1750,12 @@ __device__ __forceinline__ void ScalarFinish(const Pools<T> &P, const SolveDev &
   }
 }
 
-template <typename T, bool FULL>
+template <typename T, bool FULL, bool WAIT = false>
 __device__ __forceinline__ void SweepScalarQ(const Pools<T> &P, const SolveDev &sv, int64_t q,
                                              int forward, int sweep) {
   const Gas<T> g = GasOf<T>(sv);
   T acc[5], acct[2], other[5], othert[2];
-  OffDiagSum(P, g, sv, q, forward != 0, acc, acct);
+  OffDiagSum<T, WAIT>(P, g, sv, q, forward != 0, acc, acct);
   bool both = false;
   if constexpr (FULL) {
     if (sweep >= sv.sweeps) return;
@@ -1768,7 +1780,9 @@ __global__ void __launch_bounds__(256) k_sweep(Pools<T> P, const int2 *items, in
     sv.rans = 0;
     sv.wilcox = 0;
   }
-  SweepScalarQ<T, FULL>(P, sv, it.x, forward, sweep);
+  // programmatic launches (chained planes) wait inside before reading the
+  // previous plane's updates; threads that stop above read none
+  SweepScalarQ<T, FULL, true>(P, sv, it.x, forward, sweep);
 }
 
 // Scalar pass with a group of lanes per cell: lane d (0-2) evaluates the
@@ -1896,6 +1910,30 @@ __global__ void __launch_bounds__(256, MINB) k_sweepg(Pools<T> P, const int2 *it
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = (int)(threadIdx.x & 31);
   SweepGroupItem<T, FULL, TURB>(P, items, (t >> 5) * CPW + lane / L, n_items, forward, sweep);
+}
+
+// One hyperplane of the thread-per-cell scalar sweep (k_sweep), chained
+// launches as LaunchSweepGroup's
+template <typename T>
+void LaunchSweepCell(const Pools<T> &P, const int2 *items, int n, int forward, int sweep,
+                     bool full, int threads, bool chained, cudaStream_t s) {
+  const unsigned grid = (unsigned)((n + threads - 1) / threads);
+  const bool turb = (P.fkinds & 2) != 0;
+  void (*kern)(Pools<T>, const int2 *, int, int, int) =
+      full ? (turb ? k_sweep<T, true, true> : k_sweep<T, true, false>)
+           : (turb ? k_sweep<T, false, true> : k_sweep<T, false, false>);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = chained ? 1 : 0;
+  // a failed launch leaves its error for the caller's cudaGetLastError
+  (void)cudaLaunchKernelEx(&cfg, kern, P, items, n, forward, sweep);
 }
 
 // One hyperplane of the grouped scalar sweep over n items with CTAs of
@@ -3606,12 +3644,7 @@ void Launch<T>::Sweep(const Pools<T> &P, const int2 *items, int n, int forward, 
   } else if ((kinds & 1) && group) {
     LaunchSweepGroup<T>(P, items, n, forward, sweep, full, threads, chained, s);
   } else if (kinds & 1) {
-    const unsigned grid = (unsigned)((n + threads - 1) / threads);
-    const bool turb = (P.fkinds & 2) != 0;
-    if (full && turb) k_sweep<T, true, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (full) k_sweep<T, true, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else if (turb) k_sweep<T, false, true><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
-    else k_sweep<T, false, false><<<grid, threads, 0, s>>>(P, items, n, forward, sweep);
+    LaunchSweepCell<T>(P, items, n, forward, sweep, full, threads, chained, s);
   }
   if (kinds & 2) {
     const unsigned gridb = (unsigned)(((int64_t)n * 8 + threads - 1) / threads);

@@ -308,13 +308,16 @@ __device__ __forceinline__ void MusclFastPair1(T wm2, T wm1, T w0, T wp1, T dpL,
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const T x = xs[k], y = ys[k];
-    const T A = eps + x, B = eps + y;
     if constexpr (std::is_same<T, double>::value) {
-      const long long ia = __double_as_longlong(A), ib = __double_as_longlong(B);
+      // in FP64 the tests read the slopes x and y themselves instead of
+      // eps + x and eps + y: the increment changes only where a slope is
+      // below about eps in magnitude, by less than eps
+      const long long ia = __double_as_longlong(x), ib = __double_as_longlong(y);
       const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
       o[k] = ((ia ^ ib) < 0 || ma == 0 || mb == 0) ? up[k]
                                                      : up[k] + T(0.5) * (mb < ma ? y : x);
     } else {
+      const T A = eps + x, B = eps + y;
       o[k] = !(A * B > T(0)) ? up[k] : up[k] + T(0.5) * (fabs(B) < fabs(A) ? y : x);
     }
   }
@@ -516,14 +519,18 @@ __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<do
   const double d3 = d0 * rw + (nz * gn + beta * dW);
   const double d4 = (hR * sA + velNormR * tA) + aE * q2h +
                     beta * ((ru * dU + rv * dV + rw * dW) - velNormR * normVelDiff);
-  double fl[5], fr[5];
-  InvFluxCentral(L, g, nx, ny, nz, fl);
-  InvFluxCentral(R, g, nx, ny, nz, fr);
-  f[0] = (fl[0] + (fr[0] - d0)) * 0.5;
-  f[1] = (fl[1] + (fr[1] - d1)) * 0.5;
-  f[2] = (fl[2] + (fr[2] - d2)) * 0.5;
-  f[3] = (fl[3] + (fr[3] - d3)) * 0.5;
-  f[4] = (fl[4] + (fr[4] - d4)) * 0.5;
+  // central part FL + FR summed term by term, the two pressures once
+  const double vnL = L.u * nx + L.v * ny + L.w * nz, vnR = R.u * nx + R.v * ny + R.w * nz;
+  const double mL = L.rho * vnL, mR = R.rho * vnR;
+  const double np1 = g.n + 1.0;
+  const double rhoHL = L.rho * (g.hf + 0.5 * (L.u * L.u + L.v * L.v + L.w * L.w)) + np1 * L.p;
+  const double rhoHR = R.rho * (g.hf + 0.5 * (R.u * R.u + R.v * R.v + R.w * R.w)) + np1 * R.p;
+  const double pLR = L.p + R.p;
+  f[0] = ((mL + mR) - d0) * 0.5;
+  f[1] = ((mL * L.u + (mR * R.u + pLR * nx)) - d1) * 0.5;
+  f[2] = ((mL * L.v + (mR * R.v + pLR * ny)) - d2) * 0.5;
+  f[3] = ((mL * L.w + (mR * R.w + pLR * nz)) - d3) * 0.5;
+  f[4] = ((vnL * rhoHL + vnR * rhoHR) - d4) * 0.5;
 }
 
 // ---------------------------------------------------------------------------

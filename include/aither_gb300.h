@@ -363,11 +363,16 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
 /* Current sweep shape: mode 1 persistent cluster sweep (cluster = CTAs per
  * solve), 0 one launch per hyperplane (cluster = 0), 2 one launch per
  * hyperplane with a group of lanes per scalar-solve cell, one per neighbour
- * term, 3 persistent tile-queue sweep (threads = cells per tile). */
+ * term, 3 persistent tile-queue sweep (threads = cells per tile), 4 one
+ * launch per hyperplane, lane groups (CTAs of threads) on planes of fewer
+ * than cluster cells and a thread per cell (CTAs of 128) on larger ones.  Successive hyperplane launches of a pass are chained by
+ * programmatic dependent launch: a plane's kernel loads what the pass does
+ * not change while the previous plane's kernel runs. */
 int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluster);
 /* Sets the sweep shape (as ath_batch_sweep_shape reports it; mode 3 takes
- * tiles of 1..4096 cells); the next iteration recaptures the batch's
- * graph.  Call it outside any stream capture. */
+ * tiles of 1..4096 cells, mode 4 a threshold of at least one cell);
+ * the next iteration recaptures the batch's graph.  Call it outside any
+ * stream capture. */
 int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int cluster);
 /* The tile-queue sweep's waits are bounded: a wait for another tile polls
  * at most poll_limit times (default 2^24, about a second), then the sweep
