@@ -89,11 +89,18 @@ class DevMem {
   std::vector<std::pair<void *, size_t>> ptrs_;
 };
 
+// solve groups whose hyperplane chains a sweep pass can run concurrently
+constexpr int kSweepGroups = 4;
+
 struct Lists {
   std::vector<int32_t> cells, cell_cta_block, cell_cta_pos0;
   std::vector<int32_t> faces[3], face_cta_block[3];
   std::vector<int2> sweep_items;  // (q index, block)
   std::vector<int32_t> step_off;
+  // the items of plane s ordered by solve group (kSweepGroups groups of
+  // solves balanced by cells): group g's are [gstep_off[s * (kSweepGroups
+  // + 1) + g], ... + g + 1)
+  std::vector<int32_t> gstep_off;
   // the same items per solve, then plane, for the persistent sweep
   std::vector<int2> cl_items;
   std::vector<int32_t> cl_step_off, solve_step0, solve_nsteps;
@@ -152,6 +159,12 @@ struct BatchCore {
   // sweep mode 4: planes of fewer than hy_items cells take lane groups
   // (CTAs of sweep_threads), larger ones a thread per cell (CTAs of 128)
   int hy_items = 1 << 15;
+  // modes 0 and 2: the solves' hyperplane chains run as sweep_groups
+  // concurrent chains (1, 2 or 4 merged solve groups), forked from the
+  // batch's stream onto gstream and joined back after each pass
+  int sweep_groups = 1;
+  cudaStream_t gstream[kSweepGroups - 1] = {};
+  cudaEvent_t gfork = nullptr, gjoin[kSweepGroups - 1] = {};
   int2 *d_cl_items = nullptr;
   int32_t *d_cl_step_off = nullptr, *d_solve_step0 = nullptr, *d_solve_nsteps = nullptr;
   SweepLists Lists() const {
@@ -723,33 +736,43 @@ class Runner : public RunnerBase {
                          c_.cl_size, c_.stream);
       return;
     }
-    if (forward) {
-      // a plane's launch is chained to the pass's previous launch only
+    // K concurrent chains: solve groups g0..g1 of kSweepGroups each, the
+    // first on the batch's stream, the others forked and joined back
+    const int K = c_.sweep_mode == 4 ? 1 : c_.sweep_groups;
+    if (K > 1) {
+      Check(cudaEventRecord(c_.gfork, c_.stream), "event");
+      for (int g = 1; g < K; ++g) Check(cudaStreamWaitEvent(c_.gstream[g - 1], c_.gfork, 0), "event");
+    }
+    constexpr int W = kSweepGroups + 1;
+    for (int g = 0; g < K; ++g) {
+      cudaStream_t st = g == 0 ? c_.stream : c_.gstream[g - 1];
+      const int g0 = g * kSweepGroups / K, g1 = (g + 1) * kSweepGroups / K;
+      // a plane's launch is chained to the chain's previous launch only
       bool chained = false;
-      for (int s = 0; s < c_.nsteps; ++s) {
-        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
+      for (int k = 0; k < c_.nsteps; ++k) {
+        const int s = forward ? k : c_.nsteps - 1 - k;
+        const int a = c_.L.gstep_off[(size_t)s * W + g0], b = c_.L.gstep_off[(size_t)s * W + g1];
         if (b <= a) continue;
-        PlaneSweep(a, b - a, 1, sweep, full, chained);
+        PlaneSweep(a, b - a, forward, sweep, full, chained, st);
         chained = true;
       }
-    } else {
-      bool chained = false;
-      for (int s = c_.nsteps - 1; s >= 0; --s) {
-        const int a = c_.L.step_off[s], b = c_.L.step_off[s + 1];
-        if (b <= a) continue;
-        PlaneSweep(a, b - a, 0, sweep, full, chained);
-        chained = true;
+    }
+    if (K > 1) {
+      for (int g = 1; g < K; ++g) {
+        Check(cudaEventRecord(c_.gjoin[g - 1], c_.gstream[g - 1]), "event");
+        Check(cudaStreamWaitEvent(c_.stream, c_.gjoin[g - 1], 0), "event");
       }
     }
   }
   // one hyperplane's launch in the batch's sweep shape (mode 0: a thread
   // per cell, 2: lane groups, 4: lane groups below hy_items cells)
-  void PlaneSweep(int a, int n, int forward, int sweep, bool full, bool chained) {
+  void PlaneSweep(int a, int n, int forward, int sweep, bool full, bool chained,
+                  cudaStream_t st) {
     const bool group =
         c_.sweep_mode == 2 || (c_.sweep_mode == 4 && n < c_.hy_items);
     const int threads = (c_.sweep_mode == 4 && !group) ? 128 : c_.sweep_threads;
     Launch<T>::Sweep(P_, c_.d_sweep + a, n, forward, sweep, full, c_.skinds, threads, group,
-                     chained, c_.stream);
+                     chained, st);
   }
   void ZeroGhostUpdates() {
     if (P_.nghost <= 0) return;
@@ -1350,18 +1373,45 @@ void BuildLists(BatchCore &c) {
       }
     }
   }
-  // hyperplane steps: step s holds plane s of every block that has one
+  // hyperplane steps: step s holds plane s of every block that has one,
+  // ordered by solve group.  The groups balance the solves' cells (largest
+  // solve first into the lightest group)
   c.nsteps = 0;
   for (auto &b : st.blocks) c.nsteps = std::max(c.nsteps, (int)b.plane_offsets.size() - 1);
+  std::vector<int> sgroup(c.nsolves, 0);
+  {
+    std::vector<int64_t> scells(c.nsolves, 0);
+    for (int s = 0; s < c.nsolves; ++s)
+      for (int b : st.solves[s].blocks)
+        scells[s] += (int64_t)st.blocks[b].ni * st.blocks[b].nj * st.blocks[b].nk;
+    std::vector<int> order(c.nsolves);
+    for (int s = 0; s < c.nsolves; ++s) order[s] = s;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return scells[x] > scells[y]; });
+    int64_t load[kSweepGroups] = {};
+    for (int s : order) {
+      int g = 0;
+      for (int k = 1; k < kSweepGroups; ++k)
+        if (load[k] < load[g]) g = k;
+      sgroup[s] = g;
+      load[g] += scells[s];
+    }
+  }
   L.step_off.assign(c.nsteps + 1, 0);
+  L.gstep_off.assign((size_t)c.nsteps * (kSweepGroups + 1), 0);
   for (int s2 = 0; s2 < c.nsteps; ++s2) {
     L.step_off[s2] = (int32_t)L.sweep_items.size();
-    for (int b = 0; b < c.nblocks; ++b) {
-      const Block &bk = st.blocks[b];
-      if (s2 + 1 >= (int)bk.plane_offsets.size()) continue;
-      for (int q = bk.plane_offsets[s2]; q < bk.plane_offsets[s2 + 1]; ++q)
-        L.sweep_items.push_back(make_int2((int)(L.q0[b] + q), b));
+    for (int g = 0; g < kSweepGroups; ++g) {
+      L.gstep_off[(size_t)s2 * (kSweepGroups + 1) + g] = (int32_t)L.sweep_items.size();
+      for (int b = 0; b < c.nblocks; ++b) {
+        const Block &bk = st.blocks[b];
+        if (sgroup[bk.solve] != g || s2 + 1 >= (int)bk.plane_offsets.size()) continue;
+        for (int q = bk.plane_offsets[s2]; q < bk.plane_offsets[s2 + 1]; ++q)
+          L.sweep_items.push_back(make_int2((int)(L.q0[b] + q), b));
+      }
     }
+    L.gstep_off[(size_t)s2 * (kSweepGroups + 1) + kSweepGroups] =
+        (int32_t)L.sweep_items.size();
   }
   L.step_off[c.nsteps] = (int32_t)L.sweep_items.size();
   for (int s = 0; s < c.nsolves; ++s) {
@@ -1641,6 +1691,11 @@ void DestroyBatch(ath_batch *batch) {
   if (batch->core.ev0) cudaEventDestroy(batch->core.ev0);
   if (batch->core.ev1) cudaEventDestroy(batch->core.ev1);
   if (batch->core.stream && batch->core.own_stream) cudaStreamDestroy(batch->core.stream);
+  for (auto x : batch->core.gstream)
+    if (x) cudaStreamDestroy(x);
+  if (batch->core.gfork) cudaEventDestroy(batch->core.gfork);
+  for (auto x : batch->core.gjoin)
+    if (x) cudaEventDestroy(x);
   delete batch;
 }
 
@@ -1836,6 +1891,9 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
   } else {
     Check(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking), "stream");
   }
+  for (auto &x : c.gstream) Check(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "stream");
+  Check(cudaEventCreateWithFlags(&c.gfork, cudaEventDisableTiming), "event");
+  for (auto &x : c.gjoin) Check(cudaEventCreateWithFlags(&x, cudaEventDisableTiming), "event");
   c.mem.reset(new DevMem(ctx, c.stream));
   DevMem &m = *c.mem;
   std::vector<BlockDev> bd(c.nblocks);
@@ -2156,6 +2214,9 @@ int ath_batch_iterate(ath_batch *batch, int n, ath_norms *norms_h) {
     if (!batch || n < 0) throw ath::Error(ATH_ERR_ARG, "bad argument");
     auto &c = batch->core;
     Check(cudaSetDevice(c.ctx->device), "cudaSetDevice");
+    // the iteration graph is captured (when a shape change dropped it)
+    // before the timed interval opens
+    batch->run->Iterate(0);
     Check(cudaEventRecord(c.ev0, c.stream), "event");
     int done = 0;
     while (done < n) {
@@ -2245,6 +2306,7 @@ int ath_batch_converge(ath_batch *batch, int max_iters, double drop, int check_e
             "target upload");
     std::vector<ath::SolveDev> sv(c.nsolves);
     int done = 0;
+    batch->run->Iterate(0);  // capture the iteration graph outside the timed interval
     Check(cudaEventRecord(c.ev0, c.stream), "event");
     while (done < max_iters) {
       const int chunk = std::min(max_iters - done, std::min(check_every, c.ring_cap));
@@ -2290,6 +2352,10 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     // lane groups on small planes, a thread per cell on planes of at least
     // 32768 cells
     if (c.skinds & 1) cand.push_back({4, 32, 32768});
+    // lane groups with the solves' chains run as 2 or 4 concurrent chains
+    if ((c.skinds & 1) && c.nsolves > 1)
+      for (int t : {32, 64})
+        for (int k : {2, 4}) cand.push_back({2, t, k});
     if (c.skinds)
       for (int cl : {1, 2, 4, 8})
         if (run.MaxClusters(c.skinds, 256, cl) > 0) cand.push_back({1, 256, cl});
@@ -2299,7 +2365,8 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
     const Shape keep{c.sweep_mode,
                      c.sweep_mode == 1 ? c.cl_threads
                                        : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads),
-                     c.sweep_mode == 4 ? c.hy_items : c.cl_size};
+                     c.sweep_mode == 4 ? c.hy_items
+                                       : (c.sweep_mode == 1 ? c.cl_size : c.sweep_groups)};
     auto apply = [&](const Shape &sh) {
       c.sweep_mode = sh.mode;
       if (sh.mode == 1) {
@@ -2313,6 +2380,7 @@ int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads) {
         c.tq_size = sh.threads;
       } else {
         c.sweep_threads = sh.threads;
+        c.sweep_groups = std::max(1, sh.cluster);
       }
     };
     run.Snapshot(false);
@@ -2351,7 +2419,10 @@ int ath_batch_sweep_shape(ath_batch *batch, int *mode, int *threads, int *cluste
   if (threads)
     *threads = c.sweep_mode == 1 ? c.cl_threads : (c.sweep_mode == 3 ? c.tq_size : c.sweep_threads);
   if (cluster)
-    *cluster = c.sweep_mode == 1 ? c.cl_size : (c.sweep_mode == 4 ? c.hy_items : 0);
+    *cluster = c.sweep_mode == 1 ? c.cl_size
+               : c.sweep_mode == 4 ? c.hy_items
+               : c.sweep_mode == 3 ? 0
+                                   : c.sweep_groups;
   return ATH_OK;
 }
 
@@ -2364,7 +2435,10 @@ int ath_batch_set_sweep_shape(ath_batch *batch, int mode, int threads, int clust
         throw ath::Error(ATH_ERR_ARG, "per-plane sweeps take CTAs of 32, 64, 128 or 256 threads");
       if (mode == 2 && !(c.skinds & 1))
         throw ath::Error(ATH_ERR_ARG, "lane groups serve scalar solves only");
+      if (cluster != 0 && cluster != 1 && cluster != 2 && cluster != 4)
+        throw ath::Error(ATH_ERR_ARG, "per-plane sweeps run 1, 2 or 4 concurrent chains");
       c.sweep_threads = threads;
+      c.sweep_groups = std::max(1, cluster);
     } else if (mode == 1) {
       if (threads != 256 || cluster < 1 || cluster > 8 ||
           batch->run->MaxClusters(c.skinds, 256, cluster) <= 0)

@@ -361,9 +361,12 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
  * persistent cluster sweep sized to its largest hyperplane. */
 int ath_batch_autotune(ath_batch *batch, int reps, int *sweep_threads);
 /* Current sweep shape: mode 1 persistent cluster sweep (cluster = CTAs per
- * solve), 0 one launch per hyperplane (cluster = 0), 2 one launch per
- * hyperplane with a group of lanes per scalar-solve cell, one per neighbour
- * term, 3 persistent tile-queue sweep (threads = cells per tile), 4 one
+ * solve), 0 one launch per hyperplane, 2 one launch per hyperplane with a
+ * group of lanes per scalar-solve cell, one per neighbour term (modes 0 and
+ * 2: cluster = the number of concurrent chains, 1, 2 or 4, the batch's
+ * solves split into groups balanced by cells, each group's hyperplanes a
+ * chain of launches on its own stream; 0 reads as 1), 3 persistent
+ * tile-queue sweep (threads = cells per tile), 4 one
  * launch per hyperplane, lane groups (CTAs of threads) on planes of fewer
  * than cluster cells and a thread per cell (CTAs of 128) on larger ones.  Successive hyperplane launches of a pass are chained by
  * programmatic dependent launch: a plane's kernel loads what the pass does

@@ -63,14 +63,15 @@ def test_tile_queue_sweep_matches_per_plane_sweeps(ctx, name, precision, tmp_pat
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["bump_batch", "bump_sweeps3_it1"])
 def test_lane_group_and_hybrid_sweeps_match_thread_per_cell(ctx, name, precision, tmp_path):
-    """Lane groups on every plane (mode 2) and lane groups below a plane
-    size with a thread per cell above it (mode 4; a threshold of 40 cells
-    splits these grids' planes between the two), each launch chained to the
-    previous plane's by programmatic dependent launch: the same result bit
-    for bit as a thread per cell on every plane."""
+    """Lane groups on every plane (mode 2), lane groups below a plane size
+    with a thread per cell above it (mode 4; a threshold of 40 cells splits
+    these grids' planes between the two), and the solves' chains run as 2
+    or 4 concurrent chains, each launch chained to the previous plane's by
+    programmatic dependent launch: the same result bit for bit as one chain
+    with a thread per cell on every plane."""
     inp, st = _inputs(tmp_path, name)
     ref = _run(ctx, inp, st, precision, (0, 64, 0), 6)
-    for shape in ((2, 32, 0), (4, 32, 40), (4, 64, 1)):
+    for shape in ((2, 32, 0), (4, 32, 40), (4, 64, 1), (2, 32, 2), (2, 64, 4), (0, 64, 4)):
         got = _run(ctx, inp, st, precision, shape, 6)
         for a, b in zip(got, ref):
             assert np.array_equal(a, b), (name, shape)
