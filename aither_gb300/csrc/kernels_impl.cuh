@@ -602,7 +602,7 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 // Reconstruction and inviscid flux of face c (direction D) in arithmetic U:
 // f is the flux per unit area, L and R the reconstructed face states.
 // FAST (FP64 batches with the fast-face option): MUSCL and the Roe flux in
-// their fast forms (MusclFast, RoeFluxFast), equal to the reference to
+// their fast forms (MusclFastPair, RoeFluxFast), equal to the reference to
 // roundoff instead of bit for bit.
 template <typename U, int D, typename PT, bool FAST = false>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
@@ -965,6 +965,14 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
   if ((sv.block != 0) != BLOCK || !sv.active) return;
+  // fast FP64 option with a local time step: the solve's 1 / CFL formed
+  // once per CTA (the CTA lies in one block) for the diagonal
+  __shared__ double s_cfl_inv;
+  const bool fastdt = std::is_same<T, double>::value && P.fast_fp64 && sv.dt_global <= 0.0;
+  if (fastdt) {
+    if (threadIdx.x == 0) s_cfl_inv = 1.0 / P.cfl[b.solve];
+    __syncthreads();
+  }
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
   const int64_t n = P.ncell;
@@ -1143,10 +1151,19 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
   // src/linearSolver.cpp:146)
   const double cfl = P.cfl[b.solve];
   const double lmax = rans ? CMax(lam, lamt) : lam;
-  const double dt = sv.dt_global > 0.0 ? sv.dt_global : cfl * (vol / lmax);
+  double dt, diagVolTimeD;
+  if (fastdt) {
+    // dt = CFL V / lambda and V (1 + zeta) / (dt theta) = (1 + zeta) lambda /
+    // (CFL theta): one reciprocal of lambda
+    const double il = 1.0 / lmax;
+    dt = cfl * (vol * il);
+    diagVolTimeD = ((1.0 + sv.zeta) * sv.theta_inv * s_cfl_inv) * lmax;
+  } else {
+    dt = sv.dt_global > 0.0 ? sv.dt_global : cfl * (vol / lmax);
+    diagVolTimeD = (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
+  }
   P.dt[c] = dt;
   const int64_t nq = P.nq;
-  double diagVolTimeD = (vol * (1.0 + sv.zeta)) / (dt * sv.theta);
   if (sv.dual_cfl > 0.0) diagVolTimeD += (rans ? lmax : CMax(lam, 0.0)) / sv.dual_cfl;
   if (sv.unsteady) {
     // b = -R/theta + SolDeltaNm1 - SolDeltaMmN (procBlock::SolDeltaMmN /

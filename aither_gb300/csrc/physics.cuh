@@ -275,19 +275,7 @@ __device__ __forceinline__ T MusclFast1(T up2, T up1, T dw1, T dplus, T dminus, 
   }
   return up1 + T(0.25) * x * ((T(1) - kappa) * lim + (T(1) + kappa) * rilim);
 }
-template <typename T>
-__device__ __forceinline__ Prim<T> MusclFast(const Prim<T> &up2, const Prim<T> &up1,
-                                             const Prim<T> &dw1, T dplus, T dminus, T kappa,
-                                             int limiter) {
-  Prim<T> o;
-  o.rho = MusclFast1(up2.rho, up1.rho, dw1.rho, dplus, dminus, kappa, limiter);
-  o.u = MusclFast1(up2.u, up1.u, dw1.u, dplus, dminus, kappa, limiter);
-  o.v = MusclFast1(up2.v, up1.v, dw1.v, dplus, dminus, kappa, limiter);
-  o.w = MusclFast1(up2.w, up1.w, dw1.w, dplus, dminus, kappa, limiter);
-  o.p = MusclFast1(up2.p, up1.p, dw1.p, dplus, dminus, kappa, limiter);
-  return o;
-}
-// Both face states of the face between cells m1 and 0 in MusclFast's form
+// Both face states of the face between cells m1 and 0 in MusclFast1's form
 // (lower side: upwind2 m2, upwind1 m1, downwind 0; upper side: upwind2 p1,
 // upwind1 0, downwind m1), the difference across the face formed once:
 // the upper side's y = (wm1 - w0) dplus is -(w0 - wm1) dplus exactly

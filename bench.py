@@ -716,15 +716,15 @@ def _max_over_ranks(x: float, world: int) -> float:
 # bump-channel batch's cells; the counts scale with cells):
 #   * fast option -- `ncu --clock-control none --metrics dram__bytes_read.sum,
 #     dram__bytes_write.sum,gpu__time_duration.sum,smsp__sass_thread_inst_
-#     executed_op_{dfma,dadd,dmul}_pred_on.sum -s 1103 -c 355` (every launch of
-#     the first timed iteration) on `python bench.py --ncases 8 --steps 1
-#     --warmup 3 --no-cpu-baseline --converge-drop 0 --served-n 0 --sst-steps 0
-#     --plate-iters 0 --vortex-iters 0 --mg-iters 0 --precision fp64
-#     --sweep-shape 2,32 --exact-arm 0` (the first 8 cases, 888,004 cells;
-#     GB300, 2026-12-04): residual-pass DRAM traffic 811.4 B per cell (faces
-#     103.4 + 110.2 + 115.1, cell kernel 482.7); executed FP64 FLOP 440.3 per
-#     face direction, 684.8 in the two sweeps, 297.0 cell, 101.3 update,
-#     23.7 ghost fill;
+#     executed_op_{dfma,dadd,dmul}_pred_on.sum,... -s 1103 -c 355` (every
+#     launch of the first timed iteration) on `python bench.py --ncases 8
+#     --steps 1 --warmup 3 --no-cpu-baseline --converge-drop 0 --served-n 0
+#     --sst-steps 0 --plate-iters 0 --vortex-iters 0 --mg-iters 0 --precision
+#     fp64 --sweep-shape 2,32 --exact-arm 0` (the first 8 cases, 888,004
+#     cells; GB300, 2026-12-04): residual-pass DRAM traffic 922.2 B per cell
+#     (faces 133.2 + 140.5 + 144.1, cell kernel 504.4); executed FP64 FLOP
+#     272.6 per face direction, 560.1 in the two sweeps, 181.0 cell, 73.2
+#     update, 19.2 ghost fill;
 #   * bit-exact path -- the same counters over one iteration of a 64x48x32
 #     bump channel: 1026 FLOP per face direction, 1134 in the two sweeps,
 #     502 cell, 188 update, 25 ghosts.
@@ -734,9 +734,9 @@ NCU_PER_CELL = {
     "source": "ncu captures on GB300 of the batched bump-channel path (fast option: every "
               "launch of one iteration of the first 8 cases of the batched workload, "
               "888,004 cells; bit-exact path: one 64x48x32 case), 2026-12-04",
-    "residual_traffic_bytes": {"fast": 811.4},
-    "flop": {"fast": {"face_per_direction": 440.3, "sweeps": 684.8, "cell": 297.0,
-                      "update": 101.3, "ghost": 23.7},
+    "residual_traffic_bytes": {"fast": 922.2},
+    "flop": {"fast": {"face_per_direction": 272.6, "sweeps": 560.1, "cell": 181.0,
+                      "update": 73.2, "ghost": 19.2},
              "exact": {"face_per_direction": 1026.0, "sweeps": 1134.0, "cell": 502.0,
                        "update": 188.0, "ghost": 25.0}},
 }
