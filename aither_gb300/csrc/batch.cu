@@ -577,20 +577,23 @@ class Runner : public RunnerBase {
     P_.cfl = c.d_cfl;
     if (c.L.any_viscous) InitialViscosity(m);
     if constexpr (std::is_same<T, double>::value) {
-      if (P_.fast_fp64) {
-        // the fast option's geometry tables, formed once
-        for (int d = 0; d < 3; ++d) {
-          P_.fgeo[d] = m.Alloc<double>(4 * n);
-          P_.cgeo[d] = m.Alloc<double>(4 * n);
-          c_.mem->Zero(P_.fgeo[d], 0, 4 * n * sizeof(double));
-          c_.mem->Zero(P_.cgeo[d], 0, 4 * n * sizeof(double));
-        }
-        const int nfc[3] = {(int)c.L.face_cta_block[0].size(), (int)c.L.face_cta_block[1].size(),
-                            (int)c.L.face_cta_block[2].size()};
+      // FP64 batches: the geometry tables, formed once (the fast option's
+      // forms, or the bit-exact ones)
+      for (int d = 0; d < 3; ++d) {
+        P_.fgeo[d] = m.Alloc<double>(4 * n);
+        P_.cgeo[d] = m.Alloc<double>(4 * n);
+        c_.mem->Zero(P_.fgeo[d], 0, 4 * n * sizeof(double));
+        c_.mem->Zero(P_.cgeo[d], 0, 4 * n * sizeof(double));
+      }
+      const int nfc[3] = {(int)c.L.face_cta_block[0].size(), (int)c.L.face_cta_block[1].size(),
+                          (int)c.L.face_cta_block[2].size()};
+      if (P_.fast_fp64)
         LaunchFastGeomFp64(P_, c.d_faces, c.d_face_cta_block, nfc, c.d_cells,
                            c.d_cell_cta_block, (int)c.L.cell_cta_block.size(), c_.stream);
-        Check(cudaGetLastError(), "kernel launch");
-      }
+      else
+        LaunchExactGeomFp64(P_, c.d_faces, c.d_face_cta_block, nfc, c.d_cells,
+                            c.d_cell_cta_block, (int)c.L.cell_cta_block.size(), c_.stream);
+      Check(cudaGetLastError(), "kernel launch");
     }
   }
 
@@ -2846,6 +2849,7 @@ size_t EstimateBatchBytes(const Setup &st, int precision) {
     const double nq = (double)b.ni * b.nj * b.nk;
     const bool visc = ph.eqn != ATH_EQN_EULER, blk = IsBlockSolver(ph.solver);
     double pc = 8.0 * (5 + 5 + 15 + 1 + 1 + 1 + 3 + 12) + 4.0 * 6;  // pools, lists
+    if (precision == ATH_PREC_FP64) pc += 8.0 * 24;  // geometry tables
     if (visc) pc += 15 * ts + 8;
     if (blk) pc += 30 * ts + (visc ? 45 * ts : 0);
     double qc = ts * (5 + 5 + 5 + 24 + 6 + 2 + 1) + 4.0 * 8;

@@ -152,11 +152,13 @@ struct Pools {
   const double *vol;       // [ncell]
   const double *width[3];  // [ncell]
   const double *fa[3];     // [4][ncell] unit normal x,y,z and magnitude
-  // FP64 batches with the fast option, formed once from the geometry:
-  // fgeo[d] [4][ncell] at a face of direction d, MUSCL's width ratios dplus
-  // and dminus of its lower and of its upper side; cgeo[d] [4][ncell] at a
-  // physical cell, the normalised sum of its two face normals of direction
-  // d and their average area (the cell spectral radius's geometry)
+  // FP64 batches, formed once from the geometry: fgeo[d] [4][ncell] at a
+  // face of direction d, MUSCL's width ratios dplus and dminus of its lower
+  // and of its upper side; cgeo[d] [4][ncell] at a physical cell, the
+  // normalised average (fast option: sum) of its two face normals of
+  // direction d and their average area (the cell spectral radius's
+  // geometry).  Bit-exact batches form them with the per-face and per-cell
+  // expressions, the fast option with its own
   double *fgeo[3];
   double *cgeo[3];
   const int32_t *qpos;     // [ncell] q index of a physical cell, -1 for ghosts
@@ -392,8 +394,13 @@ void LaunchFastCellFp64(const Pools<double> &P, const int32_t *list, const int32
 void LaunchFastSweepFp64(const Pools<double> &P, const int2 *items, int n, int forward,
                          int sweep, bool full, int threads, bool group, bool chained,
                          cudaStream_t s);
-// The fast option's geometry tables (Pools::fgeo, cgeo) over the batch's
-// face lists of each direction and its physical-cell list
+// The geometry tables (Pools::fgeo, cgeo) over the batch's face lists of
+// each direction and its physical-cell list: the fast option's forms
+// (kernels_fp64_fast.cu), or the bit-exact ones (kernels_fp64.cu)
+void LaunchExactGeomFp64(const Pools<double> &P, const int32_t *const faces[3],
+                         const int32_t *const face_cta_block[3], const int nface_cta[3],
+                         const int32_t *cells, const int32_t *cell_cta_block, int ncell_cta,
+                         cudaStream_t s);
 void LaunchFastGeomFp64(const Pools<double> &P, const int32_t *const faces[3],
                         const int32_t *const face_cta_block[3], const int nface_cta[3],
                         const int32_t *cells, const int32_t *cell_cta_block, int ncell_cta,

@@ -625,6 +625,12 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
       const double *fg = P.fgeo[D];
       const U dpL = (U)fg[c], dmL = (U)fg[n + c], dpR = (U)fg[2 * n + c], dmR = (U)fg[3 * n + c];
       MusclFastPair(wm2, wm1, w0, wp1, dpL, dmL, dpR, dmR, kappa, sv.limiter, L, R);
+    } else if (P.fgeo[D] && !P.fast_fp64) {
+      // bit-exact FP64 batches: the same ratios, formed once per batch with
+      // Muscl's expressions (Pools::fgeo)
+      const double *fg = P.fgeo[D];
+      L = MusclR(wm2, wm1, w0, (U)fg[c], (U)fg[n + c], kappa, sv.limiter);
+      R = MusclR(wp1, w0, wm1, (U)fg[2 * n + c], (U)fg[3 * n + c], kappa, sv.limiter);
     } else {
       const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
       // lower side: upwind2 = c-2, upwind1 = c-1, downwind = c
@@ -696,10 +702,20 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
         Lt[q] = kt(c - s, q);
         Rt[q] = kt(c, q);
       } else if (sv.recon == ATH_RECON_MUSCL) {
-        const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c], xp1 = (U)wd[c + s];
         const U kappa = (U)sv.kappa;
-        const U dpL = (xm1 + xm1) / (xm1 + x0), dmL = (xm1 + xm1) / (xm1 + xm2);
-        const U dpR = (x0 + x0) / (x0 + xm1), dmR = (x0 + x0) / (x0 + xp1);
+        U dpL, dmL, dpR, dmR;
+        if (P.fgeo[D] && !P.fast_fp64) {
+          const double *fg = P.fgeo[D];
+          dpL = (U)fg[c];
+          dmL = (U)fg[n + c];
+          dpR = (U)fg[2 * n + c];
+          dmR = (U)fg[3 * n + c];
+        } else {
+          const U xm2 = (U)wd[c - 2 * s], xm1 = (U)wd[c - s], x0 = (U)wd[c],
+                  xp1 = (U)wd[c + s];
+          MusclRatios(xm2, xm1, x0, dpL, dmL);
+          MusclRatios(xp1, x0, xm1, dpR, dmR);
+        }
         Lt[q] = Muscl1(kt(c - 2 * s, q), kt(c - s, q), kt(c, q), dpL, dmL, kappa, sv.limiter);
         Rt[q] = Muscl1(kt(c + s, q), kt(c, q), kt(c - s, q), dpR, dmR, kappa, sv.limiter);
       } else {
@@ -1042,6 +1058,13 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
       const double *cg = P.cgeo[d];
       const T vn = fabs(Dot(w.u, w.v, w.w, (T)cg[c], (T)cg[n + c], (T)cg[2 * n + c]));
       lcd = (double)((vn + sosc) * (T)cg[3 * n + c]);
+    } else if (std::is_same<T, double>::value && P.cgeo[d]) {
+      // bit-exact FP64 batches: InvCellSpecRad with its geometry formed once
+      // per batch by the same expressions (Pools::cgeo)
+      const double *cg = P.cgeo[d];
+      lcd = (double)((fabs(Dot(w.u, w.v, w.w, (T)cg[c], (T)cg[n + c], (T)cg[2 * n + c])) +
+                      SoS(w, g)) *
+                     (T)cg[3 * n + c]);
     } else {
       lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
                                    (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u],
@@ -1052,13 +1075,18 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
     if (rans) {
       // turbModel::InviscidCellSpectralRadius (src/turbulence.cpp:94): |v.n_avg| |A|
       const Prim<double> wd = LoadW<double>(P.W, n, c);
-      double ax = 0.5 * (fa[c] + fa[u]), ay = 0.5 * (fa[n + c] + fa[n + u]),
-             az = 0.5 * (fa[2 * n + c] + fa[2 * n + u]);
-      const double am = sqrt(Dot(ax, ay, az, ax, ay, az));
-      ax = ax / am;
-      ay = ay / am;
-      az = az / am;
-      lamt = lamt + fabs(Dot(wd.u, wd.v, wd.w, ax, ay, az)) * (0.5 * (fa[3 * n + c] + fa[3 * n + u]));
+      double ax, ay, az, fm;
+      if (P.cgeo[d] && !P.fast_fp64) {
+        const double *cg = P.cgeo[d];
+        ax = cg[c];
+        ay = cg[n + c];
+        az = cg[2 * n + c];
+        fm = cg[3 * n + c];
+      } else {
+        CellAvgNormal(fa[c], fa[n + c], fa[2 * n + c], fa[3 * n + c], fa[u], fa[n + u],
+                      fa[2 * n + u], fa[3 * n + u], ax, ay, az, fm);
+      }
+      lamt = lamt + fabs(Dot(wd.u, wd.v, wd.w, ax, ay, az)) * fm;
     }
   }
   double adiagt = lamt;  // the scalar diagonal's turbulence part

@@ -219,12 +219,32 @@ __device__ __forceinline__ T MusclDelta1(T a, T b, T dplus, T dminus, T kappa,
   return T(0.25) * (a * dminus) * ((T(1) - kappa) * lim + (T(1) + kappa) * r * ilim);
 }
 
+// MUSCL's width ratios of one side: dplus = 2 uw / (uw + dw), dminus =
+// 2 uw / (uw + uw2) (FaceReconMUSCL, include/reconstruction.hpp:110)
+template <typename T>
+__device__ __forceinline__ void MusclRatios(T uw2, T uw, T dw, T &dplus, T &dminus) {
+  dplus = (uw + uw) / (uw + dw);
+  dminus = (uw + uw) / (uw + uw2);
+}
+// ... and the face state from given ratios
+template <typename T>
+__device__ __forceinline__ Prim<T> MusclR(const Prim<T> &up2, const Prim<T> &up1,
+                                          const Prim<T> &dw1, T dplus, T dminus, T kappa,
+                                          int limiter) {
+  Prim<T> o;
+  o.rho = Muscl1(up2.rho, up1.rho, dw1.rho, dplus, dminus, kappa, limiter);
+  o.u = Muscl1(up2.u, up1.u, dw1.u, dplus, dminus, kappa, limiter);
+  o.v = Muscl1(up2.v, up1.v, dw1.v, dplus, dminus, kappa, limiter);
+  o.w = Muscl1(up2.w, up1.w, dw1.w, dplus, dminus, kappa, limiter);
+  o.p = Muscl1(up2.p, up1.p, dw1.p, dplus, dminus, kappa, limiter);
+  return o;
+}
 template <typename T>
 __device__ __forceinline__ Prim<T> Muscl(const Prim<T> &up2, const Prim<T> &up1,
                                          const Prim<T> &dw1, T uw2, T uw, T dw,
                                          T kappa, int limiter) {
-  const T dplus = (uw + uw) / (uw + dw);
-  const T dminus = (uw + uw) / (uw + uw2);
+  T dplus, dminus;
+  MusclRatios(uw2, uw, dw, dplus, dminus);
   Prim<T> o;
   o.rho = Muscl1(up2.rho, up1.rho, dw1.rho, dplus, dminus, kappa, limiter);
   o.u = Muscl1(up2.u, up1.u, dw1.u, dplus, dminus, kappa, limiter);
@@ -799,16 +819,26 @@ __device__ __forceinline__ void CentralCoeffs(T wl, T wu, T &cdown, T &cup) {
 }
 
 // InvCellSpectralRadius (include/spectralRadius.hpp:44)
+// the radius's geometry of one direction: the average of the cell's two
+// face normals, normalised, and their average area
 template <typename T>
-__device__ __forceinline__ T InvCellSpecRad(const Prim<T> &s, const Gas<T> &g,
-                                            T lx, T ly, T lz, T lm, T ux,
-                                            T uy, T uz, T um) {
-  T ax = T(0.5) * (lx + ux), ay = T(0.5) * (ly + uy), az = T(0.5) * (lz + uz);
+__device__ __forceinline__ void CellAvgNormal(T lx, T ly, T lz, T lm, T ux, T uy, T uz, T um,
+                                              T &ax, T &ay, T &az, T &fMag) {
+  ax = T(0.5) * (lx + ux);
+  ay = T(0.5) * (ly + uy);
+  az = T(0.5) * (lz + uz);
   const T am = sqrt(Dot(ax, ay, az, ax, ay, az));
   ax = ax / am;
   ay = ay / am;
   az = az / am;
-  const T fMag = T(0.5) * (lm + um);
+  fMag = T(0.5) * (lm + um);
+}
+template <typename T>
+__device__ __forceinline__ T InvCellSpecRad(const Prim<T> &s, const Gas<T> &g,
+                                            T lx, T ly, T lz, T lm, T ux,
+                                            T uy, T uz, T um) {
+  T ax, ay, az, fMag;
+  CellAvgNormal(lx, ly, lz, lm, ux, uy, uz, um, ax, ay, az, fMag);
   return (fabs(Dot(s.u, s.v, s.w, ax, ay, az)) + SoS(s, g)) * fMag;
 }
 
