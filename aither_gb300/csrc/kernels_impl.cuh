@@ -603,7 +603,7 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 // f is the flux per unit area, L and R the reconstructed face states.
 // FAST (FP64 batches with the fast-face option): MUSCL and the Roe flux in
 // their fast forms (MusclFastPair, RoeFluxFast), equal to the reference to
-// roundoff instead of bit for bit.
+// roundoff instead of bit for bit, and f is the flux times the face's area.
 template <typename U, int D, typename PT, bool FAST = false>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
                                          int64_t s, U f[5], Prim<U> &L, Prim<U> &R,
@@ -685,12 +685,18 @@ __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv,
   const double *fa = P.fa[D];
   const U nx = (U)fa[c], ny = (U)fa[n + c], nz = (U)fa[2 * n + c];
   U vlr[2];
-  if (sv.flux == ATH_FLUX_AUSM)
+  if (sv.flux == ATH_FLUX_AUSM) {
     AusmFlux(L, R, g, nx, ny, nz, f, vlr);
-  else if constexpr (FAST && std::is_same<U, double>::value)
-    RoeFluxFast(L, R, g, nx, ny, nz, f);
-  else
+    if constexpr (FAST) {
+      const U mag = (U)fa[3 * n + c];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) f[v] = f[v] * mag;
+    }
+  } else if constexpr (FAST && std::is_same<U, double>::value) {
+    RoeFluxFast(L, R, g, nx, ny, nz, (U)fa[3 * n + c], f);
+  } else {
     RoeFlux(L, R, g, nx, ny, nz, f);
+  }
   if (ft) {
     // k and omega reconstructed like the flow variables, then their fluxes
     const double *Wt = P.Wt;
@@ -775,10 +781,11 @@ __device__ __forceinline__ void FaceFluxMixedRoe(const Pools<PT> &P, const Solve
     double l[5], r[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const float dl = MusclDelta1((float)(a1[v] - am[v]), (float)(a0[v] - a1[v]), dpL, dmL,
-                                   kappa, sv.limiter);
-      const float dr = MusclDelta1((float)(a0[v] - ap[v]), (float)(a1[v] - a0[v]), dpR, dmR,
-                                   kappa, sv.limiter);
+      // the difference across the face serves both sides: a1 - a0 is
+      // -(a0 - a1) exactly, before and after rounding to FP32
+      const float d0 = (float)(a0[v] - a1[v]);
+      const float dl = MusclDelta1((float)(a1[v] - am[v]), d0, dpL, dmL, kappa, sv.limiter);
+      const float dr = MusclDelta1((float)(a0[v] - ap[v]), -d0, dpR, dmR, kappa, sv.limiter);
       l[v] = a1[v] + (double)dl;
       r[v] = a0[v] + (double)dr;
     }
@@ -794,11 +801,18 @@ __device__ __forceinline__ void FaceFluxMixedRoe(const Pools<PT> &P, const Solve
   float d[5];
   RoeDissipation(Lf, Rf, dq, GasOf<float>(sv), (float)nx, (float)ny, (float)nz, d);
   const Gas<double> g = GasOf<double>(sv);
-  double fl[5], fr[5];
-  InvFluxCentral(L, g, nx, ny, nz, fl);
-  InvFluxCentral(R, g, nx, ny, nz, fr);
-#pragma unroll
-  for (int v = 0; v < 5; ++v) f[v] = (fl[v] + (fr[v] - (double)d[v])) * 0.5;
+  // FP64 central part FL + FR summed term by term, the two pressures once
+  const double vnL = L.u * nx + L.v * ny + L.w * nz, vnR = R.u * nx + R.v * ny + R.w * nz;
+  const double mL = L.rho * vnL, mR = R.rho * vnR;
+  const double np1 = g.n + 1.0;
+  const double rhoHL = L.rho * (g.hf + 0.5 * (L.u * L.u + L.v * L.v + L.w * L.w)) + np1 * L.p;
+  const double rhoHR = R.rho * (g.hf + 0.5 * (R.u * R.u + R.v * R.v + R.w * R.w)) + np1 * R.p;
+  const double pLR = L.p + R.p;
+  f[0] = ((mL + mR) - (double)d[0]) * 0.5;
+  f[1] = ((mL * L.u + (mR * R.u + pLR * nx)) - (double)d[1]) * 0.5;
+  f[2] = ((mL * L.v + (mR * R.v + pLR * ny)) - (double)d[2]) * 0.5;
+  f[3] = ((mL * L.w + (mR * R.w + pLR * nz)) - (double)d[3]) * 0.5;
+  f[4] = ((vnL * rhoHL + vnR * rhoHR) - (double)d[4]) * 0.5;
 }
 
 // WENO increment over the upwind cell value in FP32, from differences to
@@ -950,8 +964,9 @@ __global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const i
     Prim<T> L, R;
     FaceFlux<T, D, T, FAST>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
     const T magT = (T)mag;
+    // (the fast faces return F.|A| already)
 #pragma unroll
-    for (int v = 0; v < 5; ++v) out[v * n + c] = f[v] * magT;
+    for (int v = 0; v < 5; ++v) out[v * n + c] = FAST ? f[v] : f[v] * magT;
     if (RANS)
 #pragma unroll
       for (int q = 0; q < 2; ++q) P.fluxt[D][q * n + c] = ft[q] * magT;
@@ -1043,11 +1058,18 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
   // scalar main diagonal: accumulates like the radius, from zero or (a
   // multigrid level visited again in this iteration) from its previous value
   double adiag = (!BLOCK && P.mg_accum) ? (double)P.Aq[q] : 0.0;
-  // fast FP64 option: p / rho and the sound speed once per cell (p / rho
-  // also for the enthalpy), the radius's geometry from Pools::cgeo
+  // the sound speed once per cell; fast FP64 option: p / rho once (also for
+  // the enthalpy), the radius's geometry from Pools::cgeo
+  // (one sound speed per cell either way, chosen by a branch: both forms
+  // are divisions and square roots the other path must not execute)
   const bool fastc = std::is_same<T, double>::value && P.fast_fp64;
-  const T porc = fastc ? w.p / w.rho : T(0);
-  const T sosc = fastc ? sqrt(g.Gamma() * porc) : T(0);
+  T porc = T(0), sosc;
+  if (fastc) {
+    porc = w.p / w.rho;
+    sosc = sqrt(g.Gamma() * porc);
+  } else {
+    sosc = SoS(w, g);
+  }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double *fa = P.fa[d];
@@ -1063,12 +1085,14 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
       // per batch by the same expressions (Pools::cgeo)
       const double *cg = P.cgeo[d];
       lcd = (double)((fabs(Dot(w.u, w.v, w.w, (T)cg[c], (T)cg[n + c], (T)cg[2 * n + c])) +
-                      SoS(w, g)) *
+                      sosc) *
                      (T)cg[3 * n + c]);
     } else {
-      lcd = (double)InvCellSpecRad(w, g, (T)fa[c], (T)fa[n + c], (T)fa[2 * n + c],
-                                   (T)fa[3 * n + c], (T)fa[u], (T)fa[n + u], (T)fa[2 * n + u],
-                                   (T)fa[3 * n + u]);
+      // InvCellSpecRad with the cell's sound speed formed above
+      T ax, ay, az, fMag;
+      CellAvgNormal((T)fa[c], (T)fa[n + c], (T)fa[2 * n + c], (T)fa[3 * n + c], (T)fa[u],
+                    (T)fa[n + u], (T)fa[2 * n + u], (T)fa[3 * n + u], ax, ay, az, fMag);
+      lcd = (double)((fabs(Dot(w.u, w.v, w.w, ax, ay, az)) + sosc) * fMag);
     }
     lam = lam + lcd;
     adiag = adiag + lcd;
@@ -1353,7 +1377,7 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
         P.Npre[6 * nq + q] = sosc;
       } else {
         P.Npre[5 * nq + q] = Enthalpy(w, gq);
-        P.Npre[6 * nq + q] = SoS(w, gq);
+        P.Npre[6 * nq + q] = sosc;  // SoS(w, gq), formed above
       }
       if (sv.viscous) {
         P.Npre[7 * nq + q] = ViscMaxTerm(w, gq);

@@ -476,9 +476,10 @@ __device__ __forceinline__ void InvFluxCentral(const Prim<double> &s, const Gas<
 // calorically perfect gas) and sound speed; one reciprocal square root of
 // a^2 gives a and 1 / a^2; the dissipation's four waves summed in closed
 // form; and the division-free central flux.
+// f is the flux times `scale` (the face's area: F.|A| directly)
 __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<double> &R,
                                             const Gas<double> &g, double nx, double ny,
-                                            double nz, double f[5]) {
+                                            double nz, double scale, double f[5]) {
   const double dRho = R.rho - L.rho, dU = R.u - L.u, dV = R.v - L.v, dW = R.w - L.w,
                dP = R.p - L.p;
   // t = 1 / sqrt(rhoL rhoR): sqrt(rhoR / rhoL) = rhoR t, and t is the
@@ -534,11 +535,12 @@ __device__ __forceinline__ void RoeFluxFast(const Prim<double> &L, const Prim<do
   const double rhoHL = L.rho * (g.hf + 0.5 * (L.u * L.u + L.v * L.v + L.w * L.w)) + np1 * L.p;
   const double rhoHR = R.rho * (g.hf + 0.5 * (R.u * R.u + R.v * R.v + R.w * R.w)) + np1 * R.p;
   const double pLR = L.p + R.p;
-  f[0] = ((mL + mR) - d0) * 0.5;
-  f[1] = ((mL * L.u + (mR * R.u + pLR * nx)) - d1) * 0.5;
-  f[2] = ((mL * L.v + (mR * R.v + pLR * ny)) - d2) * 0.5;
-  f[3] = ((mL * L.w + (mR * R.w + pLR * nz)) - d3) * 0.5;
-  f[4] = ((vnL * rhoHL + vnR * rhoHR) - d4) * 0.5;
+  const double hs = 0.5 * scale;
+  f[0] = ((mL + mR) - d0) * hs;
+  f[1] = ((mL * L.u + (mR * R.u + pLR * nx)) - d1) * hs;
+  f[2] = ((mL * L.v + (mR * R.v + pLR * ny)) - d2) * hs;
+  f[3] = ((mL * L.w + (mR * R.w + pLR * nz)) - d3) * hs;
+  f[4] = ((vnL * rhoHL + vnR * rhoHR) - d4) * hs;
 }
 
 // ---------------------------------------------------------------------------

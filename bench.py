@@ -721,9 +721,9 @@ def _max_over_ranks(x: float, world: int) -> float:
 #     --steps 1 --warmup 3 --no-cpu-baseline --converge-drop 0 --served-n 0
 #     --sst-steps 0 --plate-iters 0 --vortex-iters 0 --mg-iters 0 --precision
 #     fp64 --sweep-shape 2,32 --exact-arm 0` (the first 8 cases, 888,004
-#     cells; GB300, 2026-12-04): residual-pass DRAM traffic 922.2 B per cell
-#     (faces 133.2 + 140.5 + 144.1, cell kernel 504.4); executed FP64 FLOP
-#     272.6 per face direction, 560.1 in the two sweeps, 181.0 cell, 73.2
+#     cells; GB300, 2026-12-04): residual-pass DRAM traffic 925.3 B per cell
+#     (faces 133.3 + 140.4 + 143.9, cell kernel 507.7); executed FP64 FLOP
+#     268.6 per face direction, 560.1 in the two sweeps, 165.0 cell, 73.2
 #     update, 19.2 ghost fill;
 #   * bit-exact path -- the same counters over one iteration of a 64x48x32
 #     bump channel: 1026 FLOP per face direction, 1134 in the two sweeps,
@@ -734,8 +734,8 @@ NCU_PER_CELL = {
     "source": "ncu captures on GB300 of the batched bump-channel path (fast option: every "
               "launch of one iteration of the first 8 cases of the batched workload, "
               "888,004 cells; bit-exact path: one 64x48x32 case), 2026-12-04",
-    "residual_traffic_bytes": {"fast": 922.2},
-    "flop": {"fast": {"face_per_direction": 272.6, "sweeps": 560.1, "cell": 181.0,
+    "residual_traffic_bytes": {"fast": 925.3},
+    "flop": {"fast": {"face_per_direction": 268.6, "sweeps": 560.1, "cell": 165.0,
                       "update": 73.2, "ghost": 19.2},
              "exact": {"face_per_direction": 1026.0, "sweeps": 1134.0, "cell": 502.0,
                        "update": 188.0, "ghost": 25.0}},
