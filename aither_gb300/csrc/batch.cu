@@ -190,6 +190,9 @@ struct BatchCore {
   bool any_rans = false;  // SST solves present: k, omega pools allocated
   bool any_unsteady = false;  // time-accurate or nonreflecting solves: time levels kept
   int fkinds = 0;  // bit 0: solves without turbulence equations, bit 1: SST
+  // every solve without turbulence equations reconstructs with MUSCL and
+  // takes the Roe flux (the fast faces then run their MUSCL-Roe kernel)
+  bool mr_only = true;
   int vkinds = 0;  // bit 0: laminar viscous solves, bit 1: SST
   cudaStream_t stream = nullptr;
   bool own_stream = true;  // false: a multigrid level on its finest batch's stream
@@ -714,7 +717,11 @@ class Runner : public RunnerBase {
   }
   // face kernels to launch: the batch's solve kinds, plus bit 2 for the
   // fast FP64 faces (batch flag bit 1)
-  int FaceKinds() const { return c_.fkinds | ((c_.flags & 2) ? 4 : 0); }
+  // bit 2: the fast faces; bit 3: the solves without turbulence equations
+  // are all MUSCL-Roe
+  int FaceKinds() const {
+    return c_.fkinds | ((c_.flags & 2) ? 4 : 0) | (c_.mr_only ? 8 : 0);
+  }
   void SweepPass(int forward, int sweep) {
     const bool full = c_.max_sweeps > 1;
     if (c_.sweep_mode == 3) {
@@ -1884,6 +1891,8 @@ void CreateBatch(ath_batch *B, ath_ctx *ctx, const Setup &st, int precision, int
     if (blk && sv.phys.eqn != ATH_EQN_EULER) c.block_viscous = true;
     const bool rans = sv.phys.eqn == ATH_EQN_RANS;
     c.fkinds |= rans ? 2 : 1;
+    if (!rans && !(sv.phys.recon == ATH_RECON_MUSCL && sv.phys.flux == ATH_FLUX_ROE))
+      c.mr_only = false;
     if (sv.phys.eqn != ATH_EQN_EULER) c.vkinds |= rans ? 2 : 1;
   }
   Check(cudaSetDevice(ctx->device), "cudaSetDevice");

@@ -301,9 +301,8 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
                         const int32_t *op_solve);
 
 // Face fluxes of direction D over the face list (CalcInvFluxI/J/K,
-// src/procBlock.cpp:384,522,660).
-template <typename T, int D>
-__global__ void k_face(Pools<T> P, const int32_t *list, const int32_t *cta_block);
+// src/procBlock.cpp:384,522,660): k_face<T, D, RANS, FAST, MR> in
+// kernels_impl.cuh.
 
 // Residual assembly, spectral radius, local time step and inverted
 // diagonal of every physical cell (procBlock residual accumulation,
@@ -385,7 +384,7 @@ __global__ void k_cfl(const SolveDev *solves, int nsolves, const SolveState *sst
 // compiled in their own unit with contracted multiply-adds: roundoff-equal
 // to the reference's faces, not bit-equal.
 void LaunchFastFaceFp64(int d, const Pools<double> &P, const int32_t *list,
-                        const int32_t *cta_block, int ncta, cudaStream_t s);
+                        const int32_t *cta_block, int ncta, bool muscl_roe, cudaStream_t s);
 // The cell kernel, the scalar LU-SGS sweeps and the update of FP64 batches
 // with the fast option, from the same unit (same arguments as
 // Launch<double>::Cell / Sweep / Update; the sweep: scalar solves only).

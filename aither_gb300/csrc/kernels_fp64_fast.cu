@@ -9,9 +9,17 @@
 
 namespace ath {
 
+// muscl_roe: every solve the kernel serves is MUSCL-Roe, and the kernel
+// built for that alone (no other reconstruction or flux) runs
 void LaunchFastFaceFp64(int d, const Pools<double> &P, const int32_t *list,
-                        const int32_t *cta_block, int ncta, cudaStream_t s) {
+                        const int32_t *cta_block, int ncta, bool muscl_roe, cudaStream_t s) {
   if (ncta <= 0) return;
+  if (muscl_roe) {
+    if (d == 0) k_face<double, 0, false, true, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+    else if (d == 1) k_face<double, 1, false, true, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+    else k_face<double, 2, false, true, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+    return;
+  }
   if (d == 0) k_face<double, 0, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
   else if (d == 1) k_face<double, 1, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
   else k_face<double, 2, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);

@@ -604,12 +604,35 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 // FAST (FP64 batches with the fast-face option): MUSCL and the Roe flux in
 // their fast forms (MusclFastPair, RoeFluxFast), equal to the reference to
 // roundoff instead of bit for bit, and f is the flux times the face's area.
-template <typename U, int D, typename PT, bool FAST = false>
+// MR (with FAST): the solve reconstructs with MUSCL and takes the Roe flux,
+// and nothing else is built in.
+template <typename U, int D, typename PT, bool FAST = false, bool MR = false>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
                                          int64_t s, U f[5], Prim<U> &L, Prim<U> &R,
                                          U ft[2] = nullptr) {
   const Gas<U> g = GasOf<U>(sv);
   const int64_t n = P.ncell;
+  if constexpr (FAST && MR && std::is_same<U, double>::value) {
+    const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s), wm1 = LoadW<U>(P.W, n, c - s),
+                  w0 = LoadW<U>(P.W, n, c), wp1 = LoadW<U>(P.W, n, c + s);
+    const double *fg = P.fgeo[D];
+    MusclFastPair(wm2, wm1, w0, wp1, fg[c], fg[n + c], fg[2 * n + c], fg[3 * n + c],
+                  (U)sv.kappa, sv.limiter, L, R);
+    const double *fa = P.fa[D];
+    RoeFluxFast(L, R, g, fa[c], fa[n + c], fa[2 * n + c], fa[3 * n + c], f);
+    return;
+  } else if constexpr (!FAST && MR && std::is_same<U, double>::value) {
+    // bit-exact MUSCL-Roe: Muscl with the batch's ratio table, RoeFlux
+    const Prim<U> wm2 = LoadW<U>(P.W, n, c - 2 * s), wm1 = LoadW<U>(P.W, n, c - s),
+                  w0 = LoadW<U>(P.W, n, c), wp1 = LoadW<U>(P.W, n, c + s);
+    const double *fg = P.fgeo[D];
+    const U kappa = (U)sv.kappa;
+    L = MusclR(wm2, wm1, w0, (U)fg[c], (U)fg[n + c], kappa, sv.limiter);
+    R = MusclR(wp1, w0, wm1, (U)fg[2 * n + c], (U)fg[3 * n + c], kappa, sv.limiter);
+    const double *fa = P.fa[D];
+    RoeFlux(L, R, g, (U)fa[c], (U)fa[n + c], (U)fa[2 * n + c], f);
+    return;
+  }
   const double *wd = P.width[D];
   const Prim<U> wm1 = LoadW<U>(P.W, n, c - s);
   const Prim<U> w0 = LoadW<U>(P.W, n, c);
@@ -933,8 +956,8 @@ __device__ __forceinline__ void FaceFluxMixed(const Pools<PT> &P, const SolveDev
   if (ft) RoeTurbFlux(L, R, lt, rt, g, nx, ny, nz, ft);
 }
 
-template <typename T, int D, bool RANS, bool FAST = false>
-__global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const int32_t *list,
+template <typename T, int D, bool RANS, bool FAST = false, bool MR = false>
+__global__ void __launch_bounds__(kCta, (MR || FAST) ? 2 : 1) k_face(Pools<T> P, const int32_t *list,
                                                const int32_t *cta_block) {
   const int32_t c = list[blockIdx.x * kCta + threadIdx.x];
   if (c < 0) return;
@@ -962,7 +985,7 @@ __global__ void __launch_bounds__(kCta, FAST ? 2 : 1) k_face(Pools<T> P, const i
   } else {
     T f[5], ft[2];
     Prim<T> L, R;
-    FaceFlux<T, D, T, FAST>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
+    FaceFlux<T, D, T, FAST, MR>(P, sv, c, s, f, L, R, RANS ? ft : nullptr);
     const T magT = (T)mag;
     // (the fast faces return F.|A| already)
 #pragma unroll
@@ -3661,15 +3684,23 @@ template <typename T, int D>
 static void LaunchFace(const Pools<T> &P, const int32_t *list, const int32_t *cta_block,
                        int ncta, int rkinds, cudaStream_t s) {
   // rkinds bit 2: the fast-face option of FP64 batches (non-RANS solves),
-  // compiled in its own unit with contracted multiply-adds
+  // compiled in its own unit with contracted multiply-adds; bit 3: every
+  // solve without turbulence equations is MUSCL-Roe
   bool fast = false;
   if constexpr (std::is_same<T, double>::value) {
     if ((rkinds & 1) && (rkinds & 4)) {
-      LaunchFastFaceFp64(D, P, list, cta_block, ncta, s);
+      LaunchFastFaceFp64(D, P, list, cta_block, ncta, (rkinds & 8) != 0, s);
       fast = true;
     }
   }
-  if ((rkinds & 1) && !fast) k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  if ((rkinds & 1) && !fast) {
+    // bit-exact FP64 batches whose solves are all MUSCL-Roe run the kernel
+    // built for that alone
+    if (std::is_same<T, double>::value && (rkinds & 8))
+      k_face<T, D, false, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+    else
+      k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
+  }
   if (rkinds & 2) k_face<T, D, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
 }
 template <typename T>
