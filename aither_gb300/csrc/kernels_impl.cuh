@@ -604,8 +604,9 @@ __global__ void k_ghost(Pools<T> P, const GhostOpDev *ops, int nops,
 // FAST (FP64 batches with the fast-face option): MUSCL and the Roe flux in
 // their fast forms (MusclFastPair, RoeFluxFast), equal to the reference to
 // roundoff instead of bit for bit, and f is the flux times the face's area.
-// MR (with FAST): the solve reconstructs with MUSCL and takes the Roe flux,
-// and nothing else is built in.
+// MR: the solve reconstructs with MUSCL and takes the Roe flux, and
+// nothing else is built in (FP64 faces; the mixed faces' FaceFluxMixed is
+// unchanged, k_face's MR only raises their occupancy).
 template <typename U, int D, typename PT, bool FAST = false, bool MR = false>
 __device__ __forceinline__ void FaceFlux(const Pools<PT> &P, const SolveDev &sv, int64_t c,
                                          int64_t s, U f[5], Prim<U> &L, Prim<U> &R,
@@ -3694,9 +3695,10 @@ static void LaunchFace(const Pools<T> &P, const int32_t *list, const int32_t *ct
     }
   }
   if ((rkinds & 1) && !fast) {
-    // bit-exact FP64 batches whose solves are all MUSCL-Roe run the kernel
-    // built for that alone
-    if (std::is_same<T, double>::value && (rkinds & 8))
+    // batches whose solves are all MUSCL-Roe run the kernel built for that
+    // alone (bit-exact FP64: the MUSCL-Roe path only; mixed: the same
+    // FaceFluxMixed, at two CTAs per SM)
+    if (rkinds & 8)
       k_face<T, D, false, false, true><<<ncta, kCta, 0, s>>>(P, list, cta_block);
     else
       k_face<T, D, false><<<ncta, kCta, 0, s>>>(P, list, cta_block);
