@@ -1020,10 +1020,12 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
   const BlockDev b = P.blocks[cta_block[blockIdx.x]];
   const SolveDev sv = P.solves[b.solve];
   if ((sv.block != 0) != BLOCK || !sv.active) return;
-  // fast FP64 option with a local time step: the solve's 1 / CFL formed
-  // once per CTA (the CTA lies in one block) for the diagonal
+  // fast FP64 option and mixed precision (roundoff-equal by construction),
+  // with a local time step: the solve's 1 / CFL formed once per CTA (the
+  // CTA lies in one block) for the diagonal
   __shared__ double s_cfl_inv;
-  const bool fastdt = std::is_same<T, double>::value && P.fast_fp64 && sv.dt_global <= 0.0;
+  const bool fastdt =
+      (std::is_same<T, float>::value || P.fast_fp64) && sv.dt_global <= 0.0;
   if (fastdt) {
     if (threadIdx.x == 0) s_cfl_inv = 1.0 / P.cfl[b.solve];
     __syncthreads();
