@@ -1371,11 +1371,12 @@ __global__ void __launch_bounds__(kCta, (!BLOCK && !RANS) ? 3 : 1) k_cell(Pools<
     }
   } else {
     const double a = adiag * sv.relax + diagVolTimeD;
-    P.Ainvq[q] = (T)(1.0 / a);
+    // mixed precision: the FP32 operator's inverse diagonal divides in FP32
+    P.Ainvq[q] = std::is_same<T, float>::value ? (T)(T(1) / (T)a) : (T)(1.0 / a);
     P.Aq[q] = (T)a;
     if (rans) {
       const double at = adiagt * sv.relax + diagVolTimeD;
-      P.Ainvtq[q] = (T)(1.0 / at);
+      P.Ainvtq[q] = std::is_same<T, float>::value ? (T)(T(1) / (T)at) : (T)(1.0 / at);
       P.Atq[q] = (T)at;
     }
   }
