@@ -347,7 +347,10 @@ int ath_batch_solve_info(ath_batch *batch, ath_converge_info *info);
 
 /* Autotuner of the LU-SGS sweep shape: times `reps` graph-captured
  * iterations for each candidate and keeps the fastest -- one launch per
- * hyperplane with CTAs of 32, 64, 128 or 256 threads, the persistent
+ * hyperplane with CTAs of 32, 64, 128 or 256 threads (a thread per cell or
+ * lane groups; lane groups also with the solves as 2 or 4 concurrent
+ * chains, and lane groups below 32,768 cells per plane with a thread per
+ * cell above), the persistent
  * cluster sweep (one launch per pass; a thread-block cluster of 1, 2, 4 or
  * 8 CTAs of 256 threads per solve walks the solve's hyperplanes with
  * cluster barriers), or the persistent tile-queue sweep (one launch per
