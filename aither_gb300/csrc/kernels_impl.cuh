@@ -1932,16 +1932,26 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
     both = sweep > 0 || sv.sweeps > 1;
   }
   const Gas<T> g = GasOf<T>(sv);
+  const bool term = valid && (side == 0 || both) && nb != -1;
+  // fast FP64 option, inviscid solves: the neighbour's own part of the term
+  // is formed before the wait (it does not depend on the updates)
+  const bool early = term && o.has_pre && P.fast_fp64 && !sv.viscous && !sv.rans;
+  FastOld<T> fo{};
+  if (early) fo = ScalarOffDiagFastOld(o.s, o.pre, fx, fy, fz, mag);
   // the previous plane's updates are read from here on: with a programmatic
   // launch after that plane's kernel, wait for it (a no-op otherwise), and
   // let the next plane's kernel start its own loads of this kind
   GridDependencyWait();
   GridDependentsLaunch();
   T r[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-  if (valid && (side == 0 || both) && nb != -1) {
+  if (term) {
     LoadNbrDu(P, nb, o);
-    LoadNbrSolve(P, sv, nb, o);
-    NbrTermFrom(P, g, sv, q, lower, d, o, fx, fy, fz, mag, r, r + 5);
+    if (early) {
+      ScalarOffDiagFastNew(fo, o.pre, o.du, g, fx, fy, fz, lower, r);
+    } else {
+      LoadNbrSolve(P, sv, nb, o);
+      NbrTermFrom(P, g, sv, q, lower, d, o, fx, fy, fz, mag, r, r + 5);
+    }
   }
   const int gbase = lane - li;
   T xs[M][L];

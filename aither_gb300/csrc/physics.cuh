@@ -957,6 +957,57 @@ __device__ __forceinline__ void ScalarOffDiagPre(const Prim<T> &s, const NbrPre<
 // fast option: the updated state with one reciprocal of the density and no
 // square root, p = (gamma - 1) (rho E - rho (hf + |v|^2 / 2)) and
 // rho H = rho E + p; equal to the reference's form to roundoff.
+// ScalarOffDiagPreFast in two parts for an inviscid neighbour term: the
+// part of the neighbour's state alone (its normal velocity and mass flux,
+// its flux F(W).n, half the face area and the term's radius), which a
+// hyperplane kernel forms before it waits for the previous plane, and the
+// part with the neighbour's update
+template <typename T>
+struct FastOld {
+  T vn, mo, f1, f2, f3, f4, half, lam;
+};
+template <typename T>
+__device__ __forceinline__ FastOld<T> ScalarOffDiagFastOld(const Prim<T> &s,
+                                                          const NbrPre<T> &pre, T nx, T ny,
+                                                          T nz, T mag) {
+  FastOld<T> o;
+  o.vn = Dot(s.u, s.v, s.w, nx, ny, nz);
+  o.mo = s.rho * o.vn;
+  o.f1 = o.mo * s.u + s.p * nx;
+  o.f2 = o.mo * s.v + s.p * ny;
+  o.f3 = o.mo * s.w + s.p * nz;
+  o.f4 = o.mo * pre.h;
+  o.half = T(0.5) * mag;
+  o.lam = o.half * (fabs(o.vn) + pre.sos);
+  return o;
+}
+template <typename T>
+__device__ __forceinline__ void ScalarOffDiagFastNew(const FastOld<T> &fo,
+                                                     const NbrPre<T> &pre, const T du[5],
+                                                     const Gas<T> &g, T nx, T ny, T nz,
+                                                     bool positive, T out[5]) {
+  T c[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) c[v] = pre.c[v] + du[v];
+  const T ir = T(1) / c[0];
+  const T u = c[1] * ir, v = c[2] * ir, w = c[3] * ir;
+  const T ke = T(0.5) * (u * u + v * v + w * w);
+  const T p = (g.gam - T(1)) * (c[4] - c[0] * (g.hf + ke));
+  const T vnn = u * nx + v * ny + w * nz;
+  const T mn = c[0] * vnn;
+  T df[5];
+  df[0] = mn - fo.mo;
+  df[1] = (mn * u + p * nx) - fo.f1;
+  df[2] = (mn * v + p * ny) - fo.f2;
+  df[3] = (mn * w + p * nz) - fo.f3;
+  df[4] = vnn * (c[4] + p) - fo.f4;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const T fc = fo.half * df[k];
+    out[k] = positive ? fc + fo.lam * du[k] : fc - fo.lam * du[k];
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void ScalarOffDiagPreFast(const Prim<T> &s, const NbrPre<T> &pre,
                                                      const T du[5], const Gas<T> &g, T nx, T ny,
