@@ -1933,11 +1933,16 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
   }
   const Gas<T> g = GasOf<T>(sv);
   const bool term = valid && (side == 0 || both) && nb != -1;
-  // fast FP64 option, inviscid solves: the neighbour's own part of the term
-  // is formed before the wait (it does not depend on the updates)
-  const bool early = term && o.has_pre && P.fast_fp64 && !sv.viscous && !sv.rans;
+  // FP64 batches, inviscid solves: the neighbour's own part of the term is
+  // formed before the wait (it does not depend on the updates), in the fast
+  // option's form or the bit-exact one
+  const bool early = term && o.has_pre && !sv.viscous && !sv.rans;
   FastOld<T> fo{};
-  if (early) fo = ScalarOffDiagFastOld(o.s, o.pre, fx, fy, fz, mag);
+  ExactOld<T> eo{};
+  if (early) {
+    if (P.fast_fp64) fo = ScalarOffDiagFastOld(o.s, o.pre, fx, fy, fz, mag);
+    else eo = ScalarOffDiagExactOld(o.s, o.pre, fx, fy, fz, mag);
+  }
   // the previous plane's updates are read from here on: with a programmatic
   // launch after that plane's kernel, wait for it (a no-op otherwise), and
   // let the next plane's kernel start its own loads of this kind
@@ -1946,8 +1951,10 @@ __device__ __forceinline__ void SweepGroupItem(const Pools<T> &P, const int2 *it
   T r[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
   if (term) {
     LoadNbrDu(P, nb, o);
-    if (early) {
+    if (early && P.fast_fp64) {
       ScalarOffDiagFastNew(fo, o.pre, o.du, g, fx, fy, fz, lower, r);
+    } else if (early) {
+      ScalarOffDiagExactNew(eo, o.pre, o.du, g, fx, fy, fz, lower, r);
     } else {
       LoadNbrSolve(P, sv, nb, o);
       NbrTermFrom(P, g, sv, q, lower, d, o, fx, fy, fz, mag, r, r + 5);

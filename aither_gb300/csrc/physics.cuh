@@ -953,10 +953,45 @@ __device__ __forceinline__ void ScalarOffDiagPre(const Prim<T> &s, const NbrPre<
   }
 }
 
-// ScalarOffDiagPre in the fast-arithmetic form of FP64 batches with the
-// fast option: the updated state with one reciprocal of the density and no
-// square root, p = (gamma - 1) (rho E - rho (hf + |v|^2 / 2)) and
-// rho H = rho E + p; equal to the reference's form to roundoff.
+// ScalarOffDiagPre in the same two parts for an inviscid neighbour term
+// (visc_sr = 0), with its operations and their order unchanged
+template <typename T>
+struct ExactOld {
+  T vn, fo[5], half, lam;
+};
+template <typename T>
+__device__ __forceinline__ ExactOld<T> ScalarOffDiagExactOld(const Prim<T> &s,
+                                                            const NbrPre<T> &pre, T nx, T ny,
+                                                            T nz, T mag) {
+  ExactOld<T> o;
+  o.vn = Dot(s.u, s.v, s.w, nx, ny, nz);
+  o.fo[0] = s.rho * o.vn;
+  o.fo[1] = s.rho * o.vn * s.u + s.p * nx;
+  o.fo[2] = s.rho * o.vn * s.v + s.p * ny;
+  o.fo[3] = s.rho * o.vn * s.w + s.p * nz;
+  o.fo[4] = s.rho * o.vn * pre.h;
+  o.half = T(0.5) * mag;
+  o.lam = T(0.5) * mag * (fabs(o.vn) + pre.sos);
+  return o;
+}
+template <typename T>
+__device__ __forceinline__ void ScalarOffDiagExactNew(const ExactOld<T> &eo,
+                                                      const NbrPre<T> &pre, const T du[5],
+                                                      const Gas<T> &g, T nx, T ny, T nz,
+                                                      bool positive, T out[5]) {
+  T c[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) c[v] = pre.c[v] + du[v];
+  const Prim<T> su = ConsToPrim(c, g);
+  T fn[5];
+  InvFlux(su, g, nx, ny, nz, fn);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const T fc = eo.half * (fn[v] - eo.fo[v]);
+    out[v] = positive ? fc + eo.lam * du[v] : fc - eo.lam * du[v];
+  }
+}
+
 // ScalarOffDiagPreFast in two parts for an inviscid neighbour term: the
 // part of the neighbour's state alone (its normal velocity and mass flux,
 // its flux F(W).n, half the face area and the term's radius), which a
@@ -1008,6 +1043,10 @@ __device__ __forceinline__ void ScalarOffDiagFastNew(const FastOld<T> &fo,
   }
 }
 
+// ScalarOffDiagPre in the fast-arithmetic form of FP64 batches with the
+// fast option: the updated state with one reciprocal of the density and no
+// square root, p = (gamma - 1) (rho E - rho (hf + |v|^2 / 2)) and
+// rho H = rho E + p; equal to the reference's form to roundoff.
 template <typename T>
 __device__ __forceinline__ void ScalarOffDiagPreFast(const Prim<T> &s, const NbrPre<T> &pre,
                                                      const T du[5], const Gas<T> &g, T nx, T ny,
