@@ -2617,10 +2617,26 @@ __global__ void __launch_bounds__(kCta) k_update(Pools<T> P, const int32_t *list
       // equal to FP64's by construction): rho E = rho hf + n p + rho |v|^2 / 2
       // (cv T rho = n p), then the updated state with one reciprocal of the
       // density
-      const double rho1 = w.rho + du[0];
-      const double c1 = w.rho * w.u + du[1], c2 = w.rho * w.v + du[2], c3 = w.rho * w.w + du[3];
-      const double rE = (w.rho * g.hf + g.n * w.p +
-                         0.5 * w.rho * Dot(w.u, w.v, w.w, w.u, w.v, w.w)) + du[4];
+      // the conserved state: the cell kernel's q-ordered copy (FP64 scalar
+      // solves; W has not changed since), else formed here
+      double k0, k1, k2, k3, k4;
+      if (std::is_same<T, double>::value && P.Npre && !sv.block) {
+        const int64_t nq = P.nq;
+        k0 = (double)P.Npre[q];
+        k1 = (double)P.Npre[nq + q];
+        k2 = (double)P.Npre[2 * nq + q];
+        k3 = (double)P.Npre[3 * nq + q];
+        k4 = (double)P.Npre[4 * nq + q];
+      } else {
+        k0 = w.rho;
+        k1 = w.rho * w.u;
+        k2 = w.rho * w.v;
+        k3 = w.rho * w.w;
+        k4 = w.rho * g.hf + g.n * w.p + 0.5 * w.rho * Dot(w.u, w.v, w.w, w.u, w.v, w.w);
+      }
+      const double rho1 = k0 + du[0];
+      const double c1 = k1 + du[1], c2 = k2 + du[2], c3 = k3 + du[3];
+      const double rE = k4 + du[4];
       const double ir = 1.0 / rho1;
       u.rho = rho1;
       u.u = c1 * ir;
